@@ -1,0 +1,304 @@
+"""Benchmark of the GPU trace path on the 1M-triangle workload.
+
+Workload (one "step" = one full frame through the C ABI):
+  mesh_spheres: 1920x1080, 1 spp, no AA; a 1,051,392-triangle displaced
+  sphere mesh2 (radius 8, smooth normals) + 1024 spheres + plane y=-9; one
+  point light with shadows; reflection 0.3 on every surface;
+  max_trace_level 3.  Synthetic, seeded (PCG64 seed 2).
+
+Metric: Mrays/s (primary+shadow) = (Number_Of_Rays + Shadow_Ray_Tests) of
+the frame / frame time -- the reference's own counters ("Rays" and "Shadow
+Ray Tests" of its statistics printout).
+
+  value  frame time by CUDA events on the launch stream, scene resident in
+         HBM, image written to device memory; L2 flushed (256 MiB write)
+         between frames, outside the timed events.
+  e2e    the same frame with host buffers: block list H2D, RGBT image D2H
+         into pinned host memory, all inside the timed region.
+
+`--impl reference` times the CPU implementation of the path (the oracle
+restatement of the reference, all host threads) on the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = ("mesh_spheres: 1920x1080 1spp, 1,051,392-tri displaced-sphere mesh2 + 1024 spheres + plane, "
+            "1 point light w/ shadows, reflection 0.3, max_trace_level 3")
+METRIC = "Mrays/s (primary+shadow)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--width", type=int, default=1920)
+    ap.add_argument("--height", type=int, default=1080)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax.append(float(f[1]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(scene, cpu_seconds_target=20.0):
+    """The oracle port (FP64 restatement of the reference), all host threads,
+    on a band of rows of the same frame; Mrays/s by its own counters."""
+    from oracle.pyoracle import Oracle
+    cores = os.cpu_count() or 1
+    t0 = time.time()
+    orc = Oracle(scene)
+    build_s = time.time() - t0
+    rows = 8
+    y0 = scene.height // 2
+    total_rays, total_t = 0, 0.0
+    while total_t < cpu_seconds_target / cores and y0 + rows <= scene.height:
+        t = time.time()
+        _, st = orc.render(0, y0, scene.width, y0 + rows, threads=0)
+        total_t += time.time() - t
+        total_rays += st["number_of_rays"] + st["shadow_ray_tests"]
+        y0 += rows
+        rows *= 2
+    rows_done = y0 - scene.height // 2
+    return {"value": total_rays / total_t / 1e6, "unit": "Mrays/s", "cores": cores, "kind": "port",
+            "sample": "oracle restatement, %d rows x %d px of the frame (rows %d..%d), %.1f s wall, "
+                      "tree build %.1f s excluded" % (rows_done, scene.width, scene.height // 2,
+                                                        scene.height // 2 + rows_done, total_t, build_s)}
+
+
+def run_reference(args, rank, world):
+    """CPU reference arm: the oracle port of the reference's trace path."""
+    if rank != 0:
+        return
+    from oracle.pyoracle import Oracle
+    from povray_gb300 import scenes
+    s = scenes.mesh_spheres(args.width, args.height)
+    orc = Oracle(s)
+    band = max(8, args.height // 10)
+    def step(i):
+        y0 = (i * band) % max(1, args.height - band)
+        t = time.time()
+        _, st = orc.render(0, y0, args.width, y0 + band, threads=0)
+        return time.time() - t, st["number_of_rays"] + st["shadow_ray_tests"]
+    for i in range(args.warmup):
+        step(i)
+    tt, rr = 0.0, 0
+    for i in range(args.steps):
+        dt, r = step(args.warmup + i)
+        tt += dt
+        rr += r
+    v = rr / tt / 1e6
+    cores = os.cpu_count() or 1
+    sample = "oracle restatement of the reference (FP64 C, pthreads), %d-row band of the %dx%d frame per step" % (
+        band, args.width, args.height)
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "Mrays/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": tt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD},
+        "cpu_baseline": {"value": v, "unit": "Mrays/s", "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from povray_gb300 import GpuScene, scenes
+    from povray_gb300.abi import STAGE_NAMES  # noqa: F401
+
+    s = scenes.mesh_spheres(args.width, args.height)
+    gpu = GpuScene(s)
+    stream = torch.cuda.current_stream()
+    gpu.set_stream(stream.cuda_stream)
+    params = s.render_params()
+    blocks = scenes.blocks_for(args.width, args.height)
+    npix = args.width * args.height
+    dev_out = torch.empty((npix, 4), dtype=torch.float32, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    # one profiling frame (outside the timed region): traversal work counts
+    gpu.set_profiling(times=False, work=True)
+    gpu.trace_blocks(blocks, params, out=dev_out.data_ptr())
+    work = gpu.timings()
+    gpu.set_profiling(times=True, work=False)
+
+    def frame_device():
+        return gpu.trace_blocks(blocks, params, out=dev_out.data_ptr())[1]
+
+    for _ in range(args.warmup):
+        frame_device()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    stage_ms = {}
+    launches = 0
+    rays = 0
+    for i in range(args.steps):
+        flush.zero_()
+        ev[i][0].record(stream)
+        st = frame_device()
+        ev[i][1].record(stream)
+        t = gpu.timings()
+        for k, v in t["stage_ms"].items():
+            stage_ms[k] = stage_ms.get(k, 0.0) + v
+        launches += t["kernel_launches"]
+        rays += st["number_of_rays"] + st["shadow_ray_tests"]
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    frame_ms = [a.elapsed_time(b) for a, b in ev]
+    t_total = sum(frame_ms) / 1e3
+
+    # e2e: host buffers through the public call (pinned output)
+    gpu.set_profiling(times=False, work=False)
+    host_out = torch.empty((npix, 4), dtype=torch.float32, pin_memory=True)
+    for _ in range(max(1, args.warmup // 2)):
+        gpu.trace_blocks(blocks, params, out=host_out.data_ptr())
+    torch.cuda.synchronize()
+    e2e_rays = 0
+    t0 = time.perf_counter()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i in range(args.steps):
+        st = gpu.trace_blocks(blocks, params, out=host_out.data_ptr())[1]
+        e2e_rays += st["number_of_rays"] + st["shadow_ray_tests"]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_wall = time.perf_counter() - t0
+    e2e_t = max(e2e_wall, e0.elapsed_time(e1) / 1e3)
+
+    # max over ranks
+    if dist:
+        tt = torch.tensor([t_total, e2e_t], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_total, e2e_t = float(tt[0]), float(tt[1])
+
+    value = world * rays / t_total / 1e6
+    e2e_value = world * e2e_rays / e2e_t / 1e6
+    # roofline of the dominant kernel (closest-hit traversal): algorithmic
+    # bytes = 32 B ray + 16 B hit per ray + 64 B per node visit (both child
+    # boxes of a two-wide node) + 48 B per triangle test + 16 B per sphere test
+    nv, pt, tt_, rt = work["node_visits"], work["prim_tests"], work["tri_tests"], work["rays_traced"]
+    k = 0 if stage_ms.get("trace_closest", 0) >= stage_ms.get("trace_shadow", 0) else 1
+    kname = ["trace_closest", "trace_shadow"][k]
+    bytes_per_frame = rt[k] * (32 + (16 if k == 0 else 1)) + nv[k] * 64 + tt_[k] * 48 + (pt[k] - tt_[k]) * 16
+    kernel_s = stage_ms[kname] / 1e3 / args.steps
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = bytes_per_frame / kernel_s / 1e9
+    traffic = None
+    try:
+        traffic = json.load(open(os.path.join(ROOT, "profiles", "traffic.json"))).get(kname)
+    except Exception:
+        pass
+    out = {
+        "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_total / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (fp64 grazing re-solve, fp64 camera)",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "l2": "flushed between steps (256 MiB write, outside timed events)",
+                   "rays_per_frame": rays // args.steps, "parallelism": "replica per GPU" if world > 1 else "1 GPU"},
+        "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": len(blocks) * 16 + (len(blocks) + 1) * 4,
+                "d2h_bytes_per_step": npix * 16},
+        "roofline": {"bound": "hbm", "kernel": "k_trace<%s>" % ("closest" if k == 0 else "any"),
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_source": "measured" if peaks else "fallback",
+                     "algorithmic_bytes_per_frame": bytes_per_frame},
+        "stage_ms_per_frame": {k2: v / args.steps for k2, v in stage_ms.items() if v > 0},
+        "gpu_launches": launches,
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(s)
+    if rank == 0:
+        print(json.dumps(out))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,338 @@
+/*
+ * povgpu.h -- C ABI of the GB300 trace path (libpovgpu.so).
+ *
+ * The reference renders a parsed scene by running one TraceTask per worker
+ * thread; each task pulls 32x32 render blocks from the view
+ * (ViewData::GetNextRectangle, source/backend/scene/view.cpp:236), traces
+ * every pixel through TracePixel/Trace::TraceRay
+ * (source/core/render/tracepixel.cpp:311, source/core/render/trace.cpp:135)
+ * and hands the finished block back (ViewData::CompletedRectangle,
+ * source/backend/scene/view.cpp:405).  This library replaces the per-pixel
+ * part of that loop: the host walks SceneData once, fills a PovGpuSceneDesc,
+ * and then submits whole batches of blocks.  Everything below the block
+ * boundary (bounding-tree traversal, the All_Intersections/Inside tests,
+ * shadow rays, Phong/specular shading, reflection, adaptive antialiasing,
+ * radiosity) runs in CUDA kernels for sm_103a.
+ *
+ * Conventions:
+ *   - every entry point returns int: 0 on success, a negative POV_GPU_E_*
+ *     code on failure.  No C++ exception crosses this boundary.
+ *   - all arrays are caller-owned and only read during the call unless the
+ *     entry point says otherwise; device memory is owned by the library.
+ *   - a scene handle may be used from several host threads; calls on one
+ *     handle are serialised by an internal mutex.
+ */
+#ifndef POVGPU_H
+#define POVGPU_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define POV_GPU_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------- */
+#define POV_GPU_OK              0
+#define POV_GPU_E_INVALID      -1  /* bad argument or malformed description    */
+#define POV_GPU_E_UNSUPPORTED  -2  /* object/material/light the GPU path lacks */
+#define POV_GPU_E_CUDA         -3  /* a CUDA runtime call failed               */
+#define POV_GPU_E_TIMEOUT      -4  /* host wait exceeded its limit             */
+#define POV_GPU_E_NOMEM        -5  /* device allocation failed                 */
+#define POV_GPU_E_DEVICE       -6  /* a kernel raised its device error word    */
+#define POV_GPU_E_NODEVICE     -7  /* no CUDA device visible                   */
+
+/* ---- object types (subset of the reference's ObjectBase zoo) ------------ */
+#define POV_OBJ_SPHERE        1   /* source/core/shape/sphere.cpp   */
+#define POV_OBJ_PLANE         2   /* source/core/shape/plane.cpp    */
+#define POV_OBJ_BOX           3   /* source/core/shape/box.cpp      */
+#define POV_OBJ_MESH          4   /* source/core/shape/mesh.cpp     */
+#define POV_OBJ_TORUS         5   /* source/core/shape/torus.cpp    */
+#define POV_OBJ_UNION         6   /* CSGUnion, source/core/shape/csg.cpp        */
+#define POV_OBJ_INTERSECTION  7   /* CSGIntersection (difference = intersection
+                                     with children 2..n inverted, as the parser
+                                     builds it: source/parser/parser.cpp:2224) */
+#define POV_OBJ_MERGE         8   /* CSGMerge                                  */
+
+/* ---- object flags (meaning of the reference's object.h:88-117 bits) ----- */
+#define POV_FLAG_INVERTED       0x0001  /* INVERTED_FLAG                      */
+#define POV_FLAG_NO_SHADOW      0x0002  /* NO_SHADOW_FLAG                     */
+#define POV_FLAG_HAS_TRANS      0x0004  /* object carries a TRANSFORM         */
+#define POV_FLAG_INFINITE       0x0008  /* INFINITE_FLAG (unbounded object)   */
+#define POV_FLAG_DOUBLE_ILLUM   0x0010  /* DOUBLE_ILLUMINATE_FLAG             */
+#define POV_FLAG_NO_REFLECTION  0x0020  /* NO_REFLECTION_FLAG                 */
+#define POV_FLAG_NO_IMAGE       0x0040  /* NO_IMAGE_FLAG                      */
+
+/*
+ * One object of SceneData::objects, flattened in depth-first order: a CSG
+ * node is followed immediately by its children (recursively), so the hit
+ * object id reported by the library is the index in this array of the leaf
+ * primitive that was hit (Intersection::Object in the reference).
+ *
+ * Parameter layout of p[] by type:
+ *   SPHERE  p[0..2] centre, p[3] radius
+ *   PLANE   p[0..2] normal, p[3] Distance (the reference's stored value, i.e.
+ *           minus the SDL offset: plane{y,-10} stores Distance=+10)
+ *   BOX     p[0..2] corner1 (min), p[3..5] corner2 (max)
+ *   TORUS   p[0] major radius, p[1] minor radius (always with a transform)
+ *   MESH    mesh = index into PovGpuSceneDesc.meshes
+ *   CSG     first_child/num_children index this array
+ * trans[] is the object's TRANSFORM as two row-major 4x4 matrices:
+ * trans[0..15] = forward matrix (object -> world), trans[16..31] = inverse.
+ */
+typedef struct PovGpuObject {
+    int32_t type;
+    int32_t flags;
+    int32_t material;      /* index into materials; -1 = inherit from parent */
+    int32_t parent;        /* index of the enclosing CSG object, -1 at top    */
+    int32_t first_child;
+    int32_t num_children;
+    int32_t mesh;
+    int32_t reserved;
+    double  p[8];
+    double  trans[32];
+} PovGpuObject;
+
+/*
+ * Texture of an object: a plain rgb pigment and a finish (the subset of
+ * FINISH, source/core/material/texture.h, that the GPU path shades).  Values
+ * are stored as the parser leaves them, e.g. roughness is 1/roughness.
+ */
+typedef struct PovGpuMaterial {
+    float pigment[5];          /* r g b filter transmit                       */
+    float ambient[3];
+    float emission[3];
+    float diffuse;
+    float diffuse_back;
+    float brilliance;
+    float brilliance_adjust;   /* FINISH::BrillianceAdjust                    */
+    float brilliance_adjust_rad;
+    float phong;
+    float phong_size;
+    float specular;
+    float roughness;           /* stored inverted, as the parser does         */
+    float metallic;
+    float reflection_max[3];
+    float reflection_min[3];
+    float reflection_falloff;
+    float reflect_exp;
+    float reflect_metallic;
+    int32_t reflection_fresnel;
+    int32_t conserve_energy;
+    float fresnel;
+    float crand;
+    float irid;
+} PovGpuMaterial;
+
+/* Light source: point light or rectangular area light (LightSource,
+ * source/core/scene/object.h:313). */
+#define POV_LIGHT_POINT 0
+#define POV_LIGHT_AREA  1
+typedef struct PovGpuLight {
+    double  center[3];
+    float   colour[3];
+    int32_t kind;
+    double  axis1[3];
+    double  axis2[3];
+    int32_t area_size1;
+    int32_t area_size2;
+    int32_t adaptive_level;
+    int32_t jitter;
+    int32_t circular;
+    int32_t orient;
+    float   fade_distance;
+    float   fade_power;
+} PovGpuLight;
+
+/* mesh2 data as the parser reads it: vertex_vectors, normal_vectors and the
+ * face/normal index triples. */
+typedef struct PovGpuMesh {
+    const float*   vertices;       /* 3 * num_vertices                       */
+    const float*   normals;        /* 3 * num_normals (may be NULL)          */
+    const int32_t* face_indices;   /* 3 * num_triangles                      */
+    const int32_t* normal_indices; /* 3 * num_triangles (NULL = flat)        */
+    int32_t        num_vertices;
+    int32_t        num_normals;
+    int32_t        num_triangles;
+    int32_t        reserved;
+} PovGpuMesh;
+
+/* Perspective camera after Parse_Camera (source/parser/parser.cpp:1335). */
+typedef struct PovGpuCamera {
+    double  location[3];
+    double  direction[3];
+    double  right[3];
+    double  up[3];
+    int32_t type;                  /* 0 = perspective (the only type taken) */
+    int32_t reserved;
+} PovGpuCamera;
+
+/* Radiosity settings (SceneRadiositySettings, radiosity.h:139-166). */
+typedef struct PovGpuRadiosity {
+    int32_t enabled;
+    int32_t count;
+    int32_t recursion_limit;
+    int32_t nearest_count;
+    float   error_bound;
+    float   low_error_factor;
+    float   gray_threshold;
+    float   minimum_reuse;
+    float   maximum_reuse;
+    float   brightness;
+    float   pretrace_start;
+    float   pretrace_end;
+    float   adc_bailout;
+    int32_t always_sample;
+    int32_t normal;
+    int32_t media;
+} PovGpuRadiosity;
+
+typedef struct PovGpuSceneDesc {
+    uint32_t              abi_version;   /* POV_GPU_ABI_VERSION */
+    int32_t               num_objects;
+    const PovGpuObject*   objects;
+    int32_t               num_materials;
+    const PovGpuMaterial* materials;
+    int32_t               num_lights;
+    const PovGpuLight*    lights;
+    int32_t               num_meshes;
+    const PovGpuMesh*     meshes;
+    PovGpuCamera          camera;
+    float                 background[4];   /* rgb + transmit             */
+    float                 ambient_light[3];
+    int32_t               max_trace_level;
+    float                 adc_bailout;
+    int32_t               language_version; /* e.g. 370                  */
+    PovGpuRadiosity       radiosity;
+} PovGpuSceneDesc;
+
+/* A render block, as POVRect (inclusive bounds) plus its serial number. */
+typedef struct PovGpuBlock {
+    int32_t  left, top, right, bottom;
+    uint32_t serial;
+    uint32_t reserved;
+} PovGpuBlock;
+
+/* Render options that the view applies to every block
+ * (View::StartRender, source/backend/scene/view.cpp:714-725). */
+typedef struct PovGpuRenderParams {
+    int32_t width;
+    int32_t height;
+    int32_t antialias;        /* 0 = off                                   */
+    int32_t sampling_method;  /* 1 or 2 (adaptive, tracetask.cpp:604)      */
+    float   aa_threshold;
+    int32_t aa_depth;
+    int32_t jitter;           /* 0 = off                                   */
+    float   jitter_amount;
+    int32_t quality;          /* +Q level, 9 = full                        */
+    int32_t high_reproducibility;
+} PovGpuRenderParams;
+
+/* Counters with the reference's statistic names (statisticids.h). */
+typedef struct PovGpuStats {
+    uint64_t number_of_rays;        /* Number_Of_Rays: every TraceRay call  */
+    uint64_t shadow_ray_tests;      /* Shadow_Ray_Tests                     */
+    uint64_t shadow_rays_succeeded; /* Shadow_Rays_Succeeded                */
+    uint64_t reflected_rays;        /* Reflected_Rays_Traced                */
+    uint64_t number_of_pixels;      /* Number_Of_Pixels                     */
+    uint64_t number_of_samples;     /* Number_Of_Samples (AA)               */
+    uint64_t radiosity_gathers;
+    uint64_t radiosity_reuse;
+    uint64_t device_error;          /* raw device error word (0 = none)     */
+    uint64_t reserved[7];
+} PovGpuStats;
+
+/* One closest-hit result of pov_gpu_trace_rays. */
+typedef struct PovGpuHit {
+    int32_t object;     /* flattened object id, -1 = miss                  */
+    int32_t triangle;   /* mesh triangle index, -1 for other shapes        */
+    double  t;          /* hit distance along the (normalised) ray         */
+} PovGpuHit;
+
+typedef struct PovGpuScene PovGpuScene;
+
+/*
+ * Copies the scene to the current CUDA device and builds the device trees.
+ * Replaces: nothing in the reference (it traces SceneData in place); called
+ * where View::StartRender creates its TraceTasks
+ * (source/backend/scene/view.cpp:1185-1190).  Unsupported object types,
+ * textures or lights return POV_GPU_E_UNSUPPORTED and store the offending
+ * object index in *bad_index (when non-NULL).
+ */
+int pov_gpu_scene_create(const PovGpuSceneDesc* desc, PovGpuScene** out, int32_t* bad_index);
+
+/*
+ * Traces whole render blocks: one call does for all blocks what
+ * TraceTask::SimpleSamplingM0 (source/backend/render/tracetask.cpp:403) or,
+ * with antialias on and sampling_method 2, AdaptiveSupersamplingM2
+ * (tracetask.cpp:604) does per block.  out_rgbt receives 4 floats per pixel
+ * in block order, each block's pixels row-major, exactly the vector that
+ * CompletedRectangle takes.  out_rgbt may be host or device memory.
+ * stats (optional) is overwritten with this call's counters.
+ */
+int pov_gpu_trace_blocks(PovGpuScene* scene, const PovGpuBlock* blocks, int32_t num_blocks,
+                         const PovGpuRenderParams* params, float* out_rgbt, PovGpuStats* stats);
+
+/*
+ * Closest-hit query for arbitrary rays: what Trace::FindIntersection
+ * (source/core/render/trace.cpp:285, bounding method 1) returns for each
+ * ray, reported as (object id, triangle, depth).  origins and directions
+ * hold 3 doubles per ray; directions must be normalised.  Used for parity.
+ */
+int pov_gpu_trace_rays(PovGpuScene* scene, const double* origins, const double* directions,
+                       int32_t num_rays, PovGpuHit* hits);
+
+/* Releases all device memory of the scene. */
+void pov_gpu_scene_destroy(PovGpuScene* scene);
+
+/*
+ * Makes the scene launch its kernels on `cuda_stream` (a cudaStream_t of the
+ * scene's device; NULL = the scene's own non-blocking stream).  Lets a host
+ * that owns a stream (e.g. one per View) order and time the work itself.
+ * No reference counterpart: the reference has no device streams.
+ */
+int pov_gpu_scene_set_stream(PovGpuScene* scene, void* cuda_stream);
+
+/* Pipeline stages reported by pov_gpu_get_timings. */
+#define POV_GPU_STAGE_CAMERA        0
+#define POV_GPU_STAGE_TRACE_CLOSEST 1
+#define POV_GPU_STAGE_SHADE         2
+#define POV_GPU_STAGE_TRACE_SHADOW  3
+#define POV_GPU_STAGE_RESOLVE       4
+#define POV_GPU_STAGE_FINALIZE      5
+#define POV_GPU_STAGES              8
+
+/* Profile of the last trace call.  Stage times are CUDA-event durations on
+ * the launch stream, filled when profiling bit 0 is set; the work counters
+ * (BVH node visits = child-box pairs tested, primitive tests, rays entering
+ * each traversal kernel) when bit 1 is set.  Launch counts are always kept.
+ * No reference counterpart: this is the GPU path's statistics sink, next to
+ * the reference-named counters of PovGpuStats. */
+typedef struct PovGpuTimings {
+    float    stage_ms[POV_GPU_STAGES];
+    uint32_t stage_launches[POV_GPU_STAGES];
+    uint64_t node_visits[2];     /* [0] closest-hit kernels, [1] any-hit kernels */
+    uint64_t prim_tests[2];
+    uint64_t tri_tests[2];
+    uint64_t rays_traced[2];
+    uint32_t kernel_launches;    /* all kernels of the call */
+    uint32_t reserved;
+} PovGpuTimings;
+
+#define POV_GPU_PROFILE_TIMES 1
+#define POV_GPU_PROFILE_WORK  2
+int pov_gpu_set_profiling(PovGpuScene* scene, int flags);
+int pov_gpu_get_timings(PovGpuScene* scene, PovGpuTimings* out);
+
+/* Human-readable text of a status code. */
+const char* pov_gpu_error_string(int status);
+
+/* ABI version compiled into the library. */
+int pov_gpu_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* POVGPU_H */

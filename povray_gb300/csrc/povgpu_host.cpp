@@ -1,0 +1,987 @@
+// povgpu_host.cpp -- C ABI of libpovgpu (include/povgpu.h): scene
+// validation, reference-identical mesh2 triangle setup, BVH construction,
+// device upload and the per-batch kernel sequence.
+//
+// The scene arrives as the reference's parser leaves it (SceneData walked by
+// the caller).  Shapes the GPU path does not implement are rejected here with
+// POV_GPU_E_UNSUPPORTED: there is no CPU fallback.
+#include "povgpu.h"
+#include "povgpu_internal.h"
+#include "povgpu_kernels.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <vector>
+
+using namespace povgpu;
+
+namespace {
+
+constexpr double EPSILON = 1.0e-10;   // source/core/configcore.h:153
+constexpr int TRACE_BLOCK = 128;
+
+// ------------------------------------------------------------ device mem --
+struct DevBuf {
+    void*  p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t n)
+    {
+        if (n <= bytes)
+            return cudaSuccess;
+        if (p)
+            cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        size_t want = std::max<size_t>(n, 256);
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e == cudaSuccess)
+            bytes = want;
+        return e;
+    }
+    void release()
+    {
+        if (p)
+            cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <class T> T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+template <class T>
+cudaError_t upload(DevBuf& b, const std::vector<T>& v)
+{
+    cudaError_t e = b.ensure(sizeof(T) * std::max<size_t>(v.size(), 1));
+    if (e != cudaSuccess || v.empty())
+        return e;
+    return cudaMemcpy(b.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice);
+}
+
+// ------------------------------------------------------------------ BVH --
+struct AABB {
+    float lo[3] = {INFINITY, INFINITY, INFINITY};
+    float hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    void grow(const AABB& b)
+    {
+        for (int k = 0; k < 3; k++) {
+            lo[k] = std::min(lo[k], b.lo[k]);
+            hi[k] = std::max(hi[k], b.hi[k]);
+        }
+    }
+    void grow(const float* p)
+    {
+        for (int k = 0; k < 3; k++) {
+            lo[k] = std::min(lo[k], p[k]);
+            hi[k] = std::max(hi[k], p[k]);
+        }
+    }
+    float area() const
+    {
+        float dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
+        if (dx < 0 || dy < 0 || dz < 0)
+            return 0.f;
+        return 2.f * (dx * dy + dy * dz + dz * dx);
+    }
+};
+
+struct BuildItem {
+    AABB     box;
+    float    c[3];
+    uint32_t ref;
+};
+
+// Binned-SAH binary BVH emitted as two-wide 64-byte nodes in depth-first
+// order.  Leaves hold at most LEAF_MAX_PRIMS prim references.
+class BvhBuilder {
+public:
+    std::vector<BuildItem> items;
+    std::vector<BvhNode>   nodes;
+    std::vector<uint32_t>  refs;
+    int max_depth = 0;
+
+    int build_root()
+    {
+        nodes.clear();
+        refs.clear();
+        max_depth = 0;
+        if (items.empty())
+            return 0x7fffffff;   // traversal sentinel: nothing to visit
+        AABB lb;
+        return build(0, (int)items.size(), 1, lb);   // an inner node or a leaf link
+    }
+
+private:
+    static void put(float4& f, float a, float b, float c, float d) { f = make_float4(a, b, c, d); }
+
+    void write_node(int ni, const AABB& b0, int l0, const AABB& b1, int l1)
+    {
+        BvhNode& n = nodes[ni];
+        put(n.a, b0.lo[0], b0.hi[0], b0.lo[1], b0.hi[1]);
+        put(n.b, b1.lo[0], b1.hi[0], b1.lo[1], b1.hi[1]);
+        put(n.c, b0.lo[2], b0.hi[2], b1.lo[2], b1.hi[2]);
+        n.d = make_float4(__builtin_bit_cast(float, l0), __builtin_bit_cast(float, l1), 0.f, 0.f);
+    }
+
+    int make_leaf(int begin, int end, AABB& bounds)
+    {
+        bounds = AABB();
+        uint32_t first = (uint32_t)refs.size();
+        for (int i = begin; i < end; i++) {
+            bounds.grow(items[i].box);
+            refs.push_back(items[i].ref);
+        }
+        uint32_t code = (first << 3) | (uint32_t)(end - begin - 1);
+        return (int)~code;
+    }
+
+    int build(int begin, int end, int depth, AABB& bounds)
+    {
+        max_depth = std::max(max_depth, depth);
+        int n = end - begin;
+        AABB cb;
+        for (int i = begin; i < end; i++)
+            cb.grow(items[i].c);
+        if (n <= 2)
+            return make_leaf(begin, end, bounds);
+        int axis = 0;
+        float ext[3] = {cb.hi[0] - cb.lo[0], cb.hi[1] - cb.lo[1], cb.hi[2] - cb.lo[2]};
+        int mid = -1;
+        if (ext[0] <= 0.f && ext[1] <= 0.f && ext[2] <= 0.f) {
+            if (n <= LEAF_MAX_PRIMS)
+                return make_leaf(begin, end, bounds);
+            mid = begin + n / 2;
+        } else if (depth >= 48) {
+            // depth guard: object-median split keeps the stack bounded
+            axis = ext[1] > ext[axis] ? 1 : axis;
+            axis = ext[2] > ext[axis] ? 2 : axis;
+            mid = begin + n / 2;
+            std::nth_element(items.begin() + begin, items.begin() + mid, items.begin() + end,
+                             [axis](const BuildItem& a, const BuildItem& b) { return a.c[axis] < b.c[axis]; });
+        } else {
+            constexpr int NB = 32;
+            float best_cost = INFINITY;
+            int best_axis = -1, best_bin = -1;
+            AABB total;
+            for (int i = begin; i < end; i++)
+                total.grow(items[i].box);
+            for (int ax = 0; ax < 3; ax++) {
+                if (ext[ax] <= 0.f)
+                    continue;
+                AABB bb[NB];
+                int cnt[NB] = {0};
+                float scale = NB / ext[ax];
+                for (int i = begin; i < end; i++) {
+                    int b = std::min(NB - 1, (int)((items[i].c[ax] - cb.lo[ax]) * scale));
+                    cnt[b]++;
+                    bb[b].grow(items[i].box);
+                }
+                float rarea[NB];
+                int rcnt[NB];
+                AABB acc;
+                int c = 0;
+                for (int b = NB - 1; b > 0; b--) {
+                    acc.grow(bb[b]);
+                    c += cnt[b];
+                    rarea[b] = acc.area();
+                    rcnt[b] = c;
+                }
+                acc = AABB();
+                c = 0;
+                for (int b = 0; b < NB - 1; b++) {
+                    acc.grow(bb[b]);
+                    c += cnt[b];
+                    if (c == 0 || rcnt[b + 1] == 0)
+                        continue;
+                    float cost = acc.area() * c + rarea[b + 1] * rcnt[b + 1];
+                    if (cost < best_cost) {
+                        best_cost = cost;
+                        best_axis = ax;
+                        best_bin = b;
+                    }
+                }
+            }
+            float leaf_cost = total.area() * n;
+            float trav = total.area() * 1.0f;
+            if (best_axis < 0 || (n <= 4 && best_cost + trav >= leaf_cost)) {
+                if (n <= LEAF_MAX_PRIMS)
+                    return make_leaf(begin, end, bounds);
+                mid = begin + n / 2;
+                axis = ext[1] > ext[axis] ? 1 : axis;
+                axis = ext[2] > ext[axis] ? 2 : axis;
+                std::nth_element(items.begin() + begin, items.begin() + mid, items.begin() + end,
+                                 [axis](const BuildItem& a, const BuildItem& b) { return a.c[axis] < b.c[axis]; });
+            } else {
+                float scale = NB / ext[best_axis];
+                float lo = cb.lo[best_axis];
+                auto it = std::partition(items.begin() + begin, items.begin() + end, [&](const BuildItem& x) {
+                    int b = std::min(NB - 1, (int)((x.c[best_axis] - lo) * scale));
+                    return b <= best_bin;
+                });
+                mid = (int)(it - items.begin());
+                if (mid == begin || mid == end)
+                    mid = begin + n / 2;
+            }
+        }
+        int ni = (int)nodes.size();
+        nodes.push_back(BvhNode{});
+        AABB b0, b1;
+        int l0 = build(begin, mid, depth + 1, b0);
+        int l1 = build(mid, end, depth + 1, b1);
+        write_node(ni, b0, l0, b1, l1);
+        bounds = b0;
+        bounds.grow(b1);
+        return ni;
+    }
+};
+
+// ------------------------------------------------- mesh2 triangle setup --
+static int max3_coordinate(double x, double y, double z)
+{
+    if (x > y)
+        return x > z ? 0 : 2;
+    return y > z ? 1 : 2;
+}
+
+struct V3d {
+    double x, y, z;
+};
+static V3d vsub(V3d a, V3d b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+static V3d vcross(V3d a, V3d b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+static double vlen(V3d a) { return std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+
+}  // namespace
+
+// ---------------------------------------------------------------- scene --
+struct PovGpuScene {
+    std::mutex  lock;
+    int         device = 0;
+    cudaStream_t stream = nullptr;
+    DeviceScene S{};
+    int         stack_depth = 32;
+    int         num_sms = 148;
+    // persistent scene data
+    DevBuf nodes, refs, tri_v0, tri_e1, tri_e2, tri_global, tri_shade, tri_normal, tri_local, normals;
+    DevBuf spheres, sphere_obj, planes, plane_obj, objects, materials, lights;
+    // per-batch work buffers (grown on demand, reused)
+    DevBuf blocks, block_off, qA, qB, pathA, pathB, hits, paths, slot_contrib, sq, sq_slot, blocked, out,
+        counters, stats, err, rays_in;
+    int     num_lights = 0;
+    int     max_trace_level = 1;
+    // streams and profiling
+    cudaStream_t user_stream = nullptr;
+    int          profiling = 0;
+    PovGpuTimings timings{};
+    std::vector<cudaEvent_t> events;   // pool, created on first profiled call
+    DevBuf       wcount;
+
+    cudaStream_t active() const { return user_stream ? user_stream : stream; }
+
+    void release_all()
+    {
+        for (cudaEvent_t e : events)
+            cudaEventDestroy(e);
+        events.clear();
+        wcount.release();
+        DevBuf* all[] = {&nodes,  &refs,       &tri_v0,   &tri_e1,    &tri_e2,     &tri_global, &tri_shade,
+                         &tri_normal, &tri_local, &normals,  &spheres,   &sphere_obj, &planes,     &plane_obj,
+                         &objects, &materials,  &lights,   &blocks,    &block_off,  &qA,         &qB,
+                         &pathA,   &pathB,      &hits,     &paths,     &slot_contrib, &sq,       &sq_slot,
+                         &blocked, &out,        &counters, &stats,     &err,        &rays_in};
+        for (DevBuf* b : all)
+            b->release();
+        if (stream)
+            cudaStreamDestroy(stream);
+        stream = nullptr;
+    }
+};
+
+namespace {
+
+#define CK(x)                                   \
+    do {                                        \
+        cudaError_t e_ = (x);                   \
+        if (e_ != cudaSuccess)                  \
+            return e_ == cudaErrorMemoryAllocation ? POV_GPU_E_NOMEM : POV_GPU_E_CUDA; \
+    } while (0)
+
+int validate(const PovGpuSceneDesc* d, int32_t* bad)
+{
+    if (!d || d->abi_version != POV_GPU_ABI_VERSION || d->num_objects < 0 || d->num_materials < 1 ||
+        d->num_lights < 0 || d->num_meshes < 0 || (d->num_objects > 0 && !d->objects) || !d->materials)
+        return POV_GPU_E_INVALID;
+    if (d->camera.type != 0) {
+        if (bad) *bad = -1;
+        return POV_GPU_E_UNSUPPORTED;
+    }
+    if (d->radiosity.enabled)
+        return POV_GPU_E_UNSUPPORTED;
+    for (int i = 0; i < d->num_lights; i++)
+        if (d->lights[i].kind != POV_LIGHT_POINT || d->lights[i].fade_power > 0.0f)
+            return POV_GPU_E_UNSUPPORTED;
+    for (int i = 0; i < d->num_materials; i++) {
+        const PovGpuMaterial& m = d->materials[i];
+        // opaque plain pigments and the classic finish terms only
+        if (m.pigment[3] != 0.0f || m.pigment[4] != 0.0f || m.reflection_fresnel || m.fresnel != 0.0f ||
+            m.metallic != 0.0f || m.reflect_metallic != 0.0f || m.reflect_exp != 1.0f || m.irid != 0.0f ||
+            m.crand != 0.0f || m.diffuse_back != 0.0f || m.conserve_energy)
+            return POV_GPU_E_UNSUPPORTED;
+    }
+    for (int i = 0; i < d->num_objects; i++) {
+        const PovGpuObject& o = d->objects[i];
+        bool ok = (o.type == POV_OBJ_SPHERE || o.type == POV_OBJ_PLANE || o.type == POV_OBJ_MESH) &&
+                  !(o.flags & POV_FLAG_HAS_TRANS) && o.parent < 0;
+        if (o.material < 0 || o.material >= d->num_materials)
+            ok = false;
+        if (o.type == POV_OBJ_MESH && (o.mesh < 0 || o.mesh >= d->num_meshes))
+            ok = false;
+        if (!ok) {
+            if (bad) *bad = i;
+            return o.type >= POV_OBJ_SPHERE && o.type <= POV_OBJ_MERGE && o.material >= 0 ? POV_GPU_E_UNSUPPORTED
+                                                                                          : POV_GPU_E_INVALID;
+        }
+    }
+    for (int i = 0; i < d->num_meshes; i++) {
+        const PovGpuMesh& m = d->meshes[i];
+        if (m.num_triangles < 0 || m.num_vertices < 0 || (m.num_triangles > 0 && (!m.face_indices || !m.vertices)))
+            return POV_GPU_E_INVALID;
+        for (int t = 0; t < 3 * m.num_triangles; t++) {
+            if (m.face_indices[t] < 0 || m.face_indices[t] >= m.num_vertices)
+                return POV_GPU_E_INVALID;
+            if (m.normal_indices && (m.normal_indices[t] < 0 || m.normal_indices[t] >= m.num_normals))
+                return POV_GPU_E_INVALID;
+        }
+    }
+    return POV_GPU_OK;
+}
+
+DevMaterial make_material(const PovGpuMaterial& m, const float* ambient_light)
+{
+    DevMaterial d{};
+    d.pigment = make_float4(m.pigment[0], m.pigment[1], m.pigment[2], m.pigment[3]);
+    // emission + ambient * ambient_light (radiosity off, trace.cpp:984-1004)
+    d.emission = make_float4(m.emission[0] + m.ambient[0] * ambient_light[0],
+                             m.emission[1] + m.ambient[1] * ambient_light[1],
+                             m.emission[2] + m.ambient[2] * ambient_light[2], 0.f);
+    float wmax = std::max(m.reflection_max[0], std::max(m.reflection_max[1], m.reflection_max[2]));
+    float wmin = std::max(m.reflection_min[0], std::max(m.reflection_min[1], m.reflection_min[2]));
+    d.reflect = make_float4(m.reflection_max[0], m.reflection_max[1], m.reflection_max[2], m.reflection_falloff);
+    d.reflect_min = make_float4(m.reflection_min[0], m.reflection_min[1], m.reflection_min[2], std::max(wmax, wmin));
+    d.diffuse = m.diffuse * m.brilliance_adjust;
+    d.brilliance = m.brilliance;
+    d.phong = m.phong;
+    d.phong_size = m.phong_size;
+    d.specular = m.specular;
+    d.roughness = m.roughness;
+    bool anyr = false;
+    for (int k = 0; k < 3; k++)
+        anyr = anyr || m.reflection_max[k] != 0.f || m.reflection_min[k] != 0.f;
+    d.has_reflection = anyr ? 1 : 0;
+    return d;
+}
+
+int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
+{
+    BvhBuilder bvh;
+    std::vector<float4> spheres, planes, tri_v0, tri_e1, tri_e2, tri_normal, normals;
+    std::vector<int32_t> sphere_obj, plane_obj, tri_global, tri_local;
+    std::vector<int4> tri_shade;
+    std::vector<ObjectShade> objects((size_t)std::max(d->num_objects, 1));
+    std::vector<int> mesh_normal_base((size_t)std::max(d->num_meshes, 1), 0);
+
+    // mesh normals: Parse_Mesh2 normalises every normal_vectors entry
+    // (source/parser/parser.cpp:4143-4152)
+    for (int mi = 0; mi < d->num_meshes; mi++) {
+        const PovGpuMesh& m = d->meshes[mi];
+        mesh_normal_base[mi] = (int)normals.size();
+        for (int i = 0; i < m.num_normals && m.normals; i++) {
+            double x = m.normals[3 * i], y = m.normals[3 * i + 1], z = m.normals[3 * i + 2];
+            if (std::fabs(x) < EPSILON && std::fabs(y) < EPSILON && std::fabs(z) < EPSILON)
+                x = 1.0;
+            double l = std::sqrt(x * x + y * y + z * z);
+            normals.push_back(make_float4((float)(x / l), (float)(y / l), (float)(z / l), 0.f));
+        }
+    }
+
+    for (int i = 0; i < d->num_objects; i++) {
+        const PovGpuObject& o = d->objects[i];
+        objects[i].material = o.material;
+        objects[i].flags = (o.flags & POV_FLAG_INVERTED ? 1 : 0) | (o.flags & POV_FLAG_DOUBLE_ILLUM ? 16 : 0);
+        objects[i].type = o.type;
+        objects[i].mesh = o.mesh;
+        if (o.type == POV_OBJ_SPHERE) {
+            uint32_t idx = (uint32_t)spheres.size();
+            spheres.push_back(make_float4((float)o.p[0], (float)o.p[1], (float)o.p[2], (float)o.p[3]));
+            sphere_obj.push_back(i);
+            BuildItem it;
+            for (int k = 0; k < 3; k++) {
+                // bounds rounded outward so the FP32 box always contains the sphere
+                it.box.lo[k] = std::nextafter((float)(o.p[k] - o.p[3]), -INFINITY);
+                it.box.hi[k] = std::nextafter((float)(o.p[k] + o.p[3]), INFINITY);
+                it.c[k] = (float)o.p[k];
+            }
+            it.ref = (PK_SPHERE << PRIM_KIND_SHIFT) | idx;
+            bvh.items.push_back(it);
+        } else if (o.type == POV_OBJ_PLANE) {
+            planes.push_back(make_float4((float)o.p[0], (float)o.p[1], (float)o.p[2], (float)o.p[3]));
+            plane_obj.push_back(i);
+        } else if (o.type == POV_OBJ_MESH) {
+            const PovGpuMesh& m = d->meshes[o.mesh];
+            int nb = mesh_normal_base[o.mesh];
+            for (int t = 0; t < m.num_triangles; t++) {
+                const int32_t* f = m.face_indices + 3 * t;
+                int p1 = f[0], p2 = f[1], p3 = f[2];
+                int n1 = 0, n2 = 0, n3 = 0;
+                bool smooth = false;
+                // without normal_indices the parser reuses the face indices when
+                // there is one normal per vertex (parser.cpp:4488-4502)
+                const int32_t* ni = m.normal_indices ? m.normal_indices
+                                    : (m.num_normals == m.num_vertices ? m.face_indices : nullptr);
+                if (ni && m.num_normals > 0 && m.normals) {
+                    n1 = ni[3 * t];
+                    n2 = ni[3 * t + 1];
+                    n3 = ni[3 * t + 2];
+                    const float4 a = normals[nb + n1], b = normals[nb + n2], c = normals[nb + n3];
+                    double d1x = (double)a.x - b.x, d1y = (double)a.y - b.y, d1z = (double)a.z - b.z;
+                    double d2x = (double)a.x - c.x, d2y = (double)a.y - c.y, d2z = (double)a.z - c.z;
+                    double l1 = d1x * d1x + d1y * d1y + d1z * d1z, l2 = d2x * d2x + d2y * d2y + d2z * d2z;
+                    smooth = (std::fabs(l1) > EPSILON) || (std::fabs(l2) > EPSILON);   // parser.cpp:4545
+                }
+                auto V = [&](int k) {
+                    return V3d{(double)m.vertices[3 * k], (double)m.vertices[3 * k + 1], (double)m.vertices[3 * k + 2]};
+                };
+                V3d P1 = V(p1), P2 = V(p2), P3 = V(p3);
+                // Compute_Mesh_Triangle (source/core/shape/mesh.cpp:838-982)
+                V3d N = vcross(vsub(P3, P1), vsub(P2, P1));
+                double len = vlen(N);
+                float4 gn = make_float4(0.f, 0.f, 0.f, __builtin_bit_cast(float, i));
+                if (len != 0.0) {
+                    N = {N.x / len, N.y / len, N.z / len};
+                    gn.x = (float)N.x;
+                    gn.y = (float)N.y;
+                    gn.z = (float)N.z;
+                    int axis = max3_coordinate(std::fabs(N.x), std::fabs(N.y), std::fabs(N.z));
+                    bool swap;
+                    if (axis == 0)
+                        swap = (P2.y - P3.y) * (P2.z - P1.z) < (P2.z - P3.z) * (P2.y - P1.y);
+                    else if (axis == 1)
+                        swap = (P2.x - P3.x) * (P2.z - P1.z) < (P2.z - P3.z) * (P2.x - P1.x);
+                    else
+                        swap = (P2.x - P3.x) * (P2.y - P1.y) < (P2.y - P3.y) * (P2.x - P1.x);
+                    if (swap) {
+                        std::swap(p1, p2);
+                        std::swap(P1, P2);
+                        if (smooth)
+                            std::swap(n1, n2);
+                    }
+                }
+                int g = (int)tri_v0.size();
+                float v0[3] = {(float)P1.x, (float)P1.y, (float)P1.z};
+                float v1[3] = {(float)P2.x, (float)P2.y, (float)P2.z};
+                float v2[3] = {(float)P3.x, (float)P3.y, (float)P3.z};
+                tri_v0.push_back(make_float4(v0[0], v0[1], v0[2], 0.f));
+                tri_e1.push_back(make_float4(v1[0] - v0[0], v1[1] - v0[1], v1[2] - v0[2], 0.f));
+                tri_e2.push_back(make_float4(v2[0] - v0[0], v2[1] - v0[1], v2[2] - v0[2], 0.f));
+                tri_normal.push_back(gn);
+                tri_shade.push_back(make_int4(nb + n1, nb + n2, nb + n3, smooth ? 1 : 0));
+                tri_local.push_back(t);
+                BuildItem it;
+                it.box = AABB();
+                it.box.grow(v0);
+                it.box.grow(v1);
+                it.box.grow(v2);
+                for (int k = 0; k < 3; k++)
+                    it.c[k] = 0.5f * (it.box.lo[k] + it.box.hi[k]);
+                it.ref = (PK_TRIANGLE << PRIM_KIND_SHIFT) | (uint32_t)g;
+                bvh.items.push_back(it);
+            }
+        }
+    }
+    if (tri_v0.size() >= (size_t)PRIM_INDEX_MASK || spheres.size() >= (size_t)PRIM_INDEX_MASK ||
+        bvh.items.size() >= (1u << 28))
+        return POV_GPU_E_UNSUPPORTED;
+
+    int root = bvh.build_root();
+    sc->stack_depth = std::max(8, bvh.max_depth + 2);
+    if (sc->stack_depth > 96)
+        return POV_GPU_E_UNSUPPORTED;
+
+    // reorder triangle records into leaf order (prim refs then index the
+    // leaf-order slot directly, so a leaf's triangles are contiguous)
+    std::vector<float4> lv0, le1, le2;
+    lv0.reserve(tri_v0.size());
+    le1.reserve(tri_v0.size());
+    le2.reserve(tri_v0.size());
+    for (uint32_t& r : bvh.refs) {
+        if ((r >> PRIM_KIND_SHIFT) == PK_TRIANGLE) {
+            uint32_t g = r & PRIM_INDEX_MASK;
+            uint32_t slot = (uint32_t)lv0.size();
+            lv0.push_back(tri_v0[g]);
+            le1.push_back(tri_e1[g]);
+            le2.push_back(tri_e2[g]);
+            tri_global.push_back((int32_t)g);
+            r = (PK_TRIANGLE << PRIM_KIND_SHIFT) | slot;
+        }
+    }
+
+    std::vector<DevMaterial> mats((size_t)d->num_materials);
+    for (int i = 0; i < d->num_materials; i++)
+        mats[i] = make_material(d->materials[i], d->ambient_light);
+    std::vector<DevLight> lights((size_t)std::max(d->num_lights, 1));
+    for (int i = 0; i < d->num_lights; i++) {
+        const PovGpuLight& L = d->lights[i];
+        lights[i].center = make_float4((float)L.center[0], (float)L.center[1], (float)L.center[2], (float)L.kind);
+        lights[i].colour = make_float4(L.colour[0], L.colour[1], L.colour[2], 0.f);
+    }
+
+    CK(upload(sc->nodes, bvh.nodes));
+    CK(upload(sc->refs, bvh.refs));
+    CK(upload(sc->tri_v0, lv0));
+    CK(upload(sc->tri_e1, le1));
+    CK(upload(sc->tri_e2, le2));
+    CK(upload(sc->tri_global, tri_global));
+    CK(upload(sc->tri_shade, tri_shade));
+    CK(upload(sc->tri_normal, tri_normal));
+    CK(upload(sc->tri_local, tri_local));
+    CK(upload(sc->normals, normals));
+    CK(upload(sc->spheres, spheres));
+    CK(upload(sc->sphere_obj, sphere_obj));
+    CK(upload(sc->planes, planes));
+    CK(upload(sc->plane_obj, plane_obj));
+    CK(upload(sc->objects, objects));
+    CK(upload(sc->materials, mats));
+    CK(upload(sc->lights, lights));
+
+    DeviceScene& S = sc->S;
+    S.nodes = sc->nodes.as<BvhNode>();
+    S.prim_refs = sc->refs.as<uint32_t>();
+    S.root = root;
+    S.tri_v0 = sc->tri_v0.as<float4>();
+    S.tri_e1 = sc->tri_e1.as<float4>();
+    S.tri_e2 = sc->tri_e2.as<float4>();
+    S.tri_global = sc->tri_global.as<int32_t>();
+    S.tri_shade = sc->tri_shade.as<int4>();
+    S.tri_normal = sc->tri_normal.as<float4>();
+    S.tri_local = sc->tri_local.as<int32_t>();
+    S.normals = sc->normals.as<float4>();
+    S.spheres = sc->spheres.as<float4>();
+    S.sphere_obj = sc->sphere_obj.as<int32_t>();
+    S.planes = sc->planes.as<float4>();
+    S.plane_obj = sc->plane_obj.as<int32_t>();
+    S.num_planes = (int)planes.size();
+    S.objects = sc->objects.as<ObjectShade>();
+    S.materials = sc->materials.as<DevMaterial>();
+    S.lights = sc->lights.as<DevLight>();
+    S.num_lights = d->num_lights;
+    S.max_trace_level = d->max_trace_level;
+    S.adc_bailout = d->adc_bailout;
+    S.background = make_float4(d->background[0], d->background[1], d->background[2], d->background[3]);
+    for (int k = 0; k < 3; k++) {
+        S.cam_loc[k] = d->camera.location[k];
+        S.cam_dir[k] = d->camera.direction[k];
+        S.cam_right[k] = d->camera.right[k];
+        S.cam_up[k] = d->camera.up[k];
+    }
+    sc->num_lights = d->num_lights;
+    sc->max_trace_level = d->max_trace_level;
+    return POV_GPU_OK;
+}
+
+// Counter slots in sc->counters.
+enum {
+    C_QA = 0,     // count of queue A
+    C_QB = 1,     // count of queue B
+    C_SQ = 2,     // shadow queue
+    C_W0 = 3,     // work counter, closest-hit
+    C_W1 = 4,     // work counter, any-hit
+    C_NUM = 8
+};
+
+int check_device_error(PovGpuScene* sc, PovGpuStats* stats, unsigned long long* host_stats)
+{
+    uint32_t errw = 0;
+    cudaStream_t st = sc->active();
+    CK(cudaMemcpyAsync(&errw, sc->err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(host_stats, sc->stats.p, sizeof(unsigned long long) * ST_COUNT, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        stats->number_of_rays = host_stats[ST_RAYS];
+        stats->shadow_ray_tests = host_stats[ST_SHADOW_TESTS];
+        stats->shadow_rays_succeeded = host_stats[ST_SHADOW_SUCCEEDED];
+        stats->reflected_rays = host_stats[ST_REFLECTED];
+        stats->device_error = errw;
+    }
+    return errw ? POV_GPU_E_DEVICE : POV_GPU_OK;
+}
+
+// Records per-stage CUDA events on the launch stream (profiling bit 0) and
+// counts launches; stage durations are summed after the final sync.
+class StageClock {
+public:
+    StageClock(PovGpuScene* sc, cudaStream_t st) : sc_(sc), st_(st)
+    {
+        std::memset(&sc_->timings, 0, sizeof(sc_->timings));
+        timing_ = (sc_->profiling & POV_GPU_PROFILE_TIMES) != 0;
+    }
+    cudaError_t begin(int stage)
+    {
+        cur_ = stage;
+        if (!timing_)
+            return cudaSuccess;
+        cudaError_t e = next_event(a_);
+        if (e == cudaSuccess)
+            e = cudaEventRecord(a_, st_);
+        return e;
+    }
+    cudaError_t end(int launches = 1)
+    {
+        sc_->timings.stage_launches[cur_] += launches;
+        sc_->timings.kernel_launches += launches;
+        if (!timing_)
+            return cudaSuccess;
+        cudaEvent_t b;
+        cudaError_t e = next_event(b);
+        if (e == cudaSuccess)
+            e = cudaEventRecord(b, st_);
+        marks_.push_back({cur_, a_, b});
+        return e;
+    }
+    void collect()
+    {
+        for (auto& m : marks_) {
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, m.a, m.b) == cudaSuccess)
+                sc_->timings.stage_ms[m.stage] += ms;
+        }
+    }
+
+private:
+    struct Mark {
+        int stage;
+        cudaEvent_t a, b;
+    };
+    cudaError_t next_event(cudaEvent_t& ev)
+    {
+        if (used_ >= sc_->events.size()) {
+            cudaEvent_t e;
+            cudaError_t r = cudaEventCreate(&e);
+            if (r != cudaSuccess)
+                return r;
+            sc_->events.push_back(e);
+        }
+        ev = sc_->events[used_++];
+        return cudaSuccess;
+    }
+    PovGpuScene* sc_;
+    cudaStream_t st_;
+    bool timing_ = false;
+    int cur_ = 0;
+    size_t used_ = 0;
+    cudaEvent_t a_ = nullptr;
+    std::vector<Mark> marks_;
+};
+
+}  // namespace
+
+extern "C" {
+
+int pov_gpu_scene_set_stream(PovGpuScene* sc, void* cuda_stream)
+{
+    if (!sc)
+        return POV_GPU_E_INVALID;
+    std::lock_guard<std::mutex> g(sc->lock);
+    sc->user_stream = reinterpret_cast<cudaStream_t>(cuda_stream);
+    return POV_GPU_OK;
+}
+
+int pov_gpu_set_profiling(PovGpuScene* sc, int flags)
+{
+    if (!sc || (flags & ~(POV_GPU_PROFILE_TIMES | POV_GPU_PROFILE_WORK)))
+        return POV_GPU_E_INVALID;
+    std::lock_guard<std::mutex> g(sc->lock);
+    sc->profiling = flags;
+    if ((flags & POV_GPU_PROFILE_WORK) && sc->wcount.ensure(sizeof(unsigned long long) * 8) != cudaSuccess)
+        return POV_GPU_E_NOMEM;
+    return POV_GPU_OK;
+}
+
+int pov_gpu_get_timings(PovGpuScene* sc, PovGpuTimings* out)
+{
+    if (!sc || !out)
+        return POV_GPU_E_INVALID;
+    std::lock_guard<std::mutex> g(sc->lock);
+    *out = sc->timings;
+    return POV_GPU_OK;
+}
+
+int pov_gpu_abi_version(void) { return POV_GPU_ABI_VERSION; }
+
+const char* pov_gpu_error_string(int status)
+{
+    switch (status) {
+    case POV_GPU_OK: return "ok";
+    case POV_GPU_E_INVALID: return "invalid argument or scene description";
+    case POV_GPU_E_UNSUPPORTED: return "object, texture or light not supported by the GPU trace path";
+    case POV_GPU_E_CUDA: return "CUDA runtime error";
+    case POV_GPU_E_TIMEOUT: return "device wait timed out";
+    case POV_GPU_E_NOMEM: return "device memory allocation failed";
+    case POV_GPU_E_DEVICE: return "kernel reported an error in its device error word";
+    case POV_GPU_E_NODEVICE: return "no CUDA device";
+    default: return "unknown status";
+    }
+}
+
+int pov_gpu_scene_create(const PovGpuSceneDesc* desc, PovGpuScene** out, int32_t* bad_index)
+{
+    if (bad_index)
+        *bad_index = -1;
+    if (!out)
+        return POV_GPU_E_INVALID;
+    *out = nullptr;
+    int st = validate(desc, bad_index);
+    if (st != POV_GPU_OK)
+        return st;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1)
+        return POV_GPU_E_NODEVICE;
+    PovGpuScene* sc = new (std::nothrow) PovGpuScene();
+    if (!sc)
+        return POV_GPU_E_NOMEM;
+    cudaGetDevice(&sc->device);
+    cudaDeviceGetAttribute(&sc->num_sms, cudaDevAttrMultiProcessorCount, sc->device);
+    if (cudaStreamCreateWithFlags(&sc->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete sc;
+        return POV_GPU_E_CUDA;
+    }
+    st = build_scene(sc, desc);
+    if (st == POV_GPU_OK) {
+        if (sc->counters.ensure(sizeof(int) * C_NUM) != cudaSuccess ||
+            sc->stats.ensure(sizeof(unsigned long long) * ST_COUNT) != cudaSuccess ||
+            sc->err.ensure(sizeof(uint32_t) * 4) != cudaSuccess)
+            st = POV_GPU_E_NOMEM;
+    }
+    if (st != POV_GPU_OK) {
+        sc->release_all();
+        delete sc;
+        return st;
+    }
+    *out = sc;
+    return POV_GPU_OK;
+}
+
+void pov_gpu_scene_destroy(PovGpuScene* scene)
+{
+    if (!scene)
+        return;
+    cudaStreamSynchronize(scene->active());
+    scene->release_all();
+    delete scene;
+}
+
+int pov_gpu_trace_blocks(PovGpuScene* sc, const PovGpuBlock* blocks, int32_t num_blocks,
+                         const PovGpuRenderParams* params, float* out_rgbt, PovGpuStats* stats)
+{
+    if (!sc || !params || num_blocks < 0 || (num_blocks > 0 && (!blocks || !out_rgbt)))
+        return POV_GPU_E_INVALID;
+    if (params->antialias)
+        return POV_GPU_E_UNSUPPORTED;
+    if (params->width <= 0 || params->height <= 0)
+        return POV_GPU_E_INVALID;
+    std::lock_guard<std::mutex> g(sc->lock);
+    cudaSetDevice(sc->device);
+    if (num_blocks == 0) {
+        if (stats)
+            std::memset(stats, 0, sizeof(*stats));
+        return POV_GPU_OK;
+    }
+    std::vector<int4> hb((size_t)num_blocks);
+    std::vector<int> off((size_t)num_blocks + 1, 0);
+    long long npix = 0;
+    for (int i = 0; i < num_blocks; i++) {
+        const PovGpuBlock& b = blocks[i];
+        if (b.left < 0 || b.top < 0 || b.right < b.left || b.bottom < b.top || b.right >= params->width ||
+            b.bottom >= params->height)
+            return POV_GPU_E_INVALID;
+        hb[i] = make_int4(b.left, b.top, b.right, b.bottom);
+        off[i] = (int)npix;
+        npix += (long long)(b.right - b.left + 1) * (b.bottom - b.top + 1);
+    }
+    off[num_blocks] = (int)npix;
+    if (npix > (1ll << 28))
+        return POV_GPU_E_INVALID;
+    const int n = (int)npix;
+    const int nl = std::max(sc->num_lights, 1);
+    const size_t maxq = (size_t)n;
+    CK(sc->blocks.ensure(sizeof(int4) * num_blocks));
+    CK(sc->block_off.ensure(sizeof(int) * (num_blocks + 1)));
+    CK(sc->qA.ensure(sizeof(QRay) * maxq));
+    CK(sc->qB.ensure(sizeof(QRay) * maxq));
+    CK(sc->pathA.ensure(sizeof(int) * maxq));
+    CK(sc->pathB.ensure(sizeof(int) * maxq));
+    CK(sc->hits.ensure(sizeof(QHit) * maxq));
+    CK(sc->paths.ensure(sizeof(PathState) * maxq));
+    CK(sc->slot_contrib.ensure(sizeof(float4) * maxq * nl));
+    CK(sc->sq.ensure(sizeof(QRay) * maxq * nl));
+    CK(sc->sq_slot.ensure(sizeof(int) * maxq * nl));
+    CK(sc->blocked.ensure(maxq * nl));
+
+    cudaPointerAttributes pa{};
+    bool out_on_device = cudaPointerGetAttributes(&pa, out_rgbt) == cudaSuccess &&
+                         (pa.type == cudaMemoryTypeDevice || pa.type == cudaMemoryTypeManaged);
+    cudaGetLastError();
+    float4* dout = reinterpret_cast<float4*>(out_rgbt);
+    if (!out_on_device) {
+        CK(sc->out.ensure(sizeof(float4) * maxq));
+        dout = sc->out.as<float4>();
+    }
+
+    cudaStream_t st = sc->active();
+    int* cnt = sc->counters.as<int>();
+    unsigned long long* dstats = sc->stats.as<unsigned long long>();
+    uint32_t* derr = sc->err.as<uint32_t>();
+    unsigned long long* wc = (sc->profiling & POV_GPU_PROFILE_WORK) ? sc->wcount.as<unsigned long long>() : nullptr;
+    StageClock clk(sc, st);
+    CK(cudaMemcpyAsync(sc->blocks.p, hb.data(), sizeof(int4) * num_blocks, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(sc->block_off.p, off.data(), sizeof(int) * (num_blocks + 1), cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(sc->counters.p, 0, sizeof(int) * C_NUM, st));
+    CK(cudaMemsetAsync(sc->stats.p, 0, sizeof(unsigned long long) * ST_COUNT, st));
+    CK(cudaMemsetAsync(sc->err.p, 0, sizeof(uint32_t) * 4, st));
+    if (wc)
+        CK(cudaMemsetAsync(wc, 0, sizeof(unsigned long long) * 8, st));
+
+    const DeviceScene& S = sc->S;
+    const int grid_trace = sc->num_sms * 8;
+    const int grid_shade = std::max(1, std::min(sc->num_sms * 16, (n + 127) / 128));
+    QRay* qcur = sc->qA.as<QRay>();
+    QRay* qnext = sc->qB.as<QRay>();
+    int* pcur = sc->pathA.as<int>();
+    int* pnext = sc->pathB.as<int>();
+    int* ccur = cnt + C_QA;
+    int* cnext = cnt + C_QB;
+    CK(clk.begin(POV_GPU_STAGE_CAMERA));
+    CK(launch_camera(S, sc->blocks.as<int4>(), sc->block_off.as<int>(), num_blocks, n, params->width,
+                     params->height, qcur, pcur, sc->paths.as<PathState>(), ccur, dstats, st));
+    CK(clk.end());
+    for (int level = 0; level < sc->max_trace_level; level++) {
+        CK(cudaMemsetAsync(cnext, 0, sizeof(int), st));
+        CK(cudaMemsetAsync(cnt + C_SQ, 0, sizeof(int) * 3, st));   // SQ, W0, W1
+        CK(clk.begin(POV_GPU_STAGE_TRACE_CLOSEST));
+        CK(launch_trace(S, false, qcur, ccur, cnt + C_W0, sc->hits.as<QHit>(), nullptr, sc->stack_depth, grid_trace,
+                        derr, dstats, wc, (int)maxq, st));
+        CK(clk.end());
+        CK(clk.begin(POV_GPU_STAGE_SHADE));
+        CK(launch_shade(S, level, qcur, pcur, sc->hits.as<QHit>(), ccur, sc->paths.as<PathState>(),
+                        sc->slot_contrib.as<float4>(), sc->sq.as<QRay>(), sc->sq_slot.as<int>(), cnt + C_SQ, qnext,
+                        pnext, cnext, (int)maxq, (int)(maxq * nl), grid_shade, derr, dstats, st));
+        CK(clk.end());
+        if (sc->num_lights > 0) {
+            CK(clk.begin(POV_GPU_STAGE_TRACE_SHADOW));
+            CK(launch_trace(S, true, sc->sq.as<QRay>(), cnt + C_SQ, cnt + C_W1, nullptr, sc->blocked.as<uint8_t>(),
+                            sc->stack_depth, grid_trace, derr, dstats, wc ? wc + 4 : nullptr, (int)(maxq * nl), st));
+            CK(clk.end());
+            CK(clk.begin(POV_GPU_STAGE_RESOLVE));
+            CK(launch_resolve(pcur, ccur, sc->num_lights, sc->sq_slot.as<int>(), sc->blocked.as<uint8_t>(),
+                              cnt + C_SQ, sc->slot_contrib.as<float4>(), sc->paths.as<PathState>(), grid_shade, st));
+            CK(clk.end(2));
+        }
+        std::swap(qcur, qnext);
+        std::swap(pcur, pnext);
+        std::swap(ccur, cnext);
+    }
+    CK(clk.begin(POV_GPU_STAGE_FINALIZE));
+    CK(launch_finalize(sc->paths.as<PathState>(), n, dout, st));
+    CK(clk.end());
+    if (!out_on_device)
+        CK(cudaMemcpyAsync(out_rgbt, dout, sizeof(float4) * n, cudaMemcpyDeviceToHost, st));
+    unsigned long long hw[8] = {0};
+    if (wc)
+        CK(cudaMemcpyAsync(hw, wc, sizeof(hw), cudaMemcpyDeviceToHost, st));
+    unsigned long long hs[ST_COUNT];
+    int rc = check_device_error(sc, stats, hs);
+    if (stats)
+        stats->number_of_pixels = (uint64_t)n;
+    clk.collect();
+    if (wc) {
+        for (int k = 0; k < 2; k++) {
+            sc->timings.node_visits[k] = hw[4 * k + 0];
+            sc->timings.prim_tests[k] = hw[4 * k + 1];
+            sc->timings.tri_tests[k] = hw[4 * k + 2];
+            sc->timings.rays_traced[k] = hw[4 * k + 3];
+        }
+    }
+    return rc;
+}
+
+int pov_gpu_trace_rays(PovGpuScene* sc, const double* origins, const double* directions, int32_t num_rays,
+                       PovGpuHit* hits)
+{
+    if (!sc || num_rays < 0 || (num_rays > 0 && (!origins || !directions || !hits)))
+        return POV_GPU_E_INVALID;
+    std::lock_guard<std::mutex> g(sc->lock);
+    cudaSetDevice(sc->device);
+    if (num_rays == 0)
+        return POV_GPU_OK;
+    cudaStream_t st = sc->active();
+    const size_t n = (size_t)num_rays;
+    CK(sc->rays_in.ensure(sizeof(double) * 6 * n));
+    CK(sc->qA.ensure(sizeof(QRay) * n));
+    CK(sc->hits.ensure(sizeof(QHit) * n));
+    double* dorg = sc->rays_in.as<double>();
+    double* ddir = dorg + 3 * n;
+    CK(cudaMemcpyAsync(dorg, origins, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(ddir, directions, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st));
+    int* cnt = sc->counters.as<int>();
+    CK(cudaMemsetAsync(sc->counters.p, 0, sizeof(int) * C_NUM, st));
+    CK(cudaMemsetAsync(sc->err.p, 0, sizeof(uint32_t) * 4, st));
+    CK(cudaMemsetAsync(sc->stats.p, 0, sizeof(unsigned long long) * ST_COUNT, st));
+    CK(launch_load_rays(dorg, ddir, num_rays, sc->qA.as<QRay>(), cnt + C_QA, st));
+    CK(launch_trace(sc->S, false, sc->qA.as<QRay>(), cnt + C_QA, cnt + C_W0, sc->hits.as<QHit>(), nullptr,
+                    sc->stack_depth, sc->num_sms * 8, sc->err.as<uint32_t>(), sc->stats.as<unsigned long long>(),
+                    nullptr, num_rays, st));
+    std::vector<QHit> hh(n);
+    CK(cudaMemcpyAsync(hh.data(), sc->hits.p, sizeof(QHit) * n, cudaMemcpyDeviceToHost, st));
+    unsigned long long hs[ST_COUNT];
+    int rc = check_device_error(sc, nullptr, hs);
+    // map prim references to flattened object ids / mesh triangle indices
+    std::vector<int32_t> sphere_obj, plane_obj, tri_global, tri_local;
+    std::vector<float4> tri_normal;
+    auto fetch_i = [&](DevBuf& b, std::vector<int32_t>& v) {
+        v.resize(b.bytes / sizeof(int32_t));
+        return cudaMemcpy(v.data(), b.p, b.bytes, cudaMemcpyDeviceToHost);
+    };
+    CK(fetch_i(sc->sphere_obj, sphere_obj));
+    CK(fetch_i(sc->plane_obj, plane_obj));
+    CK(fetch_i(sc->tri_global, tri_global));
+    CK(fetch_i(sc->tri_local, tri_local));
+    tri_normal.resize(sc->tri_normal.bytes / sizeof(float4));
+    CK(cudaMemcpy(tri_normal.data(), sc->tri_normal.p, sc->tri_normal.bytes, cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < n; i++) {
+        const QHit& h = hh[i];
+        hits[i].object = -1;
+        hits[i].triangle = -1;
+        hits[i].t = 0.0;
+        if (h.prim == 0xffffffffu)
+            continue;
+        uint32_t kind = h.prim >> PRIM_KIND_SHIFT, idx = h.prim & PRIM_INDEX_MASK;
+        hits[i].t = (double)h.t;
+        if (kind == PK_SPHERE)
+            hits[i].object = sphere_obj[idx];
+        else if (kind == PK_PLANE)
+            hits[i].object = plane_obj[idx];
+        else if (kind == PK_TRIANGLE) {
+            int gidx = tri_global[idx];
+            hits[i].object = __builtin_bit_cast(int32_t, tri_normal[gidx].w);
+            hits[i].triangle = tri_local[gidx];
+        }
+    }
+    return rc;
+}
+
+}  // extern "C"

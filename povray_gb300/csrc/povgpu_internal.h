@@ -1,0 +1,146 @@
+// povgpu_internal.h -- device data layout shared by the host builder
+// (povgpu_host.cpp) and the kernels (povgpu_kernels.cu).
+//
+// HBM layout (all arrays structure-of-arrays, 16-byte aligned):
+//   nodes      BvhNode[num_nodes]      64 B: two child AABBs + two links
+//   prim_refs  uint32[num_prim_refs]   leaf order; type in bits 28..31
+//   tri_v0/e1/e2 float4[num_tris]      48 B per triangle, leaf order
+//   tri_id     int32[num_tris]         leaf order -> (mesh-local) index
+//   spheres    float4[num_spheres]     centre.xyz, radius
+//   ...        per-primitive shading records, see DeviceScene
+#pragma once
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+namespace povgpu {
+
+// Primitive kinds stored in the top 4 bits of a prim reference.
+enum PrimKind : uint32_t {
+    PK_SPHERE = 0u,
+    PK_TRIANGLE = 1u,
+    PK_BOX = 2u,
+    PK_TORUS = 3u,
+    PK_CSG = 4u,
+    PK_PLANE = 5u,
+};
+constexpr uint32_t PRIM_KIND_SHIFT = 28;
+constexpr uint32_t PRIM_INDEX_MASK = (1u << PRIM_KIND_SHIFT) - 1u;
+
+// Two-wide BVH node (both children's boxes in one 64-byte record, loaded as
+// four float4):  a = (c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y)
+//                b = (c1.lo.x, c1.hi.x, c1.lo.y, c1.hi.y)
+//                c = (c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z)
+//                d = (link0, link1, -, -) as int bits
+// link >= 0: inner node index.  link < 0: leaf, ~link = (first << 3) | (count-1)
+// over prim_refs.
+struct __align__(16) BvhNode {
+    float4 a, b, c, d;
+};
+constexpr int LEAF_MAX_PRIMS = 8;
+
+// Shading record of one scene object (flattened object id).
+struct __align__(16) ObjectShade {
+    int32_t material;
+    int32_t flags;
+    int32_t type;
+    int32_t mesh;       // mesh index or -1
+};
+
+// Material as the shading kernel reads it (float, pre-derived terms).
+struct __align__(16) DevMaterial {
+    float4 pigment;         // rgb, filter
+    float4 emission;        // emission + ambient * ambient_light, rgb
+    float4 reflect;         // reflection_max rgb, falloff
+    float4 reflect_min;     // reflection_min rgb, max(WeightMax(max), WeightMax(min))
+    float diffuse;          // diffuse * brilliance_adjust
+    float brilliance;
+    float phong;
+    float phong_size;
+    float specular;
+    float roughness;        // already inverted
+    int32_t has_reflection;
+    int32_t pad;
+};
+
+struct __align__(16) DevLight {
+    float4 center;          // xyz, kind
+    float4 colour;          // rgb, -
+};
+
+struct __align__(16) DevMesh {
+    int32_t tri_base;        // offset of this mesh's triangles in the global tables
+    int32_t num_tris;
+    int32_t object;          // flattened object id of the mesh
+    int32_t normal_base;     // offset into the global normal table
+};
+
+struct DeviceScene {
+    const BvhNode*  nodes;
+    const uint32_t* prim_refs;
+    int32_t         root;           // -1 = no finite primitives
+    // triangles (leaf order)
+    const float4*   tri_v0;
+    const float4*   tri_e1;
+    const float4*   tri_e2;
+    const int32_t*  tri_global;     // leaf-order slot -> global triangle index
+    // triangle shading (global triangle order)
+    const int4*     tri_shade;      // n1, n2, n3 (global normal index), flags (bit0 smooth)
+    const float4*   tri_normal;     // geometric normal xyz, mesh object id (int bits)
+    const int32_t*  tri_local;      // global triangle -> triangle index within its mesh
+    const float4*   normals;        // smooth normals (normalised like the parser)
+    // spheres
+    const float4*   spheres;        // centre, radius
+    const int32_t*  sphere_obj;     // object id
+    // planes (infinite, tested by every ray)
+    const float4*   planes;         // normal xyz, Distance
+    const int32_t*  plane_obj;
+    int32_t         num_planes;
+    // objects, materials, lights
+    const ObjectShade* objects;
+    const DevMaterial* materials;
+    const DevLight*    lights;
+    int32_t         num_lights;
+    int32_t         max_trace_level;
+    float           adc_bailout;
+    float4          background;
+    // camera
+    double          cam_loc[3], cam_dir[3], cam_right[3], cam_up[3];
+};
+
+// One ray of a wavefront queue (32 B) + its path slot.
+struct __align__(16) QRay {
+    float4 org;     // xyz, tmin
+    float4 dir;     // xyz, tmax
+};
+
+// Closest-hit record (16 B).
+struct __align__(16) QHit {
+    float    t;
+    uint32_t prim;   // prim reference (kind|index), 0xffffffff = miss
+    float    u, v;   // triangle barycentrics
+};
+
+// Per-path state (one path per image sample).
+struct __align__(16) PathState {
+    float4 colour;      // accumulated rgb, transm
+    float4 throughput;  // rgb, weight
+};
+
+// Device error word bits.
+enum DevError : uint32_t {
+    DE_STACK_OVERFLOW = 1u,
+    DE_ITERATION_CAP  = 2u,
+    DE_QUEUE_OVERFLOW = 4u,
+};
+
+// Counters (device, uint64).
+enum StatIdx {
+    ST_RAYS = 0,
+    ST_SHADOW_TESTS = 1,
+    ST_SHADOW_SUCCEEDED = 2,
+    ST_REFLECTED = 3,
+    ST_SAMPLES = 4,
+    ST_COUNT = 8,
+};
+
+}  // namespace povgpu

@@ -1,0 +1,168 @@
+"""Host-side driver over the C ABI, shaped like the reference's view/task
+pair: a GpuScene is what View::StartRender builds once per view, and
+GpuTraceTask.run() is TraceTask::Run -- it pulls render blocks from a
+ViewData-like block source (GetNextRectangle), traces them in batches on the
+GPU and hands each finished block back (CompletedRectangle).
+
+There is no CPU path here: every call goes through libpovgpu.so and fails
+loudly if the library or a device is missing.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+from . import scenes as _scenes
+
+HIT_DTYPE = np.dtype([("object", "<i4"), ("triangle", "<i4"), ("t", "<f8")])
+
+
+def _check(st, what, bad=-1):
+    if st != abi.POV_GPU_OK:
+        raise abi.PovGpuError(st, what, bad)
+
+
+class GpuScene:
+    """Device copy of one parsed scene (pov_gpu_scene_create)."""
+
+    def __init__(self, scene):
+        self.lib = abi.load_library()
+        self.scene = scene
+        self.desc, self._keep = scene.desc()
+        h = C.c_void_p()
+        bad = C.c_int32(-1)
+        st = self.lib.pov_gpu_scene_create(C.byref(self.desc), C.byref(h), C.byref(bad))
+        _check(st, "pov_gpu_scene_create", bad.value)
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.pov_gpu_scene_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def trace_blocks(self, blocks, params=None, out=None):
+        """Traces `blocks` (list of (left, top, right, bottom, serial)).
+
+        `out` may be None (a host array is returned), a host float32 array,
+        or an integer device pointer (e.g. torch tensor .data_ptr()).
+        Returns (rgbt or None, stats dict)."""
+        p = params or self.scene.render_params()
+        arr = _scenes.block_array(blocks)
+        npix = sum((r - l + 1) * (b - t + 1) for (l, t, r, b, _s) in blocks)
+        stats = abi.PovGpuStats()
+        host = None
+        if out is None:
+            host = np.empty((npix, 4), dtype=np.float32)
+            ptr = host.ctypes.data
+        elif isinstance(out, np.ndarray):
+            assert out.dtype == np.float32 and out.size >= npix * 4 and out.flags.c_contiguous
+            host = out
+            ptr = out.ctypes.data
+        else:
+            ptr = int(out)
+        st = self.lib.pov_gpu_trace_blocks(self.h, arr, len(blocks), C.byref(p), C.c_void_p(ptr),
+                                           C.byref(stats))
+        _check(st, "pov_gpu_trace_blocks")
+        return host, stats.as_dict()
+
+    def render(self, params=None, block=32):
+        """Whole image (H, W, 4) through the block interface."""
+        p = params or self.scene.render_params()
+        blocks = _scenes.blocks_for(p.width, p.height, block)
+        rgbt, stats = self.trace_blocks(blocks, p)
+        return _scenes.unblock(rgbt, blocks, p.width, p.height), stats
+
+    def set_stream(self, stream_handle):
+        """Launch on a caller-owned cudaStream_t (int handle, 0 = own stream)."""
+        _check(self.lib.pov_gpu_scene_set_stream(self.h, C.c_void_p(int(stream_handle) or None)),
+               "pov_gpu_scene_set_stream")
+
+    def set_profiling(self, times=False, work=False):
+        flags = (abi.POV_GPU_PROFILE_TIMES if times else 0) | (abi.POV_GPU_PROFILE_WORK if work else 0)
+        _check(self.lib.pov_gpu_set_profiling(self.h, flags), "pov_gpu_set_profiling")
+
+    def timings(self):
+        t = abi.PovGpuTimings()
+        _check(self.lib.pov_gpu_get_timings(self.h, C.byref(t)), "pov_gpu_get_timings")
+        return {
+            "stage_ms": {abi.STAGE_NAMES[i]: float(t.stage_ms[i]) for i in range(abi.POV_GPU_STAGES)},
+            "stage_launches": {abi.STAGE_NAMES[i]: int(t.stage_launches[i]) for i in range(abi.POV_GPU_STAGES)},
+            "node_visits": [int(x) for x in t.node_visits], "prim_tests": [int(x) for x in t.prim_tests],
+            "tri_tests": [int(x) for x in t.tri_tests], "rays_traced": [int(x) for x in t.rays_traced],
+            "kernel_launches": int(t.kernel_launches),
+        }
+
+    def trace_rays(self, origins, directions):
+        o = np.ascontiguousarray(origins, dtype=np.float64)
+        d = np.ascontiguousarray(directions, dtype=np.float64)
+        n = o.shape[0]
+        hits = (abi.PovGpuHit * max(n, 1))()
+        st = self.lib.pov_gpu_trace_rays(self.h, o.ctypes.data, d.ctypes.data, n, hits)
+        _check(st, "pov_gpu_trace_rays")
+        return np.frombuffer(hits, dtype=HIT_DTYPE, count=n).copy()
+
+
+class BlockSource:
+    """ViewData's block dispenser: GetNextRectangle hands out the 32x32 grid
+    in serial order (source/backend/scene/view.cpp:236-271), skipping blocks
+    listed as already done (continue-trace skip list, view.cpp:240-252);
+    CompletedRectangle receives the finished pixels (view.cpp:405)."""
+
+    def __init__(self, width, height, block=32, skip=()):
+        self.width, self.height = width, height
+        self.blocks = [b for b in _scenes.blocks_for(width, height, block) if b[4] not in set(skip)]
+        self.next = 0
+        self.image = np.zeros((height, width, 4), dtype=np.float32)
+        self.completed = []
+
+    def get_next_rectangle(self):
+        if self.next >= len(self.blocks):
+            return None
+        b = self.blocks[self.next]
+        self.next += 1
+        return b
+
+    def completed_rectangle(self, rect, pixels):
+        l, t, r, b, s = rect
+        self.image[t:b + 1, l:r + 1] = pixels.reshape(b - t + 1, r - l + 1, 4)
+        self.completed.append(s)
+
+
+class GpuTraceTask:
+    """TraceTask::Run with SimpleSamplingM0 (source/backend/render/
+    tracetask.cpp:287,403): drains the block source in batches of
+    `batch` blocks per device call."""
+
+    def __init__(self, gpu_scene, source, params=None, batch=4096):
+        self.gpu = gpu_scene
+        self.source = source
+        self.params = params or gpu_scene.scene.render_params()
+        self.batch = batch
+        self.stats = {}
+
+    def run(self):
+        while True:
+            rects = []
+            while len(rects) < self.batch:
+                r = self.source.get_next_rectangle()
+                if r is None:
+                    break
+                rects.append(r)
+            if not rects:
+                break
+            rgbt, st = self.gpu.trace_blocks(rects, self.params)
+            for k, v in st.items():
+                self.stats[k] = self.stats.get(k, 0) + v
+            off = 0
+            for rect in rects:
+                l, t, r, b, _s = rect
+                n = (r - l + 1) * (b - t + 1)
+                self.source.completed_rectangle(rect, rgbt[off:off + n])
+                off += n
+        return self.stats

@@ -1,0 +1,505 @@
+"""Synthetic scenes of the trace-path workloads, written two ways.
+
+Every scene is generated from a seeded NumPy PCG64 stream and can be emitted
+as SDL (for the reference renderer, all numbers as round-trip literals) or as
+a PovGpuSceneDesc (for libpovgpu and the oracle).  Both forms describe the
+same parsed scene: the desc holds what the reference's parser leaves in
+SceneData (camera vectors after Parse_Camera, plane Distance negated, finish
+roughness inverted, mesh2 normals normalised), so the GPU path, the oracle
+and the reference read identical values.
+
+Workloads (names are descriptive, sizes are the defaults):
+  spheres_plane   64 spheres + plane, 2 shadowing point lights, phong 0.5
+                  (320x240, 1 spp, max_trace_level 1)
+  mesh_spheres    1,051,392-triangle displaced sphere mesh2 + 1024 spheres +
+                  plane, 1 light, reflection 0.3, max_trace_level 3
+                  (1920x1080, 1 spp)
+"""
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import abi
+
+EPSILON = 1.0e-10
+M_PI_360 = 0.00872664625997164788
+
+
+# ----------------------------------------------------------------- vectors --
+def _sub(a, b):
+    return (a[0] - b[0], a[1] - b[1], a[2] - b[2])
+
+
+def _scale(a, s):
+    return (a[0] * s, a[1] * s, a[2] * s)
+
+
+def _div(a, s):
+    return (a[0] / s, a[1] / s, a[2] / s)
+
+
+def _dot(a, b):
+    return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]
+
+
+def _cross(a, b):
+    return ((a[1] * b[2]) - (a[2] * b[1]),
+            (a[2] * b[0]) - (a[0] * b[2]),
+            (a[0] * b[1]) - (a[1] * b[0]))
+
+
+def _length(a):
+    return math.sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2])
+
+
+def _normalized(a):
+    l = _length(a)
+    return _div(a, l) if l != 0 else a
+
+
+def camera_vectors(location, look_at, angle, right_len, up_len=1.0, sky=(0.0, 1.0, 0.0)):
+    """Camera vectors as Parse_Camera leaves them for
+    ``camera { perspective location L look_at A angle a right x*r up y }``
+    (source/parser/parser.cpp:1714-1790: angle first, then look_at)."""
+    direction = (0.0, 0.0, 1.0)
+    right = (right_len, 0.0, 0.0)
+    up = (0.0, up_len, 0.0)
+    # apply "angle"
+    direction = _normalized(direction)
+    right_length = _length(right)
+    direction_length = right_length / math.tan(angle * M_PI_360) / 2.0
+    direction = _scale(direction, direction_length)
+    # apply "look_at"
+    direction_length = _length(direction)
+    up_length = _length(up)
+    right_length = _length(right)
+    handedness = _dot(_cross(up, direction), right)
+    direction = _sub(look_at, location)
+    direction = _normalized(direction)
+    right = _cross(sky, direction)
+    right = _normalized(right)
+    up = _cross(direction, right)
+    direction = _scale(direction, direction_length)
+    right = _scale(right, right_length if handedness > 0.0 else -right_length)
+    up = _scale(up, up_length)
+    return direction, right, up
+
+
+def _g(x):
+    """Round-trip literal of a double."""
+    return repr(float(x))
+
+
+def _v(v):
+    return "<%s,%s,%s>" % (_g(v[0]), _g(v[1]), _g(v[2]))
+
+
+def _f32(x):
+    """Round-trip literal of a float32 value (9 significant digits)."""
+    return "%.9g" % float(x)
+
+
+# ------------------------------------------------------------------ scenes --
+class Material:
+    def __init__(self, rgb, ambient=0.1, diffuse=0.6, phong=0.0, phong_size=40.0,
+                 specular=0.0, roughness=0.05, reflection=0.0, brilliance=1.0,
+                 emission=0.0):
+        self.rgb = tuple(float(c) for c in rgb)
+        self.ambient = float(ambient)
+        self.diffuse = float(diffuse)
+        self.phong = float(phong)
+        self.phong_size = float(phong_size)
+        self.specular = float(specular)
+        self.roughness = float(roughness)
+        self.reflection = float(reflection)
+        self.brilliance = float(brilliance)
+        self.emission = float(emission)
+
+    def sdl(self):
+        fin = "ambient %s diffuse %s" % (_g(self.ambient), _g(self.diffuse))
+        if self.brilliance != 1.0:
+            fin += " brilliance %s" % _g(self.brilliance)
+        if self.phong:
+            fin += " phong %s phong_size %s" % (_g(self.phong), _g(self.phong_size))
+        if self.specular:
+            fin += " specular %s roughness %s" % (_g(self.specular), _g(self.roughness))
+        if self.reflection:
+            fin += " reflection %s" % _g(self.reflection)
+        if self.emission:
+            fin += " emission %s" % _g(self.emission)
+        return "texture { pigment { color rgb %s } finish { %s } }" % (_v(self.rgb), fin)
+
+    def desc(self):
+        m = abi.PovGpuMaterial()
+        m.pigment[:] = [self.rgb[0], self.rgb[1], self.rgb[2], 0.0, 0.0]
+        m.ambient[:] = [self.ambient] * 3
+        m.emission[:] = [self.emission] * 3
+        m.diffuse = self.diffuse
+        m.diffuse_back = 0.0
+        m.brilliance = self.brilliance
+        m.brilliance_adjust = 1.0
+        m.brilliance_adjust_rad = 2.0 / (self.brilliance + 1.0)
+        m.phong = self.phong
+        m.phong_size = self.phong_size
+        m.specular = self.specular
+        m.roughness = 1.0 / self.roughness
+        m.metallic = 0.0
+        m.reflection_max[:] = [self.reflection] * 3
+        m.reflection_min[:] = [self.reflection] * 3
+        m.reflection_falloff = 1.0
+        m.reflect_exp = 1.0
+        m.reflect_metallic = 0.0
+        m.reflection_fresnel = 0
+        m.conserve_energy = 0
+        m.fresnel = 0.0
+        m.crand = 0.0
+        m.irid = 0.0
+        return m
+
+
+class Mesh:
+    """mesh2 with per-vertex normals (normal_indices = face_indices)."""
+
+    def __init__(self, vertices, normals, faces):
+        self.vertices = np.ascontiguousarray(vertices, dtype=np.float32)
+        self.normals = None if normals is None else np.ascontiguousarray(normals, dtype=np.float32)
+        self.faces = np.ascontiguousarray(faces, dtype=np.int32)
+
+    @property
+    def num_triangles(self):
+        return int(self.faces.shape[0])
+
+    def sdl(self, material):
+        out = ["mesh2 {\n  vertex_vectors { %d,\n" % len(self.vertices)]
+        out.append(",\n".join("<%s,%s,%s>" % (_f32(a), _f32(b), _f32(c)) for a, b, c in self.vertices))
+        out.append("\n  }\n")
+        if self.normals is not None:
+            out.append("  normal_vectors { %d,\n" % len(self.normals))
+            out.append(",\n".join("<%s,%s,%s>" % (_f32(a), _f32(b), _f32(c)) for a, b, c in self.normals))
+            out.append("\n  }\n")
+        out.append("  face_indices { %d,\n" % len(self.faces))
+        out.append(",\n".join("<%d,%d,%d>" % (a, b, c) for a, b, c in self.faces))
+        out.append("\n  }\n")
+        out.append("  %s\n}\n" % material.sdl())
+        return "".join(out)
+
+
+class Scene:
+    def __init__(self, name, width, height, location, look_at, angle,
+                 max_trace_level=5, adc_bailout=1.0 / 255.0, background=(0.0, 0.0, 0.0)):
+        self.name = name
+        self.width = int(width)
+        self.height = int(height)
+        self.location = tuple(float(x) for x in location)
+        self.look_at = tuple(float(x) for x in look_at)
+        self.angle = float(angle)
+        self.right_len = float(width) / float(height)
+        self.max_trace_level = int(max_trace_level)
+        self.adc_bailout = float(adc_bailout)
+        self.background = tuple(float(x) for x in background)
+        self.materials = []
+        self.objects = []     # list of dicts, depth-first order
+        self.lights = []
+        self.meshes = []
+        self.antialias = None  # (threshold, depth) for sampling method 2
+
+    # -- building ----------------------------------------------------------
+    def material(self, m):
+        self.materials.append(m)
+        return len(self.materials) - 1
+
+    def sphere(self, centre, radius, mat):
+        self.objects.append(dict(type=abi.POV_OBJ_SPHERE, centre=tuple(map(float, centre)),
+                                 radius=float(radius), material=mat))
+
+    def plane(self, normal, offset, mat):
+        self.objects.append(dict(type=abi.POV_OBJ_PLANE, normal=tuple(map(float, normal)),
+                                 offset=float(offset), material=mat))
+
+    def mesh(self, mesh, mat):
+        self.meshes.append(mesh)
+        self.objects.append(dict(type=abi.POV_OBJ_MESH, mesh=len(self.meshes) - 1, material=mat))
+
+    def point_light(self, pos, rgb=(1.0, 1.0, 1.0)):
+        self.lights.append(dict(kind=abi.POV_LIGHT_POINT, pos=tuple(map(float, pos)),
+                                rgb=tuple(map(float, rgb))))
+
+    # -- SDL -----------------------------------------------------------------
+    def sdl(self):
+        out = ["#version 3.7;\n",
+               "global_settings { assumed_gamma 1.0 max_trace_level %d adc_bailout %s }\n"
+               % (self.max_trace_level, _g(self.adc_bailout)),
+               "camera { perspective location %s right x*%s up y look_at %s angle %s }\n"
+               % (_v(self.location), _g(self.right_len), _v(self.look_at), _g(self.angle)),
+               "background { color rgb %s }\n" % _v(self.background)]
+        for l in self.lights:
+            out.append("light_source { %s color rgb %s }\n" % (_v(l["pos"]), _v(l["rgb"])))
+        for o in self.objects:
+            mat = self.materials[o["material"]]
+            t = o["type"]
+            if t == abi.POV_OBJ_SPHERE:
+                out.append("sphere { %s, %s %s }\n" % (_v(o["centre"]), _g(o["radius"]), mat.sdl()))
+            elif t == abi.POV_OBJ_PLANE:
+                out.append("plane { %s, %s %s }\n" % (_v(o["normal"]), _g(o["offset"]), mat.sdl()))
+            elif t == abi.POV_OBJ_MESH:
+                out.append(self.meshes[o["mesh"]].sdl(mat))
+            else:
+                raise ValueError("no SDL writer for object type %d" % t)
+        return "".join(out)
+
+    # -- C ABI ---------------------------------------------------------------
+    def camera(self):
+        return camera_vectors(self.location, self.look_at, self.angle, self.right_len)
+
+    def desc(self):
+        """Returns (PovGpuSceneDesc, keepalive) -- keep the second alive while
+        the first is in use."""
+        keep = []
+        n = len(self.objects)
+        objs = (abi.PovGpuObject * max(n, 1))()
+        for i, o in enumerate(self.objects):
+            d = objs[i]
+            d.type = o["type"]
+            d.flags = 0
+            d.material = o["material"]
+            d.parent = -1
+            d.first_child = -1
+            d.num_children = 0
+            d.mesh = -1
+            if o["type"] == abi.POV_OBJ_SPHERE:
+                d.p[0], d.p[1], d.p[2] = o["centre"]
+                d.p[3] = o["radius"]
+            elif o["type"] == abi.POV_OBJ_PLANE:
+                nrm = _normalized(o["normal"])
+                d.p[0], d.p[1], d.p[2] = nrm
+                d.p[3] = -o["offset"]
+                d.flags |= abi.POV_FLAG_INFINITE
+            elif o["type"] == abi.POV_OBJ_MESH:
+                d.mesh = o["mesh"]
+        mats = (abi.PovGpuMaterial * max(len(self.materials), 1))()
+        for i, m in enumerate(self.materials):
+            mats[i] = m.desc()
+        lights = (abi.PovGpuLight * max(len(self.lights), 1))()
+        for i, l in enumerate(self.lights):
+            lights[i].center[:] = list(l["pos"])
+            lights[i].colour[:] = list(l["rgb"])
+            lights[i].kind = l["kind"]
+        meshes = (abi.PovGpuMesh * max(len(self.meshes), 1))()
+        for i, m in enumerate(self.meshes):
+            meshes[i].vertices = m.vertices.ctypes.data_as(C.POINTER(C.c_float))
+            meshes[i].num_vertices = len(m.vertices)
+            if m.normals is not None:
+                meshes[i].normals = m.normals.ctypes.data_as(C.POINTER(C.c_float))
+                meshes[i].num_normals = len(m.normals)
+                meshes[i].normal_indices = m.faces.ctypes.data_as(C.POINTER(C.c_int32))
+            meshes[i].face_indices = m.faces.ctypes.data_as(C.POINTER(C.c_int32))
+            meshes[i].num_triangles = m.num_triangles
+            keep.append(m)
+        desc = abi.PovGpuSceneDesc()
+        desc.abi_version = abi.POV_GPU_ABI_VERSION
+        desc.num_objects = n
+        desc.objects = objs
+        desc.num_materials = len(self.materials)
+        desc.materials = mats
+        desc.num_lights = len(self.lights)
+        desc.lights = lights
+        desc.num_meshes = len(self.meshes)
+        desc.meshes = meshes
+        dvec, rvec, uvec = self.camera()
+        desc.camera.location[:] = list(self.location)
+        desc.camera.direction[:] = list(dvec)
+        desc.camera.right[:] = list(rvec)
+        desc.camera.up[:] = list(uvec)
+        desc.camera.type = 0
+        desc.background[:] = [self.background[0], self.background[1], self.background[2], 0.0]
+        desc.ambient_light[:] = [1.0, 1.0, 1.0]
+        desc.max_trace_level = self.max_trace_level
+        desc.adc_bailout = self.adc_bailout
+        desc.language_version = 370
+        desc.radiosity.enabled = 0
+        keep += [objs, mats, lights, meshes]
+        return desc, keep
+
+    def render_params(self):
+        p = abi.PovGpuRenderParams()
+        p.width = self.width
+        p.height = self.height
+        if self.antialias is not None:
+            p.antialias = 1
+            p.sampling_method = 2
+            p.aa_threshold, p.aa_depth = self.antialias
+        else:
+            p.antialias = 0
+            p.sampling_method = 1
+        p.quality = 9
+        return p
+
+    def camera_rays(self, xs=None, ys=None):
+        """Primary rays through pixel centres (x+0.5, y+0.5) exactly as
+        TracePixel::CreateCameraRay forms them
+        (source/core/render/tracepixel.cpp:357-373,924), in float64."""
+        dvec, rvec, uvec = (np.array(v) for v in self.camera())
+        if xs is None:
+            yy, xx = np.mgrid[0:self.height, 0:self.width]
+            xs, ys = xx.ravel(), yy.ravel()
+        x0 = (np.asarray(xs, dtype=np.float64) + 0.5) / self.width - 0.5
+        y0 = 0.5 - (np.asarray(ys, dtype=np.float64) + 0.5) / self.height
+        d = dvec[None, :] + x0[:, None] * rvec[None, :] + y0[:, None] * uvec[None, :]
+        d = d / np.sqrt((d * d).sum(axis=1))[:, None]
+        o = np.broadcast_to(np.array(self.location), d.shape).copy()
+        return np.ascontiguousarray(o), np.ascontiguousarray(d)
+
+
+def blocks_for(width, height, block=32):
+    """The view's render-block grid (source/backend/scene/view.cpp:810-822)."""
+    out = []
+    serial = 0
+    for top in range(0, height, block):
+        for left in range(0, width, block):
+            out.append((left, top, min(left + block, width) - 1, min(top + block, height) - 1, serial))
+            serial += 1
+    return out
+
+
+def block_array(blocks):
+    arr = (abi.PovGpuBlock * len(blocks))()
+    for i, (l, t, r, b, s) in enumerate(blocks):
+        arr[i].left, arr[i].top, arr[i].right, arr[i].bottom, arr[i].serial = l, t, r, b, s
+    return arr
+
+
+def unblock(rgbt, blocks, width, height):
+    """Scatters block-ordered RGBT back into an image (H, W, 4)."""
+    img = np.zeros((height, width, 4), dtype=np.float32)
+    off = 0
+    for (l, t, r, b, _s) in blocks:
+        w, h = r - l + 1, b - t + 1
+        img[t:b + 1, l:r + 1] = rgbt[off:off + w * h].reshape(h, w, 4)
+        off += w * h
+    return img
+
+
+# -------------------------------------------------------------- generators --
+def spheres_plane(width=320, height=240, n_spheres=64, seed=1):
+    """64 spheres, centres U[-10,10]^3, radii U[0.2,1.0], rgb U[0,1]^3 (seed 1);
+    plane y=-10; point lights (20,30,-20), (-15,25,-10); phong 0.5;
+    max_trace_level 1; camera (0,5,-25) looking at the origin, 50 deg."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    centres = rng.uniform(-10.0, 10.0, size=(n_spheres, 3))
+    radii = rng.uniform(0.2, 1.0, size=n_spheres)
+    colours = rng.uniform(0.0, 1.0, size=(n_spheres, 3))
+    s = Scene("spheres_plane", width, height, (0.0, 5.0, -25.0), (0.0, 0.0, 0.0), 50.0,
+              max_trace_level=1)
+    s.point_light((20.0, 30.0, -20.0))
+    s.point_light((-15.0, 25.0, -10.0))
+    for i in range(n_spheres):
+        m = s.material(Material(colours[i], phong=0.5))
+        s.sphere(centres[i], radii[i], m)
+    s.plane((0.0, 1.0, 0.0), -10.0, s.material(Material((0.8, 0.8, 0.8), phong=0.5)))
+    return s
+
+
+def _value_noise3(p, seed, octaves=3):
+    """Sum of `octaves` octaves of trilinear value noise on an integer lattice
+    with smoothstep weights; lattice values are a hash of (i, j, k, seed)
+    mapped to [-1, 1]."""
+    total = np.zeros(p.shape[0])
+    amp, freq, norm = 1.0, 2.0, 0.0
+    for o in range(octaves):
+        q = p * freq + 17.0 * (o + 1)
+        i0 = np.floor(q).astype(np.int64)
+        f = q - i0
+        w = f * f * (3.0 - 2.0 * f)
+
+        def lattice(di, dj, dk):
+            h = ((i0[:, 0] + di) * 73856093) ^ ((i0[:, 1] + dj) * 19349663) ^ \
+                ((i0[:, 2] + dk) * 83492791) ^ (seed * 2654435761 + o * 97)
+            h = (h ^ (h >> 13)) * 1274126177
+            h = h ^ (h >> 16)
+            return (h & 0xFFFF).astype(np.float64) / 32767.5 - 1.0
+
+        acc = 0.0
+        for di in (0, 1):
+            for dj in (0, 1):
+                for dk in (0, 1):
+                    wx = w[:, 0] if di else 1.0 - w[:, 0]
+                    wy = w[:, 1] if dj else 1.0 - w[:, 1]
+                    wz = w[:, 2] if dk else 1.0 - w[:, 2]
+                    acc = acc + wx * wy * wz * lattice(di, dj, dk)
+        total += amp * acc
+        norm += amp
+        amp *= 0.5
+        freq *= 2.0
+    return total / norm
+
+
+def displaced_sphere_mesh(n=296, amplitude=0.15, radius=8.0, seed=2):
+    """Cube-sphere with n x n quads per face (6*n*n*2 triangles; n=296 gives
+    1,051,392), every vertex pushed radially by 3-octave value noise of
+    amplitude `amplitude`, scaled to `radius`, with per-vertex normals
+    averaged from the adjacent faces (area weighted)."""
+    verts, faces = [], []
+    base = 0
+    g = np.linspace(-1.0, 1.0, n + 1)
+    uu, vv = np.meshgrid(g, g, indexing="ij")
+    axes = [(0, 1, 2, 1.0), (0, 1, 2, -1.0), (1, 2, 0, 1.0), (1, 2, 0, -1.0),
+            (2, 0, 1, 1.0), (2, 0, 1, -1.0)]
+    idx = np.arange((n + 1) * (n + 1)).reshape(n + 1, n + 1)
+    for (a, b, c, sgn) in axes:
+        p = np.zeros(((n + 1) * (n + 1), 3))
+        p[:, a] = uu.ravel()
+        p[:, b] = vv.ravel() * sgn
+        p[:, c] = sgn
+        verts.append(p)
+        q00 = idx[:-1, :-1].ravel() + base
+        q10 = idx[1:, :-1].ravel() + base
+        q01 = idx[:-1, 1:].ravel() + base
+        q11 = idx[1:, 1:].ravel() + base
+        faces.append(np.stack([q00, q10, q11], axis=1))
+        faces.append(np.stack([q00, q11, q01], axis=1))
+        base += (n + 1) * (n + 1)
+    p = np.concatenate(verts)
+    f = np.concatenate(faces).astype(np.int32)
+    d = p / np.linalg.norm(p, axis=1)[:, None]
+    r = 1.0 + amplitude * _value_noise3(d, seed)
+    pos = (d * (r * radius)[:, None]).astype(np.float32)
+    v0, v1, v2 = (pos[f[:, k]].astype(np.float64) for k in range(3))
+    fn = np.cross(v1 - v0, v2 - v0)
+    vn = np.zeros_like(p)
+    for k in range(3):
+        np.add.at(vn, f[:, k], fn)
+    # make seam duplicates share one normal: accumulate by position
+    key = np.round(pos.astype(np.float64) * 1e5).astype(np.int64)
+    _, inv = np.unique(key, axis=0, return_inverse=True)
+    inv = inv.ravel()
+    acc = np.zeros((inv.max() + 1, 3))
+    np.add.at(acc, inv, vn)
+    vn = acc[inv]
+    vn /= np.linalg.norm(vn, axis=1)[:, None]
+    return Mesh(pos, vn.astype(np.float32), f)
+
+
+def mesh_spheres(width=1920, height=1080, mesh_n=296, n_spheres=1024, seed=2):
+    """The 1M-triangle scene: displaced sphere mesh2 (radius 8) + 1024 spheres
+    r U[0.1,0.5] in [-12,12]^3 + plane y=-9; one point light with shadows;
+    reflection 0.3 on every surface; max_trace_level 3."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    centres = rng.uniform(-12.0, 12.0, size=(n_spheres, 3))
+    radii = rng.uniform(0.1, 0.5, size=n_spheres)
+    colours = rng.uniform(0.0, 1.0, size=(n_spheres, 3))
+    s = Scene("mesh_spheres", width, height, (0.0, 5.0, -25.0), (0.0, 0.0, 0.0), 50.0,
+              max_trace_level=3)
+    s.point_light((20.0, 30.0, -20.0))
+    mesh = displaced_sphere_mesh(n=mesh_n, seed=seed)
+    s.mesh(mesh, s.material(Material((0.9, 0.7, 0.4), phong=0.5, reflection=0.3)))
+    for i in range(n_spheres):
+        s.sphere(centres[i], radii[i], s.material(Material(colours[i], phong=0.5, reflection=0.3)))
+    s.plane((0.0, 1.0, 0.0), -9.0, s.material(Material((0.8, 0.8, 0.8), phong=0.5, reflection=0.3)))
+    return s
+
+
+WORKLOADS = {
+    "spheres_plane": spheres_plane,
+    "mesh_spheres": mesh_spheres,
+}

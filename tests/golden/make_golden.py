@@ -1,0 +1,93 @@
+"""Generates the golden fixtures of this directory from the reference itself.
+
+Runs only where the reference sources are present (it drives
+oracle/_ref/pov_oracle, built from them by oracle/refbuild/Makefile):
+
+    python tests/golden/make_golden.py
+
+For every case it writes the scene's SDL to a temporary directory, has the
+reference parse and render it, and stores in <case>.npz:
+  pixels       float32 (H, W, 4) linear RGBT from TracePixel::operator()
+  stats        JSON of Number_Of_Rays / Shadow_Ray_Tests / ... counters
+  ray_org/dir  float64 probe rays (strided camera rays + random rays)
+  hit_object, hit_triangle, hit_t   Trace::FindIntersection of each probe
+The cases are small so the fixtures stay a few hundred KB.
+"""
+import json
+import os
+import struct
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from povray_gb300 import scenes  # noqa: E402
+
+POV_ORACLE = os.path.join(ROOT, "oracle", "_ref", "pov_oracle")
+
+
+def cases():
+    return {
+        "spheres_plane_320x240": (scenes.spheres_plane(320, 240), 4),
+        "mesh_spheres_small_160x90": (scenes.mesh_spheres(160, 90, mesh_n=24, n_spheres=64), 2),
+    }
+
+
+def probe_rays(scene, stride, n_random=2000, seed=11):
+    hh, ww = np.mgrid[0:scene.height:stride, 0:scene.width:stride]
+    o, d = scene.camera_rays(ww.ravel(), hh.ravel())
+    rng = np.random.Generator(np.random.PCG64(seed))
+    ro = rng.uniform(-12.0, 12.0, size=(n_random, 3))
+    rd = rng.normal(size=(n_random, 3))
+    rd /= np.linalg.norm(rd, axis=1)[:, None]
+    return np.concatenate([o, ro]), np.concatenate([d, rd])
+
+
+def run(case, scene, stride, tmp):
+    pov = os.path.join(tmp, case + ".pov")
+    with open(pov, "w") as f:
+        f.write(scene.sdl())
+    w, h = str(scene.width), str(scene.height)
+    rgbt = os.path.join(tmp, case + ".rgbt")
+    out = subprocess.run([POV_ORACLE, pov, w, h, "pixels", rgbt], check=True, capture_output=True, text=True)
+    stats = json.loads(out.stdout.strip().splitlines()[-1])
+    pixels = np.fromfile(rgbt, dtype=np.float32).reshape(scene.height, scene.width, 4)
+    o, d = probe_rays(scene, stride)
+    rays = os.path.join(tmp, case + ".rays")
+    with open(rays, "wb") as f:
+        f.write(struct.pack("<i", o.shape[0]))
+        f.write(np.concatenate([o, d], axis=1).astype("<f8").tobytes())
+    hits = os.path.join(tmp, case + ".hits")
+    subprocess.run([POV_ORACLE, pov, w, h, "rays", rays, hits], check=True, capture_output=True)
+    hr = np.fromfile(hits, dtype=np.dtype([("object", "<i4"), ("triangle", "<i4"), ("t", "<f8")]))
+    # the camera vectors the reference's parser produced
+    dump = os.path.join(tmp, case + ".scene.txt")
+    subprocess.run([POV_ORACLE, pov, w, h, "scene", dump], check=True, capture_output=True)
+    cam = {}
+    with open(dump) as f:
+        for line in f:
+            k, *v = line.split()
+            if k in ("location", "direction", "right", "up"):
+                cam[k] = [float(x) for x in v]
+    camera = np.array([cam["location"], cam["direction"], cam["right"], cam["up"]], dtype=np.float64)
+    np.savez_compressed(os.path.join(HERE, case + ".npz"), pixels=pixels, stats=json.dumps(stats),
+                        ray_org=o, ray_dir=d, hit_object=hr["object"], hit_triangle=hr["triangle"],
+                        hit_t=hr["t"], camera=camera)
+    print(case, stats, "hits", int((hr["object"] >= 0).sum()), "/", len(hr))
+
+
+def main():
+    if not os.path.exists(POV_ORACLE):
+        sys.exit("build the reference first: make -C oracle/refbuild")
+    with tempfile.TemporaryDirectory() as tmp:
+        for case, (scene, stride) in cases().items():
+            run(case, scene, stride, tmp)
+
+
+if __name__ == "__main__":
+    main()

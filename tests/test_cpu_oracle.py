@@ -1,0 +1,73 @@
+"""The oracle is pinned against the reference: the golden fixtures were
+dumped by the reference renderer itself (tests/golden/make_golden.py) for
+the same SDL scenes, and the oracle must reproduce them."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle.pyoracle import Oracle
+from povray_gb300 import scenes
+from tests.golden.make_golden import cases
+from tests.parity import compare_hits, compare_pixels
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+CASES = cases()
+
+
+def _load(case):
+    return np.load(os.path.join(GOLDEN, case + ".npz"))
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_camera_vectors_match_the_parser(case):
+    scene, _ = CASES[case]
+    g = _load(case)
+    d, r, u = scene.camera()
+    assert np.array_equal(g["camera"][0], np.array(scene.location))
+    assert np.array_equal(g["camera"][1], np.array(d))
+    assert np.array_equal(g["camera"][2], np.array(r))
+    assert np.array_equal(g["camera"][3], np.array(u))
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_oracle_hits_match_reference(case):
+    scene, _ = CASES[case]
+    g = _load(case)
+    o = Oracle(scene)
+    h = o.trace_rays(g["ray_org"], g["ray_dir"])
+    r = compare_hits(h["object"], h["triangle"], h["t"], g["hit_object"], g["hit_triangle"], g["hit_t"],
+                     oracle=o, org=g["ray_org"], dirs=g["ray_dir"], t_tol=1e-12)
+    assert r["mismatch"] == 0, r
+    assert r["t_max_rel"] <= 1e-12, r
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_oracle_pixels_and_counters_match_reference(case):
+    scene, _ = CASES[case]
+    g = _load(case)
+    img, st = Oracle(scene).render(threads=4)
+    ref = g["pixels"]
+    assert np.abs(img - ref).max() <= 1e-5
+    assert compare_pixels(img, ref)["max_lsb"] <= 1
+    rs = json.loads(str(g["stats"]))
+    for k in ("number_of_rays", "shadow_ray_tests", "shadow_rays_succeeded", "reflected_rays"):
+        assert st[k] == rs[k], (k, st[k], rs[k])
+
+
+def test_oracle_is_thread_count_invariant():
+    s = scenes.mesh_spheres(96, 54, mesh_n=12, n_spheres=32)
+    o = Oracle(s)
+    a, sa = o.render(threads=1)
+    b, sb = o.render(threads=5)
+    assert np.array_equal(a, b)
+    assert sa == sb
+
+
+def test_oracle_subrectangle_equals_full_render():
+    s = scenes.spheres_plane(64, 48, n_spheres=16)
+    o = Oracle(s)
+    full, _ = o.render(threads=2)
+    part, _ = o.render(x0=10, y0=7, x1=41, y1=30, threads=2)
+    assert np.array_equal(full[7:30, 10:41], part)

@@ -1,0 +1,133 @@
+"""GPU parity: libpovgpu against the reference's golden vectors, against the
+oracle at sizes it finishes in seconds, and through size-independent
+properties at the full 1920x1080 / 1M-triangle size.
+
+Tolerances (written here, applied below):
+  hit object / triangle id   bit-exact on non-grazing rays
+  hit depth                  1e-5 relative
+  8-bit pixels               >= 99.9% of channels within 1 LSB
+  ray counters               Number_Of_Rays, Reflected_Rays exact;
+                             Shadow_Ray_Tests exact up to grazing
+                             light-terminator rays (<= 0.1%)
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle.pyoracle import Oracle
+from povray_gb300 import GpuScene, scenes
+from tests.golden.make_golden import cases
+from tests.parity import compare_hits, compare_pixels
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+CASES = cases()
+T_TOL = 1e-5
+PIX_FRAC = 0.999
+
+
+def _load(case):
+    return np.load(os.path.join(GOLDEN, case + ".npz"))
+
+
+def _counters_close(got, ref, shadow_frac=1e-3):
+    assert got["number_of_rays"] == ref["number_of_rays"], (got, ref)
+    assert got["reflected_rays"] == ref["reflected_rays"], (got, ref)
+    assert abs(got["shadow_ray_tests"] - ref["shadow_ray_tests"]) <= max(2, shadow_frac * ref["shadow_ray_tests"])
+    assert abs(got["shadow_rays_succeeded"] - ref["shadow_rays_succeeded"]) <= \
+        max(2, shadow_frac * ref["shadow_ray_tests"])
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_hits_match_reference_golden(case):
+    scene, _ = CASES[case]
+    g = _load(case)
+    gpu = GpuScene(scene)
+    h = gpu.trace_rays(g["ray_org"], g["ray_dir"])
+    r = compare_hits(h["object"], h["triangle"], h["t"], g["hit_object"], g["hit_triangle"], g["hit_t"],
+                     oracle=Oracle(scene), org=g["ray_org"], dirs=g["ray_dir"], t_tol=T_TOL)
+    assert r["bad"] == 0, r
+    assert r["t_bad"] == 0, r
+    assert r["mismatch"] <= 0.001 * r["rays"], r
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_pixels_match_reference_golden(case):
+    scene, _ = CASES[case]
+    g = _load(case)
+    img, st = GpuScene(scene).render()
+    c = compare_pixels(img, g["pixels"])
+    assert c["within_1lsb"] >= PIX_FRAC, c
+    _counters_close(st, json.loads(str(g["stats"])))
+
+
+def test_mid_size_mesh_scene_matches_oracle():
+    """1M-triangle mesh at 480x270: GPU vs oracle, pixels and counters."""
+    s = scenes.mesh_spheres(480, 270)
+    img, st = GpuScene(s).render()
+    ref, rst = Oracle(s).render(threads=0)
+    c = compare_pixels(img, ref)
+    assert c["within_1lsb"] >= PIX_FRAC, c
+    _counters_close(st, rst)
+
+
+def test_primary_hits_full_mesh_match_oracle():
+    s = scenes.mesh_spheres(1920, 1080)
+    rng = np.random.default_rng(3)
+    xs = rng.integers(0, 1920, 20000)
+    ys = rng.integers(0, 1080, 20000)
+    o, d = s.camera_rays(xs, ys)
+    orc = Oracle(s)
+    ref = orc.trace_rays(o, d)
+    h = GpuScene(s).trace_rays(o, d)
+    r = compare_hits(h["object"], h["triangle"], h["t"], ref["object"], ref["triangle"], ref["t"],
+                     oracle=orc, org=o, dirs=d, t_tol=T_TOL)
+    assert r["bad"] == 0 and r["t_bad"] == 0, r
+
+
+def test_full_size_render_is_deterministic_and_block_invariant():
+    """1920x1080, 1M triangles: two renders are bit-identical, rendering the
+    blocks in a different batch split gives the same image, and the ray
+    counters satisfy Rays = Pixels + Reflected (every TraceRay call)."""
+    s = scenes.mesh_spheres(1920, 1080)
+    gpu = GpuScene(s)
+    a, sa = gpu.render()
+    b, sb = gpu.render()
+    assert np.array_equal(a, b) and sa == sb
+    blocks = scenes.blocks_for(1920, 1080)
+    half = len(blocks) // 2
+    p1, _ = gpu.trace_blocks(blocks[half:])
+    p2, _ = gpu.trace_blocks(blocks[:half])
+    c = scenes.unblock(np.concatenate([p2, p1]), blocks[:half] + blocks[half:], 1920, 1080)
+    assert np.array_equal(c, a)
+    assert sa["number_of_rays"] == 1920 * 1080 + sa["reflected_rays"]
+    assert np.isfinite(a).all() and (a[..., :3] >= 0).all()
+
+
+def test_empty_and_single_pixel_batches():
+    s = scenes.spheres_plane(64, 48, n_spheres=8)
+    gpu = GpuScene(s)
+    img, st = gpu.trace_blocks([])
+    assert img.size == 0 and st["number_of_rays"] == 0
+    ref, _ = Oracle(s).render(x0=13, y0=9, x1=14, y1=10, threads=1)
+    one, st1 = gpu.trace_blocks([(13, 9, 13, 9, 0)])
+    assert st1["number_of_pixels"] == 1
+    assert np.abs(one.reshape(1, 1, 4) - ref).max() < 1e-4
+
+
+def test_scene_without_finite_objects():
+    """Only a plane (no BVH at all) and a scene with no lights."""
+    s = scenes.Scene("plane_only", 40, 30, (0.0, 5.0, -25.0), (0.0, 0.0, 0.0), 50.0)
+    s.plane((0.0, 1.0, 0.0), -1.0, s.material(scenes.Material((0.5, 0.6, 0.7), phong=0.3)))
+    img, _ = GpuScene(s).render()
+    ref, _ = Oracle(s).render(threads=1)
+    assert compare_pixels(img, ref)["within_1lsb"] >= PIX_FRAC
+    s.lights = []
+    s.point_light((3.0, 10.0, 0.0))
+    s.lights = []
+    img, _ = GpuScene(s).render()
+    ref, _ = Oracle(s).render(threads=1)
+    assert compare_pixels(img, ref)["within_1lsb"] >= PIX_FRAC
