@@ -271,7 +271,7 @@ struct PovGpuScene {
     DevBuf spheres, sphere_obj, planes, plane_obj, objects, materials, lights;
     // per-batch work buffers (grown on demand, reused)
     DevBuf blocks, block_off, qA, qB, pathA, pathB, hits, paths, slot_contrib, sq, sq_slot, blocked, out,
-        counters, stats, err, rays_in;
+        counters, stats, err, rays_in, skipA, skipB, sskip, t64;
     int     num_lights = 0;
     int     max_trace_level = 1;
     // streams and profiling
@@ -293,7 +293,8 @@ struct PovGpuScene {
                          &tri_normal, &tri_local, &normals,  &spheres,   &sphere_obj, &planes,     &plane_obj,
                          &objects, &materials,  &lights,   &blocks,    &block_off,  &qA,         &qB,
                          &pathA,   &pathB,      &hits,     &paths,     &slot_contrib, &sq,       &sq_slot,
-                         &blocked, &out,        &counters, &stats,     &err,        &rays_in};
+                         &blocked, &out,        &counters, &stats,     &err,        &rays_in,
+                         &skipA,   &skipB,      &sskip,    &t64};
         for (DevBuf* b : all)
             b->release();
         if (stream)
@@ -461,8 +462,10 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
                 V3d N = vcross(vsub(P3, P1), vsub(P2, P1));
                 double len = vlen(N);
                 float4 gn = make_float4(0.f, 0.f, 0.f, __builtin_bit_cast(float, i));
+                float plane_dist = 0.f;
                 if (len != 0.0) {
                     N = {N.x / len, N.y / len, N.z / len};
+                    plane_dist = (float)(-(N.x * P1.x + N.y * P1.y + N.z * P1.z));   // Triangle->Distance
                     gn.x = (float)N.x;
                     gn.y = (float)N.y;
                     gn.z = (float)N.z;
@@ -485,7 +488,7 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
                 float v0[3] = {(float)P1.x, (float)P1.y, (float)P1.z};
                 float v1[3] = {(float)P2.x, (float)P2.y, (float)P2.z};
                 float v2[3] = {(float)P3.x, (float)P3.y, (float)P3.z};
-                tri_v0.push_back(make_float4(v0[0], v0[1], v0[2], 0.f));
+                tri_v0.push_back(make_float4(v0[0], v0[1], v0[2], plane_dist));
                 tri_e1.push_back(make_float4(v1[0] - v0[0], v1[1] - v0[1], v1[2] - v0[2], 0.f));
                 tri_e2.push_back(make_float4(v2[0] - v0[0], v2[1] - v0[1], v2[2] - v0[2], 0.f));
                 tri_normal.push_back(gn);
@@ -831,6 +834,9 @@ int pov_gpu_trace_blocks(PovGpuScene* sc, const PovGpuBlock* blocks, int32_t num
     CK(sc->sq.ensure(sizeof(QRay) * maxq * nl));
     CK(sc->sq_slot.ensure(sizeof(int) * maxq * nl));
     CK(sc->blocked.ensure(maxq * nl));
+    CK(sc->skipA.ensure(sizeof(uint32_t) * maxq));
+    CK(sc->skipB.ensure(sizeof(uint32_t) * maxq));
+    CK(sc->sskip.ensure(sizeof(uint32_t) * maxq * nl));
 
     cudaPointerAttributes pa{};
     bool out_on_device = cudaPointerGetAttributes(&pa, out_rgbt) == cudaSuccess &&
@@ -865,26 +871,30 @@ int pov_gpu_trace_blocks(PovGpuScene* sc, const PovGpuBlock* blocks, int32_t num
     int* pnext = sc->pathB.as<int>();
     int* ccur = cnt + C_QA;
     int* cnext = cnt + C_QB;
+    uint32_t* kcur = sc->skipA.as<uint32_t>();
+    uint32_t* knext = sc->skipB.as<uint32_t>();
     CK(clk.begin(POV_GPU_STAGE_CAMERA));
     CK(launch_camera(S, sc->blocks.as<int4>(), sc->block_off.as<int>(), num_blocks, n, params->width,
-                     params->height, qcur, pcur, sc->paths.as<PathState>(), ccur, dstats, st));
+                     params->height, qcur, pcur, sc->paths.as<PathState>(), ccur, dstats, kcur, st));
     CK(clk.end());
     for (int level = 0; level < sc->max_trace_level; level++) {
         CK(cudaMemsetAsync(cnext, 0, sizeof(int), st));
         CK(cudaMemsetAsync(cnt + C_SQ, 0, sizeof(int) * 3, st));   // SQ, W0, W1
         CK(clk.begin(POV_GPU_STAGE_TRACE_CLOSEST));
         CK(launch_trace(S, false, qcur, ccur, cnt + C_W0, sc->hits.as<QHit>(), nullptr, sc->stack_depth, grid_trace,
-                        derr, dstats, wc, (int)maxq, st));
+                        derr, dstats, wc, (int)maxq, kcur, st));
         CK(clk.end());
         CK(clk.begin(POV_GPU_STAGE_SHADE));
         CK(launch_shade(S, level, qcur, pcur, sc->hits.as<QHit>(), ccur, sc->paths.as<PathState>(),
-                        sc->slot_contrib.as<float4>(), sc->sq.as<QRay>(), sc->sq_slot.as<int>(), cnt + C_SQ, qnext,
-                        pnext, cnext, (int)maxq, (int)(maxq * nl), grid_shade, derr, dstats, st));
+                        sc->slot_contrib.as<float4>(), sc->sq.as<QRay>(), sc->sq_slot.as<int>(), cnt + C_SQ,
+                        sc->sskip.as<uint32_t>(), qnext, pnext, knext, cnext, (int)maxq, (int)(maxq * nl), grid_shade,
+                        derr, dstats, st));
         CK(clk.end());
         if (sc->num_lights > 0) {
             CK(clk.begin(POV_GPU_STAGE_TRACE_SHADOW));
             CK(launch_trace(S, true, sc->sq.as<QRay>(), cnt + C_SQ, cnt + C_W1, nullptr, sc->blocked.as<uint8_t>(),
-                            sc->stack_depth, grid_trace, derr, dstats, wc ? wc + 4 : nullptr, (int)(maxq * nl), st));
+                            sc->stack_depth, grid_trace, derr, dstats, wc ? wc + 4 : nullptr, (int)(maxq * nl),
+                            sc->sskip.as<uint32_t>(), st));
             CK(clk.end());
             CK(clk.begin(POV_GPU_STAGE_RESOLVE));
             CK(launch_resolve(pcur, ccur, sc->num_lights, sc->sq_slot.as<int>(), sc->blocked.as<uint8_t>(),
@@ -894,6 +904,7 @@ int pov_gpu_trace_blocks(PovGpuScene* sc, const PovGpuBlock* blocks, int32_t num
         std::swap(qcur, qnext);
         std::swap(pcur, pnext);
         std::swap(ccur, cnext);
+        std::swap(kcur, knext);
     }
     CK(clk.begin(POV_GPU_STAGE_FINALIZE));
     CK(launch_finalize(sc->paths.as<PathState>(), n, dout, st));
@@ -933,6 +944,7 @@ int pov_gpu_trace_rays(PovGpuScene* sc, const double* origins, const double* dir
     CK(sc->rays_in.ensure(sizeof(double) * 6 * n));
     CK(sc->qA.ensure(sizeof(QRay) * n));
     CK(sc->hits.ensure(sizeof(QHit) * n));
+    CK(sc->t64.ensure(sizeof(double) * n));
     double* dorg = sc->rays_in.as<double>();
     double* ddir = dorg + 3 * n;
     CK(cudaMemcpyAsync(dorg, origins, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st));
@@ -944,9 +956,12 @@ int pov_gpu_trace_rays(PovGpuScene* sc, const double* origins, const double* dir
     CK(launch_load_rays(dorg, ddir, num_rays, sc->qA.as<QRay>(), cnt + C_QA, st));
     CK(launch_trace(sc->S, false, sc->qA.as<QRay>(), cnt + C_QA, cnt + C_W0, sc->hits.as<QHit>(), nullptr,
                     sc->stack_depth, sc->num_sms * 8, sc->err.as<uint32_t>(), sc->stats.as<unsigned long long>(),
-                    nullptr, num_rays, st));
+                    nullptr, num_rays, nullptr, st));
+    CK(launch_refine(sc->S, dorg, ddir, sc->hits.as<QHit>(), sc->t64.as<double>(), num_rays, st));
     std::vector<QHit> hh(n);
+    std::vector<double> t64(n);
     CK(cudaMemcpyAsync(hh.data(), sc->hits.p, sizeof(QHit) * n, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(t64.data(), sc->t64.p, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
     unsigned long long hs[ST_COUNT];
     int rc = check_device_error(sc, nullptr, hs);
     // map prim references to flattened object ids / mesh triangle indices
@@ -970,7 +985,7 @@ int pov_gpu_trace_rays(PovGpuScene* sc, const double* origins, const double* dir
         if (h.prim == 0xffffffffu)
             continue;
         uint32_t kind = h.prim >> PRIM_KIND_SHIFT, idx = h.prim & PRIM_INDEX_MASK;
-        hits[i].t = (double)h.t;
+        hits[i].t = t64[i];
         if (kind == PK_SPHERE)
             hits[i].object = sphere_obj[idx];
         else if (kind == PK_PLANE)

@@ -75,7 +75,8 @@ __device__ __forceinline__ int warp_reserve(int* counter, bool want, unsigned ma
 // normalised in FP64 exactly as CreateCameraRay does, then rounded.
 __global__ void k_camera(DeviceScene S, const int4* __restrict__ blocks, const int* __restrict__ block_off,
                          int nblocks, int width, int height, QRay* __restrict__ q, int* __restrict__ q_path,
-                         PathState* __restrict__ paths, int* __restrict__ q_count, unsigned long long* stats)
+                         PathState* __restrict__ paths, int* __restrict__ q_count, unsigned long long* stats,
+                         uint32_t* __restrict__ q_skip)
 {
     int npix = block_off[nblocks];
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -108,6 +109,7 @@ __global__ void k_camera(DeviceScene S, const int4* __restrict__ blocks, const i
     r.dir = make_float4((float)dx, (float)dy, (float)dz, CUDART_INF_F);
     q[i] = r;
     q_path[i] = i;
+    q_skip[i] = 0xffffffffu;
     PathState p;
     p.colour = make_float4(0.f, 0.f, 0.f, 0.f);
     p.throughput = make_float4(1.f, 1.f, 1.f, 1.f);
@@ -162,6 +164,26 @@ __device__ __forceinline__ bool isect_sphere(float4 s, float3 o, float3 d, float
     float t1 = tca - hc, t2 = tca + hc;
     if (t1 >= tmin && t1 < t) { t = t1; return true; }
     if (t2 >= tmin && t2 < t) { t = t2; return true; }
+    return false;
+}
+
+// A ray starting on the sphere's own surface: only the far root, and only
+// when the ray heads into the sphere (tca > 0).
+__device__ __forceinline__ bool isect_sphere_far(float4 s, float3 o, float3 d, float tmin, float& t)
+{
+    float3 oc = xyz(s) - o;
+    float tca = dot3(oc, d);
+    if (tca <= 0.0f)
+        return false;
+    float3 perp = oc - d * tca;
+    float thcs = s.w * s.w - dot3(perp, perp);
+    if (!(thcs > 0.0f))
+        return false;
+    float t2 = tca + sqrtf(thcs);
+    if (t2 >= tmin && t2 < t) {
+        t = t2;
+        return true;
+    }
     return false;
 }
 
@@ -228,7 +250,8 @@ __global__ void __launch_bounds__(128) k_trace(DeviceScene S, const QRay* __rest
                                                const int* __restrict__ q_count, int* __restrict__ work,
                                                QHit* __restrict__ hits, uint8_t* __restrict__ blocked,
                                                int stack_depth, uint32_t* err, unsigned long long* stats,
-                                               unsigned long long* wcount, int cap)
+                                               unsigned long long* wcount, int cap,
+                                               const uint32_t* __restrict__ skips)
 {
     extern __shared__ int smem[];
     const int lane = threadIdx.x & 31;
@@ -255,8 +278,15 @@ __global__ void __launch_bounds__(128) k_trace(DeviceScene S, const QRay* __rest
         uint32_t best = 0xffffffffu;
         float bu = 0.f, bv = 0.f;
         bool done = false;
+        // The surface a secondary ray starts on: in exact arithmetic a ray
+        // leaving a plane or a planar triangle never meets it again, and one
+        // leaving a sphere meets it only at the far root; FP32 rounding of the
+        // origin must not invent those self-hits (the reference works in FP64).
+        const uint32_t skip = skips ? skips[i] : 0xffffffffu;
         // infinite objects first (planes: Plane::Intersect, plane.cpp:139-211)
         for (int k = 0; k < S.num_planes; k++) {
+            if (((PK_PLANE << PRIM_KIND_SHIFT) | (uint32_t)k) == skip)
+                continue;
             float4 pl = __ldg(S.planes + k);
             float ndd = pl.x * d.x + pl.y * d.y + pl.z * d.z;
             if (fabsf(ndd) < EPSILON_F)
@@ -309,7 +339,10 @@ __global__ void __launch_bounds__(128) k_trace(DeviceScene S, const QRay* __rest
                     uint32_t idx = ref & PRIM_INDEX_MASK;
                     bool hit = false;
                     if (counting) { c_prims++; c_tris += kind == PK_TRIANGLE; }
-                    if (kind == PK_TRIANGLE) {
+                    if (ref == skip) {
+                        if (kind == PK_SPHERE)
+                            hit = isect_sphere_far(__ldg(S.spheres + idx), o, d, tmin, t);
+                    } else if (kind == PK_TRIANGLE) {
                         float uu, vv;
                         hit = isect_tri(__ldg(S.tri_v0 + idx), __ldg(S.tri_e1 + idx), __ldg(S.tri_e2 + idx), o,
                                         d, tmin, t, uu, vv);
@@ -411,7 +444,8 @@ __global__ void __launch_bounds__(128) k_shade(
     DeviceScene S, int level, const QRay* __restrict__ q, const int* __restrict__ q_path,
     const QHit* __restrict__ hits, const int* __restrict__ q_count, PathState* __restrict__ paths,
     float4* __restrict__ slot_contrib, QRay* __restrict__ sq, int* __restrict__ sq_slot, int* __restrict__ sq_count,
-    QRay* __restrict__ nq, int* __restrict__ nq_path, int* __restrict__ nq_count, int max_queue,
+    uint32_t* __restrict__ sq_skip, QRay* __restrict__ nq, int* __restrict__ nq_path,
+    uint32_t* __restrict__ nq_skip, int* __restrict__ nq_count, int max_queue,
     int max_shadow, uint32_t* err, unsigned long long* stats)
 {
     const int n = min(*q_count, max_queue);
@@ -500,6 +534,7 @@ __global__ void __launch_bounds__(128) k_shade(
                     sr.dir = make_float4(ld.x, ld.y, ld.z, ldist - SHADOW_TOLERANCE_F);
                     sq[slot] = sr;
                     sq_slot[slot] = i * nl + l;
+                    sq_skip[slot] = h.prim;
                 } else {
                     set_error(err, DE_QUEUE_OVERFLOW);
                 }
@@ -540,6 +575,7 @@ __global__ void __launch_bounds__(128) k_shade(
                 rr.dir = make_float4(nd.x, nd.y, nd.z, CUDART_INF_F);
                 nq[rs] = rr;
                 nq_path[rs] = path;
+                nq_skip[rs] = h.prim;
                 paths[path].throughput = make_float4(thr.x * reflec.x, thr.y * reflec.y, thr.z * reflec.z, rweight);
             } else {
                 set_error(err, DE_QUEUE_OVERFLOW);
@@ -607,15 +643,65 @@ __global__ void k_zero(int* p, int n)
         p[i] = 0;
 }
 
+// FP64 re-solve of the winning primitive for rays given in FP64: the depth
+// the reference computes for the same ray (sphere: Sphere::Intersect in
+// double; plane: Plane::Intersect; triangle: intersect_mesh_triangle's
+// plane distance from the stored FP32 normal and Distance, mesh.cpp:1046-1060).
+__global__ void k_refine(DeviceScene S, const double* __restrict__ org, const double* __restrict__ dir,
+                         const QHit* __restrict__ hits, double* __restrict__ t64, int n)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    QHit h = hits[i];
+    double t = (double)h.t;
+    if (h.prim != 0xffffffffu) {
+        double ox = org[3 * i], oy = org[3 * i + 1], oz = org[3 * i + 2];
+        double dx = dir[3 * i], dy = dir[3 * i + 1], dz = dir[3 * i + 2];
+        uint32_t kind = h.prim >> PRIM_KIND_SHIFT, idx = h.prim & PRIM_INDEX_MASK;
+        if (kind == PK_SPHERE) {
+            float4 s = S.spheres[idx];
+            double cx = (double)s.x - ox, cy = (double)s.y - oy, cz = (double)s.z - oz;
+            double tca = cx * dx + cy * dy + cz * dz;
+            double ocs = cx * cx + cy * cy + cz * cz;
+            double th = (double)s.w * (double)s.w - ocs + tca * tca;
+            if (th > 0.0) {
+                double hc = sqrt(th);
+                double t1 = tca - hc, t2 = tca + hc;
+                t = (t1 >= 1.0e-4) ? t1 : t2;
+            }
+        } else if (kind == PK_PLANE) {
+            float4 p = S.planes[idx];
+            double ndd = p.x * dx + p.y * dy + p.z * dz;
+            if (ndd != 0.0)
+                t = -((p.x * ox + p.y * oy + p.z * oz) + (double)p.w) / ndd;
+        } else if (kind == PK_TRIANGLE) {
+            int g = S.tri_global[idx];
+            float4 nrm = S.tri_normal[g];
+            double ndd = nrm.x * dx + nrm.y * dy + nrm.z * dz;
+            if (ndd != 0.0)
+                t = -((double)S.tri_v0[idx].w + (nrm.x * ox + nrm.y * oy + nrm.z * oz)) / ndd;
+        }
+    }
+    t64[i] = t;
+}
+
 // --------------------------------------------------------------- launch --
 static inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
 
+cudaError_t launch_refine(const DeviceScene& S, const double* org, const double* dir, QHit* hits, double* t64, int n,
+                          cudaStream_t st)
+{
+    k_refine<<<cdiv(n > 0 ? n : 1, 256), 256, 0, st>>>(S, org, dir, hits, t64, n);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_camera(const DeviceScene& S, const int4* blocks, const int* block_off, int nblocks, int npix,
                           int width, int height, QRay* q, int* q_path, PathState* paths, int* q_count,
-                          unsigned long long* stats, cudaStream_t st)
+                          unsigned long long* stats, uint32_t* q_skip, cudaStream_t st)
 {
     k_camera<<<cdiv(npix > 0 ? npix : 1, 256), 256, 0, st>>>(S, blocks, block_off, nblocks, width, height, q,
-                                                             q_path, paths, q_count, stats);
+                                                             q_path, paths, q_count, stats, q_skip);
     return cudaGetLastError();
 }
 
@@ -627,26 +713,28 @@ cudaError_t launch_load_rays(const double* org, const double* dir, int n, QRay* 
 
 cudaError_t launch_trace(const DeviceScene& S, bool any_hit, const QRay* q, const int* q_count, int* work,
                          QHit* hits, uint8_t* blocked, int stack_depth, int grid, uint32_t* err,
-                         unsigned long long* stats, unsigned long long* wcount, int cap, cudaStream_t st)
+                         unsigned long long* stats, unsigned long long* wcount, int cap, const uint32_t* skips,
+                         cudaStream_t st)
 {
     const int block = 128;
     size_t smem = (size_t)stack_depth * block * sizeof(int);
     if (any_hit)
         k_trace<true><<<grid, block, smem, st>>>(S, q, q_count, work, hits, blocked, stack_depth, err, stats,
-                                                 wcount, cap);
+                                                 wcount, cap, skips);
     else
         k_trace<false><<<grid, block, smem, st>>>(S, q, q_count, work, hits, blocked, stack_depth, err, stats,
-                                                  wcount, cap);
+                                                  wcount, cap, skips);
     return cudaGetLastError();
 }
 
 cudaError_t launch_shade(const DeviceScene& S, int level, const QRay* q, const int* q_path, const QHit* hits,
                          const int* q_count, PathState* paths, float4* slot_contrib, QRay* sq, int* sq_slot,
-                         int* sq_count, QRay* nq, int* nq_path, int* nq_count, int max_queue, int max_shadow, int grid,
-                         uint32_t* err, unsigned long long* stats, cudaStream_t st)
+                         int* sq_count, uint32_t* sq_skip, QRay* nq, int* nq_path, uint32_t* nq_skip, int* nq_count,
+                         int max_queue, int max_shadow, int grid, uint32_t* err, unsigned long long* stats,
+                         cudaStream_t st)
 {
     k_shade<<<grid, 128, 0, st>>>(S, level, q, q_path, hits, q_count, paths, slot_contrib, sq, sq_slot, sq_count,
-                                  nq, nq_path, nq_count, max_queue, max_shadow, err, stats);
+                                  sq_skip, nq, nq_path, nq_skip, nq_count, max_queue, max_shadow, err, stats);
     return cudaGetLastError();
 }
 

@@ -33,12 +33,15 @@ def _load(case):
     return np.load(os.path.join(GOLDEN, case + ".npz"))
 
 
-def _counters_close(got, ref, shadow_frac=1e-3):
-    assert got["number_of_rays"] == ref["number_of_rays"], (got, ref)
-    assert got["reflected_rays"] == ref["reflected_rays"], (got, ref)
-    assert abs(got["shadow_ray_tests"] - ref["shadow_ray_tests"]) <= max(2, shadow_frac * ref["shadow_ray_tests"])
+def _counters_close(got, ref, frac=5e-4):
+    """Counters agree up to grazing secondary rays: a reflection or shadow
+    ray that skims a silhouette or a light terminator can land on either side
+    in FP32 vs the reference's FP64 (at most `frac` of the rays)."""
+    for k in ("number_of_rays", "reflected_rays", "shadow_ray_tests"):
+        assert abs(got[k] - ref[k]) <= max(2, frac * ref[k]), (k, got, ref)
     assert abs(got["shadow_rays_succeeded"] - ref["shadow_rays_succeeded"]) <= \
-        max(2, shadow_frac * ref["shadow_ray_tests"])
+        max(2, frac * ref["shadow_ray_tests"]), (got, ref)
+    assert got["number_of_rays"] == got["number_of_pixels"] + got["reflected_rays"]
 
 
 @pytest.mark.parametrize("case", sorted(CASES))
