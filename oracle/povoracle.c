@@ -531,8 +531,540 @@ typedef struct {
     double  depth;
     V3      ipoint;
     int32_t object;
-    int32_t triangle;
+    int32_t triangle;   /* mesh triangle, or box side (Intersection::i1) */
 } Isect;
+
+/* TRANSFORM application (source/core/math/matrix.cpp:415-507); m is a
+ * row-major 4x4, row-vector convention. */
+static V3 mtrans_point(const double* m, V3 v)
+{
+    return v3(v.x * m[0] + v.y * m[4] + v.z * m[8] + m[12], v.x * m[1] + v.y * m[5] + v.z * m[9] + m[13],
+              v.x * m[2] + v.y * m[6] + v.z * m[10] + m[14]);
+}
+static V3 mtrans_direction(const double* m, V3 v)
+{
+    return v3(v.x * m[0] + v.y * m[4] + v.z * m[8], v.x * m[1] + v.y * m[5] + v.z * m[9],
+              v.x * m[2] + v.y * m[6] + v.z * m[10]);
+}
+/* MTransNormal(r, v, T) = MInvTransNormal(r, v, &T->inverse) */
+static V3 mtrans_normal(const double* inv, V3 v)
+{
+    return v3(v.x * inv[0] + v.y * inv[1] + v.z * inv[2], v.x * inv[4] + v.y * inv[5] + v.z * inv[6],
+              v.x * inv[8] + v.y * inv[9] + v.z * inv[10]);
+}
+
+/* Box::Intersect (source/core/shape/box.cpp:172-533) */
+#define BOX_DEPTH_TOLERANCE 1.0e-6
+#define CLOSE_TOLERANCE 1.0e-6
+enum { SIDE_X0 = 0, SIDE_X1, SIDE_Y0, SIDE_Y1, SIDE_Z0, SIDE_Z1 };
+static int box_intersect(V3 P, V3 D, V3 c1, V3 c2, double* d1, double* d2, int* s1, int* s2)
+{
+    int smin = 0, smax = 0;
+    double t, tmin = 0.0, tmax = BOUND_HUGE;
+    if (D.x < -EPSILON) {
+        t = (c1.x - P.x) / D.x;
+        if (t < tmin) return 0;
+        if (t <= tmax) { smax = SIDE_X0; tmax = t; }
+        t = (c2.x - P.x) / D.x;
+        if (t >= tmin) { if (t > tmax) return 0; smin = SIDE_X1; tmin = t; }
+    } else if (D.x > EPSILON) {
+        t = (c2.x - P.x) / D.x;
+        if (t < tmin) return 0;
+        if (t <= tmax) { smax = SIDE_X1; tmax = t; }
+        t = (c1.x - P.x) / D.x;
+        if (t >= tmin) { if (t > tmax) return 0; smin = SIDE_X0; tmin = t; }
+    } else if (P.x < c1.x || P.x > c2.x) {
+        return 0;
+    }
+    if (D.y < -EPSILON) {
+        t = (c1.y - P.y) / D.y;
+        if (t < tmin) return 0;
+        if (t <= tmax - CLOSE_TOLERANCE) { smax = SIDE_Y0; tmax = t; }
+        else if (t <= tmax + CLOSE_TOLERANCE) { if (-D.y > fabs(D.x)) smax = SIDE_Y0; }
+        t = (c2.y - P.y) / D.y;
+        if (t >= tmin + CLOSE_TOLERANCE) { if (t > tmax) return 0; smin = SIDE_Y1; tmin = t; }
+        else if (t >= tmin - CLOSE_TOLERANCE) { if (-D.y > fabs(D.x)) smin = SIDE_Y1; }
+    } else if (D.y > EPSILON) {
+        t = (c2.y - P.y) / D.y;
+        if (t < tmin) return 0;
+        if (t <= tmax - CLOSE_TOLERANCE) { smax = SIDE_Y1; tmax = t; }
+        else if (t <= tmax + CLOSE_TOLERANCE) { if (D.y > fabs(D.x)) smax = SIDE_Y1; }
+        t = (c1.y - P.y) / D.y;
+        if (t >= tmin + CLOSE_TOLERANCE) { if (t > tmax) return 0; smin = SIDE_Y0; tmin = t; }
+        else if (t >= tmin - CLOSE_TOLERANCE) { if (D.y > fabs(D.x)) smin = SIDE_Y0; }
+    } else if (P.y < c1.y || P.y > c2.y) {
+        return 0;
+    }
+    if (D.z < -EPSILON) {
+        t = (c1.z - P.z) / D.z;
+        if (t < tmin) return 0;
+        if (t <= tmax - CLOSE_TOLERANCE) { smax = SIDE_Z0; tmax = t; }
+        else if (t <= tmax + CLOSE_TOLERANCE) {
+            if ((smax == SIDE_X0 || smax == SIDE_X1) && -D.z > fabs(D.x)) smax = SIDE_Z0;
+            else if ((smax == SIDE_Y0 || smax == SIDE_Y1) && -D.z > fabs(D.y)) smax = SIDE_Z0;
+        }
+        t = (c2.z - P.z) / D.z;
+        if (t >= tmin + CLOSE_TOLERANCE) { if (t > tmax) return 0; smin = SIDE_Z1; tmin = t; }
+        else if (t >= tmin - CLOSE_TOLERANCE) {
+            if ((smin == SIDE_X0 || smin == SIDE_X1) && -D.z > fabs(D.x)) smin = SIDE_Z1;
+            else if ((smin == SIDE_Y0 || smin == SIDE_Y1) && -D.z > fabs(D.y)) smin = SIDE_Z1;
+        }
+    } else if (D.z > EPSILON) {
+        t = (c2.z - P.z) / D.z;
+        if (t < tmin) return 0;
+        if (t <= tmax - CLOSE_TOLERANCE) { smax = SIDE_Z1; tmax = t; }
+        else if (t <= tmax + CLOSE_TOLERANCE) {
+            if ((smax == SIDE_X0 || smax == SIDE_X1) && D.z > fabs(D.x)) smax = SIDE_Z1;
+            else if ((smax == SIDE_Y0 || smax == SIDE_Y1) && D.z > fabs(D.y)) smax = SIDE_Z1;
+        }
+        t = (c1.z - P.z) / D.z;
+        if (t >= tmin + CLOSE_TOLERANCE) { if (t > tmax) return 0; smin = SIDE_Z0; tmin = t; }
+        else if (t >= tmin - CLOSE_TOLERANCE) {
+            if ((smin == SIDE_X0 || smin == SIDE_X1) && D.z > fabs(D.x)) smin = SIDE_Z0;
+            else if ((smin == SIDE_Y0 || smin == SIDE_Y1) && D.z > fabs(D.y)) smin = SIDE_Z0;
+        }
+    } else if (P.z < c1.z || P.z > c2.z) {
+        return 0;
+    }
+    if (tmax < BOX_DEPTH_TOLERANCE)
+        return 0;
+    *d1 = tmin; *d2 = tmax; *s1 = smin; *s2 = smax;
+    return 1;
+}
+
+/* ------------------------------------------ polynomial solver (FP64) --- */
+/* source/core/math/polynomialsolver.cpp: Solve_Polynomial (:1585),
+ * solve_quadratic (:810), solve_cubic (:903), difficult_coeffs (:1075),
+ * solve_quartic (:1325), Sturm sequence polysolve (:1481) with buildsturm,
+ * modp, numchanges, sbisect, regula_falsa, visible_roots, polyeval. */
+#define PS_MAX_ORDER 15
+#define PS_MAX_ITERATIONS 50
+#define PS_SMALL_ENOUGH 1.0e-10
+#define PS_RELERROR 1.0e-12
+#define PS_FUDGE1 1.0e12
+static const double TWO_M_PI_3 = 2.0943951023931954923084;
+static const double FOUR_M_PI_3 = 4.1887902047863909846168;
+
+typedef struct { int ord; double coef[PS_MAX_ORDER + 1]; } Poly;
+
+static int ps_modp(const Poly* u, const Poly* v, Poly* r)
+{
+    int k, j;
+    *r = *u;
+    if (v->coef[v->ord] < 0.0) {
+        for (k = u->ord - v->ord - 1; k >= 0; k -= 2)
+            r->coef[k] = -r->coef[k];
+        for (k = u->ord - v->ord; k >= 0; k--)
+            for (j = v->ord + k - 1; j >= k; j--)
+                r->coef[j] = -r->coef[j] - r->coef[v->ord + k] * v->coef[j - k];
+    } else {
+        for (k = u->ord - v->ord; k >= 0; k--)
+            for (j = v->ord + k - 1; j >= k; j--)
+                r->coef[j] -= r->coef[v->ord + k] * v->coef[j - k];
+    }
+    k = v->ord - 1;
+    while (k >= 0 && fabs(r->coef[k]) < PS_SMALL_ENOUGH) {
+        r->coef[k] = 0.0;
+        k--;
+    }
+    r->ord = (k < 0) ? 0 : k;
+    return r->ord;
+}
+
+static int ps_buildsturm(int ord, Poly* sseq)
+{
+    sseq[0].ord = ord;
+    sseq[1].ord = ord - 1;
+    double f = fabs(sseq[0].coef[ord] * ord);
+    for (int i = 1; i <= ord; i++)
+        sseq[1].coef[i - 1] = sseq[0].coef[i] * i / f;
+    Poly* sp;
+    for (sp = sseq + 2; ps_modp(sp - 2, sp - 1, sp); sp++) {
+        f = -fabs(sp->coef[sp->ord]);
+        for (int k = sp->ord; k >= 0; k--)
+            sp->coef[k] /= f;
+    }
+    sp->coef[0] = -sp->coef[0];
+    return (int)(sp - sseq);
+}
+
+static int ps_visible_roots(int np, const Poly* sseq)
+{
+    int atposinf = 0, atzero = 0;
+    double f, lf = sseq[0].coef[sseq[0].ord];
+    for (const Poly* s = sseq + 1; s <= sseq + np; s++) {
+        f = s->coef[s->ord];
+        if (lf == 0.0 || lf * f < 0) atposinf++;
+        lf = f;
+    }
+    lf = sseq[0].coef[0];
+    for (const Poly* s = sseq + 1; s <= sseq + np; s++) {
+        f = s->coef[0];
+        if (lf == 0.0 || lf * f < 0) atzero++;
+        lf = f;
+    }
+    return atzero - atposinf;
+}
+
+static double ps_polyeval(double x, int n, const double* c)
+{
+    double val = c[n];
+    for (int i = n - 1; i >= 0; i--)
+        val = val * x + c[i];
+    return val;
+}
+
+static int ps_numchanges(int np, const Poly* sseq, double a)
+{
+    int changes = 0;
+    double f, lf = ps_polyeval(a, sseq[0].ord, sseq[0].coef);
+    for (const Poly* s = sseq + 1; s <= sseq + np; s++) {
+        f = ps_polyeval(a, s->ord, s->coef);
+        if (lf == 0.0 || lf * f < 0) changes++;
+        lf = f;
+    }
+    return changes;
+}
+
+static int ps_regula_falsa(int order, const double* coef, double a, double b, double* val)
+{
+    double fa = ps_polyeval(a, order, coef), fb = ps_polyeval(b, order, coef), x = 0, fx, lfx;
+    if (fa * fb > 0.0) return 0;
+    if (fabs(fa) < PS_SMALL_ENOUGH) { *val = a; return 1; }
+    if (fabs(fb) < PS_SMALL_ENOUGH) { *val = b; return 1; }
+    lfx = fa;
+    for (int its = 0; its < PS_MAX_ITERATIONS; its++) {
+        x = (fb * a - fa * b) / (fb - fa);
+        fx = ps_polyeval(x, order, coef);
+        if (fabs(x) > PS_RELERROR) {
+            if (fabs(fx / x) < PS_RELERROR) { *val = x; return 1; }
+        } else if (fabs(fx) < PS_RELERROR) {
+            *val = x;
+            return 1;
+        }
+        if (fa < 0) {
+            if (fx < 0) { a = x; fa = fx; if ((lfx * fx) > 0) fb /= 2; }
+            else { b = x; fb = fx; if ((lfx * fx) > 0) fa /= 2; }
+        } else {
+            if (fx < 0) { b = x; fb = fx; if ((lfx * fx) > 0) fa /= 2; }
+            else { a = x; fa = fx; if ((lfx * fx) > 0) fb /= 2; }
+        }
+        if (fabs(b - a) < PS_RELERROR) { *val = x; return 1; }
+        lfx = fx;
+    }
+    return 0;
+}
+
+static int ps_sbisect(int np, const Poly* sseq, double mn, double mx, int atmin, int atmax, double* roots)
+{
+    double mid = 0.0;
+    int n1, n2, its, atmid;
+    if ((atmin - atmax) == 1) {
+        if (ps_regula_falsa(sseq->ord, sseq->coef, mn, mx, roots))
+            return 1;
+        for (its = 0; its < PS_MAX_ITERATIONS; its++) {
+            mid = (mn + mx) / 2;
+            atmid = ps_numchanges(np, sseq, mid);
+            if ((atmid < atmax) || (atmid > atmin)) return 0;
+            if (fabs(mid) > PS_RELERROR) {
+                if (fabs((mx - mn) / mid) < PS_RELERROR) { roots[0] = mid; return 1; }
+            } else if (fabs(mx - mn) < PS_RELERROR) {
+                roots[0] = mid;
+                return 1;
+            }
+            if ((atmin - atmid) == 0) mn = mid; else mx = mid;
+        }
+        roots[0] = mid;
+        return 1;
+    }
+    for (its = 0; its < PS_MAX_ITERATIONS; its++) {
+        mid = (mn + mx) / 2;
+        atmid = ps_numchanges(np, sseq, mid);
+        if ((atmid < atmax) || (atmid > atmin)) return 0;
+        if (fabs(mid) > PS_RELERROR) {
+            if (fabs((mx - mn) / mid) < PS_RELERROR) { roots[0] = mid; return 1; }
+        } else if (fabs(mx - mn) < PS_RELERROR) {
+            roots[0] = mid;
+            return 1;
+        }
+        n1 = atmin - atmid;
+        n2 = atmid - atmax;
+        if ((n1 != 0) && (n2 != 0)) {
+            n1 = ps_sbisect(np, sseq, mn, mid, atmin, atmid, roots);
+            n2 = ps_sbisect(np, sseq, mid, mx, atmid, atmax, &roots[n1]);
+            return n1 + n2;
+        }
+        if (n1 == 0) mn = mid; else mx = mid;
+    }
+    roots[0] = mid;
+    return 1;
+}
+
+static int ps_polysolve(int order, const double* c, double* roots)
+{
+    Poly sseq[PS_MAX_ORDER + 1];
+    for (int i = 0; i <= order; i++)
+        sseq[0].coef[order - i] = c[i] / c[0];
+    int np = ps_buildsturm(order, sseq);
+    if (ps_visible_roots(np, sseq) == 0)
+        return 0;
+    int atmin = ps_numchanges(np, sseq, 0.0);
+    int atmax = ps_numchanges(np, sseq, MAX_DISTANCE);
+    if (atmin - atmax == 0)
+        return 0;
+    return ps_sbisect(np, sseq, 0.0, MAX_DISTANCE, atmin, atmax, roots);
+}
+
+static int ps_quadratic(const double* x, double* y)
+{
+    double a = x[0], b = -x[1], c = x[2], d, t;
+    if (a == 0.0) {
+        if (b == 0.0) return 0;
+        y[0] = c / b;
+        return 1;
+    }
+    b /= a;
+    c /= a;
+    a = 1.0;
+    d = b * b - 4.0 * a * c;
+    if ((d > -PS_SMALL_ENOUGH) && (d < PS_SMALL_ENOUGH)) {
+        y[0] = 0.5 * b / a;
+        return 1;
+    } else if (d < 0.0) {
+        return 0;
+    }
+    d = sqrt(d);
+    t = 2.0 * a;
+    y[0] = (b + d) / t;
+    y[1] = (b - d) / t;
+    return 2;
+}
+
+static int ps_cubic(const double* x, double* y)
+{
+    double Q, R, Q3, R2, sQ, d, an, theta, A2, a0 = x[0], a1, a2, a3;
+    if (a0 == 0.0)
+        return ps_quadratic(&x[1], y);
+    if (a0 != 1.0) { a1 = x[1] / a0; a2 = x[2] / a0; a3 = x[3] / a0; }
+    else { a1 = x[1]; a2 = x[2]; a3 = x[3]; }
+    A2 = a1 * a1;
+    Q = (A2 - 3.0 * a2) / 9.0;
+    R = (a1 * (A2 - 4.5 * a2) + 13.5 * a3) / 27.0;
+    Q3 = Q * Q * Q;
+    R2 = R * R;
+    d = Q3 - R2;
+    an = a1 / 3.0;
+    if (d >= 0.0) {
+        d = R / sqrt(Q3);
+        theta = acos(d) / 3.0;
+        sQ = -2.0 * sqrt(Q);
+        y[0] = sQ * cos(theta) - an;
+        y[1] = sQ * cos(theta + TWO_M_PI_3) - an;
+        y[2] = sQ * cos(theta + FOUR_M_PI_3) - an;
+        return 3;
+    }
+    sQ = pow(sqrt(R2 - Q3) + fabs(R), 1.0 / 3.0);
+    if (R < 0) y[0] = (sQ + Q / sQ) - an;
+    else y[0] = -(sQ + Q / sQ) - an;
+    return 1;
+}
+
+/* difficult_coeffs keeps the reference's signed "biggest" (polynomialsolver.cpp:1075-1111). */
+static int ps_difficult(int n, const double* x)
+{
+    double biggest = 0.0;
+    for (int i = 0; i <= n; i++)
+        if (fabs(x[i]) > biggest) biggest = x[i];
+    if (biggest == 0.0) return 0;
+    for (int i = 0; i <= n; i++)
+        if (x[i] != 0.0 && fabs(biggest / x[i]) > PS_FUDGE1) return 1;
+    return 0;
+}
+
+static int ps_quartic(const double* x, double* results)
+{
+    double cubic[4], roots[3], c12, z, p, q, q1, q2, r, d1, d2, c1, c2, c3, c4, c0 = x[0];
+    if (c0 != 1.0) { c1 = x[1] / c0; c2 = x[2] / c0; c3 = x[3] / c0; c4 = x[4] / c0; }
+    else { c1 = x[1]; c2 = x[2]; c3 = x[3]; c4 = x[4]; }
+    c12 = c1 * c1;
+    p = -0.375 * c12 + c2;
+    q = 0.125 * c12 * c1 - 0.5 * c1 * c2 + c3;
+    r = -0.01171875 * c12 * c12 + 0.0625 * c12 * c2 - 0.25 * c1 * c3 + c4;
+    cubic[0] = 1.0;
+    cubic[1] = -0.5 * p;
+    cubic[2] = -r;
+    cubic[3] = 0.5 * r * p - 0.125 * q * q;
+    if (ps_cubic(cubic, roots) > 0) z = roots[0];
+    else return 0;
+    d1 = 2.0 * z - p;
+    if (d1 < 0.0) {
+        if (d1 > -PS_SMALL_ENOUGH) d1 = 0.0;
+        else return 0;
+    }
+    if (d1 < PS_SMALL_ENOUGH) {
+        d2 = z * z - r;
+        if (d2 < 0.0) return 0;
+        d2 = sqrt(d2);
+    } else {
+        d1 = sqrt(d1);
+        d2 = 0.5 * q / d1;
+    }
+    q1 = d1 * d1;
+    q2 = -0.25 * c1;
+    int i = 0;
+    p = q1 - 4.0 * (z - d2);
+    if (p == 0) results[i++] = -0.5 * d1 - q2;
+    else if (p > 0) {
+        p = sqrt(p);
+        results[i++] = -0.5 * (d1 + p) + q2;
+        results[i++] = -0.5 * (d1 - p) + q2;
+    }
+    p = q1 - 4.0 * (z + d2);
+    if (p == 0) results[i++] = 0.5 * d1 - q2;
+    else if (p > 0) {
+        p = sqrt(p);
+        results[i++] = 0.5 * (d1 + p) + q2;
+        results[i++] = 0.5 * (d1 - p) + q2;
+    }
+    return i;
+}
+
+static int solve_polynomial(int n, const double* c0, double* r, int sturm, double epsilon)
+{
+    int roots = 0, i = 0;
+    while ((i < n) && (fabs(c0[i]) < PS_SMALL_ENOUGH))
+        i++;
+    n -= i;
+    const double* c = &c0[i];
+    switch (n) {
+    case 0: break;
+    case 1: if (c[0] != 0.0) r[roots++] = -c[1] / c[0]; break;
+    case 2: roots = ps_quadratic(c, r); break;
+    case 3:
+        if (epsilon > 0.0 && (c[2] != 0.0) && (fabs(c[3] / c[2]) < epsilon)) { roots = ps_quadratic(c, r); break; }
+        roots = sturm ? ps_polysolve(3, c, r) : ps_cubic(c, r);
+        break;
+    case 4:
+        if (epsilon > 0.0 && (c[3] != 0.0) && (fabs(c[4] / c[3]) < epsilon)) {
+            roots = sturm ? ps_polysolve(3, c, r) : ps_cubic(c, r);
+            break;
+        }
+        if (ps_difficult(4, c)) sturm = 1;
+        roots = sturm ? ps_polysolve(4, c, r) : ps_quartic(c, r);
+        break;
+    default:
+        if (epsilon > 0.0 && (c[n - 1] != 0.0) && (fabs(c[n] / c[n - 1]) < epsilon)) {
+            roots = ps_polysolve(n - 1, c, r);
+            break;
+        }
+        roots = ps_polysolve(n, c, r);
+        break;
+    }
+    return roots;
+}
+
+/* Torus (source/core/shape/torus.cpp:78-82,241-362,932-1084) */
+#define TORUS_DEPTH_TOLERANCE 1.0e-4
+#define TORUS_ROOT_TOLERANCE 1.0e-4
+static int torus_thick_cylinder(V3 P, V3 D, double h1, double h2, double r1, double r2)
+{
+    double a, b, c, d, u, v, k, r, h;
+    if (fabs(D.y) < EPSILON) {
+        if ((P.y < h1) || (P.y > h2)) return 0;
+    } else {
+        k = (h2 - P.y) / D.y;
+        u = P.x + k * D.x;
+        v = P.z + k * D.z;
+        if ((k > EPSILON) && (k < MAX_DISTANCE)) {
+            r = u * u + v * v;
+            if ((r >= r1) && (r <= r2)) return 1;
+        }
+        k = (h1 - P.y) / D.y;
+        u = P.x + k * D.x;
+        v = P.z + k * D.z;
+        if ((k > EPSILON) && (k < MAX_DISTANCE)) {
+            r = u * u + v * v;
+            if ((r >= r1) && (r <= r2)) return 1;
+        }
+    }
+    a = D.x * D.x + D.z * D.z;
+    if (a > EPSILON) {
+        b = P.x * D.x + P.z * D.z;
+        c = P.x * P.x + P.z * P.z - r2;
+        d = b * b - a * c;
+        if (d >= 0.0) {
+            d = sqrt(d);
+            k = (-b + d) / a;
+            if ((k > EPSILON) && (k < MAX_DISTANCE)) { h = P.y + k * D.y; if ((h >= h1) && (h <= h2)) return 1; }
+            k = (-b - d) / a;
+            if ((k > EPSILON) && (k < MAX_DISTANCE)) { h = P.y + k * D.y; if ((h >= h1) && (h <= h2)) return 1; }
+        }
+        c = P.x * P.x + P.z * P.z - r1;
+        d = b * b - a * c;
+        if (d >= 0.0) {
+            d = sqrt(d);
+            k = (-b + d) / a;
+            if ((k > EPSILON) && (k < MAX_DISTANCE)) { h = P.y + k * D.y; if ((h >= h1) && (h <= h2)) return 1; }
+            k = (-b - d) / a;
+            if ((k > EPSILON) && (k < MAX_DISTANCE)) { h = P.y + k * D.y; if ((h >= h1) && (h <= h2)) return 1; }
+        }
+    }
+    return 0;
+}
+
+static int torus_intersect(const PovGpuObject* o, V3 O, V3 Dw, double* depth)
+{
+    const double* inv = o->trans + 16;
+    double R = o->p[0], rr = o->p[1];
+    V3 P = mtrans_point(inv, O);
+    V3 D = mtrans_direction(inv, Dw);
+    double len = vlen(D);
+    D = vdiv(D, len);
+    int i = 0;
+    double y1 = -rr, y2 = rr, r1 = (R - rr) * (R - rr), r2 = (R + rr) * (R + rr);
+    if (R < rr) r1 = 0;
+    if (torus_thick_cylinder(P, D, y1, y2, r1, r2)) {
+        double bsr = R + rr + rr;
+        double dp = vdot(P, P);
+        double closer = 0.0;
+        if (dp > bsr * bsr) {
+            dp = sqrt(dp);
+            closer = dp - bsr;
+            P = vadd(P, vmul(D, closer));
+        }
+        double R2 = R * R, rr2 = rr * rr;
+        double Py2 = P.y * P.y, Dy2 = D.y * D.y, PDy2 = P.y * D.y;
+        double k1 = P.x * P.x + P.z * P.z + Py2 - R2 - rr2;
+        double k2 = P.x * D.x + P.z * D.z + PDy2;
+        double c[5], r[4];
+        c[0] = 1.0;
+        c[1] = 4.0 * k2;
+        c[2] = 2.0 * (k1 + 2.0 * (k2 * k2 + R2 * Dy2));
+        c[3] = 4.0 * (k2 * k1 + 2.0 * R2 * PDy2);
+        c[4] = k1 * k1 + 4.0 * R2 * (Py2 - rr2);
+        int n = solve_polynomial(4, c, r, 0, TORUS_ROOT_TOLERANCE);
+        while (n--)
+            depth[i++] = (r[n] + closer) / len;
+    }
+    return i;
+}
+
+static int torus_inside(const PovGpuObject* o, V3 p)
+{
+    V3 P = mtrans_point(o->trans + 16, p);
+    double r = sqrt(P.x * P.x + P.z * P.z);
+    double r2 = P.y * P.y + (r - o->p[0]) * (r - o->p[0]);
+    int inside = r2 <= o->p[1] * o->p[1];
+    return (o->flags & POV_FLAG_INVERTED) ? !inside : inside;
+}
+
+static V3 torus_normal(const PovGpuObject* o, V3 ip)
+{
+    V3 P = mtrans_point(o->trans + 16, ip);
+    double dist = sqrt(P.x * P.x + P.z * P.z);
+    V3 M = dist > EPSILON ? v3(o->p[0] * P.x / dist, 0.0, o->p[0] * P.z / dist) : v3(0, 0, 0);
+    return vnorm(mtrans_normal(o->trans + 16, vsub(P, M)));
+}
 
 typedef struct {
     PQueue  pq;       /* top-level queue */
@@ -642,9 +1174,126 @@ static int mesh_closest(const OMesh* m, Thread* th, V3 O, V3 D, double min_depth
     return found;
 }
 
-/* Per-object closest hit: Find_Intersection (object.cpp:118-168,172-225)
- * with All_Intersections of the shape; `min_depth` is MIN_ISECT_DEPTH,
- * raised by a postcondition (SMALL_TOLERANCE for shadow rays). */
+/* One entry of an IStack (Intersection: depth, object, aux = box side or
+ * mesh triangle). */
+typedef struct { double depth; int32_t object; int32_t aux; } Hit;
+#define MAX_HITS 64
+
+static int inside_object(const PovOracle* S, int32_t oi, V3 p);
+
+/* All_Intersections of one object (the shape files' All_Intersections and
+ * the CSG ones of source/core/shape/csg.cpp:128-403), pushing every hit in
+ * the reference's order. */
+static int object_all_hits(const PovOracle* S, Thread* th, int32_t oi, V3 O, V3 D, Hit* out, int n, int cap)
+{
+    const PovGpuObject* o = &S->objs[oi].o;
+    switch (o->type) {
+    case POV_OBJ_SPHERE: {   /* sphere.cpp:92-212 */
+        double d1, d2;
+        if (sphere_intersect(O, D, v3(o->p[0], o->p[1], o->p[2]), o->p[3] * o->p[3], &d1, &d2)) {
+            if (d1 > SPHERE_DEPTH_TOLERANCE && d1 < MAX_DISTANCE && n < cap) out[n++] = (Hit){d1, oi, -1};
+            if (d2 > SPHERE_DEPTH_TOLERANCE && d2 < MAX_DISTANCE && n < cap) out[n++] = (Hit){d2, oi, -1};
+        }
+        return n;
+    }
+    case POV_OBJ_PLANE: {    /* plane.cpp:92-211 */
+        V3 N = v3(o->p[0], o->p[1], o->p[2]);
+        double ndd = vdot(N, D);
+        if (fabs(ndd) < EPSILON) return n;
+        double t = -(vdot(N, O) + o->p[3]) / ndd;
+        if (t >= PLANE_DEPTH_TOLERANCE && t <= MAX_DISTANCE && n < cap) out[n++] = (Hit){t, oi, -1};
+        return n;
+    }
+    case POV_OBJ_BOX: {      /* box.cpp:100-170 */
+        double d1, d2;
+        int s1, s2;
+        if (box_intersect(O, D, v3(o->p[0], o->p[1], o->p[2]), v3(o->p[3], o->p[4], o->p[5]), &d1, &d2, &s1, &s2)) {
+            if (d1 > BOX_DEPTH_TOLERANCE && n < cap) out[n++] = (Hit){d1, oi, s1};
+            if (n < cap) out[n++] = (Hit){d2, oi, s2};
+        }
+        return n;
+    }
+    case POV_OBJ_TORUS: {    /* torus.cpp:133-160 */
+        double dep[4];
+        int k = torus_intersect(o, O, D, dep);
+        for (int i = 0; i < k; i++)
+            if (dep[i] > TORUS_DEPTH_TOLERANCE && dep[i] < MAX_DISTANCE && n < cap) out[n++] = (Hit){dep[i], oi, -1};
+        return n;
+    }
+    case POV_OBJ_UNION: {
+        for (int c = 0; c < o->num_children; c++)
+            n = object_all_hits(S, th, o->first_child + c, O, D, out, n, cap);
+        return n;
+    }
+    case POV_OBJ_INTERSECTION:
+    case POV_OBJ_MERGE: {
+        Hit local[MAX_HITS];
+        int merge = o->type == POV_OBJ_MERGE;
+        int c = o->first_child;
+        for (int k = 0; k < o->num_children; k++) {
+            int ln = object_all_hits(S, th, c, O, D, local, 0, MAX_HITS);
+            /* the local stack is drained from the top */
+            for (int h = ln - 1; h >= 0; h--) {
+                V3 P = vadd(O, vmul(D, local[h].depth));
+                int keep = 1;
+                /* children are leaves here (checked at create), so siblings are consecutive */
+                for (int j = 0; j < o->num_children; j++) {
+                    int s = o->first_child + j;
+                    if (s != c) {
+                        int in = inside_object(S, s, P);
+                        if (merge ? in : !in) { keep = 0; break; }
+                    }
+                }
+                if (keep && n < cap) out[n++] = local[h];
+            }
+            c++;
+        }
+        return n;
+    }
+    default:
+        return n;
+    }
+}
+
+/* ObjectBase::Inside for the supported shapes (sphere.cpp:271-303,
+ * box.cpp Box::Inside, torus.cpp Torus::Inside, plane.cpp Plane::Inside,
+ * csg.cpp:405-450). */
+static int inside_object(const PovOracle* S, int32_t oi, V3 p)
+{
+    const PovGpuObject* o = &S->objs[oi].o;
+    int inv = (o->flags & POV_FLAG_INVERTED) != 0;
+    switch (o->type) {
+    case POV_OBJ_SPHERE: {
+        V3 d = vsub(v3(o->p[0], o->p[1], o->p[2]), p);
+        double ocs = vdot(d, d), r2 = o->p[3] * o->p[3];
+        return inv ? ocs > r2 : ocs < r2;
+    }
+    case POV_OBJ_BOX:
+        if (p.x < o->p[0] || p.x > o->p[3] || p.y < o->p[1] || p.y > o->p[4] || p.z < o->p[2] || p.z > o->p[5])
+            return inv;
+        return !inv;
+    case POV_OBJ_TORUS:
+        return torus_inside(o, p);
+    case POV_OBJ_PLANE:
+        return (vdot(p, v3(o->p[0], o->p[1], o->p[2])) + o->p[3]) < EPSILON;
+    case POV_OBJ_UNION:
+    case POV_OBJ_MERGE:
+        for (int c = 0; c < o->num_children; c++)
+            if (inside_object(S, o->first_child + c, p)) return 1;
+        return 0;
+    case POV_OBJ_INTERSECTION:
+        for (int c = 0; c < o->num_children; c++)
+            if (!inside_object(S, o->first_child + c, p)) return 0;
+        return 1;
+    default:
+        return 0;
+    }
+}
+
+/* Per-object closest hit: Find_Intersection (object.cpp:118-168,172-225):
+ * the IStack is drained from the top and the closest depth >= min_depth
+ * (MIN_ISECT_DEPTH, raised by a postcondition such as SMALL_TOLERANCE for
+ * shadow rays) wins on strict '<'. */
 static int object_closest(const PovOracle* S, Thread* th, int32_t oi, V3 O, V3 D, double min_depth,
                           double closest, Isect* out)
 {
@@ -653,50 +1302,36 @@ static int object_closest(const PovOracle* S, Thread* th, int32_t oi, V3 O, V3 D
     double best = closest;
     int found = 0;
     if (th->counting) th->prims++;
-    switch (o->type) {
-    case POV_OBJ_SPHERE: {
-        double d1, d2;
-        V3 C = v3(o->p[0], o->p[1], o->p[2]);
-        if (sphere_intersect(O, D, C, o->p[3] * o->p[3], &d1, &d2)) {
-            /* both roots are pushed; the stack is scanned for the closest */
-            if (d1 > SPHERE_DEPTH_TOLERANCE && d1 < MAX_DISTANCE && d1 >= min_depth && d1 < best) {
-                best = d1; found = 1;
-            }
-            if (d2 > SPHERE_DEPTH_TOLERANCE && d2 < MAX_DISTANCE && d2 >= min_depth && d2 < best) {
-                best = d2; found = 1;
-            }
-        }
-        if (found) { out->triangle = -1; }
-        break;
-    }
-    case POV_OBJ_PLANE: {   /* Plane::Intersect (plane.cpp:139-211) */
-        V3 N = v3(o->p[0], o->p[1], o->p[2]);
-        double ndd = vdot(N, D);
-        if (fabs(ndd) < EPSILON)
-            break;
-        double ndo = vdot(N, O);
-        double t = -(ndo + o->p[3]) / ndd;
-        if (t >= PLANE_DEPTH_TOLERANCE && t <= MAX_DISTANCE && t >= min_depth && t < best) {
-            best = t; found = 1; out->triangle = -1;
-        }
-        break;
-    }
-    case POV_OBJ_MESH: {
+    if (o->type == POV_OBJ_MESH) {
         if (!intersect_bbox_dir(&ob->bbox, O, D, (float)closest))
-            break;
+            return 0;
         double t;
         int32_t tri = -1;
         if (mesh_closest(&S->meshes[o->mesh], th, O, D, min_depth, best, &t, &tri)) {
-            best = t; found = 1; out->triangle = tri;
+            out->depth = t;
+            out->object = oi;
+            out->triangle = tri;
+            out->ipoint = vadd(O, vmul(D, t));
+            return 1;
         }
-        break;
+        return 0;
     }
-    default:
-        break;
+    /* ObjectBase::Intersect_BBox pre-test: sphere, plane and box answer true */
+    if (o->type == POV_OBJ_TORUS || o->type >= POV_OBJ_UNION)
+        if (!intersect_bbox_dir(&ob->bbox, O, D, (float)closest))
+            return 0;
+    Hit hits[MAX_HITS];
+    int n = object_all_hits(S, th, oi, O, D, hits, 0, MAX_HITS);
+    for (int i = n - 1; i >= 0; i--) {
+        if (hits[i].depth < best && hits[i].depth >= min_depth) {
+            best = hits[i].depth;
+            out->object = hits[i].object;
+            out->triangle = hits[i].aux;
+            found = 1;
+        }
     }
     if (found) {
         out->depth = best;
-        out->object = oi;
         out->ipoint = vadd(O, vmul(D, best));
     }
     return found;
@@ -767,6 +1402,17 @@ static V3 object_normal(const PovOracle* S, const Isect* is)
         return vdiv(vsub(is->ipoint, v3(o->p[0], o->p[1], o->p[2])), o->p[3]);
     case POV_OBJ_PLANE:
         return v3(o->p[0], o->p[1], o->p[2]);
+    case POV_OBJ_BOX:      /* Box::Normal: the side recorded in Intersection::i1 */
+        switch (is->triangle) {
+        case SIDE_X0: return v3(-1, 0, 0);
+        case SIDE_X1: return v3(1, 0, 0);
+        case SIDE_Y0: return v3(0, -1, 0);
+        case SIDE_Y1: return v3(0, 1, 0);
+        case SIDE_Z0: return v3(0, 0, -1);
+        default: return v3(0, 0, 1);
+        }
+    case POV_OBJ_TORUS:
+        return torus_normal(o, is->ipoint);
     case POV_OBJ_MESH: {   /* Mesh::Normal, Smooth_Mesh_Normal (mesh.cpp:342-436) */
         const OMesh* m = &S->meshes[o->mesh];
         const MeshTri* T = &m->tris[is->triangle];
@@ -1072,6 +1718,48 @@ static BBox object_bbox(const PovOracle* S, const PovGpuObject* o)
         b = bbox_from_min_max(mn, mx);
         break;
     }
+    case POV_OBJ_BOX:        /* Box::Compute_BBox (box.cpp:947-957) */
+        b = bbox_from_min_max(v3(o->p[0], o->p[1], o->p[2]), v3(o->p[3], o->p[4], o->p[5]));
+        break;
+    case POV_OBJ_TORUS: {    /* Torus::Compute_BBox + Recompute_BBox (torus.cpp:849-859, boundingbox.cpp:168) */
+        double r1 = o->p[1], r2 = o->p[0] + o->p[1];
+        float ll[3] = {(float)-r2, (float)-r1, (float)-r2};
+        float sz[3] = {(float)(2.0 * r2), (float)(2.0 * r1), (float)(2.0 * r2)};
+        V3 mn = v3(BOUND_HUGE, BOUND_HUGE, BOUND_HUGE), mx = v3(-BOUND_HUGE, -BOUND_HUGE, -BOUND_HUGE);
+        for (int i = 1; i <= 8; i++) {
+            V3 c = v3(ll[0] + ((i & 1) ? sz[0] : 0.0), ll[1] + ((i & 2) ? sz[1] : 0.0), ll[2] + ((i & 4) ? sz[2] : 0.0));
+            c = mtrans_point(o->trans, c);
+            mn.x = fmin(mn.x, c.x); mn.y = fmin(mn.y, c.y); mn.z = fmin(mn.z, c.z);
+            mx.x = fmax(mx.x, c.x); mx.y = fmax(mx.y, c.y); mx.z = fmax(mx.z, c.z);
+        }
+        b = bbox_from_min_max(mn, mx);
+        break;
+    }
+    case POV_OBJ_UNION:
+    case POV_OBJ_MERGE:
+    case POV_OBJ_INTERSECTION: {   /* CSG::Compute_BBox (csg.cpp:872-): union of the
+                                      children, or the overlap of the non-inverted ones */
+        int isect = o->type == POV_OBJ_INTERSECTION;
+        V3 mn = isect ? v3(-BOUND_HUGE, -BOUND_HUGE, -BOUND_HUGE) : v3(BOUND_HUGE, BOUND_HUGE, BOUND_HUGE);
+        V3 mx = isect ? v3(BOUND_HUGE, BOUND_HUGE, BOUND_HUGE) : v3(-BOUND_HUGE, -BOUND_HUGE, -BOUND_HUGE);
+        for (int c = 0; c < o->num_children; c++) {
+            const PovGpuObject* ch = &S->objs[o->first_child + c].o;
+            if (isect && (ch->flags & POV_FLAG_INVERTED))
+                continue;
+            BBox cb = object_bbox(S, ch);
+            V3 cl = v3(cb.ll[0], cb.ll[1], cb.ll[2]);
+            V3 ch_ = v3((double)cb.ll[0] + cb.sz[0], (double)cb.ll[1] + cb.sz[1], (double)cb.ll[2] + cb.sz[2]);
+            if (isect) {
+                mn.x = fmax(mn.x, cl.x); mn.y = fmax(mn.y, cl.y); mn.z = fmax(mn.z, cl.z);
+                mx.x = fmin(mx.x, ch_.x); mx.y = fmin(mx.y, ch_.y); mx.z = fmin(mx.z, ch_.z);
+            } else {
+                mn.x = fmin(mn.x, cl.x); mn.y = fmin(mn.y, cl.y); mn.z = fmin(mn.z, cl.z);
+                mx.x = fmax(mx.x, ch_.x); mx.y = fmax(mx.y, ch_.y); mx.z = fmax(mx.z, ch_.z);
+            }
+        }
+        b = bbox_from_min_max(mn, mx);
+        break;
+    }
     default: {               /* infinite objects: Make_BBox(-BOUND_HUGE/2, BOUND_HUGE) */
         b.ll[0] = b.ll[1] = b.ll[2] = (float)(-BOUND_HUGE / 2);
         b.sz[0] = b.sz[1] = b.sz[2] = (float)BOUND_HUGE;
@@ -1107,16 +1795,39 @@ int pov_oracle_create(const PovGpuSceneDesc* desc, PovOracle** out, int32_t* bad
     int32_t* finite = (int32_t*)malloc(sizeof(int32_t) * (size_t)(S->nobjs + 1));
     int32_t* infinite = (int32_t*)malloc(sizeof(int32_t) * (size_t)(S->nobjs + 1));
     size_t nf = 0, ni = 0;
-    for (int i = 0; i < S->nobjs; i++) {
+    for (int i = 0; i < S->nobjs; i++)
         S->objs[i].o = desc->objects[i];
+    for (int i = 0; i < S->nobjs; i++) {
         const PovGpuObject* o = &S->objs[i].o;
-        if (o->type != POV_OBJ_SPHERE && o->type != POV_OBJ_PLANE && o->type != POV_OBJ_MESH) {
+        int ok = o->type >= POV_OBJ_SPHERE && o->type <= POV_OBJ_MERGE;
+        if (o->type == POV_OBJ_TORUS && !(o->flags & POV_FLAG_HAS_TRANS))
+            ok = 0;
+        if ((o->type == POV_OBJ_SPHERE || o->type == POV_OBJ_BOX || o->type == POV_OBJ_MESH ||
+             o->type == POV_OBJ_PLANE) && (o->flags & POV_FLAG_HAS_TRANS))
+            ok = 0;
+        if (o->type >= POV_OBJ_UNION) {
+            /* CSG with leaf children (spheres, boxes, tori, planes) */
+            if (o->first_child != i + 1 || o->num_children < 1 || o->first_child + o->num_children > S->nobjs)
+                ok = 0;
+            for (int c = 0; ok && c < o->num_children; c++) {
+                const PovGpuObject* ch = &S->objs[o->first_child + c].o;
+                if (ch->type == POV_OBJ_MESH || ch->type >= POV_OBJ_UNION || ch->parent != i)
+                    ok = 0;
+            }
+        }
+        if (o->parent >= 0 && S->objs[o->parent].o.type < POV_OBJ_UNION)
+            ok = 0;
+        if (!ok) {
             if (bad_index) *bad_index = i;
             free(finite); free(infinite);
             pov_oracle_destroy(S);
             return POV_GPU_E_UNSUPPORTED;
         }
-        S->objs[i].bbox = object_bbox(S, o);
+    }
+    for (int i = S->nobjs - 1; i >= 0; i--)   /* children before parents (CSG boxes) */
+        S->objs[i].bbox = object_bbox(S, &S->objs[i].o);
+    for (int i = 0; i < S->nobjs; i++) {      /* Build_Bounding_Slabs keeps object order */
+        const PovGpuObject* o = &S->objs[i].o;
         if (o->parent >= 0)
             continue;
         TNode n;
@@ -1170,7 +1881,8 @@ int pov_oracle_trace_rays(PovOracle* S, const double* org, const double* dir, in
         V3 O = vload(org + 3 * i), D = vload(dir + 3 * i);
         if (find_intersection(S, &th, O, D, HUGE_VAL, 0, &is)) {
             hits[i].object = is.object;
-            hits[i].triangle = is.triangle;
+            /* the triangle index only means something for mesh hits */
+            hits[i].triangle = S->objs[is.object].o.type == POV_OBJ_MESH ? is.triangle : -1;
             hits[i].t = is.depth;
         } else {
             hits[i].object = -1;
@@ -1222,7 +1934,162 @@ typedef struct {
     int32_t next_row;
     pthread_mutex_t lock;
     PovGpuStats stats;
+    int32_t next_block;
 } RenderJob;
+
+/* ---------------------------------------- adaptive antialiasing (M2) --- */
+typedef struct { float r, g, b, t; } Col4;
+
+static Col4 trace_sample(const PovOracle* S, Thread* th, double x, double y, double w, double h)
+{
+    float c[4];
+    trace_pixel(S, th, x, y, w, h, c);
+    Col4 r = {c[0], c[1], c[2], c[3]};
+    return r;
+}
+
+/* AA gamma: PowerLawGammaCurve with decoding gamma 2.5 (view.cpp:724-728,
+ * colourspace.cpp:310): pow(max(x, 0), 1/2.5) per colour channel. */
+static Col4 aa_encode(Col4 c)
+{
+    const float g = 1.0f / 2.5f;
+    Col4 r = {powf(fmaxf(c.r, 0.0f), g), powf(fmaxf(c.g, 0.0f), g), powf(fmaxf(c.b, 0.0f), g), c.t};
+    return r;
+}
+
+static float col_dist(Col4 a, Col4 b)   /* ColourDistanceRGBT (base/colour.h:1221) */
+{
+    return fabsf(a.r - b.r) + fabsf(a.g - b.g) + fabsf(a.b - b.b) + fabsf(a.t - b.t);
+}
+
+typedef struct {
+    Col4*    col;
+    uint8_t* sampled;
+    int      size;
+} SubBuf;
+
+static void subbuf_set(SubBuf* B, int x, int y, Col4 c)
+{
+    B->col[x + y * B->size] = c;
+    B->sampled[x + y * B->size] = 1;
+}
+
+/* TraceTask::SubdivideOnePixel (tracetask.cpp:892-1063), jitter off. */
+static void subdivide_one_pixel(const PovOracle* S, Thread* th, const PovGpuRenderParams* p, double x, double y,
+                                double d, int bx, int by, int bstep, SubBuf* B, Col4* result, int level,
+                                uint64_t* samples)
+{
+    Col4 c00 = B->col[bx + by * B->size], c02 = B->col[bx + (by + bstep) * B->size];
+    Col4 c20 = B->col[bx + bstep + by * B->size], c22 = B->col[bx + bstep + (by + bstep) * B->size];
+    int h = bstep / 2;
+    double thr = (double)p->aa_threshold;
+    Col4 g00 = aa_encode(c00), g02 = aa_encode(c02), g20 = aa_encode(c20), g22 = aa_encode(c22);
+    double W = p->width, H = p->height;
+    if (level > 0 && (col_dist(g00, g02) >= thr || col_dist(g00, g20) >= thr || col_dist(g00, g22) >= thr ||
+                      col_dist(g02, g20) >= thr || col_dist(g02, g22) >= thr || col_dist(g20, g22) >= thr)) {
+        double d2 = d * 0.5;
+        if (!B->sampled[bx + (by + h) * B->size]) {
+            subbuf_set(B, bx, by + h, trace_sample(S, th, x + 0.5 - d, y + 0.5, W, H));
+            (*samples)++;
+        }
+        if (!B->sampled[bx + h + by * B->size]) {
+            subbuf_set(B, bx + h, by, trace_sample(S, th, x + 0.5, y + 0.5 - d, W, H));
+            (*samples)++;
+        }
+        if (!B->sampled[bx + bstep + (by + h) * B->size]) {
+            subbuf_set(B, bx + bstep, by + h, trace_sample(S, th, x + 0.5 + d, y + 0.5, W, H));
+            (*samples)++;
+        }
+        if (!B->sampled[bx + h + (by + bstep) * B->size]) {
+            subbuf_set(B, bx + h, by + bstep, trace_sample(S, th, x + 0.5, y + 0.5 + d, W, H));
+            (*samples)++;
+        }
+        if (!B->sampled[bx + h + (by + h) * B->size]) {
+            subbuf_set(B, bx + h, by + h, trace_sample(S, th, x + 0.5, y + 0.5, W, H));
+            (*samples)++;
+        }
+        Col4 r00, r01, r10, r11;
+        subdivide_one_pixel(S, th, p, x - d2, y - d2, d2, bx, by, h, B, &r00, level - 1, samples);
+        subdivide_one_pixel(S, th, p, x - d2, y + d2, d2, bx, by + h, h, B, &r01, level - 1, samples);
+        subdivide_one_pixel(S, th, p, x + d2, y - d2, d2, bx + h, by, h, B, &r10, level - 1, samples);
+        subdivide_one_pixel(S, th, p, x + d2, y + d2, d2, bx + h, by + h, h, B, &r11, level - 1, samples);
+        result->r = (r00.r + r01.r + r10.r + r11.r) / 4.0f;
+        result->g = (r00.g + r01.g + r10.g + r11.g) / 4.0f;
+        result->b = (r00.b + r01.b + r10.b + r11.b) / 4.0f;
+        result->t = (r00.t + r01.t + r10.t + r11.t) / 4.0f;
+    } else {
+        result->r = (c00.r + c02.r + c20.r + c22.r) / 4.0f;
+        result->g = (c00.g + c02.g + c20.g + c22.g) / 4.0f;
+        result->b = (c00.b + c02.b + c20.b + c22.b) / 4.0f;
+        result->t = (c00.t + c02.t + c20.t + c22.t) / 4.0f;
+    }
+}
+
+/* TraceTask::AdaptiveSupersamplingM2 (tracetask.cpp:604-657) over the
+ * view's 32x32 block grid; pixels outside the requested rectangle are
+ * traced (block corners) but not written. */
+static void* render_worker_aa(void* arg)
+{
+    RenderJob* J = (RenderJob*)arg;
+    const PovGpuRenderParams* p = J->p;
+    Thread th;
+    memset(&th, 0, sizeof(th));
+    const int bs = 32;
+    int nbx = (p->width + bs - 1) / bs, nby = (p->height + bs - 1) / bs;
+    int depth = p->aa_depth < 1 ? 1 : p->aa_depth;
+    int subsize = 1 << depth;
+    SubBuf B;
+    B.size = subsize + 1;
+    B.col = (Col4*)malloc(sizeof(Col4) * B.size * B.size);
+    B.sampled = (uint8_t*)malloc((size_t)B.size * B.size);
+    Col4* corners = (Col4*)malloc(sizeof(Col4) * (bs + 1) * (bs + 1));
+    uint64_t pixels = 0, samples = 0;
+    for (;;) {
+        pthread_mutex_lock(&J->lock);
+        int b = J->next_block++;
+        pthread_mutex_unlock(&J->lock);
+        if (b >= nbx * nby)
+            break;
+        int left = (b % nbx) * bs, top = (b / nbx) * bs;
+        int right = left + bs - 1 < p->width - 1 ? left + bs - 1 : p->width - 1;
+        int bottom = top + bs - 1 < p->height - 1 ? top + bs - 1 : p->height - 1;
+        if (right < J->x0 || left >= J->x1 || bottom < J->y0 || top >= J->y1)
+            continue;
+        int cw = right - left + 2;
+        for (int y = top; y <= bottom + 1; y++)
+            for (int x = left; x <= right + 1; x++) {
+                corners[(y - top) * cw + (x - left)] = trace_sample(J->S, &th, x, y, p->width, p->height);
+                pixels++;
+            }
+        for (int y = top; y <= bottom; y++)
+            for (int x = left; x <= right; x++) {
+                memset(B.sampled, 0, (size_t)B.size * B.size);
+                subbuf_set(&B, 0, 0, corners[(y - top) * cw + (x - left)]);
+                subbuf_set(&B, 0, subsize, corners[(y + 1 - top) * cw + (x - left)]);
+                subbuf_set(&B, subsize, 0, corners[(y - top) * cw + (x + 1 - left)]);
+                subbuf_set(&B, subsize, subsize, corners[(y + 1 - top) * cw + (x + 1 - left)]);
+                Col4 r;
+                subdivide_one_pixel(J->S, &th, p, x, y, 0.5, 0, 0, subsize, &B, &r, depth - 1, &samples);
+                if (x >= J->x0 && x < J->x1 && y >= J->y0 && y < J->y1) {
+                    float* o = J->out + ((size_t)(y - J->y0) * (J->x1 - J->x0) + (x - J->x0)) * 4;
+                    o[0] = r.r; o[1] = r.g; o[2] = r.b; o[3] = r.t;
+                }
+            }
+    }
+    pthread_mutex_lock(&J->lock);
+    J->stats.number_of_rays += th.rays;
+    J->stats.shadow_ray_tests += th.shadow_tests;
+    J->stats.shadow_rays_succeeded += th.shadow_succeeded;
+    J->stats.reflected_rays += th.reflected;
+    J->stats.number_of_pixels += pixels;
+    J->stats.number_of_samples += samples;
+    pthread_mutex_unlock(&J->lock);
+    free(B.col);
+    free(B.sampled);
+    free(corners);
+    thread_free(&th);
+    return NULL;
+}
 
 static void* render_worker(void* arg)
 {
@@ -1255,7 +2122,8 @@ int pov_oracle_render(PovOracle* S, const PovGpuRenderParams* p, int32_t x0, int
 {
     if (!S || !p || !out || x1 < x0 || y1 < y0)
         return POV_GPU_E_INVALID;
-    if (p->antialias)
+    int aa = p->antialias != 0;
+    if (aa && (p->sampling_method != 2 || p->jitter))
         return POV_GPU_E_UNSUPPORTED;
     RenderJob J;
     memset(&J, 0, sizeof(J));
@@ -1265,18 +2133,20 @@ int pov_oracle_render(PovOracle* S, const PovGpuRenderParams* p, int32_t x0, int
         long n = sysconf(_SC_NPROCESSORS_ONLN);
         threads = n > 0 ? (int32_t)n : 1;
     }
+    void* (*worker)(void*) = aa ? render_worker_aa : render_worker;
     if (threads == 1) {
-        render_worker(&J);
+        worker(&J);
     } else {
         pthread_t* tids = (pthread_t*)malloc(sizeof(pthread_t) * threads);
         for (int i = 0; i < threads; i++)
-            pthread_create(&tids[i], NULL, render_worker, &J);
+            pthread_create(&tids[i], NULL, worker, &J);
         for (int i = 0; i < threads; i++)
             pthread_join(tids[i], NULL);
         free(tids);
     }
     pthread_mutex_destroy(&J.lock);
-    J.stats.number_of_pixels = (uint64_t)(x1 - x0) * (uint64_t)(y1 - y0);
+    if (!aa)
+        J.stats.number_of_pixels = (uint64_t)(x1 - x0) * (uint64_t)(y1 - y0);
     if (stats)
         *stats = J.stats;
     return POV_GPU_OK;

@@ -100,6 +100,86 @@ def _f32(x):
     return "%.9g" % float(x)
 
 
+# -------------------------------------------------------------- transforms --
+# TRANSFORM as the reference's parser builds it (source/core/math/matrix.cpp):
+# row-vector convention (p' = p . M), `matrix` and `inverse` 4x4, composed
+# by Compose_Transforms with the same multiplication order.
+M_PI_180 = 0.01745329251994329576
+
+
+def _identity():
+    return [[1.0, 0.0, 0.0, 0.0], [0.0, 1.0, 0.0, 0.0], [0.0, 0.0, 1.0, 0.0], [0.0, 0.0, 0.0, 1.0]]
+
+
+def _mtimes_a(result, m2):
+    """result = result x m2 (MTimesA, matrix.cpp:201)."""
+    for i in range(4):
+        t0, t1, t2, t3 = result[i]
+        result[i] = [t0 * m2[0][j] + t1 * m2[1][j] + t2 * m2[2][j] + t3 * m2[3][j] for j in range(4)]
+
+
+def _mtimes_b(m1, result):
+    """result = m1 x result (MTimesB, matrix.cpp:242)."""
+    for j in range(4):
+        t0, t1, t2, t3 = result[0][j], result[1][j], result[2][j], result[3][j]
+        for i in range(4):
+            result[i][j] = m1[i][0] * t0 + m1[i][1] * t1 + m1[i][2] * t2 + m1[i][3] * t3
+
+
+def _transpose(m):
+    return [[m[j][i] for j in range(4)] for i in range(4)]
+
+
+class Transform:
+    def __init__(self):
+        self.matrix = _identity()
+        self.inverse = _identity()
+
+    @staticmethod
+    def rotation(v):
+        """Compute_Rotation_Transform (matrix.cpp:685-737)."""
+        t = Transform()
+        rx, ry, rz = (float(v[0]) * M_PI_180, float(v[1]) * M_PI_180, float(v[2]) * M_PI_180)
+        cx, sx, cy, sy, cz, sz = math.cos(rx), math.sin(rx), math.cos(ry), math.sin(ry), math.cos(rz), math.sin(rz)
+        t.matrix[1][1] = cx
+        t.matrix[2][2] = cx
+        t.matrix[1][2] = sx
+        t.matrix[2][1] = 0.0 - sx
+        t.inverse = _transpose(t.matrix)
+        m = _identity()
+        m[0][0] = cy
+        m[2][2] = cy
+        m[0][2] = 0.0 - sy
+        m[2][0] = sy
+        _mtimes_a(t.matrix, m)
+        _mtimes_b(_transpose(m), t.inverse)
+        m = _identity()
+        m[0][0] = cz
+        m[1][1] = cz
+        m[0][1] = sz
+        m[1][0] = 0.0 - sz
+        _mtimes_a(t.matrix, m)
+        _mtimes_b(_transpose(m), t.inverse)
+        return t
+
+    @staticmethod
+    def translation(v):
+        """Compute_Translation_Transform (matrix.cpp:644-657)."""
+        t = Transform()
+        t.matrix[3][0], t.matrix[3][1], t.matrix[3][2] = float(v[0]), float(v[1]), float(v[2])
+        t.inverse[3][0], t.inverse[3][1], t.inverse[3][2] = -float(v[0]), -float(v[1]), -float(v[2])
+        return t
+
+    def compose(self, add):
+        """Compose_Transforms (matrix.cpp:788-793)."""
+        _mtimes_a(self.matrix, add.matrix)
+        _mtimes_b(add.inverse, self.inverse)
+        return self
+
+    def flat(self):
+        return [x for row in self.matrix for x in row] + [x for row in self.inverse for x in row]
+
+
 # ------------------------------------------------------------------ scenes --
 class Material:
     def __init__(self, rgb, ambient=0.1, diffuse=0.6, phong=0.0, phong_size=40.0,
@@ -221,6 +301,53 @@ class Scene:
         self.meshes.append(mesh)
         self.objects.append(dict(type=abi.POV_OBJ_MESH, mesh=len(self.meshes) - 1, material=mat))
 
+    def add(self, node):
+        """Adds an object tree built with the node helpers below."""
+        self.objects.append(node)
+
+    # node helpers (material -1 = inherited from the enclosing CSG)
+    @staticmethod
+    def n_sphere(centre, radius, mat=-1):
+        return dict(type=abi.POV_OBJ_SPHERE, centre=tuple(map(float, centre)), radius=float(radius), material=mat)
+
+    @staticmethod
+    def n_box(c1, c2, mat=-1):
+        lo = tuple(min(float(a), float(b)) for a, b in zip(c1, c2))
+        hi = tuple(max(float(a), float(b)) for a, b in zip(c1, c2))
+        return dict(type=abi.POV_OBJ_BOX, c1=lo, c2=hi, material=mat)
+
+    @staticmethod
+    def n_torus(major, minor, rotate=(0.0, 0.0, 0.0), translate=(0.0, 0.0, 0.0), mat=-1):
+        t = Transform().compose(Transform.rotation(rotate)).compose(Transform.translation(translate))
+        return dict(type=abi.POV_OBJ_TORUS, R=float(major), r=float(minor), trans=t,
+                    mods="rotate %s translate %s" % (_v(rotate), _v(translate)), material=mat)
+
+    @staticmethod
+    def n_csg(kind, children, translate=(0.0, 0.0, 0.0), mat=-1):
+        """kind: 'union', 'intersection', 'difference' or 'merge'.  The
+        translation is applied to the children as the parser does
+        (Sphere/Box::Translate move the geometry; CSG::Translate recurses)."""
+        tv = tuple(map(float, translate))
+        moved = []
+        for c in children:
+            c = dict(c)
+            if c["type"] == abi.POV_OBJ_SPHERE:
+                c["sdl_centre"] = c["centre"]
+                c["centre"] = tuple(a + b for a, b in zip(c["centre"], tv))
+            elif c["type"] == abi.POV_OBJ_BOX:
+                c["sdl_c1"], c["sdl_c2"] = c["c1"], c["c2"]
+                c["c1"] = tuple(a + b for a, b in zip(c["c1"], tv))
+                c["c2"] = tuple(a + b for a, b in zip(c["c2"], tv))
+            else:
+                raise ValueError("CSG children: spheres and boxes")
+            moved.append(c)
+        if kind == "difference":
+            for c in moved[1:]:
+                c["inverted"] = True
+        t = {"union": abi.POV_OBJ_UNION, "intersection": abi.POV_OBJ_INTERSECTION,
+             "difference": abi.POV_OBJ_INTERSECTION, "merge": abi.POV_OBJ_MERGE}[kind]
+        return dict(type=t, kind=kind, children=moved, translate=tv, material=mat)
+
     def point_light(self, pos, rgb=(1.0, 1.0, 1.0)):
         self.lights.append(dict(kind=abi.POV_LIGHT_POINT, pos=tuple(map(float, pos)),
                                 rgb=tuple(map(float, rgb))))
@@ -236,17 +363,26 @@ class Scene:
         for l in self.lights:
             out.append("light_source { %s color rgb %s }\n" % (_v(l["pos"]), _v(l["rgb"])))
         for o in self.objects:
-            mat = self.materials[o["material"]]
-            t = o["type"]
-            if t == abi.POV_OBJ_SPHERE:
-                out.append("sphere { %s, %s %s }\n" % (_v(o["centre"]), _g(o["radius"]), mat.sdl()))
-            elif t == abi.POV_OBJ_PLANE:
-                out.append("plane { %s, %s %s }\n" % (_v(o["normal"]), _g(o["offset"]), mat.sdl()))
-            elif t == abi.POV_OBJ_MESH:
-                out.append(self.meshes[o["mesh"]].sdl(mat))
-            else:
-                raise ValueError("no SDL writer for object type %d" % t)
+            out.append(self._sdl_node(o) + "\n")
         return "".join(out)
+
+    def _sdl_node(self, o):
+        tex = (" " + self.materials[o["material"]].sdl()) if o.get("material", -1) >= 0 else ""
+        t = o["type"]
+        if t == abi.POV_OBJ_SPHERE:
+            return "sphere { %s, %s%s }" % (_v(o.get("sdl_centre", o["centre"])), _g(o["radius"]), tex)
+        if t == abi.POV_OBJ_PLANE:
+            return "plane { %s, %s%s }" % (_v(o["normal"]), _g(o["offset"]), tex)
+        if t == abi.POV_OBJ_BOX:
+            return "box { %s, %s%s }" % (_v(o.get("sdl_c1", o["c1"])), _v(o.get("sdl_c2", o["c2"])), tex)
+        if t == abi.POV_OBJ_TORUS:
+            return "torus { %s, %s %s%s }" % (_g(o["R"]), _g(o["r"]), o["mods"], tex)
+        if t == abi.POV_OBJ_MESH:
+            return self.meshes[o["mesh"]].sdl(self.materials[o["material"]])
+        if t in (abi.POV_OBJ_UNION, abi.POV_OBJ_INTERSECTION, abi.POV_OBJ_MERGE):
+            kids = " ".join(self._sdl_node(dict(c, inverted=False)) for c in o["children"])
+            return "%s { %s translate %s%s }" % (o["kind"], kids, _v(o["translate"]), tex)
+        raise ValueError("no SDL writer for object type %d" % t)
 
     # -- C ABI ---------------------------------------------------------------
     def camera(self):
@@ -256,16 +392,31 @@ class Scene:
         """Returns (PovGpuSceneDesc, keepalive) -- keep the second alive while
         the first is in use."""
         keep = []
-        n = len(self.objects)
+        flat = []
+
+        def walk(o, parent):
+            idx = len(flat)
+            flat.append((o, parent))
+            for c in o.get("children", ()):
+                walk(c, idx)
+            return idx
+
+        for o in self.objects:
+            walk(o, -1)
+        n = len(flat)
         objs = (abi.PovGpuObject * max(n, 1))()
-        for i, o in enumerate(self.objects):
+        first_child = {}
+        for i, (o, parent) in enumerate(flat):
+            if parent >= 0 and parent not in first_child:
+                first_child[parent] = i
+        for i, (o, parent) in enumerate(flat):
             d = objs[i]
             d.type = o["type"]
-            d.flags = 0
-            d.material = o["material"]
-            d.parent = -1
-            d.first_child = -1
-            d.num_children = 0
+            d.flags = abi.POV_FLAG_INVERTED if o.get("inverted") else 0
+            d.material = o.get("material", -1)
+            d.parent = parent
+            d.first_child = first_child.get(i, -1)
+            d.num_children = len(o.get("children", ()))
             d.mesh = -1
             if o["type"] == abi.POV_OBJ_SPHERE:
                 d.p[0], d.p[1], d.p[2] = o["centre"]
@@ -275,6 +426,13 @@ class Scene:
                 d.p[0], d.p[1], d.p[2] = nrm
                 d.p[3] = -o["offset"]
                 d.flags |= abi.POV_FLAG_INFINITE
+            elif o["type"] == abi.POV_OBJ_BOX:
+                d.p[0], d.p[1], d.p[2] = o["c1"]
+                d.p[3], d.p[4], d.p[5] = o["c2"]
+            elif o["type"] == abi.POV_OBJ_TORUS:
+                d.p[0], d.p[1] = o["R"], o["r"]
+                d.flags |= abi.POV_FLAG_HAS_TRANS
+                d.trans[:] = o["trans"].flat()
             elif o["type"] == abi.POV_OBJ_MESH:
                 d.mesh = o["mesh"]
         mats = (abi.PovGpuMaterial * max(len(self.materials), 1))()
@@ -499,7 +657,49 @@ def mesh_spheres(width=1920, height=1080, mesh_n=296, n_spheres=1024, seed=2):
     return s
 
 
+def csg_torus_grid(width=1920, height=1080, n=16, seed=3, antialias=(0.1, 3)):
+    """CSG and quartic batch: n^3 objects on a grid of spacing 2 centred on the
+    origin, each jittered by U[-0.3,0.3]^3 (seed 3), cycling through
+      difference(box +-0.6, sphere r0.7), intersection(sphere r0.8, box +-0.5),
+      merge(two spheres r0.5, centres 0.4 apart), torus(0.6, 0.15) with a
+      random rotation;
+    random rgb pigments, 2 shadowing point lights, reflection 0.2,
+    max_trace_level 4, adaptive antialiasing (method 2) threshold 0.1 depth 3."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    count = n ** 3
+    jit = rng.uniform(-0.3, 0.3, size=(count, 3))
+    rot = rng.uniform(0.0, 360.0, size=(count, 3))
+    col = rng.uniform(0.0, 1.0, size=(count, 3))
+    s = Scene("csg_torus_grid", width, height, (0.0, 18.0, -42.0), (0.0, 0.0, 0.0), 50.0, max_trace_level=4)
+    s.point_light((30.0, 40.0, -30.0))
+    s.point_light((-30.0, 30.0, -20.0))
+    s.antialias = antialias
+    k = 0
+    for i in range(n):
+        for j in range(n):
+            for l in range(n):
+                c = ((i - (n - 1) / 2.0) * 2.0 + jit[k, 0], (j - (n - 1) / 2.0) * 2.0 + jit[k, 1],
+                     (l - (n - 1) / 2.0) * 2.0 + jit[k, 2])
+                m = s.material(Material(col[k], phong=0.5, reflection=0.2))
+                kind = k % 4
+                if kind == 0:
+                    node = Scene.n_csg("difference", [Scene.n_box((-0.6, -0.6, -0.6), (0.6, 0.6, 0.6)),
+                                                      Scene.n_sphere((0.0, 0.0, 0.0), 0.7)], c, m)
+                elif kind == 1:
+                    node = Scene.n_csg("intersection", [Scene.n_sphere((0.0, 0.0, 0.0), 0.8),
+                                                        Scene.n_box((-0.5, -0.5, -0.5), (0.5, 0.5, 0.5))], c, m)
+                elif kind == 2:
+                    node = Scene.n_csg("merge", [Scene.n_sphere((-0.2, 0.0, 0.0), 0.5),
+                                                 Scene.n_sphere((0.2, 0.0, 0.0), 0.5)], c, m)
+                else:
+                    node = Scene.n_torus(0.6, 0.15, rot[k], c, m)
+                s.add(node)
+                k += 1
+    return s
+
+
 WORKLOADS = {
     "spheres_plane": spheres_plane,
     "mesh_spheres": mesh_spheres,
+    "csg_torus_grid": csg_torus_grid,
 }

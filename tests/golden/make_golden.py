@@ -1,20 +1,29 @@
 """Generates the golden fixtures of this directory from the reference itself.
 
 Runs only where the reference sources are present (it drives
-oracle/_ref/pov_oracle, built from them by oracle/refbuild/Makefile):
+oracle/_ref/pov_oracle and oracle/_ref/povray_ref, built from them by
+oracle/refbuild/Makefile):
 
     python tests/golden/make_golden.py
 
 For every case it writes the scene's SDL to a temporary directory, has the
 reference parse and render it, and stores in <case>.npz:
   pixels       float32 (H, W, 4) linear RGBT from TracePixel::operator()
+               at pixel centres (no antialiasing)
   stats        JSON of Number_Of_Rays / Shadow_Ray_Tests / ... counters
   ray_org/dir  float64 probe rays (strided camera rays + random rays)
   hit_object, hit_triangle, hit_t   Trace::FindIntersection of each probe
-The cases are small so the fixtures stay a few hundred KB.
+  camera       the camera vectors after Parse_Camera
+and, for cases rendered with adaptive antialiasing, the reference CLI's own
+output (+AM2, jitter off):
+  aa_u8        uint8 (H, W, 3), the PPM it writes (BT.709 transfer curve)
+  aa_stats     JSON of its statistics printout (Pixels, Samples, Rays,
+               Shadow Ray Tests, Succeeded)
+The cases are small so the fixtures stay around a megabyte.
 """
 import json
 import os
+import re
 import struct
 import subprocess
 import sys
@@ -27,28 +36,44 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
 from povray_gb300 import scenes  # noqa: E402
+from povray_gb300.encode import read_ppm  # noqa: E402
 
 POV_ORACLE = os.path.join(ROOT, "oracle", "_ref", "pov_oracle")
+POVRAY_REF = os.path.join(ROOT, "oracle", "_ref", "povray_ref")
 
 
 def cases():
+    """name -> (scene, probe stride, random-origin half-extent)."""
     return {
-        "spheres_plane_320x240": (scenes.spheres_plane(320, 240), 4),
-        "mesh_spheres_small_160x90": (scenes.mesh_spheres(160, 90, mesh_n=24, n_spheres=64), 2),
+        "spheres_plane_320x240": (scenes.spheres_plane(320, 240), 4, 12.0),
+        "mesh_spheres_small_160x90": (scenes.mesh_spheres(160, 90, mesh_n=24, n_spheres=64), 2, 12.0),
+        "csg_torus_grid_160x90": (scenes.csg_torus_grid(160, 90, n=16), 2, 16.0),
     }
 
 
-def probe_rays(scene, stride, n_random=2000, seed=11):
+def probe_rays(scene, stride, extent=12.0, n_random=2000, seed=11):
     hh, ww = np.mgrid[0:scene.height:stride, 0:scene.width:stride]
     o, d = scene.camera_rays(ww.ravel(), hh.ravel())
     rng = np.random.Generator(np.random.PCG64(seed))
-    ro = rng.uniform(-12.0, 12.0, size=(n_random, 3))
+    ro = rng.uniform(-extent, extent, size=(n_random, 3))
     rd = rng.normal(size=(n_random, 3))
     rd /= np.linalg.norm(rd, axis=1)[:, None]
     return np.concatenate([o, ro]), np.concatenate([d, rd])
 
 
-def run(case, scene, stride, tmp):
+def cli_stats(text):
+    """Counters of the reference's statistics printout (renderfrontend.cpp:1834-1933)."""
+    out = {}
+    pats = {"number_of_pixels": r"Pixels:\s+(\d+)", "number_of_samples": r"Samples:\s+(\d+)",
+            "number_of_rays": r"Rays:\s+(\d+)", "shadow_ray_tests": r"Shadow Ray Tests:\s+(\d+)",
+            "shadow_rays_succeeded": r"Succeeded:\s+(\d+)\s*\n", "reflected_rays": r"Reflected Rays:\s+(\d+)"}
+    for k, p in pats.items():
+        m = re.search(p, text)
+        out[k] = int(m.group(1)) if m else 0
+    return out
+
+
+def run(case, scene, stride, extent, tmp):
     pov = os.path.join(tmp, case + ".pov")
     with open(pov, "w") as f:
         f.write(scene.sdl())
@@ -57,7 +82,7 @@ def run(case, scene, stride, tmp):
     out = subprocess.run([POV_ORACLE, pov, w, h, "pixels", rgbt], check=True, capture_output=True, text=True)
     stats = json.loads(out.stdout.strip().splitlines()[-1])
     pixels = np.fromfile(rgbt, dtype=np.float32).reshape(scene.height, scene.width, 4)
-    o, d = probe_rays(scene, stride)
+    o, d = probe_rays(scene, stride, extent)
     rays = os.path.join(tmp, case + ".rays")
     with open(rays, "wb") as f:
         f.write(struct.pack("<i", o.shape[0]))
@@ -75,18 +100,28 @@ def run(case, scene, stride, tmp):
             if k in ("location", "direction", "right", "up"):
                 cam[k] = [float(x) for x in v]
     camera = np.array([cam["location"], cam["direction"], cam["right"], cam["up"]], dtype=np.float64)
+    extra = {}
+    if scene.antialias is not None:
+        thr, depth = scene.antialias
+        ppm = os.path.join(tmp, case + "_aa.ppm")
+        r = subprocess.run([POVRAY_REF, "+I" + pov, "+W" + w, "+H" + h, "-D", "+FP", "+A%g" % thr, "+AM2",
+                            "+R%d" % depth, "-J", "+WT4", "+O" + ppm], capture_output=True, text=True, cwd=tmp)
+        if r.returncode != 0:
+            raise RuntimeError(r.stderr[-2000:])
+        extra["aa_u8"] = read_ppm(ppm)
+        extra["aa_stats"] = json.dumps(cli_stats(r.stdout + r.stderr))
     np.savez_compressed(os.path.join(HERE, case + ".npz"), pixels=pixels, stats=json.dumps(stats),
                         ray_org=o, ray_dir=d, hit_object=hr["object"], hit_triangle=hr["triangle"],
-                        hit_t=hr["t"], camera=camera)
-    print(case, stats, "hits", int((hr["object"] >= 0).sum()), "/", len(hr))
+                        hit_t=hr["t"], camera=camera, **extra)
+    print(case, stats, extra.get("aa_stats", ""), "hits", int((hr["object"] >= 0).sum()), "/", len(hr))
 
 
 def main():
     if not os.path.exists(POV_ORACLE):
         sys.exit("build the reference first: make -C oracle/refbuild")
     with tempfile.TemporaryDirectory() as tmp:
-        for case, (scene, stride) in cases().items():
-            run(case, scene, stride, tmp)
+        for case, (scene, stride, extent) in cases().items():
+            run(case, scene, stride, extent, tmp)
 
 
 if __name__ == "__main__":

@@ -11,6 +11,7 @@ from oracle.pyoracle import Oracle
 from povray_gb300 import scenes
 from tests.golden.make_golden import cases
 from tests.parity import compare_hits, compare_pixels
+from povray_gb300.encode import to_u8
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 CASES = cases()
@@ -22,7 +23,7 @@ def _load(case):
 
 @pytest.mark.parametrize("case", sorted(CASES))
 def test_camera_vectors_match_the_parser(case):
-    scene, _ = CASES[case]
+    scene = CASES[case][0]
     g = _load(case)
     d, r, u = scene.camera()
     assert np.array_equal(g["camera"][0], np.array(scene.location))
@@ -33,7 +34,7 @@ def test_camera_vectors_match_the_parser(case):
 
 @pytest.mark.parametrize("case", sorted(CASES))
 def test_oracle_hits_match_reference(case):
-    scene, _ = CASES[case]
+    scene = CASES[case][0]
     g = _load(case)
     o = Oracle(scene)
     h = o.trace_rays(g["ray_org"], g["ray_dir"])
@@ -43,16 +44,39 @@ def test_oracle_hits_match_reference(case):
     assert r["t_max_rel"] <= 1e-12, r
 
 
+def no_aa(scene):
+    p = scene.render_params()
+    p.antialias = 0
+    p.sampling_method = 1
+    return p
+
+
 @pytest.mark.parametrize("case", sorted(CASES))
 def test_oracle_pixels_and_counters_match_reference(case):
-    scene, _ = CASES[case]
+    scene = CASES[case][0]
     g = _load(case)
-    img, st = Oracle(scene).render(threads=4)
+    img, st = Oracle(scene).render(threads=4, params=no_aa(scene))
     ref = g["pixels"]
     assert np.abs(img - ref).max() <= 1e-5
     assert compare_pixels(img, ref)["max_lsb"] <= 1
     rs = json.loads(str(g["stats"]))
     for k in ("number_of_rays", "shadow_ray_tests", "shadow_rays_succeeded", "reflected_rays"):
+        assert st[k] == rs[k], (k, st[k], rs[k])
+
+
+@pytest.mark.parametrize("case", sorted(c for c in CASES if CASES[c][0].antialias is not None))
+def test_oracle_adaptive_aa_matches_reference_cli(case):
+    """AdaptiveSupersamplingM2 restated: the reference CLI's PPM within 1 LSB
+    and every counter of its statistics printout exact."""
+    scene = CASES[case][0]
+    g = _load(case)
+    img, st = Oracle(scene).render(threads=4)
+    got = to_u8(img, "bt709").astype(int)
+    d = np.abs(got - g["aa_u8"].astype(int))
+    assert d.max() <= 1 and (d == 0).mean() > 0.999
+    rs = json.loads(str(g["aa_stats"]))
+    for k in ("number_of_pixels", "number_of_samples", "number_of_rays", "shadow_ray_tests",
+              "shadow_rays_succeeded", "reflected_rays"):
         assert st[k] == rs[k], (k, st[k], rs[k])
 
 

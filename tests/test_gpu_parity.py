@@ -46,7 +46,7 @@ def _counters_close(got, ref, frac=5e-4):
 
 @pytest.mark.parametrize("case", sorted(CASES))
 def test_hits_match_reference_golden(case):
-    scene, _ = CASES[case]
+    scene = CASES[case][0]
     g = _load(case)
     gpu = GpuScene(scene)
     h = gpu.trace_rays(g["ray_org"], g["ray_dir"])
@@ -59,7 +59,7 @@ def test_hits_match_reference_golden(case):
 
 @pytest.mark.parametrize("case", sorted(CASES))
 def test_pixels_match_reference_golden(case):
-    scene, _ = CASES[case]
+    scene = CASES[case][0]
     g = _load(case)
     img, st = GpuScene(scene).render()
     c = compare_pixels(img, g["pixels"])
