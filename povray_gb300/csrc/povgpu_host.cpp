@@ -256,6 +256,22 @@ static V3d vsub(V3d a, V3d b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
 static V3d vcross(V3d a, V3d b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
 static double vlen(V3d a) { return std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
 
+// Object -> world point with a TRANSFORM's forward matrix (row-vector form).
+static V3d mtrans_point(const double* m, V3d v)
+{
+    return {v.x * m[0] + v.y * m[4] + v.z * m[8] + m[12], v.x * m[1] + v.y * m[5] + v.z * m[9] + m[13],
+            v.x * m[2] + v.y * m[6] + v.z * m[10] + m[14]};
+}
+
+static void grow_outward(AABB& b, double x, double y, double z)
+{
+    const float p[3] = {(float)x, (float)y, (float)z};
+    for (int k = 0; k < 3; k++) {
+        b.lo[k] = std::min(b.lo[k], std::nextafter(p[k], -INFINITY));
+        b.hi[k] = std::max(b.hi[k], std::nextafter(p[k], INFINITY));
+    }
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------- scene --
@@ -268,10 +284,17 @@ struct PovGpuScene {
     int         num_sms = 148;
     // persistent scene data
     DevBuf nodes, refs, tri_v0, tri_e1, tri_e2, tri_global, tri_shade, tri_normal, tri_local, normals;
-    DevBuf spheres, sphere_obj, planes, plane_obj, objects, materials, lights;
+    DevBuf spheres, sphere_obj, sphere_flags, planes, plane_obj, boxes, tori, csgs, csg_children, objects,
+        materials, lights;
+    // host copies of the id maps (prim -> flattened object id)
+    std::vector<int32_t> h_sphere_obj, h_plane_obj, h_box_obj, h_torus_obj, h_tri_global, h_tri_local, h_tri_obj;
+    std::vector<DevCsg> h_csgs;
+    std::vector<DevCsgChild> h_csg_children;
     // per-batch work buffers (grown on demand, reused)
-    DevBuf blocks, block_off, qA, qB, pathA, pathB, hits, paths, slot_contrib, sq, sq_slot, blocked, out,
+    DevBuf blocks, block_off, corner_off, qA, qB, pathA, pathB, hits, paths, slot_contrib, sq, sq_slot, blocked, out,
         counters, stats, err, rays_in, skipA, skipB, sskip, t64;
+    // adaptive antialiasing buffers
+    DevBuf corners, aa_grid, aa_mask, aa_subdiv, aa_xy, cellsA, cellsB, spos, sslot;
     int     num_lights = 0;
     int     max_trace_level = 1;
     // streams and profiling
@@ -288,13 +311,12 @@ struct PovGpuScene {
         for (cudaEvent_t e : events)
             cudaEventDestroy(e);
         events.clear();
-        wcount.release();
-        DevBuf* all[] = {&nodes,  &refs,       &tri_v0,   &tri_e1,    &tri_e2,     &tri_global, &tri_shade,
-                         &tri_normal, &tri_local, &normals,  &spheres,   &sphere_obj, &planes,     &plane_obj,
-                         &objects, &materials,  &lights,   &blocks,    &block_off,  &qA,         &qB,
-                         &pathA,   &pathB,      &hits,     &paths,     &slot_contrib, &sq,       &sq_slot,
-                         &blocked, &out,        &counters, &stats,     &err,        &rays_in,
-                         &skipA,   &skipB,      &sskip,    &t64};
+        DevBuf* all[] = {&nodes, &refs, &tri_v0, &tri_e1, &tri_e2, &tri_global, &tri_shade, &tri_normal, &tri_local,
+                         &normals, &spheres, &sphere_obj, &sphere_flags, &planes, &plane_obj, &boxes, &tori, &csgs,
+                         &csg_children, &objects, &materials, &lights, &blocks, &block_off, &corner_off, &qA, &qB,
+                         &pathA, &pathB, &hits, &paths, &slot_contrib, &sq, &sq_slot, &blocked, &out, &counters,
+                         &stats, &err, &rays_in, &skipA, &skipB, &sskip, &t64, &corners, &aa_grid, &aa_mask,
+                         &aa_subdiv, &aa_xy, &cellsA, &cellsB, &spos, &sslot, &wcount};
         for (DevBuf* b : all)
             b->release();
         if (stream)
@@ -305,22 +327,25 @@ struct PovGpuScene {
 
 namespace {
 
-#define CK(x)                                   \
-    do {                                        \
-        cudaError_t e_ = (x);                   \
-        if (e_ != cudaSuccess)                  \
+#define CK(x)                                                                          \
+    do {                                                                               \
+        cudaError_t e_ = (x);                                                          \
+        if (e_ != cudaSuccess)                                                         \
             return e_ == cudaErrorMemoryAllocation ? POV_GPU_E_NOMEM : POV_GPU_E_CUDA; \
     } while (0)
+
+constexpr int MAX_AA_DEPTH = 4;   // (2^4+1)^2 = 289 grid points, 21 subdividable cells per pixel
+
+bool is_csg(int t) { return t == POV_OBJ_UNION || t == POV_OBJ_INTERSECTION || t == POV_OBJ_MERGE; }
 
 int validate(const PovGpuSceneDesc* d, int32_t* bad)
 {
     if (!d || d->abi_version != POV_GPU_ABI_VERSION || d->num_objects < 0 || d->num_materials < 1 ||
-        d->num_lights < 0 || d->num_meshes < 0 || (d->num_objects > 0 && !d->objects) || !d->materials)
+        d->num_lights < 0 || d->num_meshes < 0 || (d->num_objects > 0 && !d->objects) || !d->materials ||
+        (d->num_lights > 0 && !d->lights) || (d->num_meshes > 0 && !d->meshes))
         return POV_GPU_E_INVALID;
-    if (d->camera.type != 0) {
-        if (bad) *bad = -1;
+    if (d->camera.type != 0)
         return POV_GPU_E_UNSUPPORTED;
-    }
     if (d->radiosity.enabled)
         return POV_GPU_E_UNSUPPORTED;
     for (int i = 0; i < d->num_lights; i++)
@@ -334,20 +359,40 @@ int validate(const PovGpuSceneDesc* d, int32_t* bad)
             m.crand != 0.0f || m.diffuse_back != 0.0f || m.conserve_energy)
             return POV_GPU_E_UNSUPPORTED;
     }
-    for (int i = 0; i < d->num_objects; i++) {
+    const int n = d->num_objects;
+    for (int i = 0; i < n; i++) {
         const PovGpuObject& o = d->objects[i];
-        bool ok = (o.type == POV_OBJ_SPHERE || o.type == POV_OBJ_PLANE || o.type == POV_OBJ_MESH) &&
-                  !(o.flags & POV_FLAG_HAS_TRANS) && o.parent < 0;
-        if (o.material < 0 || o.material >= d->num_materials)
-            ok = false;
+        if (bad) *bad = i;
+        if (o.type < POV_OBJ_SPHERE || o.type > POV_OBJ_MERGE || o.parent >= n || o.parent >= i)
+            return POV_GPU_E_INVALID;
+        if (o.material >= d->num_materials || (o.material < 0 && o.parent < 0))
+            return POV_GPU_E_INVALID;
         if (o.type == POV_OBJ_MESH && (o.mesh < 0 || o.mesh >= d->num_meshes))
-            ok = false;
-        if (!ok) {
-            if (bad) *bad = i;
-            return o.type >= POV_OBJ_SPHERE && o.type <= POV_OBJ_MERGE && o.material >= 0 ? POV_GPU_E_UNSUPPORTED
-                                                                                          : POV_GPU_E_INVALID;
+            return POV_GPU_E_INVALID;
+        // transforms: the torus always has one; sphere (ellipsoid), box, mesh
+        // and plane transforms are not on the GPU path
+        if (o.type == POV_OBJ_TORUS ? !(o.flags & POV_FLAG_HAS_TRANS) : (o.flags & POV_FLAG_HAS_TRANS) != 0)
+            return POV_GPU_E_UNSUPPORTED;
+        if (is_csg(o.type)) {
+            if (o.parent >= 0)
+                return POV_GPU_E_UNSUPPORTED;   // nested CSG
+            if (o.num_children < 1 || o.first_child != i + 1 || o.first_child + o.num_children > n)
+                return POV_GPU_E_INVALID;
+            for (int c = 0; c < o.num_children; c++) {
+                const PovGpuObject& ch = d->objects[o.first_child + c];
+                if (ch.parent != i)
+                    return POV_GPU_E_INVALID;
+                // leaf children: spheres, boxes and tori (no planes, meshes or nested CSG)
+                if (ch.type != POV_OBJ_SPHERE && ch.type != POV_OBJ_BOX && ch.type != POV_OBJ_TORUS) {
+                    if (bad) *bad = o.first_child + c;
+                    return POV_GPU_E_UNSUPPORTED;
+                }
+            }
+        } else if (o.parent >= 0 && !is_csg(d->objects[o.parent].type)) {
+            return POV_GPU_E_INVALID;
         }
     }
+    if (bad) *bad = -1;
     for (int i = 0; i < d->num_meshes; i++) {
         const PovGpuMesh& m = d->meshes[i];
         if (m.num_triangles < 0 || m.num_vertices < 0 || (m.num_triangles > 0 && (!m.face_indices || !m.vertices)))
@@ -387,12 +432,155 @@ DevMaterial make_material(const PovGpuMaterial& m, const float* ambient_light)
     return d;
 }
 
-int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
-{
+// Scene arrays under construction (host side).
+struct Builder {
     BvhBuilder bvh;
     std::vector<float4> spheres, planes, tri_v0, tri_e1, tri_e2, tri_normal, normals;
-    std::vector<int32_t> sphere_obj, plane_obj, tri_global, tri_local;
+    std::vector<int32_t> sphere_obj, sphere_flags, plane_obj, tri_global, tri_local, box_obj, torus_obj;
     std::vector<int4> tri_shade;
+    std::vector<DevBox> boxes;
+    std::vector<DevTorus> tori;
+    std::vector<DevCsg> csgs;
+    std::vector<DevCsgChild> csg_children;
+
+    int add_sphere(const PovGpuObject& o, int id, AABB* box)
+    {
+        int idx = (int)spheres.size();
+        spheres.push_back(make_float4((float)o.p[0], (float)o.p[1], (float)o.p[2], (float)o.p[3]));
+        sphere_obj.push_back(id);
+        sphere_flags.push_back(o.flags & POV_FLAG_INVERTED ? 1 : 0);
+        if (box)
+            for (int k = 0; k < 3; k++) {
+                box->lo[k] = std::min(box->lo[k], std::nextafter((float)(o.p[k] - o.p[3]), -INFINITY));
+                box->hi[k] = std::max(box->hi[k], std::nextafter((float)(o.p[k] + o.p[3]), INFINITY));
+            }
+        return idx;
+    }
+    int add_box(const PovGpuObject& o, int id, AABB* box)
+    {
+        int idx = (int)boxes.size();
+        DevBox b;
+        b.lo = make_float4((float)o.p[0], (float)o.p[1], (float)o.p[2], __builtin_bit_cast(float, id));
+        b.hi = make_float4((float)o.p[3], (float)o.p[4], (float)o.p[5],
+                           __builtin_bit_cast(float, (int32_t)(o.flags & POV_FLAG_INVERTED ? 1 : 0)));
+        boxes.push_back(b);
+        box_obj.push_back(id);
+        if (box) {
+            grow_outward(*box, o.p[0], o.p[1], o.p[2]);
+            grow_outward(*box, o.p[3], o.p[4], o.p[5]);
+        }
+        return idx;
+    }
+    int add_torus(const PovGpuObject& o, int id, AABB* box)
+    {
+        int idx = (int)tori.size();
+        DevTorus t{};
+        for (int r = 0; r < 4; r++)
+            for (int c = 0; c < 3; c++)
+                t.inv[r * 3 + c] = o.trans[16 + r * 4 + c];
+        t.R = o.p[0];
+        t.r = o.p[1];
+        t.object = id;
+        t.flags = o.flags & POV_FLAG_INVERTED ? 1 : 0;
+        tori.push_back(t);
+        torus_obj.push_back(id);
+        if (box) {
+            // Torus::Compute_BBox + Recompute_BBox: the local box's corners, transformed
+            double r1 = o.p[1], r2 = o.p[0] + o.p[1];
+            for (int i = 0; i < 8; i++) {
+                V3d c = {(i & 1) ? r2 : -r2, (i & 2) ? r1 : -r1, (i & 4) ? r2 : -r2};
+                V3d w = mtrans_point(o.trans, c);
+                double pad = 1e-6 * (std::fabs(w.x) + std::fabs(w.y) + std::fabs(w.z) + 1.0);
+                grow_outward(*box, w.x - pad, w.y - pad, w.z - pad);
+                grow_outward(*box, w.x + pad, w.y + pad, w.z + pad);
+            }
+        }
+        return idx;
+    }
+    void push_prim(uint32_t kind, uint32_t idx, const AABB& box)
+    {
+        BuildItem it;
+        it.box = box;
+        for (int k = 0; k < 3; k++)
+            it.c[k] = 0.5f * (box.lo[k] + box.hi[k]);
+        it.ref = (kind << PRIM_KIND_SHIFT) | idx;
+        bvh.items.push_back(it);
+    }
+};
+
+void add_mesh(Builder& B, const PovGpuSceneDesc* d, const PovGpuObject& o, int id, int nb)
+{
+    const PovGpuMesh& m = d->meshes[o.mesh];
+    for (int t = 0; t < m.num_triangles; t++) {
+        const int32_t* f = m.face_indices + 3 * t;
+        int p1 = f[0], p2 = f[1], p3 = f[2];
+        int n1 = 0, n2 = 0, n3 = 0;
+        bool smooth = false;
+        // without normal_indices the parser reuses the face indices when
+        // there is one normal per vertex (parser.cpp:4488-4502)
+        const int32_t* ni = m.normal_indices ? m.normal_indices
+                            : (m.num_normals == m.num_vertices ? m.face_indices : nullptr);
+        if (ni && m.num_normals > 0 && m.normals) {
+            n1 = ni[3 * t];
+            n2 = ni[3 * t + 1];
+            n3 = ni[3 * t + 2];
+            const float4 a = B.normals[nb + n1], b = B.normals[nb + n2], c = B.normals[nb + n3];
+            double d1x = (double)a.x - b.x, d1y = (double)a.y - b.y, d1z = (double)a.z - b.z;
+            double d2x = (double)a.x - c.x, d2y = (double)a.y - c.y, d2z = (double)a.z - c.z;
+            double l1 = d1x * d1x + d1y * d1y + d1z * d1z, l2 = d2x * d2x + d2y * d2y + d2z * d2z;
+            smooth = (std::fabs(l1) > EPSILON) || (std::fabs(l2) > EPSILON);   // parser.cpp:4545
+        }
+        auto V = [&](int k) {
+            return V3d{(double)m.vertices[3 * k], (double)m.vertices[3 * k + 1], (double)m.vertices[3 * k + 2]};
+        };
+        V3d P1 = V(p1), P2 = V(p2), P3 = V(p3);
+        // Compute_Mesh_Triangle (source/core/shape/mesh.cpp:838-982)
+        V3d N = vcross(vsub(P3, P1), vsub(P2, P1));
+        double len = vlen(N);
+        float4 gn = make_float4(0.f, 0.f, 0.f, __builtin_bit_cast(float, id));
+        float plane_dist = 0.f;
+        if (len != 0.0) {
+            N = {N.x / len, N.y / len, N.z / len};
+            plane_dist = (float)(-(N.x * P1.x + N.y * P1.y + N.z * P1.z));   // Triangle->Distance
+            gn.x = (float)N.x;
+            gn.y = (float)N.y;
+            gn.z = (float)N.z;
+            int axis = max3_coordinate(std::fabs(N.x), std::fabs(N.y), std::fabs(N.z));
+            bool swap;
+            if (axis == 0)
+                swap = (P2.y - P3.y) * (P2.z - P1.z) < (P2.z - P3.z) * (P2.y - P1.y);
+            else if (axis == 1)
+                swap = (P2.x - P3.x) * (P2.z - P1.z) < (P2.z - P3.z) * (P2.x - P1.x);
+            else
+                swap = (P2.x - P3.x) * (P2.y - P1.y) < (P2.y - P3.y) * (P2.x - P1.x);
+            if (swap) {
+                std::swap(p1, p2);
+                std::swap(P1, P2);
+                if (smooth)
+                    std::swap(n1, n2);
+            }
+        }
+        int g = (int)B.tri_v0.size();
+        float v0[3] = {(float)P1.x, (float)P1.y, (float)P1.z};
+        float v1[3] = {(float)P2.x, (float)P2.y, (float)P2.z};
+        float v2[3] = {(float)P3.x, (float)P3.y, (float)P3.z};
+        B.tri_v0.push_back(make_float4(v0[0], v0[1], v0[2], plane_dist));
+        B.tri_e1.push_back(make_float4(v1[0] - v0[0], v1[1] - v0[1], v1[2] - v0[2], 0.f));
+        B.tri_e2.push_back(make_float4(v2[0] - v0[0], v2[1] - v0[1], v2[2] - v0[2], 0.f));
+        B.tri_normal.push_back(gn);
+        B.tri_shade.push_back(make_int4(nb + n1, nb + n2, nb + n3, smooth ? 1 : 0));
+        B.tri_local.push_back(t);
+        AABB box;
+        box.grow(v0);
+        box.grow(v1);
+        box.grow(v2);
+        B.push_prim(PK_TRIANGLE, (uint32_t)g, box);
+    }
+}
+
+int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
+{
+    Builder B;
     std::vector<ObjectShade> objects((size_t)std::max(d->num_objects, 1));
     std::vector<int> mesh_normal_base((size_t)std::max(d->num_meshes, 1), 0);
 
@@ -400,134 +588,117 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
     // (source/parser/parser.cpp:4143-4152)
     for (int mi = 0; mi < d->num_meshes; mi++) {
         const PovGpuMesh& m = d->meshes[mi];
-        mesh_normal_base[mi] = (int)normals.size();
+        mesh_normal_base[mi] = (int)B.normals.size();
         for (int i = 0; i < m.num_normals && m.normals; i++) {
             double x = m.normals[3 * i], y = m.normals[3 * i + 1], z = m.normals[3 * i + 2];
             if (std::fabs(x) < EPSILON && std::fabs(y) < EPSILON && std::fabs(z) < EPSILON)
                 x = 1.0;
             double l = std::sqrt(x * x + y * y + z * z);
-            normals.push_back(make_float4((float)(x / l), (float)(y / l), (float)(z / l), 0.f));
+            B.normals.push_back(make_float4((float)(x / l), (float)(y / l), (float)(z / l), 0.f));
         }
     }
 
     for (int i = 0; i < d->num_objects; i++) {
         const PovGpuObject& o = d->objects[i];
-        objects[i].material = o.material;
+        // texture: own, else inherited from the enclosing CSG (Post_Process)
+        int mat = o.material;
+        for (int p = o.parent; mat < 0 && p >= 0; p = d->objects[p].parent)
+            mat = d->objects[p].material;
+        objects[i].material = mat < 0 ? 0 : mat;
         objects[i].flags = (o.flags & POV_FLAG_INVERTED ? 1 : 0) | (o.flags & POV_FLAG_DOUBLE_ILLUM ? 16 : 0);
         objects[i].type = o.type;
         objects[i].mesh = o.mesh;
-        if (o.type == POV_OBJ_SPHERE) {
-            uint32_t idx = (uint32_t)spheres.size();
-            spheres.push_back(make_float4((float)o.p[0], (float)o.p[1], (float)o.p[2], (float)o.p[3]));
-            sphere_obj.push_back(i);
-            BuildItem it;
-            for (int k = 0; k < 3; k++) {
-                // bounds rounded outward so the FP32 box always contains the sphere
-                it.box.lo[k] = std::nextafter((float)(o.p[k] - o.p[3]), -INFINITY);
-                it.box.hi[k] = std::nextafter((float)(o.p[k] + o.p[3]), INFINITY);
-                it.c[k] = (float)o.p[k];
+    }
+    for (int i = 0; i < d->num_objects; i++) {
+        const PovGpuObject& o = d->objects[i];
+        if (o.parent >= 0)
+            continue;   // CSG children are added with their parent
+        AABB box;
+        switch (o.type) {
+        case POV_OBJ_SPHERE: B.push_prim(PK_SPHERE, B.add_sphere(o, i, &box), box); break;
+        case POV_OBJ_BOX: B.push_prim(PK_BOX, B.add_box(o, i, &box), box); break;
+        case POV_OBJ_TORUS: B.push_prim(PK_TORUS, B.add_torus(o, i, &box), box); break;
+        case POV_OBJ_PLANE:
+            B.planes.push_back(make_float4((float)o.p[0], (float)o.p[1], (float)o.p[2], (float)o.p[3]));
+            B.plane_obj.push_back(i);
+            break;
+        case POV_OBJ_MESH: add_mesh(B, d, o, i, mesh_normal_base[o.mesh]); break;
+        case POV_OBJ_UNION:
+            // CSGUnion::All_Intersections pushes every child hit: the closest
+            // hit is the same as with the children as separate objects
+            for (int c = 0; c < o.num_children; c++) {
+                int ci = o.first_child + c;
+                const PovGpuObject& ch = d->objects[ci];
+                AABB cb;
+                if (ch.type == POV_OBJ_SPHERE) B.push_prim(PK_SPHERE, B.add_sphere(ch, ci, &cb), cb);
+                else if (ch.type == POV_OBJ_BOX) B.push_prim(PK_BOX, B.add_box(ch, ci, &cb), cb);
+                else B.push_prim(PK_TORUS, B.add_torus(ch, ci, &cb), cb);
             }
-            it.ref = (PK_SPHERE << PRIM_KIND_SHIFT) | idx;
-            bvh.items.push_back(it);
-        } else if (o.type == POV_OBJ_PLANE) {
-            planes.push_back(make_float4((float)o.p[0], (float)o.p[1], (float)o.p[2], (float)o.p[3]));
-            plane_obj.push_back(i);
-        } else if (o.type == POV_OBJ_MESH) {
-            const PovGpuMesh& m = d->meshes[o.mesh];
-            int nb = mesh_normal_base[o.mesh];
-            for (int t = 0; t < m.num_triangles; t++) {
-                const int32_t* f = m.face_indices + 3 * t;
-                int p1 = f[0], p2 = f[1], p3 = f[2];
-                int n1 = 0, n2 = 0, n3 = 0;
-                bool smooth = false;
-                // without normal_indices the parser reuses the face indices when
-                // there is one normal per vertex (parser.cpp:4488-4502)
-                const int32_t* ni = m.normal_indices ? m.normal_indices
-                                    : (m.num_normals == m.num_vertices ? m.face_indices : nullptr);
-                if (ni && m.num_normals > 0 && m.normals) {
-                    n1 = ni[3 * t];
-                    n2 = ni[3 * t + 1];
-                    n3 = ni[3 * t + 2];
-                    const float4 a = normals[nb + n1], b = normals[nb + n2], c = normals[nb + n3];
-                    double d1x = (double)a.x - b.x, d1y = (double)a.y - b.y, d1z = (double)a.z - b.z;
-                    double d2x = (double)a.x - c.x, d2y = (double)a.y - c.y, d2z = (double)a.z - c.z;
-                    double l1 = d1x * d1x + d1y * d1y + d1z * d1z, l2 = d2x * d2x + d2y * d2y + d2z * d2z;
-                    smooth = (std::fabs(l1) > EPSILON) || (std::fabs(l2) > EPSILON);   // parser.cpp:4545
-                }
-                auto V = [&](int k) {
-                    return V3d{(double)m.vertices[3 * k], (double)m.vertices[3 * k + 1], (double)m.vertices[3 * k + 2]};
-                };
-                V3d P1 = V(p1), P2 = V(p2), P3 = V(p3);
-                // Compute_Mesh_Triangle (source/core/shape/mesh.cpp:838-982)
-                V3d N = vcross(vsub(P3, P1), vsub(P2, P1));
-                double len = vlen(N);
-                float4 gn = make_float4(0.f, 0.f, 0.f, __builtin_bit_cast(float, i));
-                float plane_dist = 0.f;
-                if (len != 0.0) {
-                    N = {N.x / len, N.y / len, N.z / len};
-                    plane_dist = (float)(-(N.x * P1.x + N.y * P1.y + N.z * P1.z));   // Triangle->Distance
-                    gn.x = (float)N.x;
-                    gn.y = (float)N.y;
-                    gn.z = (float)N.z;
-                    int axis = max3_coordinate(std::fabs(N.x), std::fabs(N.y), std::fabs(N.z));
-                    bool swap;
-                    if (axis == 0)
-                        swap = (P2.y - P3.y) * (P2.z - P1.z) < (P2.z - P3.z) * (P2.y - P1.y);
-                    else if (axis == 1)
-                        swap = (P2.x - P3.x) * (P2.z - P1.z) < (P2.z - P3.z) * (P2.x - P1.x);
-                    else
-                        swap = (P2.x - P3.x) * (P2.y - P1.y) < (P2.y - P3.y) * (P2.x - P1.x);
-                    if (swap) {
-                        std::swap(p1, p2);
-                        std::swap(P1, P2);
-                        if (smooth)
-                            std::swap(n1, n2);
+            break;
+        default: {   // CSG intersection (difference) / merge as one primitive
+            DevCsg g;
+            g.type = o.type;
+            g.first = (int)B.csg_children.size();
+            g.count = o.num_children;
+            g.object = i;
+            AABB uni, inter;
+            for (int k = 0; k < 3; k++) {
+                inter.lo[k] = -INFINITY;
+                inter.hi[k] = INFINITY;
+            }
+            bool any_plain = false;
+            for (int c = 0; c < o.num_children; c++) {
+                int ci = o.first_child + c;
+                const PovGpuObject& ch = d->objects[ci];
+                AABB cb;
+                DevCsgChild cc;
+                cc.flags = ch.flags & POV_FLAG_INVERTED ? 1 : 0;
+                cc.object = ci;
+                if (ch.type == POV_OBJ_SPHERE) { cc.kind = PK_SPHERE; cc.index = B.add_sphere(ch, ci, &cb); }
+                else if (ch.type == POV_OBJ_BOX) { cc.kind = PK_BOX; cc.index = B.add_box(ch, ci, &cb); }
+                else { cc.kind = PK_TORUS; cc.index = B.add_torus(ch, ci, &cb); }
+                B.csg_children.push_back(cc);
+                uni.grow(cb);
+                if (!cc.flags) {   // CSG::Compute_BBox: overlap of the non-inverted children
+                    any_plain = true;
+                    for (int k = 0; k < 3; k++) {
+                        inter.lo[k] = std::max(inter.lo[k], cb.lo[k]);
+                        inter.hi[k] = std::min(inter.hi[k], cb.hi[k]);
                     }
                 }
-                int g = (int)tri_v0.size();
-                float v0[3] = {(float)P1.x, (float)P1.y, (float)P1.z};
-                float v1[3] = {(float)P2.x, (float)P2.y, (float)P2.z};
-                float v2[3] = {(float)P3.x, (float)P3.y, (float)P3.z};
-                tri_v0.push_back(make_float4(v0[0], v0[1], v0[2], plane_dist));
-                tri_e1.push_back(make_float4(v1[0] - v0[0], v1[1] - v0[1], v1[2] - v0[2], 0.f));
-                tri_e2.push_back(make_float4(v2[0] - v0[0], v2[1] - v0[1], v2[2] - v0[2], 0.f));
-                tri_normal.push_back(gn);
-                tri_shade.push_back(make_int4(nb + n1, nb + n2, nb + n3, smooth ? 1 : 0));
-                tri_local.push_back(t);
-                BuildItem it;
-                it.box = AABB();
-                it.box.grow(v0);
-                it.box.grow(v1);
-                it.box.grow(v2);
-                for (int k = 0; k < 3; k++)
-                    it.c[k] = 0.5f * (it.box.lo[k] + it.box.hi[k]);
-                it.ref = (PK_TRIANGLE << PRIM_KIND_SHIFT) | (uint32_t)g;
-                bvh.items.push_back(it);
             }
+            AABB gb = (o.type == POV_OBJ_INTERSECTION && any_plain) ? inter : uni;
+            if (gb.lo[0] > gb.hi[0] || gb.lo[1] > gb.hi[1] || gb.lo[2] > gb.hi[2])
+                gb = uni;   // empty overlap: keep a valid (never hit) box
+            int idx = (int)B.csgs.size();
+            B.csgs.push_back(g);
+            B.push_prim(PK_CSG, (uint32_t)idx, gb);
+            break;
+        }
         }
     }
-    if (tri_v0.size() >= (size_t)PRIM_INDEX_MASK || spheres.size() >= (size_t)PRIM_INDEX_MASK ||
-        bvh.items.size() >= (1u << 28))
+    if (B.tri_v0.size() >= (size_t)PRIM_INDEX_MASK || B.bvh.items.size() >= (1u << 28))
         return POV_GPU_E_UNSUPPORTED;
 
-    int root = bvh.build_root();
-    sc->stack_depth = std::max(8, bvh.max_depth + 2);
+    int root = B.bvh.build_root();
+    sc->stack_depth = std::max(8, B.bvh.max_depth + 2);
     if (sc->stack_depth > 96)
         return POV_GPU_E_UNSUPPORTED;
 
     // reorder triangle records into leaf order (prim refs then index the
     // leaf-order slot directly, so a leaf's triangles are contiguous)
     std::vector<float4> lv0, le1, le2;
-    lv0.reserve(tri_v0.size());
-    le1.reserve(tri_v0.size());
-    le2.reserve(tri_v0.size());
-    for (uint32_t& r : bvh.refs) {
+    std::vector<int32_t> tri_global;
+    lv0.reserve(B.tri_v0.size());
+    le1.reserve(B.tri_v0.size());
+    le2.reserve(B.tri_v0.size());
+    for (uint32_t& r : B.bvh.refs) {
         if ((r >> PRIM_KIND_SHIFT) == PK_TRIANGLE) {
             uint32_t g = r & PRIM_INDEX_MASK;
             uint32_t slot = (uint32_t)lv0.size();
-            lv0.push_back(tri_v0[g]);
-            le1.push_back(tri_e1[g]);
-            le2.push_back(tri_e2[g]);
+            lv0.push_back(B.tri_v0[g]);
+            le1.push_back(B.tri_e1[g]);
+            le2.push_back(B.tri_e2[g]);
             tri_global.push_back((int32_t)g);
             r = (PK_TRIANGLE << PRIM_KIND_SHIFT) | slot;
         }
@@ -543,23 +714,40 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
         lights[i].colour = make_float4(L.colour[0], L.colour[1], L.colour[2], 0.f);
     }
 
-    CK(upload(sc->nodes, bvh.nodes));
-    CK(upload(sc->refs, bvh.refs));
+    CK(upload(sc->nodes, B.bvh.nodes));
+    CK(upload(sc->refs, B.bvh.refs));
     CK(upload(sc->tri_v0, lv0));
     CK(upload(sc->tri_e1, le1));
     CK(upload(sc->tri_e2, le2));
     CK(upload(sc->tri_global, tri_global));
-    CK(upload(sc->tri_shade, tri_shade));
-    CK(upload(sc->tri_normal, tri_normal));
-    CK(upload(sc->tri_local, tri_local));
-    CK(upload(sc->normals, normals));
-    CK(upload(sc->spheres, spheres));
-    CK(upload(sc->sphere_obj, sphere_obj));
-    CK(upload(sc->planes, planes));
-    CK(upload(sc->plane_obj, plane_obj));
+    CK(upload(sc->tri_shade, B.tri_shade));
+    CK(upload(sc->tri_normal, B.tri_normal));
+    CK(upload(sc->tri_local, B.tri_local));
+    CK(upload(sc->normals, B.normals));
+    CK(upload(sc->spheres, B.spheres));
+    CK(upload(sc->sphere_obj, B.sphere_obj));
+    CK(upload(sc->sphere_flags, B.sphere_flags));
+    CK(upload(sc->planes, B.planes));
+    CK(upload(sc->plane_obj, B.plane_obj));
+    CK(upload(sc->boxes, B.boxes));
+    CK(upload(sc->tori, B.tori));
+    CK(upload(sc->csgs, B.csgs));
+    CK(upload(sc->csg_children, B.csg_children));
     CK(upload(sc->objects, objects));
     CK(upload(sc->materials, mats));
     CK(upload(sc->lights, lights));
+
+    sc->h_sphere_obj = B.sphere_obj;
+    sc->h_plane_obj = B.plane_obj;
+    sc->h_box_obj = B.box_obj;
+    sc->h_torus_obj = B.torus_obj;
+    sc->h_tri_global = tri_global;
+    sc->h_tri_local = B.tri_local;
+    sc->h_tri_obj.resize(B.tri_normal.size());
+    for (size_t k = 0; k < B.tri_normal.size(); k++)
+        sc->h_tri_obj[k] = __builtin_bit_cast(int32_t, B.tri_normal[k].w);
+    sc->h_csgs = B.csgs;
+    sc->h_csg_children = B.csg_children;
 
     DeviceScene& S = sc->S;
     S.nodes = sc->nodes.as<BvhNode>();
@@ -575,9 +763,15 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
     S.normals = sc->normals.as<float4>();
     S.spheres = sc->spheres.as<float4>();
     S.sphere_obj = sc->sphere_obj.as<int32_t>();
+    S.sphere_flags = sc->sphere_flags.as<int32_t>();
     S.planes = sc->planes.as<float4>();
     S.plane_obj = sc->plane_obj.as<int32_t>();
-    S.num_planes = (int)planes.size();
+    S.num_planes = (int)B.planes.size();
+    S.boxes = sc->boxes.as<DevBox>();
+    S.tori = sc->tori.as<DevTorus>();
+    S.csgs = sc->csgs.as<DevCsg>();
+    S.csg_children = sc->csg_children.as<DevCsgChild>();
+    S.has_full_prims = (!B.tori.empty() || !B.csgs.empty()) ? 1 : 0;
     S.objects = sc->objects.as<ObjectShade>();
     S.materials = sc->materials.as<DevMaterial>();
     S.lights = sc->lights.as<DevLight>();
@@ -603,6 +797,9 @@ enum {
     C_SQ = 2,     // shadow queue
     C_W0 = 3,     // work counter, closest-hit
     C_W1 = 4,     // work counter, any-hit
+    C_NS = 5,     // AA: samples of this round
+    C_NC = 6,     // AA: active cells
+    C_NN = 7,     // AA: next cells
     C_NUM = 8
 };
 
@@ -691,38 +888,89 @@ private:
     std::vector<Mark> marks_;
 };
 
+// Traces `n` image samples through every trace level and writes their RGBT
+// to out[slot[i]] (slot == nullptr: out[i]).  Samples come from the block
+// list (mode 0 centres, mode 1 corners) or from `pos` (mode 2, count in the
+// device word `npos`).  Counters accumulate into sc->stats.
+int run_samples(PovGpuScene* sc, StageClock& clk, int mode, int nblocks, const int* block_off, const double2* pos,
+                const int* npos, int n, int width, int height, const int* slot, float4* out)
+{
+    const int nl = std::max(sc->num_lights, 1);
+    const size_t maxq = (size_t)std::max(n, 1);
+    CK(sc->qA.ensure(sizeof(QRay) * maxq));
+    CK(sc->qB.ensure(sizeof(QRay) * maxq));
+    CK(sc->pathA.ensure(sizeof(int) * maxq));
+    CK(sc->pathB.ensure(sizeof(int) * maxq));
+    CK(sc->hits.ensure(sizeof(QHit) * maxq));
+    CK(sc->paths.ensure(sizeof(PathState) * maxq));
+    CK(sc->slot_contrib.ensure(sizeof(float4) * maxq * nl));
+    CK(sc->sq.ensure(sizeof(QRay) * maxq * nl));
+    CK(sc->sq_slot.ensure(sizeof(int) * maxq * nl));
+    CK(sc->blocked.ensure(maxq * nl));
+    CK(sc->skipA.ensure(sizeof(uint2) * maxq));
+    CK(sc->skipB.ensure(sizeof(uint2) * maxq));
+    CK(sc->sskip.ensure(sizeof(uint2) * maxq * nl));
+
+    cudaStream_t st = sc->active();
+    int* cnt = sc->counters.as<int>();
+    unsigned long long* dstats = sc->stats.as<unsigned long long>();
+    uint32_t* derr = sc->err.as<uint32_t>();
+    unsigned long long* wc = (sc->profiling & POV_GPU_PROFILE_WORK) ? sc->wcount.as<unsigned long long>() : nullptr;
+    const DeviceScene& S = sc->S;
+    const int grid_trace = sc->num_sms * 8;
+    const int grid_shade = std::max(1, std::min(sc->num_sms * 16, (int)((maxq + 127) / 128)));
+    QRay* qcur = sc->qA.as<QRay>();
+    QRay* qnext = sc->qB.as<QRay>();
+    int* pcur = sc->pathA.as<int>();
+    int* pnext = sc->pathB.as<int>();
+    int* ccur = cnt + C_QA;
+    int* cnext = cnt + C_QB;
+    uint2* kcur = sc->skipA.as<uint2>();
+    uint2* knext = sc->skipB.as<uint2>();
+    CK(clk.begin(POV_GPU_STAGE_CAMERA));
+    CK(launch_camera(S, mode, sc->blocks.as<int4>(), block_off, nblocks, pos, npos, n, width, height, qcur, pcur,
+                     sc->paths.as<PathState>(), ccur, dstats, kcur, st));
+    CK(clk.end());
+    for (int level = 0; level < sc->max_trace_level; level++) {
+        CK(cudaMemsetAsync(cnext, 0, sizeof(int), st));
+        CK(cudaMemsetAsync(cnt + C_SQ, 0, sizeof(int) * 3, st));   // SQ, W0, W1
+        CK(clk.begin(POV_GPU_STAGE_TRACE_CLOSEST));
+        CK(launch_trace(S, false, qcur, ccur, cnt + C_W0, sc->hits.as<QHit>(), nullptr, sc->stack_depth, grid_trace,
+                        derr, dstats, wc, (int)maxq, kcur, st));
+        CK(clk.end());
+        CK(clk.begin(POV_GPU_STAGE_SHADE));
+        CK(launch_shade(S, level, qcur, pcur, sc->hits.as<QHit>(), ccur, sc->paths.as<PathState>(),
+                        sc->slot_contrib.as<float4>(), sc->sq.as<QRay>(), sc->sq_slot.as<int>(), cnt + C_SQ,
+                        sc->sskip.as<uint2>(), qnext, pnext, knext, cnext, (int)maxq, (int)(maxq * nl), grid_shade,
+                        derr, dstats, st));
+        CK(clk.end());
+        if (sc->num_lights > 0) {
+            CK(clk.begin(POV_GPU_STAGE_TRACE_SHADOW));
+            CK(launch_trace(S, true, sc->sq.as<QRay>(), cnt + C_SQ, cnt + C_W1, nullptr, sc->blocked.as<uint8_t>(),
+                            sc->stack_depth, grid_trace, derr, dstats, wc ? wc + 4 : nullptr, (int)(maxq * nl),
+                            sc->sskip.as<uint2>(), st));
+            CK(clk.end());
+            CK(clk.begin(POV_GPU_STAGE_RESOLVE));
+            CK(launch_resolve(pcur, ccur, sc->num_lights, sc->sq_slot.as<int>(), sc->blocked.as<uint8_t>(),
+                              cnt + C_SQ, sc->slot_contrib.as<float4>(), sc->paths.as<PathState>(), grid_shade,
+                              (int)maxq, (int)(maxq * nl), st));
+            CK(clk.end(2));
+        }
+        std::swap(qcur, qnext);
+        std::swap(pcur, pnext);
+        std::swap(ccur, cnext);
+        std::swap(kcur, knext);
+    }
+    // finalize reads the sample count from the block offsets / position count
+    CK(clk.begin(POV_GPU_STAGE_FINALIZE));
+    CK(launch_finalize(sc->paths.as<PathState>(), mode == 2 ? npos : block_off + nblocks, (int)maxq, slot, out, st));
+    CK(clk.end());
+    return POV_GPU_OK;
+}
+
 }  // namespace
 
 extern "C" {
-
-int pov_gpu_scene_set_stream(PovGpuScene* sc, void* cuda_stream)
-{
-    if (!sc)
-        return POV_GPU_E_INVALID;
-    std::lock_guard<std::mutex> g(sc->lock);
-    sc->user_stream = reinterpret_cast<cudaStream_t>(cuda_stream);
-    return POV_GPU_OK;
-}
-
-int pov_gpu_set_profiling(PovGpuScene* sc, int flags)
-{
-    if (!sc || (flags & ~(POV_GPU_PROFILE_TIMES | POV_GPU_PROFILE_WORK)))
-        return POV_GPU_E_INVALID;
-    std::lock_guard<std::mutex> g(sc->lock);
-    sc->profiling = flags;
-    if ((flags & POV_GPU_PROFILE_WORK) && sc->wcount.ensure(sizeof(unsigned long long) * 8) != cudaSuccess)
-        return POV_GPU_E_NOMEM;
-    return POV_GPU_OK;
-}
-
-int pov_gpu_get_timings(PovGpuScene* sc, PovGpuTimings* out)
-{
-    if (!sc || !out)
-        return POV_GPU_E_INVALID;
-    std::lock_guard<std::mutex> g(sc->lock);
-    *out = sc->timings;
-    return POV_GPU_OK;
-}
 
 int pov_gpu_abi_version(void) { return POV_GPU_ABI_VERSION; }
 
@@ -788,12 +1036,43 @@ void pov_gpu_scene_destroy(PovGpuScene* scene)
     delete scene;
 }
 
+int pov_gpu_scene_set_stream(PovGpuScene* sc, void* cuda_stream)
+{
+    if (!sc)
+        return POV_GPU_E_INVALID;
+    std::lock_guard<std::mutex> g(sc->lock);
+    sc->user_stream = reinterpret_cast<cudaStream_t>(cuda_stream);
+    return POV_GPU_OK;
+}
+
+int pov_gpu_set_profiling(PovGpuScene* sc, int flags)
+{
+    if (!sc || (flags & ~(POV_GPU_PROFILE_TIMES | POV_GPU_PROFILE_WORK)))
+        return POV_GPU_E_INVALID;
+    std::lock_guard<std::mutex> g(sc->lock);
+    sc->profiling = flags;
+    if ((flags & POV_GPU_PROFILE_WORK) && sc->wcount.ensure(sizeof(unsigned long long) * 8) != cudaSuccess)
+        return POV_GPU_E_NOMEM;
+    return POV_GPU_OK;
+}
+
+int pov_gpu_get_timings(PovGpuScene* sc, PovGpuTimings* out)
+{
+    if (!sc || !out)
+        return POV_GPU_E_INVALID;
+    std::lock_guard<std::mutex> g(sc->lock);
+    *out = sc->timings;
+    return POV_GPU_OK;
+}
+
 int pov_gpu_trace_blocks(PovGpuScene* sc, const PovGpuBlock* blocks, int32_t num_blocks,
                          const PovGpuRenderParams* params, float* out_rgbt, PovGpuStats* stats)
 {
     if (!sc || !params || num_blocks < 0 || (num_blocks > 0 && (!blocks || !out_rgbt)))
         return POV_GPU_E_INVALID;
-    if (params->antialias)
+    const bool aa = params->antialias != 0;
+    if (aa && (params->sampling_method != 2 || params->jitter || params->aa_depth < 1 ||
+               params->aa_depth > MAX_AA_DEPTH))
         return POV_GPU_E_UNSUPPORTED;
     if (params->width <= 0 || params->height <= 0)
         return POV_GPU_E_INVALID;
@@ -805,8 +1084,8 @@ int pov_gpu_trace_blocks(PovGpuScene* sc, const PovGpuBlock* blocks, int32_t num
         return POV_GPU_OK;
     }
     std::vector<int4> hb((size_t)num_blocks);
-    std::vector<int> off((size_t)num_blocks + 1, 0);
-    long long npix = 0;
+    std::vector<int> off((size_t)num_blocks + 1, 0), coff((size_t)num_blocks + 1, 0);
+    long long npix = 0, ncorner = 0;
     for (int i = 0; i < num_blocks; i++) {
         const PovGpuBlock& b = blocks[i];
         if (b.left < 0 || b.top < 0 || b.right < b.left || b.bottom < b.top || b.right >= params->width ||
@@ -814,29 +1093,15 @@ int pov_gpu_trace_blocks(PovGpuScene* sc, const PovGpuBlock* blocks, int32_t num
             return POV_GPU_E_INVALID;
         hb[i] = make_int4(b.left, b.top, b.right, b.bottom);
         off[i] = (int)npix;
+        coff[i] = (int)ncorner;
         npix += (long long)(b.right - b.left + 1) * (b.bottom - b.top + 1);
+        ncorner += (long long)(b.right - b.left + 2) * (b.bottom - b.top + 2);
     }
     off[num_blocks] = (int)npix;
-    if (npix > (1ll << 28))
+    coff[num_blocks] = (int)ncorner;
+    if (ncorner > (1ll << 27))
         return POV_GPU_E_INVALID;
     const int n = (int)npix;
-    const int nl = std::max(sc->num_lights, 1);
-    const size_t maxq = (size_t)n;
-    CK(sc->blocks.ensure(sizeof(int4) * num_blocks));
-    CK(sc->block_off.ensure(sizeof(int) * (num_blocks + 1)));
-    CK(sc->qA.ensure(sizeof(QRay) * maxq));
-    CK(sc->qB.ensure(sizeof(QRay) * maxq));
-    CK(sc->pathA.ensure(sizeof(int) * maxq));
-    CK(sc->pathB.ensure(sizeof(int) * maxq));
-    CK(sc->hits.ensure(sizeof(QHit) * maxq));
-    CK(sc->paths.ensure(sizeof(PathState) * maxq));
-    CK(sc->slot_contrib.ensure(sizeof(float4) * maxq * nl));
-    CK(sc->sq.ensure(sizeof(QRay) * maxq * nl));
-    CK(sc->sq_slot.ensure(sizeof(int) * maxq * nl));
-    CK(sc->blocked.ensure(maxq * nl));
-    CK(sc->skipA.ensure(sizeof(uint32_t) * maxq));
-    CK(sc->skipB.ensure(sizeof(uint32_t) * maxq));
-    CK(sc->sskip.ensure(sizeof(uint32_t) * maxq * nl));
 
     cudaPointerAttributes pa{};
     bool out_on_device = cudaPointerGetAttributes(&pa, out_rgbt) == cudaSuccess &&
@@ -844,14 +1109,15 @@ int pov_gpu_trace_blocks(PovGpuScene* sc, const PovGpuBlock* blocks, int32_t num
     cudaGetLastError();
     float4* dout = reinterpret_cast<float4*>(out_rgbt);
     if (!out_on_device) {
-        CK(sc->out.ensure(sizeof(float4) * maxq));
+        CK(sc->out.ensure(sizeof(float4) * n));
         dout = sc->out.as<float4>();
     }
+    CK(sc->blocks.ensure(sizeof(int4) * num_blocks));
+    CK(sc->block_off.ensure(sizeof(int) * (num_blocks + 1)));
+    CK(sc->corner_off.ensure(sizeof(int) * (num_blocks + 1)));
 
     cudaStream_t st = sc->active();
     int* cnt = sc->counters.as<int>();
-    unsigned long long* dstats = sc->stats.as<unsigned long long>();
-    uint32_t* derr = sc->err.as<uint32_t>();
     unsigned long long* wc = (sc->profiling & POV_GPU_PROFILE_WORK) ? sc->wcount.as<unsigned long long>() : nullptr;
     StageClock clk(sc, st);
     CK(cudaMemcpyAsync(sc->blocks.p, hb.data(), sizeof(int4) * num_blocks, cudaMemcpyHostToDevice, st));
@@ -862,53 +1128,78 @@ int pov_gpu_trace_blocks(PovGpuScene* sc, const PovGpuBlock* blocks, int32_t num
     if (wc)
         CK(cudaMemsetAsync(wc, 0, sizeof(unsigned long long) * 8, st));
 
-    const DeviceScene& S = sc->S;
-    const int grid_trace = sc->num_sms * 8;
-    const int grid_shade = std::max(1, std::min(sc->num_sms * 16, (n + 127) / 128));
-    QRay* qcur = sc->qA.as<QRay>();
-    QRay* qnext = sc->qB.as<QRay>();
-    int* pcur = sc->pathA.as<int>();
-    int* pnext = sc->pathB.as<int>();
-    int* ccur = cnt + C_QA;
-    int* cnext = cnt + C_QB;
-    uint32_t* kcur = sc->skipA.as<uint32_t>();
-    uint32_t* knext = sc->skipB.as<uint32_t>();
-    CK(clk.begin(POV_GPU_STAGE_CAMERA));
-    CK(launch_camera(S, sc->blocks.as<int4>(), sc->block_off.as<int>(), num_blocks, n, params->width,
-                     params->height, qcur, pcur, sc->paths.as<PathState>(), ccur, dstats, kcur, st));
-    CK(clk.end());
-    for (int level = 0; level < sc->max_trace_level; level++) {
-        CK(cudaMemsetAsync(cnext, 0, sizeof(int), st));
-        CK(cudaMemsetAsync(cnt + C_SQ, 0, sizeof(int) * 3, st));   // SQ, W0, W1
-        CK(clk.begin(POV_GPU_STAGE_TRACE_CLOSEST));
-        CK(launch_trace(S, false, qcur, ccur, cnt + C_W0, sc->hits.as<QHit>(), nullptr, sc->stack_depth, grid_trace,
-                        derr, dstats, wc, (int)maxq, kcur, st));
-        CK(clk.end());
-        CK(clk.begin(POV_GPU_STAGE_SHADE));
-        CK(launch_shade(S, level, qcur, pcur, sc->hits.as<QHit>(), ccur, sc->paths.as<PathState>(),
-                        sc->slot_contrib.as<float4>(), sc->sq.as<QRay>(), sc->sq_slot.as<int>(), cnt + C_SQ,
-                        sc->sskip.as<uint32_t>(), qnext, pnext, knext, cnext, (int)maxq, (int)(maxq * nl), grid_shade,
-                        derr, dstats, st));
-        CK(clk.end());
-        if (sc->num_lights > 0) {
-            CK(clk.begin(POV_GPU_STAGE_TRACE_SHADOW));
-            CK(launch_trace(S, true, sc->sq.as<QRay>(), cnt + C_SQ, cnt + C_W1, nullptr, sc->blocked.as<uint8_t>(),
-                            sc->stack_depth, grid_trace, derr, dstats, wc ? wc + 4 : nullptr, (int)(maxq * nl),
-                            sc->sskip.as<uint32_t>(), st));
-            CK(clk.end());
-            CK(clk.begin(POV_GPU_STAGE_RESOLVE));
-            CK(launch_resolve(pcur, ccur, sc->num_lights, sc->sq_slot.as<int>(), sc->blocked.as<uint8_t>(),
-                              cnt + C_SQ, sc->slot_contrib.as<float4>(), sc->paths.as<PathState>(), grid_shade, st));
-            CK(clk.end(2));
+    uint64_t n_pixels = (uint64_t)n, n_samples = 0;
+    if (!aa) {
+        int rc = run_samples(sc, clk, 0, num_blocks, sc->block_off.as<int>(), nullptr, nullptr, n, params->width,
+                             params->height, nullptr, dout);
+        if (rc != POV_GPU_OK)
+            return rc;
+    } else {
+        // TraceTask::AdaptiveSupersamplingM2 (tracetask.cpp:604-657): the
+        // block corners first, then rounds of SubdivideOnePixel
+        const int depth = params->aa_depth;
+        const int sub = 1 << depth;
+        const int G = sub + 1;
+        const int MW = (G * G + 31) / 32;
+        CK(cudaMemcpyAsync(sc->corner_off.p, coff.data(), sizeof(int) * (num_blocks + 1), cudaMemcpyHostToDevice, st));
+        CK(sc->corners.ensure(sizeof(float4) * ncorner));
+        CK(sc->aa_grid.ensure(sizeof(float4) * (size_t)n * G * G));
+        CK(sc->aa_mask.ensure(sizeof(uint32_t) * (size_t)n * MW));
+        CK(sc->aa_subdiv.ensure(sizeof(uint32_t) * (size_t)n));
+        CK(sc->aa_xy.ensure(sizeof(int2) * (size_t)n));
+        // active cells per round are bounded by 4^round * pixels; both
+        // ping-pong lists are sized for the last round up front (growing a
+        // list later would drop the cells it holds)
+        size_t max_cells = (size_t)n;
+        for (int r = 0; r < depth - 1; r++)
+            max_cells *= 4;
+        CK(sc->cellsA.ensure(sizeof(int4) * std::max(max_cells, (size_t)n)));
+        CK(sc->cellsB.ensure(sizeof(int4) * std::max(max_cells, (size_t)n)));
+        int rc = run_samples(sc, clk, 1, num_blocks, sc->corner_off.as<int>(), nullptr, nullptr, (int)ncorner,
+                             params->width, params->height, nullptr, sc->corners.as<float4>());
+        if (rc != POV_GPU_OK)
+            return rc;
+        CK(launch_aa_init(sc->blocks.as<int4>(), sc->block_off.as<int>(), sc->corner_off.as<int>(), num_blocks, n,
+                          sc->corners.as<float4>(), G, MW, sc->aa_grid.as<float4>(), sc->aa_mask.as<uint32_t>(),
+                          sc->aa_subdiv.as<uint32_t>(), sc->aa_xy.as<int2>(), sc->cellsA.as<int4>(), cnt + C_NC,
+                          depth - 1, st));
+        sc->timings.kernel_launches++;
+        n_pixels = (uint64_t)ncorner;
+        int ncells = n;
+        int4* ccur = sc->cellsA.as<int4>();
+        for (int round = 0; round < depth - 1 && ncells > 0; round++) {
+            const int scap = 5 * ncells, ncap = 4 * ncells;
+            CK(sc->spos.ensure(sizeof(double2) * (size_t)scap));
+            CK(sc->sslot.ensure(sizeof(int) * (size_t)scap));
+            int4* cnext = (ccur == sc->cellsA.as<int4>()) ? sc->cellsB.as<int4>() : sc->cellsA.as<int4>();
+            CK(cudaMemsetAsync(cnt + C_NS, 0, sizeof(int), st));
+            CK(cudaMemsetAsync(cnt + C_NN, 0, sizeof(int), st));
+            int gb = std::max(1, std::min(sc->num_sms * 16, (ncells + 127) / 128));
+            CK(launch_aa_classify(ccur, cnt + C_NC, ncells, G, MW, sc->aa_grid.as<float4>(),
+                                  sc->aa_mask.as<uint32_t>(), sc->aa_subdiv.as<uint32_t>(), sc->aa_xy.as<int2>(),
+                                  (double)params->aa_threshold, (double)sub, sc->spos.as<double2>(),
+                                  sc->sslot.as<int>(), cnt + C_NS, scap, cnext, cnt + C_NN, ncap,
+                                  sc->err.as<uint32_t>(), gb, st));
+            sc->timings.kernel_launches++;
+            int hc[2] = {0, 0};
+            CK(cudaMemcpyAsync(hc, cnt + C_NS, sizeof(int), cudaMemcpyDeviceToHost, st));
+            CK(cudaMemcpyAsync(hc + 1, cnt + C_NN, sizeof(int), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            const int nsamp = std::min(hc[0], scap);
+            if (nsamp > 0) {
+                rc = run_samples(sc, clk, 2, 0, nullptr, sc->spos.as<double2>(), cnt + C_NS, nsamp, params->width,
+                                 params->height, sc->sslot.as<int>(), sc->aa_grid.as<float4>());
+                if (rc != POV_GPU_OK)
+                    return rc;
+            }
+            n_samples += (uint64_t)nsamp;
+            ncells = std::min(hc[1], ncap);
+            CK(cudaMemcpyAsync(cnt + C_NC, &ncells, sizeof(int), cudaMemcpyHostToDevice, st));
+            ccur = cnext;
         }
-        std::swap(qcur, qnext);
-        std::swap(pcur, pnext);
-        std::swap(ccur, cnext);
-        std::swap(kcur, knext);
+        CK(launch_aa_resolve(sc->aa_grid.as<float4>(), sc->aa_subdiv.as<uint32_t>(), n, G, depth, dout, st));
+        sc->timings.kernel_launches++;
     }
-    CK(clk.begin(POV_GPU_STAGE_FINALIZE));
-    CK(launch_finalize(sc->paths.as<PathState>(), n, dout, st));
-    CK(clk.end());
     if (!out_on_device)
         CK(cudaMemcpyAsync(out_rgbt, dout, sizeof(float4) * n, cudaMemcpyDeviceToHost, st));
     unsigned long long hw[8] = {0};
@@ -916,8 +1207,10 @@ int pov_gpu_trace_blocks(PovGpuScene* sc, const PovGpuBlock* blocks, int32_t num
         CK(cudaMemcpyAsync(hw, wc, sizeof(hw), cudaMemcpyDeviceToHost, st));
     unsigned long long hs[ST_COUNT];
     int rc = check_device_error(sc, stats, hs);
-    if (stats)
-        stats->number_of_pixels = (uint64_t)n;
+    if (stats) {
+        stats->number_of_pixels = n_pixels;
+        stats->number_of_samples = n_samples;
+    }
     clk.collect();
     if (wc) {
         for (int k = 0; k < 2; k++) {
@@ -965,18 +1258,6 @@ int pov_gpu_trace_rays(PovGpuScene* sc, const double* origins, const double* dir
     unsigned long long hs[ST_COUNT];
     int rc = check_device_error(sc, nullptr, hs);
     // map prim references to flattened object ids / mesh triangle indices
-    std::vector<int32_t> sphere_obj, plane_obj, tri_global, tri_local;
-    std::vector<float4> tri_normal;
-    auto fetch_i = [&](DevBuf& b, std::vector<int32_t>& v) {
-        v.resize(b.bytes / sizeof(int32_t));
-        return cudaMemcpy(v.data(), b.p, b.bytes, cudaMemcpyDeviceToHost);
-    };
-    CK(fetch_i(sc->sphere_obj, sphere_obj));
-    CK(fetch_i(sc->plane_obj, plane_obj));
-    CK(fetch_i(sc->tri_global, tri_global));
-    CK(fetch_i(sc->tri_local, tri_local));
-    tri_normal.resize(sc->tri_normal.bytes / sizeof(float4));
-    CK(cudaMemcpy(tri_normal.data(), sc->tri_normal.p, sc->tri_normal.bytes, cudaMemcpyDeviceToHost));
     for (size_t i = 0; i < n; i++) {
         const QHit& h = hh[i];
         hits[i].object = -1;
@@ -986,14 +1267,22 @@ int pov_gpu_trace_rays(PovGpuScene* sc, const double* origins, const double* dir
             continue;
         uint32_t kind = h.prim >> PRIM_KIND_SHIFT, idx = h.prim & PRIM_INDEX_MASK;
         hits[i].t = t64[i];
-        if (kind == PK_SPHERE)
-            hits[i].object = sphere_obj[idx];
-        else if (kind == PK_PLANE)
-            hits[i].object = plane_obj[idx];
-        else if (kind == PK_TRIANGLE) {
-            int gidx = tri_global[idx];
-            hits[i].object = __builtin_bit_cast(int32_t, tri_normal[gidx].w);
-            hits[i].triangle = tri_local[gidx];
+        if (kind == PK_SPHERE) {
+            hits[i].object = sc->h_sphere_obj[idx];
+        } else if (kind == PK_PLANE) {
+            hits[i].object = sc->h_plane_obj[idx];
+        } else if (kind == PK_BOX) {
+            hits[i].object = sc->h_box_obj[idx];
+        } else if (kind == PK_TORUS) {
+            hits[i].object = sc->h_torus_obj[idx];
+        } else if (kind == PK_CSG) {
+            uint32_t aux = __builtin_bit_cast(uint32_t, h.u);
+            const DevCsg& cg = sc->h_csgs[idx];
+            hits[i].object = sc->h_csg_children[cg.first + (aux & 0xffffu)].object;
+        } else if (kind == PK_TRIANGLE) {
+            int gidx = sc->h_tri_global[idx];
+            hits[i].object = sc->h_tri_obj[gidx];
+            hits[i].triangle = sc->h_tri_local[gidx];
         }
     }
     return rc;

@@ -74,6 +74,39 @@ struct __align__(16) DevMesh {
     int32_t normal_base;     // offset into the global normal table
 };
 
+// Axis-aligned box (Box without a transform): corners, object id and flags.
+struct __align__(16) DevBox {
+    float4 lo;      // xyz, w = object id (int bits)
+    float4 hi;      // xyz, w = flags (int bits, bit0 inverted)
+};
+
+// Torus in its own frame: the inverse TRANSFORM rows 0..3, columns 0..2
+// (p_local = p . M^-1), radii, object id, flags.  FP64: the quartic is
+// solved in double (source/core/shape/torus.cpp:241-362).
+struct __align__(16) DevTorus {
+    double inv[12];
+    double R, r;
+    int32_t object;
+    int32_t flags;
+    int32_t pad[2];
+};
+
+// CSG intersection / merge evaluated as one primitive over its leaf
+// children (source/core/shape/csg.cpp:219-403).  Unions are flattened into
+// their children at build time.
+struct __align__(16) DevCsg {
+    int32_t type;       // POV_OBJ_INTERSECTION or POV_OBJ_MERGE
+    int32_t first;      // into csg_children
+    int32_t count;
+    int32_t object;
+};
+struct __align__(16) DevCsgChild {
+    int32_t kind;       // PK_SPHERE, PK_BOX, PK_TORUS or PK_PLANE
+    int32_t index;      // into the per-kind arrays
+    int32_t flags;      // bit0 inverted
+    int32_t object;
+};
+
 struct DeviceScene {
     const BvhNode*  nodes;
     const uint32_t* prim_refs;
@@ -95,6 +128,13 @@ struct DeviceScene {
     const float4*   planes;         // normal xyz, Distance
     const int32_t*  plane_obj;
     int32_t         num_planes;
+    // boxes, tori, CSG
+    const DevBox*      boxes;
+    const DevTorus*    tori;
+    const DevCsg*      csgs;
+    const DevCsgChild* csg_children;
+    const int32_t*     sphere_flags;   // bit0 inverted (spheres inside CSG)
+    int32_t            has_full_prims; // tori or CSG present: full traversal variant
     // objects, materials, lights
     const ObjectShade* objects;
     const DevMaterial* materials;

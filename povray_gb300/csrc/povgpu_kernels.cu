@@ -1,8 +1,10 @@
 // povgpu_kernels.cu -- sm_103a kernels of the trace path.
 //
-// One frame (a batch of render blocks) is a short wavefront pipeline:
-//   k_camera         primary rays of every pixel (TracePixel::CreateCameraRay,
-//                    source/core/render/tracepixel.cpp:357-373,924)
+// One batch of image samples is a short wavefront pipeline:
+//   k_camera         primary rays (TracePixel::CreateCameraRay,
+//                    source/core/render/tracepixel.cpp:357-373,924) for
+//                    pixel centres, block corners (adaptive AA) or an
+//                    explicit list of sub-pixel positions
 //   per trace level L = 0 .. max_trace_level-1:
 //     k_trace<closest>  Trace::FindIntersection (trace.cpp:285) over the BVH
 //     k_shade           ComputeTextureColour/ComputeLightedTexture
@@ -12,13 +14,15 @@
 //                       trace.cpp:1264-1321) into compacted queues
 //     k_trace<any>      TracePointLightShadowRay (trace.cpp:1951-2076) for
 //                       opaque occluders: any hit in (1e-3, dist-1e-3)
-//     k_resolve         adds each unblocked light term to its path
-//   k_finalize       RGBT per pixel in block order (CompletedRectangle).
+//     k_mark_blocked, k_resolve   add each unblocked light term to its path
+//   k_finalize       RGBT per sample (CompletedRectangle order or AA slots)
+// Adaptive antialiasing (TraceTask::AdaptiveSupersamplingM2) adds
+// k_aa_init / k_aa_classify / k_aa_resolve around the same pipeline.
 // Traversal kernels are persistent: each warp pulls 32 rays at a time from
-// a device counter, so no host round trip sits between the stages and the
-// whole sequence can be captured into one CUDA graph.
+// a device counter, so no host round trip sits between the stages.
 #include "povgpu_internal.h"
 #include "povgpu_kernels.h"
+#include "povgpu_quartic.cuh"
 
 #include <cuda_runtime.h>
 #include <math_constants.h>
@@ -27,13 +31,18 @@
 namespace povgpu {
 
 // Tolerances of the reference (source/core/configcore.h:153-206,
-// source/core/render/trace.cpp:81).
+// source/core/render/trace.cpp:81, per-shape DEPTH_TOLERANCE in the shape
+// files).
 __constant__ float kMinIsectDepth = 1.0e-4f;
 #define EPSILON_D 1.0e-10
 #define EPSILON_F 1.0e-10f
 #define SMALL_TOLERANCE_F 1.0e-3f
 #define SHADOW_TOLERANCE_F 1.0e-3f
-#define MAX_DISTANCE_F 1.0e7f
+#define BOX_DEPTH_TOL 1.0e-6f
+#define CLOSE_TOL 1.0e-6f
+#define TORUS_DEPTH_TOL 1.0e-4
+#define TORUS_ROOT_TOL 1.0e-4
+#define NO_PRIM 0xffffffffu
 
 // ------------------------------------------------------------ helpers --
 __device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
@@ -52,6 +61,7 @@ __device__ __forceinline__ float3 normalize3(float3 v)
     float l = sqrtf(dot3(v, v));
     return l != 0.0f ? v * (1.0f / l) : v;
 }
+__device__ __forceinline__ float comp(float3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
 
 __device__ __forceinline__ void set_error(uint32_t* err, uint32_t bits) { atomicOr(err, bits); }
 
@@ -70,35 +80,26 @@ __device__ __forceinline__ int warp_reserve(int* counter, bool want, unsigned ma
     return want ? base + __popc(ballot & ((1u << lane) - 1u)) : -1;
 }
 
-// --------------------------------------------------------------- camera --
-// Primary ray of pixel centre (x+0.5, y+0.5); direction formed and
-// normalised in FP64 exactly as CreateCameraRay does, then rounded.
-__global__ void k_camera(DeviceScene S, const int4* __restrict__ blocks, const int* __restrict__ block_off,
-                         int nblocks, int width, int height, QRay* __restrict__ q, int* __restrict__ q_path,
-                         PathState* __restrict__ paths, int* __restrict__ q_count, unsigned long long* stats,
-                         uint32_t* __restrict__ q_skip)
+// Same, reserving `k` consecutive slots per wanting lane.
+__device__ __forceinline__ int warp_reserve_k(int* counter, bool want, int k, unsigned mask)
 {
-    int npix = block_off[nblocks];
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i == 0) {
-        *q_count = npix;
-        atomicAdd(&stats[ST_RAYS], (unsigned long long)npix);
-    }
-    if (i >= npix)
-        return;
-    // block containing pixel i (binary search over the prefix offsets)
-    int lo = 0, hi = nblocks - 1;
-    while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if (block_off[mid] <= i) lo = mid; else hi = mid - 1;
-    }
-    int4 b = blocks[lo];   // left, top, right, bottom
-    int w = b.z - b.x + 1;
-    int local = i - block_off[lo];
-    int x = b.x + local % w;
-    int y = b.y + local / w;
-    double x0 = ((double)x + 0.5) / (double)width - 0.5;
-    double y0 = 0.5 - ((double)y + 0.5) / (double)height;
+    unsigned ballot = __ballot_sync(mask, want);
+    int lane = threadIdx.x & 31;
+    int leader = __ffs(ballot) - 1;
+    int base = 0;
+    if (ballot != 0u && lane == leader)
+        base = atomicAdd(counter, k * __popc(ballot));
+    base = __shfl_sync(mask, base, leader < 0 ? 0 : leader);
+    return want ? base + k * __popc(ballot & ((1u << lane) - 1u)) : -1;
+}
+
+// --------------------------------------------------------------- camera --
+// Primary ray through image position (x, y) (pixel units, y down), formed
+// and normalised in FP64 exactly as CreateCameraRay does, then rounded.
+__device__ __forceinline__ QRay camera_ray(const DeviceScene& S, double x, double y, int width, int height)
+{
+    double x0 = x / (double)width - 0.5;
+    double y0 = 0.5 - y / (double)height;
     double dx = S.cam_dir[0] + x0 * S.cam_right[0] + y0 * S.cam_up[0];
     double dy = S.cam_dir[1] + x0 * S.cam_right[1] + y0 * S.cam_up[1];
     double dz = S.cam_dir[2] + x0 * S.cam_right[2] + y0 * S.cam_up[2];
@@ -107,9 +108,47 @@ __global__ void k_camera(DeviceScene S, const int4* __restrict__ blocks, const i
     QRay r;
     r.org = make_float4((float)S.cam_loc[0], (float)S.cam_loc[1], (float)S.cam_loc[2], kMinIsectDepth);
     r.dir = make_float4((float)dx, (float)dy, (float)dz, CUDART_INF_F);
-    q[i] = r;
+    return r;
+}
+
+// mode 0: pixel centres (x+0.5, y+0.5) of every block, block order
+// mode 1: pixel corners (x, y) of every block, (w+1) x (h+1) per block
+//         (AdaptiveSupersamplingM2 traces these, tracetask.cpp:620-628)
+// mode 2: explicit positions pos[i]; the count is read from *npos
+__global__ void k_camera(DeviceScene S, int mode, const int4* __restrict__ blocks,
+                         const int* __restrict__ block_off, int nblocks, const double2* __restrict__ pos,
+                         const int* __restrict__ npos, int width, int height, QRay* __restrict__ q,
+                         int* __restrict__ q_path, PathState* __restrict__ paths, int* __restrict__ q_count,
+                         unsigned long long* stats, uint2* __restrict__ q_skip, int cap)
+{
+    int n = min(mode == 2 ? *npos : block_off[nblocks], cap);   // never past the queue buffers
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) {
+        *q_count = n;
+        atomicAdd(&stats[ST_RAYS], (unsigned long long)n);
+    }
+    if (i >= n)
+        return;
+    double x, y;
+    if (mode == 2) {
+        double2 p = pos[i];
+        x = p.x;
+        y = p.y;
+    } else {
+        int lo = 0, hi = nblocks - 1;   // block containing sample i
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (block_off[mid] <= i) lo = mid; else hi = mid - 1;
+        }
+        int4 b = blocks[lo];            // left, top, right, bottom
+        int w = b.z - b.x + 1 + (mode == 1 ? 1 : 0);
+        int local = i - block_off[lo];
+        x = (double)(b.x + local % w) + (mode == 0 ? 0.5 : 0.0);
+        y = (double)(b.y + local / w) + (mode == 0 ? 0.5 : 0.0);
+    }
+    q[i] = camera_ray(S, x, y, width, height);
     q_path[i] = i;
-    q_skip[i] = 0xffffffffu;
+    q_skip[i] = make_uint2(NO_PRIM, 0u);
     PathState p;
     p.colour = make_float4(0.f, 0.f, 0.f, 0.f);
     p.throughput = make_float4(1.f, 1.f, 1.f, 1.f);
@@ -131,60 +170,345 @@ __global__ void k_load_rays(const double* __restrict__ org, const double* __rest
     q[i] = r;
 }
 
-// ------------------------------------------------------------ intersect --
-// Sphere (Sphere::Intersect, sphere.cpp:214-245) with the chord computed
-// from the perpendicular offset vector, which keeps FP32 accurate far from
-// the sphere; near-tangent rays (the reference's grazing band) are re-solved
-// in FP64.  Returns the nearest root in (tmin, tmax), or tmax.
-__device__ __forceinline__ bool isect_sphere(float4 s, float3 o, float3 d, float tmin, float& t)
+// ------------------------------------------------------------ sphere --
+// Sphere::Intersect (sphere.cpp:214-245) with the chord taken from the
+// perpendicular offset vector, which keeps FP32 accurate away from the
+// sphere; the near-tangent band is re-solved in FP64.  Both roots, or 0.
+__device__ __forceinline__ int sphere_roots(float4 s, float3 o, float3 d, float& t1, float& t2)
 {
     float3 oc = xyz(s) - o;
     float tca = dot3(oc, d);
     float ocs = dot3(oc, oc);
     float r2 = s.w * s.w;
     if (ocs >= r2 && tca < EPSILON_F)
-        return false;
+        return 0;
     float3 perp = oc - d * tca;
     float thcs = r2 - dot3(perp, perp);
     if (thcs <= 1.0e-4f * r2) {
-        // grazing band: FP64 re-solve (the reference works in double)
         double ox = (double)s.x - o.x, oy = (double)s.y - o.y, oz = (double)s.z - o.z;
         double tcad = ox * d.x + oy * d.y + oz * d.z;
         double px = ox - d.x * tcad, py = oy - d.y * tcad, pz = oz - d.z * tcad;
         double th = (double)s.w * s.w - (px * px + py * py + pz * pz);
         if (!(th > EPSILON_D))
-            return false;
+            return 0;
         double hc = sqrt(th);
-        double t1 = tcad - hc, t2 = tcad + hc;
-        if (t1 > 1.0e-6 && (float)t1 >= tmin && (float)t1 < t) { t = (float)t1; return true; }
-        if (t2 > 1.0e-6 && (float)t2 >= tmin && (float)t2 < t) { t = (float)t2; return true; }
-        return false;
+        t1 = (float)(tcad - hc);
+        t2 = (float)(tcad + hc);
+        return 2;
     }
     float hc = sqrtf(thcs);
-    float t1 = tca - hc, t2 = tca + hc;
-    if (t1 >= tmin && t1 < t) { t = t1; return true; }
-    if (t2 >= tmin && t2 < t) { t = t2; return true; }
+    t1 = tca - hc;
+    t2 = tca + hc;
+    return 2;
+}
+
+__device__ __forceinline__ bool sphere_inside(float4 s, int flags, float3 p)
+{
+    float3 d = xyz(s) - p;
+    float ocs = dot3(d, d), r2 = s.w * s.w;
+    return (flags & 1) ? ocs > r2 : ocs < r2;
+}
+
+// ---------------------------------------------------------------- box --
+enum { SIDE_X0 = 0, SIDE_X1, SIDE_Y0, SIDE_Y1, SIDE_Z0, SIDE_Z1 };
+
+// Box::Intersect (box.cpp:172-533): entry/exit depths and the side each
+// lies on, with the reference's CLOSE_TOLERANCE tie-breaking between
+// sides.  Returns false when the box is missed or entirely behind.
+__device__ __forceinline__ bool box_roots(const DevBox& b, float3 P, float3 D, float& tn, float& tf, int& sn, int& sf)
+{
+    int smin = 0, smax = 0;
+    float tmin = 0.0f, tmax = 2.0e10f, t;
+    float3 c1 = xyz(b.lo), c2 = xyz(b.hi);
+    // X
+    if (D.x < -EPSILON_F) {
+        t = (c1.x - P.x) / D.x;
+        if (t < tmin) return false;
+        if (t <= tmax) { smax = SIDE_X0; tmax = t; }
+        t = (c2.x - P.x) / D.x;
+        if (t >= tmin) { if (t > tmax) return false; smin = SIDE_X1; tmin = t; }
+    } else if (D.x > EPSILON_F) {
+        t = (c2.x - P.x) / D.x;
+        if (t < tmin) return false;
+        if (t <= tmax) { smax = SIDE_X1; tmax = t; }
+        t = (c1.x - P.x) / D.x;
+        if (t >= tmin) { if (t > tmax) return false; smin = SIDE_X0; tmin = t; }
+    } else if (P.x < c1.x || P.x > c2.x) {
+        return false;
+    }
+    // Y
+    if (D.y < -EPSILON_F) {
+        t = (c1.y - P.y) / D.y;
+        if (t < tmin) return false;
+        if (t <= tmax - CLOSE_TOL) { smax = SIDE_Y0; tmax = t; }
+        else if (t <= tmax + CLOSE_TOL) { if (-D.y > fabsf(D.x)) smax = SIDE_Y0; }
+        t = (c2.y - P.y) / D.y;
+        if (t >= tmin + CLOSE_TOL) { if (t > tmax) return false; smin = SIDE_Y1; tmin = t; }
+        else if (t >= tmin - CLOSE_TOL) { if (-D.y > fabsf(D.x)) smin = SIDE_Y1; }
+    } else if (D.y > EPSILON_F) {
+        t = (c2.y - P.y) / D.y;
+        if (t < tmin) return false;
+        if (t <= tmax - CLOSE_TOL) { smax = SIDE_Y1; tmax = t; }
+        else if (t <= tmax + CLOSE_TOL) { if (D.y > fabsf(D.x)) smax = SIDE_Y1; }
+        t = (c1.y - P.y) / D.y;
+        if (t >= tmin + CLOSE_TOL) { if (t > tmax) return false; smin = SIDE_Y0; tmin = t; }
+        else if (t >= tmin - CLOSE_TOL) { if (D.y > fabsf(D.x)) smin = SIDE_Y0; }
+    } else if (P.y < c1.y || P.y > c2.y) {
+        return false;
+    }
+    // Z
+    if (D.z < -EPSILON_F) {
+        t = (c1.z - P.z) / D.z;
+        if (t < tmin) return false;
+        if (t <= tmax - CLOSE_TOL) { smax = SIDE_Z0; tmax = t; }
+        else if (t <= tmax + CLOSE_TOL) {
+            if ((smax <= SIDE_X1) ? (-D.z > fabsf(D.x)) : (-D.z > fabsf(D.y))) smax = SIDE_Z0;
+        }
+        t = (c2.z - P.z) / D.z;
+        if (t >= tmin + CLOSE_TOL) { if (t > tmax) return false; smin = SIDE_Z1; tmin = t; }
+        else if (t >= tmin - CLOSE_TOL) {
+            if ((smin <= SIDE_X1) ? (-D.z > fabsf(D.x)) : (-D.z > fabsf(D.y))) smin = SIDE_Z1;
+        }
+    } else if (D.z > EPSILON_F) {
+        t = (c2.z - P.z) / D.z;
+        if (t < tmin) return false;
+        if (t <= tmax - CLOSE_TOL) { smax = SIDE_Z1; tmax = t; }
+        else if (t <= tmax + CLOSE_TOL) {
+            if ((smax <= SIDE_X1) ? (D.z > fabsf(D.x)) : (D.z > fabsf(D.y))) smax = SIDE_Z1;
+        }
+        t = (c1.z - P.z) / D.z;
+        if (t >= tmin + CLOSE_TOL) { if (t > tmax) return false; smin = SIDE_Z0; tmin = t; }
+        else if (t >= tmin - CLOSE_TOL) {
+            if ((smin <= SIDE_X1) ? (D.z > fabsf(D.x)) : (D.z > fabsf(D.y))) smin = SIDE_Z0;
+        }
+    } else if (P.z < c1.z || P.z > c2.z) {
+        return false;
+    }
+    if (tmax < BOX_DEPTH_TOL)
+        return false;
+    tn = tmin; tf = tmax; sn = smin; sf = smax;
+    return true;
+}
+
+__device__ __forceinline__ bool box_inside(const DevBox& b, int flags, float3 p)
+{
+    bool out = p.x < b.lo.x || p.x > b.hi.x || p.y < b.lo.y || p.y > b.hi.y || p.z < b.lo.z || p.z > b.hi.z;
+    return (flags & 1) ? out : !out;
+}
+
+__device__ __forceinline__ float3 box_side_normal(int side)
+{
+    float s = (side & 1) ? 1.0f : -1.0f;
+    int ax = side >> 1;
+    return f3(ax == 0 ? s : 0.f, ax == 1 ? s : 0.f, ax == 2 ? s : 0.f);
+}
+
+// -------------------------------------------------------------- torus --
+// Torus::Intersect (torus.cpp:241-362) in FP64: local frame, thick
+// cylinder bound, origin moved near the bounding sphere, quartic.
+__device__ __forceinline__ bool torus_thick_cylinder(double3 P, double3 D, double h1, double h2, double r1, double r2)
+{
+    const double MAXD = 1.0e7;
+    if (fabs(D.y) < EPSILON_D) {
+        if (P.y < h1 || P.y > h2) return false;
+    } else {
+        double k = (h2 - P.y) / D.y, u = P.x + k * D.x, v = P.z + k * D.z;
+        if (k > EPSILON_D && k < MAXD) { double r = u * u + v * v; if (r >= r1 && r <= r2) return true; }
+        k = (h1 - P.y) / D.y; u = P.x + k * D.x; v = P.z + k * D.z;
+        if (k > EPSILON_D && k < MAXD) { double r = u * u + v * v; if (r >= r1 && r <= r2) return true; }
+    }
+    double a = D.x * D.x + D.z * D.z;
+    if (a > EPSILON_D) {
+        double b = P.x * D.x + P.z * D.z;
+        double rr[2] = {r2, r1};
+        for (int c = 0; c < 2; c++) {
+            double cc = P.x * P.x + P.z * P.z - rr[c];
+            double dd = b * b - a * cc;
+            if (dd >= 0.0) {
+                dd = sqrt(dd);
+                double k = (-b + dd) / a;
+                if (k > EPSILON_D && k < MAXD) { double h = P.y + k * D.y; if (h >= h1 && h <= h2) return true; }
+                k = (-b - dd) / a;
+                if (k > EPSILON_D && k < MAXD) { double h = P.y + k * D.y; if (h >= h1 && h <= h2) return true; }
+            }
+        }
+    }
     return false;
 }
 
-// A ray starting on the sphere's own surface: only the far root, and only
-// when the ray heads into the sphere (tca > 0).
-__device__ __forceinline__ bool isect_sphere_far(float4 s, float3 o, float3 d, float tmin, float& t)
+__device__ __forceinline__ double3 torus_local_point(const DevTorus& T, double x, double y, double z)
 {
-    float3 oc = xyz(s) - o;
-    float tca = dot3(oc, d);
-    if (tca <= 0.0f)
-        return false;
-    float3 perp = oc - d * tca;
-    float thcs = s.w * s.w - dot3(perp, perp);
-    if (!(thcs > 0.0f))
-        return false;
-    float t2 = tca + sqrtf(thcs);
-    if (t2 >= tmin && t2 < t) {
-        t = t2;
-        return true;
+    const double* m = T.inv;
+    return make_double3(x * m[0] + y * m[3] + z * m[6] + m[9], x * m[1] + y * m[4] + z * m[7] + m[10],
+                        x * m[2] + y * m[5] + z * m[8] + m[11]);
+}
+
+// Roots (world depths) with depth > 1e-4; returns their count (<= 4).
+__device__ __noinline__ int torus_roots(const DevTorus& T, float3 o, float3 d, double* out)
+{
+    const double* m = T.inv;
+    double3 P = torus_local_point(T, o.x, o.y, o.z);
+    double3 D = make_double3(d.x * m[0] + d.y * m[3] + d.z * m[6], d.x * m[1] + d.y * m[4] + d.z * m[7],
+                             d.x * m[2] + d.y * m[5] + d.z * m[8]);
+    double len = sqrt(D.x * D.x + D.y * D.y + D.z * D.z);
+    D.x /= len; D.y /= len; D.z /= len;
+    double R = T.R, r = T.r;
+    double r1 = R < r ? 0.0 : (R - r) * (R - r), r2 = (R + r) * (R + r);
+    if (!torus_thick_cylinder(P, D, -r, r, r1, r2))
+        return 0;
+    double bsr = R + r + r, dp = P.x * P.x + P.y * P.y + P.z * P.z, closer = 0.0;
+    if (dp > bsr * bsr) {
+        closer = sqrt(dp) - bsr;
+        P.x += closer * D.x; P.y += closer * D.y; P.z += closer * D.z;
     }
-    return false;
+    double R2 = R * R, rr2 = r * r, Py2 = P.y * P.y, Dy2 = D.y * D.y, PDy2 = P.y * D.y;
+    double k1 = P.x * P.x + P.z * P.z + Py2 - R2 - rr2;
+    double k2 = P.x * D.x + P.z * D.z + PDy2;
+    double c[5] = {1.0, 4.0 * k2, 2.0 * (k1 + 2.0 * (k2 * k2 + R2 * Dy2)), 4.0 * (k2 * k1 + 2.0 * R2 * PDy2),
+                   k1 * k1 + 4.0 * R2 * (Py2 - rr2)};
+    double roots[4];
+    int n = quartic::solve4(c, roots, TORUS_ROOT_TOL);
+    int k = 0;
+    for (int i = n - 1; i >= 0; i--) {
+        double t = (roots[i] + closer) / len;
+        if (t > TORUS_DEPTH_TOL && t < 1.0e7)
+            out[k++] = t;
+    }
+    return k;
+}
+
+__device__ __forceinline__ bool torus_inside(const DevTorus& T, float3 p)
+{
+    double3 P = torus_local_point(T, p.x, p.y, p.z);
+    double rr = sqrt(P.x * P.x + P.z * P.z);
+    double r2 = P.y * P.y + (rr - T.R) * (rr - T.R);
+    bool in = r2 <= T.r * T.r;
+    return (T.flags & 1) ? !in : in;
+}
+
+__device__ __forceinline__ float3 torus_normal(const DevTorus& T, float3 p)
+{
+    double3 P = torus_local_point(T, p.x, p.y, p.z);
+    double dist = sqrt(P.x * P.x + P.z * P.z);
+    double mx = 0.0, mz = 0.0;
+    if (dist > EPSILON_D) { mx = T.R * P.x / dist; mz = T.R * P.z / dist; }
+    double nx = P.x - mx, ny = P.y, nz = P.z - mz;
+    const double* m = T.inv;   // MTransNormal: rows of the inverse
+    float3 n = f3((float)(nx * m[0] + ny * m[1] + nz * m[2]), (float)(nx * m[3] + ny * m[4] + nz * m[5]),
+                  (float)(nx * m[6] + ny * m[7] + nz * m[8]));
+    return normalize3(n);
+}
+
+// Drops the root of a ray's own origin surface: the root nearest zero when
+// it is within 1e-2 (FP32 origin rounding can lift it above the 1e-4 cut).
+__device__ __forceinline__ int torus_drop_self(double* t, int n)
+{
+    int m = -1;
+    for (int i = 0; i < n; i++)
+        if (m < 0 || t[i] < t[m]) m = i;
+    if (m >= 0 && t[m] < 1.0e-2) {
+        t[m] = t[n - 1];
+        return n - 1;
+    }
+    return n;
+}
+
+// ---------------------------------------------------------------- CSG --
+__device__ __forceinline__ bool child_inside(const DeviceScene& S, const DevCsgChild& c, float3 p)
+{
+    switch (c.kind) {
+    case PK_SPHERE: return sphere_inside(__ldg(S.spheres + c.index), c.flags, p);
+    case PK_BOX: return box_inside(S.boxes[c.index], c.flags, p);
+    case PK_TORUS: return torus_inside(S.tori[c.index], p);
+    case PK_PLANE: {
+        float4 pl = __ldg(S.planes + c.index);
+        return dot3(p, xyz(pl)) + pl.w < EPSILON_F;
+    }
+    default: return false;
+    }
+}
+
+// Roots of one CSG child with the aux word (box side).
+__device__ __forceinline__ int child_roots(const DeviceScene& S, const DevCsgChild& c, float3 o, float3 d,
+                                           float* t, int* side, bool self, int self_side)
+{
+    int n = 0;
+    if (c.kind == PK_SPHERE) {
+        float t1, t2;
+        float4 s = __ldg(S.spheres + c.index);
+        if (sphere_roots(s, o, d, t1, t2)) {
+            if (self) {
+                if (dot3(xyz(s) - o, d) > 0.0f) { t[n] = t2; side[n++] = 0; }   // inward: far root only
+            } else {
+                if (t1 > 1.0e-6f) { t[n] = t1; side[n++] = 0; }
+                if (t2 > 1.0e-6f) { t[n] = t2; side[n++] = 0; }
+            }
+        }
+    } else if (c.kind == PK_BOX) {
+        float tn, tf;
+        int sn, sf;
+        const DevBox b = S.boxes[c.index];
+        if (box_roots(b, o, d, tn, tf, sn, sf)) {
+            if (self) {
+                if (dot3(box_side_normal(self_side), d) < 0.0f) { t[n] = tf; side[n++] = sf; }
+            } else {
+                if (tn > BOX_DEPTH_TOL) { t[n] = tn; side[n++] = sn; }
+                t[n] = tf; side[n++] = sf;
+            }
+        }
+    } else if (c.kind == PK_TORUS) {
+        double r[4];
+        int k = torus_roots(S.tori[c.index], o, d, r);
+        if (self) k = torus_drop_self(r, k);
+        for (int i = 0; i < k; i++) { t[n] = (float)r[i]; side[n++] = 0; }
+    } else if (c.kind == PK_PLANE) {
+        float4 pl = __ldg(S.planes + c.index);
+        float ndd = dot3(xyz(pl), d);
+        if (!self && fabsf(ndd) >= EPSILON_F) {
+            float tt = -(dot3(xyz(pl), o) + pl.w) / ndd;
+            if (tt >= 1.0e-6f) { t[n] = tt; side[n++] = 0; }
+        }
+    }
+    return n;
+}
+
+// CSGIntersection / CSGMerge::All_Intersections fused with the closest-hit
+// filter: a child's root survives if the point is inside every sibling
+// (intersection) or inside none (merge).  Returns the best surviving root in
+// [tmin, t) and its (child, side) aux word.
+__device__ __forceinline__ bool csg_closest(const DeviceScene& S, uint32_t idx, float3 o, float3 d, float tmin,
+                                            float& t, uint32_t& aux, uint2 skip, uint32_t ref, bool any)
+{
+    DevCsg g = S.csgs[idx];
+    bool merge = g.type == 8;   // POV_OBJ_MERGE
+    bool found = false;
+    for (int c = 0; c < g.count; c++) {
+        DevCsgChild ch = S.csg_children[g.first + c];
+        bool self = skip.x == ref && (int)(skip.y & 0xffffu) == c;
+        float rt[4];
+        int rs[4];
+        int n = child_roots(S, ch, o, d, rt, rs, self, (int)(skip.y >> 16));
+        for (int k = 0; k < n; k++) {
+            if (!(rt[k] >= tmin && rt[k] < t))
+                continue;
+            float3 p = o + d * rt[k];
+            bool keep = true;
+            for (int s = 0; s < g.count && keep; s++) {
+                if (s == c)
+                    continue;
+                bool in = child_inside(S, S.csg_children[g.first + s], p);
+                keep = merge ? !in : in;
+            }
+            if (keep) {
+                t = rt[k];
+                aux = (uint32_t)c | ((uint32_t)rs[k] << 16);
+                found = true;
+                if (any)
+                    return true;
+            }
+        }
+    }
+    return found;
 }
 
 // Triangle: Moller-Trumbore on the precomputed (v0, e1, e2) record.
@@ -232,7 +556,7 @@ __device__ __forceinline__ void node_test(const BvhNode* __restrict__ nodes, int
     float af = fminf(fminf(fmaxf(ax0, ax1), fmaxf(ay0, ay1)), fminf(fmaxf(az0, az1), tmax));
     float bn = fmaxf(fmaxf(fminf(bx0, bx1), fminf(by0, by1)), fmaxf(fminf(bz0, bz1), tmin));
     float bf = fminf(fminf(fmaxf(bx0, bx1), fmaxf(by0, by1)), fminf(fmaxf(bz0, bz1), tmax));
-    // conservative: widen the far side by 3 ulp-ish so rounding never culls
+    // conservative: widen the far side by a few ulp so rounding never culls
     // a box the exact test would enter
     h0 = an <= af * 1.00000024f;
     h1 = bn <= bf * 1.00000024f;
@@ -242,16 +566,90 @@ __device__ __forceinline__ void node_test(const BvhNode* __restrict__ nodes, int
     l1 = __float_as_int(d.y);
 }
 
+// One primitive of a leaf against the ray.  `skip` names the surface the
+// ray starts on (prim ref, aux): in exact arithmetic a ray leaving a plane
+// or a planar triangle never meets it again, one leaving a convex sphere or
+// box meets it only at the far root and only when heading inward, and one
+// leaving a torus loses only its near-zero root; FP32 rounding of the
+// origin must not invent those self-hits (the reference works in FP64).
+template <bool ANY, bool FULL>
+__device__ __forceinline__ bool prim_test(const DeviceScene& S, uint32_t ref, float3 o, float3 d, float tmin,
+                                          float& t, float& bu, float& bv, uint32_t& aux, uint2 skip)
+{
+    uint32_t kind = ref >> PRIM_KIND_SHIFT;
+    uint32_t idx = ref & PRIM_INDEX_MASK;
+    bool self = ref == skip.x;
+    if (kind == PK_TRIANGLE) {
+        if (self)
+            return false;
+        float uu, vv;
+        if (isect_tri(__ldg(S.tri_v0 + idx), __ldg(S.tri_e1 + idx), __ldg(S.tri_e2 + idx), o, d, tmin, t, uu, vv)) {
+            bu = uu;
+            bv = vv;
+            return true;
+        }
+        return false;
+    }
+    if (kind == PK_SPHERE) {
+        float4 s = __ldg(S.spheres + idx);
+        float t1, t2;
+        if (!sphere_roots(s, o, d, t1, t2))
+            return false;
+        if (self) {
+            if (dot3(xyz(s) - o, d) > 0.0f && t2 >= tmin && t2 < t) { t = t2; return true; }
+            return false;
+        }
+        if (t1 > 1.0e-6f && t1 >= tmin && t1 < t) { t = t1; return true; }
+        if (t2 > 1.0e-6f && t2 >= tmin && t2 < t) { t = t2; return true; }
+        return false;
+    }
+    if (kind == PK_BOX) {
+        const DevBox b = S.boxes[idx];
+        float tn, tf;
+        int sn, sf;
+        if (!box_roots(b, o, d, tn, tf, sn, sf))
+            return false;
+        if (self) {
+            if (dot3(box_side_normal((int)skip.y), d) < 0.0f && tf >= tmin && tf < t) { t = tf; aux = sf; return true; }
+            return false;
+        }
+        if (tn > BOX_DEPTH_TOL && tn >= tmin && tn < t) { t = tn; aux = sn; return true; }
+        if (tf >= tmin && tf < t) { t = tf; aux = sf; return true; }
+        return false;
+    }
+    if (!FULL)
+        return false;   // lean variant: the scene has no tori and no CSG
+    if (kind == PK_TORUS) {
+        double r[4];
+        int n = torus_roots(S.tori[idx], o, d, r);
+        if (self)
+            n = torus_drop_self(r, n);
+        bool hit = false;
+        for (int k = 0; k < n; k++) {
+            float tt = (float)r[k];
+            if (tt >= tmin && tt < t) {
+                t = tt;
+                hit = true;
+                if (ANY) break;
+            }
+        }
+        return hit;
+    }
+    if (kind == PK_CSG)
+        return csg_closest(S, idx, o, d, tmin, t, aux, skip, ref, ANY);
+    return false;
+}
+
 // ------------------------------------------------------------- traversal --
 // Closest hit (ANY = false) or any hit (ANY = true) for every ray in the
 // queue.  Stack in shared memory: slot k of thread t at smem[k*blockDim+t].
-template <bool ANY>
+template <bool ANY, bool FULL>
 __global__ void __launch_bounds__(128) k_trace(DeviceScene S, const QRay* __restrict__ q,
                                                const int* __restrict__ q_count, int* __restrict__ work,
                                                QHit* __restrict__ hits, uint8_t* __restrict__ blocked,
                                                int stack_depth, uint32_t* err, unsigned long long* stats,
                                                unsigned long long* wcount, int cap,
-                                               const uint32_t* __restrict__ skips)
+                                               const uint2* __restrict__ skips)
 {
     extern __shared__ int smem[];
     const int lane = threadIdx.x & 31;
@@ -275,17 +673,13 @@ __global__ void __launch_bounds__(128) k_trace(DeviceScene S, const QRay* __rest
         float tmin = r.org.w;
         float t = r.dir.w;
         float3 inv = f3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
-        uint32_t best = 0xffffffffu;
+        uint32_t best = NO_PRIM, baux = 0;
         float bu = 0.f, bv = 0.f;
         bool done = false;
-        // The surface a secondary ray starts on: in exact arithmetic a ray
-        // leaving a plane or a planar triangle never meets it again, and one
-        // leaving a sphere meets it only at the far root; FP32 rounding of the
-        // origin must not invent those self-hits (the reference works in FP64).
-        const uint32_t skip = skips ? skips[i] : 0xffffffffu;
+        const uint2 skip = skips ? skips[i] : make_uint2(NO_PRIM, 0u);
         // infinite objects first (planes: Plane::Intersect, plane.cpp:139-211)
         for (int k = 0; k < S.num_planes; k++) {
-            if (((PK_PLANE << PRIM_KIND_SHIFT) | (uint32_t)k) == skip)
+            if (((PK_PLANE << PRIM_KIND_SHIFT) | (uint32_t)k) == skip.x)
                 continue;
             float4 pl = __ldg(S.planes + k);
             float ndd = pl.x * d.x + pl.y * d.y + pl.z * d.z;
@@ -335,23 +729,11 @@ __global__ void __launch_bounds__(128) k_trace(DeviceScene S, const QRay* __rest
                 uint32_t count = (code & 7u) + 1u;
                 for (uint32_t k = 0; k < count; k++) {
                     uint32_t ref = __ldg(S.prim_refs + first + k);
-                    uint32_t kind = ref >> PRIM_KIND_SHIFT;
-                    uint32_t idx = ref & PRIM_INDEX_MASK;
-                    bool hit = false;
-                    if (counting) { c_prims++; c_tris += kind == PK_TRIANGLE; }
-                    if (ref == skip) {
-                        if (kind == PK_SPHERE)
-                            hit = isect_sphere_far(__ldg(S.spheres + idx), o, d, tmin, t);
-                    } else if (kind == PK_TRIANGLE) {
-                        float uu, vv;
-                        hit = isect_tri(__ldg(S.tri_v0 + idx), __ldg(S.tri_e1 + idx), __ldg(S.tri_e2 + idx), o,
-                                        d, tmin, t, uu, vv);
-                        if (hit) { bu = uu; bv = vv; }
-                    } else if (kind == PK_SPHERE) {
-                        hit = isect_sphere(__ldg(S.spheres + idx), o, d, tmin, t);
-                    }
-                    if (hit) {
+                    if (counting) { c_prims++; c_tris += (ref >> PRIM_KIND_SHIFT) == PK_TRIANGLE; }
+                    uint32_t aux = 0;
+                    if (prim_test<ANY, FULL>(S, ref, o, d, tmin, t, bu, bv, aux, skip)) {
                         best = ref;
+                        baux = aux;
                         if (ANY) { done = true; break; }
                     }
                 }
@@ -367,13 +749,13 @@ __global__ void __launch_bounds__(128) k_trace(DeviceScene S, const QRay* __rest
             QHit h;
             h.t = t;
             h.prim = best;
-            h.u = bu;
+            uint32_t kind = best >> PRIM_KIND_SHIFT;
+            h.u = (kind == PK_TRIANGLE) ? bu : __uint_as_float(baux);
             h.v = bv;
             hits[i] = h;
         }
     }
     if (ANY && stats) {
-        // one atomic per warp
         for (int off = 16; off > 0; off >>= 1)
             nblocked += __shfl_down_sync(0xffffffffu, nblocked, off);
         if (lane == 0 && nblocked)
@@ -400,6 +782,7 @@ struct SurfaceInfo {
     int32_t object;
     int32_t triangle;   // mesh-local triangle, -1 otherwise
     float3  normal;     // raw normal (unflipped)
+    int32_t flags;      // bit0 inverted
 };
 
 __device__ __forceinline__ SurfaceInfo surface(const DeviceScene& S, const QHit& h, float3 p)
@@ -407,7 +790,29 @@ __device__ __forceinline__ SurfaceInfo surface(const DeviceScene& S, const QHit&
     SurfaceInfo si;
     uint32_t kind = h.prim >> PRIM_KIND_SHIFT;
     uint32_t idx = h.prim & PRIM_INDEX_MASK;
+    uint32_t aux = __float_as_uint(h.u);
     si.triangle = -1;
+    si.flags = 0;
+    if (kind == PK_CSG) {
+        DevCsg g = S.csgs[idx];
+        DevCsgChild c = S.csg_children[g.first + (aux & 0xffffu)];
+        kind = c.kind;
+        idx = c.index;
+        aux >>= 16;
+        si.object = c.object;
+        si.flags = c.flags;
+        if (kind == PK_SPHERE) {
+            float4 s = __ldg(S.spheres + idx);
+            si.normal = (p - xyz(s)) * (1.0f / s.w);
+        } else if (kind == PK_BOX) {
+            si.normal = box_side_normal((int)aux);
+        } else if (kind == PK_TORUS) {
+            si.normal = torus_normal(S.tori[idx], p);
+        } else {
+            si.normal = xyz(__ldg(S.planes + idx));
+        }
+        return si;
+    }
     if (kind == PK_SPHERE) {
         float4 s = __ldg(S.spheres + idx);
         si.object = __ldg(S.sphere_obj + idx);
@@ -416,6 +821,16 @@ __device__ __forceinline__ SurfaceInfo surface(const DeviceScene& S, const QHit&
         float4 pl = __ldg(S.planes + idx);
         si.object = __ldg(S.plane_obj + idx);
         si.normal = xyz(pl);
+    } else if (kind == PK_BOX) {
+        DevBox b = S.boxes[idx];
+        si.object = __float_as_int(b.lo.w);
+        si.flags = __float_as_int(b.hi.w);
+        si.normal = box_side_normal((int)aux);    // Box::Normal, box.cpp:600-650
+    } else if (kind == PK_TORUS) {
+        const DevTorus& T = S.tori[idx];
+        si.object = T.object;
+        si.flags = T.flags;
+        si.normal = torus_normal(T, p);           // Torus::Normal, torus.cpp:458-489
     } else {
         int g = __ldg(S.tri_global + idx);
         float4 gn = __ldg(S.tri_normal + g);
@@ -438,14 +853,21 @@ __device__ __forceinline__ SurfaceInfo surface(const DeviceScene& S, const QHit&
     return si;
 }
 
+// aux word a secondary ray carries about the surface it starts on
+__device__ __forceinline__ uint32_t skip_aux(const QHit& h)
+{
+    uint32_t kind = h.prim >> PRIM_KIND_SHIFT;
+    return (kind == PK_BOX || kind == PK_CSG) ? __float_as_uint(h.u) : 0u;
+}
+
 // One thread per ray of the level queue.  Emits shadow rays (one per lit
 // light, slot = ray*num_lights+light) and the reflection ray.
 __global__ void __launch_bounds__(128) k_shade(
     DeviceScene S, int level, const QRay* __restrict__ q, const int* __restrict__ q_path,
     const QHit* __restrict__ hits, const int* __restrict__ q_count, PathState* __restrict__ paths,
     float4* __restrict__ slot_contrib, QRay* __restrict__ sq, int* __restrict__ sq_slot, int* __restrict__ sq_count,
-    uint32_t* __restrict__ sq_skip, QRay* __restrict__ nq, int* __restrict__ nq_path,
-    uint32_t* __restrict__ nq_skip, int* __restrict__ nq_count, int max_queue,
+    uint2* __restrict__ sq_skip, QRay* __restrict__ nq, int* __restrict__ nq_path,
+    uint2* __restrict__ nq_skip, int* __restrict__ nq_count, int max_queue,
     int max_shadow, uint32_t* err, unsigned long long* stats)
 {
     const int n = min(*q_count, max_queue);
@@ -464,12 +886,13 @@ __global__ void __launch_bounds__(128) k_shade(
         PathState ps = paths[path];
         float3 thr = xyz(ps.throughput);
         float weight = ps.throughput.w;
-        bool hit = h.prim != 0xffffffffu;
+        bool hit = h.prim != NO_PRIM;
         float3 col = f3(0.f, 0.f, 0.f);
         float3 p = o + d * h.t;
         float3 N = f3(0.f, 1.f, 0.f);
         const DevMaterial* m = nullptr;
         int oflags = 0;
+        uint2 self = make_uint2(h.prim, skip_aux(h));
         if (hit) {
             SurfaceInfo si = surface(S, h, p);
             ObjectShade os = S.objects[si.object];
@@ -534,7 +957,7 @@ __global__ void __launch_bounds__(128) k_shade(
                     sr.dir = make_float4(ld.x, ld.y, ld.z, ldist - SHADOW_TOLERANCE_F);
                     sq[slot] = sr;
                     sq_slot[slot] = i * nl + l;
-                    sq_skip[slot] = h.prim;
+                    sq_skip[slot] = self;
                 } else {
                     set_error(err, DE_QUEUE_OVERFLOW);
                 }
@@ -575,7 +998,7 @@ __global__ void __launch_bounds__(128) k_shade(
                 rr.dir = make_float4(nd.x, nd.y, nd.z, CUDART_INF_F);
                 nq[rs] = rr;
                 nq_path[rs] = path;
-                nq_skip[rs] = h.prim;
+                nq_skip[rs] = self;
                 paths[path].throughput = make_float4(thr.x * reflec.x, thr.y * reflec.y, thr.z * reflec.z, rweight);
             } else {
                 set_error(err, DE_QUEUE_OVERFLOW);
@@ -600,18 +1023,18 @@ __global__ void __launch_bounds__(128) k_shade(
 // Marks blocked light terms (the any-hit kernel wrote one byte per shadow
 // ray) and adds the remaining terms to their paths in light order.
 __global__ void k_mark_blocked(const int* __restrict__ sq_slot, const uint8_t* __restrict__ blocked,
-                               const int* __restrict__ sq_count, float4* __restrict__ slot_contrib)
+                               const int* __restrict__ sq_count, float4* __restrict__ slot_contrib, int cap)
 {
-    int n = *sq_count;
+    int n = min(*sq_count, cap);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         if (blocked[i])
             slot_contrib[sq_slot[i]].w = 0.0f;
 }
 
 __global__ void k_resolve(const int* __restrict__ q_path, const int* __restrict__ q_count, int num_lights,
-                          const float4* __restrict__ slot_contrib, PathState* __restrict__ paths)
+                          const float4* __restrict__ slot_contrib, PathState* __restrict__ paths, int cap)
 {
-    int n = *q_count;
+    int n = min(*q_count, cap);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         int path = q_path[i];
         float4 c = paths[path].colour;
@@ -627,26 +1050,46 @@ __global__ void k_resolve(const int* __restrict__ q_path, const int* __restrict_
     }
 }
 
-__global__ void k_finalize(const PathState* __restrict__ paths, int npix, float4* __restrict__ out)
+// RGBT of sample i to out[slot ? slot[i] : i] (transmit 0: opaque scenes
+// and a background without alpha, trace.cpp:2874-2887).
+__global__ void k_finalize(const PathState* __restrict__ paths, const int* __restrict__ count, int cap,
+                           const int* __restrict__ slot, float4* __restrict__ out)
 {
+    int n = min(*count, cap);
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < npix) {
+    if (i < n) {
         float4 c = paths[i].colour;
-        out[i] = make_float4(c.x, c.y, c.z, 0.0f);
+        out[slot ? slot[i] : i] = make_float4(c.x, c.y, c.z, 0.0f);
     }
-}
-
-__global__ void k_zero(int* p, int n)
-{
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n)
-        p[i] = 0;
 }
 
 // FP64 re-solve of the winning primitive for rays given in FP64: the depth
 // the reference computes for the same ray (sphere: Sphere::Intersect in
 // double; plane: Plane::Intersect; triangle: intersect_mesh_triangle's
-// plane distance from the stored FP32 normal and Distance, mesh.cpp:1046-1060).
+// plane distance from the stored FP32 normal and Distance, mesh.cpp:1046-1060;
+// box: the slab of the recorded side; torus: its FP64 root as found).
+__device__ __forceinline__ double refine_sphere(float4 s, double ox, double oy, double oz, double dx, double dy,
+                                                double dz, double t)
+{
+    double cx = (double)s.x - ox, cy = (double)s.y - oy, cz = (double)s.z - oz;
+    double tca = cx * dx + cy * dy + cz * dz;
+    double ocs = cx * cx + cy * cy + cz * cz;
+    double th = (double)s.w * (double)s.w - ocs + tca * tca;
+    if (th > 0.0) {
+        double hc = sqrt(th);
+        double t1 = tca - hc, t2 = tca + hc;
+        return fabs(t1 - t) <= fabs(t2 - t) ? t1 : t2;
+    }
+    return t;
+}
+
+__device__ __forceinline__ double refine_box(const DevBox& b, int side, double o[3], double d[3], double t)
+{
+    int ax = side >> 1;
+    double plane = (side & 1) ? (&b.hi.x)[ax] : (&b.lo.x)[ax];
+    return d[ax] != 0.0 ? (plane - o[ax]) / d[ax] : t;
+}
+
 __global__ void k_refine(DeviceScene S, const double* __restrict__ org, const double* __restrict__ dir,
                          const QHit* __restrict__ hits, double* __restrict__ t64, int n)
 {
@@ -655,35 +1098,183 @@ __global__ void k_refine(DeviceScene S, const double* __restrict__ org, const do
         return;
     QHit h = hits[i];
     double t = (double)h.t;
-    if (h.prim != 0xffffffffu) {
-        double ox = org[3 * i], oy = org[3 * i + 1], oz = org[3 * i + 2];
-        double dx = dir[3 * i], dy = dir[3 * i + 1], dz = dir[3 * i + 2];
+    if (h.prim != NO_PRIM) {
+        double o[3] = {org[3 * i], org[3 * i + 1], org[3 * i + 2]};
+        double d[3] = {dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]};
         uint32_t kind = h.prim >> PRIM_KIND_SHIFT, idx = h.prim & PRIM_INDEX_MASK;
+        uint32_t aux = __float_as_uint(h.u);
+        if (kind == PK_CSG) {
+            DevCsg g = S.csgs[idx];
+            DevCsgChild c = S.csg_children[g.first + (aux & 0xffffu)];
+            kind = c.kind;
+            idx = c.index;
+            aux >>= 16;
+        }
         if (kind == PK_SPHERE) {
-            float4 s = S.spheres[idx];
-            double cx = (double)s.x - ox, cy = (double)s.y - oy, cz = (double)s.z - oz;
-            double tca = cx * dx + cy * dy + cz * dz;
-            double ocs = cx * cx + cy * cy + cz * cz;
-            double th = (double)s.w * (double)s.w - ocs + tca * tca;
-            if (th > 0.0) {
-                double hc = sqrt(th);
-                double t1 = tca - hc, t2 = tca + hc;
-                t = (t1 >= 1.0e-4) ? t1 : t2;
-            }
+            t = refine_sphere(S.spheres[idx], o[0], o[1], o[2], d[0], d[1], d[2], t);
         } else if (kind == PK_PLANE) {
             float4 p = S.planes[idx];
-            double ndd = p.x * dx + p.y * dy + p.z * dz;
+            double ndd = p.x * d[0] + p.y * d[1] + p.z * d[2];
             if (ndd != 0.0)
-                t = -((p.x * ox + p.y * oy + p.z * oz) + (double)p.w) / ndd;
+                t = -((p.x * o[0] + p.y * o[1] + p.z * o[2]) + (double)p.w) / ndd;
         } else if (kind == PK_TRIANGLE) {
             int g = S.tri_global[idx];
             float4 nrm = S.tri_normal[g];
-            double ndd = nrm.x * dx + nrm.y * dy + nrm.z * dz;
+            double ndd = nrm.x * d[0] + nrm.y * d[1] + nrm.z * d[2];
             if (ndd != 0.0)
-                t = -((double)S.tri_v0[idx].w + (nrm.x * ox + nrm.y * oy + nrm.z * oz)) / ndd;
+                t = -((double)S.tri_v0[idx].w + (nrm.x * o[0] + nrm.y * o[1] + nrm.z * o[2])) / ndd;
+        } else if (kind == PK_BOX) {
+            t = refine_box(S.boxes[idx], (int)aux, o, d, t);
         }
     }
     t64[i] = t;
+}
+
+// ---------------------------------------------------- adaptive AA (M2) --
+// Per pixel, a (2^depth+1)^2 grid of sub-samples (SubdivisionBuffer,
+// tracetask.cpp:206-233) in `grid`, a claim bitmask in `mask` (one bit per
+// grid point) and a bit per subdivided cell in `subdiv` (cell ids in
+// quadtree order: children of c are 4c+1..4c+4 in the order (-,-), (-,+),
+// (+,-), (+,+) of SubdivideOnePixel's recursion).
+
+// Copies each pixel's four corner colours from the block corner grid.
+__global__ void k_aa_init(const int4* __restrict__ blocks, const int* __restrict__ pix_off,
+                          const int* __restrict__ corner_off, int nblocks, const float4* __restrict__ corners,
+                          int G, int MW, float4* __restrict__ grid, uint32_t* __restrict__ mask,
+                          uint32_t* __restrict__ subdiv, int2* __restrict__ pix_xy, int4* __restrict__ cells,
+                          int* __restrict__ ncells, int root_level)
+{
+    int npix = pix_off[nblocks];
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0)
+        *ncells = npix;
+    if (i >= npix)
+        return;
+    int lo = 0, hi = nblocks - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (pix_off[mid] <= i) lo = mid; else hi = mid - 1;
+    }
+    int4 b = blocks[lo];
+    int w = b.z - b.x + 1;
+    int local = i - pix_off[lo];
+    int lx = local % w, ly = local / w;
+    int cw = w + 1;
+    const float4* cb = corners + corner_off[lo];
+    int S_ = G - 1;
+    float4* g = grid + (size_t)i * G * G;
+    g[0] = cb[ly * cw + lx];
+    g[S_ * G] = cb[(ly + 1) * cw + lx];
+    g[S_] = cb[ly * cw + lx + 1];
+    g[S_ * G + S_] = cb[(ly + 1) * cw + lx + 1];
+    uint32_t* m = mask + (size_t)i * MW;
+    for (int k = 0; k < MW; k++)
+        m[k] = 0u;
+    int corner_bits[4] = {0, S_ * G, S_, S_ * G + S_};
+    for (int k = 0; k < 4; k++)
+        m[corner_bits[k] >> 5] |= 1u << (corner_bits[k] & 31);
+    subdiv[i] = 0u;
+    pix_xy[i] = make_int2(b.x + lx, b.y + ly);
+    // root cell: pixel i, (bx, by) = (0, 0), step S_, level root_level, id 0
+    cells[i] = make_int4(i, 0 | (0 << 8) | (S_ << 16), root_level, 0);
+}
+
+__device__ __forceinline__ float aa_enc(float x) { return powf(fmaxf(x, 0.0f), 1.0f / 2.5f); }
+
+__device__ __forceinline__ float aa_dist(float4 a, float4 b)   // ColourDistanceRGBT on AA-gamma colours
+{
+    return fabsf(aa_enc(a.x) - aa_enc(b.x)) + fabsf(aa_enc(a.y) - aa_enc(b.y)) + fabsf(aa_enc(a.z) - aa_enc(b.z)) +
+           fabsf(a.w - b.w);
+}
+
+// One thread per active cell: subdivide when level > 0 and any of the six
+// corner pairs differs by >= threshold (SubdivideOnePixel's test); claim
+// the five new grid points (first claimant traces it, like the
+// reference's Sampled() check) and emit the four child cells.
+__global__ void k_aa_classify(const int4* __restrict__ cells, const int* __restrict__ ncells, int cap, int G, int MW,
+                              const float4* __restrict__ grid, uint32_t* __restrict__ mask,
+                              uint32_t* __restrict__ subdiv, const int2* __restrict__ pix_xy, double thr,
+                              double subsize, double2* __restrict__ spos, int* __restrict__ sslot,
+                              int* __restrict__ nsamples, int scap, int4* __restrict__ next, int* __restrict__ nnext,
+                              int ncap, uint32_t* err)
+{
+    int n = min(*ncells, cap);
+    for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        int i = base + threadIdx.x;
+        bool active = i < n;
+        unsigned amask = __ballot_sync(0xffffffffu, active);
+        if (!active)
+            continue;
+        int4 c = cells[i];
+        int pix = c.x, bx = c.y & 0xff, by = (c.y >> 8) & 0xff, step = c.y >> 16, level = c.z, id = c.w;
+        const float4* g = grid + (size_t)pix * G * G;
+        float4 c00 = g[by * G + bx], c02 = g[(by + step) * G + bx];
+        float4 c20 = g[by * G + bx + step], c22 = g[(by + step) * G + bx + step];
+        bool split = level > 0 && (aa_dist(c00, c02) >= thr || aa_dist(c00, c20) >= thr || aa_dist(c00, c22) >= thr ||
+                                   aa_dist(c02, c20) >= thr || aa_dist(c02, c22) >= thr || aa_dist(c20, c22) >= thr);
+        int h = step / 2;
+        int gx[5] = {bx, bx + h, bx + step, bx + h, bx + h};
+        int gy[5] = {by + h, by, by + h, by + step, by + h};
+        int2 pxy = pix_xy[pix];
+        for (int k = 0; k < 5; k++) {
+            bool want = false;
+            if (split) {
+                int bit = gy[k] * G + gx[k];
+                uint32_t old = atomicOr(mask + (size_t)pix * MW + (bit >> 5), 1u << (bit & 31));
+                want = !(old & (1u << (bit & 31)));
+            }
+            int s = warp_reserve(nsamples, want, amask);
+            if (want) {
+                if (s < scap) {
+                    spos[s] = make_double2((double)pxy.x + gx[k] / subsize, (double)pxy.y + gy[k] / subsize);
+                    sslot[s] = pix * G * G + gy[k] * G + gx[k];
+                } else {
+                    set_error(err, DE_QUEUE_OVERFLOW);
+                }
+            }
+        }
+        int nb = warp_reserve_k(nnext, split, 4, amask);
+        if (split) {
+            atomicOr(subdiv + pix, 1u << id);
+            if (nb + 4 <= ncap) {
+                next[nb + 0] = make_int4(pix, bx | (by << 8) | (h << 16), level - 1, 4 * id + 1);
+                next[nb + 1] = make_int4(pix, bx | ((by + h) << 8) | (h << 16), level - 1, 4 * id + 2);
+                next[nb + 2] = make_int4(pix, (bx + h) | (by << 8) | (h << 16), level - 1, 4 * id + 3);
+                next[nb + 3] = make_int4(pix, (bx + h) | ((by + h) << 8) | (h << 16), level - 1, 4 * id + 4);
+            } else {
+                set_error(err, DE_QUEUE_OVERFLOW);
+            }
+        }
+    }
+}
+
+// Bottom-up pixel colour: a subdivided cell is the mean of its four
+// children (rcx0y0 + rcx0y1 + rcx1y0 + rcx1y1) / 4, a leaf cell the mean of
+// its corners (cx0y0 + cx0y2 + cx2y0 + cx2y2) / 4 (tracetask.cpp:1058-1062).
+__device__ float4 aa_cell(const float4* g, int G, uint32_t bits, int id, int bx, int by, int step, int depth_left)
+{
+    if (depth_left > 0 && id < 32 && ((bits >> id) & 1u)) {
+        int h = step / 2;
+        float4 a = aa_cell(g, G, bits, 4 * id + 1, bx, by, h, depth_left - 1);
+        float4 b = aa_cell(g, G, bits, 4 * id + 2, bx, by + h, h, depth_left - 1);
+        float4 c = aa_cell(g, G, bits, 4 * id + 3, bx + h, by, h, depth_left - 1);
+        float4 d = aa_cell(g, G, bits, 4 * id + 4, bx + h, by + h, h, depth_left - 1);
+        return make_float4((a.x + b.x + c.x + d.x) / 4.0f, (a.y + b.y + c.y + d.y) / 4.0f,
+                           (a.z + b.z + c.z + d.z) / 4.0f, (a.w + b.w + c.w + d.w) / 4.0f);
+    }
+    float4 a = g[by * G + bx], b = g[(by + step) * G + bx], c = g[by * G + bx + step],
+           d = g[(by + step) * G + bx + step];
+    return make_float4((a.x + b.x + c.x + d.x) / 4.0f, (a.y + b.y + c.y + d.y) / 4.0f,
+                       (a.z + b.z + c.z + d.z) / 4.0f, (a.w + b.w + c.w + d.w) / 4.0f);
+}
+
+__global__ void k_aa_resolve(const float4* __restrict__ grid, const uint32_t* __restrict__ subdiv, int npix, int G,
+                             int depth, float4* __restrict__ out)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= npix)
+        return;
+    out[i] = aa_cell(grid + (size_t)i * G * G, G, subdiv[i], 0, 0, 0, G - 1, depth - 1);
 }
 
 // --------------------------------------------------------------- launch --
@@ -696,12 +1287,14 @@ cudaError_t launch_refine(const DeviceScene& S, const double* org, const double*
     return cudaGetLastError();
 }
 
-cudaError_t launch_camera(const DeviceScene& S, const int4* blocks, const int* block_off, int nblocks, int npix,
-                          int width, int height, QRay* q, int* q_path, PathState* paths, int* q_count,
-                          unsigned long long* stats, uint32_t* q_skip, cudaStream_t st)
+cudaError_t launch_camera(const DeviceScene& S, int mode, const int4* blocks, const int* block_off, int nblocks,
+                          const double2* pos, const int* npos, int max_samples, int width, int height, QRay* q,
+                          int* q_path, PathState* paths, int* q_count, unsigned long long* stats, uint2* q_skip,
+                          cudaStream_t st)
 {
-    k_camera<<<cdiv(npix > 0 ? npix : 1, 256), 256, 0, st>>>(S, blocks, block_off, nblocks, width, height, q,
-                                                             q_path, paths, q_count, stats, q_skip);
+    k_camera<<<cdiv(max_samples > 0 ? max_samples : 1, 256), 256, 0, st>>>(
+        S, mode, blocks, block_off, nblocks, pos, npos, width, height, q, q_path, paths, q_count, stats, q_skip,
+        max_samples);
     return cudaGetLastError();
 }
 
@@ -713,23 +1306,32 @@ cudaError_t launch_load_rays(const double* org, const double* dir, int n, QRay* 
 
 cudaError_t launch_trace(const DeviceScene& S, bool any_hit, const QRay* q, const int* q_count, int* work,
                          QHit* hits, uint8_t* blocked, int stack_depth, int grid, uint32_t* err,
-                         unsigned long long* stats, unsigned long long* wcount, int cap, const uint32_t* skips,
+                         unsigned long long* stats, unsigned long long* wcount, int cap, const uint2* skips,
                          cudaStream_t st)
 {
     const int block = 128;
     size_t smem = (size_t)stack_depth * block * sizeof(int);
-    if (any_hit)
-        k_trace<true><<<grid, block, smem, st>>>(S, q, q_count, work, hits, blocked, stack_depth, err, stats,
-                                                 wcount, cap, skips);
+    // the full variant carries the FP64 torus solver and CSG; scenes without
+    // them run the lean one (about half the registers)
+    const bool full = S.has_full_prims != 0;
+    if (any_hit && full)
+        k_trace<true, true><<<grid, block, smem, st>>>(S, q, q_count, work, hits, blocked, stack_depth, err, stats,
+                                                       wcount, cap, skips);
+    else if (any_hit)
+        k_trace<true, false><<<grid, block, smem, st>>>(S, q, q_count, work, hits, blocked, stack_depth, err, stats,
+                                                        wcount, cap, skips);
+    else if (full)
+        k_trace<false, true><<<grid, block, smem, st>>>(S, q, q_count, work, hits, blocked, stack_depth, err,
+                                                        stats, wcount, cap, skips);
     else
-        k_trace<false><<<grid, block, smem, st>>>(S, q, q_count, work, hits, blocked, stack_depth, err, stats,
-                                                  wcount, cap, skips);
+        k_trace<false, false><<<grid, block, smem, st>>>(S, q, q_count, work, hits, blocked, stack_depth, err,
+                                                         stats, wcount, cap, skips);
     return cudaGetLastError();
 }
 
 cudaError_t launch_shade(const DeviceScene& S, int level, const QRay* q, const int* q_path, const QHit* hits,
                          const int* q_count, PathState* paths, float4* slot_contrib, QRay* sq, int* sq_slot,
-                         int* sq_count, uint32_t* sq_skip, QRay* nq, int* nq_path, uint32_t* nq_skip, int* nq_count,
+                         int* sq_count, uint2* sq_skip, QRay* nq, int* nq_path, uint2* nq_skip, int* nq_count,
                          int max_queue, int max_shadow, int grid, uint32_t* err, unsigned long long* stats,
                          cudaStream_t st)
 {
@@ -740,22 +1342,43 @@ cudaError_t launch_shade(const DeviceScene& S, int level, const QRay* q, const i
 
 cudaError_t launch_resolve(const int* q_path, const int* q_count, int num_lights, const int* sq_slot,
                            const uint8_t* blocked, const int* sq_count, float4* slot_contrib, PathState* paths,
-                           int grid, cudaStream_t st)
+                           int grid, int cap_rays, int cap_shadow, cudaStream_t st)
 {
-    k_mark_blocked<<<grid, 256, 0, st>>>(sq_slot, blocked, sq_count, slot_contrib);
-    k_resolve<<<grid, 256, 0, st>>>(q_path, q_count, num_lights, slot_contrib, paths);
+    k_mark_blocked<<<grid, 256, 0, st>>>(sq_slot, blocked, sq_count, slot_contrib, cap_shadow);
+    k_resolve<<<grid, 256, 0, st>>>(q_path, q_count, num_lights, slot_contrib, paths, cap_rays);
     return cudaGetLastError();
 }
 
-cudaError_t launch_finalize(const PathState* paths, int npix, float4* out, cudaStream_t st)
+cudaError_t launch_finalize(const PathState* paths, const int* count, int max_samples, const int* slot, float4* out,
+                            cudaStream_t st)
 {
-    k_finalize<<<cdiv(npix > 0 ? npix : 1, 256), 256, 0, st>>>(paths, npix, out);
+    k_finalize<<<cdiv(max_samples > 0 ? max_samples : 1, 256), 256, 0, st>>>(paths, count, max_samples, slot, out);
     return cudaGetLastError();
 }
 
-cudaError_t launch_zero(int* p, int n, cudaStream_t st)
+cudaError_t launch_aa_init(const int4* blocks, const int* pix_off, const int* corner_off, int nblocks, int npix,
+                           const float4* corners, int G, int MW, float4* grid, uint32_t* mask, uint32_t* subdiv,
+                           int2* pix_xy, int4* cells, int* ncells, int root_level, cudaStream_t st)
 {
-    k_zero<<<cdiv(n, 256), 256, 0, st>>>(p, n);
+    k_aa_init<<<cdiv(npix > 0 ? npix : 1, 256), 256, 0, st>>>(blocks, pix_off, corner_off, nblocks, corners, G, MW,
+                                                               grid, mask, subdiv, pix_xy, cells, ncells, root_level);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_aa_classify(const int4* cells, const int* ncells, int cap, int G, int MW, const float4* grid,
+                               uint32_t* mask, uint32_t* subdiv, const int2* pix_xy, double thr, double subsize,
+                               double2* spos, int* sslot, int* nsamples, int scap, int4* next, int* nnext, int ncap,
+                               uint32_t* err, int grid_blocks, cudaStream_t st)
+{
+    k_aa_classify<<<grid_blocks, 128, 0, st>>>(cells, ncells, cap, G, MW, grid, mask, subdiv, pix_xy, thr, subsize,
+                                                spos, sslot, nsamples, scap, next, nnext, ncap, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_aa_resolve(const float4* grid, const uint32_t* subdiv, int npix, int G, int depth, float4* out,
+                              cudaStream_t st)
+{
+    k_aa_resolve<<<cdiv(npix > 0 ? npix : 1, 128), 128, 0, st>>>(grid, subdiv, npix, G, depth, out);
     return cudaGetLastError();
 }
 

@@ -5,25 +5,36 @@
 
 namespace povgpu {
 
-cudaError_t launch_camera(const DeviceScene& S, const int4* blocks, const int* block_off, int nblocks, int npix,
-                          int width, int height, QRay* q, int* q_path, PathState* paths, int* q_count,
-                          unsigned long long* stats, uint32_t* q_skip, cudaStream_t st);
+// mode 0: pixel centres per block, 1: block corners, 2: explicit positions
+cudaError_t launch_camera(const DeviceScene& S, int mode, const int4* blocks, const int* block_off, int nblocks,
+                          const double2* pos, const int* npos, int max_samples, int width, int height, QRay* q,
+                          int* q_path, PathState* paths, int* q_count, unsigned long long* stats, uint2* q_skip,
+                          cudaStream_t st);
 cudaError_t launch_load_rays(const double* org, const double* dir, int n, QRay* q, int* q_count, cudaStream_t st);
 cudaError_t launch_trace(const DeviceScene& S, bool any_hit, const QRay* q, const int* q_count, int* work,
                          QHit* hits, uint8_t* blocked, int stack_depth, int grid, uint32_t* err,
-                         unsigned long long* stats, unsigned long long* wcount, int cap, const uint32_t* skips,
+                         unsigned long long* stats, unsigned long long* wcount, int cap, const uint2* skips,
                          cudaStream_t st);
 cudaError_t launch_shade(const DeviceScene& S, int level, const QRay* q, const int* q_path, const QHit* hits,
                          const int* q_count, PathState* paths, float4* slot_contrib, QRay* sq, int* sq_slot,
-                         int* sq_count, uint32_t* sq_skip, QRay* nq, int* nq_path, uint32_t* nq_skip, int* nq_count,
+                         int* sq_count, uint2* sq_skip, QRay* nq, int* nq_path, uint2* nq_skip, int* nq_count,
                          int max_queue, int max_shadow, int grid, uint32_t* err, unsigned long long* stats,
                          cudaStream_t st);
 cudaError_t launch_resolve(const int* q_path, const int* q_count, int num_lights, const int* sq_slot,
                            const uint8_t* blocked, const int* sq_count, float4* slot_contrib, PathState* paths,
-                           int grid, cudaStream_t st);
-cudaError_t launch_finalize(const PathState* paths, int npix, float4* out, cudaStream_t st);
-cudaError_t launch_zero(int* p, int n, cudaStream_t st);
+                           int grid, int cap_rays, int cap_shadow, cudaStream_t st);
+cudaError_t launch_finalize(const PathState* paths, const int* count, int max_samples, const int* slot, float4* out,
+                            cudaStream_t st);
 cudaError_t launch_refine(const DeviceScene& S, const double* org, const double* dir, QHit* hits, double* t64, int n,
                           cudaStream_t st);
+cudaError_t launch_aa_init(const int4* blocks, const int* pix_off, const int* corner_off, int nblocks, int npix,
+                           const float4* corners, int G, int MW, float4* grid, uint32_t* mask, uint32_t* subdiv,
+                           int2* pix_xy, int4* cells, int* ncells, int root_level, cudaStream_t st);
+cudaError_t launch_aa_classify(const int4* cells, const int* ncells, int cap, int G, int MW, const float4* grid,
+                               uint32_t* mask, uint32_t* subdiv, const int2* pix_xy, double thr, double subsize,
+                               double2* spos, int* sslot, int* nsamples, int scap, int4* next, int* nnext, int ncap,
+                               uint32_t* err, int grid_blocks, cudaStream_t st);
+cudaError_t launch_aa_resolve(const float4* grid, const uint32_t* subdiv, int npix, int G, int depth, float4* out,
+                              cudaStream_t st);
 
 }  // namespace povgpu

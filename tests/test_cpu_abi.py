@@ -109,3 +109,27 @@ def test_null_arguments(gpu_lib):
     assert gpu_lib.pov_gpu_trace_blocks(None, None, 0, None, None, None) == abi.POV_GPU_E_INVALID
     assert gpu_lib.pov_gpu_trace_rays(None, None, None, 0, None) == abi.POV_GPU_E_INVALID
     gpu_lib.pov_gpu_scene_destroy(None)
+
+
+def test_csg_validation(gpu_lib):
+    """CSG: leaf children only; a mesh child or nested CSG is unsupported."""
+    s = scenes.csg_torus_grid(32, 18, n=2, antialias=None)
+    desc, keep = s.desc()
+    assert desc.objects[0].type == abi.POV_OBJ_INTERSECTION and desc.objects[1].parent == 0
+    desc.objects[1].type = abi.POV_OBJ_MESH
+    desc.objects[1].mesh = 0
+    st, bad = _create(gpu_lib, desc)
+    assert st in (abi.POV_GPU_E_INVALID, abi.POV_GPU_E_UNSUPPORTED)
+    desc, keep = s.desc()
+    desc.objects[2].parent = 5           # child pointing at the wrong parent
+    st, bad = _create(gpu_lib, desc)
+    assert st == abi.POV_GPU_E_INVALID
+
+
+def test_torus_requires_its_transform(gpu_lib):
+    s = scenes.csg_torus_grid(32, 18, n=2, antialias=None)
+    desc, keep = s.desc()
+    tor = [i for i in range(desc.num_objects) if desc.objects[i].type == abi.POV_OBJ_TORUS][0]
+    desc.objects[tor].flags &= ~abi.POV_FLAG_HAS_TRANS
+    st, bad = _create(gpu_lib, desc)
+    assert st == abi.POV_GPU_E_UNSUPPORTED and bad == tor
