@@ -33,8 +33,24 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-WORKLOAD = ("mesh_spheres: 1920x1080 1spp, 1,051,392-tri displaced-sphere mesh2 + 1024 spheres + plane, "
-            "1 point light w/ shadows, reflection 0.3, max_trace_level 3")
+WORKLOADS = {
+    "mesh_spheres": "mesh_spheres: %dx%d 1spp, 1,051,392-tri displaced-sphere mesh2 + 1024 spheres + plane, "
+                    "1 point light w/ shadows, reflection 0.3, max_trace_level 3",
+    "csg_torus_grid": "csg_torus_grid: %dx%d, 4096 objects (difference/intersection/merge CSG + FP64 tori), "
+                      "adaptive AA method 2 thr 0.1 depth 3, 2 lights w/ shadows, reflection 0.2, max_trace_level 4",
+    "spheres_plane": "spheres_plane: %dx%d 1spp, 64 spheres + plane, 2 lights w/ shadows, phong 0.5",
+}
+
+
+def make_scene(args):
+    from povray_gb300 import scenes
+    return scenes.WORKLOADS[args.workload](args.width, args.height)
+
+
+def workload_name(args):
+    return WORKLOADS[args.workload] % (args.width, args.height)
+
+
 METRIC = "Mrays/s (primary+shadow)"
 
 
@@ -46,6 +62,7 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
+    ap.add_argument("--workload", default="mesh_spheres", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
 
@@ -139,7 +156,7 @@ def run_reference(args, rank, world):
         return
     from oracle.pyoracle import Oracle
     from povray_gb300 import scenes
-    s = scenes.mesh_spheres(args.width, args.height)
+    s = make_scene(args)
     orc = Oracle(s)
     band = max(8, args.height // 10)
     def step(i):
@@ -162,7 +179,7 @@ def run_reference(args, rank, world):
         "impl": "reference", "metric": METRIC, "value": v, "unit": "Mrays/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": tt / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD},
+        "config": {"workload": workload_name(args)},
         "cpu_baseline": {"value": v, "unit": "Mrays/s", "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
@@ -183,7 +200,7 @@ def main():
     from povray_gb300 import GpuScene, scenes
     from povray_gb300.abi import STAGE_NAMES  # noqa: F401
 
-    s = scenes.mesh_spheres(args.width, args.height)
+    s = make_scene(args)
     gpu = GpuScene(s)
     stream = torch.cuda.current_stream()
     gpu.set_stream(stream.cuda_stream)
@@ -280,7 +297,7 @@ def main():
         "warmup": args.warmup, "ms_per_step": t_total / args.steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (fp64 grazing re-solve, fp64 camera)",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "l2": "flushed between steps (256 MiB write, outside timed events)",
+        "config": {"workload": workload_name(args), "l2": "flushed between steps (256 MiB write, outside timed events)",
                    "rays_per_frame": rays // args.steps, "parallelism": "replica per GPU" if world > 1 else "1 GPU"},
         "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": len(blocks) * 16 + (len(blocks) + 1) * 4,
                 "d2h_bytes_per_step": npix * 16},

@@ -284,7 +284,7 @@ struct PovGpuScene {
     int         num_sms = 148;
     // persistent scene data
     DevBuf nodes, refs, tri_v0, tri_e1, tri_e2, tri_global, tri_shade, tri_normal, tri_local, normals;
-    DevBuf spheres, sphere_obj, sphere_flags, planes, plane_obj, boxes, tori, csgs, csg_children, objects,
+    DevBuf spheres, spheres64, boxes64, sphere_obj, sphere_flags, planes, plane_obj, boxes, tori, csgs, csg_children, objects,
         materials, lights;
     // host copies of the id maps (prim -> flattened object id)
     std::vector<int32_t> h_sphere_obj, h_plane_obj, h_box_obj, h_torus_obj, h_tri_global, h_tri_local, h_tri_obj;
@@ -312,7 +312,7 @@ struct PovGpuScene {
             cudaEventDestroy(e);
         events.clear();
         DevBuf* all[] = {&nodes, &refs, &tri_v0, &tri_e1, &tri_e2, &tri_global, &tri_shade, &tri_normal, &tri_local,
-                         &normals, &spheres, &sphere_obj, &sphere_flags, &planes, &plane_obj, &boxes, &tori, &csgs,
+                         &normals, &spheres, &spheres64, &boxes64, &sphere_obj, &sphere_flags, &planes, &plane_obj, &boxes, &tori, &csgs,
                          &csg_children, &objects, &materials, &lights, &blocks, &block_off, &corner_off, &qA, &qB,
                          &pathA, &pathB, &hits, &paths, &slot_contrib, &sq, &sq_slot, &blocked, &out, &counters,
                          &stats, &err, &rays_in, &skipA, &skipB, &sskip, &t64, &corners, &aa_grid, &aa_mask,
@@ -436,6 +436,7 @@ DevMaterial make_material(const PovGpuMaterial& m, const float* ambient_light)
 struct Builder {
     BvhBuilder bvh;
     std::vector<float4> spheres, planes, tri_v0, tri_e1, tri_e2, tri_normal, normals;
+    std::vector<double> spheres64, boxes64;
     std::vector<int32_t> sphere_obj, sphere_flags, plane_obj, tri_global, tri_local, box_obj, torus_obj;
     std::vector<int4> tri_shade;
     std::vector<DevBox> boxes;
@@ -447,6 +448,7 @@ struct Builder {
     {
         int idx = (int)spheres.size();
         spheres.push_back(make_float4((float)o.p[0], (float)o.p[1], (float)o.p[2], (float)o.p[3]));
+        spheres64.insert(spheres64.end(), {o.p[0], o.p[1], o.p[2], o.p[3]});
         sphere_obj.push_back(id);
         sphere_flags.push_back(o.flags & POV_FLAG_INVERTED ? 1 : 0);
         if (box)
@@ -464,6 +466,7 @@ struct Builder {
         b.hi = make_float4((float)o.p[3], (float)o.p[4], (float)o.p[5],
                            __builtin_bit_cast(float, (int32_t)(o.flags & POV_FLAG_INVERTED ? 1 : 0)));
         boxes.push_back(b);
+        boxes64.insert(boxes64.end(), {o.p[0], o.p[1], o.p[2], o.p[3], o.p[4], o.p[5]});
         box_obj.push_back(id);
         if (box) {
             grow_outward(*box, o.p[0], o.p[1], o.p[2]);
@@ -725,6 +728,8 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
     CK(upload(sc->tri_local, B.tri_local));
     CK(upload(sc->normals, B.normals));
     CK(upload(sc->spheres, B.spheres));
+    CK(upload(sc->spheres64, B.spheres64));
+    CK(upload(sc->boxes64, B.boxes64));
     CK(upload(sc->sphere_obj, B.sphere_obj));
     CK(upload(sc->sphere_flags, B.sphere_flags));
     CK(upload(sc->planes, B.planes));
@@ -772,6 +777,8 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
     S.csgs = sc->csgs.as<DevCsg>();
     S.csg_children = sc->csg_children.as<DevCsgChild>();
     S.has_full_prims = (!B.tori.empty() || !B.csgs.empty()) ? 1 : 0;
+    S.spheres64 = sc->spheres64.as<double>();
+    S.boxes64 = sc->boxes64.as<double>();
     S.objects = sc->objects.as<ObjectShade>();
     S.materials = sc->materials.as<DevMaterial>();
     S.lights = sc->lights.as<DevLight>();

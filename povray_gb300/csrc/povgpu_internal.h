@@ -135,6 +135,10 @@ struct DeviceScene {
     const DevCsgChild* csg_children;
     const int32_t*     sphere_flags;   // bit0 inverted (spheres inside CSG)
     int32_t            has_full_prims; // tori or CSG present: full traversal variant
+    // FP64 geometry as the parser stores it, read only by the parity
+    // re-solve (k_refine): centre+radius per sphere, 6 corners per box
+    const double*      spheres64;
+    const double*      boxes64;
     // objects, materials, lights
     const ObjectShade* objects;
     const DevMaterial* materials;

@@ -344,7 +344,7 @@ __device__ __forceinline__ double3 torus_local_point(const DevTorus& T, double x
 }
 
 // Roots (world depths) with depth > 1e-4; returns their count (<= 4).
-__device__ __noinline__ int torus_roots(const DevTorus& T, float3 o, float3 d, double* out)
+__device__ __noinline__ int torus_roots(const DevTorus& T, double3 o, double3 d, double* out)
 {
     const double* m = T.inv;
     double3 P = torus_local_point(T, o.x, o.y, o.z);
@@ -458,7 +458,7 @@ __device__ __forceinline__ int child_roots(const DeviceScene& S, const DevCsgChi
         }
     } else if (c.kind == PK_TORUS) {
         double r[4];
-        int k = torus_roots(S.tori[c.index], o, d, r);
+        int k = torus_roots(S.tori[c.index], make_double3(o.x, o.y, o.z), make_double3(d.x, d.y, d.z), r);
         if (self) k = torus_drop_self(r, k);
         for (int i = 0; i < k; i++) { t[n] = (float)r[i]; side[n++] = 0; }
     } else if (c.kind == PK_PLANE) {
@@ -621,7 +621,7 @@ __device__ __forceinline__ bool prim_test(const DeviceScene& S, uint32_t ref, fl
         return false;   // lean variant: the scene has no tori and no CSG
     if (kind == PK_TORUS) {
         double r[4];
-        int n = torus_roots(S.tori[idx], o, d, r);
+        int n = torus_roots(S.tori[idx], make_double3(o.x, o.y, o.z), make_double3(d.x, d.y, d.z), r);
         if (self)
             n = torus_drop_self(r, n);
         bool hit = false;
@@ -1068,13 +1068,13 @@ __global__ void k_finalize(const PathState* __restrict__ paths, const int* __res
 // double; plane: Plane::Intersect; triangle: intersect_mesh_triangle's
 // plane distance from the stored FP32 normal and Distance, mesh.cpp:1046-1060;
 // box: the slab of the recorded side; torus: its FP64 root as found).
-__device__ __forceinline__ double refine_sphere(float4 s, double ox, double oy, double oz, double dx, double dy,
+__device__ __forceinline__ double refine_sphere(const double* s, double ox, double oy, double oz, double dx, double dy,
                                                 double dz, double t)
 {
-    double cx = (double)s.x - ox, cy = (double)s.y - oy, cz = (double)s.z - oz;
+    double cx = s[0] - ox, cy = s[1] - oy, cz = s[2] - oz;
     double tca = cx * dx + cy * dy + cz * dz;
     double ocs = cx * cx + cy * cy + cz * cz;
-    double th = (double)s.w * (double)s.w - ocs + tca * tca;
+    double th = s[3] * s[3] - ocs + tca * tca;
     if (th > 0.0) {
         double hc = sqrt(th);
         double t1 = tca - hc, t2 = tca + hc;
@@ -1083,10 +1083,10 @@ __device__ __forceinline__ double refine_sphere(float4 s, double ox, double oy, 
     return t;
 }
 
-__device__ __forceinline__ double refine_box(const DevBox& b, int side, double o[3], double d[3], double t)
+__device__ __forceinline__ double refine_box(const double* b, int side, double o[3], double d[3], double t)
 {
     int ax = side >> 1;
-    double plane = (side & 1) ? (&b.hi.x)[ax] : (&b.lo.x)[ax];
+    double plane = b[(side & 1) ? 3 + ax : ax];
     return d[ax] != 0.0 ? (plane - o[ax]) / d[ax] : t;
 }
 
@@ -1111,7 +1111,7 @@ __global__ void k_refine(DeviceScene S, const double* __restrict__ org, const do
             aux >>= 16;
         }
         if (kind == PK_SPHERE) {
-            t = refine_sphere(S.spheres[idx], o[0], o[1], o[2], d[0], d[1], d[2], t);
+            t = refine_sphere(S.spheres64 + 4 * idx, o[0], o[1], o[2], d[0], d[1], d[2], t);
         } else if (kind == PK_PLANE) {
             float4 p = S.planes[idx];
             double ndd = p.x * d[0] + p.y * d[1] + p.z * d[2];
@@ -1124,7 +1124,15 @@ __global__ void k_refine(DeviceScene S, const double* __restrict__ org, const do
             if (ndd != 0.0)
                 t = -((double)S.tri_v0[idx].w + (nrm.x * o[0] + nrm.y * o[1] + nrm.z * o[2])) / ndd;
         } else if (kind == PK_BOX) {
-            t = refine_box(S.boxes[idx], (int)aux, o, d, t);
+            t = refine_box(S.boxes64 + 6 * idx, (int)aux, o, d, t);
+        } else if (kind == PK_TORUS) {
+            double r[4];
+            int k = torus_roots(S.tori[idx], make_double3(o[0], o[1], o[2]), make_double3(d[0], d[1], d[2]), r);
+            double best = t;
+            for (int j = 0; j < k; j++)
+                if (fabs(r[j] - t) < fabs(best - t) || best == t)
+                    best = r[j];
+            t = best;
         }
     }
     t64[i] = t;

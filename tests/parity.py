@@ -57,6 +57,13 @@ def compare_hits(got_obj, got_tri, got_t, ref_obj, ref_tri, ref_t, oracle=None, 
         graz |= tie
     same = ~mism & (ref_obj >= 0)
     rel = np.abs(np.asarray(got_t)[same] - np.asarray(ref_t)[same]) / np.maximum(np.abs(np.asarray(ref_t)[same]), 1e-12)
+    worst = []
+    if rel.size:
+        sidx = np.nonzero(same)[0]
+        for k in np.argsort(-rel)[:8]:
+            if rel[k] > t_tol:
+                j = int(sidx[k])
+                worst.append((j, int(ref_obj[j]), float(np.asarray(ref_t)[j]), float(np.asarray(got_t)[j])))
     return {
         "rays": int(len(ref_obj)),
         "mismatch": int(len(idx)),
@@ -64,6 +71,7 @@ def compare_hits(got_obj, got_tri, got_t, ref_obj, ref_tri, ref_t, oracle=None, 
         "bad": int((~graz).sum()),
         "t_max_rel": float(rel.max()) if rel.size else 0.0,
         "t_bad": int((rel > t_tol).sum()),
+        "worst_t": worst,   # (ray, object, reference t, got t)
     }
 
 

@@ -54,8 +54,8 @@ def test_hits_match_reference_golden(case):
     h = gpu.trace_rays(g["ray_org"], g["ray_dir"])
     r = compare_hits(h["object"], h["triangle"], h["t"], g["hit_object"], g["hit_triangle"], g["hit_t"],
                      oracle=Oracle(scene), org=g["ray_org"], dirs=g["ray_dir"], t_tol=T_TOL)
-    assert r["bad"] == 0, r
-    assert r["t_bad"] == 0, r
+    assert r["bad"] == 0, json.dumps(r)
+    assert r["t_bad"] == 0, json.dumps(r)
     assert r["mismatch"] <= 0.001 * r["rays"], r
 
 
@@ -128,7 +128,7 @@ def test_primary_hits_full_mesh_match_oracle():
     h = GpuScene(s).trace_rays(o, d)
     r = compare_hits(h["object"], h["triangle"], h["t"], ref["object"], ref["triangle"], ref["t"],
                      oracle=orc, org=o, dirs=d, t_tol=T_TOL)
-    assert r["bad"] == 0 and r["t_bad"] == 0, r
+    assert r["bad"] == 0 and r["t_bad"] == 0, json.dumps(r)
 
 
 def test_full_size_render_is_deterministic_and_block_invariant():
