@@ -43,6 +43,7 @@ extern "C" {
 #define POV_GPU_E_NOMEM        -5  /* device allocation failed                 */
 #define POV_GPU_E_DEVICE       -6  /* a kernel raised its device error word    */
 #define POV_GPU_E_NODEVICE     -7  /* no CUDA device visible                   */
+#define POV_GPU_E_CAPACITY     -8  /* request above a fixed scratch capacity   */
 
 /* ---- object types (subset of the reference's ObjectBase zoo) ------------ */
 #define POV_OBJ_SPHERE        1   /* source/core/shape/sphere.cpp   */
@@ -283,6 +284,30 @@ int pov_gpu_trace_blocks(PovGpuScene* scene, const PovGpuBlock* blocks, int32_t 
  */
 int pov_gpu_trace_rays(PovGpuScene* scene, const double* origins, const double* directions,
                        int32_t num_rays, PovGpuHit* hits);
+
+/*
+ * pov_gpu_trace_rays without any device allocation.  No counterpart in the
+ * reference: FindIntersection allocates nothing, and this entry gives the
+ * same guarantee to callers that cannot allocate device memory --
+ * integrations whose device memory is committed to another allocator (a
+ * caching allocator holding the rest of HBM makes cudaMalloc fail although
+ * the caller has room), and render threads sharing the GPU with frames in
+ * flight, where cudaFree would synchronise the whole device.
+ *
+ * Same arguments and results as pov_gpu_trace_rays (objects, triangles and
+ * depths are identical).  Its scratch is a fixed device array of the
+ * library, 7.5 MiB per device, holding at most POV_GPU_STATIC_MAX_RAYS rays;
+ * num_rays above that returns POV_GPU_E_CAPACITY and touches nothing.
+ * The first call on a device does a one-time set-up (it looks up that
+ * array's device address, which can make CUDA load the library's device
+ * code there); make that call, e.g. with num_rays = 0, before any stream
+ * capture.  The array's header (counters, error word, statistics) is zeroed
+ * by every call.  There is one array per device: calls that overlap in time
+ * on one device, from different threads or scenes, race on it.
+ */
+#define POV_GPU_STATIC_MAX_RAYS 65536
+int pov_gpu_trace_rays_static(PovGpuScene* scene, const double* origins, const double* directions,
+                              int32_t num_rays, PovGpuHit* hits);
 
 /* Releases all device memory of the scene. */
 void pov_gpu_scene_destroy(PovGpuScene* scene);

@@ -19,6 +19,9 @@ POV_GPU_E_TIMEOUT = -4
 POV_GPU_E_NOMEM = -5
 POV_GPU_E_DEVICE = -6
 POV_GPU_E_NODEVICE = -7
+POV_GPU_E_CAPACITY = -8
+
+POV_GPU_STATIC_MAX_RAYS = 65536
 
 POV_OBJ_SPHERE = 1
 POV_OBJ_PLANE = 2
@@ -156,7 +159,8 @@ STRUCTS = {
 # Entry points that include/povgpu.h declares (checked by the CPU tests).
 EXPORTS = ["pov_gpu_scene_create", "pov_gpu_trace_blocks", "pov_gpu_trace_rays",
            "pov_gpu_scene_destroy", "pov_gpu_error_string", "pov_gpu_abi_version",
-           "pov_gpu_scene_set_stream", "pov_gpu_set_profiling", "pov_gpu_get_timings"]
+           "pov_gpu_scene_set_stream", "pov_gpu_set_profiling", "pov_gpu_get_timings",
+           "pov_gpu_trace_rays_static"]
 
 
 class PovGpuError(RuntimeError):
@@ -188,6 +192,9 @@ def load_library(path=None):
     lib.pov_gpu_trace_rays.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
                                        C.POINTER(PovGpuHit)]
     lib.pov_gpu_trace_rays.restype = C.c_int
+    lib.pov_gpu_trace_rays_static.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
+                                              C.POINTER(PovGpuHit)]
+    lib.pov_gpu_trace_rays_static.restype = C.c_int
     lib.pov_gpu_scene_destroy.argtypes = [C.c_void_p]
     lib.pov_gpu_scene_destroy.restype = None
     lib.pov_gpu_error_string.argtypes = [C.c_int]

@@ -992,6 +992,7 @@ const char* pov_gpu_error_string(int status)
     case POV_GPU_E_NOMEM: return "device memory allocation failed";
     case POV_GPU_E_DEVICE: return "kernel reported an error in its device error word";
     case POV_GPU_E_NODEVICE: return "no CUDA device";
+    case POV_GPU_E_CAPACITY: return "request exceeds the fixed scratch capacity (POV_GPU_STATIC_MAX_RAYS rays)";
     default: return "unknown status";
     }
 }
@@ -1293,6 +1294,59 @@ int pov_gpu_trace_rays(PovGpuScene* sc, const double* origins, const double* dir
         }
     }
     return rc;
+}
+
+
+// The same query as pov_gpu_trace_rays with every buffer in the library's
+// fixed device scratch (static_ray_scratch) instead of the scene's growable
+// buffers, and the hit mapping done by a kernel instead of host vectors:
+// nothing is allocated.  Its callers are integrations whose device memory
+// belongs to another allocator (cudaMalloc would fail although memory is
+// cached there) and render threads that must not stall frames in flight on
+// the device-wide synchronisation of cudaFree.
+int pov_gpu_trace_rays_static(PovGpuScene* sc, const double* origins, const double* directions, int32_t num_rays,
+                              PovGpuHit* hits)
+{
+    static_assert(sizeof(PovGpuHit) == 16, "scratch sizes PovGpuHit as 16 bytes");
+    static_assert(POV_GPU_STATIC_MAX_RAYS == STATIC_MAX_RAYS, "public and internal capacity differ");
+    static_assert(sizeof(int) * C_NUM <= STATIC_OFF_ERR && STATIC_OFF_ERR + 16 <= STATIC_OFF_STATS &&
+                      STATIC_OFF_STATS + sizeof(unsigned long long) * ST_COUNT <= STATIC_HEADER_BYTES,
+                  "scratch header regions overlap");
+    if (!sc || num_rays < 0 || (num_rays > 0 && (!origins || !directions || !hits)))
+        return POV_GPU_E_INVALID;
+    if (num_rays > POV_GPU_STATIC_MAX_RAYS)
+        return POV_GPU_E_CAPACITY;
+    std::lock_guard<std::mutex> g(sc->lock);
+    CK(cudaSetDevice(sc->device));
+    unsigned char* base = nullptr;
+    CK(static_ray_scratch(sc->device, &base));   // one-time set-up per device
+    if (num_rays == 0)
+        return POV_GPU_OK;
+    cudaStream_t st = sc->active();
+    const size_t n = (size_t)num_rays;
+    int* cnt = reinterpret_cast<int*>(base + STATIC_OFF_COUNTERS);
+    uint32_t* err = reinterpret_cast<uint32_t*>(base + STATIC_OFF_ERR);
+    unsigned long long* stats = reinterpret_cast<unsigned long long*>(base + STATIC_OFF_STATS);
+    double* dorg = reinterpret_cast<double*>(base + STATIC_OFF_ORG);
+    double* ddir = reinterpret_cast<double*>(base + STATIC_OFF_DIR);
+    QRay* rays = reinterpret_cast<QRay*>(base + STATIC_OFF_RAYS);
+    QHit* qh = reinterpret_cast<QHit*>(base + STATIC_OFF_HITS);
+    double* t64 = reinterpret_cast<double*>(base + STATIC_OFF_T64);
+    PovGpuHit* out = reinterpret_cast<PovGpuHit*>(base + STATIC_OFF_OUT);
+    // counters, error word and statistics start at zero
+    CK(cudaMemsetAsync(base, 0, STATIC_HEADER_BYTES, st));
+    CK(cudaMemcpyAsync(dorg, origins, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(ddir, directions, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st));
+    CK(launch_load_rays(dorg, ddir, num_rays, rays, cnt + C_QA, st));
+    CK(launch_trace(sc->S, false, rays, cnt + C_QA, cnt + C_W0, qh, nullptr, sc->stack_depth, sc->num_sms * 8, err,
+                    stats, nullptr, num_rays, nullptr, st));
+    CK(launch_refine(sc->S, dorg, ddir, qh, t64, num_rays, st));
+    CK(launch_hits_abi(sc->S, qh, t64, num_rays, out, st));
+    uint32_t errw = 0;
+    CK(cudaMemcpyAsync(hits, out, sizeof(PovGpuHit) * n, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&errw, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return errw ? POV_GPU_E_DEVICE : POV_GPU_OK;
 }
 
 }  // extern "C"

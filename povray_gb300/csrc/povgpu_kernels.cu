@@ -22,11 +22,14 @@
 // a device counter, so no host round trip sits between the stages.
 #include "povgpu_internal.h"
 #include "povgpu_kernels.h"
+#include "povgpu.h"
 #include "povgpu_quartic.cuh"
 
 #include <cuda_runtime.h>
 #include <math_constants.h>
 #include <stdint.h>
+
+#include <mutex>
 
 namespace povgpu {
 
@@ -1388,6 +1391,85 @@ cudaError_t launch_aa_resolve(const float4* grid, const uint32_t* subdiv, int np
 {
     k_aa_resolve<<<cdiv(npix > 0 ? npix : 1, 128), 128, 0, st>>>(grid, subdiv, npix, G, depth, out);
     return cudaGetLastError();
+}
+
+// ------------------------------------------------- fixed-scratch ray query --
+// Scratch of pov_gpu_trace_rays_static: one file-scope device array, which
+// CUDA places in this module's static memory on each device when it loads
+// the module, so that query allocates nothing per call.  Layout
+// (STATIC_OFF_* offsets): a 256-byte header (work counters, device error
+// word, statistics; zeroed by every call before its first launch) followed
+// by the per-ray arrays sized for STATIC_MAX_RAYS rays.  One array per
+// device: calls that overlap in time on one device share it and race.
+static __device__ __align__(256) unsigned char g_ray_scratch[STATIC_SCRATCH_BYTES];
+
+// Maps closest hits to the ABI's (object, triangle, depth) records on the
+// device: the mapping pov_gpu_trace_rays does on the host.
+__global__ void k_hits_abi(DeviceScene S, const QHit* __restrict__ hits, const double* __restrict__ t64, int n,
+                           PovGpuHit* __restrict__ out)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    QHit h = hits[i];
+    PovGpuHit r;
+    r.object = -1;
+    r.triangle = -1;
+    r.t = 0.0;
+    if (h.prim != 0xffffffffu) {
+        uint32_t kind = h.prim >> PRIM_KIND_SHIFT, idx = h.prim & PRIM_INDEX_MASK;
+        r.t = t64[i];
+        if (kind == PK_SPHERE) {
+            r.object = S.sphere_obj[idx];
+        } else if (kind == PK_PLANE) {
+            r.object = S.plane_obj[idx];
+        } else if (kind == PK_BOX) {
+            r.object = __float_as_int(S.boxes[idx].lo.w);
+        } else if (kind == PK_TORUS) {
+            r.object = S.tori[idx].object;
+        } else if (kind == PK_CSG) {
+            DevCsg cg = S.csgs[idx];
+            r.object = S.csg_children[cg.first + (__float_as_uint(h.u) & 0xffffu)].object;
+        } else if (kind == PK_TRIANGLE) {
+            int g = S.tri_global[idx];
+            r.object = __float_as_int(S.tri_normal[g].w);
+            r.triangle = S.tri_local[g];
+        }
+    }
+    out[i] = r;
+}
+
+cudaError_t launch_hits_abi(const DeviceScene& S, const QHit* hits, const double* t64, int n, PovGpuHit* out,
+                            cudaStream_t st)
+{
+    if (n <= 0)
+        return cudaSuccess;
+    k_hits_abi<<<cdiv(n, 256), 256, 0, st>>>(S, hits, t64, n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t static_ray_scratch(int device, unsigned char** out)
+{
+    // The address is looked up once per device and cached.  The first lookup
+    // on a device can make CUDA load this module there, which places
+    // g_ray_scratch in device memory; later lookups only read the cache.
+    constexpr int CACHED_DEVICES = 64;
+    static std::mutex lock;
+    static unsigned char* cache[CACHED_DEVICES] = {};
+    *out = nullptr;
+    std::lock_guard<std::mutex> g(lock);
+    if (device >= 0 && device < CACHED_DEVICES && cache[device]) {
+        *out = cache[device];
+        return cudaSuccess;
+    }
+    unsigned char* ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress((void**)&ptr, g_ray_scratch);
+    if (e != cudaSuccess)
+        return e;
+    if (device >= 0 && device < CACHED_DEVICES)
+        cache[device] = ptr;
+    *out = ptr;
+    return cudaSuccess;
 }
 
 }  // namespace povgpu

@@ -1,6 +1,7 @@
 // povgpu_kernels.h -- host-callable launchers of the kernels in
 // povgpu_kernels.cu (all asynchronous on the given stream).
 #pragma once
+#include "povgpu.h"
 #include "povgpu_internal.h"
 
 namespace povgpu {
@@ -36,5 +37,28 @@ cudaError_t launch_aa_classify(const int4* cells, const int* ncells, int cap, in
                                uint32_t* err, int grid_blocks, cudaStream_t st);
 cudaError_t launch_aa_resolve(const float4* grid, const uint32_t* subdiv, int npix, int G, int depth, float4* out,
                               cudaStream_t st);
+
+// Fixed scratch of pov_gpu_trace_rays_static (a file-scope device array in
+// povgpu_kernels.cu).  Header: work counters at 0, error word at 64,
+// statistics at 128 -- all must be zero before the first launch of a call.
+// Per-ray regions follow, each sized for STATIC_MAX_RAYS rays.
+constexpr int STATIC_MAX_RAYS = 65536;
+constexpr size_t STATIC_OFF_COUNTERS = 0;
+constexpr size_t STATIC_OFF_ERR = 64;
+constexpr size_t STATIC_OFF_STATS = 128;
+constexpr size_t STATIC_HEADER_BYTES = 256;
+constexpr size_t STATIC_OFF_ORG = STATIC_HEADER_BYTES;                               // double[3 * max]
+constexpr size_t STATIC_OFF_DIR = STATIC_OFF_ORG + sizeof(double) * 3 * STATIC_MAX_RAYS;  // double[3 * max]
+constexpr size_t STATIC_OFF_RAYS = STATIC_OFF_DIR + sizeof(double) * 3 * STATIC_MAX_RAYS; // QRay[max]
+constexpr size_t STATIC_OFF_HITS = STATIC_OFF_RAYS + sizeof(QRay) * STATIC_MAX_RAYS;      // QHit[max]
+constexpr size_t STATIC_OFF_T64 = STATIC_OFF_HITS + sizeof(QHit) * STATIC_MAX_RAYS;       // double[max]
+constexpr size_t STATIC_OFF_OUT = STATIC_OFF_T64 + sizeof(double) * STATIC_MAX_RAYS;      // PovGpuHit[max]
+constexpr size_t STATIC_SCRATCH_BYTES = STATIC_OFF_OUT + 16 * (size_t)STATIC_MAX_RAYS;     // 7.5 MiB + 256 B
+
+// Device address of that scratch on the current device (looked up once per
+// device, then cached).  Call with `device` current.
+cudaError_t static_ray_scratch(int device, unsigned char** out);
+cudaError_t launch_hits_abi(const DeviceScene& S, const QHit* hits, const double* t64, int n, PovGpuHit* out,
+                            cudaStream_t st);
 
 }  // namespace povgpu

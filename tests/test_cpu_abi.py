@@ -30,7 +30,7 @@ def test_library_exports_every_declared_symbol(gpu_lib):
 
 
 def test_error_strings(gpu_lib):
-    for code in (0, -1, -2, -3, -4, -5, -6, -7):
+    for code in (0, -1, -2, -3, -4, -5, -6, -7, -8):
         assert gpu_lib.pov_gpu_error_string(code)
     assert gpu_lib.pov_gpu_error_string(-99) == b"unknown status"
 
@@ -108,6 +108,7 @@ def test_null_arguments(gpu_lib):
     assert gpu_lib.pov_gpu_scene_create(None, None, None) == abi.POV_GPU_E_INVALID
     assert gpu_lib.pov_gpu_trace_blocks(None, None, 0, None, None, None) == abi.POV_GPU_E_INVALID
     assert gpu_lib.pov_gpu_trace_rays(None, None, None, 0, None) == abi.POV_GPU_E_INVALID
+    assert gpu_lib.pov_gpu_trace_rays_static(None, None, None, 0, None) == abi.POV_GPU_E_INVALID
     gpu_lib.pov_gpu_scene_destroy(None)
 
 
