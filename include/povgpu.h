@@ -327,6 +327,7 @@ int pov_gpu_scene_set_stream(PovGpuScene* scene, void* cuda_stream);
 #define POV_GPU_STAGE_TRACE_SHADOW  3
 #define POV_GPU_STAGE_RESOLVE       4
 #define POV_GPU_STAGE_FINALIZE      5
+#define POV_GPU_STAGE_AREA_SHADOW   6   /* area-light shadow subdivision       */
 #define POV_GPU_STAGES              8
 
 /* Profile of the last trace call.  Stage times are CUDA-event durations on

@@ -16,8 +16,13 @@
  *
  * Documented simplifications (none changes a result on non-grazing rays):
  *   - the light-source shadow cache of TracePointLightShadowRay
- *     (source/core/render/trace.cpp:1990-2025) is not restated; it only
- *     changes Shadow_Cache_Hits, which depends on render order anyway.
+ *     (source/core/render/trace.cpp:1990-2025) is not restated: which
+ *     object it holds depends on render order, and its test of that object
+ *     accepts hits in [MIN_ISECT_DEPTH, depth) (trace.cpp:1999,346-390)
+ *     where the full test needs (SHADOW_TOLERANCE, depth - SHADOW_TOLERANCE).
+ *     It changes Shadow_Cache_Hits, and the verdict of a shadow ray that
+ *     passes within SHADOW_TOLERANCE of another surface (a few area-light
+ *     samples per ten thousand in the golden scenes).
  *   - the mesh best-first loop's early "Depth > Best" exit uses the best
  *     hit so far (source/core/shape/mesh.cpp:1499 keeps the last one).
  */
@@ -37,6 +42,7 @@
 #define MAX_DISTANCE     1.0e7
 #define MIN_ISECT_DEPTH  1.0e-4
 #define SHADOW_TOLERANCE 1.0e-3
+#define AREA_MAX_POINTS  4096   /* largest area-light grid the oracle restates */
 /* per-shape DEPTH_TOLERANCE: sphere.cpp:63, plane.cpp:62, mesh.cpp:92 */
 #define SPHERE_DEPTH_TOLERANCE 1.0e-6
 #define PLANE_DEPTH_TOLERANCE  1.0e-6
@@ -1471,6 +1477,86 @@ static int shadow_blocked(const PovOracle* S, Thread* th, V3 P, V3 L, double dis
     return 0;
 }
 
+/* Grid point (u, v) of an area light as an offset from its centre
+ * (TraceAreaLightSubsetShadowRay, trace.cpp:2166-2205; no jitter). */
+static V3 area_offset(const PovGpuLight* L, V3 a1, V3 a2, int u, int v)
+{
+    double ju = u, jv = v;
+    if (L->circular) {
+        ju = ju / (L->area_size1 - 1) - 0.5 + 0.001;
+        jv = jv / (L->area_size2 - 1) - 0.5 + 0.001;
+        double sc = fabs(ju) > fabs(jv) ? fabs(ju) : fabs(jv);
+        sc /= sqrt(ju * ju + jv * jv);
+        return vadd(vmul(a1, ju * sc), vmul(a2, jv * sc));
+    }
+    V3 j1 = v3(0.0, 0.0, 0.0), j2 = v3(0.0, 0.0, 0.0);
+    if (L->area_size1 > 1)
+        j1 = vmul(a1, ju / (double)(L->area_size1 - 1) - 0.5);
+    if (L->area_size2 > 1)
+        j2 = vmul(a2, jv / (double)(L->area_size2 - 1) - 0.5);
+    return vadd(j1, j2);
+}
+
+/* TraceAreaLightSubsetShadowRay (trace.cpp:2131-2272) for opaque scenes:
+ * the fraction of the light colour that reaches P from the grid region
+ * [u1,u2]x[v1,v2].  grid[u*size2+v]: -1 not traced yet (lightGrid's
+ * Invalidate), 1 visible, 0 blocked.  A sample colour is the light colour
+ * or black, so two corners differ in ColourDistance by |r|+|g|+|b| of the
+ * light colour (float SumAbs) or not at all. */
+static double area_subset(const PovOracle* S, Thread* th, const PovGpuLight* L, V3 P, V3 a1, V3 a2,
+                          signed char* grid, int u1, int v1, int u2, int v2, int level, float lc_dist)
+{
+    double s[4];
+    for (int i = 0; i < 4; i++) {
+        int u = (i & 1) ? u2 : u1;
+        int v = (i & 2) ? v2 : v1;
+        signed char* g = &grid[u * L->area_size2 + v];
+        if (*g < 0) {
+            V3 C = vadd(vload(L->center), area_offset(L, a1, a2, u, v));
+            V3 ld = vsub(C, P);
+            double depth = vlen(ld);
+            ld = vdiv(ld, depth);
+            *g = shadow_blocked(S, th, P, ld, depth) ? 0 : 1;
+        }
+        s[i] = *g;
+    }
+    if (u2 - u1 > 1 || v2 - v1 > 1) {
+        int differ = s[0] != s[1] || s[1] != s[3] || s[3] != s[2] || s[2] != s[0];
+        if (level < L->adaptive_level || (differ && lc_dist > 0.1)) {
+            int mu0 = (int)floor((u1 + u2) / 2.0), mu1 = (int)ceil((u1 + u2) / 2.0);
+            int mv0 = (int)floor((v1 + v2) / 2.0), mv1 = (int)ceil((v1 + v2) / 2.0);
+            s[0] = area_subset(S, th, L, P, a1, a2, grid, u1, v1, mu0, mv0, level + 1, lc_dist);
+            s[1] = area_subset(S, th, L, P, a1, a2, grid, mu1, v1, u2, mv0, level + 1, lc_dist);
+            s[2] = area_subset(S, th, L, P, a1, a2, grid, u1, mv1, mu0, v2, level + 1, lc_dist);
+            s[3] = area_subset(S, th, L, P, a1, a2, grid, mu1, mv1, u2, v2, level + 1, lc_dist);
+        }
+    }
+    return (s[0] + s[1] + s[2] + s[3]) * 0.25;
+}
+
+/* TraceAreaLightShadowRay (trace.cpp:2078-2129): axes (oriented towards P
+ * when `orient`), all grid points invalid, then the whole grid as one
+ * region. */
+static double area_light_fraction(const PovOracle* S, Thread* th, const PovGpuLight* L, V3 P)
+{
+    signed char grid[AREA_MAX_POINTS];
+    int npts = L->area_size1 * L->area_size2;
+    for (int k = 0; k < npts; k++)
+        grid[k] = -1;
+    V3 a1 = vload(L->axis1), a2 = vload(L->axis2);
+    if (L->orient) {
+        V3 dir = vnorm(vsub(vload(L->center), P));
+        double len1 = vlen(a1);
+        V3 tmp = fabs(fabs(dir.z) - 1.0) < 0.01 ? v3(0.0, 1.0, 0.0) : v3(0.0, 0.0, 1.0);
+        a1 = vnorm(vcross(dir, tmp));
+        a2 = vnorm(vcross(dir, a1));
+        a1 = vmul(a1, len1);
+        a2 = vmul(a2, len1);
+    }
+    float lc_dist = fabsf(L->colour[0]) + fabsf(L->colour[1]) + fabsf(L->colour[2]);
+    return area_subset(S, th, L, P, a1, a2, grid, 0, 0, L->area_size1 - 1, L->area_size2 - 1, 0, lc_dist);
+}
+
 static void trace_ray(const PovOracle* S, Thread* th, V3 O, V3 D, double weight, int level, RGB* col);
 
 /* ComputeReflection (trace.cpp:1264-1321). */
@@ -1554,8 +1640,15 @@ static void shade(const PovOracle* S, Thread* th, const Isect* is, V3 D, double 
                     continue;
             }
             if (level <= S->desc.max_trace_level) {   /* TraceShadowRay level check */
-                if (shadow_blocked(S, th, ip, ld, ldist))
+                if (L->kind == POV_LIGHT_AREA) {
+                    double f = area_light_fraction(S, th, L, ip);
+                    if (f == 0.0)
+                        continue;
+                    for (int k = 0; k < 3; k++)
+                        lc[k] = (float)(lc[k] * f);
+                } else if (shadow_blocked(S, th, ip, ld, ldist)) {
                     continue;
+                }
             }
             /* ComputeDiffuseColour (trace.cpp:2441-2484) */
             double diffuse = m->diffuse * m->brilliance_adjust;
@@ -1774,6 +1867,13 @@ int pov_oracle_create(const PovGpuSceneDesc* desc, PovOracle** out, int32_t* bad
     if (bad_index) *bad_index = -1;
     if (!desc || !out || desc->abi_version != POV_GPU_ABI_VERSION || desc->num_materials < 1)
         return POV_GPU_E_INVALID;
+    for (int i = 0; i < desc->num_lights; i++) {
+        const PovGpuLight* L = &desc->lights[i];
+        if (L->kind == POV_LIGHT_AREA &&
+            (L->area_size1 < 1 || L->area_size2 < 1 || L->area_size1 * L->area_size2 > AREA_MAX_POINTS ||
+             L->jitter || (L->circular && (L->area_size1 < 2 || L->area_size2 < 2))))
+            return POV_GPU_E_UNSUPPORTED;   /* jitter draws on the reference's RNG stream */
+    }
     PovOracle* S = (PovOracle*)calloc(1, sizeof(PovOracle));
     S->desc = *desc;
     S->nobjs = desc->num_objects;

@@ -136,7 +136,7 @@ class PovGpuHit(C.Structure):
 
 
 POV_GPU_STAGES = 8
-STAGE_NAMES = ["camera", "trace_closest", "shade", "trace_shadow", "resolve", "finalize", "s6", "s7"]
+STAGE_NAMES = ["camera", "trace_closest", "shade", "trace_shadow", "resolve", "finalize", "area_shadow", "s7"]
 POV_GPU_PROFILE_TIMES = 1
 POV_GPU_PROFILE_WORK = 2
 

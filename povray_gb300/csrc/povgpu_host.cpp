@@ -293,6 +293,8 @@ struct PovGpuScene {
     // per-batch work buffers (grown on demand, reused)
     DevBuf blocks, block_off, corner_off, qA, qB, pathA, pathB, hits, paths, slot_contrib, sq, sq_slot, blocked, out,
         counters, stats, err, rays_in, skipA, skipB, sskip, t64;
+    // area-light shadow items (shading point, slot, origin surface)
+    DevBuf aq, aq_slot, aq_skip;
     // adaptive antialiasing buffers
     DevBuf corners, aa_grid, aa_mask, aa_subdiv, aa_xy, cellsA, cellsB, spos, sslot;
     int     num_lights = 0;
@@ -316,7 +318,7 @@ struct PovGpuScene {
                          &csg_children, &objects, &materials, &lights, &blocks, &block_off, &corner_off, &qA, &qB,
                          &pathA, &pathB, &hits, &paths, &slot_contrib, &sq, &sq_slot, &blocked, &out, &counters,
                          &stats, &err, &rays_in, &skipA, &skipB, &sskip, &t64, &corners, &aa_grid, &aa_mask,
-                         &aa_subdiv, &aa_xy, &cellsA, &cellsB, &spos, &sslot, &wcount};
+                         &aa_subdiv, &aa_xy, &cellsA, &cellsB, &spos, &sslot, &wcount, &aq, &aq_slot, &aq_skip};
         for (DevBuf* b : all)
             b->release();
         if (stream)
@@ -348,9 +350,17 @@ int validate(const PovGpuSceneDesc* d, int32_t* bad)
         return POV_GPU_E_UNSUPPORTED;
     if (d->radiosity.enabled)
         return POV_GPU_E_UNSUPPORTED;
-    for (int i = 0; i < d->num_lights; i++)
-        if (d->lights[i].kind != POV_LIGHT_POINT || d->lights[i].fade_power > 0.0f)
+    for (int i = 0; i < d->num_lights; i++) {
+        const PovGpuLight& L = d->lights[i];
+        if ((L.kind != POV_LIGHT_POINT && L.kind != POV_LIGHT_AREA) || L.fade_power > 0.0f)
             return POV_GPU_E_UNSUPPORTED;
+        // area lights: the grid fits the per-point visibility masks; jitter
+        // draws on the reference's random stream and is not restated
+        if (L.kind == POV_LIGHT_AREA &&
+            (L.area_size1 < 1 || L.area_size2 < 1 || L.area_size1 * L.area_size2 > AREA_MAX_POINTS ||
+             L.jitter || (L.circular && (L.area_size1 < 2 || L.area_size2 < 2))))
+            return POV_GPU_E_UNSUPPORTED;
+    }
     for (int i = 0; i < d->num_materials; i++) {
         const PovGpuMaterial& m = d->materials[i];
         // opaque plain pigments and the classic finish terms only
@@ -711,10 +721,18 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
     for (int i = 0; i < d->num_materials; i++)
         mats[i] = make_material(d->materials[i], d->ambient_light);
     std::vector<DevLight> lights((size_t)std::max(d->num_lights, 1));
+    int num_area = 0;
     for (int i = 0; i < d->num_lights; i++) {
         const PovGpuLight& L = d->lights[i];
         lights[i].center = make_float4((float)L.center[0], (float)L.center[1], (float)L.center[2], (float)L.kind);
         lights[i].colour = make_float4(L.colour[0], L.colour[1], L.colour[2], 0.f);
+        double len1 = std::sqrt(L.axis1[0] * L.axis1[0] + L.axis1[1] * L.axis1[1] + L.axis1[2] * L.axis1[2]);
+        lights[i].axis1 = make_float4((float)L.axis1[0], (float)L.axis1[1], (float)L.axis1[2], (float)len1);
+        lights[i].axis2 = make_float4((float)L.axis2[0], (float)L.axis2[1], (float)L.axis2[2], 0.f);
+        lights[i].area = make_int4(L.area_size1, L.area_size2, L.adaptive_level,
+                                   (L.circular ? 1 : 0) | (L.orient ? 2 : 0));
+        if (L.kind == POV_LIGHT_AREA)
+            num_area++;
     }
 
     CK(upload(sc->nodes, B.bvh.nodes));
@@ -783,6 +801,7 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
     S.materials = sc->materials.as<DevMaterial>();
     S.lights = sc->lights.as<DevLight>();
     S.num_lights = d->num_lights;
+    S.num_area_lights = num_area;
     S.max_trace_level = d->max_trace_level;
     S.adc_bailout = d->adc_bailout;
     S.background = make_float4(d->background[0], d->background[1], d->background[2], d->background[3]);
@@ -807,7 +826,8 @@ enum {
     C_NS = 5,     // AA: samples of this round
     C_NC = 6,     // AA: active cells
     C_NN = 7,     // AA: next cells
-    C_NUM = 8
+    C_AQ = 8,     // area-light shadow items
+    C_NUM = 10
 };
 
 int check_device_error(PovGpuScene* sc, PovGpuStats* stats, unsigned long long* host_stats)
@@ -917,6 +937,13 @@ int run_samples(PovGpuScene* sc, StageClock& clk, int mode, int nblocks, const i
     CK(sc->skipA.ensure(sizeof(uint2) * maxq));
     CK(sc->skipB.ensure(sizeof(uint2) * maxq));
     CK(sc->sskip.ensure(sizeof(uint2) * maxq * nl));
+    const int nal = sc->S.num_area_lights;
+    const size_t max_area = maxq * (size_t)nal;
+    if (nal > 0) {
+        CK(sc->aq.ensure(sizeof(QRay) * max_area));
+        CK(sc->aq_slot.ensure(sizeof(int) * max_area));
+        CK(sc->aq_skip.ensure(sizeof(uint2) * max_area));
+    }
 
     cudaStream_t st = sc->active();
     int* cnt = sc->counters.as<int>();
@@ -941,6 +968,7 @@ int run_samples(PovGpuScene* sc, StageClock& clk, int mode, int nblocks, const i
     for (int level = 0; level < sc->max_trace_level; level++) {
         CK(cudaMemsetAsync(cnext, 0, sizeof(int), st));
         CK(cudaMemsetAsync(cnt + C_SQ, 0, sizeof(int) * 3, st));   // SQ, W0, W1
+        CK(cudaMemsetAsync(cnt + C_AQ, 0, sizeof(int), st));
         CK(clk.begin(POV_GPU_STAGE_TRACE_CLOSEST));
         CK(launch_trace(S, false, qcur, ccur, cnt + C_W0, sc->hits.as<QHit>(), nullptr, sc->stack_depth, grid_trace,
                         derr, dstats, wc, (int)maxq, kcur, st));
@@ -948,9 +976,17 @@ int run_samples(PovGpuScene* sc, StageClock& clk, int mode, int nblocks, const i
         CK(clk.begin(POV_GPU_STAGE_SHADE));
         CK(launch_shade(S, level, qcur, pcur, sc->hits.as<QHit>(), ccur, sc->paths.as<PathState>(),
                         sc->slot_contrib.as<float4>(), sc->sq.as<QRay>(), sc->sq_slot.as<int>(), cnt + C_SQ,
-                        sc->sskip.as<uint2>(), qnext, pnext, knext, cnext, (int)maxq, (int)(maxq * nl), grid_shade,
-                        derr, dstats, st));
+                        sc->sskip.as<uint2>(), qnext, pnext, knext, cnext, (int)maxq, (int)(maxq * nl),
+                        sc->aq.as<QRay>(), sc->aq_slot.as<int>(), sc->aq_skip.as<uint2>(), cnt + C_AQ,
+                        (int)max_area, grid_shade, derr, dstats, st));
         CK(clk.end());
+        if (nal > 0) {
+            CK(clk.begin(POV_GPU_STAGE_AREA_SHADOW));
+            CK(launch_area_shadow(S, sc->aq.as<QRay>(), sc->aq_slot.as<int>(), sc->aq_skip.as<uint2>(), cnt + C_AQ,
+                                  (int)max_area, sc->slot_contrib.as<float4>(), sc->stack_depth, grid_shade, derr,
+                                  dstats, st));
+            CK(clk.end());
+        }
         if (sc->num_lights > 0) {
             CK(clk.begin(POV_GPU_STAGE_TRACE_SHADOW));
             CK(launch_trace(S, true, sc->sq.as<QRay>(), cnt + C_SQ, cnt + C_W1, nullptr, sc->blocked.as<uint8_t>(),

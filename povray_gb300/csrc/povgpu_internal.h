@@ -65,7 +65,11 @@ struct __align__(16) DevMaterial {
 struct __align__(16) DevLight {
     float4 center;          // xyz, kind
     float4 colour;          // rgb, -
+    float4 axis1;           // area light: Axis1 xyz, |Axis1|
+    float4 axis2;           // area light: Axis2 xyz, -
+    int4   area;            // Area_Size1, Area_Size2, Adaptive_Level, bit0 Circular | bit1 Orient
 };
+constexpr int AREA_MAX_POINTS = 64;   // area-light grid points the GPU path holds per shading point
 
 struct __align__(16) DevMesh {
     int32_t tri_base;        // offset of this mesh's triangles in the global tables
@@ -144,6 +148,7 @@ struct DeviceScene {
     const DevMaterial* materials;
     const DevLight*    lights;
     int32_t         num_lights;
+    int32_t         num_area_lights;
     int32_t         max_trace_level;
     float           adc_bailout;
     float4          background;

@@ -871,7 +871,8 @@ __global__ void __launch_bounds__(128) k_shade(
     float4* __restrict__ slot_contrib, QRay* __restrict__ sq, int* __restrict__ sq_slot, int* __restrict__ sq_count,
     uint2* __restrict__ sq_skip, QRay* __restrict__ nq, int* __restrict__ nq_path,
     uint2* __restrict__ nq_skip, int* __restrict__ nq_count, int max_queue,
-    int max_shadow, uint32_t* err, unsigned long long* stats)
+    int max_shadow, QRay* __restrict__ aq, int* __restrict__ aq_slot, uint2* __restrict__ aq_skip,
+    int* __restrict__ aq_count, int max_area, uint32_t* err, unsigned long long* stats)
 {
     const int n = min(*q_count, max_queue);
     const int nl = S.num_lights;
@@ -918,8 +919,10 @@ __global__ void __launch_bounds__(128) k_shade(
             float3 contrib = f3(0.f, 0.f, 0.f);
             float3 ld = f3(0.f, 0.f, 1.f);
             float ldist = 0.f;
+            bool area = false;
             if (hit) {
-                DevLight L = S.lights[l];
+                const DevLight& L = S.lights[l];
+                area = L.center.w != 0.0f;   // POV_LIGHT_AREA
                 float3 lv = xyz(L.center) - p;
                 ldist = sqrtf(dot3(lv, lv));
                 ld = lv * (1.0f / ldist);
@@ -952,8 +955,23 @@ __global__ void __launch_bounds__(128) k_shade(
                     }
                 }
             }
-            int slot = warp_reserve(sq_count, emit, mask);
-            if (emit) {
+            // point lights: one shadow ray; area lights: one item for the
+            // subdivision kernel (TraceAreaLightShadowRay)
+            int aslot = warp_reserve(aq_count, emit && area, mask);
+            if (emit && area) {
+                if (aslot < max_area) {
+                    QRay ar;
+                    ar.org = make_float4(p.x, p.y, p.z, __uint_as_float(__float_as_uint(SMALL_TOLERANCE_F) + 1u));
+                    ar.dir = make_float4(0.f, 0.f, 0.f, 0.f);
+                    aq[aslot] = ar;
+                    aq_slot[aslot] = i * nl + l;
+                    aq_skip[aslot] = self;
+                } else {
+                    set_error(err, DE_QUEUE_OVERFLOW);
+                }
+            }
+            int slot = warp_reserve(sq_count, emit && !area, mask);
+            if (emit && !area) {
                 if (slot < max_shadow) {
                     QRay sr;
                     sr.org = make_float4(p.x, p.y, p.z, __uint_as_float(__float_as_uint(SMALL_TOLERANCE_F) + 1u));
@@ -1034,6 +1052,177 @@ __global__ void k_mark_blocked(const int* __restrict__ sq_slot, const uint8_t* _
             slot_contrib[sq_slot[i]].w = 0.0f;
 }
 
+// ------------------------------------------------------- area lights --
+// Any-hit query of one ray against the whole scene (the per-ray body of
+// k_trace<true, FULL>), stack slot k of thread t at smem[k*blockDim+t].
+template <bool FULL>
+__device__ __forceinline__ bool occluded(const DeviceScene& S, float3 o, float3 d, float tmin, float tmax, uint2 skip,
+                                         int* smem, int stack_depth, uint32_t* err)
+{
+    for (int k = 0; k < S.num_planes; k++) {
+        if (((PK_PLANE << PRIM_KIND_SHIFT) | (uint32_t)k) == skip.x)
+            continue;
+        float4 pl = __ldg(S.planes + k);
+        float ndd = pl.x * d.x + pl.y * d.y + pl.z * d.z;
+        if (fabsf(ndd) < EPSILON_F)
+            continue;
+        float tt = -(pl.x * o.x + pl.y * o.y + pl.z * o.z + pl.w) / ndd;
+        if (tt >= tmin && tt < tmax)
+            return true;
+    }
+    float3 inv = f3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+    float t = tmax, bu = 0.f, bv = 0.f;
+    int sp = 0, node = S.root, iters = 0;
+    while (node != 0x7fffffff) {
+        if (++iters > (1 << 22)) {
+            set_error(err, DE_ITERATION_CAP);
+            return false;
+        }
+        if (node >= 0) {
+            bool h0, h1;
+            float t0, t1;
+            int l0, l1;
+            node_test(S.nodes, node, o, inv, tmin, t, h0, h1, t0, t1, l0, l1);
+            if (h0 && h1) {
+                if (sp >= stack_depth) {
+                    set_error(err, DE_STACK_OVERFLOW);
+                    return false;
+                }
+                smem[sp * blockDim.x + threadIdx.x] = t1 < t0 ? l0 : l1;
+                sp++;
+                node = t1 < t0 ? l1 : l0;
+            } else if (h0) {
+                node = l0;
+            } else if (h1) {
+                node = l1;
+            } else {
+                node = sp > 0 ? smem[(--sp) * blockDim.x + threadIdx.x] : 0x7fffffff;
+            }
+        } else {
+            uint32_t code = ~(uint32_t)node;
+            uint32_t first = code >> 3, count = (code & 7u) + 1u;
+            for (uint32_t k = 0; k < count; k++) {
+                uint32_t aux = 0;
+                if (prim_test<true, FULL>(S, __ldg(S.prim_refs + first + k), o, d, tmin, t, bu, bv, aux, skip))
+                    return true;
+            }
+            node = sp > 0 ? smem[(--sp) * blockDim.x + threadIdx.x] : 0x7fffffff;
+        }
+    }
+    return false;
+}
+
+// Grid point (u, v) of an area light as an offset from its centre
+// (TraceAreaLightSubsetShadowRay, trace.cpp:2166-2205; no jitter).
+__device__ __forceinline__ float3 area_offset(int4 A, float3 a1, float3 a2, int u, int v)
+{
+    float ju = (float)u, jv = (float)v;
+    if (A.w & 1) {   // circular
+        ju = ju / (float)(A.x - 1) - 0.5f + 0.001f;
+        jv = jv / (float)(A.y - 1) - 0.5f + 0.001f;
+        float sc = fmaxf(fabsf(ju), fabsf(jv)) / sqrtf(ju * ju + jv * jv);
+        return a1 * (ju * sc) + a2 * (jv * sc);
+    }
+    float3 j = f3(0.f, 0.f, 0.f);
+    if (A.x > 1)
+        j = j + a1 * (ju / (float)(A.x - 1) - 0.5f);
+    if (A.y > 1)
+        j = j + a2 * (jv / (float)(A.y - 1) - 0.5f);
+    return j;
+}
+
+// One thread per (shading point, area light): TraceAreaLightShadowRay
+// (trace.cpp:2078-2129) and its recursive 4-corner subdivision
+// (TraceAreaLightSubsetShadowRay, trace.cpp:2131-2272) for opaque scenes.
+// The recursion runs as a depth-first region stack; a region that is not
+// subdivided adds 0.25^level times the mean of its corner samples, which is
+// the reference's nested averaging written out.  Grid points are traced at
+// most once per shading point (lightGrid), their visibility held in two
+// 64-bit masks.  Writes the visible fraction of the light to the slot's w.
+template <bool FULL>
+__global__ void __launch_bounds__(128) k_area_shadow(DeviceScene S, const QRay* __restrict__ aq,
+                                                     const int* __restrict__ aq_slot,
+                                                     const uint2* __restrict__ aq_skip,
+                                                     const int* __restrict__ aq_count, int cap,
+                                                     float4* __restrict__ slot_contrib, int stack_depth,
+                                                     uint32_t* err, unsigned long long* stats)
+{
+    extern __shared__ int smem[];
+    const int n = min(*aq_count, cap);
+    const int nl = S.num_lights;
+    unsigned long long c_tests = 0, c_blocked = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        QRay it = aq[i];
+        const int slot = aq_slot[i];
+        const uint2 skip = aq_skip[i];
+        const DevLight& L = S.lights[slot % nl];
+        const float3 P = xyz(it.org);
+        const float tmin = it.org.w;
+        const float3 C = xyz(L.center);
+        const int4 A = L.area;
+        float3 a1 = xyz(L.axis1), a2 = xyz(L.axis2);
+        if (A.w & 2) {   // orient: axes perpendicular to the centre ray, |Axis1| long
+            float3 dir = normalize3(C - P);
+            float3 tmp = fabsf(fabsf(dir.z) - 1.0f) < 0.01f ? f3(0.f, 1.f, 0.f) : f3(0.f, 0.f, 1.f);
+            a1 = normalize3(cross3(dir, tmp));
+            a2 = normalize3(cross3(dir, a1));
+            a1 = a1 * L.axis1.w;
+            a2 = a2 * L.axis1.w;
+        }
+        const float3 lc = xyz(L.colour);
+        const bool far_apart = fabsf(lc.x) + fabsf(lc.y) + fabsf(lc.z) > 0.1f;   // ColourDistance of lit vs black
+        unsigned long long traced = 0, visible = 0;
+        // region: u1 | v1 << 6 | u2 << 12 | v2 << 18 | level << 24
+        uint32_t rs[24];
+        int rsp = 0;
+        rs[rsp++] = (uint32_t)(A.x - 1) << 12 | (uint32_t)(A.y - 1) << 18;
+        float frac = 0.0f;
+        while (rsp > 0) {
+            uint32_t r = rs[--rsp];
+            int u1 = r & 63, v1 = (r >> 6) & 63, u2 = (r >> 12) & 63, v2 = (r >> 18) & 63, level = r >> 24;
+            int vis[4];
+            for (int c = 0; c < 4; c++) {
+                int u = (c & 1) ? u2 : u1;
+                int v = (c & 2) ? v2 : v1;
+                int bit = u * A.y + v;
+                if (!((traced >> bit) & 1ull)) {
+                    float3 lv = C + area_offset(A, a1, a2, u, v) - P;
+                    float depth = sqrtf(dot3(lv, lv));
+                    float3 ld = lv * (1.0f / depth);
+                    bool blk = occluded<FULL>(S, P, ld, tmin, depth - SHADOW_TOLERANCE_F, skip, smem, stack_depth, err);
+                    traced |= 1ull << bit;
+                    if (!blk)
+                        visible |= 1ull << bit;
+                    c_tests++;
+                    c_blocked += blk ? 1 : 0;
+                }
+                vis[c] = (int)((visible >> bit) & 1ull);
+            }
+            bool differ = vis[0] != vis[1] || vis[1] != vis[3] || vis[3] != vis[2] || vis[2] != vis[0];
+            if ((u2 - u1 > 1 || v2 - v1 > 1) && (level < A.z || (differ && far_apart)) && rsp + 4 <= 24) {
+                int mu0 = (u1 + u2) >> 1, mu1 = (u1 + u2 + 1) >> 1;   // floor / ceil of the midpoint
+                int mv0 = (v1 + v2) >> 1, mv1 = (v1 + v2 + 1) >> 1;
+                uint32_t nl6 = (uint32_t)(level + 1) << 24;
+                rs[rsp++] = (uint32_t)u1 | (uint32_t)v1 << 6 | (uint32_t)mu0 << 12 | (uint32_t)mv0 << 18 | nl6;
+                rs[rsp++] = (uint32_t)mu1 | (uint32_t)v1 << 6 | (uint32_t)u2 << 12 | (uint32_t)mv0 << 18 | nl6;
+                rs[rsp++] = (uint32_t)u1 | (uint32_t)mv1 << 6 | (uint32_t)mu0 << 12 | (uint32_t)v2 << 18 | nl6;
+                rs[rsp++] = (uint32_t)mu1 | (uint32_t)mv1 << 6 | (uint32_t)u2 << 12 | (uint32_t)v2 << 18 | nl6;
+            } else {
+                frac += (float)(vis[0] + vis[1] + vis[2] + vis[3]) * 0.25f * exp2f(-2.0f * (float)level);
+            }
+        }
+        slot_contrib[slot].w = frac;
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        c_tests += __shfl_down_sync(0xffffffffu, c_tests, off);
+        c_blocked += __shfl_down_sync(0xffffffffu, c_blocked, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (c_tests) atomicAdd(&stats[ST_SHADOW_TESTS], c_tests);
+        if (c_blocked) atomicAdd(&stats[ST_SHADOW_SUCCEEDED], c_blocked);
+    }
+}
+
 __global__ void k_resolve(const int* __restrict__ q_path, const int* __restrict__ q_count, int num_lights,
                           const float4* __restrict__ slot_contrib, PathState* __restrict__ paths, int cap)
 {
@@ -1043,10 +1232,10 @@ __global__ void k_resolve(const int* __restrict__ q_path, const int* __restrict_
         float4 c = paths[path].colour;
         for (int l = 0; l < num_lights; l++) {
             float4 s = slot_contrib[(size_t)i * num_lights + l];
-            if (s.w != 0.0f) {
-                c.x += s.x;
-                c.y += s.y;
-                c.z += s.z;
+            if (s.w != 0.0f) {   // w: 1 lit point light, area-light fraction, 0 blocked
+                c.x += s.x * s.w;
+                c.y += s.y * s.w;
+                c.z += s.z * s.w;
             }
         }
         paths[path].colour = c;
@@ -1343,11 +1532,27 @@ cudaError_t launch_trace(const DeviceScene& S, bool any_hit, const QRay* q, cons
 cudaError_t launch_shade(const DeviceScene& S, int level, const QRay* q, const int* q_path, const QHit* hits,
                          const int* q_count, PathState* paths, float4* slot_contrib, QRay* sq, int* sq_slot,
                          int* sq_count, uint2* sq_skip, QRay* nq, int* nq_path, uint2* nq_skip, int* nq_count,
-                         int max_queue, int max_shadow, int grid, uint32_t* err, unsigned long long* stats,
-                         cudaStream_t st)
+                         int max_queue, int max_shadow, QRay* aq, int* aq_slot, uint2* aq_skip, int* aq_count,
+                         int max_area, int grid, uint32_t* err, unsigned long long* stats, cudaStream_t st)
 {
     k_shade<<<grid, 128, 0, st>>>(S, level, q, q_path, hits, q_count, paths, slot_contrib, sq, sq_slot, sq_count,
-                                  sq_skip, nq, nq_path, nq_skip, nq_count, max_queue, max_shadow, err, stats);
+                                  sq_skip, nq, nq_path, nq_skip, nq_count, max_queue, max_shadow, aq, aq_slot,
+                                  aq_skip, aq_count, max_area, err, stats);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_area_shadow(const DeviceScene& S, const QRay* aq, const int* aq_slot, const uint2* aq_skip,
+                               const int* aq_count, int cap, float4* slot_contrib, int stack_depth, int grid,
+                               uint32_t* err, unsigned long long* stats, cudaStream_t st)
+{
+    const int block = 128;
+    size_t smem = (size_t)stack_depth * block * sizeof(int);
+    if (S.has_full_prims)
+        k_area_shadow<true><<<grid, block, smem, st>>>(S, aq, aq_slot, aq_skip, aq_count, cap, slot_contrib,
+                                                       stack_depth, err, stats);
+    else
+        k_area_shadow<false><<<grid, block, smem, st>>>(S, aq, aq_slot, aq_skip, aq_count, cap, slot_contrib,
+                                                        stack_depth, err, stats);
     return cudaGetLastError();
 }
 

@@ -283,6 +283,7 @@ class Scene:
         self.lights = []
         self.meshes = []
         self.antialias = None  # (threshold, depth) for sampling method 2
+        self.radiosity = None  # dict of radiosity{} settings, None = off
 
     # -- building ----------------------------------------------------------
     def material(self, m):
@@ -352,6 +353,24 @@ class Scene:
         self.lights.append(dict(kind=abi.POV_LIGHT_POINT, pos=tuple(map(float, pos)),
                                 rgb=tuple(map(float, rgb))))
 
+    def area_light(self, pos, axis1, axis2, size1, size2, rgb=(1.0, 1.0, 1.0), adaptive=None,
+                   circular=False, orient=False):
+        """light_source with area_light (Parse_Light_Source,
+        source/parser/parser.cpp:3421-3467); `adaptive` None keeps the
+        parser's default Adaptive_Level 100 (lightsource.cpp:392).  The
+        post-parse rules apply: orient implies circular, and circular needs
+        more than one sample per axis (parser.cpp:9156-9192)."""
+        size1, size2 = int(size1), int(size2)
+        if size1 < 1 or size2 < 1:
+            raise ValueError("Area size must be greater than zero.")
+        circular = bool(circular) or bool(orient)
+        if circular and (size1 <= 1 or size2 <= 1):
+            circular = False
+        self.lights.append(dict(kind=abi.POV_LIGHT_AREA, pos=tuple(map(float, pos)),
+                                rgb=tuple(map(float, rgb)), axis1=tuple(map(float, axis1)),
+                                axis2=tuple(map(float, axis2)), size=(size1, size2),
+                                adaptive=adaptive, circular=circular, orient=bool(orient)))
+
     # -- SDL -----------------------------------------------------------------
     def sdl(self):
         out = ["#version 3.7;\n",
@@ -361,7 +380,16 @@ class Scene:
                % (_v(self.location), _g(self.right_len), _v(self.look_at), _g(self.angle)),
                "background { color rgb %s }\n" % _v(self.background)]
         for l in self.lights:
-            out.append("light_source { %s color rgb %s }\n" % (_v(l["pos"]), _v(l["rgb"])))
+            extra = ""
+            if l["kind"] == abi.POV_LIGHT_AREA:
+                extra = " area_light %s, %s, %d, %d" % (_v(l["axis1"]), _v(l["axis2"]), l["size"][0], l["size"][1])
+                if l["adaptive"] is not None:
+                    extra += " adaptive %d" % l["adaptive"]
+                if l["circular"]:
+                    extra += " circular"
+                if l["orient"]:
+                    extra += " orient"
+            out.append("light_source { %s color rgb %s%s }\n" % (_v(l["pos"]), _v(l["rgb"]), extra))
         for o in self.objects:
             out.append(self._sdl_node(o) + "\n")
         return "".join(out)
@@ -443,6 +471,15 @@ class Scene:
             lights[i].center[:] = list(l["pos"])
             lights[i].colour[:] = list(l["rgb"])
             lights[i].kind = l["kind"]
+            lights[i].adaptive_level = 100
+            if l["kind"] == abi.POV_LIGHT_AREA:
+                lights[i].axis1[:] = list(l["axis1"])
+                lights[i].axis2[:] = list(l["axis2"])
+                lights[i].area_size1, lights[i].area_size2 = l["size"]
+                if l["adaptive"] is not None:
+                    lights[i].adaptive_level = int(l["adaptive"])
+                lights[i].circular = int(l["circular"])
+                lights[i].orient = int(l["orient"])
         meshes = (abi.PovGpuMesh * max(len(self.meshes), 1))()
         for i, m in enumerate(self.meshes):
             meshes[i].vertices = m.vertices.ctypes.data_as(C.POINTER(C.c_float))
@@ -698,8 +735,49 @@ def csg_torus_grid(width=1920, height=1080, n=16, seed=3, antialias=(0.1, 3)):
     return s
 
 
+def radiosity_room(width=1280, height=720, n_spheres=200, seed=4, radiosity=True, count=200,
+                   recursion_limit=2, error_bound=0.5, area=(4, 4), adaptive=None, circular=False,
+                   orient=False):
+    """Box room [-10,10]^3 as six planes, diffuse 0.7 walls (x=-10 rgb
+    <0.7,0.1,0.1>, x=+10 rgb <0.1,0.7,0.1>, the others rgb 0.9);
+    `n_spheres` spheres r U[0.3,1.5], centres x,z U[-8.5,8.5], y U[-8.5,4]
+    (the space under the light kept clear), rgb U[0.2,0.9]^3 (seed 4), none
+    within 6 of the camera; ceiling area light at (0,9,0),
+    area_light <2,0,0>,<0,0,2>,4,4; ambient 0 everywhere;
+    radiosity { count 200 recursion_limit 2 error_bound 0.5 } when
+    `radiosity`; camera (0,4,-9.5) looking at (0,-3,0), 75 deg."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    s = Scene("radiosity_room", width, height, (0.0, 4.0, -9.5), (0.0, -3.0, 0.0), 75.0,
+              max_trace_level=3)
+    s.area_light((0.0, 9.0, 0.0), (2.0, 0.0, 0.0), (0.0, 0.0, 2.0), area[0], area[1], adaptive=adaptive,
+                 circular=circular, orient=orient)
+    white = s.material(Material((0.9, 0.9, 0.9), ambient=0.0, diffuse=0.7))
+    red = s.material(Material((0.7, 0.1, 0.1), ambient=0.0, diffuse=0.7))
+    green = s.material(Material((0.1, 0.7, 0.1), ambient=0.0, diffuse=0.7))
+    s.plane((0.0, 1.0, 0.0), -10.0, white)     # floor
+    s.plane((0.0, -1.0, 0.0), -10.0, white)    # ceiling
+    s.plane((1.0, 0.0, 0.0), -10.0, red)       # x = -10
+    s.plane((-1.0, 0.0, 0.0), -10.0, green)    # x = +10
+    s.plane((0.0, 0.0, 1.0), -10.0, white)     # z = -10
+    s.plane((0.0, 0.0, -1.0), -10.0, white)    # z = +10
+    cam = np.array(s.location)
+    placed = 0
+    while placed < n_spheres:
+        c = np.array([rng.uniform(-8.5, 8.5), rng.uniform(-8.5, 4.0), rng.uniform(-8.5, 8.5)])
+        r = rng.uniform(0.3, 1.5)
+        rgb = rng.uniform(0.2, 0.9, size=3)
+        if np.linalg.norm(c - cam) < r + 6.0:
+            continue
+        s.sphere(c, r, s.material(Material(rgb, ambient=0.0, diffuse=0.7)))
+        placed += 1
+    if radiosity:
+        s.radiosity = dict(count=count, recursion_limit=recursion_limit, error_bound=error_bound)
+    return s
+
+
 WORKLOADS = {
     "spheres_plane": spheres_plane,
     "mesh_spheres": mesh_spheres,
     "csg_torus_grid": csg_torus_grid,
+    "radiosity_room": radiosity_room,
 }

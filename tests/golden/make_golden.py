@@ -4,7 +4,7 @@ Runs only where the reference sources are present (it drives
 oracle/_ref/pov_oracle and oracle/_ref/povray_ref, built from them by
 oracle/refbuild/Makefile):
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case ...]
 
 For every case it writes the scene's SDL to a temporary directory, has the
 reference parse and render it, and stores in <case>.npz:
@@ -48,6 +48,9 @@ def cases():
         "spheres_plane_320x240": (scenes.spheres_plane(320, 240), 4, 12.0),
         "mesh_spheres_small_160x90": (scenes.mesh_spheres(160, 90, mesh_n=24, n_spheres=64), 2, 12.0),
         "csg_torus_grid_160x90": (scenes.csg_torus_grid(160, 90, n=16), 2, 16.0),
+        "area_room_160x90": (scenes.radiosity_room(160, 90, n_spheres=40, radiosity=False), 2, 9.0),
+        "area_room_adaptive_160x90": (scenes.radiosity_room(160, 90, n_spheres=40, radiosity=False, area=(5, 5),
+                                                            adaptive=1, orient=True), 2, 9.0),
     }
 
 
@@ -121,6 +124,8 @@ def main():
         sys.exit("build the reference first: make -C oracle/refbuild")
     with tempfile.TemporaryDirectory() as tmp:
         for case, (scene, stride, extent) in cases().items():
+            if len(sys.argv) > 1 and case not in sys.argv[1:]:
+                continue
             run(case, scene, stride, extent, tmp)
 
 

@@ -107,6 +107,24 @@ def test_csg_torus_grid_matches_oracle_with_aa():
         assert abs(st[k] - rst[k]) <= 2e-3 * rst[k], (k, st, rst)
 
 
+@pytest.mark.parametrize("variant", [
+    dict(),                                          # 4x4, Adaptive_Level 100: every grid point
+    dict(area=(5, 5), adaptive=1, orient=True),      # orient implies circular; adaptive refinement
+    dict(area=(8, 2), adaptive=0),                   # non-square grid, refinement only where corners differ
+], ids=["4x4", "5x5_adaptive1_orient", "8x2_adaptive0"])
+def test_area_light_room_matches_oracle(variant):
+    """Area-light shadows (TraceAreaLightShadowRay) in the 200-sphere room at
+    320x180: GPU vs oracle, pixels and shadow-ray counters."""
+    s = scenes.radiosity_room(320, 180, radiosity=False, **variant)
+    img, st = GpuScene(s).render()
+    ref, rst = Oracle(s).render(threads=0)
+    c = compare_pixels(img, ref)
+    assert c["within_1lsb"] >= PIX_FRAC, c
+    assert st["number_of_rays"] == rst["number_of_rays"]
+    for k in ("shadow_ray_tests", "shadow_rays_succeeded"):
+        assert abs(st[k] - rst[k]) <= 1e-3 * rst["shadow_ray_tests"], (k, st, rst)
+
+
 def test_mid_size_mesh_scene_matches_oracle():
     """1M-triangle mesh at 480x270: GPU vs oracle, pixels and counters."""
     s = scenes.mesh_spheres(480, 270)
