@@ -176,18 +176,19 @@ typedef struct PovGpuRadiosity {
     int32_t count;
     int32_t recursion_limit;
     int32_t nearest_count;
-    float   error_bound;
-    float   low_error_factor;
-    float   gray_threshold;
-    float   minimum_reuse;
-    float   maximum_reuse;
-    float   brightness;
-    float   pretrace_start;
-    float   pretrace_end;
-    float   adc_bailout;
+    double  error_bound;      /* the parser's doubles (SceneRadiositySettings) */
+    double  low_error_factor;
+    double  gray_threshold;
+    double  minimum_reuse;
+    double  maximum_reuse;
+    double  brightness;
+    double  pretrace_start;
+    double  pretrace_end;
+    double  adc_bailout;
     int32_t always_sample;
     int32_t normal;
     int32_t media;
+    int32_t reserved;
 } PovGpuRadiosity;
 
 typedef struct PovGpuSceneDesc {
@@ -239,10 +240,13 @@ typedef struct PovGpuStats {
     uint64_t reflected_rays;        /* Reflected_Rays_Traced                */
     uint64_t number_of_pixels;      /* Number_Of_Pixels                     */
     uint64_t number_of_samples;     /* Number_Of_Samples (AA)               */
-    uint64_t radiosity_gathers;
-    uint64_t radiosity_reuse;
+    uint64_t radiosity_gathers;     /* Radiosity samples calculated         */
+    uint64_t radiosity_reuse;       /* Radiosity samples reused             */
     uint64_t device_error;          /* raw device error word (0 = none)     */
-    uint64_t reserved[7];
+    uint64_t radiosity_rays;        /* Radiosity sample rays shot           */
+    uint64_t radiosity_gathers_d0;  /* samples calculated at bounce depth 0 */
+    uint64_t radiosity_gathers_d1;  /* samples calculated at bounce depth 1 */
+    uint64_t reserved[4];
 } PovGpuStats;
 
 /* One closest-hit result of pov_gpu_trace_rays. */

@@ -470,6 +470,7 @@ struct PovOracle {
     int32_t  nmeshes;
     Tree     top;            /* leaf item = object index */
     int32_t  top_linear;     /* no slabs: linear scan (trace.cpp:263) */
+    struct RadCache* rad;    /* radiosity sample cache (mutable during a render) */
 };
 
 static int max3_coordinate(double x, double y, double z)  /* mathutil */
@@ -1079,6 +1080,14 @@ typedef struct {
     int     counting;
     /* statistics of the render */
     uint64_t rays, shadow_tests, shadow_succeeded, reflected;
+    /* radiosity task state (RadiosityFunction, radiosity.cpp:297-330):
+     * final trace or pretrace, its error bound and pass, the position of
+     * each bounce depth's direction sequence, the top-level query count */
+    int      rad_final;
+    double   rad_error_bound;
+    int      rad_pass;
+    int      rad_dir_index[8];
+    uint64_t rad_top_queries;
 } Thread;
 
 /* Sphere::Intersect (sphere.cpp:214-245). */
@@ -1557,11 +1566,30 @@ static double area_light_fraction(const PovOracle* S, Thread* th, const PovGpuLi
     return area_subset(S, th, L, P, a1, a2, grid, 0, 0, L->area_size1 - 1, L->area_size2 - 1, 0, lc_dist);
 }
 
-static void trace_ray(const PovOracle* S, Thread* th, V3 O, V3 D, double weight, int level, RGB* col);
+/* TraceTicket (source/core/render/ray.h): trace level, its limit, the ADC
+ * bailout, radiosity bounce depth and sample quality. */
+typedef struct {
+    int    level;
+    int    max_level;
+    double adc;
+    int    rad_depth;
+    float  rad_quality;
+} Ticket;
+
+/* Ray kinds that change shading: radiosity sample rays skip highlights
+ * (trace.cpp:1714).  Pretrace camera rays would skip direct light
+ * (trace.cpp:1014-1015), but the renderer's default Radiosity_Vain_Pretrace
+ * (view.cpp:759) clears their pretrace flag (radiositytask.cpp:76), so
+ * they shade fully. */
+#define RAY_RADIOSITY 2
+
+static double trace_ray(const PovOracle* S, Thread* th, V3 O, V3 D, double weight, Ticket* tk, int flags, RGB* col);
+static void compute_ambient(const PovOracle* S, Thread* th, V3 ip, V3 raw, V3 layer, double brilliance, float amb[3],
+                            double weight, Ticket* tk);
 
 /* ComputeReflection (trace.cpp:1264-1321). */
 static void compute_reflection(const PovOracle* S, Thread* th, V3 ip, V3 D, V3 N, V3 raw, double weight,
-                               int level, RGB* col)
+                               Ticket* tk, RGB* col)
 {
     double n = -2.0 * vdot(D, N);
     V3 nd = vadd(D, vmul(N, n));
@@ -1578,13 +1606,16 @@ static void compute_reflection(const PovOracle* S, Thread* th, V3 ip, V3 D, V3 N
     }
     nd = vnorm(nd);
     th->reflected++;
-    trace_ray(S, th, ip, nd, weight, level, col);
+    trace_ray(S, th, ip, nd, weight, tk, 0, col);
 }
 
 /* ComputeTextureColour + ComputeLightedTexture (trace.cpp:457-586,739-1179)
  * for one plain layer with an opaque pigment. */
-static void shade(const PovOracle* S, Thread* th, const Isect* is, V3 D, double weight, int level, RGB* out)
+static void shade(const PovOracle* S, Thread* th, const Isect* is, V3 D, double weight, Ticket* tk, int flags,
+                  RGB* out)
 {
+    const int level = tk->level;
+    const int radiosity = S->desc.radiosity.enabled;
     const PovGpuObject* o = &S->objs[is->object].o;
     const PovGpuMaterial* m = object_material(S, is->object);
     V3 raw = object_normal(S, is);
@@ -1615,10 +1646,25 @@ static void shade(const PovOracle* S, Thread* th, const Isect* is, V3 D, double 
         reflec.b = (float)(frac * m->reflection_max[2] + (1.0 - frac) * m->reflection_min[2]);
     }
 
-    /* emission + ambient * ambient_light (radiosity off, trace.cpp:984-1004) */
+    /* radiosity ambient (trace.cpp:793-800,896-980): one query per hit
+     * while the bounce depth is below recursion_limit and the largest
+     * possible contribution beats the ADC bailout */
+    if (radiosity && tk->rad_depth < S->desc.radiosity.recursion_limit) {
+        double diffuse = m->diffuse;
+        float amb[3] = {0.0f, 0.0f, 0.0f};
+        double maxc = (0.297 * pig.r + 0.589 * pig.g + 0.114 * pig.b) * 1.0 * diffuse;   /* WeightGreyscale */
+        if (maxc > tk->adc)
+            compute_ambient(S, th, ip, raw, N, 1.0, amb, weight * maxc, tk);
+        r += (float)(pig.r * amb[0]) * diffuse;
+        g += (float)(pig.g * amb[1]) * diffuse;
+        b += (float)(pig.b * amb[2]) * diffuse;
+    }
+
+    /* emission, plus ambient * ambient_light when radiosity is off
+     * (trace.cpp:982-1004) */
     double em[3];
     for (int k = 0; k < 3; k++)
-        em[k] = m->emission[k] + m->ambient[k] * S->desc.ambient_light[k];
+        em[k] = m->emission[k] + (radiosity ? 0.0 : m->ambient[k] * S->desc.ambient_light[k]);
     r += pig.r * em[0];
     g += pig.g * em[1];
     b += pig.b * em[2];
@@ -1639,8 +1685,13 @@ static void shade(const PovOracle* S, Thread* th, const Isect* is, V3 D, double 
                 if (cs < EPSILON)
                     continue;
             }
-            if (level <= S->desc.max_trace_level) {   /* TraceShadowRay level check */
-                if (L->kind == POV_LIGHT_AREA) {
+            if (level > tk->max_level)   /* TraceShadowRay level check (trace.cpp:1897-1901) */
+                continue;
+            {
+                /* the radiosity Trace runs with areaLights off
+                 * (GetRadiosityQualityFlags, radiosity.cpp:148-161): inside a
+                 * gather an area light casts its centre's shadow */
+                if (L->kind == POV_LIGHT_AREA && tk->rad_depth == 0) {
                     double f = area_light_fraction(S, th, L, ip);
                     if (f == 0.0)
                         continue;
@@ -1660,8 +1711,8 @@ static void shade(const PovOracle* S, Thread* th, const Isect* is, V3 D, double 
                 g += inten * pig.g * lc[1];
                 b += inten * pig.b * lc[2];
             }
-            /* ComputePhongColour (trace.cpp:2520-2558) */
-            if (m->phong > 0.0f) {
+            /* ComputePhongColour (trace.cpp:2520-2558); not for radiosity rays */
+            if (m->phong > 0.0f && !(flags & RAY_RADIOSITY)) {
                 double c2 = -2.0 * vdot(D, N);
                 V3 rd = vadd(D, vmul(N, c2));
                 double ci = vdot(rd, ld);
@@ -1672,8 +1723,8 @@ static void shade(const PovOracle* S, Thread* th, const Isect* is, V3 D, double 
                     b += inten * lc[2];
                 }
             }
-            /* ComputeSpecularColour (trace.cpp:2560-2593) */
-            if (m->specular > 0.0f) {
+            /* ComputeSpecularColour (trace.cpp:2560-2593); not for radiosity rays */
+            if (m->specular > 0.0f && !(flags & RAY_RADIOSITY)) {
                 V3 half = vmul(vadd(vmul(D, -1.0), ld), 0.5);
                 double hl = vlen(half);
                 if (hl > 0.0) {
@@ -1692,7 +1743,7 @@ static void shade(const PovOracle* S, Thread* th, const Isect* is, V3 D, double 
     /* reflected component (trace.cpp:1155-1178) */
     if (!(reflec.r == 0.0f && reflec.g == 0.0f && reflec.b == 0.0f)) {
         RGB rc = {0, 0, 0};
-        compute_reflection(S, th, ip, D, N, raw, rweight, level, &rc);
+        compute_reflection(S, th, ip, D, N, raw, rweight, tk, &rc);
         r += reflec.r * rc.r;
         g += reflec.g * rc.g;
         b += reflec.b * rc.b;
@@ -1702,23 +1753,503 @@ static void shade(const PovOracle* S, Thread* th, const Isect* is, V3 D, double 
     out->b = (float)b;
 }
 
-/* Trace::TraceRay (trace.cpp:135-228).  `level` is the trace level before
- * this ray (TraceTicket::traceLevel). */
-static void trace_ray(const PovOracle* S, Thread* th, V3 O, V3 D, double weight, int level, RGB* col)
+/* Trace::TraceRay (trace.cpp:135-228): the ticket's level is raised while
+ * the hit is shaded.  Returns the hit depth, HUGE_VAL for a miss or a ray
+ * that bails at the trace level or ADC check. */
+static double trace_ray(const PovOracle* S, Thread* th, V3 O, V3 D, double weight, Ticket* tk, int flags, RGB* col)
 {
     th->rays++;   /* Number_Of_Rays */
     col->r = col->g = col->b = 0.0f;
-    if (level >= S->desc.max_trace_level || weight < S->desc.adc_bailout)
-        return;
+    if (tk->level >= tk->max_level || weight < tk->adc)
+        return HUGE_VAL;
     Isect is;
+    double depth = HUGE_VAL;
+    tk->level++;
     if (find_intersection(S, th, O, D, HUGE_VAL, 0, &is)) {
-        shade(S, th, &is, D, weight, level + 1, col);
+        depth = is.depth;
+        shade(S, th, &is, D, weight, tk, flags, col);
     } else {
         /* ComputeSky: background only (trace.cpp:2839-2888) */
         col->r = S->desc.background[0];
         col->g = S->desc.background[1];
         col->b = S->desc.background[2];
     }
+    tk->level--;
+    return depth;
+}
+
+/* ============================================================ radiosity ==
+ * RadiosityFunction and RadiosityCache (source/core/lighting/radiosity.cpp)
+ * with the octree addressing of source/core/support/octree.cpp.  The cache
+ * is one object per render; renders with radiosity run on one thread in
+ * the reference's single-thread order (pov_oracle_render). */
+
+#define RAD_EPSILON               0.001      /* radiosity.cpp:110 */
+#define AVG_NEAR_EPSILON          0.000001   /* radiosity.cpp:109 */
+#define IN_FRONT_LIMIT            (-0.05)    /* radiosity.cpp:100 */
+#define WEIGHT_ERROR_BOUND_OFFSET 0.25       /* radiosity.cpp:111 */
+#define BRILLIANCE_EPSILON        1e-5       /* radiosity.cpp:116 */
+#define OT_BIAS                   10000000.  /* octree.h:81 */
+#define RAD_DIRECTIONS            1600       /* RADIOSITY_MAX_SAMPLE_DIRECTIONS */
+#define RAD_MAX_DEPTH             8
+#define PASS_FIRST                1          /* kOctreePassFirst */
+#define PASS_FINAL                65535      /* kOctreePassFinal (unsigned short max) */
+
+/* RadiosityRecursionSettings (radiosity.cpp:177-294). */
+typedef struct {
+    int    rays_per_sample, reuse_count, trace_level;
+    double error_bound_factor, min_reuse_factor, max_reuse_factor, address_factor, weight;
+} RadRec;
+
+/* ot_block_struct (octree.h:86-104). */
+typedef struct {
+    V3    point, normal, to_nearest;
+    float ill[3];
+    float hmd, nearest, quality, brilliance;
+    int   depth, pass;
+    int   next;          /* next block of the same octree node */
+} RadBlock;
+
+typedef struct { int size, x, y, z; } OtId;   /* OT_ID: biased log2 size, cell */
+
+typedef struct RadCache {
+    RadBlock* blocks;
+    int       nblocks, cap;
+    OtId*     keys;      /* octree nodes: open-addressing hash -> head block */
+    int*      heads;
+    int       nslots, nnodes;
+    int       min_size, max_size;
+    RadRec    rec[RAD_MAX_DEPTH];
+    V3        dirs[RAD_DIRECTIONS];
+    const double* jitter;
+    int       njitter;
+    uint64_t  gathers, reused, rays, pixels;
+    uint64_t  gathers_depth[RAD_MAX_DEPTH];
+} RadCache;
+
+/* HaltonGenerator::operator[] (source/core/math/randomsequence.cpp:730-747). */
+static double halton(unsigned base, size_t index)
+{
+    size_t i = 1 + index;
+    double h = 0.0, q = 1.0 / base;
+    while (i > 0) {
+        h += (double)(i % base) * q;
+        i /= base;
+        q /= base;
+    }
+    return h;
+}
+
+/* SceneRadiositySettings::GetRecursionSettings (radiosity.cpp:177-294) and
+ * the direction pool GetSubRandomCosWeightedDirectionGenerator(0, 1600)
+ * picks (randomsequence.cpp:1019-1037): 1600 is not below the legacy
+ * table's size, so it is the Halton(2, 3) cosine-weighted sequence
+ * (HaltonCosWeightedDirectionGenerator, randomsequence.cpp:907-915). */
+static void rad_setup(RadCache* R, const PovGpuRadiosity* rs)
+{
+    for (int d = 0; d < RAD_MAX_DEPTH; d++) {
+        RadRec* r = &R->rec[d];
+        int n = (int)(rs->count * pow(0.5, (double)d));
+        r->rays_per_sample = n > 5 ? n : 5;
+        r->reuse_count = d == 0 ? rs->nearest_count : (d == 1 ? (rs->nearest_count < 2 ? rs->nearest_count : 2) : 1);
+        r->error_bound_factor = pow(2.0, (double)d);
+        r->min_reuse_factor = rs->minimum_reuse * pow(2.0, (double)d);
+        r->max_reuse_factor = rs->maximum_reuse * pow(2.0, (double)d);
+        double overfill = d == 0 ? 1.0 : 8.0;
+        r->trace_level = (int)(1.5 * ((double)d + 1));
+        r->weight = pow(0.5 * rs->brightness, (double)d + 1);
+        double max_error_bound = rs->error_bound * r->error_bound_factor;
+        r->address_factor = max_error_bound / overfill;
+    }
+    for (int i = 0; i < RAD_DIRECTIONS; i++) {
+        double rr = sqrt(halton(2, (size_t)i));
+        double th = halton(3, (size_t)i) * (2 * 3.14159265358979323846);   /* 2*M_PI */
+        double x = rr * cos(th), z = rr * sin(th);
+        R->dirs[i] = v3(x, sqrt(1 - x * x - z * z), z);
+    }
+}
+
+static void rad_reset(RadCache* R)
+{
+    R->nblocks = 0;
+    R->nnodes = 0;
+    for (int i = 0; i < R->nslots; i++)
+        R->keys[i].size = -1;
+    R->min_size = 1 << 30;
+    R->max_size = -1;
+    R->gathers = R->reused = R->rays = R->pixels = 0;
+    memset(R->gathers_depth, 0, sizeof(R->gathers_depth));
+}
+
+static RadCache* rad_create(const PovGpuRadiosity* rs)
+{
+    RadCache* R = (RadCache*)calloc(1, sizeof(RadCache));
+    R->nslots = 1 << 16;
+    R->keys = (OtId*)malloc(sizeof(OtId) * R->nslots);
+    R->heads = (int*)malloc(sizeof(int) * R->nslots);
+    rad_setup(R, rs);
+    rad_reset(R);
+    return R;
+}
+
+static void rad_free(RadCache* R)
+{
+    if (!R) return;
+    free(R->blocks);
+    free(R->keys);
+    free(R->heads);
+    free(R);
+}
+
+/* Pow2Floor / BiasedIntLog2 / BiasedIntPow2 (octree.cpp:169-250): float
+ * exponent arithmetic. */
+static float pow2_floor(float a)
+{
+    uint32_t i;
+    memcpy(&i, &a, 4);
+    i &= 0xFF800000u;
+    memcpy(&a, &i, 4);
+    return a;
+}
+static int biased_log2(float a)
+{
+    uint32_t i;
+    memcpy(&i, &a, 4);
+    return (int)((i & 0x7F800000u) >> 23);
+}
+static float biased_pow2(int e)
+{
+    uint32_t i = ((uint32_t)e & 0xFFu) << 23;
+    float a;
+    memcpy(&a, &i, 4);
+    return a;
+}
+
+/* ot_point_in_node (octree.cpp:985-997). */
+static int ot_point_in_node(V3 p, const OtId* id)
+{
+    double sized = biased_pow2(id->size);
+    if (fabs(p.x + OT_BIAS - ((double)id->x + 0.5) * sized) >= sized) return 0;
+    if (fabs(p.y + OT_BIAS - ((double)id->y + 0.5) * sized) >= sized) return 0;
+    if (fabs(p.z + OT_BIAS - ((double)id->z + 0.5) * sized) >= sized) return 0;
+    return 1;
+}
+
+/* ot_index_sphere / ot_index_box with SAFE_METHOD (octree.cpp:1035-1190),
+ * ot_parent (octree.cpp:1220-1238). */
+static OtId ot_index_sphere(V3 c, double radius)
+{
+    V3 lo = v3(c.x - radius, c.y - radius, c.z - radius), hi = v3(c.x + radius, c.y + radius, c.z + radius);
+    double desired = fmax(fmax(hi.x - lo.x, hi.y - lo.y), hi.z - lo.z);
+    double bsized = pow2_floor((float)desired);
+    if (bsized == 0.0)
+        bsized = 1.0;
+    double maxord = fmax(fmax(fabs(lo.x), fabs(lo.y)), fabs(lo.z)) + OT_BIAS;
+    while (maxord / bsized > 1000000000.0)
+        bsized *= 2.0;
+    V3 ctr = vdiv(vadd(lo, hi), 2);
+    OtId id;
+    id.x = (int)floor((ctr.x + OT_BIAS) / bsized);
+    id.y = (int)floor((ctr.y + OT_BIAS) / bsized);
+    id.z = (int)floor((ctr.z + OT_BIAS) / bsized);
+    id.size = biased_log2((float)bsized);
+    while (!ot_point_in_node(lo, &id) || !ot_point_in_node(hi, &id)) {
+        id.size += 1;
+        id.x = id.x >= 0 ? id.x >> 1 : (id.x + 1) / 2;
+        id.y = id.y >= 0 ? id.y >> 1 : (id.y + 1) / 2;
+        id.z = id.z >= 0 ? id.z >> 1 : (id.z + 1) / 2;
+    }
+    return id;
+}
+
+static uint32_t ot_hash(const OtId* k)
+{
+    uint32_t h = (uint32_t)k->size * 0x9E3779B1u;
+    h ^= (uint32_t)k->x * 0x85EBCA77u;
+    h ^= (uint32_t)k->y * 0xC2B2AE3Du;
+    h ^= (uint32_t)k->z * 0x27D4EB2Fu;
+    return h ^ (h >> 15);
+}
+
+static int ot_slot(const RadCache* R, const OtId* k)
+{
+    uint32_t m = (uint32_t)R->nslots - 1, i = ot_hash(k) & m;
+    for (;;) {
+        const OtId* e = &R->keys[i];
+        if (e->size < 0 || (e->size == k->size && e->x == k->x && e->y == k->y && e->z == k->z))
+            return (int)i;
+        i = (i + 1) & m;
+    }
+}
+
+static void ot_grow(RadCache* R)
+{
+    OtId* ok = R->keys;
+    int* oh = R->heads;
+    int on = R->nslots;
+    R->nslots *= 2;
+    R->keys = (OtId*)malloc(sizeof(OtId) * R->nslots);
+    R->heads = (int*)malloc(sizeof(int) * R->nslots);
+    for (int i = 0; i < R->nslots; i++)
+        R->keys[i].size = -1;
+    for (int i = 0; i < on; i++)
+        if (ok[i].size >= 0) {
+            int j = ot_slot(R, &ok[i]);
+            R->keys[j] = ok[i];
+            R->heads[j] = oh[i];
+        }
+    free(ok);
+    free(oh);
+}
+
+/* RadiosityCache::AddBlock (radiosity.cpp:1194-1233) and InsertBlock
+ * (radiosity.cpp:1421-1429: new blocks go to the head of the node's list). */
+static void rad_add_block(RadCache* R, V3 point, V3 normal, double brilliance, V3 to_nearest, const float ill[3],
+                          double hmd, double nearest, double quality, int depth, int pass)
+{
+    if (R->nblocks == R->cap) {
+        R->cap = R->cap ? 2 * R->cap : 4096;
+        R->blocks = (RadBlock*)realloc(R->blocks, sizeof(RadBlock) * R->cap);
+    }
+    RadBlock* b = &R->blocks[R->nblocks];
+    b->ill[0] = ill[0]; b->ill[1] = ill[1]; b->ill[2] = ill[2];
+    b->to_nearest = to_nearest;
+    b->brilliance = (float)brilliance;
+    b->hmd = (float)hmd;
+    b->nearest = (float)nearest;
+    b->quality = (float)quality;
+    b->depth = depth;
+    b->pass = pass;
+    b->point = point;
+    b->normal = normal;
+    OtId id = ot_index_sphere(point, hmd * R->rec[depth].address_factor);
+    if (2 * (R->nnodes + 1) > R->nslots)
+        ot_grow(R);
+    int slot = ot_slot(R, &id);
+    if (R->keys[slot].size < 0) {
+        R->keys[slot] = id;
+        R->heads[slot] = -1;
+        R->nnodes++;
+    }
+    b->next = R->heads[slot];
+    R->heads[slot] = R->nblocks++;
+    if (id.size < R->min_size) R->min_size = id.size;
+    if (id.size > R->max_size) R->max_size = id.size;
+}
+
+/* WT_AVG of RadiosityCache::FindReusableBlock (radiosity.cpp:1458-1549). */
+typedef struct {
+    V3     P, N;
+    double brilliance, error_bound, weights;
+    float  wi[3];
+    int    pass;
+} WtAvg;
+
+/* RadiosityCache::AverageNearBlock (radiosity.cpp:1551-1770), pseudo-sigmoid
+ * weighting at final trace depth 0, linear otherwise; no gradient. */
+static void rad_average_near(const RadBlock* b, WtAvg* w)
+{
+    if (fabs(b->brilliance - w->brilliance) > BRILLIANCE_EPSILON)
+        return;
+    V3 delta = vsub(w->P, b->point);
+    double sq = vdot(delta, delta);
+    double quick = (double)b->hmd * w->error_bound;
+    if (!(sq < quick * quick))
+        return;
+    double dist = sqrt(sq);
+    double ri = b->hmd;
+    int far = dist > AVG_NEAR_EPSILON;
+    V3 du = v3(0, 0, 0);
+    if (far) {
+        du = vdiv(delta, dist);
+        double c = vdot(b->to_nearest, du);
+        if (c > 0.0)
+            ri = c * (double)b->nearest + (1.0 - c) * ri;
+    }
+    if (!(dist < ri * w->error_bound))
+        return;
+    double dd = vdot(w->N, b->normal);
+    double e = dist / ri + 2.0 * sqrt(fabs(1.0 - dd));
+    if (!(e < w->error_bound))
+        return;
+    double in_front = 1.0;
+    if (far) {
+        V3 half = vadd(w->N, b->normal);
+        in_front = vdot(du, half) / vlen(half);
+    }
+    if (!(in_front > IN_FRONT_LIMIT))
+        return;
+    double wt;
+    if (w->pass != PASS_FINAL || b->depth > 0) {
+        wt = 1.0 - e / w->error_bound;
+    } else {
+        wt = e / w->error_bound;
+        if (wt < 0.5)
+            wt = 1.0 - (wt * 2.0) * (wt * 2.0) / 2.0;
+        else
+            wt = ((1.0 - wt) * 2.0) * ((1.0 - wt) * 2.0) / 2.0;
+    }
+    if (in_front <= 0)
+        wt *= 1 - in_front / IN_FRONT_LIMIT;
+    if (wt > RAD_EPSILON) {
+        wt *= b->quality;
+        for (int k = 0; k < 3; k++)
+            w->wi[k] += (float)(b->ill[k] * wt);
+        w->weights += wt;
+    }
+}
+
+/* RadiosityCache::FindReusableBlock (radiosity.cpp:1458-1512) over the
+ * octree nodes whose half-size-extended box holds P (ot_dist_traverse,
+ * octree.cpp:800-855, visits exactly those), only blocks of this bounce
+ * depth.  Returns the summed weight; sets ill when it is positive. */
+static double rad_find_reusable(const RadCache* R, double error_bound, V3 P, V3 N, double brilliance, float ill[3],
+                                int depth, int pass)
+{
+    if (R->nblocks == 0)
+        return 0.0;
+    WtAvg w;
+    memset(&w, 0, sizeof(w));
+    w.P = P; w.N = N; w.brilliance = brilliance; w.error_bound = error_bound; w.pass = pass;
+    double c[3] = {P.x + OT_BIAS, P.y + OT_BIAS, P.z + OT_BIAS};
+    for (int size = R->min_size; size <= R->max_size; size++) {
+        double sz = biased_pow2(size);
+        int lo[3], n[3];
+        for (int a = 0; a < 3; a++) {
+            lo[a] = (int)floor(c[a] / sz - 1.5);
+            n[a] = 4;
+        }
+        for (int i = 0; i < n[0]; i++)
+            for (int j = 0; j < n[1]; j++)
+                for (int k = 0; k < n[2]; k++) {
+                    OtId id = {size, lo[0] + i, lo[1] + j, lo[2] + k};
+                    if (!ot_point_in_node(P, &id))
+                        continue;
+                    int slot = ot_slot(R, &id);
+                    if (R->keys[slot].size < 0)
+                        continue;
+                    for (int bi = R->heads[slot]; bi >= 0; bi = R->blocks[bi].next)
+                        if (R->blocks[bi].depth == depth)
+                            rad_average_near(&R->blocks[bi], &w);
+                }
+    }
+    if (w.weights > 0)
+        for (int k = 0; k < 3; k++)
+            ill[k] = (float)(w.wi[k] / w.weights);
+    return w.weights;
+}
+
+/* RadiosityFunction::GatherLight (radiosity.cpp:509-756) with the
+ * SampleDirectionGenerator of an unperturbed normal (radiosity.cpp:772-888):
+ * every direction of the bounce depth's sequence is usable. */
+static double gather_light(const PovOracle* S, Thread* th, V3 ip, V3 raw, double brilliance, float ill[3],
+                           Ticket* tk)
+{
+    RadCache* R = S->rad;
+    const PovGpuRadiosity* rs = &S->desc.radiosity;
+    const int depth = tk->rad_depth;
+    const RadRec* rec = &R->rec[depth];
+    double to_eye = vlen(vsub(vload(S->desc.camera.location), ip));
+    double reuse_dist_min = to_eye * rec->min_reuse_factor;
+    double maximum_distance = to_eye * rec->max_reuse_factor;
+    int count = rec->rays_per_sample < RAD_DIRECTIONS ? rec->rays_per_sample : RAD_DIRECTIONS;
+    Ticket save = *tk;
+    tk->level = rec->trace_level;
+    if (tk->max_level < tk->level + 1)
+        tk->max_level = tk->level + 1;
+    tk->adc = rs->adc_bailout;
+    double inverse_distance_sum = 0.0, smallest = BOUND_HUGE;
+    V3 min_dist_vec = v3(0, 0, 0);
+    double weight = fmax(tk->adc + EPSILON, rec->weight);
+    double qsum = 0.0;
+    float sums[3] = {0.0f, 0.0f, 0.0f};
+    /* InitSequence: frame around the normal */
+    V3 fy = raw;
+    V3 off = fabs(fy.z) > 0.9 ? v3(0, 1, 0) : v3(0, 0, 1);
+    V3 fx = vnorm(vcross(fy, off));
+    V3 fz = vnorm(vcross(fx, fy));
+    int* idx = &th->rad_dir_index[depth];
+    for (int i = 0; i < count; i++) {
+        V3 rv = R->dirs[*idx];
+        *idx = (*idx + 1) % RAD_DIRECTIONS;
+        rv.y = fabs(rv.y);
+        V3 dir;
+        if (fy.y > 1.0 - RAD_EPSILON)
+            dir = rv;
+        else if (fy.y < -1.0 + RAD_EPSILON)
+            dir = vmul(rv, -1.0);
+        else
+            dir = vadd(vadd(vmul(fx, rv.x), vmul(fy, rv.y)), vmul(fz, rv.z));
+        tk->rad_quality = 1.0f;
+        tk->rad_depth++;
+        RGB c;
+        double d = trace_ray(S, th, ip, dir, weight, tk, RAY_RADIOSITY, &c);
+        tk->rad_depth--;
+        double quality = tk->rad_quality;
+        qsum += quality;
+        sums[0] += (float)(c.r * quality);
+        sums[1] += (float)(c.g * quality);
+        sums[2] += (float)(c.b * quality);
+        if (d < smallest) {
+            smallest = d;
+            min_dist_vec = dir;
+        }
+        inverse_distance_sum += 1.0 / d;
+    }
+    R->rays += (uint64_t)count;
+    for (int k = 0; k < 3; k++)
+        ill[k] = qsum == 0 ? sums[k] : (float)(sums[k] / qsum);
+    double mean_dist = count / inverse_distance_sum;
+    if (smallest > maximum_distance * 0.0001) {
+        if (mean_dist < reuse_dist_min)
+            mean_dist = reuse_dist_min;
+        if (mean_dist > maximum_distance)
+            mean_dist = maximum_distance;
+        rad_add_block(R, ip, raw, brilliance, min_dist_vec, ill, mean_dist, smallest, qsum / count, depth,
+                      th->rad_pass);
+    }
+    tk->max_level = save.max_level;
+    tk->level = save.level;
+    tk->adc = save.adc;
+    tk->rad_quality = (float)fmax(save.rad_quality, qsum / count);
+    return qsum / count;
+}
+
+/* RadiosityFunction::ComputeAmbient (radiosity.cpp:385-462), "normal" and
+ * "brilliance" settings off (their defaults). */
+static void compute_ambient(const PovOracle* S, Thread* th, V3 ip, V3 raw, V3 layer, double brilliance, float amb[3],
+                            double weight, Ticket* tk)
+{
+    (void)layer;
+    (void)brilliance;
+    RadCache* R = S->rad;
+    const PovGpuRadiosity* rs = &S->desc.radiosity;
+    const RadRec* rec = &R->rec[tk->rad_depth];
+    double eb = th->rad_error_bound;
+    if (weight < WEIGHT_ERROR_BOUND_OFFSET)
+        eb += WEIGHT_ERROR_BOUND_OFFSET - weight;
+    if (tk->rad_depth == 0)
+        th->rad_top_queries++;
+    double reuse = rad_find_reusable(R, eb * rec->error_bound_factor, ip, raw, 1.0, amb, tk->rad_depth,
+                                     th->rad_pass);
+    if (reuse * 4 >= rec->reuse_count || (th->rad_final && !rs->always_sample && reuse > 0)) {
+        R->reused++;
+    } else {
+        float tmp[3];
+        double quality = gather_light(S, th, ip, raw, 1.0, tmp, tk);
+        for (int k = 0; k < 3; k++)
+            amb[k] = reuse > 0 ? (float)((float)((float)(amb[k] * reuse) + (float)(tmp[k] * quality)) / (reuse + quality))
+                               : tmp[k];
+        reuse += quality;
+        R->gathers++;
+        R->gathers_depth[tk->rad_depth]++;
+    }
+    float q = (float)(4 * reuse) / (float)rec->reuse_count;
+    tk->rad_quality = q < tk->rad_quality ? q : tk->rad_quality;
+    float gray = (float)rs->gray_threshold;
+    float grey = (float)(0.297 * amb[0] + 0.589 * amb[1] + 0.114 * amb[2]);
+    for (int k = 0; k < 3; k++)
+        amb[k] = (float)((amb[k] * (1.0f - gray) + gray * grey) * rs->brightness);
 }
 
 /* ----------------------------------------------------------- build --- */
@@ -1876,6 +2407,8 @@ int pov_oracle_create(const PovGpuSceneDesc* desc, PovOracle** out, int32_t* bad
     }
     PovOracle* S = (PovOracle*)calloc(1, sizeof(PovOracle));
     S->desc = *desc;
+    if (desc->radiosity.enabled)
+        S->rad = rad_create(&desc->radiosity);
     S->nobjs = desc->num_objects;
     S->objs = (OObj*)calloc((size_t)(S->nobjs > 0 ? S->nobjs : 1), sizeof(OObj));
     S->mats = (PovGpuMaterial*)malloc(sizeof(PovGpuMaterial) * desc->num_materials);
@@ -1967,6 +2500,7 @@ void pov_oracle_destroy(PovOracle* S)
     free(S->objs);
     free(S->mats);
     free(S->lights);
+    rad_free(S->rad);
     free(S);
 }
 
@@ -2019,7 +2553,8 @@ static void trace_pixel(const PovOracle* S, Thread* th, double x, double y, doub
     V3 D = vadd(vadd(vload(c->direction), vmul(vload(c->right), x0)), vmul(vload(c->up), y0));
     D = vnorm(D);
     RGB col;
-    trace_ray(S, th, vload(c->location), D, 1.0, 0, &col);
+    Ticket tk = {0, S->desc.max_trace_level, S->desc.adc_bailout, 0, 1.0f};
+    trace_ray(S, th, vload(c->location), D, 1.0, &tk, 0, &col);
     rgbt[0] = col.r;
     rgbt[1] = col.g;
     rgbt[2] = col.b;
@@ -2217,11 +2752,127 @@ static void* render_worker(void* arg)
     return NULL;
 }
 
+/* Radiosity render in the reference's single-thread order: the pretrace
+ * of View::StartRender (view.cpp:1056-1123) as RadiosityTask::Run
+ * (radiositytask.cpp:95-263) runs it without high reproducibility -- pass
+ * after pass over the 32x32 blocks in serial order, jitter from the task's
+ * table -- then the final trace of the requested pixels block by block
+ * (TraceTask::SimpleSamplingM0, tracetask.cpp:403-454) with a fresh
+ * RadiosityFunction (final trace: full error bound, own direction
+ * sequences) on the same cache. */
+static int render_radiosity(PovOracle* S, const PovGpuRenderParams* p, int32_t x0, int32_t y0, int32_t x1,
+                            int32_t y1, float* out, PovGpuStats* stats)
+{
+    RadCache* R = S->rad;
+    const PovGpuRadiosity* rs = &S->desc.radiosity;
+    if (!R->jitter || p->antialias)
+        return POV_GPU_E_UNSUPPORTED;
+    rad_reset(R);
+    const int W = p->width, H = p->height, B = 32;
+    const int bw = (W + B - 1) / B, bh = (H + B - 1) / B, nb = bw * bh;
+    Thread th;
+    memset(&th, 0, sizeof(th));
+    double maxwh = (double)(W > H ? W : H);
+    double start = maxwh * rs->pretrace_start, end = maxwh * rs->pretrace_end;
+    if (end < 1.0)
+        end = 1.0;
+    int steps = (int)floor(log(start / end) / log(2.0) + (1.0 - EPSILON)) + 1;
+    if (steps > 253) {
+        steps = 253;
+        start = end * pow(2.0, (double)steps);
+    }
+    /* pretrace task */
+    th.rad_final = 0;
+    th.rad_error_bound = rs->error_bound * rs->low_error_factor;
+    char* active = (char*)malloc((size_t)nb);
+    memset(active, 1, (size_t)nb);
+    float rgbt[4];
+    for (int pass = 0; pass < steps; pass++) {
+        double size = fmax(start * pow(0.5f, (float)pass), end);
+        double jit = fmin(1.0, size / 2.0), offset = (size - 1.0) / 2.0;
+        for (int serial = 0; serial < nb; serial++) {
+            if (!active[serial])
+                continue;
+            int left = (serial % bw) * B, top = (serial / bw) * B;
+            int right = left + B - 1 < W - 1 ? left + B - 1 : W - 1;
+            int bottom = top + B - 1 < H - 1 ? top + B - 1 : H - 1;
+            th.rad_pass = PASS_FIRST + pass;
+            size_t ji = (size_t)((PASS_FIRST + pass) * 17 + serial * 13) % (size_t)R->njitter;
+            double sx = ceil((left - 0.5) / size) * size, sy = ceil((top - 0.5) / size) * size;
+            double ex = left + (double)(right - left + 1), ey = top + (double)(bottom - top + 1);
+            th.rad_top_queries = 0;
+            int count = 0;
+            for (double y = sy; y < ey; y += size) {
+                if (y < top)
+                    continue;
+                for (double x = sx; x < ex; x += size) {
+                    if (x < left)
+                        continue;
+                    /* the reference's compiler evaluates the second
+                     * argument's jitter first */
+                    ji = (ji + 1) % (size_t)R->njitter;
+                    double jy = R->jitter[ji];
+                    ji = (ji + 1) % (size_t)R->njitter;
+                    double jx = R->jitter[ji];
+                    trace_pixel(S, &th, x + offset + jit * jx, y + offset + jit * jy, W, H, rgbt);
+                    count++;
+                }
+            }
+            R->pixels += (uint64_t)count;
+            /* another pass unless the block saw no radiosity query at all */
+            if (count >= 9 && th.rad_top_queries == 0)
+                active[serial] = 0;
+        }
+    }
+    free(active);
+    /* final trace */
+    memset(th.rad_dir_index, 0, sizeof(th.rad_dir_index));
+    th.rad_final = 1;
+    th.rad_error_bound = rs->error_bound;
+    th.rad_pass = PASS_FINAL;
+    int32_t w = x1 - x0;
+    for (int serial = 0; serial < nb; serial++) {
+        int left = (serial % bw) * B, top = (serial / bw) * B;
+        for (int y = top; y < top + B && y < H; y++)
+            for (int x = left; x < left + B && x < W; x++) {
+                if (x < x0 || x >= x1 || y < y0 || y >= y1)
+                    continue;
+                trace_pixel(S, &th, x + 0.5, y + 0.5, W, H, out + ((size_t)(y - y0) * w + (x - x0)) * 4);
+            }
+    }
+    if (stats) {
+        memset(stats, 0, sizeof(*stats));
+        stats->number_of_rays = th.rays;
+        stats->shadow_ray_tests = th.shadow_tests;
+        stats->shadow_rays_succeeded = th.shadow_succeeded;
+        stats->reflected_rays = th.reflected;
+        stats->number_of_pixels = (uint64_t)(x1 - x0) * (uint64_t)(y1 - y0) + R->pixels;
+        stats->radiosity_gathers = R->gathers;
+        stats->radiosity_reuse = R->reused;
+        stats->radiosity_rays = R->rays;
+        stats->radiosity_gathers_d0 = R->gathers_depth[0];
+        stats->radiosity_gathers_d1 = R->gathers_depth[1];
+    }
+    thread_free(&th);
+    return POV_GPU_OK;
+}
+
+int pov_oracle_set_pretrace_jitter(PovOracle* S, const double* table, int32_t n)
+{
+    if (!S || !S->rad || !table || n <= 0)
+        return POV_GPU_E_INVALID;
+    S->rad->jitter = table;
+    S->rad->njitter = n;
+    return POV_GPU_OK;
+}
+
 int pov_oracle_render(PovOracle* S, const PovGpuRenderParams* p, int32_t x0, int32_t y0, int32_t x1,
                       int32_t y1, int32_t threads, float* out, PovGpuStats* stats)
 {
     if (!S || !p || !out || x1 < x0 || y1 < y0)
         return POV_GPU_E_INVALID;
+    if (S->desc.radiosity.enabled)
+        return render_radiosity(S, p, x0, y0, x1, y1, out, stats);
     int aa = p->antialias != 0;
     if (aa && (p->sampling_method != 2 || p->jitter))
         return POV_GPU_E_UNSUPPORTED;

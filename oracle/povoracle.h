@@ -32,6 +32,11 @@ int  pov_oracle_trace_rays(PovOracle* o, const double* origins, const double* di
 int  pov_oracle_render(PovOracle* o, const PovGpuRenderParams* params, int32_t x0, int32_t y0,
                        int32_t x1, int32_t y1, int32_t threads, float* out_rgbt, PovGpuStats* stats);
 
+/* Radiosity renders need the reference's pretrace jitter table
+ * (RadiosityTask's RandomDoubleSequence, tests/golden/pretrace_jitter.npy);
+ * the table is borrowed, not copied. */
+int  pov_oracle_set_pretrace_jitter(PovOracle* o, const double* table, int32_t n);
+
 /* Per-ray work counters of the restated traversal, for the roofline byte
  * model: node boxes tested and primitives tested over the given rays. */
 int  pov_oracle_count_work(PovOracle* o, const double* origins, const double* directions,

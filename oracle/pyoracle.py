@@ -24,6 +24,7 @@ def build(force=False):
 
 
 _lib = None
+JITTER_TABLE = os.path.join(os.path.dirname(HERE), "tests", "golden", "pretrace_jitter.npy")
 
 
 def lib():
@@ -47,6 +48,8 @@ def lib():
         L.pov_oracle_count_work.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
                                             C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
         L.pov_oracle_count_work.restype = C.c_int
+        L.pov_oracle_set_pretrace_jitter.argtypes = [C.c_void_p, C.c_void_p, C.c_int32]
+        L.pov_oracle_set_pretrace_jitter.restype = C.c_int
         _lib = L
     return _lib
 
@@ -64,6 +67,11 @@ class Oracle:
         if st != 0:
             raise abi.PovGpuError(st, "pov_oracle_create", bad.value)
         self.h = h
+        if scene.radiosity is not None:
+            # the reference's pretrace jitter table, dumped from it by
+            # tests/golden/make_golden.py
+            self._jitter = np.ascontiguousarray(np.load(JITTER_TABLE), dtype=np.float64)
+            lib().pov_oracle_set_pretrace_jitter(self.h, self._jitter.ctypes.data, len(self._jitter))
 
     def close(self):
         if self.h:

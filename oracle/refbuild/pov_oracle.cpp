@@ -38,6 +38,7 @@
 #include "core/bounding/boundingbox.h"
 #include "core/lighting/lightsource.h"
 #include "core/math/matrix.h"
+#include "core/math/randomsequence.h"
 #include "core/render/ray.h"
 #include "core/render/trace.h"
 #include "core/render/tracepixel.h"
@@ -196,13 +197,28 @@ int main(int argc, char **argv)
         std::signal(SIGSEGV, OnSegv);
     if (argc < 6)
     {
-        std::fprintf(stderr, "usage: pov_oracle SCENE W H pixels|rays|scene ...\n");
+        std::fprintf(stderr, "usage: pov_oracle SCENE W H pixels|rays|scene|jitter ...\n");
         return 2;
     }
     const char *scene = argv[1];
     int width = std::atoi(argv[2]);
     int height = std::atoi(argv[3]);
     std::string mode = argv[4];
+
+    if (mode == "jitter")
+    {
+        // the pretrace jitter table of RadiosityTask::Run (radiositytask.cpp:99):
+        // RandomDoubleSequence(-1, 1, 2047), as the reference generates it
+        pov::RandomDoubleSequence rands(-1.0, 1.0, 2047);
+        FILE *f = std::fopen(argv[5], "wb");
+        for (size_t i = 0; i < 2047; i++)
+        {
+            double v = rands(i);
+            std::fwrite(&v, sizeof(v), 1, f);
+        }
+        std::fclose(f);
+        return 0;
+    }
 
     DefaultPlatformBase platform;  // file access for the parser (vfe provides this in the CLI)
     try

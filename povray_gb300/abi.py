@@ -89,12 +89,13 @@ class PovGpuCamera(C.Structure):
 
 class PovGpuRadiosity(C.Structure):
     _fields_ = [("enabled", C.c_int32), ("count", C.c_int32), ("recursion_limit", C.c_int32),
-                ("nearest_count", C.c_int32), ("error_bound", C.c_float),
-                ("low_error_factor", C.c_float), ("gray_threshold", C.c_float),
-                ("minimum_reuse", C.c_float), ("maximum_reuse", C.c_float),
-                ("brightness", C.c_float), ("pretrace_start", C.c_float),
-                ("pretrace_end", C.c_float), ("adc_bailout", C.c_float),
-                ("always_sample", C.c_int32), ("normal", C.c_int32), ("media", C.c_int32)]
+                ("nearest_count", C.c_int32), ("error_bound", C.c_double),
+                ("low_error_factor", C.c_double), ("gray_threshold", C.c_double),
+                ("minimum_reuse", C.c_double), ("maximum_reuse", C.c_double),
+                ("brightness", C.c_double), ("pretrace_start", C.c_double),
+                ("pretrace_end", C.c_double), ("adc_bailout", C.c_double),
+                ("always_sample", C.c_int32), ("normal", C.c_int32), ("media", C.c_int32),
+                ("reserved", C.c_int32)]
 
 
 class PovGpuSceneDesc(C.Structure):
@@ -125,7 +126,9 @@ class PovGpuStats(C.Structure):
                 ("shadow_rays_succeeded", C.c_uint64), ("reflected_rays", C.c_uint64),
                 ("number_of_pixels", C.c_uint64), ("number_of_samples", C.c_uint64),
                 ("radiosity_gathers", C.c_uint64), ("radiosity_reuse", C.c_uint64),
-                ("device_error", C.c_uint64), ("reserved", C.c_uint64 * 7)]
+                ("device_error", C.c_uint64), ("radiosity_rays", C.c_uint64),
+                ("radiosity_gathers_d0", C.c_uint64), ("radiosity_gathers_d1", C.c_uint64),
+                ("reserved", C.c_uint64 * 4)]
 
     def as_dict(self):
         return {k: int(getattr(self, k)) for k, _ in self._fields_ if k != "reserved"}

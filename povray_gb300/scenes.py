@@ -373,9 +373,19 @@ class Scene:
 
     # -- SDL -----------------------------------------------------------------
     def sdl(self):
+        rad = ""
+        if self.radiosity is not None:
+            r = self.radiosity_settings()
+            rad = (" radiosity { count %d recursion_limit %d error_bound %s nearest_count %d"
+                   " pretrace_start %s pretrace_end %s minimum_reuse %s maximum_reuse %s"
+                   " low_error_factor %s gray_threshold %s brightness %s adc_bailout %s }"
+                   % (r["count"], r["recursion_limit"], _g(r["error_bound"]), r["nearest_count"],
+                      _g(r["pretrace_start"]), _g(r["pretrace_end"]), _g(r["minimum_reuse"]),
+                      _g(r["maximum_reuse"]), _g(r["low_error_factor"]), _g(r["gray_threshold"]),
+                      _g(r["brightness"]), _g(r["adc_bailout"])))
         out = ["#version 3.7;\n",
-               "global_settings { assumed_gamma 1.0 max_trace_level %d adc_bailout %s }\n"
-               % (self.max_trace_level, _g(self.adc_bailout)),
+               "global_settings { assumed_gamma 1.0 max_trace_level %d adc_bailout %s%s }\n"
+               % (self.max_trace_level, _g(self.adc_bailout), rad),
                "camera { perspective location %s right x*%s up y look_at %s angle %s }\n"
                % (_v(self.location), _g(self.right_len), _v(self.look_at), _g(self.angle)),
                "background { color rgb %s }\n" % _v(self.background)]
@@ -393,6 +403,15 @@ class Scene:
         for o in self.objects:
             out.append(self._sdl_node(o) + "\n")
         return "".join(out)
+
+    def radiosity_settings(self):
+        """The radiosity{} block with the parser's defaults filled in
+        (SceneRadiositySettings, source/core/lighting/radiosity.h:137-165)."""
+        r = dict(count=35, recursion_limit=2, error_bound=1.8, nearest_count=5, pretrace_start=0.08,
+                 pretrace_end=0.04, minimum_reuse=0.015, maximum_reuse=0.2, low_error_factor=0.5,
+                 gray_threshold=0.0, brightness=1.0, adc_bailout=0.01, always_sample=False)
+        r.update(self.radiosity or {})
+        return r
 
     def _sdl_node(self, o):
         tex = (" " + self.materials[o["material"]].sdl()) if o.get("material", -1) >= 0 else ""
@@ -513,6 +532,18 @@ class Scene:
         desc.adc_bailout = self.adc_bailout
         desc.language_version = 370
         desc.radiosity.enabled = 0
+        if self.radiosity is not None:
+            r = self.radiosity_settings()
+            rd = desc.radiosity
+            rd.enabled = 1
+            rd.count, rd.recursion_limit, rd.nearest_count = r["count"], r["recursion_limit"], r["nearest_count"]
+            rd.error_bound, rd.low_error_factor, rd.gray_threshold = r["error_bound"], r["low_error_factor"], \
+                r["gray_threshold"]
+            rd.minimum_reuse, rd.maximum_reuse, rd.brightness = r["minimum_reuse"], r["maximum_reuse"], \
+                r["brightness"]
+            rd.pretrace_start, rd.pretrace_end, rd.adc_bailout = r["pretrace_start"], r["pretrace_end"], \
+                r["adc_bailout"]
+            rd.always_sample = int(r["always_sample"])
         keep += [objs, mats, lights, meshes]
         return desc, keep
 

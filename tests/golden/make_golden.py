@@ -19,6 +19,9 @@ output (+AM2, jitter off):
   aa_u8        uint8 (H, W, 3), the PPM it writes (BT.709 transfer curve)
   aa_stats     JSON of its statistics printout (Pixels, Samples, Rays,
                Shadow Ray Tests, Succeeded)
+Radiosity cases (radiosity_cases) hold the reference CLI's own radiosity
+renders instead (run_radiosity), and pretrace_jitter.npy the pretrace jitter
+table of the reference's radiosity task.
 The cases are small so the fixtures stay around a megabyte.
 """
 import json
@@ -54,6 +57,13 @@ def cases():
     }
 
 
+def radiosity_cases():
+    """name -> scene, rendered by the reference CLI with radiosity."""
+    return {
+        "radiosity_room_160x90": scenes.radiosity_room(160, 90, n_spheres=40, count=50),
+    }
+
+
 def probe_rays(scene, stride, extent=12.0, n_random=2000, seed=11):
     hh, ww = np.mgrid[0:scene.height:stride, 0:scene.width:stride]
     o, d = scene.camera_rays(ww.ravel(), hh.ravel())
@@ -62,6 +72,61 @@ def probe_rays(scene, stride, extent=12.0, n_random=2000, seed=11):
     rd = rng.normal(size=(n_random, 3))
     rd /= np.linalg.norm(rd, axis=1)[:, None]
     return np.concatenate([o, ro]), np.concatenate([d, rd])
+
+
+def read_hdr(path):
+    """Radiance RGBE file (+FH output) -> float32 (H, W, 3); new-style
+    run-length scanlines and flat scanlines."""
+    data = open(path, "rb").read()
+    pos = 0
+    while True:                                  # header up to the blank line
+        end = data.index(b"\n", pos)
+        line = data[pos:end]
+        pos = end + 1
+        if line == b"":
+            break
+    end = data.index(b"\n", pos)
+    dims = data[pos:end].split()
+    pos = end + 1
+    h, w = int(dims[1]), int(dims[3])
+    out = np.zeros((h, w, 4), dtype=np.uint8)
+    for y in range(h):
+        if data[pos] == 2 and data[pos + 1] == 2 and (data[pos + 2] << 8 | data[pos + 3]) == w:
+            pos += 4
+            for c in range(4):
+                x = 0
+                while x < w:
+                    n = data[pos]
+                    pos += 1
+                    if n > 128:
+                        out[y, x:x + n - 128, c] = data[pos]
+                        pos += 1
+                        x += n - 128
+                    else:
+                        out[y, x:x + n, c] = np.frombuffer(data[pos:pos + n], dtype=np.uint8)
+                        pos += n
+                        x += n
+        else:
+            out[y] = np.frombuffer(data[pos:pos + 4 * w], dtype=np.uint8).reshape(w, 4)
+            pos += 4 * w
+    e = out[..., 3].astype(np.int32)
+    f = np.where(e > 0, np.ldexp(1.0, e - 136), 0.0)
+    return ((out[..., :3].astype(np.float64) + 0.5) * f[..., None] * (e > 0)[..., None]).astype(np.float32)
+
+
+def radiosity_stats(text):
+    """Radiosity counters of the reference's statistics printout
+    (renderfrontend.cpp): samples per pass and depth, reuse, rays shot."""
+    out = {}
+    m = re.search(r"Radiosity samples calculated:\s+(\d+)", text)
+    out["samples"] = int(m.group(1)) if m else 0
+    m = re.search(r"Radiosity samples reused:\s+(\d+)", text)
+    out["reused"] = int(m.group(1)) if m else 0
+    m = re.search(r"Radiosity sample rays shot:\s+(\d+)", text)
+    out["rays_shot"] = int(m.group(1)) if m else 0
+    for row in re.finditer(r"^\s+(\d+|Final|Total)\s+(\d+)\s+(\d+)\s+(\d+)\s*$", text, re.M):
+        out["pass_" + row.group(1).lower()] = [int(row.group(2)), int(row.group(3))]
+    return out
 
 
 def cli_stats(text):
@@ -119,10 +184,49 @@ def run(case, scene, stride, extent, tmp):
     print(case, stats, extra.get("aa_stats", ""), "hits", int((hr["object"] >= 0).sum()), "/", len(hr))
 
 
+def run_radiosity(case, scene, tmp):
+    """The reference CLI renders the scene with radiosity, once with one
+    render thread (a fixed sample order: the oracle restates that order) and
+    once with eight (another valid order: their difference is the sampling
+    noise floor).  Stores linear RGB from the +FH (RGBE) output and the
+    statistics printout."""
+    pov = os.path.join(tmp, case + ".pov")
+    with open(pov, "w") as f:
+        f.write(scene.sdl())
+    w, h = str(scene.width), str(scene.height)
+    out = {}
+    for threads in (1, 8):
+        hdr = os.path.join(tmp, "%s_wt%d.hdr" % (case, threads))
+        r = subprocess.run([POVRAY_REF, "+I" + pov, "+W" + w, "+H" + h, "-D", "+FH", "-A", "+WT%d" % threads,
+                            "+O" + hdr], capture_output=True, text=True, cwd=tmp)
+        if r.returncode != 0:
+            raise RuntimeError(r.stderr[-2000:])
+        text = r.stdout + r.stderr
+        out["rad_pixels_wt%d" % threads] = read_hdr(hdr)
+        out["rad_stats_wt%d" % threads] = json.dumps(dict(radiosity_stats(text), **cli_stats(text)))
+    np.savez_compressed(os.path.join(HERE, case + ".npz"), **out)
+    print(case, out["rad_stats_wt1"])
+
+
+def write_jitter_table():
+    """RadiosityTask's pretrace jitter table (RandomDoubleSequence(-1,1,2047),
+    radiositytask.cpp:99) as the reference generates it."""
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "jitter.bin")
+        subprocess.run([POV_ORACLE, "-", "0", "0", "jitter", path], check=True)
+        np.save(os.path.join(HERE, "pretrace_jitter.npy"), np.fromfile(path, dtype="<f8"))
+
+
 def main():
     if not os.path.exists(POV_ORACLE):
         sys.exit("build the reference first: make -C oracle/refbuild")
+    if len(sys.argv) == 1 or "pretrace_jitter" in sys.argv[1:]:
+        write_jitter_table()
     with tempfile.TemporaryDirectory() as tmp:
+        for case, scene in radiosity_cases().items():
+            if len(sys.argv) > 1 and case not in sys.argv[1:]:
+                continue
+            run_radiosity(case, scene, tmp)
         for case, (scene, stride, extent) in cases().items():
             if len(sys.argv) > 1 and case not in sys.argv[1:]:
                 continue

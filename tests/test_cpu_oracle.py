@@ -116,3 +116,32 @@ def test_oracle_subrectangle_equals_full_render():
     full, _ = o.render(threads=2)
     part, _ = o.render(x0=10, y0=7, x1=41, y1=30, threads=2)
     assert np.array_equal(full[7:30, 10:41], part)
+
+
+def test_oracle_radiosity_matches_reference_single_thread_render():
+    """Radiosity (pretrace passes + final trace, octree-addressed sample
+    cache, Halton gather directions) restated in the reference's
+    single-thread order: every radiosity counter of the reference CLI's
+    statistics printout equal, and its +FH image within the RGBE format's
+    own precision (relative RMSE well under the 8-thread render's distance
+    from the 1-thread one)."""
+    from tests.golden.make_golden import radiosity_cases
+    scene = radiosity_cases()["radiosity_room_160x90"]
+    g = _load("radiosity_room_160x90")
+    img, st = Oracle(scene).render(threads=1)
+    rs = json.loads(str(g["rad_stats_wt1"]))
+    assert st["radiosity_gathers"] == rs["samples"]
+    assert st["radiosity_reuse"] == rs["reused"]
+    assert st["radiosity_rays"] == rs["rays_shot"]
+    assert [st["radiosity_gathers_d0"], st["radiosity_gathers_d1"]] == rs["pass_total"]
+    assert st["number_of_rays"] == rs["number_of_rays"]
+    assert st["number_of_pixels"] == rs["number_of_pixels"]
+    # the shadow cache may decide a few shadow rays (see above)
+    assert abs(st["shadow_ray_tests"] - rs["shadow_ray_tests"]) <= 1e-4 * rs["shadow_ray_tests"]
+    assert abs(st["shadow_rays_succeeded"] - rs["shadow_rays_succeeded"]) <= 1e-4 * rs["shadow_ray_tests"]
+    ref = g["rad_pixels_wt1"]
+    a = img[..., :3]
+    rel = np.sqrt(((a - ref) ** 2).mean()) / ref.mean()
+    floor = np.sqrt(((g["rad_pixels_wt8"] - ref) ** 2).mean()) / ref.mean()
+    assert rel < 0.005 and rel < 0.2 * floor, (rel, floor)
+    assert np.abs(a - ref).max() < 0.01
