@@ -39,6 +39,8 @@ WORKLOADS = {
     "csg_torus_grid": "csg_torus_grid: %dx%d, 4096 objects (difference/intersection/merge CSG + FP64 tori), "
                       "adaptive AA method 2 thr 0.1 depth 3, 2 lights w/ shadows, reflection 0.2, max_trace_level 4",
     "spheres_plane": "spheres_plane: %dx%d 1spp, 64 spheres + plane, 2 lights w/ shadows, phong 0.5",
+    "radiosity_room": "radiosity_room: %dx%d 1spp, 6-plane room + 200 spheres, 4x4 area light, radiosity count 200 "
+                      "recursion_limit 2 error_bound 0.5 (pretrace + final trace per frame)",
 }
 
 
@@ -212,12 +214,25 @@ def main():
 
     # one profiling frame (outside the timed region): traversal work counts
     gpu.set_profiling(times=False, work=True)
-    gpu.trace_blocks(blocks, params, out=dev_out.data_ptr())
-    work = gpu.timings()
+    _, wt = frame_device()
+    work = {k: [sum(t[k][j] for t in wt) for j in range(2)] for k in ("node_visits", "prim_tests", "tri_tests",
+                                                                          "rays_traced")}
     gpu.set_profiling(times=True, work=False)
 
-    def frame_device():
-        return gpu.trace_blocks(blocks, params, out=dev_out.data_ptr())[1]
+    radiosity = s.radiosity is not None
+
+    def frame_device(out_ptr=None):
+        """One frame: with radiosity the pretrace over all blocks, then the
+        final trace.  Returns the frame's counters and per-call timings."""
+        st_all, tims = None, []
+        if radiosity:
+            st_all = gpu.radiosity_pretrace(blocks, params)
+            tims.append(gpu.timings())
+        st = gpu.trace_blocks(blocks, params, out=out_ptr or dev_out.data_ptr())[1]
+        tims.append(gpu.timings())
+        if st_all is not None:
+            st = {k: st[k] + st_all[k] for k in st if k != "device_error"}
+        return st, tims
 
     for _ in range(args.warmup):
         frame_device()
@@ -233,12 +248,12 @@ def main():
     for i in range(args.steps):
         flush.zero_()
         ev[i][0].record(stream)
-        st = frame_device()
+        st, tims = frame_device()
         ev[i][1].record(stream)
-        t = gpu.timings()
-        for k, v in t["stage_ms"].items():
-            stage_ms[k] = stage_ms.get(k, 0.0) + v
-        launches += t["kernel_launches"]
+        for t in tims:
+            for k, v in t["stage_ms"].items():
+                stage_ms[k] = stage_ms.get(k, 0.0) + v
+            launches += t["kernel_launches"]
         rays += st["number_of_rays"] + st["shadow_ray_tests"]
     torch.cuda.synchronize()
     clocks = sampler.stop()
@@ -249,7 +264,7 @@ def main():
     gpu.set_profiling(times=False, work=False)
     host_out = torch.empty((npix, 4), dtype=torch.float32, pin_memory=True)
     for _ in range(max(1, args.warmup // 2)):
-        gpu.trace_blocks(blocks, params, out=host_out.data_ptr())
+        frame_device(host_out.data_ptr())
     torch.cuda.synchronize()
     e2e_rays = 0
     t0 = time.perf_counter()
@@ -257,7 +272,7 @@ def main():
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for i in range(args.steps):
-        st = gpu.trace_blocks(blocks, params, out=host_out.data_ptr())[1]
+        st = frame_device(host_out.data_ptr())[0]
         e2e_rays += st["number_of_rays"] + st["shadow_ray_tests"]
     e1.record(stream)
     torch.cuda.synchronize()
@@ -298,7 +313,10 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (fp64 grazing re-solve, fp64 camera)",
         "data": "synthetic",
         "config": {"workload": workload_name(args), "l2": "flushed between steps (256 MiB write, outside timed events)",
-                   "rays_per_frame": rays // args.steps, "parallelism": "replica per GPU" if world > 1 else "1 GPU"},
+                   "rays_per_frame": rays // args.steps, "parallelism": "replica per GPU" if world > 1 else "1 GPU",
+                   **({"radiosity": {k: st[k] for k in ("radiosity_gathers", "radiosity_reuse", "radiosity_rays",
+                                                         "radiosity_gathers_d0", "radiosity_gathers_d1")}}
+                      if radiosity else {})},
         "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": len(blocks) * 16 + (len(blocks) + 1) * 4,
                 "d2h_bytes_per_step": npix * 16},
         "roofline": {"bound": "hbm", "kernel": "k_trace<%s>" % ("closest" if k == 0 else "any"),

@@ -313,6 +313,25 @@ int pov_gpu_trace_rays(PovGpuScene* scene, const double* origins, const double* 
 int pov_gpu_trace_rays_static(PovGpuScene* scene, const double* origins, const double* directions,
                               int32_t num_rays, PovGpuHit* hits);
 
+/*
+ * Radiosity pretrace: what RadiosityTask::Run (source/backend/render/
+ * radiositytask.cpp:95-263) does for the view's blocks before the final
+ * render (View::StartRender, source/backend/scene/view.cpp:1056-1123):
+ * empties the scene's sample cache, then traces every pretrace pass
+ * (pretrace_start down to pretrace_end spacing) over the blocks, filling the
+ * cache.  Call it once per frame with all blocks, before
+ * pov_gpu_trace_blocks.  POV_GPU_E_INVALID when the scene has no radiosity.
+ */
+int pov_gpu_radiosity_pretrace(PovGpuScene* scene, const PovGpuBlock* blocks, int32_t num_blocks,
+                               const PovGpuRenderParams* params, PovGpuStats* stats);
+
+/*
+ * The pretrace jitter table: RadiosityTask's RandomDoubleSequence(-1, 1,
+ * 2047) values (radiositytask.cpp:99), which the reference-side caller holds.
+ * Copied.  Without a table the pretrace jitters by its own hash.
+ */
+int pov_gpu_set_pretrace_jitter(PovGpuScene* scene, const double* table, int32_t n);
+
 /* Releases all device memory of the scene. */
 void pov_gpu_scene_destroy(PovGpuScene* scene);
 
@@ -332,6 +351,7 @@ int pov_gpu_scene_set_stream(PovGpuScene* scene, void* cuda_stream);
 #define POV_GPU_STAGE_RESOLVE       4
 #define POV_GPU_STAGE_FINALIZE      5
 #define POV_GPU_STAGE_AREA_SHADOW   6   /* area-light shadow subdivision       */
+#define POV_GPU_STAGE_RADIOSITY     7   /* radiosity cache queries and gathers  */
 #define POV_GPU_STAGES              8
 
 /* Profile of the last trace call.  Stage times are CUDA-event durations on

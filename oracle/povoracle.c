@@ -2756,8 +2756,8 @@ static void* render_worker(void* arg)
  * of View::StartRender (view.cpp:1056-1123) as RadiosityTask::Run
  * (radiositytask.cpp:95-263) runs it without high reproducibility -- pass
  * after pass over the 32x32 blocks in serial order, jitter from the task's
- * table -- then the final trace of the requested pixels block by block
- * (TraceTask::SimpleSamplingM0, tracetask.cpp:403-454) with a fresh
+ * table -- then the final trace block by block (TraceTask::SimpleSamplingM0,
+ * tracetask.cpp:403-454) with a fresh
  * RadiosityFunction (final trace: full error bound, own direction
  * sequences) on the same cache. */
 static int render_radiosity(PovOracle* S, const PovGpuRenderParams* p, int32_t x0, int32_t y0, int32_t x1,
@@ -2768,8 +2768,12 @@ static int render_radiosity(PovOracle* S, const PovGpuRenderParams* p, int32_t x
     if (!R->jitter || p->antialias)
         return POV_GPU_E_UNSUPPORTED;
     rad_reset(R);
+    /* the view's blocks tile the render area from its top-left corner
+     * (ViewData::GetNextRectangle, view.cpp:384-388); pass spacing follows
+     * the full image size */
     const int W = p->width, H = p->height, B = 32;
-    const int bw = (W + B - 1) / B, bh = (H + B - 1) / B, nb = bw * bh;
+    const int AW = x1 - x0, AH = y1 - y0;
+    const int bw = (AW + B - 1) / B, bh = (AH + B - 1) / B, nb = bw * bh;
     Thread th;
     memset(&th, 0, sizeof(th));
     double maxwh = (double)(W > H ? W : H);
@@ -2793,9 +2797,9 @@ static int render_radiosity(PovOracle* S, const PovGpuRenderParams* p, int32_t x
         for (int serial = 0; serial < nb; serial++) {
             if (!active[serial])
                 continue;
-            int left = (serial % bw) * B, top = (serial / bw) * B;
-            int right = left + B - 1 < W - 1 ? left + B - 1 : W - 1;
-            int bottom = top + B - 1 < H - 1 ? top + B - 1 : H - 1;
+            int left = x0 + (serial % bw) * B, top = y0 + (serial / bw) * B;
+            int right = left + B - 1 < x1 - 1 ? left + B - 1 : x1 - 1;
+            int bottom = top + B - 1 < y1 - 1 ? top + B - 1 : y1 - 1;
             th.rad_pass = PASS_FIRST + pass;
             size_t ji = (size_t)((PASS_FIRST + pass) * 17 + serial * 13) % (size_t)R->njitter;
             double sx = ceil((left - 0.5) / size) * size, sy = ceil((top - 0.5) / size) * size;
@@ -2832,13 +2836,10 @@ static int render_radiosity(PovOracle* S, const PovGpuRenderParams* p, int32_t x
     th.rad_pass = PASS_FINAL;
     int32_t w = x1 - x0;
     for (int serial = 0; serial < nb; serial++) {
-        int left = (serial % bw) * B, top = (serial / bw) * B;
-        for (int y = top; y < top + B && y < H; y++)
-            for (int x = left; x < left + B && x < W; x++) {
-                if (x < x0 || x >= x1 || y < y0 || y >= y1)
-                    continue;
+        int left = x0 + (serial % bw) * B, top = y0 + (serial / bw) * B;
+        for (int y = top; y < top + B && y < y1; y++)
+            for (int x = left; x < left + B && x < x1; x++)
                 trace_pixel(S, &th, x + 0.5, y + 0.5, W, H, out + ((size_t)(y - y0) * w + (x - x0)) * 4);
-            }
     }
     if (stats) {
         memset(stats, 0, sizeof(*stats));

@@ -57,7 +57,7 @@ def lib():
 class Oracle:
     """One oracle scene built from a povray_gb300.scenes.Scene."""
 
-    def __init__(self, scene):
+    def __init__(self, scene, jitter=None):
         from povray_gb300 import abi
         self.scene = scene
         self.desc, self._keep = scene.desc()
@@ -70,7 +70,8 @@ class Oracle:
         if scene.radiosity is not None:
             # the reference's pretrace jitter table, dumped from it by
             # tests/golden/make_golden.py
-            self._jitter = np.ascontiguousarray(np.load(JITTER_TABLE), dtype=np.float64)
+            table = np.load(JITTER_TABLE) if jitter is None else jitter
+            self._jitter = np.ascontiguousarray(table, dtype=np.float64)
             lib().pov_oracle_set_pretrace_jitter(self.h, self._jitter.ctypes.data, len(self._jitter))
 
     def close(self):

@@ -139,7 +139,7 @@ class PovGpuHit(C.Structure):
 
 
 POV_GPU_STAGES = 8
-STAGE_NAMES = ["camera", "trace_closest", "shade", "trace_shadow", "resolve", "finalize", "area_shadow", "s7"]
+STAGE_NAMES = ["camera", "trace_closest", "shade", "trace_shadow", "resolve", "finalize", "area_shadow", "radiosity"]
 POV_GPU_PROFILE_TIMES = 1
 POV_GPU_PROFILE_WORK = 2
 
@@ -163,7 +163,7 @@ STRUCTS = {
 EXPORTS = ["pov_gpu_scene_create", "pov_gpu_trace_blocks", "pov_gpu_trace_rays",
            "pov_gpu_scene_destroy", "pov_gpu_error_string", "pov_gpu_abi_version",
            "pov_gpu_scene_set_stream", "pov_gpu_set_profiling", "pov_gpu_get_timings",
-           "pov_gpu_trace_rays_static"]
+           "pov_gpu_trace_rays_static", "pov_gpu_radiosity_pretrace", "pov_gpu_set_pretrace_jitter"]
 
 
 class PovGpuError(RuntimeError):
@@ -198,6 +198,11 @@ def load_library(path=None):
     lib.pov_gpu_trace_rays_static.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
                                               C.POINTER(PovGpuHit)]
     lib.pov_gpu_trace_rays_static.restype = C.c_int
+    lib.pov_gpu_radiosity_pretrace.argtypes = [C.c_void_p, C.POINTER(PovGpuBlock), C.c_int32,
+                                               C.POINTER(PovGpuRenderParams), C.POINTER(PovGpuStats)]
+    lib.pov_gpu_radiosity_pretrace.restype = C.c_int
+    lib.pov_gpu_set_pretrace_jitter.argtypes = [C.c_void_p, C.c_void_p, C.c_int32]
+    lib.pov_gpu_set_pretrace_jitter.restype = C.c_int
     lib.pov_gpu_scene_destroy.argtypes = [C.c_void_p]
     lib.pov_gpu_scene_destroy.restype = None
     lib.pov_gpu_error_string.argtypes = [C.c_int]

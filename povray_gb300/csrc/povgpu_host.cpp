@@ -8,6 +8,7 @@
 #include "povgpu.h"
 #include "povgpu_internal.h"
 #include "povgpu_kernels.h"
+#include "povgpu_radiosity.h"
 
 #include <cuda_runtime.h>
 
@@ -275,6 +276,145 @@ static void grow_outward(AABB& b, double x, double y, double z)
 }  // namespace
 
 // ---------------------------------------------------------------- scene --
+namespace {
+
+// Counter slots of a wavefront (PathBufs::counters).
+enum {
+    C_QA = 0,     // count of queue A
+    C_QB = 1,     // count of queue B
+    C_SQ = 2,     // shadow queue
+    C_W0 = 3,     // work counter, closest-hit
+    C_W1 = 4,     // work counter, any-hit
+    C_NS = 5,     // AA: samples of this round
+    C_NC = 6,     // AA: active cells
+    C_NN = 7,     // AA: next cells
+    C_AQ = 8,     // area-light shadow items
+    C_RQ = 9,     // radiosity queries
+    C_NUM = 10
+};
+
+// One wavefront of ray queues and per-path state: the camera's, or the
+// sample rays of one radiosity bounce depth.  Counters live in `counters`
+// (C_* slots).
+struct PathBufs {
+    DevBuf qA, qB, pathA, pathB, hits, paths, slot_contrib, sq, sq_slot, blocked, skipA, skipB, sskip;
+    DevBuf aq, aq_slot, aq_skip;   // area-light shadow items
+    DevBuf rq, rq_amb;             // radiosity queries of the hits, and their answers
+    DevBuf quality, first_t;       // sample rays: quality of each, depth of its first hit
+    DevBuf counters;
+
+    cudaError_t ensure(size_t maxq, int nl, int nal, bool rad, bool sample_rays)
+    {
+        maxq = std::max<size_t>(maxq, 1);
+        nl = std::max(nl, 1);
+        cudaError_t e;
+#define PB_ENSURE(buf, bytes) if ((e = (buf).ensure(bytes)) != cudaSuccess) return e
+        PB_ENSURE(counters, sizeof(int) * C_NUM);
+        PB_ENSURE(qA, sizeof(QRay) * maxq);
+        PB_ENSURE(qB, sizeof(QRay) * maxq);
+        PB_ENSURE(pathA, sizeof(int) * maxq);
+        PB_ENSURE(pathB, sizeof(int) * maxq);
+        PB_ENSURE(hits, sizeof(QHit) * maxq);
+        PB_ENSURE(paths, sizeof(PathState) * maxq);
+        PB_ENSURE(slot_contrib, sizeof(float4) * maxq * nl);
+        PB_ENSURE(sq, sizeof(QRay) * maxq * nl);
+        PB_ENSURE(sq_slot, sizeof(int) * maxq * nl);
+        PB_ENSURE(blocked, maxq * nl);
+        PB_ENSURE(skipA, sizeof(uint2) * maxq);
+        PB_ENSURE(skipB, sizeof(uint2) * maxq);
+        PB_ENSURE(sskip, sizeof(uint2) * maxq * nl);
+        if (nal > 0) {
+            PB_ENSURE(aq, sizeof(QRay) * maxq * nal);
+            PB_ENSURE(aq_slot, sizeof(int) * maxq * nal);
+            PB_ENSURE(aq_skip, sizeof(uint2) * maxq * nal);
+        }
+        if (rad) {
+            PB_ENSURE(rq, sizeof(RadQuery) * maxq);
+            PB_ENSURE(rq_amb, sizeof(float4) * maxq);
+        }
+        if (sample_rays) {
+            PB_ENSURE(quality, sizeof(float) * maxq);
+            PB_ENSURE(first_t, sizeof(float) * maxq);
+        }
+#undef PB_ENSURE
+        return cudaSuccess;
+    }
+    void release()
+    {
+        DevBuf* all[] = {&qA, &qB, &pathA, &pathB, &hits, &paths, &slot_contrib, &sq, &sq_slot, &blocked, &skipA,
+                         &skipB, &sskip, &aq, &aq_slot, &aq_skip, &rq, &rq_amb, &quality, &first_t, &counters};
+        for (DevBuf* b : all)
+            b->release();
+    }
+};
+
+// Buffers of one radiosity bounce depth: the open / waiting / seed query
+// lists of the rounds, each query's partial cache sums and answer, the
+// round's cell claims, and the wavefront of the depth's sample rays.
+struct RadLevel {
+    DevBuf open, next, seeds, partial, claims, counts;
+    PathBufs rays;
+    cudaError_t ensure(size_t nq)
+    {
+        nq = std::max<size_t>(nq, 1);
+        cudaError_t e;
+        if ((e = open.ensure(sizeof(int) * nq)) != cudaSuccess) return e;
+        if ((e = next.ensure(sizeof(int) * nq)) != cudaSuccess) return e;
+        if ((e = seeds.ensure(sizeof(int) * nq)) != cudaSuccess) return e;
+        if ((e = partial.ensure(sizeof(float4) * nq)) != cudaSuccess) return e;
+        size_t slots = 64;
+        while (slots < 2 * nq)
+            slots *= 2;
+        if ((e = claims.ensure(sizeof(unsigned long long) * slots)) != cudaSuccess) return e;
+        return counts.ensure(sizeof(int) * 4);
+    }
+    uint32_t claim_mask() const
+    {
+        size_t slots = claims.bytes / sizeof(unsigned long long);
+        size_t p = 64;
+        while (p * 2 <= slots)
+            p *= 2;
+        return (uint32_t)(p - 1);
+    }
+    void release()
+    {
+        open.release(); next.release(); seeds.release(); partial.release(); claims.release(); counts.release();
+        rays.release();
+    }
+};
+
+constexpr int RAD_LEVELS = 4;                    // bounce depths with their own buffers
+constexpr size_t GATHER_CHUNK_RAYS = 1u << 20;   // sample rays in flight per depth
+constexpr int RAD_ROUNDS = 8;                    // query rounds before every open query gathers
+
+}  // namespace
+
+// Radiosity state of a scene: settings, the device sample cache, and the
+// running position of each bounce depth's direction sequence.
+struct RadiosityState {
+    bool            enabled = false;
+    PovGpuRadiosity set{};
+    DevBuf          blocks, next, count, keys, heads, range, rstats;
+    int             cap_blocks = 0;
+    uint32_t        key_mask = 0;
+    bool            dirs_uploaded = false;
+    int             dir_base[RAD_LEVELS] = {0, 0, 0, 0};
+    bool            final_trace = true;
+    double          error_bound = 0.0;
+    uint64_t        rays_shot = 0;
+    std::vector<double> jitter;
+    RadLevel        level[RAD_LEVELS];
+    void release()
+    {
+        DevBuf* all[] = {&blocks, &next, &count, &keys, &heads, &range, &rstats};
+        for (DevBuf* b : all)
+            b->release();
+        for (auto& l : level)
+            l.release();
+    }
+};
+
+
 struct PovGpuScene {
     std::mutex  lock;
     int         device = 0;
@@ -290,13 +430,16 @@ struct PovGpuScene {
     std::vector<int32_t> h_sphere_obj, h_plane_obj, h_box_obj, h_torus_obj, h_tri_global, h_tri_local, h_tri_obj;
     std::vector<DevCsg> h_csgs;
     std::vector<DevCsgChild> h_csg_children;
-    // per-batch work buffers (grown on demand, reused)
-    DevBuf blocks, block_off, corner_off, qA, qB, pathA, pathB, hits, paths, slot_contrib, sq, sq_slot, blocked, out,
-        counters, stats, err, rays_in, skipA, skipB, sskip, t64;
-    // area-light shadow items (shading point, slot, origin surface)
-    DevBuf aq, aq_slot, aq_skip;
+    // per-batch work buffers (grown on demand, reused); qA, hits, rays_in
+    // and t64 serve pov_gpu_trace_rays
+    DevBuf blocks, block_off, corner_off, qA, hits, out, counters, stats, err, rays_in, t64;
+    // the camera wavefront
+    PathBufs top;
+    // radiosity cache and buffers
+    RadiosityState rad;
     // adaptive antialiasing buffers
     DevBuf corners, aa_grid, aa_mask, aa_subdiv, aa_xy, cellsA, cellsB, spos, sslot;
+    DevBuf pos_count;   // explicit sample positions in spos (radiosity pretrace)
     int     num_lights = 0;
     int     max_trace_level = 1;
     // streams and profiling
@@ -315,12 +458,13 @@ struct PovGpuScene {
         events.clear();
         DevBuf* all[] = {&nodes, &refs, &tri_v0, &tri_e1, &tri_e2, &tri_global, &tri_shade, &tri_normal, &tri_local,
                          &normals, &spheres, &spheres64, &boxes64, &sphere_obj, &sphere_flags, &planes, &plane_obj, &boxes, &tori, &csgs,
-                         &csg_children, &objects, &materials, &lights, &blocks, &block_off, &corner_off, &qA, &qB,
-                         &pathA, &pathB, &hits, &paths, &slot_contrib, &sq, &sq_slot, &blocked, &out, &counters,
-                         &stats, &err, &rays_in, &skipA, &skipB, &sskip, &t64, &corners, &aa_grid, &aa_mask,
-                         &aa_subdiv, &aa_xy, &cellsA, &cellsB, &spos, &sslot, &wcount, &aq, &aq_slot, &aq_skip};
+                         &csg_children, &objects, &materials, &lights, &blocks, &block_off, &corner_off, &qA,
+                         &hits, &out, &counters, &stats, &err, &rays_in, &t64, &corners, &aa_grid, &aa_mask,
+                         &aa_subdiv, &aa_xy, &cellsA, &cellsB, &spos, &sslot, &wcount, &pos_count};
         for (DevBuf* b : all)
             b->release();
+        top.release();
+        rad.release();
         if (stream)
             cudaStreamDestroy(stream);
         stream = nullptr;
@@ -348,8 +492,16 @@ int validate(const PovGpuSceneDesc* d, int32_t* bad)
         return POV_GPU_E_INVALID;
     if (d->camera.type != 0)
         return POV_GPU_E_UNSUPPORTED;
-    if (d->radiosity.enabled)
-        return POV_GPU_E_UNSUPPORTED;
+    if (d->radiosity.enabled) {
+        // radiosity{} as the GPU path restates it: default normal/media off,
+        // bounce depths within the buffer levels, sensible counts
+        const PovGpuRadiosity& r = d->radiosity;
+        if (r.count < 1 || r.nearest_count < 1 || r.recursion_limit < 1 || r.error_bound <= 0.0 ||
+            r.pretrace_start <= 0.0 || r.pretrace_end <= 0.0 || r.pretrace_end > r.pretrace_start)
+            return POV_GPU_E_INVALID;
+        if (r.recursion_limit > RAD_LEVELS || r.normal || r.media)
+            return POV_GPU_E_UNSUPPORTED;
+    }
     for (int i = 0; i < d->num_lights; i++) {
         const PovGpuLight& L = d->lights[i];
         if ((L.kind != POV_LIGHT_POINT && L.kind != POV_LIGHT_AREA) || L.fade_power > 0.0f)
@@ -417,14 +569,16 @@ int validate(const PovGpuSceneDesc* d, int32_t* bad)
     return POV_GPU_OK;
 }
 
-DevMaterial make_material(const PovGpuMaterial& m, const float* ambient_light)
+DevMaterial make_material(const PovGpuMaterial& m, const float* ambient_light, bool radiosity)
 {
     DevMaterial d{};
     d.pigment = make_float4(m.pigment[0], m.pigment[1], m.pigment[2], m.pigment[3]);
-    // emission + ambient * ambient_light (radiosity off, trace.cpp:984-1004)
-    d.emission = make_float4(m.emission[0] + m.ambient[0] * ambient_light[0],
-                             m.emission[1] + m.ambient[1] * ambient_light[1],
-                             m.emission[2] + m.ambient[2] * ambient_light[2], 0.f);
+    // emission, plus ambient * ambient_light unless radiosity replaces the
+    // ambient term (trace.cpp:982-987)
+    const float a = radiosity ? 0.0f : 1.0f;
+    d.emission = make_float4(m.emission[0] + a * m.ambient[0] * ambient_light[0],
+                             m.emission[1] + a * m.ambient[1] * ambient_light[1],
+                             m.emission[2] + a * m.ambient[2] * ambient_light[2], 0.f);
     float wmax = std::max(m.reflection_max[0], std::max(m.reflection_max[1], m.reflection_max[2]));
     float wmin = std::max(m.reflection_min[0], std::max(m.reflection_min[1], m.reflection_min[2]));
     d.reflect = make_float4(m.reflection_max[0], m.reflection_max[1], m.reflection_max[2], m.reflection_falloff);
@@ -439,6 +593,7 @@ DevMaterial make_material(const PovGpuMaterial& m, const float* ambient_light)
     for (int k = 0; k < 3; k++)
         anyr = anyr || m.reflection_max[k] != 0.f || m.reflection_min[k] != 0.f;
     d.has_reflection = anyr ? 1 : 0;
+    d.diffuse_raw = m.diffuse;
     return d;
 }
 
@@ -591,6 +746,8 @@ void add_mesh(Builder& B, const PovGpuSceneDesc* d, const PovGpuObject& o, int i
     }
 }
 
+int rad_reset(PovGpuScene* sc);
+
 int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
 {
     Builder B;
@@ -719,7 +876,8 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
 
     std::vector<DevMaterial> mats((size_t)d->num_materials);
     for (int i = 0; i < d->num_materials; i++)
-        mats[i] = make_material(d->materials[i], d->ambient_light);
+        mats[i] = make_material(d->materials[i], d->ambient_light,
+                                d->radiosity.enabled && d->language_version >= 370);
     std::vector<DevLight> lights((size_t)std::max(d->num_lights, 1));
     int num_area = 0;
     for (int i = 0; i < d->num_lights; i++) {
@@ -813,22 +971,53 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
     }
     sc->num_lights = d->num_lights;
     sc->max_trace_level = d->max_trace_level;
+    if (d->radiosity.enabled) {
+        // the sample cache and the direction pool: Halton(2,3) cosine-weighted
+        // (GetSubRandomCosWeightedDirectionGenerator(0, 1600) picks that
+        // generator, randomsequence.cpp:1019-1037; HaltonGenerator and
+        // HaltonCosWeightedDirectionGenerator, randomsequence.cpp:730-747,
+        // 907-915)
+        RadiosityState& R = sc->rad;
+        R.enabled = true;
+        R.set = d->radiosity;
+        R.cap_blocks = 1 << 21;
+        size_t slots = 1u << 22;
+        R.key_mask = (uint32_t)(slots - 1);
+        CK(R.blocks.ensure(sizeof(RadBlock) * (size_t)R.cap_blocks));
+        CK(R.next.ensure(sizeof(int32_t) * (size_t)R.cap_blocks));
+        CK(R.count.ensure(sizeof(int32_t)));
+        CK(R.keys.ensure(sizeof(unsigned long long) * slots));
+        CK(R.heads.ensure(sizeof(int32_t) * slots));
+        CK(R.range.ensure(sizeof(int32_t) * 2));
+        CK(R.rstats.ensure(sizeof(unsigned long long) * RST_COUNT));
+        std::vector<float> dirs(3 * (size_t)RAD_DIRECTIONS);
+        for (int i = 0; i < RAD_DIRECTIONS; i++) {
+            double hb[2];
+            const unsigned base[2] = {2, 3};
+            for (int k = 0; k < 2; k++) {
+                size_t idx = (size_t)i + 1;
+                double h = 0.0, q = 1.0 / base[k];
+                while (idx > 0) {
+                    h += (double)(idx % base[k]) * q;
+                    idx /= base[k];
+                    q /= base[k];
+                }
+                hb[k] = h;
+            }
+            double r = std::sqrt(hb[0]), th = hb[1] * (2 * 3.14159265358979323846);
+            double x = r * std::cos(th), z = r * std::sin(th);
+            dirs[3 * i + 0] = (float)x;
+            dirs[3 * i + 1] = (float)std::sqrt(1 - x * x - z * z);
+            dirs[3 * i + 2] = (float)z;
+        }
+        CK(rad_upload_directions(dirs.data()));
+        int rc = rad_reset(sc);
+        if (rc != POV_GPU_OK)
+            return rc;
+    }
     return POV_GPU_OK;
 }
 
-// Counter slots in sc->counters.
-enum {
-    C_QA = 0,     // count of queue A
-    C_QB = 1,     // count of queue B
-    C_SQ = 2,     // shadow queue
-    C_W0 = 3,     // work counter, closest-hit
-    C_W1 = 4,     // work counter, any-hit
-    C_NS = 5,     // AA: samples of this round
-    C_NC = 6,     // AA: active cells
-    C_NN = 7,     // AA: next cells
-    C_AQ = 8,     // area-light shadow items
-    C_NUM = 10
-};
 
 int check_device_error(PovGpuScene* sc, PovGpuStats* stats, unsigned long long* host_stats)
 {
@@ -915,6 +1104,248 @@ private:
     std::vector<Mark> marks_;
 };
 
+
+int rad_resolve(PovGpuScene* sc, StageClock& clk, int d, const RadQuery* queries, int n, float4* out);
+
+// RadiosityRecursionSettings of bounce depth d (radiosity.cpp:177-294) and
+// the current task's error bound.
+RadParams rad_params(const PovGpuScene* sc, int d)
+{
+    const RadiosityState& R = sc->rad;
+    const PovGpuRadiosity& rs = R.set;
+    RadParams p{};
+    p.depth = d;
+    p.final_trace = R.final_trace ? 1 : 0;
+    p.always_sample = rs.always_sample;
+    p.reuse_count = d == 0 ? rs.nearest_count : (d == 1 ? std::min(2, rs.nearest_count) : 1);
+    int n = (int)(rs.count * std::pow(0.5, (double)d));
+    p.rays_per_sample = std::min(std::max(5, n), RAD_DIRECTIONS);
+    p.error_bound = (float)R.error_bound;
+    p.error_bound_factor = (float)std::pow(2.0, (double)d);
+    p.min_reuse_factor = (float)(rs.minimum_reuse * std::pow(2.0, (double)d));
+    p.max_reuse_factor = (float)(rs.maximum_reuse * std::pow(2.0, (double)d));
+    p.address_factor = (float)(rs.error_bound * std::pow(2.0, (double)d) / (d == 0 ? 1.0 : 8.0));
+    p.gather_weight = (float)std::max(rs.adc_bailout + EPSILON, std::pow(0.5 * rs.brightness, (double)d + 1));
+    p.gray = (float)rs.gray_threshold;
+    p.brightness = (float)rs.brightness;
+    p.adc = (float)rs.adc_bailout;
+    return p;
+}
+
+RadCacheView cache_view(PovGpuScene* sc)
+{
+    RadiosityState& R = sc->rad;
+    RadCacheView c{};
+    c.blocks = R.blocks.as<RadBlock>();
+    c.next = R.next.as<int32_t>();
+    c.count = R.count.as<int32_t>();
+    c.cap = R.cap_blocks;
+    c.keys = R.keys.as<unsigned long long>();
+    c.heads = R.heads.as<int32_t>();
+    c.mask = R.key_mask;
+    c.size_range = R.range.as<int32_t>();
+    return c;
+}
+
+// Empties the sample cache and restarts the direction sequences (a new
+// frame: the reference keeps one cache per view).
+int rad_reset(PovGpuScene* sc)
+{
+    RadiosityState& R = sc->rad;
+    cudaStream_t st = sc->active();
+    CK(cudaMemsetAsync(R.count.p, 0, sizeof(int32_t), st));
+    CK(cudaMemsetAsync(R.keys.p, 0, R.keys.bytes, st));
+    CK(cudaMemsetAsync(R.heads.p, 0xff, R.heads.bytes, st));
+    const int32_t range[2] = {1 << 30, -1};
+    CK(cudaMemcpy(R.range.p, range, sizeof(range), cudaMemcpyHostToDevice));
+    for (int& b : R.dir_base)
+        b = 0;
+    return POV_GPU_OK;
+}
+
+// Traces one wavefront through trace levels level0 .. max_level-1: the rays
+// in B.qA (count in the C_QA counter, path index in B.pathA, origin surface
+// in B.skipA) and the reflection rays they spawn.  With radiosity on and
+// `hit_depth` below the recursion limit, every level's hits query the
+// radiosity cache at that bounce depth (RadiosityFunction::ComputeAmbient)
+// and the answers are added to their paths before the next level.
+// `sample_rays`: the wavefront holds radiosity sample rays, shaded the way
+// the radiosity Trace shades them.
+int run_levels(PovGpuScene* sc, StageClock& clk, PathBufs& B, size_t maxq, int level0, int max_level, int hit_depth,
+               bool sample_rays)
+{
+    const int nl = std::max(sc->num_lights, 1);
+    const int nal = sample_rays ? 0 : sc->S.num_area_lights;
+    const bool rad = sc->rad.enabled && hit_depth < sc->rad.set.recursion_limit;
+    CK(B.ensure(maxq, nl, nal, rad, sample_rays));
+    cudaStream_t st = sc->active();
+    int* cnt = B.counters.as<int>();
+    unsigned long long* dstats = sc->stats.as<unsigned long long>();
+    uint32_t* derr = sc->err.as<uint32_t>();
+    unsigned long long* wc = (sc->profiling & POV_GPU_PROFILE_WORK) ? sc->wcount.as<unsigned long long>() : nullptr;
+    const DeviceScene& S = sc->S;
+    const int grid_trace = sc->num_sms * 8;
+    const int grid_shade = std::max(1, std::min(sc->num_sms * 16, (int)((maxq + 127) / 128)));
+    const size_t max_area = maxq * (size_t)nal;
+    QRay* qcur = B.qA.as<QRay>();
+    QRay* qnext = B.qB.as<QRay>();
+    int* pcur = B.pathA.as<int>();
+    int* pnext = B.pathB.as<int>();
+    int* ccur = cnt + C_QA;
+    int* cnext = cnt + C_QB;
+    uint2* kcur = B.skipA.as<uint2>();
+    uint2* knext = B.skipB.as<uint2>();
+    ShadeRad sr{};
+    sr.rq = rad ? B.rq.as<RadQuery>() : nullptr;
+    sr.rq_count = cnt + C_RQ;
+    sr.rq_cap = (int)maxq;
+    sr.adc = sample_rays ? (float)sc->rad.set.adc_bailout : S.adc_bailout;
+    sr.gather = sample_rays ? 1 : 0;
+    for (int level = level0; level < max_level; level++) {
+        CK(cudaMemsetAsync(cnext, 0, sizeof(int), st));
+        CK(cudaMemsetAsync(cnt + C_SQ, 0, sizeof(int) * 3, st));   // SQ, W0, W1
+        CK(cudaMemsetAsync(cnt + C_AQ, 0, sizeof(int) * 2, st));   // AQ, RQ
+        CK(clk.begin(POV_GPU_STAGE_TRACE_CLOSEST));
+        CK(launch_trace(S, false, qcur, ccur, cnt + C_W0, B.hits.as<QHit>(), nullptr, sc->stack_depth, grid_trace,
+                        derr, dstats, wc, (int)maxq, kcur, st));
+        CK(clk.end());
+        if (sample_rays && level == level0)
+            CK(launch_first_hit(B.hits.as<QHit>(), ccur, (int)maxq, B.first_t.as<float>(), grid_shade, st));
+        CK(clk.begin(POV_GPU_STAGE_SHADE));
+        CK(launch_shade(S, level, max_level, qcur, pcur, B.hits.as<QHit>(), ccur, B.paths.as<PathState>(),
+                        B.slot_contrib.as<float4>(), B.sq.as<QRay>(), B.sq_slot.as<int>(), cnt + C_SQ,
+                        B.sskip.as<uint2>(), qnext, pnext, knext, cnext, (int)maxq, (int)(maxq * nl),
+                        B.aq.as<QRay>(), B.aq_slot.as<int>(), B.aq_skip.as<uint2>(), cnt + C_AQ, (int)max_area, sr,
+                        grid_shade, derr, dstats, st));
+        CK(clk.end());
+        if (nal > 0) {
+            CK(clk.begin(POV_GPU_STAGE_AREA_SHADOW));
+            CK(launch_area_shadow(S, B.aq.as<QRay>(), B.aq_slot.as<int>(), B.aq_skip.as<uint2>(), cnt + C_AQ,
+                                  (int)max_area, B.slot_contrib.as<float4>(), sc->stack_depth, grid_shade, derr,
+                                  dstats, st));
+            CK(clk.end());
+        }
+        if (sc->num_lights > 0) {
+            CK(clk.begin(POV_GPU_STAGE_TRACE_SHADOW));
+            CK(launch_trace(S, true, B.sq.as<QRay>(), cnt + C_SQ, cnt + C_W1, nullptr, B.blocked.as<uint8_t>(),
+                            sc->stack_depth, grid_trace, derr, dstats, wc ? wc + 4 : nullptr, (int)(maxq * nl),
+                            B.sskip.as<uint2>(), st));
+            CK(clk.end());
+            CK(clk.begin(POV_GPU_STAGE_RESOLVE));
+            CK(launch_resolve(pcur, ccur, sc->num_lights, B.sq_slot.as<int>(), B.blocked.as<uint8_t>(), cnt + C_SQ,
+                              B.slot_contrib.as<float4>(), B.paths.as<PathState>(), grid_shade, (int)maxq,
+                              (int)(maxq * nl), st));
+            CK(clk.end(2));
+        }
+        if (rad) {
+            int nq = 0;
+            CK(cudaMemcpyAsync(&nq, cnt + C_RQ, sizeof(int), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            nq = std::min(nq, (int)maxq);
+            if (nq > 0) {
+                int rc = rad_resolve(sc, clk, hit_depth, B.rq.as<RadQuery>(), nq, B.rq_amb.as<float4>());
+                if (rc != POV_GPU_OK)
+                    return rc;
+                CK(clk.begin(POV_GPU_STAGE_RADIOSITY));
+                CK(launch_rad_apply(B.rq.as<RadQuery>(), cnt + C_RQ, (int)maxq, B.rq_amb.as<float4>(),
+                                    B.paths.as<PathState>(), sample_rays ? B.quality.as<float>() : nullptr,
+                                    grid_shade, st));
+                CK(clk.end());
+            }
+        }
+        std::swap(qcur, qnext);
+        std::swap(pcur, pnext);
+        std::swap(ccur, cnext);
+        std::swap(kcur, knext);
+    }
+    return POV_GPU_OK;
+}
+
+// New samples for `ns` queries of bounce depth d (RadiosityFunction::
+// GatherLight, radiosity.cpp:509-756): count sample rays each, traced as
+// one wavefront by the radiosity Trace starting at the depth's trace level
+// (radiosity.cpp:544-549), then reduced per seed into the new block and the
+// seed's ambient answer.
+int rad_gather(PovGpuScene* sc, StageClock& clk, int d, const RadQuery* queries, const int* seeds, int ns,
+               const float4* partial, float4* out)
+{
+    RadiosityState& R = sc->rad;
+    const RadParams P = rad_params(sc, d);
+    PathBufs& B = R.level[d].rays;
+    const int count = P.rays_per_sample;
+    const size_t nr = (size_t)ns * count;
+    const bool nested = d + 1 < R.set.recursion_limit;
+    CK(B.ensure(nr, std::max(sc->num_lights, 1), 0, nested, true));
+    cudaStream_t st = sc->active();
+    int* cnt = B.counters.as<int>();
+    const int grid = std::max(1, std::min(sc->num_sms * 16, (int)((nr + 255) / 256)));
+    CK(cudaMemsetAsync(cnt, 0, sizeof(int) * C_NUM, st));
+    const int base = R.dir_base[d];
+    CK(clk.begin(POV_GPU_STAGE_RADIOSITY));
+    CK(launch_gather_rays(queries, seeds, ns, count, base, P.gather_weight, B.qA.as<QRay>(), B.pathA.as<int>(),
+                          B.skipA.as<uint2>(), B.paths.as<PathState>(), B.quality.as<float>(), cnt + C_QA,
+                          sc->stats.as<unsigned long long>(), grid, st));
+    CK(clk.end());
+    R.dir_base[d] = (int)(((long long)base + (long long)nr) % RAD_DIRECTIONS);
+    R.rays_shot += nr;
+    const int tl = (int)(1.5 * (d + 1));
+    const int maxl = std::max(sc->max_trace_level, tl + 1);
+    int rc = run_levels(sc, clk, B, nr, tl, maxl, d + 1, true);
+    if (rc != POV_GPU_OK)
+        return rc;
+    CK(clk.begin(POV_GPU_STAGE_RADIOSITY));
+    CK(launch_gather_reduce(sc->S, cache_view(sc), P, queries, seeds, ns, base, B.first_t.as<float>(),
+                            B.paths.as<PathState>(), B.quality.as<float>(), partial, out,
+                            R.rstats.as<unsigned long long>(), sc->err.as<uint32_t>(),
+                            std::max(1, std::min(sc->num_sms * 16, (ns * 32 + 127) / 128)), st));
+    CK(clk.end());
+    return POV_GPU_OK;
+}
+
+// Answers n radiosity queries of bounce depth d into out[] (ambient colour,
+// quality): rounds of cache queries and gathers, see povgpu_radiosity.cu.
+int rad_resolve(PovGpuScene* sc, StageClock& clk, int d, const RadQuery* queries, int n, float4* out)
+{
+    RadiosityState& R = sc->rad;
+    if (d >= RAD_LEVELS)
+        return POV_GPU_E_UNSUPPORTED;
+    RadLevel& L = R.level[d];
+    CK(L.ensure((size_t)n));
+    const RadParams P = rad_params(sc, d);
+    const RadCacheView C = cache_view(sc);
+    cudaStream_t st = sc->active();
+    int* cn = L.counts.as<int>();
+    int* lists[2] = {L.open.as<int>(), L.next.as<int>()};
+    const int* open = nullptr;
+    int n_open = n;
+    const int grid = std::max(1, std::min(sc->num_sms * 16, (n + 127) / 128));
+    const int per_chunk = std::max(1, (int)(GATHER_CHUNK_RAYS / (size_t)P.rays_per_sample));
+    for (int round = 0; round < RAD_ROUNDS && n_open > 0; round++) {
+        int* nxt = lists[round & 1];
+        CK(cudaMemsetAsync(cn, 0, sizeof(int) * 2, st));
+        CK(cudaMemsetAsync(L.claims.p, 0, L.claims.bytes, st));
+        CK(clk.begin(POV_GPU_STAGE_RADIOSITY));
+        CK(launch_rad_query(sc->S, C, P, queries, open, n_open, n, round, RAD_ROUNDS - 1, out,
+                            L.partial.as<float4>(), L.claims.as<unsigned long long>(), L.claim_mask(),
+                            L.seeds.as<int>(), cn, nxt, cn + 1, R.rstats.as<unsigned long long>(),
+                            sc->err.as<uint32_t>(), grid, st));
+        CK(clk.end());
+        int hc[2] = {0, 0};
+        CK(cudaMemcpyAsync(hc, cn, sizeof(hc), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        const int ns = std::min(hc[0], n), nn = std::min(hc[1], n);
+        for (int c0 = 0; c0 < ns; c0 += per_chunk) {
+            int rc = rad_gather(sc, clk, d, queries, L.seeds.as<int>() + c0, std::min(per_chunk, ns - c0),
+                                L.partial.as<float4>(), out);
+            if (rc != POV_GPU_OK)
+                return rc;
+        }
+        open = nxt;
+        n_open = nn;
+    }
+    return POV_GPU_OK;
+}
+
 // Traces `n` image samples through every trace level and writes their RGBT
 // to out[slot[i]] (slot == nullptr: out[i]).  Samples come from the block
 // list (mode 0 centres, mode 1 corners) or from `pos` (mode 2, count in the
@@ -922,92 +1353,51 @@ private:
 int run_samples(PovGpuScene* sc, StageClock& clk, int mode, int nblocks, const int* block_off, const double2* pos,
                 const int* npos, int n, int width, int height, const int* slot, float4* out)
 {
-    const int nl = std::max(sc->num_lights, 1);
+    PathBufs& B = sc->top;
     const size_t maxq = (size_t)std::max(n, 1);
-    CK(sc->qA.ensure(sizeof(QRay) * maxq));
-    CK(sc->qB.ensure(sizeof(QRay) * maxq));
-    CK(sc->pathA.ensure(sizeof(int) * maxq));
-    CK(sc->pathB.ensure(sizeof(int) * maxq));
-    CK(sc->hits.ensure(sizeof(QHit) * maxq));
-    CK(sc->paths.ensure(sizeof(PathState) * maxq));
-    CK(sc->slot_contrib.ensure(sizeof(float4) * maxq * nl));
-    CK(sc->sq.ensure(sizeof(QRay) * maxq * nl));
-    CK(sc->sq_slot.ensure(sizeof(int) * maxq * nl));
-    CK(sc->blocked.ensure(maxq * nl));
-    CK(sc->skipA.ensure(sizeof(uint2) * maxq));
-    CK(sc->skipB.ensure(sizeof(uint2) * maxq));
-    CK(sc->sskip.ensure(sizeof(uint2) * maxq * nl));
-    const int nal = sc->S.num_area_lights;
-    const size_t max_area = maxq * (size_t)nal;
-    if (nal > 0) {
-        CK(sc->aq.ensure(sizeof(QRay) * max_area));
-        CK(sc->aq_slot.ensure(sizeof(int) * max_area));
-        CK(sc->aq_skip.ensure(sizeof(uint2) * max_area));
-    }
-
+    CK(B.ensure(maxq, std::max(sc->num_lights, 1), sc->S.num_area_lights, sc->rad.enabled, false));
     cudaStream_t st = sc->active();
-    int* cnt = sc->counters.as<int>();
-    unsigned long long* dstats = sc->stats.as<unsigned long long>();
-    uint32_t* derr = sc->err.as<uint32_t>();
-    unsigned long long* wc = (sc->profiling & POV_GPU_PROFILE_WORK) ? sc->wcount.as<unsigned long long>() : nullptr;
-    const DeviceScene& S = sc->S;
-    const int grid_trace = sc->num_sms * 8;
-    const int grid_shade = std::max(1, std::min(sc->num_sms * 16, (int)((maxq + 127) / 128)));
-    QRay* qcur = sc->qA.as<QRay>();
-    QRay* qnext = sc->qB.as<QRay>();
-    int* pcur = sc->pathA.as<int>();
-    int* pnext = sc->pathB.as<int>();
-    int* ccur = cnt + C_QA;
-    int* cnext = cnt + C_QB;
-    uint2* kcur = sc->skipA.as<uint2>();
-    uint2* knext = sc->skipB.as<uint2>();
+    int* cnt = B.counters.as<int>();
+    CK(cudaMemsetAsync(cnt, 0, sizeof(int) * C_NUM, st));
     CK(clk.begin(POV_GPU_STAGE_CAMERA));
-    CK(launch_camera(S, mode, sc->blocks.as<int4>(), block_off, nblocks, pos, npos, n, width, height, qcur, pcur,
-                     sc->paths.as<PathState>(), ccur, dstats, kcur, st));
+    CK(launch_camera(sc->S, mode, sc->blocks.as<int4>(), block_off, nblocks, pos, npos, n, width, height,
+                     B.qA.as<QRay>(), B.pathA.as<int>(), B.paths.as<PathState>(), cnt + C_QA,
+                     sc->stats.as<unsigned long long>(), B.skipA.as<uint2>(), st));
     CK(clk.end());
-    for (int level = 0; level < sc->max_trace_level; level++) {
-        CK(cudaMemsetAsync(cnext, 0, sizeof(int), st));
-        CK(cudaMemsetAsync(cnt + C_SQ, 0, sizeof(int) * 3, st));   // SQ, W0, W1
-        CK(cudaMemsetAsync(cnt + C_AQ, 0, sizeof(int), st));
-        CK(clk.begin(POV_GPU_STAGE_TRACE_CLOSEST));
-        CK(launch_trace(S, false, qcur, ccur, cnt + C_W0, sc->hits.as<QHit>(), nullptr, sc->stack_depth, grid_trace,
-                        derr, dstats, wc, (int)maxq, kcur, st));
-        CK(clk.end());
-        CK(clk.begin(POV_GPU_STAGE_SHADE));
-        CK(launch_shade(S, level, qcur, pcur, sc->hits.as<QHit>(), ccur, sc->paths.as<PathState>(),
-                        sc->slot_contrib.as<float4>(), sc->sq.as<QRay>(), sc->sq_slot.as<int>(), cnt + C_SQ,
-                        sc->sskip.as<uint2>(), qnext, pnext, knext, cnext, (int)maxq, (int)(maxq * nl),
-                        sc->aq.as<QRay>(), sc->aq_slot.as<int>(), sc->aq_skip.as<uint2>(), cnt + C_AQ,
-                        (int)max_area, grid_shade, derr, dstats, st));
-        CK(clk.end());
-        if (nal > 0) {
-            CK(clk.begin(POV_GPU_STAGE_AREA_SHADOW));
-            CK(launch_area_shadow(S, sc->aq.as<QRay>(), sc->aq_slot.as<int>(), sc->aq_skip.as<uint2>(), cnt + C_AQ,
-                                  (int)max_area, sc->slot_contrib.as<float4>(), sc->stack_depth, grid_shade, derr,
-                                  dstats, st));
-            CK(clk.end());
-        }
-        if (sc->num_lights > 0) {
-            CK(clk.begin(POV_GPU_STAGE_TRACE_SHADOW));
-            CK(launch_trace(S, true, sc->sq.as<QRay>(), cnt + C_SQ, cnt + C_W1, nullptr, sc->blocked.as<uint8_t>(),
-                            sc->stack_depth, grid_trace, derr, dstats, wc ? wc + 4 : nullptr, (int)(maxq * nl),
-                            sc->sskip.as<uint2>(), st));
-            CK(clk.end());
-            CK(clk.begin(POV_GPU_STAGE_RESOLVE));
-            CK(launch_resolve(pcur, ccur, sc->num_lights, sc->sq_slot.as<int>(), sc->blocked.as<uint8_t>(),
-                              cnt + C_SQ, sc->slot_contrib.as<float4>(), sc->paths.as<PathState>(), grid_shade,
-                              (int)maxq, (int)(maxq * nl), st));
-            CK(clk.end(2));
-        }
-        std::swap(qcur, qnext);
-        std::swap(pcur, pnext);
-        std::swap(ccur, cnext);
-        std::swap(kcur, knext);
-    }
+    int rc = run_levels(sc, clk, B, maxq, 0, sc->max_trace_level, 0, false);
+    if (rc != POV_GPU_OK)
+        return rc;
     // finalize reads the sample count from the block offsets / position count
     CK(clk.begin(POV_GPU_STAGE_FINALIZE));
-    CK(launch_finalize(sc->paths.as<PathState>(), mode == 2 ? npos : block_off + nblocks, (int)maxq, slot, out, st));
+    CK(launch_finalize(B.paths.as<PathState>(), mode == 2 ? npos : block_off + nblocks, (int)maxq, slot, out, st));
     CK(clk.end());
+    return POV_GPU_OK;
+}
+
+// Radiosity counters of the call into the public statistics.
+int rad_collect(PovGpuScene* sc, PovGpuStats* stats)
+{
+    if (!sc->rad.enabled || !stats)
+        return POV_GPU_OK;
+    unsigned long long h[RST_COUNT] = {0};
+    CK(cudaMemcpy(h, sc->rad.rstats.p, sizeof(h), cudaMemcpyDeviceToHost));
+    stats->radiosity_reuse = h[RST_REUSED];
+    stats->radiosity_gathers_d0 = h[RST_GATHERS0];
+    stats->radiosity_gathers_d1 = h[RST_GATHERS1];
+    stats->radiosity_gathers = h[RST_GATHERS0] + h[RST_GATHERS1];
+    stats->radiosity_rays = sc->rad.rays_shot;
+    return POV_GPU_OK;
+}
+
+int rad_begin_call(PovGpuScene* sc, bool final_trace)
+{
+    RadiosityState& R = sc->rad;
+    if (!R.enabled)
+        return POV_GPU_OK;
+    R.final_trace = final_trace;
+    R.error_bound = R.set.error_bound * (final_trace ? 1.0 : R.set.low_error_factor);
+    R.rays_shot = 0;
+    CK(cudaMemsetAsync(R.rstats.p, 0, sizeof(unsigned long long) * RST_COUNT, sc->active()));
     return POV_GPU_OK;
 }
 
@@ -1171,6 +1561,8 @@ int pov_gpu_trace_blocks(PovGpuScene* sc, const PovGpuBlock* blocks, int32_t num
     CK(cudaMemsetAsync(sc->err.p, 0, sizeof(uint32_t) * 4, st));
     if (wc)
         CK(cudaMemsetAsync(wc, 0, sizeof(unsigned long long) * 8, st));
+    if (int rr = rad_begin_call(sc, true))
+        return rr;
 
     uint64_t n_pixels = (uint64_t)n, n_samples = 0;
     if (!aa) {
@@ -1254,6 +1646,8 @@ int pov_gpu_trace_blocks(PovGpuScene* sc, const PovGpuBlock* blocks, int32_t num
     if (stats) {
         stats->number_of_pixels = n_pixels;
         stats->number_of_samples = n_samples;
+        if (int rr = rad_collect(sc, stats))
+            return rr;
     }
     clk.collect();
     if (wc) {
@@ -1264,6 +1658,116 @@ int pov_gpu_trace_blocks(PovGpuScene* sc, const PovGpuBlock* blocks, int32_t num
             sc->timings.rays_traced[k] = hw[4 * k + 3];
         }
     }
+    return rc;
+}
+
+int pov_gpu_set_pretrace_jitter(PovGpuScene* sc, const double* table, int32_t n)
+{
+    if (!sc || n < 0 || (n > 0 && !table))
+        return POV_GPU_E_INVALID;
+    std::lock_guard<std::mutex> g(sc->lock);
+    sc->rad.jitter.assign(table, table + n);
+    return POV_GPU_OK;
+}
+
+int pov_gpu_radiosity_pretrace(PovGpuScene* sc, const PovGpuBlock* blocks, int32_t num_blocks,
+                               const PovGpuRenderParams* params, PovGpuStats* stats)
+{
+    if (!sc || !params || num_blocks < 0 || (num_blocks > 0 && !blocks) || params->width <= 0 ||
+        params->height <= 0)
+        return POV_GPU_E_INVALID;
+    std::lock_guard<std::mutex> g(sc->lock);
+    if (!sc->rad.enabled)
+        return POV_GPU_E_INVALID;
+    cudaSetDevice(sc->device);
+    RadiosityState& R = sc->rad;
+    const PovGpuRadiosity& rs = R.set;
+    // pass sizes (View::StartRender, view.cpp:1060-1080)
+    const double maxwh = (double)std::max(params->width, params->height);
+    double start = maxwh * rs.pretrace_start, end = maxwh * rs.pretrace_end;
+    if (end < 1.0)
+        end = 1.0;
+    int steps = (int)std::floor(std::log(start / end) / std::log(2.0) + (1.0 - EPSILON)) + 1;
+    if (steps > 253) {
+        steps = 253;
+        start = end * std::pow(2.0, (double)steps);
+    }
+    // sample positions of every pass (RadiosityTask::Run,
+    // radiositytask.cpp:123-207): a grid of the pass's spacing over each
+    // block, jittered by the task's table when the caller supplied it
+    std::vector<std::vector<double2>> passes((size_t)steps);
+    for (int pass = 0; pass < steps; pass++) {
+        const double size = std::max(start * (double)std::pow(0.5f, (float)pass), end);
+        const double jit = std::min(1.0, size / 2.0), offset = (size - 1.0) / 2.0;
+        const unsigned step_id = 1u + (unsigned)pass;   // kOctreePassFirst + pass
+        for (int b = 0; b < num_blocks; b++) {
+            const PovGpuBlock& B = blocks[b];
+            if (B.left < 0 || B.top < 0 || B.right < B.left || B.bottom < B.top || B.right >= params->width ||
+                B.bottom >= params->height)
+                return POV_GPU_E_INVALID;
+            const double sx = std::ceil((B.left - 0.5) / size) * size, sy = std::ceil((B.top - 0.5) / size) * size;
+            const double ex = B.left + (double)(B.right - B.left + 1), ey = B.top + (double)(B.bottom - B.top + 1);
+            size_t ji = R.jitter.empty() ? 0 : (size_t)(step_id * 17u + B.serial * 13u) % R.jitter.size();
+            uint32_t hseed = step_id * 0x9E3779B1u ^ B.serial * 0x85EBCA77u;
+            for (double y = sy; y < ey; y += size) {
+                if (y < B.top)
+                    continue;
+                for (double x = sx; x < ex; x += size) {
+                    if (x < B.left)
+                        continue;
+                    double jx, jy;
+                    if (!R.jitter.empty()) {
+                        // the reference build evaluates the y argument's
+                        // jitter first (radiositytask.cpp:197)
+                        ji = (ji + 1) % R.jitter.size();
+                        jy = R.jitter[ji];
+                        ji = (ji + 1) % R.jitter.size();
+                        jx = R.jitter[ji];
+                    } else {
+                        hseed = hseed * 1664525u + 1013904223u;
+                        jy = (double)(hseed >> 8) / 8388608.0 - 1.0;
+                        hseed = hseed * 1664525u + 1013904223u;
+                        jx = (double)(hseed >> 8) / 8388608.0 - 1.0;
+                    }
+                    passes[pass].push_back(make_double2(x + offset + jit * jx, y + offset + jit * jy));
+                }
+            }
+        }
+    }
+    cudaStream_t st = sc->active();
+    StageClock clk(sc, st);
+    CK(cudaMemsetAsync(sc->stats.p, 0, sizeof(unsigned long long) * ST_COUNT, st));
+    CK(cudaMemsetAsync(sc->err.p, 0, sizeof(uint32_t) * 4, st));
+    if (int rr = rad_reset(sc))
+        return rr;
+    if (int rr = rad_begin_call(sc, false))
+        return rr;
+    uint64_t npix = 0;
+    for (int pass = 0; pass < steps; pass++) {
+        const std::vector<double2>& pos = passes[pass];
+        const int n = (int)pos.size();
+        if (n == 0)
+            continue;
+        npix += (uint64_t)n;
+        CK(sc->spos.ensure(sizeof(double2) * (size_t)n));
+        CK(sc->pos_count.ensure(sizeof(int)));
+        CK(sc->out.ensure(sizeof(float4) * (size_t)n));
+        CK(cudaMemcpyAsync(sc->spos.p, pos.data(), sizeof(double2) * (size_t)n, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(sc->pos_count.p, &n, sizeof(int), cudaMemcpyHostToDevice, st));
+        int rc = run_samples(sc, clk, 2, 0, nullptr, sc->spos.as<double2>(), sc->pos_count.as<int>(), n,
+                             params->width, params->height, nullptr, sc->out.as<float4>());
+        CK(cudaStreamSynchronize(st));   // `n` and `pos` must outlive the copies
+        if (rc != POV_GPU_OK)
+            return rc;
+    }
+    unsigned long long hs[ST_COUNT];
+    int rc = check_device_error(sc, stats, hs);
+    if (stats) {
+        stats->number_of_pixels = npix;
+        if (int rr = rad_collect(sc, stats))
+            return rr;
+    }
+    clk.collect();
     return rc;
 }
 

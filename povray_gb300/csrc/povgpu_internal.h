@@ -59,7 +59,7 @@ struct __align__(16) DevMaterial {
     float specular;
     float roughness;        // already inverted
     int32_t has_reflection;
-    int32_t pad;
+    float   diffuse_raw;    // Finish->Diffuse, the radiosity ambient's factor (trace.cpp:898)
 };
 
 struct __align__(16) DevLight {
@@ -175,11 +175,75 @@ struct __align__(16) PathState {
     float4 throughput;  // rgb, weight
 };
 
+// ------------------------------------------------------------ radiosity --
+// One radiosity ambient query (RadiosityFunction::ComputeAmbient): a hit
+// point, its ray-facing normal, the query weight, the factor the ambient
+// colour is added with (pigment * Diffuse * path throughput), the path or
+// gather ray it adds to, and the surface a gather from it starts on.
+struct __align__(16) RadQuery {
+    float4   p;         // xyz, weight (ray weight * largest possible contribution)
+    float4   n;         // xyz, -
+    float4   factor;    // rgb, -
+    int32_t  path;
+    uint32_t prim, aux;
+    int32_t  pad;
+};
+
+// One cached radiosity sample (ot_block_struct, octree.h:86-104).
+struct __align__(16) RadBlock {
+    float4 p;           // Point, Harmonic_Mean_Distance
+    float4 n;           // S_Normal, Nearest_Distance
+    float4 tn;          // To_Nearest_Surface, Quality
+    float4 ill;         // Illuminance, Bounce_Depth (int bits)
+};
+
+// The sample cache in device memory: blocks, and the octree nodes as an
+// open-addressing hash (64-bit node key -> head of the node's block list).
+struct RadCacheView {
+    RadBlock*           blocks;
+    int32_t*            next;
+    int32_t*            count;      // blocks in use (device word)
+    int32_t             cap;
+    unsigned long long* keys;       // 0 = empty slot
+    int32_t*            heads;
+    uint32_t            mask;       // slots - 1
+    int32_t*            size_range; // smallest, largest node size (biased log2) in use
+};
+
+// Settings of one bounce depth for the query and gather kernels
+// (RadiosityRecursionSettings, radiosity.cpp:177-294, plus the task's state).
+struct RadParams {
+    int32_t depth;
+    int32_t final_trace;        // final trace (1) or pretrace (0)
+    int32_t always_sample;
+    int32_t reuse_count;
+    int32_t rays_per_sample;
+    float   error_bound;        // errorBound, times low_error_factor in pretrace
+    float   error_bound_factor;
+    float   min_reuse_factor, max_reuse_factor, address_factor;
+    float   gather_weight;      // weight of this depth's sample rays
+    float   gray, brightness;
+    float   adc;                // radiosity adc_bailout
+};
+
+// What the shading kernel does for radiosity: emit an ambient query per
+// hit (rq non-null) when the hit's largest possible contribution beats
+// `adc`; `gather` marks radiosity sample rays, shaded by the radiosity
+// Trace (no highlights, area lights as point lights, no reflection rays).
+struct ShadeRad {
+    RadQuery* rq;
+    int32_t*  rq_count;
+    int32_t   rq_cap;
+    float     adc;
+    int32_t   gather;
+};
+
 // Device error word bits.
 enum DevError : uint32_t {
     DE_STACK_OVERFLOW = 1u,
     DE_ITERATION_CAP  = 2u,
     DE_QUEUE_OVERFLOW = 4u,
+    DE_CACHE_FULL     = 8u,
 };
 
 // Counters (device, uint64).

@@ -866,13 +866,13 @@ __device__ __forceinline__ uint32_t skip_aux(const QHit& h)
 // One thread per ray of the level queue.  Emits shadow rays (one per lit
 // light, slot = ray*num_lights+light) and the reflection ray.
 __global__ void __launch_bounds__(128) k_shade(
-    DeviceScene S, int level, const QRay* __restrict__ q, const int* __restrict__ q_path,
+    DeviceScene S, int level, int max_level, const QRay* __restrict__ q, const int* __restrict__ q_path,
     const QHit* __restrict__ hits, const int* __restrict__ q_count, PathState* __restrict__ paths,
     float4* __restrict__ slot_contrib, QRay* __restrict__ sq, int* __restrict__ sq_slot, int* __restrict__ sq_count,
     uint2* __restrict__ sq_skip, QRay* __restrict__ nq, int* __restrict__ nq_path,
     uint2* __restrict__ nq_skip, int* __restrict__ nq_count, int max_queue,
     int max_shadow, QRay* __restrict__ aq, int* __restrict__ aq_slot, uint2* __restrict__ aq_skip,
-    int* __restrict__ aq_count, int max_area, uint32_t* err, unsigned long long* stats)
+    int* __restrict__ aq_count, int max_area, ShadeRad rad, uint32_t* err, unsigned long long* stats)
 {
     const int n = min(*q_count, max_queue);
     const int nl = S.num_lights;
@@ -885,7 +885,7 @@ __global__ void __launch_bounds__(128) k_shade(
             continue;
         QRay r = q[i];
         QHit h = hits[i];
-        int path = q_path[i];
+        int path = q_path ? q_path[i] : i;
         float3 o = xyz(r.org), d = xyz(r.dir);
         PathState ps = paths[path];
         float3 thr = xyz(ps.throughput);
@@ -913,6 +913,34 @@ __global__ void __launch_bounds__(128) k_shade(
         } else {
             col = xyz(S.background);   // ComputeSky, background only
         }
+        // radiosity ambient query (ComputeLightedTexture, trace.cpp:896-921):
+        // the largest possible contribution (pigment greyscale * Diffuse)
+        // must beat the ray's ADC bailout
+        bool rq_emit = false;
+        float rq_maxc = 0.f;
+        if (hit && rad.rq) {
+            float3 pg = xyz(m->pigment);
+            rq_maxc = (0.297f * pg.x + 0.589f * pg.y + 0.114f * pg.z) * m->diffuse_raw;
+            rq_emit = rq_maxc > rad.adc;
+        }
+        int rqs = rad.rq ? warp_reserve(rad.rq_count, rq_emit, mask) : 0;
+        if (rq_emit) {
+            if (rqs < rad.rq_cap) {
+                RadQuery qq;
+                float3 pg = xyz(m->pigment);
+                qq.p = make_float4(p.x, p.y, p.z, weight * rq_maxc);
+                qq.n = make_float4(N.x, N.y, N.z, 0.f);
+                float dr = m->diffuse_raw;
+                qq.factor = make_float4(pg.x * dr * thr.x, pg.y * dr * thr.y, pg.z * dr * thr.z, 0.f);
+                qq.path = path;
+                qq.prim = self.x;
+                qq.aux = self.y;
+                qq.pad = 0;
+                rad.rq[rqs] = qq;
+            } else {
+                set_error(err, DE_QUEUE_OVERFLOW);
+            }
+        }
         // per-light terms (ComputeOneDiffuseLight, trace.cpp:1637-1729)
         for (int l = 0; l < nl; l++) {
             bool emit = false;
@@ -922,7 +950,9 @@ __global__ void __launch_bounds__(128) k_shade(
             bool area = false;
             if (hit) {
                 const DevLight& L = S.lights[l];
-                area = L.center.w != 0.0f;   // POV_LIGHT_AREA
+                // the radiosity Trace runs with area lights off
+                // (GetRadiosityQualityFlags, radiosity.cpp:148-161)
+                area = L.center.w != 0.0f && !rad.gather;   // POV_LIGHT_AREA
                 float3 lv = xyz(L.center) - p;
                 ldist = sqrtf(dot3(lv, lv));
                 ld = lv * (1.0f / ldist);
@@ -937,14 +967,14 @@ __global__ void __launch_bounds__(128) k_shade(
                         inten *= m->diffuse;
                         contrib = contrib + pig * lc * inten;
                     }
-                    if (m->phong > 0.0f) {     // ComputePhongColour, trace.cpp:2520-2558
+                    if (m->phong > 0.0f && !rad.gather) {     // ComputePhongColour, trace.cpp:2520-2558
                         float c2 = -2.0f * dot3(d, N);
                         float3 rd = d + N * c2;
                         float ci = dot3(rd, ld);
                         if (ci > 0.0f && (m->phong_size < 60.0f || ci > 0.0008f))
                             contrib = contrib + lc * (m->phong * powf(ci, m->phong_size));
                     }
-                    if (m->specular > 0.0f) {  // ComputeSpecularColour, trace.cpp:2560-2593
+                    if (m->specular > 0.0f && !rad.gather) {  // ComputeSpecularColour, trace.cpp:2560-2593
                         float3 half = (ld - d) * 0.5f;
                         float hl = sqrtf(dot3(half, half));
                         if (hl > 0.0f) {
@@ -992,7 +1022,7 @@ __global__ void __launch_bounds__(128) k_shade(
         float3 reflec = f3(0.f, 0.f, 0.f);
         float rweight = 0.f;
         float3 nd = f3(0.f, 0.f, 1.f);
-        if (hit && m->has_reflection) {
+        if (hit && m->has_reflection && !rad.gather) {
             float cos_inc = -dot3(d, N);
             float falloff = m->reflect.w;
             float frac = fabsf(falloff - 1.0f) > EPSILON_F ? powf(1.0f - cos_inc, falloff) : 1.0f - cos_inc;
@@ -1008,7 +1038,7 @@ __global__ void __launch_bounds__(128) k_shade(
                 // fix-ups of ComputeReflection never trigger
                 float n2 = -2.0f * dot3(d, N);
                 nd = normalize3(d + N * n2);
-                refl = (level + 1 < S.max_trace_level) && (rweight >= S.adc_bailout);
+                refl = (level + 1 < max_level) && (rweight >= rad.adc);
             }
         }
         int rs = warp_reserve(nq_count, refl, mask);
@@ -1529,15 +1559,17 @@ cudaError_t launch_trace(const DeviceScene& S, bool any_hit, const QRay* q, cons
     return cudaGetLastError();
 }
 
-cudaError_t launch_shade(const DeviceScene& S, int level, const QRay* q, const int* q_path, const QHit* hits,
+cudaError_t launch_shade(const DeviceScene& S, int level, int max_level, const QRay* q, const int* q_path,
+                         const QHit* hits,
                          const int* q_count, PathState* paths, float4* slot_contrib, QRay* sq, int* sq_slot,
                          int* sq_count, uint2* sq_skip, QRay* nq, int* nq_path, uint2* nq_skip, int* nq_count,
                          int max_queue, int max_shadow, QRay* aq, int* aq_slot, uint2* aq_skip, int* aq_count,
-                         int max_area, int grid, uint32_t* err, unsigned long long* stats, cudaStream_t st)
+                         int max_area, const ShadeRad& rad, int grid, uint32_t* err, unsigned long long* stats,
+                         cudaStream_t st)
 {
-    k_shade<<<grid, 128, 0, st>>>(S, level, q, q_path, hits, q_count, paths, slot_contrib, sq, sq_slot, sq_count,
+    k_shade<<<grid, 128, 0, st>>>(S, level, max_level, q, q_path, hits, q_count, paths, slot_contrib, sq, sq_slot, sq_count,
                                   sq_skip, nq, nq_path, nq_skip, nq_count, max_queue, max_shadow, aq, aq_slot,
-                                  aq_skip, aq_count, max_area, err, stats);
+                                  aq_skip, aq_count, max_area, rad, err, stats);
     return cudaGetLastError();
 }
 

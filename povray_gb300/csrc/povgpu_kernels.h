@@ -16,11 +16,13 @@ cudaError_t launch_trace(const DeviceScene& S, bool any_hit, const QRay* q, cons
                          QHit* hits, uint8_t* blocked, int stack_depth, int grid, uint32_t* err,
                          unsigned long long* stats, unsigned long long* wcount, int cap, const uint2* skips,
                          cudaStream_t st);
-cudaError_t launch_shade(const DeviceScene& S, int level, const QRay* q, const int* q_path, const QHit* hits,
+cudaError_t launch_shade(const DeviceScene& S, int level, int max_level, const QRay* q, const int* q_path,
+                         const QHit* hits,
                          const int* q_count, PathState* paths, float4* slot_contrib, QRay* sq, int* sq_slot,
                          int* sq_count, uint2* sq_skip, QRay* nq, int* nq_path, uint2* nq_skip, int* nq_count,
                          int max_queue, int max_shadow, QRay* aq, int* aq_slot, uint2* aq_skip, int* aq_count,
-                         int max_area, int grid, uint32_t* err, unsigned long long* stats, cudaStream_t st);
+                         int max_area, const ShadeRad& rad, int grid, uint32_t* err, unsigned long long* stats,
+                         cudaStream_t st);
 cudaError_t launch_area_shadow(const DeviceScene& S, const QRay* aq, const int* aq_slot, const uint2* aq_skip,
                                const int* aq_count, int cap, float4* slot_contrib, int stack_depth, int grid,
                                uint32_t* err, unsigned long long* stats, cudaStream_t st);

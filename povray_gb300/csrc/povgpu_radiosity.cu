@@ -1,0 +1,501 @@
+// povgpu_radiosity.cu -- radiosity on the GPU: the sample cache query
+// (RadiosityCache::FindReusableBlock / AverageNearBlock), the gather of new
+// samples (RadiosityFunction::GatherLight) and their insertion
+// (RadiosityCache::AddBlock), source/core/lighting/radiosity.cpp.
+//
+// The reference answers queries one at a time, each one either reusing the
+// cache or gathering a new sample that later queries see.  Here a batch of
+// queries runs in rounds: every round queries the cache for all open
+// queries; those the cache satisfies resolve, and of the rest one per
+// spatial cell (cells shrinking round by round from the largest reuse
+// radius to the smallest) gathers a new sample; the others wait for the
+// next round and see the new samples.  The last round gathers for all that
+// remain.
+//
+// The cache keeps the reference's octree addressing: a sample is filed at
+// the node ot_index_sphere picks (source/core/support/octree.cpp:1035-1190)
+// and a query sees exactly the samples of nodes whose half-size-extended
+// box holds the query point (what ot_dist_traverse visits, octree.cpp:
+// 800-855).  Nodes live in an open-addressing hash keyed by a 64-bit mix of
+// (size, x, y, z); each node holds a lock-free list of its blocks.
+#include "povgpu_internal.h"
+#include "povgpu_kernels.h"
+#include "povgpu_radiosity.h"
+
+#include <cuda_runtime.h>
+#include <math_constants.h>
+#include <stdint.h>
+
+namespace povgpu {
+
+namespace {
+
+constexpr double OT_BIAS = 10000000.;            // octree.h:81
+constexpr float RAD_EPSILON = 0.001f;            // radiosity.cpp:110
+constexpr float AVG_NEAR_EPSILON = 0.000001f;    // radiosity.cpp:109
+constexpr float IN_FRONT_LIMIT = -0.05f;         // radiosity.cpp:100
+constexpr float WEIGHT_ERROR_BOUND_OFFSET = 0.25f;   // radiosity.cpp:111
+constexpr int MAX_PROBES = 1 << 20;
+
+__constant__ float3 c_dirs[RAD_DIRECTIONS];      // Halton(2,3) cosine-weighted directions
+
+__device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
+__device__ __forceinline__ float3 add(float3 a, float3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ float3 sub(float3 a, float3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ float3 mul(float3 a, float s) { return f3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float dot(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float3 cross(float3 a, float3 b)
+{
+    return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ float3 xyz(float4 v) { return f3(v.x, v.y, v.z); }
+__device__ __forceinline__ float3 normalized(float3 v) { return mul(v, rsqrtf(dot(v, v))); }
+
+__device__ __forceinline__ float to_eye(const DeviceScene& S, float3 p)
+{
+    double dx = S.cam_loc[0] - p.x, dy = S.cam_loc[1] - p.y, dz = S.cam_loc[2] - p.z;
+    return (float)sqrt(dx * dx + dy * dy + dz * dz);
+}
+
+// Pow2Floor / BiasedIntLog2 / BiasedIntPow2 (octree.cpp:169-250).
+__device__ __forceinline__ float pow2_floor(float a) { return __uint_as_float(__float_as_uint(a) & 0xFF800000u); }
+__device__ __forceinline__ int biased_log2(float a) { return (int)((__float_as_uint(a) & 0x7F800000u) >> 23); }
+__device__ __forceinline__ double biased_pow2(int e) { return (double)__uint_as_float(((uint32_t)e & 0xFFu) << 23); }
+
+// ot_point_in_node (octree.cpp:985-997).
+__device__ __forceinline__ bool in_node(double px, double py, double pz, int size, int x, int y, int z)
+{
+    double s = biased_pow2(size);
+    return fabs(px + OT_BIAS - ((double)x + 0.5) * s) < s && fabs(py + OT_BIAS - ((double)y + 0.5) * s) < s &&
+           fabs(pz + OT_BIAS - ((double)z + 0.5) * s) < s;
+}
+
+__device__ __forceinline__ unsigned long long node_key(int size, int x, int y, int z)
+{
+    unsigned long long h = (unsigned long long)(uint32_t)size * 0x9E3779B97F4A7C15ull;
+    h ^= (unsigned long long)(uint32_t)x * 0xC2B2AE3D27D4EB4Full;
+    h = (h ^ (h >> 29)) * 0xBF58476D1CE4E5B9ull;
+    h ^= (unsigned long long)(uint32_t)y * 0x94D049BB133111EBull;
+    h = (h ^ (h >> 32)) * 0x9E3779B97F4A7C15ull;
+    h ^= (unsigned long long)(uint32_t)z * 0xD6E8FEB86659FD93ull;
+    h ^= h >> 31;
+    return h ? h : 1ull;
+}
+
+// Head of the node's block list, -1 when the node holds nothing.
+__device__ __forceinline__ int node_lookup(const RadCacheView& C, unsigned long long key)
+{
+    uint32_t slot = (uint32_t)key & C.mask;
+    for (int n = 0; n < MAX_PROBES; n++) {
+        unsigned long long k = C.keys[slot];
+        if (k == key)
+            return C.heads[slot];
+        if (k == 0ull)
+            return -1;
+        slot = (slot + 1) & C.mask;
+    }
+    return -1;
+}
+
+// Slot of the node, created when absent; -1 when the table is full.
+__device__ __forceinline__ int node_insert(const RadCacheView& C, unsigned long long key)
+{
+    uint32_t slot = (uint32_t)key & C.mask;
+    for (int n = 0; n < MAX_PROBES && n <= (int)C.mask; n++) {
+        unsigned long long k = atomicCAS(&C.keys[slot], 0ull, key);
+        if (k == 0ull || k == key)
+            return (int)slot;
+        slot = (slot + 1) & C.mask;
+    }
+    return -1;
+}
+
+// ot_index_sphere / ot_index_box with SAFE_METHOD and ot_parent
+// (octree.cpp:1035-1238): the node a sample of this address radius is
+// filed at.
+__device__ void ot_index_sphere(float3 c, double radius, int& size, int& x, int& y, int& z)
+{
+    double lo[3] = {c.x - radius, c.y - radius, c.z - radius};
+    double hi[3] = {c.x + radius, c.y + radius, c.z + radius};
+    double desired = fmax(fmax(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
+    double bsized = pow2_floor((float)desired);
+    if (bsized == 0.0)
+        bsized = 1.0;
+    double maxord = fmax(fmax(fabs(lo[0]), fabs(lo[1])), fabs(lo[2])) + OT_BIAS;
+    for (int k = 0; k < 64 && maxord / bsized > 1000000000.0; k++)
+        bsized *= 2.0;
+    x = (int)floor(((lo[0] + hi[0]) / 2 + OT_BIAS) / bsized);
+    y = (int)floor(((lo[1] + hi[1]) / 2 + OT_BIAS) / bsized);
+    z = (int)floor(((lo[2] + hi[2]) / 2 + OT_BIAS) / bsized);
+    size = biased_log2((float)bsized);
+    for (int k = 0; k < 64 && !(in_node(lo[0], lo[1], lo[2], size, x, y, z) && in_node(hi[0], hi[1], hi[2], size, x, y, z));
+         k++) {
+        size += 1;
+        x = x >= 0 ? x >> 1 : (x + 1) / 2;
+        y = y >= 0 ? y >> 1 : (y + 1) / 2;
+        z = z >= 0 ? z >> 1 : (z + 1) / 2;
+    }
+}
+
+// RadiosityCache::AverageNearBlock (radiosity.cpp:1551-1770): pseudo-sigmoid
+// weight for final-trace depth-0 queries, linear otherwise; no gradient.
+__device__ __forceinline__ void average_near(const RadBlock& b, float3 P, float3 N, float eb, bool final_trace,
+                                             float& W, float3& WI)
+{
+    float3 bp = xyz(b.p);
+    float3 delta = sub(P, bp);
+    float sq = dot(delta, delta);
+    float quick = b.p.w * eb;
+    if (!(sq < quick * quick))
+        return;
+    float dist = sqrtf(sq);
+    float ri = b.p.w;
+    bool far = dist > AVG_NEAR_EPSILON;
+    float3 du = f3(0.f, 0.f, 0.f);
+    if (far) {
+        du = mul(delta, 1.0f / dist);
+        float c = dot(xyz(b.tn), du);
+        if (c > 0.0f)
+            ri = c * b.n.w + (1.0f - c) * ri;
+    }
+    if (!(dist < ri * eb))
+        return;
+    float3 bn = xyz(b.n);
+    float e = dist / ri + 2.0f * sqrtf(fabsf(1.0f - dot(N, bn)));
+    if (!(e < eb))
+        return;
+    float in_front = 1.0f;
+    if (far) {
+        float3 half = add(N, bn);
+        in_front = dot(du, half) * rsqrtf(dot(half, half));
+    }
+    if (!(in_front > IN_FRONT_LIMIT))
+        return;
+    int bdepth = __float_as_int(b.ill.w);
+    float w;
+    if (!final_trace || bdepth > 0) {
+        w = 1.0f - e / eb;
+    } else {
+        w = e / eb;
+        w = w < 0.5f ? 1.0f - (w * 2.0f) * (w * 2.0f) / 2.0f : ((1.0f - w) * 2.0f) * ((1.0f - w) * 2.0f) / 2.0f;
+    }
+    if (in_front <= 0.0f)
+        w *= 1.0f - in_front / IN_FRONT_LIMIT;
+    if (w > RAD_EPSILON) {
+        w *= b.tn.w;
+        WI = add(WI, mul(xyz(b.ill), w));
+        W += w;
+    }
+}
+
+// RadiosityCache::FindReusableBlock (radiosity.cpp:1458-1512).
+__device__ void find_reusable(const RadCacheView& C, int smin, int smax, float3 P, float3 N, float eb, int depth,
+                              bool final_trace, float& W, float3& WI)
+{
+    W = 0.0f;
+    WI = f3(0.f, 0.f, 0.f);
+    const double px = P.x, py = P.y, pz = P.z;
+    for (int size = smin; size <= smax; size++) {
+        double s = biased_pow2(size);
+        int bx = (int)floor((px + OT_BIAS) / s - 1.5);
+        int by = (int)floor((py + OT_BIAS) / s - 1.5);
+        int bz = (int)floor((pz + OT_BIAS) / s - 1.5);
+        // a node's extended box holds the point only for cells bx+1, bx+2
+        // per axis
+        for (int c = 0; c < 8; c++) {
+            int x = bx + 1 + (c & 1), y = by + 1 + ((c >> 1) & 1), z = bz + 1 + (c >> 2);
+            if (!in_node(px, py, pz, size, x, y, z))
+                continue;
+            int b = node_lookup(C, node_key(size, x, y, z));
+            for (int n = 0; b >= 0 && n < (1 << 20); n++) {
+                RadBlock blk = C.blocks[b];
+                if (__float_as_int(blk.ill.w) == depth)
+                    average_near(blk, P, N, eb, final_trace, W, WI);
+                b = C.next[b];
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ float4 finish_ambient(float3 a, float quality, const RadParams& R)
+{
+    // ComputeAmbient's grey threshold and brightness (radiosity.cpp:457-461)
+    float grey = 0.297f * a.x + 0.589f * a.y + 0.114f * a.z;
+    a = f3((a.x * (1.0f - R.gray) + R.gray * grey) * R.brightness, (a.y * (1.0f - R.gray) + R.gray * grey) * R.brightness,
+           (a.z * (1.0f - R.gray) + R.gray * grey) * R.brightness);
+    return make_float4(a.x, a.y, a.z, quality);
+}
+
+// One thread per open query: the cache lookup of ComputeAmbient
+// (radiosity.cpp:385-413).  Reusable -> the ambient colour and quality go to
+// out[q]; else the query's partial sums are kept and it either claims its
+// cell for this round (a seed: gathers now) or waits for the next round.
+__global__ void k_rad_query(DeviceScene S, RadCacheView C, RadParams R, const RadQuery* __restrict__ queries,
+                            const int* __restrict__ open, int n_open, int cap, int round,
+                            int last_round, float4* __restrict__ out, float4* __restrict__ partial,
+                            unsigned long long* __restrict__ claims, uint32_t claim_mask, int* __restrict__ seeds,
+                            int* __restrict__ n_seeds, int* __restrict__ next, int* __restrict__ n_next,
+                            unsigned long long* __restrict__ rstats, uint32_t* err)
+{
+    const int n = min(n_open, cap);
+    const int smin = C.size_range[0], smax = C.size_range[1];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int qi = open ? open[i] : i;
+        RadQuery q = queries[qi];
+        float3 P = xyz(q.p), N = xyz(q.n);
+        float eb = R.error_bound;
+        if (q.p.w < WEIGHT_ERROR_BOUND_OFFSET)
+            eb += WEIGHT_ERROR_BOUND_OFFSET - q.p.w;
+        eb *= R.error_bound_factor;
+        float W = 0.f;
+        float3 WI = f3(0.f, 0.f, 0.f);
+        if (smax >= smin)
+            find_reusable(C, smin, smax, P, N, eb, R.depth, R.final_trace != 0, W, WI);
+        bool reuse = W * 4.0f >= (float)R.reuse_count || (R.final_trace && !R.always_sample && W > 0.0f);
+        if (reuse) {
+            float3 a = mul(WI, 1.0f / W);
+            out[qi] = finish_ambient(a, fminf(4.0f * W / (float)R.reuse_count, 1.0f), R);
+            atomicAdd(&rstats[RST_REUSED], 1ull);
+            continue;
+        }
+        partial[qi] = make_float4(WI.x, WI.y, WI.z, W);
+        bool seed = round >= last_round;
+        if (!seed) {
+            // cell of this round: the largest reuse radius halved per round,
+            // not below the smallest (GatherLight's reuse distance clamps)
+            float te = to_eye(S, P);
+            float h = fmaxf(te * R.max_reuse_factor * eb * exp2f(-(float)round), te * R.min_reuse_factor * eb);
+            int lvl = (int)ceilf(log2f(fmaxf(h, 1e-6f)));
+            float cs = exp2f((float)lvl);
+            int cx = (int)floorf(P.x / cs), cy = (int)floorf(P.y / cs), cz = (int)floorf(P.z / cs);
+            unsigned long long key = node_key(lvl + 1024 * round, cx, cy, cz);
+            uint32_t slot = (uint32_t)key & claim_mask;
+            for (int k = 0; k <= (int)claim_mask; k++) {
+                unsigned long long old = atomicCAS(&claims[slot], 0ull, key);
+                if (old == 0ull) { seed = true; break; }
+                if (old == key) break;
+                slot = (slot + 1) & claim_mask;
+            }
+        }
+        if (seed) {
+            int s = atomicAdd(n_seeds, 1);
+            if (s < cap) seeds[s] = qi; else atomicOr(err, DE_QUEUE_OVERFLOW);
+        } else {
+            int s = atomicAdd(n_next, 1);
+            if (s < cap) next[s] = qi; else atomicOr(err, DE_QUEUE_OVERFLOW);
+        }
+    }
+}
+
+// Direction k of seed s: entry (base + s*count + k) of the direction pool,
+// turned into the frame of the seed's normal (SampleDirectionGenerator::
+// InitSequence / GetDirection, radiosity.cpp:815-888).
+__device__ __forceinline__ float3 sample_direction(float3 fy, int base, int s, int count, int k)
+{
+    float3 off = fabsf(fy.z) > 0.9f ? f3(0.f, 1.f, 0.f) : f3(0.f, 0.f, 1.f);
+    float3 fx = normalized(cross(fy, off));
+    float3 fz = normalized(cross(fx, fy));
+    float3 rv = c_dirs[(int)(((long long)base + (long long)s * count + k) % RAD_DIRECTIONS)];
+    rv.y = fabsf(rv.y);
+    if (fy.y > 1.0f - RAD_EPSILON)
+        return rv;
+    if (fy.y < -1.0f + RAD_EPSILON)
+        return mul(rv, -1.0f);
+    return add(add(mul(fx, rv.x), mul(fy, rv.y)), mul(fz, rv.z));
+}
+
+// One thread per sample ray of the seeds: the first queue of the sample
+// rays' wavefront (path i = ray i, quality 1, weight of the depth).
+__global__ void k_gather_rays(const RadQuery* __restrict__ queries, const int* __restrict__ seeds, int ns, int count,
+                              int base, float weight, QRay* __restrict__ rays, int* __restrict__ q_path,
+                              uint2* __restrict__ skips, PathState* __restrict__ paths, float* __restrict__ quality,
+                              int* __restrict__ q_count, unsigned long long* __restrict__ stats)
+{
+    const long total = (long)ns * count;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        *q_count = (int)total;
+        atomicAdd(&stats[ST_RAYS], (unsigned long long)total);   // each is a TraceRay call
+    }
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+        int s = (int)(i / count), k = (int)(i % count);
+        RadQuery q = queries[seeds[s]];
+        float3 d = sample_direction(xyz(q.n), base, s, count, k);
+        QRay r;
+        r.org = make_float4(q.p.x, q.p.y, q.p.z, 1.0e-4f);   // MIN_ISECT_DEPTH
+        r.dir = make_float4(d.x, d.y, d.z, CUDART_INF_F);
+        rays[i] = r;
+        q_path[i] = (int)i;
+        skips[i] = make_uint2(q.prim, q.aux);
+        PathState ps;
+        ps.colour = make_float4(0.f, 0.f, 0.f, 0.f);
+        ps.throughput = make_float4(1.f, 1.f, 1.f, weight);
+        paths[i] = ps;
+        quality[i] = 1.0f;
+    }
+}
+
+// Depth of each sample ray's first hit (infinite for a miss), kept for the
+// reduction while the wavefront moves on to reflection levels.
+__global__ void k_first_hit(const QHit* __restrict__ hits, const int* __restrict__ q_count, int cap,
+                            float* __restrict__ first_t)
+{
+    const int n = min(*q_count, cap);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        QHit h = hits[i];
+        first_t[i] = h.prim == 0xffffffffu ? CUDART_INF_F : h.t;
+    }
+}
+
+// Ambient answers of nested queries (the sample rays' hits) into their rays:
+// colour += ambient * factor; the ray's sample quality is the nested
+// query's (ComputeAmbient's ticket.radiosityQuality, radiosity.cpp:454).
+__global__ void k_rad_apply(const RadQuery* __restrict__ queries, const int* __restrict__ n_queries, int cap,
+                            const float4* __restrict__ amb, PathState* __restrict__ paths,
+                            float* __restrict__ quality)
+{
+    const int n = min(*n_queries, cap);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        RadQuery q = queries[i];
+        float4 a = amb[i];
+        float4 c = paths[q.path].colour;
+        paths[q.path].colour = make_float4(c.x + a.x * q.factor.x, c.y + a.y * q.factor.y, c.z + a.z * q.factor.z, c.w);
+        if (quality)
+            quality[q.path] = fminf(quality[q.path], a.w);
+    }
+}
+
+// One warp per seed: the sums of GatherLight (radiosity.cpp:583-681) over
+// the seed's sample rays, the new block (AddBlock, radiosity.cpp:1194-1233)
+// and the seed's ambient colour (ComputeAmbient, radiosity.cpp:428-461).
+__global__ void k_gather_reduce(DeviceScene S, RadCacheView C, RadParams R, const RadQuery* __restrict__ queries,
+                                const int* __restrict__ seeds, int ns, int base, const float* __restrict__ first_t,
+                                const PathState* __restrict__ paths, const float* __restrict__ quality,
+                                const float4* __restrict__ partial, float4* __restrict__ out,
+                                unsigned long long* __restrict__ rstats, uint32_t* err)
+{
+    const int lane = threadIdx.x & 31;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    const int count = R.rays_per_sample;
+    for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < ns; s += warps) {
+        float3 sum = f3(0.f, 0.f, 0.f);
+        float qsum = 0.f, inv = 0.f, best = CUDART_INF_F;
+        int best_k = -1;
+        for (int k = lane; k < count; k += 32) {
+            long i = (long)s * count + k;
+            float q = quality[i];
+            float3 c = xyz(paths[i].colour);
+            sum = add(sum, mul(c, q));
+            qsum += q;
+            float t = first_t[i];
+            inv += 1.0f / t;
+            if (t < best || (t == best && k < best_k)) { best = t; best_k = k; }
+        }
+        for (int off = 16; off > 0; off >>= 1) {
+            sum.x += __shfl_down_sync(0xffffffffu, sum.x, off);
+            sum.y += __shfl_down_sync(0xffffffffu, sum.y, off);
+            sum.z += __shfl_down_sync(0xffffffffu, sum.z, off);
+            qsum += __shfl_down_sync(0xffffffffu, qsum, off);
+            inv += __shfl_down_sync(0xffffffffu, inv, off);
+            float ob = __shfl_down_sync(0xffffffffu, best, off);
+            int ok = __shfl_down_sync(0xffffffffu, best_k, off);
+            if (ok >= 0 && (ob < best || (ob == best && (best_k < 0 || ok < best_k)))) { best = ob; best_k = ok; }
+        }
+        if (lane != 0)
+            continue;
+        int qi = seeds[s];
+        RadQuery q = queries[qi];
+        float3 P = xyz(q.p);
+        float3 ill = qsum == 0.f ? sum : mul(sum, 1.0f / qsum);
+        float quality_s = qsum / (float)count;
+        float te = to_eye(S, P);
+        float min_d = te * R.min_reuse_factor, max_d = te * R.max_reuse_factor;
+        float mean = (float)count / inv;
+        if (best > max_d * 0.0001f) {
+            mean = fminf(fmaxf(mean, min_d), max_d);
+            int b = atomicAdd(C.count, 1);
+            if (b < C.cap) {
+                float3 tn = best_k >= 0 ? sample_direction(xyz(q.n), base, s, count, best_k) : f3(0.f, 0.f, 0.f);
+                RadBlock blk;
+                blk.p = make_float4(P.x, P.y, P.z, mean);
+                blk.n = make_float4(q.n.x, q.n.y, q.n.z, best);
+                blk.tn = make_float4(tn.x, tn.y, tn.z, quality_s);
+                blk.ill = make_float4(ill.x, ill.y, ill.z, __int_as_float(R.depth));
+                C.blocks[b] = blk;
+                int size, x, y, z;
+                ot_index_sphere(P, (double)mean * R.address_factor, size, x, y, z);
+                int slot = node_insert(C, node_key(size, x, y, z));
+                if (slot >= 0) {
+                    __threadfence();
+                    C.next[b] = atomicExch(&C.heads[slot], b);
+                    atomicMin(&C.size_range[0], size);
+                    atomicMax(&C.size_range[1], size);
+                } else {
+                    atomicOr(err, DE_CACHE_FULL);
+                }
+            } else {
+                atomicOr(err, DE_CACHE_FULL);
+            }
+        }
+        float4 pw = partial[qi];
+        float W = pw.w;
+        // (reused mean * reuse + gathered * quality) / (reuse + quality);
+        // the reused mean times its weight is the weighted sum kept in partial
+        float3 a = W > 0.f ? mul(add(xyz(pw), mul(ill, quality_s)), 1.0f / (W + quality_s)) : ill;
+        out[qi] = finish_ambient(a, fminf(4.0f * (W + quality_s) / (float)R.reuse_count, 1.0f), R);
+        atomicAdd(&rstats[RST_GATHERS0 + min(R.depth, 1)], 1ull);
+    }
+}
+
+inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
+
+}  // namespace
+
+cudaError_t rad_upload_directions(const float* xyz3)
+{
+    return cudaMemcpyToSymbol(c_dirs, xyz3, sizeof(float3) * RAD_DIRECTIONS);
+}
+
+cudaError_t launch_rad_query(const DeviceScene& S, const RadCacheView& C, const RadParams& R, const RadQuery* queries,
+                             const int* open, int n_open, int cap, int round, int last_round, float4* out,
+                             float4* partial, unsigned long long* claims, uint32_t claim_mask, int* seeds,
+                             int* n_seeds, int* next, int* n_next, unsigned long long* rstats, uint32_t* err,
+                             int grid, cudaStream_t st)
+{
+    k_rad_query<<<grid, 128, 0, st>>>(S, C, R, queries, open, n_open, cap, round, last_round, out, partial, claims,
+                                      claim_mask, seeds, n_seeds, next, n_next, rstats, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather_rays(const RadQuery* queries, const int* seeds, int ns, int count, int base, float weight,
+                               QRay* rays, int* q_path, uint2* skips, PathState* paths, float* quality, int* q_count,
+                               unsigned long long* stats, int grid, cudaStream_t st)
+{
+    k_gather_rays<<<grid, 256, 0, st>>>(queries, seeds, ns, count, base, weight, rays, q_path, skips, paths, quality,
+                                        q_count, stats);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_first_hit(const QHit* hits, const int* q_count, int cap, float* first_t, int grid, cudaStream_t st)
+{
+    k_first_hit<<<grid, 128, 0, st>>>(hits, q_count, cap, first_t);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rad_apply(const RadQuery* queries, const int* n_queries, int cap, const float4* amb,
+                             PathState* paths, float* quality, int grid, cudaStream_t st)
+{
+    k_rad_apply<<<grid, 256, 0, st>>>(queries, n_queries, cap, amb, paths, quality);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather_reduce(const DeviceScene& S, const RadCacheView& C, const RadParams& R,
+                                 const RadQuery* queries, const int* seeds, int ns, int base, const float* first_t,
+                                 const PathState* paths, const float* quality, const float4* partial, float4* out,
+                                 unsigned long long* rstats, uint32_t* err, int grid, cudaStream_t st)
+{
+    k_gather_reduce<<<grid, 128, 0, st>>>(S, C, R, queries, seeds, ns, base, first_t, paths, quality, partial, out,
+                                          rstats, err);
+    return cudaGetLastError();
+}
+
+}  // namespace povgpu

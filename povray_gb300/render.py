@@ -71,11 +71,34 @@ class GpuScene:
         _check(st, "pov_gpu_trace_blocks")
         return host, stats.as_dict()
 
+    def radiosity_pretrace(self, blocks, params=None):
+        """RadiosityTask: empties the sample cache and runs every pretrace
+        pass over `blocks`.  Returns the pass's stats dict."""
+        p = params or self.scene.render_params()
+        arr = _scenes.block_array(blocks)
+        stats = abi.PovGpuStats()
+        _check(self.lib.pov_gpu_radiosity_pretrace(self.h, arr, len(blocks), C.byref(p), C.byref(stats)),
+               "pov_gpu_radiosity_pretrace")
+        return stats.as_dict()
+
+    def set_pretrace_jitter(self, table):
+        """The reference's pretrace jitter table (RadiosityTask's
+        RandomDoubleSequence(-1, 1, 2047) values)."""
+        t = np.ascontiguousarray(table, dtype=np.float64)
+        _check(self.lib.pov_gpu_set_pretrace_jitter(self.h, t.ctypes.data, len(t)), "pov_gpu_set_pretrace_jitter")
+
     def render(self, params=None, block=32):
-        """Whole image (H, W, 4) through the block interface."""
+        """Whole image (H, W, 4) through the block interface; with radiosity
+        the pretrace runs over all blocks first and the returned stats add
+        its counters (pixels, rays, shadow rays, radiosity samples)."""
         p = params or self.scene.render_params()
         blocks = _scenes.blocks_for(p.width, p.height, block)
+        pre = None
+        if self.scene.radiosity is not None:
+            pre = self.radiosity_pretrace(blocks, p)
         rgbt, stats = self.trace_blocks(blocks, p)
+        if pre is not None:
+            stats = {k: stats[k] + pre[k] if k != "device_error" else stats[k] | pre[k] for k in stats}
         return _scenes.unblock(rgbt, blocks, p.width, p.height), stats
 
     def set_stream(self, stream_handle):
