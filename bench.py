@@ -131,7 +131,8 @@ def cpu_baseline(scene, cpu_seconds_target=20.0):
     """The oracle port (FP64 restatement of the reference), all host threads,
     on a band of rows of the same frame; Mrays/s by its own counters."""
     from oracle.pyoracle import Oracle
-    cores = os.cpu_count() or 1
+    # radiosity renders run on one thread in the reference's sample order
+    cores = 1 if scene.radiosity is not None else (os.cpu_count() or 1)
     t0 = time.time()
     orc = Oracle(scene)
     build_s = time.time() - t0
@@ -174,7 +175,7 @@ def run_reference(args, rank, world):
         tt += dt
         rr += r
     v = rr / tt / 1e6
-    cores = os.cpu_count() or 1
+    cores = 1 if s.radiosity is not None else (os.cpu_count() or 1)
     sample = "oracle restatement of the reference (FP64 C, pthreads), %d-row band of the %dx%d frame per step" % (
         band, args.width, args.height)
     print(json.dumps({
@@ -212,12 +213,6 @@ def main():
     dev_out = torch.empty((npix, 4), dtype=torch.float32, device="cuda")
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
-    # one profiling frame (outside the timed region): traversal work counts
-    gpu.set_profiling(times=False, work=True)
-    _, wt = frame_device()
-    work = {k: [sum(t[k][j] for t in wt) for j in range(2)] for k in ("node_visits", "prim_tests", "tri_tests",
-                                                                          "rays_traced")}
-    gpu.set_profiling(times=True, work=False)
 
     radiosity = s.radiosity is not None
 
@@ -233,6 +228,13 @@ def main():
         if st_all is not None:
             st = {k: st[k] + st_all[k] for k in st if k != "device_error"}
         return st, tims
+
+    # one profiling frame (outside the timed region): traversal work counts
+    gpu.set_profiling(times=False, work=True)
+    _, wt = frame_device()
+    work = {k: [sum(t[k][j] for t in wt) for j in range(2)] for k in ("node_visits", "prim_tests", "tri_tests",
+                                                                          "rays_traced")}
+    gpu.set_profiling(times=True, work=False)
 
     for _ in range(args.warmup):
         frame_device()
