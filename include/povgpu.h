@@ -246,7 +246,9 @@ typedef struct PovGpuStats {
     uint64_t radiosity_rays;        /* Radiosity sample rays shot           */
     uint64_t radiosity_gathers_d0;  /* samples calculated at bounce depth 0 */
     uint64_t radiosity_gathers_d1;  /* samples calculated at bounce depth 1 */
-    uint64_t reserved[4];
+    uint64_t nic_answers;           /* radiosity queries the neural cache answered */
+    uint64_t nic_val_error_ppm;     /* its held-out relative RMSE, parts per million */
+    uint64_t reserved[2];
 } PovGpuStats;
 
 /* One closest-hit result of pov_gpu_trace_rays. */
@@ -331,6 +333,38 @@ int pov_gpu_radiosity_pretrace(PovGpuScene* scene, const PovGpuBlock* blocks, in
  * Copied.  Without a table the pretrace jitters by its own hash.
  */
 int pov_gpu_set_pretrace_jitter(PovGpuScene* scene, const double* table, int32_t n);
+
+/*
+ * Neural irradiance cache (no reference counterpart).  When enabled, the
+ * radiosity pretrace ends by training a 4x64 MLP (hand-written tcgen05
+ * kernels) on the depth-0 samples it gathered, `steps` Adam steps of `batch`
+ * samples; every eighth sample is held out.  If the held-out relative RMSE
+ * is at most `gate`, final-trace queries that no cached sample covers take
+ * the network's answer instead of gathering a new sample.
+ */
+typedef struct PovGpuNeuralCache {
+    int32_t enabled;
+    int32_t steps;            /* Adam steps per pretrace                      */
+    int32_t batch;            /* samples per step (multiple of 128 is best)   */
+    float   learning_rate;
+    float   gate;             /* largest held-out relative RMSE it may answer */
+    uint32_t seed;            /* batch sampling                               */
+} PovGpuNeuralCache;
+int pov_gpu_set_neural_cache(PovGpuScene* scene, const PovGpuNeuralCache* config);
+
+/*
+ * The neural cache's kernels on caller data, for checking them: params holds
+ * the FP32 parameter vector (POV_GPU_NIC_PARAMS floats: W1[64x112], b1[64],
+ * W2[64x64], b2, W3, b3, W4, b4, W5[16x64], b5[16]; weights row-major
+ * [out][in]), bounds the box (lo xyz, hi xyz) points are scaled into.
+ * out (n x 3, may be NULL) receives the predictions; with targets (n x 3),
+ * grad (POV_GPU_NIC_PARAMS floats) and *loss receive the gradient and value
+ * of (1/n) sum (p - y)^2 / (p^2 + 0.01).  Host pointers; runs on the current
+ * device.
+ */
+#define POV_GPU_NIC_PARAMS 20752
+int pov_gpu_nic_eval(const float* params, const float* bounds, const float* points, const float* normals,
+                     const float* targets, int32_t n, float* out, float* grad, float* loss);
 
 /* Releases all device memory of the scene. */
 void pov_gpu_scene_destroy(PovGpuScene* scene);

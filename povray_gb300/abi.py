@@ -128,10 +128,18 @@ class PovGpuStats(C.Structure):
                 ("radiosity_gathers", C.c_uint64), ("radiosity_reuse", C.c_uint64),
                 ("device_error", C.c_uint64), ("radiosity_rays", C.c_uint64),
                 ("radiosity_gathers_d0", C.c_uint64), ("radiosity_gathers_d1", C.c_uint64),
-                ("reserved", C.c_uint64 * 4)]
+                ("nic_answers", C.c_uint64), ("nic_val_error_ppm", C.c_uint64), ("reserved", C.c_uint64 * 2)]
 
     def as_dict(self):
         return {k: int(getattr(self, k)) for k, _ in self._fields_ if k != "reserved"}
+
+
+class PovGpuNeuralCache(C.Structure):
+    _fields_ = [("enabled", C.c_int32), ("steps", C.c_int32), ("batch", C.c_int32),
+                ("learning_rate", C.c_float), ("gate", C.c_float), ("seed", C.c_uint32)]
+
+
+POV_GPU_NIC_PARAMS = 20752
 
 
 class PovGpuHit(C.Structure):
@@ -157,13 +165,15 @@ STRUCTS = {
     "PovGpuRadiosity": PovGpuRadiosity, "PovGpuSceneDesc": PovGpuSceneDesc,
     "PovGpuBlock": PovGpuBlock, "PovGpuRenderParams": PovGpuRenderParams,
     "PovGpuStats": PovGpuStats, "PovGpuHit": PovGpuHit, "PovGpuTimings": PovGpuTimings,
+    "PovGpuNeuralCache": PovGpuNeuralCache,
 }
 
 # Entry points that include/povgpu.h declares (checked by the CPU tests).
 EXPORTS = ["pov_gpu_scene_create", "pov_gpu_trace_blocks", "pov_gpu_trace_rays",
            "pov_gpu_scene_destroy", "pov_gpu_error_string", "pov_gpu_abi_version",
            "pov_gpu_scene_set_stream", "pov_gpu_set_profiling", "pov_gpu_get_timings",
-           "pov_gpu_trace_rays_static", "pov_gpu_radiosity_pretrace", "pov_gpu_set_pretrace_jitter"]
+           "pov_gpu_trace_rays_static", "pov_gpu_radiosity_pretrace", "pov_gpu_set_pretrace_jitter",
+           "pov_gpu_set_neural_cache", "pov_gpu_nic_eval"]
 
 
 class PovGpuError(RuntimeError):
@@ -203,6 +213,10 @@ def load_library(path=None):
     lib.pov_gpu_radiosity_pretrace.restype = C.c_int
     lib.pov_gpu_set_pretrace_jitter.argtypes = [C.c_void_p, C.c_void_p, C.c_int32]
     lib.pov_gpu_set_pretrace_jitter.restype = C.c_int
+    lib.pov_gpu_set_neural_cache.argtypes = [C.c_void_p, C.POINTER(PovGpuNeuralCache)]
+    lib.pov_gpu_set_neural_cache.restype = C.c_int
+    lib.pov_gpu_nic_eval.argtypes = [C.c_void_p] * 5 + [C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.pov_gpu_nic_eval.restype = C.c_int
     lib.pov_gpu_scene_destroy.argtypes = [C.c_void_p]
     lib.pov_gpu_scene_destroy.restype = None
     lib.pov_gpu_error_string.argtypes = [C.c_int]

@@ -9,6 +9,7 @@
 #include "povgpu_internal.h"
 #include "povgpu_kernels.h"
 #include "povgpu_radiosity.h"
+#include "povgpu_nic.h"
 
 #include <cuda_runtime.h>
 
@@ -17,6 +18,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <random>
 #include <mutex>
 #include <new>
 #include <vector>
@@ -404,9 +406,19 @@ struct RadiosityState {
     uint64_t        rays_shot = 0;
     std::vector<double> jitter;
     RadLevel        level[RAD_LEVELS];
+    // neural irradiance cache: configuration, parameters (FP32 master, BF16
+    // copy, Adam moments, gradient), training batches, and whether the last
+    // training passed its held-out gate
+    PovGpuNeuralCache nic_cfg{};
+    bool            nic_ok = false;
+    bool            nic_init = false;
+    double          nic_val_error = 0.0;
+    float3          nic_lo{}, nic_scale{};
+    DevBuf          nic_params, nic_wb, nic_m, nic_v, nic_grad, nic_loss, nic_idx, nic_pred, nic_err;
     void release()
     {
-        DevBuf* all[] = {&blocks, &next, &count, &keys, &heads, &range, &rstats};
+        DevBuf* all[] = {&blocks, &next, &count, &keys, &heads, &range, &rstats, &nic_params, &nic_wb, &nic_m,
+                         &nic_v, &nic_grad, &nic_loss, &nic_idx, &nic_pred, &nic_err};
         for (DevBuf* b : all)
             b->release();
         for (auto& l : level)
@@ -1320,12 +1332,16 @@ int rad_resolve(PovGpuScene* sc, StageClock& clk, int d, const RadQuery* queries
     int n_open = n;
     const int grid = std::max(1, std::min(sc->num_sms * 16, (n + 127) / 128));
     const int per_chunk = std::max(1, (int)(GATHER_CHUNK_RAYS / (size_t)P.rays_per_sample));
-    for (int round = 0; round < RAD_ROUNDS && n_open > 0; round++) {
+    // final trace with a trained neural cache: one round; what no cached
+    // sample covers is answered by the network instead of a new gather
+    const bool use_nic = R.nic_ok && d == 0 && R.final_trace;
+    const int last_round = use_nic ? 0 : RAD_ROUNDS - 1;
+    for (int round = 0; round <= last_round && n_open > 0; round++) {
         int* nxt = lists[round & 1];
         CK(cudaMemsetAsync(cn, 0, sizeof(int) * 2, st));
         CK(cudaMemsetAsync(L.claims.p, 0, L.claims.bytes, st));
         CK(clk.begin(POV_GPU_STAGE_RADIOSITY));
-        CK(launch_rad_query(sc->S, C, P, queries, open, n_open, n, round, RAD_ROUNDS - 1, out,
+        CK(launch_rad_query(sc->S, C, P, queries, open, n_open, n, round, last_round, out,
                             L.partial.as<float4>(), L.claims.as<unsigned long long>(), L.claim_mask(),
                             L.seeds.as<int>(), cn, nxt, cn + 1, R.rstats.as<unsigned long long>(),
                             sc->err.as<uint32_t>(), grid, st));
@@ -1334,6 +1350,27 @@ int rad_resolve(PovGpuScene* sc, StageClock& clk, int d, const RadQuery* queries
         CK(cudaMemcpyAsync(hc, cn, sizeof(hc), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
         const int ns = std::min(hc[0], n), nn = std::min(hc[1], n);
+        if (use_nic) {
+            if (ns > 0) {
+                CK(R.nic_pred.ensure(sizeof(float4) * (size_t)ns));
+                nic::NicIO io{};
+                io.pos = reinterpret_cast<const float4*>(queries);
+                io.nrm = reinterpret_cast<const float4*>(queries) + 1;
+                io.stride = (int)(sizeof(RadQuery) / sizeof(float4));
+                io.idx = L.seeds.as<int>();
+                io.n = ns;
+                io.out = R.nic_pred.as<float4>();
+                io.lo = R.nic_lo;
+                io.scale = R.nic_scale;
+                CK(clk.begin(POV_GPU_STAGE_RADIOSITY));
+                CK(nic::launch_forward(io, R.nic_wb.as<__nv_bfloat16>(), R.nic_params.as<float>(),
+                                       sc->err.as<uint32_t>(), sc->num_sms * 2, st));
+                CK(launch_rad_nic_answer(P, L.seeds.as<int>(), ns, R.nic_pred.as<float4>(), out,
+                                         R.rstats.as<unsigned long long>(), grid, st));
+                CK(clk.end(2));
+            }
+            break;
+        }
         for (int c0 = 0; c0 < ns; c0 += per_chunk) {
             int rc = rad_gather(sc, clk, d, queries, L.seeds.as<int>() + c0, std::min(per_chunk, ns - c0),
                                 L.partial.as<float4>(), out);
@@ -1386,7 +1423,136 @@ int rad_collect(PovGpuScene* sc, PovGpuStats* stats)
     stats->radiosity_gathers_d1 = h[RST_GATHERS1];
     stats->radiosity_gathers = h[RST_GATHERS0] + h[RST_GATHERS1];
     stats->radiosity_rays = sc->rad.rays_shot;
+    stats->nic_answers = h[RST_NIC];
+    stats->nic_val_error_ppm = sc->rad.nic_cfg.enabled ? (uint64_t)(sc->rad.nic_val_error * 1e6) : 0;
     return POV_GPU_OK;
+}
+
+// Trains the neural cache on the depth-0 samples of the cache (every eighth
+// held out) and decides the gate.  Runs at the end of the pretrace.
+int nic_train(PovGpuScene* sc)
+{
+    RadiosityState& R = sc->rad;
+    const PovGpuNeuralCache& cfg = R.nic_cfg;
+    R.nic_ok = false;
+    R.nic_val_error = 0.0;
+    cudaStream_t st = sc->active();
+    int nb = 0;
+    CK(cudaMemcpyAsync(&nb, R.count.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    nb = std::min(nb, R.cap_blocks);
+    if (nb <= 0)
+        return POV_GPU_OK;
+    std::vector<RadBlock> hb((size_t)nb);
+    CK(cudaMemcpy(hb.data(), R.blocks.p, sizeof(RadBlock) * (size_t)nb, cudaMemcpyDeviceToHost));
+    std::vector<int> train, val;
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int i = 0; i < nb; i++) {
+        const RadBlock& b = hb[i];
+        int depth;
+        std::memcpy(&depth, &b.ill.w, sizeof(int));
+        if (depth != 0)
+            continue;
+        (((train.size() + val.size()) % 8) == 7 ? val : train).push_back(i);
+        const float p[3] = {b.p.x, b.p.y, b.p.z};
+        for (int k = 0; k < 3; k++) {
+            lo[k] = std::min(lo[k], p[k]);
+            hi[k] = std::max(hi[k], p[k]);
+        }
+    }
+    if (train.size() < 256 || val.empty())
+        return POV_GPU_OK;
+    float sc3[3];
+    for (int k = 0; k < 3; k++) {
+        float ext = std::max(hi[k] - lo[k], 1e-6f);
+        lo[k] -= 0.01f * ext;
+        sc3[k] = 2.0f / (1.02f * ext);
+    }
+    R.nic_lo = make_float3(lo[0], lo[1], lo[2]);
+    R.nic_scale = make_float3(sc3[0], sc3[1], sc3[2]);
+    // parameters: He-uniform initialisation, zero biases, padded rows zero
+    const size_t NP = (size_t)nic::NPARAM;
+    CK(R.nic_params.ensure(sizeof(float) * NP));
+    CK(R.nic_wb.ensure(sizeof(__nv_bfloat16) * NP));
+    CK(R.nic_m.ensure(sizeof(float) * NP));
+    CK(R.nic_v.ensure(sizeof(float) * NP));
+    CK(R.nic_grad.ensure(sizeof(float) * NP));
+    CK(R.nic_loss.ensure(sizeof(float)));
+    CK(R.nic_err.ensure(sizeof(uint32_t)));
+    std::mt19937 rng(cfg.seed);
+    std::vector<float> hp(NP, 0.0f);
+    auto init = [&](int off, int rows, int cols, int live_rows) {
+        std::uniform_real_distribution<float> u(-std::sqrt(6.0f / cols), std::sqrt(6.0f / cols));
+        for (int r = 0; r < live_rows; r++)
+            for (int c = 0; c < cols; c++)
+                hp[(size_t)off + (size_t)r * cols + c] = (cols == nic::K1 && c >= nic::FEAT) ? 0.0f : u(rng);
+        (void)rows;
+    };
+    init(nic::P_W1, nic::HID, nic::K1, nic::HID);
+    init(nic::P_W2, nic::HID, nic::HID, nic::HID);
+    init(nic::P_W3, nic::HID, nic::HID, nic::HID);
+    init(nic::P_W4, nic::HID, nic::HID, nic::HID);
+    init(nic::P_W5, nic::NO, nic::HID, nic::NOUT);
+    CK(cudaMemcpyAsync(R.nic_params.p, hp.data(), sizeof(float) * NP, cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(R.nic_m.p, 0, sizeof(float) * NP, st));
+    CK(cudaMemsetAsync(R.nic_v.p, 0, sizeof(float) * NP, st));
+    CK(cudaMemsetAsync(R.nic_err.p, 0, sizeof(uint32_t), st));
+    CK(nic::launch_to_bf16(R.nic_params.as<float>(), R.nic_wb.as<__nv_bfloat16>(), st));
+    // every step's batch, drawn up front
+    const int steps = std::max(cfg.steps, 1), batch = std::max(cfg.batch, nic::TILE);
+    std::vector<int> idx((size_t)steps * batch + val.size());
+    std::uniform_int_distribution<int> pick(0, (int)train.size() - 1);
+    for (size_t i = 0; i < (size_t)steps * batch; i++)
+        idx[i] = train[(size_t)pick(rng)];
+    std::copy(val.begin(), val.end(), idx.begin() + (size_t)steps * batch);
+    CK(R.nic_idx.ensure(sizeof(int) * idx.size()));
+    CK(cudaMemcpyAsync(R.nic_idx.p, idx.data(), sizeof(int) * idx.size(), cudaMemcpyHostToDevice, st));
+    nic::NicIO io{};
+    io.pos = reinterpret_cast<const float4*>(R.blocks.p);
+    io.nrm = io.pos + 1;
+    io.target = io.pos + 3;
+    io.stride = (int)(sizeof(RadBlock) / sizeof(float4));
+    io.lo = R.nic_lo;
+    io.scale = R.nic_scale;
+    StageClock clk(sc, st);
+    CK(clk.begin(POV_GPU_STAGE_RADIOSITY));
+    for (int s = 0; s < steps; s++) {
+        io.idx = R.nic_idx.as<int>() + (size_t)s * batch;
+        io.n = batch;
+        CK(cudaMemsetAsync(R.nic_grad.p, 0, sizeof(float) * NP, st));
+        CK(nic::launch_train(io, R.nic_wb.as<__nv_bfloat16>(), R.nic_params.as<float>(), R.nic_grad.as<float>(),
+                             R.nic_loss.as<float>(), 1.0f / (float)batch, R.nic_err.as<uint32_t>(), sc->num_sms,
+                             st));
+        CK(nic::launch_adam(R.nic_params.as<float>(), R.nic_m.as<float>(), R.nic_v.as<float>(),
+                            R.nic_grad.as<float>(), R.nic_wb.as<__nv_bfloat16>(), cfg.learning_rate, s + 1, st));
+    }
+    CK(clk.end(3 * steps));
+    // held-out relative RMSE
+    const int nv = (int)val.size();
+    CK(R.nic_pred.ensure(sizeof(float4) * (size_t)nv));
+    io.idx = R.nic_idx.as<int>() + (size_t)steps * batch;
+    io.n = nv;
+    io.out = R.nic_pred.as<float4>();
+    CK(nic::launch_forward(io, R.nic_wb.as<__nv_bfloat16>(), R.nic_params.as<float>(), R.nic_err.as<uint32_t>(),
+                           sc->num_sms * 2, st));
+    std::vector<float4> pred((size_t)nv);
+    uint32_t nerr = 0;
+    CK(cudaMemcpyAsync(pred.data(), R.nic_pred.p, sizeof(float4) * (size_t)nv, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&nerr, R.nic_err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    double se = 0.0, sy = 0.0;
+    for (int i = 0; i < nv; i++) {
+        const RadBlock& b = hb[(size_t)val[i]];
+        const float y[3] = {b.ill.x, b.ill.y, b.ill.z}, p[3] = {pred[i].x, pred[i].y, pred[i].z};
+        for (int k = 0; k < 3; k++) {
+            se += (double)(p[k] - y[k]) * (p[k] - y[k]);
+            sy += (double)y[k];
+        }
+    }
+    double mean = sy / (3.0 * nv);
+    R.nic_val_error = mean > 0 ? std::sqrt(se / (3.0 * nv)) / mean : 1.0;
+    R.nic_ok = nerr == 0 && R.nic_val_error <= cfg.gate;
+    return nerr ? POV_GPU_E_DEVICE : POV_GPU_OK;
 }
 
 int rad_begin_call(PovGpuScene* sc, bool final_trace)
@@ -1760,6 +1926,18 @@ int pov_gpu_radiosity_pretrace(PovGpuScene* sc, const PovGpuBlock* blocks, int32
         if (rc != POV_GPU_OK)
             return rc;
     }
+    clk.collect();
+    PovGpuTimings keep = sc->timings;
+    R.nic_ok = false;
+    if (R.nic_cfg.enabled) {
+        if (int rr = nic_train(sc))
+            return rr;
+        for (int k = 0; k < POV_GPU_STAGES; k++) {   // this call's stages plus the training's
+            keep.stage_ms[k] += sc->timings.stage_ms[k];
+            keep.stage_launches[k] += sc->timings.stage_launches[k];
+        }
+        keep.kernel_launches += sc->timings.kernel_launches;
+    }
     unsigned long long hs[ST_COUNT];
     int rc = check_device_error(sc, stats, hs);
     if (stats) {
@@ -1767,8 +1945,95 @@ int pov_gpu_radiosity_pretrace(PovGpuScene* sc, const PovGpuBlock* blocks, int32
         if (int rr = rad_collect(sc, stats))
             return rr;
     }
-    clk.collect();
+    sc->timings = keep;
     return rc;
+}
+
+static_assert(POV_GPU_NIC_PARAMS == nic::NPARAM, "public and internal parameter counts differ");
+
+int pov_gpu_set_neural_cache(PovGpuScene* sc, const PovGpuNeuralCache* cfg)
+{
+    if (!sc || !cfg || (cfg->enabled && (cfg->steps < 1 || cfg->batch < 1 || cfg->learning_rate <= 0.0f)))
+        return POV_GPU_E_INVALID;
+    std::lock_guard<std::mutex> g(sc->lock);
+    if (!sc->rad.enabled)
+        return POV_GPU_E_INVALID;
+    sc->rad.nic_cfg = *cfg;
+    sc->rad.nic_ok = false;
+    return POV_GPU_OK;
+}
+
+int pov_gpu_nic_eval(const float* params, const float* bounds, const float* points, const float* normals,
+                     const float* targets, int32_t n, float* out, float* grad, float* loss)
+{
+    if (!params || !bounds || n < 0 || (n > 0 && (!points || !normals)) || (targets && (!grad || !loss)))
+        return POV_GPU_E_INVALID;
+    if (n == 0)
+        return POV_GPU_OK;
+    const size_t NP = (size_t)nic::NPARAM;
+    DevBuf dp, dwb, dpos, dnrm, dtg, dout, dgrad, dloss, derr;
+    struct Free {
+        DevBuf* b[9];
+        ~Free() { for (DevBuf* x : b) x->release(); }
+    } fr{{&dp, &dwb, &dpos, &dnrm, &dtg, &dout, &dgrad, &dloss, &derr}};
+    CK(dp.ensure(sizeof(float) * NP));
+    CK(dwb.ensure(sizeof(__nv_bfloat16) * NP));
+    CK(dpos.ensure(sizeof(float4) * (size_t)n));
+    CK(dnrm.ensure(sizeof(float4) * (size_t)n));
+    CK(dout.ensure(sizeof(float4) * (size_t)n));
+    CK(derr.ensure(sizeof(uint32_t)));
+    std::vector<float4> hp((size_t)n), hn((size_t)n), ht((size_t)n);
+    for (int i = 0; i < n; i++) {
+        hp[i] = make_float4(points[3 * i], points[3 * i + 1], points[3 * i + 2], 0.f);
+        hn[i] = make_float4(normals[3 * i], normals[3 * i + 1], normals[3 * i + 2], 0.f);
+        if (targets)
+            ht[i] = make_float4(targets[3 * i], targets[3 * i + 1], targets[3 * i + 2], 0.f);
+    }
+    CK(cudaMemcpy(dp.p, params, sizeof(float) * NP, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(dpos.p, hp.data(), sizeof(float4) * (size_t)n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(dnrm.p, hn.data(), sizeof(float4) * (size_t)n, cudaMemcpyHostToDevice));
+    CK(cudaMemset(derr.p, 0, sizeof(uint32_t)));
+    CK(nic::launch_to_bf16(dp.as<float>(), dwb.as<__nv_bfloat16>(), 0));
+    nic::NicIO io{};
+    io.pos = dpos.as<float4>();
+    io.nrm = dnrm.as<float4>();
+    io.stride = 1;
+    io.n = n;
+    io.out = dout.as<float4>();
+    for (int k = 0; k < 3; k++) {
+        float ext = std::max(bounds[3 + k] - bounds[k], 1e-6f);
+        (&io.lo.x)[k] = bounds[k];
+        (&io.scale.x)[k] = 2.0f / ext;
+    }
+    int dev = 0, sms = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    if (out) {
+        CK(nic::launch_forward(io, dwb.as<__nv_bfloat16>(), dp.as<float>(), derr.as<uint32_t>(), sms * 2, 0));
+        std::vector<float4> ho((size_t)n);
+        CK(cudaMemcpy(ho.data(), dout.p, sizeof(float4) * (size_t)n, cudaMemcpyDeviceToHost));
+        for (int i = 0; i < n; i++) {
+            out[3 * i] = ho[i].x;
+            out[3 * i + 1] = ho[i].y;
+            out[3 * i + 2] = ho[i].z;
+        }
+    }
+    if (targets) {
+        CK(dtg.ensure(sizeof(float4) * (size_t)n));
+        CK(dgrad.ensure(sizeof(float) * NP));
+        CK(dloss.ensure(sizeof(float)));
+        CK(cudaMemcpy(dtg.p, ht.data(), sizeof(float4) * (size_t)n, cudaMemcpyHostToDevice));
+        CK(cudaMemset(dgrad.p, 0, sizeof(float) * NP));
+        CK(cudaMemset(dloss.p, 0, sizeof(float)));
+        io.target = dtg.as<float4>();
+        CK(nic::launch_train(io, dwb.as<__nv_bfloat16>(), dp.as<float>(), dgrad.as<float>(), dloss.as<float>(),
+                             1.0f / (float)n, derr.as<uint32_t>(), sms, 0));
+        CK(cudaMemcpy(grad, dgrad.p, sizeof(float) * NP, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(loss, dloss.p, sizeof(float), cudaMemcpyDeviceToHost));
+    }
+    uint32_t e = 0;
+    CK(cudaMemcpy(&e, derr.p, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    return e ? POV_GPU_E_DEVICE : POV_GPU_OK;
 }
 
 int pov_gpu_trace_rays(PovGpuScene* sc, const double* origins, const double* directions, int32_t num_rays,

@@ -446,6 +446,17 @@ __global__ void k_gather_reduce(DeviceScene S, RadCacheView C, RadParams R, cons
     }
 }
 
+__global__ void k_rad_nic_answer(RadParams R, const int* __restrict__ seeds, int ns, const float4* __restrict__ pred,
+                                 float4* __restrict__ out, unsigned long long* __restrict__ rstats)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ns; i += gridDim.x * blockDim.x) {
+        float4 p = pred[i];
+        out[seeds[i]] = finish_ambient(f3(fmaxf(p.x, 0.f), fmaxf(p.y, 0.f), fmaxf(p.z, 0.f)), 1.0f, R);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        atomicAdd(&rstats[RST_NIC], (unsigned long long)ns);
+}
+
 inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
 
 }  // namespace
@@ -485,6 +496,13 @@ cudaError_t launch_rad_apply(const RadQuery* queries, const int* n_queries, int 
                              PathState* paths, float* quality, int grid, cudaStream_t st)
 {
     k_rad_apply<<<grid, 256, 0, st>>>(queries, n_queries, cap, amb, paths, quality);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rad_nic_answer(const RadParams& R, const int* seeds, int ns, const float4* pred, float4* out,
+                                  unsigned long long* rstats, int grid, cudaStream_t st)
+{
+    k_rad_nic_answer<<<grid, 256, 0, st>>>(R, seeds, ns, pred, out, rstats);
     return cudaGetLastError();
 }
 

@@ -12,6 +12,7 @@ enum RadStatIdx {
     RST_REUSED = 0,     // queries answered from the cache
     RST_GATHERS0 = 1,   // samples gathered at bounce depth 0
     RST_GATHERS1 = 2,   // ... at depth 1 and deeper
+    RST_NIC = 3,        // queries the neural cache answered
     RST_COUNT = 4,
 };
 
@@ -29,6 +30,9 @@ cudaError_t launch_gather_rays(const RadQuery* queries, const int* seeds, int ns
 cudaError_t launch_first_hit(const QHit* hits, const int* q_count, int cap, float* first_t, int grid, cudaStream_t st);
 cudaError_t launch_rad_apply(const RadQuery* queries, const int* n_queries, int cap, const float4* amb,
                              PathState* paths, float* quality, int grid, cudaStream_t st);
+// Answers of the neural cache (pred[i] for query seeds[i]) into out[].
+cudaError_t launch_rad_nic_answer(const RadParams& R, const int* seeds, int ns, const float4* pred, float4* out,
+                                  unsigned long long* rstats, int grid, cudaStream_t st);
 cudaError_t launch_gather_reduce(const DeviceScene& S, const RadCacheView& C, const RadParams& R,
                                  const RadQuery* queries, const int* seeds, int ns, int base, const float* first_t,
                                  const PathState* paths, const float* quality, const float4* partial, float4* out,

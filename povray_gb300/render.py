@@ -81,6 +81,13 @@ class GpuScene:
                "pov_gpu_radiosity_pretrace")
         return stats.as_dict()
 
+    def set_neural_cache(self, enabled=True, steps=300, batch=4096, learning_rate=3e-3, gate=0.5, seed=1):
+        """Neural irradiance cache (pov_gpu_set_neural_cache): trained at the
+        end of each pretrace; answers uncovered final-trace queries when its
+        held-out relative RMSE is at most `gate`."""
+        c = abi.PovGpuNeuralCache(int(enabled), int(steps), int(batch), float(learning_rate), float(gate), int(seed))
+        _check(self.lib.pov_gpu_set_neural_cache(self.h, C.byref(c)), "pov_gpu_set_neural_cache")
+
     def set_pretrace_jitter(self, table):
         """The reference's pretrace jitter table (RadiosityTask's
         RandomDoubleSequence(-1, 1, 2047) values)."""
@@ -189,3 +196,29 @@ class GpuTraceTask:
                 self.source.completed_rectangle(rect, rgbt[off:off + n])
                 off += n
         return self.stats
+
+
+def nic_eval(params, bounds, points, normals, targets=None):
+    """pov_gpu_nic_eval: the neural cache's forward pass on (points, normals)
+    and, with targets, the gradient and loss of its training objective.
+    Returns (pred (n,3), grad or None, loss or None)."""
+    lib = abi.load_library()
+    p = np.ascontiguousarray(params, dtype=np.float32)
+    assert p.size == abi.POV_GPU_NIC_PARAMS
+    b = np.ascontiguousarray(bounds, dtype=np.float32)
+    x = np.ascontiguousarray(points, dtype=np.float32)
+    nrm = np.ascontiguousarray(normals, dtype=np.float32)
+    n = x.shape[0]
+    out = np.zeros((n, 3), dtype=np.float32)
+    grad = loss = None
+    tg = None
+    if targets is not None:
+        tg = np.ascontiguousarray(targets, dtype=np.float32)
+        grad = np.zeros(abi.POV_GPU_NIC_PARAMS, dtype=np.float32)
+        loss = np.zeros(1, dtype=np.float32)
+    st = lib.pov_gpu_nic_eval(p.ctypes.data, b.ctypes.data, x.ctypes.data, nrm.ctypes.data,
+                              tg.ctypes.data if tg is not None else None, n, out.ctypes.data,
+                              grad.ctypes.data if grad is not None else None,
+                              loss.ctypes.data if loss is not None else None)
+    _check(st, "pov_gpu_nic_eval")
+    return out, grad, (float(loss[0]) if loss is not None else None)
