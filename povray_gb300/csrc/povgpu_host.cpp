@@ -396,7 +396,7 @@ constexpr int RAD_ROUNDS = 8;                    // query rounds before every op
 struct RadiosityState {
     bool            enabled = false;
     PovGpuRadiosity set{};
-    DevBuf          blocks, next, count, keys, heads, range, rstats;
+    DevBuf          blocks, next, count, keys, heads, range, occupancy, rstats;
     int             cap_blocks = 0;
     uint32_t        key_mask = 0;
     bool            dirs_uploaded = false;
@@ -417,7 +417,7 @@ struct RadiosityState {
     DevBuf          nic_params, nic_wb, nic_m, nic_v, nic_grad, nic_loss, nic_idx, nic_pred, nic_err;
     void release()
     {
-        DevBuf* all[] = {&blocks, &next, &count, &keys, &heads, &range, &rstats, &nic_params, &nic_wb, &nic_m,
+        DevBuf* all[] = {&blocks, &next, &count, &keys, &heads, &range, &occupancy, &rstats, &nic_params, &nic_wb, &nic_m,
                          &nic_v, &nic_grad, &nic_loss, &nic_idx, &nic_pred, &nic_err};
         for (DevBuf* b : all)
             b->release();
@@ -1000,7 +1000,8 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
         CK(R.count.ensure(sizeof(int32_t)));
         CK(R.keys.ensure(sizeof(unsigned long long) * slots));
         CK(R.heads.ensure(sizeof(int32_t) * slots));
-        CK(R.range.ensure(sizeof(int32_t) * 2));
+        CK(R.range.ensure(sizeof(int32_t) * 2 * RAD_LEVELS));
+        CK(R.occupancy.ensure(1u << 21));   // 2^24 occupancy bits
         CK(R.rstats.ensure(sizeof(unsigned long long) * RST_COUNT));
         std::vector<float> dirs(3 * (size_t)RAD_DIRECTIONS);
         for (int i = 0; i < RAD_DIRECTIONS; i++) {
@@ -1156,6 +1157,8 @@ RadCacheView cache_view(PovGpuScene* sc)
     c.heads = R.heads.as<int32_t>();
     c.mask = R.key_mask;
     c.size_range = R.range.as<int32_t>();
+    c.occupancy = R.occupancy.as<uint32_t>();
+    c.occ_mask = (uint32_t)(R.occupancy.bytes * 8 - 1);
     return c;
 }
 
@@ -1168,8 +1171,13 @@ int rad_reset(PovGpuScene* sc)
     CK(cudaMemsetAsync(R.count.p, 0, sizeof(int32_t), st));
     CK(cudaMemsetAsync(R.keys.p, 0, R.keys.bytes, st));
     CK(cudaMemsetAsync(R.heads.p, 0xff, R.heads.bytes, st));
-    const int32_t range[2] = {1 << 30, -1};
+    int32_t range[2 * RAD_LEVELS];
+    for (int d = 0; d < RAD_LEVELS; d++) {
+        range[2 * d] = 1 << 30;
+        range[2 * d + 1] = -1;
+    }
     CK(cudaMemcpy(R.range.p, range, sizeof(range), cudaMemcpyHostToDevice));
+    CK(cudaMemsetAsync(R.occupancy.p, 0, R.occupancy.bytes, st));
     for (int& b : R.dir_base)
         b = 0;
     return POV_GPU_OK;

@@ -207,7 +207,9 @@ struct RadCacheView {
     unsigned long long* keys;       // 0 = empty slot
     int32_t*            heads;
     uint32_t            mask;       // slots - 1
-    int32_t*            size_range; // smallest, largest node size (biased log2) in use
+    int32_t*            size_range; // per bounce depth d: [2d] smallest, [2d+1] largest node size in use
+    uint32_t*           occupancy;  // one bit per hashed node key: set once the node holds a block
+    uint32_t            occ_mask;   // bits - 1
 };
 
 // Settings of one bounce depth for the query and gather kernels

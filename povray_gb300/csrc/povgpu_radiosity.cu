@@ -189,29 +189,47 @@ __device__ __forceinline__ void average_near(const RadBlock& b, float3 P, float3
 }
 
 // RadiosityCache::FindReusableBlock (radiosity.cpp:1458-1512).
+__device__ __forceinline__ uint32_t occ_bit(const RadCacheView& C, unsigned long long key)
+{
+    return (uint32_t)(key >> 29) & C.occ_mask;
+}
+
+// RadiosityCache::FindReusableBlock (radiosity.cpp:1458-1512).  Nodes are
+// keyed per bounce depth (ot_dist_traverse passes only blocks of the query's
+// depth to AverageNearBlock, octree.cpp:843), so lists hold one depth; the
+// occupancy bits skip the probe of nodes that hold nothing.
 __device__ void find_reusable(const RadCacheView& C, int smin, int smax, float3 P, float3 N, float eb, int depth,
                               bool final_trace, float& W, float3& WI)
 {
     W = 0.0f;
     WI = f3(0.f, 0.f, 0.f);
-    const double px = P.x, py = P.y, pz = P.z;
+    const double c[3] = {(double)P.x + OT_BIAS, (double)P.y + OT_BIAS, (double)P.z + OT_BIAS};
     for (int size = smin; size <= smax; size++) {
-        double s = biased_pow2(size);
-        int bx = (int)floor((px + OT_BIAS) / s - 1.5);
-        int by = (int)floor((py + OT_BIAS) / s - 1.5);
-        int bz = (int)floor((pz + OT_BIAS) / s - 1.5);
-        // a node's extended box holds the point only for cells bx+1, bx+2
-        // per axis
-        for (int c = 0; c < 8; c++) {
-            int x = bx + 1 + (c & 1), y = by + 1 + ((c >> 1) & 1), z = bz + 1 + (c >> 2);
-            if (!in_node(px, py, pz, size, x, y, z))
+        const double s = biased_pow2(size), inv = 1.0 / s;   // powers of two: exact
+        // ot_point_in_node per axis: of the cells b+1, b+2 (b = floor(c/s - 1.5))
+        // those whose half-size-extended interval holds the coordinate
+        int base[3];
+        uint32_t ok[3];
+        for (int a = 0; a < 3; a++) {
+            int b = (int)floor(c[a] * inv - 1.5);
+            base[a] = b + 1;
+            ok[a] = (fabs(c[a] - ((double)b + 1.5) * s) < s ? 1u : 0u) |
+                    (fabs(c[a] - ((double)b + 2.5) * s) < s ? 2u : 0u);
+        }
+        for (int k = 0; k < 8; k++) {
+            const int dx = k & 1, dy = (k >> 1) & 1, dz = k >> 2;
+            if (!((ok[0] >> dx) & (ok[1] >> dy) & (ok[2] >> dz) & 1u))
                 continue;
-            int b = node_lookup(C, node_key(size, x, y, z));
-            for (int n = 0; b >= 0 && n < (1 << 20); n++) {
-                RadBlock blk = C.blocks[b];
+            unsigned long long key = node_key(size + 256 * depth, base[0] + dx, base[1] + dy, base[2] + dz);
+            uint32_t bit = occ_bit(C, key);
+            if (!((C.occupancy[bit >> 5] >> (bit & 31)) & 1u))
+                continue;
+            int bi = node_lookup(C, key);
+            for (int n = 0; bi >= 0 && n < (1 << 20); n++) {
+                RadBlock blk = C.blocks[bi];
                 if (__float_as_int(blk.ill.w) == depth)
                     average_near(blk, P, N, eb, final_trace, W, WI);
-                b = C.next[b];
+                bi = C.next[bi];
             }
         }
     }
@@ -238,7 +256,7 @@ __global__ void k_rad_query(DeviceScene S, RadCacheView C, RadParams R, const Ra
                             unsigned long long* __restrict__ rstats, uint32_t* err)
 {
     const int n = min(n_open, cap);
-    const int smin = C.size_range[0], smax = C.size_range[1];
+    const int smin = C.size_range[2 * R.depth], smax = C.size_range[2 * R.depth + 1];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         int qi = open ? open[i] : i;
         RadQuery q = queries[qi];
@@ -423,12 +441,15 @@ __global__ void k_gather_reduce(DeviceScene S, RadCacheView C, RadParams R, cons
                 C.blocks[b] = blk;
                 int size, x, y, z;
                 ot_index_sphere(P, (double)mean * R.address_factor, size, x, y, z);
-                int slot = node_insert(C, node_key(size, x, y, z));
+                unsigned long long key = node_key(size + 256 * R.depth, x, y, z);
+                int slot = node_insert(C, key);
                 if (slot >= 0) {
                     __threadfence();
                     C.next[b] = atomicExch(&C.heads[slot], b);
-                    atomicMin(&C.size_range[0], size);
-                    atomicMax(&C.size_range[1], size);
+                    uint32_t bit = occ_bit(C, key);
+                    atomicOr(&C.occupancy[bit >> 5], 1u << (bit & 31));
+                    atomicMin(&C.size_range[2 * R.depth], size);
+                    atomicMax(&C.size_range[2 * R.depth + 1], size);
                 } else {
                     atomicOr(err, DE_CACHE_FULL);
                 }
