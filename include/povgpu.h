@@ -65,6 +65,7 @@ extern "C" {
 #define POV_FLAG_DOUBLE_ILLUM   0x0010  /* DOUBLE_ILLUMINATE_FLAG             */
 #define POV_FLAG_NO_REFLECTION  0x0020  /* NO_REFLECTION_FLAG                 */
 #define POV_FLAG_NO_IMAGE       0x0040  /* NO_IMAGE_FLAG                      */
+#define POV_FLAG_HOLLOW         0x0080  /* HOLLOW_FLAG (Interior::hollow)     */
 
 /*
  * One object of SceneData::objects, flattened in depth-first order: a CSG
@@ -80,6 +81,8 @@ extern "C" {
  *   TORUS   p[0] major radius, p[1] minor radius (always with a transform)
  *   MESH    mesh = index into PovGpuSceneDesc.meshes
  *   CSG     first_child/num_children index this array
+ * media is the object's interior media: 1 + index into
+ * PovGpuSceneDesc.medias, 0 = none.
  * trans[] is the object's TRANSFORM as two row-major 4x4 matrices:
  * trans[0..15] = forward matrix (object -> world), trans[16..31] = inverse.
  */
@@ -91,7 +94,7 @@ typedef struct PovGpuObject {
     int32_t first_child;
     int32_t num_children;
     int32_t mesh;
-    int32_t reserved;
+    int32_t media;         /* 1 + index into medias, 0 = no interior media */
     double  p[8];
     double  trans[32];
 } PovGpuObject;
@@ -191,6 +194,28 @@ typedef struct PovGpuRadiosity {
     int32_t reserved;
 } PovGpuRadiosity;
 
+/*
+ * Interior media of an object (source/core/material/media.h), as the parser
+ * leaves it after Media::PostProcess: coefficients per channel (extinction
+ * = absorption + sc_ext * scattering), the sampling settings, constant
+ * density.  scattering_type: 1 isotropic (the reference's types 1..5).
+ */
+typedef struct PovGpuMedia {
+    int32_t scattering_type;
+    int32_t method;           /* Sample_Method: 1, 2 or 3                   */
+    int32_t intervals;
+    int32_t min_samples, max_samples;
+    int32_t aa_level;
+    float   aa_threshold;
+    float   jitter;
+    float   absorption[3];
+    float   emission[3];
+    float   scattering[3];
+    float   extinction[3];
+    float   eccentricity;
+    int32_t reserved;
+} PovGpuMedia;
+
 typedef struct PovGpuSceneDesc {
     uint32_t              abi_version;   /* POV_GPU_ABI_VERSION */
     int32_t               num_objects;
@@ -208,6 +233,8 @@ typedef struct PovGpuSceneDesc {
     float                 adc_bailout;
     int32_t               language_version; /* e.g. 370                  */
     PovGpuRadiosity       radiosity;
+    int32_t               num_medias;
+    const struct PovGpuMedia* medias;
 } PovGpuSceneDesc;
 
 /* A render block, as POVRect (inclusive bounds) plus its serial number. */
@@ -248,7 +275,8 @@ typedef struct PovGpuStats {
     uint64_t radiosity_gathers_d1;  /* samples calculated at bounce depth 1 */
     uint64_t nic_answers;           /* radiosity queries the neural cache answered */
     uint64_t nic_val_error_ppm;     /* its held-out relative RMSE, parts per million */
-    uint64_t reserved[2];
+    uint64_t transmitted_rays;      /* Transmitted_Rays_Traced              */
+    uint64_t media_samples;         /* Media_Samples                        */
 } PovGpuStats;
 
 /* One closest-hit result of pov_gpu_trace_rays. */

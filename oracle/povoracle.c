@@ -1079,7 +1079,7 @@ typedef struct {
     uint64_t boxes, prims;
     int     counting;
     /* statistics of the render */
-    uint64_t rays, shadow_tests, shadow_succeeded, reflected;
+    uint64_t rays, shadow_tests, shadow_succeeded, reflected, transmitted, media_samples;
     /* radiosity task state (RadiosityFunction, radiosity.cpp:297-330):
      * final trace or pretrace, its error bound and pass, the position of
      * each bounce depth's direction sequence, the top-level query count */
@@ -1471,19 +1471,60 @@ static const PovGpuMaterial* object_material(const PovOracle* S, int32_t oi)
 
 static inline float clampf(float v, float lo, float hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
-/* Trace::TraceShadowRay / TracePointLightShadowRay for opaque scenes
- * (trace.cpp:1892-2076): 1 = light blocked. */
+/* Media container: a hollow object whose interior holds media; its surface
+ * transmits fully (validated at create).  Returns the media index, -1 for
+ * any other object. */
+static int container_media(const PovOracle* S, int32_t oi)
+{
+    const PovGpuObject* o = &S->objs[oi].o;
+    return (o->media > 0 && (o->flags & POV_FLAG_HOLLOW)) ? o->media - 1 : -1;
+}
+
+/* Ray flags: the medium a ray travels in (the object id of its media
+ * container, the reference's interior list, which containers that do not
+ * overlap keep at one entry) rides in bits 8 and up. */
+#define RAY_MEDIUM(f)      (((f) >> 8) - 1)
+#define WITH_MEDIUM(f, m)  (((f) & 0xff) | (((m) + 1) << 8))
+
+/* Trace::TraceShadowRay / TracePointLightShadowRay (trace.cpp:1892-2076)
+ * for opaque objects and media containers: 1 = light blocked.  A container
+ * wall is a transparent hit (a test and a success of its own, trace.cpp:
+ * 2032-2072): ComputeShadowColour passes the light through it, attenuated by
+ * the media of the segment the ray has crossed inside (trace.cpp:2429-2433;
+ * for a shadow ray the constant media is one interval, od = extinction *
+ * depth), and ComputeShadowMedia toggles the ray's interior
+ * (trace.cpp:3064-3066); the ray then continues from the wall. */
+static int shadow_trace(const PovOracle* S, Thread* th, V3 P, V3 L, double dist, int medium, int media_on,
+                        double lc[3])
+{
+    V3 O = P;
+    double depth = dist;
+    for (;;) {
+        Isect is;
+        th->shadow_tests++;   /* Shadow_Ray_Tests (trace.cpp:2032) */
+        if (!find_intersection(S, th, O, L, depth, 1, &is) || !(is.depth < depth - SHADOW_TOLERANCE) ||
+            !(is.depth > SHADOW_TOLERANCE))
+            return 0;
+        th->shadow_succeeded++;
+        int mi = container_media(S, is.object);
+        if (mi < 0)
+            return 1;
+        if (medium >= 0 && media_on) {
+            th->media_samples++;   /* the shadow ray's one media sample (media.cpp:384-398) */
+            const PovGpuMedia* md = &S->desc.medias[container_media(S, medium)];
+            for (int k = 0; k < 3; k++)
+                lc[k] *= exp(-md->extinction[k] * is.depth);
+        }
+        medium = (medium == is.object) ? -1 : is.object;
+        depth -= is.depth;
+        O = is.ipoint;
+    }
+}
+
 static int shadow_blocked(const PovOracle* S, Thread* th, V3 P, V3 L, double dist)
 {
-    Isect is;
-    th->shadow_tests++;   /* Shadow_Ray_Tests (trace.cpp:2032) */
-    if (find_intersection(S, th, P, L, dist, 1, &is)) {
-        if (is.depth < dist - SHADOW_TOLERANCE && is.depth > SHADOW_TOLERANCE) {
-            th->shadow_succeeded++;
-            return 1;
-        }
-    }
-    return 0;
+    double lc[3] = {1.0, 1.0, 1.0};
+    return shadow_trace(S, th, P, L, dist, -1, 0, lc);
 }
 
 /* Grid point (u, v) of an area light as an offset from its centre
@@ -1582,6 +1623,7 @@ typedef struct {
  * (view.cpp:759) clears their pretrace flag (radiositytask.cpp:76), so
  * they shade fully. */
 #define RAY_RADIOSITY 2
+#define RAY_CONTINUED 4   /* transmitted ray: TraceRay(continuedRay = true) */
 
 static double trace_ray(const PovOracle* S, Thread* th, V3 O, V3 D, double weight, Ticket* tk, int flags, RGB* col);
 static void compute_ambient(const PovOracle* S, Thread* th, V3 ip, V3 raw, V3 layer, double brilliance, float amb[3],
@@ -1589,7 +1631,7 @@ static void compute_ambient(const PovOracle* S, Thread* th, V3 ip, V3 raw, V3 la
 
 /* ComputeReflection (trace.cpp:1264-1321). */
 static void compute_reflection(const PovOracle* S, Thread* th, V3 ip, V3 D, V3 N, V3 raw, double weight,
-                               Ticket* tk, RGB* col)
+                               Ticket* tk, int flags, RGB* col)
 {
     double n = -2.0 * vdot(D, N);
     V3 nd = vadd(D, vmul(N, n));
@@ -1606,7 +1648,7 @@ static void compute_reflection(const PovOracle* S, Thread* th, V3 ip, V3 D, V3 N
     }
     nd = vnorm(nd);
     th->reflected++;
-    trace_ray(S, th, ip, nd, weight, tk, 0, col);
+    trace_ray(S, th, ip, nd, weight, tk, flags & ~RAY_CONTINUED, col);   /* SetFlags(ReflectionRay, ray) */
 }
 
 /* ComputeTextureColour + ComputeLightedTexture (trace.cpp:457-586,739-1179)
@@ -1616,6 +1658,17 @@ static void shade(const PovOracle* S, Thread* th, const Isect* is, V3 D, double 
 {
     const int level = tk->level;
     const int radiosity = S->desc.radiosity.enabled;
+    if (container_media(S, is->object) >= 0) {
+        /* a media container's surface only transmits (all of its finish
+         * terms are zero): ComputeRefraction with equal iors traces the
+         * continued ray (trace.cpp:1343-1400), entering or leaving the
+         * container's interior */
+        const int m = RAY_MEDIUM(flags);
+        th->transmitted++;   /* Transmitted_Rays_Traced */
+        trace_ray(S, th, is->ipoint, D, weight, tk, WITH_MEDIUM(flags, m == is->object ? -1 : is->object) | RAY_CONTINUED,
+                  out);
+        return;
+    }
     const PovGpuObject* o = &S->objs[is->object].o;
     const PovGpuMaterial* m = object_material(S, is->object);
     V3 raw = object_normal(S, is);
@@ -1697,8 +1750,12 @@ static void shade(const PovOracle* S, Thread* th, const Isect* is, V3 D, double 
                         continue;
                     for (int k = 0; k < 3; k++)
                         lc[k] = (float)(lc[k] * f);
-                } else if (shadow_blocked(S, th, ip, ld, ldist)) {
-                    continue;
+                } else {
+                    double t3[3] = {1.0, 1.0, 1.0};
+                    if (shadow_trace(S, th, ip, ld, ldist, RAY_MEDIUM(flags), !(flags & RAY_RADIOSITY), t3))
+                        continue;
+                    for (int k = 0; k < 3; k++)
+                        lc[k] = (float)(lc[k] * t3[k]);
                 }
             }
             /* ComputeDiffuseColour (trace.cpp:2441-2484) */
@@ -1743,7 +1800,7 @@ static void shade(const PovOracle* S, Thread* th, const Isect* is, V3 D, double 
     /* reflected component (trace.cpp:1155-1178) */
     if (!(reflec.r == 0.0f && reflec.g == 0.0f && reflec.b == 0.0f)) {
         RGB rc = {0, 0, 0};
-        compute_reflection(S, th, ip, D, N, raw, rweight, tk, &rc);
+        compute_reflection(S, th, ip, D, N, raw, rweight, tk, flags, &rc);
         r += reflec.r * rc.r;
         g += reflec.g * rc.g;
         b += reflec.b * rc.b;
@@ -1756,26 +1813,185 @@ static void shade(const PovOracle* S, Thread* th, const Isect* is, V3 D, double 
 /* Trace::TraceRay (trace.cpp:135-228): the ticket's level is raised while
  * the hit is shaded.  Returns the hit depth, HUGE_VAL for a miss or a ray
  * that bails at the trace level or ADC check. */
+static void compute_media(const PovOracle* S, Thread* th, V3 O, V3 D, double dist, int medium, Ticket* tk, RGB* col);
+
 static double trace_ray(const PovOracle* S, Thread* th, V3 O, V3 D, double weight, Ticket* tk, int flags, RGB* col)
 {
     th->rays++;   /* Number_Of_Rays */
     col->r = col->g = col->b = 0.0f;
     if (tk->level >= tk->max_level || weight < tk->adc)
         return HUGE_VAL;
+    const int cont = flags & RAY_CONTINUED;
+    flags &= ~RAY_CONTINUED;
     Isect is;
     double depth = HUGE_VAL;
-    tk->level++;
+    if (!cont)
+        tk->level++;
     if (find_intersection(S, th, O, D, HUGE_VAL, 0, &is)) {
         depth = is.depth;
         shade(S, th, &is, D, weight, tk, flags, col);
+        /* interior media of the segment the ray crossed (ComputeTextureColour,
+         * trace.cpp:577-580); the radiosity Trace runs with media off */
+        if (RAY_MEDIUM(flags) >= 0 && !(flags & RAY_RADIOSITY))
+            compute_media(S, th, O, D, is.depth, RAY_MEDIUM(flags), tk, col);
     } else {
         /* ComputeSky: background only (trace.cpp:2839-2888) */
         col->r = S->desc.background[0];
         col->g = S->desc.background[1];
         col->b = S->desc.background[2];
     }
-    tk->level--;
+    if (!cont)
+        tk->level--;
     return depth;
+}
+
+/* One media sample (MediaFunction::ComputeOneMediaSample, media.cpp:935-1038,
+ * sample method 3, constant density): at fraction d of the interval
+ * [s0, s0 + ds], the in-scattered light of every point light not in shadow
+ * (TestShadow, trace.cpp:3173-3203, from inside the container), isotropic
+ * phase (ComputeMediaScatteringAttenuation, media.cpp:1183-1220), times ds;
+ * the interval's optical depth estimate extinction * ds. */
+static void media_sample(const PovOracle* S, Thread* th, const PovGpuMedia* md, V3 O, V3 D, double s0, double ds,
+                         double d, int medium, double lit, Ticket* tk, float C[3], float od[3])
+{
+    double x = s0 + d * ds;
+    V3 P = vadd(O, vmul(D, x));
+    th->media_samples++;   /* Media_Samples */
+    double em[3] = {md->emission[0], md->emission[1], md->emission[2]};
+    int scattering = md->scattering[0] != 0.0f || md->scattering[1] != 0.0f || md->scattering[2] != 0.0f;
+    /* lit: the end of the lit span [0, lit] of a point light
+     * (ComputeOneMediaLightInterval, media.cpp:715-750), < 0 for an unlit
+     * interval; a sample beyond it sees no light (media.cpp:990) */
+    if (lit >= 0.0 && x >= 0.0 && x <= lit && scattering) {
+        for (int li = 0; li < S->nlights; li++) {
+            const PovGpuLight* L = &S->lights[li];
+            V3 ld = vsub(vload(L->center), P);
+            double ldist = vlen(ld);
+            ld = vdiv(ld, ldist);
+            double lc[3] = {L->colour[0], L->colour[1], L->colour[2]};
+            if (fabs(lc[0]) < EPSILON && fabs(lc[1]) < EPSILON && fabs(lc[2]) < EPSILON)
+                continue;
+            if (tk->level > tk->max_level)
+                continue;
+            if (shadow_trace(S, th, P, ld, ldist, medium, 1, lc))
+                continue;
+            if (fabs(lc[0]) < EPSILON && fabs(lc[1]) < EPSILON && fabs(lc[2]) < EPSILON)
+                continue;
+            for (int k = 0; k < 3; k++)
+                em[k] += 1.0 * md->scattering[k] * (float)lc[k];
+        }
+    }
+    for (int k = 0; k < 3; k++) {
+        C[k] = (float)(em[k] * ds);
+        od[k] = (float)(md->extinction[k] * ds);
+    }
+}
+
+static float col3_dist(const float a[3], const float b[3])   /* ColourDistance */
+{
+    return fabsf(a[0] - b[0]) + fabsf(a[1] - b[1]) + fabsf(a[2] - b[2]);
+}
+
+/* MediaFunction::ComputeOneMediaSampleRecursive (media.cpp:1040-1125), jitter 0. */
+static void media_recursive(const PovOracle* S, Thread* th, const PovGpuMedia* md, V3 O, V3 D, double s0, double ds,
+                            int medium, double lit, Ticket* tk, double d1, double d3, const float C1[3], const float C3[3],
+                            const float od1[3], const float od3[3], int depth, float R[3], float ODR[3])
+{
+    float C2[3], od2[3], R2[3], ODR2[3];
+    double d2 = 0.5 * (d1 + d3);
+    media_sample(S, th, md, O, D, s0, ds, d2, medium, lit, tk, C2, od2);
+    if (depth <= 0) {
+        for (int k = 0; k < 3; k++) {
+            R[k] = (C1[k] + C2[k] + C3[k]) / 3.0f;
+            ODR[k] = (od1[k] + od2[k] + od3[k]) / 3.0f;
+        }
+        return;
+    }
+    if (col3_dist(C1, C2) > md->aa_threshold) {
+        media_recursive(S, th, md, O, D, s0, ds, medium, lit, tk, d1, d2, C1, C2, od1, od2, depth - 1, R2, ODR2);
+        for (int k = 0; k < 3; k++) {
+            R[k] = R2[k] / 2.0f;
+            ODR[k] = ODR2[k] / 2.0f;
+        }
+    } else {
+        for (int k = 0; k < 3; k++) {
+            R[k] = C1[k] / 3.0f + C2[k] / 6.0f;
+            ODR[k] = od1[k] / 3.0f + od2[k] / 6.0f;
+        }
+    }
+    if (col3_dist(C2, C3) > md->aa_threshold) {
+        media_recursive(S, th, md, O, D, s0, ds, medium, lit, tk, d2, d3, C2, C3, od2, od3, depth - 1, R2, ODR2);
+        for (int k = 0; k < 3; k++) {
+            R[k] += R2[k] / 2.0f;
+            ODR[k] += ODR2[k] / 2.0f;
+        }
+    } else {
+        for (int k = 0; k < 3; k++) {
+            R[k] += C2[k] / 6.0f + C3[k] / 3.0f;
+            ODR[k] += od2[k] / 6.0f + od3[k] / 3.0f;
+        }
+    }
+}
+
+/* MediaFunction::ComputeMedia (media.cpp:287-364) for the media of one
+ * container over the segment [0, dist] of the ray: point lights make one lit
+ * interval (ComputeMediaLightInterval, media.cpp:598-751), split into
+ * `intervals` uniform intervals (ComputeMediaSampleInterval, media.cpp:
+ * 527-596; unlit constant media keep one), each sampled adaptively
+ * (ComputeMediaAdaptiveSampling, media.cpp:432-501), then combined
+ * (ComputeMediaColour, media.cpp:503-525): colour * exp(-Od) + Te. */
+static void compute_media(const PovOracle* S, Thread* th, V3 O, V3 D, double dist, int medium, Ticket* tk, RGB* col)
+{
+    const PovGpuMedia* md = &S->desc.medias[container_media(S, medium)];
+    const int lit = S->nlights > 0;
+    /* ComputeMediaSampleInterval (media.cpp:527-596): with a light, the
+     * span [0, dist] in `intervals` equal intervals, s1 = delta * (i + 1);
+     * when rounding leaves the last s1 short of dist, ComputeMedia
+     * (media.cpp:346-352) pads with an unlit interval up to dist.  Without
+     * one, constant media takes the whole span as one unlit interval. */
+    const int nuni = lit ? (md->intervals > 1 ? md->intervals : 1) : 1;
+    const double delta = dist / (double)nuni;
+    const int pad = lit && delta * (double)nuni < dist;
+    const int nint = nuni + pad;
+    int sub = (md->min_samples + 1) / 2;
+    if (sub < 1)
+        sub = 1;
+    const double dd = 1.0 / (double)sub;
+    double Od[3] = {0.0, 0.0, 0.0};
+    float Te[3] = {0.0f, 0.0f, 0.0f};
+    for (int i = 0; i < nint; i++) {
+        const double s0 = delta * (double)i;
+        const double ds = (i < nuni) ? delta : dist - delta * (double)nuni;
+        const double lit_end = (lit && i < nuni) ? dist : -1.0;
+        float C0[3], od0[3], C1[3], od1[3], R[3], ODR[3];
+        float te[3] = {0.0f, 0.0f, 0.0f}, odi[3] = {0.0f, 0.0f, 0.0f};
+        media_sample(S, th, md, O, D, s0, ds, 0.0, medium, lit_end, tk, C0, od0);
+        double d0 = 0.0;
+        for (int j = 1; j <= sub; j++) {
+            double d1 = d0 + dd;
+            media_sample(S, th, md, O, D, s0, ds, d1, medium, lit_end, tk, C1, od1);
+            media_recursive(S, th, md, O, D, s0, ds, medium, lit_end, tk, d0, d1, C0, C1, od0, od1, md->aa_level - 1, R,
+                            ODR);
+            for (int k = 0; k < 3; k++) {
+                R[k] = (float)(R[k] * exp(-odi[k] * dd));
+                if (ODR[k] != 0.0f)
+                    R[k] = (float)(R[k] * ((1.0 - exp(-ODR[k] * dd)) / (ODR[k] * dd)));
+                te[k] += R[k];
+                odi[k] += ODR[k];
+                C0[k] = C1[k];
+                od0[k] = od1[k];
+            }
+            d0 = d1;
+        }
+        const double n = 1.0 / (double)sub;
+        for (int k = 0; k < 3; k++) {
+            Te[k] += (float)(te[k] * n * exp(-Od[k]));
+            Od[k] += odi[k] * n;
+        }
+    }
+    col->r = (float)(col->r * exp(-Od[0]) + Te[0]);
+    col->g = (float)(col->g * exp(-Od[1]) + Te[1]);
+    col->b = (float)(col->b * exp(-Od[2]) + Te[2]);
 }
 
 /* ============================================================ radiosity ==
@@ -2398,8 +2614,36 @@ int pov_oracle_create(const PovGpuSceneDesc* desc, PovOracle** out, int32_t* bad
     if (bad_index) *bad_index = -1;
     if (!desc || !out || desc->abi_version != POV_GPU_ABI_VERSION || desc->num_materials < 1)
         return POV_GPU_E_INVALID;
+    /* media containers: hollow top-level boxes whose surface only
+     * transmits, holding one constant isotropic media sampled by method 3
+     * without jitter; point lights only; no other transmitting surface */
+    int containers = 0;
+    for (int i = 0; i < desc->num_objects; i++) {
+        const PovGpuObject* o = &desc->objects[i];
+        if (o->media < 0 || o->media > desc->num_medias || (o->media > 0 && !desc->medias))
+            return POV_GPU_E_INVALID;
+        const PovGpuMaterial* m = (o->material >= 0 && o->material < desc->num_materials) ? &desc->materials[o->material]
+                                                                                           : NULL;
+        int transmits = m && (m->pigment[3] != 0.0f || m->pigment[4] != 0.0f);
+        if (o->media > 0 || transmits) {
+            if (bad_index) *bad_index = i;
+            const PovGpuMedia* md = o->media > 0 ? &desc->medias[o->media - 1] : NULL;
+            if (!md || o->type != POV_OBJ_BOX || !(o->flags & POV_FLAG_HOLLOW) || o->parent >= 0 || !m ||
+                m->pigment[3] != 0.0f || m->pigment[4] != 1.0f || m->diffuse != 0.0f || m->phong != 0.0f ||
+                m->specular != 0.0f || m->emission[0] != 0.0f || m->emission[1] != 0.0f || m->emission[2] != 0.0f ||
+                m->ambient[0] != 0.0f || m->ambient[1] != 0.0f || m->ambient[2] != 0.0f ||
+                m->reflection_max[0] != 0.0f || m->reflection_max[1] != 0.0f || m->reflection_max[2] != 0.0f ||
+                md->method != 3 || md->jitter != 0.0f || md->scattering_type != 1 ||
+                md->min_samples != md->max_samples || md->min_samples < 1 || md->aa_level < 1)
+                return POV_GPU_E_UNSUPPORTED;
+            containers++;
+        }
+    }
+    if (bad_index) *bad_index = -1;
     for (int i = 0; i < desc->num_lights; i++) {
         const PovGpuLight* L = &desc->lights[i];
+        if (containers && L->kind != POV_LIGHT_POINT)
+            return POV_GPU_E_UNSUPPORTED;   /* media samples test point-light shadows only */
         if (L->kind == POV_LIGHT_AREA &&
             (L->area_size1 < 1 || L->area_size2 < 1 || L->area_size1 * L->area_size2 > AREA_MAX_POINTS ||
              L->jitter || (L->circular && (L->area_size1 < 2 || L->area_size2 < 2))))
@@ -2716,6 +2960,8 @@ static void* render_worker_aa(void* arg)
     J->stats.shadow_ray_tests += th.shadow_tests;
     J->stats.shadow_rays_succeeded += th.shadow_succeeded;
     J->stats.reflected_rays += th.reflected;
+    J->stats.transmitted_rays += th.transmitted;
+    J->stats.media_samples += th.media_samples;
     J->stats.number_of_pixels += pixels;
     J->stats.number_of_samples += samples;
     pthread_mutex_unlock(&J->lock);
@@ -2747,6 +2993,8 @@ static void* render_worker(void* arg)
     J->stats.shadow_ray_tests += th.shadow_tests;
     J->stats.shadow_rays_succeeded += th.shadow_succeeded;
     J->stats.reflected_rays += th.reflected;
+    J->stats.transmitted_rays += th.transmitted;
+    J->stats.media_samples += th.media_samples;
     pthread_mutex_unlock(&J->lock);
     thread_free(&th);
     return NULL;
@@ -2847,6 +3095,8 @@ static int render_radiosity(PovOracle* S, const PovGpuRenderParams* p, int32_t x
         stats->shadow_ray_tests = th.shadow_tests;
         stats->shadow_rays_succeeded = th.shadow_succeeded;
         stats->reflected_rays = th.reflected;
+        stats->transmitted_rays = th.transmitted;
+        stats->media_samples = th.media_samples;
         stats->number_of_pixels = (uint64_t)(x1 - x0) * (uint64_t)(y1 - y0) + R->pixels;
         stats->radiosity_gathers = R->gathers;
         stats->radiosity_reuse = R->reused;

@@ -37,6 +37,7 @@
 #include "base/stringutilities.h"
 #include "core/bounding/boundingbox.h"
 #include "core/lighting/lightsource.h"
+#include "core/material/media.h"
 #include "core/math/matrix.h"
 #include "core/math/randomsequence.h"
 #include "core/render/ray.h"
@@ -170,10 +171,12 @@ void PrintStats(TraceThreadData& td)
 {
     RenderStatistics& st = td.Stats();
     std::printf("{\"number_of_rays\": %llu, \"shadow_ray_tests\": %llu, \"shadow_rays_succeeded\": %llu, "
-                "\"reflected_rays\": %llu, \"shadow_cache_hits\": %llu}\n",
+                "\"reflected_rays\": %llu, \"shadow_cache_hits\": %llu, \"transmitted_rays\": %llu, "
+                "\"media_samples\": %llu, \"media_intervals\": %llu}\n",
                 (unsigned long long)st[Number_Of_Rays], (unsigned long long)st[Shadow_Ray_Tests],
                 (unsigned long long)st[Shadow_Rays_Succeeded], (unsigned long long)st[Reflected_Rays_Traced],
-                (unsigned long long)st[Shadow_Cache_Hits]);
+                (unsigned long long)st[Shadow_Cache_Hits], (unsigned long long)st[Transmitted_Rays_Traced],
+                (unsigned long long)st[Media_Samples], (unsigned long long)st[Media_Intervals]);
 }
 
 void Vec(FILE *f, const char *name, const Vector3d& v)
@@ -226,21 +229,43 @@ int main(int argc, char **argv)
         Harness h;
         h.Parse(scene, width, height);
         Trace::CooperateFunctor cooperate;
-        Trace::MediaFunctor media;
         Trace::RadiosityFunctor radiosity;
         QualityFlags quality(9);
         TraceThreadData td(h.sd, 0);
-        TracePixel trace(h.sd, &h.sd->parsedCamera, &td, h.sd->parsedMaxTraceLevel,
-                         h.sd->parsedAdcBailout, quality, cooperate, media, radiosity);
-
-        if (mode == "pixels")
+        // the pixel tracer with the renderer's own MediaFunction wired to it,
+        // as TraceTask holds them (tracetask.h:122-126, tracetask.cpp:253)
+        struct PixelTracer
         {
+            TracePixel trace;
+            MediaFunction media;
+            PixelTracer(std::shared_ptr<SceneData> sd, TraceThreadData *td, const QualityFlags& q,
+                        Trace::CooperateFunctor& coop, Trace::RadiosityFunctor& rad) :
+                trace(sd, &sd->parsedCamera, td, sd->parsedMaxTraceLevel, sd->parsedAdcBailout, q, coop, media, rad),
+                media(td, &trace, nullptr)
+            {}
+        } pt(h.sd, &td, quality, cooperate, radiosity);
+        TracePixel& trace = pt.trace;
+
+        if (mode == "pixels" || mode == "pixelstats")
+        {
+            // pixelstats: per pixel, the counters it added (rays, shadow
+            // tests, shadow successes, media samples, media intervals)
+            const bool per_pixel = (mode == "pixelstats");
+            std::vector<uint64_t> counts;
+            const int which[5] = {Number_Of_Rays, Shadow_Ray_Tests, Shadow_Rays_Succeeded, Media_Samples,
+                                  Media_Intervals};
             std::vector<float> out((size_t)width * height * 4);
             for (int y = 0; y < height; y++)
                 for (int x = 0; x < width; x++)
                 {
                     RGBTColour col;
+                    uint64_t before[5];
+                    for (int k = 0; k < 5; k++)
+                        before[k] = td.Stats()[(IntStatsIndex)which[k]];
                     trace(x + 0.5, y + 0.5, width, height, col);
+                    if (per_pixel)
+                        for (int k = 0; k < 5; k++)
+                            counts.push_back(td.Stats()[(IntStatsIndex)which[k]] - before[k]);
                     float *p = &out[((size_t)y * width + x) * 4];
                     p[0] = col.red();
                     p[1] = col.green();
@@ -248,7 +273,10 @@ int main(int argc, char **argv)
                     p[3] = col.transm();
                 }
             FILE *f = std::fopen(argv[5], "wb");
-            std::fwrite(out.data(), sizeof(float), out.size(), f);
+            if (per_pixel)
+                std::fwrite(counts.data(), sizeof(uint64_t), counts.size(), f);
+            else
+                std::fwrite(out.data(), sizeof(float), out.size(), f);
             std::fclose(f);
             PrintStats(td);
         }

@@ -39,6 +39,7 @@ POV_FLAG_INFINITE = 0x0008
 POV_FLAG_DOUBLE_ILLUM = 0x0010
 POV_FLAG_NO_REFLECTION = 0x0020
 POV_FLAG_NO_IMAGE = 0x0040
+POV_FLAG_HOLLOW = 0x0080
 
 POV_LIGHT_POINT = 0
 POV_LIGHT_AREA = 1
@@ -47,7 +48,7 @@ POV_LIGHT_AREA = 1
 class PovGpuObject(C.Structure):
     _fields_ = [("type", C.c_int32), ("flags", C.c_int32), ("material", C.c_int32),
                 ("parent", C.c_int32), ("first_child", C.c_int32),
-                ("num_children", C.c_int32), ("mesh", C.c_int32), ("reserved", C.c_int32),
+                ("num_children", C.c_int32), ("mesh", C.c_int32), ("media", C.c_int32),
                 ("p", C.c_double * 8), ("trans", C.c_double * 32)]
 
 
@@ -98,6 +99,14 @@ class PovGpuRadiosity(C.Structure):
                 ("reserved", C.c_int32)]
 
 
+class PovGpuMedia(C.Structure):
+    _fields_ = [("scattering_type", C.c_int32), ("method", C.c_int32), ("intervals", C.c_int32),
+                ("min_samples", C.c_int32), ("max_samples", C.c_int32), ("aa_level", C.c_int32),
+                ("aa_threshold", C.c_float), ("jitter", C.c_float), ("absorption", C.c_float * 3),
+                ("emission", C.c_float * 3), ("scattering", C.c_float * 3), ("extinction", C.c_float * 3),
+                ("eccentricity", C.c_float), ("reserved", C.c_int32)]
+
+
 class PovGpuSceneDesc(C.Structure):
     _fields_ = [("abi_version", C.c_uint32), ("num_objects", C.c_int32),
                 ("objects", C.POINTER(PovGpuObject)), ("num_materials", C.c_int32),
@@ -106,7 +115,8 @@ class PovGpuSceneDesc(C.Structure):
                 ("meshes", C.POINTER(PovGpuMesh)), ("camera", PovGpuCamera),
                 ("background", C.c_float * 4), ("ambient_light", C.c_float * 3),
                 ("max_trace_level", C.c_int32), ("adc_bailout", C.c_float),
-                ("language_version", C.c_int32), ("radiosity", PovGpuRadiosity)]
+                ("language_version", C.c_int32), ("radiosity", PovGpuRadiosity),
+                ("num_medias", C.c_int32), ("medias", C.POINTER(PovGpuMedia))]
 
 
 class PovGpuBlock(C.Structure):
@@ -128,7 +138,8 @@ class PovGpuStats(C.Structure):
                 ("radiosity_gathers", C.c_uint64), ("radiosity_reuse", C.c_uint64),
                 ("device_error", C.c_uint64), ("radiosity_rays", C.c_uint64),
                 ("radiosity_gathers_d0", C.c_uint64), ("radiosity_gathers_d1", C.c_uint64),
-                ("nic_answers", C.c_uint64), ("nic_val_error_ppm", C.c_uint64), ("reserved", C.c_uint64 * 2)]
+                ("nic_answers", C.c_uint64), ("nic_val_error_ppm", C.c_uint64),
+                ("transmitted_rays", C.c_uint64), ("media_samples", C.c_uint64)]
 
     def as_dict(self):
         return {k: int(getattr(self, k)) for k, _ in self._fields_ if k != "reserved"}
@@ -165,7 +176,7 @@ STRUCTS = {
     "PovGpuRadiosity": PovGpuRadiosity, "PovGpuSceneDesc": PovGpuSceneDesc,
     "PovGpuBlock": PovGpuBlock, "PovGpuRenderParams": PovGpuRenderParams,
     "PovGpuStats": PovGpuStats, "PovGpuHit": PovGpuHit, "PovGpuTimings": PovGpuTimings,
-    "PovGpuNeuralCache": PovGpuNeuralCache,
+    "PovGpuNeuralCache": PovGpuNeuralCache, "PovGpuMedia": PovGpuMedia,
 }
 
 # Entry points that include/povgpu.h declares (checked by the CPU tests).

@@ -184,8 +184,9 @@ class Transform:
 class Material:
     def __init__(self, rgb, ambient=0.1, diffuse=0.6, phong=0.0, phong_size=40.0,
                  specular=0.0, roughness=0.05, reflection=0.0, brilliance=1.0,
-                 emission=0.0):
+                 emission=0.0, transmit=0.0):
         self.rgb = tuple(float(c) for c in rgb)
+        self.transmit = float(transmit)
         self.ambient = float(ambient)
         self.diffuse = float(diffuse)
         self.phong = float(phong)
@@ -208,11 +209,15 @@ class Material:
             fin += " reflection %s" % _g(self.reflection)
         if self.emission:
             fin += " emission %s" % _g(self.emission)
-        return "texture { pigment { color rgb %s } finish { %s } }" % (_v(self.rgb), fin)
+        if self.transmit:
+            pig = "color rgbt <%s,%s,%s,%s>" % (_g(self.rgb[0]), _g(self.rgb[1]), _g(self.rgb[2]), _g(self.transmit))
+        else:
+            pig = "color rgb %s" % _v(self.rgb)
+        return "texture { pigment { %s } finish { %s } }" % (pig, fin)
 
     def desc(self):
         m = abi.PovGpuMaterial()
-        m.pigment[:] = [self.rgb[0], self.rgb[1], self.rgb[2], 0.0, 0.0]
+        m.pigment[:] = [self.rgb[0], self.rgb[1], self.rgb[2], 0.0, self.transmit]
         m.ambient[:] = [self.ambient] * 3
         m.emission[:] = [self.emission] * 3
         m.diffuse = self.diffuse
@@ -284,6 +289,7 @@ class Scene:
         self.meshes = []
         self.antialias = None  # (threshold, depth) for sampling method 2
         self.radiosity = None  # dict of radiosity{} settings, None = off
+        self.medias = []       # interior media of container objects
 
     # -- building ----------------------------------------------------------
     def material(self, m):
@@ -348,6 +354,21 @@ class Scene:
         t = {"union": abi.POV_OBJ_UNION, "intersection": abi.POV_OBJ_INTERSECTION,
              "difference": abi.POV_OBJ_INTERSECTION, "merge": abi.POV_OBJ_MERGE}[kind]
         return dict(type=t, kind=kind, children=moved, translate=tv, material=mat)
+
+    def media_box(self, c1, c2, scattering=(0.05, 0.05, 0.05), absorption=(0.0, 0.0, 0.0),
+                  emission=(0.0, 0.0, 0.0), intervals=10, samples=10, aa_level=3, aa_threshold=0.1):
+        """A hollow, fully transmitting box holding one uniform media
+        (Parse_Media defaults, source/parser/parser_materials.cpp:3500-3630:
+        method 3, jitter 0; isotropic scattering; Media::PostProcess sets
+        extinction = absorption + scattering)."""
+        mat = self.material(Material((1.0, 1.0, 1.0), ambient=0.0, diffuse=0.0, transmit=1.0))
+        self.medias.append(dict(scattering=tuple(map(float, scattering)), absorption=tuple(map(float, absorption)),
+                                emission=tuple(map(float, emission)), intervals=int(intervals),
+                                samples=int(samples), aa_level=int(aa_level), aa_threshold=float(aa_threshold)))
+        node = self.n_box(c1, c2, mat)
+        node["hollow"] = True
+        node["media"] = len(self.medias)
+        self.objects.append(node)
 
     def point_light(self, pos, rgb=(1.0, 1.0, 1.0)):
         self.lights.append(dict(kind=abi.POV_LIGHT_POINT, pos=tuple(map(float, pos)),
@@ -421,7 +442,16 @@ class Scene:
         if t == abi.POV_OBJ_PLANE:
             return "plane { %s, %s%s }" % (_v(o["normal"]), _g(o["offset"]), tex)
         if t == abi.POV_OBJ_BOX:
-            return "box { %s, %s%s }" % (_v(o.get("sdl_c1", o["c1"])), _v(o.get("sdl_c2", o["c2"])), tex)
+            extra = ""
+            if o.get("hollow"):
+                extra += " hollow"
+            if o.get("media"):
+                md = self.medias[o["media"] - 1]
+                extra += (" interior { media { scattering { 1, rgb %s } absorption rgb %s emission rgb %s"
+                          " intervals %d samples %d aa_level %d aa_threshold %s } }"
+                          % (_v(md["scattering"]), _v(md["absorption"]), _v(md["emission"]), md["intervals"],
+                             md["samples"], md["aa_level"], _g(md["aa_threshold"])))
+            return "box { %s, %s%s%s }" % (_v(o.get("sdl_c1", o["c1"])), _v(o.get("sdl_c2", o["c2"])), tex, extra)
         if t == abi.POV_OBJ_TORUS:
             return "torus { %s, %s %s%s }" % (_g(o["R"]), _g(o["r"]), o["mods"], tex)
         if t == abi.POV_OBJ_MESH:
@@ -459,7 +489,9 @@ class Scene:
         for i, (o, parent) in enumerate(flat):
             d = objs[i]
             d.type = o["type"]
-            d.flags = abi.POV_FLAG_INVERTED if o.get("inverted") else 0
+            d.flags = (abi.POV_FLAG_INVERTED if o.get("inverted") else 0) | \
+                (abi.POV_FLAG_HOLLOW if o.get("hollow") else 0)
+            d.media = int(o.get("media", 0))
             d.material = o.get("material", -1)
             d.parent = parent
             d.first_child = first_child.get(i, -1)
@@ -532,6 +564,23 @@ class Scene:
         desc.adc_bailout = self.adc_bailout
         desc.language_version = 370
         desc.radiosity.enabled = 0
+        medias = (abi.PovGpuMedia * max(len(self.medias), 1))()
+        for i, md in enumerate(self.medias):
+            m = medias[i]
+            m.scattering_type = 1
+            m.method = 3
+            m.intervals = md["intervals"]
+            m.min_samples = m.max_samples = md["samples"]
+            m.aa_level = md["aa_level"]
+            m.aa_threshold = md["aa_threshold"]
+            m.jitter = 0.0
+            m.absorption[:] = list(md["absorption"])
+            m.emission[:] = list(md["emission"])
+            m.scattering[:] = list(md["scattering"])
+            m.extinction[:] = [a + sc for a, sc in zip(md["absorption"], md["scattering"])]
+        desc.num_medias = len(self.medias)
+        desc.medias = medias
+        keep.append(medias)
         if self.radiosity is not None:
             r = self.radiosity_settings()
             rd = desc.radiosity
@@ -806,9 +855,31 @@ def radiosity_room(width=1280, height=720, n_spheres=200, seed=4, radiosity=True
     return s
 
 
+def media_spheres(width=320, height=240, n_spheres=24, seed=5, intervals=10, samples=10, scattering=0.05):
+    """A uniform scattering media box [-7,7]^3 (hollow, fully transmitting;
+    scattering {1, rgb 0.05}, intervals 10, samples 10, method 3) around
+    `n_spheres` spheres r U[0.4,1.2], centres U[-5.5,5.5]^3, rgb U[0.2,0.9]^3
+    (seed 5), every other one with reflection 0.2; plane y=-8; one point
+    light (20,30,-20); camera (0,4,-25) looking at the origin, 50 deg;
+    max_trace_level 3."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    s = Scene("media_spheres", width, height, (0.0, 4.0, -25.0), (0.0, 0.0, 0.0), 50.0, max_trace_level=3)
+    s.point_light((20.0, 30.0, -20.0))
+    s.media_box((-7.0, -7.0, -7.0), (7.0, 7.0, 7.0), scattering=(scattering,) * 3, intervals=intervals,
+                samples=samples)
+    for i in range(n_spheres):
+        c = rng.uniform(-5.5, 5.5, size=3)
+        r = rng.uniform(0.4, 1.2)
+        rgb = rng.uniform(0.2, 0.9, size=3)
+        s.sphere(c, r, s.material(Material(rgb, phong=0.4, reflection=0.2 if i % 2 else 0.0)))
+    s.plane((0.0, 1.0, 0.0), -8.0, s.material(Material((0.8, 0.8, 0.8))))
+    return s
+
+
 WORKLOADS = {
     "spheres_plane": spheres_plane,
     "mesh_spheres": mesh_spheres,
     "csg_torus_grid": csg_torus_grid,
     "radiosity_room": radiosity_room,
+    "media_spheres": media_spheres,
 }

@@ -54,6 +54,7 @@ def cases():
         "area_room_160x90": (scenes.radiosity_room(160, 90, n_spheres=40, radiosity=False), 2, 9.0),
         "area_room_adaptive_160x90": (scenes.radiosity_room(160, 90, n_spheres=40, radiosity=False, area=(5, 5),
                                                             adaptive=1, orient=True), 2, 9.0),
+        "media_spheres_160x120": (scenes.media_spheres(160, 120), 2, 9.0),
     }
 
 

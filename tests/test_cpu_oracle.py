@@ -55,6 +55,10 @@ def _has_area_light(scene):
     return any(l["kind"] == 1 for l in scene.lights)
 
 
+def _has_media(scene):
+    return bool(getattr(scene, "medias", None))
+
+
 @pytest.mark.parametrize("case", sorted(CASES))
 def test_oracle_pixels_and_counters_match_reference(case):
     """Exact, except where the reference's light-source shadow cache decides
@@ -65,14 +69,24 @@ def test_oracle_pixels_and_counters_match_reference(case):
     (many shadow rays per point) a few samples of a point whose shadow ray
     passes within 1e-3 of another surface flip: bounded here at 0.01% of the
     shadow rays, less than 1/255 linear per pixel and 99.9% of 8-bit
-    channels within one step."""
+    channels within one step.  Inside a media container the cached object
+    can lie beyond the container wall, which the full test counts as a hit
+    of its own: one test and one success fewer in the reference (bounded
+    the same way); media samples are counted exactly."""
     scene = CASES[case][0]
     g = _load(case)
     img, st = Oracle(scene).render(threads=4, params=no_aa(scene))
     ref = g["pixels"]
     rs = json.loads(str(g["stats"]))
     diff = np.abs(img - ref).max(axis=2)
-    if _has_area_light(scene):
+    if _has_media(scene):
+        assert diff.max() <= 1e-5, float(diff.max())
+        for k in ("number_of_rays", "reflected_rays", "transmitted_rays", "media_samples"):
+            assert st[k] == rs[k], (k, st[k], rs[k])
+        for k in ("shadow_ray_tests", "shadow_rays_succeeded"):
+            assert 0 <= st[k] - rs[k] <= 1e-4 * rs["shadow_ray_tests"], (k, st[k], rs[k])
+        assert compare_pixels(img, ref)["max_lsb"] <= 1
+    elif _has_area_light(scene):
         assert diff.max() < 1.0 / 255.0 and (diff <= 1e-5).mean() >= 0.999, float(diff.max())
         for k in ("shadow_ray_tests", "shadow_rays_succeeded"):
             assert abs(st[k] - rs[k]) <= 1e-4 * rs["shadow_ray_tests"], (k, st[k], rs[k])
