@@ -414,7 +414,8 @@ int pov_gpu_scene_set_stream(PovGpuScene* scene, void* cuda_stream);
 #define POV_GPU_STAGE_FINALIZE      5
 #define POV_GPU_STAGE_AREA_SHADOW   6   /* area-light shadow subdivision       */
 #define POV_GPU_STAGE_RADIOSITY     7   /* radiosity cache queries and gathers  */
-#define POV_GPU_STAGES              8
+#define POV_GPU_STAGE_MEDIA         8   /* media of rays inside containers      */
+#define POV_GPU_STAGES              9
 
 /* Profile of the last trace call.  Stage times are CUDA-event durations on
  * the launch stream, filled when profiling bit 0 is set; the work counters

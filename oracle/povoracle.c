@@ -2636,6 +2636,15 @@ int pov_oracle_create(const PovGpuSceneDesc* desc, PovOracle** out, int32_t* bad
                 md->method != 3 || md->jitter != 0.0f || md->scattering_type != 1 ||
                 md->min_samples != md->max_samples || md->min_samples < 1 || md->aa_level < 1)
                 return POV_GPU_E_UNSUPPORTED;
+            /* camera rays start outside every container: a camera inside one
+             * would need the interior list of its location */
+            int inside = 1;
+            for (int k = 0; k < 3; k++) {
+                double lo = fmin(o->p[k], o->p[3 + k]), hi = fmax(o->p[k], o->p[3 + k]);
+                inside = inside && desc->camera.location[k] >= lo && desc->camera.location[k] <= hi;
+            }
+            if (inside)
+                return POV_GPU_E_UNSUPPORTED;
             containers++;
         }
     }

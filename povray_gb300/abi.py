@@ -157,8 +157,9 @@ class PovGpuHit(C.Structure):
     _fields_ = [("object", C.c_int32), ("triangle", C.c_int32), ("t", C.c_double)]
 
 
-POV_GPU_STAGES = 8
-STAGE_NAMES = ["camera", "trace_closest", "shade", "trace_shadow", "resolve", "finalize", "area_shadow", "radiosity"]
+POV_GPU_STAGES = 9
+STAGE_NAMES = ["camera", "trace_closest", "shade", "trace_shadow", "resolve", "finalize", "area_shadow", "radiosity",
+               "media"]
 POV_GPU_PROFILE_TIMES = 1
 POV_GPU_PROFILE_WORK = 2
 

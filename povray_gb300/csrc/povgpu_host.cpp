@@ -292,7 +292,8 @@ enum {
     C_NN = 7,     // AA: next cells
     C_AQ = 8,     // area-light shadow items
     C_RQ = 9,     // radiosity queries
-    C_NUM = 10
+    C_MC = 10,    // rays crossing a media container's interior
+    C_NUM = 11
 };
 
 // One wavefront of ray queues and per-path state: the camera's, or the
@@ -303,9 +304,12 @@ struct PathBufs {
     DevBuf aq, aq_slot, aq_skip;   // area-light shadow items
     DevBuf rq, rq_amb;             // radiosity queries of the hits, and their answers
     DevBuf quality, first_t;       // sample rays: quality of each, depth of its first hit
+    DevBuf stateA, stateB, smedium; // media containers: per-ray level and medium, shadow-ray medium
+    DevBuf mlist, mte, mod;         // media containers: listed rays, per-interval sums
     DevBuf counters;
 
-    cudaError_t ensure(size_t maxq, int nl, int nal, bool rad, bool sample_rays)
+    // media_ni: interval slots per ray segment (0: the scene has no media containers)
+    cudaError_t ensure(size_t maxq, int nl, int nal, bool rad, bool sample_rays, int media_ni = 0)
     {
         maxq = std::max<size_t>(maxq, 1);
         nl = std::max(nl, 1);
@@ -338,13 +342,22 @@ struct PathBufs {
             PB_ENSURE(quality, sizeof(float) * maxq);
             PB_ENSURE(first_t, sizeof(float) * maxq);
         }
+        if (media_ni > 0) {
+            PB_ENSURE(stateA, sizeof(int) * maxq);
+            PB_ENSURE(stateB, sizeof(int) * maxq);
+            PB_ENSURE(smedium, sizeof(int) * maxq * nl);
+            PB_ENSURE(mlist, sizeof(int) * maxq);
+            PB_ENSURE(mte, sizeof(float4) * maxq * media_ni);
+            PB_ENSURE(mod, sizeof(float4) * maxq * media_ni);
+        }
 #undef PB_ENSURE
         return cudaSuccess;
     }
     void release()
     {
         DevBuf* all[] = {&qA, &qB, &pathA, &pathB, &hits, &paths, &slot_contrib, &sq, &sq_slot, &blocked, &skipA,
-                         &skipB, &sskip, &aq, &aq_slot, &aq_skip, &rq, &rq_amb, &quality, &first_t, &counters};
+                         &skipB, &sskip, &aq, &aq_slot, &aq_skip, &rq, &rq_amb, &quality, &first_t, &stateA,
+                         &stateB, &smedium, &mlist, &mte, &mod, &counters};
         for (DevBuf* b : all)
             b->release();
     }
@@ -437,7 +450,8 @@ struct PovGpuScene {
     // persistent scene data
     DevBuf nodes, refs, tri_v0, tri_e1, tri_e2, tri_global, tri_shade, tri_normal, tri_local, normals;
     DevBuf spheres, spheres64, boxes64, sphere_obj, sphere_flags, planes, plane_obj, boxes, tori, csgs, csg_children, objects,
-        materials, lights;
+        materials, lights, medias;
+    int    media_ni = 0;   // interval slots per media segment (0: no media containers)
     // host copies of the id maps (prim -> flattened object id)
     std::vector<int32_t> h_sphere_obj, h_plane_obj, h_box_obj, h_torus_obj, h_tri_global, h_tri_local, h_tri_obj;
     std::vector<DevCsg> h_csgs;
@@ -472,7 +486,7 @@ struct PovGpuScene {
                          &normals, &spheres, &spheres64, &boxes64, &sphere_obj, &sphere_flags, &planes, &plane_obj, &boxes, &tori, &csgs,
                          &csg_children, &objects, &materials, &lights, &blocks, &block_off, &corner_off, &qA,
                          &hits, &out, &counters, &stats, &err, &rays_in, &t64, &corners, &aa_grid, &aa_mask,
-                         &aa_subdiv, &aa_xy, &cellsA, &cellsB, &spos, &sslot, &wcount, &pos_count};
+                         &aa_subdiv, &aa_xy, &cellsA, &cellsB, &spos, &sslot, &wcount, &pos_count, &medias};
         for (DevBuf* b : all)
             b->release();
         top.release();
@@ -495,6 +509,58 @@ namespace {
 constexpr int MAX_AA_DEPTH = 4;   // (2^4+1)^2 = 289 grid points, 21 subdividable cells per pixel
 
 bool is_csg(int t) { return t == POV_OBJ_UNION || t == POV_OBJ_INTERSECTION || t == POV_OBJ_MERGE; }
+
+// Media container: a hollow object holding media (validated to be a
+// top-level box whose surface only transmits).
+bool is_container(const PovGpuObject& o) { return o.media > 0 && (o.flags & POV_FLAG_HOLLOW); }
+
+// Media containers as the GPU path restates them: hollow top-level boxes
+// without transform whose surface only transmits (pigment transmit 1, no
+// finish terms), each holding one constant isotropic media sampled by
+// method 3 without jitter (Min_Samples = Max_Samples), the camera outside,
+// point lights only; no other surface transmits.  Marks the materials the
+// containers use in `cmat`.
+int validate_media(const PovGpuSceneDesc* d, std::vector<char>& cmat, int32_t* bad)
+{
+    cmat.assign((size_t)d->num_materials, 0);
+    int containers = 0;
+    for (int i = 0; i < d->num_objects; i++) {
+        const PovGpuObject& o = d->objects[i];
+        if (o.media < 0 || o.media > d->num_medias || (o.media > 0 && !d->medias))
+            return POV_GPU_E_INVALID;
+        const PovGpuMaterial* m =
+            (o.material >= 0 && o.material < d->num_materials) ? &d->materials[o.material] : nullptr;
+        const bool transmits = m && (m->pigment[3] != 0.0f || m->pigment[4] != 0.0f);
+        if (o.media == 0 && !transmits)
+            continue;
+        if (bad) *bad = i;
+        const PovGpuMedia* md = o.media > 0 ? &d->medias[o.media - 1] : nullptr;
+        if (!md || o.type != POV_OBJ_BOX || !(o.flags & POV_FLAG_HOLLOW) || o.parent >= 0 || !m ||
+            m->pigment[3] != 0.0f || m->pigment[4] != 1.0f || m->diffuse != 0.0f || m->phong != 0.0f ||
+            m->specular != 0.0f || m->emission[0] != 0.0f || m->emission[1] != 0.0f || m->emission[2] != 0.0f ||
+            m->ambient[0] != 0.0f || m->ambient[1] != 0.0f || m->ambient[2] != 0.0f ||
+            m->reflection_max[0] != 0.0f || m->reflection_max[1] != 0.0f || m->reflection_max[2] != 0.0f ||
+            md->method != 3 || md->jitter != 0.0f || md->scattering_type != 1 || md->min_samples != md->max_samples ||
+            md->min_samples < 1 || md->aa_level < 1 || md->aa_level > MEDIA_MAX_AA_LEVEL || md->intervals < 1 ||
+            md->intervals > MEDIA_MAX_INTERVALS || containers >= MAX_CONTAINERS)
+            return POV_GPU_E_UNSUPPORTED;
+        bool cam_inside = true;
+        for (int k = 0; k < 3; k++)
+            cam_inside = cam_inside && d->camera.location[k] >= std::min(o.p[k], o.p[3 + k]) &&
+                         d->camera.location[k] <= std::max(o.p[k], o.p[3 + k]);
+        if (cam_inside)
+            return POV_GPU_E_UNSUPPORTED;   // camera rays would start inside the media
+        cmat[o.material] = 1;
+        containers++;
+    }
+    if (bad) *bad = -1;
+    if (containers > 0 && d->max_trace_level > 255)
+        return POV_GPU_E_UNSUPPORTED;   // a ray's level is held in 8 bits of its state
+    for (int i = 0; containers > 0 && i < d->num_lights; i++)
+        if (d->lights[i].kind != POV_LIGHT_POINT)
+            return POV_GPU_E_UNSUPPORTED;   // media samples test point-light shadows only
+    return POV_GPU_OK;
+}
 
 int validate(const PovGpuSceneDesc* d, int32_t* bad)
 {
@@ -525,10 +591,17 @@ int validate(const PovGpuSceneDesc* d, int32_t* bad)
              L.jitter || (L.circular && (L.area_size1 < 2 || L.area_size2 < 2))))
             return POV_GPU_E_UNSUPPORTED;
     }
+    std::vector<char> cmat;
+    {
+        int rc = validate_media(d, cmat, bad);
+        if (rc != POV_GPU_OK)
+            return rc;
+    }
     for (int i = 0; i < d->num_materials; i++) {
         const PovGpuMaterial& m = d->materials[i];
-        // opaque plain pigments and the classic finish terms only
-        if (m.pigment[3] != 0.0f || m.pigment[4] != 0.0f || m.reflection_fresnel || m.fresnel != 0.0f ||
+        // opaque plain pigments and the classic finish terms only (media
+        // containers' surfaces transmit)
+        if ((!cmat[i] && (m.pigment[3] != 0.0f || m.pigment[4] != 0.0f)) || m.reflection_fresnel || m.fresnel != 0.0f ||
             m.metallic != 0.0f || m.reflect_metallic != 0.0f || m.reflect_exp != 1.0f || m.irid != 0.0f ||
             m.crand != 0.0f || m.diffuse_back != 0.0f || m.conserve_energy)
             return POV_GPU_E_UNSUPPORTED;
@@ -640,8 +713,8 @@ struct Builder {
         int idx = (int)boxes.size();
         DevBox b;
         b.lo = make_float4((float)o.p[0], (float)o.p[1], (float)o.p[2], __builtin_bit_cast(float, id));
-        b.hi = make_float4((float)o.p[3], (float)o.p[4], (float)o.p[5],
-                           __builtin_bit_cast(float, (int32_t)(o.flags & POV_FLAG_INVERTED ? 1 : 0)));
+        const int32_t bflags = (o.flags & POV_FLAG_INVERTED ? 1 : 0) | (is_container(o) ? BOX_CONTAINER : 0);
+        b.hi = make_float4((float)o.p[3], (float)o.p[4], (float)o.p[5], __builtin_bit_cast(float, bflags));
         boxes.push_back(b);
         boxes64.insert(boxes64.end(), {o.p[0], o.p[1], o.p[2], o.p[3], o.p[4], o.p[5]});
         box_obj.push_back(id);
@@ -791,6 +864,13 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
         objects[i].type = o.type;
         objects[i].mesh = o.mesh;
     }
+    // media containers, numbered in object order
+    std::vector<int> container_obj;
+    for (int i = 0; i < d->num_objects; i++)
+        if (is_container(d->objects[i])) {
+            objects[i].flags |= OBJ_CONTAINER | ((int)container_obj.size() << 16);
+            container_obj.push_back(i);
+        }
     for (int i = 0; i < d->num_objects; i++) {
         const PovGpuObject& o = d->objects[i];
         if (o.parent >= 0)
@@ -926,9 +1006,31 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
     CK(upload(sc->tori, B.tori));
     CK(upload(sc->csgs, B.csgs));
     CK(upload(sc->csg_children, B.csg_children));
+    // one DevMedia per container: its media and its box primitive
+    std::vector<DevMedia> medias(std::max<size_t>(container_obj.size(), 1));
+    int media_ni = 0;
+    for (size_t c = 0; c < container_obj.size(); c++) {
+        const PovGpuObject& o = d->objects[container_obj[c]];
+        const PovGpuMedia& md = d->medias[o.media - 1];
+        int box = -1;
+        for (size_t b = 0; b < B.box_obj.size(); b++)
+            if (B.box_obj[b] == container_obj[c])
+                box = (int)b;
+        if (box < 0)
+            return POV_GPU_E_INVALID;
+        DevMedia& m = medias[c];
+        m.emission = make_float4(md.emission[0], md.emission[1], md.emission[2], md.aa_threshold);
+        bool scat = md.scattering[0] != 0.0f || md.scattering[1] != 0.0f || md.scattering[2] != 0.0f;
+        m.scattering = make_float4(md.scattering[0], md.scattering[1], md.scattering[2], scat ? 1.0f : 0.0f);
+        m.extinction = make_float4(md.extinction[0], md.extinction[1], md.extinction[2], 0.0f);
+        m.n = make_int4(md.intervals, std::max((md.min_samples + 1) / 2, 1), md.aa_level, box);
+        media_ni = std::max(media_ni, md.intervals + 1);   // + the padding interval
+    }
+
     CK(upload(sc->objects, objects));
     CK(upload(sc->materials, mats));
     CK(upload(sc->lights, lights));
+    CK(upload(sc->medias, medias));
 
     sc->h_sphere_obj = B.sphere_obj;
     sc->h_plane_obj = B.plane_obj;
@@ -972,6 +1074,9 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
     S.lights = sc->lights.as<DevLight>();
     S.num_lights = d->num_lights;
     S.num_area_lights = num_area;
+    S.medias = sc->medias.as<DevMedia>();
+    S.num_containers = (int)container_obj.size();
+    sc->media_ni = container_obj.empty() ? 0 : media_ni;
     S.max_trace_level = d->max_trace_level;
     S.adc_bailout = d->adc_bailout;
     S.background = make_float4(d->background[0], d->background[1], d->background[2], d->background[3]);
@@ -1045,6 +1150,8 @@ int check_device_error(PovGpuScene* sc, PovGpuStats* stats, unsigned long long* 
         stats->shadow_ray_tests = host_stats[ST_SHADOW_TESTS];
         stats->shadow_rays_succeeded = host_stats[ST_SHADOW_SUCCEEDED];
         stats->reflected_rays = host_stats[ST_REFLECTED];
+        stats->transmitted_rays = host_stats[ST_TRANSMITTED];
+        stats->media_samples = host_stats[ST_MEDIA_SAMPLES];
         stats->device_error = errw;
     }
     return errw ? POV_GPU_E_DEVICE : POV_GPU_OK;
@@ -1197,7 +1304,8 @@ int run_levels(PovGpuScene* sc, StageClock& clk, PathBufs& B, size_t maxq, int l
     const int nl = std::max(sc->num_lights, 1);
     const int nal = sample_rays ? 0 : sc->S.num_area_lights;
     const bool rad = sc->rad.enabled && hit_depth < sc->rad.set.recursion_limit;
-    CK(B.ensure(maxq, nl, nal, rad, sample_rays));
+    const bool media = sc->media_ni > 0;
+    CK(B.ensure(maxq, nl, nal, rad, sample_rays, sc->media_ni));
     cudaStream_t st = sc->active();
     int* cnt = B.counters.as<int>();
     unsigned long long* dstats = sc->stats.as<unsigned long long>();
@@ -1221,7 +1329,25 @@ int run_levels(PovGpuScene* sc, StageClock& clk, PathBufs& B, size_t maxq, int l
     sr.rq_cap = (int)maxq;
     sr.adc = sample_rays ? (float)sc->rad.set.adc_bailout : S.adc_bailout;
     sr.gather = sample_rays ? 1 : 0;
-    for (int level = level0; level < max_level; level++) {
+    // media containers: rays carry their own level and medium; a ray that
+    // crosses a container wall goes on at its level in the next pass, so
+    // the passes run until the queue is empty (each pass raises a ray's
+    // level or takes it across a wall: at most 1 + 2 * containers passes a
+    // level)
+    int* scur = media ? B.stateA.as<int>() : nullptr;
+    int* snext = media ? B.stateB.as<int>() : nullptr;
+    const int max_pass = media ? (max_level - level0) * (1 + 2 * S.num_containers) : max_level - level0;
+    if (media)
+        CK(launch_fill_int(scur, ccur, (int)maxq, ray_state(level0, -1), grid_shade, st));
+    for (int pass = 0; pass < max_pass; pass++) {
+        const int level = level0 + pass;   // the level of every ray without media containers
+        if (media && pass > 0) {
+            int nq = 0;
+            CK(cudaMemcpyAsync(&nq, ccur, sizeof(int), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            if (nq == 0)
+                break;
+        }
         CK(cudaMemsetAsync(cnext, 0, sizeof(int), st));
         CK(cudaMemsetAsync(cnt + C_SQ, 0, sizeof(int) * 3, st));   // SQ, W0, W1
         CK(cudaMemsetAsync(cnt + C_AQ, 0, sizeof(int) * 2, st));   // AQ, RQ
@@ -1229,14 +1355,23 @@ int run_levels(PovGpuScene* sc, StageClock& clk, PathBufs& B, size_t maxq, int l
         CK(launch_trace(S, false, qcur, ccur, cnt + C_W0, B.hits.as<QHit>(), nullptr, sc->stack_depth, grid_trace,
                         derr, dstats, wc, (int)maxq, kcur, st));
         CK(clk.end());
-        if (sample_rays && level == level0)
+        if (sample_rays && pass == 0)
             CK(launch_first_hit(B.hits.as<QHit>(), ccur, (int)maxq, B.first_t.as<float>(), grid_shade, st));
+        if (media && !sample_rays) {   // the radiosity Trace runs with media off
+            CK(clk.begin(POV_GPU_STAGE_MEDIA));
+            CK(cudaMemsetAsync(cnt + C_MC, 0, sizeof(int), st));
+            CK(launch_media(S, qcur, scur, pcur, B.hits.as<QHit>(), ccur, (int)maxq, B.mlist.as<int>(), cnt + C_MC,
+                            sc->media_ni, B.mte.as<float4>(), B.mod.as<float4>(), B.paths.as<PathState>(),
+                            sc->stack_depth, grid_trace, derr, dstats, st));
+            CK(clk.end(3));
+        }
         CK(clk.begin(POV_GPU_STAGE_SHADE));
+        ShadeMedia sm{scur, snext, media ? B.smedium.as<int>() : nullptr};
         CK(launch_shade(S, level, max_level, qcur, pcur, B.hits.as<QHit>(), ccur, B.paths.as<PathState>(),
                         B.slot_contrib.as<float4>(), B.sq.as<QRay>(), B.sq_slot.as<int>(), cnt + C_SQ,
                         B.sskip.as<uint2>(), qnext, pnext, knext, cnext, (int)maxq, (int)(maxq * nl),
                         B.aq.as<QRay>(), B.aq_slot.as<int>(), B.aq_skip.as<uint2>(), cnt + C_AQ, (int)max_area, sr,
-                        grid_shade, derr, dstats, st));
+                        sm, grid_shade, derr, dstats, st));
         CK(clk.end());
         if (nal > 0) {
             CK(clk.begin(POV_GPU_STAGE_AREA_SHADOW));
@@ -1247,9 +1382,15 @@ int run_levels(PovGpuScene* sc, StageClock& clk, PathBufs& B, size_t maxq, int l
         }
         if (sc->num_lights > 0) {
             CK(clk.begin(POV_GPU_STAGE_TRACE_SHADOW));
-            CK(launch_trace(S, true, B.sq.as<QRay>(), cnt + C_SQ, cnt + C_W1, nullptr, B.blocked.as<uint8_t>(),
-                            sc->stack_depth, grid_trace, derr, dstats, wc ? wc + 4 : nullptr, (int)(maxq * nl),
-                            B.sskip.as<uint2>(), st));
+            if (media)
+                CK(launch_shadow_through(S, B.sq.as<QRay>(), B.sq_slot.as<int>(), B.sskip.as<uint2>(),
+                                         B.smedium.as<int>(), cnt + C_SQ, (int)(maxq * nl), B.blocked.as<uint8_t>(),
+                                         B.slot_contrib.as<float4>(), !sample_rays, sc->stack_depth, grid_trace,
+                                         derr, dstats, st));
+            else
+                CK(launch_trace(S, true, B.sq.as<QRay>(), cnt + C_SQ, cnt + C_W1, nullptr, B.blocked.as<uint8_t>(),
+                                sc->stack_depth, grid_trace, derr, dstats, wc ? wc + 4 : nullptr, (int)(maxq * nl),
+                                B.sskip.as<uint2>(), st));
             CK(clk.end());
             CK(clk.begin(POV_GPU_STAGE_RESOLVE));
             CK(launch_resolve(pcur, ccur, sc->num_lights, B.sq_slot.as<int>(), B.blocked.as<uint8_t>(), cnt + C_SQ,
@@ -1277,6 +1418,7 @@ int run_levels(PovGpuScene* sc, StageClock& clk, PathBufs& B, size_t maxq, int l
         std::swap(pcur, pnext);
         std::swap(ccur, cnext);
         std::swap(kcur, knext);
+        std::swap(scur, snext);
     }
     return POV_GPU_OK;
 }

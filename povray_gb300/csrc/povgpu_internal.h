@@ -81,7 +81,7 @@ struct __align__(16) DevMesh {
 // Axis-aligned box (Box without a transform): corners, object id and flags.
 struct __align__(16) DevBox {
     float4 lo;      // xyz, w = object id (int bits)
-    float4 hi;      // xyz, w = flags (int bits, bit0 inverted)
+    float4 hi;      // xyz, w = flags (int bits, bit0 inverted, bit1 BOX_CONTAINER)
 };
 
 // Torus in its own frame: the inverse TRANSFORM rows 0..3, columns 0..2
@@ -110,6 +110,28 @@ struct __align__(16) DevCsgChild {
     int32_t flags;      // bit0 inverted
     int32_t object;
 };
+
+// One media container: a hollow axis-aligned box (its box primitive carries
+// BOX_CONTAINER) holding one constant isotropic media sampled by method 3
+// (MediaFunction::ComputeMedia, source/core/material/media.cpp:287-364).
+struct __align__(16) DevMedia {
+    float4 emission;     // rgb, AA_Threshold
+    float4 scattering;   // rgb, 1 when any channel scatters
+    float4 extinction;   // rgb (absorption + scattering), -
+    int4   n;            // Intervals, sub-intervals (Min_Samples+1)/2, AA_Level, box index
+};
+constexpr int BOX_CONTAINER = 2;         // DevBox flag: surface of a media container
+constexpr int OBJ_CONTAINER = 1 << 30;   // ObjectShade flag; container index in bits 16..23
+constexpr int MAX_CONTAINERS = 8;
+constexpr int MEDIA_MAX_INTERVALS = 32;  // Intervals the GPU path holds per ray segment
+constexpr int MEDIA_MAX_AA_LEVEL = 6;
+
+// Per-ray state of a wavefront queue in scenes with media containers: the
+// ray's trace level (bits 0..7) and the container it travels in, plus one
+// (bits 8..15; 0 = none).  Transmitted rays keep their parent's level.
+__host__ __device__ __forceinline__ int ray_state(int level, int medium) { return level | ((medium + 1) << 8); }
+__host__ __device__ __forceinline__ int state_level(int s) { return s & 0xff; }
+__host__ __device__ __forceinline__ int state_medium(int s) { return ((s >> 8) & 0xff) - 1; }
 
 struct DeviceScene {
     const BvhNode*  nodes;
@@ -149,6 +171,9 @@ struct DeviceScene {
     const DevLight*    lights;
     int32_t         num_lights;
     int32_t         num_area_lights;
+    // media containers
+    const DevMedia* medias;         // one per container
+    int32_t         num_containers;
     int32_t         max_trace_level;
     float           adc_bailout;
     float4          background;
@@ -240,6 +265,15 @@ struct ShadeRad {
     int32_t   gather;
 };
 
+// What the level loop does for media containers (all null without them):
+// per-ray state of the current and next queue, and the medium each shadow
+// ray starts in.
+struct ShadeMedia {
+    const int32_t* q_state;
+    int32_t*       nq_state;
+    int32_t*       sq_medium;
+};
+
 // Device error word bits.
 enum DevError : uint32_t {
     DE_STACK_OVERFLOW = 1u,
@@ -255,6 +289,8 @@ enum StatIdx {
     ST_SHADOW_SUCCEEDED = 2,
     ST_REFLECTED = 3,
     ST_SAMPLES = 4,
+    ST_TRANSMITTED = 5,
+    ST_MEDIA_SAMPLES = 6,
     ST_COUNT = 8,
 };
 

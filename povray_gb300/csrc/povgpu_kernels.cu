@@ -53,6 +53,7 @@ __device__ __forceinline__ float3 operator+(float3 a, float3 b) { return f3(a.x 
 __device__ __forceinline__ float3 operator-(float3 a, float3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
 __device__ __forceinline__ float3 operator*(float3 a, float s) { return f3(a.x * s, a.y * s, a.z * s); }
 __device__ __forceinline__ float3 operator*(float3 a, float3 b) { return f3(a.x * b.x, a.y * b.y, a.z * b.z); }
+__device__ __forceinline__ float3 operator/(float3 a, float s) { return f3(a.x / s, a.y / s, a.z / s); }
 __device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 __device__ __forceinline__ float3 cross3(float3 a, float3 b)
 {
@@ -608,6 +609,10 @@ __device__ __forceinline__ bool prim_test(const DeviceScene& S, uint32_t ref, fl
     }
     if (kind == PK_BOX) {
         const DevBox b = S.boxes[idx];
+        // a media container's surface passes light: shadow rays cross it
+        // (shadow_through counts and attenuates the crossings)
+        if (ANY && (__float_as_int(b.hi.w) & BOX_CONTAINER))
+            return false;
         float tn, tf;
         int sn, sf;
         if (!box_roots(b, o, d, tn, tf, sn, sf))
@@ -872,11 +877,12 @@ __global__ void __launch_bounds__(128) k_shade(
     uint2* __restrict__ sq_skip, QRay* __restrict__ nq, int* __restrict__ nq_path,
     uint2* __restrict__ nq_skip, int* __restrict__ nq_count, int max_queue,
     int max_shadow, QRay* __restrict__ aq, int* __restrict__ aq_slot, uint2* __restrict__ aq_skip,
-    int* __restrict__ aq_count, int max_area, ShadeRad rad, uint32_t* err, unsigned long long* stats)
+    int* __restrict__ aq_count, int max_area, ShadeRad rad, ShadeMedia med, uint32_t* err,
+    unsigned long long* stats)
 {
     const int n = min(*q_count, max_queue);
     const int nl = S.num_lights;
-    unsigned long long c_rays = 0, c_refl = 0, c_shadow = 0;
+    unsigned long long c_rays = 0, c_refl = 0, c_shadow = 0, c_trans = 0;
     for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         int i = base + threadIdx.x;
         bool active = i < n;
@@ -886,6 +892,10 @@ __global__ void __launch_bounds__(128) k_shade(
         QRay r = q[i];
         QHit h = hits[i];
         int path = q_path ? q_path[i] : i;
+        // the ray's own trace level and medium (scenes with media containers)
+        const int rstate = med.q_state ? med.q_state[i] : ray_state(level, -1);
+        const int lvl = state_level(rstate);
+        const int medium = state_medium(rstate);
         float3 o = xyz(r.org), d = xyz(r.dir);
         PathState ps = paths[path];
         float3 thr = xyz(ps.throughput);
@@ -897,10 +907,12 @@ __global__ void __launch_bounds__(128) k_shade(
         const DevMaterial* m = nullptr;
         int oflags = 0;
         uint2 self = make_uint2(h.prim, skip_aux(h));
+        bool container = false;
         if (hit) {
             SurfaceInfo si = surface(S, h, p);
             ObjectShade os = S.objects[si.object];
             oflags = os.flags;
+            container = (oflags & OBJ_CONTAINER) != 0;
             m = S.materials + os.material;
             N = si.normal;
             if (oflags & 1)            // INVERTED_FLAG
@@ -909,16 +921,19 @@ __global__ void __launch_bounds__(128) k_shade(
                 N = N * -1.0f;
             float4 pig = m->pigment;
             float4 em = m->emission;
-            col = f3(pig.x * em.x, pig.y * em.y, pig.z * em.z);
+            col = container ? f3(0.f, 0.f, 0.f) : f3(pig.x * em.x, pig.y * em.y, pig.z * em.z);
         } else {
             col = xyz(S.background);   // ComputeSky, background only
         }
         // radiosity ambient query (ComputeLightedTexture, trace.cpp:896-921):
         // the largest possible contribution (pigment greyscale * Diffuse)
         // must beat the ray's ADC bailout
+        // a media container's surface only transmits: ComputeRefraction with
+        // equal iors traces the continued ray (trace.cpp:1343-1400)
+        const bool shaded = hit && !container;
         bool rq_emit = false;
         float rq_maxc = 0.f;
-        if (hit && rad.rq) {
+        if (shaded && rad.rq) {
             float3 pg = xyz(m->pigment);
             rq_maxc = (0.297f * pg.x + 0.589f * pg.y + 0.114f * pg.z) * m->diffuse_raw;
             rq_emit = rq_maxc > rad.adc;
@@ -948,7 +963,7 @@ __global__ void __launch_bounds__(128) k_shade(
             float3 ld = f3(0.f, 0.f, 1.f);
             float ldist = 0.f;
             bool area = false;
-            if (hit) {
+            if (shaded) {
                 const DevLight& L = S.lights[l];
                 // the radiosity Trace runs with area lights off
                 // (GetRadiosityQualityFlags, radiosity.cpp:148-161)
@@ -1009,6 +1024,8 @@ __global__ void __launch_bounds__(128) k_shade(
                     sq[slot] = sr;
                     sq_slot[slot] = i * nl + l;
                     sq_skip[slot] = self;
+                    if (med.sq_medium)
+                        med.sq_medium[slot] = medium;
                 } else {
                     set_error(err, DE_QUEUE_OVERFLOW);
                 }
@@ -1022,7 +1039,7 @@ __global__ void __launch_bounds__(128) k_shade(
         float3 reflec = f3(0.f, 0.f, 0.f);
         float rweight = 0.f;
         float3 nd = f3(0.f, 0.f, 1.f);
-        if (hit && m->has_reflection && !rad.gather) {
+        if (shaded && m->has_reflection && !rad.gather) {
             float cos_inc = -dot3(d, N);
             float falloff = m->reflect.w;
             float frac = fabsf(falloff - 1.0f) > EPSILON_F ? powf(1.0f - cos_inc, falloff) : 1.0f - cos_inc;
@@ -1038,19 +1055,35 @@ __global__ void __launch_bounds__(128) k_shade(
                 // fix-ups of ComputeReflection never trigger
                 float n2 = -2.0f * dot3(d, N);
                 nd = normalize3(d + N * n2);
-                refl = (level + 1 < max_level) && (rweight >= rad.adc);
+                refl = (lvl + 1 < max_level) && (rweight >= rad.adc);
             }
         }
-        int rs = warp_reserve(nq_count, refl, mask);
-        if (refl) {
+        // transmitted ray through a container wall: counted like any traced
+        // ray, at the parent's trace level (TraceRay with continuedRay,
+        // trace.cpp:155-160), entering or leaving the container's interior
+        bool cont = false;
+        int cont_medium = -1;
+        if (container) {
+            c_rays++;
+            c_trans++;
+            cont = lvl + 1 < max_level;
+            const int c = (oflags >> 16) & 0xff;
+            cont_medium = medium == c ? -1 : c;
+        }
+        int rs = warp_reserve(nq_count, refl || cont, mask);
+        if (refl || cont) {
             if (rs < max_queue) {
                 QRay rr;
                 rr.org = make_float4(p.x, p.y, p.z, kMinIsectDepth);
-                rr.dir = make_float4(nd.x, nd.y, nd.z, CUDART_INF_F);
+                rr.dir = refl ? make_float4(nd.x, nd.y, nd.z, CUDART_INF_F) : make_float4(d.x, d.y, d.z, CUDART_INF_F);
                 nq[rs] = rr;
                 nq_path[rs] = path;
                 nq_skip[rs] = self;
-                paths[path].throughput = make_float4(thr.x * reflec.x, thr.y * reflec.y, thr.z * reflec.z, rweight);
+                if (med.nq_state)
+                    med.nq_state[rs] = refl ? ray_state(lvl + 1, medium) : ray_state(lvl, cont_medium);
+                if (refl)
+                    paths[path].throughput =
+                        make_float4(thr.x * reflec.x, thr.y * reflec.y, thr.z * reflec.z, rweight);
             } else {
                 set_error(err, DE_QUEUE_OVERFLOW);
             }
@@ -1063,8 +1096,10 @@ __global__ void __launch_bounds__(128) k_shade(
         c_rays += __shfl_down_sync(0xffffffffu, c_rays, off);
         c_refl += __shfl_down_sync(0xffffffffu, c_refl, off);
         c_shadow += __shfl_down_sync(0xffffffffu, c_shadow, off);
+        c_trans += __shfl_down_sync(0xffffffffu, c_trans, off);
     }
     if ((threadIdx.x & 31) == 0) {
+        if (c_trans) atomicAdd(&stats[ST_TRANSMITTED], c_trans);
         if (c_rays) atomicAdd(&stats[ST_RAYS], c_rays);
         if (c_refl) atomicAdd(&stats[ST_REFLECTED], c_refl);
         if (c_shadow) atomicAdd(&stats[ST_SHADOW_TESTS], c_shadow);
@@ -1250,6 +1285,402 @@ __global__ void __launch_bounds__(128) k_area_shadow(DeviceScene S, const QRay* 
     if ((threadIdx.x & 31) == 0) {
         if (c_tests) atomicAdd(&stats[ST_SHADOW_TESTS], c_tests);
         if (c_blocked) atomicAdd(&stats[ST_SHADOW_SUCCEEDED], c_blocked);
+    }
+}
+
+// a[i] = value for the first min(*count, cap) entries
+__global__ void k_fill_int(int* __restrict__ a, const int* __restrict__ count, int cap, int value)
+{
+    const int n = min(*count, cap);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        a[i] = value;
+}
+
+cudaError_t launch_fill_int(int* a, const int* count, int cap, int value, int grid, cudaStream_t st)
+{
+    k_fill_int<<<grid, 128, 0, st>>>(a, count, cap, value);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------ media containers --
+// Shadow ray from P towards a point light at ray distance tmax +
+// SHADOW_TOLERANCE, through media containers (Trace::TracePointLightShadowRay,
+// trace.cpp:1951-2076, with the media term of ComputeShadowColour,
+// trace.cpp:2429-2433, and the interior toggle of ComputeShadowMedia,
+// trace.cpp:3064-3066).  The reference takes the nearest intersection
+// first; a container wall is a transparent hit -- one test and one success
+// -- after which the shadow ray goes on from the wall.  A ray that was
+// inside the container has its light attenuated by the constant media of
+// the crossed segment, exp(-extinction * length), one media sample
+// (media.cpp:366-398).  Walls are found from the containers' boxes, opaque
+// blockers by an any-hit test of each segment between walls (the any-hit
+// test passes container walls).  Counts the tests, successes and media
+// samples; returns true when the light is blocked.
+template <bool FULL>
+__device__ bool shadow_through(const DeviceScene& S, float3 P, float3 d, float tmin, float tmax, uint2 skip,
+                               int medium, bool media_on, float3& atten, int* smem, int stack_depth,
+                               uint32_t* err, unsigned long long& tests, unsigned long long& succ,
+                               unsigned long long& msamples)
+{
+    float et[2 * MAX_CONTAINERS];
+    int ec[2 * MAX_CONTAINERS];
+    int ne = 0;
+    for (int c = 0; c < S.num_containers; c++) {
+        float tb[2];
+        int sn, sf;
+        if (!box_roots(S.boxes[S.medias[c].n.w], P, d, tb[0], tb[1], sn, sf))
+            continue;
+        for (int e = 0; e < 2; e++) {
+            float t = tb[e];
+            if (!(t > SMALL_TOLERANCE_F && t < tmax))
+                continue;
+            int k = ne++;
+            while (k > 0 && et[k - 1] > t) {   // insertion in distance order
+                et[k] = et[k - 1];
+                ec[k] = ec[k - 1];
+                k--;
+            }
+            et[k] = t;
+            ec[k] = c;
+        }
+    }
+    float seg0 = tmin;    // the current shadow ray's first accepted distance
+    float org_t = 0.0f;   // where the current shadow ray starts (P or the last wall)
+    int k = 0;
+    for (;;) {
+        while (k < ne && et[k] <= seg0)   // walls within the new origin's tolerance
+            k++;
+        tests++;
+        const float seg1 = k < ne ? et[k] : tmax;
+        if (occluded<FULL>(S, P, d, seg0, seg1, skip, smem, stack_depth, err)) {
+            succ++;
+            return true;
+        }
+        if (k >= ne)
+            return false;
+        succ++;
+        if (medium >= 0 && media_on) {
+            const float3 ext = xyz(S.medias[medium].extinction);
+            const float len = et[k] - org_t;
+            msamples++;
+            atten = f3(atten.x * expf(-ext.x * len), atten.y * expf(-ext.y * len), atten.z * expf(-ext.z * len));
+        }
+        medium = medium == ec[k] ? -1 : ec[k];
+        org_t = et[k];
+        seg0 = et[k] + SMALL_TOLERANCE_F;
+        k++;
+    }
+}
+
+// Shadow rays of the shading kernel in scenes with media containers: each
+// ray's blocked byte, and its light term scaled by the media it crossed.
+// The shading kernel counted each ray's first test.
+template <bool FULL>
+__global__ void __launch_bounds__(128) k_shadow_through(DeviceScene S, const QRay* __restrict__ sq,
+                                                        const int* __restrict__ sq_slot,
+                                                        const uint2* __restrict__ sq_skip,
+                                                        const int* __restrict__ sq_medium,
+                                                        const int* __restrict__ sq_count, int cap,
+                                                        uint8_t* __restrict__ blocked,
+                                                        float4* __restrict__ slot_contrib, int media_on,
+                                                        int stack_depth, uint32_t* err, unsigned long long* stats)
+{
+    extern __shared__ int smem[];
+    const int n = min(*sq_count, cap);
+    unsigned long long c_tests = 0, c_succ = 0, c_ms = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const QRay r = sq[i];
+        float3 atten = f3(1.f, 1.f, 1.f);
+        unsigned long long t = 0;
+        const bool b = shadow_through<FULL>(S, xyz(r.org), xyz(r.dir), r.org.w, r.dir.w, sq_skip[i], sq_medium[i],
+                                            media_on != 0, atten, smem, stack_depth, err, t, c_succ, c_ms);
+        c_tests += t - 1;
+        blocked[i] = b ? 1 : 0;
+        if (!b && (atten.x != 1.f || atten.y != 1.f || atten.z != 1.f)) {
+            const int slot = sq_slot[i];
+            float4 c = slot_contrib[slot];
+            slot_contrib[slot] = make_float4(c.x * atten.x, c.y * atten.y, c.z * atten.z, c.w);
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        c_tests += __shfl_down_sync(0xffffffffu, c_tests, off);
+        c_succ += __shfl_down_sync(0xffffffffu, c_succ, off);
+        c_ms += __shfl_down_sync(0xffffffffu, c_ms, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (c_tests) atomicAdd(&stats[ST_SHADOW_TESTS], c_tests);
+        if (c_succ) atomicAdd(&stats[ST_SHADOW_SUCCEEDED], c_succ);
+        if (c_ms) atomicAdd(&stats[ST_MEDIA_SAMPLES], c_ms);
+    }
+}
+
+// Rays of the level queue that crossed a container's interior up to their
+// hit: their queue indices, in queue order.
+__global__ void k_media_list(const int* __restrict__ q_state, const QHit* __restrict__ hits,
+                             const int* __restrict__ q_count, int cap, int* __restrict__ mlist,
+                             int* __restrict__ mcount)
+{
+    const int n = min(*q_count, cap);
+    for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const int i = base + threadIdx.x;
+        const bool in = i < n && state_medium(q_state[i]) >= 0 && hits[i].prim != NO_PRIM;
+        const unsigned mask = __ballot_sync(0xffffffffu, i < n);
+        if (i >= n)
+            continue;
+        const int slot = warp_reserve(mcount, in, mask);
+        if (in)
+            mlist[slot] = i;
+    }
+}
+
+struct MediaSeg {
+    float3 O, D;
+    int    medium;
+    const DevMedia* md;
+};
+
+// One media sample (MediaFunction::ComputeOneMediaSample, media.cpp:935-1038,
+// sample method 3, constant density) at fraction f of the interval
+// [s0, s0 + ds]: emission plus, where the point lies in the lit span
+// [0, lit] of the point lights (ComputeOneMediaLightInterval,
+// media.cpp:715-750; lit < 0: an unlit interval), the scattered light of
+// every light not in shadow (TestShadow, trace.cpp:3173-3203; isotropic
+// phase, ComputeMediaScatteringAttenuation), times ds; the optical depth
+// estimate extinction * ds.
+template <bool FULL>
+__device__ void media_point(const DeviceScene& S, const MediaSeg& g, double s0, double ds, double f, double lit,
+                            float3& C, float3& od, int* smem, int stack_depth, uint32_t* err,
+                            unsigned long long& tests, unsigned long long& succ, unsigned long long& ms)
+{
+    const double x = s0 + f * ds;
+    const float3 P = g.O + g.D * (float)x;
+    ms++;
+    float3 em = xyz(g.md->emission);
+    if (lit >= 0.0 && x >= 0.0 && x <= lit && g.md->scattering.w != 0.0f) {
+        const float3 sc = xyz(g.md->scattering);
+        for (int l = 0; l < S.num_lights; l++) {
+            const DevLight& L = S.lights[l];
+            float3 lc = xyz(L.colour);
+            if (fabsf(lc.x) < EPSILON_F && fabsf(lc.y) < EPSILON_F && fabsf(lc.z) < EPSILON_F)
+                continue;
+            float3 lv = xyz(L.center) - P;
+            float ldist = sqrtf(dot3(lv, lv));
+            float3 ld = lv * (1.0f / ldist);
+            float3 atten = f3(1.f, 1.f, 1.f);
+            if (shadow_through<FULL>(S, P, ld, __uint_as_float(__float_as_uint(SMALL_TOLERANCE_F) + 1u),
+                                     ldist - SHADOW_TOLERANCE_F, make_uint2(NO_PRIM, 0u), g.medium, true, atten,
+                                     smem, stack_depth, err, tests, succ, ms))
+                continue;
+            em = em + sc * (lc * atten);
+        }
+    }
+    const float dsf = (float)ds;
+    C = em * dsf;
+    od = xyz(g.md->extinction) * dsf;
+}
+
+__device__ __forceinline__ float col3_dist(float3 a, float3 b)   // ColourDistance
+{
+    return fabsf(a.x - b.x) + fabsf(a.y - b.y) + fabsf(a.z - b.z);
+}
+
+// MediaFunction::ComputeOneMediaSampleRecursive (media.cpp:1040-1125, jitter
+// 0) as a depth-first frame stack: the midpoint sample of [d1, d3], then the
+// halves whose end colours differ by more than the threshold, down to
+// `depth` levels; R and ODR weight the samples as the reference does.
+struct MediaFrame {
+    double d1, d3;
+    float3 C1, C3, C2, od1, od3, od2, R, ODR;
+    int depth, stage;
+};
+
+template <bool FULL>
+__device__ void media_subdivide(const DeviceScene& S, const MediaSeg& g, double s0, double ds, double lit, double d1,
+                                double d3, float3 C1, float3 C3, float3 od1, float3 od3, int depth, float3& R,
+                                float3& ODR, int* smem, int stack_depth, uint32_t* err, unsigned long long& tests,
+                                unsigned long long& succ, unsigned long long& ms)
+{
+    const float thr = g.md->emission.w;
+    MediaFrame st[MEDIA_MAX_AA_LEVEL];
+    int sp = 0;
+    st[0].d1 = d1; st[0].d3 = d3; st[0].C1 = C1; st[0].C3 = C3; st[0].od1 = od1; st[0].od3 = od3;
+    st[0].depth = depth; st[0].stage = 0;
+    float3 rR = f3(0.f, 0.f, 0.f), rO = f3(0.f, 0.f, 0.f);   // the last finished frame's result
+    for (;;) {
+        MediaFrame& f = st[sp];
+        bool done = false;
+        if (f.stage == 0) {
+            media_point<FULL>(S, g, s0, ds, 0.5 * (f.d1 + f.d3), lit, f.C2, f.od2, smem, stack_depth, err, tests, succ,
+                              ms);
+            if (f.depth <= 0) {
+                rR = (f.C1 + f.C2 + f.C3) / 3.0f;
+                rO = (f.od1 + f.od2 + f.od3) / 3.0f;
+                f.R = rR;
+                f.ODR = rO;
+                done = true;
+            } else if (col3_dist(f.C1, f.C2) > thr && sp + 1 < MEDIA_MAX_AA_LEVEL) {
+                f.stage = 1;
+                MediaFrame& c = st[++sp];
+                c.d1 = f.d1; c.d3 = 0.5 * (f.d1 + f.d3); c.C1 = f.C1; c.C3 = f.C2; c.od1 = f.od1; c.od3 = f.od2;
+                c.depth = f.depth - 1; c.stage = 0;
+                continue;
+            } else {
+                f.R = f.C1 / 3.0f + f.C2 / 6.0f;
+                f.ODR = f.od1 / 3.0f + f.od2 / 6.0f;
+                f.stage = 2;
+            }
+        } else if (f.stage == 1) {   // first half returned
+            f.R = rR / 2.0f;
+            f.ODR = rO / 2.0f;
+            f.stage = 2;
+        } else if (f.stage == 3) {   // second half returned
+            f.R = f.R + rR / 2.0f;
+            f.ODR = f.ODR + rO / 2.0f;
+            done = true;
+        }
+        if (!done && f.stage == 2) {
+            if (col3_dist(f.C2, f.C3) > thr && sp + 1 < MEDIA_MAX_AA_LEVEL) {
+                f.stage = 3;
+                MediaFrame& c = st[++sp];
+                c.d1 = 0.5 * (f.d1 + f.d3); c.d3 = f.d3; c.C1 = f.C2; c.C3 = f.C3; c.od1 = f.od2; c.od3 = f.od3;
+                c.depth = f.depth - 1; c.stage = 0;
+                continue;
+            }
+            f.R = f.R + (f.C2 / 6.0f + f.C3 / 3.0f);
+            f.ODR = f.ODR + (f.od2 / 6.0f + f.od3 / 3.0f);
+            done = true;
+        }
+        if (done) {
+            rR = f.R;
+            rO = f.ODR;
+            if (sp == 0)
+                break;
+            sp--;
+        }
+    }
+    R = rR;
+    ODR = rO;
+}
+
+// Interval layout of one segment (ComputeMediaSampleInterval,
+// media.cpp:527-596, and the padding of ComputeMedia, media.cpp:346-352):
+// with a light, `intervals` equal intervals of [0, dist]; when rounding
+// leaves the last end short of dist, one unlit interval up to dist.
+// Without lights, constant media is one unlit interval.
+__device__ __forceinline__ int media_intervals(const DevMedia& md, bool lit, double dist, double& delta, int& nuni)
+{
+    nuni = lit ? max(md.n.x, 1) : 1;
+    delta = dist / (double)nuni;
+    return nuni + ((lit && delta * (double)nuni < dist) ? 1 : 0);
+}
+
+// One thread per (listed ray, interval): the interval's adaptive samples
+// (ComputeMediaAdaptiveSampling, media.cpp:432-525) -- its emission te and
+// optical depth od sums before the 1/samples normalisation.
+template <bool FULL>
+__global__ void __launch_bounds__(128) k_media(DeviceScene S, const QRay* __restrict__ q,
+                                               const int* __restrict__ q_state, const QHit* __restrict__ hits,
+                                               const int* __restrict__ mlist, const int* __restrict__ mcount,
+                                               int mcap, int NI, float4* __restrict__ te_out,
+                                               float4* __restrict__ od_out, int stack_depth, uint32_t* err,
+                                               unsigned long long* stats)
+{
+    extern __shared__ int smem[];
+    const long long items = (long long)min(*mcount, mcap) * NI;
+    unsigned long long c_tests = 0, c_succ = 0, c_ms = 0;
+    const bool lit = S.num_lights > 0;
+    for (long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x; it < items;
+         it += (long long)gridDim.x * blockDim.x) {
+        const int j = (int)(it / NI), iv = (int)(it % NI);
+        const int i = mlist[j];
+        const QRay r = q[i];
+        MediaSeg g;
+        g.O = xyz(r.org);
+        g.D = xyz(r.dir);
+        g.medium = state_medium(q_state[i]);
+        g.md = S.medias + g.medium;
+        const double dist = (double)hits[i].t;
+        double delta;
+        int nuni;
+        const int nint = media_intervals(*g.md, lit, dist, delta, nuni);
+        float3 te = f3(0.f, 0.f, 0.f), odi = f3(0.f, 0.f, 0.f);
+        if (iv < nint) {
+            const double s0 = delta * (double)iv;
+            const double ds = iv < nuni ? delta : dist - delta * (double)nuni;
+            const double litend = (lit && iv < nuni) ? dist : -1.0;
+            const int sub = g.md->n.y;
+            const double dd = 1.0 / (double)sub;
+            const float ddf = (float)dd;
+            float3 C0, od0, C1, od1, R, ODR;
+            media_point<FULL>(S, g, s0, ds, 0.0, litend, C0, od0, smem, stack_depth, err, c_tests, c_succ, c_ms);
+            double d0 = 0.0;
+            for (int k = 1; k <= sub; k++) {
+                const double d1 = d0 + dd;
+                media_point<FULL>(S, g, s0, ds, d1, litend, C1, od1, smem, stack_depth, err, c_tests, c_succ, c_ms);
+                media_subdivide<FULL>(S, g, s0, ds, litend, d0, d1, C0, C1, od0, od1, g.md->n.z - 1, R, ODR, smem,
+                                      stack_depth, err, c_tests, c_succ, c_ms);
+                // attenuation by the earlier sub-intervals, then by this one's
+                // own depth (media.cpp:470-487)
+                R = f3(R.x * expf(-odi.x * ddf), R.y * expf(-odi.y * ddf), R.z * expf(-odi.z * ddf));
+                if (ODR.x != 0.0f) R.x *= (1.0f - expf(-ODR.x * ddf)) / (ODR.x * ddf);
+                if (ODR.y != 0.0f) R.y *= (1.0f - expf(-ODR.y * ddf)) / (ODR.y * ddf);
+                if (ODR.z != 0.0f) R.z *= (1.0f - expf(-ODR.z * ddf)) / (ODR.z * ddf);
+                te = te + R;
+                odi = odi + ODR;
+                C0 = C1;
+                od0 = od1;
+                d0 = d1;
+            }
+        }
+        te_out[it] = make_float4(te.x, te.y, te.z, 0.f);
+        od_out[it] = make_float4(odi.x, odi.y, odi.z, 0.f);
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        c_tests += __shfl_down_sync(0xffffffffu, c_tests, off);
+        c_succ += __shfl_down_sync(0xffffffffu, c_succ, off);
+        c_ms += __shfl_down_sync(0xffffffffu, c_ms, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (c_tests) atomicAdd(&stats[ST_SHADOW_TESTS], c_tests);
+        if (c_succ) atomicAdd(&stats[ST_SHADOW_SUCCEEDED], c_succ);
+        if (c_ms) atomicAdd(&stats[ST_MEDIA_SAMPLES], c_ms);
+    }
+}
+
+// One thread per listed ray: the intervals in order (ComputeMediaColour,
+// media.cpp:527-545 of the interval sums) give the segment's emission Te and
+// transmittance exp(-Od); what the ray's hit adds to its path is seen through
+// the media, so the path takes Te at its current throughput and continues
+// with throughput * exp(-Od).
+__global__ void k_media_combine(const int* __restrict__ q_state, const int* __restrict__ q_path,
+                                const QHit* __restrict__ hits, const int* __restrict__ mlist,
+                                const int* __restrict__ mcount, int mcap, int NI, const DeviceScene S,
+                                const float4* __restrict__ te_in, const float4* __restrict__ od_in,
+                                PathState* __restrict__ paths)
+{
+    const int n = min(*mcount, mcap);
+    const bool lit = S.num_lights > 0;
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const int i = mlist[j];
+        const DevMedia& md = S.medias[state_medium(q_state[i])];
+        double delta;
+        int nuni;
+        const int nint = media_intervals(md, lit, (double)hits[i].t, delta, nuni);
+        const float nrm = (float)(1.0 / (double)md.n.y);
+        float3 Te = f3(0.f, 0.f, 0.f), Od = f3(0.f, 0.f, 0.f);
+        for (int iv = 0; iv < nint; iv++) {
+            const float4 te = te_in[(size_t)j * NI + iv];
+            const float4 od = od_in[(size_t)j * NI + iv];
+            Te = Te + f3(te.x * nrm * expf(-Od.x), te.y * nrm * expf(-Od.y), te.z * nrm * expf(-Od.z));
+            Od = Od + f3(od.x, od.y, od.z) * nrm;
+        }
+        const int path = q_path ? q_path[i] : i;
+        PathState ps = paths[path];
+        const float3 thr = xyz(ps.throughput);
+        ps.colour = make_float4(ps.colour.x + thr.x * Te.x, ps.colour.y + thr.y * Te.y, ps.colour.z + thr.z * Te.z,
+                                ps.colour.w);
+        ps.throughput = make_float4(thr.x * expf(-Od.x), thr.y * expf(-Od.y), thr.z * expf(-Od.z), ps.throughput.w);
+        paths[path] = ps;
     }
 }
 
@@ -1564,12 +1995,46 @@ cudaError_t launch_shade(const DeviceScene& S, int level, int max_level, const Q
                          const int* q_count, PathState* paths, float4* slot_contrib, QRay* sq, int* sq_slot,
                          int* sq_count, uint2* sq_skip, QRay* nq, int* nq_path, uint2* nq_skip, int* nq_count,
                          int max_queue, int max_shadow, QRay* aq, int* aq_slot, uint2* aq_skip, int* aq_count,
-                         int max_area, const ShadeRad& rad, int grid, uint32_t* err, unsigned long long* stats,
-                         cudaStream_t st)
+                         int max_area, const ShadeRad& rad, const ShadeMedia& med, int grid, uint32_t* err,
+                         unsigned long long* stats, cudaStream_t st)
 {
     k_shade<<<grid, 128, 0, st>>>(S, level, max_level, q, q_path, hits, q_count, paths, slot_contrib, sq, sq_slot, sq_count,
                                   sq_skip, nq, nq_path, nq_skip, nq_count, max_queue, max_shadow, aq, aq_slot,
-                                  aq_skip, aq_count, max_area, rad, err, stats);
+                                  aq_skip, aq_count, max_area, rad, med, err, stats);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_shadow_through(const DeviceScene& S, const QRay* sq, const int* sq_slot, const uint2* sq_skip,
+                                  const int* sq_medium, const int* sq_count, int cap, uint8_t* blocked,
+                                  float4* slot_contrib, bool media_on, int stack_depth, int grid, uint32_t* err,
+                                  unsigned long long* stats, cudaStream_t st)
+{
+    const int block = 128;
+    size_t smem = (size_t)stack_depth * block * sizeof(int);
+    if (S.has_full_prims)
+        k_shadow_through<true><<<grid, block, smem, st>>>(S, sq, sq_slot, sq_skip, sq_medium, sq_count, cap, blocked,
+                                                          slot_contrib, media_on ? 1 : 0, stack_depth, err, stats);
+    else
+        k_shadow_through<false><<<grid, block, smem, st>>>(S, sq, sq_slot, sq_skip, sq_medium, sq_count, cap, blocked,
+                                                           slot_contrib, media_on ? 1 : 0, stack_depth, err, stats);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_media(const DeviceScene& S, const QRay* q, const int* q_state, const int* q_path, const QHit* hits,
+                         const int* q_count, int cap, int* mlist, int* mcount, int NI, float4* te, float4* od,
+                         PathState* paths, int stack_depth, int grid, uint32_t* err, unsigned long long* stats,
+                         cudaStream_t st)
+{
+    const int block = 128;
+    k_media_list<<<grid, block, 0, st>>>(q_state, hits, q_count, cap, mlist, mcount);
+    size_t smem = (size_t)stack_depth * block * sizeof(int);
+    if (S.has_full_prims)
+        k_media<true><<<grid, block, smem, st>>>(S, q, q_state, hits, mlist, mcount, cap, NI, te, od, stack_depth,
+                                                 err, stats);
+    else
+        k_media<false><<<grid, block, smem, st>>>(S, q, q_state, hits, mlist, mcount, cap, NI, te, od, stack_depth,
+                                                  err, stats);
+    k_media_combine<<<grid, block, 0, st>>>(q_state, q_path, hits, mlist, mcount, cap, NI, S, te, od, paths);
     return cudaGetLastError();
 }
 

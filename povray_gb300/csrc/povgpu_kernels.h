@@ -21,7 +21,21 @@ cudaError_t launch_shade(const DeviceScene& S, int level, int max_level, const Q
                          const int* q_count, PathState* paths, float4* slot_contrib, QRay* sq, int* sq_slot,
                          int* sq_count, uint2* sq_skip, QRay* nq, int* nq_path, uint2* nq_skip, int* nq_count,
                          int max_queue, int max_shadow, QRay* aq, int* aq_slot, uint2* aq_skip, int* aq_count,
-                         int max_area, const ShadeRad& rad, int grid, uint32_t* err, unsigned long long* stats,
+                         int max_area, const ShadeRad& rad, const ShadeMedia& med, int grid, uint32_t* err,
+                         unsigned long long* stats, cudaStream_t st);
+cudaError_t launch_fill_int(int* a, const int* count, int cap, int value, int grid, cudaStream_t st);
+// Shadow rays through media containers (scenes with containers: replaces
+// the any-hit trace of the shadow queue).
+cudaError_t launch_shadow_through(const DeviceScene& S, const QRay* sq, const int* sq_slot, const uint2* sq_skip,
+                                  const int* sq_medium, const int* sq_count, int cap, uint8_t* blocked,
+                                  float4* slot_contrib, bool media_on, int stack_depth, int grid, uint32_t* err,
+                                  unsigned long long* stats, cudaStream_t st);
+// Media of the queue's rays inside containers, applied to their paths
+// before shading: lists the rays (mcount zeroed by the caller), samples
+// NI interval slots per ray, combines them in order.
+cudaError_t launch_media(const DeviceScene& S, const QRay* q, const int* q_state, const int* q_path, const QHit* hits,
+                         const int* q_count, int cap, int* mlist, int* mcount, int NI, float4* te, float4* od,
+                         PathState* paths, int stack_depth, int grid, uint32_t* err, unsigned long long* stats,
                          cudaStream_t st);
 cudaError_t launch_area_shadow(const DeviceScene& S, const QRay* aq, const int* aq_slot, const uint2* aq_skip,
                                const int* aq_count, int cap, float4* slot_contrib, int stack_depth, int grid,

@@ -37,13 +37,25 @@ def _load(case):
 def _counters_close(got, ref, frac=5e-4):
     """Counters agree up to grazing secondary rays: a reflection or shadow
     ray that skims a silhouette or a light terminator can land on either side
-    in FP32 vs the reference's FP64 (at most `frac` of the rays)."""
+    in FP32 vs the reference's FP64 (at most `frac` of the rays).
+
+    With media: the segment lengths the reference splits into intervals are
+    FP64 distances; where rounding leaves the last interval's end short of
+    the segment it pads one more interval (11 samples at 10 samples), so
+    which segments get the padding differs between FP32 and FP64 distances:
+    media samples within 1.5%; the samples' own shadow rays then move the
+    shadow counters by up to 1%."""
+    media = ref.get("media_samples", 0) > 0
+    if media:
+        frac = 1e-2
+        assert got["transmitted_rays"] == ref["transmitted_rays"], (got, ref)
+        assert abs(got["media_samples"] - ref["media_samples"]) <= 0.015 * ref["media_samples"], (got, ref)
     for k in ("number_of_rays", "reflected_rays", "shadow_ray_tests"):
         assert abs(got[k] - ref[k]) <= max(2, frac * ref[k]), (k, got, ref)
     assert abs(got["shadow_rays_succeeded"] - ref["shadow_rays_succeeded"]) <= \
         max(2, frac * ref["shadow_ray_tests"]), (got, ref)
     if not got.get("number_of_samples"):
-        assert got["number_of_rays"] == got["number_of_pixels"] + got["reflected_rays"]
+        assert got["number_of_rays"] == got["number_of_pixels"] + got["reflected_rays"] + got["transmitted_rays"]
 
 
 @pytest.mark.parametrize("case", sorted(CASES))
