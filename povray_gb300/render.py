@@ -105,7 +105,10 @@ class GpuScene:
             pre = self.radiosity_pretrace(blocks, p)
         rgbt, stats = self.trace_blocks(blocks, p)
         if pre is not None:
-            stats = {k: stats[k] + pre[k] if k != "device_error" else stats[k] | pre[k] for k in stats}
+            # counters add up; the error word and the network's held-out
+            # error (reported by both calls) do not
+            merge = {"device_error": lambda a, b: a | b, "nic_val_error_ppm": max}
+            stats = {k: merge.get(k, lambda a, b: a + b)(stats[k], pre[k]) for k in stats}
         return _scenes.unblock(rgbt, blocks, p.width, p.height), stats
 
     def set_stream(self, stream_handle):

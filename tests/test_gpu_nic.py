@@ -138,7 +138,7 @@ def test_gradient_matches_torch_autograd(data):
     mask[-NO + 3:] = False
     rel = np.linalg.norm(grad[mask] - ref[mask]) / np.linalg.norm(ref[mask])
     info = json.dumps(dict(rel=float(rel), loss=loss, ref_loss=float(L.detach())))
-    assert abs(loss / float(L) - 1) < 1e-3, info
+    assert abs(loss / float(L.detach()) - 1) < 1e-3, info
     assert rel <= 5e-2, info
 
 
