@@ -377,6 +377,9 @@ typedef struct PovGpuNeuralCache {
     float   learning_rate;
     float   gate;             /* largest held-out relative RMSE it may answer */
     uint32_t seed;            /* batch sampling                               */
+    int32_t shared;           /* 1: one network across pretraces (views): each
+                                 pretrace goes on training it from its current
+                                 weights and input bounds                      */
 } PovGpuNeuralCache;
 int pov_gpu_set_neural_cache(PovGpuScene* scene, const PovGpuNeuralCache* config);
 
@@ -404,6 +407,19 @@ void pov_gpu_scene_destroy(PovGpuScene* scene);
  * No reference counterpart: the reference has no device streams.
  */
 int pov_gpu_scene_set_stream(PovGpuScene* scene, void* cuda_stream);
+
+/*
+ * Replaces the view's camera without re-parsing or rebuilding the scene:
+ * the "camera changes without parsing" of View::StartRender
+ * (source/backend/scene/view.cpp:862-975, render option SceneCamera).
+ * `camera` holds location, direction, right and up before look_at; with
+ * `look_at` non-NULL the vectors are re-aimed as that code applies look_at,
+ * about `sky` (NULL = <0,1,0>).  Applies to the following trace calls; the
+ * BVH, materials and lights are shared by every view.  POV_GPU_E_INVALID
+ * when look_at equals the location, POV_GPU_E_UNSUPPORTED for a camera
+ * inside a media container.
+ */
+int pov_gpu_set_camera(PovGpuScene* scene, const PovGpuCamera* camera, const double* look_at, const double* sky);
 
 /* Pipeline stages reported by pov_gpu_get_timings. */
 #define POV_GPU_STAGE_CAMERA        0

@@ -147,7 +147,7 @@ class PovGpuStats(C.Structure):
 
 class PovGpuNeuralCache(C.Structure):
     _fields_ = [("enabled", C.c_int32), ("steps", C.c_int32), ("batch", C.c_int32),
-                ("learning_rate", C.c_float), ("gate", C.c_float), ("seed", C.c_uint32)]
+                ("learning_rate", C.c_float), ("gate", C.c_float), ("seed", C.c_uint32), ("shared", C.c_int32)]
 
 
 POV_GPU_NIC_PARAMS = 20752
@@ -185,7 +185,7 @@ EXPORTS = ["pov_gpu_scene_create", "pov_gpu_trace_blocks", "pov_gpu_trace_rays",
            "pov_gpu_scene_destroy", "pov_gpu_error_string", "pov_gpu_abi_version",
            "pov_gpu_scene_set_stream", "pov_gpu_set_profiling", "pov_gpu_get_timings",
            "pov_gpu_trace_rays_static", "pov_gpu_radiosity_pretrace", "pov_gpu_set_pretrace_jitter",
-           "pov_gpu_set_neural_cache", "pov_gpu_nic_eval"]
+           "pov_gpu_set_neural_cache", "pov_gpu_nic_eval", "pov_gpu_set_camera"]
 
 
 class PovGpuError(RuntimeError):
@@ -235,6 +235,8 @@ def load_library(path=None):
     lib.pov_gpu_error_string.restype = C.c_char_p
     lib.pov_gpu_abi_version.argtypes = []
     lib.pov_gpu_abi_version.restype = C.c_int
+    lib.pov_gpu_set_camera.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.pov_gpu_set_camera.restype = C.c_int
     lib.pov_gpu_scene_set_stream.argtypes = [C.c_void_p, C.c_void_p]
     lib.pov_gpu_scene_set_stream.restype = C.c_int
     lib.pov_gpu_set_profiling.argtypes = [C.c_void_p, C.c_int]

@@ -424,9 +424,10 @@ struct RadiosityState {
     // training passed its held-out gate
     PovGpuNeuralCache nic_cfg{};
     bool            nic_ok = false;
-    bool            nic_init = false;
     double          nic_val_error = 0.0;
     float3          nic_lo{}, nic_scale{};
+    bool            nic_init = false;   // shared network: weights, moments and bounds in place
+    int             nic_step = 0;       // Adam steps taken by the shared network
     DevBuf          nic_params, nic_wb, nic_m, nic_v, nic_grad, nic_loss, nic_idx, nic_pred, nic_err;
     void release()
     {
@@ -452,6 +453,7 @@ struct PovGpuScene {
     DevBuf spheres, spheres64, boxes64, sphere_obj, sphere_flags, planes, plane_obj, boxes, tori, csgs, csg_children, objects,
         materials, lights, medias;
     int    media_ni = 0;   // interval slots per media segment (0: no media containers)
+    std::vector<double> h_container_boxes;   // corners of the media containers, 6 per box
     // host copies of the id maps (prim -> flattened object id)
     std::vector<int32_t> h_sphere_obj, h_plane_obj, h_box_obj, h_torus_obj, h_tri_global, h_tri_local, h_tri_obj;
     std::vector<DevCsg> h_csgs;
@@ -1018,6 +1020,7 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
                 box = (int)b;
         if (box < 0)
             return POV_GPU_E_INVALID;
+        sc->h_container_boxes.insert(sc->h_container_boxes.end(), o.p, o.p + 6);
         DevMedia& m = medias[c];
         m.emission = make_float4(md.emission[0], md.emission[1], md.emission[2], md.aa_threshold);
         bool scat = md.scattering[0] != 0.0f || md.scattering[1] != 0.0f || md.scattering[2] != 0.0f;
@@ -1612,14 +1615,20 @@ int nic_train(PovGpuScene* sc)
     }
     if (train.size() < 256 || val.empty())
         return POV_GPU_OK;
-    float sc3[3];
-    for (int k = 0; k < 3; k++) {
-        float ext = std::max(hi[k] - lo[k], 1e-6f);
-        lo[k] -= 0.01f * ext;
-        sc3[k] = 2.0f / (1.02f * ext);
+    // a shared network keeps its weights, Adam moments and input bounds
+    // from the pretraces before (other views of the same scene)
+    const bool resume = cfg.shared && R.nic_init;
+    if (!resume) {
+        float sc3[3];
+        for (int k = 0; k < 3; k++) {
+            float ext = std::max(hi[k] - lo[k], 1e-6f);
+            lo[k] -= 0.01f * ext;
+            sc3[k] = 2.0f / (1.02f * ext);
+        }
+        R.nic_lo = make_float3(lo[0], lo[1], lo[2]);
+        R.nic_scale = make_float3(sc3[0], sc3[1], sc3[2]);
+        R.nic_step = 0;
     }
-    R.nic_lo = make_float3(lo[0], lo[1], lo[2]);
-    R.nic_scale = make_float3(sc3[0], sc3[1], sc3[2]);
     // parameters: He-uniform initialisation, zero biases, padded rows zero
     const size_t NP = (size_t)nic::NPARAM;
     CK(R.nic_params.ensure(sizeof(float) * NP));
@@ -1629,7 +1638,7 @@ int nic_train(PovGpuScene* sc)
     CK(R.nic_grad.ensure(sizeof(float) * NP));
     CK(R.nic_loss.ensure(sizeof(float)));
     CK(R.nic_err.ensure(sizeof(uint32_t)));
-    std::mt19937 rng(cfg.seed);
+    std::mt19937 rng(cfg.seed + (uint32_t)R.nic_step);
     std::vector<float> hp(NP, 0.0f);
     auto init = [&](int off, int rows, int cols, int live_rows) {
         std::uniform_real_distribution<float> u(-std::sqrt(6.0f / cols), std::sqrt(6.0f / cols));
@@ -1643,11 +1652,14 @@ int nic_train(PovGpuScene* sc)
     init(nic::P_W3, nic::HID, nic::HID, nic::HID);
     init(nic::P_W4, nic::HID, nic::HID, nic::HID);
     init(nic::P_W5, nic::NO, nic::HID, nic::NOUT);
-    CK(cudaMemcpyAsync(R.nic_params.p, hp.data(), sizeof(float) * NP, cudaMemcpyHostToDevice, st));
-    CK(cudaMemsetAsync(R.nic_m.p, 0, sizeof(float) * NP, st));
-    CK(cudaMemsetAsync(R.nic_v.p, 0, sizeof(float) * NP, st));
+    if (!resume) {
+        CK(cudaMemcpyAsync(R.nic_params.p, hp.data(), sizeof(float) * NP, cudaMemcpyHostToDevice, st));
+        CK(cudaMemsetAsync(R.nic_m.p, 0, sizeof(float) * NP, st));
+        CK(cudaMemsetAsync(R.nic_v.p, 0, sizeof(float) * NP, st));
+        CK(nic::launch_to_bf16(R.nic_params.as<float>(), R.nic_wb.as<__nv_bfloat16>(), st));
+        R.nic_init = true;
+    }
     CK(cudaMemsetAsync(R.nic_err.p, 0, sizeof(uint32_t), st));
-    CK(nic::launch_to_bf16(R.nic_params.as<float>(), R.nic_wb.as<__nv_bfloat16>(), st));
     // every step's batch, drawn up front
     const int steps = std::max(cfg.steps, 1), batch = std::max(cfg.batch, nic::TILE);
     std::vector<int> idx((size_t)steps * batch + val.size());
@@ -1674,8 +1686,10 @@ int nic_train(PovGpuScene* sc)
                              R.nic_loss.as<float>(), 1.0f / (float)batch, R.nic_err.as<uint32_t>(), sc->num_sms,
                              st));
         CK(nic::launch_adam(R.nic_params.as<float>(), R.nic_m.as<float>(), R.nic_v.as<float>(),
-                            R.nic_grad.as<float>(), R.nic_wb.as<__nv_bfloat16>(), cfg.learning_rate, s + 1, st));
+                            R.nic_grad.as<float>(), R.nic_wb.as<__nv_bfloat16>(), cfg.learning_rate,
+                            R.nic_step + s + 1, st));
     }
+    R.nic_step += steps;
     CK(clk.end(3 * steps));
     // held-out relative RMSE
     const int nv = (int)val.size();
@@ -1792,6 +1806,77 @@ int pov_gpu_scene_set_stream(PovGpuScene* sc, void* cuda_stream)
         return POV_GPU_E_INVALID;
     std::lock_guard<std::mutex> g(sc->lock);
     sc->user_stream = reinterpret_cast<cudaStream_t>(cuda_stream);
+    return POV_GPU_OK;
+}
+
+int pov_gpu_set_camera(PovGpuScene* sc, const PovGpuCamera* cam, const double* look_at, const double* sky)
+{
+    if (!sc || !cam)
+        return POV_GPU_E_INVALID;
+    if (cam->type != 0)
+        return POV_GPU_E_UNSUPPORTED;
+    double loc[3], dir[3], right[3], up[3];
+    for (int k = 0; k < 3; k++) {
+        loc[k] = cam->location[k];
+        dir[k] = cam->direction[k];
+        right[k] = cam->right[k];
+        up[k] = cam->up[k];
+    }
+    auto dot = [](const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; };
+    auto cross = [](const double* a, const double* b, double* o) {
+        double x = a[1] * b[2] - a[2] * b[1], y = a[2] * b[0] - a[0] * b[2], z = a[0] * b[1] - a[1] * b[0];
+        o[0] = x;
+        o[1] = y;
+        o[2] = z;
+    };
+    if (look_at) {
+        // View::StartRender applies look_at to the view camera
+        // (source/backend/scene/view.cpp:922-975): lengths and handedness
+        // kept, direction towards look_at, right from sky x direction
+        // (unchanged when degenerate), up = direction x right
+        const double sk[3] = {sky ? sky[0] : 0.0, sky ? sky[1] : 1.0, sky ? sky[2] : 0.0};
+        const double dlen = std::sqrt(dot(dir, dir)), ulen = std::sqrt(dot(up, up)), rlen = std::sqrt(dot(right, right));
+        double t[3];
+        cross(up, dir, t);
+        const double hand = dot(t, right);
+        for (int k = 0; k < 3; k++)
+            dir[k] = look_at[k] - loc[k];
+        if (dot(dir, dir) < EPSILON)
+            return POV_GPU_E_INVALID;   // location and look_at must differ
+        double l = std::sqrt(dot(dir, dir));
+        for (double& v : dir)
+            v /= l;
+        double r[3];
+        cross(sk, dir, r);
+        if (!(std::fabs(r[0]) < EPSILON && std::fabs(r[1]) < EPSILON && std::fabs(r[2]) < EPSILON))
+            for (int k = 0; k < 3; k++)
+                right[k] = r[k];
+        l = std::sqrt(dot(right, right));
+        for (double& v : right)
+            v /= l;
+        cross(dir, right, up);
+        for (int k = 0; k < 3; k++) {
+            dir[k] *= dlen;
+            right[k] *= hand > 0.0 ? rlen : -rlen;
+            up[k] *= ulen;
+        }
+    }
+    std::lock_guard<std::mutex> g(sc->lock);
+    // camera rays start outside every media container
+    for (size_t c = 0; c + 6 <= sc->h_container_boxes.size(); c += 6) {
+        const double* b = &sc->h_container_boxes[c];
+        bool inside = true;
+        for (int k = 0; k < 3; k++)
+            inside = inside && loc[k] >= std::min(b[k], b[3 + k]) && loc[k] <= std::max(b[k], b[3 + k]);
+        if (inside)
+            return POV_GPU_E_UNSUPPORTED;
+    }
+    for (int k = 0; k < 3; k++) {
+        sc->S.cam_loc[k] = loc[k];
+        sc->S.cam_dir[k] = dir[k];
+        sc->S.cam_right[k] = right[k];
+        sc->S.cam_up[k] = up[k];
+    }
     return POV_GPU_OK;
 }
 
@@ -2110,6 +2195,7 @@ int pov_gpu_set_neural_cache(PovGpuScene* sc, const PovGpuNeuralCache* cfg)
         return POV_GPU_E_INVALID;
     sc->rad.nic_cfg = *cfg;
     sc->rad.nic_ok = false;
+    sc->rad.nic_init = false;   // a new configuration starts a new network
     return POV_GPU_OK;
 }
 

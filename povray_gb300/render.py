@@ -81,12 +81,32 @@ class GpuScene:
                "pov_gpu_radiosity_pretrace")
         return stats.as_dict()
 
-    def set_neural_cache(self, enabled=True, steps=300, batch=4096, learning_rate=3e-3, gate=0.5, seed=1):
+    def set_neural_cache(self, enabled=True, steps=300, batch=4096, learning_rate=3e-3, gate=0.5, seed=1,
+                         shared=False):
         """Neural irradiance cache (pov_gpu_set_neural_cache): trained at the
         end of each pretrace; answers uncovered final-trace queries when its
-        held-out relative RMSE is at most `gate`."""
-        c = abi.PovGpuNeuralCache(int(enabled), int(steps), int(batch), float(learning_rate), float(gate), int(seed))
+        held-out relative RMSE is at most `gate`.  `shared`: one network for
+        all views, each pretrace training it further."""
+        c = abi.PovGpuNeuralCache(int(enabled), int(steps), int(batch), float(learning_rate), float(gate), int(seed),
+                                  int(shared))
         _check(self.lib.pov_gpu_set_neural_cache(self.h, C.byref(c)), "pov_gpu_set_neural_cache")
+
+    def set_camera(self, location, look_at, angle, width, height, sky=(0.0, 1.0, 0.0)):
+        """The view's camera (pov_gpu_set_camera): ``camera { perspective
+        location L right x*width/height up y look_at A angle a }`` for a view
+        of width x height pixels, the look_at applied by the library the way
+        View::StartRender applies it."""
+        right_len = float(width) / float(height)
+        dl = right_len / np.tan(float(angle) * _scenes.M_PI_360) / 2.0   # Parse_Camera's "angle"
+        cam = abi.PovGpuCamera()
+        for k in range(3):
+            cam.location[k] = float(location[k])
+        cam.direction[:] = (0.0, 0.0, dl)
+        cam.right[:] = (right_len, 0.0, 0.0)
+        cam.up[:] = (0.0, 1.0, 0.0)
+        la = (C.c_double * 3)(*map(float, look_at))
+        sk = (C.c_double * 3)(*map(float, sky))
+        _check(self.lib.pov_gpu_set_camera(self.h, C.byref(cam), la, sk), "pov_gpu_set_camera")
 
     def set_pretrace_jitter(self, table):
         """The reference's pretrace jitter table (RadiosityTask's

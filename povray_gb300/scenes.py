@@ -16,6 +16,7 @@ Workloads (names are descriptive, sizes are the defaults):
                   (1920x1080, 1 spp)
 """
 import ctypes as C
+import copy
 import math
 
 import numpy as np
@@ -876,10 +877,68 @@ def media_spheres(width=320, height=240, n_spheres=24, seed=5, intervals=10, sam
     return s
 
 
+VIEW_SIZES = ((256, 256), (640, 480), (1280, 720), (1920, 1080))
+
+
+def circle_views(n_views=64, radius=30.0, y=5.0, seed=5, sizes=VIEW_SIZES):
+    """`n_views` cameras evenly spaced on a circle of `radius` at height `y`,
+    all looking at the origin; each view's resolution drawn uniformly from
+    `sizes` (seed 5).  Returns [(location, look_at, width, height)]."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    pick = rng.integers(0, len(sizes), size=n_views)
+    views = []
+    for i in range(n_views):
+        a = 2.0 * math.pi * i / n_views
+        loc = (radius * math.sin(a), y, -radius * math.cos(a))
+        w, h = sizes[int(pick[i])]
+        views.append((loc, (0.0, 0.0, 0.0), int(w), int(h)))
+    return views
+
+
+def view_of(scene, location, look_at, width, height):
+    """The same scene seen from another camera at another resolution (what
+    a View with its own camera renders), as a Scene of its own."""
+    v = copy.copy(scene)
+    v.location = tuple(float(x) for x in location)
+    v.look_at = tuple(float(x) for x in look_at)
+    v.width = int(width)
+    v.height = int(height)
+    v.right_len = float(width) / float(height)
+    return v
+
+
+def multiview_media(mesh_n=296, n_spheres=10000, seed=5, box=12.5, radiosity=True, count=200,
+                    recursion_limit=2, error_bound=0.5, intervals=10, samples=10, scattering=0.05):
+    """The batched multi-view scene: the displaced sphere mesh2 of
+    mesh_spheres (radius 8, seed 2) + `n_spheres` spheres r U[0.1,0.5] in
+    [-12,12]^3 (seed 5) + plane y=-9, one point light (20,30,-20), reflection
+    0.3, max_trace_level 3; a uniform scattering media box [-box,box]^3
+    (scattering rgb 0.05, intervals 10, samples 10, method 3) around it; with
+    `radiosity`, radiosity { count 200 recursion_limit 2 error_bound 0.5 }.
+    Its views come from circle_views (64 cameras, r 30, y 5)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    centres = rng.uniform(-12.0, 12.0, size=(n_spheres, 3))
+    radii = rng.uniform(0.1, 0.5, size=n_spheres)
+    colours = rng.uniform(0.0, 1.0, size=(n_spheres, 3))
+    s = Scene("multiview_media", 1920, 1080, (0.0, 5.0, -30.0), (0.0, 0.0, 0.0), 50.0, max_trace_level=3)
+    s.point_light((20.0, 30.0, -20.0))
+    s.media_box((-box, -box, -box), (box, box, box), scattering=(scattering,) * 3, intervals=intervals,
+                samples=samples)
+    mesh = displaced_sphere_mesh(n=mesh_n, seed=2)
+    s.mesh(mesh, s.material(Material((0.9, 0.7, 0.4), phong=0.5, reflection=0.3)))
+    for i in range(n_spheres):
+        s.sphere(centres[i], radii[i], s.material(Material(colours[i], phong=0.5, reflection=0.3)))
+    s.plane((0.0, 1.0, 0.0), -9.0, s.material(Material((0.8, 0.8, 0.8), phong=0.5, reflection=0.3)))
+    if radiosity:
+        s.radiosity = dict(count=count, recursion_limit=recursion_limit, error_bound=error_bound)
+    return s
+
+
 WORKLOADS = {
     "spheres_plane": spheres_plane,
     "mesh_spheres": mesh_spheres,
     "csg_torus_grid": csg_torus_grid,
     "radiosity_room": radiosity_room,
     "media_spheres": media_spheres,
+    "multiview_media": multiview_media,
 }
