@@ -41,15 +41,24 @@ WORKLOADS = {
     "spheres_plane": "spheres_plane: %dx%d 1spp, 64 spheres + plane, 2 lights w/ shadows, phong 0.5",
     "radiosity_room": "radiosity_room: %dx%d 1spp, 6-plane room + 200 spheres, 4x4 area light, radiosity count 200 "
                       "recursion_limit 2 error_bound 0.5 (pretrace + final trace per frame)",
+    "multiview_media": "multiview_media: 64 views on a circle r=30 y=5 at 256x256/640x480/1280x720/1920x1080 "
+                       "(seed 5) of the 1,051,392-tri mesh2 + 10,000 spheres + plane inside a scattering media box "
+                       "(rgb 0.05, intervals 10, samples 10), radiosity count 200 recursion_limit 2 error_bound 0.5 "
+                       "(pretrace + final trace per view), one step = the next view",
 }
+MULTIVIEW = ("multiview_media",)
 
 
 def make_scene(args):
     from povray_gb300 import scenes
+    if args.workload in MULTIVIEW:
+        return scenes.WORKLOADS[args.workload]()
     return scenes.WORKLOADS[args.workload](args.width, args.height)
 
 
 def workload_name(args):
+    if args.workload in MULTIVIEW:
+        return WORKLOADS[args.workload]
     return WORKLOADS[args.workload] % (args.width, args.height)
 
 
@@ -127,15 +136,26 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(scene, cpu_seconds_target=20.0):
+def cpu_baseline(scene, cpu_seconds_target=20.0, crop=None):
     """The oracle port (FP64 restatement of the reference), all host threads,
-    on a band of rows of the same frame; Mrays/s by its own counters."""
+    on a band of rows of the same frame (or a `crop` square at the centre);
+    Mrays/s by its own counters."""
     from oracle.pyoracle import Oracle
     # radiosity renders run on one thread in the reference's sample order
     cores = 1 if scene.radiosity is not None else (os.cpu_count() or 1)
     t0 = time.time()
     orc = Oracle(scene)
     build_s = time.time() - t0
+    if crop:
+        x0, y0 = (scene.width - crop) // 2, (scene.height - crop) // 2
+        t = time.time()
+        _, st = orc.render(x0, y0, x0 + crop, y0 + crop, threads=0)
+        dt = time.time() - t
+        return {"value": (st["number_of_rays"] + st["shadow_ray_tests"]) / dt / 1e6, "unit": "Mrays/s",
+                "cores": cores, "kind": "port",
+                "sample": "oracle restatement, %dx%d px at the centre of a %dx%d view (pretrace over the crop, "
+                          "then the final trace), %.1f s wall, tree build %.1f s excluded"
+                          % (crop, crop, scene.width, scene.height, dt, build_s)}
     rows = 8
     y0 = scene.height // 2
     total_rays, total_t = 0, 0.0
@@ -160,12 +180,22 @@ def run_reference(args, rank, world):
     from oracle.pyoracle import Oracle
     from povray_gb300 import scenes
     s = make_scene(args)
+    if args.workload in MULTIVIEW:
+        # a 16x16 crop at the centre of the first view per step: radiosity
+        # and media make every pixel of this scene cost milliseconds on a CPU
+        loc, at, w, h = scenes.circle_views()[0]
+        s = scenes.view_of(s, loc, at, w, h)
+        args.width, args.height = w, h
     orc = Oracle(s)
     band = max(8, args.height // 10)
     def step(i):
-        y0 = (i * band) % max(1, args.height - band)
         t = time.time()
-        _, st = orc.render(0, y0, args.width, y0 + band, threads=0)
+        if args.workload in MULTIVIEW:
+            x0, y0 = (args.width - 16) // 2, (args.height - 16) // 2
+            _, st = orc.render(x0, y0, x0 + 16, y0 + 16, threads=0)
+        else:
+            y0 = (i * band) % max(1, args.height - band)
+            _, st = orc.render(0, y0, args.width, y0 + band, threads=0)
         return time.time() - t, st["number_of_rays"] + st["shadow_ray_tests"]
     for i in range(args.warmup):
         step(i)
@@ -178,6 +208,10 @@ def run_reference(args, rank, world):
     cores = 1 if s.radiosity is not None else (os.cpu_count() or 1)
     sample = "oracle restatement of the reference (FP64 C, pthreads), %d-row band of the %dx%d frame per step" % (
         band, args.width, args.height)
+    if args.workload in MULTIVIEW:
+        sample = "oracle restatement of the reference (FP64 C, one thread: radiosity), 16x16 px at the centre of " \
+                 "the first %dx%d view per step (pretrace over the crop, then the final trace)" % (args.width,
+                                                                                                   args.height)
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": v, "unit": "Mrays/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": tt / args.steps * 1e3,
@@ -207,37 +241,52 @@ def main():
     gpu = GpuScene(s)
     stream = torch.cuda.current_stream()
     gpu.set_stream(stream.cuda_stream)
+    multiview = args.workload in MULTIVIEW
+    views = scenes.circle_views() if multiview else None
     params = s.render_params()
     blocks = scenes.blocks_for(args.width, args.height)
-    npix = args.width * args.height
+    npix = max(w * h for _, _, w, h in views) if multiview else args.width * args.height
     dev_out = torch.empty((npix, 4), dtype=torch.float32, device="cuda")
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
-
     radiosity = s.radiosity is not None
+    if multiview and radiosity:
+        # the neural cache shared across the views, each pretrace training it on
+        gpu.set_neural_cache(True, steps=300, batch=4096, gate=0.5, shared=True)
 
-    def frame_device(out_ptr=None):
+    def view(i):
+        """Render params and blocks of step i: the frame, or the next view
+        (its camera set without re-parsing)."""
+        if not multiview:
+            return params, blocks
+        loc, at, w, h = views[i % len(views)]
+        gpu.set_camera(loc, at, s.angle, w, h)
+        return scenes.view_of(s, loc, at, w, h).render_params(), scenes.blocks_for(w, h)
+
+    def frame_device(i=0, out_ptr=None):
         """One frame: with radiosity the pretrace over all blocks, then the
-        final trace.  Returns the frame's counters and per-call timings."""
+        final trace.  Returns the frame's counters, per-call timings and the
+        block count and pixels of the frame."""
+        p, bl = view(i)
         st_all, tims = None, []
         if radiosity:
-            st_all = gpu.radiosity_pretrace(blocks, params)
+            st_all = gpu.radiosity_pretrace(bl, p)
             tims.append(gpu.timings())
-        st = gpu.trace_blocks(blocks, params, out=out_ptr or dev_out.data_ptr())[1]
+        st = gpu.trace_blocks(bl, p, out=out_ptr or dev_out.data_ptr())[1]
         tims.append(gpu.timings())
         if st_all is not None:
             st = {k: st[k] + st_all[k] for k in st if k != "device_error"}
-        return st, tims
+        return st, tims, len(bl), p.width * p.height
 
     # one profiling frame (outside the timed region): traversal work counts
     gpu.set_profiling(times=False, work=True)
-    _, wt = frame_device()
+    _, wt, _, _ = frame_device(args.warmup)   # the first timed frame (view)
     work = {k: [sum(t[k][j] for t in wt) for j in range(2)] for k in ("node_visits", "prim_tests", "tri_tests",
                                                                           "rays_traced")}
     gpu.set_profiling(times=True, work=False)
 
-    for _ in range(args.warmup):
-        frame_device()
+    for i in range(args.warmup):
+        frame_device(i)
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
@@ -250,7 +299,7 @@ def main():
     for i in range(args.steps):
         flush.zero_()
         ev[i][0].record(stream)
-        st, tims = frame_device()
+        st, tims, _, _ = frame_device(args.warmup + i)
         ev[i][1].record(stream)
         for t in tims:
             for k, v in t["stage_ms"].items():
@@ -265,17 +314,19 @@ def main():
     # e2e: host buffers through the public call (pinned output)
     gpu.set_profiling(times=False, work=False)
     host_out = torch.empty((npix, 4), dtype=torch.float32, pin_memory=True)
-    for _ in range(max(1, args.warmup // 2)):
-        frame_device(host_out.data_ptr())
+    for i in range(max(1, args.warmup // 2)):
+        frame_device(i, host_out.data_ptr())
     torch.cuda.synchronize()
-    e2e_rays = 0
+    e2e_rays, h2d, d2h = 0, 0, 0
     t0 = time.perf_counter()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for i in range(args.steps):
-        st = frame_device(host_out.data_ptr())[0]
+        st, _, nb, npx = frame_device(args.warmup + i, host_out.data_ptr())
         e2e_rays += st["number_of_rays"] + st["shadow_ray_tests"]
+        h2d += nb * 16 + (nb + 1) * 4
+        d2h += npx * 16
     e1.record(stream)
     torch.cuda.synchronize()
     e2e_wall = time.perf_counter() - t0
@@ -294,6 +345,8 @@ def main():
     # boxes of a two-wide node) + 48 B per triangle test + 16 B per sphere test
     nv, pt, tt_, rt = work["node_visits"], work["prim_tests"], work["tri_tests"], work["rays_traced"]
     k = 0 if stage_ms.get("trace_closest", 0) >= stage_ms.get("trace_shadow", 0) else 1
+    if rt[k] == 0:   # shadow rays through media containers run outside the counted any-hit kernel
+        k = 0
     kname = ["trace_closest", "trace_shadow"][k]
     bytes_per_frame = rt[k] * (32 + (16 if k == 0 else 1)) + nv[k] * 64 + tt_[k] * 48 + (pt[k] - tt_[k]) * 16
     kernel_s = stage_ms[kname] / 1e3 / args.steps
@@ -319,8 +372,8 @@ def main():
                    **({"radiosity": {k: st[k] for k in ("radiosity_gathers", "radiosity_reuse", "radiosity_rays",
                                                          "radiosity_gathers_d0", "radiosity_gathers_d1")}}
                       if radiosity else {})},
-        "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": len(blocks) * 16 + (len(blocks) + 1) * 4,
-                "d2h_bytes_per_step": npix * 16},
+        "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": h2d // args.steps,
+                "d2h_bytes_per_step": d2h // args.steps},
         "roofline": {"bound": "hbm", "kernel": "k_trace<%s>" % ("closest" if k == 0 else "any"),
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_source": "measured" if peaks else "fallback",
@@ -330,7 +383,11 @@ def main():
         "clocks": clocks,
     }
     if rank == 0 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(s)
+        if multiview:
+            loc, at, w, h = views[0]
+            out["cpu_baseline"] = cpu_baseline(scenes.view_of(s, loc, at, w, h), crop=16)
+        else:
+            out["cpu_baseline"] = cpu_baseline(s)
     if rank == 0:
         print(json.dumps(out))
     if dist:
