@@ -293,7 +293,8 @@ enum {
     C_AQ = 8,     // area-light shadow items
     C_RQ = 9,     // radiosity queries
     C_MC = 10,    // rays crossing a media container's interior
-    C_NUM = 11
+    C_ML = 11,    // media samples listed for the next round
+    C_NUM = 12
 };
 
 // One wavefront of ray queues and per-path state: the camera's, or the
@@ -306,6 +307,7 @@ struct PathBufs {
     DevBuf quality, first_t;       // sample rays: quality of each, depth of its first hit
     DevBuf stateA, stateB, smedium; // media containers: per-ray level and medium, shadow-ray medium
     DevBuf mlist, mte, mod;         // media containers: listed rays, per-interval sums
+    DevBuf mcbuf, mrounds;          // media containers: sample slots of a chunk, round lists
     DevBuf counters;
 
     // media_ni: interval slots per ray segment (0: the scene has no media containers)
@@ -357,7 +359,7 @@ struct PathBufs {
     {
         DevBuf* all[] = {&qA, &qB, &pathA, &pathB, &hits, &paths, &slot_contrib, &sq, &sq_slot, &blocked, &skipA,
                          &skipB, &sskip, &aq, &aq_slot, &aq_skip, &rq, &rq_amb, &quality, &first_t, &stateA,
-                         &stateB, &smedium, &mlist, &mte, &mod, &counters};
+                         &stateB, &smedium, &mlist, &mte, &mod, &mcbuf, &mrounds, &counters};
         for (DevBuf* b : all)
             b->release();
     }
@@ -453,6 +455,10 @@ struct PovGpuScene {
     DevBuf spheres, spheres64, boxes64, sphere_obj, sphere_flags, planes, plane_obj, boxes, tori, csgs, csg_children, objects,
         materials, lights, medias;
     int    media_ni = 0;   // interval slots per media segment (0: no media containers)
+    int    media_smax = 0;  // sample slots per interval (ends + sample-tree nodes)
+    int    media_sub = 0;   // largest sub-interval count
+    int    media_levels = 0;   // largest AA_Level
+    int    media_stamp = 0;    // marks the slots a chunk's samples fill
     std::vector<double> h_container_boxes;   // corners of the media containers, 6 per box
     // host copies of the id maps (prim -> flattened object id)
     std::vector<int32_t> h_sphere_obj, h_plane_obj, h_box_obj, h_torus_obj, h_tri_global, h_tri_local, h_tri_obj;
@@ -1028,6 +1034,10 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
         m.extinction = make_float4(md.extinction[0], md.extinction[1], md.extinction[2], 0.0f);
         m.n = make_int4(md.intervals, std::max((md.min_samples + 1) / 2, 1), md.aa_level, box);
         media_ni = std::max(media_ni, md.intervals + 1);   // + the padding interval
+        const int sub = m.n.y, T = (1 << md.aa_level) - 1;
+        sc->media_smax = std::max(sc->media_smax, sub + 1 + sub * T);
+        sc->media_sub = std::max(sc->media_sub, sub);
+        sc->media_levels = std::max(sc->media_levels, md.aa_level);
     }
 
     CK(upload(sc->objects, objects));
@@ -1293,6 +1303,50 @@ int rad_reset(PovGpuScene* sc)
     return POV_GPU_OK;
 }
 
+// Media of the current queue's rays inside containers (MediaFunction::
+// ComputeMedia per segment): lists them, samples them in chunks whose sample
+// slots fit the scratch (rounds of the adaptive recursion), and folds each
+// segment's emission and transmittance into its path before shading.
+int run_media(PovGpuScene* sc, PathBufs& B, const QRay* q, const int* state, const int* path, const int* qcount,
+              size_t maxq, int grid, int* launches)
+{
+    cudaStream_t st = sc->active();
+    int* cnt = B.counters.as<int>();
+    const DeviceScene& S = sc->S;
+    const int NI = sc->media_ni, SMAX = sc->media_smax;
+    CK(cudaMemsetAsync(cnt + C_MC, 0, sizeof(int), st));
+    CK(launch_media_list(state, B.hits.as<QHit>(), qcount, (int)maxq, B.mlist.as<int>(), cnt + C_MC, grid, st));
+    int nm = 0;
+    CK(cudaMemcpyAsync(&nm, cnt + C_MC, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    nm = std::min<int>(nm, (int)maxq);
+    *launches = 1;
+    if (nm == 0)
+        return POV_GPU_OK;
+    // chunk: sample slots within ~1 GiB; a round lists at most every node
+    // of the deepest tree level
+    const size_t per_seg = (size_t)NI * SMAX;
+    const int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)nm, ((size_t)1 << 30) / (per_seg * 16)));
+    const size_t list_cap = (size_t)chunk * NI * sc->media_sub * ((size_t)1 << (sc->media_levels - 1));
+    CK(B.mcbuf.ensure(sizeof(float4) * (size_t)chunk * per_seg));
+    CK(B.mrounds.ensure(sizeof(int) * list_cap));
+    for (int first = 0; first < nm; first += chunk) {
+        const int nseg = std::min(chunk, nm - first);
+        if (++sc->media_stamp == 0)
+            ++sc->media_stamp;
+        CK(launch_media_chunk(S, q, state, B.hits.as<QHit>(), B.mlist.as<int>(), first, nseg, NI, SMAX,
+                              sc->media_sub, sc->media_levels, B.mcbuf.as<float4>(), B.mrounds.as<int>(),
+                              B.mrounds.as<int>(), cnt + C_ML, (int)list_cap, sc->media_stamp, B.mte.as<float4>(),
+                              B.mod.as<float4>(), sc->stack_depth, grid, sc->err.as<uint32_t>(),
+                              sc->stats.as<unsigned long long>(), st));
+        *launches += 2 + 2 * (sc->media_levels - 1);
+    }
+    CK(launch_media_combine(S, state, path, B.hits.as<QHit>(), B.mlist.as<int>(), cnt + C_MC, (int)maxq, NI,
+                            B.mte.as<float4>(), B.mod.as<float4>(), B.paths.as<PathState>(), grid, st));
+    *launches += 1;
+    return POV_GPU_OK;
+}
+
 // Traces one wavefront through trace levels level0 .. max_level-1: the rays
 // in B.qA (count in the C_QA counter, path index in B.pathA, origin surface
 // in B.skipA) and the reflection rays they spawn.  With radiosity on and
@@ -1362,11 +1416,11 @@ int run_levels(PovGpuScene* sc, StageClock& clk, PathBufs& B, size_t maxq, int l
             CK(launch_first_hit(B.hits.as<QHit>(), ccur, (int)maxq, B.first_t.as<float>(), grid_shade, st));
         if (media && !sample_rays) {   // the radiosity Trace runs with media off
             CK(clk.begin(POV_GPU_STAGE_MEDIA));
-            CK(cudaMemsetAsync(cnt + C_MC, 0, sizeof(int), st));
-            CK(launch_media(S, qcur, scur, pcur, B.hits.as<QHit>(), ccur, (int)maxq, B.mlist.as<int>(), cnt + C_MC,
-                            sc->media_ni, B.mte.as<float4>(), B.mod.as<float4>(), B.paths.as<PathState>(),
-                            sc->stack_depth, grid_trace, derr, dstats, st));
-            CK(clk.end(3));
+            int nlaunch = 0;
+            int rc = run_media(sc, B, qcur, scur, pcur, ccur, maxq, grid_trace, &nlaunch);
+            if (rc != POV_GPU_OK)
+                return rc;
+            CK(clk.end(nlaunch));
         }
         CK(clk.begin(POV_GPU_STAGE_SHADE));
         ShadeMedia sm{scur, snext, media ? B.smedium.as<int>() : nullptr};

@@ -124,7 +124,8 @@ constexpr int BOX_CONTAINER = 2;         // DevBox flag: surface of a media cont
 constexpr int OBJ_CONTAINER = 1 << 30;   // ObjectShade flag; container index in bits 16..23
 constexpr int MAX_CONTAINERS = 8;
 constexpr int MEDIA_MAX_INTERVALS = 32;  // Intervals the GPU path holds per ray segment
-constexpr int MEDIA_MAX_AA_LEVEL = 6;
+constexpr int MEDIA_MAX_AA_LEVEL = 4;
+constexpr int MEDIA_MAX_NODES = (1 << MEDIA_MAX_AA_LEVEL) - 1;   // sample tree nodes per sub-interval
 
 // Per-ray state of a wavefront queue in scenes with media containers: the
 // ray's trace level (bits 0..7) and the container it travels in, plus one

@@ -1484,84 +1484,6 @@ __device__ __forceinline__ float col3_dist(float3 a, float3 b)   // ColourDistan
     return fabsf(a.x - b.x) + fabsf(a.y - b.y) + fabsf(a.z - b.z);
 }
 
-// MediaFunction::ComputeOneMediaSampleRecursive (media.cpp:1040-1125, jitter
-// 0) as a depth-first frame stack: the midpoint sample of [d1, d3], then the
-// halves whose end colours differ by more than the threshold, down to
-// `depth` levels; R and ODR weight the samples as the reference does.
-struct MediaFrame {
-    double d1, d3;
-    float3 C1, C3, C2, od1, od3, od2, R, ODR;
-    int depth, stage;
-};
-
-template <bool FULL>
-__device__ void media_subdivide(const DeviceScene& S, const MediaSeg& g, double s0, double ds, double lit, double d1,
-                                double d3, float3 C1, float3 C3, float3 od1, float3 od3, int depth, float3& R,
-                                float3& ODR, int* smem, int stack_depth, uint32_t* err, unsigned long long& tests,
-                                unsigned long long& succ, unsigned long long& ms)
-{
-    const float thr = g.md->emission.w;
-    MediaFrame st[MEDIA_MAX_AA_LEVEL];
-    int sp = 0;
-    st[0].d1 = d1; st[0].d3 = d3; st[0].C1 = C1; st[0].C3 = C3; st[0].od1 = od1; st[0].od3 = od3;
-    st[0].depth = depth; st[0].stage = 0;
-    float3 rR = f3(0.f, 0.f, 0.f), rO = f3(0.f, 0.f, 0.f);   // the last finished frame's result
-    for (;;) {
-        MediaFrame& f = st[sp];
-        bool done = false;
-        if (f.stage == 0) {
-            media_point<FULL>(S, g, s0, ds, 0.5 * (f.d1 + f.d3), lit, f.C2, f.od2, smem, stack_depth, err, tests, succ,
-                              ms);
-            if (f.depth <= 0) {
-                rR = (f.C1 + f.C2 + f.C3) / 3.0f;
-                rO = (f.od1 + f.od2 + f.od3) / 3.0f;
-                f.R = rR;
-                f.ODR = rO;
-                done = true;
-            } else if (col3_dist(f.C1, f.C2) > thr && sp + 1 < MEDIA_MAX_AA_LEVEL) {
-                f.stage = 1;
-                MediaFrame& c = st[++sp];
-                c.d1 = f.d1; c.d3 = 0.5 * (f.d1 + f.d3); c.C1 = f.C1; c.C3 = f.C2; c.od1 = f.od1; c.od3 = f.od2;
-                c.depth = f.depth - 1; c.stage = 0;
-                continue;
-            } else {
-                f.R = f.C1 / 3.0f + f.C2 / 6.0f;
-                f.ODR = f.od1 / 3.0f + f.od2 / 6.0f;
-                f.stage = 2;
-            }
-        } else if (f.stage == 1) {   // first half returned
-            f.R = rR / 2.0f;
-            f.ODR = rO / 2.0f;
-            f.stage = 2;
-        } else if (f.stage == 3) {   // second half returned
-            f.R = f.R + rR / 2.0f;
-            f.ODR = f.ODR + rO / 2.0f;
-            done = true;
-        }
-        if (!done && f.stage == 2) {
-            if (col3_dist(f.C2, f.C3) > thr && sp + 1 < MEDIA_MAX_AA_LEVEL) {
-                f.stage = 3;
-                MediaFrame& c = st[++sp];
-                c.d1 = 0.5 * (f.d1 + f.d3); c.d3 = f.d3; c.C1 = f.C2; c.C3 = f.C3; c.od1 = f.od2; c.od3 = f.od3;
-                c.depth = f.depth - 1; c.stage = 0;
-                continue;
-            }
-            f.R = f.R + (f.C2 / 6.0f + f.C3 / 3.0f);
-            f.ODR = f.ODR + (f.od2 / 6.0f + f.od3 / 3.0f);
-            done = true;
-        }
-        if (done) {
-            rR = f.R;
-            rO = f.ODR;
-            if (sp == 0)
-                break;
-            sp--;
-        }
-    }
-    R = rR;
-    ODR = rO;
-}
-
 // Interval layout of one segment (ComputeMediaSampleInterval,
 // media.cpp:527-596, and the padding of ComputeMedia, media.cpp:346-352):
 // with a light, `intervals` equal intervals of [0, dist]; when rounding
@@ -1574,66 +1496,155 @@ __device__ __forceinline__ int media_intervals(const DevMedia& md, bool lit, dou
     return nuni + ((lit && delta * (double)nuni < dist) ? 1 : 0);
 }
 
-// One thread per (listed ray, interval): the interval's adaptive samples
-// (ComputeMediaAdaptiveSampling, media.cpp:432-525) -- its emission te and
-// optical depth od sums before the 1/samples normalisation.
+// ------------------------------------------------ media sample wavefront --
+// ComputeMediaAdaptiveSampling (media.cpp:432-525) with
+// ComputeOneMediaSampleRecursive (media.cpp:1040-1125, jitter 0), run as
+// rounds of independent samples: round 0 takes every interval's sub-interval
+// ends and midpoints (the recursion always samples its midpoint), round s
+// the tree nodes of level s whose parent's half differs by more than the
+// threshold.  Every sample lands in a slot of its interval:
+//   slots 0 .. sub            the sub-interval ends, d = 0, dd, dd+dd, ...
+//   sub+1 + k*T + (node-1)    node (heap order, 1 = midpoint) of sub-interval
+//                             k's tree, T = 2^AA_Level - 1 nodes
+// and the reduction replays the reference's weighting from the slots.
+
+struct MediaWork {
+    const QRay*  q;
+    const int*   q_state;
+    const QHit*  hits;
+    const int*   mlist;       // listed rays (queue indices)
+    int          first;       // this chunk's first listed ray
+    int          nseg;        // listed rays in this chunk
+    int          NI;          // interval slots per ray
+    int          SMAX;        // sample slots per interval
+    float4*      cbuf;        // [nseg][NI][SMAX]: sample colour, w = stamp when taken
+    const int*   list;        // round s >= 1: slots to sample
+    const int*   list_count;
+    int*         next;        // expansion output
+    int*         next_count;
+    int          list_cap;
+    int          stamp;       // marks the slots taken in this chunk
+    float4*      te;          // [listed ray][NI] interval sums
+    float4*      od;
+};
+
+// One interval of a listed ray: its segment and its place in the segment.
+struct MediaInterval {
+    MediaSeg g;
+    double   s0, ds, lit;
+    int      nint, sub, T;
+};
+
+__device__ __forceinline__ bool media_interval(const DeviceScene& S, const MediaWork& W, int j, int iv,
+                                               MediaInterval& I)
+{
+    const int i = W.mlist[W.first + j];
+    const QRay r = W.q[i];
+    I.g.O = xyz(r.org);
+    I.g.D = xyz(r.dir);
+    I.g.medium = state_medium(W.q_state[i]);
+    I.g.md = S.medias + I.g.medium;
+    const bool lit = S.num_lights > 0;
+    const double dist = (double)W.hits[i].t;
+    double delta;
+    int nuni;
+    I.nint = media_intervals(*I.g.md, lit, dist, delta, nuni);
+    if (iv >= I.nint)
+        return false;
+    I.s0 = delta * (double)iv;
+    I.ds = iv < nuni ? delta : dist - delta * (double)nuni;
+    I.lit = (lit && iv < nuni) ? dist : -1.0;
+    I.sub = I.g.md->n.y;
+    I.T = (1 << I.g.md->n.z) - 1;
+    return true;
+}
+
+// Sub-interval end e at d = dd + dd + ... (the reference's running sum).
+__device__ __forceinline__ double media_end(int e, double dd)
+{
+    double d = 0.0;
+    for (int k = 0; k < e; k++)
+        d = d + dd;
+    return d;
+}
+
+// Fraction of the interval of tree node `node` of sub-interval k, and the
+// slots holding the colours at its two ends.
+__device__ __forceinline__ double media_node(const MediaInterval& I, int k, int node, int& lslot, int& rslot)
+{
+    const double dd = 1.0 / (double)I.sub;
+    double a = media_end(k, dd);
+    double b = a + dd;
+    lslot = k;
+    rslot = k + 1;
+    const int base = I.sub + 1 + k * I.T - 1;
+    int level = 31 - __clz(node);
+    for (int l = level - 1; l >= 0; l--) {
+        const int anc = node >> (l + 1);   // the node whose half is taken
+        const double mid = 0.5 * (a + b);
+        if ((node >> l) & 1) {
+            a = mid;
+            lslot = base + anc;
+        } else {
+            b = mid;
+            rslot = base + anc;
+        }
+    }
+    return 0.5 * (a + b);
+}
+
+__device__ __forceinline__ float4* media_slot(const MediaWork& W, int j, int iv, int slot)
+{
+    return W.cbuf + ((size_t)j * W.NI + iv) * W.SMAX + slot;
+}
+
+// One sample per thread: round 0 (list == nullptr) enumerates every
+// interval's ends and midpoints, later rounds take the listed slots.
 template <bool FULL>
-__global__ void __launch_bounds__(128) k_media(DeviceScene S, const QRay* __restrict__ q,
-                                               const int* __restrict__ q_state, const QHit* __restrict__ hits,
-                                               const int* __restrict__ mlist, const int* __restrict__ mcount,
-                                               int mcap, int NI, float4* __restrict__ te_out,
-                                               float4* __restrict__ od_out, int stack_depth, uint32_t* err,
-                                               unsigned long long* stats)
+__global__ void __launch_bounds__(128) k_media_sample(DeviceScene S, MediaWork W, int round0_per_interval,
+                                                      int stack_depth, uint32_t* err, unsigned long long* stats)
 {
     extern __shared__ int smem[];
-    const long long items = (long long)min(*mcount, mcap) * NI;
+    const long long n = W.list ? (long long)min(*W.list_count, W.list_cap)
+                               : (long long)W.nseg * W.NI * round0_per_interval;
     unsigned long long c_tests = 0, c_succ = 0, c_ms = 0;
-    const bool lit = S.num_lights > 0;
-    for (long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x; it < items;
+    for (long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x; it < n;
          it += (long long)gridDim.x * blockDim.x) {
-        const int j = (int)(it / NI), iv = (int)(it % NI);
-        const int i = mlist[j];
-        const QRay r = q[i];
-        MediaSeg g;
-        g.O = xyz(r.org);
-        g.D = xyz(r.dir);
-        g.medium = state_medium(q_state[i]);
-        g.md = S.medias + g.medium;
-        const double dist = (double)hits[i].t;
-        double delta;
-        int nuni;
-        const int nint = media_intervals(*g.md, lit, dist, delta, nuni);
-        float3 te = f3(0.f, 0.f, 0.f), odi = f3(0.f, 0.f, 0.f);
-        if (iv < nint) {
-            const double s0 = delta * (double)iv;
-            const double ds = iv < nuni ? delta : dist - delta * (double)nuni;
-            const double litend = (lit && iv < nuni) ? dist : -1.0;
-            const int sub = g.md->n.y;
-            const double dd = 1.0 / (double)sub;
-            const float ddf = (float)dd;
-            float3 C0, od0, C1, od1, R, ODR;
-            media_point<FULL>(S, g, s0, ds, 0.0, litend, C0, od0, smem, stack_depth, err, c_tests, c_succ, c_ms);
-            double d0 = 0.0;
-            for (int k = 1; k <= sub; k++) {
-                const double d1 = d0 + dd;
-                media_point<FULL>(S, g, s0, ds, d1, litend, C1, od1, smem, stack_depth, err, c_tests, c_succ, c_ms);
-                media_subdivide<FULL>(S, g, s0, ds, litend, d0, d1, C0, C1, od0, od1, g.md->n.z - 1, R, ODR, smem,
-                                      stack_depth, err, c_tests, c_succ, c_ms);
-                // attenuation by the earlier sub-intervals, then by this one's
-                // own depth (media.cpp:470-487)
-                R = f3(R.x * expf(-odi.x * ddf), R.y * expf(-odi.y * ddf), R.z * expf(-odi.z * ddf));
-                if (ODR.x != 0.0f) R.x *= (1.0f - expf(-ODR.x * ddf)) / (ODR.x * ddf);
-                if (ODR.y != 0.0f) R.y *= (1.0f - expf(-ODR.y * ddf)) / (ODR.y * ddf);
-                if (ODR.z != 0.0f) R.z *= (1.0f - expf(-ODR.z * ddf)) / (ODR.z * ddf);
-                te = te + R;
-                odi = odi + ODR;
-                C0 = C1;
-                od0 = od1;
-                d0 = d1;
-            }
+        int j, iv, slot;
+        if (W.list) {
+            const int code = W.list[it];
+            slot = code % W.SMAX;
+            iv = (code / W.SMAX) % W.NI;
+            j = code / (W.SMAX * W.NI);
+        } else {
+            j = (int)(it / ((long long)W.NI * round0_per_interval));
+            const int rem = (int)(it % ((long long)W.NI * round0_per_interval));
+            iv = rem / round0_per_interval;
+            slot = rem % round0_per_interval;   // re-based below
         }
-        te_out[it] = make_float4(te.x, te.y, te.z, 0.f);
-        od_out[it] = make_float4(odi.x, odi.y, odi.z, 0.f);
+        MediaInterval I;
+        if (!media_interval(S, W, j, iv, I))
+            continue;
+        double f;
+        if (!W.list) {
+            if (slot >= 2 * I.sub + 1)
+                continue;
+            if (slot <= I.sub) {
+                f = media_end(slot, 1.0 / (double)I.sub);
+            } else {
+                const int k = slot - (I.sub + 1);
+                int ls, rs;
+                f = media_node(I, k, 1, ls, rs);
+                slot = I.sub + 1 + k * I.T;
+            }
+        } else {
+            const int t = slot - (I.sub + 1);
+            int ls, rs;
+            f = media_node(I, t / I.T, t % I.T + 1, ls, rs);
+        }
+        float3 C, od;
+        media_point<FULL>(S, I.g, I.s0, I.ds, f, I.lit, C, od, smem, stack_depth, err, c_tests, c_succ, c_ms);
+        *media_slot(W, j, iv, slot) = make_float4(C.x, C.y, C.z, __int_as_float(W.stamp));
     }
     for (int off = 16; off > 0; off >>= 1) {
         c_tests += __shfl_down_sync(0xffffffffu, c_tests, off);
@@ -1644,6 +1655,124 @@ __global__ void __launch_bounds__(128) k_media(DeviceScene S, const QRay* __rest
         if (c_tests) atomicAdd(&stats[ST_SHADOW_TESTS], c_tests);
         if (c_succ) atomicAdd(&stats[ST_SHADOW_SUCCEEDED], c_succ);
         if (c_ms) atomicAdd(&stats[ST_MEDIA_SAMPLES], c_ms);
+    }
+}
+
+__device__ __forceinline__ bool media_taken(const float4& c, int stamp) { return __float_as_int(c.w) == stamp; }
+
+__device__ __forceinline__ float3 media_c(const float4& c) { return f3(c.x, c.y, c.z); }
+
+// Round s: one thread per (ray, interval, sub-interval, taken node of level
+// s-1 whose depth is above 0); lists each half whose end colours differ by
+// more than the threshold (ColourDistance, media.cpp:1072,1100).
+__global__ void k_media_expand(DeviceScene S, MediaWork W, int s, int max_sub, uint32_t* err)
+{
+    const int per = max_sub << (s - 1);
+    const long long n = (long long)W.nseg * W.NI * per;
+    for (long long base = (long long)blockIdx.x * blockDim.x; base < n; base += (long long)gridDim.x * blockDim.x) {
+        const long long it = base + threadIdx.x;
+        bool want[2] = {false, false};
+        int code[2] = {0, 0};
+        if (it < n) {
+            const int j = (int)(it / ((long long)W.NI * per));
+            const int rem = (int)(it % ((long long)W.NI * per));
+            const int iv = rem / per;
+            const int k = (rem % per) >> (s - 1);
+            const int p = (1 << (s - 1)) + ((rem % per) & ((1 << (s - 1)) - 1));   // parent node, level s-1
+            MediaInterval I;
+            if (media_interval(S, W, j, iv, I) && k < I.sub && s < I.g.md->n.z) {
+                const int pslot = I.sub + 1 + k * I.T + p - 1;
+                const float4 cp = *media_slot(W, j, iv, pslot);
+                if (media_taken(cp, W.stamp)) {
+                    int ls, rs;
+                    media_node(I, k, p, ls, rs);
+                    const float thr = I.g.md->emission.w;
+                    const float3 c1 = media_c(*media_slot(W, j, iv, ls)), c2 = media_c(cp),
+                                 c3 = media_c(*media_slot(W, j, iv, rs));
+                    const int cbase = ((j * W.NI) + iv) * W.SMAX + I.sub + 1 + k * I.T - 1;
+                    want[0] = col3_dist(c1, c2) > thr;
+                    code[0] = cbase + 2 * p;
+                    want[1] = col3_dist(c2, c3) > thr;
+                    code[1] = cbase + 2 * p + 1;
+                }
+            }
+        }
+        for (int h = 0; h < 2; h++) {
+            const int slot = warp_reserve(W.next_count, want[h], 0xffffffffu);
+            if (want[h]) {
+                if (slot < W.list_cap)
+                    W.next[slot] = code[h];
+                else
+                    set_error(err, DE_QUEUE_OVERFLOW);
+            }
+        }
+    }
+}
+
+// One thread per (ray, interval): the reference's weighting of the taken
+// samples, sub-interval by sub-interval (ComputeOneMediaSampleRecursive's
+// Result / ODResult, then the attenuation of media.cpp:470-487), leaves
+// first; the interval's te and od sums go to the combine step.
+__global__ void k_media_reduce(DeviceScene S, MediaWork W)
+{
+    const long long n = (long long)W.nseg * W.NI;
+    for (long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x; it < n;
+         it += (long long)gridDim.x * blockDim.x) {
+        const int j = (int)(it / W.NI), iv = (int)(it % W.NI);
+        MediaInterval I;
+        float3 te = f3(0.f, 0.f, 0.f), odi = f3(0.f, 0.f, 0.f);
+        if (media_interval(S, W, j, iv, I)) {
+            const float ddf = (float)(1.0 / (double)I.sub);
+            const float3 a = xyz(I.g.md->extinction) * (float)I.ds;   // every sample's optical depth
+            const int levels = I.g.md->n.z;
+            for (int k = 0; k < I.sub; k++) {
+                float3 R[MEDIA_MAX_NODES], O[MEDIA_MAX_NODES];
+                const int base = I.sub + 1 + k * I.T - 1;
+                for (int node = I.T; node >= 1; node--) {
+                    const float4 cn = *media_slot(W, j, iv, base + node);
+                    if (!media_taken(cn, W.stamp))
+                        continue;
+                    int ls, rs;
+                    media_node(I, k, node, ls, rs);
+                    const float3 C1 = media_c(*media_slot(W, j, iv, ls)), C2 = media_c(cn),
+                                 C3 = media_c(*media_slot(W, j, iv, rs));
+                    const int level = 31 - __clz(node);
+                    float3 r, o;
+                    if (levels - 1 - level <= 0) {
+                        r = (C1 + C2 + C3) / 3.0f;
+                        o = (a + a + a) / 3.0f;
+                    } else {
+                        const bool lt = media_taken(*media_slot(W, j, iv, base + 2 * node), W.stamp);
+                        const bool rt = media_taken(*media_slot(W, j, iv, base + 2 * node + 1), W.stamp);
+                        if (lt) {
+                            r = R[2 * node - 1] / 2.0f;
+                            o = O[2 * node - 1] / 2.0f;
+                        } else {
+                            r = C1 / 3.0f + C2 / 6.0f;
+                            o = a / 3.0f + a / 6.0f;
+                        }
+                        if (rt) {
+                            r = r + R[2 * node] / 2.0f;
+                            o = o + O[2 * node] / 2.0f;
+                        } else {
+                            r = r + (C2 / 6.0f + C3 / 3.0f);
+                            o = o + (a / 6.0f + a / 3.0f);
+                        }
+                    }
+                    R[node - 1] = r;
+                    O[node - 1] = o;
+                }
+                float3 r = R[0], o = O[0];
+                r = f3(r.x * expf(-odi.x * ddf), r.y * expf(-odi.y * ddf), r.z * expf(-odi.z * ddf));
+                if (o.x != 0.0f) r.x *= (1.0f - expf(-o.x * ddf)) / (o.x * ddf);
+                if (o.y != 0.0f) r.y *= (1.0f - expf(-o.y * ddf)) / (o.y * ddf);
+                if (o.z != 0.0f) r.z *= (1.0f - expf(-o.z * ddf)) / (o.z * ddf);
+                te = te + r;
+                odi = odi + o;
+            }
+        }
+        W.te[(size_t)(W.first + j) * W.NI + iv] = make_float4(te.x, te.y, te.z, 0.f);
+        W.od[(size_t)(W.first + j) * W.NI + iv] = make_float4(odi.x, odi.y, odi.z, 0.f);
     }
 }
 
@@ -2020,21 +2149,73 @@ cudaError_t launch_shadow_through(const DeviceScene& S, const QRay* sq, const in
     return cudaGetLastError();
 }
 
-cudaError_t launch_media(const DeviceScene& S, const QRay* q, const int* q_state, const int* q_path, const QHit* hits,
-                         const int* q_count, int cap, int* mlist, int* mcount, int NI, float4* te, float4* od,
-                         PathState* paths, int stack_depth, int grid, uint32_t* err, unsigned long long* stats,
-                         cudaStream_t st)
+cudaError_t launch_media_list(const int* q_state, const QHit* hits, const int* q_count, int cap, int* mlist,
+                              int* mcount, int grid, cudaStream_t st)
 {
+    k_media_list<<<grid, 128, 0, st>>>(q_state, hits, q_count, cap, mlist, mcount);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_media_chunk(const DeviceScene& S, const QRay* q, const int* q_state, const QHit* hits,
+                               const int* mlist, int first, int nseg, int NI, int SMAX, int max_sub, int max_levels,
+                               float4* cbuf, int* listA, int* listB, int* counts, int list_cap, int stamp,
+                               float4* te, float4* od, int stack_depth, int grid, uint32_t* err,
+                               unsigned long long* stats, cudaStream_t st)
+{
+    MediaWork W{};
+    W.q = q;
+    W.q_state = q_state;
+    W.hits = hits;
+    W.mlist = mlist;
+    W.first = first;
+    W.nseg = nseg;
+    W.NI = NI;
+    W.SMAX = SMAX;
+    W.cbuf = cbuf;
+    W.list_cap = list_cap;
+    W.stamp = stamp;
+    W.te = te;
+    W.od = od;
     const int block = 128;
-    k_media_list<<<grid, block, 0, st>>>(q_state, hits, q_count, cap, mlist, mcount);
-    size_t smem = (size_t)stack_depth * block * sizeof(int);
-    if (S.has_full_prims)
-        k_media<true><<<grid, block, smem, st>>>(S, q, q_state, hits, mlist, mcount, cap, NI, te, od, stack_depth,
-                                                 err, stats);
-    else
-        k_media<false><<<grid, block, smem, st>>>(S, q, q_state, hits, mlist, mcount, cap, NI, te, od, stack_depth,
-                                                  err, stats);
-    k_media_combine<<<grid, block, 0, st>>>(q_state, q_path, hits, mlist, mcount, cap, NI, S, te, od, paths);
+    const size_t smem = (size_t)stack_depth * block * sizeof(int);
+    cudaError_t e;
+    auto sample = [&](const MediaWork& w) {
+        if (S.has_full_prims)
+            k_media_sample<true><<<grid, block, smem, st>>>(S, w, 2 * max_sub + 1, stack_depth, err, stats);
+        else
+            k_media_sample<false><<<grid, block, smem, st>>>(S, w, 2 * max_sub + 1, stack_depth, err, stats);
+        return cudaGetLastError();
+    };
+    // round 0: every interval's ends and midpoints
+    if ((e = sample(W)) != cudaSuccess)
+        return e;
+    // rounds 1 .. levels-1: the halves that differ
+    for (int s = 1; s < max_levels; s++) {
+        int* out = (s & 1) ? listA : listB;   // the list of round s (consumed before round s+1 fills one)
+        int* out_count = counts;
+        if ((e = cudaMemsetAsync(out_count, 0, sizeof(int), st)) != cudaSuccess)
+            return e;
+        MediaWork X = W;
+        X.next = out;
+        X.next_count = out_count;
+        k_media_expand<<<grid, block, 0, st>>>(S, X, s, max_sub, err);
+        if ((e = cudaGetLastError()) != cudaSuccess)
+            return e;
+        MediaWork Y = W;
+        Y.list = out;
+        Y.list_count = out_count;
+        if ((e = sample(Y)) != cudaSuccess)
+            return e;
+    }
+    k_media_reduce<<<grid, block, 0, st>>>(S, W);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_media_combine(const DeviceScene& S, const int* q_state, const int* q_path, const QHit* hits,
+                                 const int* mlist, const int* mcount, int cap, int NI, const float4* te,
+                                 const float4* od, PathState* paths, int grid, cudaStream_t st)
+{
+    k_media_combine<<<grid, 128, 0, st>>>(q_state, q_path, hits, mlist, mcount, cap, NI, S, te, od, paths);
     return cudaGetLastError();
 }
 

@@ -31,12 +31,19 @@ cudaError_t launch_shadow_through(const DeviceScene& S, const QRay* sq, const in
                                   float4* slot_contrib, bool media_on, int stack_depth, int grid, uint32_t* err,
                                   unsigned long long* stats, cudaStream_t st);
 // Media of the queue's rays inside containers, applied to their paths
-// before shading: lists the rays (mcount zeroed by the caller), samples
-// NI interval slots per ray, combines them in order.
-cudaError_t launch_media(const DeviceScene& S, const QRay* q, const int* q_state, const int* q_path, const QHit* hits,
-                         const int* q_count, int cap, int* mlist, int* mcount, int NI, float4* te, float4* od,
-                         PathState* paths, int stack_depth, int grid, uint32_t* err, unsigned long long* stats,
-                         cudaStream_t st);
+// before shading: list the rays (mcount zeroed by the caller); per chunk of
+// listed rays, the sample rounds into cbuf and the per-interval sums; then
+// combine every listed ray's intervals into its path.
+cudaError_t launch_media_list(const int* q_state, const QHit* hits, const int* q_count, int cap, int* mlist,
+                              int* mcount, int grid, cudaStream_t st);
+cudaError_t launch_media_chunk(const DeviceScene& S, const QRay* q, const int* q_state, const QHit* hits,
+                               const int* mlist, int first, int nseg, int NI, int SMAX, int max_sub, int max_levels,
+                               float4* cbuf, int* listA, int* listB, int* counts, int list_cap, int stamp,
+                               float4* te, float4* od, int stack_depth, int grid, uint32_t* err,
+                               unsigned long long* stats, cudaStream_t st);
+cudaError_t launch_media_combine(const DeviceScene& S, const int* q_state, const int* q_path, const QHit* hits,
+                                 const int* mlist, const int* mcount, int cap, int NI, const float4* te,
+                                 const float4* od, PathState* paths, int grid, cudaStream_t st);
 cudaError_t launch_area_shadow(const DeviceScene& S, const QRay* aq, const int* aq_slot, const uint2* aq_skip,
                                const int* aq_count, int cap, float4* slot_contrib, int stack_depth, int grid,
                                uint32_t* err, unsigned long long* stats, cudaStream_t st);
