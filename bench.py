@@ -41,6 +41,8 @@ WORKLOADS = {
     "spheres_plane": "spheres_plane: %dx%d 1spp, 64 spheres + plane, 2 lights w/ shadows, phong 0.5",
     "radiosity_room": "radiosity_room: %dx%d 1spp, 6-plane room + 200 spheres, 4x4 area light, radiosity count 200 "
                       "recursion_limit 2 error_bound 0.5 (pretrace + final trace per frame)",
+    "media_spheres": "media_spheres: %dx%d 1spp, 24 spheres + plane in a scattering media box (rgb 0.05, "
+                     "intervals 10, samples 10), 1 point light, reflection 0.2, max_trace_level 3",
     "multiview_media": "multiview_media: 64 views on a circle r=30 y=5 at 256x256/640x480/1280x720/1920x1080 "
                        "(seed 5) of the 1,051,392-tri mesh2 + 10,000 spheres + plane inside a scattering media box "
                        "(rgb 0.05, intervals 10, samples 10), radiosity count 200 recursion_limit 2 error_bound 0.5 "
