@@ -343,14 +343,15 @@ def main():
     value = world * rays / t_total / 1e6
     e2e_value = world * e2e_rays / e2e_t / 1e6
     # roofline of the dominant kernel (closest-hit traversal): algorithmic
-    # bytes = 32 B ray + 16 B hit per ray + 64 B per node visit (both child
-    # boxes of a two-wide node) + 48 B per triangle test + 16 B per sphere test
+    # bytes = 32 B ray + 16 B hit per ray + 112 B per node visit (the four
+    # child boxes and links of a four-wide node) + 48 B per triangle test +
+    # 16 B per sphere test
     nv, pt, tt_, rt = work["node_visits"], work["prim_tests"], work["tri_tests"], work["rays_traced"]
     k = 0 if stage_ms.get("trace_closest", 0) >= stage_ms.get("trace_shadow", 0) else 1
     if rt[k] == 0:   # shadow rays through media containers run outside the counted any-hit kernel
         k = 0
     kname = ["trace_closest", "trace_shadow"][k]
-    bytes_per_frame = rt[k] * (32 + (16 if k == 0 else 1)) + nv[k] * 64 + tt_[k] * 48 + (pt[k] - tt_[k]) * 16
+    bytes_per_frame = rt[k] * (32 + (16 if k == 0 else 1)) + nv[k] * 112 + tt_[k] * 48 + (pt[k] - tt_[k]) * 16
     kernel_s = stage_ms[kname] / 1e3 / args.steps
     peaks = {}
     try:

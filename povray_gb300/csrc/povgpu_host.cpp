@@ -244,6 +244,80 @@ private:
     }
 };
 
+// Collapses the binary tree into four-wide nodes: starting from a node's two
+// children, the inner child with the largest box surface area is replaced
+// by its own two children until four are held or only leaves remain.
+struct Bvh4Collapse {
+    const std::vector<BvhNode>& in;
+    std::vector<Bvh4Node> out;
+    int max_depth = 0;
+
+    explicit Bvh4Collapse(const std::vector<BvhNode>& n) : in(n) {}
+
+    struct Child {
+        float lo[3], hi[3];
+        int link;
+    };
+
+    static float area(const Child& c)
+    {
+        float d[3] = {c.hi[0] - c.lo[0], c.hi[1] - c.lo[1], c.hi[2] - c.lo[2]};
+        return 2.0f * (d[0] * d[1] + d[1] * d[2] + d[2] * d[0]);
+    }
+
+    void children_of(int ni, Child& a, Child& b) const
+    {
+        const BvhNode& n = in[ni];
+        a = {{n.a.x, n.a.z, n.c.x}, {n.a.y, n.a.w, n.c.y}, __builtin_bit_cast(int, n.d.x)};
+        b = {{n.b.x, n.b.z, n.c.z}, {n.b.y, n.b.w, n.c.w}, __builtin_bit_cast(int, n.d.y)};
+    }
+
+    // returns the index of the four-wide node for binary inner node ni
+    int collapse(int ni, int depth)
+    {
+        max_depth = std::max(max_depth, depth);
+        Child ch[4];
+        int n = 2;
+        children_of(ni, ch[0], ch[1]);
+        while (n < 4) {
+            int best = -1;
+            float ba = -1.0f;
+            for (int k = 0; k < n; k++)
+                if (ch[k].link >= 0 && area(ch[k]) > ba) {
+                    ba = area(ch[k]);
+                    best = k;
+                }
+            if (best < 0)
+                break;
+            Child a, b;
+            children_of(ch[best].link, a, b);
+            ch[best] = a;
+            ch[n++] = b;
+        }
+        const int me = (int)out.size();
+        out.push_back(Bvh4Node{});
+        int links[4];
+        for (int k = 0; k < 4; k++)
+            links[k] = k < n ? (ch[k].link >= 0 ? collapse(ch[k].link, depth + 1) : ch[k].link) : BVH_EMPTY;
+        Bvh4Node& o = out[me];
+        float v[6][4];
+        for (int k = 0; k < 4; k++)
+            for (int a = 0; a < 3; a++) {
+                v[2 * a][k] = k < n ? ch[k].lo[a] : INFINITY;
+                v[2 * a + 1][k] = k < n ? ch[k].hi[a] : -INFINITY;
+            }
+        o.lox = make_float4(v[0][0], v[0][1], v[0][2], v[0][3]);
+        o.hix = make_float4(v[1][0], v[1][1], v[1][2], v[1][3]);
+        o.loy = make_float4(v[2][0], v[2][1], v[2][2], v[2][3]);
+        o.hiy = make_float4(v[3][0], v[3][1], v[3][2], v[3][3]);
+        o.loz = make_float4(v[4][0], v[4][1], v[4][2], v[4][3]);
+        o.hiz = make_float4(v[5][0], v[5][1], v[5][2], v[5][3]);
+        o.link = make_int4(links[0], links[1], links[2], links[3]);
+        o.pad = make_int4(0, 0, 0, 0);
+        return me;
+    }
+};
+
 // ------------------------------------------------- mesh2 triangle setup --
 static int max3_coordinate(double x, double y, double z)
 {
@@ -950,9 +1024,15 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
     if (B.tri_v0.size() >= (size_t)PRIM_INDEX_MASK || B.bvh.items.size() >= (1u << 28))
         return POV_GPU_E_UNSUPPORTED;
 
-    int root = B.bvh.build_root();
-    sc->stack_depth = std::max(8, B.bvh.max_depth + 2);
-    if (sc->stack_depth > 96)
+    int root2 = B.bvh.build_root();
+    // four-wide nodes for the traversal; a node pushes at most three
+    // children, so the stack holds 3 per level of the collapsed tree
+    Bvh4Collapse wide(B.bvh.nodes);
+    int root = root2 >= 0 && root2 != BVH_EMPTY ? wide.collapse(root2, 1) : root2;
+    if (wide.out.empty())
+        wide.out.push_back(Bvh4Node{});
+    sc->stack_depth = std::max(8, 3 * wide.max_depth + 2);
+    if (sc->stack_depth > 160)
         return POV_GPU_E_UNSUPPORTED;
 
     // reorder triangle records into leaf order (prim refs then index the
@@ -993,7 +1073,7 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
             num_area++;
     }
 
-    CK(upload(sc->nodes, B.bvh.nodes));
+    CK(upload(sc->nodes, wide.out));
     CK(upload(sc->refs, B.bvh.refs));
     CK(upload(sc->tri_v0, lv0));
     CK(upload(sc->tri_e1, le1));
@@ -1058,7 +1138,7 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
     sc->h_csg_children = B.csg_children;
 
     DeviceScene& S = sc->S;
-    S.nodes = sc->nodes.as<BvhNode>();
+    S.nodes = sc->nodes.as<Bvh4Node>();
     S.prim_refs = sc->refs.as<uint32_t>();
     S.root = root;
     S.tri_v0 = sc->tri_v0.as<float4>();

@@ -38,6 +38,17 @@ struct __align__(16) BvhNode {
 };
 constexpr int LEAF_MAX_PRIMS = 8;
 
+// Four-wide BVH node (128 B, the binary tree collapsed: each node takes the
+// children and grandchildren with the largest surface area): child c's box
+// in component c of the six slab vectors, child links as in BvhNode; an
+// empty child has an inverted box and link BVH_EMPTY.
+struct __align__(16) Bvh4Node {
+    float4 lox, hix, loy, hiy, loz, hiz;
+    int4   link;
+    int4   pad;
+};
+constexpr int BVH_EMPTY = 0x7fffffff;   // no node: the traversal's stop value
+
 // Shading record of one scene object (flattened object id).
 struct __align__(16) ObjectShade {
     int32_t material;
@@ -135,9 +146,9 @@ __host__ __device__ __forceinline__ int state_level(int s) { return s & 0xff; }
 __host__ __device__ __forceinline__ int state_medium(int s) { return ((s >> 8) & 0xff) - 1; }
 
 struct DeviceScene {
-    const BvhNode*  nodes;
+    const Bvh4Node* nodes;
     const uint32_t* prim_refs;
-    int32_t         root;           // -1 = no finite primitives
+    int32_t         root;           // BVH_EMPTY = no finite primitives
     // triangles (leaf order)
     const float4*   tri_v0;
     const float4*   tri_e1;

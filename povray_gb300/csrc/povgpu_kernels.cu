@@ -544,30 +544,56 @@ __device__ __forceinline__ bool isect_tri(float4 v0, float4 e1, float4 e2, float
 }
 
 // Slab test of both children of a node; returns entry distances.
-__device__ __forceinline__ void node_test(const BvhNode* __restrict__ nodes, int ni, float3 o, float3 inv,
-                                          float tmin, float tmax, bool& h0, bool& h1, float& t0, float& t1,
-                                          int& l0, int& l1)
+// One inner node of the four-wide tree: the children whose boxes the ray
+// enters within [tmin, tmax] (slab test, far side widened by a few ulp so
+// rounding never culls a box the exact test would enter), ordered near to
+// far by a 4-input sorting network; the nearest becomes `node`, the others
+// are pushed farthest first.  With no child entered, `node` is the next
+// stack entry (BVH_EMPTY when the stack is empty).  False on stack overflow.
+__device__ __forceinline__ bool node4_step(const Bvh4Node* __restrict__ nodes, int& node, float3 o, float3 inv,
+                                           float tmin, float tmax, int* smem, int& sp, int stack_depth)
 {
-    const float4* p = reinterpret_cast<const float4*>(nodes + ni);
-    float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2), d = __ldg(p + 3);
-    float ax0 = (a.x - o.x) * inv.x, ax1 = (a.y - o.x) * inv.x;
-    float ay0 = (a.z - o.y) * inv.y, ay1 = (a.w - o.y) * inv.y;
-    float az0 = (c.x - o.z) * inv.z, az1 = (c.y - o.z) * inv.z;
-    float bx0 = (b.x - o.x) * inv.x, bx1 = (b.y - o.x) * inv.x;
-    float by0 = (b.z - o.y) * inv.y, by1 = (b.w - o.y) * inv.y;
-    float bz0 = (c.z - o.z) * inv.z, bz1 = (c.w - o.z) * inv.z;
-    float an = fmaxf(fmaxf(fminf(ax0, ax1), fminf(ay0, ay1)), fmaxf(fminf(az0, az1), tmin));
-    float af = fminf(fminf(fmaxf(ax0, ax1), fmaxf(ay0, ay1)), fminf(fmaxf(az0, az1), tmax));
-    float bn = fmaxf(fmaxf(fminf(bx0, bx1), fminf(by0, by1)), fmaxf(fminf(bz0, bz1), tmin));
-    float bf = fminf(fminf(fmaxf(bx0, bx1), fmaxf(by0, by1)), fminf(fmaxf(bz0, bz1), tmax));
-    // conservative: widen the far side by a few ulp so rounding never culls
-    // a box the exact test would enter
-    h0 = an <= af * 1.00000024f;
-    h1 = bn <= bf * 1.00000024f;
-    t0 = an;
-    t1 = bn;
-    l0 = __float_as_int(d.x);
-    l1 = __float_as_int(d.y);
+    const float4* p = reinterpret_cast<const float4*>(nodes + node);
+    const float4 lox = __ldg(p), hix = __ldg(p + 1), loy = __ldg(p + 2), hiy = __ldg(p + 3);
+    const float4 loz = __ldg(p + 4), hiz = __ldg(p + 5);
+    const int4 lk = __ldg(reinterpret_cast<const int4*>(p + 6));
+    float t0, t1, t2, t3;
+    int l0, l1, l2, l3;
+#define POVGPU_CHILD(TN, LN, X)                                                                   \
+    {                                                                                             \
+        float x0 = (lox.X - o.x) * inv.x, x1 = (hix.X - o.x) * inv.x;                           \
+        float y0 = (loy.X - o.y) * inv.y, y1 = (hiy.X - o.y) * inv.y;                           \
+        float z0 = (loz.X - o.z) * inv.z, z1 = (hiz.X - o.z) * inv.z;                           \
+        float tn = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fmaxf(fminf(z0, z1), tmin));      \
+        float tf = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fminf(fmaxf(z0, z1), tmax));      \
+        bool in = lk.X != BVH_EMPTY && tn <= tf * 1.00000024f;                                    \
+        TN = in ? tn : CUDART_INF_F;                                                              \
+        LN = in ? lk.X : BVH_EMPTY;                                                               \
+    }
+    POVGPU_CHILD(t0, l0, x)
+    POVGPU_CHILD(t1, l1, y)
+    POVGPU_CHILD(t2, l2, z)
+    POVGPU_CHILD(t3, l3, w)
+#undef POVGPU_CHILD
+#define POVGPU_CSWAP(TA, LA, TB, LB)                   \
+    if (TB < TA) {                                     \
+        float tt = TA; TA = TB; TB = tt;               \
+        int ll = LA; LA = LB; LB = ll;                 \
+    }
+    POVGPU_CSWAP(t0, l0, t1, l1)
+    POVGPU_CSWAP(t2, l2, t3, l3)
+    POVGPU_CSWAP(t0, l0, t2, l2)
+    POVGPU_CSWAP(t1, l1, t3, l3)
+    POVGPU_CSWAP(t1, l1, t2, l2)
+#undef POVGPU_CSWAP
+    const int pushes = (l1 != BVH_EMPTY) + (l2 != BVH_EMPTY) + (l3 != BVH_EMPTY);
+    if (sp + pushes > stack_depth)
+        return false;
+    if (l3 != BVH_EMPTY) smem[(sp++) * blockDim.x + threadIdx.x] = l3;
+    if (l2 != BVH_EMPTY) smem[(sp++) * blockDim.x + threadIdx.x] = l2;
+    if (l1 != BVH_EMPTY) smem[(sp++) * blockDim.x + threadIdx.x] = l1;
+    node = l0 != BVH_EMPTY ? l0 : (sp > 0 ? smem[(--sp) * blockDim.x + threadIdx.x] : BVH_EMPTY);
+    return true;
 }
 
 // One primitive of a leaf against the ray.  `skip` names the surface the
@@ -703,33 +729,16 @@ __global__ void __launch_bounds__(128) k_trace(DeviceScene S, const QRay* __rest
         int sp = 0;
         int node = S.root;
         int iters = 0;
-        while (!done && node != 0x7fffffff) {
+        while (!done && node != BVH_EMPTY) {
             if (++iters > (1 << 22)) {
                 set_error(err, DE_ITERATION_CAP);
                 break;
             }
             if (node >= 0) {
-                bool h0, h1;
-                float t0, t1;
-                int l0, l1;
-                node_test(S.nodes, node, o, inv, tmin, t, h0, h1, t0, t1, l0, l1);
                 if (counting) c_nodes++;
-                if (h0 && h1) {
-                    int nearl = l0, farl = l1;
-                    if (t1 < t0) { nearl = l1; farl = l0; }
-                    if (sp >= stack_depth) {
-                        set_error(err, DE_STACK_OVERFLOW);
-                        break;
-                    }
-                    smem[sp * blockDim.x + threadIdx.x] = farl;
-                    sp++;
-                    node = nearl;
-                } else if (h0) {
-                    node = l0;
-                } else if (h1) {
-                    node = l1;
-                } else {
-                    node = sp > 0 ? smem[(--sp) * blockDim.x + threadIdx.x] : 0x7fffffff;
+                if (!node4_step(S.nodes, node, o, inv, tmin, t, smem, sp, stack_depth)) {
+                    set_error(err, DE_STACK_OVERFLOW);
+                    break;
                 }
             } else {
                 uint32_t code = ~(uint32_t)node;
@@ -747,7 +756,7 @@ __global__ void __launch_bounds__(128) k_trace(DeviceScene S, const QRay* __rest
                 }
                 if (done)
                     break;
-                node = sp > 0 ? smem[(--sp) * blockDim.x + threadIdx.x] : 0x7fffffff;
+                node = sp > 0 ? smem[(--sp) * blockDim.x + threadIdx.x] : BVH_EMPTY;
             }
         }
         if (ANY) {
@@ -1138,30 +1147,15 @@ __device__ __forceinline__ bool occluded(const DeviceScene& S, float3 o, float3 
     float3 inv = f3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
     float t = tmax, bu = 0.f, bv = 0.f;
     int sp = 0, node = S.root, iters = 0;
-    while (node != 0x7fffffff) {
+    while (node != BVH_EMPTY) {
         if (++iters > (1 << 22)) {
             set_error(err, DE_ITERATION_CAP);
             return false;
         }
         if (node >= 0) {
-            bool h0, h1;
-            float t0, t1;
-            int l0, l1;
-            node_test(S.nodes, node, o, inv, tmin, t, h0, h1, t0, t1, l0, l1);
-            if (h0 && h1) {
-                if (sp >= stack_depth) {
-                    set_error(err, DE_STACK_OVERFLOW);
-                    return false;
-                }
-                smem[sp * blockDim.x + threadIdx.x] = t1 < t0 ? l0 : l1;
-                sp++;
-                node = t1 < t0 ? l1 : l0;
-            } else if (h0) {
-                node = l0;
-            } else if (h1) {
-                node = l1;
-            } else {
-                node = sp > 0 ? smem[(--sp) * blockDim.x + threadIdx.x] : 0x7fffffff;
+            if (!node4_step(S.nodes, node, o, inv, tmin, t, smem, sp, stack_depth)) {
+                set_error(err, DE_STACK_OVERFLOW);
+                return false;
             }
         } else {
             uint32_t code = ~(uint32_t)node;
@@ -1171,7 +1165,7 @@ __device__ __forceinline__ bool occluded(const DeviceScene& S, float3 o, float3 
                 if (prim_test<true, FULL>(S, __ldg(S.prim_refs + first + k), o, d, tmin, t, bu, bv, aux, skip))
                     return true;
             }
-            node = sp > 0 ? smem[(--sp) * blockDim.x + threadIdx.x] : 0x7fffffff;
+            node = sp > 0 ? smem[(--sp) * blockDim.x + threadIdx.x] : BVH_EMPTY;
         }
     }
     return false;
