@@ -134,6 +134,7 @@ __global__ void k_camera(DeviceScene S, int mode, const int4* __restrict__ block
     if (i >= n)
         return;
     double x, y;
+    int path = i;
     if (mode == 2) {
         double2 p = pos[i];
         x = p.x;
@@ -146,17 +147,28 @@ __global__ void k_camera(DeviceScene S, int mode, const int4* __restrict__ block
         }
         int4 b = blocks[lo];            // left, top, right, bottom
         int w = b.z - b.x + 1 + (mode == 1 ? 1 : 0);
+        int h = b.w - b.y + 1 + (mode == 1 ? 1 : 0);
         int local = i - block_off[lo];
-        x = (double)(b.x + local % w) + (mode == 0 ? 0.5 : 0.0);
-        y = (double)(b.y + local / w) + (mode == 0 ? 0.5 : 0.0);
+        int lx = local % w, ly = local / w;
+        if (mode == 0 && w == 32 && h == 32) {
+            // full blocks queue their pixels in 8x4 tiles (one warp each) so
+            // a warp's rays stay close together; the path keeps the pixel's
+            // row-major place in the block's output
+            int tile = local >> 5, lane = local & 31;
+            lx = (tile & 3) * 8 + (lane & 7);
+            ly = (tile >> 2) * 4 + (lane >> 3);
+            path = block_off[lo] + ly * w + lx;
+        }
+        x = (double)(b.x + lx) + (mode == 0 ? 0.5 : 0.0);
+        y = (double)(b.y + ly) + (mode == 0 ? 0.5 : 0.0);
     }
     q[i] = camera_ray(S, x, y, width, height);
-    q_path[i] = i;
+    q_path[i] = path;
     q_skip[i] = make_uint2(NO_PRIM, 0u);
     PathState p;
     p.colour = make_float4(0.f, 0.f, 0.f, 0.f);
     p.throughput = make_float4(1.f, 1.f, 1.f, 1.f);
-    paths[i] = p;
+    paths[path] = p;
 }
 
 // Rays given by the caller (FP64 in, FP32 on the device).
