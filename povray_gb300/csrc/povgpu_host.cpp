@@ -368,7 +368,8 @@ enum {
     C_RQ = 9,     // radiosity queries
     C_MC = 10,    // rays crossing a media container's interior
     C_ML = 11,    // media samples listed for the next round
-    C_NUM = 12
+    C_MW = 12,    // work counter of the media sample rounds
+    C_NUM = 13
 };
 
 // One wavefront of ray queues and per-path state: the camera's, or the
@@ -1521,7 +1522,8 @@ int run_levels(PovGpuScene* sc, StageClock& clk, PathBufs& B, size_t maxq, int l
             CK(clk.begin(POV_GPU_STAGE_TRACE_SHADOW));
             if (media)
                 CK(launch_shadow_through(S, B.sq.as<QRay>(), B.sq_slot.as<int>(), B.sskip.as<uint2>(),
-                                         B.smedium.as<int>(), cnt + C_SQ, (int)(maxq * nl), B.blocked.as<uint8_t>(),
+                                         B.smedium.as<int>(), cnt + C_SQ, (int)(maxq * nl), cnt + C_W1,
+                                         B.blocked.as<uint8_t>(),
                                          B.slot_contrib.as<float4>(), !sample_rays, sc->stack_depth, grid_trace,
                                          derr, dstats, st));
             else

@@ -1387,14 +1387,24 @@ __global__ void __launch_bounds__(128) k_shadow_through(DeviceScene S, const QRa
                                                         const uint2* __restrict__ sq_skip,
                                                         const int* __restrict__ sq_medium,
                                                         const int* __restrict__ sq_count, int cap,
-                                                        uint8_t* __restrict__ blocked,
+                                                        int* __restrict__ work, uint8_t* __restrict__ blocked,
                                                         float4* __restrict__ slot_contrib, int media_on,
                                                         int stack_depth, uint32_t* err, unsigned long long* stats)
 {
     extern __shared__ int smem[];
     const int n = min(*sq_count, cap);
+    const int lane = threadIdx.x & 31;
     unsigned long long c_tests = 0, c_succ = 0, c_ms = 0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (;;) {   // persistent: each warp claims 32 rays at a time
+        int base = 0;
+        if (lane == 0)
+            base = atomicAdd(work, 32);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n)
+            break;
+        const int i = base + lane;
+        if (i >= n)
+            continue;
         const QRay r = sq[i];
         float3 atten = f3(1.f, 1.f, 1.f);
         unsigned long long t = 0;
@@ -1608,14 +1618,23 @@ __device__ __forceinline__ float4* media_slot(const MediaWork& W, int j, int iv,
 // interval's ends and midpoints, later rounds take the listed slots.
 template <bool FULL>
 __global__ void __launch_bounds__(128) k_media_sample(DeviceScene S, MediaWork W, int round0_per_interval,
-                                                      int stack_depth, uint32_t* err, unsigned long long* stats)
+                                                      int* __restrict__ work, int stack_depth, uint32_t* err,
+                                                      unsigned long long* stats)
 {
     extern __shared__ int smem[];
-    const long long n = W.list ? (long long)min(*W.list_count, W.list_cap)
-                               : (long long)W.nseg * W.NI * round0_per_interval;
+    const int n = W.list ? min(*W.list_count, W.list_cap) : W.nseg * W.NI * round0_per_interval;
+    const int lane = threadIdx.x & 31;
     unsigned long long c_tests = 0, c_succ = 0, c_ms = 0;
-    for (long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x; it < n;
-         it += (long long)gridDim.x * blockDim.x) {
+    for (;;) {   // persistent: each warp claims 32 samples at a time
+        int base = 0;
+        if (lane == 0)
+            base = atomicAdd(work, 32);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n)
+            break;
+        const int it = base + lane;
+        if (it >= n)
+            continue;
         int j, iv, slot;
         if (W.list) {
             const int code = W.list[it];
@@ -1623,8 +1642,8 @@ __global__ void __launch_bounds__(128) k_media_sample(DeviceScene S, MediaWork W
             iv = (code / W.SMAX) % W.NI;
             j = code / (W.SMAX * W.NI);
         } else {
-            j = (int)(it / ((long long)W.NI * round0_per_interval));
-            const int rem = (int)(it % ((long long)W.NI * round0_per_interval));
+            j = it / (W.NI * round0_per_interval);
+            const int rem = it % (W.NI * round0_per_interval);
             iv = rem / round0_per_interval;
             slot = rem % round0_per_interval;   // re-based below
         }
@@ -2140,18 +2159,20 @@ cudaError_t launch_shade(const DeviceScene& S, int level, int max_level, const Q
 }
 
 cudaError_t launch_shadow_through(const DeviceScene& S, const QRay* sq, const int* sq_slot, const uint2* sq_skip,
-                                  const int* sq_medium, const int* sq_count, int cap, uint8_t* blocked,
+                                  const int* sq_medium, const int* sq_count, int cap, int* work, uint8_t* blocked,
                                   float4* slot_contrib, bool media_on, int stack_depth, int grid, uint32_t* err,
                                   unsigned long long* stats, cudaStream_t st)
 {
     const int block = 128;
     size_t smem = (size_t)stack_depth * block * sizeof(int);
     if (S.has_full_prims)
-        k_shadow_through<true><<<grid, block, smem, st>>>(S, sq, sq_slot, sq_skip, sq_medium, sq_count, cap, blocked,
-                                                          slot_contrib, media_on ? 1 : 0, stack_depth, err, stats);
+        k_shadow_through<true><<<grid, block, smem, st>>>(S, sq, sq_slot, sq_skip, sq_medium, sq_count, cap, work,
+                                                          blocked, slot_contrib, media_on ? 1 : 0, stack_depth, err,
+                                                          stats);
     else
-        k_shadow_through<false><<<grid, block, smem, st>>>(S, sq, sq_slot, sq_skip, sq_medium, sq_count, cap, blocked,
-                                                           slot_contrib, media_on ? 1 : 0, stack_depth, err, stats);
+        k_shadow_through<false><<<grid, block, smem, st>>>(S, sq, sq_slot, sq_skip, sq_medium, sq_count, cap, work,
+                                                           blocked, slot_contrib, media_on ? 1 : 0, stack_depth, err,
+                                                           stats);
     return cudaGetLastError();
 }
 
@@ -2185,11 +2206,15 @@ cudaError_t launch_media_chunk(const DeviceScene& S, const QRay* q, const int* q
     const int block = 128;
     const size_t smem = (size_t)stack_depth * block * sizeof(int);
     cudaError_t e;
+    int* work = counts + 1;   // the sample rounds' work counter
     auto sample = [&](const MediaWork& w) {
+        cudaError_t r = cudaMemsetAsync(work, 0, sizeof(int), st);
+        if (r != cudaSuccess)
+            return r;
         if (S.has_full_prims)
-            k_media_sample<true><<<grid, block, smem, st>>>(S, w, 2 * max_sub + 1, stack_depth, err, stats);
+            k_media_sample<true><<<grid, block, smem, st>>>(S, w, 2 * max_sub + 1, work, stack_depth, err, stats);
         else
-            k_media_sample<false><<<grid, block, smem, st>>>(S, w, 2 * max_sub + 1, stack_depth, err, stats);
+            k_media_sample<false><<<grid, block, smem, st>>>(S, w, 2 * max_sub + 1, work, stack_depth, err, stats);
         return cudaGetLastError();
     };
     // round 0: every interval's ends and midpoints

@@ -27,12 +27,13 @@ cudaError_t launch_fill_int(int* a, const int* count, int cap, int value, int gr
 // Shadow rays through media containers (scenes with containers: replaces
 // the any-hit trace of the shadow queue).
 cudaError_t launch_shadow_through(const DeviceScene& S, const QRay* sq, const int* sq_slot, const uint2* sq_skip,
-                                  const int* sq_medium, const int* sq_count, int cap, uint8_t* blocked,
+                                  const int* sq_medium, const int* sq_count, int cap, int* work, uint8_t* blocked,
                                   float4* slot_contrib, bool media_on, int stack_depth, int grid, uint32_t* err,
                                   unsigned long long* stats, cudaStream_t st);
 // Media of the queue's rays inside containers, applied to their paths
 // before shading: list the rays (mcount zeroed by the caller); per chunk of
-// listed rays, the sample rounds into cbuf and the per-interval sums; then
+// listed rays, the sample rounds into cbuf and the per-interval sums (counts:
+// the round list's count, then the rounds' work counter); then
 // combine every listed ray's intervals into its path.
 cudaError_t launch_media_list(const int* q_state, const QHit* hits, const int* q_count, int cap, int* mlist,
                               int* mcount, int grid, cudaStream_t st);
