@@ -421,6 +421,20 @@ int pov_gpu_scene_set_stream(PovGpuScene* scene, void* cuda_stream);
  */
 int pov_gpu_set_camera(PovGpuScene* scene, const PovGpuCamera* camera, const double* look_at, const double* sky);
 
+/*
+ * Image output on the device: linear RGBT pixels quantised to 8 bits per
+ * channel as the reference's image writers do it -- clip to [0,1], the
+ * file's transfer curve, then IntEncode(gamma, x, 255) without dithering
+ * (source/base/image/encoding.cpp:67-91) -- so a caller reads back 3 bytes
+ * per pixel instead of 16.  `rgbt`: npix x 4 floats in device memory (e.g.
+ * pov_gpu_trace_blocks' device output); `out`: npix x 3 bytes (RGB), device
+ * or host memory.  Curves (source/base/image/colourspace.cpp): sRGB, the
+ * default of most formats, and ITU-R BT.709, the PPM writer's.
+ */
+#define POV_GPU_CURVE_SRGB  0
+#define POV_GPU_CURVE_BT709 1
+int pov_gpu_encode_u8(PovGpuScene* scene, const float* rgbt, int64_t npix, int32_t curve, uint8_t* out);
+
 /* Pipeline stages reported by pov_gpu_get_timings. */
 #define POV_GPU_STAGE_CAMERA        0
 #define POV_GPU_STAGE_TRACE_CLOSEST 1

@@ -157,6 +157,8 @@ class PovGpuHit(C.Structure):
     _fields_ = [("object", C.c_int32), ("triangle", C.c_int32), ("t", C.c_double)]
 
 
+POV_GPU_CURVE_SRGB = 0
+POV_GPU_CURVE_BT709 = 1
 POV_GPU_STAGES = 9
 STAGE_NAMES = ["camera", "trace_closest", "shade", "trace_shadow", "resolve", "finalize", "area_shadow", "radiosity",
                "media"]
@@ -185,7 +187,7 @@ EXPORTS = ["pov_gpu_scene_create", "pov_gpu_trace_blocks", "pov_gpu_trace_rays",
            "pov_gpu_scene_destroy", "pov_gpu_error_string", "pov_gpu_abi_version",
            "pov_gpu_scene_set_stream", "pov_gpu_set_profiling", "pov_gpu_get_timings",
            "pov_gpu_trace_rays_static", "pov_gpu_radiosity_pretrace", "pov_gpu_set_pretrace_jitter",
-           "pov_gpu_set_neural_cache", "pov_gpu_nic_eval", "pov_gpu_set_camera"]
+           "pov_gpu_set_neural_cache", "pov_gpu_nic_eval", "pov_gpu_set_camera", "pov_gpu_encode_u8"]
 
 
 class PovGpuError(RuntimeError):
@@ -235,6 +237,8 @@ def load_library(path=None):
     lib.pov_gpu_error_string.restype = C.c_char_p
     lib.pov_gpu_abi_version.argtypes = []
     lib.pov_gpu_abi_version.restype = C.c_int
+    lib.pov_gpu_encode_u8.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_void_p]
+    lib.pov_gpu_encode_u8.restype = C.c_int
     lib.pov_gpu_set_camera.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     lib.pov_gpu_set_camera.restype = C.c_int
     lib.pov_gpu_scene_set_stream.argtypes = [C.c_void_p, C.c_void_p]

@@ -529,6 +529,7 @@ struct PovGpuScene {
     DevBuf nodes, refs, tri_v0, tri_e1, tri_e2, tri_global, tri_shade, tri_normal, tri_local, normals;
     DevBuf spheres, spheres64, boxes64, sphere_obj, sphere_flags, planes, plane_obj, boxes, tori, csgs, csg_children, objects,
         materials, lights, medias;
+    DevBuf encode_buf;     // staging of pov_gpu_encode_u8 for host outputs
     int    media_ni = 0;   // interval slots per media segment (0: no media containers)
     int    media_smax = 0;  // sample slots per interval (ends + sample-tree nodes)
     int    media_sub = 0;   // largest sub-interval count
@@ -569,7 +570,8 @@ struct PovGpuScene {
                          &normals, &spheres, &spheres64, &boxes64, &sphere_obj, &sphere_flags, &planes, &plane_obj, &boxes, &tori, &csgs,
                          &csg_children, &objects, &materials, &lights, &blocks, &block_off, &corner_off, &qA,
                          &hits, &out, &counters, &stats, &err, &rays_in, &t64, &corners, &aa_grid, &aa_mask,
-                         &aa_subdiv, &aa_xy, &cellsA, &cellsB, &spos, &sslot, &wcount, &pos_count, &medias};
+                         &aa_subdiv, &aa_xy, &cellsA, &cellsB, &spos, &sslot, &wcount, &pos_count, &medias,
+                         &encode_buf};
         for (DevBuf* b : all)
             b->release();
         top.release();
@@ -2013,6 +2015,45 @@ int pov_gpu_set_camera(PovGpuScene* sc, const PovGpuCamera* cam, const double* l
         sc->S.cam_right[k] = right[k];
         sc->S.cam_up[k] = up[k];
     }
+    return POV_GPU_OK;
+}
+
+int pov_gpu_encode_u8(PovGpuScene* sc, const float* rgbt, int64_t npix, int32_t curve, uint8_t* out)
+{
+    if (!sc || npix < 0 || (npix > 0 && (!rgbt || !out)) ||
+        (curve != POV_GPU_CURVE_SRGB && curve != POV_GPU_CURVE_BT709))
+        return POV_GPU_E_INVALID;
+    if (npix == 0)
+        return POV_GPU_OK;
+    std::lock_guard<std::mutex> g(sc->lock);
+    CK(cudaSetDevice(sc->device));
+    cudaPointerAttributes in{}, oa{};
+    CK(cudaPointerGetAttributes(&in, rgbt));
+    if (in.type != cudaMemoryTypeDevice && in.type != cudaMemoryTypeManaged)
+        return POV_GPU_E_INVALID;   // the pixels must already be on the device
+    // midpoints of neighbouring decoded levels, in FP32 as IntEncode forms them
+    auto decode = [curve](float x) {
+        if (curve == POV_GPU_CURVE_BT709)   // colourspace.cpp:211-222
+            return x < 0.081f ? x / 4.5f : std::pow((x + 0.099f) / 1.099f, 1.0f / 0.45f);
+        return x < 0.04045f ? x / 12.92f : std::pow((x + 0.055f) / 1.055f, 2.4f);   // sRGB, :181-191
+    };
+    float thr[255];
+    for (int v = 0; v < 255; v++)
+        thr[v] = 0.5f * decode((float)v / 255.0f) + 0.5f * decode((float)(v + 1) / 255.0f);
+    cudaStream_t st = sc->active();
+    const bool direct = cudaPointerGetAttributes(&oa, out) == cudaSuccess &&
+                        (oa.type == cudaMemoryTypeDevice || oa.type == cudaMemoryTypeManaged);
+    cudaGetLastError();   // an unregistered host pointer may leave an error behind
+    uint8_t* dst = out;
+    if (!direct) {
+        CK(sc->encode_buf.ensure((size_t)npix * 3));
+        dst = sc->encode_buf.as<uint8_t>();
+    }
+    const int grid = sc->num_sms * 8;
+    CK(launch_encode_u8(reinterpret_cast<const float4*>(rgbt), (long long)npix, curve, thr, dst, grid, st));
+    if (!direct)
+        CK(cudaMemcpyAsync(out, dst, (size_t)npix * 3, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
     return POV_GPU_OK;
 }
 

@@ -1294,6 +1294,51 @@ __global__ void __launch_bounds__(128) k_area_shadow(DeviceScene S, const QRay* 
     }
 }
 
+// ------------------------------------------------------------- encode --
+// IntEncode(g, x, 255) without dithering (encoding.cpp:67-91): the floor of
+// the encoded value, raised by one where x passes the midpoint of the two
+// neighbouring decoded levels (thr[v], computed by the host in FP32).
+struct EncodeTable {
+    float thr[255];
+};
+
+__device__ __forceinline__ float curve_encode(float x, int curve)
+{
+    if (curve == POV_GPU_CURVE_BT709)   // colourspace.cpp:211-222
+        return x < 0.018f ? x * 4.5f : 1.099f * powf(fmaxf(x, 0.0f), 0.45f) - 0.099f;
+    return x <= 0.0031308f ? x * 12.92f : 1.055f * powf(fmaxf(x, 0.0f), 1.0f / 2.4f) - 0.055f;   // sRGB, :181-191
+}
+
+__global__ void k_encode_u8(const float4* __restrict__ rgbt, long long n, int curve, EncodeTable T,
+                            uint8_t* __restrict__ out)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const float4 c = rgbt[i];
+        const float ch[3] = {c.x, c.y, c.z};
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            // clip (NaN to 0, as the reference's clip leaves no NaN through)
+            const float xe = ch[k] > 0.0f ? fminf(ch[k], 1.0f) : 0.0f;
+            int v = (int)floorf(curve_encode(xe, curve) * 255.0f);
+            v = v < 0 ? 0 : (v > 255 ? 255 : v);
+            if (v < 255 && xe > T.thr[v])
+                v++;
+            out[3 * i + k] = (uint8_t)v;
+        }
+    }
+}
+
+cudaError_t launch_encode_u8(const float4* rgbt, long long n, int curve, const float* thr, uint8_t* out, int grid,
+                             cudaStream_t st)
+{
+    EncodeTable T;
+    for (int v = 0; v < 255; v++)
+        T.thr[v] = thr[v];
+    k_encode_u8<<<grid, 256, 0, st>>>(rgbt, n, curve, T, out);
+    return cudaGetLastError();
+}
+
 // a[i] = value for the first min(*count, cap) entries
 __global__ void k_fill_int(int* __restrict__ a, const int* __restrict__ count, int cap, int value)
 {

@@ -24,6 +24,9 @@ cudaError_t launch_shade(const DeviceScene& S, int level, int max_level, const Q
                          int max_area, const ShadeRad& rad, const ShadeMedia& med, int grid, uint32_t* err,
                          unsigned long long* stats, cudaStream_t st);
 cudaError_t launch_fill_int(int* a, const int* count, int cap, int value, int grid, cudaStream_t st);
+// 8-bit RGB of n RGBT pixels; thr[v] (v < 255) = the midpoint of decoded levels v and v+1
+cudaError_t launch_encode_u8(const float4* rgbt, long long n, int curve, const float* thr, uint8_t* out, int grid,
+                             cudaStream_t st);
 // Shadow rays through media containers (scenes with containers: replaces
 // the any-hit trace of the shadow queue).
 cudaError_t launch_shadow_through(const DeviceScene& S, const QRay* sq, const int* sq_slot, const uint2* sq_skip,

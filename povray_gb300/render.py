@@ -108,6 +108,24 @@ class GpuScene:
         sk = (C.c_double * 3)(*map(float, sky))
         _check(self.lib.pov_gpu_set_camera(self.h, C.byref(cam), la, sk), "pov_gpu_set_camera")
 
+    def encode_u8(self, rgbt_device_ptr, npix, curve="srgb", out=None):
+        """8-bit RGB of `npix` linear RGBT pixels already in device memory
+        (pov_gpu_encode_u8).  `out`: None (a host array is returned), a host
+        uint8 array, or an integer device pointer."""
+        c = {"srgb": abi.POV_GPU_CURVE_SRGB, "bt709": abi.POV_GPU_CURVE_BT709}[curve]
+        host = None
+        if out is None:
+            host = np.empty((npix, 3), dtype=np.uint8)
+            ptr = host.ctypes.data
+        elif isinstance(out, np.ndarray):
+            assert out.dtype == np.uint8 and out.size >= npix * 3 and out.flags.c_contiguous
+            host, ptr = out, out.ctypes.data
+        else:
+            ptr = int(out)
+        _check(self.lib.pov_gpu_encode_u8(self.h, C.c_void_p(int(rgbt_device_ptr)), int(npix), c, C.c_void_p(ptr)),
+               "pov_gpu_encode_u8")
+        return host
+
     def set_pretrace_jitter(self, table):
         """The reference's pretrace jitter table (RadiosityTask's
         RandomDoubleSequence(-1, 1, 2047) values)."""
