@@ -1654,7 +1654,7 @@ int rad_resolve(PovGpuScene* sc, StageClock& clk, int d, const RadQuery* queries
                 io.lo = R.nic_lo;
                 io.scale = R.nic_scale;
                 CK(clk.begin(POV_GPU_STAGE_RADIOSITY));
-                CK(nic::launch_forward(io, R.nic_wb.as<__nv_bfloat16>(), R.nic_params.as<float>(),
+                CK(nic::launch_forward(io, R.nic_wb.as<unsigned char>(), R.nic_params.as<float>(),
                                        sc->err.as<uint32_t>(), sc->num_sms * 2, st));
                 CK(launch_rad_nic_answer(P, L.seeds.as<int>(), ns, R.nic_pred.as<float4>(), out,
                                          R.rstats.as<unsigned long long>(), grid, st));
@@ -1770,7 +1770,7 @@ int nic_train(PovGpuScene* sc)
     // parameters: He-uniform initialisation, zero biases, padded rows zero
     const size_t NP = (size_t)nic::NPARAM;
     CK(R.nic_params.ensure(sizeof(float) * NP));
-    CK(R.nic_wb.ensure(sizeof(__nv_bfloat16) * NP));
+    CK(R.nic_wb.ensure(nic::WIMG_BYTES));
     CK(R.nic_m.ensure(sizeof(float) * NP));
     CK(R.nic_v.ensure(sizeof(float) * NP));
     CK(R.nic_grad.ensure(sizeof(float) * NP));
@@ -1794,7 +1794,7 @@ int nic_train(PovGpuScene* sc)
         CK(cudaMemcpyAsync(R.nic_params.p, hp.data(), sizeof(float) * NP, cudaMemcpyHostToDevice, st));
         CK(cudaMemsetAsync(R.nic_m.p, 0, sizeof(float) * NP, st));
         CK(cudaMemsetAsync(R.nic_v.p, 0, sizeof(float) * NP, st));
-        CK(nic::launch_to_bf16(R.nic_params.as<float>(), R.nic_wb.as<__nv_bfloat16>(), st));
+        CK(nic::launch_to_bf16(R.nic_params.as<float>(), R.nic_wb.as<unsigned char>(), st));
         R.nic_init = true;
     }
     CK(cudaMemsetAsync(R.nic_err.p, 0, sizeof(uint32_t), st));
@@ -1820,11 +1820,11 @@ int nic_train(PovGpuScene* sc)
         io.idx = R.nic_idx.as<int>() + (size_t)s * batch;
         io.n = batch;
         CK(cudaMemsetAsync(R.nic_grad.p, 0, sizeof(float) * NP, st));
-        CK(nic::launch_train(io, R.nic_wb.as<__nv_bfloat16>(), R.nic_params.as<float>(), R.nic_grad.as<float>(),
+        CK(nic::launch_train(io, R.nic_wb.as<unsigned char>(), R.nic_params.as<float>(), R.nic_grad.as<float>(),
                              R.nic_loss.as<float>(), 1.0f / (float)batch, R.nic_err.as<uint32_t>(), sc->num_sms,
                              st));
         CK(nic::launch_adam(R.nic_params.as<float>(), R.nic_m.as<float>(), R.nic_v.as<float>(),
-                            R.nic_grad.as<float>(), R.nic_wb.as<__nv_bfloat16>(), cfg.learning_rate,
+                            R.nic_grad.as<float>(), R.nic_wb.as<unsigned char>(), cfg.learning_rate,
                             R.nic_step + s + 1, st));
     }
     R.nic_step += steps;
@@ -1835,7 +1835,7 @@ int nic_train(PovGpuScene* sc)
     io.idx = R.nic_idx.as<int>() + (size_t)steps * batch;
     io.n = nv;
     io.out = R.nic_pred.as<float4>();
-    CK(nic::launch_forward(io, R.nic_wb.as<__nv_bfloat16>(), R.nic_params.as<float>(), R.nic_err.as<uint32_t>(),
+    CK(nic::launch_forward(io, R.nic_wb.as<unsigned char>(), R.nic_params.as<float>(), R.nic_err.as<uint32_t>(),
                            sc->num_sms * 2, st));
     std::vector<float4> pred((size_t)nv);
     uint32_t nerr = 0;
@@ -2390,7 +2390,7 @@ int pov_gpu_nic_eval(const float* params, const float* bounds, const float* poin
         ~Free() { for (DevBuf* x : b) x->release(); }
     } fr{{&dp, &dwb, &dpos, &dnrm, &dtg, &dout, &dgrad, &dloss, &derr}};
     CK(dp.ensure(sizeof(float) * NP));
-    CK(dwb.ensure(sizeof(__nv_bfloat16) * NP));
+    CK(dwb.ensure(nic::WIMG_BYTES));
     CK(dpos.ensure(sizeof(float4) * (size_t)n));
     CK(dnrm.ensure(sizeof(float4) * (size_t)n));
     CK(dout.ensure(sizeof(float4) * (size_t)n));
@@ -2406,7 +2406,7 @@ int pov_gpu_nic_eval(const float* params, const float* bounds, const float* poin
     CK(cudaMemcpy(dpos.p, hp.data(), sizeof(float4) * (size_t)n, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(dnrm.p, hn.data(), sizeof(float4) * (size_t)n, cudaMemcpyHostToDevice));
     CK(cudaMemset(derr.p, 0, sizeof(uint32_t)));
-    CK(nic::launch_to_bf16(dp.as<float>(), dwb.as<__nv_bfloat16>(), 0));
+    CK(nic::launch_to_bf16(dp.as<float>(), dwb.as<unsigned char>(), 0));
     nic::NicIO io{};
     io.pos = dpos.as<float4>();
     io.nrm = dnrm.as<float4>();
@@ -2422,7 +2422,7 @@ int pov_gpu_nic_eval(const float* params, const float* bounds, const float* poin
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     if (out) {
-        CK(nic::launch_forward(io, dwb.as<__nv_bfloat16>(), dp.as<float>(), derr.as<uint32_t>(), sms * 2, 0));
+        CK(nic::launch_forward(io, dwb.as<unsigned char>(), dp.as<float>(), derr.as<uint32_t>(), sms * 2, 0));
         std::vector<float4> ho((size_t)n);
         CK(cudaMemcpy(ho.data(), dout.p, sizeof(float4) * (size_t)n, cudaMemcpyDeviceToHost));
         for (int i = 0; i < n; i++) {
@@ -2439,7 +2439,7 @@ int pov_gpu_nic_eval(const float* params, const float* bounds, const float* poin
         CK(cudaMemset(dgrad.p, 0, sizeof(float) * NP));
         CK(cudaMemset(dloss.p, 0, sizeof(float)));
         io.target = dtg.as<float4>();
-        CK(nic::launch_train(io, dwb.as<__nv_bfloat16>(), dp.as<float>(), dgrad.as<float>(), dloss.as<float>(),
+        CK(nic::launch_train(io, dwb.as<unsigned char>(), dp.as<float>(), dgrad.as<float>(), dloss.as<float>(),
                              1.0f / (float)n, derr.as<uint32_t>(), sms, 0));
         CK(cudaMemcpy(grad, dgrad.p, sizeof(float) * NP, cudaMemcpyDeviceToHost));
         CK(cudaMemcpy(loss, dloss.p, sizeof(float), cudaMemcpyDeviceToHost));

@@ -49,14 +49,17 @@ constexpr uint32_t OFF_X0T = END_P_TRAIN, OFF_H1T = OFF_X0T + K1 * TILE * 2, OFF
 
 template <bool TRAIN> struct Map {
     static constexpr uint32_t BIAS = TRAIN ? END_T : END_P_FWD;          // 4*64 + 16 floats
-    static constexpr uint32_t BGRAD = BIAS + (4 * HID + NO) * 4;          // 64 floats
-    static constexpr uint32_t LOSS = BGRAD + HID * 4;                     // 4 floats
-    static constexpr uint32_t MBAR = LOSS + 16;                           // 8-byte aligned
-    static constexpr uint32_t TSLOT = MBAR + 8;
+    static constexpr uint32_t BGRAD = BIAS + (4 * HID + NO) * 4;          // 4 warps x 64 floats
+    static constexpr uint32_t LOSS = BGRAD + 4 * HID * 4;                 // 8 floats (1 + 4 warps used)
+    static constexpr uint32_t MBAR = LOSS + 32;                           // 8-byte aligned
+    static constexpr uint32_t CBAR = MBAR + 8;                            // bulk-copy barrier
+    static constexpr uint32_t TSLOT = CBAR + 8;
     static constexpr uint32_t BYTES = TSLOT + 8;
     static constexpr uint32_t TMEM_COLS = TRAIN ? 256 : 64;
 };
 static_assert(Map<true>::BYTES <= 227 * 1024, "training tile exceeds shared memory");
+static_assert(END_W == WIMG_FWD && OFF_W5T + NO * HID * 2 == WIMG_BWD, "weight image and tile map differ");
+static_assert(WIMG_FWD % 16 == 0 && WIMG_BWD % 16 == 0, "bulk copies move multiples of 16 bytes");
 static_assert(END_W >= OFF_W5T + NO * HID * 2, "transposed weights overflow the weight region");
 
 __device__ __forceinline__ void st_bf16(unsigned char* base, uint32_t off, float v)
@@ -68,22 +71,76 @@ __device__ __forceinline__ float ld_bf16(const unsigned char* base, uint32_t off
     return __bfloat162float(*reinterpret_cast<const __nv_bfloat16*>(base + off));
 }
 
-// rows x cols weights (row-major BF16 in global) into a K-major tile (K = cols)
-__device__ void load_w(unsigned char* dst, const __nv_bfloat16* __restrict__ w, int rows, int cols)
+// Byte offset of weight (r, k) of layer l (rows x cols, row-major [out][in])
+// in the weight image: its forward tile, and for l >= 1 its transposed tile.
+__device__ __forceinline__ uint32_t wimg_fwd(int l, int r, int k)
 {
-    for (int i = threadIdx.x; i < rows * cols; i += blockDim.x) {
-        int r = i / cols, k = i % cols;
-        *reinterpret_cast<__nv_bfloat16*>(dst + umma::kmajor_offset(r, k, cols)) = w[i];
-    }
+    const uint32_t base[5] = {OFF_W1, OFF_W2, OFF_W3, OFF_W4, OFF_W5};
+    return base[l] + umma::kmajor_offset(r, k, l == 0 ? K1 : HID);
+}
+__device__ __forceinline__ uint32_t wimg_bwd(int l, int r, int k)
+{
+    const uint32_t base[5] = {0, OFF_W2T, OFF_W3T, OFF_W4T, OFF_W5T};
+    return WIMG_FWD + base[l] + umma::kmajor_offset(k, r, l == 4 ? NO : HID);
 }
 
-// the transposed tile: W^T (cols x rows), K-major over rows
-__device__ void load_wt(unsigned char* dst, const __nv_bfloat16* __restrict__ w, int rows, int cols)
+// Layer, row and column of weight parameter i; false for a bias.
+__device__ __forceinline__ bool weight_of(int i, int& l, int& r, int& k)
 {
-    for (int i = threadIdx.x; i < rows * cols; i += blockDim.x) {
-        int r = i / cols, k = i % cols;
-        *reinterpret_cast<__nv_bfloat16*>(dst + umma::kmajor_offset(k, r, rows)) = w[i];
+    const int wb[5] = {P_W1, P_W2, P_W3, P_W4, P_W5}, we[5] = {P_B1, P_B2, P_B3, P_B4, P_B5};
+    for (l = 0; l < 5; l++)
+        if (i >= wb[l] && i < we[l]) {
+            const int cols = l == 0 ? K1 : HID;
+            r = (i - wb[l]) / cols;
+            k = (i - wb[l]) % cols;
+            return true;
+        }
+    return false;
+}
+
+__device__ __forceinline__ void wimg_store(unsigned char* img, int i, float p)
+{
+    int l, r, k;
+    if (!weight_of(i, l, r, k))
+        return;
+    const __nv_bfloat16 b = __float2bfloat16_rn(p);
+    *reinterpret_cast<__nv_bfloat16*>(img + wimg_fwd(l, r, k)) = b;
+    if (l > 0)
+        *reinterpret_cast<__nv_bfloat16*>(img + wimg_bwd(l, r, k)) = b;
+}
+
+// One bulk copy global -> shared (cp.async.bulk, completion counted on the
+// mbarrier in bytes), issued by thread 0; every thread waits.  Addresses and
+// size are multiples of 16.  False when the wait gave up.
+__device__ __forceinline__ bool bulk_load(unsigned char* sm, uint32_t dst_off, const unsigned char* src,
+                                          uint32_t bytes, uint64_t* cbar, uint32_t& phase)
+{
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(umma::smem_u32(cbar)),
+                     "r"(bytes)
+                     : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                umma::smem_u32(sm + dst_off)),
+            "l"(src), "r"(bytes), "r"(umma::smem_u32(cbar))
+            : "memory");
     }
+    const bool ok = umma::mbar_wait(cbar, phase);
+    phase ^= 1u;
+    return ok;
+}
+
+// Eight BF16 values as one 16-byte row of a core matrix.
+__device__ __forceinline__ void st_bf16x8(unsigned char* base, uint32_t off, const float* v)
+{
+    uint4 u;
+    __nv_bfloat162 h0 = __floats2bfloat162_rn(v[0], v[1]), h1 = __floats2bfloat162_rn(v[2], v[3]);
+    __nv_bfloat162 h2 = __floats2bfloat162_rn(v[4], v[5]), h3 = __floats2bfloat162_rn(v[6], v[7]);
+    u.x = *reinterpret_cast<uint32_t*>(&h0);
+    u.y = *reinterpret_cast<uint32_t*>(&h1);
+    u.z = *reinterpret_cast<uint32_t*>(&h2);
+    u.w = *reinterpret_cast<uint32_t*>(&h3);
+    *reinterpret_cast<uint4*>(base + off) = u;
 }
 
 // Feature f of the encoding (f < FEAT; FEAT..K1-1 are zero padding).
@@ -126,26 +183,35 @@ __device__ __forceinline__ void sync_for_mma()
 
 // Hidden-layer epilogue: this thread's row + bias, ReLU, BF16 into the next
 // input tile (row t, K = 64) and, training, into the transposed tile.
+// Returns the ReLU mask of this thread's row (bit c: the BF16 activation of
+// column c is positive), the backward pass's gate.
 template <bool TRAIN>
-__device__ __forceinline__ void hidden_epilogue(uint32_t taddr, const float* bias, unsigned char* sm,
-                                                uint32_t next_off, uint32_t ht_off)
+__device__ __forceinline__ uint64_t hidden_epilogue(uint32_t taddr, const float* bias, unsigned char* sm,
+                                                    uint32_t next_off, uint32_t ht_off)
 {
     const int t = threadIdx.x;
+    uint64_t mask = 0;
+#pragma unroll
     for (int c = 0; c < HID; c += 16) {
         float v[16];
         umma::tmem_ld16(taddr + c, v);
 #pragma unroll
         for (int j = 0; j < 16; j++) {
-            float h = fmaxf(v[j] + bias[c + j], 0.0f);
-            st_bf16(sm, next_off + umma::kmajor_offset(t, c + j, HID), h);
-            if (TRAIN)
-                st_bf16(sm, ht_off + umma::kmajor_offset(c + j, t, TILE), h);
+            v[j] = fmaxf(v[j] + bias[c + j], 0.0f);
+            if (TRAIN) {
+                st_bf16(sm, ht_off + umma::kmajor_offset(c + j, t, TILE), v[j]);
+                if (__bfloat162float(__float2bfloat16_rn(v[j])) > 0.0f)
+                    mask |= 1ull << (c + j);
+            }
         }
+        st_bf16x8(sm, next_off + umma::kmajor_offset(t, c, HID), v);
+        st_bf16x8(sm, next_off + umma::kmajor_offset(t, c + 8, HID), v + 8);
     }
+    return mask;
 }
 
 template <bool TRAIN>
-__global__ void __launch_bounds__(128, 1) k_nic(NicIO io, const __nv_bfloat16* __restrict__ wb,
+__global__ void __launch_bounds__(128, 1) k_nic(NicIO io, const unsigned char* __restrict__ wimg,
                                                const float* __restrict__ params, float* __restrict__ grad,
                                                float* __restrict__ loss, float inv_batch, uint32_t* err)
 {
@@ -153,6 +219,7 @@ __global__ void __launch_bounds__(128, 1) k_nic(NicIO io, const __nv_bfloat16* _
     using MP = Map<TRAIN>;
     const int t = threadIdx.x, warp = t >> 5;
     uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + MP::MBAR);
+    uint64_t* cbar = reinterpret_cast<uint64_t*>(sm + MP::CBAR);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + MP::TSLOT);
     float* sbias = reinterpret_cast<float*>(sm + MP::BIAS);
     float* sbgrad = reinterpret_cast<float*>(sm + MP::BGRAD);
@@ -161,27 +228,24 @@ __global__ void __launch_bounds__(128, 1) k_nic(NicIO io, const __nv_bfloat16* _
         umma::tmem_alloc(tslot, MP::TMEM_COLS);
     if (t == 0) {
         umma::mbar_init(mbar, 1);
+        umma::mbar_init(cbar, 1);
         asm volatile("fence.mbarrier_init.release.cluster;");
-        sloss[0] = 0.0f;
+        for (int w = 0; w < 5; w++)
+            sloss[w] = 0.0f;
     }
     for (int i = t; i < 4 * HID + NO; i += blockDim.x)
         sbias[i] = params[i < 4 * HID ? P_B1 + (i / HID) * (P_B2 - P_B1) + (i % HID) : P_B5 + (i - 4 * HID)];
-    if (TRAIN && t < HID)
-        sbgrad[t] = 0.0f;
+
     umma::fence_before_sync();
     __syncthreads();
     umma::fence_after_sync();
     const uint32_t tm = *tslot;
     const uint32_t lane = (uint32_t)(warp * 32) << 16;
     const uint32_t s0 = umma::smem_u32(sm);
-    uint32_t phase = 0;
+    uint32_t phase = 0, cphase = 0;
     bool ok = true;
     for (int tile = blockIdx.x; tile * TILE < io.n; tile += gridDim.x) {
-        load_w(sm + OFF_W1, wb + P_W1, HID, K1);
-        load_w(sm + OFF_W2, wb + P_W2, HID, HID);
-        load_w(sm + OFF_W3, wb + P_W3, HID, HID);
-        load_w(sm + OFF_W4, wb + P_W4, HID, HID);
-        load_w(sm + OFF_W5, wb + P_W5, NO, HID);
+        ok &= bulk_load(sm, OFF_W1, wimg, WIMG_FWD, cbar, cphase);   // the forward tiles
         const int i = tile * TILE + t;
         const bool valid = i < io.n;
         const int si = valid ? (io.idx ? io.idx[i] : i) : 0;
@@ -195,25 +259,30 @@ __global__ void __launch_bounds__(128, 1) k_nic(NicIO io, const __nv_bfloat16* _
             c6[4] = nv.y;
             c6[5] = nv.z;
         }
-        for (int f = 0; f < K1; f++) {
-            float v = valid ? feature(c6, f) : 0.0f;
-            st_bf16(sm, OFF_A0 + umma::kmajor_offset(t, f, K1), v);
-            if (TRAIN)
-                st_bf16(sm, OFF_X0T + umma::kmajor_offset(f, t, TILE), v);
+        for (int f0 = 0; f0 < K1; f0 += 8) {
+            float v8[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                v8[j] = valid ? feature(c6, f0 + j) : 0.0f;
+                if (TRAIN)
+                    st_bf16(sm, OFF_X0T + umma::kmajor_offset(f0 + j, t, TILE), v8[j]);
+            }
+            st_bf16x8(sm, OFF_A0 + umma::kmajor_offset(t, f0, K1), v8);
         }
         sync_for_mma();
         // forward: A0(112) -> A1 -> A0 -> A1 -> A0 -> out
         ok &= layer_mma(tm, s0 + OFF_A0, s0 + OFF_W1, K1, HID, mbar, phase);
-        hidden_epilogue<TRAIN>(tm + lane, sbias + 0 * HID, sm, OFF_A1, OFF_H1T);
+        uint64_t relu[4];
+        relu[0] = hidden_epilogue<TRAIN>(tm + lane, sbias + 0 * HID, sm, OFF_A1, OFF_H1T);
         sync_for_mma();
         ok &= layer_mma(tm, s0 + OFF_A1, s0 + OFF_W2, HID, HID, mbar, phase);
-        hidden_epilogue<TRAIN>(tm + lane, sbias + 1 * HID, sm, OFF_A0, OFF_H2T);
+        relu[1] = hidden_epilogue<TRAIN>(tm + lane, sbias + 1 * HID, sm, OFF_A0, OFF_H2T);
         sync_for_mma();
         ok &= layer_mma(tm, s0 + OFF_A0, s0 + OFF_W3, HID, HID, mbar, phase);
-        hidden_epilogue<TRAIN>(tm + lane, sbias + 2 * HID, sm, OFF_A1, OFF_H3T);
+        relu[2] = hidden_epilogue<TRAIN>(tm + lane, sbias + 2 * HID, sm, OFF_A1, OFF_H3T);
         sync_for_mma();
         ok &= layer_mma(tm, s0 + OFF_A1, s0 + OFF_W4, HID, HID, mbar, phase);
-        hidden_epilogue<TRAIN>(tm + lane, sbias + 3 * HID, sm, OFF_A0, OFF_H4T);
+        relu[3] = hidden_epilogue<TRAIN>(tm + lane, sbias + 3 * HID, sm, OFF_A0, OFF_H4T);
         sync_for_mma();
         ok &= layer_mma(tm, s0 + OFF_A0, s0 + OFF_W5, HID, NO, mbar, phase);
         float y[16];
@@ -247,13 +316,14 @@ __global__ void __launch_bounds__(128, 1) k_nic(NicIO io, const __nv_bfloat16* _
             }
             dz[c] = g;
         }
-        atomicAdd(&sloss[0], lsum);
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1)
+            lsum += __shfl_xor_sync(0xffffffffu, lsum, off);
+        if ((t & 31) == 0)
+            sloss[1 + warp] += lsum;   // one partial per warp, summed at the end
         // the weight region now holds the transposed weights; rows 16..63
         // of dZ^T are cleared for the 16-output layer
-        load_wt(sm + OFF_W2T, wb + P_W2, HID, HID);
-        load_wt(sm + OFF_W3T, wb + P_W3, HID, HID);
-        load_wt(sm + OFF_W4T, wb + P_W4, HID, HID);
-        load_wt(sm + OFF_W5T, wb + P_W5, NO, HID);
+        ok &= bulk_load(sm, OFF_W2T, wimg + WIMG_FWD, WIMG_BWD, cbar, cphase);
         // the forward pass reused the dZ^T region: its padded rows are
         // cleared again (rows 16..127 for the 16-output layer; 64..127 stay)
         for (int r = NO; r < TILE; r++)
@@ -265,10 +335,22 @@ __global__ void __launch_bounds__(128, 1) k_nic(NicIO io, const __nv_bfloat16* _
         for (int l = 4; l >= 0; l--) {
             const int nout = l == 4 ? NO : HID;
             const int nin = l == 0 ? K1 : HID;
-            for (int o = 0; o < nout; o++) {
-                st_bf16(sm, OFF_DZ + umma::kmajor_offset(t, o, nout), dz[o]);
-                st_bf16(sm, OFF_DZT + umma::kmajor_offset(o, t, TILE), dz[o]);
-                atomicAdd(&sbgrad[o], dz[o]);
+            for (int o = 0; o < nout; o += 8) {
+                float d8[8];
+#pragma unroll
+                for (int j = 0; j < 8; j++) {
+                    d8[j] = dz[o + j];
+                    st_bf16(sm, OFF_DZT + umma::kmajor_offset(o + j, t, TILE), d8[j]);
+                    // bias gradient: the warp's sum of this column, one
+                    // shared partial per warp (no shared-memory atomics)
+                    float w = d8[j];
+#pragma unroll
+                    for (int off = 16; off > 0; off >>= 1)
+                        w += __shfl_xor_sync(0xffffffffu, w, off);
+                    if ((t & 31) == 0)
+                        sbgrad[warp * HID + o + j] = w;
+                }
+                st_bf16x8(sm, OFF_DZ + umma::kmajor_offset(t, o, nout), d8);
             }
             sync_for_mma();
             if (t == 0) {
@@ -294,23 +376,21 @@ __global__ void __launch_bounds__(128, 1) k_nic(NicIO io, const __nv_bfloat16* _
                         atomicAdd(&grad[wofs[l] + t * nin + c + j], v[j]);
             }
             if (l > 0) {
+                const uint64_t m = relu[l - 1];   // the input of layer l is hidden layer l's output
+#pragma unroll
                 for (int c = 0; c < HID; c += 16) {
                     float v[16];
                     umma::tmem_ld16(tm + lane + c, v);
 #pragma unroll
-                    for (int j = 0; j < 16; j++) {
-                        float h = ld_bf16(sm, ht_off[l] + umma::kmajor_offset(c + j, t, TILE));
-                        dz[c + j] = h > 0.0f ? v[j] : 0.0f;
-                    }
+                    for (int j = 0; j < 16; j++)
+                        dz[c + j] = ((m >> (c + j)) & 1ull) ? v[j] : 0.0f;
                 }
             }
             umma::fence_before_sync();
             __syncthreads();
             umma::fence_after_sync();
-            if (t < nout) {
-                atomicAdd(&grad[bofs[l] + t], sbgrad[t]);
-                sbgrad[t] = 0.0f;
-            }
+            if (t < nout)
+                atomicAdd(&grad[bofs[l] + t], sbgrad[t] + sbgrad[HID + t] + sbgrad[2 * HID + t] + sbgrad[3 * HID + t]);
             __syncthreads();
         }
     }
@@ -320,7 +400,7 @@ __global__ void __launch_bounds__(128, 1) k_nic(NicIO io, const __nv_bfloat16* _
     if (warp == 0)
         umma::tmem_dealloc(tm, MP::TMEM_COLS);
     if (TRAIN && t == 0)
-        atomicAdd(loss, sloss[0]);
+        atomicAdd(loss, sloss[1] + sloss[2] + sloss[3] + sloss[4]);
     if (!ok && t == 0)
         atomicOr(err, DE_ITERATION_CAP);
 }
@@ -328,7 +408,7 @@ __global__ void __launch_bounds__(128, 1) k_nic(NicIO io, const __nv_bfloat16* _
 // Adam on the FP32 master parameters; refreshes the BF16 copy.  Parameters
 // of the padded output rows stay zero.
 __global__ void k_nic_adam(float* __restrict__ params, float* __restrict__ m, float* __restrict__ v,
-                           const float* __restrict__ grad, __nv_bfloat16* __restrict__ wb, float lr, float b1,
+                           const float* __restrict__ grad, unsigned char* __restrict__ wimg, float lr, float b1,
                            float b2, float eps, float c1, float c2)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NPARAM; i += gridDim.x * blockDim.x) {
@@ -340,21 +420,21 @@ __global__ void k_nic_adam(float* __restrict__ params, float* __restrict__ m, fl
         v[i] = vi;
         float p = pad ? 0.0f : params[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
         params[i] = p;
-        wb[i] = __float2bfloat16_rn(p);
+        wimg_store(wimg, i, p);
     }
 }
 
-__global__ void k_nic_to_bf16(const float* __restrict__ params, __nv_bfloat16* __restrict__ wb)
+__global__ void k_nic_to_bf16(const float* __restrict__ params, unsigned char* __restrict__ wimg)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NPARAM; i += gridDim.x * blockDim.x)
-        wb[i] = __float2bfloat16_rn(params[i]);
+        wimg_store(wimg, i, params[i]);
 }
 
 }  // namespace
 
 size_t smem_bytes(bool train) { return train ? Map<true>::BYTES : Map<false>::BYTES; }
 
-cudaError_t launch_forward(const NicIO& io, const __nv_bfloat16* wb, const float* params, uint32_t* err, int grid,
+cudaError_t launch_forward(const NicIO& io, const unsigned char* wimg, const float* params, uint32_t* err, int grid,
                            cudaStream_t st)
 {
     if (io.n <= 0)
@@ -368,12 +448,12 @@ cudaError_t launch_forward(const NicIO& io, const __nv_bfloat16* wb, const float
         attr = true;
     }
     int tiles = (io.n + TILE - 1) / TILE;
-    k_nic<false><<<grid < tiles ? grid : tiles, TILE, Map<false>::BYTES, st>>>(io, wb, params, nullptr, nullptr,
+    k_nic<false><<<grid < tiles ? grid : tiles, TILE, Map<false>::BYTES, st>>>(io, wimg, params, nullptr, nullptr,
                                                                                0.0f, err);
     return cudaGetLastError();
 }
 
-cudaError_t launch_train(const NicIO& io, const __nv_bfloat16* wb, const float* params, float* grad, float* loss,
+cudaError_t launch_train(const NicIO& io, const unsigned char* wimg, const float* params, float* grad, float* loss,
                          float inv_batch, uint32_t* err, int grid, cudaStream_t st)
 {
     if (io.n <= 0)
@@ -387,23 +467,23 @@ cudaError_t launch_train(const NicIO& io, const __nv_bfloat16* wb, const float* 
         attr = true;
     }
     int tiles = (io.n + TILE - 1) / TILE;
-    k_nic<true><<<grid < tiles ? grid : tiles, TILE, Map<true>::BYTES, st>>>(io, wb, params, grad, loss, inv_batch,
+    k_nic<true><<<grid < tiles ? grid : tiles, TILE, Map<true>::BYTES, st>>>(io, wimg, params, grad, loss, inv_batch,
                                                                              err);
     return cudaGetLastError();
 }
 
-cudaError_t launch_adam(float* params, float* m, float* v, const float* grad, __nv_bfloat16* wb, float lr, int step,
+cudaError_t launch_adam(float* params, float* m, float* v, const float* grad, unsigned char* wimg, float lr, int step,
                         cudaStream_t st)
 {
     const float b1 = 0.9f, b2 = 0.99f, eps = 1e-8f;
     float c1 = 1.0f - powf(b1, (float)step), c2 = 1.0f - powf(b2, (float)step);
-    k_nic_adam<<<(NPARAM + 255) / 256, 256, 0, st>>>(params, m, v, grad, wb, lr, b1, b2, eps, c1, c2);
+    k_nic_adam<<<(NPARAM + 255) / 256, 256, 0, st>>>(params, m, v, grad, wimg, lr, b1, b2, eps, c1, c2);
     return cudaGetLastError();
 }
 
-cudaError_t launch_to_bf16(const float* params, __nv_bfloat16* wb, cudaStream_t st)
+cudaError_t launch_to_bf16(const float* params, unsigned char* wimg, cudaStream_t st)
 {
-    k_nic_to_bf16<<<(NPARAM + 255) / 256, 256, 0, st>>>(params, wb);
+    k_nic_to_bf16<<<(NPARAM + 255) / 256, 256, 0, st>>>(params, wimg);
     return cudaGetLastError();
 }
 

@@ -36,16 +36,24 @@ struct NicIO {
     float3        lo, scale;
 };
 
+// The BF16 weights as the kernels' shared-memory tiles want them (the
+// "weight image", written by the Adam step): the forward tiles W1..W5 then
+// the transposed tiles W2^T..W5^T of the backward pass, each K-major in
+// 8x16-byte core matrices, so a CTA fetches them with one bulk copy each.
+constexpr uint32_t WIMG_FWD = (HID * K1 + 3 * HID * HID + NO * HID) * 2;
+constexpr uint32_t WIMG_BWD = (3 * HID * HID + NO * HID) * 2;
+constexpr uint32_t WIMG_BYTES = WIMG_FWD + WIMG_BWD;
+
 size_t smem_bytes(bool train);
-cudaError_t launch_forward(const NicIO& io, const __nv_bfloat16* wb, const float* params, uint32_t* err, int grid,
+cudaError_t launch_forward(const NicIO& io, const unsigned char* wimg, const float* params, uint32_t* err, int grid,
                            cudaStream_t st);
 // Accumulates the gradient of (1/batch) * sum (p - y)^2 / (p^2 + 0.01) into
 // grad and the loss into *loss.
-cudaError_t launch_train(const NicIO& io, const __nv_bfloat16* wb, const float* params, float* grad, float* loss,
+cudaError_t launch_train(const NicIO& io, const unsigned char* wimg, const float* params, float* grad, float* loss,
                          float inv_batch, uint32_t* err, int grid, cudaStream_t st);
-cudaError_t launch_adam(float* params, float* m, float* v, const float* grad, __nv_bfloat16* wb, float lr, int step,
+cudaError_t launch_adam(float* params, float* m, float* v, const float* grad, unsigned char* wimg, float lr, int step,
                         cudaStream_t st);
-cudaError_t launch_to_bf16(const float* params, __nv_bfloat16* wb, cudaStream_t st);
+cudaError_t launch_to_bf16(const float* params, unsigned char* wimg, cudaStream_t st);
 
 }  // namespace nic
 }  // namespace povgpu
