@@ -486,7 +486,8 @@ constexpr int RAD_ROUNDS = 8;                    // query rounds before every op
 struct RadiosityState {
     bool            enabled = false;
     PovGpuRadiosity set{};
-    DevBuf          blocks, next, count, keys, heads, range, occupancy, rstats;
+    DevBuf          blocks, quick, bslot, members, count, keys, seg_off, seg_cnt, seg_cur, range, occupancy, rstats;
+    bool            seg_dirty = false;   // blocks added since the node segments were rebuilt
     int             cap_blocks = 0;
     uint32_t        key_mask = 0;
     bool            dirs_uploaded = false;
@@ -508,7 +509,8 @@ struct RadiosityState {
     DevBuf          nic_params, nic_wb, nic_m, nic_v, nic_grad, nic_loss, nic_idx, nic_pred, nic_err;
     void release()
     {
-        DevBuf* all[] = {&blocks, &next, &count, &keys, &heads, &range, &occupancy, &rstats, &nic_params, &nic_wb, &nic_m,
+        DevBuf* all[] = {&blocks, &quick, &bslot, &members, &count, &keys, &seg_off, &seg_cnt, &seg_cur, &range,
+                         &occupancy, &rstats, &nic_params, &nic_wb, &nic_m,
                          &nic_v, &nic_grad, &nic_loss, &nic_idx, &nic_pred, &nic_err};
         for (DevBuf* b : all)
             b->release();
@@ -1197,10 +1199,14 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
         size_t slots = 1u << 22;
         R.key_mask = (uint32_t)(slots - 1);
         CK(R.blocks.ensure(sizeof(RadBlock) * (size_t)R.cap_blocks));
-        CK(R.next.ensure(sizeof(int32_t) * (size_t)R.cap_blocks));
-        CK(R.count.ensure(sizeof(int32_t)));
+        CK(R.quick.ensure(sizeof(float4) * (size_t)R.cap_blocks));
+        CK(R.bslot.ensure(sizeof(int32_t) * (size_t)R.cap_blocks));
+        CK(R.members.ensure(sizeof(int32_t) * (size_t)R.cap_blocks));
+        CK(R.count.ensure(sizeof(int32_t) * 2));   // block count, rebuild allocation cursor
         CK(R.keys.ensure(sizeof(unsigned long long) * slots));
-        CK(R.heads.ensure(sizeof(int32_t) * slots));
+        CK(R.seg_off.ensure(sizeof(int32_t) * slots));
+        CK(R.seg_cnt.ensure(sizeof(int32_t) * slots));
+        CK(R.seg_cur.ensure(sizeof(int32_t) * slots));
         CK(R.range.ensure(sizeof(int32_t) * 2 * RAD_LEVELS));
         CK(R.occupancy.ensure(1u << 21));   // 2^24 occupancy bits
         CK(R.rstats.ensure(sizeof(unsigned long long) * RST_COUNT));
@@ -1353,11 +1359,16 @@ RadCacheView cache_view(PovGpuScene* sc)
     RadiosityState& R = sc->rad;
     RadCacheView c{};
     c.blocks = R.blocks.as<RadBlock>();
-    c.next = R.next.as<int32_t>();
+    c.quick = R.quick.as<float4>();
+    c.bslot = R.bslot.as<int32_t>();
     c.count = R.count.as<int32_t>();
     c.cap = R.cap_blocks;
     c.keys = R.keys.as<unsigned long long>();
-    c.heads = R.heads.as<int32_t>();
+    c.seg_off = R.seg_off.as<int32_t>();
+    c.seg_cnt = R.seg_cnt.as<int32_t>();
+    c.seg_cur = R.seg_cur.as<int32_t>();
+    c.members = R.members.as<int32_t>();
+    c.seg_total = R.count.as<int32_t>() + 1;
     c.mask = R.key_mask;
     c.size_range = R.range.as<int32_t>();
     c.occupancy = R.occupancy.as<uint32_t>();
@@ -1373,7 +1384,7 @@ int rad_reset(PovGpuScene* sc)
     cudaStream_t st = sc->active();
     CK(cudaMemsetAsync(R.count.p, 0, sizeof(int32_t), st));
     CK(cudaMemsetAsync(R.keys.p, 0, R.keys.bytes, st));
-    CK(cudaMemsetAsync(R.heads.p, 0xff, R.heads.bytes, st));
+    R.seg_dirty = false;   // no blocks, no node keys
     int32_t range[2 * RAD_LEVELS];
     for (int d = 0; d < RAD_LEVELS; d++) {
         range[2 * d] = 1 << 30;
@@ -1602,6 +1613,7 @@ int rad_gather(PovGpuScene* sc, StageClock& clk, int d, const RadQuery* queries,
                             R.rstats.as<unsigned long long>(), sc->err.as<uint32_t>(),
                             std::max(1, std::min(sc->num_sms * 16, (ns * 32 + 127) / 128)), st));
     CK(clk.end());
+    R.seg_dirty = true;   // the new blocks join their nodes at the next query round
     return POV_GPU_OK;
 }
 
@@ -1632,10 +1644,16 @@ int rad_resolve(PovGpuScene* sc, StageClock& clk, int d, const RadQuery* queries
         CK(cudaMemsetAsync(cn, 0, sizeof(int) * 2, st));
         CK(cudaMemsetAsync(L.claims.p, 0, L.claims.bytes, st));
         CK(clk.begin(POV_GPU_STAGE_RADIOSITY));
+        if (R.seg_dirty) {   // file the blocks added since the last rebuild
+            CK(launch_seg_rebuild(C, sc->num_sms * 4, st));
+            R.seg_dirty = false;
+        }
+        // one warp per open query
+        const int qgrid = std::max(1, std::min(sc->num_sms * 16, (int)(((long)n_open * 32 + 127) / 128)));
         CK(launch_rad_query(sc->S, C, P, queries, open, n_open, n, round, last_round, out,
                             L.partial.as<float4>(), L.claims.as<unsigned long long>(), L.claim_mask(),
                             L.seeds.as<int>(), cn, nxt, cn + 1, R.rstats.as<unsigned long long>(),
-                            sc->err.as<uint32_t>(), grid, st));
+                            sc->err.as<uint32_t>(), qgrid, st));
         CK(clk.end());
         int hc[2] = {0, 0};
         CK(cudaMemcpyAsync(hc, cn, sizeof(hc), cudaMemcpyDeviceToHost, st));

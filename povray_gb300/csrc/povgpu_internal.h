@@ -235,14 +235,22 @@ struct __align__(16) RadBlock {
 };
 
 // The sample cache in device memory: blocks, and the octree nodes as an
-// open-addressing hash (64-bit node key -> head of the node's block list).
+// open-addressing hash (64-bit node key -> slot).  Each node's blocks sit
+// contiguously in `members` (segment seg_off/seg_cnt of the node's slot),
+// rebuilt from every block's slot after blocks are added, so a lookup reads
+// a node's blocks with independent loads instead of chasing a list.
 struct RadCacheView {
     RadBlock*           blocks;
-    int32_t*            next;
+    float4*             quick;      // per block: point, harmonic mean distance (the quick reuse test)
+    int32_t*            bslot;      // per block: the hash slot of its node
     int32_t*            count;      // blocks in use (device word)
     int32_t             cap;
     unsigned long long* keys;       // 0 = empty slot
-    int32_t*            heads;
+    int32_t*            seg_off;    // per slot: first entry of the node's blocks in members
+    int32_t*            seg_cnt;    // per slot: number of the node's blocks
+    int32_t*            seg_cur;    // per slot: rebuild cursor / allocation flag
+    int32_t*            members;    // block indices grouped by node
+    int32_t*            seg_total;  // rebuild: entries allocated (device word)
     uint32_t            mask;       // slots - 1
     int32_t*            size_range; // per bounce depth d: [2d] smallest, [2d+1] largest node size in use
     uint32_t*           occupancy;  // one bit per hashed node key: set once the node holds a block

@@ -82,14 +82,14 @@ __device__ __forceinline__ unsigned long long node_key(int size, int x, int y, i
     return h ? h : 1ull;
 }
 
-// Head of the node's block list, -1 when the node holds nothing.
+// Slot of the node, -1 when the node holds nothing.
 __device__ __forceinline__ int node_lookup(const RadCacheView& C, unsigned long long key)
 {
     uint32_t slot = (uint32_t)key & C.mask;
     for (int n = 0; n < MAX_PROBES; n++) {
         unsigned long long k = C.keys[slot];
         if (k == key)
-            return C.heads[slot];
+            return (int)slot;
         if (k == 0ull)
             return -1;
         slot = (slot + 1) & C.mask;
@@ -194,44 +194,77 @@ __device__ __forceinline__ uint32_t occ_bit(const RadCacheView& C, unsigned long
     return (uint32_t)(key >> 29) & C.occ_mask;
 }
 
-// RadiosityCache::FindReusableBlock (radiosity.cpp:1458-1512).  Nodes are
-// keyed per bounce depth (ot_dist_traverse passes only blocks of the query's
-// depth to AverageNearBlock, octree.cpp:843), so lists hold one depth; the
-// occupancy bits skip the probe of nodes that hold nothing.
-__device__ void find_reusable(const RadCacheView& C, int smin, int smax, float3 P, float3 N, float eb, int depth,
-                              bool final_trace, float& W, float3& WI)
+// RadiosityCache::FindReusableBlock (radiosity.cpp:1458-1512), one warp per
+// query.  Nodes are keyed per bounce depth (ot_dist_traverse passes only
+// blocks of the query's depth to AverageNearBlock, octree.cpp:843), so lists
+// hold one depth; the occupancy bits skip the probe of nodes that hold
+// nothing.  The candidate nodes -- per node size in use, the cells of the
+// 2x2x2 neighbourhood whose half-size-extended interval holds the point
+// (ot_point_in_node) -- are dealt to the lanes, each lane walks its nodes'
+// block lists, and the warp sums the weights (every lane gets the sums).
+__device__ void find_reusable_warp(const RadCacheView& C, int smin, int smax, float3 P, float3 N, float eb,
+                                   int depth, bool final_trace, int lane, float& W, float3& WI)
 {
     W = 0.0f;
     WI = f3(0.f, 0.f, 0.f);
     const double c[3] = {(double)P.x + OT_BIAS, (double)P.y + OT_BIAS, (double)P.z + OT_BIAS};
-    for (int size = smin; size <= smax; size++) {
-        const double s = biased_pow2(size), inv = 1.0 / s;   // powers of two: exact
-        // ot_point_in_node per axis: of the cells b+1, b+2 (b = floor(c/s - 1.5))
-        // those whose half-size-extended interval holds the coordinate
-        int base[3];
-        uint32_t ok[3];
-        for (int a = 0; a < 3; a++) {
-            int b = (int)floor(c[a] * inv - 1.5);
-            base[a] = b + 1;
-            ok[a] = (fabs(c[a] - ((double)b + 1.5) * s) < s ? 1u : 0u) |
-                    (fabs(c[a] - ((double)b + 2.5) * s) < s ? 2u : 0u);
+    const float pf[3] = {P.x, P.y, P.z};
+    const int ncand = (smax - smin + 1) * 8;
+    for (int cand = lane; cand < ncand; cand += 32) {
+        const int size = smin + (cand >> 3), k = cand & 7;
+        const int d3[3] = {k & 1, (k >> 1) & 1, k >> 2};
+        int cell[3];
+        bool in = true;
+        const int e = size - 127;   // node edge 2^e
+        if (e >= -7 && e <= 7) {
+            // OT_BIAS = 10^7 = 2^7 * 78125 is a whole number of such nodes,
+            // so the node grid is the unbiased one shifted by 10^7 / 2^e
+            // nodes: the same cells and the same inside test in FP32
+            const float sf = __int_as_float((e + 127) << 23), invf = __int_as_float((127 - e) << 23);
+            const int shift = e >= 0 ? (10000000 >> e) : (10000000 << -e);
+            for (int a = 0; a < 3; a++) {
+                const float bu = floorf(pf[a] * invf - 1.5f);
+                cell[a] = (int)bu + shift + 1 + d3[a];
+                in = in && fabsf(pf[a] - (bu + 1.5f + (float)d3[a]) * sf) < sf;
+            }
+        } else {
+            const double s = biased_pow2(size), inv = 1.0 / s;   // powers of two: exact
+            for (int a = 0; a < 3; a++) {
+                const int b = (int)floor(c[a] * inv - 1.5);
+                cell[a] = b + 1 + d3[a];
+                in = in && fabs(c[a] - ((double)b + 1.5 + d3[a]) * s) < s;
+            }
         }
-        for (int k = 0; k < 8; k++) {
-            const int dx = k & 1, dy = (k >> 1) & 1, dz = k >> 2;
-            if (!((ok[0] >> dx) & (ok[1] >> dy) & (ok[2] >> dz) & 1u))
-                continue;
-            unsigned long long key = node_key(size + 256 * depth, base[0] + dx, base[1] + dy, base[2] + dz);
-            uint32_t bit = occ_bit(C, key);
-            if (!((C.occupancy[bit >> 5] >> (bit & 31)) & 1u))
-                continue;
-            int bi = node_lookup(C, key);
-            for (int n = 0; bi >= 0 && n < (1 << 20); n++) {
+        if (!in)
+            continue;
+        const unsigned long long key = node_key(size + 256 * depth, cell[0], cell[1], cell[2]);
+        const uint32_t bit = occ_bit(C, key);
+        if (!((C.occupancy[bit >> 5] >> (bit & 31)) & 1u))
+            continue;
+        const int slot = node_lookup(C, key);
+        if (slot < 0)
+            continue;
+        const int off = C.seg_off[slot], cnt = min(C.seg_cnt[slot], C.cap);
+        for (int j = 0; j < cnt; j++) {
+            // the quick test (AverageNearBlock's first check) on the 16-byte
+            // record; the whole block only for the blocks that pass it
+            const int bi = C.members[off + j];
+            const float4 qk = C.quick[bi];
+            const float3 dl = sub(P, xyz(qk));
+            const float qr = qk.w * eb;
+            if (dot(dl, dl) < qr * qr) {
                 RadBlock blk = C.blocks[bi];
                 if (__float_as_int(blk.ill.w) == depth)
                     average_near(blk, P, N, eb, final_trace, W, WI);
-                bi = C.next[bi];
             }
         }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        W += __shfl_xor_sync(0xffffffffu, W, off);
+        WI.x += __shfl_xor_sync(0xffffffffu, WI.x, off);
+        WI.y += __shfl_xor_sync(0xffffffffu, WI.y, off);
+        WI.z += __shfl_xor_sync(0xffffffffu, WI.z, off);
     }
 }
 
@@ -242,6 +275,49 @@ __device__ __forceinline__ float4 finish_ambient(float3 a, float quality, const 
     a = f3((a.x * (1.0f - R.gray) + R.gray * grey) * R.brightness, (a.y * (1.0f - R.gray) + R.gray * grey) * R.brightness,
            (a.z * (1.0f - R.gray) + R.gray * grey) * R.brightness);
     return make_float4(a.x, a.y, a.z, quality);
+}
+
+// Node segments rebuilt from every block's slot (a counting sort by node):
+// reset the touched slots, count, give each node its segment, file the blocks.
+__global__ void k_seg_reset(RadCacheView C)
+{
+    const int n = min(*C.count, C.cap);
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < n; b += gridDim.x * blockDim.x) {
+        const int s = C.bslot[b];
+        if (s < 0)
+            continue;
+        C.seg_cnt[s] = 0;
+        C.seg_cur[s] = 0;
+    }
+}
+__global__ void k_seg_count(RadCacheView C)
+{
+    const int n = min(*C.count, C.cap);
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < n; b += gridDim.x * blockDim.x)
+        if (C.bslot[b] >= 0)
+            atomicAdd(&C.seg_cnt[C.bslot[b]], 1);
+}
+__global__ void k_seg_alloc(RadCacheView C)
+{
+    const int n = min(*C.count, C.cap);
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < n; b += gridDim.x * blockDim.x) {
+        const int s = C.bslot[b];
+        if (s >= 0 && atomicCAS(&C.seg_cur[s], 0, -1) == 0)   // the node's first block allocates
+            C.seg_off[s] = atomicAdd(C.seg_total, C.seg_cnt[s]);
+    }
+}
+__global__ void k_seg_fill(RadCacheView C)
+{
+    const int n = min(*C.count, C.cap);
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < n; b += gridDim.x * blockDim.x) {
+        const int s = C.bslot[b];
+        if (s < 0)
+            continue;
+        // after the allocation seg_cur holds -1 and counts down: -1 - old is
+        // the block's place in its node's segment
+        const int old = atomicSub(&C.seg_cur[s], 1);
+        C.members[C.seg_off[s] + (-1 - old)] = b;
+    }
 }
 
 // One thread per open query: the cache lookup of ComputeAmbient
@@ -257,7 +333,10 @@ __global__ void k_rad_query(DeviceScene S, RadCacheView C, RadParams R, const Ra
 {
     const int n = min(n_open, cap);
     const int smin = C.size_range[2 * R.depth], smax = C.size_range[2 * R.depth + 1];
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    unsigned long long reused = 0;   // this warp's reused queries (lane 0), one atomic at the end
+    for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += nwarps) {   // one warp per query
         int qi = open ? open[i] : i;
         RadQuery q = queries[qi];
         float3 P = xyz(q.p), N = xyz(q.n);
@@ -268,12 +347,14 @@ __global__ void k_rad_query(DeviceScene S, RadCacheView C, RadParams R, const Ra
         float W = 0.f;
         float3 WI = f3(0.f, 0.f, 0.f);
         if (smax >= smin)
-            find_reusable(C, smin, smax, P, N, eb, R.depth, R.final_trace != 0, W, WI);
+            find_reusable_warp(C, smin, smax, P, N, eb, R.depth, R.final_trace != 0, lane, W, WI);
+        if (lane != 0)
+            continue;
         bool reuse = W * 4.0f >= (float)R.reuse_count || (R.final_trace && !R.always_sample && W > 0.0f);
         if (reuse) {
             float3 a = mul(WI, 1.0f / W);
             out[qi] = finish_ambient(a, fminf(4.0f * W / (float)R.reuse_count, 1.0f), R);
-            atomicAdd(&rstats[RST_REUSED], 1ull);
+            reused++;
             continue;
         }
         partial[qi] = make_float4(WI.x, WI.y, WI.z, W);
@@ -303,6 +384,8 @@ __global__ void k_rad_query(DeviceScene S, RadCacheView C, RadParams R, const Ra
             if (s < cap) next[s] = qi; else atomicOr(err, DE_QUEUE_OVERFLOW);
         }
     }
+    if (reused)
+        atomicAdd(&rstats[RST_REUSED], reused);
 }
 
 // Direction k of seed s: entry (base + s*count + k) of the direction pool,
@@ -439,18 +522,19 @@ __global__ void k_gather_reduce(DeviceScene S, RadCacheView C, RadParams R, cons
                 blk.tn = make_float4(tn.x, tn.y, tn.z, quality_s);
                 blk.ill = make_float4(ill.x, ill.y, ill.z, __int_as_float(R.depth));
                 C.blocks[b] = blk;
+                C.quick[b] = blk.p;
                 int size, x, y, z;
                 ot_index_sphere(P, (double)mean * R.address_factor, size, x, y, z);
                 unsigned long long key = node_key(size + 256 * R.depth, x, y, z);
                 int slot = node_insert(C, key);
                 if (slot >= 0) {
-                    __threadfence();
-                    C.next[b] = atomicExch(&C.heads[slot], b);
+                    C.bslot[b] = slot;   // filed into the node's segment by the next rebuild
                     uint32_t bit = occ_bit(C, key);
                     atomicOr(&C.occupancy[bit >> 5], 1u << (bit & 31));
                     atomicMin(&C.size_range[2 * R.depth], size);
                     atomicMax(&C.size_range[2 * R.depth + 1], size);
                 } else {
+                    C.bslot[b] = -1;
                     atomicOr(err, DE_CACHE_FULL);
                 }
             } else {
@@ -485,6 +569,18 @@ inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
 cudaError_t rad_upload_directions(const float* xyz3)
 {
     return cudaMemcpyToSymbol(c_dirs, xyz3, sizeof(float3) * RAD_DIRECTIONS);
+}
+
+cudaError_t launch_seg_rebuild(const RadCacheView& C, int grid, cudaStream_t st)
+{
+    cudaError_t e = cudaMemsetAsync(C.seg_total, 0, sizeof(int32_t), st);
+    if (e != cudaSuccess)
+        return e;
+    k_seg_reset<<<grid, 256, 0, st>>>(C);
+    k_seg_count<<<grid, 256, 0, st>>>(C);
+    k_seg_alloc<<<grid, 256, 0, st>>>(C);
+    k_seg_fill<<<grid, 256, 0, st>>>(C);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_rad_query(const DeviceScene& S, const RadCacheView& C, const RadParams& R, const RadQuery* queries,

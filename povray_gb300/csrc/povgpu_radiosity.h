@@ -19,6 +19,8 @@ enum RadStatIdx {
 // The Halton(2,3) cosine-weighted direction pool, 3 floats per direction.
 cudaError_t rad_upload_directions(const float* xyz3);
 
+// Rebuilds the node segments from every block's slot (after blocks were added).
+cudaError_t launch_seg_rebuild(const RadCacheView& C, int grid, cudaStream_t st);
 cudaError_t launch_rad_query(const DeviceScene& S, const RadCacheView& C, const RadParams& R, const RadQuery* queries,
                              const int* open, int n_open, int cap, int round, int last_round, float4* out,
                              float4* partial, unsigned long long* claims, uint32_t claim_mask, int* seeds,
