@@ -57,6 +57,14 @@ __device__ __forceinline__ float to_eye(const DeviceScene& S, float3 p)
     return (float)sqrt(dx * dx + dy * dy + dz * dz);
 }
 
+// The same distance in FP32, for the rounds' claim cells (a GPU schedule,
+// not a reference decision).
+__device__ __forceinline__ float to_eye_f(const DeviceScene& S, float3 p)
+{
+    float dx = (float)S.cam_loc[0] - p.x, dy = (float)S.cam_loc[1] - p.y, dz = (float)S.cam_loc[2] - p.z;
+    return sqrtf(dx * dx + dy * dy + dz * dz);
+}
+
 // Pow2Floor / BiasedIntLog2 / BiasedIntPow2 (octree.cpp:169-250).
 __device__ __forceinline__ float pow2_floor(float a) { return __uint_as_float(__float_as_uint(a) & 0xFF800000u); }
 __device__ __forceinline__ int biased_log2(float a) { return (int)((__float_as_uint(a) & 0x7F800000u) >> 23); }
@@ -207,7 +215,6 @@ __device__ void find_reusable_warp(const RadCacheView& C, int smin, int smax, fl
 {
     W = 0.0f;
     WI = f3(0.f, 0.f, 0.f);
-    const double c[3] = {(double)P.x + OT_BIAS, (double)P.y + OT_BIAS, (double)P.z + OT_BIAS};
     const float pf[3] = {P.x, P.y, P.z};
     const int ncand = (smax - smin + 1) * 8;
     for (int cand = lane; cand < ncand; cand += 32) {
@@ -229,6 +236,7 @@ __device__ void find_reusable_warp(const RadCacheView& C, int smin, int smax, fl
             }
         } else {
             const double s = biased_pow2(size), inv = 1.0 / s;   // powers of two: exact
+            const double c[3] = {(double)P.x + OT_BIAS, (double)P.y + OT_BIAS, (double)P.z + OT_BIAS};
             for (int a = 0; a < 3; a++) {
                 const int b = (int)floor(c[a] * inv - 1.5);
                 cell[a] = b + 1 + d3[a];
@@ -362,7 +370,7 @@ __global__ void k_rad_query(DeviceScene S, RadCacheView C, RadParams R, const Ra
         if (!seed) {
             // cell of this round: the largest reuse radius halved per round,
             // not below the smallest (GatherLight's reuse distance clamps)
-            float te = to_eye(S, P);
+            float te = to_eye_f(S, P);
             float h = fmaxf(te * R.max_reuse_factor * eb * exp2f(-(float)round), te * R.min_reuse_factor * eb);
             int lvl = (int)ceilf(log2f(fmaxf(h, 1e-6f)));
             float cs = exp2f((float)lvl);
