@@ -128,7 +128,35 @@ typedef struct PovGpuMaterial {
     float fresnel;
     float crand;
     float irid;
+    int32_t pattern;           /* pigment pattern: 1-based index into the scene's
+                                  patterns, 0 = the plain pigment above       */
 } PovGpuMaterial;
+
+/* Pattern pigments (PIGMENT with a pattern and a colour map: Compute_Pigment,
+ * source/core/material/pigment.cpp:395-475; patterns in
+ * source/core/material/pattern.cpp, noise in noise.cpp / portablenoise.cpp).
+ * The point is the pattern's TRANSFORM warp applied inversely (Warp_EPoint,
+ * warp.cpp:103-122); continuous patterns take the default ramp wave
+ * (frequency 1, phase 0: ContinuousPattern::Evaluate, pattern.cpp:354-390);
+ * the colour map blends linearly between its entries (BlendMap::Search,
+ * pattern.cpp:1068-1109).  Opaque colours only. */
+#define POV_PATTERN_CHECKER   1   /* CheckerPattern::Evaluate, pattern.cpp:5691      */
+#define POV_PATTERN_GRADIENT  2   /* GradientPattern::EvaluateRaw, pattern.cpp:6386  */
+#define POV_PATTERN_BOZO      3   /* bozo / spotted: NoisePattern, pattern.cpp:7858  */
+#define POV_PATTERN_GRANITE   4   /* GranitePattern::EvaluateRaw, pattern.cpp:6429   */
+#define POV_PATTERN_MAX_ENTRIES 16
+typedef struct PovGpuPattern {
+    int32_t type;
+    int32_t noise_generator;      /* 1 original, 2 range corrected (default), 3 Perlin */
+    int32_t num_entries;          /* colour map entries (checker: its two colours)    */
+    int32_t reserved;
+    double  inverse[16];          /* inverse of the pattern's TRANSFORM, row-vector form
+                                     (p' = p * M), as MInvTransPoint applies it      */
+    double  gradient[3];          /* gradient: the pattern's vector                  */
+    double  pad;
+    float   values[POV_PATTERN_MAX_ENTRIES];        /* colour map values, ascending   */
+    float   colours[POV_PATTERN_MAX_ENTRIES][3];    /* colour map rgb                 */
+} PovGpuPattern;
 
 /* Light source: point light or rectangular area light (LightSource,
  * source/core/scene/object.h:313). */
@@ -235,6 +263,8 @@ typedef struct PovGpuSceneDesc {
     PovGpuRadiosity       radiosity;
     int32_t               num_medias;
     const struct PovGpuMedia* medias;
+    int32_t               num_patterns;
+    const PovGpuPattern*  patterns;
 } PovGpuSceneDesc;
 
 /* A render block, as POVRect (inclusive bounds) plus its serial number. */

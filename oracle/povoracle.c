@@ -27,6 +27,7 @@
  *     hit so far (source/core/shape/mesh.cpp:1499 keeps the last one).
  */
 #include "povoracle.h"
+#include "../povray_gb300/csrc/povgpu_noise_table.h"
 
 #include <math.h>
 #include <pthread.h>
@@ -1458,6 +1459,222 @@ static V3 object_normal(const PovOracle* S, const Isect* is)
     }
 }
 
+/* ====================================================== pattern pigments ==
+ * Noise tables: the hash permutation (InitTextureTable, noise.cpp:231-256),
+ * the lattice values (RTable, noise.cpp:98-182) and the Perlin gradient
+ * tables (InitSolidNoise, noise.cpp:306-347), all from the reference's
+ * linear congruential sequence next = next * 1812433253 + 12345 kept in a
+ * 32-bit int. */
+#define NOISE_ENTRIES 2048
+static unsigned short g_hash[8192];
+static double g_rtab[2 * POV_NOISE_RTABLE_SIZE];
+static int g_perm[2 * (NOISE_ENTRIES + 1)];
+static V3 g_ngrad[2 * (NOISE_ENTRIES + 1)];
+static pthread_once_t g_noise_once = PTHREAD_ONCE_INIT;
+
+static int32_t lcg_next(int32_t x) { return (int32_t)(uint32_t)((int64_t)x * 1812433253LL + 12345LL); }
+
+static void noise_init(void)
+{
+    int32_t next = 0;
+    for (int i = 0; i < 4096; i++)
+        g_hash[i] = (unsigned short)i;
+    for (int i = 4095; i >= 0; i--) {
+        next = lcg_next(next);
+        int j = ((int)(next >> 16) & 0x7FFF) % 4096;
+        unsigned short t = g_hash[i];
+        g_hash[i] = g_hash[j];
+        g_hash[j] = t;
+    }
+    for (int i = 0; i < 4096; i++)
+        g_hash[4096 + i] = g_hash[i];
+    for (int i = 0; i < POV_NOISE_RTABLE_SIZE; i++) {
+        g_rtab[2 * i] = kPovNoiseRTable[i];
+        g_rtab[2 * i + 1] = kPovNoiseRTable[i] * 0.5;
+    }
+    next = 1;
+    for (int i = 0; i < NOISE_ENTRIES; i++) {
+        double v[3], q;
+        do {
+            for (int k = 0; k < 3; k++) {
+                next = lcg_next(next);
+                v[k] = (double)((((int)(next >> 16) & 0x7FFF) % (NOISE_ENTRIES << 1)) - NOISE_ENTRIES) /
+                       (double)NOISE_ENTRIES;
+            }
+            q = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+        } while (q > 1.0 || q < 1.0e-5);
+        q = sqrt(q);
+        g_ngrad[i] = v3(v[0] / q, v[1] / q, v[2] / q);
+    }
+    for (int i = 0; i < NOISE_ENTRIES; i++)
+        g_perm[i] = i;
+    for (int i = NOISE_ENTRIES; i > 0; i -= 2) {
+        int k = g_perm[i];
+        next = lcg_next(next);
+        int j = ((int)(next >> 16) & 0x7FFF) % NOISE_ENTRIES;
+        g_perm[i] = g_perm[j];
+        g_perm[j] = k;
+    }
+    for (int i = 0; i < NOISE_ENTRIES + 2; i++) {
+        g_perm[NOISE_ENTRIES + i] = g_perm[i];
+        g_ngrad[NOISE_ENTRIES + i] = g_ngrad[i];
+    }
+}
+
+static double scurve(double t) { return t * t * (3.0 - 2.0 * t); }
+static double lerp(double t, double a, double b) { return a + t * (b - a); }
+
+/* SolidNoise (noise.cpp:392-440): Perlin gradient noise, generator 3. */
+static double solid_noise(V3 P)
+{
+    const double ROLLOVER = 10000000.023157213;
+    int b0[3], b1[3];
+    double r0[3], r1[3];
+    const double p[3] = {P.x, P.y, P.z};
+    for (int a = 0; a < 3; a++) {
+        double t = p[a] + ROLLOVER;
+        int it = (int)floor(t);
+        b0[a] = it & (NOISE_ENTRIES - 1);
+        b1[a] = (b0[a] + 1) & (NOISE_ENTRIES - 1);
+        r0[a] = t - it;
+        r1[a] = r0[a] - 1.0;
+    }
+    int i = g_perm[b0[0]], j = g_perm[b1[0]];
+    int b00 = g_perm[i + b0[1]], b10 = g_perm[j + b0[1]], b01 = g_perm[i + b1[1]], b11 = g_perm[j + b1[1]];
+    double sx = scurve(r0[0]), sy = scurve(r0[1]), sz = scurve(r0[2]);
+#define AT(g, rx, ry, rz) (g.x * (rx) + g.y * (ry) + g.z * (rz))
+    double u = AT(g_ngrad[b00 + b0[2]], r0[0], r0[1], r0[2]), v = AT(g_ngrad[b10 + b0[2]], r1[0], r0[1], r0[2]);
+    double a = lerp(sx, u, v);
+    u = AT(g_ngrad[b01 + b0[2]], r0[0], r1[1], r0[2]);
+    v = AT(g_ngrad[b11 + b0[2]], r1[0], r1[1], r0[2]);
+    double b = lerp(sx, u, v);
+    double c = lerp(sy, a, b);
+    u = AT(g_ngrad[b00 + b1[2]], r0[0], r0[1], r1[2]);
+    v = AT(g_ngrad[b10 + b1[2]], r1[0], r0[1], r1[2]);
+    a = lerp(sx, u, v);
+    u = AT(g_ngrad[b01 + b1[2]], r0[0], r1[1], r1[2]);
+    v = AT(g_ngrad[b11 + b1[2]], r1[0], r1[1], r1[2]);
+    b = lerp(sx, u, v);
+    double d = lerp(sy, a, b);
+#undef AT
+    return lerp(sz, c, d);
+}
+
+/* PortableNoise (portablenoise.cpp:103-225): the lattice noise of generators
+ * 1 (original) and 2 (range corrected), Perlin noise for 3. */
+static double pov_noise(V3 P, int gen)
+{
+    if (gen == 3) {
+        double sum = 0.5 * (1.59 * solid_noise(P) + 0.985);
+        return sum < 0.0 ? 0.0 : (sum > 1.0 ? 1.0 : sum);
+    }
+    const double p[3] = {P.x, P.y, P.z};
+    int ii[3];
+    double f[3], g[3], sc[3], tc[3];
+    for (int a = 0; a < 3; a++) {
+        int tmp = p[a] >= 0 ? (int)p[a] : (int)(p[a] - (1 - EPSILON));
+        ii[a] = (tmp - (-10000)) & 0xFFF;
+        f[a] = p[a] - tmp;
+        g[a] = f[a] - 1;
+        sc[a] = scurve(f[a]);
+        tc[a] = 1 - sc[a];
+    }
+    const double txty = tc[0] * tc[1], sxty = sc[0] * tc[1], txsy = tc[0] * sc[1], sxsy = sc[0] * sc[1];
+#define HASH2(a, b) g_hash[(int)(g_hash[(int)(a)] ^ (b))]
+#define RIDX(a, b) ((g_hash[(int)(a) ^ (b)] & 0xFF) * 2)
+#define INCR(m, s, x, y, z) ((s) * (g_rtab[(m) + 1] + g_rtab[(m) + 2] * (x) + g_rtab[(m) + 4] * (y) + g_rtab[(m) + 6] * (z)))
+    const int h00 = HASH2(ii[0], ii[1]), h10 = HASH2(ii[0] + 1, ii[1]);
+    const int h01 = HASH2(ii[0], ii[1] + 1), h11 = HASH2(ii[0] + 1, ii[1] + 1);
+    double sum = INCR(RIDX(h00, ii[2]), txty * tc[2], f[0], f[1], f[2]);
+    sum += INCR(RIDX(h10, ii[2]), sxty * tc[2], g[0], f[1], f[2]);
+    sum += INCR(RIDX(h01, ii[2]), txsy * tc[2], f[0], g[1], f[2]);
+    sum += INCR(RIDX(h11, ii[2]), sxsy * tc[2], g[0], g[1], f[2]);
+    sum += INCR(RIDX(h00, ii[2] + 1), txty * sc[2], f[0], f[1], g[2]);
+    sum += INCR(RIDX(h10, ii[2] + 1), sxty * sc[2], g[0], f[1], g[2]);
+    sum += INCR(RIDX(h01, ii[2] + 1), txsy * sc[2], f[0], g[1], g[2]);
+    sum += INCR(RIDX(h11, ii[2] + 1), sxsy * sc[2], g[0], g[1], g[2]);
+#undef HASH2
+#undef RIDX
+#undef INCR
+    if (gen == 2) {
+        sum += 1.05242;
+        sum *= 0.48985582;
+    } else {
+        sum = sum + 0.5;
+    }
+    return sum < 0.0 ? 0.0 : (sum > 1.0 ? 1.0 : sum);
+}
+
+/* Compute_Pigment for a pattern pigment (pigment.cpp:395-475): the point
+ * through the pattern's inverse TRANSFORM (Warp_EPoint, warp.cpp:103-122),
+ * the pattern value, the colour map (BlendMap::Search, pattern.cpp:
+ * 1068-1109, linear blend). */
+static RGB pattern_pigment(const PovGpuPattern* pt, V3 P)
+{
+    const double* m = pt->inverse;
+    double q[3];
+    for (int i = 0; i < 3; i++) {
+        q[i] = P.x * m[0 * 4 + i] + P.y * m[1 * 4 + i] + P.z * m[2 * 4 + i] + m[3 * 4 + i];
+        if (q[i] > 1.0e17) q[i] = 1.0e17;   /* COORDINATE_LIMIT */
+        if (q[i] < -1.0e17) q[i] = -1.0e17;
+    }
+    const V3 T = v3(q[0], q[1], q[2]);
+    double value;
+    if (pt->type == POV_PATTERN_CHECKER) {   /* CheckerPattern::Evaluate, pattern.cpp:5691-5706 */
+        int c = (int)(floor(T.x + EPSILON) + floor(T.y + EPSILON) + floor(T.z + EPSILON));
+        value = (c & 1) ? 1.0 : 0.0;
+    } else {
+        if (pt->type == POV_PATTERN_GRADIENT) {   /* pattern.cpp:6386-6393 */
+            value = T.x * pt->gradient[0] + T.y * pt->gradient[1] + T.z * pt->gradient[2];
+            if (value > 1.0)
+                value = fmod(value, 1.0);
+        } else if (pt->type == POV_PATTERN_BOZO) {   /* NoisePattern, pattern.cpp:7858-7861 */
+            value = pov_noise(T, pt->noise_generator);
+        } else {   /* GranitePattern, pattern.cpp:6429-6465 */
+            value = 0.0;
+            double freq = 1.0;
+            const V3 t1 = vmul(T, 4.0);
+            for (int i = 0; i < 6; freq *= 2.0, i++) {
+                double tmp;
+                if (pt->noise_generator == 1) {
+                    tmp = fabs(0.5 - pov_noise(vmul(t1, freq), 1));
+                } else {
+                    tmp = fabs(1.0 - 2.0 * pov_noise(vmul(t1, freq), pt->noise_generator));
+                    if (tmp > 0.5)
+                        tmp = 0.5;
+                }
+                value += tmp / freq;
+            }
+        }
+        /* ContinuousPattern::Evaluate, ramp wave, frequency 1, phase 0
+         * (pattern.cpp:354-390) */
+        value = fmod(value * 1.0 + 0.0, 1.00001);
+        if (value < 0.0)
+            value -= floor(value);
+    }
+    const int n = pt->num_entries;
+    RGB c;
+    if (value >= pt->values[n - 1]) {
+        c.r = pt->colours[n - 1][0]; c.g = pt->colours[n - 1][1]; c.b = pt->colours[n - 1][2];
+        return c;
+    }
+    int ip = 0, in = 0;
+    while (value > pt->values[in]) {
+        ip = in;
+        in++;
+    }
+    if (value == pt->values[in] || ip == in) {
+        c.r = pt->colours[in][0]; c.g = pt->colours[in][1]; c.b = pt->colours[in][2];
+        return c;
+    }
+    const double pw = ((double)pt->values[in] - value) / ((double)pt->values[in] - (double)pt->values[ip]);
+    const float wp = (float)pw, wn = (float)(1.0 - pw);
+    c.r = pt->colours[ip][0] * wp + pt->colours[in][0] * wn;
+    c.g = pt->colours[ip][1] * wp + pt->colours[in][1] * wn;
+    c.b = pt->colours[ip][2] * wp + pt->colours[in][2] * wn;
+    return c;
+}
+
 /* Material of an object: its own, else the nearest CSG ancestor's. */
 static const PovGpuMaterial* object_material(const PovOracle* S, int32_t oi)
 {
@@ -1679,6 +1896,8 @@ static void shade(const PovOracle* S, Thread* th, const Isect* is, V3 D, double 
     V3 N = raw;
     V3 ip = is->ipoint;
     RGB pig = {m->pigment[0], m->pigment[1], m->pigment[2]};
+    if (m->pattern > 0)
+        pig = pattern_pigment(&S->desc.patterns[m->pattern - 1], is->ipoint);
     double r = 0.0, g = 0.0, b = 0.0;
 
     /* ComputeReflectivity (trace.cpp:2627-2656), non-fresnel */
@@ -2658,6 +2877,24 @@ int pov_oracle_create(const PovGpuSceneDesc* desc, PovOracle** out, int32_t* bad
              L->jitter || (L->circular && (L->area_size1 < 2 || L->area_size2 < 2))))
             return POV_GPU_E_UNSUPPORTED;   /* jitter draws on the reference's RNG stream */
     }
+    /* pattern pigments: the four patterns with a colour map of 1..16
+     * ascending entries (checker: 2), noise generators 1..3 */
+    if (desc->num_patterns < 0 || (desc->num_patterns > 0 && !desc->patterns))
+        return POV_GPU_E_INVALID;
+    for (int i = 0; i < desc->num_patterns; i++) {
+        const PovGpuPattern* pt = &desc->patterns[i];
+        if (pt->type < POV_PATTERN_CHECKER || pt->type > POV_PATTERN_GRANITE || pt->num_entries < 1 ||
+            pt->num_entries > POV_PATTERN_MAX_ENTRIES || pt->noise_generator < 1 || pt->noise_generator > 3 ||
+            (pt->type == POV_PATTERN_CHECKER && pt->num_entries != 2))
+            return POV_GPU_E_UNSUPPORTED;
+        for (int k = 1; k < pt->num_entries; k++)
+            if (pt->values[k] < pt->values[k - 1])
+                return POV_GPU_E_INVALID;
+    }
+    for (int i = 0; i < desc->num_materials; i++)
+        if (desc->materials[i].pattern < 0 || desc->materials[i].pattern > desc->num_patterns)
+            return POV_GPU_E_INVALID;
+    pthread_once(&g_noise_once, noise_init);
     PovOracle* S = (PovOracle*)calloc(1, sizeof(PovOracle));
     S->desc = *desc;
     if (desc->radiosity.enabled)

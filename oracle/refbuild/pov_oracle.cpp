@@ -38,6 +38,8 @@
 #include "core/bounding/boundingbox.h"
 #include "core/lighting/lightsource.h"
 #include "core/material/media.h"
+#include "core/material/noise.h"
+#include "core/material/pattern.h"
 #include "core/math/matrix.h"
 #include "core/math/randomsequence.h"
 #include "core/render/ray.h"
@@ -223,6 +225,11 @@ int main(int argc, char **argv)
         return 0;
     }
 
+    // the process-wide tables the renderer sets up at start-up
+    // (povray_init, source/backend/povray.cpp:653-654): noise lattice and
+    // permutations, pattern generators
+    pov::Initialize_Noise();
+    pov::InitializePatternGenerators();
     DefaultPlatformBase platform;  // file access for the parser (vfe provides this in the CLI)
     try
     {

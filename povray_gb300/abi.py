@@ -63,7 +63,21 @@ class PovGpuMaterial(C.Structure):
                 ("reflection_falloff", C.c_float), ("reflect_exp", C.c_float),
                 ("reflect_metallic", C.c_float), ("reflection_fresnel", C.c_int32),
                 ("conserve_energy", C.c_int32), ("fresnel", C.c_float),
-                ("crand", C.c_float), ("irid", C.c_float)]
+                ("crand", C.c_float), ("irid", C.c_float), ("pattern", C.c_int32)]
+
+
+POV_PATTERN_CHECKER = 1
+POV_PATTERN_GRADIENT = 2
+POV_PATTERN_BOZO = 3
+POV_PATTERN_GRANITE = 4
+POV_PATTERN_MAX_ENTRIES = 16
+
+
+class PovGpuPattern(C.Structure):
+    _fields_ = [("type", C.c_int32), ("noise_generator", C.c_int32), ("num_entries", C.c_int32),
+                ("reserved", C.c_int32), ("inverse", C.c_double * 16), ("gradient", C.c_double * 3),
+                ("pad", C.c_double), ("values", C.c_float * POV_PATTERN_MAX_ENTRIES),
+                ("colours", (C.c_float * 3) * POV_PATTERN_MAX_ENTRIES)]
 
 
 class PovGpuLight(C.Structure):
@@ -116,7 +130,8 @@ class PovGpuSceneDesc(C.Structure):
                 ("background", C.c_float * 4), ("ambient_light", C.c_float * 3),
                 ("max_trace_level", C.c_int32), ("adc_bailout", C.c_float),
                 ("language_version", C.c_int32), ("radiosity", PovGpuRadiosity),
-                ("num_medias", C.c_int32), ("medias", C.POINTER(PovGpuMedia))]
+                ("num_medias", C.c_int32), ("medias", C.POINTER(PovGpuMedia)),
+                ("num_patterns", C.c_int32), ("patterns", C.POINTER(PovGpuPattern))]
 
 
 class PovGpuBlock(C.Structure):
@@ -179,7 +194,7 @@ STRUCTS = {
     "PovGpuRadiosity": PovGpuRadiosity, "PovGpuSceneDesc": PovGpuSceneDesc,
     "PovGpuBlock": PovGpuBlock, "PovGpuRenderParams": PovGpuRenderParams,
     "PovGpuStats": PovGpuStats, "PovGpuHit": PovGpuHit, "PovGpuTimings": PovGpuTimings,
-    "PovGpuNeuralCache": PovGpuNeuralCache, "PovGpuMedia": PovGpuMedia,
+    "PovGpuNeuralCache": PovGpuNeuralCache, "PovGpuMedia": PovGpuMedia, "PovGpuPattern": PovGpuPattern,
 }
 
 # Entry points that include/povgpu.h declares (checked by the CPU tests).

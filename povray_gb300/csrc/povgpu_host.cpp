@@ -10,6 +10,7 @@
 #include "povgpu_kernels.h"
 #include "povgpu_radiosity.h"
 #include "povgpu_nic.h"
+#include "povgpu_noise_table.h"
 
 #include <cuda_runtime.h>
 
@@ -530,7 +531,7 @@ struct PovGpuScene {
     // persistent scene data
     DevBuf nodes, refs, tri_v0, tri_e1, tri_e2, tri_global, tri_shade, tri_normal, tri_local, normals;
     DevBuf spheres, spheres64, boxes64, sphere_obj, sphere_flags, planes, plane_obj, boxes, tori, csgs, csg_children, objects,
-        materials, lights, medias;
+        materials, lights, medias, patterns, noise_hash, noise_rtab, noise_perm, noise_grad;
     DevBuf encode_buf;     // staging of pov_gpu_encode_u8 for host outputs
     int    media_ni = 0;   // interval slots per media segment (0: no media containers)
     int    media_smax = 0;  // sample slots per interval (ends + sample-tree nodes)
@@ -573,7 +574,7 @@ struct PovGpuScene {
                          &csg_children, &objects, &materials, &lights, &blocks, &block_off, &corner_off, &qA,
                          &hits, &out, &counters, &stats, &err, &rays_in, &t64, &corners, &aa_grid, &aa_mask,
                          &aa_subdiv, &aa_xy, &cellsA, &cellsB, &spos, &sslot, &wcount, &pos_count, &medias,
-                         &encode_buf};
+                         &encode_buf, &patterns, &noise_hash, &noise_rtab, &noise_perm, &noise_grad};
         for (DevBuf* b : all)
             b->release();
         top.release();
@@ -684,6 +685,23 @@ int validate(const PovGpuSceneDesc* d, int32_t* bad)
         if (rc != POV_GPU_OK)
             return rc;
     }
+    // pattern pigments: the four patterns, 1..16 ascending colour map entries
+    // (checker: 2), noise generators 1..3
+    if (d->num_patterns < 0 || (d->num_patterns > 0 && !d->patterns))
+        return POV_GPU_E_INVALID;
+    for (int i = 0; i < d->num_patterns; i++) {
+        const PovGpuPattern& pt = d->patterns[i];
+        if (pt.type < POV_PATTERN_CHECKER || pt.type > POV_PATTERN_GRANITE || pt.num_entries < 1 ||
+            pt.num_entries > POV_PATTERN_MAX_ENTRIES || pt.noise_generator < 1 || pt.noise_generator > 3 ||
+            (pt.type == POV_PATTERN_CHECKER && pt.num_entries != 2))
+            return POV_GPU_E_UNSUPPORTED;
+        for (int k = 1; k < pt.num_entries; k++)
+            if (pt.values[k] < pt.values[k - 1])
+                return POV_GPU_E_INVALID;
+    }
+    for (int i = 0; i < d->num_materials; i++)
+        if (d->materials[i].pattern < 0 || d->materials[i].pattern > d->num_patterns)
+            return POV_GPU_E_INVALID;
     for (int i = 0; i < d->num_materials; i++) {
         const PovGpuMaterial& m = d->materials[i];
         // opaque plain pigments and the classic finish terms only (media
@@ -766,6 +784,7 @@ DevMaterial make_material(const PovGpuMaterial& m, const float* ambient_light, b
         anyr = anyr || m.reflection_max[k] != 0.f || m.reflection_min[k] != 0.f;
     d.has_reflection = anyr ? 1 : 0;
     d.diffuse_raw = m.diffuse;
+    d.pattern = m.pattern;
     return d;
 }
 
@@ -917,6 +936,68 @@ void add_mesh(Builder& B, const PovGpuSceneDesc* d, const PovGpuObject& o, int i
         B.push_prim(PK_TRIANGLE, (uint32_t)g, box);
     }
 }
+
+// The noise tables the renderer builds at start-up (InitTextureTable,
+// noise.cpp:231-256; RTable with its odd entries halved, noise.cpp:181-182;
+// InitSolidNoise, noise.cpp:306-347), from the reference's linear
+// congruential sequence kept in a 32-bit int.
+struct NoiseTables {
+    std::vector<uint16_t> hash = std::vector<uint16_t>(1, 0);
+    std::vector<float> rtab = std::vector<float>(1, 0.f);
+    std::vector<int32_t> perm = std::vector<int32_t>(1, 0);
+    std::vector<float4> grad = std::vector<float4>(1, make_float4(0.f, 0.f, 0.f, 0.f));
+
+    static int32_t next(int32_t x) { return (int32_t)(uint32_t)((int64_t)x * 1812433253LL + 12345LL); }
+
+    void build()
+    {
+        hash.assign(8192, 0);
+        int32_t r = 0;
+        for (int i = 0; i < 4096; i++)
+            hash[i] = (uint16_t)i;
+        for (int i = 4095; i >= 0; i--) {
+            r = next(r);
+            int j = ((int)(r >> 16) & 0x7FFF) % 4096;
+            std::swap(hash[i], hash[j]);
+        }
+        for (int i = 0; i < 4096; i++)
+            hash[4096 + i] = hash[i];
+        rtab.assign(2 * POV_NOISE_RTABLE_SIZE, 0.f);
+        for (int i = 0; i < POV_NOISE_RTABLE_SIZE; i++) {
+            rtab[2 * i] = (float)kPovNoiseRTable[i];
+            rtab[2 * i + 1] = (float)(kPovNoiseRTable[i] * 0.5);
+        }
+        const int E = 2048;
+        perm.assign(2 * (E + 1), 0);
+        grad.assign(2 * (E + 1), make_float4(0.f, 0.f, 0.f, 0.f));
+        r = 1;
+        for (int i = 0; i < E; i++) {
+            double v[3], q;
+            do {
+                for (int k = 0; k < 3; k++) {
+                    r = next(r);
+                    v[k] = (double)((((int)(r >> 16) & 0x7FFF) % (E << 1)) - E) / (double)E;
+                }
+                q = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+            } while (q > 1.0 || q < 1.0e-5);
+            q = std::sqrt(q);
+            grad[i] = make_float4((float)(v[0] / q), (float)(v[1] / q), (float)(v[2] / q), 0.f);
+        }
+        for (int i = 0; i < E; i++)
+            perm[i] = i;
+        for (int i = E; i > 0; i -= 2) {
+            int k = perm[i];
+            r = next(r);
+            int j = ((int)(r >> 16) & 0x7FFF) % E;
+            perm[i] = perm[j];
+            perm[j] = k;
+        }
+        for (int i = 0; i < E + 2; i++) {
+            perm[E + i] = perm[i];
+            grad[E + i] = grad[i];
+        }
+    }
+};
 
 int rad_reset(PovGpuScene* sc);
 
@@ -1125,10 +1206,34 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
         sc->media_levels = std::max(sc->media_levels, md.aa_level);
     }
 
+    // pattern pigments and the noise tables they read
+    std::vector<DevPattern> pats(std::max(d->num_patterns, 1));
+    for (int i = 0; i < d->num_patterns; i++) {
+        const PovGpuPattern& pt = d->patterns[i];
+        DevPattern& q = pats[i];
+        for (int c = 0; c < 3; c++)
+            q.col[c] = make_float4((float)pt.inverse[0 * 4 + c], (float)pt.inverse[1 * 4 + c],
+                                   (float)pt.inverse[2 * 4 + c], (float)pt.inverse[3 * 4 + c]);
+        q.gradient = make_float4((float)pt.gradient[0], (float)pt.gradient[1], (float)pt.gradient[2], 0.f);
+        q.kind = make_int4(pt.type, pt.noise_generator, pt.num_entries, 0);
+        for (int k = 0; k < POV_PATTERN_MAX_ENTRIES; k++) {
+            q.values[k] = pt.values[k];
+            q.colours[k] = make_float4(pt.colours[k][0], pt.colours[k][1], pt.colours[k][2], 0.f);
+        }
+    }
+    NoiseTables nt;
+    if (d->num_patterns > 0)
+        nt.build();
+
     CK(upload(sc->objects, objects));
     CK(upload(sc->materials, mats));
     CK(upload(sc->lights, lights));
     CK(upload(sc->medias, medias));
+    CK(upload(sc->patterns, pats));
+    CK(upload(sc->noise_hash, nt.hash));
+    CK(upload(sc->noise_rtab, nt.rtab));
+    CK(upload(sc->noise_perm, nt.perm));
+    CK(upload(sc->noise_grad, nt.grad));
 
     sc->h_sphere_obj = B.sphere_obj;
     sc->h_plane_obj = B.plane_obj;
@@ -1173,6 +1278,11 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
     S.num_lights = d->num_lights;
     S.num_area_lights = num_area;
     S.medias = sc->medias.as<DevMedia>();
+    S.patterns = sc->patterns.as<DevPattern>();
+    S.noise.hash = sc->noise_hash.as<uint16_t>();
+    S.noise.rtab = sc->noise_rtab.as<float>();
+    S.noise.perm = sc->noise_perm.as<int32_t>();
+    S.noise.grad = sc->noise_grad.as<float4>();
     S.num_containers = (int)container_obj.size();
     sc->media_ni = container_obj.empty() ? 0 : media_ni;
     S.max_trace_level = d->max_trace_level;

@@ -71,6 +71,26 @@ struct __align__(16) DevMaterial {
     float roughness;        // already inverted
     int32_t has_reflection;
     float   diffuse_raw;    // Finish->Diffuse, the radiosity ambient's factor (trace.cpp:898)
+    int32_t pattern;        // pigment pattern + 1 (0: the plain pigment above)
+};
+
+// Pattern pigment (Compute_Pigment with a colour map): the inverse TRANSFORM
+// as three columns (q_i = p . col_i + col_i.w), the gradient vector, the
+// colour map.
+struct __align__(16) DevPattern {
+    float4 col[3];
+    float4 gradient;        // xyz, -
+    int4   kind;            // type, noise generator, entries, -
+    float  values[16];
+    float4 colours[16];
+};
+
+// Noise tables in device memory (the reference's start-up tables).
+struct DevNoise {
+    const uint16_t* hash;   // 8192 (InitTextureTable)
+    const float*    rtab;   // 534 (RTable, odd entries halved)
+    const int32_t*  perm;   // 2 * (2048 + 1) (InitSolidNoise)
+    const float4*   grad;   // 2 * (2048 + 1)
 };
 
 struct __align__(16) DevLight {
@@ -186,6 +206,9 @@ struct DeviceScene {
     // media containers
     const DevMedia* medias;         // one per container
     int32_t         num_containers;
+    // pattern pigments
+    const DevPattern* patterns;
+    DevNoise          noise;
     int32_t         max_trace_level;
     float           adc_bailout;
     float4          background;

@@ -882,6 +882,147 @@ __device__ __forceinline__ SurfaceInfo surface(const DeviceScene& S, const QHit&
     return si;
 }
 
+// ------------------------------------------------------ pattern pigments --
+// Solid noise and the patterns of the pattern pigments in FP32, following
+// portablenoise.cpp:103-225 (generators 1 and 2), noise.cpp:392-440 (Perlin,
+// generator 3) and pattern.cpp (checker :5691, gradient :6386, noise :7858,
+// granite :6429) with the reference's start-up tables.
+__device__ __forceinline__ float noise_scurve(float t) { return t * t * (3.0f - 2.0f * t); }
+
+__device__ float solid_noise(const DevNoise& N, float3 P)
+{
+    const float p[3] = {P.x, P.y, P.z};
+    int b0[3], b1[3];
+    float r0[3], r1[3];
+    for (int a = 0; a < 3; a++) {
+        // the reference adds ROLLOVER (10^7 + 0.023157213) in FP64; the cell
+        // and fraction are taken the same way here without the large offset
+        const double t = (double)p[a] + 10000000.023157213;
+        const int it = (int)floor(t);
+        b0[a] = it & 2047;
+        b1[a] = (b0[a] + 1) & 2047;
+        r0[a] = (float)(t - it);
+        r1[a] = r0[a] - 1.0f;
+    }
+    const int i = __ldg(N.perm + b0[0]), j = __ldg(N.perm + b1[0]);
+    const int b00 = __ldg(N.perm + i + b0[1]), b10 = __ldg(N.perm + j + b0[1]);
+    const int b01 = __ldg(N.perm + i + b1[1]), b11 = __ldg(N.perm + j + b1[1]);
+    const float sx = noise_scurve(r0[0]), sy = noise_scurve(r0[1]), sz = noise_scurve(r0[2]);
+    auto at = [&](int k, float rx, float ry, float rz) {
+        const float4 g = __ldg(N.grad + k);
+        return g.x * rx + g.y * ry + g.z * rz;
+    };
+    float u = at(b00 + b0[2], r0[0], r0[1], r0[2]), v = at(b10 + b0[2], r1[0], r0[1], r0[2]);
+    float a = u + sx * (v - u);
+    u = at(b01 + b0[2], r0[0], r1[1], r0[2]);
+    v = at(b11 + b0[2], r1[0], r1[1], r0[2]);
+    float b = u + sx * (v - u);
+    const float c = a + sy * (b - a);
+    u = at(b00 + b1[2], r0[0], r0[1], r1[2]);
+    v = at(b10 + b1[2], r1[0], r0[1], r1[2]);
+    a = u + sx * (v - u);
+    u = at(b01 + b1[2], r0[0], r1[1], r1[2]);
+    v = at(b11 + b1[2], r1[0], r1[1], r1[2]);
+    b = u + sx * (v - u);
+    const float d = a + sy * (b - a);
+    return c + sz * (d - c);
+}
+
+__device__ float pov_noise(const DevNoise& N, float3 P, int gen)
+{
+    if (gen == 3) {
+        const float sum = 0.5f * (1.59f * solid_noise(N, P) + 0.985f);
+        return fminf(fmaxf(sum, 0.0f), 1.0f);
+    }
+    const float p[3] = {P.x, P.y, P.z};
+    int ii[3];
+    float f[3], g[3], sc[3], tc[3];
+    for (int a = 0; a < 3; a++) {
+        // the lattice cell as the reference takes it (x - (1 - EPSILON) in FP64)
+        const int tmp = p[a] >= 0.0f ? (int)p[a] : (int)((double)p[a] - (1.0 - 1.0e-10));
+        ii[a] = (tmp + 10000) & 0xFFF;
+        f[a] = p[a] - (float)tmp;
+        g[a] = f[a] - 1.0f;
+        sc[a] = noise_scurve(f[a]);
+        tc[a] = 1.0f - sc[a];
+    }
+    auto h2 = [&](int a, int b) { return (int)__ldg(N.hash + ((int)__ldg(N.hash + a) ^ b)); };
+    auto incr = [&](int a, int b, float s, float x, float y, float z) {
+        const int m = (__ldg(N.hash + (a ^ b)) & 0xFF) * 2;
+        return s * (__ldg(N.rtab + m + 1) + __ldg(N.rtab + m + 2) * x + __ldg(N.rtab + m + 4) * y +
+                    __ldg(N.rtab + m + 6) * z);
+    };
+    const float txty = tc[0] * tc[1], sxty = sc[0] * tc[1], txsy = tc[0] * sc[1], sxsy = sc[0] * sc[1];
+    const int h00 = h2(ii[0], ii[1]), h10 = h2(ii[0] + 1, ii[1]), h01 = h2(ii[0], ii[1] + 1),
+              h11 = h2(ii[0] + 1, ii[1] + 1);
+    float sum = incr(h00, ii[2], txty * tc[2], f[0], f[1], f[2]);
+    sum += incr(h10, ii[2], sxty * tc[2], g[0], f[1], f[2]);
+    sum += incr(h01, ii[2], txsy * tc[2], f[0], g[1], f[2]);
+    sum += incr(h11, ii[2], sxsy * tc[2], g[0], g[1], f[2]);
+    sum += incr(h00, ii[2] + 1, txty * sc[2], f[0], f[1], g[2]);
+    sum += incr(h10, ii[2] + 1, sxty * sc[2], g[0], f[1], g[2]);
+    sum += incr(h01, ii[2] + 1, txsy * sc[2], f[0], g[1], g[2]);
+    sum += incr(h11, ii[2] + 1, sxsy * sc[2], g[0], g[1], g[2]);
+    sum = gen == 2 ? (sum + 1.05242f) * 0.48985582f : sum + 0.5f;
+    return fminf(fmaxf(sum, 0.0f), 1.0f);
+}
+
+// Compute_Pigment of a pattern pigment at world point P (pigment.cpp:395-475):
+// the pattern's inverse TRANSFORM, the pattern value with the default ramp
+// wave, the colour map's linear blend.
+__device__ float3 pattern_pigment(const DeviceScene& S, int pi, float3 P)
+{
+    const DevPattern& pt = S.patterns[pi];
+    float3 T;
+    {
+        const float4 c0 = pt.col[0], c1 = pt.col[1], c2 = pt.col[2];
+        T = f3(P.x * c0.x + P.y * c0.y + P.z * c0.z + c0.w, P.x * c1.x + P.y * c1.y + P.z * c1.z + c1.w,
+               P.x * c2.x + P.y * c2.y + P.z * c2.z + c2.w);
+    }
+    const int kind = pt.kind.x, gen = pt.kind.y, n = pt.kind.z;
+    float value;
+    if (kind == POV_PATTERN_CHECKER) {
+        const int c = (int)(floorf(T.x + 1.0e-10f) + floorf(T.y + 1.0e-10f) + floorf(T.z + 1.0e-10f));
+        value = (c & 1) ? 1.0f : 0.0f;
+    } else {
+        if (kind == POV_PATTERN_GRADIENT) {
+            value = T.x * pt.gradient.x + T.y * pt.gradient.y + T.z * pt.gradient.z;
+            if (value > 1.0f)
+                value = fmodf(value, 1.0f);
+        } else if (kind == POV_PATTERN_BOZO) {
+            value = pov_noise(S.noise, T, gen);
+        } else {   // granite: six octaves of |noise| (pattern.cpp:6429-6465)
+            value = 0.0f;
+            float freq = 1.0f;
+            for (int i = 0; i < 6; freq *= 2.0f, i++) {
+                const float3 t2 = T * (4.0f * freq);
+                float tmp;
+                if (gen == 1) {
+                    tmp = fabsf(0.5f - pov_noise(S.noise, t2, 1));
+                } else {
+                    tmp = fminf(fabsf(1.0f - 2.0f * pov_noise(S.noise, t2, gen)), 0.5f);
+                }
+                value += tmp / freq;
+            }
+        }
+        value = fmodf(value, 1.00001f);   // ramp wave, frequency 1, phase 0
+        if (value < 0.0f)
+            value -= floorf(value);
+    }
+    if (value >= pt.values[n - 1])
+        return xyz(pt.colours[n - 1]);
+    int ip = 0, in = 0;
+    while (in < n - 1 && value > pt.values[in]) {
+        ip = in;
+        in++;
+    }
+    if (value == pt.values[in] || ip == in)
+        return xyz(pt.colours[in]);
+    const float wp = (pt.values[in] - value) / (pt.values[in] - pt.values[ip]), wn = 1.0f - wp;
+    const float3 a = xyz(pt.colours[ip]), b = xyz(pt.colours[in]);
+    return f3(a.x * wp + b.x * wn, a.y * wp + b.y * wn, a.z * wp + b.z * wn);
+}
+
 // aux word a secondary ray carries about the surface it starts on
 __device__ __forceinline__ uint32_t skip_aux(const QHit& h)
 {
@@ -929,6 +1070,7 @@ __global__ void __launch_bounds__(128) k_shade(
         int oflags = 0;
         uint2 self = make_uint2(h.prim, skip_aux(h));
         bool container = false;
+        float3 pigc = f3(0.f, 0.f, 0.f);   // the hit's pigment colour
         if (hit) {
             SurfaceInfo si = surface(S, h, p);
             ObjectShade os = S.objects[si.object];
@@ -940,9 +1082,9 @@ __global__ void __launch_bounds__(128) k_shade(
                 N = N * -1.0f;
             if (dot3(N, d) > 0.0f)     // face the ray (trace.cpp:492-494)
                 N = N * -1.0f;
-            float4 pig = m->pigment;
+            pigc = m->pattern ? pattern_pigment(S, m->pattern - 1, p) : xyz(m->pigment);
             float4 em = m->emission;
-            col = container ? f3(0.f, 0.f, 0.f) : f3(pig.x * em.x, pig.y * em.y, pig.z * em.z);
+            col = container ? f3(0.f, 0.f, 0.f) : f3(pigc.x * em.x, pigc.y * em.y, pigc.z * em.z);
         } else {
             col = xyz(S.background);   // ComputeSky, background only
         }
@@ -955,7 +1097,7 @@ __global__ void __launch_bounds__(128) k_shade(
         bool rq_emit = false;
         float rq_maxc = 0.f;
         if (shaded && rad.rq) {
-            float3 pg = xyz(m->pigment);
+            float3 pg = pigc;
             rq_maxc = (0.297f * pg.x + 0.589f * pg.y + 0.114f * pg.z) * m->diffuse_raw;
             rq_emit = rq_maxc > rad.adc;
         }
@@ -963,7 +1105,7 @@ __global__ void __launch_bounds__(128) k_shade(
         if (rq_emit) {
             if (rqs < rad.rq_cap) {
                 RadQuery qq;
-                float3 pg = xyz(m->pigment);
+                float3 pg = pigc;
                 qq.p = make_float4(p.x, p.y, p.z, weight * rq_maxc);
                 qq.n = make_float4(N.x, N.y, N.z, 0.f);
                 float dr = m->diffuse_raw;
@@ -997,7 +1139,7 @@ __global__ void __launch_bounds__(128) k_shade(
                 float3 lc = xyz(L.colour);
                 if (lit && !(fabsf(lc.x) < EPSILON_F && fabsf(lc.y) < EPSILON_F && fabsf(lc.z) < EPSILON_F)) {
                     emit = true;
-                    float3 pig = xyz(m->pigment);
+                    float3 pig = pigc;
                     if (m->diffuse > 0.0f) {   // ComputeDiffuseColour, trace.cpp:2441-2484
                         float inten = m->brilliance != 1.0f ? powf(fabsf(cs), m->brilliance) : fabsf(cs);
                         inten *= m->diffuse;

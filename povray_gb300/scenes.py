@@ -164,6 +164,15 @@ class Transform:
         return t
 
     @staticmethod
+    def scaling(v):
+        """Compute_Scaling_Transform (matrix.cpp:596-612)."""
+        t = Transform()
+        for k in range(3):
+            t.matrix[k][k] = float(v[k])
+            t.inverse[k][k] = 1.0 / float(v[k])
+        return t
+
+    @staticmethod
     def translation(v):
         """Compute_Translation_Transform (matrix.cpp:644-657)."""
         t = Transform()
@@ -182,10 +191,65 @@ class Transform:
 
 
 # ------------------------------------------------------------------ scenes --
+class Pattern:
+    """A pattern pigment: `kind` one of checker, gradient, bozo, granite;
+    `colours` the colour map as [(value, rgb), ...] (checker: its two
+    colours as [(0, rgb_a), (1, rgb_b)]); `transforms` the pigment's
+    transformations in SDL order, each ("scale" | "rotate" | "translate",
+    vector); `gradient` the gradient pattern's vector; `noise_generator`
+    1-3 or None for the scene's default (2, range corrected)."""
+    KINDS = {"checker": abi.POV_PATTERN_CHECKER, "gradient": abi.POV_PATTERN_GRADIENT,
+             "bozo": abi.POV_PATTERN_BOZO, "granite": abi.POV_PATTERN_GRANITE}
+
+    def __init__(self, kind, colours, transforms=(), gradient=(1.0, 0.0, 0.0), noise_generator=None):
+        assert kind in self.KINDS
+        self.kind = kind
+        self.colours = [(float(v), tuple(float(c) for c in rgb)) for v, rgb in colours]
+        self.transforms = [(op, tuple(float(x) for x in vec)) for op, vec in transforms]
+        self.gradient = tuple(float(x) for x in gradient)
+        self.noise_generator = noise_generator
+
+    def sdl(self):
+        if self.kind == "checker":
+            body = "checker color rgb %s color rgb %s" % (_v(self.colours[0][1]), _v(self.colours[1][1]))
+        else:
+            head = "gradient %s" % _v(self.gradient) if self.kind == "gradient" else self.kind
+            cmap = " ".join("[%s color rgb %s]" % (_f32(v), _v(c)) for v, c in self.colours)
+            body = "%s color_map { %s }" % (head, cmap)
+        if self.noise_generator is not None:
+            body += " noise_generator %d" % self.noise_generator
+        for op, vec in self.transforms:
+            body += " %s %s" % (op, _v(vec))
+        return body
+
+    def transform(self):
+        t = Transform()
+        for op, vec in self.transforms:
+            t.compose({"scale": Transform.scaling, "rotate": Transform.rotation,
+                       "translate": Transform.translation}[op](vec))
+        return t
+
+    def desc(self):
+        d = abi.PovGpuPattern()
+        d.type = self.KINDS[self.kind]
+        d.noise_generator = 2 if self.noise_generator is None else int(self.noise_generator)
+        d.num_entries = len(self.colours)
+        inv = self.transform().inverse
+        for i in range(4):
+            for j in range(4):
+                d.inverse[4 * i + j] = inv[i][j]
+        d.gradient[:] = self.gradient
+        for k, (v, c) in enumerate(self.colours):
+            d.values[k] = v
+            d.colours[k][:] = c
+        return d
+
+
 class Material:
     def __init__(self, rgb, ambient=0.1, diffuse=0.6, phong=0.0, phong_size=40.0,
                  specular=0.0, roughness=0.05, reflection=0.0, brilliance=1.0,
-                 emission=0.0, transmit=0.0):
+                 emission=0.0, transmit=0.0, pattern=None):
+        self.pattern = pattern
         self.rgb = tuple(float(c) for c in rgb)
         self.transmit = float(transmit)
         self.ambient = float(ambient)
@@ -210,7 +274,9 @@ class Material:
             fin += " reflection %s" % _g(self.reflection)
         if self.emission:
             fin += " emission %s" % _g(self.emission)
-        if self.transmit:
+        if self.pattern is not None:
+            pig = self.pattern.sdl()
+        elif self.transmit:
             pig = "color rgbt <%s,%s,%s,%s>" % (_g(self.rgb[0]), _g(self.rgb[1]), _g(self.rgb[2]), _g(self.transmit))
         else:
             pig = "color rgb %s" % _v(self.rgb)
@@ -516,8 +582,12 @@ class Scene:
             elif o["type"] == abi.POV_OBJ_MESH:
                 d.mesh = o["mesh"]
         mats = (abi.PovGpuMaterial * max(len(self.materials), 1))()
+        pats = []
         for i, m in enumerate(self.materials):
             mats[i] = m.desc()
+            if m.pattern is not None:
+                pats.append(m.pattern.desc())
+                mats[i].pattern = len(pats)
         lights = (abi.PovGpuLight * max(len(self.lights), 1))()
         for i, l in enumerate(self.lights):
             lights[i].center[:] = list(l["pos"])
@@ -582,6 +652,10 @@ class Scene:
         desc.num_medias = len(self.medias)
         desc.medias = medias
         keep.append(medias)
+        patterns = (abi.PovGpuPattern * max(len(pats), 1))(*pats)
+        desc.num_patterns = len(pats)
+        desc.patterns = patterns
+        keep.append(patterns)
         if self.radiosity is not None:
             r = self.radiosity_settings()
             rd = desc.radiosity
@@ -877,6 +951,35 @@ def media_spheres(width=320, height=240, n_spheres=24, seed=5, intervals=10, sam
     return s
 
 
+def textured_spheres(width=320, height=240, n_spheres=12, seed=6, noise_generator=None):
+    """Pattern pigments: a checker floor (plane y=-2, checker scale 1.5),
+    `n_spheres` spheres r U[0.5,1.2] in a 6x6 area (seed 6) cycling through
+    bozo (3-entry colour map, scale 0.4), granite (scale 1.5), gradient y
+    (scale 2, translated) and bozo rotated; one point light, phong 0.3;
+    camera (0,3,-10) looking at (0,0,2), 55 deg; max_trace_level 2."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    s = Scene("textured_spheres", width, height, (0.0, 3.0, -10.0), (0.0, 0.0, 2.0), 55.0, max_trace_level=2)
+    s.point_light((10.0, 15.0, -10.0))
+    ng = noise_generator
+    floor = Pattern("checker", [(0.0, (0.9, 0.9, 0.9)), (1.0, (0.15, 0.2, 0.5))], [("scale", (1.5, 1.5, 1.5))])
+    s.plane((0.0, 1.0, 0.0), -2.0, s.material(Material((1.0, 1.0, 1.0), pattern=floor)))
+    kinds = [
+        Pattern("bozo", [(0.0, (0.9, 0.3, 0.1)), (0.5, (0.95, 0.9, 0.3)), (1.0, (0.1, 0.5, 0.2))],
+                [("scale", (0.4, 0.4, 0.4))], noise_generator=ng),
+        Pattern("granite", [(0.0, (0.2, 0.2, 0.25)), (0.4, (0.8, 0.7, 0.7)), (1.0, (0.95, 0.95, 0.9))],
+                [("scale", (1.5, 1.5, 1.5))], noise_generator=ng),
+        Pattern("gradient", [(0.0, (0.1, 0.2, 0.8)), (1.0, (0.9, 0.9, 1.0))],
+                [("scale", (2.0, 2.0, 2.0)), ("translate", (0.0, 0.3, 0.0))], gradient=(0.0, 1.0, 0.0)),
+        Pattern("bozo", [(0.0, (0.1, 0.1, 0.1)), (0.3, (0.6, 0.2, 0.6)), (1.0, (1.0, 1.0, 1.0))],
+                [("scale", (0.7, 0.3, 0.7)), ("rotate", (20.0, 35.0, 0.0))], noise_generator=ng),
+    ]
+    for i in range(n_spheres):
+        c = (rng.uniform(-3.0, 3.0), rng.uniform(-1.0, 1.5), rng.uniform(0.0, 6.0))
+        r = rng.uniform(0.5, 1.2)
+        s.sphere(c, r, s.material(Material((1.0, 1.0, 1.0), phong=0.3, pattern=kinds[i % len(kinds)])))
+    return s
+
+
 VIEW_SIZES = ((256, 256), (640, 480), (1280, 720), (1920, 1080))
 
 
@@ -941,4 +1044,5 @@ WORKLOADS = {
     "radiosity_room": radiosity_room,
     "media_spheres": media_spheres,
     "multiview_media": multiview_media,
+    "textured_spheres": textured_spheres,
 }
