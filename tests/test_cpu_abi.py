@@ -134,3 +134,66 @@ def test_torus_requires_its_transform(gpu_lib):
     desc.objects[tor].flags &= ~abi.POV_FLAG_HAS_TRANS
     st, bad = _create(gpu_lib, desc)
     assert st == abi.POV_GPU_E_UNSUPPORTED and bad == tor
+
+
+def test_media_container_validation(gpu_lib):
+    """Media containers: hollow boxes whose surface only transmits, method 3
+    without jitter, intervals and AA level within the GPU path's limits,
+    point lights only, camera outside; rejected before any device work."""
+    def fresh():
+        return scenes.media_spheres(32, 24, n_spheres=2).desc()
+    desc, keep = fresh()
+    box = [i for i in range(desc.num_objects) if desc.objects[i].media > 0][0]
+    assert _create(gpu_lib, desc)[0] in (abi.POV_GPU_OK, abi.POV_GPU_E_NODEVICE, abi.POV_GPU_E_CUDA)
+    desc, keep = fresh()
+    desc.objects[box].flags &= ~abi.POV_FLAG_HOLLOW     # a media object that is not hollow
+    assert _create(gpu_lib, desc) == (abi.POV_GPU_E_UNSUPPORTED, box)
+    desc, keep = fresh()
+    desc.medias[0].jitter = 0.5                          # jitter draws on the reference's RNG
+    assert _create(gpu_lib, desc)[0] == abi.POV_GPU_E_UNSUPPORTED
+    desc, keep = fresh()
+    desc.medias[0].intervals = 1000                      # above the per-segment slots
+    assert _create(gpu_lib, desc)[0] == abi.POV_GPU_E_UNSUPPORTED
+    desc, keep = fresh()
+    desc.medias[0].method = 2
+    assert _create(gpu_lib, desc)[0] == abi.POV_GPU_E_UNSUPPORTED
+    desc, keep = fresh()
+    desc.camera.location[0], desc.camera.location[1], desc.camera.location[2] = 0.0, 0.0, 0.0   # inside the box
+    assert _create(gpu_lib, desc)[0] == abi.POV_GPU_E_UNSUPPORTED
+    desc, keep = fresh()
+    desc.objects[box].media = 5                          # no such media
+    assert _create(gpu_lib, desc)[0] == abi.POV_GPU_E_INVALID
+
+
+def test_pattern_validation(gpu_lib):
+    """Pattern pigments: known pattern types, 1..16 ascending colour map
+    entries (checker exactly 2), noise generators 1..3, material indices in
+    range."""
+    def fresh():
+        return scenes.textured_spheres(32, 24, n_spheres=4).desc()
+    desc, keep = fresh()
+    desc.patterns[0].type = 42
+    assert _create(gpu_lib, desc)[0] == abi.POV_GPU_E_UNSUPPORTED
+    desc, keep = fresh()
+    desc.patterns[1].noise_generator = 7
+    assert _create(gpu_lib, desc)[0] == abi.POV_GPU_E_UNSUPPORTED
+    desc, keep = fresh()
+    desc.patterns[1].values[0], desc.patterns[1].values[1] = 0.8, 0.2   # descending map
+    assert _create(gpu_lib, desc)[0] == abi.POV_GPU_E_INVALID
+    desc, keep = fresh()
+    desc.patterns[0].num_entries = 3                      # checker takes two colours
+    assert _create(gpu_lib, desc)[0] == abi.POV_GPU_E_UNSUPPORTED
+    desc, keep = fresh()
+    desc.materials[0].pattern = desc.num_patterns + 1
+    assert _create(gpu_lib, desc)[0] == abi.POV_GPU_E_INVALID
+
+
+def test_oracle_rejects_the_same_scenes():
+    """The oracle applies the same rules as the library."""
+    from oracle.pyoracle import Oracle
+    s = scenes.textured_spheres(32, 24, n_spheres=4)
+    Oracle(s)     # accepted
+    bad = scenes.textured_spheres(32, 24, n_spheres=4)
+    bad.materials[1].pattern.kind = "checker"   # a checker with a three-entry map
+    with pytest.raises(abi.PovGpuError):
+        Oracle(bad)
