@@ -134,26 +134,44 @@ typedef struct PovGpuMaterial {
 
 /* Pattern pigments (PIGMENT with a pattern and a colour map: Compute_Pigment,
  * source/core/material/pigment.cpp:395-475; patterns in
- * source/core/material/pattern.cpp, noise in noise.cpp / portablenoise.cpp).
- * The point is the pattern's TRANSFORM warp applied inversely (Warp_EPoint,
- * warp.cpp:103-122); continuous patterns take the default ramp wave
- * (frequency 1, phase 0: ContinuousPattern::Evaluate, pattern.cpp:354-390);
- * the colour map blends linearly between its entries (BlendMap::Search,
+ * source/core/material/pattern.cpp, noise and turbulence in noise.cpp /
+ * portablenoise.cpp).  The point goes through the pattern's warps as
+ * Warp_EPoint applies them (warp.cpp:103-122): the inverse TRANSFORM, then
+ * the classic turbulence (GenericTurbulenceWarp::WarpPoint, warp.cpp:553-558,
+ * which the parser keeps first in the list); continuous patterns take their
+ * wave (ContinuousPattern::Evaluate, pattern.cpp:354-390); the colour map
+ * blends linearly between its entries (BlendMap::Search,
  * pattern.cpp:1068-1109).  Opaque colours only. */
 #define POV_PATTERN_CHECKER   1   /* CheckerPattern::Evaluate, pattern.cpp:5691      */
 #define POV_PATTERN_GRADIENT  2   /* GradientPattern::EvaluateRaw, pattern.cpp:6386  */
 #define POV_PATTERN_BOZO      3   /* bozo / spotted: NoisePattern, pattern.cpp:7858  */
 #define POV_PATTERN_GRANITE   4   /* GranitePattern::EvaluateRaw, pattern.cpp:6429   */
+#define POV_PATTERN_MARBLE    5   /* MarblePattern::EvaluateRaw, pattern.cpp:7831    */
+#define POV_PATTERN_WOOD      6   /* WoodPattern::EvaluateRaw, pattern.cpp:8651      */
+#define POV_PATTERN_AGATE     7   /* AgatePattern::EvaluateRaw, pattern.cpp:5396     */
+#define POV_PATTERN_ONION     8   /* OnionPattern::EvaluateRaw, pattern.cpp:7934     */
+#define POV_PATTERN_LEOPARD   9   /* LeopardPattern::EvaluateRaw, pattern.cpp:7179   */
+#define POV_WAVE_RAMP     0       /* the default of most patterns                    */
+#define POV_WAVE_SINE     1
+#define POV_WAVE_TRIANGLE 2       /* the default of marble and wood                  */
+#define POV_WAVE_SCALLOP  3
+#define POV_WAVE_CUBIC    4
+#define POV_WAVE_POLY     5
 #define POV_PATTERN_MAX_ENTRIES 16
 typedef struct PovGpuPattern {
     int32_t type;
     int32_t noise_generator;      /* 1 original, 2 range corrected (default), 3 Perlin */
     int32_t num_entries;          /* colour map entries (checker: its two colours)    */
-    int32_t reserved;
+    int32_t wave_type;            /* POV_WAVE_*                                       */
     double  inverse[16];          /* inverse of the pattern's TRANSFORM, row-vector form
                                      (p' = p * M), as MInvTransPoint applies it      */
     double  gradient[3];          /* gradient: the pattern's vector                  */
-    double  pad;
+    double  frequency, phase, exponent;   /* wave modifiers (1, 0, 1 by default)     */
+    double  turbulence[3];        /* classic turbulence vector                       */
+    double  omega, lambda;        /* turbulence: 0.5, 2.0 by default                 */
+    double  agate_turb;           /* agate_turb (1.0 by default)                     */
+    int32_t octaves;              /* turbulence: 6 by default                        */
+    int32_t has_turbulence;       /* the pattern has a classic turbulence warp       */
     float   values[POV_PATTERN_MAX_ENTRIES];        /* colour map values, ascending   */
     float   colours[POV_PATTERN_MAX_ENTRIES][3];    /* colour map rgb                 */
 } PovGpuPattern;

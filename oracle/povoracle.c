@@ -1605,6 +1605,105 @@ static double pov_noise(V3 P, int gen)
     return sum < 0.0 ? 0.0 : (sum > 1.0 ? 1.0 : sum);
 }
 
+/* PortableDNoise (portablenoise.cpp:260-361): vector noise, the lattice
+ * functions of three consecutive table entries per corner (every
+ * generator: DNoise has no Perlin variant). */
+static V3 pov_dnoise(V3 P)
+{
+    const double p[3] = {P.x, P.y, P.z};
+    int ii[3];
+    double f[3], g[3], sc[3], tc[3];
+    for (int a = 0; a < 3; a++) {
+        int tmp = p[a] >= 0 ? (int)p[a] : (int)(p[a] - (1 - EPSILON));
+        ii[a] = (tmp - (-10000)) & 0xFFF;
+        f[a] = p[a] - tmp;
+        g[a] = f[a] - 1;
+        sc[a] = scurve(f[a]);
+        tc[a] = 1 - sc[a];
+    }
+    const double txty = tc[0] * tc[1], sxty = sc[0] * tc[1], txsy = tc[0] * sc[1], sxsy = sc[0] * sc[1];
+#define HASH2(a, b) g_hash[(int)(g_hash[(int)(a)] ^ (b))]
+#define RIDX(a, b) ((g_hash[(int)(a) ^ (b)] & 0xFF) * 2)
+#define INCR(m, s, x, y, z) ((s) * (g_rtab[(m) + 1] + g_rtab[(m) + 2] * (x) + g_rtab[(m) + 4] * (y) + g_rtab[(m) + 6] * (z)))
+    const int h00 = HASH2(ii[0], ii[1]), h10 = HASH2(ii[0] + 1, ii[1]);
+    const int h01 = HASH2(ii[0], ii[1] + 1), h11 = HASH2(ii[0] + 1, ii[1] + 1);
+    /* corners in the reference's order; each adds its three components */
+    const int hc[8] = {h00, h10, h11, h01, h01, h11, h10, h00};
+    const int zc[8] = {0, 0, 0, 0, 1, 1, 1, 1};
+    const double sw[8] = {txty * tc[2], sxty * tc[2], sxsy * tc[2], txsy * tc[2],
+                          txsy * sc[2], sxsy * sc[2], sxty * sc[2], txty * sc[2]};
+    const int xo[8] = {0, 1, 1, 0, 0, 1, 1, 0}, yo[8] = {0, 0, 1, 1, 1, 1, 0, 0};
+    double r[3] = {0.0, 0.0, 0.0};
+    for (int k = 0; k < 8; k++) {
+        int m = RIDX(hc[k], ii[2] + zc[k]);
+        const double x = xo[k] ? g[0] : f[0], y = yo[k] ? g[1] : f[1], z = zc[k] ? g[2] : f[2];
+        for (int c = 0; c < 3; c++, m += 8) {
+            const double v = INCR(m, sw[k], x, y, z);
+            r[c] = k == 0 ? v : r[c] + v;
+        }
+    }
+#undef HASH2
+#undef RIDX
+#undef INCR
+    return v3(r[0], r[1], r[2]);
+}
+
+/* Turbulence and DTurbulence (noise.cpp:522-630): Octaves of the noise at
+ * lambda^k-scaled points, weighted by omega^k. */
+static double pov_turbulence(V3 P, const PovGpuPattern* t, int gen)
+{
+    double value;
+    if (gen == 1) {
+        value = pov_noise(P, gen);
+    } else {
+        value = 2.0 * pov_noise(P, gen) - 0.5;
+        value = value < 0.0 ? 0.0 : (value > 1.0 ? 1.0 : value);
+    }
+    double l = t->lambda, o = t->omega;
+    for (int i = 2; i <= t->octaves; i++) {
+        const V3 q = vmul(P, l);
+        if (gen == 1)
+            value += o * pov_noise(q, gen);
+        else
+            value += o * (2.0 * pov_noise(q, gen) - 0.5);
+        if (i < t->octaves) {
+            l *= t->lambda;
+            o *= t->omega;
+        }
+    }
+    return value;
+}
+
+static V3 pov_dturbulence(V3 P, const PovGpuPattern* t)
+{
+    V3 r = pov_dnoise(P);
+    double l = t->lambda, o = t->omega;
+    for (int i = 2; i <= t->octaves; i++) {
+        const V3 v = pov_dnoise(vmul(P, l));
+        r = vadd(r, vmul(v, o));
+        if (i < t->octaves) {
+            l *= t->lambda;
+            o *= t->omega;
+        }
+    }
+    return r;
+}
+
+/* cycloidal (texture.cpp:98-108) and Triangle_Wave (texture.cpp:138-156). */
+#define TWO_M_PI 6.283185307179586476925286766560
+static double cycloidal(double v)
+{
+    if (v >= 0.0)
+        return sin((double)((v - floor(v)) * 50000.0) / 50000.0 * TWO_M_PI);
+    return 0.0 - sin((double)((0.0 - (v + floor(0.0 - v))) * 50000.0) / 50000.0 * TWO_M_PI);
+}
+
+static double triangle_wave(double v)
+{
+    double off = v >= 0.0 ? v - floor(v) : v + 1.0 + floor(fabs(v));
+    return off >= 0.5 ? 2.0 * (1.0 - off) : 2.0 * off;
+}
+
 /* Compute_Pigment for a pattern pigment (pigment.cpp:395-475): the point
  * through the pattern's inverse TRANSFORM (Warp_EPoint, warp.cpp:103-122),
  * the pattern value, the colour map (BlendMap::Search, pattern.cpp:
@@ -1613,44 +1712,104 @@ static RGB pattern_pigment(const PovGpuPattern* pt, V3 P)
 {
     const double* m = pt->inverse;
     double q[3];
-    for (int i = 0; i < 3; i++) {
+    for (int i = 0; i < 3; i++)
         q[i] = P.x * m[0 * 4 + i] + P.y * m[1 * 4 + i] + P.z * m[2 * 4 + i] + m[3 * 4 + i];
-        if (q[i] > 1.0e17) q[i] = 1.0e17;   /* COORDINATE_LIMIT */
-        if (q[i] < -1.0e17) q[i] = -1.0e17;
+    V3 T = v3(q[0], q[1], q[2]);
+    /* the classic turbulence warp, applied after the transform (the parser
+     * keeps it first in the warp list, Warp_EPoint walks the list backwards) */
+    if (pt->has_turbulence) {
+        const V3 d = pov_dturbulence(T, pt);
+        T = v3(T.x + d.x * pt->turbulence[0], T.y + d.y * pt->turbulence[1], T.z + d.z * pt->turbulence[2]);
     }
-    const V3 T = v3(q[0], q[1], q[2]);
+    {
+        double* c3[3] = {&T.x, &T.y, &T.z};
+        for (int i = 0; i < 3; i++) {   /* COORDINATE_LIMIT */
+            if (*c3[i] > 1.0e17) *c3[i] = 1.0e17;
+            if (*c3[i] < -1.0e17) *c3[i] = -1.0e17;
+        }
+    }
+    const int gen = pt->noise_generator;
     double value;
     if (pt->type == POV_PATTERN_CHECKER) {   /* CheckerPattern::Evaluate, pattern.cpp:5691-5706 */
         int c = (int)(floor(T.x + EPSILON) + floor(T.y + EPSILON) + floor(T.z + EPSILON));
         value = (c & 1) ? 1.0 : 0.0;
     } else {
-        if (pt->type == POV_PATTERN_GRADIENT) {   /* pattern.cpp:6386-6393 */
+        switch (pt->type) {
+        case POV_PATTERN_GRADIENT:   /* pattern.cpp:6386-6393 */
             value = T.x * pt->gradient[0] + T.y * pt->gradient[1] + T.z * pt->gradient[2];
             if (value > 1.0)
                 value = fmod(value, 1.0);
-        } else if (pt->type == POV_PATTERN_BOZO) {   /* NoisePattern, pattern.cpp:7858-7861 */
-            value = pov_noise(T, pt->noise_generator);
-        } else {   /* GranitePattern, pattern.cpp:6429-6465 */
+            break;
+        case POV_PATTERN_BOZO:   /* NoisePattern, pattern.cpp:7858-7861 */
+            value = pov_noise(T, gen);
+            break;
+        case POV_PATTERN_GRANITE: {   /* pattern.cpp:6429-6465 */
             value = 0.0;
             double freq = 1.0;
             const V3 t1 = vmul(T, 4.0);
             for (int i = 0; i < 6; freq *= 2.0, i++) {
                 double tmp;
-                if (pt->noise_generator == 1) {
+                if (gen == 1) {
                     tmp = fabs(0.5 - pov_noise(vmul(t1, freq), 1));
                 } else {
-                    tmp = fabs(1.0 - 2.0 * pov_noise(vmul(t1, freq), pt->noise_generator));
+                    tmp = fabs(1.0 - 2.0 * pov_noise(vmul(t1, freq), gen));
                     if (tmp > 0.5)
                         tmp = 0.5;
                 }
                 value += tmp / freq;
             }
+            break;
         }
-        /* ContinuousPattern::Evaluate, ramp wave, frequency 1, phase 0
-         * (pattern.cpp:354-390) */
-        value = fmod(value * 1.0 + 0.0, 1.00001);
+        case POV_PATTERN_MARBLE:   /* pattern.cpp:7831-7850 */
+            value = T.x + (pt->has_turbulence ? pt->turbulence[0] * pov_turbulence(T, pt, gen) : 0.0);
+            break;
+        case POV_PATTERN_WOOD: {   /* pattern.cpp:8651-8680 */
+            double px = 0.0, py = 0.0;
+            if (pt->has_turbulence) {
+                const V3 wt = pov_dturbulence(T, pt);
+                px = cycloidal((T.x + wt.x) * pt->turbulence[0]);
+                py = cycloidal((T.y + wt.y) * pt->turbulence[1]);
+            }
+            px += T.x;
+            py += T.y;
+            value = sqrt(px * px + py * py + 0.0 * 0.0);
+            break;
+        }
+        case POV_PATTERN_AGATE: {   /* pattern.cpp:5396-5418 */
+            const double tv = pt->agate_turb * pov_turbulence(T, pt, gen);
+            value = 0.5 * (cycloidal(1.3 * tv + 1.1 * T.z) + 1.0);
+            if (value < 0.0) {
+                value = 0.0;
+            } else {
+                value = value < 1.0 ? value : 1.0;
+                value = pow(value, 0.77);
+            }
+            break;
+        }
+        case POV_PATTERN_ONION:   /* pattern.cpp:7934-7952 */
+            value = fmod(sqrt(T.x * T.x + T.y * T.y + T.z * T.z), 1.0);
+            break;
+        default: {   /* leopard, pattern.cpp:7179-7194 */
+            const double t1 = sin(T.x), t2 = sin(T.y), t3 = sin(T.z);
+            const double v = (t1 + t2 + t3) / 3.0;
+            value = v * v;
+            break;
+        }
+        }
+        /* ContinuousPattern::Evaluate (pattern.cpp:354-390): frequency and
+         * phase, then the wave */
+        if (pt->frequency != 0.0)
+            value = fmod(value * pt->frequency + pt->phase, 1.00001);
         if (value < 0.0)
             value -= floor(value);
+        switch (pt->wave_type) {
+        case POV_WAVE_SINE: value = (1.0 + cycloidal(value)) * 0.5; break;
+        case POV_WAVE_TRIANGLE: value = triangle_wave(value); break;
+        case POV_WAVE_SCALLOP: value = fabs(cycloidal(value * 0.5)); break;
+        case POV_WAVE_CUBIC: value = value * value * ((-2.0 * value) + 3.0); break;
+        case POV_WAVE_POLY: value = pow(value, pt->exponent); break;
+        default: break;
+        }
     }
     const int n = pt->num_entries;
     RGB c;
@@ -2883,9 +3042,10 @@ int pov_oracle_create(const PovGpuSceneDesc* desc, PovOracle** out, int32_t* bad
         return POV_GPU_E_INVALID;
     for (int i = 0; i < desc->num_patterns; i++) {
         const PovGpuPattern* pt = &desc->patterns[i];
-        if (pt->type < POV_PATTERN_CHECKER || pt->type > POV_PATTERN_GRANITE || pt->num_entries < 1 ||
+        if (pt->type < POV_PATTERN_CHECKER || pt->type > POV_PATTERN_LEOPARD || pt->num_entries < 1 ||
             pt->num_entries > POV_PATTERN_MAX_ENTRIES || pt->noise_generator < 1 || pt->noise_generator > 3 ||
-            (pt->type == POV_PATTERN_CHECKER && pt->num_entries != 2))
+            (pt->type == POV_PATTERN_CHECKER && pt->num_entries != 2) || pt->wave_type < POV_WAVE_RAMP ||
+            pt->wave_type > POV_WAVE_POLY || pt->octaves < 1 || pt->octaves > 32)
             return POV_GPU_E_UNSUPPORTED;
         for (int k = 1; k < pt->num_entries; k++)
             if (pt->values[k] < pt->values[k - 1])

@@ -70,13 +70,22 @@ POV_PATTERN_CHECKER = 1
 POV_PATTERN_GRADIENT = 2
 POV_PATTERN_BOZO = 3
 POV_PATTERN_GRANITE = 4
+POV_PATTERN_MARBLE = 5
+POV_PATTERN_WOOD = 6
+POV_PATTERN_AGATE = 7
+POV_PATTERN_ONION = 8
+POV_PATTERN_LEOPARD = 9
+POV_WAVES = {"ramp": 0, "sine": 1, "triangle": 2, "scallop": 3, "cubic": 4, "poly": 5}
 POV_PATTERN_MAX_ENTRIES = 16
 
 
 class PovGpuPattern(C.Structure):
     _fields_ = [("type", C.c_int32), ("noise_generator", C.c_int32), ("num_entries", C.c_int32),
-                ("reserved", C.c_int32), ("inverse", C.c_double * 16), ("gradient", C.c_double * 3),
-                ("pad", C.c_double), ("values", C.c_float * POV_PATTERN_MAX_ENTRIES),
+                ("wave_type", C.c_int32), ("inverse", C.c_double * 16), ("gradient", C.c_double * 3),
+                ("frequency", C.c_double), ("phase", C.c_double), ("exponent", C.c_double),
+                ("turbulence", C.c_double * 3), ("omega", C.c_double), ("lambda", C.c_double),
+                ("agate_turb", C.c_double), ("octaves", C.c_int32), ("has_turbulence", C.c_int32),
+                ("values", C.c_float * POV_PATTERN_MAX_ENTRIES),
                 ("colours", (C.c_float * 3) * POV_PATTERN_MAX_ENTRIES)]
 
 

@@ -685,15 +685,16 @@ int validate(const PovGpuSceneDesc* d, int32_t* bad)
         if (rc != POV_GPU_OK)
             return rc;
     }
-    // pattern pigments: the four patterns, 1..16 ascending colour map entries
-    // (checker: 2), noise generators 1..3
+    // pattern pigments: the nine patterns, 1..16 ascending colour map entries
+    // (checker: 2), noise generators 1..3, the six waves, 1..32 octaves
     if (d->num_patterns < 0 || (d->num_patterns > 0 && !d->patterns))
         return POV_GPU_E_INVALID;
     for (int i = 0; i < d->num_patterns; i++) {
         const PovGpuPattern& pt = d->patterns[i];
-        if (pt.type < POV_PATTERN_CHECKER || pt.type > POV_PATTERN_GRANITE || pt.num_entries < 1 ||
+        if (pt.type < POV_PATTERN_CHECKER || pt.type > POV_PATTERN_LEOPARD || pt.num_entries < 1 ||
             pt.num_entries > POV_PATTERN_MAX_ENTRIES || pt.noise_generator < 1 || pt.noise_generator > 3 ||
-            (pt.type == POV_PATTERN_CHECKER && pt.num_entries != 2))
+            (pt.type == POV_PATTERN_CHECKER && pt.num_entries != 2) || pt.wave_type < POV_WAVE_RAMP ||
+            pt.wave_type > POV_WAVE_POLY || pt.octaves < 1 || pt.octaves > 32)
             return POV_GPU_E_UNSUPPORTED;
         for (int k = 1; k < pt.num_entries; k++)
             if (pt.values[k] < pt.values[k - 1])
@@ -1214,8 +1215,13 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
         for (int c = 0; c < 3; c++)
             q.col[c] = make_float4((float)pt.inverse[0 * 4 + c], (float)pt.inverse[1 * 4 + c],
                                    (float)pt.inverse[2 * 4 + c], (float)pt.inverse[3 * 4 + c]);
-        q.gradient = make_float4((float)pt.gradient[0], (float)pt.gradient[1], (float)pt.gradient[2], 0.f);
-        q.kind = make_int4(pt.type, pt.noise_generator, pt.num_entries, 0);
+        q.gradient = make_float4((float)pt.gradient[0], (float)pt.gradient[1], (float)pt.gradient[2],
+                                 (float)pt.agate_turb);
+        q.turb = make_float4((float)pt.turbulence[0], (float)pt.turbulence[1], (float)pt.turbulence[2],
+                             (float)pt.omega);
+        q.wave = make_float4((float)pt.frequency, (float)pt.phase, (float)pt.exponent, (float)pt.lambda);
+        q.kind = make_int4(pt.type, pt.noise_generator, pt.num_entries, pt.wave_type);
+        q.kind2 = make_int4(pt.octaves, pt.has_turbulence, 0, 0);
         for (int k = 0; k < POV_PATTERN_MAX_ENTRIES; k++) {
             q.values[k] = pt.values[k];
             q.colours[k] = make_float4(pt.colours[k][0], pt.colours[k][1], pt.colours[k][2], 0.f);

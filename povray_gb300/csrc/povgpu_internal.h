@@ -79,8 +79,11 @@ struct __align__(16) DevMaterial {
 // colour map.
 struct __align__(16) DevPattern {
     float4 col[3];
-    float4 gradient;        // xyz, -
-    int4   kind;            // type, noise generator, entries, -
+    float4 gradient;        // xyz (normalised), agate_turb
+    float4 turb;            // classic turbulence vector xyz, omega
+    float4 wave;            // frequency, phase, exponent, lambda
+    int4   kind;            // type, noise generator, entries, wave type
+    int4   kind2;           // octaves, has turbulence, -, -
     float  values[16];
     float4 colours[16];
 };

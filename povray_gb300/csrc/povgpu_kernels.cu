@@ -967,6 +967,89 @@ __device__ float pov_noise(const DevNoise& N, float3 P, int gen)
     return fminf(fmaxf(sum, 0.0f), 1.0f);
 }
 
+// PortableDNoise (portablenoise.cpp:260-361): three lattice functions per
+// corner, the corners in the reference's order.
+__device__ float3 pov_dnoise(const DevNoise& N, float3 P)
+{
+    const float p[3] = {P.x, P.y, P.z};
+    int ii[3];
+    float f[3], g[3], sc[3], tc[3];
+    for (int a = 0; a < 3; a++) {
+        const int tmp = p[a] >= 0.0f ? (int)p[a] : (int)((double)p[a] - (1.0 - 1.0e-10));
+        ii[a] = (tmp + 10000) & 0xFFF;
+        f[a] = p[a] - (float)tmp;
+        g[a] = f[a] - 1.0f;
+        sc[a] = noise_scurve(f[a]);
+        tc[a] = 1.0f - sc[a];
+    }
+    auto h2 = [&](int a, int b) { return (int)__ldg(N.hash + ((int)__ldg(N.hash + a) ^ b)); };
+    const int h00 = h2(ii[0], ii[1]), h10 = h2(ii[0] + 1, ii[1]), h01 = h2(ii[0], ii[1] + 1),
+              h11 = h2(ii[0] + 1, ii[1] + 1);
+    const float txty = tc[0] * tc[1], sxty = sc[0] * tc[1], txsy = tc[0] * sc[1], sxsy = sc[0] * sc[1];
+    const int hc[8] = {h00, h10, h11, h01, h01, h11, h10, h00};
+    const float sw[8] = {txty * tc[2], sxty * tc[2], sxsy * tc[2], txsy * tc[2],
+                         txsy * sc[2], sxsy * sc[2], sxty * sc[2], txty * sc[2]};
+    float3 r = f3(0.f, 0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const int zc = k >> 2;
+        const int xo = (k == 1 || k == 2 || k == 5 || k == 6), yo = (k == 2 || k == 3 || k == 4 || k == 5);
+        int m = (__ldg(N.hash + (hc[k] ^ (ii[2] + zc))) & 0xFF) * 2;
+        const float x = xo ? g[0] : f[0], y = yo ? g[1] : f[1], z = zc ? g[2] : f[2];
+        float v[3];
+        for (int c = 0; c < 3; c++, m += 8)
+            v[c] = sw[k] * (__ldg(N.rtab + m + 1) + __ldg(N.rtab + m + 2) * x + __ldg(N.rtab + m + 4) * y +
+                            __ldg(N.rtab + m + 6) * z);
+        r = f3(r.x + v[0], r.y + v[1], r.z + v[2]);
+    }
+    return r;
+}
+
+// Turbulence and DTurbulence (noise.cpp:522-630).
+__device__ float pov_turbulence(const DevNoise& N, float3 P, const DevPattern& pt, int gen)
+{
+    float value = gen == 1 ? pov_noise(N, P, 1) : fminf(fmaxf(2.0f * pov_noise(N, P, gen) - 0.5f, 0.0f), 1.0f);
+    const int oct = pt.kind2.x;
+    float l = pt.wave.w, o = pt.turb.w;
+    for (int i = 2; i <= oct; i++) {
+        const float3 q = P * l;
+        value += gen == 1 ? o * pov_noise(N, q, 1) : o * (2.0f * pov_noise(N, q, gen) - 0.5f);
+        if (i < oct) {
+            l *= pt.wave.w;
+            o *= pt.turb.w;
+        }
+    }
+    return value;
+}
+
+__device__ float3 pov_dturbulence(const DevNoise& N, float3 P, const DevPattern& pt)
+{
+    float3 r = pov_dnoise(N, P);
+    const int oct = pt.kind2.x;
+    float l = pt.wave.w, o = pt.turb.w;
+    for (int i = 2; i <= oct; i++) {
+        r = r + pov_dnoise(N, P * l) * o;
+        if (i < oct) {
+            l *= pt.wave.w;
+            o *= pt.turb.w;
+        }
+    }
+    return r;
+}
+
+// cycloidal (texture.cpp:98-108) and Triangle_Wave (texture.cpp:138-156).
+__device__ __forceinline__ float pat_cycloidal(float v)
+{
+    const float twopi = 6.2831853071795864769f;
+    return v >= 0.0f ? sinf((v - floorf(v)) * twopi) : -sinf((-(v + floorf(-v))) * twopi);
+}
+
+__device__ __forceinline__ float pat_triangle(float v)
+{
+    const float off = v >= 0.0f ? v - floorf(v) : v + 1.0f + floorf(fabsf(v));
+    return off >= 0.5f ? 2.0f * (1.0f - off) : 2.0f * off;
+}
+
 // Compute_Pigment of a pattern pigment at world point P (pigment.cpp:395-475):
 // the pattern's inverse TRANSFORM, the pattern value with the default ramp
 // wave, the colour map's linear blend.
@@ -978,6 +1061,11 @@ __device__ float3 pattern_pigment(const DeviceScene& S, int pi, float3 P)
         const float4 c0 = pt.col[0], c1 = pt.col[1], c2 = pt.col[2];
         T = f3(P.x * c0.x + P.y * c0.y + P.z * c0.z + c0.w, P.x * c1.x + P.y * c1.y + P.z * c1.z + c1.w,
                P.x * c2.x + P.y * c2.y + P.z * c2.z + c2.w);
+    }
+    // the classic turbulence warp after the transform (warp.cpp:553-558)
+    if (pt.kind2.y) {
+        const float3 d = pov_dturbulence(S.noise, T, pt);
+        T = f3(T.x + d.x * pt.turb.x, T.y + d.y * pt.turb.y, T.z + d.z * pt.turb.z);
     }
     const int kind = pt.kind.x, gen = pt.kind.y, n = pt.kind.z;
     float value;
@@ -991,23 +1079,50 @@ __device__ float3 pattern_pigment(const DeviceScene& S, int pi, float3 P)
                 value = fmodf(value, 1.0f);
         } else if (kind == POV_PATTERN_BOZO) {
             value = pov_noise(S.noise, T, gen);
-        } else {   // granite: six octaves of |noise| (pattern.cpp:6429-6465)
+        } else if (kind == POV_PATTERN_GRANITE) {   // six octaves of |noise| (pattern.cpp:6429-6465)
             value = 0.0f;
             float freq = 1.0f;
             for (int i = 0; i < 6; freq *= 2.0f, i++) {
                 const float3 t2 = T * (4.0f * freq);
-                float tmp;
-                if (gen == 1) {
-                    tmp = fabsf(0.5f - pov_noise(S.noise, t2, 1));
-                } else {
-                    tmp = fminf(fabsf(1.0f - 2.0f * pov_noise(S.noise, t2, gen)), 0.5f);
-                }
+                const float tmp = gen == 1 ? fabsf(0.5f - pov_noise(S.noise, t2, 1))
+                                           : fminf(fabsf(1.0f - 2.0f * pov_noise(S.noise, t2, gen)), 0.5f);
                 value += tmp / freq;
             }
+        } else if (kind == POV_PATTERN_MARBLE) {   // pattern.cpp:7831-7850
+            value = T.x + (pt.kind2.y ? pt.turb.x * pov_turbulence(S.noise, T, pt, gen) : 0.0f);
+        } else if (kind == POV_PATTERN_WOOD) {     // pattern.cpp:8651-8680
+            float px = 0.0f, py = 0.0f;
+            if (pt.kind2.y) {
+                const float3 wt = pov_dturbulence(S.noise, T, pt);
+                px = pat_cycloidal((T.x + wt.x) * pt.turb.x);
+                py = pat_cycloidal((T.y + wt.y) * pt.turb.y);
+            }
+            px += T.x;
+            py += T.y;
+            value = sqrtf(px * px + py * py);
+        } else if (kind == POV_PATTERN_AGATE) {    // pattern.cpp:5396-5418
+            const float tv = pt.gradient.w * pov_turbulence(S.noise, T, pt, gen);
+            value = 0.5f * (pat_cycloidal(1.3f * tv + 1.1f * T.z) + 1.0f);
+            value = value < 0.0f ? 0.0f : powf(fminf(value, 1.0f), 0.77f);
+        } else if (kind == POV_PATTERN_ONION) {    // pattern.cpp:7934-7952
+            value = fmodf(sqrtf(T.x * T.x + T.y * T.y + T.z * T.z), 1.0f);
+        } else {                                   // leopard, pattern.cpp:7179-7194
+            const float v = (sinf(T.x) + sinf(T.y) + sinf(T.z)) / 3.0f;
+            value = v * v;
         }
-        value = fmodf(value, 1.00001f);   // ramp wave, frequency 1, phase 0
+        // frequency, phase and wave (ContinuousPattern::Evaluate, pattern.cpp:354-390)
+        if (pt.wave.x != 0.0f)
+            value = fmodf(value * pt.wave.x + pt.wave.y, 1.00001f);
         if (value < 0.0f)
             value -= floorf(value);
+        switch (pt.kind.w) {
+        case POV_WAVE_SINE: value = (1.0f + pat_cycloidal(value)) * 0.5f; break;
+        case POV_WAVE_TRIANGLE: value = pat_triangle(value); break;
+        case POV_WAVE_SCALLOP: value = fabsf(pat_cycloidal(value * 0.5f)); break;
+        case POV_WAVE_CUBIC: value = value * value * ((-2.0f * value) + 3.0f); break;
+        case POV_WAVE_POLY: value = powf(value, pt.wave.z); break;
+        default: break;
+        }
     }
     if (value >= pt.values[n - 1])
         return xyz(pt.colours[n - 1]);

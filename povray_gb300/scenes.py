@@ -192,22 +192,35 @@ class Transform:
 
 # ------------------------------------------------------------------ scenes --
 class Pattern:
-    """A pattern pigment: `kind` one of checker, gradient, bozo, granite;
-    `colours` the colour map as [(value, rgb), ...] (checker: its two
-    colours as [(0, rgb_a), (1, rgb_b)]); `transforms` the pigment's
-    transformations in SDL order, each ("scale" | "rotate" | "translate",
-    vector); `gradient` the gradient pattern's vector; `noise_generator`
-    1-3 or None for the scene's default (2, range corrected)."""
+    """A pattern pigment: `kind` one of checker, gradient, bozo, spotted,
+    granite, marble, wood, agate, onion, leopard; `colours` the colour map
+    as [(value, rgb), ...] (checker: its two colours as [(0, rgb_a),
+    (1, rgb_b)]); `transforms` the pigment's transformations in SDL order,
+    each ("scale" | "rotate" | "translate", vector); `gradient` the gradient
+    pattern's vector; `noise_generator` 1-3 or None for the scene's default
+    (2, range corrected); `turbulence` the classic turbulence vector (None:
+    no turbulence; agate always has one) with `octaves`, `omega`, `lambda_`;
+    `wave` one of ramp, sine, triangle, scallop, cubic, poly (None: the
+    pattern's default) with `frequency`, `phase`, `exponent`; `agate_turb`."""
     KINDS = {"checker": abi.POV_PATTERN_CHECKER, "gradient": abi.POV_PATTERN_GRADIENT,
-             "bozo": abi.POV_PATTERN_BOZO, "granite": abi.POV_PATTERN_GRANITE}
+             "bozo": abi.POV_PATTERN_BOZO, "spotted": abi.POV_PATTERN_BOZO, "granite": abi.POV_PATTERN_GRANITE,
+             "marble": abi.POV_PATTERN_MARBLE, "wood": abi.POV_PATTERN_WOOD, "agate": abi.POV_PATTERN_AGATE,
+             "onion": abi.POV_PATTERN_ONION, "leopard": abi.POV_PATTERN_LEOPARD}
 
-    def __init__(self, kind, colours, transforms=(), gradient=(1.0, 0.0, 0.0), noise_generator=None):
+    def __init__(self, kind, colours, transforms=(), gradient=(1.0, 0.0, 0.0), noise_generator=None,
+                 turbulence=None, octaves=6, omega=0.5, lambda_=2.0, wave=None, frequency=1.0, phase=0.0,
+                 exponent=1.0, agate_turb=1.0):
         assert kind in self.KINDS
         self.kind = kind
         self.colours = [(float(v), tuple(float(c) for c in rgb)) for v, rgb in colours]
         self.transforms = [(op, tuple(float(x) for x in vec)) for op, vec in transforms]
         self.gradient = tuple(float(x) for x in gradient)
         self.noise_generator = noise_generator
+        self.turbulence = None if turbulence is None else tuple(float(x) for x in turbulence)
+        self.octaves, self.omega, self.lambda_ = int(octaves), float(omega), float(lambda_)
+        self.wave = wave
+        self.frequency, self.phase, self.exponent = float(frequency), float(phase), float(exponent)
+        self.agate_turb = float(agate_turb)
 
     def sdl(self):
         if self.kind == "checker":
@@ -216,8 +229,19 @@ class Pattern:
             head = "gradient %s" % _v(self.gradient) if self.kind == "gradient" else self.kind
             cmap = " ".join("[%s color rgb %s]" % (_f32(v), _v(c)) for v, c in self.colours)
             body = "%s color_map { %s }" % (head, cmap)
+            if self.kind == "agate" and self.agate_turb != 1.0:
+                body += " agate_turb %s" % _g(self.agate_turb)
+            if self.wave is not None:
+                body += " %s_wave" % self.wave if self.wave != "poly" else " poly_wave %s" % _g(self.exponent)
+            if self.frequency != 1.0:
+                body += " frequency %s" % _g(self.frequency)
+            if self.phase != 0.0:
+                body += " phase %s" % _g(self.phase)
         if self.noise_generator is not None:
             body += " noise_generator %d" % self.noise_generator
+        if self.turbulence is not None:
+            body += " turbulence %s octaves %d omega %s lambda %s" % (_v(self.turbulence), self.octaves,
+                                                                      _g(self.omega), _g(self.lambda_))
         for op, vec in self.transforms:
             body += " %s %s" % (op, _v(vec))
         return body
@@ -234,11 +258,24 @@ class Pattern:
         d.type = self.KINDS[self.kind]
         d.noise_generator = 2 if self.noise_generator is None else int(self.noise_generator)
         d.num_entries = len(self.colours)
+        default_wave = "triangle" if self.kind in ("marble", "wood") else "ramp"
+        d.wave_type = abi.POV_WAVES[self.wave or default_wave]
         inv = self.transform().inverse
         for i in range(4):
             for j in range(4):
                 d.inverse[4 * i + j] = inv[i][j]
-        d.gradient[:] = self.gradient
+        # the parser normalises the gradient vector (parser_materials.cpp:1443)
+        gl = math.sqrt(sum(x * x for x in self.gradient))
+        d.gradient[:] = tuple(x / gl for x in self.gradient) if gl > 0.0 else self.gradient
+        d.frequency, d.phase, d.exponent = self.frequency, self.phase, self.exponent
+        turb = self.turbulence
+        # agate always carries a classic turbulence warp (Check_Turb in the parser)
+        d.has_turbulence = 1 if (turb is not None or self.kind == "agate") else 0
+        d.turbulence[:] = turb if turb is not None else (0.0, 0.0, 0.0)
+        d.omega = self.omega
+        setattr(d, "lambda", self.lambda_)
+        d.octaves = self.octaves
+        d.agate_turb = self.agate_turb
         for k, (v, c) in enumerate(self.colours):
             d.values[k] = v
             d.colours[k][:] = c
@@ -951,12 +988,15 @@ def media_spheres(width=320, height=240, n_spheres=24, seed=5, intervals=10, sam
     return s
 
 
-def textured_spheres(width=320, height=240, n_spheres=12, seed=6, noise_generator=None):
+def textured_spheres(width=320, height=240, n_spheres=12, seed=6, noise_generator=None, turbulent=False):
     """Pattern pigments: a checker floor (plane y=-2, checker scale 1.5),
     `n_spheres` spheres r U[0.5,1.2] in a 6x6 area (seed 6) cycling through
     bozo (3-entry colour map, scale 0.4), granite (scale 1.5), gradient y
-    (scale 2, translated) and bozo rotated; one point light, phong 0.3;
-    camera (0,3,-10) looking at (0,0,2), 55 deg; max_trace_level 2."""
+    (scale 2, translated) and bozo rotated -- or, with `turbulent`, marble
+    and wood with turbulence, agate, onion, leopard, bozo with turbulence
+    (3 octaves), a sine-wave gradient with frequency and phase and granite
+    with turbulence; one point light, phong 0.3; camera (0,3,-10) looking
+    at (0,0,2), 55 deg; max_trace_level 2."""
     rng = np.random.Generator(np.random.PCG64(seed))
     s = Scene("textured_spheres", width, height, (0.0, 3.0, -10.0), (0.0, 0.0, 2.0), 55.0, max_trace_level=2)
     s.point_light((10.0, 15.0, -10.0))
@@ -973,6 +1013,21 @@ def textured_spheres(width=320, height=240, n_spheres=12, seed=6, noise_generato
         Pattern("bozo", [(0.0, (0.1, 0.1, 0.1)), (0.3, (0.6, 0.2, 0.6)), (1.0, (1.0, 1.0, 1.0))],
                 [("scale", (0.7, 0.3, 0.7)), ("rotate", (20.0, 35.0, 0.0))], noise_generator=ng),
     ]
+    if turbulent:
+        warm = [(0.0, (0.9, 0.85, 0.7)), (0.6, (0.6, 0.3, 0.15)), (1.0, (0.2, 0.1, 0.05))]
+        cool = [(0.0, (0.05, 0.1, 0.3)), (0.5, (0.5, 0.7, 0.9)), (1.0, (1.0, 1.0, 1.0))]
+        kinds = [
+            Pattern("marble", cool, [("scale", (0.8, 0.8, 0.8))], turbulence=(0.7, 0.7, 0.7), noise_generator=ng),
+            Pattern("wood", warm, [("scale", (0.15, 0.15, 0.15)), ("rotate", (90.0, 0.0, 0.0))],
+                    turbulence=(0.05, 0.05, 0.05)),
+            Pattern("agate", warm, [("scale", (0.5, 0.5, 0.5))], agate_turb=0.8, noise_generator=ng),
+            Pattern("onion", cool, [("scale", (0.3, 0.3, 0.3))]),
+            Pattern("leopard", warm, [("scale", (0.1, 0.1, 0.1))]),
+            Pattern("bozo", cool, [("scale", (0.5, 0.5, 0.5))], turbulence=(0.5, 0.3, 0.5), octaves=3, omega=0.6,
+                    lambda_=2.5, noise_generator=ng),
+            Pattern("gradient", warm, gradient=(1.0, 1.0, 0.0), wave="sine", frequency=2.0, phase=0.25),
+            Pattern("granite", cool, [("scale", (2.0, 2.0, 2.0))], turbulence=(0.3, 0.3, 0.3), noise_generator=ng),
+        ]
     for i in range(n_spheres):
         c = (rng.uniform(-3.0, 3.0), rng.uniform(-1.0, 1.5), rng.uniform(0.0, 6.0))
         r = rng.uniform(0.5, 1.2)

@@ -58,6 +58,9 @@ def cases():
         "textured_spheres_160x120": (scenes.textured_spheres(160, 120), 2, 8.0),
         "textured_perlin_160x120": (scenes.textured_spheres(160, 120, noise_generator=3), 2, 8.0),
         "textured_original_160x120": (scenes.textured_spheres(160, 120, noise_generator=1), 2, 8.0),
+        "textured_turbulent_160x120": (scenes.textured_spheres(160, 120, n_spheres=16, turbulent=True), 2, 8.0),
+        "textured_turbulent_perlin_160x120": (scenes.textured_spheres(160, 120, n_spheres=16, turbulent=True,
+                                                                      noise_generator=3), 2, 8.0),
     }
 
 
