@@ -130,6 +130,8 @@ typedef struct PovGpuMaterial {
     float irid;
     int32_t pattern;           /* pigment pattern: 1-based index into the scene's
                                   patterns, 0 = the plain pigment above       */
+    int32_t normal;            /* normal perturbation: 1-based index into the
+                                  scene's normals, 0 = the surface's own      */
 } PovGpuMaterial;
 
 /* Pattern pigments (PIGMENT with a pattern and a colour map: Compute_Pigment,
@@ -151,6 +153,11 @@ typedef struct PovGpuMaterial {
 #define POV_PATTERN_AGATE     7   /* AgatePattern::EvaluateRaw, pattern.cpp:5396     */
 #define POV_PATTERN_ONION     8   /* OnionPattern::EvaluateRaw, pattern.cpp:7934     */
 #define POV_PATTERN_LEOPARD   9   /* LeopardPattern::EvaluateRaw, pattern.cpp:7179   */
+/* normal-only patterns (the special normals of Perturb_Normal,
+ * source/core/material/normal.cpp:855-878) */
+#define POV_PATTERN_BUMPS    10   /* bumps, normal.cpp:235-246                       */
+#define POV_PATTERN_DENTS    11   /* dents, normal.cpp:272-288                       */
+#define POV_PATTERN_WRINKLES 12   /* wrinkles, normal.cpp:325-346                    */
 #define POV_WAVE_RAMP     0       /* the default of most patterns                    */
 #define POV_WAVE_SINE     1
 #define POV_WAVE_TRIANGLE 2       /* the default of marble and wood                  */
@@ -166,6 +173,9 @@ typedef struct PovGpuPattern {
     double  inverse[16];          /* inverse of the pattern's TRANSFORM, row-vector form
                                      (p' = p * M), as MInvTransPoint applies it      */
     double  gradient[3];          /* gradient: the pattern's vector                  */
+    /* frequency, phase, exponent, omega, lambda and agate_turb are used
+       rounded to single precision, as the reference stores them (SNGL
+       waveFrequency, wavePhase, waveExponent, Lambda, Omega, agateTurbScale) */
     double  frequency, phase, exponent;   /* wave modifiers (1, 0, 1 by default)     */
     double  turbulence[3];        /* classic turbulence vector                       */
     double  omega, lambda;        /* turbulence: 0.5, 2.0 by default                 */
@@ -175,6 +185,25 @@ typedef struct PovGpuPattern {
     float   values[POV_PATTERN_MAX_ENTRIES];        /* colour map values, ascending   */
     float   colours[POV_PATTERN_MAX_ENTRIES][3];    /* colour map rgb                 */
 } PovGpuPattern;
+
+/* Normal perturbation (TNORMAL, source/core/material/pattern.h; applied by
+ * Perturb_Normal, source/core/material/normal.cpp:784-905, from
+ * ComputeLightedTexture, source/core/render/trace.cpp:812-832).  The
+ * referenced pattern gives the kind (bumps, dents, wrinkles, or a continuous
+ * pattern whose value the four-point slope of normal.cpp:880-902 samples),
+ * the noise generator, the warps (its inverse TRANSFORM and classic
+ * turbulence) and the wave; its colour map is not read.  The normal enters
+ * the pattern's space through the forward TRANSFORM (Warp_Normal,
+ * warp.cpp:563-580) and leaves it through the inverse (UnWarp_Normal,
+ * warp.cpp:603-620).  Without a normal_map or slope_map. */
+typedef struct PovGpuNormal {
+    int32_t pattern;           /* 1-based index into the scene's patterns     */
+    int32_t dont_scale_bumps;  /* no_bump_scale (DONT_SCALE_BUMPS_FLAG)       */
+    float   amount;            /* TNORMAL::Amount, 0.5 by default             */
+    float   delta;             /* TNORMAL::Delta (accuracy), 0.02 by default  */
+    double  matrix[16];        /* the pattern's forward TRANSFORM, row-vector
+                                  form (p' = p * M)                           */
+} PovGpuNormal;
 
 /* Light source: point light or rectangular area light (LightSource,
  * source/core/scene/object.h:313). */
@@ -283,6 +312,8 @@ typedef struct PovGpuSceneDesc {
     const struct PovGpuMedia* medias;
     int32_t               num_patterns;
     const PovGpuPattern*  patterns;
+    int32_t               num_normals;
+    const PovGpuNormal*   normals;
 } PovGpuSceneDesc;
 
 /* A render block, as POVRect (inclusive bounds) plus its serial number. */

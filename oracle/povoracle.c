@@ -1659,7 +1659,9 @@ static double pov_turbulence(V3 P, const PovGpuPattern* t, int gen)
         value = 2.0 * pov_noise(P, gen) - 0.5;
         value = value < 0.0 ? 0.0 : (value > 1.0 ? 1.0 : value);
     }
-    double l = t->lambda, o = t->omega;
+    /* GenericTurbulenceWarp keeps Lambda and Omega in single precision */
+    const double lambda = (float)t->lambda, omega = (float)t->omega;
+    double l = lambda, o = omega;
     for (int i = 2; i <= t->octaves; i++) {
         const V3 q = vmul(P, l);
         if (gen == 1)
@@ -1667,8 +1669,8 @@ static double pov_turbulence(V3 P, const PovGpuPattern* t, int gen)
         else
             value += o * (2.0 * pov_noise(q, gen) - 0.5);
         if (i < t->octaves) {
-            l *= t->lambda;
-            o *= t->omega;
+            l *= lambda;
+            o *= omega;
         }
     }
     return value;
@@ -1677,13 +1679,15 @@ static double pov_turbulence(V3 P, const PovGpuPattern* t, int gen)
 static V3 pov_dturbulence(V3 P, const PovGpuPattern* t)
 {
     V3 r = pov_dnoise(P);
-    double l = t->lambda, o = t->omega;
+    /* GenericTurbulenceWarp keeps Lambda and Omega in single precision */
+    const double lambda = (float)t->lambda, omega = (float)t->omega;
+    double l = lambda, o = omega;
     for (int i = 2; i <= t->octaves; i++) {
         const V3 v = pov_dnoise(vmul(P, l));
         r = vadd(r, vmul(v, o));
         if (i < t->octaves) {
-            l *= t->lambda;
-            o *= t->omega;
+            l *= lambda;
+            o *= omega;
         }
     }
     return r;
@@ -1708,7 +1712,9 @@ static double triangle_wave(double v)
  * through the pattern's inverse TRANSFORM (Warp_EPoint, warp.cpp:103-122),
  * the pattern value, the colour map (BlendMap::Search, pattern.cpp:
  * 1068-1109, linear blend). */
-static RGB pattern_pigment(const PovGpuPattern* pt, V3 P)
+/* Warp_EPoint (warp.cpp:103-122): the pattern's inverse TRANSFORM, then
+ * the classic turbulence, then COORDINATE_LIMIT. */
+static V3 pattern_warp(const PovGpuPattern* pt, V3 P)
 {
     const double* m = pt->inverse;
     double q[3];
@@ -1728,6 +1734,14 @@ static RGB pattern_pigment(const PovGpuPattern* pt, V3 P)
             if (*c3[i] < -1.0e17) *c3[i] = -1.0e17;
         }
     }
+    return T;
+}
+
+/* Evaluate_TPat of a warped point T: the pattern's value with its
+ * frequency, phase and wave (ContinuousPattern::Evaluate,
+ * pattern.cpp:354-390). */
+static double pattern_value(const PovGpuPattern* pt, V3 T)
+{
     const int gen = pt->noise_generator;
     double value;
     if (pt->type == POV_PATTERN_CHECKER) {   /* CheckerPattern::Evaluate, pattern.cpp:5691-5706 */
@@ -1776,7 +1790,7 @@ static RGB pattern_pigment(const PovGpuPattern* pt, V3 P)
             break;
         }
         case POV_PATTERN_AGATE: {   /* pattern.cpp:5396-5418 */
-            const double tv = pt->agate_turb * pov_turbulence(T, pt, gen);
+            const double tv = (double)(float)pt->agate_turb * pov_turbulence(T, pt, gen);   /* SNGL agateTurbScale */
             value = 0.5 * (cycloidal(1.3 * tv + 1.1 * T.z) + 1.0);
             if (value < 0.0) {
                 value = 0.0;
@@ -1798,8 +1812,9 @@ static RGB pattern_pigment(const PovGpuPattern* pt, V3 P)
         }
         /* ContinuousPattern::Evaluate (pattern.cpp:354-390): frequency and
          * phase, then the wave */
-        if (pt->frequency != 0.0)
-            value = fmod(value * pt->frequency + pt->phase, 1.00001);
+        /* waveFrequency, wavePhase and waveExponent are single precision */
+        if ((float)pt->frequency != 0.0f)
+            value = fmod(value * (double)(float)pt->frequency + (double)(float)pt->phase, 1.00001);
         if (value < 0.0)
             value -= floor(value);
         switch (pt->wave_type) {
@@ -1807,10 +1822,16 @@ static RGB pattern_pigment(const PovGpuPattern* pt, V3 P)
         case POV_WAVE_TRIANGLE: value = triangle_wave(value); break;
         case POV_WAVE_SCALLOP: value = fabs(cycloidal(value * 0.5)); break;
         case POV_WAVE_CUBIC: value = value * value * ((-2.0 * value) + 3.0); break;
-        case POV_WAVE_POLY: value = pow(value, pt->exponent); break;
+        case POV_WAVE_POLY: value = pow(value, (double)(float)pt->exponent); break;
         default: break;
         }
     }
+    return value;
+}
+
+static RGB pattern_pigment(const PovGpuPattern* pt, V3 P)
+{
+    const double value = pattern_value(pt, pattern_warp(pt, P));
     const int n = pt->num_entries;
     RGB c;
     if (value >= pt->values[n - 1]) {
@@ -1832,6 +1853,78 @@ static RGB pattern_pigment(const PovGpuPattern* pt, V3 P)
     c.g = pt->colours[ip][1] * wp + pt->colours[in][1] * wn;
     c.b = pt->colours[ip][2] * wp + pt->colours[in][2] * wn;
     return c;
+}
+
+/* MInvTransNormal (matrix.cpp:495-508): temp[i] = v . M[i][0..2]; with the
+ * forward matrix it takes a normal into the pattern's space (Warp_Normal,
+ * TransformWarp::WarpNormal, warp.cpp:582-586), with the inverse back out
+ * (UnWarp_Normal, TransformWarp::UnwarpNormal, warp.cpp:622-626). */
+static V3 normal_through(const double* m, V3 v)
+{
+    return v3(v.x * m[0] + v.y * m[1] + v.z * m[2], v.x * m[4] + v.y * m[5] + v.z * m[6],
+              v.x * m[8] + v.y * m[9] + v.z * m[10]);
+}
+
+/* The four pyramid directions of the slope sampling (normal.cpp:88-91). */
+static const double kPyramid[4][3] = {{0.942809041, -0.333333333, 0.0},
+                                      {-0.471404521, -0.333333333, 0.816496581},
+                                      {-0.471404521, -0.333333333, -0.816496581},
+                                      {0.0, 1.0, 0.0}};
+
+/* The layer normal of a textured hit (trace.cpp:812-832): Perturb_Normal
+ * (normal.cpp:784-905) of the raw normal N at world point P, normalised
+ * afterwards under no_bump_scale. */
+static V3 perturb_normal(const PovGpuNormal* nm, const PovGpuPattern* pt, V3 P, V3 N)
+{
+    const int scale = !nm->dont_scale_bumps;
+    /* Warp_Normal (warp.cpp:563-580): normalise, the TRANSFORM, normalise */
+    if (scale)
+        N = vnorm(N);
+    N = normal_through(nm->matrix, N);
+    if (scale)
+        N = vnorm(N);
+    const V3 T = pattern_warp(pt, P);
+    const double amount = (double)nm->amount;
+    switch (pt->type) {
+    case POV_PATTERN_BUMPS:   /* bumps, normal.cpp:235-246 */
+        N = vadd(N, vmul(pov_dnoise(T), amount));
+        break;
+    case POV_PATTERN_DENTS: {  /* dents, normal.cpp:272-288 */
+        double v = pov_noise(T, pt->noise_generator);
+        v = v * v * v * amount;
+        N = vadd(N, vmul(pov_dnoise(T), v));
+        break;
+    }
+    case POV_PATTERN_WRINKLES: {  /* wrinkles, normal.cpp:325-346 */
+        double r[3] = {0.0, 0.0, 0.0};
+        double sc = 1.0;
+        for (int i = 0; i < 10; sc *= 2.0, i++) {
+            const V3 d = pov_dnoise(vmul(T, sc));
+            r[0] += fabs(d.x / sc);
+            r[1] += fabs(d.y / sc);
+            r[2] += fabs(d.z / sc);
+        }
+        N = vadd(N, vmul(v3(r[0], r[1], r[2]), amount));
+        break;
+    }
+    default: {  /* the slope of a continuous pattern, normal.cpp:880-902 */
+        const double delta = (double)nm->delta;
+        const double a = amount * -5.0 * (0.02 / delta);
+        for (int i = 0; i < 4; i++) {
+            const V3 d = v3(kPyramid[i][0], kPyramid[i][1], kPyramid[i][2]);
+            const double v = pattern_value(pt, vadd(T, vmul(d, delta)));
+            N = vadd(N, vmul(d, v * a));
+        }
+        break;
+    }
+    }
+    /* UnWarp_Normal (warp.cpp:603-620) */
+    if (scale)
+        N = vnorm(N);
+    N = normal_through(pt->inverse, N);
+    /* UnWarp_Normal's last normalisation; under no_bump_scale the one of
+     * trace.cpp:821-822 */
+    return vnorm(N);
 }
 
 /* Material of an object: its own, else the nearest CSG ancestor's. */
@@ -2057,6 +2150,10 @@ static void shade(const PovOracle* S, Thread* th, const Isect* is, V3 D, double 
     RGB pig = {m->pigment[0], m->pigment[1], m->pigment[2]};
     if (m->pattern > 0)
         pig = pattern_pigment(&S->desc.patterns[m->pattern - 1], is->ipoint);
+    if (m->normal > 0) {
+        const PovGpuNormal* nm = &S->desc.normals[m->normal - 1];
+        N = perturb_normal(nm, &S->desc.patterns[nm->pattern - 1], ip, raw);
+    }
     double r = 0.0, g = 0.0, b = 0.0;
 
     /* ComputeReflectivity (trace.cpp:2627-2656), non-fresnel */
@@ -3036,24 +3133,44 @@ int pov_oracle_create(const PovGpuSceneDesc* desc, PovOracle** out, int32_t* bad
              L->jitter || (L->circular && (L->area_size1 < 2 || L->area_size2 < 2))))
             return POV_GPU_E_UNSUPPORTED;   /* jitter draws on the reference's RNG stream */
     }
-    /* pattern pigments: the four patterns with a colour map of 1..16
-     * ascending entries (checker: 2), noise generators 1..3 */
+    /* patterns: the nine pigment patterns and the three normal-only ones,
+     * 0..16 ascending colour map entries, noise generators 1..3; a pigment
+     * reads one of the nine with 1..16 entries (checker: 2), a normal any
+     * but checker (whose normal form is a normal map) */
     if (desc->num_patterns < 0 || (desc->num_patterns > 0 && !desc->patterns))
         return POV_GPU_E_INVALID;
     for (int i = 0; i < desc->num_patterns; i++) {
         const PovGpuPattern* pt = &desc->patterns[i];
-        if (pt->type < POV_PATTERN_CHECKER || pt->type > POV_PATTERN_LEOPARD || pt->num_entries < 1 ||
+        if (pt->type < POV_PATTERN_CHECKER || pt->type > POV_PATTERN_WRINKLES || pt->num_entries < 0 ||
             pt->num_entries > POV_PATTERN_MAX_ENTRIES || pt->noise_generator < 1 || pt->noise_generator > 3 ||
-            (pt->type == POV_PATTERN_CHECKER && pt->num_entries != 2) || pt->wave_type < POV_WAVE_RAMP ||
-            pt->wave_type > POV_WAVE_POLY || pt->octaves < 1 || pt->octaves > 32)
+            pt->wave_type < POV_WAVE_RAMP || pt->wave_type > POV_WAVE_POLY || pt->octaves < 1 || pt->octaves > 32 ||
+            (pt->type == POV_PATTERN_CHECKER && pt->num_entries != 2))
             return POV_GPU_E_UNSUPPORTED;
         for (int k = 1; k < pt->num_entries; k++)
             if (pt->values[k] < pt->values[k - 1])
                 return POV_GPU_E_INVALID;
     }
-    for (int i = 0; i < desc->num_materials; i++)
-        if (desc->materials[i].pattern < 0 || desc->materials[i].pattern > desc->num_patterns)
+    if (desc->num_normals < 0 || (desc->num_normals > 0 && !desc->normals))
+        return POV_GPU_E_INVALID;
+    for (int i = 0; i < desc->num_normals; i++) {
+        const PovGpuNormal* nm = &desc->normals[i];
+        if (nm->pattern < 1 || nm->pattern > desc->num_patterns)
             return POV_GPU_E_INVALID;
+        if (desc->patterns[nm->pattern - 1].type == POV_PATTERN_CHECKER || !(nm->delta > 0.0f) ||
+            !isfinite(nm->amount))
+            return POV_GPU_E_UNSUPPORTED;
+    }
+    for (int i = 0; i < desc->num_materials; i++) {
+        const PovGpuMaterial* m = &desc->materials[i];
+        if (m->pattern < 0 || m->pattern > desc->num_patterns || m->normal < 0 || m->normal > desc->num_normals)
+            return POV_GPU_E_INVALID;
+        if (m->pattern > 0) {
+            const PovGpuPattern* pt = &desc->patterns[m->pattern - 1];
+            if (pt->type > POV_PATTERN_LEOPARD || pt->num_entries < 1 ||
+                (pt->type == POV_PATTERN_CHECKER && pt->num_entries != 2))
+                return POV_GPU_E_UNSUPPORTED;
+        }
+    }
     pthread_once(&g_noise_once, noise_init);
     PovOracle* S = (PovOracle*)calloc(1, sizeof(PovOracle));
     S->desc = *desc;

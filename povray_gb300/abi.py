@@ -63,7 +63,8 @@ class PovGpuMaterial(C.Structure):
                 ("reflection_falloff", C.c_float), ("reflect_exp", C.c_float),
                 ("reflect_metallic", C.c_float), ("reflection_fresnel", C.c_int32),
                 ("conserve_energy", C.c_int32), ("fresnel", C.c_float),
-                ("crand", C.c_float), ("irid", C.c_float), ("pattern", C.c_int32)]
+                ("crand", C.c_float), ("irid", C.c_float), ("pattern", C.c_int32),
+                ("normal", C.c_int32)]
 
 
 POV_PATTERN_CHECKER = 1
@@ -75,6 +76,9 @@ POV_PATTERN_WOOD = 6
 POV_PATTERN_AGATE = 7
 POV_PATTERN_ONION = 8
 POV_PATTERN_LEOPARD = 9
+POV_PATTERN_BUMPS = 10
+POV_PATTERN_DENTS = 11
+POV_PATTERN_WRINKLES = 12
 POV_WAVES = {"ramp": 0, "sine": 1, "triangle": 2, "scallop": 3, "cubic": 4, "poly": 5}
 POV_PATTERN_MAX_ENTRIES = 16
 
@@ -96,6 +100,11 @@ class PovGpuLight(C.Structure):
                 ("adaptive_level", C.c_int32), ("jitter", C.c_int32),
                 ("circular", C.c_int32), ("orient", C.c_int32),
                 ("fade_distance", C.c_float), ("fade_power", C.c_float)]
+
+
+class PovGpuNormal(C.Structure):
+    _fields_ = [("pattern", C.c_int32), ("dont_scale_bumps", C.c_int32), ("amount", C.c_float),
+                ("delta", C.c_float), ("matrix", C.c_double * 16)]
 
 
 class PovGpuMesh(C.Structure):
@@ -140,7 +149,8 @@ class PovGpuSceneDesc(C.Structure):
                 ("max_trace_level", C.c_int32), ("adc_bailout", C.c_float),
                 ("language_version", C.c_int32), ("radiosity", PovGpuRadiosity),
                 ("num_medias", C.c_int32), ("medias", C.POINTER(PovGpuMedia)),
-                ("num_patterns", C.c_int32), ("patterns", C.POINTER(PovGpuPattern))]
+                ("num_patterns", C.c_int32), ("patterns", C.POINTER(PovGpuPattern)),
+                ("num_normals", C.c_int32), ("normals", C.POINTER(PovGpuNormal))]
 
 
 class PovGpuBlock(C.Structure):

@@ -531,7 +531,7 @@ struct PovGpuScene {
     // persistent scene data
     DevBuf nodes, refs, tri_v0, tri_e1, tri_e2, tri_global, tri_shade, tri_normal, tri_local, normals;
     DevBuf spheres, spheres64, boxes64, sphere_obj, sphere_flags, planes, plane_obj, boxes, tori, csgs, csg_children, objects,
-        materials, lights, medias, patterns, noise_hash, noise_rtab, noise_perm, noise_grad;
+        materials, lights, medias, patterns, tnormals, noise_hash, noise_rtab, noise_perm, noise_grad;
     DevBuf encode_buf;     // staging of pov_gpu_encode_u8 for host outputs
     int    media_ni = 0;   // interval slots per media segment (0: no media containers)
     int    media_smax = 0;  // sample slots per interval (ends + sample-tree nodes)
@@ -574,7 +574,7 @@ struct PovGpuScene {
                          &csg_children, &objects, &materials, &lights, &blocks, &block_off, &corner_off, &qA,
                          &hits, &out, &counters, &stats, &err, &rays_in, &t64, &corners, &aa_grid, &aa_mask,
                          &aa_subdiv, &aa_xy, &cellsA, &cellsB, &spos, &sslot, &wcount, &pos_count, &medias,
-                         &encode_buf, &patterns, &noise_hash, &noise_rtab, &noise_perm, &noise_grad};
+                         &encode_buf, &patterns, &tnormals, &noise_hash, &noise_rtab, &noise_perm, &noise_grad};
         for (DevBuf* b : all)
             b->release();
         top.release();
@@ -685,24 +685,44 @@ int validate(const PovGpuSceneDesc* d, int32_t* bad)
         if (rc != POV_GPU_OK)
             return rc;
     }
-    // pattern pigments: the nine patterns, 1..16 ascending colour map entries
-    // (checker: 2), noise generators 1..3, the six waves, 1..32 octaves
+    // patterns: the nine pigment patterns and the three normal-only ones,
+    // 0..16 ascending colour map entries, noise generators 1..3, the six
+    // waves, 1..32 octaves; a pigment reads one of the nine with 1..16
+    // entries (checker: 2), a normal any but checker (whose normal form is a
+    // normal map), with a positive delta
     if (d->num_patterns < 0 || (d->num_patterns > 0 && !d->patterns))
         return POV_GPU_E_INVALID;
     for (int i = 0; i < d->num_patterns; i++) {
         const PovGpuPattern& pt = d->patterns[i];
-        if (pt.type < POV_PATTERN_CHECKER || pt.type > POV_PATTERN_LEOPARD || pt.num_entries < 1 ||
+        if (pt.type < POV_PATTERN_CHECKER || pt.type > POV_PATTERN_WRINKLES || pt.num_entries < 0 ||
             pt.num_entries > POV_PATTERN_MAX_ENTRIES || pt.noise_generator < 1 || pt.noise_generator > 3 ||
-            (pt.type == POV_PATTERN_CHECKER && pt.num_entries != 2) || pt.wave_type < POV_WAVE_RAMP ||
-            pt.wave_type > POV_WAVE_POLY || pt.octaves < 1 || pt.octaves > 32)
+            pt.wave_type < POV_WAVE_RAMP || pt.wave_type > POV_WAVE_POLY || pt.octaves < 1 || pt.octaves > 32 ||
+            (pt.type == POV_PATTERN_CHECKER && pt.num_entries != 2))
             return POV_GPU_E_UNSUPPORTED;
         for (int k = 1; k < pt.num_entries; k++)
             if (pt.values[k] < pt.values[k - 1])
                 return POV_GPU_E_INVALID;
     }
-    for (int i = 0; i < d->num_materials; i++)
-        if (d->materials[i].pattern < 0 || d->materials[i].pattern > d->num_patterns)
+    if (d->num_normals < 0 || (d->num_normals > 0 && !d->normals))
+        return POV_GPU_E_INVALID;
+    for (int i = 0; i < d->num_normals; i++) {
+        const PovGpuNormal& nm = d->normals[i];
+        if (nm.pattern < 1 || nm.pattern > d->num_patterns)
             return POV_GPU_E_INVALID;
+        if (d->patterns[nm.pattern - 1].type == POV_PATTERN_CHECKER || !(nm.delta > 0.0f) || !std::isfinite(nm.amount))
+            return POV_GPU_E_UNSUPPORTED;
+    }
+    for (int i = 0; i < d->num_materials; i++) {
+        const PovGpuMaterial& m = d->materials[i];
+        if (m.pattern < 0 || m.pattern > d->num_patterns || m.normal < 0 || m.normal > d->num_normals)
+            return POV_GPU_E_INVALID;
+        if (m.pattern > 0) {
+            const PovGpuPattern& pt = d->patterns[m.pattern - 1];
+            if (pt.type > POV_PATTERN_LEOPARD || pt.num_entries < 1 ||
+                (pt.type == POV_PATTERN_CHECKER && pt.num_entries != 2))
+                return POV_GPU_E_UNSUPPORTED;
+        }
+    }
     for (int i = 0; i < d->num_materials; i++) {
         const PovGpuMaterial& m = d->materials[i];
         // opaque plain pigments and the classic finish terms only (media
@@ -786,6 +806,7 @@ DevMaterial make_material(const PovGpuMaterial& m, const float* ambient_light, b
     d.has_reflection = anyr ? 1 : 0;
     d.diffuse_raw = m.diffuse;
     d.pattern = m.pattern;
+    d.normal = m.normal;
     return d;
 }
 
@@ -1227,6 +1248,21 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
             q.colours[k] = make_float4(pt.colours[k][0], pt.colours[k][1], pt.colours[k][2], 0.f);
         }
     }
+    // normal perturbations: the forward TRANSFORM's 3x3 rows
+    // (MInvTransNormal with the matrix, matrix.cpp:495-508)
+    std::vector<DevNormal> nrms(std::max(d->num_normals, 1));
+    for (int i = 0; i < d->num_normals; i++) {
+        const PovGpuNormal& nm = d->normals[i];
+        DevNormal& q = nrms[i];
+        for (int r = 0; r < 3; r++)
+            q.fwd[r] = make_float4((float)nm.matrix[r * 4 + 0], (float)nm.matrix[r * 4 + 1],
+                                   (float)nm.matrix[r * 4 + 2], 0.f);
+        // the slope's factor as the reference forms it in double
+        // (normal.cpp:887-889)
+        const double slope = (double)nm.amount * -5.0 * (0.02 / (double)nm.delta);
+        q.params = make_float4(nm.amount, nm.delta, (float)slope, 0.f);
+        q.kind = make_int4(nm.pattern - 1, nm.dont_scale_bumps ? 1 : 0, 0, 0);
+    }
     NoiseTables nt;
     if (d->num_patterns > 0)
         nt.build();
@@ -1236,6 +1272,7 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
     CK(upload(sc->lights, lights));
     CK(upload(sc->medias, medias));
     CK(upload(sc->patterns, pats));
+    CK(upload(sc->tnormals, nrms));
     CK(upload(sc->noise_hash, nt.hash));
     CK(upload(sc->noise_rtab, nt.rtab));
     CK(upload(sc->noise_perm, nt.perm));
@@ -1285,6 +1322,7 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
     S.num_area_lights = num_area;
     S.medias = sc->medias.as<DevMedia>();
     S.patterns = sc->patterns.as<DevPattern>();
+    S.tnormals = sc->tnormals.as<DevNormal>();
     S.noise.hash = sc->noise_hash.as<uint16_t>();
     S.noise.rtab = sc->noise_rtab.as<float>();
     S.noise.perm = sc->noise_perm.as<int32_t>();

@@ -72,6 +72,7 @@ struct __align__(16) DevMaterial {
     int32_t has_reflection;
     float   diffuse_raw;    // Finish->Diffuse, the radiosity ambient's factor (trace.cpp:898)
     int32_t pattern;        // pigment pattern + 1 (0: the plain pigment above)
+    int32_t normal;         // normal perturbation + 1 (0: the raw normal)
 };
 
 // Pattern pigment (Compute_Pigment with a colour map): the inverse TRANSFORM
@@ -86,6 +87,16 @@ struct __align__(16) DevPattern {
     int4   kind2;           // octaves, has turbulence, -, -
     float  values[16];
     float4 colours[16];
+};
+
+// Normal perturbation (Perturb_Normal): the pattern's forward TRANSFORM as
+// three rows of its 3x3 part (a normal enters the pattern's space as
+// n'_i = n . fwd_i), the amount, the slope's delta, the pattern (0-based)
+// and the no_bump_scale flag.
+struct __align__(16) DevNormal {
+    float4 fwd[3];
+    float4 params;          // amount, delta, -5 * amount * (0.02 / delta), -
+    int4   kind;            // pattern, dont_scale_bumps, -, -
 };
 
 // Noise tables in device memory (the reference's start-up tables).
@@ -211,6 +222,7 @@ struct DeviceScene {
     int32_t         num_containers;
     // pattern pigments
     const DevPattern* patterns;
+    const DevNormal*  tnormals;       // normal perturbations (TNORMAL)
     DevNoise          noise;
     int32_t         max_trace_level;
     float           adc_bailout;

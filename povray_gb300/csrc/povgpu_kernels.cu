@@ -1050,12 +1050,10 @@ __device__ __forceinline__ float pat_triangle(float v)
     return off >= 0.5f ? 2.0f * (1.0f - off) : 2.0f * off;
 }
 
-// Compute_Pigment of a pattern pigment at world point P (pigment.cpp:395-475):
-// the pattern's inverse TRANSFORM, the pattern value with the default ramp
-// wave, the colour map's linear blend.
-__device__ float3 pattern_pigment(const DeviceScene& S, int pi, float3 P)
+// Warp_EPoint (warp.cpp:103-122): the pattern's inverse TRANSFORM, then the
+// classic turbulence (warp.cpp:553-558).
+__device__ float3 pattern_warp(const DeviceScene& S, const DevPattern& pt, float3 P)
 {
-    const DevPattern& pt = S.patterns[pi];
     float3 T;
     {
         const float4 c0 = pt.col[0], c1 = pt.col[1], c2 = pt.col[2];
@@ -1067,7 +1065,14 @@ __device__ float3 pattern_pigment(const DeviceScene& S, int pi, float3 P)
         const float3 d = pov_dturbulence(S.noise, T, pt);
         T = f3(T.x + d.x * pt.turb.x, T.y + d.y * pt.turb.y, T.z + d.z * pt.turb.z);
     }
-    const int kind = pt.kind.x, gen = pt.kind.y, n = pt.kind.z;
+    return T;
+}
+
+// Evaluate_TPat of a warped point T: the pattern's value with its frequency,
+// phase and wave (ContinuousPattern::Evaluate, pattern.cpp:354-390).
+__device__ float pattern_value(const DeviceScene& S, const DevPattern& pt, float3 T)
+{
+    const int kind = pt.kind.x, gen = pt.kind.y;
     float value;
     if (kind == POV_PATTERN_CHECKER) {
         const int c = (int)(floorf(T.x + 1.0e-10f) + floorf(T.y + 1.0e-10f) + floorf(T.z + 1.0e-10f));
@@ -1124,6 +1129,17 @@ __device__ float3 pattern_pigment(const DeviceScene& S, int pi, float3 P)
         default: break;
         }
     }
+    return value;
+}
+
+// Compute_Pigment of a pattern pigment at world point P (pigment.cpp:395-475):
+// the warped point's value through the colour map's linear blend
+// (BlendMap::Search, pattern.cpp:1068-1109).
+__device__ float3 pattern_pigment(const DeviceScene& S, int pi, float3 P)
+{
+    const DevPattern& pt = S.patterns[pi];
+    const float value = pattern_value(S, pt, pattern_warp(S, pt, P));
+    const int n = pt.kind.z;
     if (value >= pt.values[n - 1])
         return xyz(pt.colours[n - 1]);
     int ip = 0, in = 0;
@@ -1136,6 +1152,57 @@ __device__ float3 pattern_pigment(const DeviceScene& S, int pi, float3 P)
     const float wp = (pt.values[in] - value) / (pt.values[in] - pt.values[ip]), wn = 1.0f - wp;
     const float3 a = xyz(pt.colours[ip]), b = xyz(pt.colours[in]);
     return f3(a.x * wp + b.x * wn, a.y * wp + b.y * wn, a.z * wp + b.z * wn);
+}
+
+// The layer normal of a textured hit (ComputeLightedTexture,
+// trace.cpp:812-832): Perturb_Normal (normal.cpp:784-905) of the raw normal
+// N at world point P -- into the pattern's space through the forward
+// TRANSFORM (Warp_Normal, warp.cpp:563-580), displaced by bumps, dents,
+// wrinkles or the four-point slope of a continuous pattern, back through the
+// inverse (UnWarp_Normal, warp.cpp:603-620) -- and normalised.
+__device__ float3 perturb_normal(const DeviceScene& S, int ni, float3 P, float3 N)
+{
+    const DevNormal& nm = S.tnormals[ni];
+    const DevPattern& pt = S.patterns[nm.kind.x];
+    const bool scale = nm.kind.y == 0;
+    if (scale)
+        N = normalize3(N);
+    N = f3(dot3(N, xyz(nm.fwd[0])), dot3(N, xyz(nm.fwd[1])), dot3(N, xyz(nm.fwd[2])));
+    if (scale)
+        N = normalize3(N);
+    const float3 T = pattern_warp(S, pt, P);
+    const int kind = pt.kind.x;
+    const float amount = nm.params.x;
+    if (kind == POV_PATTERN_BUMPS) {            // bumps, normal.cpp:235-246
+        N = N + pov_dnoise(S.noise, T) * amount;
+    } else if (kind == POV_PATTERN_DENTS) {     // dents, normal.cpp:272-288
+        float v = pov_noise(S.noise, T, pt.kind.y);
+        v = v * v * v * amount;
+        N = N + pov_dnoise(S.noise, T) * v;
+    } else if (kind == POV_PATTERN_WRINKLES) {  // wrinkles, normal.cpp:325-346
+        float3 r = f3(0.f, 0.f, 0.f);
+        float sc = 1.0f;
+        for (int i = 0; i < 10; sc *= 2.0f, i++) {
+            const float3 d = pov_dnoise(S.noise, T * sc);
+            r = r + f3(fabsf(d.x / sc), fabsf(d.y / sc), fabsf(d.z / sc));
+        }
+        N = N + r * amount;
+    } else {                                    // slope, normal.cpp:880-902
+        // the four pyramid directions (normal.cpp:88-91)
+        const float3 pyr[4] = {f3(0.942809041f, -0.333333333f, 0.0f), f3(-0.471404521f, -0.333333333f, 0.816496581f),
+                               f3(-0.471404521f, -0.333333333f, -0.816496581f), f3(0.0f, 1.0f, 0.0f)};
+        const float delta = nm.params.y, a = nm.params.z;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const float v = pattern_value(S, pt, T + pyr[i] * delta);
+            N = N + pyr[i] * (v * a);
+        }
+    }
+    if (scale)
+        N = normalize3(N);
+    // n'_i = n . Inv[i][0..2]; col[j] holds the inverse's column j
+    N = xyz(pt.col[0]) * N.x + xyz(pt.col[1]) * N.y + xyz(pt.col[2]) * N.z;
+    return normalize3(N);
 }
 
 // aux word a secondary ray carries about the surface it starts on
@@ -1181,6 +1248,7 @@ __global__ void __launch_bounds__(128) k_shade(
         float3 col = f3(0.f, 0.f, 0.f);
         float3 p = o + d * h.t;
         float3 N = f3(0.f, 1.f, 0.f);
+        float3 raw = N;        // the raw normal facing the ray; N is the layer normal
         const DevMaterial* m = nullptr;
         int oflags = 0;
         uint2 self = make_uint2(h.prim, skip_aux(h));
@@ -1197,7 +1265,10 @@ __global__ void __launch_bounds__(128) k_shade(
                 N = N * -1.0f;
             if (dot3(N, d) > 0.0f)     // face the ray (trace.cpp:492-494)
                 N = N * -1.0f;
+            raw = N;
             pigc = m->pattern ? pattern_pigment(S, m->pattern - 1, p) : xyz(m->pigment);
+            if (m->normal)
+                N = perturb_normal(S, m->normal - 1, p, N);
             float4 em = m->emission;
             col = container ? f3(0.f, 0.f, 0.f) : f3(pigc.x * em.x, pigc.y * em.y, pigc.z * em.z);
         } else {
@@ -1222,7 +1293,9 @@ __global__ void __launch_bounds__(128) k_shade(
                 RadQuery qq;
                 float3 pg = pigc;
                 qq.p = make_float4(p.x, p.y, p.z, weight * rq_maxc);
-                qq.n = make_float4(N.x, N.y, N.z, 0.f);
+                // the cache and the gather see the raw normal (ComputeAmbient
+                // with radiosity's normal setting off, radiosity.cpp:393)
+                qq.n = make_float4(raw.x, raw.y, raw.z, 0.f);
                 float dr = m->diffuse_raw;
                 qq.factor = make_float4(pg.x * dr * thr.x, pg.y * dr * thr.y, pg.z * dr * thr.z, 0.f);
                 qq.path = path;
@@ -1329,10 +1402,20 @@ __global__ void __launch_bounds__(128) k_shade(
             if (reflec.x != 0.0f || reflec.y != 0.0f || reflec.z != 0.0f) {
                 c_refl++;
                 c_rays++;   // the TraceRay call is counted even when it bails
-                // mirror direction; with an unperturbed normal the raw-normal
-                // fix-ups of ComputeReflection never trigger
+                // mirror direction, with the raw-normal fix-ups of a
+                // perturbed normal (ComputeReflection, trace.cpp:1272-1299)
                 float n2 = -2.0f * dot3(d, N);
-                nd = normalize3(d + N * n2);
+                nd = d + N * n2;
+                float rn = dot3(nd, raw);
+                if (rn < 0.0f) {
+                    if (dot3(nd, N) < 0.0f) {   // inside the rear virtual surface
+                        rn = -2.0f * dot3(d, raw);
+                        nd = d + raw * rn;
+                    } else {                    // reflect once more about the raw normal
+                        nd = nd + raw * (-2.0f * rn);
+                    }
+                }
+                nd = normalize3(nd);
                 refl = (lvl + 1 < max_level) && (rweight >= rad.adc);
             }
         }

@@ -205,7 +205,10 @@ class Pattern:
     KINDS = {"checker": abi.POV_PATTERN_CHECKER, "gradient": abi.POV_PATTERN_GRADIENT,
              "bozo": abi.POV_PATTERN_BOZO, "spotted": abi.POV_PATTERN_BOZO, "granite": abi.POV_PATTERN_GRANITE,
              "marble": abi.POV_PATTERN_MARBLE, "wood": abi.POV_PATTERN_WOOD, "agate": abi.POV_PATTERN_AGATE,
-             "onion": abi.POV_PATTERN_ONION, "leopard": abi.POV_PATTERN_LEOPARD}
+             "onion": abi.POV_PATTERN_ONION, "leopard": abi.POV_PATTERN_LEOPARD,
+             # normal-only patterns
+             "bumps": abi.POV_PATTERN_BUMPS, "dents": abi.POV_PATTERN_DENTS,
+             "wrinkles": abi.POV_PATTERN_WRINKLES}
 
     def __init__(self, kind, colours, transforms=(), gradient=(1.0, 0.0, 0.0), noise_generator=None,
                  turbulence=None, octaves=6, omega=0.5, lambda_=2.0, wave=None, frequency=1.0, phase=0.0,
@@ -222,13 +225,18 @@ class Pattern:
         self.frequency, self.phase, self.exponent = float(frequency), float(phase), float(exponent)
         self.agate_turb = float(agate_turb)
 
-    def sdl(self):
+    def sdl(self, amount=None):
+        """The pigment body; with `amount`, the body of a normal of that
+        amount (no colour map, the amount right after the pattern)."""
         if self.kind == "checker":
             body = "checker color rgb %s color rgb %s" % (_v(self.colours[0][1]), _v(self.colours[1][1]))
         else:
             head = "gradient %s" % _v(self.gradient) if self.kind == "gradient" else self.kind
-            cmap = " ".join("[%s color rgb %s]" % (_f32(v), _v(c)) for v, c in self.colours)
-            body = "%s color_map { %s }" % (head, cmap)
+            if amount is not None:
+                body = "%s, %s" % (head, _g(amount))
+            else:
+                cmap = " ".join("[%s color rgb %s]" % (_f32(v), _v(c)) for v, c in self.colours)
+                body = "%s color_map { %s }" % (head, cmap)
             if self.kind == "agate" and self.agate_turb != 1.0:
                 body += " agate_turb %s" % _g(self.agate_turb)
             if self.wave is not None:
@@ -282,11 +290,47 @@ class Pattern:
         return d
 
 
+class Normal:
+    """A normal perturbation: `pattern` a Pattern whose kind is bumps, dents,
+    wrinkles or a continuous pattern (gradient, bozo, spotted, granite,
+    marble, wood, agate, onion, leopard; no colour map needed), `amount`
+    (0.5 by default), `accuracy` (the slope's delta, 0.02 by default) and
+    `no_bump_scale`."""
+
+    def __init__(self, pattern, amount=0.5, accuracy=0.02, no_bump_scale=False):
+        assert pattern.kind != "checker"
+        self.pattern = pattern
+        self.amount = float(amount)
+        self.accuracy = float(accuracy)
+        self.no_bump_scale = bool(no_bump_scale)
+
+    def sdl(self):
+        body = self.pattern.sdl(amount=self.amount)
+        if self.accuracy != 0.02:
+            body += " accuracy %s" % _g(self.accuracy)
+        if self.no_bump_scale:
+            body += " no_bump_scale"
+        return body
+
+    def desc(self, pattern_index):
+        d = abi.PovGpuNormal()
+        d.pattern = pattern_index
+        d.dont_scale_bumps = 1 if self.no_bump_scale else 0
+        d.amount = self.amount
+        d.delta = self.accuracy
+        fwd = self.pattern.transform().matrix
+        for i in range(4):
+            for j in range(4):
+                d.matrix[4 * i + j] = fwd[i][j]
+        return d
+
+
 class Material:
     def __init__(self, rgb, ambient=0.1, diffuse=0.6, phong=0.0, phong_size=40.0,
                  specular=0.0, roughness=0.05, reflection=0.0, brilliance=1.0,
-                 emission=0.0, transmit=0.0, pattern=None):
+                 emission=0.0, transmit=0.0, pattern=None, normal=None):
         self.pattern = pattern
+        self.normal = normal
         self.rgb = tuple(float(c) for c in rgb)
         self.transmit = float(transmit)
         self.ambient = float(ambient)
@@ -317,7 +361,8 @@ class Material:
             pig = "color rgbt <%s,%s,%s,%s>" % (_g(self.rgb[0]), _g(self.rgb[1]), _g(self.rgb[2]), _g(self.transmit))
         else:
             pig = "color rgb %s" % _v(self.rgb)
-        return "texture { pigment { %s } finish { %s } }" % (pig, fin)
+        nrm = "" if self.normal is None else " normal { %s }" % self.normal.sdl()
+        return "texture { pigment { %s }%s finish { %s } }" % (pig, nrm, fin)
 
     def desc(self):
         m = abi.PovGpuMaterial()
@@ -619,12 +664,16 @@ class Scene:
             elif o["type"] == abi.POV_OBJ_MESH:
                 d.mesh = o["mesh"]
         mats = (abi.PovGpuMaterial * max(len(self.materials), 1))()
-        pats = []
+        pats, nrms = [], []
         for i, m in enumerate(self.materials):
             mats[i] = m.desc()
             if m.pattern is not None:
                 pats.append(m.pattern.desc())
                 mats[i].pattern = len(pats)
+            if m.normal is not None:
+                pats.append(m.normal.pattern.desc())
+                nrms.append(m.normal.desc(len(pats)))
+                mats[i].normal = len(nrms)
         lights = (abi.PovGpuLight * max(len(self.lights), 1))()
         for i, l in enumerate(self.lights):
             lights[i].center[:] = list(l["pos"])
@@ -693,6 +742,10 @@ class Scene:
         desc.num_patterns = len(pats)
         desc.patterns = patterns
         keep.append(patterns)
+        normals = (abi.PovGpuNormal * max(len(nrms), 1))(*nrms)
+        desc.num_normals = len(nrms)
+        desc.normals = normals
+        keep.append(normals)
         if self.radiosity is not None:
             r = self.radiosity_settings()
             rd = desc.radiosity
@@ -1035,6 +1088,51 @@ def textured_spheres(width=320, height=240, n_spheres=12, seed=6, noise_generato
     return s
 
 
+def bumpy_spheres(width=320, height=240, n_spheres=12, seed=7, noise_generator=None):
+    """Normal perturbation: a bumpy (scale 0.5, amount 0.3), mirror-ish
+    (reflection 0.2) grey floor (plane y=-2) and `n_spheres` spheres r
+    U[0.5,1.2] in a 6x6 area (seed 7) cycling through bumps (scale 0.2),
+    dents (amount 0.8), wrinkles, granite (scale 2), marble and wood with
+    turbulence, agate, onion, leopard, a sine-wave gradient, bozo with
+    accuracy 0.05 and bumps with no_bump_scale under a rotation and a
+    non-uniform scale; every sphere has phong 0.6, specular 0.3 and
+    reflection 0.25 and a plain or bozo pigment; one point light; camera
+    (0,3,-10) looking at (0,0,2), 55 deg; max_trace_level 3."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    s = Scene("bumpy_spheres", width, height, (0.0, 3.0, -10.0), (0.0, 0.0, 2.0), 55.0, max_trace_level=3)
+    s.point_light((10.0, 15.0, -10.0))
+    ng = noise_generator
+    floor_n = Normal(Pattern("bumps", [], [("scale", (0.5, 0.5, 0.5))], noise_generator=ng), amount=0.3)
+    s.plane((0.0, 1.0, 0.0), -2.0, s.material(Material((0.6, 0.6, 0.65), reflection=0.2, normal=floor_n)))
+    normals = [
+        Normal(Pattern("bumps", [], [("scale", (0.2, 0.2, 0.2))], noise_generator=ng), amount=0.6),
+        Normal(Pattern("dents", [], [("scale", (0.3, 0.3, 0.3))], noise_generator=ng), amount=0.8),
+        Normal(Pattern("wrinkles", [], [("scale", (0.4, 0.4, 0.4))]), amount=0.5),
+        Normal(Pattern("granite", [], [("scale", (2.0, 2.0, 2.0))], noise_generator=ng), amount=0.4),
+        Normal(Pattern("marble", [], [("scale", (0.8, 0.8, 0.8))], turbulence=(0.7, 0.7, 0.7), noise_generator=ng),
+               amount=0.7),
+        Normal(Pattern("wood", [], [("scale", (0.15, 0.15, 0.15)), ("rotate", (90.0, 0.0, 0.0))],
+                       turbulence=(0.05, 0.05, 0.05)), amount=0.5),
+        Normal(Pattern("agate", [], [("scale", (0.5, 0.5, 0.5))], agate_turb=0.8, noise_generator=ng), amount=0.4),
+        Normal(Pattern("onion", [], [("scale", (0.3, 0.3, 0.3))]), amount=0.6),
+        Normal(Pattern("leopard", [], [("scale", (0.1, 0.1, 0.1))]), amount=0.5),
+        Normal(Pattern("gradient", [], gradient=(1.0, 1.0, 0.0), wave="sine", frequency=2.0, phase=0.25), amount=0.8),
+        Normal(Pattern("bozo", [], [("scale", (0.5, 0.5, 0.5))], noise_generator=ng), amount=0.6, accuracy=0.05),
+        Normal(Pattern("bumps", [], [("scale", (0.3, 0.15, 0.3)), ("rotate", (30.0, 0.0, 20.0))], noise_generator=ng),
+               amount=0.7, no_bump_scale=True),
+    ]
+    pig = Pattern("bozo", [(0.0, (0.9, 0.3, 0.1)), (0.5, (0.95, 0.9, 0.3)), (1.0, (0.1, 0.5, 0.2))],
+                  [("scale", (0.4, 0.4, 0.4))], noise_generator=ng)
+    for i in range(n_spheres):
+        c = (rng.uniform(-3.0, 3.0), rng.uniform(-1.0, 1.5), rng.uniform(0.0, 6.0))
+        r = rng.uniform(0.5, 1.2)
+        rgb = tuple(float(x) for x in rng.uniform(0.3, 1.0, size=3))
+        s.sphere(c, r, s.material(Material(rgb, phong=0.6, specular=0.3, reflection=0.25,
+                                           pattern=pig if i % 3 == 0 else None,
+                                           normal=normals[i % len(normals)])))
+    return s
+
+
 VIEW_SIZES = ((256, 256), (640, 480), (1280, 720), (1920, 1080))
 
 
@@ -1100,4 +1198,5 @@ WORKLOADS = {
     "media_spheres": media_spheres,
     "multiview_media": multiview_media,
     "textured_spheres": textured_spheres,
+    "bumpy_spheres": bumpy_spheres,
 }

@@ -61,6 +61,8 @@ def cases():
         "textured_turbulent_160x120": (scenes.textured_spheres(160, 120, n_spheres=16, turbulent=True), 2, 8.0),
         "textured_turbulent_perlin_160x120": (scenes.textured_spheres(160, 120, n_spheres=16, turbulent=True,
                                                                       noise_generator=3), 2, 8.0),
+        "bumpy_spheres_160x120": (scenes.bumpy_spheres(160, 120), 2, 8.0),
+        "bumpy_perlin_160x120": (scenes.bumpy_spheres(160, 120, noise_generator=3), 2, 8.0),
     }
 
 

@@ -6,6 +6,7 @@ import os
 import re
 import subprocess
 
+import numpy as np
 import pytest
 
 from povray_gb300 import abi, scenes
@@ -188,6 +189,50 @@ def test_pattern_validation(gpu_lib):
     assert _create(gpu_lib, desc)[0] == abi.POV_GPU_E_INVALID
 
 
+def test_normal_validation(gpu_lib):
+    """Normal perturbations: a pattern index in range whose pattern is not a
+    checker, a positive delta, a finite amount; material indices in range; a
+    pigment may not read a normal-only pattern."""
+    def fresh():
+        return scenes.bumpy_spheres(32, 24, n_spheres=4).desc()
+    desc, keep = fresh()
+    assert desc.num_normals == 5 and desc.materials[1].normal == 2
+    desc.normals[1].pattern = desc.num_patterns + 1
+    assert _create(gpu_lib, desc)[0] == abi.POV_GPU_E_INVALID
+    desc, keep = fresh()
+    desc.normals[1].delta = 0.0
+    assert _create(gpu_lib, desc)[0] == abi.POV_GPU_E_UNSUPPORTED
+    desc, keep = fresh()
+    desc.normals[1].amount = float("nan")
+    assert _create(gpu_lib, desc)[0] == abi.POV_GPU_E_UNSUPPORTED
+    desc, keep = fresh()
+    desc.patterns[desc.normals[1].pattern - 1].type = abi.POV_PATTERN_CHECKER
+    assert _create(gpu_lib, desc)[0] == abi.POV_GPU_E_UNSUPPORTED
+    desc, keep = fresh()
+    desc.materials[0].normal = desc.num_normals + 1
+    assert _create(gpu_lib, desc)[0] == abi.POV_GPU_E_INVALID
+    desc, keep = fresh()
+    desc.materials[0].pattern = desc.normals[0].pattern   # a pigment reading bumps
+    assert _create(gpu_lib, desc)[0] == abi.POV_GPU_E_UNSUPPORTED
+
+
+def test_normal_sdl_and_desc_agree():
+    """The normal's SDL carries the amount right after the pattern and its
+    modifiers after; the descriptor's forward matrix and the pattern's
+    inverse are each other's inverse."""
+    s = scenes.bumpy_spheres(32, 24, n_spheres=12)
+    sdl = s.sdl()
+    assert "normal { bumps, 0.3 scale <0.5,0.5,0.5> }" in sdl
+    assert "no_bump_scale" in sdl and "accuracy 0.05" in sdl
+    desc, keep = s.desc()
+    for i in range(desc.num_normals):
+        nm = desc.normals[i]
+        pt = desc.patterns[nm.pattern - 1]
+        fwd = np.array(nm.matrix[:]).reshape(4, 4)
+        inv = np.array(pt.inverse[:]).reshape(4, 4)
+        assert np.allclose(fwd @ inv, np.eye(4), atol=1e-12)
+
+
 def test_oracle_rejects_the_same_scenes():
     """The oracle applies the same rules as the library."""
     from oracle.pyoracle import Oracle
@@ -195,5 +240,10 @@ def test_oracle_rejects_the_same_scenes():
     Oracle(s)     # accepted
     bad = scenes.textured_spheres(32, 24, n_spheres=4)
     bad.materials[1].pattern.kind = "checker"   # a checker with a three-entry map
+    with pytest.raises(abi.PovGpuError):
+        Oracle(bad)
+    Oracle(scenes.bumpy_spheres(32, 24, n_spheres=4))
+    bad = scenes.bumpy_spheres(32, 24, n_spheres=4)
+    bad.materials[1].normal.accuracy = 0.0           # the slope's delta must be positive
     with pytest.raises(abi.PovGpuError):
         Oracle(bad)
