@@ -158,6 +158,13 @@ typedef struct PovGpuMaterial {
 #define POV_PATTERN_BUMPS    10   /* bumps, normal.cpp:235-246                       */
 #define POV_PATTERN_DENTS    11   /* dents, normal.cpp:272-288                       */
 #define POV_PATTERN_WRINKLES 12   /* wrinkles, normal.cpp:325-346                    */
+/* pigment or normal: a continuous pattern as a pigment (RipplesPattern /
+ * WavesPattern::EvaluateRaw, pattern.cpp:8163-8186 / 8593-8618), the special
+ * normal of Perturb_Normal as a normal (ripples / waves, normal.cpp:130-225);
+ * over the scene's 10 wave sources (number_of_waves 10, Initialize_Waves,
+ * noise.cpp:189-205) */
+#define POV_PATTERN_RIPPLES  13
+#define POV_PATTERN_WAVES    14
 #define POV_WAVE_RAMP     0       /* the default of most patterns                    */
 #define POV_WAVE_SINE     1
 #define POV_WAVE_TRIANGLE 2       /* the default of marble and wood                  */

@@ -1472,6 +1472,13 @@ static int g_perm[2 * (NOISE_ENTRIES + 1)];
 static V3 g_ngrad[2 * (NOISE_ENTRIES + 1)];
 static pthread_once_t g_noise_once = PTHREAD_ONCE_INIT;
 
+/* the scene's wave sources and frequencies (SceneData::numberOfWaves = 10,
+ * Initialize_Waves, noise.cpp:189-205) */
+#define NUM_WAVES 10
+static V3 g_wave_src[NUM_WAVES];
+static double g_wave_freq[NUM_WAVES];
+static void waves_init(void);
+
 static int32_t lcg_next(int32_t x) { return (int32_t)(uint32_t)((int64_t)x * 1812433253LL + 12345LL); }
 
 static void noise_init(void)
@@ -1519,6 +1526,7 @@ static void noise_init(void)
         g_perm[NOISE_ENTRIES + i] = g_perm[i];
         g_ngrad[NOISE_ENTRIES + i] = g_ngrad[i];
     }
+    waves_init();
 }
 
 static double scurve(double t) { return t * t * (3.0 - 2.0 * t); }
@@ -1646,6 +1654,18 @@ static V3 pov_dnoise(V3 P)
 #undef RIDX
 #undef INCR
     return v3(r[0], r[1], r[2]);
+}
+
+/* Initialize_Waves (noise.cpp:189-205): source i is the normalised DNoise
+ * at (i, 0, 0), its frequency the next value of the start-up sequence. */
+static void waves_init(void)
+{
+    int32_t next = -560851967;
+    for (int i = 0; i < NUM_WAVES; i++) {
+        g_wave_src[i] = vnorm(pov_dnoise(v3((double)i, 0.0, 0.0)));
+        next = lcg_next(next);
+        g_wave_freq[i] = (double)((int)(next >> 16) & 0x7FFF) * 0.000030518509476 + 0.01;
+    }
 }
 
 /* Turbulence and DTurbulence (noise.cpp:522-630): Octaves of the noise at
@@ -1800,6 +1820,30 @@ static double pattern_value(const PovGpuPattern* pt, V3 T)
             }
             break;
         }
+        case POV_PATTERN_RIPPLES: {   /* RipplesPattern::EvaluateRaw, pattern.cpp:8163-8186 */
+            const double fr = (float)pt->frequency, ph = (float)pt->phase;
+            double sc = 0.0;
+            for (int i = 0; i < NUM_WAVES; i++) {
+                double len = vlen(vsub(T, g_wave_src[i]));
+                if (len == 0.0)
+                    len = 1.0;
+                sc += cycloidal(len * fr + ph);
+            }
+            value = 0.5 * (1.0 + (sc / (double)NUM_WAVES));
+            break;
+        }
+        case POV_PATTERN_WAVES: {     /* WavesPattern::EvaluateRaw, pattern.cpp:8593-8618 */
+            const double fr = (float)pt->frequency, ph = (float)pt->phase;
+            double sc = 0.0;
+            for (int i = 0; i < NUM_WAVES; i++) {
+                double len = vlen(vsub(T, g_wave_src[i]));
+                if (len == 0.0)
+                    len = 1.0;
+                sc += cycloidal(len * fr * g_wave_freq[i] + ph) / g_wave_freq[i];
+            }
+            value = 0.2 * (2.5 + (sc / (double)NUM_WAVES));
+            break;
+        }
         case POV_PATTERN_ONION:   /* pattern.cpp:7934-7952 */
             value = fmod(sqrt(T.x * T.x + T.y * T.y + T.z * T.z), 1.0);
             break;
@@ -1905,6 +1949,23 @@ static V3 perturb_normal(const PovGpuNormal* nm, const PovGpuPattern* pt, V3 P, 
             r[2] += fabs(d.z / sc);
         }
         N = vadd(N, vmul(v3(r[0], r[1], r[2]), amount));
+        break;
+    }
+    case POV_PATTERN_RIPPLES:    /* ripples, normal.cpp:130-155 */
+    case POV_PATTERN_WAVES: {    /* waves, normal.cpp:180-206 */
+        const double fr = (float)pt->frequency, ph = (float)pt->phase;
+        for (int i = 0; i < NUM_WAVES; i++) {
+            const V3 d = vsub(T, g_wave_src[i]);
+            double len = vlen(d);
+            if (len == 0.0)
+                len = 1.0;
+            double sc;
+            if (pt->type == POV_PATTERN_RIPPLES)
+                sc = cycloidal(len * fr + ph) * amount;
+            else
+                sc = cycloidal(len * fr * g_wave_freq[i] + ph) * amount / g_wave_freq[i];
+            N = vadd(N, vmul(d, sc / (len * (double)NUM_WAVES)));
+        }
         break;
     }
     default: {  /* the slope of a continuous pattern, normal.cpp:880-902 */
@@ -3141,7 +3202,7 @@ int pov_oracle_create(const PovGpuSceneDesc* desc, PovOracle** out, int32_t* bad
         return POV_GPU_E_INVALID;
     for (int i = 0; i < desc->num_patterns; i++) {
         const PovGpuPattern* pt = &desc->patterns[i];
-        if (pt->type < POV_PATTERN_CHECKER || pt->type > POV_PATTERN_WRINKLES || pt->num_entries < 0 ||
+        if (pt->type < POV_PATTERN_CHECKER || pt->type > POV_PATTERN_WAVES || pt->num_entries < 0 ||
             pt->num_entries > POV_PATTERN_MAX_ENTRIES || pt->noise_generator < 1 || pt->noise_generator > 3 ||
             pt->wave_type < POV_WAVE_RAMP || pt->wave_type > POV_WAVE_POLY || pt->octaves < 1 || pt->octaves > 32 ||
             (pt->type == POV_PATTERN_CHECKER && pt->num_entries != 2))
@@ -3166,7 +3227,7 @@ int pov_oracle_create(const PovGpuSceneDesc* desc, PovOracle** out, int32_t* bad
             return POV_GPU_E_INVALID;
         if (m->pattern > 0) {
             const PovGpuPattern* pt = &desc->patterns[m->pattern - 1];
-            if (pt->type > POV_PATTERN_LEOPARD || pt->num_entries < 1 ||
+            if ((pt->type >= POV_PATTERN_BUMPS && pt->type <= POV_PATTERN_WRINKLES) || pt->num_entries < 1 ||
                 (pt->type == POV_PATTERN_CHECKER && pt->num_entries != 2))
                 return POV_GPU_E_UNSUPPORTED;
         }

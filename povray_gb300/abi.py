@@ -79,6 +79,8 @@ POV_PATTERN_LEOPARD = 9
 POV_PATTERN_BUMPS = 10
 POV_PATTERN_DENTS = 11
 POV_PATTERN_WRINKLES = 12
+POV_PATTERN_RIPPLES = 13
+POV_PATTERN_WAVES = 14
 POV_WAVES = {"ramp": 0, "sine": 1, "triangle": 2, "scallop": 3, "cubic": 4, "poly": 5}
 POV_PATTERN_MAX_ENTRIES = 16
 

@@ -531,7 +531,7 @@ struct PovGpuScene {
     // persistent scene data
     DevBuf nodes, refs, tri_v0, tri_e1, tri_e2, tri_global, tri_shade, tri_normal, tri_local, normals;
     DevBuf spheres, spheres64, boxes64, sphere_obj, sphere_flags, planes, plane_obj, boxes, tori, csgs, csg_children, objects,
-        materials, lights, medias, patterns, tnormals, noise_hash, noise_rtab, noise_perm, noise_grad;
+        materials, lights, medias, patterns, tnormals, noise_hash, noise_rtab, noise_perm, noise_grad, noise_waves;
     DevBuf encode_buf;     // staging of pov_gpu_encode_u8 for host outputs
     int    media_ni = 0;   // interval slots per media segment (0: no media containers)
     int    media_smax = 0;  // sample slots per interval (ends + sample-tree nodes)
@@ -574,7 +574,8 @@ struct PovGpuScene {
                          &csg_children, &objects, &materials, &lights, &blocks, &block_off, &corner_off, &qA,
                          &hits, &out, &counters, &stats, &err, &rays_in, &t64, &corners, &aa_grid, &aa_mask,
                          &aa_subdiv, &aa_xy, &cellsA, &cellsB, &spos, &sslot, &wcount, &pos_count, &medias,
-                         &encode_buf, &patterns, &tnormals, &noise_hash, &noise_rtab, &noise_perm, &noise_grad};
+                         &encode_buf, &patterns, &tnormals, &noise_hash, &noise_rtab, &noise_perm, &noise_grad,
+                         &noise_waves};
         for (DevBuf* b : all)
             b->release();
         top.release();
@@ -694,7 +695,7 @@ int validate(const PovGpuSceneDesc* d, int32_t* bad)
         return POV_GPU_E_INVALID;
     for (int i = 0; i < d->num_patterns; i++) {
         const PovGpuPattern& pt = d->patterns[i];
-        if (pt.type < POV_PATTERN_CHECKER || pt.type > POV_PATTERN_WRINKLES || pt.num_entries < 0 ||
+        if (pt.type < POV_PATTERN_CHECKER || pt.type > POV_PATTERN_WAVES || pt.num_entries < 0 ||
             pt.num_entries > POV_PATTERN_MAX_ENTRIES || pt.noise_generator < 1 || pt.noise_generator > 3 ||
             pt.wave_type < POV_WAVE_RAMP || pt.wave_type > POV_WAVE_POLY || pt.octaves < 1 || pt.octaves > 32 ||
             (pt.type == POV_PATTERN_CHECKER && pt.num_entries != 2))
@@ -718,7 +719,7 @@ int validate(const PovGpuSceneDesc* d, int32_t* bad)
             return POV_GPU_E_INVALID;
         if (m.pattern > 0) {
             const PovGpuPattern& pt = d->patterns[m.pattern - 1];
-            if (pt.type > POV_PATTERN_LEOPARD || pt.num_entries < 1 ||
+            if ((pt.type >= POV_PATTERN_BUMPS && pt.type <= POV_PATTERN_WRINKLES) || pt.num_entries < 1 ||
                 (pt.type == POV_PATTERN_CHECKER && pt.num_entries != 2))
                 return POV_GPU_E_UNSUPPORTED;
         }
@@ -968,6 +969,7 @@ struct NoiseTables {
     std::vector<float> rtab = std::vector<float>(1, 0.f);
     std::vector<int32_t> perm = std::vector<int32_t>(1, 0);
     std::vector<float4> grad = std::vector<float4>(1, make_float4(0.f, 0.f, 0.f, 0.f));
+    std::vector<float4> waves = std::vector<float4>(1, make_float4(0.f, 0.f, 0.f, 0.f));
 
     static int32_t next(int32_t x) { return (int32_t)(uint32_t)((int64_t)x * 1812433253LL + 12345LL); }
 
@@ -1017,6 +1019,58 @@ struct NoiseTables {
         for (int i = 0; i < E + 2; i++) {
             perm[E + i] = perm[i];
             grad[E + i] = grad[i];
+        }
+        // the scene's wave sources and frequencies (Initialize_Waves,
+        // noise.cpp:189-205; SceneData::numberOfWaves = 10): source i is the
+        // normalised DNoise at (i, 0, 0), in double as the reference has it
+        waves.assign(POV_NUM_WAVES, make_float4(0.f, 0.f, 0.f, 0.f));
+        r = -560851967;
+        for (int i = 0; i < POV_NUM_WAVES; i++) {
+            double d[3];
+            dnoise((double)i, 0.0, 0.0, d);
+            const double l = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+            if (l != 0.0)
+                for (double& c : d)
+                    c /= l;
+            r = next(r);
+            const double f = (double)((int)(r >> 16) & 0x7FFF) * 0.000030518509476 + 0.01;
+            waves[i] = make_float4((float)d[0], (float)d[1], (float)d[2], (float)f);
+        }
+    }
+
+    // DNoise (PortableDNoise, portablenoise.cpp:261-360) in double over the
+    // hash table and RTable: the eight lattice corners in the reference's
+    // order, three components each.
+    void dnoise(double x, double y, double z, double out[3]) const
+    {
+        const double p[3] = {x, y, z};
+        int ii[3];
+        double f[3], g[3], sc[3], tc[3];
+        for (int a = 0; a < 3; a++) {
+            const int tmp = p[a] >= 0 ? (int)p[a] : (int)(p[a] - (1 - 1.0e-10));
+            ii[a] = (tmp + 10000) & 0xFFF;
+            f[a] = p[a] - tmp;
+            g[a] = f[a] - 1;
+            sc[a] = f[a] * f[a] * (3.0 - 2.0 * f[a]);
+            tc[a] = 1 - sc[a];
+        }
+        auto h2 = [&](int a, int b) { return (int)hash[(int)hash[a] ^ b]; };
+        auto rt = [&](int m) { return (m & 1) ? kPovNoiseRTable[m >> 1] * 0.5 : kPovNoiseRTable[m >> 1]; };
+        const int h00 = h2(ii[0], ii[1]), h10 = h2(ii[0] + 1, ii[1]), h01 = h2(ii[0], ii[1] + 1),
+                  h11 = h2(ii[0] + 1, ii[1] + 1);
+        const double txty = tc[0] * tc[1], sxty = sc[0] * tc[1], txsy = tc[0] * sc[1], sxsy = sc[0] * sc[1];
+        const int hc[8] = {h00, h10, h11, h01, h01, h11, h10, h00};
+        const double sw[8] = {txty * tc[2], sxty * tc[2], sxsy * tc[2], txsy * tc[2],
+                              txsy * sc[2], sxsy * sc[2], sxty * sc[2], txty * sc[2]};
+        for (int k = 0; k < 8; k++) {
+            const int zc = k >> 2;
+            const int xo = (k == 1 || k == 2 || k == 5 || k == 6), yo = (k == 2 || k == 3 || k == 4 || k == 5);
+            int m = (hash[hc[k] ^ (ii[2] + zc)] & 0xFF) * 2;
+            const double xx = xo ? g[0] : f[0], yy = yo ? g[1] : f[1], zz = zc ? g[2] : f[2];
+            for (int c = 0; c < 3; c++, m += 8) {
+                const double v = sw[k] * (rt(m + 1) + rt(m + 2) * xx + rt(m + 4) * yy + rt(m + 6) * zz);
+                out[c] = k == 0 ? v : out[c] + v;
+            }
         }
     }
 };
@@ -1277,6 +1331,7 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
     CK(upload(sc->noise_rtab, nt.rtab));
     CK(upload(sc->noise_perm, nt.perm));
     CK(upload(sc->noise_grad, nt.grad));
+    CK(upload(sc->noise_waves, nt.waves));
 
     sc->h_sphere_obj = B.sphere_obj;
     sc->h_plane_obj = B.plane_obj;
@@ -1327,6 +1382,7 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
     S.noise.rtab = sc->noise_rtab.as<float>();
     S.noise.perm = sc->noise_perm.as<int32_t>();
     S.noise.grad = sc->noise_grad.as<float4>();
+    S.noise.waves = sc->noise_waves.as<float4>();
     S.num_containers = (int)container_obj.size();
     sc->media_ni = container_obj.empty() ? 0 : media_ni;
     S.max_trace_level = d->max_trace_level;

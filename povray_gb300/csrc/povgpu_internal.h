@@ -99,12 +99,16 @@ struct __align__(16) DevNormal {
     int4   kind;            // pattern, dont_scale_bumps, -, -
 };
 
+// The scene's number of wave sources (SceneData::numberOfWaves).
+#define POV_NUM_WAVES 10
+
 // Noise tables in device memory (the reference's start-up tables).
 struct DevNoise {
     const uint16_t* hash;   // 8192 (InitTextureTable)
     const float*    rtab;   // 534 (RTable, odd entries halved)
     const int32_t*  perm;   // 2 * (2048 + 1) (InitSolidNoise)
     const float4*   grad;   // 2 * (2048 + 1)
+    const float4*   waves;  // POV_NUM_WAVES wave sources xyz, frequency w (Initialize_Waves)
 };
 
 struct __align__(16) DevLight {

@@ -1109,6 +1109,21 @@ __device__ float pattern_value(const DeviceScene& S, const DevPattern& pt, float
             const float tv = pt.gradient.w * pov_turbulence(S.noise, T, pt, gen);
             value = 0.5f * (pat_cycloidal(1.3f * tv + 1.1f * T.z) + 1.0f);
             value = value < 0.0f ? 0.0f : powf(fminf(value, 1.0f), 0.77f);
+        } else if (kind == POV_PATTERN_RIPPLES || kind == POV_PATTERN_WAVES) {
+            // RipplesPattern / WavesPattern::EvaluateRaw (pattern.cpp:8163-8186,
+            // 8593-8618): rings about the scene's wave sources
+            const bool rip = kind == POV_PATTERN_RIPPLES;
+            float sc = 0.0f;
+            for (int i = 0; i < POV_NUM_WAVES; i++) {
+                const float4 w = __ldg(S.noise.waves + i);
+                const float3 d = T - xyz(w);
+                float len = sqrtf(dot3(d, d));
+                if (len == 0.0f)
+                    len = 1.0f;
+                sc += rip ? pat_cycloidal(len * pt.wave.x + pt.wave.y)
+                          : pat_cycloidal(len * pt.wave.x * w.w + pt.wave.y) / w.w;
+            }
+            value = rip ? 0.5f * (1.0f + sc / (float)POV_NUM_WAVES) : 0.2f * (2.5f + sc / (float)POV_NUM_WAVES);
         } else if (kind == POV_PATTERN_ONION) {    // pattern.cpp:7934-7952
             value = fmodf(sqrtf(T.x * T.x + T.y * T.y + T.z * T.z), 1.0f);
         } else {                                   // leopard, pattern.cpp:7179-7194
@@ -1187,6 +1202,19 @@ __device__ float3 perturb_normal(const DeviceScene& S, int ni, float3 P, float3 
             r = r + f3(fabsf(d.x / sc), fabsf(d.y / sc), fabsf(d.z / sc));
         }
         N = N + r * amount;
+    } else if (kind == POV_PATTERN_RIPPLES || kind == POV_PATTERN_WAVES) {
+        // ripples, waves (normal.cpp:130-155, 180-206)
+        const bool rip = kind == POV_PATTERN_RIPPLES;
+        for (int i = 0; i < POV_NUM_WAVES; i++) {
+            const float4 w = __ldg(S.noise.waves + i);
+            const float3 d = T - xyz(w);
+            float len = sqrtf(dot3(d, d));
+            if (len == 0.0f)
+                len = 1.0f;
+            const float sc = rip ? pat_cycloidal(len * pt.wave.x + pt.wave.y) * amount
+                                 : pat_cycloidal(len * pt.wave.x * w.w + pt.wave.y) * amount / w.w;
+            N = N + d * (sc / (len * (float)POV_NUM_WAVES));
+        }
     } else {                                    // slope, normal.cpp:880-902
         // the four pyramid directions (normal.cpp:88-91)
         const float3 pyr[4] = {f3(0.942809041f, -0.333333333f, 0.0f), f3(-0.471404521f, -0.333333333f, 0.816496581f),

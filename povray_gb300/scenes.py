@@ -208,7 +208,9 @@ class Pattern:
              "onion": abi.POV_PATTERN_ONION, "leopard": abi.POV_PATTERN_LEOPARD,
              # normal-only patterns
              "bumps": abi.POV_PATTERN_BUMPS, "dents": abi.POV_PATTERN_DENTS,
-             "wrinkles": abi.POV_PATTERN_WRINKLES}
+             "wrinkles": abi.POV_PATTERN_WRINKLES,
+             # pigment or normal
+             "ripples": abi.POV_PATTERN_RIPPLES, "waves": abi.POV_PATTERN_WAVES}
 
     def __init__(self, kind, colours, transforms=(), gradient=(1.0, 0.0, 0.0), noise_generator=None,
                  turbulence=None, octaves=6, omega=0.5, lambda_=2.0, wave=None, frequency=1.0, phase=0.0,
@@ -1088,7 +1090,7 @@ def textured_spheres(width=320, height=240, n_spheres=12, seed=6, noise_generato
     return s
 
 
-def bumpy_spheres(width=320, height=240, n_spheres=12, seed=7, noise_generator=None):
+def bumpy_spheres(width=320, height=240, n_spheres=12, seed=7, noise_generator=None, waves=False):
     """Normal perturbation: a bumpy (scale 0.5, amount 0.3), mirror-ish
     (reflection 0.2) grey floor (plane y=-2) and `n_spheres` spheres r
     U[0.5,1.2] in a 6x6 area (seed 7) cycling through bumps (scale 0.2),
@@ -1097,7 +1099,9 @@ def bumpy_spheres(width=320, height=240, n_spheres=12, seed=7, noise_generator=N
     accuracy 0.05 and bumps with no_bump_scale under a rotation and a
     non-uniform scale; every sphere has phong 0.6, specular 0.3 and
     reflection 0.25 and a plain or bozo pigment; one point light; camera
-    (0,3,-10) looking at (0,0,2), 55 deg; max_trace_level 3."""
+    (0,3,-10) looking at (0,0,2), 55 deg; max_trace_level 3.  With `waves`
+    the spheres alternate ripples and waves normals (frequency, phase,
+    scale) over ripples and waves pigments."""
     rng = np.random.Generator(np.random.PCG64(seed))
     s = Scene("bumpy_spheres", width, height, (0.0, 3.0, -10.0), (0.0, 0.0, 2.0), 55.0, max_trace_level=3)
     s.point_light((10.0, 15.0, -10.0))
@@ -1123,6 +1127,19 @@ def bumpy_spheres(width=320, height=240, n_spheres=12, seed=7, noise_generator=N
     ]
     pig = Pattern("bozo", [(0.0, (0.9, 0.3, 0.1)), (0.5, (0.95, 0.9, 0.3)), (1.0, (0.1, 0.5, 0.2))],
                   [("scale", (0.4, 0.4, 0.4))], noise_generator=ng)
+    if waves:
+        normals = [
+            Normal(Pattern("ripples", [], [("scale", (0.5, 0.5, 0.5))], frequency=3.0), amount=0.8),
+            Normal(Pattern("waves", [], [("scale", (0.3, 0.3, 0.3)), ("translate", (0.2, 0.0, 0.1))],
+                           frequency=2.0, phase=0.3), amount=0.6),
+            Normal(Pattern("ripples", [], [("rotate", (0.0, 30.0, 0.0))], phase=0.5), amount=1.2),
+            Normal(Pattern("waves", [], [("scale", (0.6, 0.6, 0.6))]), amount=0.9, no_bump_scale=True),
+        ]
+        pig = Pattern("ripples", [(0.0, (0.1, 0.2, 0.6)), (1.0, (0.9, 0.95, 1.0))], [("scale", (0.3, 0.3, 0.3))],
+                      frequency=2.0)
+        floor_pig = Pattern("waves", [(0.0, (0.2, 0.4, 0.3)), (0.5, (0.8, 0.8, 0.6)), (1.0, (0.3, 0.2, 0.1))],
+                            [("scale", (0.7, 0.7, 0.7))], frequency=1.5, phase=0.2)
+        s.materials[0].pattern = floor_pig
     for i in range(n_spheres):
         c = (rng.uniform(-3.0, 3.0), rng.uniform(-1.0, 1.5), rng.uniform(0.0, 6.0))
         r = rng.uniform(0.5, 1.2)

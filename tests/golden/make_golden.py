@@ -63,6 +63,7 @@ def cases():
                                                                       noise_generator=3), 2, 8.0),
         "bumpy_spheres_160x120": (scenes.bumpy_spheres(160, 120), 2, 8.0),
         "bumpy_perlin_160x120": (scenes.bumpy_spheres(160, 120, noise_generator=3), 2, 8.0),
+        "bumpy_waves_160x120": (scenes.bumpy_spheres(160, 120, waves=True), 2, 8.0),
     }
 
 
