@@ -165,6 +165,14 @@ typedef struct PovGpuMaterial {
  * noise.cpp:189-205) */
 #define POV_PATTERN_RIPPLES  13
 #define POV_PATTERN_WAVES    14
+/* geometric patterns (pattern.cpp; the last four through CLIP_DENSITY,
+ * pattern.cpp:85); dents and wrinkles are pigments too (DentsPattern /
+ * WrinklesPattern::EvaluateRaw, pattern.cpp:6307-6313 / 8720-8770) */
+#define POV_PATTERN_RADIAL      15   /* RadialPattern::EvaluateRaw, pattern.cpp:8115   */
+#define POV_PATTERN_PLANAR      16   /* PlanarPattern::EvaluateRaw, pattern.cpp:8024   */
+#define POV_PATTERN_SPHERICAL   17   /* SphericalPattern::EvaluateRaw, pattern.cpp:8551 */
+#define POV_PATTERN_CYLINDRICAL 18   /* CylindricalPattern::EvaluateRaw, pattern.cpp:6025 */
+#define POV_PATTERN_BOXED       19   /* BoxedPattern::EvaluateRaw, pattern.cpp:5454    */
 #define POV_WAVE_RAMP     0       /* the default of most patterns                    */
 #define POV_WAVE_SINE     1
 #define POV_WAVE_TRIANGLE 2       /* the default of marble and wood                  */

@@ -1715,6 +1715,7 @@ static V3 pov_dturbulence(V3 P, const PovGpuPattern* t)
 
 /* cycloidal (texture.cpp:98-108) and Triangle_Wave (texture.cpp:138-156). */
 #define TWO_M_PI 6.283185307179586476925286766560
+#define M_PI_D 3.141592653589793238462643383280
 static double cycloidal(double v)
 {
     if (v >= 0.0)
@@ -1844,6 +1845,54 @@ static double pattern_value(const PovGpuPattern* pt, V3 T)
             value = 0.2 * (2.5 + (sc / (double)NUM_WAVES));
             break;
         }
+        case POV_PATTERN_DENTS: {   /* DentsPattern::EvaluateRaw, pattern.cpp:6307-6313 */
+            const double nz = pov_noise(T, gen);
+            value = nz * nz * nz;
+            break;
+        }
+        case POV_PATTERN_WRINKLES: {   /* WrinklesPattern::EvaluateRaw, pattern.cpp:8720-8770 */
+            double lambda = 2.0, omega = 0.5;
+            if (gen == 1) {
+                value = pov_noise(T, 1);
+            } else {
+                const double nz = pov_noise(T, gen) * 2.0 - 0.5;
+                value = fmin(fmax(nz, 0.0), 1.0);
+            }
+            for (int i = 1; i < 10; i++) {
+                const V3 q = vmul(T, lambda);
+                if (gen == 1) {
+                    value += omega * pov_noise(q, 1);
+                } else {
+                    const double nz = pov_noise(q, gen) * 2.0 - 0.5;
+                    value += omega * fmin(fmax(nz, 0.0), 1.0);
+                }
+                lambda *= 2.0;
+                omega *= 0.5;
+            }
+            value = value / 2.0;
+            break;
+        }
+        case POV_PATTERN_RADIAL:   /* pattern.cpp:8115-8128 */
+            if (fabs(T.x) < 0.001 && fabs(T.z) < 0.001)
+                value = 0.25;
+            else
+                value = 0.25 + (atan2(T.x, T.z) + M_PI_D) / TWO_M_PI;
+            break;
+        case POV_PATTERN_PLANAR:        /* pattern.cpp:8024-8030 */
+        case POV_PATTERN_SPHERICAL:     /* pattern.cpp:8551-8558 */
+        case POV_PATTERN_CYLINDRICAL:   /* pattern.cpp:6025-6032 */
+        case POV_PATTERN_BOXED:         /* pattern.cpp:5454-5461 */
+            if (pt->type == POV_PATTERN_PLANAR)
+                value = fabs(T.y);
+            else if (pt->type == POV_PATTERN_SPHERICAL)
+                value = vlen(T);
+            else if (pt->type == POV_PATTERN_CYLINDRICAL)
+                value = sqrt(T.x * T.x + T.z * T.z);
+            else
+                value = fmax(fabs(T.x), fmax(fabs(T.y), fabs(T.z)));
+            /* CLIP_DENSITY (pattern.cpp:85) */
+            value = value < 0.0 ? 1.0 : (value > 1.0 ? 0.0 : 1.0 - value);
+            break;
         case POV_PATTERN_ONION:   /* pattern.cpp:7934-7952 */
             value = fmod(sqrt(T.x * T.x + T.y * T.y + T.z * T.z), 1.0);
             break;
@@ -3202,7 +3251,7 @@ int pov_oracle_create(const PovGpuSceneDesc* desc, PovOracle** out, int32_t* bad
         return POV_GPU_E_INVALID;
     for (int i = 0; i < desc->num_patterns; i++) {
         const PovGpuPattern* pt = &desc->patterns[i];
-        if (pt->type < POV_PATTERN_CHECKER || pt->type > POV_PATTERN_WAVES || pt->num_entries < 0 ||
+        if (pt->type < POV_PATTERN_CHECKER || pt->type > POV_PATTERN_BOXED || pt->num_entries < 0 ||
             pt->num_entries > POV_PATTERN_MAX_ENTRIES || pt->noise_generator < 1 || pt->noise_generator > 3 ||
             pt->wave_type < POV_WAVE_RAMP || pt->wave_type > POV_WAVE_POLY || pt->octaves < 1 || pt->octaves > 32 ||
             (pt->type == POV_PATTERN_CHECKER && pt->num_entries != 2))
@@ -3227,7 +3276,7 @@ int pov_oracle_create(const PovGpuSceneDesc* desc, PovOracle** out, int32_t* bad
             return POV_GPU_E_INVALID;
         if (m->pattern > 0) {
             const PovGpuPattern* pt = &desc->patterns[m->pattern - 1];
-            if ((pt->type >= POV_PATTERN_BUMPS && pt->type <= POV_PATTERN_WRINKLES) || pt->num_entries < 1 ||
+            if (pt->type == POV_PATTERN_BUMPS || pt->num_entries < 1 ||
                 (pt->type == POV_PATTERN_CHECKER && pt->num_entries != 2))
                 return POV_GPU_E_UNSUPPORTED;
         }

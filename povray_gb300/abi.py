@@ -81,6 +81,11 @@ POV_PATTERN_DENTS = 11
 POV_PATTERN_WRINKLES = 12
 POV_PATTERN_RIPPLES = 13
 POV_PATTERN_WAVES = 14
+POV_PATTERN_RADIAL = 15
+POV_PATTERN_PLANAR = 16
+POV_PATTERN_SPHERICAL = 17
+POV_PATTERN_CYLINDRICAL = 18
+POV_PATTERN_BOXED = 19
 POV_WAVES = {"ramp": 0, "sine": 1, "triangle": 2, "scallop": 3, "cubic": 4, "poly": 5}
 POV_PATTERN_MAX_ENTRIES = 16
 

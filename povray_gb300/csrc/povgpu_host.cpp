@@ -695,7 +695,7 @@ int validate(const PovGpuSceneDesc* d, int32_t* bad)
         return POV_GPU_E_INVALID;
     for (int i = 0; i < d->num_patterns; i++) {
         const PovGpuPattern& pt = d->patterns[i];
-        if (pt.type < POV_PATTERN_CHECKER || pt.type > POV_PATTERN_WAVES || pt.num_entries < 0 ||
+        if (pt.type < POV_PATTERN_CHECKER || pt.type > POV_PATTERN_BOXED || pt.num_entries < 0 ||
             pt.num_entries > POV_PATTERN_MAX_ENTRIES || pt.noise_generator < 1 || pt.noise_generator > 3 ||
             pt.wave_type < POV_WAVE_RAMP || pt.wave_type > POV_WAVE_POLY || pt.octaves < 1 || pt.octaves > 32 ||
             (pt.type == POV_PATTERN_CHECKER && pt.num_entries != 2))
@@ -719,7 +719,7 @@ int validate(const PovGpuSceneDesc* d, int32_t* bad)
             return POV_GPU_E_INVALID;
         if (m.pattern > 0) {
             const PovGpuPattern& pt = d->patterns[m.pattern - 1];
-            if ((pt.type >= POV_PATTERN_BUMPS && pt.type <= POV_PATTERN_WRINKLES) || pt.num_entries < 1 ||
+            if (pt.type == POV_PATTERN_BUMPS || pt.num_entries < 1 ||
                 (pt.type == POV_PATTERN_CHECKER && pt.num_entries != 2))
                 return POV_GPU_E_UNSUPPORTED;
         }

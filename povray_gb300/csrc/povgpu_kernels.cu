@@ -1124,6 +1124,33 @@ __device__ float pattern_value(const DeviceScene& S, const DevPattern& pt, float
                           : pat_cycloidal(len * pt.wave.x * w.w + pt.wave.y) / w.w;
             }
             value = rip ? 0.5f * (1.0f + sc / (float)POV_NUM_WAVES) : 0.2f * (2.5f + sc / (float)POV_NUM_WAVES);
+        } else if (kind == POV_PATTERN_DENTS) {    // pattern.cpp:6307-6313
+            const float nz = pov_noise(S.noise, T, gen);
+            value = nz * nz * nz;
+        } else if (kind == POV_PATTERN_WRINKLES) { // pattern.cpp:8720-8770
+            float lambda = 2.0f, omega = 0.5f;
+            value = gen == 1 ? pov_noise(S.noise, T, 1)
+                             : fminf(fmaxf(pov_noise(S.noise, T, gen) * 2.0f - 0.5f, 0.0f), 1.0f);
+            for (int i = 1; i < 10; i++) {
+                const float3 q = T * lambda;
+                value += omega * (gen == 1 ? pov_noise(S.noise, q, 1)
+                                           : fminf(fmaxf(pov_noise(S.noise, q, gen) * 2.0f - 0.5f, 0.0f), 1.0f));
+                lambda *= 2.0f;
+                omega *= 0.5f;
+            }
+            value = value / 2.0f;
+        } else if (kind == POV_PATTERN_RADIAL) {   // pattern.cpp:8115-8128
+            value = (fabsf(T.x) < 0.001f && fabsf(T.z) < 0.001f)
+                        ? 0.25f
+                        : 0.25f + (atan2f(T.x, T.z) + 3.14159265358979f) / 6.2831853071795864769f;
+        } else if (kind >= POV_PATTERN_PLANAR && kind <= POV_PATTERN_BOXED) {
+            // planar, spherical, cylindrical, boxed (pattern.cpp:8024, 8551,
+            // 6025, 5454) through CLIP_DENSITY (pattern.cpp:85)
+            value = kind == POV_PATTERN_PLANAR      ? fabsf(T.y)
+                    : kind == POV_PATTERN_SPHERICAL ? sqrtf(dot3(T, T))
+                    : kind == POV_PATTERN_CYLINDRICAL ? sqrtf(T.x * T.x + T.z * T.z)
+                                                      : fmaxf(fabsf(T.x), fmaxf(fabsf(T.y), fabsf(T.z)));
+            value = value < 0.0f ? 1.0f : (value > 1.0f ? 0.0f : 1.0f - value);
         } else if (kind == POV_PATTERN_ONION) {    // pattern.cpp:7934-7952
             value = fmodf(sqrtf(T.x * T.x + T.y * T.y + T.z * T.z), 1.0f);
         } else {                                   // leopard, pattern.cpp:7179-7194

@@ -210,7 +210,10 @@ class Pattern:
              "bumps": abi.POV_PATTERN_BUMPS, "dents": abi.POV_PATTERN_DENTS,
              "wrinkles": abi.POV_PATTERN_WRINKLES,
              # pigment or normal
-             "ripples": abi.POV_PATTERN_RIPPLES, "waves": abi.POV_PATTERN_WAVES}
+             "ripples": abi.POV_PATTERN_RIPPLES, "waves": abi.POV_PATTERN_WAVES,
+             "radial": abi.POV_PATTERN_RADIAL, "planar": abi.POV_PATTERN_PLANAR,
+             "spherical": abi.POV_PATTERN_SPHERICAL, "cylindrical": abi.POV_PATTERN_CYLINDRICAL,
+             "boxed": abi.POV_PATTERN_BOXED}
 
     def __init__(self, kind, colours, transforms=(), gradient=(1.0, 0.0, 0.0), noise_generator=None,
                  turbulence=None, octaves=6, omega=0.5, lambda_=2.0, wave=None, frequency=1.0, phase=0.0,
@@ -1150,6 +1153,42 @@ def bumpy_spheres(width=320, height=240, n_spheres=12, seed=7, noise_generator=N
     return s
 
 
+def shaped_spheres(width=320, height=240, n_spheres=12, seed=8, noise_generator=None):
+    """Geometric and noise pigments: a boxed-pattern floor (plane y=-2,
+    scale 3) and `n_spheres` spheres r U[0.5,1.2] in a 6x6 area (seed 8)
+    cycling through radial (frequency 6), planar, spherical (scale 1.2,
+    centred on the sphere), cylindrical, boxed, dents and wrinkles pigments,
+    half of them with a radial or spherical slope normal; phong 0.4; one
+    point light; camera (0,3,-10) looking at (0,0,2), 55 deg;
+    max_trace_level 2."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    s = Scene("shaped_spheres", width, height, (0.0, 3.0, -10.0), (0.0, 0.0, 2.0), 55.0, max_trace_level=2)
+    s.point_light((10.0, 15.0, -10.0))
+    ng = noise_generator
+    warm = [(0.0, (0.9, 0.85, 0.7)), (0.6, (0.6, 0.3, 0.15)), (1.0, (0.2, 0.1, 0.05))]
+    cool = [(0.0, (0.05, 0.1, 0.3)), (0.5, (0.5, 0.7, 0.9)), (1.0, (1.0, 1.0, 1.0))]
+    floor = Pattern("boxed", cool, [("scale", (3.0, 3.0, 3.0))], wave="sine", frequency=2.0)
+    s.plane((0.0, 1.0, 0.0), -2.0, s.material(Material((1.0, 1.0, 1.0), pattern=floor)))
+    for i in range(n_spheres):
+        c = (rng.uniform(-3.0, 3.0), rng.uniform(-1.0, 1.5), rng.uniform(0.0, 6.0))
+        r = rng.uniform(0.5, 1.2)
+        at = [("translate", c)]
+        kinds = [
+            Pattern("radial", warm, [("rotate", (90.0, 0.0, 0.0))] + at, frequency=6.0),
+            Pattern("planar", cool, [("scale", (r, r, r))] + at),
+            Pattern("spherical", warm, [("scale", (1.2 * r, 1.2 * r, 1.2 * r))] + at),
+            Pattern("cylindrical", cool, [("scale", (r, r, r))] + at, wave="scallop"),
+            Pattern("boxed", warm, [("scale", (0.8 * r, 0.8 * r, 0.8 * r))] + at, wave="cubic"),
+            Pattern("dents", cool, [("scale", (0.3, 0.3, 0.3))], noise_generator=ng),
+            Pattern("wrinkles", warm, [("scale", (0.5, 0.5, 0.5))], noise_generator=ng),
+        ]
+        nrm = None
+        if i % 2 == 1:
+            nrm = Normal(Pattern("radial" if i % 4 == 1 else "spherical", [], at, frequency=8.0), amount=0.6)
+        s.sphere(c, r, s.material(Material((1.0, 1.0, 1.0), phong=0.4, pattern=kinds[i % len(kinds)], normal=nrm)))
+    return s
+
+
 VIEW_SIZES = ((256, 256), (640, 480), (1280, 720), (1920, 1080))
 
 
@@ -1216,4 +1255,5 @@ WORKLOADS = {
     "multiview_media": multiview_media,
     "textured_spheres": textured_spheres,
     "bumpy_spheres": bumpy_spheres,
+    "shaped_spheres": shaped_spheres,
 }
