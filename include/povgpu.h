@@ -173,6 +173,11 @@ typedef struct PovGpuMaterial {
 #define POV_PATTERN_SPHERICAL   17   /* SphericalPattern::EvaluateRaw, pattern.cpp:8551 */
 #define POV_PATTERN_CYLINDRICAL 18   /* CylindricalPattern::EvaluateRaw, pattern.cpp:6025 */
 #define POV_PATTERN_BOXED       19   /* BoxedPattern::EvaluateRaw, pattern.cpp:5454    */
+/* discrete patterns with a colour list (pigments only, like checker; no
+ * wave): 4, 6 and 6 entries at the values 0..n-1 */
+#define POV_PATTERN_SQUARE      20   /* SquarePattern::Evaluate, pattern.cpp:6740      */
+#define POV_PATTERN_TRIANGULAR  21   /* TriangularPattern::Evaluate, pattern.cpp:6799  */
+#define POV_PATTERN_CUBIC       22   /* CubicPattern::Evaluate, pattern.cpp:6699       */
 #define POV_WAVE_RAMP     0       /* the default of most patterns                    */
 #define POV_WAVE_SINE     1
 #define POV_WAVE_TRIANGLE 2       /* the default of marble and wood                  */

@@ -1768,6 +1768,38 @@ static double pattern_value(const PovGpuPattern* pt, V3 T)
     if (pt->type == POV_PATTERN_CHECKER) {   /* CheckerPattern::Evaluate, pattern.cpp:5691-5706 */
         int c = (int)(floor(T.x + EPSILON) + floor(T.y + EPSILON) + floor(T.z + EPSILON));
         value = (c & 1) ? 1.0 : 0.0;
+    } else if (pt->type == POV_PATTERN_SQUARE) {   /* pattern.cpp:6740-6770 */
+        const int vx = (int)floor(T.x), vz = (int)floor(T.z);
+        value = (vx & 1) ? ((vz & 1) ? 2.0 : 3.0) : ((vz & 1) ? 1.0 : 0.0);
+    } else if (pt->type == POV_PATTERN_CUBIC) {    /* pattern.cpp:6699-6714 */
+        const double x = T.x, y = T.y, z = T.z, ax = fabs(x), ay = fabs(y), az = fabs(z);
+        if (x >= 0 && x >= ay && x >= az) value = 0.0;
+        else if (y >= 0 && y >= ax && y >= az) value = 1.0;
+        else if (z >= 0 && z >= ax && z >= ay) value = 2.0;
+        else if (x < 0 && x <= -ay && x <= -az) value = 3.0;
+        else if (y < 0 && y <= -ax && y <= -az) value = 4.0;
+        else value = 5.0;
+    } else if (pt->type == POV_PATTERN_TRIANGULAR) {   /* pattern.cpp:6799-6866 */
+        const double SQ3 = 1.7320508075688772935274463415059, SQ3_2 = 0.86602540378443864676372317075294;
+        double xs = T.x - 3.0 * floor(T.x / 3.0);
+        double zs = T.z - SQ3 * floor(T.z / SQ3);
+        const int a = (int)floor(xs);
+        xs -= a;
+        const int b = zs < SQ3_2 ? 0 : 1;
+        if (b)
+            zs = SQ3 - zs;
+        const double k = 1.0 - xs;
+        double ans = 1.0;
+        if (xs != 0.0 && k != 0.0) {
+            const double s1 = zs / xs, s2 = zs / k;
+            const int c = (s1 < SQ3 ? 1 : 0) + (s2 < SQ3 ? 2 : 0);
+            ans = c == 3 ? 0.0 : (c == 2 ? 1.0 : 3.0);
+        }
+        const int mask = (int)ans;
+        ans = (mask & 1) ? fmod(ans + 2.0 * a, 6.0) : fmod(6.0 + ans - 2.0 * a, 6.0);
+        if (b)
+            ans = 5.0 - ans;
+        value = ans;
     } else {
         switch (pt->type) {
         case POV_PATTERN_GRADIENT:   /* pattern.cpp:6386-6393 */
@@ -3251,10 +3283,12 @@ int pov_oracle_create(const PovGpuSceneDesc* desc, PovOracle** out, int32_t* bad
         return POV_GPU_E_INVALID;
     for (int i = 0; i < desc->num_patterns; i++) {
         const PovGpuPattern* pt = &desc->patterns[i];
-        if (pt->type < POV_PATTERN_CHECKER || pt->type > POV_PATTERN_BOXED || pt->num_entries < 0 ||
+        if (pt->type < POV_PATTERN_CHECKER || pt->type > POV_PATTERN_CUBIC || pt->num_entries < 0 ||
             pt->num_entries > POV_PATTERN_MAX_ENTRIES || pt->noise_generator < 1 || pt->noise_generator > 3 ||
             pt->wave_type < POV_WAVE_RAMP || pt->wave_type > POV_WAVE_POLY || pt->octaves < 1 || pt->octaves > 32 ||
-            (pt->type == POV_PATTERN_CHECKER && pt->num_entries != 2))
+            (pt->type == POV_PATTERN_CHECKER && pt->num_entries != 2) ||
+            (pt->type == POV_PATTERN_SQUARE && pt->num_entries != 4) ||
+            ((pt->type == POV_PATTERN_TRIANGULAR || pt->type == POV_PATTERN_CUBIC) && pt->num_entries != 6))
             return POV_GPU_E_UNSUPPORTED;
         for (int k = 1; k < pt->num_entries; k++)
             if (pt->values[k] < pt->values[k - 1])
@@ -3266,7 +3300,8 @@ int pov_oracle_create(const PovGpuSceneDesc* desc, PovOracle** out, int32_t* bad
         const PovGpuNormal* nm = &desc->normals[i];
         if (nm->pattern < 1 || nm->pattern > desc->num_patterns)
             return POV_GPU_E_INVALID;
-        if (desc->patterns[nm->pattern - 1].type == POV_PATTERN_CHECKER || !(nm->delta > 0.0f) ||
+        const int nt = desc->patterns[nm->pattern - 1].type;
+        if (nt == POV_PATTERN_CHECKER || nt >= POV_PATTERN_SQUARE || !(nm->delta > 0.0f) ||
             !isfinite(nm->amount))
             return POV_GPU_E_UNSUPPORTED;
     }

@@ -695,10 +695,12 @@ int validate(const PovGpuSceneDesc* d, int32_t* bad)
         return POV_GPU_E_INVALID;
     for (int i = 0; i < d->num_patterns; i++) {
         const PovGpuPattern& pt = d->patterns[i];
-        if (pt.type < POV_PATTERN_CHECKER || pt.type > POV_PATTERN_BOXED || pt.num_entries < 0 ||
+        if (pt.type < POV_PATTERN_CHECKER || pt.type > POV_PATTERN_CUBIC || pt.num_entries < 0 ||
             pt.num_entries > POV_PATTERN_MAX_ENTRIES || pt.noise_generator < 1 || pt.noise_generator > 3 ||
             pt.wave_type < POV_WAVE_RAMP || pt.wave_type > POV_WAVE_POLY || pt.octaves < 1 || pt.octaves > 32 ||
-            (pt.type == POV_PATTERN_CHECKER && pt.num_entries != 2))
+            (pt.type == POV_PATTERN_CHECKER && pt.num_entries != 2) ||
+            (pt.type == POV_PATTERN_SQUARE && pt.num_entries != 4) ||
+            ((pt.type == POV_PATTERN_TRIANGULAR || pt.type == POV_PATTERN_CUBIC) && pt.num_entries != 6))
             return POV_GPU_E_UNSUPPORTED;
         for (int k = 1; k < pt.num_entries; k++)
             if (pt.values[k] < pt.values[k - 1])
@@ -710,7 +712,8 @@ int validate(const PovGpuSceneDesc* d, int32_t* bad)
         const PovGpuNormal& nm = d->normals[i];
         if (nm.pattern < 1 || nm.pattern > d->num_patterns)
             return POV_GPU_E_INVALID;
-        if (d->patterns[nm.pattern - 1].type == POV_PATTERN_CHECKER || !(nm.delta > 0.0f) || !std::isfinite(nm.amount))
+        const int nt = d->patterns[nm.pattern - 1].type;
+        if (nt == POV_PATTERN_CHECKER || nt >= POV_PATTERN_SQUARE || !(nm.delta > 0.0f) || !std::isfinite(nm.amount))
             return POV_GPU_E_UNSUPPORTED;
     }
     for (int i = 0; i < d->num_materials; i++) {

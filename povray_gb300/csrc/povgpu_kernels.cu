@@ -1077,6 +1077,35 @@ __device__ float pattern_value(const DeviceScene& S, const DevPattern& pt, float
     if (kind == POV_PATTERN_CHECKER) {
         const int c = (int)(floorf(T.x + 1.0e-10f) + floorf(T.y + 1.0e-10f) + floorf(T.z + 1.0e-10f));
         value = (c & 1) ? 1.0f : 0.0f;
+    } else if (kind == POV_PATTERN_SQUARE) {       // pattern.cpp:6740-6770
+        const int vx = (int)floorf(T.x), vz = (int)floorf(T.z);
+        value = (vx & 1) ? ((vz & 1) ? 2.0f : 3.0f) : ((vz & 1) ? 1.0f : 0.0f);
+    } else if (kind == POV_PATTERN_CUBIC) {        // pattern.cpp:6699-6714
+        const float x = T.x, y = T.y, z = T.z, ax = fabsf(x), ay = fabsf(y), az = fabsf(z);
+        value = (x >= 0.f && x >= ay && x >= az)     ? 0.0f
+                : (y >= 0.f && y >= ax && y >= az)   ? 1.0f
+                : (z >= 0.f && z >= ax && z >= ay)   ? 2.0f
+                : (x < 0.f && x <= -ay && x <= -az)  ? 3.0f
+                : (y < 0.f && y <= -ax && y <= -az)  ? 4.0f
+                                                     : 5.0f;
+    } else if (kind == POV_PATTERN_TRIANGULAR) {   // pattern.cpp:6799-6866
+        const float SQ3 = 1.7320508075688772935f, SQ3_2 = 0.86602540378443864676f;
+        float xs = T.x - 3.0f * floorf(T.x / 3.0f);
+        float zs = T.z - SQ3 * floorf(T.z / SQ3);
+        const int a = (int)floorf(xs);
+        xs -= (float)a;
+        const int b = zs < SQ3_2 ? 0 : 1;
+        if (b)
+            zs = SQ3 - zs;
+        const float k = 1.0f - xs;
+        float ans = 1.0f;
+        if (xs != 0.0f && k != 0.0f) {
+            const int c = (zs / xs < SQ3 ? 1 : 0) + (zs / k < SQ3 ? 2 : 0);
+            ans = c == 3 ? 0.0f : (c == 2 ? 1.0f : 3.0f);
+        }
+        const int mask = (int)ans;
+        ans = (mask & 1) ? fmodf(ans + 2.0f * (float)a, 6.0f) : fmodf(6.0f + ans - 2.0f * (float)a, 6.0f);
+        value = b ? 5.0f - ans : ans;
     } else {
         if (kind == POV_PATTERN_GRADIENT) {
             value = T.x * pt.gradient.x + T.y * pt.gradient.y + T.z * pt.gradient.z;

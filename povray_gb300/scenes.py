@@ -213,7 +213,11 @@ class Pattern:
              "ripples": abi.POV_PATTERN_RIPPLES, "waves": abi.POV_PATTERN_WAVES,
              "radial": abi.POV_PATTERN_RADIAL, "planar": abi.POV_PATTERN_PLANAR,
              "spherical": abi.POV_PATTERN_SPHERICAL, "cylindrical": abi.POV_PATTERN_CYLINDRICAL,
-             "boxed": abi.POV_PATTERN_BOXED}
+             "boxed": abi.POV_PATTERN_BOXED,
+             # discrete, with a colour list of 4, 6 and 6 entries at 0..n-1
+             "square": abi.POV_PATTERN_SQUARE, "triangular": abi.POV_PATTERN_TRIANGULAR,
+             "cubic": abi.POV_PATTERN_CUBIC}
+    DISCRETE = ("checker", "square", "triangular", "cubic")
 
     def __init__(self, kind, colours, transforms=(), gradient=(1.0, 0.0, 0.0), noise_generator=None,
                  turbulence=None, octaves=6, omega=0.5, lambda_=2.0, wave=None, frequency=1.0, phase=0.0,
@@ -233,8 +237,8 @@ class Pattern:
     def sdl(self, amount=None):
         """The pigment body; with `amount`, the body of a normal of that
         amount (no colour map, the amount right after the pattern)."""
-        if self.kind == "checker":
-            body = "checker color rgb %s color rgb %s" % (_v(self.colours[0][1]), _v(self.colours[1][1]))
+        if self.kind in self.DISCRETE:
+            body = self.kind + "".join(" color rgb %s" % _v(c) for _, c in self.colours)
         else:
             head = "gradient %s" % _v(self.gradient) if self.kind == "gradient" else self.kind
             if amount is not None:
@@ -303,7 +307,7 @@ class Normal:
     `no_bump_scale`."""
 
     def __init__(self, pattern, amount=0.5, accuracy=0.02, no_bump_scale=False):
-        assert pattern.kind != "checker"
+        assert pattern.kind not in Pattern.DISCRETE
         self.pattern = pattern
         self.amount = float(amount)
         self.accuracy = float(accuracy)
@@ -1157,7 +1161,8 @@ def shaped_spheres(width=320, height=240, n_spheres=12, seed=8, noise_generator=
     """Geometric and noise pigments: a boxed-pattern floor (plane y=-2,
     scale 3) and `n_spheres` spheres r U[0.5,1.2] in a 6x6 area (seed 8)
     cycling through radial (frequency 6), planar, spherical (scale 1.2,
-    centred on the sphere), cylindrical, boxed, dents and wrinkles pigments,
+    centred on the sphere), cylindrical, boxed, dents, wrinkles, square,
+    triangular and cubic (centred on the sphere) pigments,
     half of them with a radial or spherical slope normal; phong 0.4; one
     point light; camera (0,3,-10) looking at (0,0,2), 55 deg;
     max_trace_level 2."""
@@ -1181,6 +1186,11 @@ def shaped_spheres(width=320, height=240, n_spheres=12, seed=8, noise_generator=
             Pattern("boxed", warm, [("scale", (0.8 * r, 0.8 * r, 0.8 * r))] + at, wave="cubic"),
             Pattern("dents", cool, [("scale", (0.3, 0.3, 0.3))], noise_generator=ng),
             Pattern("wrinkles", warm, [("scale", (0.5, 0.5, 0.5))], noise_generator=ng),
+            Pattern("square", [(k, rgb) for k, rgb in enumerate(((0.9, 0.2, 0.2), (0.2, 0.9, 0.2), (0.2, 0.2, 0.9),
+                                                                  (0.9, 0.9, 0.2)))], [("scale", (0.3, 0.3, 0.3))]),
+            Pattern("triangular", [(k, (0.15 * k + 0.1, 0.9 - 0.12 * k, 0.5)) for k in range(6)],
+                    [("scale", (0.25, 0.25, 0.25)), ("rotate", (90.0, 0.0, 0.0))]),
+            Pattern("cubic", [(k, (0.5, 0.15 * k + 0.1, 0.9 - 0.12 * k)) for k in range(6)], at),
         ]
         nrm = None
         if i % 2 == 1:
