@@ -47,6 +47,8 @@ WORKLOADS = {
                        "(seed 5) of the 1,051,392-tri mesh2 + 10,000 spheres + plane inside a scattering media box "
                        "(rgb 0.05, intervals 10, samples 10), radiosity count 200 recursion_limit 2 error_bound 0.5 "
                        "(pretrace + final trace per view), one step = the next view",
+    "bumpy_spheres": "bumpy_spheres: %dx%d 1spp, 12 spheres + plane with bumps/dents/wrinkles/slope normals "
+                     "and bozo pigments, phong + specular + reflection 0.25, 1 point light, max_trace_level 3",
 }
 MULTIVIEW = ("multiview_media",)
 
