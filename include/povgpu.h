@@ -178,6 +178,7 @@ typedef struct PovGpuMaterial {
 #define POV_PATTERN_SQUARE      20   /* SquarePattern::Evaluate, pattern.cpp:6740      */
 #define POV_PATTERN_TRIANGULAR  21   /* TriangularPattern::Evaluate, pattern.cpp:6799  */
 #define POV_PATTERN_CUBIC       22   /* CubicPattern::Evaluate, pattern.cpp:6699       */
+#define POV_PATTERN_HEXAGON     23   /* HexagonPattern::Evaluate, pattern.cpp:6512 (3) */
 #define POV_WAVE_RAMP     0       /* the default of most patterns                    */
 #define POV_WAVE_SINE     1
 #define POV_WAVE_TRIANGLE 2       /* the default of marble and wood                  */

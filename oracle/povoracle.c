@@ -1779,6 +1779,34 @@ static double pattern_value(const PovGpuPattern* pt, V3 T)
         else if (x < 0 && x <= -ay && x <= -az) value = 3.0;
         else if (y < 0 && y <= -ax && y <= -az) value = 4.0;
         else value = 5.0;
+    } else if (pt->type == POV_PATTERN_HEXAGON) {   /* pattern.cpp:6512-6655 */
+        /* the colour of each block of the 6 x 6 grid, by zm: blocks 0/5 and
+         * 2/3 of xm whole, 1/4 split on the diagonal */
+        static const int even[6] = {0, 1, 1, 2, 2, 0}, mid[6] = {2, 2, 0, 0, 1, 1};
+        static const int below[6] = {0, 2, 1, 0, 2, 1}, above[6] = {2, 1, 0, 2, 1, 0};
+        const double x = fabs(T.x);
+        const double z = T.z < 0.0 ? 5.196152424 - fabs(T.z) : T.z;
+        double xs = x / 0.5, zs = z / 0.866025404;
+        xs -= floor(xs / 6.0) * 6.0;
+        zs -= floor(zs / 6.0) * 6.0;
+        const int xm = (int)floor(xs) % 6, zm = (int)floor(zs) % 6;
+        value = 0.0;
+        if (zm >= 0 && zm < 6) {
+            if (xm == 0 || xm == 5) {
+                value = even[zm];
+            } else if (xm == 2 || xm == 3) {
+                value = mid[zm];
+            } else if (xm == 1 || xm == 4) {
+                double xl = xs - xm;
+                const double zl = zs - zm;
+                if (((xm + zm) % 2) == 1)
+                    xl = 1.0 - xl;
+                if (xl == 0.0)
+                    xl = 0.0001;
+                value = (zl / xl) < 1.0 ? below[zm] : above[zm];
+            }
+        }
+        value = fmod(value, 3.0);
     } else if (pt->type == POV_PATTERN_TRIANGULAR) {   /* pattern.cpp:6799-6866 */
         const double SQ3 = 1.7320508075688772935274463415059, SQ3_2 = 0.86602540378443864676372317075294;
         double xs = T.x - 3.0 * floor(T.x / 3.0);
@@ -3283,12 +3311,13 @@ int pov_oracle_create(const PovGpuSceneDesc* desc, PovOracle** out, int32_t* bad
         return POV_GPU_E_INVALID;
     for (int i = 0; i < desc->num_patterns; i++) {
         const PovGpuPattern* pt = &desc->patterns[i];
-        if (pt->type < POV_PATTERN_CHECKER || pt->type > POV_PATTERN_CUBIC || pt->num_entries < 0 ||
+        if (pt->type < POV_PATTERN_CHECKER || pt->type > POV_PATTERN_HEXAGON || pt->num_entries < 0 ||
             pt->num_entries > POV_PATTERN_MAX_ENTRIES || pt->noise_generator < 1 || pt->noise_generator > 3 ||
             pt->wave_type < POV_WAVE_RAMP || pt->wave_type > POV_WAVE_POLY || pt->octaves < 1 || pt->octaves > 32 ||
             (pt->type == POV_PATTERN_CHECKER && pt->num_entries != 2) ||
             (pt->type == POV_PATTERN_SQUARE && pt->num_entries != 4) ||
-            ((pt->type == POV_PATTERN_TRIANGULAR || pt->type == POV_PATTERN_CUBIC) && pt->num_entries != 6))
+            ((pt->type == POV_PATTERN_TRIANGULAR || pt->type == POV_PATTERN_CUBIC) && pt->num_entries != 6) ||
+            (pt->type == POV_PATTERN_HEXAGON && pt->num_entries != 3))
             return POV_GPU_E_UNSUPPORTED;
         for (int k = 1; k < pt->num_entries; k++)
             if (pt->values[k] < pt->values[k - 1])

@@ -89,6 +89,7 @@ POV_PATTERN_BOXED = 19
 POV_PATTERN_SQUARE = 20
 POV_PATTERN_TRIANGULAR = 21
 POV_PATTERN_CUBIC = 22
+POV_PATTERN_HEXAGON = 23
 POV_WAVES = {"ramp": 0, "sine": 1, "triangle": 2, "scallop": 3, "cubic": 4, "poly": 5}
 POV_PATTERN_MAX_ENTRIES = 16
 

@@ -695,12 +695,13 @@ int validate(const PovGpuSceneDesc* d, int32_t* bad)
         return POV_GPU_E_INVALID;
     for (int i = 0; i < d->num_patterns; i++) {
         const PovGpuPattern& pt = d->patterns[i];
-        if (pt.type < POV_PATTERN_CHECKER || pt.type > POV_PATTERN_CUBIC || pt.num_entries < 0 ||
+        if (pt.type < POV_PATTERN_CHECKER || pt.type > POV_PATTERN_HEXAGON || pt.num_entries < 0 ||
             pt.num_entries > POV_PATTERN_MAX_ENTRIES || pt.noise_generator < 1 || pt.noise_generator > 3 ||
             pt.wave_type < POV_WAVE_RAMP || pt.wave_type > POV_WAVE_POLY || pt.octaves < 1 || pt.octaves > 32 ||
             (pt.type == POV_PATTERN_CHECKER && pt.num_entries != 2) ||
             (pt.type == POV_PATTERN_SQUARE && pt.num_entries != 4) ||
-            ((pt.type == POV_PATTERN_TRIANGULAR || pt.type == POV_PATTERN_CUBIC) && pt.num_entries != 6))
+            ((pt.type == POV_PATTERN_TRIANGULAR || pt.type == POV_PATTERN_CUBIC) && pt.num_entries != 6) ||
+            (pt.type == POV_PATTERN_HEXAGON && pt.num_entries != 3))
             return POV_GPU_E_UNSUPPORTED;
         for (int k = 1; k < pt.num_entries; k++)
             if (pt.values[k] < pt.values[k - 1])

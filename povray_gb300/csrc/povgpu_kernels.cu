@@ -1088,6 +1088,31 @@ __device__ float pattern_value(const DeviceScene& S, const DevPattern& pt, float
                 : (x < 0.f && x <= -ay && x <= -az)  ? 3.0f
                 : (y < 0.f && y <= -ax && y <= -az)  ? 4.0f
                                                      : 5.0f;
+    } else if (kind == POV_PATTERN_HEXAGON) {      // pattern.cpp:6512-6655
+        // block colours of the 6 x 6 grid by zm, two bits each: blocks 0/5
+        // and 2/3 of xm whole, 1/4 split on the diagonal (below / above)
+        const unsigned even = 0x294u, mid = 0x50Au, below = 0x618u, above = 0x186u;
+        const float x = fabsf(T.x);
+        const float z = T.z < 0.0f ? 5.196152424f - fabsf(T.z) : T.z;
+        float xs = x / 0.5f, zs = z / 0.866025404f;
+        xs -= floorf(xs / 6.0f) * 6.0f;
+        zs -= floorf(zs / 6.0f) * 6.0f;
+        const int xm = (int)floorf(xs) % 6, zm = (int)floorf(zs) % 6;
+        unsigned tab = 0u;
+        if (xm == 0 || xm == 5) {
+            tab = even;
+        } else if (xm == 2 || xm == 3) {
+            tab = mid;
+        } else if (xm == 1 || xm == 4) {
+            float xl = xs - (float)xm;
+            const float zl = zs - (float)zm;
+            if (((xm + zm) % 2) == 1)
+                xl = 1.0f - xl;
+            if (xl == 0.0f)
+                xl = 0.0001f;
+            tab = (zl / xl) < 1.0f ? below : above;
+        }
+        value = (zm >= 0 && zm < 6) ? (float)((tab >> (2 * zm)) & 3u) : 0.0f;
     } else if (kind == POV_PATTERN_TRIANGULAR) {   // pattern.cpp:6799-6866
         const float SQ3 = 1.7320508075688772935f, SQ3_2 = 0.86602540378443864676f;
         float xs = T.x - 3.0f * floorf(T.x / 3.0f);

@@ -216,8 +216,8 @@ class Pattern:
              "boxed": abi.POV_PATTERN_BOXED,
              # discrete, with a colour list of 4, 6 and 6 entries at 0..n-1
              "square": abi.POV_PATTERN_SQUARE, "triangular": abi.POV_PATTERN_TRIANGULAR,
-             "cubic": abi.POV_PATTERN_CUBIC}
-    DISCRETE = ("checker", "square", "triangular", "cubic")
+             "cubic": abi.POV_PATTERN_CUBIC, "hexagon": abi.POV_PATTERN_HEXAGON}
+    DISCRETE = ("checker", "square", "triangular", "cubic", "hexagon")
 
     def __init__(self, kind, colours, transforms=(), gradient=(1.0, 0.0, 0.0), noise_generator=None,
                  turbulence=None, octaves=6, omega=0.5, lambda_=2.0, wave=None, frequency=1.0, phase=0.0,
@@ -1162,7 +1162,7 @@ def shaped_spheres(width=320, height=240, n_spheres=12, seed=8, noise_generator=
     scale 3) and `n_spheres` spheres r U[0.5,1.2] in a 6x6 area (seed 8)
     cycling through radial (frequency 6), planar, spherical (scale 1.2,
     centred on the sphere), cylindrical, boxed, dents, wrinkles, square,
-    triangular and cubic (centred on the sphere) pigments,
+    triangular, cubic (centred on the sphere) and hexagon pigments,
     half of them with a radial or spherical slope normal; phong 0.4; one
     point light; camera (0,3,-10) looking at (0,0,2), 55 deg;
     max_trace_level 2."""
@@ -1191,6 +1191,8 @@ def shaped_spheres(width=320, height=240, n_spheres=12, seed=8, noise_generator=
             Pattern("triangular", [(k, (0.15 * k + 0.1, 0.9 - 0.12 * k, 0.5)) for k in range(6)],
                     [("scale", (0.25, 0.25, 0.25)), ("rotate", (90.0, 0.0, 0.0))]),
             Pattern("cubic", [(k, (0.5, 0.15 * k + 0.1, 0.9 - 0.12 * k)) for k in range(6)], at),
+            Pattern("hexagon", [(0, (0.9, 0.8, 0.2)), (1, (0.2, 0.6, 0.9)), (2, (0.8, 0.2, 0.5))],
+                    [("scale", (0.2, 0.2, 0.2)), ("rotate", (-70.0, 0.0, 0.0))]),
         ]
         nrm = None
         if i % 2 == 1:
