@@ -216,6 +216,25 @@ def test_normal_validation(gpu_lib):
     assert _create(gpu_lib, desc)[0] == abi.POV_GPU_E_UNSUPPORTED
 
 
+def test_discrete_pattern_validation(gpu_lib):
+    """Colour lists: square takes 4 entries, triangular and cubic 6,
+    hexagon 3; a normal cannot read a discrete pattern (the reference
+    parses those as normal maps)."""
+    def fresh():
+        return scenes.shaped_spheres(32, 24, n_spheres=11).desc()
+    desc, keep = fresh()
+    kinds = {desc.patterns[i].type: i for i in range(desc.num_patterns)}
+    for t, n in ((abi.POV_PATTERN_SQUARE, 4), (abi.POV_PATTERN_TRIANGULAR, 6), (abi.POV_PATTERN_CUBIC, 6),
+                 (abi.POV_PATTERN_HEXAGON, 3)):
+        assert desc.patterns[kinds[t]].num_entries == n
+        desc, keep = fresh()
+        desc.patterns[kinds[t]].num_entries = n - 1
+        assert _create(gpu_lib, desc)[0] == abi.POV_GPU_E_UNSUPPORTED, t
+    desc, keep = fresh()
+    desc.normals[0].pattern = kinds[abi.POV_PATTERN_HEXAGON] + 1
+    assert _create(gpu_lib, desc)[0] == abi.POV_GPU_E_UNSUPPORTED
+
+
 def test_normal_sdl_and_desc_agree():
     """The normal's SDL carries the amount right after the pattern and its
     modifiers after; the descriptor's forward matrix and the pattern's
