@@ -1070,7 +1070,7 @@ __device__ float3 pattern_warp(const DeviceScene& S, const DevPattern& pt, float
 
 // Evaluate_TPat of a warped point T: the pattern's value with its frequency,
 // phase and wave (ContinuousPattern::Evaluate, pattern.cpp:354-390).
-__device__ float pattern_value(const DeviceScene& S, const DevPattern& pt, float3 T)
+__device__ __noinline__ float pattern_value(const DeviceScene& S, const DevPattern& pt, float3 T)
 {
     const int kind = pt.kind.x, gen = pt.kind.y;
     float value;
@@ -1231,7 +1231,7 @@ __device__ float pattern_value(const DeviceScene& S, const DevPattern& pt, float
 // Compute_Pigment of a pattern pigment at world point P (pigment.cpp:395-475):
 // the warped point's value through the colour map's linear blend
 // (BlendMap::Search, pattern.cpp:1068-1109).
-__device__ float3 pattern_pigment(const DeviceScene& S, int pi, float3 P)
+__device__ __noinline__ float3 pattern_pigment(const DeviceScene& S, int pi, float3 P)
 {
     const DevPattern& pt = S.patterns[pi];
     const float value = pattern_value(S, pt, pattern_warp(S, pt, P));
@@ -1256,7 +1256,7 @@ __device__ float3 pattern_pigment(const DeviceScene& S, int pi, float3 P)
 // TRANSFORM (Warp_Normal, warp.cpp:563-580), displaced by bumps, dents,
 // wrinkles or the four-point slope of a continuous pattern, back through the
 // inverse (UnWarp_Normal, warp.cpp:603-620) -- and normalised.
-__device__ float3 perturb_normal(const DeviceScene& S, int ni, float3 P, float3 N)
+__device__ __noinline__ float3 perturb_normal(const DeviceScene& S, int ni, float3 P, float3 N)
 {
     const DevNormal& nm = S.tnormals[ni];
     const DevPattern& pt = S.patterns[nm.kind.x];
