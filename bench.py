@@ -67,6 +67,14 @@ def workload_name(args):
 
 
 METRIC = "Mrays/s (primary+shadow)"
+L2_NOTE = ("GPU arm: L2 flushed between steps (256 MiB write, outside the timed events); "
+           "CPU arm: host caches as they are")
+
+
+def bench_config(args):
+    """The config object both arms print (identical, so that the two lines
+    describe the same workload)."""
+    return {"workload": workload_name(args), "l2": L2_NOTE}
 
 
 def parse():
@@ -160,6 +168,15 @@ def cpu_baseline(scene, cpu_seconds_target=20.0, crop=None):
                 "sample": "oracle restatement, %dx%d px at the centre of a %dx%d view (pretrace over the crop, "
                           "then the final trace), %.1f s wall, tree build %.1f s excluded"
                           % (crop, crop, scene.width, scene.height, dt, build_s)}
+    if scene.radiosity is None:
+        # the whole frame, as the GPU renders it
+        t = time.time()
+        _, st = orc.render(0, 0, scene.width, scene.height, threads=0)
+        dt = time.time() - t
+        return {"value": (st["number_of_rays"] + st["shadow_ray_tests"]) / dt / 1e6, "unit": "Mrays/s",
+                "cores": cores, "kind": "port",
+                "sample": "oracle restatement, the whole %dx%d frame, %.1f s wall, tree build %.1f s excluded"
+                          % (scene.width, scene.height, dt, build_s)}
     rows = 8
     y0 = scene.height // 2
     total_rays, total_t = 0, 0.0
@@ -191,7 +208,9 @@ def run_reference(args, rank, world):
         s = scenes.view_of(s, loc, at, w, h)
         args.width, args.height = w, h
     orc = Oracle(s)
-    band = max(8, args.height // 10)
+    # the whole frame per step, as the GPU arm renders it; radiosity frames
+    # (one thread, the reference's sample order) take a band of rows
+    band = args.height if s.radiosity is None else max(8, args.height // 10)
     def step(i):
         t = time.time()
         if args.workload in MULTIVIEW:
@@ -210,8 +229,12 @@ def run_reference(args, rank, world):
         rr += r
     v = rr / tt / 1e6
     cores = 1 if s.radiosity is not None else (os.cpu_count() or 1)
-    sample = "oracle restatement of the reference (FP64 C, pthreads), %d-row band of the %dx%d frame per step" % (
-        band, args.width, args.height)
+    if band == args.height:
+        sample = "oracle restatement of the reference (FP64 C, pthreads), the whole %dx%d frame per step" % (
+            args.width, args.height)
+    else:
+        sample = "oracle restatement of the reference (FP64 C, one thread: radiosity), %d-row band of the %dx%d " \
+                 "frame per step" % (band, args.width, args.height)
     if args.workload in MULTIVIEW:
         sample = "oracle restatement of the reference (FP64 C, one thread: radiosity), 16x16 px at the centre of " \
                  "the first %dx%d view per step (pretrace over the crop, then the final trace)" % (args.width,
@@ -220,10 +243,63 @@ def run_reference(args, rank, world):
         "impl": "reference", "metric": METRIC, "value": v, "unit": "Mrays/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": tt / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": workload_name(args)},
+        "config": bench_config(args), "rays_per_step": rr // max(1, args.steps),
         "cpu_baseline": {"value": v, "unit": "Mrays/s", "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
+
+
+TRUTH = os.path.join(ROOT, "tests", "golden", "radiosity_room_converged_1280x720.npz")
+
+
+def radiosity_forms(args, scene, gpu, stream, params, blocks, dev_out, flush, plain_ms):
+    """The radiosity half of the metric: frame time of the plain GPU form
+    (the timed frames above) and of the neural-cache form (the network
+    trained at the end of each pretrace answers the final trace's uncovered
+    queries, gated by its held-out error against error_bound), each with its
+    linear-radiance relative RMSE against the FP64 converged truth of this
+    scene (tests/golden, the oracle with 4096 / 16 rays per query and no
+    reuse) on the truth's pixel grid."""
+    import torch
+    from povray_gb300 import GpuScene, scenes
+    if (args.width, args.height) != (1280, 720) or not os.path.exists(TRUTH):
+        return None
+    t = np.load(TRUTH)
+    px, truth = t["pixels"], t["rgb"]
+
+    def rmse_of_last():
+        img = scenes.unblock(dev_out.cpu().numpy(), blocks, args.width, args.height)
+        a = img[px[:, 1], px[:, 0], :3]
+        return float(np.sqrt(((a - truth) ** 2).mean()) / truth.mean()), float(a.mean() / truth.mean())
+
+    rmse_plain, mean_plain = rmse_of_last()
+    nic = GpuScene(scene)
+    nic.set_stream(stream.cuda_stream)
+    nic.set_neural_cache(True)   # the library's defaults, gate = error_bound
+    for _ in range(args.warmup):
+        nic.radiosity_pretrace(blocks, params)
+        nic.trace_blocks(blocks, params, out=dev_out.data_ptr())
+    torch.cuda.synchronize()
+    ms, answers, val = [], 0, 0
+    for _ in range(args.steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        nic.radiosity_pretrace(blocks, params)
+        st = nic.trace_blocks(blocks, params, out=dev_out.data_ptr())[1]
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+        answers, val = st["nic_answers"], st["nic_val_error_ppm"]
+    rmse_nic, mean_nic = rmse_of_last()
+    nic_ms = sum(ms) / len(ms)
+    return {"plain": {"frame_ms": plain_ms, "rmse_vs_fp64": rmse_plain, "mean_vs_fp64": mean_plain},
+            "neural_cache": {"frame_ms": nic_ms, "rmse_vs_fp64": rmse_nic, "mean_vs_fp64": mean_nic,
+                             "nic_answers": answers, "held_out_error": val / 1e6},
+            "speedup": plain_ms / nic_ms,
+            "truth": "oracle converged radiosity (FP64 sums, 4096 / 16 stratified rays per query at depth 0 / 1, "
+                     "no reuse) on %d pixels (8x8 grid), own noise %.4f" % (len(px), json.loads(str(t["info"]))
+                                                                          ["noise_rel_rmse"])}
 
 
 def main():
@@ -256,7 +332,7 @@ def main():
     radiosity = s.radiosity is not None
     if multiview and radiosity:
         # the neural cache shared across the views, each pretrace training it on
-        gpu.set_neural_cache(True, steps=300, batch=4096, gate=0.5, shared=True)
+        gpu.set_neural_cache(True, shared=True)
 
     def view(i):
         """Render params and blocks of step i: the frame, or the next view
@@ -298,6 +374,7 @@ def main():
     sampler.start()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     stage_ms = {}
+    stage_launches = {}
     launches = 0
     rays = 0
     for i in range(args.steps):
@@ -308,6 +385,8 @@ def main():
         for t in tims:
             for k, v in t["stage_ms"].items():
                 stage_ms[k] = stage_ms.get(k, 0.0) + v
+            for k, v in t["stage_launches"].items():
+                stage_launches[k] = stage_launches.get(k, 0) + v
             launches += t["kernel_launches"]
         rays += st["number_of_rays"] + st["shadow_ray_tests"]
     torch.cuda.synchronize()
@@ -362,31 +441,48 @@ def main():
         pass
     peak = peaks.get("hbm_gbs", 6800.0)
     achieved = bytes_per_frame / kernel_s / 1e9
-    traffic = None
+    launches_per_frame = max(1.0, stage_launches.get(kname, args.steps) / args.steps)
+    # DRAM bytes of this kernel on this workload from an ncu capture
+    # (profiles/traffic.json, keyed by workload, then kernel stage)
+    prof = {}
     try:
-        traffic = json.load(open(os.path.join(ROOT, "profiles", "traffic.json"))).get(kname)
+        prof = json.load(open(os.path.join(ROOT, "profiles", "traffic.json"))).get(args.workload, {}).get(kname, {})
     except Exception:
         pass
+    dram_frame = prof.get("dram_bytes_per_frame")
     out = {
         "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_total / args.steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (fp64 grazing re-solve, fp64 camera)",
         "data": "synthetic",
-        "config": {"workload": workload_name(args), "l2": "flushed between steps (256 MiB write, outside timed events)",
-                   "rays_per_frame": rays // args.steps, "parallelism": "replica per GPU" if world > 1 else "1 GPU",
-                   **({"radiosity": {k: st[k] for k in ("radiosity_gathers", "radiosity_reuse", "radiosity_rays",
-                                                         "radiosity_gathers_d0", "radiosity_gathers_d1")}}
-                      if radiosity else {})},
+        "config": bench_config(args),
+        "rays_per_frame": rays // args.steps, "parallelism": "replica per GPU" if world > 1 else "1 GPU",
+        **({"radiosity": {k: st[k] for k in ("radiosity_gathers", "radiosity_reuse", "radiosity_rays",
+                                             "radiosity_gathers_d0", "radiosity_gathers_d1")}}
+           if radiosity else {}),
         "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": h2d // args.steps,
                 "d2h_bytes_per_step": d2h // args.steps},
         "roofline": {"bound": "hbm", "kernel": "k_trace<%s>" % ("closest" if k == 0 else "any"),
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "peak_source": "measured" if peaks else "fallback",
-                     "algorithmic_bytes_per_frame": bytes_per_frame},
+                     "traffic": (dram_frame / prof.get("launches_per_frame", launches_per_frame)
+                                 if dram_frame else None),
+                     "peak_source": "measured" if peaks else "fallback",
+                     "algorithmic_bytes_per_launch": bytes_per_frame / launches_per_frame,
+                     "launches_per_frame": launches_per_frame,
+                     # the byte model charges every node and primitive fetch
+                     # as if it came from HBM; ncu's DRAM bytes give the
+                     # fraction of HBM the kernel really uses
+                     "dram_gbs": dram_frame / kernel_s / 1e9 if dram_frame else None,
+                     "dram_frac": dram_frame / kernel_s / 1e9 / peak if dram_frame else None,
+                     "l2_hit_rate": prof.get("l2_hit_rate"),
+                     "traffic_source": prof.get("source")},
         "stage_ms_per_frame": {k2: v / args.steps for k2, v in stage_ms.items() if v > 0},
         "gpu_launches": launches,
         "clocks": clocks,
     }
+    if radiosity and not multiview:
+        out["radiosity_forms"] = radiosity_forms(args, s, gpu, stream, params, blocks, dev_out, flush,
+                                                 t_total / args.steps * 1e3)
     if rank == 0 and not args.no_cpu_baseline:
         if multiview:
             loc, at, w, h = views[0]

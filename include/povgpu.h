@@ -405,7 +405,9 @@ int pov_gpu_scene_create(const PovGpuSceneDesc* desc, PovGpuScene** out, int32_t
  * (tracetask.cpp:604) does per block.  out_rgbt receives 4 floats per pixel
  * in block order, each block's pixels row-major, exactly the vector that
  * CompletedRectangle takes.  out_rgbt may be host or device memory.
- * stats (optional) is overwritten with this call's counters.
+ * stats (optional) is overwritten with this call's counters.  It blocks
+ * until the blocks are done, or returns POV_GPU_E_TIMEOUT when the scene's
+ * host wait limit (pov_gpu_set_timeout) runs out first.
  */
 int pov_gpu_trace_blocks(PovGpuScene* scene, const PovGpuBlock* blocks, int32_t num_blocks,
                          const PovGpuRenderParams* params, float* out_rgbt, PovGpuStats* stats);
@@ -437,7 +439,11 @@ int pov_gpu_trace_rays(PovGpuScene* scene, const double* origins, const double* 
  * code there); make that call, e.g. with num_rays = 0, before any stream
  * capture.  The array's header (counters, error word, statistics) is zeroed
  * by every call.  There is one array per device: calls that overlap in time
- * on one device, from different threads or scenes, race on it.
+ * on one device, from different threads or scenes, race on it.  The
+ * array's address is looked up once per device and kept for the life of
+ * the process: after cudaDeviceReset (or any teardown of the device's
+ * primary context) the kept address is stale, so calls after such a reset
+ * are not supported.
  */
 #define POV_GPU_STATIC_MAX_RAYS 65536
 int pov_gpu_trace_rays_static(PovGpuScene* scene, const double* origins, const double* directions,
@@ -456,6 +462,27 @@ int pov_gpu_radiosity_pretrace(PovGpuScene* scene, const PovGpuBlock* blocks, in
                                const PovGpuRenderParams* params, PovGpuStats* stats);
 
 /*
+ * Radiosity cache files, the reference's .rca format
+ * (RadiosityCache::Load / BlockPool::Save, source/core/lighting/
+ * radiosity.cpp:909-1010,1142-1170; one text line per sample as
+ * ot_write_block writes it, source/core/support/octree.cpp:1345-1370).
+ * pov_gpu_cache_save writes the scene's current cache (after a pretrace,
+ * or after a final trace, which adds its own samples) to `path`.
+ * pov_gpu_cache_load reads `path` (NULL: forget a loaded file) and makes
+ * its samples the start of every following frame's cache: the cache holds
+ * them at once, and each pov_gpu_radiosity_pretrace starts from them
+ * instead of from an empty cache -- what +RFI does for a reference view.
+ * Loaded samples have quality 1 and the file's precision (6 significant
+ * digits, illuminance to 4 decimals, unit vectors packed to bytes).
+ * *loaded (optional) receives the number of samples read.  Both return
+ * POV_GPU_E_INVALID without radiosity or when the file cannot be opened,
+ * and load returns POV_GPU_E_CAPACITY for more samples than the cache
+ * holds.
+ */
+int pov_gpu_cache_save(PovGpuScene* scene, const char* path);
+int pov_gpu_cache_load(PovGpuScene* scene, const char* path, int32_t* loaded);
+
+/*
  * The pretrace jitter table: RadiosityTask's RandomDoubleSequence(-1, 1,
  * 2047) values (radiositytask.cpp:99), which the reference-side caller holds.
  * Copied.  Without a table the pretrace jitters by its own hash.
@@ -467,13 +494,18 @@ int pov_gpu_set_pretrace_jitter(PovGpuScene* scene, const double* table, int32_t
  * radiosity pretrace ends by training a 4x64 MLP (hand-written tcgen05
  * kernels) on the depth-0 samples it gathered, `steps` Adam steps of `batch`
  * samples; every eighth sample is held out.  If the held-out relative RMSE
- * is at most `gate`, final-trace queries that no cached sample covers take
- * the network's answer instead of gathering a new sample.
+ * is at most `gate` (the radiosity error_bound is the natural choice),
+ * final-trace queries that no cached sample covers take the network's
+ * answer instead of gathering a new sample; otherwise the plain gather
+ * answers them.  Training is deterministic for given samples: each CTA
+ * keeps its own gradient slice and the Adam step sums the slices in a
+ * fixed order.
  */
 typedef struct PovGpuNeuralCache {
     int32_t enabled;
     int32_t steps;            /* Adam steps per pretrace                      */
-    int32_t batch;            /* samples per step (multiple of 128 is best)   */
+    int32_t batch;            /* samples per step (multiple of 128 is best);
+                                 0 = 128 per SM of the device                 */
     float   learning_rate;
     float   gate;             /* largest held-out relative RMSE it may answer */
     uint32_t seed;            /* batch sampling                               */
@@ -497,7 +529,23 @@ int pov_gpu_set_neural_cache(PovGpuScene* scene, const PovGpuNeuralCache* config
 int pov_gpu_nic_eval(const float* params, const float* bounds, const float* points, const float* normals,
                      const float* targets, int32_t n, float* out, float* grad, float* loss);
 
-/* Releases all device memory of the scene. */
+/*
+ * Host wait limit of the scene's calls, in seconds (0 = no limit, the
+ * default).  A call whose queued device work has not finished when the
+ * limit runs out returns POV_GPU_E_TIMEOUT instead of waiting on -- so a
+ * render task can poll for stop/pause (the reference's TraceTask calls
+ * Cooperate() between pixels, tracetask.cpp:403-454) -- and its outputs
+ * are undefined.  The work already queued keeps running on the device and
+ * still writes the scene's buffers and that call's output buffer: keep the
+ * buffer alive until the next call on the scene returns (it first waits
+ * for that work, within its own limit) or the scene is destroyed
+ * (pov_gpu_scene_destroy waits without a limit).  POV_GPU_E_INVALID for a
+ * negative or non-finite limit.
+ */
+int pov_gpu_set_timeout(PovGpuScene* scene, double seconds);
+
+/* Releases all device memory of the scene (after waiting for its queued
+ * work, without a limit). */
 void pov_gpu_scene_destroy(PovGpuScene* scene);
 
 /*

@@ -472,6 +472,7 @@ struct PovOracle {
     Tree     top;            /* leaf item = object index */
     int32_t  top_linear;     /* no slabs: linear scan (trace.cpp:263) */
     struct RadCache* rad;    /* radiosity sample cache (mutable during a render) */
+    int32_t  gt_count[8];    /* converged mode: directions per query and depth (0 = off) */
 };
 
 static int max3_coordinate(double x, double y, double z)  /* mathutil */
@@ -1089,6 +1090,7 @@ typedef struct {
     int      rad_pass;
     int      rad_dir_index[8];
     uint64_t rad_top_queries;
+    uint64_t gt_rng;          /* converged mode: the pixel's random sequence */
 } Thread;
 
 /* Sphere::Intersect (sphere.cpp:214-245). */
@@ -3076,6 +3078,76 @@ static double gather_light(const PovOracle* S, Thread* th, V3 ip, V3 raw, double
     return qsum / count;
 }
 
+/* ------------------------------------------- converged radiosity ---
+ * The FP64 ground truth for the radiosity images (test infrastructure; no
+ * counterpart in the reference).  ComputeAmbient without the sample cache:
+ * every query at bounce depth d averages S->gt_count[d] cosine-weighted
+ * directions of the radiance Trace returns along them, summed in FP64.  The
+ * directions are stratified -- an a x a grid of jittered cells of the unit
+ * square (a = round(sqrt(count))) mapped to the hemisphere by Malley's
+ * method (uniform disc point lifted to the hemisphere: cosine-weighted
+ * density) and turned by a random angle about the normal -- and drawn from
+ * a per-pixel random sequence (splitmix64 seeded by the pixel), so the
+ * image does not depend on the thread count.  Each sample ray is traced as
+ * GatherLight traces its rays (radiosity.cpp:509-756: trace level, ADC
+ * bailout and weight of the bounce depth, radiosity ray flags); the query
+ * then gets ComputeAmbient's grey threshold and brightness
+ * (radiosity.cpp:457-461).  Without reuse the only error left is the
+ * sampling noise of gt_count directions per query. */
+static const double GT_PI = 3.14159265358979323846;
+
+static double gt_uniform(Thread* th)
+{
+    uint64_t z = (th->gt_rng += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+}
+
+static void gather_converged(const PovOracle* S, Thread* th, V3 ip, V3 raw, double amb[3], Ticket* tk)
+{
+    RadCache* R = S->rad;
+    const PovGpuRadiosity* rs = &S->desc.radiosity;
+    const int depth = tk->rad_depth;
+    const RadRec* rec = &R->rec[depth];
+    int a = (int)floor(sqrt((double)S->gt_count[depth]) + 0.5);
+    if (a < 1)
+        a = 1;
+    Ticket save = *tk;
+    tk->level = rec->trace_level;
+    if (tk->max_level < tk->level + 1)
+        tk->max_level = tk->level + 1;
+    tk->adc = rs->adc_bailout;
+    double weight = fmax(tk->adc + EPSILON, rec->weight);
+    V3 fy = raw;
+    V3 off = fabs(fy.z) > 0.9 ? v3(0, 1, 0) : v3(0, 0, 1);
+    V3 fx = vnorm(vcross(fy, off));
+    V3 fz = vnorm(vcross(fx, fy));
+    double turn = 2.0 * GT_PI * gt_uniform(th);
+    double sum[3] = {0.0, 0.0, 0.0};
+    for (int i = 0; i < a * a; i++) {
+        double u = ((i % a) + gt_uniform(th)) / a, v = ((i / a) + gt_uniform(th)) / a;
+        double r = sqrt(u), phi = 2.0 * GT_PI * v + turn;
+        double lx = r * cos(phi), ly = sqrt(fmax(0.0, 1.0 - u)), lz = r * sin(phi);
+        V3 dir = vnorm(vadd(vadd(vmul(fx, lx), vmul(fy, ly)), vmul(fz, lz)));
+        tk->rad_quality = 1.0f;
+        tk->rad_depth++;
+        RGB c;
+        trace_ray(S, th, ip, dir, weight, tk, RAY_RADIOSITY, &c);
+        tk->rad_depth--;
+        sum[0] += c.r;
+        sum[1] += c.g;
+        sum[2] += c.b;
+    }
+    for (int k = 0; k < 3; k++)
+        amb[k] = sum[k] / (double)(a * a);
+    tk->max_level = save.max_level;
+    tk->level = save.level;
+    tk->adc = save.adc;
+    tk->rad_quality = save.rad_quality;
+}
+
 /* RadiosityFunction::ComputeAmbient (radiosity.cpp:385-462), "normal" and
  * "brilliance" settings off (their defaults). */
 static void compute_ambient(const PovOracle* S, Thread* th, V3 ip, V3 raw, V3 layer, double brilliance, float amb[3],
@@ -3085,6 +3157,14 @@ static void compute_ambient(const PovOracle* S, Thread* th, V3 ip, V3 raw, V3 la
     (void)brilliance;
     RadCache* R = S->rad;
     const PovGpuRadiosity* rs = &S->desc.radiosity;
+    if (S->gt_count[0] > 0) {   /* converged mode: no cache */
+        double a[3];
+        gather_converged(S, th, ip, raw, a, tk);
+        double grey = 0.297 * a[0] + 0.589 * a[1] + 0.114 * a[2];
+        for (int k = 0; k < 3; k++)
+            amb[k] = (float)((a[k] * (1.0 - rs->gray_threshold) + rs->gray_threshold * grey) * rs->brightness);
+        return;
+    }
     const RadRec* rec = &R->rec[tk->rad_depth];
     double eb = th->rad_error_bound;
     if (weight < WEIGHT_ERROR_BOUND_OFFSET)
@@ -3802,6 +3882,75 @@ static int render_radiosity(PovOracle* S, const PovGpuRenderParams* p, int32_t x
         stats->radiosity_gathers_d1 = R->gathers_depth[1];
     }
     thread_free(&th);
+    return POV_GPU_OK;
+}
+
+typedef struct {
+    PovOracle* S;
+    const PovGpuRenderParams* p;
+    const int32_t* px;
+    int32_t n, next;
+    uint64_t seed;
+    float* out;
+    PovGpuStats stats;
+    pthread_mutex_t lock;
+} ConvergedJob;
+
+static void* converged_worker(void* arg)
+{
+    ConvergedJob* J = (ConvergedJob*)arg;
+    Thread th;
+    memset(&th, 0, sizeof(th));
+    th.rad_final = 1;
+    th.rad_pass = PASS_FINAL;
+    th.rad_error_bound = J->S->desc.radiosity.error_bound;
+    for (;;) {
+        pthread_mutex_lock(&J->lock);
+        int32_t i = J->next++;
+        pthread_mutex_unlock(&J->lock);
+        if (i >= J->n)
+            break;
+        int32_t x = J->px[2 * i], y = J->px[2 * i + 1];
+        th.gt_rng = J->seed ^ ((uint64_t)(uint32_t)y << 32 | (uint32_t)x) * 0xD1B54A32D192ED03ull;
+        trace_pixel(J->S, &th, x + 0.5, y + 0.5, J->p->width, J->p->height, J->out + (size_t)i * 4);
+    }
+    pthread_mutex_lock(&J->lock);
+    J->stats.number_of_rays += th.rays;
+    J->stats.shadow_ray_tests += th.shadow_tests;
+    J->stats.shadow_rays_succeeded += th.shadow_succeeded;
+    pthread_mutex_unlock(&J->lock);
+    thread_free(&th);
+    return NULL;
+}
+
+int pov_oracle_render_converged(PovOracle* S, const PovGpuRenderParams* p, const int32_t* pixels, int32_t n,
+                                const int32_t* counts, int32_t ncounts, uint64_t seed, int32_t threads,
+                                float* out, PovGpuStats* stats)
+{
+    if (!S || !p || !S->rad || !S->desc.radiosity.enabled || (n > 0 && (!pixels || !out)) || !counts ||
+        ncounts < 1 || ncounts > 8 || counts[0] < 1 || p->antialias)
+        return POV_GPU_E_INVALID;
+    ConvergedJob J;
+    memset(&J, 0, sizeof(J));
+    J.S = S; J.p = p; J.px = pixels; J.n = n; J.seed = seed; J.out = out;
+    pthread_mutex_init(&J.lock, NULL);
+    for (int d = 0; d < 8; d++)
+        S->gt_count[d] = counts[d < ncounts ? d : ncounts - 1];
+    if (threads <= 0) {
+        long c = sysconf(_SC_NPROCESSORS_ONLN);
+        threads = c > 0 ? (int32_t)c : 1;
+    }
+    pthread_t* tids = (pthread_t*)malloc(sizeof(pthread_t) * threads);
+    for (int i = 0; i < threads; i++)
+        pthread_create(&tids[i], NULL, converged_worker, &J);
+    for (int i = 0; i < threads; i++)
+        pthread_join(tids[i], NULL);
+    free(tids);
+    memset(S->gt_count, 0, sizeof(S->gt_count));
+    pthread_mutex_destroy(&J.lock);
+    J.stats.number_of_pixels = (uint64_t)n;
+    if (stats)
+        *stats = J.stats;
     return POV_GPU_OK;
 }
 

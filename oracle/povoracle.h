@@ -37,6 +37,18 @@ int  pov_oracle_render(PovOracle* o, const PovGpuRenderParams* params, int32_t x
  * the table is borrowed, not copied. */
 int  pov_oracle_set_pretrace_jitter(PovOracle* o, const double* table, int32_t n);
 
+/* Converged radiosity, the FP64 ground truth of radiosity images (no
+ * counterpart in the reference): the final trace of the given pixels
+ * (x, y pairs of the full image; row-major RGBT floats out, one per pixel)
+ * with every radiosity query answered without the sample cache, by
+ * counts[d] stratified cosine-weighted sample rays at bounce depth d
+ * (counts shorter than the recursion depth repeat their last entry),
+ * summed in FP64.  `seed` fixes the per-pixel random sequences; the result
+ * does not depend on `threads`. */
+int  pov_oracle_render_converged(PovOracle* o, const PovGpuRenderParams* params, const int32_t* pixels,
+                                 int32_t n, const int32_t* counts, int32_t ncounts, uint64_t seed,
+                                 int32_t threads, float* out_rgbt, PovGpuStats* stats);
+
 /* Per-ray work counters of the restated traversal, for the roofline byte
  * model: node boxes tested and primitives tested over the given rays. */
 int  pov_oracle_count_work(PovOracle* o, const double* origins, const double* directions,

@@ -48,6 +48,10 @@ def lib():
         L.pov_oracle_count_work.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
                                             C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
         L.pov_oracle_count_work.restype = C.c_int
+        L.pov_oracle_render_converged.argtypes = [C.c_void_p, C.POINTER(abi.PovGpuRenderParams), C.c_void_p,
+                                                  C.c_int32, C.c_void_p, C.c_int32, C.c_uint64, C.c_int32,
+                                                  C.c_void_p, C.POINTER(abi.PovGpuStats)]
+        L.pov_oracle_render_converged.restype = C.c_int
         L.pov_oracle_set_pretrace_jitter.argtypes = [C.c_void_p, C.c_void_p, C.c_int32]
         L.pov_oracle_set_pretrace_jitter.restype = C.c_int
         _lib = L
@@ -109,6 +113,24 @@ class Oracle:
                                      C.byref(stats))
         if st != 0:
             raise abi.PovGpuError(st, "pov_oracle_render")
+        return out, stats.as_dict()
+
+    def render_converged(self, pixels, counts, seed=1, threads=0, params=None):
+        """Converged radiosity (the FP64 ground truth): RGBT of the given
+        pixels ((n, 2) int array of x, y in the full image), every radiosity
+        query answered without the cache by counts[d] stratified
+        cosine-weighted rays at bounce depth d.  Returns ((n, 4) float32,
+        stats)."""
+        from povray_gb300 import abi
+        p = params or self.scene.render_params()
+        px = np.ascontiguousarray(pixels, dtype=np.int32).reshape(-1, 2)
+        cn = np.ascontiguousarray(counts, dtype=np.int32)
+        out = np.zeros((px.shape[0], 4), dtype=np.float32)
+        stats = abi.PovGpuStats()
+        st = lib().pov_oracle_render_converged(self.h, C.byref(p), px.ctypes.data, px.shape[0], cn.ctypes.data,
+                                               len(cn), int(seed), threads, out.ctypes.data, C.byref(stats))
+        if st != 0:
+            raise abi.PovGpuError(st, "pov_oracle_render_converged")
         return out, stats.as_dict()
 
     def count_work(self, origins, directions):

@@ -17,6 +17,8 @@
 //        IN.rays:  int32 n, then n * (origin[3], dir[3]) doubles
 //        OUT.hits: n * (int32 object, int32 triangle, double depth)
 //   pov_oracle SCENE.pov W H scene  OUT.txt          parsed camera + objects
+//   pov_oracle SCENE.pov W H desc   OUT.pgsf         the parsed scene flattened
+//        into the C ABI's scene description (pov_flatten.cpp), as a scene file
 // Every mode prints one JSON line of render statistics on stdout.
 
 #include <cstdio>
@@ -52,6 +54,8 @@
 #include "core/shape/mesh.h"
 #include "core/support/statistics.h"
 #include "parser/parser.h"
+
+#include "pov_flatten.h"
 
 using namespace pov;
 using namespace pov_base;
@@ -318,6 +322,19 @@ int main(int argc, char **argv)
                 std::fwrite(&depth, 8, 1, o);
             }
             std::fclose(o);
+            PrintStats(td);
+        }
+        else if (mode == "desc")
+        {
+            povgpu_ref::FlatScene flat;
+            std::string why;
+            if (!povgpu_ref::FlattenScene(*h.sd, flat, why))
+            {
+                std::fprintf(stderr, "pov_oracle: not flattened: %s\n", why.c_str());
+                return 4;
+            }
+            if (!povgpu_ref::WriteSceneFile(flat, argv[5]))
+                return 3;
             PrintStats(td);
         }
         else if (mode == "scene")

@@ -232,7 +232,8 @@ EXPORTS = ["pov_gpu_scene_create", "pov_gpu_trace_blocks", "pov_gpu_trace_rays",
            "pov_gpu_scene_destroy", "pov_gpu_error_string", "pov_gpu_abi_version",
            "pov_gpu_scene_set_stream", "pov_gpu_set_profiling", "pov_gpu_get_timings",
            "pov_gpu_trace_rays_static", "pov_gpu_radiosity_pretrace", "pov_gpu_set_pretrace_jitter",
-           "pov_gpu_set_neural_cache", "pov_gpu_nic_eval", "pov_gpu_set_camera", "pov_gpu_encode_u8"]
+           "pov_gpu_set_neural_cache", "pov_gpu_nic_eval", "pov_gpu_set_camera", "pov_gpu_encode_u8",
+           "pov_gpu_set_timeout", "pov_gpu_cache_save", "pov_gpu_cache_load"]
 
 
 class PovGpuError(RuntimeError):
@@ -286,6 +287,12 @@ def load_library(path=None):
     lib.pov_gpu_encode_u8.restype = C.c_int
     lib.pov_gpu_set_camera.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     lib.pov_gpu_set_camera.restype = C.c_int
+    lib.pov_gpu_cache_save.argtypes = [C.c_void_p, C.c_char_p]
+    lib.pov_gpu_cache_save.restype = C.c_int
+    lib.pov_gpu_cache_load.argtypes = [C.c_void_p, C.c_char_p, C.POINTER(C.c_int32)]
+    lib.pov_gpu_cache_load.restype = C.c_int
+    lib.pov_gpu_set_timeout.argtypes = [C.c_void_p, C.c_double]
+    lib.pov_gpu_set_timeout.restype = C.c_int
     lib.pov_gpu_scene_set_stream.argtypes = [C.c_void_p, C.c_void_p]
     lib.pov_gpu_scene_set_stream.restype = C.c_int
     lib.pov_gpu_set_profiling.argtypes = [C.c_void_p, C.c_int]

@@ -16,12 +16,14 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <random>
 #include <mutex>
 #include <new>
+#include <thread>
 #include <vector>
 
 using namespace povgpu;
@@ -476,7 +478,6 @@ struct RadLevel {
     }
 };
 
-constexpr int RAD_LEVELS = 4;                    // bounce depths with their own buffers
 constexpr size_t GATHER_CHUNK_RAYS = 1u << 20;   // sample rays in flight per depth
 constexpr int RAD_ROUNDS = 8;                    // query rounds before every open query gathers
 
@@ -497,6 +498,7 @@ struct RadiosityState {
     double          error_bound = 0.0;
     uint64_t        rays_shot = 0;
     std::vector<double> jitter;
+    std::vector<RadBlock> loaded;   // samples of a loaded cache file, in every frame's cache from its start
     RadLevel        level[RAD_LEVELS];
     // neural irradiance cache: configuration, parameters (FP32 master, BF16
     // copy, Adam moments, gradient), training batches, and whether the last
@@ -563,12 +565,22 @@ struct PovGpuScene {
     DevBuf       wcount;
 
     cudaStream_t active() const { return user_stream ? user_stream : stream; }
+    // host wait limit of a call (pov_gpu_set_timeout; 0 = wait as long as
+    // the work takes), the current call's deadline, and whether work of a
+    // call that gave up is still on the stream
+    double       timeout_s = 0.0;
+    std::chrono::steady_clock::time_point deadline{};
+    bool         pending = false;
+    cudaEvent_t  wait_event = nullptr;
 
     void release_all()
     {
         for (cudaEvent_t e : events)
             cudaEventDestroy(e);
         events.clear();
+        if (wait_event)
+            cudaEventDestroy(wait_event);
+        wait_event = nullptr;
         DevBuf* all[] = {&nodes, &refs, &tri_v0, &tri_e1, &tri_e2, &tri_global, &tri_shade, &tri_normal, &tri_local,
                          &normals, &spheres, &spheres64, &boxes64, &sphere_obj, &sphere_flags, &planes, &plane_obj, &boxes, &tori, &csgs,
                          &csg_children, &objects, &materials, &lights, &blocks, &block_off, &corner_off, &qA,
@@ -594,6 +606,55 @@ namespace {
         if (e_ != cudaSuccess)                                                         \
             return e_ == cudaErrorMemoryAllocation ? POV_GPU_E_NOMEM : POV_GPU_E_CUDA; \
     } while (0)
+
+// The host's wait for the work queued on the scene's stream.  Without a
+// limit: cudaStreamSynchronize.  With one (pov_gpu_set_timeout): an event
+// recorded behind the work is polled until it completes or the call's
+// deadline passes; then the scene is marked pending (its work still runs
+// and still owns the scene's buffers and the call's output) and the call
+// returns POV_GPU_E_TIMEOUT.
+int host_wait(PovGpuScene* sc, cudaStream_t st)
+{
+    if (sc->timeout_s <= 0.0) {
+        CK(cudaStreamSynchronize(st));
+        sc->pending = false;
+        return POV_GPU_OK;
+    }
+    if (!sc->wait_event)
+        CK(cudaEventCreateWithFlags(&sc->wait_event, cudaEventDisableTiming));
+    CK(cudaEventRecord(sc->wait_event, st));
+    for (;;) {
+        cudaError_t q = cudaEventQuery(sc->wait_event);
+        if (q == cudaSuccess) {
+            sc->pending = false;
+            return POV_GPU_OK;
+        }
+        if (q != cudaErrorNotReady)
+            CK(q);
+        if (std::chrono::steady_clock::now() >= sc->deadline) {
+            sc->pending = true;
+            return POV_GPU_E_TIMEOUT;
+        }
+        std::this_thread::sleep_for(std::chrono::microseconds(20));
+    }
+}
+
+#define HW(st)                                      \
+    do {                                            \
+        if (int hw_ = host_wait(sc, (st)))          \
+            return hw_;                             \
+    } while (0)
+
+// Start of a call that queues work: its deadline, and the wait for work a
+// call before it left on the stream when it gave up.
+int begin_call(PovGpuScene* sc)
+{
+    sc->deadline = std::chrono::steady_clock::now() +
+                   std::chrono::microseconds((long long)(sc->timeout_s * 1e6));
+    if (sc->pending)
+        return host_wait(sc, sc->active());
+    return POV_GPU_OK;
+}
 
 constexpr int MAX_AA_DEPTH = 4;   // (2^4+1)^2 = 289 grid points, 21 subdividable cells per pixel
 
@@ -1459,7 +1520,7 @@ int check_device_error(PovGpuScene* sc, PovGpuStats* stats, unsigned long long* 
     cudaStream_t st = sc->active();
     CK(cudaMemcpyAsync(&errw, sc->err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(host_stats, sc->stats.p, sizeof(unsigned long long) * ST_COUNT, cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
+    HW(st);
     if (stats) {
         std::memset(stats, 0, sizeof(*stats));
         stats->number_of_rays = host_stats[ST_RAYS];
@@ -1608,6 +1669,19 @@ int rad_reset(PovGpuScene* sc)
     CK(cudaMemsetAsync(R.occupancy.p, 0, R.occupancy.bytes, st));
     for (int& b : R.dir_base)
         b = 0;
+    // a loaded cache file's samples start every frame's cache, as the
+    // reference's RadiosityCache loads its file when it is built
+    const int nl = (int)std::min<size_t>(R.loaded.size(), (size_t)R.cap_blocks);
+    if (nl > 0) {
+        CK(cudaMemcpyAsync(R.blocks.p, R.loaded.data(), sizeof(RadBlock) * (size_t)nl, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(R.count.p, &nl, sizeof(int32_t), cudaMemcpyHostToDevice, st));
+        float af[RAD_LEVELS];
+        for (int d = 0; d < RAD_LEVELS; d++)
+            af[d] = rad_params(sc, d).address_factor;
+        CK(launch_rad_file(cache_view(sc), af, 0, nl, sc->err.as<uint32_t>(), st));
+        R.seg_dirty = true;
+        CK(cudaStreamSynchronize(st));   // the host vectors above must outlive the copies
+    }
     return POV_GPU_OK;
 }
 
@@ -1626,7 +1700,7 @@ int run_media(PovGpuScene* sc, PathBufs& B, const QRay* q, const int* state, con
     CK(launch_media_list(state, B.hits.as<QHit>(), qcount, (int)maxq, B.mlist.as<int>(), cnt + C_MC, grid, st));
     int nm = 0;
     CK(cudaMemcpyAsync(&nm, cnt + C_MC, sizeof(int), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
+    HW(st);
     nm = std::min<int>(nm, (int)maxq);
     *launches = 1;
     if (nm == 0)
@@ -1709,7 +1783,7 @@ int run_levels(PovGpuScene* sc, StageClock& clk, PathBufs& B, size_t maxq, int l
         if (media && pass > 0) {
             int nq = 0;
             CK(cudaMemcpyAsync(&nq, ccur, sizeof(int), cudaMemcpyDeviceToHost, st));
-            CK(cudaStreamSynchronize(st));
+            HW(st);
             if (nq == 0)
                 break;
         }
@@ -1767,7 +1841,7 @@ int run_levels(PovGpuScene* sc, StageClock& clk, PathBufs& B, size_t maxq, int l
         if (rad) {
             int nq = 0;
             CK(cudaMemcpyAsync(&nq, cnt + C_RQ, sizeof(int), cudaMemcpyDeviceToHost, st));
-            CK(cudaStreamSynchronize(st));
+            HW(st);
             nq = std::min(nq, (int)maxq);
             if (nq > 0) {
                 int rc = rad_resolve(sc, clk, hit_depth, B.rq.as<RadQuery>(), nq, B.rq_amb.as<float4>());
@@ -1871,7 +1945,7 @@ int rad_resolve(PovGpuScene* sc, StageClock& clk, int d, const RadQuery* queries
         CK(clk.end());
         int hc[2] = {0, 0};
         CK(cudaMemcpyAsync(hc, cn, sizeof(hc), cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
+        HW(st);
         const int ns = std::min(hc[0], n), nn = std::min(hc[1], n);
         if (use_nic) {
             if (ns > 0) {
@@ -1962,7 +2036,7 @@ int nic_train(PovGpuScene* sc)
     cudaStream_t st = sc->active();
     int nb = 0;
     CK(cudaMemcpyAsync(&nb, R.count.p, sizeof(int), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
+    HW(st);
     nb = std::min(nb, R.cap_blocks);
     if (nb <= 0)
         return POV_GPU_OK;
@@ -2005,8 +2079,12 @@ int nic_train(PovGpuScene* sc)
     CK(R.nic_wb.ensure(nic::WIMG_BYTES));
     CK(R.nic_m.ensure(sizeof(float) * NP));
     CK(R.nic_v.ensure(sizeof(float) * NP));
-    CK(R.nic_grad.ensure(sizeof(float) * NP));
-    CK(R.nic_loss.ensure(sizeof(float)));
+    // batch 0: one 128-sample tile per SM, every SM busy in each step
+    const int steps = std::max(cfg.steps, 1),
+              batch = cfg.batch > 0 ? std::max(cfg.batch, nic::TILE) : nic::TILE * sc->num_sms;
+    const int slices = nic::train_slices(batch, sc->num_sms);
+    CK(R.nic_grad.ensure(sizeof(float) * NP * (size_t)slices));
+    CK(R.nic_loss.ensure(sizeof(float) * (size_t)slices));
     CK(R.nic_err.ensure(sizeof(uint32_t)));
     std::mt19937 rng(cfg.seed + (uint32_t)R.nic_step);
     std::vector<float> hp(NP, 0.0f);
@@ -2031,7 +2109,6 @@ int nic_train(PovGpuScene* sc)
     }
     CK(cudaMemsetAsync(R.nic_err.p, 0, sizeof(uint32_t), st));
     // every step's batch, drawn up front
-    const int steps = std::max(cfg.steps, 1), batch = std::max(cfg.batch, nic::TILE);
     std::vector<int> idx((size_t)steps * batch + val.size());
     std::uniform_int_distribution<int> pick(0, (int)train.size() - 1);
     for (size_t i = 0; i < (size_t)steps * batch; i++)
@@ -2051,16 +2128,15 @@ int nic_train(PovGpuScene* sc)
     for (int s = 0; s < steps; s++) {
         io.idx = R.nic_idx.as<int>() + (size_t)s * batch;
         io.n = batch;
-        CK(cudaMemsetAsync(R.nic_grad.p, 0, sizeof(float) * NP, st));
         CK(nic::launch_train(io, R.nic_wb.as<unsigned char>(), R.nic_params.as<float>(), R.nic_grad.as<float>(),
                              R.nic_loss.as<float>(), 1.0f / (float)batch, R.nic_err.as<uint32_t>(), sc->num_sms,
                              st));
         CK(nic::launch_adam(R.nic_params.as<float>(), R.nic_m.as<float>(), R.nic_v.as<float>(),
-                            R.nic_grad.as<float>(), R.nic_wb.as<unsigned char>(), cfg.learning_rate,
+                            R.nic_grad.as<float>(), slices, R.nic_wb.as<unsigned char>(), cfg.learning_rate,
                             R.nic_step + s + 1, st));
     }
     R.nic_step += steps;
-    CK(clk.end(3 * steps));
+    CK(clk.end(2 * steps));
     // held-out relative RMSE
     const int nv = (int)val.size();
     CK(R.nic_pred.ensure(sizeof(float4) * (size_t)nv));
@@ -2073,7 +2149,7 @@ int nic_train(PovGpuScene* sc)
     uint32_t nerr = 0;
     CK(cudaMemcpyAsync(pred.data(), R.nic_pred.p, sizeof(float4) * (size_t)nv, cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(&nerr, R.nic_err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
+    HW(st);
     double se = 0.0, sy = 0.0;
     for (int i = 0; i < nv; i++) {
         const RadBlock& b = hb[(size_t)val[i]];
@@ -2114,7 +2190,7 @@ const char* pov_gpu_error_string(int status)
     case POV_GPU_E_INVALID: return "invalid argument or scene description";
     case POV_GPU_E_UNSUPPORTED: return "object, texture or light not supported by the GPU trace path";
     case POV_GPU_E_CUDA: return "CUDA runtime error";
-    case POV_GPU_E_TIMEOUT: return "device wait timed out";
+    case POV_GPU_E_TIMEOUT: return "host wait limit reached (pov_gpu_set_timeout); device work still queued";
     case POV_GPU_E_NOMEM: return "device memory allocation failed";
     case POV_GPU_E_DEVICE: return "kernel reported an error in its device error word";
     case POV_GPU_E_NODEVICE: return "no CUDA device";
@@ -2168,6 +2244,137 @@ void pov_gpu_scene_destroy(PovGpuScene* scene)
     cudaStreamSynchronize(scene->active());
     scene->release_all();
     delete scene;
+}
+
+// Cache files: the reference's .rca text format, one "C" line per sample
+// (ot_write_block, source/core/support/octree.cpp:1345-1370: 1-based bounce
+// depth, point, packed normal, illuminance, harmonic mean and nearest
+// distance, packed direction to the nearest surface); read back as
+// RadiosityCache::Load reads it (radiosity.cpp:909-1010: packed vectors
+// unpacked and normalised, quality 1).
+namespace {
+
+unsigned pack_unit(float v) { return (unsigned)((v + 1.0) * 0.5 * 254.0 + 0.499999); }
+
+double unpack_unit(unsigned u) { return ((double)u * (1.0 / 254.0)) * 2.0 - 1.0; }
+
+void unpack_dir(const char* s, double out[3])
+{
+    unsigned t[3] = {0, 0, 0};
+    std::sscanf(s, "%02x%02x%02x", &t[0], &t[1], &t[2]);
+    double len = 0.0;
+    for (int k = 0; k < 3; k++) {
+        out[k] = unpack_unit(t[k]);
+        len += out[k] * out[k];
+    }
+    len = std::sqrt(len);
+    for (int k = 0; k < 3; k++)
+        out[k] = len > 0.0 ? out[k] / len : 0.0;
+}
+
+}  // namespace
+
+int pov_gpu_cache_save(PovGpuScene* sc, const char* path)
+{
+    if (!sc || !path)
+        return POV_GPU_E_INVALID;
+    std::lock_guard<std::mutex> g(sc->lock);
+    RadiosityState& R = sc->rad;
+    if (!R.enabled)
+        return POV_GPU_E_INVALID;
+    CK(cudaSetDevice(sc->device));
+    if (int bc = begin_call(sc))
+        return bc;
+    cudaStream_t st = sc->active();
+    int nb = 0;
+    CK(cudaMemcpyAsync(&nb, R.count.p, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    HW(st);
+    nb = std::min(nb, R.cap_blocks);
+    std::vector<RadBlock> hb((size_t)std::max(nb, 0));
+    if (nb > 0) {
+        CK(cudaMemcpyAsync(hb.data(), R.blocks.p, sizeof(RadBlock) * (size_t)nb, cudaMemcpyDeviceToHost, st));
+        HW(st);
+    }
+    std::FILE* f = std::fopen(path, "w");
+    if (!f)
+        return POV_GPU_E_INVALID;
+    for (const RadBlock& b : hb) {
+        int depth;
+        std::memcpy(&depth, &b.ill.w, sizeof(int));
+        std::fprintf(f, "C%d\t%g\t%g\t%g\t%02x%02x%02x\t%.4f\t%.4f\t%.4f\t%g\t%g\t%02x%02x%02x\n", depth + 1,
+                     (double)b.p.x, (double)b.p.y, (double)b.p.z, pack_unit(b.n.x), pack_unit(b.n.y), pack_unit(b.n.z),
+                     (double)b.ill.x, (double)b.ill.y, (double)b.ill.z, (double)b.p.w, (double)b.n.w,
+                     pack_unit(b.tn.x), pack_unit(b.tn.y), pack_unit(b.tn.z));
+    }
+    const bool ok = std::ferror(f) == 0;
+    std::fclose(f);
+    return ok ? POV_GPU_OK : POV_GPU_E_INVALID;
+}
+
+int pov_gpu_cache_load(PovGpuScene* sc, const char* path, int32_t* loaded)
+{
+    if (loaded)
+        *loaded = 0;
+    if (!sc)
+        return POV_GPU_E_INVALID;
+    std::lock_guard<std::mutex> g(sc->lock);
+    RadiosityState& R = sc->rad;
+    if (!R.enabled)
+        return POV_GPU_E_INVALID;
+    std::vector<RadBlock> blocks;
+    if (path) {
+        std::FILE* f = std::fopen(path, "r");
+        if (!f)
+            return POV_GPU_E_INVALID;
+        char line[256];
+        while (std::fgets(line, sizeof(line), f)) {
+            if (line[0] != 'C')
+                continue;   // B and P lines carry nothing the cache uses; others are skipped
+            int depth = 0;
+            double p[3], hmd = 0.0, nearest = 0.0;
+            float ill[3];
+            char ns[32], tns[32];
+            if (std::sscanf(line, "C%d %lf %lf %lf %31s %f %f %f %lf %lf %31s", &depth, &p[0], &p[1], &p[2], ns,
+                            &ill[0], &ill[1], &ill[2], &hmd, &nearest, tns) != 11)
+                continue;
+            depth -= 1;   // the file counts bounce depths from 1
+            if (depth < 0 || depth >= RAD_LEVELS)
+                continue;
+            double n[3], tn[3];
+            unpack_dir(ns, n);
+            unpack_dir(tns, tn);
+            RadBlock b;
+            b.p = make_float4((float)p[0], (float)p[1], (float)p[2], (float)hmd);
+            b.n = make_float4((float)n[0], (float)n[1], (float)n[2], (float)nearest);
+            b.tn = make_float4((float)tn[0], (float)tn[1], (float)tn[2], 1.0f);
+            int32_t dbits = depth;
+            float dw;
+            std::memcpy(&dw, &dbits, sizeof(float));
+            b.ill = make_float4(ill[0], ill[1], ill[2], dw);
+            blocks.push_back(b);
+        }
+        std::fclose(f);
+        if ((int)blocks.size() > R.cap_blocks)
+            return POV_GPU_E_CAPACITY;
+    }
+    CK(cudaSetDevice(sc->device));
+    if (int bc = begin_call(sc))
+        return bc;
+    R.loaded.swap(blocks);
+    if (int rc = rad_reset(sc))
+        return rc;
+    if (loaded)
+        *loaded = (int32_t)R.loaded.size();
+    return POV_GPU_OK;
+}
+
+int pov_gpu_set_timeout(PovGpuScene* sc, double seconds)
+{
+    if (!sc || !(seconds >= 0.0) || !std::isfinite(seconds))
+        return POV_GPU_E_INVALID;
+    std::lock_guard<std::mutex> g(sc->lock);
+    sc->timeout_s = seconds;
+    return POV_GPU_OK;
 }
 
 int pov_gpu_scene_set_stream(PovGpuScene* sc, void* cuda_stream)
@@ -2232,6 +2439,8 @@ int pov_gpu_set_camera(PovGpuScene* sc, const PovGpuCamera* cam, const double* l
         }
     }
     std::lock_guard<std::mutex> g(sc->lock);
+    if (int bc = begin_call(sc))
+        return bc;
     // camera rays start outside every media container
     for (size_t c = 0; c + 6 <= sc->h_container_boxes.size(); c += 6) {
         const double* b = &sc->h_container_boxes[c];
@@ -2259,6 +2468,8 @@ int pov_gpu_encode_u8(PovGpuScene* sc, const float* rgbt, int64_t npix, int32_t 
         return POV_GPU_OK;
     std::lock_guard<std::mutex> g(sc->lock);
     CK(cudaSetDevice(sc->device));
+    if (int bc = begin_call(sc))
+        return bc;
     cudaPointerAttributes in{}, oa{};
     CK(cudaPointerGetAttributes(&in, rgbt));
     if (in.type != cudaMemoryTypeDevice && in.type != cudaMemoryTypeManaged)
@@ -2285,7 +2496,7 @@ int pov_gpu_encode_u8(PovGpuScene* sc, const float* rgbt, int64_t npix, int32_t 
     CK(launch_encode_u8(reinterpret_cast<const float4*>(rgbt), (long long)npix, curve, thr, dst, grid, st));
     if (!direct)
         CK(cudaMemcpyAsync(out, dst, (size_t)npix * 3, cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
+    HW(st);
     return POV_GPU_OK;
 }
 
@@ -2322,6 +2533,8 @@ int pov_gpu_trace_blocks(PovGpuScene* sc, const PovGpuBlock* blocks, int32_t num
         return POV_GPU_E_INVALID;
     std::lock_guard<std::mutex> g(sc->lock);
     cudaSetDevice(sc->device);
+    if (int bc = begin_call(sc))
+        return bc;
     if (num_blocks == 0) {
         if (stats)
             std::memset(stats, 0, sizeof(*stats));
@@ -2430,7 +2643,7 @@ int pov_gpu_trace_blocks(PovGpuScene* sc, const PovGpuBlock* blocks, int32_t num
             int hc[2] = {0, 0};
             CK(cudaMemcpyAsync(hc, cnt + C_NS, sizeof(int), cudaMemcpyDeviceToHost, st));
             CK(cudaMemcpyAsync(hc + 1, cnt + C_NN, sizeof(int), cudaMemcpyDeviceToHost, st));
-            CK(cudaStreamSynchronize(st));
+            HW(st);
             const int nsamp = std::min(hc[0], scap);
             if (nsamp > 0) {
                 rc = run_samples(sc, clk, 2, 0, nullptr, sc->spos.as<double2>(), cnt + C_NS, nsamp, params->width,
@@ -2490,6 +2703,8 @@ int pov_gpu_radiosity_pretrace(PovGpuScene* sc, const PovGpuBlock* blocks, int32
     if (!sc->rad.enabled)
         return POV_GPU_E_INVALID;
     cudaSetDevice(sc->device);
+    if (int bc = begin_call(sc))
+        return bc;
     RadiosityState& R = sc->rad;
     const PovGpuRadiosity& rs = R.set;
     // pass sizes (View::StartRender, view.cpp:1060-1080)
@@ -2566,7 +2781,7 @@ int pov_gpu_radiosity_pretrace(PovGpuScene* sc, const PovGpuBlock* blocks, int32
         CK(cudaMemcpyAsync(sc->pos_count.p, &n, sizeof(int), cudaMemcpyHostToDevice, st));
         int rc = run_samples(sc, clk, 2, 0, nullptr, sc->spos.as<double2>(), sc->pos_count.as<int>(), n,
                              params->width, params->height, nullptr, sc->out.as<float4>());
-        CK(cudaStreamSynchronize(st));   // `n` and `pos` must outlive the copies
+        HW(st);   // `n` and `pos` must outlive the copies
         if (rc != POV_GPU_OK)
             return rc;
     }
@@ -2597,7 +2812,7 @@ static_assert(POV_GPU_NIC_PARAMS == nic::NPARAM, "public and internal parameter 
 
 int pov_gpu_set_neural_cache(PovGpuScene* sc, const PovGpuNeuralCache* cfg)
 {
-    if (!sc || !cfg || (cfg->enabled && (cfg->steps < 1 || cfg->batch < 1 || cfg->learning_rate <= 0.0f)))
+    if (!sc || !cfg || (cfg->enabled && (cfg->steps < 1 || cfg->batch < 0 || cfg->learning_rate <= 0.0f)))
         return POV_GPU_E_INVALID;
     std::lock_guard<std::mutex> g(sc->lock);
     if (!sc->rad.enabled)
@@ -2664,17 +2879,19 @@ int pov_gpu_nic_eval(const float* params, const float* bounds, const float* poin
         }
     }
     if (targets) {
+        const int slices = nic::train_slices(n, sms);
         CK(dtg.ensure(sizeof(float4) * (size_t)n));
-        CK(dgrad.ensure(sizeof(float) * NP));
-        CK(dloss.ensure(sizeof(float)));
+        CK(dgrad.ensure(sizeof(float) * NP * (size_t)(slices + 1)));
+        CK(dloss.ensure(sizeof(float) * (size_t)(slices + 1)));
         CK(cudaMemcpy(dtg.p, ht.data(), sizeof(float4) * (size_t)n, cudaMemcpyHostToDevice));
-        CK(cudaMemset(dgrad.p, 0, sizeof(float) * NP));
-        CK(cudaMemset(dloss.p, 0, sizeof(float)));
         io.target = dtg.as<float4>();
+        float* gsum = dgrad.as<float>() + NP * (size_t)slices;   // the summed gradient after the slices
+        float* lsum = dloss.as<float>() + slices;
         CK(nic::launch_train(io, dwb.as<unsigned char>(), dp.as<float>(), dgrad.as<float>(), dloss.as<float>(),
                              1.0f / (float)n, derr.as<uint32_t>(), sms, 0));
-        CK(cudaMemcpy(grad, dgrad.p, sizeof(float) * NP, cudaMemcpyDeviceToHost));
-        CK(cudaMemcpy(loss, dloss.p, sizeof(float), cudaMemcpyDeviceToHost));
+        CK(nic::launch_reduce(dgrad.as<float>(), dloss.as<float>(), slices, gsum, lsum, 0));
+        CK(cudaMemcpy(grad, gsum, sizeof(float) * NP, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(loss, lsum, sizeof(float), cudaMemcpyDeviceToHost));
     }
     uint32_t e = 0;
     CK(cudaMemcpy(&e, derr.p, sizeof(uint32_t), cudaMemcpyDeviceToHost));
@@ -2688,6 +2905,8 @@ int pov_gpu_trace_rays(PovGpuScene* sc, const double* origins, const double* dir
         return POV_GPU_E_INVALID;
     std::lock_guard<std::mutex> g(sc->lock);
     cudaSetDevice(sc->device);
+    if (int bc = begin_call(sc))
+        return bc;
     if (num_rays == 0)
         return POV_GPU_OK;
     cudaStream_t st = sc->active();
@@ -2768,6 +2987,8 @@ int pov_gpu_trace_rays_static(PovGpuScene* sc, const double* origins, const doub
         return POV_GPU_E_CAPACITY;
     std::lock_guard<std::mutex> g(sc->lock);
     CK(cudaSetDevice(sc->device));
+    if (int bc = begin_call(sc))
+        return bc;
     unsigned char* base = nullptr;
     CK(static_ray_scratch(sc->device, &base));   // one-time set-up per device
     if (num_rays == 0)
@@ -2795,7 +3016,7 @@ int pov_gpu_trace_rays_static(PovGpuScene* sc, const double* origins, const doub
     uint32_t errw = 0;
     CK(cudaMemcpyAsync(hits, out, sizeof(PovGpuHit) * n, cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(&errw, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
+    HW(st);
     return errw ? POV_GPU_E_DEVICE : POV_GPU_OK;
 }
 

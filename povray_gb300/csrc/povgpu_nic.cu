@@ -17,7 +17,9 @@
 // the same units: dH = dZ * W (A = dZ tile, B = W^T tile) and
 // dW = dZ^T * H (A = dZ^T tile, M = 128 padded output rows, K = the 128
 // samples, B = H^T tile), the transposed tiles written by the threads.
-// Weight gradients leave through FP32 atomics; an Adam step follows.
+// Each CTA keeps its own gradient slice in global memory (the sum over its
+// tiles, in tile order); the Adam step sums the slices in CTA order, so a
+// training step gives the same parameters on every run.
 #include "povgpu_internal.h"
 #include "povgpu_nic.h"
 #include "povgpu_umma.cuh"
@@ -244,7 +246,10 @@ __global__ void __launch_bounds__(128, 1) k_nic(NicIO io, const unsigned char* _
     const uint32_t s0 = umma::smem_u32(sm);
     uint32_t phase = 0, cphase = 0;
     bool ok = true;
+    // this CTA's gradient slice: its first tile stores, later tiles add
+    float* const gslice = TRAIN ? grad + (size_t)blockIdx.x * NPARAM : nullptr;
     for (int tile = blockIdx.x; tile * TILE < io.n; tile += gridDim.x) {
+        const bool first = tile == (int)blockIdx.x;
         ok &= bulk_load(sm, OFF_W1, wimg, WIMG_FWD, cbar, cphase);   // the forward tiles
         const int i = tile * TILE + t;
         const bool valid = i < io.n;
@@ -370,10 +375,12 @@ __global__ void __launch_bounds__(128, 1) k_nic(NicIO io, const unsigned char* _
             for (int c = 0; c < nin; c += 16) {   // lane t = output row t of dW
                 float v[16];
                 umma::tmem_ld16(tm + lane + 128 + c, v);
-                if (t < nout)
+                if (t < nout) {
+                    float* g = gslice + wofs[l] + t * nin + c;
 #pragma unroll
                     for (int j = 0; j < 16; j++)
-                        atomicAdd(&grad[wofs[l] + t * nin + c + j], v[j]);
+                        g[j] = first ? v[j] : g[j] + v[j];
+                }
             }
             if (l > 0) {
                 const uint64_t m = relu[l - 1];   // the input of layer l is hidden layer l's output
@@ -389,8 +396,10 @@ __global__ void __launch_bounds__(128, 1) k_nic(NicIO io, const unsigned char* _
             umma::fence_before_sync();
             __syncthreads();
             umma::fence_after_sync();
-            if (t < nout)
-                atomicAdd(&grad[bofs[l] + t], sbgrad[t] + sbgrad[HID + t] + sbgrad[2 * HID + t] + sbgrad[3 * HID + t]);
+            if (t < nout) {
+                const float b = sbgrad[t] + sbgrad[HID + t] + sbgrad[2 * HID + t] + sbgrad[3 * HID + t];
+                gslice[bofs[l] + t] = first ? b : gslice[bofs[l] + t] + b;
+            }
             __syncthreads();
         }
     }
@@ -400,20 +409,38 @@ __global__ void __launch_bounds__(128, 1) k_nic(NicIO io, const unsigned char* _
     if (warp == 0)
         umma::tmem_dealloc(tm, MP::TMEM_COLS);
     if (TRAIN && t == 0)
-        atomicAdd(loss, sloss[1] + sloss[2] + sloss[3] + sloss[4]);
+        loss[blockIdx.x] = sloss[1] + sloss[2] + sloss[3] + sloss[4];
     if (!ok && t == 0)
         atomicOr(err, DE_ITERATION_CAP);
 }
 
-// Adam on the FP32 master parameters; refreshes the BF16 copy.  Parameters
-// of the padded output rows stay zero.
+// Sum of parameter i's gradient over the CTA slices in a fixed order: eight
+// running sums over slices b = j (mod 8), then those eight in order.  The
+// eight independent loads per round keep the slice reads in flight.
+__device__ __forceinline__ float slice_sum(const float* __restrict__ parts, int nparts, int i)
+{
+    float g[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    int b = 0;
+    for (; b + 8 <= nparts; b += 8) {
+#pragma unroll
+        for (int j = 0; j < 8; j++)
+            g[j] += __ldcg(parts + (size_t)(b + j) * NPARAM + i);
+    }
+    for (int j = 0; b + j < nparts; j++)
+        g[j] += __ldcg(parts + (size_t)(b + j) * NPARAM + i);
+    return ((g[0] + g[1]) + (g[2] + g[3])) + ((g[4] + g[5]) + (g[6] + g[7]));
+}
+
+// Adam on the FP32 master parameters, the gradient summed from the CTA
+// slices; refreshes the BF16 copy.  Parameters of the padded output rows
+// stay zero.
 __global__ void k_nic_adam(float* __restrict__ params, float* __restrict__ m, float* __restrict__ v,
-                           const float* __restrict__ grad, unsigned char* __restrict__ wimg, float lr, float b1,
-                           float b2, float eps, float c1, float c2)
+                           const float* __restrict__ parts, int nparts, unsigned char* __restrict__ wimg, float lr,
+                           float b1, float b2, float eps, float c1, float c2)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NPARAM; i += gridDim.x * blockDim.x) {
         bool pad = (i >= P_W5 && i < P_B5 && (i - P_W5) / HID >= NOUT) || (i >= P_B5 && i - P_B5 >= NOUT);
-        float g = pad ? 0.0f : grad[i];
+        float g = pad ? 0.0f : slice_sum(parts, nparts, i);
         float mi = b1 * m[i] + (1.0f - b1) * g;
         float vi = b2 * v[i] + (1.0f - b2) * g * g;
         m[i] = mi;
@@ -421,6 +448,20 @@ __global__ void k_nic_adam(float* __restrict__ params, float* __restrict__ m, fl
         float p = pad ? 0.0f : params[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
         params[i] = p;
         wimg_store(wimg, i, p);
+    }
+}
+
+// The gradient and loss of a training launch summed from its CTA slices.
+__global__ void k_nic_reduce(const float* __restrict__ parts, const float* __restrict__ loss_parts, int nparts,
+                             float* __restrict__ grad, float* __restrict__ loss)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NPARAM; i += gridDim.x * blockDim.x)
+        grad[i] = slice_sum(parts, nparts, i);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        float l = 0.0f;
+        for (int b = 0; b < nparts; b++)
+            l += loss_parts[b];
+        *loss = l;
     }
 }
 
@@ -453,6 +494,12 @@ cudaError_t launch_forward(const NicIO& io, const unsigned char* wimg, const flo
     return cudaGetLastError();
 }
 
+int train_slices(int n, int grid)
+{
+    const int tiles = (n + TILE - 1) / TILE;
+    return n <= 0 ? 0 : (grid < tiles ? grid : tiles);
+}
+
 cudaError_t launch_train(const NicIO& io, const unsigned char* wimg, const float* params, float* grad, float* loss,
                          float inv_batch, uint32_t* err, int grid, cudaStream_t st)
 {
@@ -472,12 +519,19 @@ cudaError_t launch_train(const NicIO& io, const unsigned char* wimg, const float
     return cudaGetLastError();
 }
 
-cudaError_t launch_adam(float* params, float* m, float* v, const float* grad, unsigned char* wimg, float lr, int step,
-                        cudaStream_t st)
+cudaError_t launch_adam(float* params, float* m, float* v, const float* grad, int slices, unsigned char* wimg,
+                        float lr, int step, cudaStream_t st)
 {
     const float b1 = 0.9f, b2 = 0.99f, eps = 1e-8f;
     float c1 = 1.0f - powf(b1, (float)step), c2 = 1.0f - powf(b2, (float)step);
-    k_nic_adam<<<(NPARAM + 255) / 256, 256, 0, st>>>(params, m, v, grad, wimg, lr, b1, b2, eps, c1, c2);
+    k_nic_adam<<<(NPARAM + 255) / 256, 256, 0, st>>>(params, m, v, grad, slices, wimg, lr, b1, b2, eps, c1, c2);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_reduce(const float* grad_slices, const float* loss_slices, int slices, float* grad, float* loss,
+                          cudaStream_t st)
+{
+    k_nic_reduce<<<(NPARAM + 255) / 256, 256, 0, st>>>(grad_slices, loss_slices, slices, grad, loss);
     return cudaGetLastError();
 }
 

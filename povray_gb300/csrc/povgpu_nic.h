@@ -47,12 +47,19 @@ constexpr uint32_t WIMG_BYTES = WIMG_FWD + WIMG_BWD;
 size_t smem_bytes(bool train);
 cudaError_t launch_forward(const NicIO& io, const unsigned char* wimg, const float* params, uint32_t* err, int grid,
                            cudaStream_t st);
-// Accumulates the gradient of (1/batch) * sum (p - y)^2 / (p^2 + 0.01) into
-// grad and the loss into *loss.
+// Gradient of (1/batch) * sum (p - y)^2 / (p^2 + 0.01) over io's samples:
+// CTA b writes its part to grad[b * NPARAM ...] and loss[b], for the
+// train_slices(io.n, grid) CTAs the launch uses (the buffers hold that many
+// slices).  Nothing is accumulated across launches.
+int train_slices(int n, int grid);
 cudaError_t launch_train(const NicIO& io, const unsigned char* wimg, const float* params, float* grad, float* loss,
                          float inv_batch, uint32_t* err, int grid, cudaStream_t st);
-cudaError_t launch_adam(float* params, float* m, float* v, const float* grad, unsigned char* wimg, float lr, int step,
-                        cudaStream_t st);
+// Adam step on the gradient summed (in slice order) from `slices` slices.
+cudaError_t launch_adam(float* params, float* m, float* v, const float* grad, int slices, unsigned char* wimg,
+                        float lr, int step, cudaStream_t st);
+// The slices' sum into grad[NPARAM] and *loss.
+cudaError_t launch_reduce(const float* grad_slices, const float* loss_slices, int slices, float* grad, float* loss,
+                          cudaStream_t st);
 cudaError_t launch_to_bf16(const float* params, unsigned char* wimg, cudaStream_t st);
 
 }  // namespace nic

@@ -147,8 +147,11 @@ __device__ void ot_index_sphere(float3 c, double radius, int& size, int& x, int&
 
 // RadiosityCache::AverageNearBlock (radiosity.cpp:1551-1770): pseudo-sigmoid
 // weight for final-trace depth-0 queries, linear otherwise; no gradient.
+// The weight of one block is formed in FP32; the sums of weights and of
+// weighted illuminances accumulate in FP64, as the reference's WT_AVG sums
+// them in DBL (radiosity.cpp:122, 1755-1757).
 __device__ __forceinline__ void average_near(const RadBlock& b, float3 P, float3 N, float eb, bool final_trace,
-                                             float& W, float3& WI)
+                                             double& W, double3& WI)
 {
     float3 bp = xyz(b.p);
     float3 delta = sub(P, bp);
@@ -190,9 +193,11 @@ __device__ __forceinline__ void average_near(const RadBlock& b, float3 P, float3
     if (in_front <= 0.0f)
         w *= 1.0f - in_front / IN_FRONT_LIMIT;
     if (w > RAD_EPSILON) {
-        w *= b.tn.w;
-        WI = add(WI, mul(xyz(b.ill), w));
-        W += w;
+        const double wq = (double)w * (double)b.tn.w;
+        WI.x = fma((double)b.ill.x, wq, WI.x);
+        WI.y = fma((double)b.ill.y, wq, WI.y);
+        WI.z = fma((double)b.ill.z, wq, WI.z);
+        W += wq;
     }
 }
 
@@ -211,10 +216,10 @@ __device__ __forceinline__ uint32_t occ_bit(const RadCacheView& C, unsigned long
 // (ot_point_in_node) -- are dealt to the lanes, each lane walks its nodes'
 // block lists, and the warp sums the weights (every lane gets the sums).
 __device__ void find_reusable_warp(const RadCacheView& C, int smin, int smax, float3 P, float3 N, float eb,
-                                   int depth, bool final_trace, int lane, float& W, float3& WI)
+                                   int depth, bool final_trace, int lane, double& W, double3& WI)
 {
-    W = 0.0f;
-    WI = f3(0.f, 0.f, 0.f);
+    W = 0.0;
+    WI = make_double3(0.0, 0.0, 0.0);
     const float pf[3] = {P.x, P.y, P.z};
     const int ncand = (smax - smin + 1) * 8;
     for (int cand = lane; cand < ncand; cand += 32) {
@@ -267,13 +272,24 @@ __device__ void find_reusable_warp(const RadCacheView& C, int smin, int smax, fl
             }
         }
     }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        W += __shfl_xor_sync(0xffffffffu, W, off);
-        WI.x += __shfl_xor_sync(0xffffffffu, WI.x, off);
-        WI.y += __shfl_xor_sync(0xffffffffu, WI.y, off);
-        WI.z += __shfl_xor_sync(0xffffffffu, WI.z, off);
-    }
+    // FP64 warp sum of the four values as a reduce-scatter: across lane
+    // halves each lane keeps two of the values, across quarters one, then
+    // eight lanes sum that one -- 6 FP64 adds per lane instead of the 20 of
+    // a butterfly on all four (FP64 is a narrow pipe on this part).  The
+    // order of the adds is fixed, so the sums are reproducible.
+    const bool h16 = (lane & 16) != 0, h8 = (lane & 8) != 0;
+    const double s0 = h16 ? W : WI.y, s1 = h16 ? WI.x : WI.z;
+    const double a0 = (h16 ? WI.y : W) + __shfl_xor_sync(0xffffffffu, s0, 16);
+    const double a1 = (h16 ? WI.z : WI.x) + __shfl_xor_sync(0xffffffffu, s1, 16);
+    double b = (h8 ? a1 : a0) + __shfl_xor_sync(0xffffffffu, h8 ? a0 : a1, 8);
+    b += __shfl_xor_sync(0xffffffffu, b, 4);
+    b += __shfl_xor_sync(0xffffffffu, b, 2);
+    b += __shfl_xor_sync(0xffffffffu, b, 1);
+    // lanes 0-7 hold W, 8-15 WI.x, 16-23 WI.y, 24-31 WI.z
+    W = __shfl_sync(0xffffffffu, b, 0);
+    WI.x = __shfl_sync(0xffffffffu, b, 8);
+    WI.y = __shfl_sync(0xffffffffu, b, 16);
+    WI.z = __shfl_sync(0xffffffffu, b, 24);
 }
 
 __device__ __forceinline__ float4 finish_ambient(float3 a, float quality, const RadParams& R)
@@ -352,20 +368,23 @@ __global__ void k_rad_query(DeviceScene S, RadCacheView C, RadParams R, const Ra
         if (q.p.w < WEIGHT_ERROR_BOUND_OFFSET)
             eb += WEIGHT_ERROR_BOUND_OFFSET - q.p.w;
         eb *= R.error_bound_factor;
-        float W = 0.f;
-        float3 WI = f3(0.f, 0.f, 0.f);
+        double W = 0.0;
+        double3 WI = make_double3(0.0, 0.0, 0.0);
         if (smax >= smin)
             find_reusable_warp(C, smin, smax, P, N, eb, R.depth, R.final_trace != 0, lane, W, WI);
         if (lane != 0)
             continue;
-        bool reuse = W * 4.0f >= (float)R.reuse_count || (R.final_trace && !R.always_sample && W > 0.0f);
+        bool reuse = W * 4.0 >= (double)R.reuse_count || (R.final_trace && !R.always_sample && W > 0.0);
         if (reuse) {
-            float3 a = mul(WI, 1.0f / W);
-            out[qi] = finish_ambient(a, fminf(4.0f * W / (float)R.reuse_count, 1.0f), R);
+            // the weighted mean formed from the FP64 sums, then kept in
+            // single precision like the reference's ambient colour
+            const double inv = 1.0 / W;
+            float3 a = f3((float)(WI.x * inv), (float)(WI.y * inv), (float)(WI.z * inv));
+            out[qi] = finish_ambient(a, (float)fmin(4.0 * W / (double)R.reuse_count, 1.0), R);
             reused++;
             continue;
         }
-        partial[qi] = make_float4(WI.x, WI.y, WI.z, W);
+        partial[qi] = make_float4((float)WI.x, (float)WI.y, (float)WI.z, (float)W);
         bool seed = round >= last_round;
         if (!seed) {
             // cell of this round: the largest reuse radius halved per round,
@@ -559,6 +578,43 @@ __global__ void k_gather_reduce(DeviceScene S, RadCacheView C, RadParams R, cons
     }
 }
 
+// Blocks written by the host (a loaded cache file, RadiosityCache::Load,
+// radiosity.cpp:909-1010, which AddBlock's every line) filed as
+// k_gather_reduce files a new sample: the quick-test record, the node
+// ot_index_sphere picks for the harmonic mean distance times the depth's
+// address factor, the node's occupancy bit and the depth's node-size range.
+struct AddressFactors {
+    float f[RAD_LEVELS];
+};
+
+__global__ void k_rad_file(RadCacheView C, AddressFactors af, int first, int n, uint32_t* err)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int b = first + i;
+        if (b >= C.cap)
+            break;
+        const RadBlock blk = C.blocks[b];
+        const int depth = __float_as_int(blk.ill.w);
+        C.quick[b] = blk.p;
+        C.bslot[b] = -1;
+        if (depth < 0 || depth >= RAD_LEVELS)
+            continue;
+        int size, x, y, z;
+        ot_index_sphere(xyz(blk.p), (double)blk.p.w * af.f[depth], size, x, y, z);
+        const unsigned long long key = node_key(size + 256 * depth, x, y, z);
+        const int slot = node_insert(C, key);
+        if (slot < 0) {
+            atomicOr(err, DE_CACHE_FULL);
+            continue;
+        }
+        C.bslot[b] = slot;
+        const uint32_t bit = occ_bit(C, key);
+        atomicOr(&C.occupancy[bit >> 5], 1u << (bit & 31));
+        atomicMin(&C.size_range[2 * depth], size);
+        atomicMax(&C.size_range[2 * depth + 1], size);
+    }
+}
+
 __global__ void k_rad_nic_answer(RadParams R, const int* __restrict__ seeds, int ns, const float4* __restrict__ pred,
                                  float4* __restrict__ out, unsigned long long* __restrict__ rstats)
 {
@@ -621,6 +677,18 @@ cudaError_t launch_rad_apply(const RadQuery* queries, const int* n_queries, int 
                              PathState* paths, float* quality, int grid, cudaStream_t st)
 {
     k_rad_apply<<<grid, 256, 0, st>>>(queries, n_queries, cap, amb, paths, quality);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rad_file(const RadCacheView& C, const float* address_factor, int first, int n, uint32_t* err,
+                            cudaStream_t st)
+{
+    if (n <= 0)
+        return cudaSuccess;
+    AddressFactors af;
+    for (int d = 0; d < RAD_LEVELS; d++)
+        af.f[d] = address_factor[d];
+    k_rad_file<<<cdiv(n, 256), 256, 0, st>>>(C, af, first, n, err);
     return cudaGetLastError();
 }
 

@@ -6,6 +6,7 @@
 namespace povgpu {
 
 constexpr int RAD_DIRECTIONS = 1600;   // RADIOSITY_MAX_SAMPLE_DIRECTIONS (radiosity.h:78)
+constexpr int RAD_LEVELS = 4;          // bounce depths with their own buffers and cache nodes
 
 // Radiosity counters (device, uint64).
 enum RadStatIdx {
@@ -32,6 +33,11 @@ cudaError_t launch_gather_rays(const RadQuery* queries, const int* seeds, int ns
 cudaError_t launch_first_hit(const QHit* hits, const int* q_count, int cap, float* first_t, int grid, cudaStream_t st);
 cudaError_t launch_rad_apply(const RadQuery* queries, const int* n_queries, int cap, const float4* amb,
                              PathState* paths, float* quality, int grid, cudaStream_t st);
+// Files blocks [first, first + n) of the cache, written there by the host
+// (a loaded cache file), into their octree nodes; address_factor[d] is
+// bounce depth d's (RadParams::address_factor).
+cudaError_t launch_rad_file(const RadCacheView& C, const float* address_factor, int first, int n, uint32_t* err,
+                            cudaStream_t st);
 // Answers of the neural cache (pred[i] for query seeds[i]) into out[].
 cudaError_t launch_rad_nic_answer(const RadParams& R, const int* seeds, int ns, const float4* pred, float4* out,
                                   unsigned long long* rstats, int grid, cudaStream_t st);

@@ -81,12 +81,19 @@ class GpuScene:
                "pov_gpu_radiosity_pretrace")
         return stats.as_dict()
 
-    def set_neural_cache(self, enabled=True, steps=300, batch=4096, learning_rate=3e-3, gate=0.5, seed=1,
+    def set_neural_cache(self, enabled=True, steps=64, batch=None, learning_rate=1e-2, gate=None, seed=1,
                          shared=False):
         """Neural irradiance cache (pov_gpu_set_neural_cache): trained at the
         end of each pretrace; answers uncovered final-trace queries when its
-        held-out relative RMSE is at most `gate`.  `shared`: one network for
-        all views, each pretrace training it further."""
+        held-out relative RMSE is at most `gate` (None: the scene's radiosity
+        error_bound).  `batch` None: one 128-sample tile per SM of the
+        device.  `shared`: one network for all views, each pretrace training
+        it further."""
+        if gate is None:
+            rs = self.scene.radiosity_settings() if self.scene.radiosity is not None else {"error_bound": 0.5}
+            gate = rs["error_bound"]
+        if batch is None:
+            batch = 0
         c = abi.PovGpuNeuralCache(int(enabled), int(steps), int(batch), float(learning_rate), float(gate), int(seed),
                                   int(shared))
         _check(self.lib.pov_gpu_set_neural_cache(self.h, C.byref(c)), "pov_gpu_set_neural_cache")
@@ -148,6 +155,24 @@ class GpuScene:
             merge = {"device_error": lambda a, b: a | b, "nic_val_error_ppm": max}
             stats = {k: merge.get(k, lambda a, b: a + b)(stats[k], pre[k]) for k in stats}
         return _scenes.unblock(rgbt, blocks, p.width, p.height), stats
+
+    def cache_save(self, path):
+        """Writes the radiosity sample cache as a .rca file (pov_gpu_cache_save)."""
+        _check(self.lib.pov_gpu_cache_save(self.h, str(path).encode()), "pov_gpu_cache_save")
+
+    def cache_load(self, path):
+        """Loads a .rca file (pov_gpu_cache_load); its samples start every
+        following frame's cache.  None forgets a loaded file.  Returns the
+        number of samples read."""
+        n = C.c_int32(0)
+        _check(self.lib.pov_gpu_cache_load(self.h, None if path is None else str(path).encode(), C.byref(n)),
+               "pov_gpu_cache_load")
+        return n.value
+
+    def set_timeout(self, seconds):
+        """Host wait limit of this scene's calls (pov_gpu_set_timeout); a
+        call that runs out raises PovGpuError with POV_GPU_E_TIMEOUT."""
+        _check(self.lib.pov_gpu_set_timeout(self.h, float(seconds)), "pov_gpu_set_timeout")
 
     def set_stream(self, stream_handle):
         """Launch on a caller-owned cudaStream_t (int handle, 0 = own stream)."""

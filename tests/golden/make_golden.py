@@ -21,7 +21,11 @@ output (+AM2, jitter off):
                Shadow Ray Tests, Succeeded)
 Radiosity cases (radiosity_cases) hold the reference CLI's own radiosity
 renders instead (run_radiosity), and pretrace_jitter.npy the pretrace jitter
-table of the reference's radiosity task.
+table of the reference's radiosity task.  <case>.pgsf.gz (SCENE_FILE_CASES)
+is the reference parser's SceneData of the case flattened into the C ABI's
+scene description (write_scene_files; format in povray_gb300/scenefile.py),
+and radiosity_room_160x90.rca.gz the reference CLI's own radiosity cache
+file of that room (write_radiosity_cache_file, +RFO).
 The cases are small so the fixtures stay around a megabyte.
 """
 import json
@@ -219,6 +223,53 @@ def run_radiosity(case, scene, tmp):
     print(case, out["rad_stats_wt1"])
 
 
+def write_radiosity_cache_file(tmp, case="radiosity_room_160x90"):
+    """The reference CLI's own radiosity cache file (+RFO, one thread) of
+    the golden room -> <case>.rca.gz: every sample its pretrace and final
+    trace gathered, in the .rca text format (ot_write_block,
+    source/core/support/octree.cpp:1345-1370)."""
+    import gzip
+    scene = radiosity_cases()[case]
+    pov = os.path.join(tmp, case + ".pov")
+    with open(pov, "w") as f:
+        f.write(scene.sdl())
+    rca = os.path.join(tmp, case + ".rca")
+    hdr = os.path.join(tmp, case + "_rfo.hdr")
+    r = subprocess.run([POVRAY_REF, "+I" + pov, "+W%d" % scene.width, "+H%d" % scene.height, "-D", "+FH", "-A",
+                        "+WT1", "+RFO", "+RF" + rca, "+O" + hdr], capture_output=True, text=True, cwd=tmp)
+    if r.returncode != 0:
+        raise RuntimeError(r.stderr[-2000:])
+    with open(rca, "rb") as f, gzip.GzipFile(os.path.join(HERE, case + ".rca.gz"), "wb", mtime=0) as g:
+        data = f.read()
+        g.write(data)
+    print(case, "cache file:", data.count(b"\nC") + data.startswith(b"C"), "samples")
+
+
+SCENE_FILE_CASES = ("spheres_plane_320x240", "mesh_spheres_small_160x90", "csg_torus_grid_160x90",
+                    "area_room_160x90", "media_spheres_160x120", "radiosity_room_160x90")
+
+
+def write_scene_files(tmp):
+    """The reference's parse of each case flattened into the C ABI's scene
+    description (pov_oracle ... desc: oracle/refbuild/pov_flatten.cpp walks
+    the SceneData the reference's parser built) -> <case>.pgsf.gz.  Cases
+    with pattern pigments or normals are not flattened by it."""
+    import gzip
+    allc = dict((k, v[0]) for k, v in cases().items())
+    allc.update(radiosity_cases())
+    for case in SCENE_FILE_CASES:
+        scene = allc[case]
+        pov = os.path.join(tmp, case + ".pov")
+        with open(pov, "w") as f:
+            f.write(scene.sdl())
+        raw = os.path.join(tmp, case + ".pgsf")
+        subprocess.run([POV_ORACLE, pov, str(scene.width), str(scene.height), "desc", raw], check=True,
+                       capture_output=True)
+        with open(raw, "rb") as f, gzip.GzipFile(os.path.join(HERE, case + ".pgsf.gz"), "wb", mtime=0) as g:
+            g.write(f.read())
+        print(case, "scene file")
+
+
 def write_jitter_table():
     """RadiosityTask's pretrace jitter table (RandomDoubleSequence(-1,1,2047),
     radiositytask.cpp:99) as the reference generates it."""
@@ -233,6 +284,12 @@ def main():
         sys.exit("build the reference first: make -C oracle/refbuild")
     if len(sys.argv) == 1 or "pretrace_jitter" in sys.argv[1:]:
         write_jitter_table()
+    if len(sys.argv) == 1 or "scene_files" in sys.argv[1:]:
+        with tempfile.TemporaryDirectory() as tmp:
+            write_scene_files(tmp)
+    if len(sys.argv) == 1 or "radiosity_cache_file" in sys.argv[1:]:
+        with tempfile.TemporaryDirectory() as tmp:
+            write_radiosity_cache_file(tmp)
     with tempfile.TemporaryDirectory() as tmp:
         for case, scene in radiosity_cases().items():
             if len(sys.argv) > 1 and case not in sys.argv[1:]:

@@ -266,3 +266,12 @@ def test_oracle_rejects_the_same_scenes():
     bad.materials[1].normal.accuracy = 0.0           # the slope's delta must be positive
     with pytest.raises(abi.PovGpuError):
         Oracle(bad)
+
+
+def test_timeout_argument_validation(gpu_lib):
+    """pov_gpu_set_timeout validates on the host before touching the device:
+    no scene, a negative or a non-finite limit are POV_GPU_E_INVALID."""
+    assert gpu_lib.pov_gpu_set_timeout(None, 1.0) == abi.POV_GPU_E_INVALID
+    assert gpu_lib.pov_gpu_set_timeout(None, -1.0) == abi.POV_GPU_E_INVALID
+    assert gpu_lib.pov_gpu_set_timeout(None, float("nan")) == abi.POV_GPU_E_INVALID
+    assert b"wait limit" in gpu_lib.pov_gpu_error_string(abi.POV_GPU_E_TIMEOUT)

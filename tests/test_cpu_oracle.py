@@ -159,3 +159,55 @@ def test_oracle_radiosity_matches_reference_single_thread_render():
     floor = np.sqrt(((g["rad_pixels_wt8"] - ref) ** 2).mean()) / ref.mean()
     assert rel < 0.005 and rel < 0.2 * floor, (rel, floor)
     assert np.abs(a - ref).max() < 0.01
+
+
+def _grid(width, height, stride):
+    ys, xs = np.mgrid[stride // 2:height:stride, stride // 2:width:stride]
+    return np.stack([xs.ravel(), ys.ravel()], 1)
+
+
+def test_converged_radiosity_agrees_with_reference_render():
+    """The oracle's converged mode (every radiosity query gathered without
+    the cache, 256 / 16 stratified rays at depth 0 / 1, FP64 sums) against
+    the reference's own one-thread radiosity render of the golden room:
+    the means agree within 1%, and the converged image is closer to the
+    reference's render than the reference's own 8-thread render is (the
+    reference's sampling-and-reuse error is the larger one)."""
+    from tests.golden.make_golden import radiosity_cases
+    scene = radiosity_cases()["radiosity_room_160x90"]
+    g = _load("radiosity_room_160x90")
+    px = _grid(scene.width, scene.height, 4)
+    out, _ = Oracle(scene).render_converged(px, (256, 16), seed=1)
+    a = out[:, :3]
+    r1 = g["rad_pixels_wt1"][px[:, 1], px[:, 0]]
+    r8 = g["rad_pixels_wt8"][px[:, 1], px[:, 0]]
+
+    def rel(x, y):
+        return float(np.sqrt(((x - y) ** 2).mean()) / y.mean())
+    info = dict(mean_ratio=float(a.mean() / r1.mean()), gt_ref1=rel(r1, a), ref8_ref1=rel(r8, r1))
+    assert abs(a.mean() / r1.mean() - 1.0) < 0.01, info
+    assert rel(r1, a) < rel(r8, r1), info
+
+
+def test_converged_radiosity_is_thread_count_invariant():
+    scene = scenes.radiosity_room(64, 36, n_spheres=20, count=50)
+    px = _grid(64, 36, 6)
+    o = Oracle(scene)
+    a, _ = o.render_converged(px, (64, 4), seed=3, threads=1)
+    b, _ = o.render_converged(px, (64, 4), seed=3, threads=4)
+    c, _ = o.render_converged(px, (64, 4), seed=4, threads=4)
+    assert np.array_equal(a, b)
+    assert not np.array_equal(a, c)
+
+
+def test_converged_truth_fixture_reproduces():
+    """A few pixels of the committed FP64 truth of the 1280x720 room
+    (tests/golden/make_converged.py) rendered again: the same values (the
+    per-pixel random sequences depend only on the seed and the pixel)."""
+    t = np.load(os.path.join(GOLDEN, "radiosity_room_converged_1280x720.npz"))
+    info = json.loads(str(t["info"]))
+    scene = scenes.radiosity_room(1280, 720)
+    pick = np.arange(0, len(t["pixels"]), 997)
+    out, _ = Oracle(scene).render_converged(t["pixels"][pick], info["counts"], seed=info["seed"])
+    assert np.allclose(out[:, :3], t["rgb"][pick], rtol=1e-5, atol=1e-7)
+    assert info["noise_rel_rmse"] < 0.005

@@ -1,0 +1,109 @@
+"""The drop-in boundary from the reference side: the reference's own parse
+of each golden scene, flattened into the C ABI's scene description by the
+reference-side flattener (oracle/refbuild/pov_flatten.cpp, compiled against
+the reference's headers; dumped by tests/golden/make_golden.py as
+<case>.pgsf.gz), against the description the project's scene generator
+(povray_gb300/scenes.py) builds for the same SDL, field by field.
+
+Tolerances (written here, applied below):
+  ids, counts, types, flags, links   exact
+  camera vectors                     1e-15 relative (the parser's FP64 math)
+  object parameters, transforms      1e-12
+  material, light and media floats   1e-7 (single-precision fields)
+  mesh vertices and indices          exact; normals 1e-6 (the parser
+                                     normalises normal_vectors in FP64 and
+                                     stores them as floats)
+Materials are compared per object after resolving inheritance (a CSG
+child without a texture takes its parent's, Parser::Post_Process,
+parser.cpp:9025-9030), because the two sides number shared textures
+differently.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+from povray_gb300 import abi
+from povray_gb300.scenefile import ParsedScene
+from tests.golden.make_golden import SCENE_FILE_CASES, cases, radiosity_cases
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _scenes():
+    allc = dict((k, v[0]) for k, v in cases().items())
+    allc.update(radiosity_cases())
+    return allc
+
+
+def _close(tag, x, y, tol, skip=()):
+    for name, _ in x._fields_:
+        if name in skip:
+            continue
+        a, b = getattr(x, name), getattr(y, name)
+        if isinstance(a, C._Pointer):
+            continue
+        av = np.array(a[:] if hasattr(a, "__len__") else a, dtype=float)
+        bv = np.array(b[:] if hasattr(b, "__len__") else b, dtype=float)
+        assert av.shape == bv.shape and np.allclose(av, bv, rtol=tol, atol=tol), (tag, name, av, bv)
+
+
+def _material_of(d, i):
+    o = d.objects[i]
+    while o.material < 0 and o.parent >= 0:
+        o = d.objects[o.parent]
+    return o.material
+
+
+@pytest.mark.parametrize("case", SCENE_FILE_CASES)
+def test_reference_flattened_scene_equals_generator_desc(case):
+    scene = _scenes()[case]
+    a, _keep = scene.desc()
+    ps = ParsedScene(os.path.join(GOLDEN, case + ".pgsf.gz"), scene.width, scene.height)
+    b, _keep2 = ps.desc()
+    _close("camera", a.camera, b.camera, 1e-15)
+    for k in ("max_trace_level", "language_version", "num_objects", "num_lights", "num_meshes", "num_medias",
+              "num_patterns", "num_normals"):
+        assert getattr(a, k) == getattr(b, k), k
+    assert abs(a.adc_bailout - b.adc_bailout) <= 1e-9
+    assert list(a.background) == list(b.background)
+    assert list(a.ambient_light) == list(b.ambient_light)
+    assert a.radiosity.enabled == b.radiosity.enabled
+    if a.radiosity.enabled:
+        _close("radiosity", a.radiosity, b.radiosity, 1e-12)
+    for i in range(a.num_objects):
+        oa, ob = a.objects[i], b.objects[i]
+        for k in ("type", "flags", "parent", "first_child", "num_children", "mesh", "media"):
+            assert getattr(oa, k) == getattr(ob, k), (i, k, getattr(oa, k), getattr(ob, k))
+        assert np.allclose(oa.p[:], ob.p[:], rtol=1e-12, atol=1e-12), (i, oa.p[:], ob.p[:])
+        assert np.allclose(oa.trans[:], ob.trans[:], rtol=1e-12, atol=1e-12), i
+        ma, mb = _material_of(a, i), _material_of(b, i)
+        assert (ma >= 0) == (mb >= 0), i
+        if ma >= 0:
+            _close("material of object %d" % i, a.materials[ma], b.materials[mb], 1e-7)
+    for i in range(a.num_lights):
+        _close("light %d" % i, a.lights[i], b.lights[i], 1e-7)
+    for i in range(a.num_medias):
+        _close("media %d" % i, a.medias[i], b.medias[i], 1e-7)
+    for i, m in enumerate(scene.meshes):
+        pm = ps.meshes[i]
+        assert np.array_equal(m.vertices.ravel(), pm["vertices"])
+        assert np.array_equal(m.faces.ravel(), pm["faces"])
+        if m.normals is not None:
+            assert np.allclose(m.normals.ravel(), pm["normals"], atol=1e-6)
+            assert np.array_equal(m.faces.ravel(), pm["normal_indices"])
+
+
+def test_scene_file_rejects_damage(tmp_path):
+    src = os.path.join(GOLDEN, "spheres_plane_320x240.pgsf.gz")
+    import gzip
+    data = gzip.open(src, "rb").read()
+    bad = tmp_path / "bad.pgsf"
+    bad.write_bytes(data[:-5])
+    with pytest.raises(ValueError):
+        ParsedScene(str(bad), 320, 240)
+    bad.write_bytes(b"XXXX" + data[4:])
+    with pytest.raises(ValueError):
+        ParsedScene(str(bad), 320, 240)
+    assert abi.POV_GPU_ABI_VERSION == 1

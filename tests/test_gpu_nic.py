@@ -15,7 +15,7 @@ import numpy as np
 import pytest
 import torch
 
-from povray_gb300 import GpuScene, abi, scenes
+from povray_gb300 import abi
 from povray_gb300.render import nic_eval
 
 pytestmark = pytest.mark.gpu
@@ -142,25 +142,12 @@ def test_gradient_matches_torch_autograd(data):
     assert rel <= 5e-2, info
 
 
-def test_neural_cache_trains_and_answers_in_the_room():
-    """Trained on the pretrace samples, the network's held-out error is
-    reported, and with it answering the final trace's uncovered queries the
-    image keeps the gather-only render's mean within 3%; its RMSE distance
-    stays under 20% (the gather-only renders' own distance is about 6%: the
-    network's answers are smoother and coarser than gathered samples)."""
-    s = scenes.radiosity_room(320, 180, count=100)
-    base = GpuScene(s)
-    ref, rst = base.render()
-    nicg = GpuScene(s)
-    nicg.set_neural_cache(True, steps=300, batch=4096, gate=1.0)
-    img, st = nicg.render()
-    a, b = img[..., :3], ref[..., :3]
-    rel = float(np.sqrt(((a - b) ** 2).mean()) / b.mean())
-    info = json.dumps(dict(rel=rel, mean_ratio=float(a.mean() / b.mean()), gpu=st, base=rst))
-    assert st["device_error"] == 0, info
-    # held-out error against noisy gathered samples: far below the untrained
-    # network's (several times the mean), not near zero
-    assert 0 < st["nic_val_error_ppm"] < 900000, info
-    assert st["nic_answers"] > 0, info
-    assert abs(a.mean() / b.mean() - 1) < 0.03, info
-    assert rel < 0.20, info
+def test_gradient_is_reproducible(data):
+    """Each CTA keeps its own gradient slice and the slices are summed in a
+    fixed order: the same samples give bit-identical gradients and loss."""
+    pts, nrm, bounds, tgt = data
+    params = _params(3)
+    _, g1, l1 = nic_eval(params, bounds, pts, nrm, tgt)
+    _, g2, l2 = nic_eval(params, bounds, pts, nrm, tgt)
+    assert np.array_equal(g1, g2)
+    assert l1 == l2

@@ -18,7 +18,8 @@ import pytest
 
 from oracle.pyoracle import Oracle
 from povray_gb300 import GpuScene, scenes
-from tests.golden.make_golden import cases
+from povray_gb300.scenefile import ParsedScene
+from tests.golden.make_golden import SCENE_FILE_CASES, cases
 from tests.parity import compare_hits, compare_pixels
 from povray_gb300.encode import to_u8
 
@@ -76,6 +77,25 @@ def _no_aa(scene):
     p.antialias = 0
     p.sampling_method = 1
     return p
+
+
+@pytest.mark.parametrize("case", [c for c in SCENE_FILE_CASES if c in CASES])
+def test_reference_parsed_scene_renders_unchanged(case):
+    """The reference's own parse of the scene, flattened by the
+    reference-side flattener (tests/golden/<case>.pgsf.gz), rendered through
+    the library: the reference's TracePixel pixels (>= 99.9% of channels
+    within 1 LSB) and counters, and the same image as the project's scene
+    generator gives for the same SDL (within 1e-5: mesh normals are the
+    parser's floats)."""
+    scene = CASES[case][0]
+    g = _load(case)
+    parsed = ParsedScene(os.path.join(GOLDEN, case + ".pgsf.gz"), scene.width, scene.height)
+    img, st = GpuScene(parsed).render(params=_no_aa(scene))
+    c = compare_pixels(img, g["pixels"])
+    assert c["within_1lsb"] >= PIX_FRAC, c
+    _counters_close(st, json.loads(str(g["stats"])))
+    gen, _ = GpuScene(scene).render(params=_no_aa(scene))
+    assert float(np.abs(img - gen).max()) <= 1e-5
 
 
 @pytest.mark.parametrize("case", sorted(CASES))
@@ -204,3 +224,32 @@ def test_scene_without_finite_objects():
     img, _ = GpuScene(s).render()
     ref, _ = Oracle(s).render(threads=1)
     assert compare_pixels(img, ref)["within_1lsb"] >= PIX_FRAC
+
+
+def test_host_timeout_returns_and_the_next_call_recovers():
+    """pov_gpu_set_timeout: with a limit far below the frame's time the call
+    returns POV_GPU_E_TIMEOUT (its work stays queued; its output buffer is
+    kept alive here, as the header asks); the next call without a limit
+    waits for that work and renders the same image as a call that never
+    timed out."""
+    from povray_gb300 import abi
+    # media and reflection: the host reads queue counts between launches,
+    # so it waits while device work is still running
+    scene = scenes.media_spheres(640, 480)
+    gpu = GpuScene(scene)
+    blocks = scenes.blocks_for(scene.width, scene.height)
+    ref = np.empty((scene.width * scene.height, 4), dtype=np.float32)
+    gpu.trace_blocks(blocks, out=ref)
+    kept = np.empty_like(ref)
+    gpu.set_timeout(1e-6)
+    with pytest.raises(abi.PovGpuError) as e:
+        gpu.trace_blocks(blocks, out=kept)
+    assert e.value.status == abi.POV_GPU_E_TIMEOUT
+    gpu.set_timeout(0.0)
+    again = np.empty_like(ref)
+    gpu.trace_blocks(blocks, out=again)
+    assert np.array_equal(again, ref)
+    gpu.set_timeout(60.0)   # a generous limit changes nothing
+    gpu.trace_blocks(blocks, out=again)
+    assert np.array_equal(again, ref)
+    del kept

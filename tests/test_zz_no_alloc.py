@@ -2,7 +2,9 @@
 pov_gpu_trace_rays on the same rays, called through the C-ABI.
 
 Named to be collected last, so that it runs both after every other test
-(device memory already used by other scenes) and alone.
+(device memory already used by other scenes) and alone.  Besides the
+results, it checks the property the entry exists for: the device's free
+memory does not change across its calls.
 
 Tolerances: object and triangle ids exact; depths within 1e-5 relative
 (the parity tests' depth tolerance).
@@ -51,20 +53,33 @@ def _same(got, ref):
     assert np.all(got["t"][~hit] == 0.0)
 
 
+def _free_bytes():
+    import torch
+    torch.cuda.synchronize()
+    return torch.cuda.mem_get_info()[0]
+
+
 @pytest.mark.parametrize("make", [
     lambda: scenes.csg_torus_grid(96, 54, n=4, antialias=None),   # sphere, plane, box, torus, CSG
     lambda: scenes.mesh_spheres(96, 54, mesh_n=24, n_spheres=8),   # triangles
 ], ids=["csg_torus_grid", "mesh_spheres"])
 def test_static_matches_trace_rays_twice(make):
+    """The fixed-scratch query runs before any pov_gpu_trace_rays call on the
+    scene (so it cannot lean on that call's buffers), leaves the device's
+    free memory unchanged across two calls, and agrees with
+    pov_gpu_trace_rays on both."""
     scene = make()
     gpu = GpuScene(scene)
     # one-time set-up on this device (n = 0 does only that)
     assert gpu.lib.pov_gpu_trace_rays_static(gpu.h, None, None, 0, None) == abi.POV_GPU_OK
     o, d = _rays(scene, 20000, seed=7)
-    ref = gpu.trace_rays(o, d)
-    assert (ref["object"] >= 0).sum() > 0.2 * len(ref)
+    _static(gpu, o[:64], d[:64])   # first launches of its kernels (CUDA loads them lazily)
+    free0 = _free_bytes()
     first = _static(gpu, o, d)
     second = _static(gpu, o, d)
+    assert _free_bytes() == free0
+    ref = gpu.trace_rays(o, d)
+    assert (ref["object"] >= 0).sum() > 0.2 * len(ref)
     _same(first, ref)
     _same(second, ref)
 
