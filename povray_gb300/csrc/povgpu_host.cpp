@@ -532,7 +532,7 @@ struct PovGpuScene {
     int         num_sms = 148;
     // persistent scene data
     DevBuf nodes, refs, tri_v0, tri_e1, tri_e2, tri_global, tri_shade, tri_normal, tri_local, normals;
-    DevBuf spheres, spheres64, boxes64, sphere_obj, sphere_flags, planes, plane_obj, boxes, tori, csgs, csg_children, objects,
+    DevBuf spheres, spheres64, boxes64, sphere_obj, sphere_flags, planes, plane_obj, boxes, tori, tori32, csgs, csg_children, objects,
         materials, lights, medias, patterns, tnormals, noise_hash, noise_rtab, noise_perm, noise_grad, noise_waves;
     DevBuf encode_buf;     // staging of pov_gpu_encode_u8 for host outputs
     int    media_ni = 0;   // interval slots per media segment (0: no media containers)
@@ -572,6 +572,12 @@ struct PovGpuScene {
     std::chrono::steady_clock::time_point deadline{};
     bool         pending = false;
     cudaEvent_t  wait_event = nullptr;
+    // pinned host words the host reads device counts and statistics into:
+    // a copy into pageable memory would block the host until the device is
+    // done, without the wait limit
+    unsigned char* pinned = nullptr;
+    static constexpr size_t PIN_BYTES = 4096, PIN_ERR = 256, PIN_STATS = 512, PIN_WORK = 1536;
+    int* pin_int(int k) { return reinterpret_cast<int*>(pinned) + k; }
 
     void release_all()
     {
@@ -581,8 +587,11 @@ struct PovGpuScene {
         if (wait_event)
             cudaEventDestroy(wait_event);
         wait_event = nullptr;
+        if (pinned)
+            cudaFreeHost(pinned);
+        pinned = nullptr;
         DevBuf* all[] = {&nodes, &refs, &tri_v0, &tri_e1, &tri_e2, &tri_global, &tri_shade, &tri_normal, &tri_local,
-                         &normals, &spheres, &spheres64, &boxes64, &sphere_obj, &sphere_flags, &planes, &plane_obj, &boxes, &tori, &csgs,
+                         &normals, &spheres, &spheres64, &boxes64, &sphere_obj, &sphere_flags, &planes, &plane_obj, &boxes, &tori, &tori32, &csgs,
                          &csg_children, &objects, &materials, &lights, &blocks, &block_off, &corner_off, &qA,
                          &hits, &out, &counters, &stats, &err, &rays_in, &t64, &corners, &aa_grid, &aa_mask,
                          &aa_subdiv, &aa_xy, &cellsA, &cellsB, &spos, &sslot, &wcount, &pos_count, &medias,
@@ -1319,6 +1328,18 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
     CK(upload(sc->plane_obj, B.plane_obj));
     CK(upload(sc->boxes, B.boxes));
     CK(upload(sc->tori, B.tori));
+    {
+        // FP32 copy of each torus's local frame for the pre-cull: the rows
+        // giving local x, y and z (p' = p * M of the inverse), then R, r
+        std::vector<float4> t32(std::max<size_t>(B.tori.size(), 1) * 4);
+        for (size_t i = 0; i < B.tori.size(); i++) {
+            const double* m = B.tori[i].inv;
+            for (int c = 0; c < 3; c++)
+                t32[4 * i + c] = make_float4((float)m[c], (float)m[3 + c], (float)m[6 + c], (float)m[9 + c]);
+            t32[4 * i + 3] = make_float4((float)B.tori[i].R, (float)B.tori[i].r, 0.f, 0.f);
+        }
+        CK(upload(sc->tori32, t32));
+    }
     CK(upload(sc->csgs, B.csgs));
     CK(upload(sc->csg_children, B.csg_children));
     // one DevMedia per container: its media and its box primitive
@@ -1430,6 +1451,7 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
     S.num_planes = (int)B.planes.size();
     S.boxes = sc->boxes.as<DevBox>();
     S.tori = sc->tori.as<DevTorus>();
+    S.tori32 = sc->tori32.as<float4>();
     S.csgs = sc->csgs.as<DevCsg>();
     S.csg_children = sc->csg_children.as<DevCsgChild>();
     S.has_full_prims = (!B.tori.empty() || !B.csgs.empty()) ? 1 : 0;
@@ -1514,13 +1536,20 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
 }
 
 
+static_assert(PovGpuScene::PIN_STATS + sizeof(unsigned long long) * ST_COUNT <= PovGpuScene::PIN_WORK &&
+                  PovGpuScene::PIN_WORK + 8 * sizeof(unsigned long long) <= PovGpuScene::PIN_BYTES,
+              "pinned readback regions overlap");
+
 int check_device_error(PovGpuScene* sc, PovGpuStats* stats, unsigned long long* host_stats)
 {
-    uint32_t errw = 0;
     cudaStream_t st = sc->active();
-    CK(cudaMemcpyAsync(&errw, sc->err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(host_stats, sc->stats.p, sizeof(unsigned long long) * ST_COUNT, cudaMemcpyDeviceToHost, st));
+    uint32_t* perr = reinterpret_cast<uint32_t*>(sc->pinned + PovGpuScene::PIN_ERR);
+    unsigned long long* pst = reinterpret_cast<unsigned long long*>(sc->pinned + PovGpuScene::PIN_STATS);
+    CK(cudaMemcpyAsync(perr, sc->err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(pst, sc->stats.p, sizeof(unsigned long long) * ST_COUNT, cudaMemcpyDeviceToHost, st));
     HW(st);
+    const uint32_t errw = *perr;
+    std::memcpy(host_stats, pst, sizeof(unsigned long long) * ST_COUNT);
     if (stats) {
         std::memset(stats, 0, sizeof(*stats));
         stats->number_of_rays = host_stats[ST_RAYS];
@@ -1698,10 +1727,9 @@ int run_media(PovGpuScene* sc, PathBufs& B, const QRay* q, const int* state, con
     const int NI = sc->media_ni, SMAX = sc->media_smax;
     CK(cudaMemsetAsync(cnt + C_MC, 0, sizeof(int), st));
     CK(launch_media_list(state, B.hits.as<QHit>(), qcount, (int)maxq, B.mlist.as<int>(), cnt + C_MC, grid, st));
-    int nm = 0;
-    CK(cudaMemcpyAsync(&nm, cnt + C_MC, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(sc->pin_int(0), cnt + C_MC, sizeof(int), cudaMemcpyDeviceToHost, st));
     HW(st);
-    nm = std::min<int>(nm, (int)maxq);
+    const int nm = std::min<int>(*sc->pin_int(0), (int)maxq);
     *launches = 1;
     if (nm == 0)
         return POV_GPU_OK;
@@ -1781,10 +1809,9 @@ int run_levels(PovGpuScene* sc, StageClock& clk, PathBufs& B, size_t maxq, int l
     for (int pass = 0; pass < max_pass; pass++) {
         const int level = level0 + pass;   // the level of every ray without media containers
         if (media && pass > 0) {
-            int nq = 0;
-            CK(cudaMemcpyAsync(&nq, ccur, sizeof(int), cudaMemcpyDeviceToHost, st));
+            CK(cudaMemcpyAsync(sc->pin_int(1), ccur, sizeof(int), cudaMemcpyDeviceToHost, st));
             HW(st);
-            if (nq == 0)
+            if (*sc->pin_int(1) == 0)
                 break;
         }
         CK(cudaMemsetAsync(cnext, 0, sizeof(int), st));
@@ -1839,10 +1866,9 @@ int run_levels(PovGpuScene* sc, StageClock& clk, PathBufs& B, size_t maxq, int l
             CK(clk.end(2));
         }
         if (rad) {
-            int nq = 0;
-            CK(cudaMemcpyAsync(&nq, cnt + C_RQ, sizeof(int), cudaMemcpyDeviceToHost, st));
+            CK(cudaMemcpyAsync(sc->pin_int(2), cnt + C_RQ, sizeof(int), cudaMemcpyDeviceToHost, st));
             HW(st);
-            nq = std::min(nq, (int)maxq);
+            const int nq = std::min(*sc->pin_int(2), (int)maxq);
             if (nq > 0) {
                 int rc = rad_resolve(sc, clk, hit_depth, B.rq.as<RadQuery>(), nq, B.rq_amb.as<float4>());
                 if (rc != POV_GPU_OK)
@@ -1943,10 +1969,9 @@ int rad_resolve(PovGpuScene* sc, StageClock& clk, int d, const RadQuery* queries
                             L.seeds.as<int>(), cn, nxt, cn + 1, R.rstats.as<unsigned long long>(),
                             sc->err.as<uint32_t>(), qgrid, st));
         CK(clk.end());
-        int hc[2] = {0, 0};
-        CK(cudaMemcpyAsync(hc, cn, sizeof(hc), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(sc->pin_int(3), cn, sizeof(int) * 2, cudaMemcpyDeviceToHost, st));
         HW(st);
-        const int ns = std::min(hc[0], n), nn = std::min(hc[1], n);
+        const int ns = std::min(*sc->pin_int(3), n), nn = std::min(*sc->pin_int(4), n);
         if (use_nic) {
             if (ns > 0) {
                 CK(R.nic_pred.ensure(sizeof(float4) * (size_t)ns));
@@ -2221,6 +2246,13 @@ int pov_gpu_scene_create(const PovGpuSceneDesc* desc, PovGpuScene** out, int32_t
         delete sc;
         return POV_GPU_E_CUDA;
     }
+    if (cudaHostAlloc(reinterpret_cast<void**>(&sc->pinned), PovGpuScene::PIN_BYTES, cudaHostAllocDefault) !=
+        cudaSuccess) {
+        sc->release_all();
+        delete sc;
+        return POV_GPU_E_NOMEM;
+    }
+    std::memset(sc->pinned, 0, PovGpuScene::PIN_BYTES);
     st = build_scene(sc, desc);
     if (st == POV_GPU_OK) {
         if (sc->counters.ensure(sizeof(int) * C_NUM) != cudaSuccess ||
@@ -2640,10 +2672,10 @@ int pov_gpu_trace_blocks(PovGpuScene* sc, const PovGpuBlock* blocks, int32_t num
                                   sc->sslot.as<int>(), cnt + C_NS, scap, cnext, cnt + C_NN, ncap,
                                   sc->err.as<uint32_t>(), gb, st));
             sc->timings.kernel_launches++;
-            int hc[2] = {0, 0};
-            CK(cudaMemcpyAsync(hc, cnt + C_NS, sizeof(int), cudaMemcpyDeviceToHost, st));
-            CK(cudaMemcpyAsync(hc + 1, cnt + C_NN, sizeof(int), cudaMemcpyDeviceToHost, st));
+            CK(cudaMemcpyAsync(sc->pin_int(5), cnt + C_NS, sizeof(int), cudaMemcpyDeviceToHost, st));
+            CK(cudaMemcpyAsync(sc->pin_int(6), cnt + C_NN, sizeof(int), cudaMemcpyDeviceToHost, st));
             HW(st);
+            const int hc[2] = {*sc->pin_int(5), *sc->pin_int(6)};
             const int nsamp = std::min(hc[0], scap);
             if (nsamp > 0) {
                 rc = run_samples(sc, clk, 2, 0, nullptr, sc->spos.as<double2>(), cnt + C_NS, nsamp, params->width,
@@ -2661,11 +2693,15 @@ int pov_gpu_trace_blocks(PovGpuScene* sc, const PovGpuBlock* blocks, int32_t num
     }
     if (!out_on_device)
         CK(cudaMemcpyAsync(out_rgbt, dout, sizeof(float4) * n, cudaMemcpyDeviceToHost, st));
-    unsigned long long hw[8] = {0};
+    unsigned long long* pwork = reinterpret_cast<unsigned long long*>(sc->pinned + PovGpuScene::PIN_WORK);
     if (wc)
-        CK(cudaMemcpyAsync(hw, wc, sizeof(hw), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(pwork, wc, sizeof(unsigned long long) * 8, cudaMemcpyDeviceToHost, st));
     unsigned long long hs[ST_COUNT];
     int rc = check_device_error(sc, stats, hs);
+    if (rc == POV_GPU_E_TIMEOUT)
+        return rc;
+    unsigned long long hw[8];
+    std::memcpy(hw, pwork, sizeof(hw));
     if (stats) {
         stats->number_of_pixels = n_pixels;
         stats->number_of_samples = n_samples;
@@ -2799,6 +2835,8 @@ int pov_gpu_radiosity_pretrace(PovGpuScene* sc, const PovGpuBlock* blocks, int32
     }
     unsigned long long hs[ST_COUNT];
     int rc = check_device_error(sc, stats, hs);
+    if (rc == POV_GPU_E_TIMEOUT)
+        return rc;
     if (stats) {
         stats->number_of_pixels = npix;
         if (int rr = rad_collect(sc, stats))
@@ -2934,6 +2972,8 @@ int pov_gpu_trace_rays(PovGpuScene* sc, const double* origins, const double* dir
     CK(cudaMemcpyAsync(t64.data(), sc->t64.p, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
     unsigned long long hs[ST_COUNT];
     int rc = check_device_error(sc, nullptr, hs);
+    if (rc == POV_GPU_E_TIMEOUT)
+        return rc;
     // map prim references to flattened object ids / mesh triangle indices
     for (size_t i = 0; i < n; i++) {
         const QHit& h = hh[i];

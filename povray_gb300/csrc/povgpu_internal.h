@@ -207,6 +207,7 @@ struct DeviceScene {
     // boxes, tori, CSG
     const DevBox*      boxes;
     const DevTorus*    tori;
+    const float4*      tori32;      // per torus 4 float4: local x, y, z rows of the inverse (FP32), (R, r, 0, 0)
     const DevCsg*      csgs;
     const DevCsgChild* csg_children;
     const int32_t*     sphere_flags;   // bit0 inverted (spheres inside CSG)

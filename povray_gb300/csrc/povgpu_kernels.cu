@@ -359,6 +359,45 @@ __device__ __forceinline__ double3 torus_local_point(const DevTorus& T, double x
                         x * m[2] + y * m[5] + z * m[8] + m[11]);
 }
 
+// FP32 pre-cull in front of torus_roots: can the ray reach the torus
+// before world depth tmax?  The ray is taken into the torus's frame in FP32
+// and tested against the torus's bounding sphere (radius R + r, which holds
+// every root) and the slab |y| <= r of Torus::Test_Thick_Cylinder
+// (torus.cpp:932-1084), both widened by a margin (1e-3 of the bound plus
+// 1e-4 of the origin's distance) far above FP32's rounding at these
+// magnitudes, so only rays that surely miss are dropped; torus_roots
+// decides the rest in FP64.  Its cost is ~40 FP32 operations against the
+// FP64 bound and quartic it saves (FP64 is a narrow pipe on this part).
+__device__ __forceinline__ bool torus_may_hit(const float4* __restrict__ t32, float3 o, float3 d, float tmax)
+{
+    const float4 X = __ldg(t32), Y = __ldg(t32 + 1), Z = __ldg(t32 + 2), Rr = __ldg(t32 + 3);
+    const float3 P = f3(fmaf(o.x, X.x, fmaf(o.y, X.y, fmaf(o.z, X.z, X.w))),
+                        fmaf(o.x, Y.x, fmaf(o.y, Y.y, fmaf(o.z, Y.z, Y.w))),
+                        fmaf(o.x, Z.x, fmaf(o.y, Z.y, fmaf(o.z, Z.z, Z.w))));
+    float3 D = f3(fmaf(d.x, X.x, fmaf(d.y, X.y, d.z * X.z)), fmaf(d.x, Y.x, fmaf(d.y, Y.y, d.z * Y.z)),
+                  fmaf(d.x, Z.x, fmaf(d.y, Z.y, d.z * Z.z)));
+    const float inv_len = rsqrtf(dot3(D, D));   // local depth * inv_len = world depth
+    D = D * inv_len;
+    const float rb = Rr.x + Rr.y;
+    const float pp = dot3(P, P);
+    const float margin = 1e-3f * rb + 1e-4f * sqrtf(pp);
+    const float br = rb + margin;
+    const float b = dot3(P, D), disc = b * b - (pp - br * br);
+    if (disc < 0.0f)
+        return false;
+    const float sq = sqrtf(disc);
+    const float t_far = sq - b;
+    float t_near = -b - sq;
+    if (t_far < 0.0f || t_near * inv_len > tmax * (1.0f + 1e-3f) + margin)
+        return false;
+    t_near = fmaxf(t_near, 0.0f);
+    const float h = Rr.y + margin;
+    if (fabsf(D.y) < 1e-6f)
+        return fabsf(P.y) <= h;
+    const float ta = (-h - P.y) / D.y, tb = (h - P.y) / D.y;
+    return fmaxf(ta, tb) >= t_near && fminf(ta, tb) <= t_far;
+}
+
 // Roots (world depths) with depth > 1e-4; returns their count (<= 4).
 __device__ __noinline__ int torus_roots(const DevTorus& T, double3 o, double3 d, double* out)
 {
@@ -666,6 +705,8 @@ __device__ __forceinline__ bool prim_test(const DeviceScene& S, uint32_t ref, fl
     if (!FULL)
         return false;   // lean variant: the scene has no tori and no CSG
     if (kind == PK_TORUS) {
+        if (!torus_may_hit(S.tori32 + 4 * (size_t)idx, o, d, t))
+            return false;
         double r[4];
         int n = torus_roots(S.tori[idx], make_double3(o.x, o.y, o.z), make_double3(d.x, d.y, d.z), r);
         if (self)
