@@ -386,10 +386,12 @@ struct PathBufs {
     DevBuf stateA, stateB, smedium; // media containers: per-ray level and medium, shadow-ray medium
     DevBuf mlist, mte, mod;         // media containers: listed rays, per-interval sums
     DevBuf mcbuf, mrounds;          // media containers: sample slots of a chunk, round lists
+    DevBuf bin_keys, bin_hist, bin_order;   // textured scenes: the shade queue binned by material
     DevBuf counters;
 
     // media_ni: interval slots per ray segment (0: the scene has no media containers)
-    cudaError_t ensure(size_t maxq, int nl, int nal, bool rad, bool sample_rays, int media_ni = 0)
+    cudaError_t ensure(size_t maxq, int nl, int nal, bool rad, bool sample_rays, int media_ni = 0,
+                       bool binned = false)
     {
         maxq = std::max<size_t>(maxq, 1);
         nl = std::max(nl, 1);
@@ -422,6 +424,11 @@ struct PathBufs {
             PB_ENSURE(quality, sizeof(float) * maxq);
             PB_ENSURE(first_t, sizeof(float) * maxq);
         }
+        if (binned) {
+            PB_ENSURE(bin_keys, maxq);
+            PB_ENSURE(bin_hist, sizeof(int) * 2 * SHADE_BINS);
+            PB_ENSURE(bin_order, sizeof(int) * maxq);
+        }
         if (media_ni > 0) {
             PB_ENSURE(stateA, sizeof(int) * maxq);
             PB_ENSURE(stateB, sizeof(int) * maxq);
@@ -437,7 +444,8 @@ struct PathBufs {
     {
         DevBuf* all[] = {&qA, &qB, &pathA, &pathB, &hits, &paths, &slot_contrib, &sq, &sq_slot, &blocked, &skipA,
                          &skipB, &sskip, &aq, &aq_slot, &aq_skip, &rq, &rq_amb, &quality, &first_t, &stateA,
-                         &stateB, &smedium, &mlist, &mte, &mod, &mcbuf, &mrounds, &counters};
+                         &stateB, &smedium, &mlist, &mte, &mod, &mcbuf, &mrounds, &bin_keys, &bin_hist,
+                         &bin_order, &counters};
         for (DevBuf* b : all)
             b->release();
     }
@@ -535,6 +543,7 @@ struct PovGpuScene {
     DevBuf spheres, spheres64, boxes64, sphere_obj, sphere_flags, planes, plane_obj, boxes, tori, tori32, csgs, csg_children, objects,
         materials, lights, medias, patterns, tnormals, noise_hash, noise_rtab, noise_perm, noise_grad, noise_waves;
     DevBuf encode_buf;     // staging of pov_gpu_encode_u8 for host outputs
+    bool   textured = false;   // some material has a pattern pigment or a normal: bin the shade queue
     int    media_ni = 0;   // interval slots per media segment (0: no media containers)
     int    media_smax = 0;  // sample slots per interval (ends + sample-tree nodes)
     int    media_sub = 0;   // largest sub-interval count
@@ -1406,6 +1415,9 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
     NoiseTables nt;
     if (d->num_patterns > 0)
         nt.build();
+    sc->textured = false;
+    for (int i = 0; i < d->num_materials; i++)
+        sc->textured = sc->textured || d->materials[i].pattern > 0 || d->materials[i].normal > 0;
 
     CK(upload(sc->objects, objects));
     CK(upload(sc->materials, mats));
@@ -1772,7 +1784,7 @@ int run_levels(PovGpuScene* sc, StageClock& clk, PathBufs& B, size_t maxq, int l
     const int nal = sample_rays ? 0 : sc->S.num_area_lights;
     const bool rad = sc->rad.enabled && hit_depth < sc->rad.set.recursion_limit;
     const bool media = sc->media_ni > 0;
-    CK(B.ensure(maxq, nl, nal, rad, sample_rays, sc->media_ni));
+    CK(B.ensure(maxq, nl, nal, rad, sample_rays, sc->media_ni, sc->textured));
     cudaStream_t st = sc->active();
     int* cnt = B.counters.as<int>();
     unsigned long long* dstats = sc->stats.as<unsigned long long>();
@@ -1833,12 +1845,18 @@ int run_levels(PovGpuScene* sc, StageClock& clk, PathBufs& B, size_t maxq, int l
         }
         CK(clk.begin(POV_GPU_STAGE_SHADE));
         ShadeMedia sm{scur, snext, media ? B.smedium.as<int>() : nullptr};
+        const int* order = nullptr;
+        if (sc->textured) {   // one material per warp in k_shade
+            CK(launch_shade_bins(S, B.hits.as<QHit>(), ccur, (int)maxq, B.bin_keys.as<uint8_t>(),
+                                 B.bin_hist.as<int>(), B.bin_order.as<int>(), grid_shade, st));
+            order = B.bin_order.as<int>();
+        }
         CK(launch_shade(S, level, max_level, qcur, pcur, B.hits.as<QHit>(), ccur, B.paths.as<PathState>(),
                         B.slot_contrib.as<float4>(), B.sq.as<QRay>(), B.sq_slot.as<int>(), cnt + C_SQ,
                         B.sskip.as<uint2>(), qnext, pnext, knext, cnext, (int)maxq, (int)(maxq * nl),
                         B.aq.as<QRay>(), B.aq_slot.as<int>(), B.aq_skip.as<uint2>(), cnt + C_AQ, (int)max_area, sr,
-                        sm, grid_shade, derr, dstats, st));
-        CK(clk.end());
+                        sm, order, grid_shade, derr, dstats, st));
+        CK(clk.end(sc->textured ? 4 : 1));
         if (nal > 0) {
             CK(clk.begin(POV_GPU_STAGE_AREA_SHADOW));
             CK(launch_area_shadow(S, B.aq.as<QRay>(), B.aq_slot.as<int>(), B.aq_skip.as<uint2>(), cnt + C_AQ,

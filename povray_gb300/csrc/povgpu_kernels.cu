@@ -1371,8 +1371,8 @@ __global__ void __launch_bounds__(128) k_shade(
     uint2* __restrict__ sq_skip, QRay* __restrict__ nq, int* __restrict__ nq_path,
     uint2* __restrict__ nq_skip, int* __restrict__ nq_count, int max_queue,
     int max_shadow, QRay* __restrict__ aq, int* __restrict__ aq_slot, uint2* __restrict__ aq_skip,
-    int* __restrict__ aq_count, int max_area, ShadeRad rad, ShadeMedia med, uint32_t* err,
-    unsigned long long* stats)
+    int* __restrict__ aq_count, int max_area, ShadeRad rad, ShadeMedia med, const int* __restrict__ order,
+    uint32_t* err, unsigned long long* stats)
 {
     const int n = min(*q_count, max_queue);
     const int nl = S.num_lights;
@@ -1383,6 +1383,8 @@ __global__ void __launch_bounds__(128) k_shade(
         unsigned mask = __ballot_sync(0xffffffffu, active);
         if (!active)
             continue;
+        if (order)   // the queue binned by material: this thread's item
+            i = order[i];
         QRay r = q[i];
         QHit h = hits[i];
         int path = q_path ? q_path[i] : i;
@@ -2684,12 +2686,116 @@ cudaError_t launch_shade(const DeviceScene& S, int level, int max_level, const Q
                          const int* q_count, PathState* paths, float4* slot_contrib, QRay* sq, int* sq_slot,
                          int* sq_count, uint2* sq_skip, QRay* nq, int* nq_path, uint2* nq_skip, int* nq_count,
                          int max_queue, int max_shadow, QRay* aq, int* aq_slot, uint2* aq_skip, int* aq_count,
-                         int max_area, const ShadeRad& rad, const ShadeMedia& med, int grid, uint32_t* err,
-                         unsigned long long* stats, cudaStream_t st)
+                         int max_area, const ShadeRad& rad, const ShadeMedia& med, const int* order, int grid,
+                         uint32_t* err, unsigned long long* stats, cudaStream_t st)
 {
     k_shade<<<grid, 128, 0, st>>>(S, level, max_level, q, q_path, hits, q_count, paths, slot_contrib, sq, sq_slot, sq_count,
                                   sq_skip, nq, nq_path, nq_skip, nq_count, max_queue, max_shadow, aq, aq_slot,
-                                  aq_skip, aq_count, max_area, rad, med, err, stats);
+                                  aq_skip, aq_count, max_area, rad, med, order, err, stats);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------- shade-queue binning --
+// Textured scenes: a hit's shading cost is its material's pattern pigment
+// and normal perturbation, which differ ~50x between materials; a warp
+// that mixes materials runs as slow as its slowest lane.  Before k_shade
+// the queue is binned by material (a counting sort on a small key: 0 for
+// misses and plain materials, 1 + material mod 255 for textured ones), so a
+// warp shades one material.  Within a bin the items keep roughly their
+// queue order (warps claim their places in turn), which keeps the rays a
+// warp emits next to each other.
+__device__ __forceinline__ int shade_key(const DeviceScene& S, const QHit& h)
+{
+    if (h.prim == NO_PRIM)
+        return 0;
+    uint32_t kind = h.prim >> PRIM_KIND_SHIFT, idx = h.prim & PRIM_INDEX_MASK;
+    int obj;
+    if (kind == PK_CSG) {
+        const DevCsg g = S.csgs[idx];
+        obj = S.csg_children[g.first + (__float_as_uint(h.u) & 0xffffu)].object;
+    } else if (kind == PK_SPHERE) {
+        obj = __ldg(S.sphere_obj + idx);
+    } else if (kind == PK_PLANE) {
+        obj = __ldg(S.plane_obj + idx);
+    } else if (kind == PK_BOX) {
+        obj = __float_as_int(S.boxes[idx].lo.w);
+    } else if (kind == PK_TORUS) {
+        obj = S.tori[idx].object;
+    } else {
+        obj = __float_as_int(__ldg(S.tri_normal + __ldg(S.tri_global + idx)).w);
+    }
+    const int mat = S.objects[obj].material;
+    const DevMaterial& m = S.materials[mat];
+    return (m.pattern || m.normal) ? 1 + mat % (SHADE_BINS - 1) : 0;
+}
+
+// Per item its key, and the keys' counts (one atomic per key per warp).
+__global__ void k_bin_count(DeviceScene S, const QHit* __restrict__ hits, const int* __restrict__ q_count, int cap,
+                            uint8_t* __restrict__ keys, int* __restrict__ hist)
+{
+    const int n = min(*q_count, cap);
+    for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const int i = base + threadIdx.x;
+        const bool active = i < n;
+        const int key = active ? shade_key(S, hits[i]) : -1;
+        if (active)
+            keys[i] = (uint8_t)key;
+        const unsigned same = __match_any_sync(0xffffffffu, key);
+        if (active && (threadIdx.x & 31) == __ffs(same) - 1)
+            atomicAdd(&hist[key], __popc(same));
+    }
+}
+
+// Exclusive scan of the key counts into each bin's first place (one block).
+__global__ void k_bin_scan(int* __restrict__ hist, int* __restrict__ cursor)
+{
+    __shared__ int s[SHADE_BINS];
+    const int t = threadIdx.x;
+    s[t] = hist[t];
+    __syncthreads();
+    if (t == 0) {
+        int run = 0;
+        for (int k = 0; k < SHADE_BINS; k++) {
+            const int c = s[k];
+            s[k] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+    cursor[t] = s[t];
+}
+
+// Every item to its place in its bin: lanes of a warp with the same key
+// take consecutive places in lane order (one atomic per key per warp).
+__global__ void k_bin_scatter(const int* __restrict__ q_count, int cap, const uint8_t* __restrict__ keys,
+                              int* __restrict__ cursor, int* __restrict__ order)
+{
+    const int n = min(*q_count, cap);
+    const int lane = threadIdx.x & 31;
+    for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const int i = base + threadIdx.x;
+        const bool active = i < n;
+        const int key = active ? (int)keys[i] : -1;
+        const unsigned same = __match_any_sync(0xffffffffu, key);
+        const int leader = __ffs(same) - 1;
+        int first = 0;
+        if (active && lane == leader)
+            first = atomicAdd(&cursor[key], __popc(same));
+        first = __shfl_sync(0xffffffffu, first, leader);
+        if (active)
+            order[first + __popc(same & ((1u << lane) - 1u))] = i;
+    }
+}
+
+cudaError_t launch_shade_bins(const DeviceScene& S, const QHit* hits, const int* q_count, int cap, uint8_t* keys,
+                              int* hist, int* order, int grid, cudaStream_t st)
+{
+    cudaError_t e = cudaMemsetAsync(hist, 0, sizeof(int) * SHADE_BINS, st);
+    if (e != cudaSuccess)
+        return e;
+    k_bin_count<<<grid, 128, 0, st>>>(S, hits, q_count, cap, keys, hist);
+    k_bin_scan<<<1, SHADE_BINS, 0, st>>>(hist, hist + SHADE_BINS);
+    k_bin_scatter<<<grid, 128, 0, st>>>(q_count, cap, keys, hist + SHADE_BINS, order);
     return cudaGetLastError();
 }
 

@@ -21,8 +21,14 @@ cudaError_t launch_shade(const DeviceScene& S, int level, int max_level, const Q
                          const int* q_count, PathState* paths, float4* slot_contrib, QRay* sq, int* sq_slot,
                          int* sq_count, uint2* sq_skip, QRay* nq, int* nq_path, uint2* nq_skip, int* nq_count,
                          int max_queue, int max_shadow, QRay* aq, int* aq_slot, uint2* aq_skip, int* aq_count,
-                         int max_area, const ShadeRad& rad, const ShadeMedia& med, int grid, uint32_t* err,
+                         int max_area, const ShadeRad& rad, const ShadeMedia& med, const int* order, int grid, uint32_t* err,
                          unsigned long long* stats, cudaStream_t st);
+// Bins the shade queue by material (SHADE_BINS keys): keys[cap] bytes,
+// hist[2 * SHADE_BINS] ints (counts, then cursors), order[cap] receives the
+// binned item order for k_shade.
+constexpr int SHADE_BINS = 256;
+cudaError_t launch_shade_bins(const DeviceScene& S, const QHit* hits, const int* q_count, int cap, uint8_t* keys,
+                              int* hist, int* order, int grid, cudaStream_t st);
 cudaError_t launch_fill_int(int* a, const int* count, int cap, int value, int grid, cudaStream_t st);
 // 8-bit RGB of n RGBT pixels; thr[v] (v < 255) = the midpoint of decoded levels v and v+1
 cudaError_t launch_encode_u8(const float4* rgbt, long long n, int curve, const float* thr, uint8_t* out, int grid,
