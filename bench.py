@@ -319,6 +319,11 @@ def main():
 
     s = make_scene(args)
     gpu = GpuScene(s)
+    # the autotuner's launch shape for this workload, when it recorded one
+    from povray_gb300 import autotune
+    launch_cfg = None if args.workload in MULTIVIEW else autotune.tuned_config(args.workload, args.width, args.height)
+    if launch_cfg:
+        gpu.set_launch_config(**launch_cfg)
     stream = torch.cuda.current_stream()
     gpu.set_stream(stream.cuda_stream)
     multiview = args.workload in MULTIVIEW
@@ -477,6 +482,7 @@ def main():
                      "l2_hit_rate": prof.get("l2_hit_rate"),
                      "traffic_source": prof.get("source")},
         "stage_ms_per_frame": {k2: v / args.steps for k2, v in stage_ms.items() if v > 0},
+        "launch_config": launch_cfg or "library defaults (no tuned entry)",
         "gpu_launches": launches,
         "clocks": clocks,
     }

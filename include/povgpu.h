@@ -617,6 +617,24 @@ typedef struct PovGpuTimings {
 int pov_gpu_set_profiling(PovGpuScene* scene, int flags);
 int pov_gpu_get_timings(PovGpuScene* scene, PovGpuTimings* out);
 
+/*
+ * Launch shapes of the trace path's kernels (no reference counterpart).
+ * The project's autotuner (povray_gb300/autotune.py) times candidate
+ * shapes on the device and records the best per workload in a table;
+ * zero fields keep the library's defaults.  Applies to later calls.
+ * POV_GPU_E_INVALID for values outside the ranges below.
+ */
+typedef struct PovGpuLaunchConfig {
+    int32_t trace_blocks_per_sm;   /* traversal grid, blocks per SM: 1..32 (default 8)        */
+    int32_t trace_block;           /* traversal block: 64 or 128 threads (default 128)       */
+    int32_t trace_occupancy;       /* 1: registers capped for 8 resident blocks per SM (lean
+                                      traversal of scenes without tori and CSG); 0: default */
+    int32_t shade_blocks_per_sm;   /* grid cap of the queue kernels, blocks per SM: 1..64
+                                      (default 16)                                           */
+    int32_t reserved[4];
+} PovGpuLaunchConfig;
+int pov_gpu_set_launch_config(PovGpuScene* scene, const PovGpuLaunchConfig* config);
+
 /* Human-readable text of a status code. */
 const char* pov_gpu_error_string(int status);
 

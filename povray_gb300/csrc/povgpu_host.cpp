@@ -543,6 +543,21 @@ struct PovGpuScene {
     DevBuf spheres, spheres64, boxes64, sphere_obj, sphere_flags, planes, plane_obj, boxes, tori, tori32, csgs, csg_children, objects,
         materials, lights, medias, patterns, tnormals, noise_hash, noise_rtab, noise_perm, noise_grad, noise_waves;
     DevBuf encode_buf;     // staging of pov_gpu_encode_u8 for host outputs
+    DevBuf cam_tab;        // per-call column / row offsets of the camera rays
+    PovGpuLaunchConfig lc{8, 128, 0, 16, {0, 0, 0, 0}};   // launch shapes (pov_gpu_set_launch_config)
+    // the device work of a plain frame (no radiosity, media or AA) as a
+    // captured CUDA graph, replayed while the frame's shape stays the same
+    struct GraphKey {
+        int n, nblocks, width, height;
+        const void* out;
+        const void* bufs[16];
+        PovGpuLaunchConfig lc;
+        DeviceScene S;
+    };
+    GraphKey graph_key{}, graph_last{};
+    bool graph_last_valid = false;
+    cudaGraphExec_t graph_exec = nullptr;
+    uint32_t graph_launches = 0;   // kernels in the graph
     bool   textured = false;   // some material has a pattern pigment or a normal: bin the shade queue
     int    media_ni = 0;   // interval slots per media segment (0: no media containers)
     int    media_smax = 0;  // sample slots per interval (ends + sample-tree nodes)
@@ -599,12 +614,15 @@ struct PovGpuScene {
         if (pinned)
             cudaFreeHost(pinned);
         pinned = nullptr;
+        if (graph_exec)
+            cudaGraphExecDestroy(graph_exec);
+        graph_exec = nullptr;
         DevBuf* all[] = {&nodes, &refs, &tri_v0, &tri_e1, &tri_e2, &tri_global, &tri_shade, &tri_normal, &tri_local,
                          &normals, &spheres, &spheres64, &boxes64, &sphere_obj, &sphere_flags, &planes, &plane_obj, &boxes, &tori, &tori32, &csgs,
                          &csg_children, &objects, &materials, &lights, &blocks, &block_off, &corner_off, &qA,
                          &hits, &out, &counters, &stats, &err, &rays_in, &t64, &corners, &aa_grid, &aa_mask,
                          &aa_subdiv, &aa_xy, &cellsA, &cellsB, &spos, &sslot, &wcount, &pos_count, &medias,
-                         &encode_buf, &patterns, &tnormals, &noise_hash, &noise_rtab, &noise_perm, &noise_grad,
+                         &encode_buf, &cam_tab, &patterns, &tnormals, &noise_hash, &noise_rtab, &noise_perm, &noise_grad,
                          &noise_waves};
         for (DevBuf* b : all)
             b->release();
@@ -1791,8 +1809,9 @@ int run_levels(PovGpuScene* sc, StageClock& clk, PathBufs& B, size_t maxq, int l
     uint32_t* derr = sc->err.as<uint32_t>();
     unsigned long long* wc = (sc->profiling & POV_GPU_PROFILE_WORK) ? sc->wcount.as<unsigned long long>() : nullptr;
     const DeviceScene& S = sc->S;
-    const int grid_trace = sc->num_sms * 8;
-    const int grid_shade = std::max(1, std::min(sc->num_sms * 16, (int)((maxq + 127) / 128)));
+    const int grid_trace = sc->num_sms * sc->lc.trace_blocks_per_sm;
+    const int grid_shade = std::max(1, std::min(sc->num_sms * sc->lc.shade_blocks_per_sm, (int)((maxq + 127) / 128)));
+    const int tblock = sc->lc.trace_block, tocc = sc->lc.trace_occupancy;
     const size_t max_area = maxq * (size_t)nal;
     QRay* qcur = B.qA.as<QRay>();
     QRay* qnext = B.qB.as<QRay>();
@@ -1831,7 +1850,7 @@ int run_levels(PovGpuScene* sc, StageClock& clk, PathBufs& B, size_t maxq, int l
         CK(cudaMemsetAsync(cnt + C_AQ, 0, sizeof(int) * 2, st));   // AQ, RQ
         CK(clk.begin(POV_GPU_STAGE_TRACE_CLOSEST));
         CK(launch_trace(S, false, qcur, ccur, cnt + C_W0, B.hits.as<QHit>(), nullptr, sc->stack_depth, grid_trace,
-                        derr, dstats, wc, (int)maxq, kcur, st));
+                        derr, dstats, wc, (int)maxq, kcur, st, tblock, tocc));
         CK(clk.end());
         if (sample_rays && pass == 0)
             CK(launch_first_hit(B.hits.as<QHit>(), ccur, (int)maxq, B.first_t.as<float>(), grid_shade, st));
@@ -1875,7 +1894,7 @@ int run_levels(PovGpuScene* sc, StageClock& clk, PathBufs& B, size_t maxq, int l
             else
                 CK(launch_trace(S, true, B.sq.as<QRay>(), cnt + C_SQ, cnt + C_W1, nullptr, B.blocked.as<uint8_t>(),
                                 sc->stack_depth, grid_trace, derr, dstats, wc ? wc + 4 : nullptr, (int)(maxq * nl),
-                                B.sskip.as<uint2>(), st));
+                                B.sskip.as<uint2>(), st, tblock, tocc));
             CK(clk.end());
             CK(clk.begin(POV_GPU_STAGE_RESOLVE));
             CK(launch_resolve(pcur, ccur, sc->num_lights, B.sq_slot.as<int>(), B.blocked.as<uint8_t>(), cnt + C_SQ,
@@ -2036,11 +2055,13 @@ int run_samples(PovGpuScene* sc, StageClock& clk, int mode, int nblocks, const i
     cudaStream_t st = sc->active();
     int* cnt = B.counters.as<int>();
     CK(cudaMemsetAsync(cnt, 0, sizeof(int) * C_NUM, st));
+    if (mode != 2)
+        CK(sc->cam_tab.ensure(sizeof(double) * ((size_t)width + (size_t)height + 2)));
     CK(clk.begin(POV_GPU_STAGE_CAMERA));
     CK(launch_camera(sc->S, mode, sc->blocks.as<int4>(), block_off, nblocks, pos, npos, n, width, height,
                      B.qA.as<QRay>(), B.pathA.as<int>(), B.paths.as<PathState>(), cnt + C_QA,
-                     sc->stats.as<unsigned long long>(), B.skipA.as<uint2>(), st));
-    CK(clk.end());
+                     sc->stats.as<unsigned long long>(), B.skipA.as<uint2>(), sc->cam_tab.as<double>(), st));
+    CK(clk.end(mode != 2 ? 2 : 1));
     int rc = run_levels(sc, clk, B, maxq, 0, sc->max_trace_level, 0, false);
     if (rc != POV_GPU_OK)
         return rc;
@@ -2217,6 +2238,86 @@ int rad_begin_call(PovGpuScene* sc, bool final_trace)
     R.error_bound = R.set.error_bound * (final_trace ? 1.0 : R.set.low_error_factor);
     R.rays_shot = 0;
     CK(cudaMemsetAsync(R.rstats.p, 0, sizeof(unsigned long long) * RST_COUNT, sc->active()));
+    return POV_GPU_OK;
+}
+
+// The device work of a plain frame, run through a CUDA graph: the first
+// call of a frame shape runs it directly (which sizes every buffer), the
+// second captures it into a graph and launches that, later calls of the
+// same shape (same pixel count, blocks, image size, output buffer, work
+// buffers, launch shapes and scene/camera state) launch the graph alone --
+// one launch instead of ~17.  The kernels read their queue counts from
+// device memory, so the captured sequence is the frame for any block list
+// of that shape; the block list itself is copied before the graph runs.
+int trace_plain_graph(PovGpuScene* sc, StageClock& clk, int num_blocks, int n, int width, int height, float4* dout)
+{
+    cudaStream_t st = sc->active();
+    PovGpuScene::GraphKey key;
+    std::memset(&key, 0, sizeof(key));
+    key.n = n;
+    key.nblocks = num_blocks;
+    key.width = width;
+    key.height = height;
+    key.out = dout;
+    const DevBuf* bufs[] = {&sc->top.qA, &sc->top.qB, &sc->top.pathA, &sc->top.pathB, &sc->top.hits,
+                            &sc->top.paths, &sc->top.slot_contrib, &sc->top.sq, &sc->top.sq_slot, &sc->top.blocked,
+                            &sc->top.sskip, &sc->top.aq, &sc->top.bin_order, &sc->cam_tab, &sc->blocks,
+                            &sc->block_off};
+    static_assert(sizeof(bufs) / sizeof(bufs[0]) == sizeof(key.bufs) / sizeof(key.bufs[0]), "graph key buffers");
+    for (size_t i = 0; i < sizeof(bufs) / sizeof(bufs[0]); i++)
+        key.bufs[i] = bufs[i]->p;
+    std::memcpy(&key.lc, &sc->lc, sizeof(key.lc));
+    std::memcpy(&key.S, &sc->S, sizeof(key.S));   // bytes, padding included, for the comparison
+    auto same = [](const PovGpuScene::GraphKey& a, const PovGpuScene::GraphKey& b) {
+        return std::memcmp(&a, &b, sizeof(a)) == 0;
+    };
+    auto body = [&]() -> int {
+        CK(cudaMemsetAsync(sc->counters.p, 0, sizeof(int) * C_NUM, st));
+        CK(cudaMemsetAsync(sc->stats.p, 0, sizeof(unsigned long long) * ST_COUNT, st));
+        CK(cudaMemsetAsync(sc->err.p, 0, sizeof(uint32_t) * 4, st));
+        return run_samples(sc, clk, 0, num_blocks, sc->block_off.as<int>(), nullptr, nullptr, n, width, height,
+                           nullptr, dout);
+    };
+    if (sc->graph_exec && same(key, sc->graph_key)) {
+        CK(cudaGraphLaunch(sc->graph_exec, st));
+        sc->timings.kernel_launches += sc->graph_launches;
+        return POV_GPU_OK;
+    }
+    if (!(sc->graph_last_valid && same(key, sc->graph_last))) {
+        // first call of this shape: run directly; it sizes the buffers
+        int rc = body();
+        // the buffers may have grown: the key is taken after the run
+        for (size_t i = 0; i < sizeof(bufs) / sizeof(bufs[0]); i++)
+            key.bufs[i] = bufs[i]->p;
+        sc->graph_last = key;
+        sc->graph_last_valid = rc == POV_GPU_OK;
+        return rc;
+    }
+    // second call of the shape: capture, then launch
+    const uint32_t launches0 = sc->timings.kernel_launches;
+    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    int rc = body();
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(st, &graph);
+    if (rc != POV_GPU_OK || e != cudaSuccess) {
+        if (graph)
+            cudaGraphDestroy(graph);
+        cudaGetLastError();
+        sc->graph_last_valid = false;
+        return rc != POV_GPU_OK ? rc : POV_GPU_E_CUDA;
+    }
+    if (sc->graph_exec)
+        cudaGraphExecDestroy(sc->graph_exec);
+    sc->graph_exec = nullptr;
+    e = cudaGraphInstantiate(&sc->graph_exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        sc->graph_exec = nullptr;
+        return POV_GPU_E_CUDA;
+    }
+    sc->graph_key = key;
+    sc->graph_launches = sc->timings.kernel_launches - launches0;
+    CK(cudaGraphLaunch(sc->graph_exec, st));
     return POV_GPU_OK;
 }
 
@@ -2415,6 +2516,26 @@ int pov_gpu_cache_load(PovGpuScene* sc, const char* path, int32_t* loaded)
         return rc;
     if (loaded)
         *loaded = (int32_t)R.loaded.size();
+    return POV_GPU_OK;
+}
+
+int pov_gpu_set_launch_config(PovGpuScene* sc, const PovGpuLaunchConfig* cfg)
+{
+    if (!sc || !cfg)
+        return POV_GPU_E_INVALID;
+    PovGpuLaunchConfig c = *cfg;
+    if (c.trace_blocks_per_sm == 0)
+        c.trace_blocks_per_sm = 8;
+    if (c.trace_block == 0)
+        c.trace_block = 128;
+    if (c.shade_blocks_per_sm == 0)
+        c.shade_blocks_per_sm = 16;
+    if (c.trace_blocks_per_sm < 1 || c.trace_blocks_per_sm > 32 || (c.trace_block != 64 && c.trace_block != 128) ||
+        (c.trace_occupancy != 0 && c.trace_occupancy != 1) || c.shade_blocks_per_sm < 1 ||
+        c.shade_blocks_per_sm > 64)
+        return POV_GPU_E_INVALID;
+    std::lock_guard<std::mutex> g(sc->lock);
+    sc->lc = c;
     return POV_GPU_OK;
 }
 
@@ -2638,7 +2759,14 @@ int pov_gpu_trace_blocks(PovGpuScene* sc, const PovGpuBlock* blocks, int32_t num
         return rr;
 
     uint64_t n_pixels = (uint64_t)n, n_samples = 0;
-    if (!aa) {
+    // plain frames (no radiosity, media containers or AA: no host reads
+    // between the launches) replay a captured graph of their device work
+    const bool graphable = !aa && !sc->rad.enabled && sc->media_ni == 0 && sc->profiling == 0;
+    if (graphable) {
+        int rc = trace_plain_graph(sc, clk, num_blocks, n, params->width, params->height, dout);
+        if (rc != POV_GPU_OK)
+            return rc;
+    } else if (!aa) {
         int rc = run_samples(sc, clk, 0, num_blocks, sc->block_off.as<int>(), nullptr, nullptr, n, params->width,
                              params->height, nullptr, dout);
         if (rc != POV_GPU_OK)

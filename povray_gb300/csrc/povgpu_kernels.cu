@@ -100,19 +100,50 @@ __device__ __forceinline__ int warp_reserve_k(int* counter, bool want, int k, un
 // --------------------------------------------------------------- camera --
 // Primary ray through image position (x, y) (pixel units, y down), formed
 // and normalised in FP64 exactly as CreateCameraRay does, then rounded.
-__device__ __forceinline__ QRay camera_ray(const DeviceScene& S, double x, double y, int width, int height)
+// x0, y0: the pixel's offsets from the image centre, x / width - 0.5 and
+// 0.5 - y / height (TracePixel::CreateCameraRay, tracepixel.cpp:357-373).
+// The direction is formed and normalised in FP64; the three divisions by
+// the length are each one multiplication by the FP64 reciprocal plus one
+// FMA correction step (the residual dx - q l times the reciprocal), which
+// gives the correctly rounded quotient except in double-rounding corner
+// cases -- FP64 divisions are a long instruction sequence on this part's
+// narrow FP64 pipe, and this kernel was bound by them.
+__device__ __forceinline__ QRay camera_ray_xy(const DeviceScene& S, double x0, double y0)
 {
-    double x0 = x / (double)width - 0.5;
-    double y0 = 0.5 - y / (double)height;
     double dx = S.cam_dir[0] + x0 * S.cam_right[0] + y0 * S.cam_up[0];
     double dy = S.cam_dir[1] + x0 * S.cam_right[1] + y0 * S.cam_up[1];
     double dz = S.cam_dir[2] + x0 * S.cam_right[2] + y0 * S.cam_up[2];
     double l = sqrt(dx * dx + dy * dy + dz * dz);
-    if (l != 0.0) { dx /= l; dy /= l; dz /= l; }
+    if (l != 0.0) {
+        const double rl = 1.0 / l;
+        double q = dx * rl;
+        dx = fma(fma(-q, l, dx), rl, q);
+        q = dy * rl;
+        dy = fma(fma(-q, l, dy), rl, q);
+        q = dz * rl;
+        dz = fma(fma(-q, l, dz), rl, q);
+    }
     QRay r;
     r.org = make_float4((float)S.cam_loc[0], (float)S.cam_loc[1], (float)S.cam_loc[2], kMinIsectDepth);
     r.dir = make_float4((float)dx, (float)dy, (float)dz, CUDART_INF_F);
     return r;
+}
+
+__device__ __forceinline__ QRay camera_ray(const DeviceScene& S, double x, double y, int width, int height)
+{
+    return camera_ray_xy(S, x / (double)width - 0.5, 0.5 - y / (double)height);
+}
+
+// The offsets of every column and row of the image for pixel centres
+// (mode 0: x + 0.5) or corners (mode 1: x), width + 1 then height + 1
+// entries: k_camera looks them up instead of dividing per pixel.
+__global__ void k_cam_table(int width, int height, double off, double* __restrict__ tab)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i <= width)
+        tab[i] = ((double)i + off) / (double)width - 0.5;
+    else if (i <= width + 1 + height)
+        tab[i] = 0.5 - ((double)(i - width - 1) + off) / (double)height;
 }
 
 // mode 0: pixel centres (x+0.5, y+0.5) of every block, block order
@@ -123,7 +154,7 @@ __global__ void k_camera(DeviceScene S, int mode, const int4* __restrict__ block
                          const int* __restrict__ block_off, int nblocks, const double2* __restrict__ pos,
                          const int* __restrict__ npos, int width, int height, QRay* __restrict__ q,
                          int* __restrict__ q_path, PathState* __restrict__ paths, int* __restrict__ q_count,
-                         unsigned long long* stats, uint2* __restrict__ q_skip, int cap)
+                         unsigned long long* stats, uint2* __restrict__ q_skip, int cap, const double* __restrict__ tab)
 {
     int n = min(mode == 2 ? *npos : block_off[nblocks], cap);   // never past the queue buffers
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -159,10 +190,10 @@ __global__ void k_camera(DeviceScene S, int mode, const int4* __restrict__ block
             ly = (tile >> 2) * 4 + (lane >> 3);
             path = block_off[lo] + ly * w + lx;
         }
-        x = (double)(b.x + lx) + (mode == 0 ? 0.5 : 0.0);
-        y = (double)(b.y + ly) + (mode == 0 ? 0.5 : 0.0);
+        x = tab[b.x + lx];
+        y = tab[width + 1 + b.y + ly];
     }
-    q[i] = camera_ray(S, x, y, width, height);
+    q[i] = mode == 2 ? camera_ray(S, x, y, width, height) : camera_ray_xy(S, x, y);
     q_path[i] = path;
     q_skip[i] = make_uint2(NO_PRIM, 0u);
     PathState p;
@@ -730,8 +761,12 @@ __device__ __forceinline__ bool prim_test(const DeviceScene& S, uint32_t ref, fl
 // ------------------------------------------------------------- traversal --
 // Closest hit (ANY = false) or any hit (ANY = true) for every ray in the
 // queue.  Stack in shared memory: slot k of thread t at smem[k*blockDim+t].
-template <bool ANY, bool FULL>
-__global__ void __launch_bounds__(128) k_trace(DeviceScene S, const QRay* __restrict__ q,
+// MINB: the resident blocks per SM the register allocation must allow
+// (1: the compiler's choice; 8: at most 64 registers a thread, more warps
+// to hide the node and triangle load latency at the price of spills) --
+// one of the autotuner's choices for the lean variant.
+template <bool ANY, bool FULL, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_trace(DeviceScene S, const QRay* __restrict__ q,
                                                const int* __restrict__ q_count, int* __restrict__ work,
                                                QHit* __restrict__ hits, uint8_t* __restrict__ blocked,
                                                int stack_depth, uint32_t* err, unsigned long long* stats,
@@ -2642,11 +2677,13 @@ cudaError_t launch_refine(const DeviceScene& S, const double* org, const double*
 cudaError_t launch_camera(const DeviceScene& S, int mode, const int4* blocks, const int* block_off, int nblocks,
                           const double2* pos, const int* npos, int max_samples, int width, int height, QRay* q,
                           int* q_path, PathState* paths, int* q_count, unsigned long long* stats, uint2* q_skip,
-                          cudaStream_t st)
+                          double* tab, cudaStream_t st)
 {
+    if (mode != 2)
+        k_cam_table<<<cdiv(width + height + 2, 256), 256, 0, st>>>(width, height, mode == 0 ? 0.5 : 0.0, tab);
     k_camera<<<cdiv(max_samples > 0 ? max_samples : 1, 256), 256, 0, st>>>(
         S, mode, blocks, block_off, nblocks, pos, npos, width, height, q, q_path, paths, q_count, stats, q_skip,
-        max_samples);
+        max_samples, tab);
     return cudaGetLastError();
 }
 
@@ -2659,25 +2696,31 @@ cudaError_t launch_load_rays(const double* org, const double* dir, int n, QRay* 
 cudaError_t launch_trace(const DeviceScene& S, bool any_hit, const QRay* q, const int* q_count, int* work,
                          QHit* hits, uint8_t* blocked, int stack_depth, int grid, uint32_t* err,
                          unsigned long long* stats, unsigned long long* wcount, int cap, const uint2* skips,
-                         cudaStream_t st)
+                         cudaStream_t st, int block, int occ)
 {
-    const int block = 128;
+    block = block == 64 ? 64 : 128;   // warps claim 32 rays; the stack is smem[k * blockDim + tid]
     size_t smem = (size_t)stack_depth * block * sizeof(int);
     // the full variant carries the FP64 torus solver and CSG; scenes without
     // them run the lean one (about half the registers)
     const bool full = S.has_full_prims != 0;
     if (any_hit && full)
-        k_trace<true, true><<<grid, block, smem, st>>>(S, q, q_count, work, hits, blocked, stack_depth, err, stats,
-                                                       wcount, cap, skips);
+        k_trace<true, true, 1><<<grid, block, smem, st>>>(S, q, q_count, work, hits, blocked, stack_depth, err,
+                                                          stats, wcount, cap, skips);
+    else if (any_hit && occ)
+        k_trace<true, false, 8><<<grid, block, smem, st>>>(S, q, q_count, work, hits, blocked, stack_depth, err,
+                                                           stats, wcount, cap, skips);
     else if (any_hit)
-        k_trace<true, false><<<grid, block, smem, st>>>(S, q, q_count, work, hits, blocked, stack_depth, err, stats,
-                                                        wcount, cap, skips);
+        k_trace<true, false, 1><<<grid, block, smem, st>>>(S, q, q_count, work, hits, blocked, stack_depth, err,
+                                                           stats, wcount, cap, skips);
     else if (full)
-        k_trace<false, true><<<grid, block, smem, st>>>(S, q, q_count, work, hits, blocked, stack_depth, err,
-                                                        stats, wcount, cap, skips);
+        k_trace<false, true, 1><<<grid, block, smem, st>>>(S, q, q_count, work, hits, blocked, stack_depth, err,
+                                                           stats, wcount, cap, skips);
+    else if (occ)
+        k_trace<false, false, 8><<<grid, block, smem, st>>>(S, q, q_count, work, hits, blocked, stack_depth, err,
+                                                            stats, wcount, cap, skips);
     else
-        k_trace<false, false><<<grid, block, smem, st>>>(S, q, q_count, work, hits, blocked, stack_depth, err,
-                                                         stats, wcount, cap, skips);
+        k_trace<false, false, 1><<<grid, block, smem, st>>>(S, q, q_count, work, hits, blocked, stack_depth, err,
+                                                            stats, wcount, cap, skips);
     return cudaGetLastError();
 }
 

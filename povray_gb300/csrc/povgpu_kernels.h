@@ -10,12 +10,13 @@ namespace povgpu {
 cudaError_t launch_camera(const DeviceScene& S, int mode, const int4* blocks, const int* block_off, int nblocks,
                           const double2* pos, const int* npos, int max_samples, int width, int height, QRay* q,
                           int* q_path, PathState* paths, int* q_count, unsigned long long* stats, uint2* q_skip,
+                          double* tab /* width + height + 2 doubles (modes 0, 1) */,
                           cudaStream_t st);
 cudaError_t launch_load_rays(const double* org, const double* dir, int n, QRay* q, int* q_count, cudaStream_t st);
 cudaError_t launch_trace(const DeviceScene& S, bool any_hit, const QRay* q, const int* q_count, int* work,
                          QHit* hits, uint8_t* blocked, int stack_depth, int grid, uint32_t* err,
                          unsigned long long* stats, unsigned long long* wcount, int cap, const uint2* skips,
-                         cudaStream_t st);
+                         cudaStream_t st, int block = 128, int occ = 0);
 cudaError_t launch_shade(const DeviceScene& S, int level, int max_level, const QRay* q, const int* q_path,
                          const QHit* hits,
                          const int* q_count, PathState* paths, float4* slot_contrib, QRay* sq, int* sq_slot,

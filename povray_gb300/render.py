@@ -156,6 +156,13 @@ class GpuScene:
             stats = {k: merge.get(k, lambda a, b: a + b)(stats[k], pre[k]) for k in stats}
         return _scenes.unblock(rgbt, blocks, p.width, p.height), stats
 
+    def set_launch_config(self, trace_blocks_per_sm=0, trace_block=0, trace_occupancy=0, shade_blocks_per_sm=0):
+        """Launch shapes of the trace path's kernels (pov_gpu_set_launch_config;
+        0 = the library's default), e.g. an entry of the autotuner's table."""
+        c = abi.PovGpuLaunchConfig(int(trace_blocks_per_sm), int(trace_block), int(trace_occupancy),
+                                   int(shade_blocks_per_sm))
+        _check(self.lib.pov_gpu_set_launch_config(self.h, C.byref(c)), "pov_gpu_set_launch_config")
+
     def cache_save(self, path):
         """Writes the radiosity sample cache as a .rca file (pov_gpu_cache_save)."""
         _check(self.lib.pov_gpu_cache_save(self.h, str(path).encode()), "pov_gpu_cache_save")

@@ -253,3 +253,26 @@ def test_host_timeout_returns_and_the_next_call_recovers():
     gpu.trace_blocks(blocks, out=again)
     assert np.array_equal(again, ref)
     del kept
+
+
+def test_plain_frames_replay_a_captured_graph():
+    """A plain frame's device work runs directly on the first call of its
+    shape, is captured into a CUDA graph on the second and replayed after:
+    every call gives the same image and counters.  A camera change (new
+    scene state) runs directly again and matches a fresh scene given the
+    same camera."""
+    scene = scenes.spheres_plane(320, 240, n_spheres=64)
+    gpu = GpuScene(scene)
+    runs = [gpu.render() for _ in range(4)]
+    for img, st in runs[1:]:
+        assert np.array_equal(img, runs[0][0])
+        assert st == runs[0][1]
+    loc, at = (3.0, 6.0, -22.0), (0.5, 0.0, 0.0)
+    gpu.set_camera(loc, at, scene.angle, scene.width, scene.height)
+    moved = [gpu.render()[0] for _ in range(3)]
+    fresh = GpuScene(scene)
+    fresh.set_camera(loc, at, scene.angle, scene.width, scene.height)
+    ref = fresh.render()[0]
+    assert not np.array_equal(ref, runs[0][0])
+    for img in moved:
+        assert np.array_equal(img, ref)
