@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define POV_GPU_ABI_VERSION 1
+#define POV_GPU_ABI_VERSION 2
 
 /* ---- status codes ------------------------------------------------------- */
 #define POV_GPU_OK              0
@@ -312,6 +312,26 @@ typedef struct PovGpuMedia {
     int32_t reserved;
 } PovGpuMedia;
 
+/*
+ * Interior of an object (Interior, source/core/coretypes.h:193-215, after
+ * Interior::PostProcess): what a ray entering or leaving the object through
+ * a transmitting surface sees (ComputeRefraction, trace.cpp:1323-1454;
+ * the fade of ComputeLightedTexture, trace.cpp:1104-1124, and of
+ * ComputeShadowTexture, trace.cpp:1229-1247).  Every object of the reference
+ * has one: the parser gives objects without an interior{} a default one
+ * (Parser::Post_Process, parser.cpp:9225-9230), and a CSG child without its
+ * own shares its parent's (parser.cpp:9040-9044).
+ */
+typedef struct PovGpuInterior {
+    double  ior;              /* IOR (1 by default)                               */
+    double  dispersion;       /* Dispersion (1 = none; the GPU path takes 1 only)  */
+    double  caustics;         /* Caustics (0 = none; the GPU path takes 0 only)    */
+    double  fade_distance;    /* Fade_Distance (0 = no distance attenuation)      */
+    double  fade_power;       /* Fade_Power                                       */
+    float   fade_colour[3];   /* Fade_Colour                                      */
+    float   old_refract;      /* Old_Refract: the legacy `refraction` factor (1)  */
+} PovGpuInterior;
+
 typedef struct PovGpuSceneDesc {
     uint32_t              abi_version;   /* POV_GPU_ABI_VERSION */
     int32_t               num_objects;
@@ -335,6 +355,13 @@ typedef struct PovGpuSceneDesc {
     const PovGpuPattern*  patterns;
     int32_t               num_normals;
     const PovGpuNormal*   normals;
+    /* interiors: object_interior[i] = 1 + index into interiors for object i,
+     * 0 = the default interior (ior 1, no fade); NULL: every object has the
+     * default one */
+    int32_t               num_interiors;
+    const PovGpuInterior* interiors;
+    const int32_t*        object_interior;
+    double                atmosphere_ior;   /* SceneData::atmosphereIOR (1)   */
 } PovGpuSceneDesc;
 
 /* A render block, as POVRect (inclusive bounds) plus its serial number. */

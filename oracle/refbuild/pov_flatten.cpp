@@ -55,6 +55,34 @@ struct Walker
     std::map<const TEXTURE*, int> material_of;
     std::map<const Mesh_Data_Struct*, int> mesh_of;
     std::map<const Interior*, int> media_of;
+    std::map<const Interior*, int> interior_of;
+
+    // Interior (source/core/coretypes.h:193-215) after Interior::PostProcess;
+    // one entry per distinct Interior object (CSG children share their
+    // parent's), 1-based.
+    int InteriorOf(const Interior* in)
+    {
+        if (in == nullptr)
+            return 0;
+        auto it = interior_of.find(in);
+        if (it != interior_of.end())
+            return it->second;
+        PovGpuInterior d;
+        std::memset(&d, 0, sizeof(d));
+        d.ior = in->IOR;
+        d.dispersion = in->Dispersion;
+        d.caustics = in->Caustics;
+        d.fade_distance = in->Fade_Distance;
+        d.fade_power = in->Fade_Power;
+        d.fade_colour[0] = in->Fade_Colour.Red();
+        d.fade_colour[1] = in->Fade_Colour.Green();
+        d.fade_colour[2] = in->Fade_Colour.Blue();
+        d.old_refract = in->Old_Refract;
+        out.interiors.push_back(d);
+        const int idx = (int)out.interiors.size();
+        interior_of[in] = idx;
+        return idx;
+    }
 
     bool Fail(int index, const std::string& what)
     {
@@ -232,6 +260,7 @@ struct Walker
     {
         const int index = (int)out.objects.size();
         out.objects.emplace_back();
+        out.object_interior.push_back(InteriorOf(o->interior.get()));
         PovGpuObject d;
         std::memset(&d, 0, sizeof(d));
         d.parent = parent;
@@ -416,6 +445,10 @@ bool FlattenScene(const SceneData& sd, FlatScene& out, std::string& why)
     d.patterns = out.patterns.data();
     d.num_normals = (int32_t)out.normals.size();
     d.normals = out.normals.data();
+    d.num_interiors = (int32_t)out.interiors.size();
+    d.interiors = out.interiors.data();
+    d.object_interior = out.object_interior.data();
+    d.atmosphere_ior = sd.atmosphereIOR;
     return true;
 }
 
@@ -439,7 +472,7 @@ bool WriteSceneFile(const FlatScene& fs, const char* path)
         return false;
     const PovGpuSceneDesc& d = fs.desc;
     std::fwrite("PGSF", 1, 4, f);
-    Put(f, (uint32_t)1);
+    Put(f, (uint32_t)2);
     Put(f, (uint32_t)POV_GPU_ABI_VERSION);
     Put(f, d.camera);
     std::fwrite(d.background, sizeof(float), 4, f);
@@ -454,6 +487,9 @@ bool WriteSceneFile(const FlatScene& fs, const char* path)
     PutArray(f, fs.medias);
     PutArray(f, fs.patterns);
     PutArray(f, fs.normals);
+    PutArray(f, fs.interiors);
+    PutArray(f, fs.object_interior);
+    Put(f, d.atmosphere_ior);
     Put(f, (uint32_t)fs.meshes.size());
     for (size_t i = 0; i < fs.meshes.size(); i++)
     {

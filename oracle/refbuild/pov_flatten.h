@@ -26,6 +26,8 @@ struct FlatScene
     std::vector<PovGpuMedia>    medias;
     std::vector<PovGpuPattern>  patterns;
     std::vector<PovGpuNormal>   normals;
+    std::vector<PovGpuInterior> interiors;
+    std::vector<int32_t>        object_interior;
     std::vector<PovGpuMesh>     meshes;
     std::vector<std::vector<float>>   mesh_vertices, mesh_normals;
     std::vector<std::vector<int32_t>> mesh_faces, mesh_normal_indices;

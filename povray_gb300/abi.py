@@ -9,7 +9,7 @@ import os
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "lib", "libpovgpu.so")
 
-POV_GPU_ABI_VERSION = 1
+POV_GPU_ABI_VERSION = 2
 
 POV_GPU_OK = 0
 POV_GPU_E_INVALID = -1
@@ -150,6 +150,12 @@ class PovGpuMedia(C.Structure):
                 ("eccentricity", C.c_float), ("reserved", C.c_int32)]
 
 
+class PovGpuInterior(C.Structure):
+    _fields_ = [("ior", C.c_double), ("dispersion", C.c_double), ("caustics", C.c_double),
+                ("fade_distance", C.c_double), ("fade_power", C.c_double), ("fade_colour", C.c_float * 3),
+                ("old_refract", C.c_float)]
+
+
 class PovGpuSceneDesc(C.Structure):
     _fields_ = [("abi_version", C.c_uint32), ("num_objects", C.c_int32),
                 ("objects", C.POINTER(PovGpuObject)), ("num_materials", C.c_int32),
@@ -161,7 +167,9 @@ class PovGpuSceneDesc(C.Structure):
                 ("language_version", C.c_int32), ("radiosity", PovGpuRadiosity),
                 ("num_medias", C.c_int32), ("medias", C.POINTER(PovGpuMedia)),
                 ("num_patterns", C.c_int32), ("patterns", C.POINTER(PovGpuPattern)),
-                ("num_normals", C.c_int32), ("normals", C.POINTER(PovGpuNormal))]
+                ("num_normals", C.c_int32), ("normals", C.POINTER(PovGpuNormal)),
+                ("num_interiors", C.c_int32), ("interiors", C.POINTER(PovGpuInterior)),
+                ("object_interior", C.POINTER(C.c_int32)), ("atmosphere_ior", C.c_double)]
 
 
 class PovGpuBlock(C.Structure):
@@ -224,7 +232,7 @@ class PovGpuLaunchConfig(C.Structure):
 
 
 STRUCTS = {
-    "PovGpuLaunchConfig": PovGpuLaunchConfig, "PovGpuNormal": PovGpuNormal,
+    "PovGpuLaunchConfig": PovGpuLaunchConfig, "PovGpuNormal": PovGpuNormal, "PovGpuInterior": PovGpuInterior,
     "PovGpuObject": PovGpuObject, "PovGpuMaterial": PovGpuMaterial,
     "PovGpuLight": PovGpuLight, "PovGpuMesh": PovGpuMesh, "PovGpuCamera": PovGpuCamera,
     "PovGpuRadiosity": PovGpuRadiosity, "PovGpuSceneDesc": PovGpuSceneDesc,

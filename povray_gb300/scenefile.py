@@ -7,13 +7,15 @@ generator in between.
 Files may be gzip-compressed (name ending in .gz).  Format (little-endian, the C structs of include/povgpu.h laid out as the C
 compiler lays them out on a 64-bit target):
 
-    char[4]  "PGSF";  uint32 format version (1);  uint32 ABI version
+    char[4]  "PGSF";  uint32 format version (2);  uint32 ABI version
     PovGpuCamera camera
     float background[4];  float ambient_light[3]
     int32 max_trace_level;  float adc_bailout;  int32 language_version
     PovGpuRadiosity radiosity
-    for objects, materials, lights, medias, patterns, normals in that order:
-        uint32 count, then count records of the struct
+    for objects, materials, lights, medias, patterns, normals, interiors in
+    that order: uint32 count, then count records of the struct
+    uint32 count, then that many int32: each object's 1-based interior
+    double atmosphere_ior
     uint32 mesh count, then per mesh:
         int32 num_vertices, num_normals, num_triangles, has_normal_indices
         float vertices[3 * num_vertices];  float normals[3 * num_normals]
@@ -29,7 +31,7 @@ import numpy as np
 from . import abi
 
 MAGIC = b"PGSF"
-VERSION = 1
+VERSION = 2
 
 
 class _Reader:
@@ -99,6 +101,10 @@ class ParsedScene:
         self.num_medias, self.medias = r.records(abi.PovGpuMedia)
         self.num_patterns, self.patterns = r.records(abi.PovGpuPattern)
         self.num_normals, self.normals = r.records(abi.PovGpuNormal)
+        self.num_interiors, self.interiors = r.records(abi.PovGpuInterior)
+        no = r.u32()
+        self.object_interior = (C.c_int32 * max(no, 1))(*[r.i32() for _ in range(no)])
+        self.atmosphere_ior = struct.unpack("<d", r.take(8))[0]
         self.meshes = []
         for _ in range(r.u32()):
             nv, nn, nt, has_ni = r.i32(), r.i32(), r.i32(), r.i32()
@@ -118,7 +124,8 @@ class ParsedScene:
         return dict(count=rd.count, recursion_limit=rd.recursion_limit, error_bound=rd.error_bound)
 
     def desc(self):
-        keep = [self.objects, self.materials, self.lights, self.medias, self.patterns, self.normals]
+        keep = [self.objects, self.materials, self.lights, self.medias, self.patterns, self.normals,
+                self.interiors, self.object_interior]
         meshes = (abi.PovGpuMesh * max(len(self.meshes), 1))()
         for i, m in enumerate(self.meshes):
             meshes[i].vertices = m["vertices"].ctypes.data_as(C.POINTER(C.c_float))
@@ -147,6 +154,9 @@ class ParsedScene:
         d.num_medias, d.medias = self.num_medias, self.medias
         d.num_patterns, d.patterns = self.num_patterns, self.patterns
         d.num_normals, d.normals = self.num_normals, self.normals
+        d.num_interiors, d.interiors = self.num_interiors, self.interiors
+        d.object_interior = self.object_interior
+        d.atmosphere_ior = self.atmosphere_ior
         return d, keep
 
     def render_params(self):

@@ -337,11 +337,12 @@ class Normal:
 class Material:
     def __init__(self, rgb, ambient=0.1, diffuse=0.6, phong=0.0, phong_size=40.0,
                  specular=0.0, roughness=0.05, reflection=0.0, brilliance=1.0,
-                 emission=0.0, transmit=0.0, pattern=None, normal=None):
+                 emission=0.0, transmit=0.0, pattern=None, normal=None, filter=0.0):
         self.pattern = pattern
         self.normal = normal
         self.rgb = tuple(float(c) for c in rgb)
         self.transmit = float(transmit)
+        self.filter = float(filter)
         self.ambient = float(ambient)
         self.diffuse = float(diffuse)
         self.phong = float(phong)
@@ -366,6 +367,9 @@ class Material:
             fin += " emission %s" % _g(self.emission)
         if self.pattern is not None:
             pig = self.pattern.sdl()
+        elif self.filter:
+            pig = "color rgbft <%s,%s,%s,%s,%s>" % (_g(self.rgb[0]), _g(self.rgb[1]), _g(self.rgb[2]),
+                                                   _g(self.filter), _g(self.transmit))
         elif self.transmit:
             pig = "color rgbt <%s,%s,%s,%s>" % (_g(self.rgb[0]), _g(self.rgb[1]), _g(self.rgb[2]), _g(self.transmit))
         else:
@@ -375,7 +379,7 @@ class Material:
 
     def desc(self):
         m = abi.PovGpuMaterial()
-        m.pigment[:] = [self.rgb[0], self.rgb[1], self.rgb[2], 0.0, self.transmit]
+        m.pigment[:] = [self.rgb[0], self.rgb[1], self.rgb[2], self.filter, self.transmit]
         m.ambient[:] = [self.ambient] * 3
         m.emission[:] = [self.emission] * 3
         m.diffuse = self.diffuse
@@ -399,6 +403,37 @@ class Material:
         m.crand = 0.0
         m.irid = 0.0
         return m
+
+
+class Interior:
+    """interior { ior fade_distance fade_power fade_color } of an object
+    (Parse_Interior, source/parser/parser_materials.cpp); the defaults are
+    the parser's (Interior::Interior, source/core/material/interior.cpp:
+    58-73, with IOR 0 replaced by the atmosphere's 1.0 in Post_Process)."""
+
+    def __init__(self, ior=1.0, fade_distance=0.0, fade_power=0.0, fade_colour=(0.0, 0.0, 0.0)):
+        self.ior = float(ior)
+        self.fade_distance = float(fade_distance)
+        self.fade_power = float(fade_power)
+        self.fade_colour = tuple(float(c) for c in fade_colour)
+
+    def sdl(self):
+        out = "interior { ior %s" % _g(self.ior)
+        if self.fade_distance or self.fade_power:
+            out += " fade_distance %s fade_power %s fade_color rgb %s" % (
+                _g(self.fade_distance), _g(self.fade_power), _v(self.fade_colour))
+        return out + " }"
+
+    def desc(self):
+        d = abi.PovGpuInterior()
+        d.ior = self.ior
+        d.dispersion = 1.0
+        d.caustics = 0.0
+        d.fade_distance = self.fade_distance
+        d.fade_power = self.fade_power
+        d.fade_colour[:] = list(self.fade_colour)
+        d.old_refract = 1.0
+        return d
 
 
 class Mesh:
@@ -454,9 +489,9 @@ class Scene:
         self.materials.append(m)
         return len(self.materials) - 1
 
-    def sphere(self, centre, radius, mat):
+    def sphere(self, centre, radius, mat, interior=None):
         self.objects.append(dict(type=abi.POV_OBJ_SPHERE, centre=tuple(map(float, centre)),
-                                 radius=float(radius), material=mat))
+                                 radius=float(radius), material=mat, interior=interior))
 
     def plane(self, normal, offset, mat):
         self.objects.append(dict(type=abi.POV_OBJ_PLANE, normal=tuple(map(float, normal)),
@@ -472,14 +507,15 @@ class Scene:
 
     # node helpers (material -1 = inherited from the enclosing CSG)
     @staticmethod
-    def n_sphere(centre, radius, mat=-1):
-        return dict(type=abi.POV_OBJ_SPHERE, centre=tuple(map(float, centre)), radius=float(radius), material=mat)
+    def n_sphere(centre, radius, mat=-1, interior=None):
+        return dict(type=abi.POV_OBJ_SPHERE, centre=tuple(map(float, centre)), radius=float(radius), material=mat,
+                    interior=interior)
 
     @staticmethod
-    def n_box(c1, c2, mat=-1):
+    def n_box(c1, c2, mat=-1, interior=None):
         lo = tuple(min(float(a), float(b)) for a, b in zip(c1, c2))
         hi = tuple(max(float(a), float(b)) for a, b in zip(c1, c2))
-        return dict(type=abi.POV_OBJ_BOX, c1=lo, c2=hi, material=mat)
+        return dict(type=abi.POV_OBJ_BOX, c1=lo, c2=hi, material=mat, interior=interior)
 
     @staticmethod
     def n_torus(major, minor, rotate=(0.0, 0.0, 0.0), translate=(0.0, 0.0, 0.0), mat=-1):
@@ -488,7 +524,7 @@ class Scene:
                     mods="rotate %s translate %s" % (_v(rotate), _v(translate)), material=mat)
 
     @staticmethod
-    def n_csg(kind, children, translate=(0.0, 0.0, 0.0), mat=-1):
+    def n_csg(kind, children, translate=(0.0, 0.0, 0.0), mat=-1, interior=None):
         """kind: 'union', 'intersection', 'difference' or 'merge'.  The
         translation is applied to the children as the parser does
         (Sphere/Box::Translate move the geometry; CSG::Translate recurses)."""
@@ -511,7 +547,7 @@ class Scene:
                 c["inverted"] = True
         t = {"union": abi.POV_OBJ_UNION, "intersection": abi.POV_OBJ_INTERSECTION,
              "difference": abi.POV_OBJ_INTERSECTION, "merge": abi.POV_OBJ_MERGE}[kind]
-        return dict(type=t, kind=kind, children=moved, translate=tv, material=mat)
+        return dict(type=t, kind=kind, children=moved, translate=tv, material=mat, interior=interior)
 
     def media_box(self, c1, c2, scattering=(0.05, 0.05, 0.05), absorption=(0.0, 0.0, 0.0),
                   emission=(0.0, 0.0, 0.0), intervals=10, samples=10, aa_level=3, aa_threshold=0.1):
@@ -594,6 +630,8 @@ class Scene:
 
     def _sdl_node(self, o):
         tex = (" " + self.materials[o["material"]].sdl()) if o.get("material", -1) >= 0 else ""
+        if o.get("interior") is not None:
+            tex += " " + o["interior"].sdl()
         t = o["type"]
         if t == abi.POV_OBJ_SPHERE:
             return "sphere { %s, %s%s }" % (_v(o.get("sdl_centre", o["centre"])), _g(o["radius"]), tex)
@@ -755,6 +793,25 @@ class Scene:
         desc.num_normals = len(nrms)
         desc.normals = normals
         keep.append(normals)
+        # interiors: every object has one (Parser::Post_Process gives an
+        # object without interior{} a default one, parser.cpp:9225-9230, and
+        # a CSG child without its own its parent's, parser.cpp:9040-9044)
+        ints, obj_int = [], (C.c_int32 * max(n, 1))()
+        for i, (o, parent) in enumerate(flat):
+            if o.get("interior") is not None:
+                ints.append(o["interior"].desc())
+                obj_int[i] = len(ints)
+            elif parent >= 0:
+                obj_int[i] = obj_int[parent]
+            else:
+                ints.append(Interior().desc())
+                obj_int[i] = len(ints)
+        interiors = (abi.PovGpuInterior * max(len(ints), 1))(*ints)
+        desc.num_interiors = len(ints)
+        desc.interiors = interiors
+        desc.object_interior = obj_int
+        desc.atmosphere_ior = 1.0
+        keep += [interiors, obj_int]
         if self.radiosity is not None:
             r = self.radiosity_settings()
             rd = desc.radiosity

@@ -82,6 +82,15 @@ def test_reference_flattened_scene_equals_generator_desc(case):
         assert (ma >= 0) == (mb >= 0), i
         if ma >= 0:
             _close("material of object %d" % i, a.materials[ma], b.materials[mb], 1e-7)
+    # interiors: the same content per object, and the same sharing (which
+    # objects have one interior between them)
+    assert abs(a.atmosphere_ior - b.atmosphere_ior) == 0.0
+    for i in range(a.num_objects):
+        ia, ib = a.object_interior[i], b.object_interior[i]
+        assert ia > 0 and ib > 0, i
+        _close("interior of object %d" % i, a.interiors[ia - 1], b.interiors[ib - 1], 1e-7)
+        for j in range(i):
+            assert (a.object_interior[j] == ia) == (b.object_interior[j] == ib), (i, j)
     for i in range(a.num_lights):
         _close("light %d" % i, a.lights[i], b.lights[i], 1e-7)
     for i in range(a.num_medias):
@@ -106,4 +115,4 @@ def test_scene_file_rejects_damage(tmp_path):
     bad.write_bytes(b"XXXX" + data[4:])
     with pytest.raises(ValueError):
         ParsedScene(str(bad), 320, 240)
-    assert abi.POV_GPU_ABI_VERSION == 1
+    assert abi.POV_GPU_ABI_VERSION == 2
