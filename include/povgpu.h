@@ -404,6 +404,8 @@ typedef struct PovGpuStats {
     uint64_t nic_val_error_ppm;     /* its held-out relative RMSE, parts per million */
     uint64_t transmitted_rays;      /* Transmitted_Rays_Traced              */
     uint64_t media_samples;         /* Media_Samples                        */
+    uint64_t refracted_rays;        /* Refracted_Rays_Traced                */
+    uint64_t internal_reflected_rays; /* Internal_Reflected_Rays_Traced     */
 } PovGpuStats;
 
 /* One closest-hit result of pov_gpu_trace_rays. */

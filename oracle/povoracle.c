@@ -473,6 +473,14 @@ struct PovOracle {
     int32_t  top_linear;     /* no slabs: linear scan (trace.cpp:263) */
     struct RadCache* rad;    /* radiosity sample cache (mutable during a render) */
     int32_t  gt_count[8];    /* converged mode: directions per query and depth (0 = off) */
+    /* interiors: one id per object (CSG children share their parent's),
+     * the interiors' parameters, the atmosphere's IOR; transparent = some
+     * surface filters or transmits (outside media containers) */
+    int32_t* obj_int;
+    PovGpuInterior* ints;
+    int32_t  nints;
+    double   atm_ior;
+    int      transparent;
 };
 
 static int max3_coordinate(double x, double y, double z)  /* mathutil */
@@ -1075,6 +1083,8 @@ static V3 torus_normal(const PovGpuObject* o, V3 ip)
     return vnorm(mtrans_normal(o->trans + 16, vsub(P, M)));
 }
 
+#define MAX_RIN 16   /* interiors a ray can be inside at once */
+
 typedef struct {
     PQueue  pq;       /* top-level queue */
     PQueue  mpq;      /* mesh queue (mesh.cpp:110 keeps a thread-local one) */
@@ -1091,6 +1101,11 @@ typedef struct {
     int      rad_dir_index[8];
     uint64_t rad_top_queries;
     uint64_t gt_rng;          /* converged mode: the pixel's random sequence */
+    /* the current ray's interior list (Ray::GetInteriors): interior ids of
+     * the objects the ray travels inside, innermost last */
+    int      rin[MAX_RIN];
+    int      nrin;
+    uint64_t refracted, internal_reflected;
 } Thread;
 
 /* Sphere::Intersect (sphere.cpp:214-245). */
@@ -2121,6 +2136,45 @@ static int container_media(const PovOracle* S, int32_t oi)
     return (o->media > 0 && (o->flags & POV_FLAG_HOLLOW)) ? o->media - 1 : -1;
 }
 
+/* Transparent surfaces.  TransColour::TransmittedColour (colour.h:1912):
+ * pigment * filter + transmit, in float. */
+static void transmitted_colour(const PovGpuMaterial* m, const float pig[3], float out[3])
+{
+    for (int k = 0; k < 3; k++)
+        out[k] = pig[k] * m->pigment[3] + m->pigment[4];
+}
+
+/* Object::IsOpaque (OPAQUE_FLAG, parser.cpp:9296-9297): a leaf whose plain
+ * pigment neither filters nor transmits; a CSG whose children all are. */
+static int object_opaque(const PovOracle* S, int32_t oi)
+{
+    const PovGpuObject* o = &S->objs[oi].o;
+    if (o->type >= POV_OBJ_UNION) {
+        for (int c = 0; c < o->num_children; c++)
+            if (!object_opaque(S, o->first_child + c))
+                return 0;
+        return 1;
+    }
+    const PovGpuMaterial* m = object_material(S, oi);
+    return m->pigment[3] == 0.0f && m->pigment[4] == 0.0f;
+}
+
+/* Ray::IsInterior: the current ray's interior list holds `id`. */
+static int ray_inside(const Thread* th, int id)
+{
+    for (int i = 0; i < th->nrin; i++)
+        if (th->rin[i] == id)
+            return 1;
+    return 0;
+}
+
+static int top_ancestor(const PovOracle* S, int32_t oi)
+{
+    while (S->objs[oi].o.parent >= 0)
+        oi = S->objs[oi].o.parent;
+    return oi;
+}
+
 /* Ray flags: the medium a ray travels in (the object id of its media
  * container, the reference's interior list, which containers that do not
  * overlap keep at one entry) rides in bits 8 and up. */
@@ -2138,6 +2192,12 @@ static int container_media(const PovOracle* S, int32_t oi)
 static int shadow_trace(const PovOracle* S, Thread* th, V3 P, V3 L, double dist, int medium, int media_on,
                         double lc[3])
 {
+    const double shadow_adc = S->desc.adc_bailout;
+    /* the shadow ray's own interior list (Ray lightsourceray(eye)): a copy
+     * of the eye ray's, toggled at every transparent surface it passes
+     * (ComputeShadowMedia, trace.cpp:3065-3068) */
+    int rin[MAX_RIN], nrin = th->nrin;
+    memcpy(rin, th->rin, sizeof(int) * (size_t)nrin);
     V3 O = P;
     double depth = dist;
     for (;;) {
@@ -2148,8 +2208,60 @@ static int shadow_trace(const PovOracle* S, Thread* th, V3 P, V3 L, double dist,
             return 0;
         th->shadow_succeeded++;
         int mi = container_media(S, is.object);
-        if (mi < 0)
+        if (mi < 0 && !S->transparent)
             return 1;
+        if (mi < 0) {
+            /* ComputeShadowColour (trace.cpp:2274-2439) for plain textures:
+             * an opaque surface clears the light; a transparent one filters
+             * it by its TransmittedColour and, when the ray is inside the
+             * object's interior, its fade (ComputeShadowTexture,
+             * trace.cpp:1180-1250); below ADC_Bailout the light is cleared
+             * (trace.cpp:2412-2417).  The ray goes on unless the light is
+             * gone and the object (the CSG it belongs to) is opaque
+             * (TracePointLightShadowRay, trace.cpp:2040-2072). */
+            const PovGpuMaterial* m = object_material(S, is.object);
+            if (m->pigment[3] == 0.0f && m->pigment[4] == 0.0f) {
+                lc[0] = lc[1] = lc[2] = 0.0;
+            } else {
+                float pig[3] = {m->pigment[0], m->pigment[1], m->pigment[2]}, fc[3];
+                transmitted_colour(m, pig, fc);
+                const int id = S->obj_int[is.object];
+                const PovGpuInterior* I = &S->ints[id];
+                int in = -1;
+                for (int k = 0; k < nrin; k++)
+                    if (rin[k] == id) { in = k; break; }
+                if (in >= 0 && I->fade_power > 0.0 && fabs(I->fade_distance) > EPSILON) {
+                    for (int k = 0; k < 3; k++) {
+                        if (I->fade_power >= 1000.0)
+                            fc[k] = (float)(fc[k] * exp(-(1.0 - I->fade_colour[k]) * (is.depth / I->fade_distance)));
+                        else
+                            fc[k] = (float)(fc[k] * (I->fade_colour[k] + (1.0 - I->fade_colour[k]) /
+                                                     (1.0 + pow(is.depth / I->fade_distance, I->fade_power))));
+                    }
+                }
+                if (fabs((double)((fabsf(fc[0]) + fabsf(fc[1]) + fabsf(fc[2])) / 3.0)) < shadow_adc) {
+                    lc[0] = lc[1] = lc[2] = 0.0;
+                } else {
+                    for (int k = 0; k < 3; k++)
+                        lc[k] = (float)((float)lc[k] * fc[k]);
+                    if (!(fabs(lc[0]) < EPSILON && fabs(lc[1]) < EPSILON && fabs(lc[2]) < EPSILON)) {
+                        if (in >= 0) {   /* leaving: removed */
+                            for (int k = in; k + 1 < nrin; k++)
+                                rin[k] = rin[k + 1];
+                            nrin--;
+                        } else if (nrin < MAX_RIN) {   /* entering: appended */
+                            rin[nrin++] = id;
+                        }
+                    }
+                }
+            }
+            if (fabs(lc[0]) < EPSILON && fabs(lc[1]) < EPSILON && fabs(lc[2]) < EPSILON &&
+                object_opaque(S, top_ancestor(S, is.object)))
+                return 1;
+            depth -= is.depth;
+            O = is.ipoint;
+            continue;
+        }
         if (medium >= 0 && media_on) {
             th->media_samples++;   /* the shadow ray's one media sample (media.cpp:384-398) */
             const PovGpuMedia* md = &S->desc.medias[container_media(S, medium)];
@@ -2292,8 +2404,79 @@ static void compute_reflection(const PovOracle* S, Thread* th, V3 ip, V3 D, V3 N
     trace_ray(S, th, ip, nd, weight, tk, flags & ~RAY_CONTINUED, col);   /* SetFlags(ReflectionRay, ray) */
 }
 
+/* ComputeRefraction / TraceRefractionRay (trace.cpp:1323-1486) through the
+ * surface of object `oi` at `is`: the ray's interior list changes as the
+ * reference changes it (entering: appended; leaving the innermost:
+ * removed; leaving an overlap: removed with ior 1; entering within
+ * another: appended), the ior ratio follows; equal iors trace the
+ * continued ray (Transmitted_Rays_Traced, same trace level), otherwise
+ * Heckbert's refraction, or on total internal reflection the mirror ray of
+ * the unchanged ray (Internal_Reflected_Rays_Traced).  Returns 1 on total
+ * internal reflection. */
+static int compute_refraction(const PovOracle* S, Thread* th, const Isect* is, V3 D, V3 N, V3 raw, double weight,
+                              Ticket* tk, int flags, RGB* out)
+{
+    const int id = S->obj_int[is->object];
+    const PovGpuInterior* I = &S->ints[id];
+    int saved[MAX_RIN];
+    const int nsaved = th->nrin;
+    memcpy(saved, th->rin, sizeof(int) * (size_t)nsaved);
+    double ior;
+    if (th->nrin == 0) {
+        th->rin[th->nrin++] = id;
+        ior = S->atm_ior / I->ior;
+    } else if (th->rin[th->nrin - 1] == id) {
+        th->nrin--;
+        ior = th->nrin == 0 ? I->ior / S->atm_ior : I->ior / S->ints[th->rin[th->nrin - 1]].ior;
+    } else {
+        int found = -1;
+        for (int i = 0; i < th->nrin; i++)
+            if (th->rin[i] == id) { found = i; break; }
+        if (found >= 0) {
+            for (int i = found; i + 1 < th->nrin; i++)
+                th->rin[i] = th->rin[i + 1];
+            th->nrin--;
+            ior = 1.0;
+        } else {
+            ior = S->ints[th->rin[th->nrin - 1]].ior / I->ior;
+            if (th->nrin < MAX_RIN)
+                th->rin[th->nrin++] = id;
+        }
+    }
+    int tir = 0;
+    if (fabs(ior - 1.0) < EPSILON) {
+        th->transmitted++;   /* Transmitted_Rays_Traced */
+        trace_ray(S, th, is->ipoint, D, weight, tk, flags | RAY_CONTINUED, out);
+    } else {
+        double n = vdot(D, N);
+        V3 ln = N;
+        if (n <= 0.0)
+            n = -n;
+        else
+            ln = vmul(N, -1.0);
+        double t = 1.0 + ior * ior * (n * n - 1.0);
+        if (t < 0.0) {
+            th->internal_reflected++;   /* Internal_Reflected_Rays_Traced */
+            th->nrin = nsaved;          /* the mirror ray keeps the incoming ray's interiors */
+            memcpy(th->rin, saved, sizeof(int) * (size_t)nsaved);
+            compute_reflection(S, th, is->ipoint, D, N, raw, weight, tk, flags, out);
+            tir = 1;
+        } else {
+            t = ior * n - sqrt(t);
+            V3 nd = vadd(vmul(D, ior), vmul(ln, t));
+            th->refracted++;   /* Refracted_Rays_Traced */
+            trace_ray(S, th, is->ipoint, nd, weight, tk, flags & ~RAY_CONTINUED, out);
+        }
+    }
+    th->nrin = nsaved;
+    memcpy(th->rin, saved, sizeof(int) * (size_t)nsaved);
+    return tir;
+}
+
 /* ComputeTextureColour + ComputeLightedTexture (trace.cpp:457-586,739-1179)
- * for one plain layer with an opaque pigment. */
+ * for one plain layer; a pigment that filters or transmits gives its own
+ * light scaled by its opacity and passes the transmitted ray's colour
+ * through its filter colour. */
 static void shade(const PovOracle* S, Thread* th, const Isect* is, V3 D, double weight, Ticket* tk, int flags,
                   RGB* out)
 {
@@ -2327,6 +2510,15 @@ static void shade(const PovOracle* S, Thread* th, const Isect* is, V3 D, double 
         N = perturb_normal(nm, &S->desc.patterns[nm->pattern - 1], ip, raw);
     }
     double r = 0.0, g = 0.0, b = 0.0;
+    /* a transparent layer's own light is scaled by its opacity, 1 - filter -
+     * transmit (TransColour::Opacity; LegacyOpacity before 3.7,
+     * trace.cpp:877-881) */
+    const float filt = m->pigment[3], trm = m->pigment[4];
+    const int see_through = filt != 0.0f || trm != 0.0f;
+    double att = 1.0;
+    if (see_through)
+        att = S->desc.language_version < 370 ? (float)(1.0 - (filt * fmaxf(pig.r, fmaxf(pig.g, pig.b)) + trm))
+                                             : (float)(1.0 - filt - trm);
 
     /* ComputeReflectivity (trace.cpp:2627-2656), non-fresnel */
     double cos_inc = -vdot(D, N);
@@ -2365,9 +2557,9 @@ static void shade(const PovOracle* S, Thread* th, const Isect* is, V3 D, double 
     double em[3];
     for (int k = 0; k < 3; k++)
         em[k] = m->emission[k] + (radiosity ? 0.0 : m->ambient[k] * S->desc.ambient_light[k]);
-    r += pig.r * em[0];
-    g += pig.g * em[1];
-    b += pig.b * em[2];
+    r += pig.r * em[0] * att;
+    g += pig.g * em[1] * att;
+    b += pig.b * em[2] * att;
 
     /* ComputeDiffuseLight (trace.cpp:1488-1510,1637-1729) */
     if (m->diffuse != 0.0f || m->diffuse_back != 0.0f || m->specular != 0.0f || m->phong != 0.0f) {
@@ -2410,7 +2602,7 @@ static void shade(const PovOracle* S, Thread* th, const Isect* is, V3 D, double 
             if (diffuse > 0.0) {
                 double ci = vdot(N, ld);
                 double inten = m->brilliance != 1.0f ? pow(fabs(ci), m->brilliance) : fabs(ci);
-                inten *= diffuse;
+                inten *= diffuse * att;
                 r += inten * pig.r * lc[0];
                 g += inten * pig.g * lc[1];
                 b += inten * pig.b * lc[2];
@@ -2444,8 +2636,49 @@ static void shade(const PovOracle* S, Thread* th, const Isect* is, V3 D, double 
         }
     }
 
-    /* reflected component (trace.cpp:1155-1178) */
-    if (!(reflec.r == 0.0f && reflec.g == 0.0f && reflec.b == 0.0f)) {
+    /* transmitted component (trace.cpp:1063-1142): the filter colour
+     * TransmittedColour, trans = its greyscale; above ADC_Bailout the
+     * refracted ray at weight * max|filter|, attenuated by Old_Refract and,
+     * leaving the object's interior, its fade; not filtered after total
+     * internal reflection */
+    int tir = 0;
+    if (see_through) {
+        float pf[3] = {pig.r, pig.g, pig.b}, fil[3];
+        transmitted_colour(m, pf, fil);
+        const double trans = fmin(1.0, fabs((double)(float)(0.297 * fil[0] + 0.589 * fil[1] + 0.114 * fil[2])));
+        if (trans > tk->adc) {
+            const double w1 = fmax(fabs(fil[0]), fmax(fabs(fil[1]), fabs(fil[2])));
+            const int id = S->obj_int[is->object];
+            const PovGpuInterior* I = &S->ints[id];
+            const int leaving = ray_inside(th, id);
+            RGB rc = {0, 0, 0};
+            tir = compute_refraction(S, th, is, D, N, raw, weight * w1, tk, flags, &rc);
+            float ac[3] = {I->old_refract, I->old_refract, I->old_refract};
+            if (leaving && fabs(I->fade_distance) > EPSILON) {
+                for (int k = 0; k < 3; k++) {
+                    if (I->fade_power >= 1000.0)
+                        ac[k] = (float)(ac[k] * exp(-(1.0 - I->fade_colour[k]) * (is->depth / I->fade_distance)));
+                    else
+                        ac[k] = (float)(ac[k] * (I->fade_colour[k] + (1.0 - I->fade_colour[k]) /
+                                                 (1.0 + pow(is->depth / I->fade_distance, I->fade_power))));
+                }
+            }
+            if (tir) {
+                r += ac[0] * rc.r;
+                g += ac[1] * rc.g;
+                b += ac[2] * rc.b;
+            } else {
+                r += ac[0] * rc.r * fil[0];
+                g += ac[1] * rc.g * fil[1];
+                b += ac[2] * rc.b * fil[2];
+            }
+        }
+    }
+
+    /* reflected component (trace.cpp:1155-1178); after total internal
+     * reflection only layers whose normal differs from the top one
+     * reflect (a single layer: none) */
+    if (!tir && !(reflec.r == 0.0f && reflec.g == 0.0f && reflec.b == 0.0f)) {
         RGB rc = {0, 0, 0};
         compute_reflection(S, th, ip, D, N, raw, rweight, tk, flags, &rc);
         r += reflec.r * rc.r;
@@ -3350,7 +3583,9 @@ int pov_oracle_create(const PovGpuSceneDesc* desc, PovOracle** out, int32_t* bad
         const PovGpuMaterial* m = (o->material >= 0 && o->material < desc->num_materials) ? &desc->materials[o->material]
                                                                                            : NULL;
         int transmits = m && (m->pigment[3] != 0.0f || m->pigment[4] != 0.0f);
-        if (o->media > 0 || transmits) {
+        if (o->media == 0 && transmits)
+            continue;   /* a transparent surface (checked below) */
+        if (o->media > 0) {
             if (bad_index) *bad_index = i;
             const PovGpuMedia* md = o->media > 0 ? &desc->medias[o->media - 1] : NULL;
             if (!md || o->type != POV_OBJ_BOX || !(o->flags & POV_FLAG_HOLLOW) || o->parent >= 0 || !m ||
@@ -3374,6 +3609,38 @@ int pov_oracle_create(const PovGpuSceneDesc* desc, PovOracle** out, int32_t* bad
         }
     }
     if (bad_index) *bad_index = -1;
+    /* transparent surfaces (filter or transmit outside media containers):
+     * plain pigments, interiors without dispersion or caustics; not with
+     * media containers, radiosity or area lights (whose shadow colours
+     * would need the filtered form of TraceAreaLightShadowRay) */
+    int transparent = 0;
+    for (int i = 0; i < desc->num_materials; i++) {
+        const PovGpuMaterial* m = &desc->materials[i];
+        int used_by_container = 0;
+        for (int k = 0; k < desc->num_objects; k++)
+            used_by_container = used_by_container || (desc->objects[k].media > 0 && desc->objects[k].material == i);
+        if ((m->pigment[3] != 0.0f || m->pigment[4] != 0.0f) && !used_by_container) {
+            if (m->pattern != 0)
+                return POV_GPU_E_UNSUPPORTED;
+            transparent = 1;
+        }
+    }
+    if (desc->num_interiors < 0 || (desc->num_interiors > 0 && !desc->interiors))
+        return POV_GPU_E_INVALID;
+    if (desc->object_interior)
+        for (int i = 0; i < desc->num_objects; i++)
+            if (desc->object_interior[i] < 0 || desc->object_interior[i] > desc->num_interiors)
+                return POV_GPU_E_INVALID;
+    if (transparent) {
+        if (containers || desc->radiosity.enabled)
+            return POV_GPU_E_UNSUPPORTED;
+        for (int i = 0; i < desc->num_interiors; i++)
+            if (desc->interiors[i].dispersion != 1.0 || desc->interiors[i].caustics != 0.0)
+                return POV_GPU_E_UNSUPPORTED;
+        for (int i = 0; i < desc->num_lights; i++)
+            if (desc->lights[i].kind != POV_LIGHT_POINT)
+                return POV_GPU_E_UNSUPPORTED;
+    }
     for (int i = 0; i < desc->num_lights; i++) {
         const PovGpuLight* L = &desc->lights[i];
         if (containers && L->kind != POV_LIGHT_POINT)
@@ -3501,6 +3768,43 @@ int pov_oracle_create(const PovGpuSceneDesc* desc, PovOracle** out, int32_t* bad
         build_bbox_tree(&S->top, finite, nf, infinite, ni);
     free(finite);
     free(infinite);
+    /* interiors: the description's, plus a default one (ior = the
+     * atmosphere's, Post_Process, parser.cpp:9225-9267) for every top-level
+     * object given none; CSG children without their own share their
+     * parent's (parser.cpp:9040-9044) */
+    S->atm_ior = desc->atmosphere_ior > 0.0 ? desc->atmosphere_ior : 1.0;
+    S->transparent = transparent;
+    S->ints = (PovGpuInterior*)calloc((size_t)(desc->num_interiors + S->nobjs + 1), sizeof(PovGpuInterior));
+    S->obj_int = (int32_t*)malloc(sizeof(int32_t) * (size_t)(S->nobjs + 1));
+    if (desc->num_interiors > 0)
+        memcpy(S->ints, desc->interiors, sizeof(PovGpuInterior) * (size_t)desc->num_interiors);
+    S->nints = desc->num_interiors;
+    for (int i = 0; i < S->nobjs; i++) {
+        const int32_t given = desc->object_interior ? desc->object_interior[i] : 0;
+        const int32_t parent = S->objs[i].o.parent;
+        if (given > 0) {
+            S->obj_int[i] = given - 1;
+        } else if (parent >= 0) {
+            S->obj_int[i] = S->obj_int[parent];
+        } else {
+            PovGpuInterior* d = &S->ints[S->nints];
+            d->ior = S->atm_ior;
+            d->dispersion = 1.0;
+            d->old_refract = 1.0f;
+            S->obj_int[i] = S->nints++;
+        }
+    }
+    /* camera rays start with no interior (TracePixel::InitRayContainerState,
+     * tracepixel.cpp:929-963, would list the objects around the camera in
+     * the bounding tree's order): with transparent surfaces the camera must
+     * be inside no object */
+    if (transparent)
+        for (int i = 0; i < S->nobjs; i++)
+            if (S->objs[i].o.parent < 0 && inside_object(S, i, vload(desc->camera.location))) {
+                if (bad_index) *bad_index = i;
+                pov_oracle_destroy(S);
+                return POV_GPU_E_UNSUPPORTED;
+            }
     *out = S;
     return POV_GPU_OK;
 }
@@ -3521,6 +3825,8 @@ void pov_oracle_destroy(PovOracle* S)
     free(S->objs);
     free(S->mats);
     free(S->lights);
+    free(S->ints);
+    free(S->obj_int);
     rad_free(S->rad);
     free(S);
 }
@@ -3737,6 +4043,8 @@ static void* render_worker_aa(void* arg)
     J->stats.shadow_ray_tests += th.shadow_tests;
     J->stats.shadow_rays_succeeded += th.shadow_succeeded;
     J->stats.reflected_rays += th.reflected;
+    J->stats.refracted_rays += th.refracted;
+    J->stats.internal_reflected_rays += th.internal_reflected;
     J->stats.transmitted_rays += th.transmitted;
     J->stats.media_samples += th.media_samples;
     J->stats.number_of_pixels += pixels;
@@ -3770,6 +4078,8 @@ static void* render_worker(void* arg)
     J->stats.shadow_ray_tests += th.shadow_tests;
     J->stats.shadow_rays_succeeded += th.shadow_succeeded;
     J->stats.reflected_rays += th.reflected;
+    J->stats.refracted_rays += th.refracted;
+    J->stats.internal_reflected_rays += th.internal_reflected;
     J->stats.transmitted_rays += th.transmitted;
     J->stats.media_samples += th.media_samples;
     pthread_mutex_unlock(&J->lock);
@@ -3872,6 +4182,8 @@ static int render_radiosity(PovOracle* S, const PovGpuRenderParams* p, int32_t x
         stats->shadow_ray_tests = th.shadow_tests;
         stats->shadow_rays_succeeded = th.shadow_succeeded;
         stats->reflected_rays = th.reflected;
+        stats->refracted_rays = th.refracted;
+        stats->internal_reflected_rays = th.internal_reflected;
         stats->transmitted_rays = th.transmitted;
         stats->media_samples = th.media_samples;
         stats->number_of_pixels = (uint64_t)(x1 - x0) * (uint64_t)(y1 - y0) + R->pixels;

@@ -178,11 +178,13 @@ void PrintStats(TraceThreadData& td)
     RenderStatistics& st = td.Stats();
     std::printf("{\"number_of_rays\": %llu, \"shadow_ray_tests\": %llu, \"shadow_rays_succeeded\": %llu, "
                 "\"reflected_rays\": %llu, \"shadow_cache_hits\": %llu, \"transmitted_rays\": %llu, "
-                "\"media_samples\": %llu, \"media_intervals\": %llu}\n",
+                "\"media_samples\": %llu, \"media_intervals\": %llu, \"refracted_rays\": %llu, "
+                "\"internal_reflected_rays\": %llu}\n",
                 (unsigned long long)st[Number_Of_Rays], (unsigned long long)st[Shadow_Ray_Tests],
                 (unsigned long long)st[Shadow_Rays_Succeeded], (unsigned long long)st[Reflected_Rays_Traced],
                 (unsigned long long)st[Shadow_Cache_Hits], (unsigned long long)st[Transmitted_Rays_Traced],
-                (unsigned long long)st[Media_Samples], (unsigned long long)st[Media_Intervals]);
+                (unsigned long long)st[Media_Samples], (unsigned long long)st[Media_Intervals],
+                (unsigned long long)st[Refracted_Rays_Traced], (unsigned long long)st[Internal_Reflected_Rays_Traced]);
 }
 
 void Vec(FILE *f, const char *name, const Vector3d& v)

@@ -192,7 +192,8 @@ class PovGpuStats(C.Structure):
                 ("device_error", C.c_uint64), ("radiosity_rays", C.c_uint64),
                 ("radiosity_gathers_d0", C.c_uint64), ("radiosity_gathers_d1", C.c_uint64),
                 ("nic_answers", C.c_uint64), ("nic_val_error_ppm", C.c_uint64),
-                ("transmitted_rays", C.c_uint64), ("media_samples", C.c_uint64)]
+                ("transmitted_rays", C.c_uint64), ("media_samples", C.c_uint64),
+                ("refracted_rays", C.c_uint64), ("internal_reflected_rays", C.c_uint64)]
 
     def as_dict(self):
         return {k: int(getattr(self, k)) for k, _ in self._fields_ if k != "reserved"}

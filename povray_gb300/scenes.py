@@ -1154,6 +1154,52 @@ def textured_spheres(width=320, height=240, n_spheres=12, seed=6, noise_generato
     return s
 
 
+def glass_spheres(width=320, height=240, max_trace_level=10):
+    """Refraction and interiors: over a checker floor (plane y=-1) and a
+    checker wall (z=9), transparent spheres -- clear glass (rgb 1, filter
+    0.9, ior 1.5), tinted glass (rgb <1,0.45,0.45>, filter 0.85, ior 1.33),
+    a transmit-only ball (transmit 0.7, ior 1: transmitted rays), dense glass
+    (ior 2.4: total internal reflection towards its rim), a fading sphere
+    (fade_distance 1.2, fade_power 2, fade colour <0.4,0.7,1>), an
+    exponential fade (fade_power 1001), a big glass sphere holding a small
+    one of another ior, two overlapping glass spheres, a glass CSG
+    intersection of a sphere and a box (one interior) -- in front of three
+    opaque spheres; two point lights whose shadows pass through the glass.
+    Transparent surfaces have phong highlights but no reflection.  Camera
+    (0,3,-12) looking at (0,0.5,0), 55 deg; max_trace_level 10."""
+    s = Scene("glass_spheres", width, height, (0.0, 3.0, -12.0), (0.0, 0.5, 0.0), 55.0,
+              max_trace_level=max_trace_level)
+    s.point_light((8.0, 14.0, -10.0))
+    s.point_light((-10.0, 9.0, -4.0), (0.5, 0.5, 0.55))
+    floor = Pattern("checker", [(0.0, (0.9, 0.9, 0.85)), (1.0, (0.2, 0.3, 0.55))], [("scale", (1.0, 1.0, 1.0))])
+    wall = Pattern("checker", [(0.0, (0.85, 0.6, 0.3)), (1.0, (0.95, 0.95, 0.9))], [("scale", (1.5, 1.5, 1.5))])
+    s.plane((0.0, 1.0, 0.0), -1.0, s.material(Material((1.0, 1.0, 1.0), pattern=floor)))
+    s.plane((0.0, 0.0, -1.0), -9.0, s.material(Material((1.0, 1.0, 1.0), pattern=wall)))
+    for c, r, rgb in (((-3.0, 0.2, 5.0), 1.2, (0.8, 0.2, 0.15)), ((1.5, 0.0, 6.0), 1.0, (0.2, 0.7, 0.25)),
+                      ((4.5, 0.5, 4.0), 1.5, (0.25, 0.3, 0.85))):
+        s.sphere(c, r, s.material(Material(rgb, phong=0.4)))
+
+    def glass(rgb=(1.0, 1.0, 1.0), filter=0.0, transmit=0.0):
+        return s.material(Material(rgb, ambient=0.0, diffuse=0.1, phong=0.8, phong_size=80.0, filter=filter,
+                                   transmit=transmit))
+    s.sphere((-4.2, 0.0, 0.0), 1.0, glass(filter=0.9), Interior(ior=1.5))
+    s.sphere((-1.8, 0.0, -0.5), 1.0, glass((1.0, 0.45, 0.45), filter=0.85), Interior(ior=1.33))
+    s.sphere((0.6, 0.0, 0.0), 1.0, glass((0.6, 0.9, 0.6), transmit=0.7), Interior(ior=1.0))
+    s.sphere((3.0, 0.0, -0.5), 1.0, glass(filter=0.95), Interior(ior=2.4))
+    s.sphere((-3.0, 2.6, 1.5), 0.9, glass(filter=0.9),
+             Interior(ior=1.45, fade_distance=1.2, fade_power=2.0, fade_colour=(0.4, 0.7, 1.0)))
+    s.sphere((-0.6, 2.7, 1.8), 0.9, glass(filter=0.9),
+             Interior(ior=1.2, fade_distance=0.8, fade_power=1001.0, fade_colour=(1.0, 0.6, 0.3)))
+    s.sphere((2.4, 2.8, 2.0), 1.3, glass(filter=0.92), Interior(ior=1.5))          # holds the next one
+    s.sphere((2.4, 2.8, 2.0), 0.5, glass((0.5, 0.6, 1.0), filter=0.8), Interior(ior=1.9))
+    s.sphere((-5.0, 2.4, 3.5), 0.8, glass(filter=0.9), Interior(ior=1.3))             # two overlapping
+    s.sphere((-4.3, 2.6, 3.3), 0.7, glass((1.0, 1.0, 0.6), filter=0.9), Interior(ior=1.6))
+    s.add(Scene.n_csg("intersection", [Scene.n_sphere((0.0, 0.0, 0.0), 0.9),
+                                       Scene.n_box((-0.65, -0.65, -0.65), (0.65, 0.65, 0.65))],
+                      translate=(5.3, 0.0, 1.0), mat=glass((0.7, 0.8, 1.0), filter=0.9), interior=Interior(ior=1.5)))
+    return s
+
+
 def bumpy_spheres(width=320, height=240, n_spheres=12, seed=7, noise_generator=None, waves=False):
     """Normal perturbation: a bumpy (scale 0.5, amount 0.3), mirror-ish
     (reflection 0.2) grey floor (plane y=-2) and `n_spheres` spheres r
@@ -1325,4 +1371,5 @@ WORKLOADS = {
     "textured_spheres": textured_spheres,
     "bumpy_spheres": bumpy_spheres,
     "shaped_spheres": shaped_spheres,
+    "glass_spheres": glass_spheres,
 }

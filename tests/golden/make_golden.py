@@ -69,6 +69,7 @@ def cases():
         "bumpy_perlin_160x120": (scenes.bumpy_spheres(160, 120, noise_generator=3), 2, 8.0),
         "bumpy_waves_160x120": (scenes.bumpy_spheres(160, 120, waves=True), 2, 8.0),
         "shaped_spheres_160x120": (scenes.shaped_spheres(160, 120, n_spheres=22), 2, 8.0),
+        "glass_spheres_160x120": (scenes.glass_spheres(160, 120), 2, 8.0),
     }
 
 

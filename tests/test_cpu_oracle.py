@@ -96,6 +96,9 @@ def test_oracle_pixels_and_counters_match_reference(case):
         assert diff.max() <= 1e-5
         for k in ("number_of_rays", "shadow_ray_tests", "shadow_rays_succeeded", "reflected_rays"):
             assert st[k] == rs[k], (k, st[k], rs[k])
+        if "refracted_rays" in rs:   # transparent scenes: the refraction counters too
+            for k in ("transmitted_rays", "refracted_rays", "internal_reflected_rays"):
+                assert st[k] == rs[k], (k, st[k], rs[k])
         assert compare_pixels(img, ref)["max_lsb"] <= 1
 
 
