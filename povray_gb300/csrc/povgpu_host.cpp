@@ -387,11 +387,13 @@ struct PathBufs {
     DevBuf mlist, mte, mod;         // media containers: listed rays, per-interval sums
     DevBuf mcbuf, mrounds;          // media containers: sample slots of a chunk, round lists
     DevBuf bin_keys, bin_hist, bin_order;   // textured scenes: the shade queue binned by material
+    DevBuf rinA, rinB, srin;        // transparent scenes: per-ray and shadow-ray interior lists
     DevBuf counters;
 
-    // media_ni: interval slots per ray segment (0: the scene has no media containers)
+    // media_ni: interval slots per ray segment (0: the scene has no media
+    // containers); transparent: rays carry their level and interior list
     cudaError_t ensure(size_t maxq, int nl, int nal, bool rad, bool sample_rays, int media_ni = 0,
-                       bool binned = false)
+                       bool binned = false, bool transparent = false)
     {
         maxq = std::max<size_t>(maxq, 1);
         nl = std::max(nl, 1);
@@ -437,6 +439,13 @@ struct PathBufs {
             PB_ENSURE(mte, sizeof(float4) * maxq * media_ni);
             PB_ENSURE(mod, sizeof(float4) * maxq * media_ni);
         }
+        if (transparent) {
+            PB_ENSURE(stateA, sizeof(int) * maxq);
+            PB_ENSURE(stateB, sizeof(int) * maxq);
+            PB_ENSURE(rinA, sizeof(uint64_t) * maxq);
+            PB_ENSURE(rinB, sizeof(uint64_t) * maxq);
+            PB_ENSURE(srin, sizeof(uint64_t) * maxq * nl);
+        }
 #undef PB_ENSURE
         return cudaSuccess;
     }
@@ -445,7 +454,7 @@ struct PathBufs {
         DevBuf* all[] = {&qA, &qB, &pathA, &pathB, &hits, &paths, &slot_contrib, &sq, &sq_slot, &blocked, &skipA,
                          &skipB, &sskip, &aq, &aq_slot, &aq_skip, &rq, &rq_amb, &quality, &first_t, &stateA,
                          &stateB, &smedium, &mlist, &mte, &mod, &mcbuf, &mrounds, &bin_keys, &bin_hist,
-                         &bin_order, &counters};
+                         &bin_order, &rinA, &rinB, &srin, &counters};
         for (DevBuf* b : all)
             b->release();
     }
@@ -559,6 +568,8 @@ struct PovGpuScene {
     cudaGraphExec_t graph_exec = nullptr;
     uint32_t graph_launches = 0;   // kernels in the graph
     bool   textured = false;   // some material has a pattern pigment or a normal: bin the shade queue
+    bool   transparent = false;   // some surface filters or transmits: rays carry interior lists
+    DevBuf obj_interior, interiors;   // per object its interior id; per interior its float4 pair
     int    media_ni = 0;   // interval slots per media segment (0: no media containers)
     int    media_smax = 0;  // sample slots per interval (ends + sample-tree nodes)
     int    media_sub = 0;   // largest sub-interval count
@@ -623,7 +634,7 @@ struct PovGpuScene {
                          &hits, &out, &counters, &stats, &err, &rays_in, &t64, &corners, &aa_grid, &aa_mask,
                          &aa_subdiv, &aa_xy, &cellsA, &cellsB, &spos, &sslot, &wcount, &pos_count, &medias,
                          &encode_buf, &cam_tab, &patterns, &tnormals, &noise_hash, &noise_rtab, &noise_perm, &noise_grad,
-                         &noise_waves};
+                         &noise_waves, &obj_interior, &interiors};
         for (DevBuf* b : all)
             b->release();
         top.release();
@@ -692,6 +703,7 @@ int begin_call(PovGpuScene* sc)
     return POV_GPU_OK;
 }
 
+constexpr int TRANSPARENT_PASSES_PER_LEVEL = 64;   // surfaces a ray crosses straight on at one trace level
 constexpr int MAX_AA_DEPTH = 4;   // (2^4+1)^2 = 289 grid points, 21 subdividable cells per pixel
 
 bool is_csg(int t) { return t == POV_OBJ_UNION || t == POV_OBJ_INTERSECTION || t == POV_OBJ_MERGE; }
@@ -716,9 +728,8 @@ int validate_media(const PovGpuSceneDesc* d, std::vector<char>& cmat, int32_t* b
             return POV_GPU_E_INVALID;
         const PovGpuMaterial* m =
             (o.material >= 0 && o.material < d->num_materials) ? &d->materials[o.material] : nullptr;
-        const bool transmits = m && (m->pigment[3] != 0.0f || m->pigment[4] != 0.0f);
-        if (o.media == 0 && !transmits)
-            continue;
+        if (o.media == 0)
+            continue;   // a transparent surface outside containers: validate_transparency
         if (bad) *bad = i;
         const PovGpuMedia* md = o.media > 0 ? &d->medias[o.media - 1] : nullptr;
         if (!md || o.type != POV_OBJ_BOX || !(o.flags & POV_FLAG_HOLLOW) || o.parent >= 0 || !m ||
@@ -745,6 +756,104 @@ int validate_media(const PovGpuSceneDesc* d, std::vector<char>& cmat, int32_t* b
     for (int i = 0; containers > 0 && i < d->num_lights; i++)
         if (d->lights[i].kind != POV_LIGHT_POINT)
             return POV_GPU_E_UNSUPPORTED;   // media samples test point-light shadows only
+    return POV_GPU_OK;
+}
+
+// Object::Inside in FP64 for the camera test below (sphere.cpp:333-382,
+// box.cpp:535-598, plane.cpp:213-258, torus.cpp:364-385, csg.cpp:405-484);
+// a mesh is solid only with an inside_vector, which the GPU path does not
+// take, so it contains no point.
+bool host_inside(const PovGpuSceneDesc* d, int i, const double* P)
+{
+    const PovGpuObject& o = d->objects[i];
+    const bool inv = (o.flags & POV_FLAG_INVERTED) != 0;
+    switch (o.type) {
+    case POV_OBJ_SPHERE: {
+        double dd = 0.0;
+        for (int k = 0; k < 3; k++)
+            dd += (o.p[k] - P[k]) * (o.p[k] - P[k]);
+        return inv ? dd > o.p[3] * o.p[3] : dd < o.p[3] * o.p[3];
+    }
+    case POV_OBJ_BOX: {
+        bool in = true;
+        for (int k = 0; k < 3; k++)
+            in = in && P[k] >= std::min(o.p[k], o.p[3 + k]) && P[k] <= std::max(o.p[k], o.p[3 + k]);
+        return inv ? !in : in;
+    }
+    case POV_OBJ_PLANE:
+        return (P[0] * o.p[0] + P[1] * o.p[1] + P[2] * o.p[2] + o.p[3]) < EPSILON;
+    case POV_OBJ_TORUS: {
+        const double* m = o.trans + 16;
+        double q[3];
+        for (int k = 0; k < 3; k++)
+            q[k] = P[0] * m[k] + P[1] * m[4 + k] + P[2] * m[8 + k] + m[12 + k];
+        const double r = std::sqrt(q[0] * q[0] + q[2] * q[2]);
+        const bool in = q[1] * q[1] + (r - o.p[0]) * (r - o.p[0]) <= o.p[1] * o.p[1];
+        return inv ? !in : in;
+    }
+    case POV_OBJ_UNION:
+    case POV_OBJ_MERGE:
+        for (int c = 0; c < o.num_children; c++)
+            if (host_inside(d, o.first_child + c, P))
+                return true;
+        return false;
+    case POV_OBJ_INTERSECTION:
+        for (int c = 0; c < o.num_children; c++)
+            if (!host_inside(d, o.first_child + c, P))
+                return false;
+        return true;
+    default:
+        return false;
+    }
+}
+
+// Transparent surfaces (a plain pigment that filters or transmits, outside
+// media containers) as the GPU path restates them: every hit continues into
+// at most one ray, so a transparent material reflects nothing (its
+// transmitted or refracted ray is the one; total internal reflection takes
+// its place); interiors without dispersion or caustics; no media
+// containers, radiosity or area lights beside them; the camera inside no
+// object (its rays start with an empty interior list); a ray inside at most
+// RIN_MAX interiors (checked on the device).  Sets *transparent.
+int validate_transparency(const PovGpuSceneDesc* d, const std::vector<char>& cmat, bool* transparent,
+                          int32_t* bad)
+{
+    *transparent = false;
+    for (int i = 0; i < d->num_materials; i++) {
+        const PovGpuMaterial& m = d->materials[i];
+        if (cmat[i] || (m.pigment[3] == 0.0f && m.pigment[4] == 0.0f))
+            continue;
+        *transparent = true;
+        bool refl = false;
+        for (int k = 0; k < 3; k++)
+            refl = refl || m.reflection_max[k] != 0.0f || m.reflection_min[k] != 0.0f;
+        if (m.pattern != 0 || refl)
+            return POV_GPU_E_UNSUPPORTED;
+    }
+    if (d->num_interiors < 0 || (d->num_interiors > 0 && !d->interiors))
+        return POV_GPU_E_INVALID;
+    if (d->object_interior)
+        for (int i = 0; i < d->num_objects; i++)
+            if (d->object_interior[i] < 0 || d->object_interior[i] > d->num_interiors)
+                return POV_GPU_E_INVALID;
+    if (!*transparent)
+        return POV_GPU_OK;
+    for (char c : cmat)
+        if (c)
+            return POV_GPU_E_UNSUPPORTED;
+    if (d->radiosity.enabled || d->max_trace_level > 255)
+        return POV_GPU_E_UNSUPPORTED;
+    for (int i = 0; i < d->num_lights; i++)
+        if (d->lights[i].kind != POV_LIGHT_POINT)
+            return POV_GPU_E_UNSUPPORTED;
+    for (int i = 0; i < d->num_interiors; i++)
+        if (d->interiors[i].dispersion != 1.0 || d->interiors[i].caustics != 0.0 || !(d->interiors[i].ior > 0.0))
+            return POV_GPU_E_UNSUPPORTED;
+    for (int i = 0; i < d->num_objects; i++)
+        if (d->objects[i].parent < 0 && host_inside(d, i, d->camera.location)) {
+            if (bad) *bad = i;
+            return POV_GPU_E_UNSUPPORTED;
+        }
     return POV_GPU_OK;
 }
 
@@ -780,6 +889,10 @@ int validate(const PovGpuSceneDesc* d, int32_t* bad)
     std::vector<char> cmat;
     {
         int rc = validate_media(d, cmat, bad);
+        if (rc != POV_GPU_OK)
+            return rc;
+        bool transparent = false;
+        rc = validate_transparency(d, cmat, &transparent, bad);
         if (rc != POV_GPU_OK)
             return rc;
     }
@@ -827,9 +940,8 @@ int validate(const PovGpuSceneDesc* d, int32_t* bad)
     }
     for (int i = 0; i < d->num_materials; i++) {
         const PovGpuMaterial& m = d->materials[i];
-        // opaque plain pigments and the classic finish terms only (media
-        // containers' surfaces transmit)
-        if ((!cmat[i] && (m.pigment[3] != 0.0f || m.pigment[4] != 0.0f)) || m.reflection_fresnel || m.fresnel != 0.0f ||
+        // the classic finish terms only (transparency: validate_transparency)
+        if (m.reflection_fresnel || m.fresnel != 0.0f ||
             m.metallic != 0.0f || m.reflect_metallic != 0.0f || m.reflect_exp != 1.0f || m.irid != 0.0f ||
             m.crand != 0.0f || m.diffuse_back != 0.0f || m.conserve_energy)
             return POV_GPU_E_UNSUPPORTED;
@@ -882,7 +994,7 @@ int validate(const PovGpuSceneDesc* d, int32_t* bad)
     return POV_GPU_OK;
 }
 
-DevMaterial make_material(const PovGpuMaterial& m, const float* ambient_light, bool radiosity)
+DevMaterial make_material(const PovGpuMaterial& m, const float* ambient_light, bool radiosity, int language_version)
 {
     DevMaterial d{};
     d.pigment = make_float4(m.pigment[0], m.pigment[1], m.pigment[2], m.pigment[3]);
@@ -909,6 +1021,15 @@ DevMaterial make_material(const PovGpuMaterial& m, const float* ambient_light, b
     d.diffuse_raw = m.diffuse;
     d.pattern = m.pattern;
     d.normal = m.normal;
+    d.transmit = m.pigment[4];
+    d.see_through = (m.pigment[3] != 0.0f || m.pigment[4] != 0.0f) ? 1 : 0;
+    // TransColour::Opacity (LegacyOpacity before 3.7), in the colour's float
+    d.opacity = 1.0f;
+    if (d.see_through)
+        d.opacity = language_version < 370
+                        ? (float)(1.0 - (m.pigment[3] * std::max(m.pigment[0], std::max(m.pigment[1], m.pigment[2])) +
+                                         m.pigment[4]))
+                        : (float)(1.0 - (double)m.pigment[3] - (double)m.pigment[4]);
     return d;
 }
 
@@ -1209,6 +1330,86 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
         objects[i].type = o.type;
         objects[i].mesh = o.mesh;
     }
+    // interiors (Post_Process, parser.cpp:9225-9267): the description's,
+    // plus a default one (the atmosphere's ior) for every top-level object
+    // given none; a CSG child without one shares its parent's.  Each
+    // object's id goes with whether its top-level object is opaque
+    // (OPAQUE_FLAG, parser.cpp:9296-9297: a leaf whose plain pigment neither
+    // filters nor transmits; a CSG whose children all are).
+    const double atm_ior = d->atmosphere_ior > 0.0 ? d->atmosphere_ior : 1.0;
+    sc->transparent = false;
+    for (int i = 0; i < d->num_objects; i++) {
+        const PovGpuMaterial& m = d->materials[objects[i].material];
+        if (d->objects[i].type < POV_OBJ_UNION && !is_container(d->objects[i]) &&
+            (m.pigment[3] != 0.0f || m.pigment[4] != 0.0f))
+            sc->transparent = true;
+    }
+    std::vector<float4> interiors;
+    std::vector<int32_t> obj_interior((size_t)std::max(d->num_objects, 1), 0);
+    {
+        auto pair_of = [](const PovGpuInterior& I, std::vector<float4>& out) {
+            out.push_back(make_float4((float)I.ior, (float)I.fade_distance, (float)I.fade_power, I.old_refract));
+            out.push_back(make_float4(I.fade_colour[0], I.fade_colour[1], I.fade_colour[2], 0.f));
+        };
+        for (int k = 0; k < d->num_interiors; k++)
+            pair_of(d->interiors[k], interiors);
+        int nints = d->num_interiors;
+        for (int i = 0; i < d->num_objects; i++) {
+            const int given = d->object_interior ? d->object_interior[i] : 0;
+            const int parent = d->objects[i].parent;
+            if (given > 0) {
+                obj_interior[i] = given - 1;
+            } else if (parent >= 0) {
+                obj_interior[i] = obj_interior[parent];
+            } else {
+                PovGpuInterior def{};
+                def.ior = atm_ior;
+                def.dispersion = 1.0;
+                def.old_refract = 1.0f;
+                pair_of(def, interiors);
+                obj_interior[i] = nints++;
+            }
+        }
+        // ids: only the interiors of transparent surfaces ever enter an
+        // interior list; they are numbered 0.. (8-bit ids in the lists),
+        // every other object gets id 0, which is never looked up
+        std::vector<int> remap((size_t)std::max(nints, 1), -1);
+        int nused = 0;
+        for (int i = 0; i < d->num_objects; i++) {
+            const PovGpuMaterial& m = d->materials[objects[i].material];
+            if (d->objects[i].type < POV_OBJ_UNION && !is_container(d->objects[i]) &&
+                (m.pigment[3] != 0.0f || m.pigment[4] != 0.0f) && remap[obj_interior[i]] < 0)
+                remap[obj_interior[i]] = nused++;
+        }
+        if (nused > 256)
+            return POV_GPU_E_UNSUPPORTED;   // interior lists hold 8-bit ids
+        std::vector<float4> used(2 * (size_t)std::max(nused, 1), make_float4(1.f, 0.f, 0.f, 1.f));
+        for (int k = 0; k < nints; k++)
+            if (remap[k] >= 0) {
+                used[2 * (size_t)remap[k]] = interiors[2 * (size_t)k];
+                used[2 * (size_t)remap[k] + 1] = interiors[2 * (size_t)k + 1];
+            }
+        interiors.swap(used);
+        for (int i = 0; i < d->num_objects; i++)
+            obj_interior[i] = std::max(remap[obj_interior[i]], 0);
+        // opacity, children before parents
+        std::vector<char> opaque((size_t)std::max(d->num_objects, 1), 1);
+        for (int i = d->num_objects - 1; i >= 0; i--) {
+            const PovGpuObject& o = d->objects[i];
+            if (o.type < POV_OBJ_UNION) {
+                const PovGpuMaterial& m = d->materials[objects[i].material];
+                opaque[i] = m.pigment[3] == 0.0f && m.pigment[4] == 0.0f;
+            }
+            if (o.parent >= 0 && !opaque[i])
+                opaque[o.parent] = 0;
+        }
+        for (int i = 0; i < d->num_objects; i++) {
+            int top = i;
+            while (d->objects[top].parent >= 0)
+                top = d->objects[top].parent;
+            obj_interior[i] = (obj_interior[i] & 0xffff) | (opaque[top] ? (1 << 16) : 0);
+        }
+    }
     // media containers, numbered in object order
     std::vector<int> container_obj;
     for (int i = 0; i < d->num_objects; i++)
@@ -1320,7 +1521,7 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
     std::vector<DevMaterial> mats((size_t)d->num_materials);
     for (int i = 0; i < d->num_materials; i++)
         mats[i] = make_material(d->materials[i], d->ambient_light,
-                                d->radiosity.enabled && d->language_version >= 370);
+                                d->radiosity.enabled && d->language_version >= 370, d->language_version);
     std::vector<DevLight> lights((size_t)std::max(d->num_lights, 1));
     int num_area = 0;
     for (int i = 0; i < d->num_lights; i++) {
@@ -1439,6 +1640,8 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
 
     CK(upload(sc->objects, objects));
     CK(upload(sc->materials, mats));
+    CK(upload(sc->obj_interior, obj_interior));
+    CK(upload(sc->interiors, interiors));
     CK(upload(sc->lights, lights));
     CK(upload(sc->medias, medias));
     CK(upload(sc->patterns, pats));
@@ -1489,6 +1692,10 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
     S.boxes64 = sc->boxes64.as<double>();
     S.objects = sc->objects.as<ObjectShade>();
     S.materials = sc->materials.as<DevMaterial>();
+    S.obj_interior = sc->obj_interior.as<int32_t>();
+    S.interiors = sc->interiors.as<float4>();
+    S.atm_ior = (float)atm_ior;
+    S.transparent = sc->transparent ? 1 : 0;
     S.lights = sc->lights.as<DevLight>();
     S.num_lights = d->num_lights;
     S.num_area_lights = num_area;
@@ -1588,6 +1795,8 @@ int check_device_error(PovGpuScene* sc, PovGpuStats* stats, unsigned long long* 
         stats->reflected_rays = host_stats[ST_REFLECTED];
         stats->transmitted_rays = host_stats[ST_TRANSMITTED];
         stats->media_samples = host_stats[ST_MEDIA_SAMPLES];
+        stats->refracted_rays = host_stats[ST_REFRACTED];
+        stats->internal_reflected_rays = host_stats[ST_INTERNAL_REFLECTED];
         stats->device_error = errw;
     }
     return errw ? POV_GPU_E_DEVICE : POV_GPU_OK;
@@ -1802,7 +2011,9 @@ int run_levels(PovGpuScene* sc, StageClock& clk, PathBufs& B, size_t maxq, int l
     const int nal = sample_rays ? 0 : sc->S.num_area_lights;
     const bool rad = sc->rad.enabled && hit_depth < sc->rad.set.recursion_limit;
     const bool media = sc->media_ni > 0;
-    CK(B.ensure(maxq, nl, nal, rad, sample_rays, sc->media_ni, sc->textured));
+    const bool transparent = sc->transparent;
+    const bool staged = media || transparent;   // rays carry their own level
+    CK(B.ensure(maxq, nl, nal, rad, sample_rays, sc->media_ni, sc->textured, transparent));
     cudaStream_t st = sc->active();
     int* cnt = B.counters.as<int>();
     unsigned long long* dstats = sc->stats.as<unsigned long long>();
@@ -1832,19 +2043,34 @@ int run_levels(PovGpuScene* sc, StageClock& clk, PathBufs& B, size_t maxq, int l
     // the passes run until the queue is empty (each pass raises a ray's
     // level or takes it across a wall: at most 1 + 2 * containers passes a
     // level)
-    int* scur = media ? B.stateA.as<int>() : nullptr;
-    int* snext = media ? B.stateB.as<int>() : nullptr;
-    const int max_pass = media ? (max_level - level0) * (1 + 2 * S.num_containers) : max_level - level0;
-    if (media)
+    // Transparent surfaces likewise: a ray continued through a surface
+    // with equal iors on both sides stays at its level; each pass takes
+    // every ray across one surface, and a pass limit ends a frame whose
+    // rays still cross surfaces after it with an error (no ray is dropped
+    // silently).
+    int* scur = staged ? B.stateA.as<int>() : nullptr;
+    int* snext = staged ? B.stateB.as<int>() : nullptr;
+    uint64_t* rcur = transparent ? B.rinA.as<uint64_t>() : nullptr;
+    uint64_t* rnext = transparent ? B.rinB.as<uint64_t>() : nullptr;
+    const int max_pass = media         ? (max_level - level0) * (1 + 2 * S.num_containers)
+                         : transparent ? (max_level - level0) * TRANSPARENT_PASSES_PER_LEVEL
+                                       : max_level - level0;
+    if (staged)
         CK(launch_fill_int(scur, ccur, (int)maxq, ray_state(level0, -1), grid_shade, st));
-    for (int pass = 0; pass < max_pass; pass++) {
-        const int level = level0 + pass;   // the level of every ray without media containers
-        if (media && pass > 0) {
+    if (transparent)   // camera and sample rays start inside no interior
+        CK(cudaMemsetAsync(rcur, 0, sizeof(uint64_t) * maxq, st));
+    for (int pass = 0;; pass++) {
+        const int level = level0 + pass;   // the level of every ray without media or transparency
+        if (staged && pass > 0) {
             CK(cudaMemcpyAsync(sc->pin_int(1), ccur, sizeof(int), cudaMemcpyDeviceToHost, st));
             HW(st);
             if (*sc->pin_int(1) == 0)
                 break;
+            if (pass >= max_pass && transparent)
+                return POV_GPU_E_CAPACITY;
         }
+        if (pass >= max_pass)
+            break;
         CK(cudaMemsetAsync(cnext, 0, sizeof(int), st));
         CK(cudaMemsetAsync(cnt + C_SQ, 0, sizeof(int) * 3, st));   // SQ, W0, W1
         CK(cudaMemsetAsync(cnt + C_AQ, 0, sizeof(int) * 2, st));   // AQ, RQ
@@ -1863,7 +2089,8 @@ int run_levels(PovGpuScene* sc, StageClock& clk, PathBufs& B, size_t maxq, int l
             CK(clk.end(nlaunch));
         }
         CK(clk.begin(POV_GPU_STAGE_SHADE));
-        ShadeMedia sm{scur, snext, media ? B.smedium.as<int>() : nullptr};
+        ShadeMedia sm{scur, snext, media ? B.smedium.as<int>() : nullptr, rcur, rnext,
+                      transparent ? B.srin.as<uint64_t>() : nullptr};
         const int* order = nullptr;
         if (sc->textured) {   // one material per warp in k_shade
             CK(launch_shade_bins(S, B.hits.as<QHit>(), ccur, (int)maxq, B.bin_keys.as<uint8_t>(),
@@ -1891,6 +2118,11 @@ int run_levels(PovGpuScene* sc, StageClock& clk, PathBufs& B, size_t maxq, int l
                                          B.blocked.as<uint8_t>(),
                                          B.slot_contrib.as<float4>(), !sample_rays, sc->stack_depth, grid_trace,
                                          derr, dstats, st));
+            else if (transparent)
+                CK(launch_shadow_filter(S, B.sq.as<QRay>(), B.sq_slot.as<int>(), B.sskip.as<uint2>(),
+                                        B.srin.as<uint64_t>(), cnt + C_SQ, (int)(maxq * nl), cnt + C_W1,
+                                        B.blocked.as<uint8_t>(), B.slot_contrib.as<float4>(), sc->stack_depth,
+                                        grid_trace, derr, dstats, st));
             else
                 CK(launch_trace(S, true, B.sq.as<QRay>(), cnt + C_SQ, cnt + C_W1, nullptr, B.blocked.as<uint8_t>(),
                                 sc->stack_depth, grid_trace, derr, dstats, wc ? wc + 4 : nullptr, (int)(maxq * nl),
@@ -1922,6 +2154,7 @@ int run_levels(PovGpuScene* sc, StageClock& clk, PathBufs& B, size_t maxq, int l
         std::swap(ccur, cnext);
         std::swap(kcur, knext);
         std::swap(scur, snext);
+        std::swap(rcur, rnext);
     }
     return POV_GPU_OK;
 }
@@ -2761,7 +2994,7 @@ int pov_gpu_trace_blocks(PovGpuScene* sc, const PovGpuBlock* blocks, int32_t num
     uint64_t n_pixels = (uint64_t)n, n_samples = 0;
     // plain frames (no radiosity, media containers or AA: no host reads
     // between the launches) replay a captured graph of their device work
-    const bool graphable = !aa && !sc->rad.enabled && sc->media_ni == 0 && sc->profiling == 0;
+    const bool graphable = !aa && !sc->rad.enabled && sc->media_ni == 0 && !sc->transparent && sc->profiling == 0;
     if (graphable) {
         int rc = trace_plain_graph(sc, clk, num_blocks, n, params->width, params->height, dout);
         if (rc != POV_GPU_OK)

@@ -73,6 +73,12 @@ struct __align__(16) DevMaterial {
     float   diffuse_raw;    // Finish->Diffuse, the radiosity ambient's factor (trace.cpp:898)
     int32_t pattern;        // pigment pattern + 1 (0: the plain pigment above)
     int32_t normal;         // normal perturbation + 1 (0: the raw normal)
+    // transparency: the plain pigment's transmit, its opacity (the factor of
+    // the layer's own light, TransColour::Opacity), whether it filters or
+    // transmits at all
+    float   transmit;
+    float   opacity;
+    int32_t see_through;
 };
 
 // Pattern pigment (Compute_Pigment with a colour map): the inverse TRANSFORM
@@ -212,6 +218,14 @@ struct DeviceScene {
     const DevCsgChild* csg_children;
     const int32_t*     sphere_flags;   // bit0 inverted (spheres inside CSG)
     int32_t            has_full_prims; // tori or CSG present: full traversal variant
+    // transparency: per object its interior id (bits 0-15) and whether the
+    // top-level object it belongs to is opaque (bit 16: the OPAQUE_FLAG of
+    // the CSG a child belongs to); per interior (ior, fade_distance,
+    // fade_power, old_refract) and (fade colour rgb, 0); the atmosphere's ior
+    const int32_t*     obj_interior;
+    const float4*      interiors;
+    float              atm_ior;
+    int32_t            transparent;
     // FP64 geometry as the parser stores it, read only by the parity
     // re-solve (k_refine): centre+radius per sphere, 6 corners per box
     const double*      spheres64;
@@ -335,7 +349,48 @@ struct ShadeMedia {
     const int32_t* q_state;
     int32_t*       nq_state;
     int32_t*       sq_medium;
+    // transparent scenes: each queued ray's interior list (rin_*), handed
+    // to its shadow rays and to the transmitted or refracted ray
+    const uint64_t* q_rin;
+    uint64_t*       nq_rin;
+    uint64_t*       sq_rin;
 };
+
+// A ray's interior list (Ray::GetInteriors): the ids of the interiors it
+// travels inside, innermost last, as bytes 1..7 of a 64-bit word whose
+// byte 0 holds the count.
+constexpr int RIN_MAX = 7;
+__host__ __device__ __forceinline__ int rin_count(uint64_t r) { return (int)(r & 0xffu); }
+__host__ __device__ __forceinline__ int rin_get(uint64_t r, int k) { return (int)((r >> (8 * (k + 1))) & 0xffu); }
+__host__ __device__ __forceinline__ uint64_t rin_set(uint64_t r, int k, int id)
+{
+    const int sh = 8 * (k + 1);
+    return (r & ~(0xffull << sh)) | ((uint64_t)(id & 0xff) << sh);
+}
+__host__ __device__ __forceinline__ int rin_find(uint64_t r, int id)
+{
+    for (int k = 0; k < rin_count(r); k++)
+        if (rin_get(r, k) == id)
+            return k;
+    return -1;
+}
+__host__ __device__ __forceinline__ uint64_t rin_remove(uint64_t r, int k)
+{
+    const int n = rin_count(r);
+    for (int j = k; j + 1 < n; j++)
+        r = rin_set(r, j, rin_get(r, j + 1));
+    r = rin_set(r, n - 1, 0);
+    return (r & ~0xffull) | (uint64_t)(n - 1);
+}
+// false when the list is full (the caller flags the device error)
+__host__ __device__ __forceinline__ bool rin_append(uint64_t& r, int id)
+{
+    const int n = rin_count(r);
+    if (n >= RIN_MAX)
+        return false;
+    r = (rin_set(r, n, id) & ~0xffull) | (uint64_t)(n + 1);
+    return true;
+}
 
 // Device error word bits.
 enum DevError : uint32_t {
@@ -343,6 +398,7 @@ enum DevError : uint32_t {
     DE_ITERATION_CAP  = 2u,
     DE_QUEUE_OVERFLOW = 4u,
     DE_CACHE_FULL     = 8u,
+    DE_INTERIORS      = 16u,   // a ray inside more than RIN_MAX interiors
 };
 
 // Counters (device, uint64).
@@ -354,7 +410,9 @@ enum StatIdx {
     ST_SAMPLES = 4,
     ST_TRANSMITTED = 5,
     ST_MEDIA_SAMPLES = 6,
-    ST_COUNT = 8,
+    ST_REFRACTED = 7,
+    ST_INTERNAL_REFLECTED = 8,
+    ST_COUNT = 10,
 };
 
 }  // namespace povgpu

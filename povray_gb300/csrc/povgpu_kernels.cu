@@ -1397,8 +1397,42 @@ __device__ __forceinline__ uint32_t skip_aux(const QHit& h)
     return (kind == PK_BOX || kind == PK_CSG) ? __float_as_uint(h.u) : 0u;
 }
 
+// Mirror direction of d about the layer normal N, with the raw-normal
+// fix-ups of a perturbed normal (ComputeReflection, trace.cpp:1272-1299).
+__device__ __forceinline__ float3 mirror_dir(float3 d, float3 N, float3 raw)
+{
+    float n2 = -2.0f * dot3(d, N);
+    float3 nd = d + N * n2;
+    float rn = dot3(nd, raw);
+    if (rn < 0.0f) {
+        if (dot3(nd, N) < 0.0f) {   // inside the rear virtual surface
+            rn = -2.0f * dot3(d, raw);
+            nd = d + raw * rn;
+        } else {                    // reflect once more about the raw normal
+            nd = nd + raw * (-2.0f * rn);
+        }
+    }
+    return normalize3(nd);
+}
+
+// Fade of the light that crossed `depth` inside an interior
+// (Trace::ComputeRefraction / ComputeShadowTexture, trace.cpp:1108-1128,
+// 1225-1240): exponential for fade_power >= 1000, else
+// fade_colour + (1 - fade_colour) / (1 + (depth / fade_distance)^fade_power).
+__device__ __forceinline__ float3 interior_fade(float4 I0, float4 I1, float depth)
+{
+    const float x = depth / I0.y;
+    if (I0.z >= 1000.0f)
+        return f3(expf(-(1.0f - I1.x) * x), expf(-(1.0f - I1.y) * x), expf(-(1.0f - I1.z) * x));
+    const float q = 1.0f / (1.0f + powf(x, I0.z));
+    return f3(I1.x + (1.0f - I1.x) * q, I1.y + (1.0f - I1.y) * q, I1.z + (1.0f - I1.z) * q);
+}
+
 // One thread per ray of the level queue.  Emits shadow rays (one per lit
-// light, slot = ray*num_lights+light) and the reflection ray.
+// light, slot = ray*num_lights+light) and the one secondary ray of the hit:
+// the reflection ray, the continued ray through a media container's wall,
+// or the transmitted / refracted / totally reflected ray of a transparent
+// surface.
 __global__ void __launch_bounds__(128) k_shade(
     DeviceScene S, int level, int max_level, const QRay* __restrict__ q, const int* __restrict__ q_path,
     const QHit* __restrict__ hits, const int* __restrict__ q_count, PathState* __restrict__ paths,
@@ -1411,7 +1445,7 @@ __global__ void __launch_bounds__(128) k_shade(
 {
     const int n = min(*q_count, max_queue);
     const int nl = S.num_lights;
-    unsigned long long c_rays = 0, c_refl = 0, c_shadow = 0, c_trans = 0;
+    unsigned long long c_rays = 0, c_refl = 0, c_shadow = 0, c_trans = 0, c_refr = 0, c_tir = 0;
     for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         int i = base + threadIdx.x;
         bool active = i < n;
@@ -1441,8 +1475,10 @@ __global__ void __launch_bounds__(128) k_shade(
         uint2 self = make_uint2(h.prim, skip_aux(h));
         bool container = false;
         float3 pigc = f3(0.f, 0.f, 0.f);   // the hit's pigment colour
+        int hobj = 0;
         if (hit) {
             SurfaceInfo si = surface(S, h, p);
+            hobj = si.object;
             ObjectShade os = S.objects[si.object];
             oflags = os.flags;
             container = (oflags & OBJ_CONTAINER) != 0;
@@ -1457,7 +1493,10 @@ __global__ void __launch_bounds__(128) k_shade(
             if (m->normal)
                 N = perturb_normal(S, m->normal - 1, p, N);
             float4 em = m->emission;
-            col = container ? f3(0.f, 0.f, 0.f) : f3(pigc.x * em.x, pigc.y * em.y, pigc.z * em.z);
+            // a transparent layer's own light is scaled by its opacity
+            // (trace.cpp:877-881,1002-1004)
+            const float att = m->opacity;
+            col = container ? f3(0.f, 0.f, 0.f) : f3(pigc.x * em.x * att, pigc.y * em.y * att, pigc.z * em.z * att);
         } else {
             col = xyz(S.background);   // ComputeSky, background only
         }
@@ -1517,7 +1556,7 @@ __global__ void __launch_bounds__(128) k_shade(
                     float3 pig = pigc;
                     if (m->diffuse > 0.0f) {   // ComputeDiffuseColour, trace.cpp:2441-2484
                         float inten = m->brilliance != 1.0f ? powf(fabsf(cs), m->brilliance) : fabsf(cs);
-                        inten *= m->diffuse;
+                        inten *= m->diffuse * m->opacity;
                         contrib = contrib + pig * lc * inten;
                     }
                     if (m->phong > 0.0f && !rad.gather) {     // ComputePhongColour, trace.cpp:2520-2558
@@ -1564,6 +1603,8 @@ __global__ void __launch_bounds__(128) k_shade(
                     sq_skip[slot] = self;
                     if (med.sq_medium)
                         med.sq_medium[slot] = medium;
+                    if (med.sq_rin)
+                        med.sq_rin[slot] = med.q_rin[i];
                 } else {
                     set_error(err, DE_QUEUE_OVERFLOW);
                 }
@@ -1589,20 +1630,7 @@ __global__ void __launch_bounds__(128) k_shade(
             if (reflec.x != 0.0f || reflec.y != 0.0f || reflec.z != 0.0f) {
                 c_refl++;
                 c_rays++;   // the TraceRay call is counted even when it bails
-                // mirror direction, with the raw-normal fix-ups of a
-                // perturbed normal (ComputeReflection, trace.cpp:1272-1299)
-                float n2 = -2.0f * dot3(d, N);
-                nd = d + N * n2;
-                float rn = dot3(nd, raw);
-                if (rn < 0.0f) {
-                    if (dot3(nd, N) < 0.0f) {   // inside the rear virtual surface
-                        rn = -2.0f * dot3(d, raw);
-                        nd = d + raw * rn;
-                    } else {                    // reflect once more about the raw normal
-                        nd = nd + raw * (-2.0f * rn);
-                    }
-                }
-                nd = normalize3(nd);
+                nd = mirror_dir(d, N, raw);
                 refl = (lvl + 1 < max_level) && (rweight >= rad.adc);
             }
         }
@@ -1618,20 +1646,104 @@ __global__ void __launch_bounds__(128) k_shade(
             const int c = (oflags >> 16) & 0xff;
             cont_medium = medium == c ? -1 : c;
         }
-        int rs = warp_reserve(nq_count, refl || cont, mask);
-        if (refl || cont) {
+        // transparent surface (ComputeLightedTexture's transmitted
+        // component, trace.cpp:1063-1142, and ComputeRefraction,
+        // trace.cpp:1323-1486): the filter colour TransmittedColour =
+        // pigment * filter + transmit and its greyscale; above the ADC
+        // bailout one ray at weight * max|filter| goes on with the ray's
+        // interior list changed as the reference changes it -- the continued
+        // ray at the same trace level when the iors are equal, else the
+        // refracted ray (Heckbert) or, on total internal reflection, the
+        // mirror ray with the unchanged list.  Its light reaches the path
+        // through Old_Refract, the fade of the interior it leaves and,
+        // except after total internal reflection, the filter colour.
+        bool tr = false;
+        uint64_t trin = 0;
+        int tstate = 0;
+        float4 tthr = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (shaded && m->see_through && med.q_rin) {
+            const float3 fil = f3(pigc.x * m->pigment.w + m->transmit, pigc.y * m->pigment.w + m->transmit,
+                                  pigc.z * m->pigment.w + m->transmit);
+            const float trans = fminf(1.0f, fabsf(0.297f * fil.x + 0.589f * fil.y + 0.114f * fil.z));
+            if (trans > rad.adc) {
+                const float w1 = fmaxf(fabsf(fil.x), fmaxf(fabsf(fil.y), fabsf(fil.z)));
+                const int oid = S.obj_interior[hobj] & 0xffff;
+                const float4 I0 = S.interiors[2 * oid], I1 = S.interiors[2 * oid + 1];
+                const uint64_t rin = med.q_rin[i];
+                const int nr = rin_count(rin);
+                const int at = rin_find(rin, oid);
+                uint64_t nrin = rin;
+                float ior;
+                if (nr == 0) {                          // entering from the atmosphere
+                    rin_append(nrin, oid);
+                    ior = S.atm_ior / I0.x;
+                } else if (at == nr - 1) {              // leaving the innermost interior
+                    nrin = rin_remove(rin, at);
+                    ior = nr == 1 ? I0.x / S.atm_ior : I0.x / S.interiors[2 * rin_get(rin, nr - 2)].x;
+                } else if (at >= 0) {                   // leaving an overlap
+                    nrin = rin_remove(rin, at);
+                    ior = 1.0f;
+                } else {                                // entering within another
+                    if (!rin_append(nrin, oid))
+                        set_error(err, DE_INTERIORS);
+                    ior = S.interiors[2 * rin_get(rin, nr - 1)].x / I0.x;
+                }
+                float3 ac = f3(I0.w, I0.w, I0.w);   // Old_Refract
+                if (at >= 0 && fabsf(I0.y) > EPSILON_F)
+                    ac = ac * interior_fade(I0, I1, h.t);
+                float3 tfac = ac * fil;
+                c_rays++;   // the TraceRay call is counted even when it bails
+                if (fabsf(ior - 1.0f) < EPSILON_F) {
+                    c_trans++;                          // Transmitted_Rays_Traced
+                    nd = d;
+                    tstate = ray_state(lvl, -1);
+                    trin = nrin;
+                } else {
+                    float nn = dot3(d, N);
+                    float3 ln = N;
+                    if (nn <= 0.0f)
+                        nn = -nn;
+                    else
+                        ln = N * -1.0f;
+                    float tt = 1.0f + ior * ior * (nn * nn - 1.0f);
+                    if (tt < 0.0f) {
+                        c_tir++;                        // Internal_Reflected_Rays_Traced
+                        c_refl++;
+                        nd = mirror_dir(d, N, raw);
+                        trin = rin;
+                        tfac = ac;
+                    } else {
+                        c_refr++;                       // Refracted_Rays_Traced
+                        tt = ior * nn - sqrtf(tt);
+                        nd = normalize3(d * ior + ln * tt);
+                        trin = nrin;
+                    }
+                    tstate = ray_state(lvl + 1, -1);
+                }
+                tthr = make_float4(thr.x * tfac.x, thr.y * tfac.y, thr.z * tfac.z, weight * w1);
+                tr = (lvl + 1 < max_level) && (weight * w1 >= rad.adc);
+            }
+        }
+        const bool spawn = refl || cont || tr;
+        int rs = warp_reserve(nq_count, spawn, mask);
+        if (spawn) {
             if (rs < max_queue) {
                 QRay rr;
                 rr.org = make_float4(p.x, p.y, p.z, kMinIsectDepth);
-                rr.dir = refl ? make_float4(nd.x, nd.y, nd.z, CUDART_INF_F) : make_float4(d.x, d.y, d.z, CUDART_INF_F);
+                rr.dir = (refl || tr) ? make_float4(nd.x, nd.y, nd.z, CUDART_INF_F)
+                                      : make_float4(d.x, d.y, d.z, CUDART_INF_F);
                 nq[rs] = rr;
                 nq_path[rs] = path;
                 nq_skip[rs] = self;
                 if (med.nq_state)
-                    med.nq_state[rs] = refl ? ray_state(lvl + 1, medium) : ray_state(lvl, cont_medium);
+                    med.nq_state[rs] = tr ? tstate : (refl ? ray_state(lvl + 1, medium) : ray_state(lvl, cont_medium));
+                if (med.nq_rin)
+                    med.nq_rin[rs] = trin;
                 if (refl)
                     paths[path].throughput =
                         make_float4(thr.x * reflec.x, thr.y * reflec.y, thr.z * reflec.z, rweight);
+                else if (tr)
+                    paths[path].throughput = tthr;
             } else {
                 set_error(err, DE_QUEUE_OVERFLOW);
             }
@@ -1645,9 +1757,13 @@ __global__ void __launch_bounds__(128) k_shade(
         c_refl += __shfl_down_sync(0xffffffffu, c_refl, off);
         c_shadow += __shfl_down_sync(0xffffffffu, c_shadow, off);
         c_trans += __shfl_down_sync(0xffffffffu, c_trans, off);
+        c_refr += __shfl_down_sync(0xffffffffu, c_refr, off);
+        c_tir += __shfl_down_sync(0xffffffffu, c_tir, off);
     }
     if ((threadIdx.x & 31) == 0) {
         if (c_trans) atomicAdd(&stats[ST_TRANSMITTED], c_trans);
+        if (c_refr) atomicAdd(&stats[ST_REFRACTED], c_refr);
+        if (c_tir) atomicAdd(&stats[ST_INTERNAL_REFLECTED], c_tir);
         if (c_rays) atomicAdd(&stats[ST_RAYS], c_rays);
         if (c_refl) atomicAdd(&stats[ST_REFLECTED], c_refl);
         if (c_shadow) atomicAdd(&stats[ST_SHADOW_TESTS], c_shadow);
@@ -1999,6 +2115,192 @@ __global__ void __launch_bounds__(128) k_shadow_through(DeviceScene S, const QRa
         if (c_tests) atomicAdd(&stats[ST_SHADOW_TESTS], c_tests);
         if (c_succ) atomicAdd(&stats[ST_SHADOW_SUCCEEDED], c_succ);
         if (c_ms) atomicAdd(&stats[ST_MEDIA_SAMPLES], c_ms);
+    }
+}
+
+// ------------------------------------------------ transparent surfaces --
+// Closest hit of one ray in [tmin, tmax) (the per-ray body of
+// k_trace<false, FULL>): the primitive, its aux word and depth.
+template <bool FULL>
+__device__ __forceinline__ bool nearest(const DeviceScene& S, float3 o, float3 d, float tmin, float tmax, uint2 skip,
+                                        int* smem, int stack_depth, uint32_t* err, float& t, uint32_t& prim,
+                                        uint32_t& paux)
+{
+    t = tmax;
+    prim = NO_PRIM;
+    paux = 0;
+    for (int k = 0; k < S.num_planes; k++) {
+        const uint32_t ref = (PK_PLANE << PRIM_KIND_SHIFT) | (uint32_t)k;
+        if (ref == skip.x)
+            continue;
+        float4 pl = __ldg(S.planes + k);
+        float ndd = pl.x * d.x + pl.y * d.y + pl.z * d.z;
+        if (fabsf(ndd) < EPSILON_F)
+            continue;
+        float tt = -(pl.x * o.x + pl.y * o.y + pl.z * o.z + pl.w) / ndd;
+        if (tt >= tmin && tt < t) {
+            t = tt;
+            prim = ref;
+        }
+    }
+    float3 inv = f3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+    float bu = 0.f, bv = 0.f;
+    int sp = 0, node = S.root, iters = 0;
+    while (node != BVH_EMPTY) {
+        if (++iters > (1 << 22)) {
+            set_error(err, DE_ITERATION_CAP);
+            return false;
+        }
+        if (node >= 0) {
+            if (!node4_step(S.nodes, node, o, inv, tmin, t, smem, sp, stack_depth)) {
+                set_error(err, DE_STACK_OVERFLOW);
+                return false;
+            }
+        } else {
+            uint32_t code = ~(uint32_t)node;
+            uint32_t first = code >> 3, count = (code & 7u) + 1u;
+            for (uint32_t k = 0; k < count; k++) {
+                uint32_t aux = 0;
+                const uint32_t ref = __ldg(S.prim_refs + first + k);
+                if (prim_test<false, FULL>(S, ref, o, d, tmin, t, bu, bv, aux, skip)) {
+                    prim = ref;
+                    paux = aux;
+                }
+            }
+            node = sp > 0 ? smem[(--sp) * blockDim.x + threadIdx.x] : BVH_EMPTY;
+        }
+    }
+    return prim != NO_PRIM;
+}
+
+// The flattened object a primitive hit belongs to (the object id of
+// surface(), without the normal).
+__device__ __forceinline__ int hit_object(const DeviceScene& S, uint32_t prim, uint32_t aux)
+{
+    const uint32_t kind = prim >> PRIM_KIND_SHIFT, idx = prim & PRIM_INDEX_MASK;
+    if (kind == PK_CSG)
+        return S.csg_children[S.csgs[idx].first + (aux & 0xffffu)].object;
+    if (kind == PK_SPHERE)
+        return __ldg(S.sphere_obj + idx);
+    if (kind == PK_PLANE)
+        return __ldg(S.plane_obj + idx);
+    if (kind == PK_BOX)
+        return __float_as_int(S.boxes[idx].lo.w);
+    if (kind == PK_TORUS)
+        return S.tori[idx].object;
+    return __float_as_int(__ldg(S.tri_normal + __ldg(S.tri_global + idx)).w);
+}
+
+constexpr int MAX_SHADOW_CROSSINGS = 4096;
+
+// Shadow rays of the shading kernel in scenes with transparent surfaces
+// (Trace::TracePointLightShadowRay, trace.cpp:1951-2076, with
+// ComputeShadowColour / ComputeShadowTexture, trace.cpp:1180-1250,
+// 2274-2439): the nearest hit first; an opaque surface clears the light, a
+// transparent one filters it by its TransmittedColour and, when the shadow
+// ray is inside the surface's interior, that interior's fade over the
+// crossed depth; below ADC_Bailout the light is cleared; while light is
+// left the shadow ray's own interior list (a copy of its eye ray's) toggles
+// the interior (ComputeShadowMedia, trace.cpp:3064-3068).  The ray stops,
+// blocked, when no light is left and the object hit (the CSG it belongs
+// to) is opaque, else goes on from the hit.  Writes each ray's blocked byte
+// and scales its light term by the filtered light; counts every test after
+// the first (which the shading kernel counted) and every success.
+template <bool FULL>
+__global__ void __launch_bounds__(128) k_shadow_filter(DeviceScene S, const QRay* __restrict__ sq,
+                                                       const int* __restrict__ sq_slot,
+                                                       const uint2* __restrict__ sq_skip,
+                                                       const uint64_t* __restrict__ sq_rin,
+                                                       const int* __restrict__ sq_count, int cap,
+                                                       int* __restrict__ work, uint8_t* __restrict__ blocked,
+                                                       float4* __restrict__ slot_contrib, int stack_depth,
+                                                       uint32_t* err, unsigned long long* stats)
+{
+    extern __shared__ int smem[];
+    const int n = min(*sq_count, cap);
+    const int lane = threadIdx.x & 31;
+    const float adc = S.adc_bailout;
+    unsigned long long c_tests = 0, c_succ = 0;
+    for (;;) {   // persistent: each warp claims 32 rays at a time
+        int base = 0;
+        if (lane == 0)
+            base = atomicAdd(work, 32);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n)
+            break;
+        const int i = base + lane;
+        if (i >= n)
+            continue;
+        const QRay r = sq[i];
+        float3 o = xyz(r.org);
+        const float3 d = xyz(r.dir);
+        const float tmin = r.org.w;
+        float tmax = r.dir.w;
+        uint2 skip = sq_skip[i];
+        uint64_t rin = sq_rin[i];
+        float3 lc = f3(1.f, 1.f, 1.f);
+        bool b = false;
+        for (int cross = 0;; cross++) {
+            if (cross > 0)
+                c_tests++;
+            if (cross >= MAX_SHADOW_CROSSINGS) {
+                set_error(err, DE_ITERATION_CAP);
+                b = true;
+                break;
+            }
+            float t;
+            uint32_t prim, aux;
+            if (!nearest<FULL>(S, o, d, tmin, tmax, skip, smem, stack_depth, err, t, prim, aux))
+                break;
+            c_succ++;
+            const int obj = hit_object(S, prim, aux);
+            const DevMaterial& m = S.materials[S.objects[obj].material];
+            const int code = S.obj_interior[obj];
+            if (!m.see_through) {
+                lc = f3(0.f, 0.f, 0.f);
+            } else {
+                const float w = m.pigment.w, tm = m.transmit;
+                float3 fc = f3(m.pigment.x * w + tm, m.pigment.y * w + tm, m.pigment.z * w + tm);
+                const int id = code & 0xffff;
+                const int at = rin_find(rin, id);
+                const float4 I0 = S.interiors[2 * id];
+                if (at >= 0 && I0.z > 0.0f && fabsf(I0.y) > EPSILON_F)
+                    fc = fc * interior_fade(I0, S.interiors[2 * id + 1], t);
+                if (fabsf((fabsf(fc.x) + fabsf(fc.y) + fabsf(fc.z)) / 3.0f) < adc) {
+                    lc = f3(0.f, 0.f, 0.f);
+                } else {
+                    lc = lc * fc;
+                    if (!(fabsf(lc.x) < EPSILON_F && fabsf(lc.y) < EPSILON_F && fabsf(lc.z) < EPSILON_F)) {
+                        if (at >= 0)
+                            rin = rin_remove(rin, at);
+                        else if (!rin_append(rin, id))
+                            set_error(err, DE_INTERIORS);
+                    }
+                }
+            }
+            if (fabsf(lc.x) < EPSILON_F && fabsf(lc.y) < EPSILON_F && fabsf(lc.z) < EPSILON_F && (code >> 16) & 1) {
+                b = true;
+                break;
+            }
+            o = o + d * t;
+            tmax -= t;
+            skip = make_uint2(prim, (prim >> PRIM_KIND_SHIFT) == PK_BOX || (prim >> PRIM_KIND_SHIFT) == PK_CSG
+                                        ? aux : 0u);
+        }
+        blocked[i] = b ? 1 : 0;
+        if (!b && (lc.x != 1.f || lc.y != 1.f || lc.z != 1.f)) {
+            const int slot = sq_slot[i];
+            float4 c = slot_contrib[slot];
+            slot_contrib[slot] = make_float4(c.x * lc.x, c.y * lc.y, c.z * lc.z, c.w);
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        c_tests += __shfl_down_sync(0xffffffffu, c_tests, off);
+        c_succ += __shfl_down_sync(0xffffffffu, c_succ, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (c_tests) atomicAdd(&stats[ST_SHADOW_TESTS], c_tests);
+        if (c_succ) atomicAdd(&stats[ST_SHADOW_SUCCEEDED], c_succ);
     }
 }
 
@@ -2857,6 +3159,22 @@ cudaError_t launch_shadow_through(const DeviceScene& S, const QRay* sq, const in
         k_shadow_through<false><<<grid, block, smem, st>>>(S, sq, sq_slot, sq_skip, sq_medium, sq_count, cap, work,
                                                            blocked, slot_contrib, media_on ? 1 : 0, stack_depth, err,
                                                            stats);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_shadow_filter(const DeviceScene& S, const QRay* sq, const int* sq_slot, const uint2* sq_skip,
+                                 const uint64_t* sq_rin, const int* sq_count, int cap, int* work, uint8_t* blocked,
+                                 float4* slot_contrib, int stack_depth, int grid, uint32_t* err,
+                                 unsigned long long* stats, cudaStream_t st)
+{
+    const int block = 128;
+    size_t smem = (size_t)stack_depth * block * sizeof(int);
+    if (S.has_full_prims)
+        k_shadow_filter<true><<<grid, block, smem, st>>>(S, sq, sq_slot, sq_skip, sq_rin, sq_count, cap, work,
+                                                         blocked, slot_contrib, stack_depth, err, stats);
+    else
+        k_shadow_filter<false><<<grid, block, smem, st>>>(S, sq, sq_slot, sq_skip, sq_rin, sq_count, cap, work,
+                                                          blocked, slot_contrib, stack_depth, err, stats);
     return cudaGetLastError();
 }
 

@@ -40,6 +40,13 @@ cudaError_t launch_shadow_through(const DeviceScene& S, const QRay* sq, const in
                                   const int* sq_medium, const int* sq_count, int cap, int* work, uint8_t* blocked,
                                   float4* slot_contrib, bool media_on, int stack_depth, int grid, uint32_t* err,
                                   unsigned long long* stats, cudaStream_t st);
+// Shadow rays through transparent surfaces: each ray's blocked byte and
+// its light term scaled by the filters it crossed (sq_rin: each shadow
+// ray's interior list, from its eye ray).
+cudaError_t launch_shadow_filter(const DeviceScene& S, const QRay* sq, const int* sq_slot, const uint2* sq_skip,
+                                 const uint64_t* sq_rin, const int* sq_count, int cap, int* work, uint8_t* blocked,
+                                 float4* slot_contrib, int stack_depth, int grid, uint32_t* err,
+                                 unsigned long long* stats, cudaStream_t st);
 // Media of the queue's rays inside containers, applied to their paths
 // before shading: list the rays (mcount zeroed by the caller); per chunk of
 // listed rays, the sample rounds into cbuf and the per-interval sums (counts:

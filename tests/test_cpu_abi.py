@@ -81,12 +81,49 @@ def test_transformed_primitive_is_unsupported(gpu_lib):
     assert st == abi.POV_GPU_E_UNSUPPORTED and bad == 1
 
 
-def test_transparent_pigment_is_unsupported(gpu_lib):
-    s = scenes.spheres_plane(32, 24, n_spheres=4)
-    desc, keep = s.desc()
-    desc.materials[0].pigment[4] = 0.5    # transmit: needs refraction
-    st, _ = _create(gpu_lib, desc)
-    assert st == abi.POV_GPU_E_UNSUPPORTED
+def test_transparency_validation(gpu_lib):
+    """Transparent surfaces: a plain pigment that filters or transmits, no
+    reflection beside it (one secondary ray per hit), interiors without
+    dispersion or caustics, no radiosity or area lights in the scene, the
+    camera inside no object; rejected before any device work."""
+    ok = (abi.POV_GPU_OK, abi.POV_GPU_E_NODEVICE, abi.POV_GPU_E_CUDA)
+
+    def fresh():
+        return scenes.glass_spheres(32, 24).desc()
+    desc, keep = fresh()
+    assert _create(gpu_lib, desc)[0] in ok
+    glass = [i for i in range(desc.num_materials) if desc.materials[i].pigment[3] > 0.0][0]
+    desc, keep = fresh()
+    desc.materials[glass].reflection_max[0] = 0.2        # a second secondary ray
+    assert _create(gpu_lib, desc)[0] == abi.POV_GPU_E_UNSUPPORTED
+    desc, keep = fresh()
+    desc.interiors[0].dispersion = 1.02
+    assert _create(gpu_lib, desc)[0] == abi.POV_GPU_E_UNSUPPORTED
+    desc, keep = fresh()
+    desc.interiors[0].caustics = 0.5
+    assert _create(gpu_lib, desc)[0] == abi.POV_GPU_E_UNSUPPORTED
+    desc, keep = fresh()
+    rdesc, rkeep = scenes.radiosity_room(32, 24, n_spheres=4).desc()
+    desc.radiosity = rdesc.radiosity                     # valid radiosity settings
+    assert desc.radiosity.enabled == 1
+    assert _create(gpu_lib, desc)[0] == abi.POV_GPU_E_UNSUPPORTED
+    desc, keep = fresh()
+    desc.lights[0].kind = abi.POV_LIGHT_AREA
+    assert _create(gpu_lib, desc)[0] == abi.POV_GPU_E_UNSUPPORTED
+    desc, keep = fresh()
+    desc.object_interior[3] = desc.num_interiors + 1     # no such interior
+    assert _create(gpu_lib, desc)[0] == abi.POV_GPU_E_INVALID
+    desc, keep = fresh()
+    sph = [i for i in range(desc.num_objects) if desc.objects[i].type == abi.POV_OBJ_SPHERE
+           and desc.objects[i].parent < 0][0]
+    for k in range(3):
+        desc.camera.location[k] = desc.objects[sph].p[k]  # the camera inside a sphere
+    assert _create(gpu_lib, desc) == (abi.POV_GPU_E_UNSUPPORTED, sph)
+    # an opaque scene is not held to these rules
+    desc, keep = scenes.spheres_plane(32, 24, n_spheres=4).desc()
+    for k in range(3):
+        desc.camera.location[k] = desc.objects[1].p[k]
+    assert _create(gpu_lib, desc)[0] in ok
 
 
 def test_bad_mesh_index_is_invalid(gpu_lib):
