@@ -90,6 +90,22 @@ def parse():
     return ap.parse_args()
 
 
+def job_totals(times, units, dist=None, device="cpu"):
+    """Whole-job figures of a replica run: each time the largest over the
+    ranks (the job ends with its slowest rank), each unit count summed over
+    the ranks (every replica renders its own frames).  No data-path
+    collective: this is the one reduction of the run, after the timed
+    region."""
+    if dist is None:
+        return [float(t) for t in times], [int(u) for u in units]
+    import torch
+    t = torch.tensor([float(x) for x in times], dtype=torch.float64, device=device)
+    u = torch.tensor([int(x) for x in units], dtype=torch.int64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return [float(x) for x in t.tolist()], [int(x) for x in u.tolist()]
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -420,14 +436,10 @@ def main():
     e2e_wall = time.perf_counter() - t0
     e2e_t = max(e2e_wall, e0.elapsed_time(e1) / 1e3)
 
-    # max over ranks
-    if dist:
-        tt = torch.tensor([t_total, e2e_t], device="cuda", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_total, e2e_t = float(tt[0]), float(tt[1])
-
-    value = world * rays / t_total / 1e6
-    e2e_value = world * e2e_rays / e2e_t / 1e6
+    # max over ranks of the times, rays summed over the replicas
+    (t_total, e2e_t), (job_rays, job_e2e_rays) = job_totals([t_total, e2e_t], [rays, e2e_rays], dist, "cuda")
+    value = job_rays / t_total / 1e6
+    e2e_value = job_e2e_rays / e2e_t / 1e6
     # roofline of the dominant kernel (closest-hit traversal): algorithmic
     # bytes = 32 B ray + 16 B hit per ray + 112 B per node visit (the four
     # child boxes and links of a four-wide node) + 48 B per triangle test +
