@@ -357,6 +357,13 @@ static void grow_outward(AABB& b, double x, double y, double z)
 // ---------------------------------------------------------------- scene --
 namespace {
 
+// Deferred torus tests a wavefront's list holds: four per shadow ray
+// (64 Mi at most); beyond it the traversal solves them in line.
+inline size_t tcand_cap(size_t maxq, int nl)
+{
+    return std::min<size_t>((size_t)4 * maxq * (size_t)std::max(nl, 1), (size_t)64 << 20);
+}
+
 // Counter slots of a wavefront (PathBufs::counters).
 enum {
     C_QA = 0,     // count of queue A
@@ -372,7 +379,8 @@ enum {
     C_MC = 10,    // rays crossing a media container's interior
     C_ML = 11,    // media samples listed for the next round
     C_MW = 12,    // work counter of the media sample rounds
-    C_NUM = 13
+    C_TC = 13,    // deferred torus tests of the current traversal launch
+    C_NUM = 14
 };
 
 // One wavefront of ray queues and per-path state: the camera's, or the
@@ -388,12 +396,13 @@ struct PathBufs {
     DevBuf mcbuf, mrounds;          // media containers: sample slots of a chunk, round lists
     DevBuf bin_keys, bin_hist, bin_order;   // textured scenes: the shade queue binned by material
     DevBuf rinA, rinB, srin;        // transparent scenes: per-ray and shadow-ray interior lists
+    DevBuf tcand, tkey;             // scenes with tori: deferred torus tests, per-ray nearest roots
     DevBuf counters;
 
     // media_ni: interval slots per ray segment (0: the scene has no media
     // containers); transparent: rays carry their level and interior list
     cudaError_t ensure(size_t maxq, int nl, int nal, bool rad, bool sample_rays, int media_ni = 0,
-                       bool binned = false, bool transparent = false)
+                       bool binned = false, bool transparent = false, bool tori = false)
     {
         maxq = std::max<size_t>(maxq, 1);
         nl = std::max(nl, 1);
@@ -409,7 +418,7 @@ struct PathBufs {
         PB_ENSURE(slot_contrib, sizeof(float4) * maxq * nl);
         PB_ENSURE(sq, sizeof(QRay) * maxq * nl);
         PB_ENSURE(sq_slot, sizeof(int) * maxq * nl);
-        PB_ENSURE(blocked, maxq * nl);
+        PB_ENSURE(blocked, (maxq * nl + 3) & ~(size_t)3);   // whole words (k_torus_solve's atomicOr)
         PB_ENSURE(skipA, sizeof(uint2) * maxq);
         PB_ENSURE(skipB, sizeof(uint2) * maxq);
         PB_ENSURE(sskip, sizeof(uint2) * maxq * nl);
@@ -439,6 +448,10 @@ struct PathBufs {
             PB_ENSURE(mte, sizeof(float4) * maxq * media_ni);
             PB_ENSURE(mod, sizeof(float4) * maxq * media_ni);
         }
+        if (tori) {
+            PB_ENSURE(tcand, sizeof(uint2) * tcand_cap(maxq, nl));
+            PB_ENSURE(tkey, sizeof(unsigned long long) * maxq);
+        }
         if (transparent) {
             PB_ENSURE(stateA, sizeof(int) * maxq);
             PB_ENSURE(stateB, sizeof(int) * maxq);
@@ -454,7 +467,7 @@ struct PathBufs {
         DevBuf* all[] = {&qA, &qB, &pathA, &pathB, &hits, &paths, &slot_contrib, &sq, &sq_slot, &blocked, &skipA,
                          &skipB, &sskip, &aq, &aq_slot, &aq_skip, &rq, &rq_amb, &quality, &first_t, &stateA,
                          &stateB, &smedium, &mlist, &mte, &mod, &mcbuf, &mrounds, &bin_keys, &bin_hist,
-                         &bin_order, &rinA, &rinB, &srin, &counters};
+                         &bin_order, &rinA, &rinB, &srin, &tcand, &tkey, &counters};
         for (DevBuf* b : all)
             b->release();
     }
@@ -569,6 +582,7 @@ struct PovGpuScene {
     uint32_t graph_launches = 0;   // kernels in the graph
     bool   textured = false;   // some material has a pattern pigment or a normal: bin the shade queue
     bool   transparent = false;   // some surface filters or transmits: rays carry interior lists
+    bool   top_tori = false;      // tori outside CSG: traversal defers their FP64 tests
     DevBuf obj_interior, interiors;   // per object its interior id; per interior its float4 pair
     int    media_ni = 0;   // interval slots per media segment (0: no media containers)
     int    media_smax = 0;  // sample slots per interval (ends + sample-tree nodes)
@@ -1503,6 +1517,9 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
     // leaf-order slot directly, so a leaf's triangles are contiguous)
     std::vector<float4> lv0, le1, le2;
     std::vector<int32_t> tri_global;
+    sc->top_tori = false;
+    for (uint32_t r : B.bvh.refs)
+        sc->top_tori = sc->top_tori || (r >> PRIM_KIND_SHIFT) == PK_TORUS;
     lv0.reserve(B.tri_v0.size());
     le1.reserve(B.tri_v0.size());
     le2.reserve(B.tri_v0.size());
@@ -2013,7 +2030,14 @@ int run_levels(PovGpuScene* sc, StageClock& clk, PathBufs& B, size_t maxq, int l
     const bool media = sc->media_ni > 0;
     const bool transparent = sc->transparent;
     const bool staged = media || transparent;   // rays carry their own level
-    CK(B.ensure(maxq, nl, nal, rad, sample_rays, sc->media_ni, sc->textured, transparent));
+    CK(B.ensure(maxq, nl, nal, rad, sample_rays, sc->media_ni, sc->textured, transparent, sc->top_tori));
+    TorusDefer tdc{}, tds{};   // closest-hit and any-hit launches
+    if (sc->top_tori) {
+        tdc.cand = tds.cand = B.tcand.as<uint2>();
+        tdc.count = tds.count = B.counters.as<int>() + C_TC;
+        tdc.cap = tds.cap = (int)tcand_cap(maxq, nl);
+        tdc.key = B.tkey.as<unsigned long long>();
+    }
     cudaStream_t st = sc->active();
     int* cnt = B.counters.as<int>();
     unsigned long long* dstats = sc->stats.as<unsigned long long>();
@@ -2076,7 +2100,7 @@ int run_levels(PovGpuScene* sc, StageClock& clk, PathBufs& B, size_t maxq, int l
         CK(cudaMemsetAsync(cnt + C_AQ, 0, sizeof(int) * 2, st));   // AQ, RQ
         CK(clk.begin(POV_GPU_STAGE_TRACE_CLOSEST));
         CK(launch_trace(S, false, qcur, ccur, cnt + C_W0, B.hits.as<QHit>(), nullptr, sc->stack_depth, grid_trace,
-                        derr, dstats, wc, (int)maxq, kcur, st, tblock, tocc));
+                        derr, dstats, wc, (int)maxq, kcur, st, tblock, tocc, sc->top_tori ? &tdc : nullptr));
         CK(clk.end());
         if (sample_rays && pass == 0)
             CK(launch_first_hit(B.hits.as<QHit>(), ccur, (int)maxq, B.first_t.as<float>(), grid_shade, st));
@@ -2126,7 +2150,7 @@ int run_levels(PovGpuScene* sc, StageClock& clk, PathBufs& B, size_t maxq, int l
             else
                 CK(launch_trace(S, true, B.sq.as<QRay>(), cnt + C_SQ, cnt + C_W1, nullptr, B.blocked.as<uint8_t>(),
                                 sc->stack_depth, grid_trace, derr, dstats, wc ? wc + 4 : nullptr, (int)(maxq * nl),
-                                B.sskip.as<uint2>(), st, tblock, tocc));
+                                B.sskip.as<uint2>(), st, tblock, tocc, sc->top_tori ? &tds : nullptr));
             CK(clk.end());
             CK(clk.begin(POV_GPU_STAGE_RESOLVE));
             CK(launch_resolve(pcur, ccur, sc->num_lights, B.sq_slot.as<int>(), B.blocked.as<uint8_t>(), cnt + C_SQ,

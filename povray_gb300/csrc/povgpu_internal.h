@@ -263,6 +263,23 @@ struct __align__(16) QHit {
     float    u, v;   // triangle barycentrics
 };
 
+// Deferred torus tests of one traversal launch.  The traversal kernel
+// appends each (ray, torus) pair that passes the FP32 pre-cull to `cand`
+// (ray index | bit 31 when the torus is the ray's own origin surface, torus
+// index) instead of running the FP64 quartic in the one lane that met it;
+// k_torus_solve then solves the pairs one per thread, so a warp's FP64
+// instructions run with all 32 lanes instead of the few that reached a
+// torus together.  Closest hits keep the nearest root per ray in `key`
+// (depth bits << 32 | prim reference, atomicMin), merged into the hits
+// afterwards; any-hit rays set their blocked byte.  Pairs beyond `cap` are
+// solved in line, as without deferral.
+struct TorusDefer {
+    uint2*              cand;
+    int*                count;
+    int                 cap;
+    unsigned long long* key;   // per ray (closest hits)
+};
+
 // Per-path state (one path per image sample).
 struct __align__(16) PathState {
     float4 colour;      // accumulated rgb, transm

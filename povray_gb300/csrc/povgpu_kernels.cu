@@ -25,6 +25,7 @@
 #include "povgpu.h"
 #include "povgpu_quartic.cuh"
 
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <math_constants.h>
 #include <stdint.h>
@@ -771,8 +772,9 @@ __global__ void __launch_bounds__(128, MINB) k_trace(DeviceScene S, const QRay* 
                                                QHit* __restrict__ hits, uint8_t* __restrict__ blocked,
                                                int stack_depth, uint32_t* err, unsigned long long* stats,
                                                unsigned long long* wcount, int cap,
-                                               const uint2* __restrict__ skips)
+                                               const uint2* __restrict__ skips, TorusDefer td)
 {
+    namespace cg = cooperative_groups;
     extern __shared__ int smem[];
     const int lane = threadIdx.x & 31;
     const int n = min(*q_count, cap);   // never read past the queue buffer
@@ -799,6 +801,8 @@ __global__ void __launch_bounds__(128, MINB) k_trace(DeviceScene S, const QRay* 
         float bu = 0.f, bv = 0.f;
         bool done = false;
         const uint2 skip = skips ? skips[i] : make_uint2(NO_PRIM, 0u);
+        if (FULL && !ANY && td.key)
+            td.key[i] = ~0ull;   // no deferred torus root yet
         // infinite objects first (planes: Plane::Intersect, plane.cpp:139-211)
         for (int k = 0; k < S.num_planes; k++) {
             if (((PK_PLANE << PRIM_KIND_SHIFT) | (uint32_t)k) == skip.x)
@@ -835,6 +839,22 @@ __global__ void __launch_bounds__(128, MINB) k_trace(DeviceScene S, const QRay* 
                 for (uint32_t k = 0; k < count; k++) {
                     uint32_t ref = __ldg(S.prim_refs + first + k);
                     if (counting) { c_prims++; c_tris += (ref >> PRIM_KIND_SHIFT) == PK_TRIANGLE; }
+                    if (FULL && td.cand && (ref >> PRIM_KIND_SHIFT) == PK_TORUS) {
+                        const uint32_t idx = ref & PRIM_INDEX_MASK;
+                        if (!torus_may_hit(S.tori32 + 4 * (size_t)idx, o, d, t))
+                            continue;
+                        // one slot per lane that got here, one atomic per group
+                        cg::coalesced_group g = cg::coalesced_threads();
+                        int slot = 0;
+                        if (g.thread_rank() == 0)
+                            slot = atomicAdd(td.count, (int)g.size());
+                        slot = g.shfl(slot, 0) + (int)g.thread_rank();
+                        if (slot < td.cap) {
+                            td.cand[slot] = make_uint2((uint32_t)i | (ref == skip.x ? 0x80000000u : 0u), idx);
+                            continue;
+                        }
+                        // the list is full: solved here
+                    }
                     uint32_t aux = 0;
                     if (prim_test<ANY, FULL>(S, ref, o, d, tmin, t, bu, bv, aux, skip)) {
                         best = ref;
@@ -878,6 +898,89 @@ __global__ void __launch_bounds__(128, MINB) k_trace(DeviceScene S, const QRay* 
             atomicAdd(&wcount[1], c_prims);
             atomicAdd(&wcount[2], c_tris);
             atomicAdd(&wcount[3], c_rays);
+        }
+    }
+}
+
+// The deferred torus tests of one traversal launch, one pair per thread
+// (TorusDefer): Torus::Intersect's roots in FP64 (torus_roots), the ray's
+// own origin root dropped, the nearest root in [tmin, tmax) -- tmax the
+// ray's nearest other hit so far -- kept per ray with a 64-bit atomicMin on
+// (depth bits, prim); any-hit rays with a root in range are blocked (and
+// counted once per ray).
+template <bool ANY>
+__global__ void __launch_bounds__(128) k_torus_solve(DeviceScene S, const QRay* __restrict__ q, TorusDefer td,
+                                                     const QHit* __restrict__ hits, uint8_t* __restrict__ blocked,
+                                                     unsigned long long* stats)
+{
+    const int n = min(*td.count, td.cap);
+    unsigned long long nblocked = 0;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+        const uint2 e = td.cand[c];
+        const int ray = (int)(e.x & 0x7fffffffu);
+        const bool self = (e.x >> 31) != 0;
+        if (ANY && *(volatile const uint8_t*)(blocked + ray))
+            continue;   // blocked already
+        const QRay r = q[ray];
+        float tmax = r.dir.w;
+        if (!ANY)
+            tmax = fminf(hits[ray].t, __uint_as_float((uint32_t)(td.key[ray] >> 32)));
+        double rt[4];
+        int nr = torus_roots(S.tori[e.y], make_double3(r.org.x, r.org.y, r.org.z),
+                             make_double3(r.dir.x, r.dir.y, r.dir.z), rt);
+        if (self)
+            nr = torus_drop_self(rt, nr);
+        float best = tmax;
+        bool hit = false;
+        for (int k = 0; k < nr; k++) {
+            const float tt = (float)rt[k];
+            if (tt >= r.org.w && tt < best) {
+                best = tt;
+                hit = true;
+            }
+        }
+        if (!hit)
+            continue;
+        if (ANY) {
+            // the ray's byte within its aligned word (the buffer is padded
+            // to whole words)
+            const size_t off = (size_t)ray;
+            unsigned int* w = reinterpret_cast<unsigned int*>(blocked + (off & ~(size_t)3));
+            const unsigned int bit = 1u << (8 * (unsigned)(off & 3));
+            const unsigned int old = atomicOr(w, bit);
+            if (!(old & (0xffu << (8 * (unsigned)(off & 3)))))
+                nblocked++;
+        } else {
+            const uint32_t ref = (PK_TORUS << PRIM_KIND_SHIFT) | e.y;
+            atomicMin(td.key + ray, ((unsigned long long)__float_as_uint(best) << 32) | ref);
+        }
+    }
+    if (ANY) {
+        for (int off = 16; off > 0; off >>= 1)
+            nblocked += __shfl_down_sync(0xffffffffu, nblocked, off);
+        if ((threadIdx.x & 31) == 0 && nblocked)
+            atomicAdd(&stats[ST_SHADOW_SUCCEEDED], nblocked);
+    }
+}
+
+// Deferred torus roots into the closest hits: a root nearer than the ray's
+// other hit replaces it (k_trace wrote every ray's key).
+__global__ void k_torus_merge(const int* __restrict__ q_count, int cap, const TorusDefer td,
+                              QHit* __restrict__ hits)
+{
+    const int n = min(*q_count, cap);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const unsigned long long key = td.key[i];
+        if (key == ~0ull)
+            continue;
+        const float t = __uint_as_float((uint32_t)(key >> 32));
+        if (t < hits[i].t) {
+            QHit h;
+            h.t = t;
+            h.prim = (uint32_t)key;
+            h.u = 0.0f;
+            h.v = 0.0f;
+            hits[i] = h;
         }
     }
 }
@@ -2998,31 +3101,47 @@ cudaError_t launch_load_rays(const double* org, const double* dir, int n, QRay* 
 cudaError_t launch_trace(const DeviceScene& S, bool any_hit, const QRay* q, const int* q_count, int* work,
                          QHit* hits, uint8_t* blocked, int stack_depth, int grid, uint32_t* err,
                          unsigned long long* stats, unsigned long long* wcount, int cap, const uint2* skips,
-                         cudaStream_t st, int block, int occ)
+                         cudaStream_t st, int block, int occ, const TorusDefer* defer)
 {
     block = block == 64 ? 64 : 128;   // warps claim 32 rays; the stack is smem[k * blockDim + tid]
     size_t smem = (size_t)stack_depth * block * sizeof(int);
     // the full variant carries the FP64 torus solver and CSG; scenes without
     // them run the lean one (about half the registers)
     const bool full = S.has_full_prims != 0;
+    TorusDefer td{};
+    if (full && defer && defer->cand && defer->count && (any_hit || defer->key)) {
+        td = *defer;
+        cudaError_t e = cudaMemsetAsync(td.count, 0, sizeof(int), st);
+        if (e != cudaSuccess)
+            return e;
+    }
     if (any_hit && full)
         k_trace<true, true, 1><<<grid, block, smem, st>>>(S, q, q_count, work, hits, blocked, stack_depth, err,
-                                                          stats, wcount, cap, skips);
+                                                          stats, wcount, cap, skips, td);
     else if (any_hit && occ)
         k_trace<true, false, 8><<<grid, block, smem, st>>>(S, q, q_count, work, hits, blocked, stack_depth, err,
-                                                           stats, wcount, cap, skips);
+                                                           stats, wcount, cap, skips, td);
     else if (any_hit)
         k_trace<true, false, 1><<<grid, block, smem, st>>>(S, q, q_count, work, hits, blocked, stack_depth, err,
-                                                           stats, wcount, cap, skips);
+                                                           stats, wcount, cap, skips, td);
     else if (full)
         k_trace<false, true, 1><<<grid, block, smem, st>>>(S, q, q_count, work, hits, blocked, stack_depth, err,
-                                                           stats, wcount, cap, skips);
+                                                           stats, wcount, cap, skips, td);
     else if (occ)
         k_trace<false, false, 8><<<grid, block, smem, st>>>(S, q, q_count, work, hits, blocked, stack_depth, err,
-                                                            stats, wcount, cap, skips);
+                                                            stats, wcount, cap, skips, td);
     else
         k_trace<false, false, 1><<<grid, block, smem, st>>>(S, q, q_count, work, hits, blocked, stack_depth, err,
-                                                            stats, wcount, cap, skips);
+                                                            stats, wcount, cap, skips, td);
+    if (td.cand) {
+        const int g = grid;   // the traversal's persistent grid: SMs x blocks per SM
+        if (any_hit) {
+            k_torus_solve<true><<<g, 128, 0, st>>>(S, q, td, hits, blocked, stats);
+        } else {
+            k_torus_solve<false><<<g, 128, 0, st>>>(S, q, td, hits, blocked, stats);
+            k_torus_merge<<<g, 256, 0, st>>>(q_count, cap, td, hits);
+        }
+    }
     return cudaGetLastError();
 }
 

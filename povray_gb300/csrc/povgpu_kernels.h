@@ -16,7 +16,7 @@ cudaError_t launch_load_rays(const double* org, const double* dir, int n, QRay* 
 cudaError_t launch_trace(const DeviceScene& S, bool any_hit, const QRay* q, const int* q_count, int* work,
                          QHit* hits, uint8_t* blocked, int stack_depth, int grid, uint32_t* err,
                          unsigned long long* stats, unsigned long long* wcount, int cap, const uint2* skips,
-                         cudaStream_t st, int block = 128, int occ = 0);
+                         cudaStream_t st, int block = 128, int occ = 0, const TorusDefer* defer = nullptr);
 cudaError_t launch_shade(const DeviceScene& S, int level, int max_level, const QRay* q, const int* q_path,
                          const QHit* hits,
                          const int* q_count, PathState* paths, float4* slot_contrib, QRay* sq, int* sq_slot,
