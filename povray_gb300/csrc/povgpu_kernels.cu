@@ -221,7 +221,8 @@ __global__ void k_load_rays(const double* __restrict__ org, const double* __rest
 // ------------------------------------------------------------ sphere --
 // Sphere::Intersect (sphere.cpp:214-245) with the chord taken from the
 // perpendicular offset vector, which keeps FP32 accurate away from the
-// sphere; the near-tangent band is re-solved in FP64.  Both roots, or 0.
+// sphere; the near-tangent band |r^2 - perp^2| <= 1e-4 r^2 is re-solved in
+// FP64, FP32 decides outside it (hits and misses alike).  Both roots, or 0.
 __device__ __forceinline__ int sphere_roots(float4 s, float3 o, float3 d, float& t1, float& t2)
 {
     float3 oc = xyz(s) - o;
@@ -232,6 +233,8 @@ __device__ __forceinline__ int sphere_roots(float4 s, float3 o, float3 d, float&
         return 0;
     float3 perp = oc - d * tca;
     float thcs = r2 - dot3(perp, perp);
+    if (thcs < -1.0e-4f * r2)
+        return 0;   // a clear miss: outside the band on the far side as well
     if (thcs <= 1.0e-4f * r2) {
         double ox = (double)s.x - o.x, oy = (double)s.y - o.y, oz = (double)s.z - o.z;
         double tcad = ox * d.x + oy * d.y + oz * d.z;
