@@ -43,7 +43,10 @@ extern "C" {
 #define POV_GPU_E_NOMEM        -5  /* device allocation failed                 */
 #define POV_GPU_E_DEVICE       -6  /* a kernel raised its device error word    */
 #define POV_GPU_E_NODEVICE     -7  /* no CUDA device visible                   */
-#define POV_GPU_E_CAPACITY     -8  /* request above a fixed scratch capacity   */
+#define POV_GPU_E_CAPACITY     -8  /* request above a fixed scratch capacity;
+                                      also a frame whose rays cross more than
+                                      64 surfaces straight on at one trace
+                                      level (transparent scenes)           */
 
 /* ---- object types (subset of the reference's ObjectBase zoo) ------------ */
 #define POV_OBJ_SPHERE        1   /* source/core/shape/sphere.cpp   */
@@ -424,6 +427,14 @@ typedef struct PovGpuScene PovGpuScene;
  * (source/backend/scene/view.cpp:1185-1190).  Unsupported object types,
  * textures or lights return POV_GPU_E_UNSUPPORTED and store the offending
  * object index in *bad_index (when non-NULL).
+ *
+ * Transparent surfaces (a plain pigment with filter or transmit, outside
+ * media containers) are taken when each hit continues into one ray: no
+ * reflection on a transparent material, interiors with dispersion 1 and
+ * caustics 0, no media containers, radiosity or area lights in the scene,
+ * the camera inside no object (*bad_index: the object around it), at most
+ * 256 interiors of transparent surfaces.  A ray inside more than 7
+ * interiors at once sets the device error (POV_GPU_E_DEVICE).
  */
 int pov_gpu_scene_create(const PovGpuSceneDesc* desc, PovGpuScene** out, int32_t* bad_index);
 

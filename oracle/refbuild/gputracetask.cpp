@@ -71,6 +71,8 @@ void GpuTraceTask::Run()
         stats[Shadow_Rays_Succeeded] += st.shadow_rays_succeeded;
         stats[Reflected_Rays_Traced] += st.reflected_rays;
         stats[Transmitted_Rays_Traced] += st.transmitted_rays;
+        stats[Refracted_Rays_Traced] += st.refracted_rays;
+        stats[Internal_Reflected_Rays_Traced] += st.internal_reflected_rays;
         stats[Media_Samples] += st.media_samples;
         Cooperate();   // stop / pause between library calls
     }
