@@ -380,7 +380,9 @@ enum {
     C_ML = 11,    // media samples listed for the next round
     C_MW = 12,    // work counter of the media sample rounds
     C_TC = 13,    // deferred torus tests of the current traversal launch
-    C_NUM = 14
+    C_TO = 14,    // rays handed to the second traversal launch (torus-free variant)
+    C_TW = 15,    // work counter of that launch
+    C_NUM = 16
 };
 
 // One wavefront of ray queues and per-path state: the camera's, or the
@@ -397,12 +399,13 @@ struct PathBufs {
     DevBuf bin_keys, bin_hist, bin_order;   // textured scenes: the shade queue binned by material
     DevBuf rinA, rinB, srin;        // transparent scenes: per-ray and shadow-ray interior lists
     DevBuf tcand, tkey;             // scenes with tori: deferred torus tests, per-ray nearest roots
+    DevBuf tovf;                    // torus-free traversal: rays for the second launch
     DevBuf counters;
 
     // media_ni: interval slots per ray segment (0: the scene has no media
     // containers); transparent: rays carry their level and interior list
     cudaError_t ensure(size_t maxq, int nl, int nal, bool rad, bool sample_rays, int media_ni = 0,
-                       bool binned = false, bool transparent = false, bool tori = false)
+                       bool binned = false, bool transparent = false, bool tori = false, bool torus_free = false)
     {
         maxq = std::max<size_t>(maxq, 1);
         nl = std::max(nl, 1);
@@ -452,6 +455,8 @@ struct PathBufs {
             PB_ENSURE(tcand, sizeof(uint2) * tcand_cap(maxq, nl));
             PB_ENSURE(tkey, sizeof(unsigned long long) * maxq);
         }
+        if (torus_free)
+            PB_ENSURE(tovf, sizeof(int) * maxq * nl);
         if (transparent) {
             PB_ENSURE(stateA, sizeof(int) * maxq);
             PB_ENSURE(stateB, sizeof(int) * maxq);
@@ -467,7 +472,7 @@ struct PathBufs {
         DevBuf* all[] = {&qA, &qB, &pathA, &pathB, &hits, &paths, &slot_contrib, &sq, &sq_slot, &blocked, &skipA,
                          &skipB, &sskip, &aq, &aq_slot, &aq_skip, &rq, &rq_amb, &quality, &first_t, &stateA,
                          &stateB, &smedium, &mlist, &mte, &mod, &mcbuf, &mrounds, &bin_keys, &bin_hist,
-                         &bin_order, &rinA, &rinB, &srin, &tcand, &tkey, &counters};
+                         &bin_order, &rinA, &rinB, &srin, &tcand, &tkey, &tovf, &counters};
         for (DevBuf* b : all)
             b->release();
     }
@@ -583,6 +588,7 @@ struct PovGpuScene {
     bool   textured = false;   // some material has a pattern pigment or a normal: bin the shade queue
     bool   transparent = false;   // some surface filters or transmits: rays carry interior lists
     bool   top_tori = false;      // tori outside CSG: traversal defers their FP64 tests
+    bool   csg_torus = false;     // a CSG has a torus child: no torus-free traversal variant
     DevBuf obj_interior, interiors;   // per object its interior id; per interior its float4 pair
     int    media_ni = 0;   // interval slots per media segment (0: no media containers)
     int    media_smax = 0;  // sample slots per interval (ends + sample-tree nodes)
@@ -1520,6 +1526,9 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
     sc->top_tori = false;
     for (uint32_t r : B.bvh.refs)
         sc->top_tori = sc->top_tori || (r >> PRIM_KIND_SHIFT) == PK_TORUS;
+    sc->csg_torus = false;
+    for (const DevCsgChild& c : B.csg_children)
+        sc->csg_torus = sc->csg_torus || c.kind == PK_TORUS;
     lv0.reserve(B.tri_v0.size());
     le1.reserve(B.tri_v0.size());
     le2.reserve(B.tri_v0.size());
@@ -2030,13 +2039,27 @@ int run_levels(PovGpuScene* sc, StageClock& clk, PathBufs& B, size_t maxq, int l
     const bool media = sc->media_ni > 0;
     const bool transparent = sc->transparent;
     const bool staged = media || transparent;   // rays carry their own level
-    CK(B.ensure(maxq, nl, nal, rad, sample_rays, sc->media_ni, sc->textured, transparent, sc->top_tori));
+    // scenes with tori or CSG: torus tests deferred out of the traversal,
+    // and where no CSG holds a torus the traversal's torus-free variant
+    const bool torus_free = sc->S.has_full_prims && !sc->csg_torus;
+    CK(B.ensure(maxq, nl, nal, rad, sample_rays, sc->media_ni, sc->textured, transparent, sc->top_tori,
+                torus_free));
     TorusDefer tdc{}, tds{};   // closest-hit and any-hit launches
+    const bool defer = sc->top_tori || torus_free;
+    if (defer) {
+        tdc.count = tds.count = B.counters.as<int>() + C_TC;
+        tdc.ovf_count = tds.ovf_count = B.counters.as<int>() + C_TO;
+        tdc.ovf_work = tds.ovf_work = B.counters.as<int>() + C_TW;
+    }
     if (sc->top_tori) {
         tdc.cand = tds.cand = B.tcand.as<uint2>();
-        tdc.count = tds.count = B.counters.as<int>() + C_TC;
         tdc.cap = tds.cap = (int)tcand_cap(maxq, nl);
         tdc.key = B.tkey.as<unsigned long long>();
+    }
+    if (torus_free) {
+        tdc.ovf = tds.ovf = B.tovf.as<int>();
+        tdc.ovf_cap = (int)maxq;
+        tds.ovf_cap = (int)(maxq * nl);
     }
     cudaStream_t st = sc->active();
     int* cnt = B.counters.as<int>();
@@ -2100,7 +2123,7 @@ int run_levels(PovGpuScene* sc, StageClock& clk, PathBufs& B, size_t maxq, int l
         CK(cudaMemsetAsync(cnt + C_AQ, 0, sizeof(int) * 2, st));   // AQ, RQ
         CK(clk.begin(POV_GPU_STAGE_TRACE_CLOSEST));
         CK(launch_trace(S, false, qcur, ccur, cnt + C_W0, B.hits.as<QHit>(), nullptr, sc->stack_depth, grid_trace,
-                        derr, dstats, wc, (int)maxq, kcur, st, tblock, tocc, sc->top_tori ? &tdc : nullptr));
+                        derr, dstats, wc, (int)maxq, kcur, st, tblock, tocc, defer ? &tdc : nullptr));
         CK(clk.end());
         if (sample_rays && pass == 0)
             CK(launch_first_hit(B.hits.as<QHit>(), ccur, (int)maxq, B.first_t.as<float>(), grid_shade, st));
@@ -2150,7 +2173,7 @@ int run_levels(PovGpuScene* sc, StageClock& clk, PathBufs& B, size_t maxq, int l
             else
                 CK(launch_trace(S, true, B.sq.as<QRay>(), cnt + C_SQ, cnt + C_W1, nullptr, B.blocked.as<uint8_t>(),
                                 sc->stack_depth, grid_trace, derr, dstats, wc ? wc + 4 : nullptr, (int)(maxq * nl),
-                                B.sskip.as<uint2>(), st, tblock, tocc, sc->top_tori ? &tds : nullptr));
+                                B.sskip.as<uint2>(), st, tblock, tocc, defer ? &tds : nullptr));
             CK(clk.end());
             CK(clk.begin(POV_GPU_STAGE_RESOLVE));
             CK(launch_resolve(pcur, ccur, sc->num_lights, B.sq_slot.as<int>(), B.blocked.as<uint8_t>(), cnt + C_SQ,

@@ -272,12 +272,19 @@ struct __align__(16) QHit {
 // torus together.  Closest hits keep the nearest root per ray in `key`
 // (depth bits << 32 | prim reference, atomicMin), merged into the hits
 // afterwards; any-hit rays set their blocked byte.  Pairs beyond `cap` are
-// solved in line, as without deferral.
+// solved in line, as without deferral -- or, with `ovf` set (scenes whose
+// CSGs have no torus children), the traversal runs its torus-free variant
+// and lists such rays in `ovf` for a second launch of the ordinary one.
+// count, ovf_count and ovf_work are three consecutive ints, zeroed per launch.
 struct TorusDefer {
     uint2*              cand;
     int*                count;
     int                 cap;
     unsigned long long* key;   // per ray (closest hits)
+    int*                ovf;       // rays to trace again with the full variant
+    int*                ovf_count;
+    int*                ovf_work;  // the second launch's work counter
+    int                 ovf_cap;
 };
 
 // Per-path state (one path per image sample).

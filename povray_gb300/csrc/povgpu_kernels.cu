@@ -504,12 +504,15 @@ __device__ __forceinline__ int torus_drop_self(double* t, int n)
 }
 
 // ---------------------------------------------------------------- CSG --
+// NT: the scene's CSGs have no torus children (the torus-free traversal
+// variant carries no FP64 torus code, which halves its registers).
+template <bool NT = false>
 __device__ __forceinline__ bool child_inside(const DeviceScene& S, const DevCsgChild& c, float3 p)
 {
     switch (c.kind) {
     case PK_SPHERE: return sphere_inside(__ldg(S.spheres + c.index), c.flags, p);
     case PK_BOX: return box_inside(S.boxes[c.index], c.flags, p);
-    case PK_TORUS: return torus_inside(S.tori[c.index], p);
+    case PK_TORUS: return NT ? false : torus_inside(S.tori[c.index], p);
     case PK_PLANE: {
         float4 pl = __ldg(S.planes + c.index);
         return dot3(p, xyz(pl)) + pl.w < EPSILON_F;
@@ -519,6 +522,7 @@ __device__ __forceinline__ bool child_inside(const DeviceScene& S, const DevCsgC
 }
 
 // Roots of one CSG child with the aux word (box side).
+template <bool NT = false>
 __device__ __forceinline__ int child_roots(const DeviceScene& S, const DevCsgChild& c, float3 o, float3 d,
                                            float* t, int* side, bool self, int self_side)
 {
@@ -546,7 +550,7 @@ __device__ __forceinline__ int child_roots(const DeviceScene& S, const DevCsgChi
                 t[n] = tf; side[n++] = sf;
             }
         }
-    } else if (c.kind == PK_TORUS) {
+    } else if (!NT && c.kind == PK_TORUS) {
         double r[4];
         int k = torus_roots(S.tori[c.index], make_double3(o.x, o.y, o.z), make_double3(d.x, d.y, d.z), r);
         if (self) k = torus_drop_self(r, k);
@@ -566,6 +570,7 @@ __device__ __forceinline__ int child_roots(const DeviceScene& S, const DevCsgChi
 // filter: a child's root survives if the point is inside every sibling
 // (intersection) or inside none (merge).  Returns the best surviving root in
 // [tmin, t) and its (child, side) aux word.
+template <bool NT = false>
 __device__ __forceinline__ bool csg_closest(const DeviceScene& S, uint32_t idx, float3 o, float3 d, float tmin,
                                             float& t, uint32_t& aux, uint2 skip, uint32_t ref, bool any)
 {
@@ -577,7 +582,7 @@ __device__ __forceinline__ bool csg_closest(const DeviceScene& S, uint32_t idx, 
         bool self = skip.x == ref && (int)(skip.y & 0xffffu) == c;
         float rt[4];
         int rs[4];
-        int n = child_roots(S, ch, o, d, rt, rs, self, (int)(skip.y >> 16));
+        int n = child_roots<NT>(S, ch, o, d, rt, rs, self, (int)(skip.y >> 16));
         for (int k = 0; k < n; k++) {
             if (!(rt[k] >= tmin && rt[k] < t))
                 continue;
@@ -586,7 +591,7 @@ __device__ __forceinline__ bool csg_closest(const DeviceScene& S, uint32_t idx, 
             for (int s = 0; s < g.count && keep; s++) {
                 if (s == c)
                     continue;
-                bool in = child_inside(S, S.csg_children[g.first + s], p);
+                bool in = child_inside<NT>(S, S.csg_children[g.first + s], p);
                 keep = merge ? !in : in;
             }
             if (keep) {
@@ -688,7 +693,7 @@ __device__ __forceinline__ bool node4_step(const Bvh4Node* __restrict__ nodes, i
 // box meets it only at the far root and only when heading inward, and one
 // leaving a torus loses only its near-zero root; FP32 rounding of the
 // origin must not invent those self-hits (the reference works in FP64).
-template <bool ANY, bool FULL>
+template <bool ANY, bool FULL, bool NT = false>
 __device__ __forceinline__ bool prim_test(const DeviceScene& S, uint32_t ref, float3 o, float3 d, float tmin,
                                           float& t, float& bu, float& bv, uint32_t& aux, uint2 skip)
 {
@@ -740,6 +745,8 @@ __device__ __forceinline__ bool prim_test(const DeviceScene& S, uint32_t ref, fl
     if (!FULL)
         return false;   // lean variant: the scene has no tori and no CSG
     if (kind == PK_TORUS) {
+        if (NT)
+            return false;   // the torus-free variant never gets here (its caller defers tori)
         if (!torus_may_hit(S.tori32 + 4 * (size_t)idx, o, d, t))
             return false;
         double r[4];
@@ -758,7 +765,7 @@ __device__ __forceinline__ bool prim_test(const DeviceScene& S, uint32_t ref, fl
         return hit;
     }
     if (kind == PK_CSG)
-        return csg_closest(S, idx, o, d, tmin, t, aux, skip, ref, ANY);
+        return csg_closest<NT>(S, idx, o, d, tmin, t, aux, skip, ref, ANY);
     return false;
 }
 
@@ -769,13 +776,19 @@ __device__ __forceinline__ bool prim_test(const DeviceScene& S, uint32_t ref, fl
 // (1: the compiler's choice; 8: at most 64 registers a thread, more warps
 // to hide the node and triangle load latency at the price of spills) --
 // one of the autotuner's choices for the lean variant.
-template <bool ANY, bool FULL, int MINB>
+// NT: the torus-free full variant (TorusDefer::ovf set): every torus test
+// is deferred, and a ray whose pair does not fit the list is handed to a
+// second launch of the ordinary full variant (listed in td.ovf, its
+// blocked byte 2 meanwhile) instead of being solved here.
+// index (optional): the queue slots to trace (slot i traces ray index[i]).
+template <bool ANY, bool FULL, int MINB, bool NT = false>
 __global__ void __launch_bounds__(128, MINB) k_trace(DeviceScene S, const QRay* __restrict__ q,
                                                const int* __restrict__ q_count, int* __restrict__ work,
                                                QHit* __restrict__ hits, uint8_t* __restrict__ blocked,
                                                int stack_depth, uint32_t* err, unsigned long long* stats,
                                                unsigned long long* wcount, int cap,
-                                               const uint2* __restrict__ skips, TorusDefer td)
+                                               const uint2* __restrict__ skips, TorusDefer td,
+                                               const int* __restrict__ index)
 {
     namespace cg = cooperative_groups;
     extern __shared__ int smem[];
@@ -794,6 +807,8 @@ __global__ void __launch_bounds__(128, MINB) k_trace(DeviceScene S, const QRay* 
         int i = base + lane;
         if (i >= n)
             continue;
+        if (index)
+            i = index[i];
         QRay r = q[i];
         if (counting) c_rays++;
         float3 o = xyz(r.org), d = xyz(r.dir);
@@ -803,6 +818,7 @@ __global__ void __launch_bounds__(128, MINB) k_trace(DeviceScene S, const QRay* 
         uint32_t best = NO_PRIM, baux = 0;
         float bu = 0.f, bv = 0.f;
         bool done = false;
+        bool ovf = false;   // NT: a torus pair did not fit the list
         const uint2 skip = skips ? skips[i] : make_uint2(NO_PRIM, 0u);
         if (FULL && !ANY && td.key)
             td.key[i] = ~0ull;   // no deferred torus root yet
@@ -842,24 +858,30 @@ __global__ void __launch_bounds__(128, MINB) k_trace(DeviceScene S, const QRay* 
                 for (uint32_t k = 0; k < count; k++) {
                     uint32_t ref = __ldg(S.prim_refs + first + k);
                     if (counting) { c_prims++; c_tris += (ref >> PRIM_KIND_SHIFT) == PK_TRIANGLE; }
-                    if (FULL && td.cand && (ref >> PRIM_KIND_SHIFT) == PK_TORUS) {
+                    if (FULL && (NT || td.cand) && (ref >> PRIM_KIND_SHIFT) == PK_TORUS) {
                         const uint32_t idx = ref & PRIM_INDEX_MASK;
                         if (!torus_may_hit(S.tori32 + 4 * (size_t)idx, o, d, t))
                             continue;
-                        // one slot per lane that got here, one atomic per group
-                        cg::coalesced_group g = cg::coalesced_threads();
-                        int slot = 0;
-                        if (g.thread_rank() == 0)
-                            slot = atomicAdd(td.count, (int)g.size());
-                        slot = g.shfl(slot, 0) + (int)g.thread_rank();
-                        if (slot < td.cap) {
-                            td.cand[slot] = make_uint2((uint32_t)i | (ref == skip.x ? 0x80000000u : 0u), idx);
-                            continue;
+                        if (td.cand) {
+                            // one slot per lane that got here, one atomic per group
+                            cg::coalesced_group g = cg::coalesced_threads();
+                            int slot = 0;
+                            if (g.thread_rank() == 0)
+                                slot = atomicAdd(td.count, (int)g.size());
+                            slot = g.shfl(slot, 0) + (int)g.thread_rank();
+                            if (slot < td.cap) {
+                                td.cand[slot] = make_uint2((uint32_t)i | (ref == skip.x ? 0x80000000u : 0u), idx);
+                                continue;
+                            }
+                        }
+                        if (NT) {   // the list is full: the second launch traces this ray
+                            ovf = done = true;
+                            break;
                         }
                         // the list is full: solved here
                     }
                     uint32_t aux = 0;
-                    if (prim_test<ANY, FULL>(S, ref, o, d, tmin, t, bu, bv, aux, skip)) {
+                    if (prim_test<ANY, FULL, NT>(S, ref, o, d, tmin, t, bu, bv, aux, skip)) {
                         best = ref;
                         baux = aux;
                         if (ANY) { done = true; break; }
@@ -870,7 +892,15 @@ __global__ void __launch_bounds__(128, MINB) k_trace(DeviceScene S, const QRay* 
                 node = sp > 0 ? smem[(--sp) * blockDim.x + threadIdx.x] : BVH_EMPTY;
             }
         }
-        if (ANY) {
+        if (NT && ovf) {
+            const int k = atomicAdd(td.ovf_count, 1);
+            if (k < td.ovf_cap)
+                td.ovf[k] = i;
+            else
+                set_error(err, DE_QUEUE_OVERFLOW);
+            if (ANY)
+                blocked[i] = 2;   // k_torus_solve leaves it alone
+        } else if (ANY) {
             blocked[i] = done ? 1 : 0;
             nblocked += done ? 1 : 0;
         } else {
@@ -3112,30 +3142,37 @@ cudaError_t launch_trace(const DeviceScene& S, bool any_hit, const QRay* q, cons
     // them run the lean one (about half the registers)
     const bool full = S.has_full_prims != 0;
     TorusDefer td{};
-    if (full && defer && defer->cand && defer->count && (any_hit || defer->key)) {
+    if (full && defer && defer->count && ((defer->cand && (any_hit || defer->key)) || defer->ovf)) {
         td = *defer;
-        cudaError_t e = cudaMemsetAsync(td.count, 0, sizeof(int), st);
+        if (td.cand && !any_hit && !td.key)
+            td.cand = nullptr;
+        // count, ovf_count and ovf_work: three consecutive ints
+        cudaError_t e = cudaMemsetAsync(td.count, 0, sizeof(int) * 3, st);
         if (e != cudaSuccess)
             return e;
     }
-    if (any_hit && full)
-        k_trace<true, true, 1><<<grid, block, smem, st>>>(S, q, q_count, work, hits, blocked, stack_depth, err,
-                                                          stats, wcount, cap, skips, td);
+    const bool nt = td.ovf != nullptr;   // the torus-free variant and its second launch
+    const TorusDefer none{};
+    const int* no_index = nullptr;
+#define POVGPU_TRACE(A, F, M, N, TD, QC, W, CAP, IDX)                                                             \
+    k_trace<A, F, M, N><<<grid, block, smem, st>>>(S, q, QC, W, hits, blocked, stack_depth, err, stats, wcount, \
+                                                   CAP, skips, TD, IDX)
+    if (any_hit && full && nt)
+        POVGPU_TRACE(true, true, 1, true, td, q_count, work, cap, no_index);
+    else if (any_hit && full)
+        POVGPU_TRACE(true, true, 1, false, td, q_count, work, cap, no_index);
     else if (any_hit && occ)
-        k_trace<true, false, 8><<<grid, block, smem, st>>>(S, q, q_count, work, hits, blocked, stack_depth, err,
-                                                           stats, wcount, cap, skips, td);
+        POVGPU_TRACE(true, false, 8, false, td, q_count, work, cap, no_index);
     else if (any_hit)
-        k_trace<true, false, 1><<<grid, block, smem, st>>>(S, q, q_count, work, hits, blocked, stack_depth, err,
-                                                           stats, wcount, cap, skips, td);
+        POVGPU_TRACE(true, false, 1, false, td, q_count, work, cap, no_index);
+    else if (full && nt)
+        POVGPU_TRACE(false, true, 1, true, td, q_count, work, cap, no_index);
     else if (full)
-        k_trace<false, true, 1><<<grid, block, smem, st>>>(S, q, q_count, work, hits, blocked, stack_depth, err,
-                                                           stats, wcount, cap, skips, td);
+        POVGPU_TRACE(false, true, 1, false, td, q_count, work, cap, no_index);
     else if (occ)
-        k_trace<false, false, 8><<<grid, block, smem, st>>>(S, q, q_count, work, hits, blocked, stack_depth, err,
-                                                            stats, wcount, cap, skips, td);
+        POVGPU_TRACE(false, false, 8, false, td, q_count, work, cap, no_index);
     else
-        k_trace<false, false, 1><<<grid, block, smem, st>>>(S, q, q_count, work, hits, blocked, stack_depth, err,
-                                                            stats, wcount, cap, skips, td);
+        POVGPU_TRACE(false, false, 1, false, td, q_count, work, cap, no_index);
     if (td.cand) {
         const int g = grid;   // the traversal's persistent grid: SMs x blocks per SM
         if (any_hit) {
@@ -3145,6 +3182,13 @@ cudaError_t launch_trace(const DeviceScene& S, bool any_hit, const QRay* q, cons
             k_torus_merge<<<g, 256, 0, st>>>(q_count, cap, td, hits);
         }
     }
+    if (nt) {   // the rays whose torus pairs did not fit: the ordinary full variant
+        if (any_hit)
+            POVGPU_TRACE(true, true, 1, false, none, td.ovf_count, td.ovf_work, td.ovf_cap, td.ovf);
+        else
+            POVGPU_TRACE(false, true, 1, false, none, td.ovf_count, td.ovf_work, td.ovf_cap, td.ovf);
+    }
+#undef POVGPU_TRACE
     return cudaGetLastError();
 }
 

@@ -539,8 +539,8 @@ class Scene:
                 c["sdl_c1"], c["sdl_c2"] = c["c1"], c["c2"]
                 c["c1"] = tuple(a + b for a, b in zip(c["c1"], tv))
                 c["c2"] = tuple(a + b for a, b in zip(c["c2"], tv))
-            else:
-                raise ValueError("CSG children: spheres and boxes")
+            elif not (c["type"] == abi.POV_OBJ_TORUS and tv == (0.0, 0.0, 0.0)):
+                raise ValueError("CSG children: spheres and boxes (tori in an untranslated CSG)")
             moved.append(c)
         if kind == "difference":
             for c in moved[1:]:
@@ -1043,6 +1043,28 @@ def csg_torus_grid(width=1920, height=1080, n=16, seed=3, antialias=(0.1, 3)):
                     node = Scene.n_torus(0.6, 0.15, rot[k], c, m)
                 s.add(node)
                 k += 1
+    return s
+
+
+def torus_tunnel(width=160, height=120, n_rings=48, csg_child=False):
+    """A tunnel of `n_rings` tori (major 3, minor 0.3, rings facing the
+    camera, every 2 units along +z from z=2) ending at a wall (plane z=100),
+    seen from (0,0,-5) looking down the axis, one light beside the camera:
+    every camera ray passes a few dozen tori, so the traversal's list of
+    deferred torus tests fills up and the rays beyond it take the second,
+    ordinary traversal.  With `csg_child` the last ring is a torus merged
+    with a sphere (a CSG with a torus child: no torus-free variant).  Reflection 0.3 on the rings, max_trace_level 3."""
+    s = Scene("torus_tunnel", width, height, (0.0, 0.0, -5.0), (0.0, 0.0, 100.0), 60.0, max_trace_level=3)
+    s.point_light((1.0, 1.5, -4.0))
+    wall = s.material(Material((0.8, 0.8, 0.7)))
+    s.plane((0.0, 0.0, -1.0), -100.0, wall)
+    rng = np.random.Generator(np.random.PCG64(9))
+    for k in range(n_rings):
+        m = s.material(Material(tuple(rng.uniform(0.2, 1.0, 3)), phong=0.4, reflection=0.3))
+        node = Scene.n_torus(3.0, 0.3, (90.0, 0.0, 0.0), (0.0, 0.0, 2.0 + 2.0 * k), m)
+        if csg_child and k == n_rings - 1:
+            node = Scene.n_csg("merge", [node, Scene.n_sphere((0.0, 0.0, 2.0 + 2.0 * k), 0.5)], mat=m)
+        s.add(node)
     return s
 
 

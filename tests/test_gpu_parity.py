@@ -145,6 +145,22 @@ def test_csg_torus_grid_matches_oracle_with_aa():
         assert abs(st[k] - rst[k]) <= 2e-3 * rst[k], (k, st, rst)
 
 
+@pytest.mark.parametrize("csg_child", [False, True], ids=["torus_free", "csg_torus"])
+def test_torus_tunnel_matches_oracle(csg_child):
+    """48 rings down the view axis: every camera ray meets a few dozen tori,
+    far more than the traversal's list of deferred torus tests holds (four
+    per ray), so most rays are traced again by the second launch (torus-free
+    variant), or solve the rest in line (a CSG with a torus child).  Pixels
+    and counters against the oracle."""
+    s = scenes.torus_tunnel(96, 72, csg_child=csg_child)
+    img, st = GpuScene(s).render()
+    ref, rst = Oracle(s).render(threads=0)
+    c = compare_pixels(img, ref)
+    assert c["within_1lsb"] >= PIX_FRAC, c
+    for k in ("number_of_rays", "reflected_rays", "shadow_ray_tests", "shadow_rays_succeeded"):
+        assert abs(st[k] - rst[k]) <= max(2, 5e-4 * rst[k]), (k, st, rst)
+
+
 @pytest.mark.parametrize("variant", [
     dict(),                                          # 4x4, Adaptive_Level 100: every grid point
     dict(area=(5, 5), adaptive=1, orient=True),      # orient implies circular; adaptive refinement
