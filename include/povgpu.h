@@ -671,9 +671,32 @@ typedef struct PovGpuLaunchConfig {
                                       traversal of scenes without tori and CSG); 0: default */
     int32_t shade_blocks_per_sm;   /* grid cap of the queue kernels, blocks per SM: 1..64
                                       (default 16)                                           */
-    int32_t reserved[4];
+    int32_t bounding_tree;         /* the tree the traversal walks: 0 = the library's
+                                      binned-SAH four-wide tree (default); 1 = the
+                                      reference's bounding tree (Build_Bounding_Slabs /
+                                      Build_BBox_Tree over the top-level objects,
+                                      boundingbox.cpp:262-430,834-928, each mesh2's own
+                                      tree, mesh.cpp:1376-1450, grafted under its leaf),
+                                      flattened into four-wide nodes, built on first use */
+    int32_t reserved[3];
 } PovGpuLaunchConfig;
 int pov_gpu_set_launch_config(PovGpuScene* scene, const PovGpuLaunchConfig* config);
+
+/*
+ * The traversal tree in use (no reference counterpart): its four-wide
+ * nodes and levels, and -- once the reference's tree has been built -- the
+ * composite nodes of the reference's top tree and of its mesh trees
+ * (BBOX_TREE nodes with entries), -1 before.
+ */
+typedef struct PovGpuTreeInfo {
+    int32_t bounding_tree;
+    int32_t nodes;
+    int32_t depth;
+    int32_t ref_top_nodes;
+    int32_t ref_mesh_nodes;
+    int32_t reserved[3];
+} PovGpuTreeInfo;
+int pov_gpu_get_tree_info(PovGpuScene* scene, PovGpuTreeInfo* info);
 
 /* Human-readable text of a status code. */
 const char* pov_gpu_error_string(int status);

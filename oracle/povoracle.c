@@ -3811,6 +3811,21 @@ int pov_oracle_create(const PovGpuSceneDesc* desc, PovOracle** out, int32_t* bad
 
 static void free_tree(Tree* t) { free(t->nodes); free(t->kids); }
 
+/* Composite nodes (nodes with entries) of the bounding trees the oracle
+ * built: the top tree (none below Bounding_Threshold) and all mesh trees. */
+void pov_oracle_tree_info(const PovOracle* S, int32_t* top_nodes, int32_t* mesh_nodes)
+{
+    int32_t t = 0, m = 0;
+    if (!S->top_linear && S->top.root >= 0)
+        for (int32_t i = 0; i < S->top.num_nodes; i++)
+            t += S->top.nodes[i].entries > 0;
+    for (int32_t k = 0; k < S->nmeshes; k++)
+        for (int32_t i = 0; i < S->meshes[k].tree.num_nodes; i++)
+            m += S->meshes[k].tree.nodes[i].entries > 0;
+    *top_nodes = t;
+    *mesh_nodes = m;
+}
+
 void pov_oracle_destroy(PovOracle* S)
 {
     if (!S) return;

@@ -21,6 +21,7 @@ typedef struct PovOracle PovOracle;
 
 int  pov_oracle_create(const PovGpuSceneDesc* desc, PovOracle** out, int32_t* bad_index);
 void pov_oracle_destroy(PovOracle* o);
+void pov_oracle_tree_info(const PovOracle* o, int32_t* top_nodes, int32_t* mesh_nodes);
 
 /* Trace::FindIntersection for each ray (origins/directions: 3 doubles each). */
 int  pov_oracle_trace_rays(PovOracle* o, const double* origins, const double* directions,

@@ -54,6 +54,8 @@ def lib():
         L.pov_oracle_render_converged.restype = C.c_int
         L.pov_oracle_set_pretrace_jitter.argtypes = [C.c_void_p, C.c_void_p, C.c_int32]
         L.pov_oracle_set_pretrace_jitter.restype = C.c_int
+        L.pov_oracle_tree_info.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+        L.pov_oracle_tree_info.restype = None
         _lib = L
     return _lib
 
@@ -132,6 +134,13 @@ class Oracle:
         if st != 0:
             raise abi.PovGpuError(st, "pov_oracle_render_converged")
         return out, stats.as_dict()
+
+    def tree_info(self):
+        """Composite nodes of the oracle's bounding trees: (top tree, all mesh
+        trees) -- the reference's Build_BBox_Tree restated."""
+        t, m = C.c_int32(0), C.c_int32(0)
+        lib().pov_oracle_tree_info(self.h, C.byref(t), C.byref(m))
+        return t.value, m.value
 
     def count_work(self, origins, directions):
         o = np.ascontiguousarray(origins, dtype=np.float64)

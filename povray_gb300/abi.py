@@ -229,11 +229,17 @@ class PovGpuTimings(C.Structure):
 
 class PovGpuLaunchConfig(C.Structure):
     _fields_ = [("trace_blocks_per_sm", C.c_int32), ("trace_block", C.c_int32), ("trace_occupancy", C.c_int32),
-                ("shade_blocks_per_sm", C.c_int32), ("reserved", C.c_int32 * 4)]
+                ("shade_blocks_per_sm", C.c_int32), ("bounding_tree", C.c_int32), ("reserved", C.c_int32 * 3)]
+
+
+class PovGpuTreeInfo(C.Structure):
+    _fields_ = [("bounding_tree", C.c_int32), ("nodes", C.c_int32), ("depth", C.c_int32),
+                ("ref_top_nodes", C.c_int32), ("ref_mesh_nodes", C.c_int32), ("reserved", C.c_int32 * 3)]
 
 
 STRUCTS = {
-    "PovGpuLaunchConfig": PovGpuLaunchConfig, "PovGpuNormal": PovGpuNormal, "PovGpuInterior": PovGpuInterior,
+    "PovGpuLaunchConfig": PovGpuLaunchConfig, "PovGpuTreeInfo": PovGpuTreeInfo, "PovGpuNormal": PovGpuNormal,
+    "PovGpuInterior": PovGpuInterior,
     "PovGpuObject": PovGpuObject, "PovGpuMaterial": PovGpuMaterial,
     "PovGpuLight": PovGpuLight, "PovGpuMesh": PovGpuMesh, "PovGpuCamera": PovGpuCamera,
     "PovGpuRadiosity": PovGpuRadiosity, "PovGpuSceneDesc": PovGpuSceneDesc,
@@ -248,7 +254,8 @@ EXPORTS = ["pov_gpu_scene_create", "pov_gpu_trace_blocks", "pov_gpu_trace_rays",
            "pov_gpu_scene_set_stream", "pov_gpu_set_profiling", "pov_gpu_get_timings",
            "pov_gpu_trace_rays_static", "pov_gpu_radiosity_pretrace", "pov_gpu_set_pretrace_jitter",
            "pov_gpu_set_neural_cache", "pov_gpu_nic_eval", "pov_gpu_set_camera", "pov_gpu_encode_u8",
-           "pov_gpu_set_timeout", "pov_gpu_cache_save", "pov_gpu_cache_load", "pov_gpu_set_launch_config"]
+           "pov_gpu_set_timeout", "pov_gpu_cache_save", "pov_gpu_cache_load", "pov_gpu_set_launch_config",
+           "pov_gpu_get_tree_info"]
 
 
 class PovGpuError(RuntimeError):
@@ -304,6 +311,8 @@ def load_library(path=None):
     lib.pov_gpu_set_camera.restype = C.c_int
     lib.pov_gpu_set_launch_config.argtypes = [C.c_void_p, C.POINTER(PovGpuLaunchConfig)]
     lib.pov_gpu_set_launch_config.restype = C.c_int
+    lib.pov_gpu_get_tree_info.argtypes = [C.c_void_p, C.POINTER(PovGpuTreeInfo)]
+    lib.pov_gpu_get_tree_info.restype = C.c_int
     lib.pov_gpu_cache_save.argtypes = [C.c_void_p, C.c_char_p]
     lib.pov_gpu_cache_save.restype = C.c_int
     lib.pov_gpu_cache_load.argtypes = [C.c_void_p, C.c_char_p, C.POINTER(C.c_int32)]

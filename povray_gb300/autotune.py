@@ -12,6 +12,11 @@ per workload and image size in launch_table.json beside this file.
 bench.py and callers apply the recorded entry with
 GpuScene.set_launch_config(**entry["config"]).
 
+The tree itself is one of the choices: the library's binned-SAH tree or
+the reference's own bounding tree (objects as single leaves with their
+Compute_BBox boxes, each mesh2's tree under its leaf), which suits scenes of
+few expensive objects (CSG, tori) better than leaves of up to eight.
+
 The traversal stack depth is not a tuning knob: it is set from the depth of
 the scene's tree so that no push can overflow (a smaller one would not be
 correct, a larger one only costs shared memory).
@@ -26,8 +31,10 @@ import statistics
 HERE = os.path.dirname(os.path.abspath(__file__))
 TABLE = os.path.join(HERE, "launch_table.json")
 
-DEFAULT = {"trace_blocks_per_sm": 8, "trace_block": 128, "trace_occupancy": 0, "shade_blocks_per_sm": 16}
+DEFAULT = {"trace_blocks_per_sm": 8, "trace_block": 128, "trace_occupancy": 0, "shade_blocks_per_sm": 16,
+           "bounding_tree": 0}
 SPACE = {
+    "bounding_tree": [0, 1],
     "trace_blocks_per_sm": [4, 6, 8, 12, 16],
     "trace_block": [64, 128],
     "trace_occupancy": [0, 1],

@@ -17,7 +17,7 @@ OBJ_DIR = os.path.join(HERE, "lib", "obj")
 LIB = os.path.join(OUT_DIR, "libpovgpu.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["povgpu_host.cpp", "povgpu_kernels.cu", "povgpu_radiosity.cu", "povgpu_nic.cu"]
+SOURCES = ["povgpu_host.cpp", "povgpu_reftree.cpp", "povgpu_kernels.cu", "povgpu_radiosity.cu", "povgpu_nic.cu"]
 
 
 def nvcc():

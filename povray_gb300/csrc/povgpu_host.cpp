@@ -7,6 +7,7 @@
 // POV_GPU_E_UNSUPPORTED: there is no CPU fallback.
 #include "povgpu.h"
 #include "povgpu_internal.h"
+#include "povgpu_reftree.h"
 #include "povgpu_kernels.h"
 #include "povgpu_radiosity.h"
 #include "povgpu_nic.h"
@@ -571,7 +572,7 @@ struct PovGpuScene {
         materials, lights, medias, patterns, tnormals, noise_hash, noise_rtab, noise_perm, noise_grad, noise_waves;
     DevBuf encode_buf;     // staging of pov_gpu_encode_u8 for host outputs
     DevBuf cam_tab;        // per-call column / row offsets of the camera rays
-    PovGpuLaunchConfig lc{8, 128, 0, 16, {0, 0, 0, 0}};   // launch shapes (pov_gpu_set_launch_config)
+    PovGpuLaunchConfig lc{8, 128, 0, 16, 0, {0, 0, 0}};   // launch shapes (pov_gpu_set_launch_config)
     // the device work of a plain frame (no radiosity, media or AA) as a
     // captured CUDA graph, replayed while the frame's shape stays the same
     struct GraphKey {
@@ -589,6 +590,15 @@ struct PovGpuScene {
     bool   transparent = false;   // some surface filters or transmits: rays carry interior lists
     bool   top_tori = false;      // tori outside CSG: traversal defers their FP64 tests
     bool   csg_torus = false;     // a CSG has a torus child: no torus-free traversal variant
+    // bounding trees: the library's binned-SAH tree (nodes, refs) and, on
+    // request, the reference's (ref_nodes, ref_refs, built from ref_input)
+    int32_t sah_root = BVH_EMPTY;
+    int     sah_stack_depth = 8, sah_depth = 0, sah_nodes = 0;
+    int     tree_mode = 0;        // 0 SAH, 1 the reference's tree
+    bool    ref_built = false;
+    RefTreeInput  ref_input;
+    RefTreeOutput ref_output;
+    DevBuf ref_nodes, ref_refs;
     DevBuf obj_interior, interiors;   // per object its interior id; per interior its float4 pair
     int    media_ni = 0;   // interval slots per media segment (0: no media containers)
     int    media_smax = 0;  // sample slots per interval (ends + sample-tree nodes)
@@ -654,7 +664,7 @@ struct PovGpuScene {
                          &hits, &out, &counters, &stats, &err, &rays_in, &t64, &corners, &aa_grid, &aa_mask,
                          &aa_subdiv, &aa_xy, &cellsA, &cellsB, &spos, &sslot, &wcount, &pos_count, &medias,
                          &encode_buf, &cam_tab, &patterns, &tnormals, &noise_hash, &noise_rtab, &noise_perm, &noise_grad,
-                         &noise_waves, &obj_interior, &interiors};
+                         &noise_waves, &obj_interior, &interiors, &ref_nodes, &ref_refs};
         for (DevBuf* b : all)
             b->release();
         top.release();
@@ -1064,6 +1074,10 @@ struct Builder {
     std::vector<DevTorus> tori;
     std::vector<DevCsg> csgs;
     std::vector<DevCsgChild> csg_children;
+    // every primitive pushed, with the top-level object it belongs to (the
+    // input of the reference's bounding tree)
+    int32_t cur_obj = -1;
+    std::vector<std::pair<int32_t, uint32_t>> pushed;
 
     int add_sphere(const PovGpuObject& o, int id, AABB* box)
     {
@@ -1129,8 +1143,94 @@ struct Builder {
             it.c[k] = 0.5f * (box.lo[k] + box.hi[k]);
         it.ref = (kind << PRIM_KIND_SHIFT) | idx;
         bvh.items.push_back(it);
+        pushed.push_back({cur_obj, it.ref});
     }
 };
+
+// Compute_BBox of a top-level object as the reference stores it (float
+// lower-left and size): Sphere (sphere.cpp:646-658), Box (box.cpp:947-957),
+// Torus with Recompute_BBox of its local box (torus.cpp:849-859,
+// boundingbox.cpp:168), Mesh over its vertices (mesh.cpp:790-808), CSG as
+// the union of its children or, for an intersection, the overlap of the
+// children that are not inverted (csg.cpp).
+RefBox ref_object_box(const PovGpuSceneDesc* d, int i)
+{
+    const PovGpuObject& o = d->objects[i];
+    const double H = 2.0e10;   // BOUND_HUGE
+    double mn[3] = {H, H, H}, mx[3] = {-H, -H, -H};
+    RefBox b{};
+    auto from = [&](const double* lo, const double* hi) {
+        for (int k = 0; k < 3; k++) {
+            b.ll[k] = (float)lo[k];
+            b.sz[k] = (float)(hi[k] - lo[k]);
+        }
+    };
+    switch (o.type) {
+    case POV_OBJ_SPHERE:
+        for (int k = 0; k < 3; k++) {
+            b.ll[k] = (float)(o.p[k] - o.p[3]);
+            b.sz[k] = (float)(2.0 * o.p[3]);
+        }
+        return b;
+    case POV_OBJ_BOX:
+        from(o.p, o.p + 3);
+        return b;
+    case POV_OBJ_TORUS: {
+        const double r1 = o.p[1], r2 = o.p[0] + o.p[1];
+        const float ll[3] = {(float)-r2, (float)-r1, (float)-r2};
+        const float sz[3] = {(float)(2.0 * r2), (float)(2.0 * r1), (float)(2.0 * r2)};
+        for (int c = 1; c <= 8; c++) {
+            V3d p = {ll[0] + ((c & 1) ? (double)sz[0] : 0.0), ll[1] + ((c & 2) ? (double)sz[1] : 0.0),
+                     ll[2] + ((c & 4) ? (double)sz[2] : 0.0)};
+            V3d w = mtrans_point(o.trans, p);
+            const double v[3] = {w.x, w.y, w.z};
+            for (int k = 0; k < 3; k++) {
+                mn[k] = std::min(mn[k], v[k]);
+                mx[k] = std::max(mx[k], v[k]);
+            }
+        }
+        from(mn, mx);
+        return b;
+    }
+    case POV_OBJ_MESH: {
+        const PovGpuMesh& m = d->meshes[o.mesh];
+        for (int t = 0; t < 3 * m.num_triangles; t++) {
+            const float* v = m.vertices + 3 * m.face_indices[t];
+            for (int k = 0; k < 3; k++) {
+                mn[k] = std::min(mn[k], (double)v[k]);
+                mx[k] = std::max(mx[k], (double)v[k]);
+            }
+        }
+        from(mn, mx);
+        return b;
+    }
+    case POV_OBJ_UNION:
+    case POV_OBJ_MERGE:
+    case POV_OBJ_INTERSECTION: {
+        const bool isect = o.type == POV_OBJ_INTERSECTION;
+        if (isect)
+            for (int k = 0; k < 3; k++) {
+                mn[k] = -H;
+                mx[k] = H;
+            }
+        for (int c = 0; c < o.num_children; c++) {
+            const PovGpuObject& ch = d->objects[o.first_child + c];
+            if (isect && (ch.flags & POV_FLAG_INVERTED))
+                continue;
+            const RefBox cb = ref_object_box(d, o.first_child + c);
+            for (int k = 0; k < 3; k++) {
+                const double lo = cb.ll[k], hi = (double)cb.ll[k] + cb.sz[k];
+                mn[k] = isect ? std::max(mn[k], lo) : std::min(mn[k], lo);
+                mx[k] = isect ? std::min(mx[k], hi) : std::max(mx[k], hi);
+            }
+        }
+        from(mn, mx);
+        return b;
+    }
+    default:
+        return b;
+    }
+}
 
 void add_mesh(Builder& B, const PovGpuSceneDesc* d, const PovGpuObject& o, int id, int nb)
 {
@@ -1319,6 +1419,41 @@ struct NoiseTables {
 
 int rad_reset(PovGpuScene* sc);
 
+// Switches the traversal between the library's binned-SAH tree (0) and the
+// reference's bounding tree (1), built and uploaded on first use.
+int apply_tree(PovGpuScene* sc, int mode)
+{
+    DeviceScene& S = sc->S;
+    if (mode == 1) {
+        if (!sc->ref_built) {
+            build_reference_tree(sc->ref_input, sc->ref_output);
+            std::vector<Bvh4Node> nodes = sc->ref_output.nodes;
+            std::vector<uint32_t> refs = sc->ref_output.refs;
+            if (nodes.empty())
+                nodes.push_back(Bvh4Node{});
+            if (refs.empty())
+                refs.push_back(0u);
+            CK(upload(sc->ref_nodes, nodes));
+            CK(upload(sc->ref_refs, refs));
+            sc->ref_built = true;
+        }
+        const int sd = std::max(8, 3 * sc->ref_output.depth + 2);
+        if (sd > 160)
+            return POV_GPU_E_UNSUPPORTED;
+        S.nodes = sc->ref_nodes.as<Bvh4Node>();
+        S.prim_refs = sc->ref_refs.as<uint32_t>();
+        S.root = sc->ref_output.root;
+        sc->stack_depth = sd;
+    } else {
+        S.nodes = sc->nodes.as<Bvh4Node>();
+        S.prim_refs = sc->refs.as<uint32_t>();
+        S.root = sc->sah_root;
+        sc->stack_depth = sc->sah_stack_depth;
+    }
+    sc->tree_mode = mode;
+    return POV_GPU_OK;
+}
+
 int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
 {
     Builder B;
@@ -1441,6 +1576,7 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
         const PovGpuObject& o = d->objects[i];
         if (o.parent >= 0)
             continue;   // CSG children are added with their parent
+        B.cur_obj = i;
         AABB box;
         switch (o.type) {
         case POV_OBJ_SPHERE: B.push_prim(PK_SPHERE, B.add_sphere(o, i, &box), box); break;
@@ -1518,6 +1654,10 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
     sc->stack_depth = std::max(8, 3 * wide.max_depth + 2);
     if (sc->stack_depth > 160)
         return POV_GPU_E_UNSUPPORTED;
+    sc->sah_root = root;
+    sc->sah_stack_depth = sc->stack_depth;
+    sc->sah_depth = wide.max_depth;
+    sc->sah_nodes = (int)wide.out.size();
 
     // reorder triangle records into leaf order (prim refs then index the
     // leaf-order slot directly, so a leaf's triangles are contiguous)
@@ -1542,6 +1682,74 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
             tri_global.push_back((int32_t)g);
             r = (PK_TRIANGLE << PRIM_KIND_SHIFT) | slot;
         }
+    }
+
+    // the input of the reference's bounding tree (built when a launch
+    // configuration asks for it): the finite top-level objects in scene
+    // order with their Compute_BBox boxes and primitives, each mesh2's
+    // triangles with their boxes (min/max of the vertices)
+    {
+        std::vector<uint32_t> tri_slot(B.tri_v0.size(), 0);
+        for (size_t sl = 0; sl < tri_global.size(); sl++)
+            tri_slot[(size_t)tri_global[sl]] = (uint32_t)sl;
+        RefTreeInput& R = sc->ref_input;
+        R = RefTreeInput{};
+        std::vector<int> obj_slot((size_t)std::max(d->num_objects, 1), -1);
+        for (int i = 0; i < d->num_objects; i++) {
+            const PovGpuObject& o = d->objects[i];
+            if (o.parent < 0 && o.type == POV_OBJ_PLANE)
+                R.infinite++;
+            if (o.parent >= 0 || o.type == POV_OBJ_PLANE)
+                continue;
+            RefObject ro;
+            ro.box = ref_object_box(d, i);
+            if (o.type == POV_OBJ_MESH) {
+                ro.mesh = (int32_t)R.meshes.size();
+                R.meshes.emplace_back();
+            }
+            obj_slot[i] = (int)R.objects.size();
+            R.objects.push_back(ro);
+        }
+        // the pushes come in object order: gather each object's primitives
+        for (size_t k = 0; k < B.pushed.size();) {
+            const int32_t obj = B.pushed[k].first;
+            size_t e = k;
+            while (e < B.pushed.size() && B.pushed[e].first == obj)
+                e++;
+            if (obj >= 0 && obj_slot[obj] >= 0) {
+                RefObject& ro = R.objects[obj_slot[obj]];
+                if (ro.mesh >= 0) {
+                    const PovGpuMesh& m = d->meshes[d->objects[obj].mesh];
+                    for (size_t j = k; j < e; j++) {
+                        const uint32_t g = B.pushed[j].second & PRIM_INDEX_MASK;
+                        const int t = B.tri_local[g];   // the triangle's place in the mesh
+                        double mn[3] = {2.0e10, 2.0e10, 2.0e10}, mx[3] = {-2.0e10, -2.0e10, -2.0e10};
+                        for (int c = 0; c < 3; c++) {
+                            const float* v = m.vertices + 3 * m.face_indices[3 * t + c];
+                            for (int a = 0; a < 3; a++) {
+                                mn[a] = std::min(mn[a], (double)v[a]);
+                                mx[a] = std::max(mx[a], (double)v[a]);
+                            }
+                        }
+                        RefTriangle rt;
+                        for (int a = 0; a < 3; a++) {
+                            rt.box.ll[a] = (float)mn[a];
+                            rt.box.sz[a] = (float)(mx[a] - mn[a]);
+                        }
+                        rt.ref = (PK_TRIANGLE << PRIM_KIND_SHIFT) | tri_slot[g];
+                        R.meshes[ro.mesh].push_back(rt);
+                    }
+                } else {
+                    ro.first = (uint32_t)R.refs.size();
+                    ro.count = (uint32_t)(e - k);
+                    for (size_t j = k; j < e; j++)
+                        R.refs.push_back(B.pushed[j].second);
+                }
+            }
+            k = e;
+        }
+        sc->ref_built = false;
+        sc->tree_mode = 0;
     }
 
     std::vector<DevMaterial> mats((size_t)d->num_materials);
@@ -2812,10 +3020,36 @@ int pov_gpu_set_launch_config(PovGpuScene* sc, const PovGpuLaunchConfig* cfg)
         c.shade_blocks_per_sm = 16;
     if (c.trace_blocks_per_sm < 1 || c.trace_blocks_per_sm > 32 || (c.trace_block != 64 && c.trace_block != 128) ||
         (c.trace_occupancy != 0 && c.trace_occupancy != 1) || c.shade_blocks_per_sm < 1 ||
-        c.shade_blocks_per_sm > 64)
+        c.shade_blocks_per_sm > 64 || (c.bounding_tree != 0 && c.bounding_tree != 1))
         return POV_GPU_E_INVALID;
     std::lock_guard<std::mutex> g(sc->lock);
+    if (c.bounding_tree != sc->tree_mode) {
+        CK(cudaSetDevice(sc->device));
+        CK(cudaStreamSynchronize(sc->active()));   // no traversal may run on the old tree
+        const int rc = apply_tree(sc, c.bounding_tree);
+        if (rc != POV_GPU_OK)
+            return rc;
+    }
     sc->lc = c;
+    return POV_GPU_OK;
+}
+
+int pov_gpu_get_tree_info(PovGpuScene* sc, PovGpuTreeInfo* info)
+{
+    if (!sc || !info)
+        return POV_GPU_E_INVALID;
+    std::lock_guard<std::mutex> g(sc->lock);
+    std::memset(info, 0, sizeof(*info));
+    info->bounding_tree = sc->tree_mode;
+    if (sc->tree_mode == 1) {
+        info->nodes = (int32_t)sc->ref_output.nodes.size();
+        info->depth = sc->ref_output.depth;
+    } else {
+        info->nodes = sc->sah_nodes;
+        info->depth = sc->sah_depth;
+    }
+    info->ref_top_nodes = sc->ref_built ? sc->ref_output.top_nodes : -1;
+    info->ref_mesh_nodes = sc->ref_built ? sc->ref_output.mesh_nodes : -1;
     return POV_GPU_OK;
 }
 

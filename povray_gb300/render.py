@@ -156,12 +156,20 @@ class GpuScene:
             stats = {k: merge.get(k, lambda a, b: a + b)(stats[k], pre[k]) for k in stats}
         return _scenes.unblock(rgbt, blocks, p.width, p.height), stats
 
-    def set_launch_config(self, trace_blocks_per_sm=0, trace_block=0, trace_occupancy=0, shade_blocks_per_sm=0):
+    def set_launch_config(self, trace_blocks_per_sm=0, trace_block=0, trace_occupancy=0, shade_blocks_per_sm=0,
+                          bounding_tree=0):
         """Launch shapes of the trace path's kernels (pov_gpu_set_launch_config;
-        0 = the library's default), e.g. an entry of the autotuner's table."""
+        0 = the library's default), e.g. an entry of the autotuner's table;
+        bounding_tree=1 traces the reference's own bounding tree."""
         c = abi.PovGpuLaunchConfig(int(trace_blocks_per_sm), int(trace_block), int(trace_occupancy),
-                                   int(shade_blocks_per_sm))
+                                   int(shade_blocks_per_sm), int(bounding_tree))
         _check(self.lib.pov_gpu_set_launch_config(self.h, C.byref(c)), "pov_gpu_set_launch_config")
+
+    def tree_info(self):
+        """The traversal tree in use (pov_gpu_get_tree_info) as a dict."""
+        t = abi.PovGpuTreeInfo()
+        _check(self.lib.pov_gpu_get_tree_info(self.h, C.byref(t)), "pov_gpu_get_tree_info")
+        return {k: getattr(t, k) for k, _ in t._fields_ if k != "reserved"}
 
     def cache_save(self, path):
         """Writes the radiosity sample cache as a .rca file (pov_gpu_cache_save)."""

@@ -145,6 +145,38 @@ def test_csg_torus_grid_matches_oracle_with_aa():
         assert abs(st[k] - rst[k]) <= 2e-3 * rst[k], (k, st, rst)
 
 
+@pytest.mark.parametrize("case", ["spheres_plane_320x240", "mesh_spheres_small_160x90", "csg_torus_grid_160x90"])
+def test_reference_bounding_tree(case):
+    """The traversal on the reference's own bounding tree (bounding_tree=1:
+    Build_BBox_Tree over the objects, each mesh2's tree under its leaf): the
+    tree has as many composite nodes as the oracle's restatement of the
+    reference's build (top tree and mesh trees), and hits, pixels and
+    counters match the reference's golden vectors as on the library's
+    tree; switching back restores the library's tree and its image."""
+    scene = CASES[case][0]
+    g = _load(case)
+    gpu = GpuScene(scene)
+    base, _ = gpu.render(params=_no_aa(scene))
+    assert gpu.tree_info()["bounding_tree"] == 0 and gpu.tree_info()["ref_top_nodes"] == -1
+    gpu.set_launch_config(bounding_tree=1)
+    info = gpu.tree_info()
+    assert info["bounding_tree"] == 1 and info["nodes"] > 0
+    assert (info["ref_top_nodes"], info["ref_mesh_nodes"]) == Oracle(scene).tree_info(), info
+    h = gpu.trace_rays(g["ray_org"], g["ray_dir"])
+    r = compare_hits(h["object"], h["triangle"], h["t"], g["hit_object"], g["hit_triangle"], g["hit_t"],
+                     oracle=Oracle(scene), org=g["ray_org"], dirs=g["ray_dir"], t_tol=T_TOL)
+    assert r["bad"] == 0 and r["t_bad"] == 0, json.dumps(r)
+    img, st = gpu.render(params=_no_aa(scene))
+    c = compare_pixels(img, g["pixels"])
+    assert c["within_1lsb"] >= PIX_FRAC, c
+    _counters_close(st, json.loads(str(g["stats"])))
+    assert float(np.abs(img - base).max()) <= 1e-5
+    gpu.set_launch_config(bounding_tree=0)
+    assert gpu.tree_info()["bounding_tree"] == 0
+    again, _ = gpu.render(params=_no_aa(scene))
+    assert np.array_equal(again, base)
+
+
 @pytest.mark.parametrize("csg_child", [False, True], ids=["torus_free", "csg_torus"])
 def test_torus_tunnel_matches_oracle(csg_child):
     """48 rings down the view axis: every camera ray meets a few dozen tori,
