@@ -87,9 +87,9 @@ def parse():
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--workload", default="mesh_spheres", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--bounding-tree", default="sah", choices=["sah", "reference"],
-                    help="the traversal's tree: the library's binned-SAH tree (default) or the reference's "
-                         "bounding tree (Build_BBox_Tree, each mesh2's own tree)")
+    ap.add_argument("--bounding-tree", default=None, choices=["sah", "reference"],
+                    help="the traversal's tree: the library's binned-SAH tree or the reference's bounding tree "
+                         "(Build_BBox_Tree, each mesh2's own tree); default: the launch table's choice")
     return ap.parse_args()
 
 
@@ -341,8 +341,8 @@ def main():
     # the autotuner's launch shape for this workload, when it recorded one
     from povray_gb300 import autotune
     launch_cfg = None if args.workload in MULTIVIEW else autotune.tuned_config(args.workload, args.width, args.height)
-    if args.bounding_tree == "reference":
-        launch_cfg = dict(launch_cfg or {}, bounding_tree=1)
+    if args.bounding_tree is not None:
+        launch_cfg = dict(launch_cfg or {}, bounding_tree=1 if args.bounding_tree == "reference" else 0)
     if launch_cfg:
         gpu.set_launch_config(**launch_cfg)
     stream = torch.cuda.current_stream()

@@ -102,10 +102,25 @@ struct BuildItem {
     AABB     box;
     float    c[3];
     uint32_t ref;
+    float    cost;   // relative cost of its intersection test (a triangle's is 1)
 };
 
+// Relative test costs per primitive kind for the SAH: a torus runs the FP32
+// pre-cull and, when it passes, the FP64 quartic; a CSG finds every child's
+// roots and tests each against the siblings; boxes take three slabs.
+inline float prim_cost(uint32_t kind)
+{
+    switch (kind) {
+    case PK_TORUS: return 8.0f;
+    case PK_CSG: return 6.0f;
+    case PK_BOX: return 1.5f;
+    default: return 1.0f;
+    }
+}
+
 // Binned-SAH binary BVH emitted as two-wide 64-byte nodes in depth-first
-// order.  Leaves hold at most LEAF_MAX_PRIMS prim references.
+// order, each primitive weighted by its test cost.  Leaves hold at most
+// LEAF_MAX_PRIMS prim references.
 class BvhBuilder {
 public:
     std::vector<BuildItem> items;
@@ -153,9 +168,12 @@ private:
         max_depth = std::max(max_depth, depth);
         int n = end - begin;
         AABB cb;
-        for (int i = begin; i < end; i++)
+        float cost_all = 0.0f;
+        for (int i = begin; i < end; i++) {
             cb.grow(items[i].c);
-        if (n <= 2)
+            cost_all += items[i].cost;
+        }
+        if (n == 1 || (n <= 2 && cost_all <= 2.0f))   // two cheap primitives: a leaf
             return make_leaf(begin, end, bounds);
         int axis = 0;
         float ext[3] = {cb.hi[0] - cb.lo[0], cb.hi[1] - cb.lo[1], cb.hi[2] - cb.lo[2]};
@@ -183,30 +201,37 @@ private:
                     continue;
                 AABB bb[NB];
                 int cnt[NB] = {0};
+                float bcost[NB] = {0.0f};
                 float scale = NB / ext[ax];
                 for (int i = begin; i < end; i++) {
                     int b = std::min(NB - 1, (int)((items[i].c[ax] - cb.lo[ax]) * scale));
                     cnt[b]++;
+                    bcost[b] += items[i].cost;
                     bb[b].grow(items[i].box);
                 }
-                float rarea[NB];
+                float rarea[NB], rcost[NB];
                 int rcnt[NB];
                 AABB acc;
                 int c = 0;
+                float w = 0.0f;
                 for (int b = NB - 1; b > 0; b--) {
                     acc.grow(bb[b]);
                     c += cnt[b];
+                    w += bcost[b];
                     rarea[b] = acc.area();
                     rcnt[b] = c;
+                    rcost[b] = w;
                 }
                 acc = AABB();
                 c = 0;
+                w = 0.0f;
                 for (int b = 0; b < NB - 1; b++) {
                     acc.grow(bb[b]);
                     c += cnt[b];
+                    w += bcost[b];
                     if (c == 0 || rcnt[b + 1] == 0)
                         continue;
-                    float cost = acc.area() * c + rarea[b + 1] * rcnt[b + 1];
+                    float cost = acc.area() * w + rarea[b + 1] * rcost[b + 1];
                     if (cost < best_cost) {
                         best_cost = cost;
                         best_axis = ax;
@@ -214,7 +239,7 @@ private:
                     }
                 }
             }
-            float leaf_cost = total.area() * n;
+            float leaf_cost = total.area() * cost_all;
             float trav = total.area() * 1.0f;
             if (best_axis < 0 || (n <= 4 && best_cost + trav >= leaf_cost)) {
                 if (n <= LEAF_MAX_PRIMS)
@@ -1142,6 +1167,7 @@ struct Builder {
         for (int k = 0; k < 3; k++)
             it.c[k] = 0.5f * (box.lo[k] + box.hi[k]);
         it.ref = (kind << PRIM_KIND_SHIFT) | idx;
+        it.cost = prim_cost(kind);
         bvh.items.push_back(it);
         pushed.push_back({cur_obj, it.ref});
     }
