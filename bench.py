@@ -87,6 +87,9 @@ def parse():
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--workload", default="mesh_spheres", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--radiosity-sweep", action="store_true",
+                    help="radiosity_room at 1280x720: frame time and RMSE against the FP64 truth over radiosity "
+                         "count / error_bound, plain and neural-cache forms (one JSON line each; not the bench line)")
     ap.add_argument("--bounding-tree", default=None, choices=["sah", "reference"],
                     help="the traversal's tree: the library's binned-SAH tree or the reference's bounding tree "
                          "(Build_BBox_Tree, each mesh2's own tree); default: the launch table's choice")
@@ -321,11 +324,58 @@ def radiosity_forms(args, scene, gpu, stream, params, blocks, dev_out, flush, pl
                                                                           ["noise_rel_rmse"])}
 
 
+def radiosity_sweep():
+    """Frame time at fixed RMSE: the 1280x720 room over radiosity count and
+    error_bound, plain and with the neural cache, each frame (pretrace +
+    final trace) the median of 3 after one, its linear-radiance relative RMSE
+    against the FP64 converged truth on the truth's pixels."""
+    import torch
+    from povray_gb300 import GpuScene, scenes
+    t = np.load(TRUTH)
+    px, truth = t["pixels"], t["rgb"]
+    stream = torch.cuda.current_stream()
+    runs = [("plain", c, e) for c, e in [(50, 1.0), (100, 0.8), (200, 0.5), (200, 0.3), (400, 0.3), (400, 0.2),
+                                          (800, 0.2), (800, 0.1), (1600, 0.1), (1600, 0.05)]]
+    runs += [("neural_cache", c, e) for c, e in [(200, 0.5), (400, 0.3), (800, 0.2)]]
+    for form, count, eb in runs:
+        s = scenes.radiosity_room(1280, 720, count=count, error_bound=eb)
+        g = GpuScene(s)
+        g.set_stream(stream.cuda_stream)
+        if form == "neural_cache":
+            g.set_neural_cache(True)
+        p = s.render_params()
+        blocks = scenes.blocks_for(p.width, p.height)
+        out = torch.empty((p.width * p.height, 4), dtype=torch.float32, device="cuda")
+        ms = []
+        for r in range(4):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            g.radiosity_pretrace(blocks, p)
+            g.trace_blocks(blocks, p, out=out.data_ptr())
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if r > 0:
+                ms.append(e0.elapsed_time(e1))
+        img = scenes.unblock(out.cpu().numpy(), blocks, p.width, p.height)
+        a = img[px[:, 1], px[:, 0], :3]
+        print(json.dumps({"form": form, "count": count, "error_bound": eb, "frame_ms": float(np.median(ms)),
+                          "rmse_vs_fp64": float(np.sqrt(((a - truth) ** 2).mean()) / truth.mean()),
+                          "mean_vs_fp64": float(a.mean() / truth.mean())}), flush=True)
+        del g
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.radiosity_sweep:
+        if rank == 0:
+            import torch
+            torch.cuda.set_device(local)
+            radiosity_sweep()
         return
     import torch
     torch.cuda.set_device(local)
