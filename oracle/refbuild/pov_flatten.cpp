@@ -16,6 +16,7 @@
 #include "core/material/pattern.h"
 #include "core/material/pigment.h"
 #include "core/material/texture.h"
+#include "core/material/warp.h"
 #include "core/math/matrix.h"
 #include "core/scene/camera.h"
 #include "core/scene/object.h"
@@ -90,6 +91,164 @@ struct Walker
         return false;
     }
 
+    // The ABI's pattern kind of a pattern object (the kinds the GPU path
+    // takes), 0 for any other.  `normal`: the pattern stands in a normal,
+    // where bumps is its own kind (in a pigment it is bozo's noise).
+    static int PatternKind(const BasicPattern* p, bool normal)
+    {
+        if (dynamic_cast<const CheckerPattern*>(p)) return POV_PATTERN_CHECKER;
+        if (dynamic_cast<const GradientPattern*>(p)) return POV_PATTERN_GRADIENT;
+        if (dynamic_cast<const BumpsPattern*>(p)) return normal ? POV_PATTERN_BUMPS : POV_PATTERN_BOZO;
+        if (dynamic_cast<const BozoPattern*>(p) || dynamic_cast<const SpottedPattern*>(p)) return POV_PATTERN_BOZO;
+        if (dynamic_cast<const GranitePattern*>(p)) return POV_PATTERN_GRANITE;
+        if (dynamic_cast<const MarblePattern*>(p)) return POV_PATTERN_MARBLE;
+        if (dynamic_cast<const WoodPattern*>(p)) return POV_PATTERN_WOOD;
+        if (dynamic_cast<const AgatePattern*>(p)) return POV_PATTERN_AGATE;
+        if (dynamic_cast<const OnionPattern*>(p)) return POV_PATTERN_ONION;
+        if (dynamic_cast<const LeopardPattern*>(p)) return POV_PATTERN_LEOPARD;
+        if (dynamic_cast<const DentsPattern*>(p)) return POV_PATTERN_DENTS;
+        if (dynamic_cast<const WrinklesPattern*>(p)) return POV_PATTERN_WRINKLES;
+        if (dynamic_cast<const RipplesPattern*>(p)) return POV_PATTERN_RIPPLES;
+        if (dynamic_cast<const WavesPattern*>(p)) return POV_PATTERN_WAVES;
+        if (dynamic_cast<const RadialPattern*>(p)) return POV_PATTERN_RADIAL;
+        if (dynamic_cast<const PlanarPattern*>(p)) return POV_PATTERN_PLANAR;
+        if (dynamic_cast<const SphericalPattern*>(p)) return POV_PATTERN_SPHERICAL;
+        if (dynamic_cast<const CylindricalPattern*>(p)) return POV_PATTERN_CYLINDRICAL;
+        if (dynamic_cast<const BoxedPattern*>(p)) return POV_PATTERN_BOXED;
+        if (dynamic_cast<const SquarePattern*>(p)) return POV_PATTERN_SQUARE;
+        if (dynamic_cast<const TriangularPattern*>(p)) return POV_PATTERN_TRIANGULAR;
+        if (dynamic_cast<const CubicPattern*>(p)) return POV_PATTERN_CUBIC;
+        if (dynamic_cast<const HexagonPattern*>(p)) return POV_PATTERN_HEXAGON;
+        return 0;
+    }
+
+    // A pattern (BasicPattern, source/core/material/pattern.h:151-283, with
+    // ContinuousPattern's wave and the kinds' own fields) and its warps as
+    // the ABI takes them: the list the parser builds for `turbulence` and
+    // transforms -- a ClassicTurbulence first, then one TransformWarp
+    // (Warp_EPoint walks the list backwards: the transform, then the
+    // turbulence).  `map`: the colour map (nullptr for a normal's pattern).
+    // `fwd` receives the transform's forward matrix (identity without one).
+    bool Pattern(const BasicPattern* p, bool normal, const ColourBlendMap* map, int index, PovGpuPattern& d,
+                 double* fwd)
+    {
+        std::memset(&d, 0, sizeof(d));
+        d.type = PatternKind(p, normal);
+        if (d.type == 0)
+            return Fail(index, "pattern kind the GPU path lacks");
+        d.noise_generator = p->noiseGenerator != 0 ? p->noiseGenerator : sd.noiseGenerator;
+        d.frequency = 1.0;
+        d.phase = 0.0;
+        d.exponent = 1.0;
+        d.omega = 0.5;
+        d.lambda = 2.0;
+        d.octaves = 6;
+        d.agate_turb = 1.0;
+        if (const ContinuousPattern* c = dynamic_cast<const ContinuousPattern*>(p)) {
+            if (c->waveType == kWaveType_Raw)
+                return Fail(index, "raw pattern wave");
+            d.wave_type = (int32_t)c->waveType - (int32_t)kWaveType_Ramp;   // ramp, sine, ... poly as POV_WAVE_*
+            d.frequency = c->waveFrequency;
+            d.phase = c->wavePhase;
+            d.exponent = c->waveExponent;
+        }
+        if (const GradientPattern* g = dynamic_cast<const GradientPattern*>(p))
+            Copy3(d.gradient, g->gradient);
+        if (const AgatePattern* a = dynamic_cast<const AgatePattern*>(p))
+            d.agate_turb = a->agateTurbScale;
+        MATRIX ident;
+        MIdentity(ident);
+        CopyMatrix(d.inverse, ident);
+        CopyMatrix(fwd, ident);
+        for (size_t k = 0; k < p->warps.size(); k++) {
+            const GenericWarp* w = p->warps[k];
+            if (const ClassicTurbulence* t = dynamic_cast<const ClassicTurbulence*>(w)) {
+                if (k != 0)
+                    return Fail(index, "turbulence after another warp");
+                d.has_turbulence = 1;
+                Copy3(d.turbulence, t->Turbulence);
+                d.octaves = t->Octaves;
+                d.omega = t->Omega;
+                d.lambda = t->Lambda;
+            } else if (const TransformWarp* tw = dynamic_cast<const TransformWarp*>(w)) {
+                if (k + 1 != p->warps.size())
+                    return Fail(index, "warp after the pattern's transform");
+                CopyMatrix(d.inverse, tw->Trans.inverse);
+                CopyMatrix(fwd, tw->Trans.matrix);
+            } else {
+                return Fail(index, "warp the GPU path lacks");
+            }
+        }
+        if (map != nullptr) {
+            const auto& e = map->Blend_Map_Entries;
+            if (e.empty() || e.size() > POV_PATTERN_MAX_ENTRIES)
+                return Fail(index, "colour map size");
+            d.num_entries = (int32_t)e.size();
+            for (size_t k = 0; k < e.size(); k++) {
+                if (e[k].Vals.filter() != 0.0f || e[k].Vals.transm() != 0.0f)
+                    return Fail(index, "colour map entry with filter or transmit");
+                d.values[k] = e[k].value;
+                d.colours[k][0] = e[k].Vals.colour().Red();
+                d.colours[k][1] = e[k].Vals.colour().Green();
+                d.colours[k][2] = e[k].Vals.colour().Blue();
+            }
+        }
+        return true;
+    }
+
+    // A texture's pigment pattern (Compute_Pigment's pattern path,
+    // source/core/material/pigment.cpp:395-475): its colour map, or the
+    // pattern's default one; 1-based index into the patterns.
+    bool PigmentPattern(const PIGMENT* pig, int index, int& out_index)
+    {
+        const ColourBlendMap* map = nullptr;
+        ColourBlendMapConstPtr def;
+        if (pig->Blend_Map) {
+            map = dynamic_cast<const ColourBlendMap*>(pig->Blend_Map.get());
+            if (map == nullptr)
+                return Fail(index, "pigment map (not a colour map)");
+        } else {
+            def = pig->pattern->GetDefaultBlendMap();
+            map = def.get();
+            if (map == nullptr)
+                return Fail(index, "pattern without a colour map");
+        }
+        PovGpuPattern d;
+        double fwd[16];
+        if (!Pattern(pig->pattern.get(), false, map, index, d, fwd))
+            return false;
+        out.patterns.push_back(d);
+        out_index = (int)out.patterns.size();
+        return true;
+    }
+
+    // A texture's normal (Tnormal_Struct, normal.h:118-123, perturbed by
+    // Perturb_Normal, normal.cpp:784-905): its pattern, Amount, Delta, the
+    // no_bump_scale flag and the pattern transform's forward matrix;
+    // 1-based index into the normals.
+    bool NormalOf(const TNORMAL* n, int index, int& out_index)
+    {
+        if (n->Blend_Map)
+            return Fail(index, "normal map or slope map");
+        const bool special = n->Type == BUMPS_PATTERN || n->Type == DENTS_PATTERN || n->Type == WRINKLES_PATTERN ||
+                             n->Type == RIPPLES_PATTERN || n->Type == WAVES_PATTERN;
+        if (!special && n->Type != GENERIC_PATTERN)
+            return Fail(index, "normal pattern kind the GPU path lacks");
+        PovGpuPattern p;
+        PovGpuNormal d;
+        std::memset(&d, 0, sizeof(d));
+        if (!Pattern(n->pattern.get(), true, nullptr, index, p, d.matrix))
+            return false;
+        out.patterns.push_back(p);
+        d.pattern = (int32_t)out.patterns.size();
+        d.dont_scale_bumps = (n->Flags & DONT_SCALE_BUMPS_FLAG) ? 1 : 0;
+        d.amount = n->Amount;
+        d.delta = n->Delta;
+        out.normals.push_back(d);
+        out_index = (int)out.normals.size();
+        return true;
+    }
+
     // TEXTURE + its FINISH (source/core/material/texture.h:108-141) as the
     // ABI's single-layer material: a plain pigment colour and the finish
     // values as the parser leaves them.
@@ -103,10 +262,13 @@ struct Walker
         }
         if (t == nullptr || t->Type != PLAIN_PATTERN || t->Next != nullptr)
             return Fail(index, "layered or mapped texture");
-        if (t->Pigment == nullptr || t->Pigment->Type != PLAIN_PATTERN)
-            return Fail(index, "pattern pigment (not flattened here)");
-        if (t->Tnormal != nullptr)
-            return Fail(index, "normal perturbation (not flattened here)");
+        if (t->Pigment == nullptr || (t->Pigment->Type != PLAIN_PATTERN && !t->Pigment->pattern))
+            return Fail(index, "pigment without a pattern");
+        int pattern = 0, normal = 0;
+        if (t->Pigment->Type != PLAIN_PATTERN && !PigmentPattern(t->Pigment, index, pattern))
+            return false;
+        if (t->Tnormal != nullptr && !NormalOf(t->Tnormal, index, normal))
+            return false;
         const FINISH* f = t->Finish;
         PovGpuMaterial m;
         std::memset(&m, 0, sizeof(m));
@@ -146,8 +308,8 @@ struct Walker
         m.fresnel = f->Fresnel;
         m.crand = f->Crand;
         m.irid = f->Irid;
-        m.pattern = 0;
-        m.normal = 0;
+        m.pattern = pattern;
+        m.normal = normal;
         mat = (int)out.materials.size();
         out.materials.push_back(m);
         material_of[t] = mat;

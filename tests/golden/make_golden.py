@@ -247,14 +247,15 @@ def write_radiosity_cache_file(tmp, case="radiosity_room_160x90"):
 
 
 SCENE_FILE_CASES = ("spheres_plane_320x240", "mesh_spheres_small_160x90", "csg_torus_grid_160x90",
-                    "area_room_160x90", "media_spheres_160x120", "radiosity_room_160x90")
+                    "area_room_160x90", "media_spheres_160x120", "radiosity_room_160x90",
+                    "textured_spheres_160x120", "textured_turbulent_perlin_160x120", "bumpy_spheres_160x120",
+                    "bumpy_waves_160x120", "shaped_spheres_160x120", "glass_spheres_160x120")
 
 
 def write_scene_files(tmp):
     """The reference's parse of each case flattened into the C ABI's scene
     description (pov_oracle ... desc: oracle/refbuild/pov_flatten.cpp walks
-    the SceneData the reference's parser built) -> <case>.pgsf.gz.  Cases
-    with pattern pigments or normals are not flattened by it."""
+    the SceneData the reference's parser built) -> <case>.pgsf.gz."""
     import gzip
     allc = dict((k, v[0]) for k, v in cases().items())
     allc.update(radiosity_cases())

@@ -10,6 +10,9 @@ Tolerances (written here, applied below):
   camera vectors                     1e-15 relative (the parser's FP64 math)
   object parameters, transforms      1e-12
   material, light and media floats   1e-7 (single-precision fields)
+  patterns and normals               by content: ids exact, matrices 1e-12,
+                                     single-precision parameters and
+                                     colour maps 1e-7
   mesh vertices and indices          exact; normals 1e-6 (the parser
                                      normalises normal_vectors in FP64 and
                                      stores them as floats)
@@ -49,6 +52,33 @@ def _close(tag, x, y, tol, skip=()):
         assert av.shape == bv.shape and np.allclose(av, bv, rtol=tol, atol=tol), (tag, name, av, bv)
 
 
+def _pattern_close(i, pa, pb):
+    """A pattern record: ids and counts exact, matrices and FP64 parameters
+    1e-12, the single-precision ones (wave, turbulence omega/lambda,
+    agate_turb, colour map) 1e-7."""
+    from povray_gb300 import abi
+    for k in ("type", "noise_generator", "num_entries", "wave_type", "has_turbulence"):
+        assert getattr(pa, k) == getattr(pb, k), (i, k, getattr(pa, k), getattr(pb, k))
+    # the kind's own fields only where the kind reads them
+    skip = ["type", "noise_generator", "num_entries", "wave_type", "octaves", "has_turbulence", "values", "colours",
+            "frequency", "phase", "exponent", "omega", "lambda", "agate_turb", "turbulence"]
+    if pa.type != abi.POV_PATTERN_GRADIENT:
+        skip.append("gradient")
+    _close("pattern of object %d" % i, pa, pb, 1e-12, skip=tuple(skip))
+    single = ["frequency", "phase", "exponent"]
+    if pa.has_turbulence:
+        assert pa.octaves == pb.octaves, i
+        assert np.allclose(pa.turbulence[:], pb.turbulence[:], rtol=1e-12, atol=1e-12), i
+        single += ["omega", "lambda"]
+    if pa.type == abi.POV_PATTERN_AGATE:
+        single.append("agate_turb")
+    for k in single:
+        assert abs(getattr(pa, k) - getattr(pb, k)) <= 1e-7 * max(1.0, abs(getattr(pa, k))), (i, k)
+    n = pa.num_entries
+    assert np.allclose(pa.values[:n], pb.values[:n], atol=1e-7), i
+    assert np.allclose(np.array(pa.colours[:n]), np.array(pb.colours[:n]), atol=1e-7), i
+
+
 def _material_of(d, i):
     o = d.objects[i]
     while o.material < 0 and o.parent >= 0:
@@ -81,7 +111,20 @@ def test_reference_flattened_scene_equals_generator_desc(case):
         ma, mb = _material_of(a, i), _material_of(b, i)
         assert (ma >= 0) == (mb >= 0), i
         if ma >= 0:
-            _close("material of object %d" % i, a.materials[ma], b.materials[mb], 1e-7)
+            A, Bm = a.materials[ma], b.materials[mb]
+            assert (A.pattern > 0) == (Bm.pattern > 0) and (A.normal > 0) == (Bm.normal > 0), i
+            # pattern and normal records are compared by content (the two
+            # sides number them in different orders); a pattern pigment's
+            # own colour is unused
+            skip = ("pattern", "normal") + (("pigment",) if A.pattern > 0 else ())
+            _close("material of object %d" % i, A, Bm, 1e-7, skip=skip)
+            if A.pattern > 0:
+                _pattern_close(i, a.patterns[A.pattern - 1], b.patterns[Bm.pattern - 1])
+            if A.normal > 0:
+                na, nb = a.normals[A.normal - 1], b.normals[Bm.normal - 1]
+                _close("normal of object %d" % i, na, nb, 1e-12, skip=("pattern", "amount", "delta"))
+                assert abs(na.amount - nb.amount) <= 1e-7 and abs(na.delta - nb.delta) <= 1e-7, i
+                _pattern_close(i, a.patterns[na.pattern - 1], b.patterns[nb.pattern - 1])
     # interiors: the same content per object, and the same sharing (which
     # objects have one interior between them)
     assert abs(a.atmosphere_ior - b.atmosphere_ior) == 0.0
