@@ -87,6 +87,8 @@ def parse():
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--workload", default="mesh_spheres", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-other-configs", action="store_true",
+                    help="skip the short lines of the reference's other configurations")
     ap.add_argument("--radiosity-sweep", action="store_true",
                     help="radiosity_room at 1280x720: frame time and RMSE against the FP64 truth over radiosity "
                          "count / error_bound, plain and neural-cache forms (one JSON line each; not the bench line)")
@@ -365,6 +367,75 @@ def radiosity_sweep():
         del g
 
 
+# The reference's other configurations (config 1: 64 spheres at 320x240;
+# config 3: the CSG/torus grid with AA; config 4: the radiosity room; config
+# 5: the multi-view media scene), each timed briefly in the same run beside
+# the main line.
+OTHER_CONFIGS = (("spheres_plane", 320, 240), ("csg_torus_grid", 1920, 1080), ("radiosity_room", 1280, 720),
+                 ("multiview_media", 0, 0))
+
+
+def other_configs(args, stream, flush, steps=3, warmup=2):
+    """One compact line per other configuration: frames by CUDA events on the
+    launch stream, L2 flushed between them, scene resident, image in device
+    memory; rays (primary + shadow) per second of the timed frames; the
+    launch table's shape; radiosity frames include the pretrace, the
+    multi-view steps are consecutive views."""
+    import torch
+    from povray_gb300 import GpuScene, autotune, scenes
+    out = []
+    for wl, w, h in OTHER_CONFIGS:
+        if wl == args.workload:
+            continue
+        try:
+            multiview = wl in MULTIVIEW
+            s = scenes.WORKLOADS[wl]() if multiview else scenes.WORKLOADS[wl](w, h)
+            gpu = GpuScene(s)
+            gpu.set_stream(stream.cuda_stream)
+            cfg = None if multiview else autotune.tuned_config(wl, w, h)
+            if cfg:
+                gpu.set_launch_config(**cfg)
+            views = scenes.circle_views() if multiview else None
+            if multiview:
+                gpu.set_neural_cache(True, shared=True)
+            npix = max(vw * vh for _, _, vw, vh in views) if multiview else w * h
+            dev = torch.empty((npix, 4), dtype=torch.float32, device="cuda")
+
+            def frame(i):
+                if multiview:
+                    loc, at, vw, vh = views[i % len(views)]
+                    gpu.set_camera(loc, at, s.angle, vw, vh)
+                    p, bl = scenes.view_of(s, loc, at, vw, vh).render_params(), scenes.blocks_for(vw, vh)
+                else:
+                    p, bl = s.render_params(), scenes.blocks_for(w, h)
+                st_pre = gpu.radiosity_pretrace(bl, p) if s.radiosity is not None else None
+                st = gpu.trace_blocks(bl, p, out=dev.data_ptr())[1]
+                r = st["number_of_rays"] + st["shadow_ray_tests"]
+                if st_pre is not None:
+                    r += st_pre["number_of_rays"] + st_pre["shadow_ray_tests"]
+                return r
+
+            for i in range(warmup):
+                frame(i)
+            ms, rays = [], 0
+            for i in range(steps):
+                flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                rays += frame(warmup + i)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ms.append(e0.elapsed_time(e1))
+            desc = WORKLOADS[wl] if multiview else WORKLOADS[wl] % (w, h)
+            out.append({"workload": desc, "value": rays / (sum(ms) / 1e3) / 1e6, "unit": "Mrays/s",
+                        "ms_per_step": sum(ms) / len(ms), "steps": steps, "warmup": warmup,
+                        "launch_config": cfg or "library defaults"})
+            del gpu, dev
+        except Exception as e:   # a failing extra line must not lose the main one
+            out.append({"workload": wl, "error": str(e)[:300]})
+    return out
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -556,6 +627,8 @@ def main():
     if radiosity and not multiview:
         out["radiosity_forms"] = radiosity_forms(args, s, gpu, stream, params, blocks, dev_out, flush,
                                                  t_total / args.steps * 1e3)
+    if rank == 0 and world == 1 and not args.no_other_configs:
+        out["other_configs"] = other_configs(args, stream, flush)
     if rank == 0 and not args.no_cpu_baseline:
         if multiview:
             loc, at, w, h = views[0]
