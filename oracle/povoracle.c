@@ -2725,12 +2725,30 @@ static double trace_ray(const PovOracle* S, Thread* th, V3 O, V3 D, double weigh
     return depth;
 }
 
+/* The phase factor of ComputeMediaScatteringAttenuation (media.cpp:1183-
+ * 1220) for one media, alpha = the cosine between the light ray (towards
+ * the light) and the viewing ray: isotropic 1, Mie hazy, Mie murky,
+ * Rayleigh, Henyey-Greenstein with the eccentricity g. */
+static double media_phase(const PovGpuMedia* md, double alpha)
+{
+    switch (md->scattering_type) {
+    case 2: return 0.576655375 * (1.0 + 9.0 * pow(0.5 * (1.0 + alpha), 8.0));
+    case 3: return 0.495714547 * (1.0 + 50.0 * pow(0.5 * (1.0 + alpha), 32.0));
+    case 4: return 0.799372013 * (1.0 + alpha * alpha);
+    case 5: {
+        const double g = md->eccentricity, g2 = g * g;
+        return (1.0 - g2) / pow(1.0 + g2 - 2.0 * g * alpha, 1.5);
+    }
+    default: return 1.0;
+    }
+}
+
 /* One media sample (MediaFunction::ComputeOneMediaSample, media.cpp:935-1038,
  * sample method 3, constant density): at fraction d of the interval
  * [s0, s0 + ds], the in-scattered light of every point light not in shadow
- * (TestShadow, trace.cpp:3173-3203, from inside the container), isotropic
- * phase (ComputeMediaScatteringAttenuation, media.cpp:1183-1220), times ds;
- * the interval's optical depth estimate extinction * ds. */
+ * (TestShadow, trace.cpp:3173-3203, from inside the container) times the
+ * media's phase factor (media_phase), times ds; the interval's optical
+ * depth estimate extinction * ds. */
 static void media_sample(const PovOracle* S, Thread* th, const PovGpuMedia* md, V3 O, V3 D, double s0, double ds,
                          double d, int medium, double lit, Ticket* tk, float C[3], float od[3])
 {
@@ -2757,8 +2775,9 @@ static void media_sample(const PovOracle* S, Thread* th, const PovGpuMedia* md, 
                 continue;
             if (fabs(lc[0]) < EPSILON && fabs(lc[1]) < EPSILON && fabs(lc[2]) < EPSILON)
                 continue;
+            const double ph = media_phase(md, vdot(ld, D));
             for (int k = 0; k < 3; k++)
-                em[k] += 1.0 * md->scattering[k] * (float)lc[k];
+                em[k] += (float)(ph * md->scattering[k]) * (float)lc[k];
         }
     }
     for (int k = 0; k < 3; k++) {
@@ -3593,7 +3612,7 @@ int pov_oracle_create(const PovGpuSceneDesc* desc, PovOracle** out, int32_t* bad
                 m->specular != 0.0f || m->emission[0] != 0.0f || m->emission[1] != 0.0f || m->emission[2] != 0.0f ||
                 m->ambient[0] != 0.0f || m->ambient[1] != 0.0f || m->ambient[2] != 0.0f ||
                 m->reflection_max[0] != 0.0f || m->reflection_max[1] != 0.0f || m->reflection_max[2] != 0.0f ||
-                md->method != 3 || md->jitter != 0.0f || md->scattering_type != 1 ||
+                md->method != 3 || md->jitter != 0.0f || md->scattering_type < 1 || md->scattering_type > 5 ||
                 md->min_samples != md->max_samples || md->min_samples < 1 || md->aa_level < 1)
                 return POV_GPU_E_UNSUPPORTED;
             /* camera rays start outside every container: a camera inside one

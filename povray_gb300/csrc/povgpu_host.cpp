@@ -792,7 +792,8 @@ int validate_media(const PovGpuSceneDesc* d, std::vector<char>& cmat, int32_t* b
             m->specular != 0.0f || m->emission[0] != 0.0f || m->emission[1] != 0.0f || m->emission[2] != 0.0f ||
             m->ambient[0] != 0.0f || m->ambient[1] != 0.0f || m->ambient[2] != 0.0f ||
             m->reflection_max[0] != 0.0f || m->reflection_max[1] != 0.0f || m->reflection_max[2] != 0.0f ||
-            md->method != 3 || md->jitter != 0.0f || md->scattering_type != 1 || md->min_samples != md->max_samples ||
+            md->method != 3 || md->jitter != 0.0f || md->scattering_type < 1 || md->scattering_type > 5 ||
+            md->min_samples != md->max_samples ||
             md->min_samples < 1 || md->aa_level < 1 || md->aa_level > MEDIA_MAX_AA_LEVEL || md->intervals < 1 ||
             md->intervals > MEDIA_MAX_INTERVALS || containers >= MAX_CONTAINERS)
             return POV_GPU_E_UNSUPPORTED;
@@ -1849,6 +1850,7 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
         m.scattering = make_float4(md.scattering[0], md.scattering[1], md.scattering[2], scat ? 1.0f : 0.0f);
         m.extinction = make_float4(md.extinction[0], md.extinction[1], md.extinction[2], 0.0f);
         m.n = make_int4(md.intervals, std::max((md.min_samples + 1) / 2, 1), md.aa_level, box);
+        m.phase = make_float4((float)md.scattering_type, md.eccentricity, 0.0f, 0.0f);
         media_ni = std::max(media_ni, md.intervals + 1);   // + the padding interval
         const int sub = m.n.y, T = (1 << md.aa_level) - 1;
         sc->media_smax = std::max(sc->media_smax, sub + 1 + sub * T);

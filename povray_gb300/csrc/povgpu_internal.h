@@ -174,6 +174,7 @@ struct __align__(16) DevMedia {
     float4 scattering;   // rgb, 1 when any channel scatters
     float4 extinction;   // rgb (absorption + scattering), -
     int4   n;            // Intervals, sub-intervals (Min_Samples+1)/2, AA_Level, box index
+    float4 phase;        // scattering type (1 isotropic .. 5 Henyey-Greenstein), eccentricity, -, -
 };
 constexpr int BOX_CONTAINER = 2;         // DevBox flag: surface of a media container
 constexpr int OBJ_CONTAINER = 1 << 30;   // ObjectShade flag; container index in bits 16..23

@@ -2473,6 +2473,26 @@ struct MediaSeg {
 // every light not in shadow (TestShadow, trace.cpp:3173-3203; isotropic
 // phase, ComputeMediaScatteringAttenuation), times ds; the optical depth
 // estimate extinction * ds.
+// The phase factor of ComputeMediaScatteringAttenuation (media.cpp:1183-
+// 1220), alpha = the cosine between the ray towards the light and the
+// viewing ray: isotropic 1, Mie hazy, Mie murky, Rayleigh, Henyey-Greenstein.
+__device__ __forceinline__ float media_phase(float4 ph, float alpha)
+{
+    const int type = (int)ph.x;
+    if (type == 2)
+        return 0.576655375f * (1.0f + 9.0f * powf(0.5f * (1.0f + alpha), 8.0f));
+    if (type == 3)
+        return 0.495714547f * (1.0f + 50.0f * powf(0.5f * (1.0f + alpha), 32.0f));
+    if (type == 4)
+        return 0.799372013f * (1.0f + alpha * alpha);
+    if (type == 5) {
+        const float g = ph.y, g2 = g * g;
+        const float b = 1.0f + g2 - 2.0f * g * alpha;
+        return (1.0f - g2) / (b * sqrtf(b));
+    }
+    return 1.0f;
+}
+
 template <bool FULL>
 __device__ void media_point(const DeviceScene& S, const MediaSeg& g, double s0, double ds, double f, double lit,
                             float3& C, float3& od, int* smem, int stack_depth, uint32_t* err,
@@ -2497,7 +2517,8 @@ __device__ void media_point(const DeviceScene& S, const MediaSeg& g, double s0, 
                                      ldist - SHADOW_TOLERANCE_F, make_uint2(NO_PRIM, 0u), g.medium, true, atten,
                                      smem, stack_depth, err, tests, succ, ms))
                 continue;
-            em = em + sc * (lc * atten);
+            const float ph = media_phase(g.md->phase, dot3(ld, g.D));
+            em = em + (sc * ph) * (lc * atten);
         }
     }
     const float dsf = (float)ds;

@@ -550,15 +550,18 @@ class Scene:
         return dict(type=t, kind=kind, children=moved, translate=tv, material=mat, interior=interior)
 
     def media_box(self, c1, c2, scattering=(0.05, 0.05, 0.05), absorption=(0.0, 0.0, 0.0),
-                  emission=(0.0, 0.0, 0.0), intervals=10, samples=10, aa_level=3, aa_threshold=0.1):
+                  emission=(0.0, 0.0, 0.0), intervals=10, samples=10, aa_level=3, aa_threshold=0.1,
+                  scattering_type=1, eccentricity=0.0):
         """A hollow, fully transmitting box holding one uniform media
         (Parse_Media defaults, source/parser/parser_materials.cpp:3500-3630:
-        method 3, jitter 0; isotropic scattering; Media::PostProcess sets
-        extinction = absorption + scattering)."""
+        method 3, jitter 0; Media::PostProcess sets extinction = absorption +
+        scattering).  scattering_type: 1 isotropic, 2 Mie hazy, 3 Mie murky,
+        4 Rayleigh, 5 Henyey-Greenstein with `eccentricity`."""
         mat = self.material(Material((1.0, 1.0, 1.0), ambient=0.0, diffuse=0.0, transmit=1.0))
         self.medias.append(dict(scattering=tuple(map(float, scattering)), absorption=tuple(map(float, absorption)),
                                 emission=tuple(map(float, emission)), intervals=int(intervals),
-                                samples=int(samples), aa_level=int(aa_level), aa_threshold=float(aa_threshold)))
+                                samples=int(samples), aa_level=int(aa_level), aa_threshold=float(aa_threshold),
+                                scattering_type=int(scattering_type), eccentricity=float(eccentricity)))
         node = self.n_box(c1, c2, mat)
         node["hollow"] = True
         node["media"] = len(self.medias)
@@ -643,10 +646,12 @@ class Scene:
                 extra += " hollow"
             if o.get("media"):
                 md = self.medias[o["media"] - 1]
-                extra += (" interior { media { scattering { 1, rgb %s } absorption rgb %s emission rgb %s"
+                ecc = (" eccentricity %s" % _g(md["eccentricity"])) if md["scattering_type"] == 5 else ""
+                extra += (" interior { media { scattering { %d, rgb %s%s } absorption rgb %s emission rgb %s"
                           " intervals %d samples %d aa_level %d aa_threshold %s } }"
-                          % (_v(md["scattering"]), _v(md["absorption"]), _v(md["emission"]), md["intervals"],
-                             md["samples"], md["aa_level"], _g(md["aa_threshold"])))
+                          % (md["scattering_type"], _v(md["scattering"]), ecc, _v(md["absorption"]),
+                             _v(md["emission"]), md["intervals"], md["samples"], md["aa_level"],
+                             _g(md["aa_threshold"])))
             return "box { %s, %s%s%s }" % (_v(o.get("sdl_c1", o["c1"])), _v(o.get("sdl_c2", o["c2"])), tex, extra)
         if t == abi.POV_OBJ_TORUS:
             return "torus { %s, %s %s%s }" % (_g(o["R"]), _g(o["r"]), o["mods"], tex)
@@ -771,7 +776,8 @@ class Scene:
         medias = (abi.PovGpuMedia * max(len(self.medias), 1))()
         for i, md in enumerate(self.medias):
             m = medias[i]
-            m.scattering_type = 1
+            m.scattering_type = md["scattering_type"]
+            m.eccentricity = md["eccentricity"] if md["scattering_type"] == 5 else 0.0
             m.method = 3
             m.intervals = md["intervals"]
             m.min_samples = m.max_samples = md["samples"]
@@ -1108,9 +1114,11 @@ def radiosity_room(width=1280, height=720, n_spheres=200, seed=4, radiosity=True
     return s
 
 
-def media_spheres(width=320, height=240, n_spheres=24, seed=5, intervals=10, samples=10, scattering=0.05):
+def media_spheres(width=320, height=240, n_spheres=24, seed=5, intervals=10, samples=10, scattering=0.05,
+                  scattering_type=1, eccentricity=0.0):
     """A uniform scattering media box [-7,7]^3 (hollow, fully transmitting;
-    scattering {1, rgb 0.05}, intervals 10, samples 10, method 3) around
+    scattering {1, rgb 0.05} -- or another scattering type, with its
+    eccentricity for Henyey-Greenstein --, intervals 10, samples 10, method 3) around
     `n_spheres` spheres r U[0.4,1.2], centres U[-5.5,5.5]^3, rgb U[0.2,0.9]^3
     (seed 5), every other one with reflection 0.2; plane y=-8; one point
     light (20,30,-20); camera (0,4,-25) looking at the origin, 50 deg;
@@ -1119,7 +1127,7 @@ def media_spheres(width=320, height=240, n_spheres=24, seed=5, intervals=10, sam
     s = Scene("media_spheres", width, height, (0.0, 4.0, -25.0), (0.0, 0.0, 0.0), 50.0, max_trace_level=3)
     s.point_light((20.0, 30.0, -20.0))
     s.media_box((-7.0, -7.0, -7.0), (7.0, 7.0, 7.0), scattering=(scattering,) * 3, intervals=intervals,
-                samples=samples)
+                samples=samples, scattering_type=scattering_type, eccentricity=eccentricity)
     for i in range(n_spheres):
         c = rng.uniform(-5.5, 5.5, size=3)
         r = rng.uniform(0.4, 1.2)

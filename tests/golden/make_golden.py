@@ -59,6 +59,10 @@ def cases():
         "area_room_adaptive_160x90": (scenes.radiosity_room(160, 90, n_spheres=40, radiosity=False, area=(5, 5),
                                                             adaptive=1, orient=True), 2, 9.0),
         "media_spheres_160x120": (scenes.media_spheres(160, 120), 2, 9.0),
+        "media_hazy_160x120": (scenes.media_spheres(160, 120, scattering_type=2), 4, 9.0),
+        "media_murky_160x120": (scenes.media_spheres(160, 120, scattering_type=3), 4, 9.0),
+        "media_rayleigh_160x120": (scenes.media_spheres(160, 120, scattering_type=4), 4, 9.0),
+        "media_hg_160x120": (scenes.media_spheres(160, 120, scattering_type=5, eccentricity=0.6), 4, 9.0),
         "textured_spheres_160x120": (scenes.textured_spheres(160, 120), 2, 8.0),
         "textured_perlin_160x120": (scenes.textured_spheres(160, 120, noise_generator=3), 2, 8.0),
         "textured_original_160x120": (scenes.textured_spheres(160, 120, noise_generator=1), 2, 8.0),
