@@ -1115,10 +1115,11 @@ def radiosity_room(width=1280, height=720, n_spheres=200, seed=4, radiosity=True
 
 
 def media_spheres(width=320, height=240, n_spheres=24, seed=5, intervals=10, samples=10, scattering=0.05,
-                  scattering_type=1, eccentricity=0.0):
+                  scattering_type=1, eccentricity=0.0, absorption=(0.0, 0.0, 0.0), emission=(0.0, 0.0, 0.0)):
     """A uniform scattering media box [-7,7]^3 (hollow, fully transmitting;
     scattering {1, rgb 0.05} -- or another scattering type, with its
-    eccentricity for Henyey-Greenstein --, intervals 10, samples 10, method 3) around
+    eccentricity for Henyey-Greenstein, absorption and emission --,
+    intervals 10, samples 10, method 3) around
     `n_spheres` spheres r U[0.4,1.2], centres U[-5.5,5.5]^3, rgb U[0.2,0.9]^3
     (seed 5), every other one with reflection 0.2; plane y=-8; one point
     light (20,30,-20); camera (0,4,-25) looking at the origin, 50 deg;
@@ -1127,7 +1128,8 @@ def media_spheres(width=320, height=240, n_spheres=24, seed=5, intervals=10, sam
     s = Scene("media_spheres", width, height, (0.0, 4.0, -25.0), (0.0, 0.0, 0.0), 50.0, max_trace_level=3)
     s.point_light((20.0, 30.0, -20.0))
     s.media_box((-7.0, -7.0, -7.0), (7.0, 7.0, 7.0), scattering=(scattering,) * 3, intervals=intervals,
-                samples=samples, scattering_type=scattering_type, eccentricity=eccentricity)
+                samples=samples, scattering_type=scattering_type, eccentricity=eccentricity, absorption=absorption,
+                emission=emission)
     for i in range(n_spheres):
         c = rng.uniform(-5.5, 5.5, size=3)
         r = rng.uniform(0.4, 1.2)

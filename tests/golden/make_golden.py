@@ -63,6 +63,8 @@ def cases():
         "media_murky_160x120": (scenes.media_spheres(160, 120, scattering_type=3), 4, 9.0),
         "media_rayleigh_160x120": (scenes.media_spheres(160, 120, scattering_type=4), 4, 9.0),
         "media_hg_160x120": (scenes.media_spheres(160, 120, scattering_type=5, eccentricity=0.6), 4, 9.0),
+        "media_glow_160x120": (scenes.media_spheres(160, 120, scattering=0.0, absorption=(0.06, 0.03, 0.01),
+                                                    emission=(0.02, 0.01, 0.03)), 4, 9.0),
         "textured_spheres_160x120": (scenes.textured_spheres(160, 120), 2, 8.0),
         "textured_perlin_160x120": (scenes.textured_spheres(160, 120, noise_generator=3), 2, 8.0),
         "textured_original_160x120": (scenes.textured_spheres(160, 120, noise_generator=1), 2, 8.0),

@@ -83,8 +83,12 @@ def test_oracle_pixels_and_counters_match_reference(case):
         assert diff.max() <= 1e-5, float(diff.max())
         for k in ("number_of_rays", "reflected_rays", "transmitted_rays", "media_samples"):
             assert st[k] == rs[k], (k, st[k], rs[k])
+        # at most one test and one success per shadow ray that starts inside
+        # the container: 1e-4 of the shadow tests where the media samples'
+        # own shadow rays dominate, 1% of the rays without scattering
+        bound = max(1e-4 * rs["shadow_ray_tests"], 0.01 * rs["number_of_rays"])
         for k in ("shadow_ray_tests", "shadow_rays_succeeded"):
-            assert 0 <= st[k] - rs[k] <= 1e-4 * rs["shadow_ray_tests"], (k, st[k], rs[k])
+            assert 0 <= st[k] - rs[k] <= bound, (k, st[k], rs[k])
         assert compare_pixels(img, ref)["max_lsb"] <= 1
     elif _has_area_light(scene):
         assert diff.max() < 1.0 / 255.0 and (diff <= 1e-5).mean() >= 0.999, float(diff.max())
