@@ -3591,9 +3591,9 @@ int pov_oracle_create(const PovGpuSceneDesc* desc, PovOracle** out, int32_t* bad
     if (bad_index) *bad_index = -1;
     if (!desc || !out || desc->abi_version != POV_GPU_ABI_VERSION || desc->num_materials < 1)
         return POV_GPU_E_INVALID;
-    /* media containers: hollow top-level boxes whose surface only
-     * transmits, holding one constant isotropic media sampled by method 3
-     * without jitter; point lights only; no other transmitting surface */
+    /* media containers: hollow top-level boxes or spheres whose surface only
+     * transmits, holding one constant media (any scattering type) sampled
+     * by method 3 without jitter; point lights only */
     int containers = 0;
     for (int i = 0; i < desc->num_objects; i++) {
         const PovGpuObject* o = &desc->objects[i];
@@ -3607,7 +3607,8 @@ int pov_oracle_create(const PovGpuSceneDesc* desc, PovOracle** out, int32_t* bad
         if (o->media > 0) {
             if (bad_index) *bad_index = i;
             const PovGpuMedia* md = o->media > 0 ? &desc->medias[o->media - 1] : NULL;
-            if (!md || o->type != POV_OBJ_BOX || !(o->flags & POV_FLAG_HOLLOW) || o->parent >= 0 || !m ||
+            if (!md || (o->type != POV_OBJ_BOX && o->type != POV_OBJ_SPHERE) || (o->flags & POV_FLAG_INVERTED) ||
+                !(o->flags & POV_FLAG_HOLLOW) || o->parent >= 0 || !m ||
                 m->pigment[3] != 0.0f || m->pigment[4] != 1.0f || m->diffuse != 0.0f || m->phong != 0.0f ||
                 m->specular != 0.0f || m->emission[0] != 0.0f || m->emission[1] != 0.0f || m->emission[2] != 0.0f ||
                 m->ambient[0] != 0.0f || m->ambient[1] != 0.0f || m->ambient[2] != 0.0f ||
@@ -3618,9 +3619,16 @@ int pov_oracle_create(const PovGpuSceneDesc* desc, PovOracle** out, int32_t* bad
             /* camera rays start outside every container: a camera inside one
              * would need the interior list of its location */
             int inside = 1;
-            for (int k = 0; k < 3; k++) {
-                double lo = fmin(o->p[k], o->p[3 + k]), hi = fmax(o->p[k], o->p[3 + k]);
-                inside = inside && desc->camera.location[k] >= lo && desc->camera.location[k] <= hi;
+            if (o->type == POV_OBJ_SPHERE) {
+                double dd = 0.0;
+                for (int k = 0; k < 3; k++)
+                    dd += (desc->camera.location[k] - o->p[k]) * (desc->camera.location[k] - o->p[k]);
+                inside = dd < o->p[3] * o->p[3];
+            } else {
+                for (int k = 0; k < 3; k++) {
+                    double lo = fmin(o->p[k], o->p[3 + k]), hi = fmax(o->p[k], o->p[3 + k]);
+                    inside = inside && desc->camera.location[k] >= lo && desc->camera.location[k] <= hi;
+                }
             }
             if (inside)
                 return POV_GPU_E_UNSUPPORTED;

@@ -630,7 +630,8 @@ struct PovGpuScene {
     int    media_sub = 0;   // largest sub-interval count
     int    media_levels = 0;   // largest AA_Level
     int    media_stamp = 0;    // marks the slots a chunk's samples fill
-    std::vector<double> h_container_boxes;   // corners of the media containers, 6 per box
+    std::vector<int32_t> h_containers;   // the media containers' object ids
+    std::vector<PovGpuObject> h_objects; // the scene's objects (the camera-inside tests of set_camera)
     // host copies of the id maps (prim -> flattened object id)
     std::vector<int32_t> h_sphere_obj, h_plane_obj, h_box_obj, h_torus_obj, h_tri_global, h_tri_local, h_tri_obj;
     std::vector<DevCsg> h_csgs;
@@ -773,6 +774,8 @@ bool is_container(const PovGpuObject& o) { return o.media > 0 && (o.flags & POV_
 // method 3 without jitter (Min_Samples = Max_Samples), the camera outside,
 // point lights only; no other surface transmits.  Marks the materials the
 // containers use in `cmat`.
+bool host_inside(const PovGpuSceneDesc* d, int i, const double* P);
+
 int validate_media(const PovGpuSceneDesc* d, std::vector<char>& cmat, int32_t* bad)
 {
     cmat.assign((size_t)d->num_materials, 0);
@@ -787,7 +790,8 @@ int validate_media(const PovGpuSceneDesc* d, std::vector<char>& cmat, int32_t* b
             continue;   // a transparent surface outside containers: validate_transparency
         if (bad) *bad = i;
         const PovGpuMedia* md = o.media > 0 ? &d->medias[o.media - 1] : nullptr;
-        if (!md || o.type != POV_OBJ_BOX || !(o.flags & POV_FLAG_HOLLOW) || o.parent >= 0 || !m ||
+        if (!md || (o.type != POV_OBJ_BOX && o.type != POV_OBJ_SPHERE) || (o.flags & POV_FLAG_INVERTED) ||
+            !(o.flags & POV_FLAG_HOLLOW) || o.parent >= 0 || !m ||
             m->pigment[3] != 0.0f || m->pigment[4] != 1.0f || m->diffuse != 0.0f || m->phong != 0.0f ||
             m->specular != 0.0f || m->emission[0] != 0.0f || m->emission[1] != 0.0f || m->emission[2] != 0.0f ||
             m->ambient[0] != 0.0f || m->ambient[1] != 0.0f || m->ambient[2] != 0.0f ||
@@ -797,11 +801,7 @@ int validate_media(const PovGpuSceneDesc* d, std::vector<char>& cmat, int32_t* b
             md->min_samples < 1 || md->aa_level < 1 || md->aa_level > MEDIA_MAX_AA_LEVEL || md->intervals < 1 ||
             md->intervals > MEDIA_MAX_INTERVALS || containers >= MAX_CONTAINERS)
             return POV_GPU_E_UNSUPPORTED;
-        bool cam_inside = true;
-        for (int k = 0; k < 3; k++)
-            cam_inside = cam_inside && d->camera.location[k] >= std::min(o.p[k], o.p[3 + k]) &&
-                         d->camera.location[k] <= std::max(o.p[k], o.p[3 + k]);
-        if (cam_inside)
+        if (host_inside(d, i, d->camera.location))
             return POV_GPU_E_UNSUPPORTED;   // camera rays would start inside the media
         cmat[o.material] = 1;
         containers++;
@@ -1111,7 +1111,8 @@ struct Builder {
         spheres.push_back(make_float4((float)o.p[0], (float)o.p[1], (float)o.p[2], (float)o.p[3]));
         spheres64.insert(spheres64.end(), {o.p[0], o.p[1], o.p[2], o.p[3]});
         sphere_obj.push_back(id);
-        sphere_flags.push_back(o.flags & POV_FLAG_INVERTED ? 1 : 0);
+        // bit 0 inverted; bit 1 (SPHERE_CONTAINER) the surface of a media container
+        sphere_flags.push_back((o.flags & POV_FLAG_INVERTED ? 1 : 0) | (is_container(o) ? SPHERE_CONTAINER : 0));
         if (box)
             for (int k = 0; k < 3; k++) {
                 box->lo[k] = std::min(box->lo[k], std::nextafter((float)(o.p[k] - o.p[3]), -INFINITY));
@@ -1837,20 +1838,23 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
     for (size_t c = 0; c < container_obj.size(); c++) {
         const PovGpuObject& o = d->objects[container_obj[c]];
         const PovGpuMedia& md = d->medias[o.media - 1];
+        // the container's primitive: a box or a sphere
+        const bool sphere = o.type == POV_OBJ_SPHERE;
         int box = -1;
-        for (size_t b = 0; b < B.box_obj.size(); b++)
-            if (B.box_obj[b] == container_obj[c])
+        const std::vector<int32_t>& owners = sphere ? B.sphere_obj : B.box_obj;
+        for (size_t b = 0; b < owners.size(); b++)
+            if (owners[b] == container_obj[c])
                 box = (int)b;
         if (box < 0)
             return POV_GPU_E_INVALID;
-        sc->h_container_boxes.insert(sc->h_container_boxes.end(), o.p, o.p + 6);
+        sc->h_containers.push_back(container_obj[c]);
         DevMedia& m = medias[c];
         m.emission = make_float4(md.emission[0], md.emission[1], md.emission[2], md.aa_threshold);
         bool scat = md.scattering[0] != 0.0f || md.scattering[1] != 0.0f || md.scattering[2] != 0.0f;
         m.scattering = make_float4(md.scattering[0], md.scattering[1], md.scattering[2], scat ? 1.0f : 0.0f);
         m.extinction = make_float4(md.extinction[0], md.extinction[1], md.extinction[2], 0.0f);
         m.n = make_int4(md.intervals, std::max((md.min_samples + 1) / 2, 1), md.aa_level, box);
-        m.phase = make_float4((float)md.scattering_type, md.eccentricity, 0.0f, 0.0f);
+        m.phase = make_float4((float)md.scattering_type, md.eccentricity, sphere ? 1.0f : 0.0f, 0.0f);
         media_ni = std::max(media_ni, md.intervals + 1);   // + the padding interval
         const int sub = m.n.y, T = (1 << md.aa_level) - 1;
         sc->media_smax = std::max(sc->media_smax, sub + 1 + sub * T);
@@ -1924,6 +1928,7 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
     for (size_t k = 0; k < B.tri_normal.size(); k++)
         sc->h_tri_obj[k] = __builtin_bit_cast(int32_t, B.tri_normal[k].w);
     sc->h_csgs = B.csgs;
+    sc->h_objects.assign(d->objects, d->objects + d->num_objects);
     sc->h_csg_children = B.csg_children;
 
     DeviceScene& S = sc->S;
@@ -3155,13 +3160,13 @@ int pov_gpu_set_camera(PovGpuScene* sc, const PovGpuCamera* cam, const double* l
     if (int bc = begin_call(sc))
         return bc;
     // camera rays start outside every media container
-    for (size_t c = 0; c + 6 <= sc->h_container_boxes.size(); c += 6) {
-        const double* b = &sc->h_container_boxes[c];
-        bool inside = true;
-        for (int k = 0; k < 3; k++)
-            inside = inside && loc[k] >= std::min(b[k], b[3 + k]) && loc[k] <= std::max(b[k], b[3 + k]);
-        if (inside)
-            return POV_GPU_E_UNSUPPORTED;
+    if (!sc->h_containers.empty()) {
+        PovGpuSceneDesc dd{};
+        dd.num_objects = (int32_t)sc->h_objects.size();
+        dd.objects = sc->h_objects.data();
+        for (int32_t c : sc->h_containers)
+            if (host_inside(&dd, c, loc))
+                return POV_GPU_E_UNSUPPORTED;
     }
     for (int k = 0; k < 3; k++) {
         sc->S.cam_loc[k] = loc[k];

@@ -173,10 +173,12 @@ struct __align__(16) DevMedia {
     float4 emission;     // rgb, AA_Threshold
     float4 scattering;   // rgb, 1 when any channel scatters
     float4 extinction;   // rgb (absorption + scattering), -
-    int4   n;            // Intervals, sub-intervals (Min_Samples+1)/2, AA_Level, box index
-    float4 phase;        // scattering type (1 isotropic .. 5 Henyey-Greenstein), eccentricity, -, -
+    int4   n;            // Intervals, sub-intervals (Min_Samples+1)/2, AA_Level, container primitive
+    float4 phase;        // scattering type (1 isotropic .. 5 Henyey-Greenstein), eccentricity,
+                         // container kind (0 box: n.w a box, 1 sphere: n.w a sphere), -
 };
 constexpr int BOX_CONTAINER = 2;         // DevBox flag: surface of a media container
+constexpr int SPHERE_CONTAINER = 2;      // sphere_flags bit: surface of a media container
 constexpr int OBJ_CONTAINER = 1 << 30;   // ObjectShade flag; container index in bits 16..23
 constexpr int MAX_CONTAINERS = 8;
 constexpr int MEDIA_MAX_INTERVALS = 32;  // Intervals the GPU path holds per ray segment

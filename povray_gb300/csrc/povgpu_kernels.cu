@@ -712,6 +712,10 @@ __device__ __forceinline__ bool prim_test(const DeviceScene& S, uint32_t ref, fl
         return false;
     }
     if (kind == PK_SPHERE) {
+        // a media container's surface passes light: shadow rays cross it
+        // (shadow_through counts and attenuates the crossings)
+        if (ANY && S.num_containers > 0 && (__ldg(S.sphere_flags + idx) & SPHERE_CONTAINER))
+            return false;
         float4 s = __ldg(S.spheres + idx);
         float t1, t2;
         if (!sphere_roots(s, o, d, t1, t2))
@@ -2142,7 +2146,7 @@ cudaError_t launch_fill_int(int* a, const int* count, int cap, int value, int gr
 // -- after which the shadow ray goes on from the wall.  A ray that was
 // inside the container has its light attenuated by the constant media of
 // the crossed segment, exp(-extinction * length), one media sample
-// (media.cpp:366-398).  Walls are found from the containers' boxes, opaque
+// (media.cpp:366-398).  Walls are found from the containers' shapes, opaque
 // blockers by an any-hit test of each segment between walls (the any-hit
 // test passes container walls).  Counts the tests, successes and media
 // samples; returns true when the light is blocked.
@@ -2158,8 +2162,12 @@ __device__ bool shadow_through(const DeviceScene& S, float3 P, float3 d, float t
     for (int c = 0; c < S.num_containers; c++) {
         float tb[2];
         int sn, sf;
-        if (!box_roots(S.boxes[S.medias[c].n.w], P, d, tb[0], tb[1], sn, sf))
+        if (S.medias[c].phase.z != 0.0f) {   // a sphere
+            if (!sphere_roots(__ldg(S.spheres + S.medias[c].n.w), P, d, tb[0], tb[1]))
+                continue;
+        } else if (!box_roots(S.boxes[S.medias[c].n.w], P, d, tb[0], tb[1], sn, sf)) {
             continue;
+        }
         for (int e = 0; e < 2; e++) {
             float t = tb[e];
             if (!(t > SMALL_TOLERANCE_F && t < tmax))

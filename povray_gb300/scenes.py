@@ -551,18 +551,24 @@ class Scene:
 
     def media_box(self, c1, c2, scattering=(0.05, 0.05, 0.05), absorption=(0.0, 0.0, 0.0),
                   emission=(0.0, 0.0, 0.0), intervals=10, samples=10, aa_level=3, aa_threshold=0.1,
-                  scattering_type=1, eccentricity=0.0):
+                  scattering_type=1, eccentricity=0.0, sphere=None):
         """A hollow, fully transmitting box holding one uniform media
         (Parse_Media defaults, source/parser/parser_materials.cpp:3500-3630:
         method 3, jitter 0; Media::PostProcess sets extinction = absorption +
         scattering).  scattering_type: 1 isotropic, 2 Mie hazy, 3 Mie murky,
-        4 Rayleigh, 5 Henyey-Greenstein with `eccentricity`."""
+        4 Rayleigh, 5 Henyey-Greenstein with `eccentricity`.  `sphere`
+        (centre, radius): a hollow sphere holds the media instead of the box
+        c1, c2."""
         mat = self.material(Material((1.0, 1.0, 1.0), ambient=0.0, diffuse=0.0, transmit=1.0))
         self.medias.append(dict(scattering=tuple(map(float, scattering)), absorption=tuple(map(float, absorption)),
                                 emission=tuple(map(float, emission)), intervals=int(intervals),
                                 samples=int(samples), aa_level=int(aa_level), aa_threshold=float(aa_threshold),
                                 scattering_type=int(scattering_type), eccentricity=float(eccentricity)))
-        node = self.n_box(c1, c2, mat)
+        if sphere is not None:   # a sphere container: centre, radius
+            node = dict(type=abi.POV_OBJ_SPHERE, centre=tuple(map(float, sphere[0])), radius=float(sphere[1]),
+                        material=mat, interior=None)
+        else:
+            node = self.n_box(c1, c2, mat)
         node["hollow"] = True
         node["media"] = len(self.medias)
         self.objects.append(node)
@@ -631,28 +637,33 @@ class Scene:
         r.update(self.radiosity or {})
         return r
 
+    def _media_sdl(self, o):
+        """`hollow` and the interior media of a container object."""
+        extra = ""
+        if o.get("hollow"):
+            extra += " hollow"
+        if o.get("media"):
+            md = self.medias[o["media"] - 1]
+            ecc = (" eccentricity %s" % _g(md["eccentricity"])) if md["scattering_type"] == 5 else ""
+            extra += (" interior { media { scattering { %d, rgb %s%s } absorption rgb %s emission rgb %s"
+                      " intervals %d samples %d aa_level %d aa_threshold %s } }"
+                      % (md["scattering_type"], _v(md["scattering"]), ecc, _v(md["absorption"]),
+                         _v(md["emission"]), md["intervals"], md["samples"], md["aa_level"], _g(md["aa_threshold"])))
+        return extra
+
     def _sdl_node(self, o):
         tex = (" " + self.materials[o["material"]].sdl()) if o.get("material", -1) >= 0 else ""
         if o.get("interior") is not None:
             tex += " " + o["interior"].sdl()
         t = o["type"]
         if t == abi.POV_OBJ_SPHERE:
-            return "sphere { %s, %s%s }" % (_v(o.get("sdl_centre", o["centre"])), _g(o["radius"]), tex)
+            return "sphere { %s, %s%s%s }" % (_v(o.get("sdl_centre", o["centre"])), _g(o["radius"]), tex,
+                                              self._media_sdl(o))
         if t == abi.POV_OBJ_PLANE:
             return "plane { %s, %s%s }" % (_v(o["normal"]), _g(o["offset"]), tex)
         if t == abi.POV_OBJ_BOX:
-            extra = ""
-            if o.get("hollow"):
-                extra += " hollow"
-            if o.get("media"):
-                md = self.medias[o["media"] - 1]
-                ecc = (" eccentricity %s" % _g(md["eccentricity"])) if md["scattering_type"] == 5 else ""
-                extra += (" interior { media { scattering { %d, rgb %s%s } absorption rgb %s emission rgb %s"
-                          " intervals %d samples %d aa_level %d aa_threshold %s } }"
-                          % (md["scattering_type"], _v(md["scattering"]), ecc, _v(md["absorption"]),
-                             _v(md["emission"]), md["intervals"], md["samples"], md["aa_level"],
-                             _g(md["aa_threshold"])))
-            return "box { %s, %s%s%s }" % (_v(o.get("sdl_c1", o["c1"])), _v(o.get("sdl_c2", o["c2"])), tex, extra)
+            return "box { %s, %s%s%s }" % (_v(o.get("sdl_c1", o["c1"])), _v(o.get("sdl_c2", o["c2"])), tex,
+                                           self._media_sdl(o))
         if t == abi.POV_OBJ_TORUS:
             return "torus { %s, %s %s%s }" % (_g(o["R"]), _g(o["r"]), o["mods"], tex)
         if t == abi.POV_OBJ_MESH:
@@ -1115,10 +1126,12 @@ def radiosity_room(width=1280, height=720, n_spheres=200, seed=4, radiosity=True
 
 
 def media_spheres(width=320, height=240, n_spheres=24, seed=5, intervals=10, samples=10, scattering=0.05,
-                  scattering_type=1, eccentricity=0.0, absorption=(0.0, 0.0, 0.0), emission=(0.0, 0.0, 0.0)):
+                  scattering_type=1, eccentricity=0.0, absorption=(0.0, 0.0, 0.0), emission=(0.0, 0.0, 0.0),
+                  container="box"):
     """A uniform scattering media box [-7,7]^3 (hollow, fully transmitting;
     scattering {1, rgb 0.05} -- or another scattering type, with its
-    eccentricity for Henyey-Greenstein, absorption and emission --,
+    eccentricity for Henyey-Greenstein, absorption and emission; with
+    container="sphere" a hollow sphere of radius 11 at the origin holds it --,
     intervals 10, samples 10, method 3) around
     `n_spheres` spheres r U[0.4,1.2], centres U[-5.5,5.5]^3, rgb U[0.2,0.9]^3
     (seed 5), every other one with reflection 0.2; plane y=-8; one point
@@ -1129,7 +1142,7 @@ def media_spheres(width=320, height=240, n_spheres=24, seed=5, intervals=10, sam
     s.point_light((20.0, 30.0, -20.0))
     s.media_box((-7.0, -7.0, -7.0), (7.0, 7.0, 7.0), scattering=(scattering,) * 3, intervals=intervals,
                 samples=samples, scattering_type=scattering_type, eccentricity=eccentricity, absorption=absorption,
-                emission=emission)
+                emission=emission, sphere=((0.0, 0.0, 0.0), 11.0) if container == "sphere" else None)
     for i in range(n_spheres):
         c = rng.uniform(-5.5, 5.5, size=3)
         r = rng.uniform(0.4, 1.2)

@@ -63,6 +63,8 @@ def cases():
         "media_murky_160x120": (scenes.media_spheres(160, 120, scattering_type=3), 4, 9.0),
         "media_rayleigh_160x120": (scenes.media_spheres(160, 120, scattering_type=4), 4, 9.0),
         "media_hg_160x120": (scenes.media_spheres(160, 120, scattering_type=5, eccentricity=0.6), 4, 9.0),
+        "media_sphere_160x120": (scenes.media_spheres(160, 120, container="sphere", scattering_type=5,
+                                                      eccentricity=-0.3), 4, 9.0),
         "media_glow_160x120": (scenes.media_spheres(160, 120, scattering=0.0, absorption=(0.06, 0.03, 0.01),
                                                     emission=(0.02, 0.01, 0.03)), 4, 9.0),
         "textured_spheres_160x120": (scenes.textured_spheres(160, 120), 2, 8.0),
@@ -255,7 +257,8 @@ def write_radiosity_cache_file(tmp, case="radiosity_room_160x90"):
 SCENE_FILE_CASES = ("spheres_plane_320x240", "mesh_spheres_small_160x90", "csg_torus_grid_160x90",
                     "area_room_160x90", "media_spheres_160x120", "radiosity_room_160x90",
                     "textured_spheres_160x120", "textured_turbulent_perlin_160x120", "bumpy_spheres_160x120",
-                    "bumpy_waves_160x120", "shaped_spheres_160x120", "glass_spheres_160x120")
+                    "bumpy_waves_160x120", "shaped_spheres_160x120", "glass_spheres_160x120",
+                    "media_sphere_160x120", "media_hg_160x120")
 
 
 def write_scene_files(tmp):
