@@ -47,14 +47,15 @@ class GpuScene:
             pass
 
     def trace_blocks(self, blocks, params=None, out=None):
-        """Traces `blocks` (list of (left, top, right, bottom, serial)).
+        """Traces `blocks` (list of (left, top, right, bottom, serial), or a
+        scenes.BlockBatch packed once).
 
         `out` may be None (a host array is returned), a host float32 array,
         or an integer device pointer (e.g. torch tensor .data_ptr()).
         Returns (rgbt or None, stats dict)."""
         p = params or self.scene.render_params()
-        arr = _scenes.block_array(blocks)
-        npix = sum((r - l + 1) * (b - t + 1) for (l, t, r, b, _s) in blocks)
+        bb = _scenes.block_batch(blocks)
+        arr, npix = bb.arr, bb.npix
         stats = abi.PovGpuStats()
         host = None
         if out is None:
@@ -66,7 +67,7 @@ class GpuScene:
             ptr = out.ctypes.data
         else:
             ptr = int(out)
-        st = self.lib.pov_gpu_trace_blocks(self.h, arr, len(blocks), C.byref(p), C.c_void_p(ptr),
+        st = self.lib.pov_gpu_trace_blocks(self.h, arr, len(bb), C.byref(p), C.c_void_p(ptr),
                                            C.byref(stats))
         _check(st, "pov_gpu_trace_blocks")
         return host, stats.as_dict()
@@ -75,9 +76,9 @@ class GpuScene:
         """RadiosityTask: empties the sample cache and runs every pretrace
         pass over `blocks`.  Returns the pass's stats dict."""
         p = params or self.scene.render_params()
-        arr = _scenes.block_array(blocks)
+        bb = _scenes.block_batch(blocks)
         stats = abi.PovGpuStats()
-        _check(self.lib.pov_gpu_radiosity_pretrace(self.h, arr, len(blocks), C.byref(p), C.byref(stats)),
+        _check(self.lib.pov_gpu_radiosity_pretrace(self.h, bb.arr, len(bb), C.byref(p), C.byref(stats)),
                "pov_gpu_radiosity_pretrace")
         return stats.as_dict()
 

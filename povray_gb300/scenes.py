@@ -885,11 +885,37 @@ def blocks_for(width, height, block=32):
     return out
 
 
+class BlockBatch:
+    """Render blocks packed once for the C ABI: the PovGpuBlock array
+    (`arr`, over a numpy buffer), the block list and the pixels it covers.
+    The render calls take one in place of a list, so a caller that traces
+    the same blocks every frame packs them once (the reference's render
+    task hands the library its C array the same way)."""
+
+    def __init__(self, blocks):
+        self.blocks = list(blocks)
+        buf = np.zeros((len(self.blocks), 6), dtype=np.int32)   # left, top, right, bottom, serial, reserved
+        if self.blocks:
+            buf[:, :5] = np.asarray(self.blocks, dtype=np.int64)
+        self._buf = buf
+        self.arr = (abi.PovGpuBlock * len(self.blocks)).from_buffer(buf)
+        w = buf[:, 2].astype(np.int64) - buf[:, 0] + 1
+        h = buf[:, 3].astype(np.int64) - buf[:, 1] + 1
+        self.npix = int((w * h).sum())
+
+    def __len__(self):
+        return len(self.blocks)
+
+    def __iter__(self):
+        return iter(self.blocks)
+
+
+def block_batch(blocks):
+    return blocks if isinstance(blocks, BlockBatch) else BlockBatch(blocks)
+
+
 def block_array(blocks):
-    arr = (abi.PovGpuBlock * len(blocks))()
-    for i, (l, t, r, b, s) in enumerate(blocks):
-        arr[i].left, arr[i].top, arr[i].right, arr[i].bottom, arr[i].serial = l, t, r, b, s
-    return arr
+    return block_batch(blocks).arr
 
 
 def unblock(rgbt, blocks, width, height):
