@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define POV_GPU_ABI_VERSION 2
+#define POV_GPU_ABI_VERSION 3
 
 /* ---- status codes ------------------------------------------------------- */
 #define POV_GPU_OK              0
@@ -229,10 +229,25 @@ typedef struct PovGpuNormal {
                                   form (p' = p * M)                           */
 } PovGpuNormal;
 
-/* Light source: point light or rectangular area light (LightSource,
- * source/core/scene/object.h:313). */
+/* Light source (LightSource, source/core/scene/object.h:313) as
+ * Parse_Light_Source leaves it (source/parser/parser.cpp:3345-3406):
+ * `kind` says whether it is a single point or a rectangular area grid,
+ * `light_type` is Light_Type (source/core/lighting/lightsource.h:78-81).
+ * The light ray and its attenuation follow ComputeOneWhiteLightRay
+ * (source/core/render/trace.cpp:2710-2766) and Attenuate_Light
+ * (source/core/lighting/lightsource.cpp:544-612): a spotlight's cone, a
+ * cylinder light's parallel beam, a parallel light's fixed direction and
+ * the fade with distance.  A shadowless light casts no shadow and adds no
+ * highlight (trace.cpp:1664-1714).  Area lights take the point and spot
+ * types, not parallel or cylinder beams; scenes with media containers take
+ * plain point lights only (the media's light intervals of spot and
+ * cylinder lights, media.cpp:715-750, are not built). */
 #define POV_LIGHT_POINT 0
 #define POV_LIGHT_AREA  1
+#define POV_LIGHT_TYPE_POINT      1   /* 0 reads as point too */
+#define POV_LIGHT_TYPE_SPOT       2
+#define POV_LIGHT_TYPE_SHADOWLESS 3   /* FILL_LIGHT_SOURCE */
+#define POV_LIGHT_TYPE_CYLINDER   4
 typedef struct PovGpuLight {
     double  center[3];
     float   colour[3];
@@ -245,8 +260,16 @@ typedef struct PovGpuLight {
     int32_t jitter;
     int32_t circular;
     int32_t orient;
-    float   fade_distance;
-    float   fade_power;
+    double  fade_distance;    /* Fade_Distance                                   */
+    double  fade_power;       /* Fade_Power (0: no fade with distance)           */
+    int32_t light_type;       /* POV_LIGHT_TYPE_*                                */
+    int32_t parallel;         /* Parallel (a cylinder light is always parallel)  */
+    double  points_at[3];     /* Points_At: the beam's direction is points_at - center */
+    double  radius;           /* Radius: spot, the cosine of the hotspot angle;
+                                 cylinder, the hotspot radius                    */
+    double  falloff;          /* Falloff: spot, the cosine of the falloff angle;
+                                 cylinder, the falloff radius                    */
+    double  tightness;        /* Coeff                                           */
 } PovGpuLight;
 
 /* mesh2 data as the parser reads it: vertex_vectors, normal_vectors and the

@@ -2337,10 +2337,103 @@ static double area_subset(const PovOracle* S, Thread* th, const PovGpuLight* L, 
     return (s[0] + s[1] + s[2] + s[3]) * 0.25;
 }
 
+/* LightSource::Direction (parser.cpp:3521-3528): points_at - center, unit
+ * length unless shorter than EPSILON. */
+static V3 light_direction(const PovGpuLight* L)
+{
+    V3 d = vsub(vload(L->points_at), vload(L->center));
+    double len = vlen(d);
+    return len > EPSILON ? vdiv(d, len) : d;
+}
+
+/* ComputeOneWhiteLightRay (trace.cpp:2710-2766) without jitter: the unit
+ * direction from P towards the light and the distance along it.  A
+ * cylinder light's rays run parallel to its axis, their length the
+ * projection of P's offset on it; a parallel light's rays all take the
+ * light's direction, reversed, their length scaled by the cosine. */
+static void light_ray(const PovGpuLight* L, V3 P, V3* dir, double* depth)
+{
+    V3 C = vload(L->center);
+    if (L->light_type == POV_LIGHT_TYPE_CYLINDER) {
+        V3 d = vsub(C, vload(L->points_at));
+        double len = vlen(d);
+        *depth = vdot(vsub(C, P), d) / len;
+        *dir = vnorm(d);
+    } else {
+        V3 d = vsub(C, P);
+        *depth = vlen(d);
+        *dir = vdiv(d, *depth);
+    }
+    if (L->parallel) {
+        V3 ldir = light_direction(L);
+        *depth *= -vdot(ldir, *dir);
+        *dir = vmul(ldir, -1.0);
+    }
+}
+
+/* cubic_spline (lightsource.cpp:497-514). */
+static double cubic_spline(double low, double high, double pos)
+{
+    if (pos < low)
+        return 0.0;
+    if (pos >= high)
+        return 1.0;
+    pos = (pos - low) / (high - low);
+    return (3 - 2 * pos) * pos * pos;
+}
+
+/* Attenuate_Light (lightsource.cpp:544-632): a spotlight's cone, a cylinder
+ * light's beam, then the fade with distance.  `P` is the light ray's
+ * origin, `dir` and `depth` its direction and length. */
+static double attenuate_light(const PovGpuLight* L, V3 P, V3 dir, double depth)
+{
+    double att = 1.0;
+    if (L->light_type == POV_LIGHT_TYPE_SPOT) {
+        double costheta = vdot(dir, light_direction(L));
+        if (depth > 0.0)
+            costheta = -costheta;
+        if (costheta <= 0.0)
+            return 0.0;
+        att = pow(costheta, L->tightness);
+        if (L->radius > 0.0 && costheta < L->radius)
+            att *= cubic_spline(L->falloff, L->radius, costheta);
+    } else if (L->light_type == POV_LIGHT_TYPE_CYLINDER) {
+        V3 ldir = light_direction(L);
+        V3 v1 = vsub(P, vload(L->center));
+        double k = vdot(v1, ldir);
+        if (k <= 0.0)
+            return 0.0;
+        double len = vlen(vsub(v1, vmul(ldir, k)));
+        if (len >= L->falloff)
+            return 0.0;
+        double dist = 1.0 - len / L->falloff;
+        att = pow(dist, L->tightness);
+        if (L->radius > 0.0 && len > L->radius)
+            att *= cubic_spline(0.0, 1.0 - L->radius / L->falloff, dist);
+    }
+    if (att > 0.0 && L->fade_power > 0.0) {
+        if (fabs(L->fade_distance) >= EPSILON)
+            att *= 2.0 / (1.0 + pow(depth / L->fade_distance, L->fade_power));
+        else
+            att *= pow(depth, -L->fade_power);
+    }
+    return att;
+}
+
+/* ComputeOneLightRay (trace.cpp:1873-1889): the light ray and the light's
+ * colour attenuated along it (MathColour *= double: float channels). */
+static void one_light_ray(const PovGpuLight* L, V3 P, V3* dir, double* depth, double lc[3])
+{
+    light_ray(L, P, dir, depth);
+    const double att = attenuate_light(L, P, *dir, *depth);
+    for (int k = 0; k < 3; k++)
+        lc[k] = (float)(L->colour[k] * att);
+}
+
 /* TraceAreaLightShadowRay (trace.cpp:2078-2129): axes (oriented towards P
  * when `orient`), all grid points invalid, then the whole grid as one
  * region. */
-static double area_light_fraction(const PovOracle* S, Thread* th, const PovGpuLight* L, V3 P)
+static double area_light_fraction(const PovOracle* S, Thread* th, const PovGpuLight* L, V3 P, const double lc[3])
 {
     signed char grid[AREA_MAX_POINTS];
     int npts = L->area_size1 * L->area_size2;
@@ -2356,7 +2449,8 @@ static double area_light_fraction(const PovOracle* S, Thread* th, const PovGpuLi
         a1 = vmul(a1, len1);
         a2 = vmul(a2, len1);
     }
-    float lc_dist = fabsf(L->colour[0]) + fabsf(L->colour[1]) + fabsf(L->colour[2]);
+    /* the samples are the attenuated light colour or black */
+    float lc_dist = fabsf((float)lc[0]) + fabsf((float)lc[1]) + fabsf((float)lc[2]);
     return area_subset(S, th, L, P, a1, a2, grid, 0, 0, L->area_size1 - 1, L->area_size2 - 1, 0, lc_dist);
 }
 
@@ -2565,26 +2659,27 @@ static void shade(const PovOracle* S, Thread* th, const Isect* is, V3 D, double 
     if (m->diffuse != 0.0f || m->diffuse_back != 0.0f || m->specular != 0.0f || m->phong != 0.0f) {
         for (int li = 0; li < S->nlights; li++) {
             const PovGpuLight* L = &S->lights[li];
-            V3 C = vload(L->center);
-            V3 ld = vsub(C, ip);
-            double ldist = vlen(ld);
-            ld = vdiv(ld, ldist);
-            double lc[3] = {L->colour[0], L->colour[1], L->colour[2]};
+            V3 ld;
+            double ldist, lc[3];
+            one_light_ray(L, ip, &ld, &ldist, lc);
             if (fabs(lc[0]) < EPSILON && fabs(lc[1]) < EPSILON && fabs(lc[2]) < EPSILON)
-                continue;
+                continue;   /* outside a spotlight's cone (trace.cpp:1648-1650) */
             if (!(o->flags & POV_FLAG_DOUBLE_ILLUM)) {
                 double cs = vdot(N, ld);
                 if (cs < EPSILON)
                     continue;
             }
-            if (level > tk->max_level)   /* TraceShadowRay level check (trace.cpp:1897-1901) */
+            const int fill = L->light_type == POV_LIGHT_TYPE_SHADOWLESS;
+            /* TraceShadowRay level check (trace.cpp:1897-1901); a shadowless
+             * light traces no shadow ray (trace.cpp:1664) */
+            if (!fill && level > tk->max_level)
                 continue;
-            {
+            if (!fill) {
                 /* the radiosity Trace runs with areaLights off
                  * (GetRadiosityQualityFlags, radiosity.cpp:148-161): inside a
                  * gather an area light casts its centre's shadow */
                 if (L->kind == POV_LIGHT_AREA && tk->rad_depth == 0) {
-                    double f = area_light_fraction(S, th, L, ip);
+                    double f = area_light_fraction(S, th, L, ip, lc);
                     if (f == 0.0)
                         continue;
                     for (int k = 0; k < 3; k++)
@@ -2607,8 +2702,9 @@ static void shade(const PovOracle* S, Thread* th, const Isect* is, V3 D, double 
                 g += inten * pig.g * lc[1];
                 b += inten * pig.b * lc[2];
             }
-            /* ComputePhongColour (trace.cpp:2520-2558); not for radiosity rays */
-            if (m->phong > 0.0f && !(flags & RAY_RADIOSITY)) {
+            /* ComputePhongColour (trace.cpp:2520-2558); not for radiosity
+             * rays nor shadowless lights (trace.cpp:1714) */
+            if (m->phong > 0.0f && !(flags & RAY_RADIOSITY) && !fill) {
                 double c2 = -2.0 * vdot(D, N);
                 V3 rd = vadd(D, vmul(N, c2));
                 double ci = vdot(rd, ld);
@@ -2619,8 +2715,9 @@ static void shade(const PovOracle* S, Thread* th, const Isect* is, V3 D, double 
                     b += inten * lc[2];
                 }
             }
-            /* ComputeSpecularColour (trace.cpp:2560-2593); not for radiosity rays */
-            if (m->specular > 0.0f && !(flags & RAY_RADIOSITY)) {
+            /* ComputeSpecularColour (trace.cpp:2560-2593); not for radiosity
+             * rays nor shadowless lights */
+            if (m->specular > 0.0f && !(flags & RAY_RADIOSITY) && !fill) {
                 V3 half = vmul(vadd(vmul(D, -1.0), ld), 0.5);
                 double hl = vlen(half);
                 if (hl > 0.0) {
@@ -3670,8 +3767,17 @@ int pov_oracle_create(const PovGpuSceneDesc* desc, PovOracle** out, int32_t* bad
     }
     for (int i = 0; i < desc->num_lights; i++) {
         const PovGpuLight* L = &desc->lights[i];
-        if (containers && L->kind != POV_LIGHT_POINT)
-            return POV_GPU_E_UNSUPPORTED;   /* media samples test point-light shadows only */
+        if ((L->kind != POV_LIGHT_POINT && L->kind != POV_LIGHT_AREA) || L->light_type < 0 ||
+            L->light_type > POV_LIGHT_TYPE_CYLINDER)
+            return POV_GPU_E_INVALID;
+        const int plain = L->light_type <= POV_LIGHT_TYPE_POINT && !L->parallel && L->fade_power <= 0.0;
+        if (containers && (L->kind != POV_LIGHT_POINT || !plain))
+            return POV_GPU_E_UNSUPPORTED;   /* media samples test plain point-light shadows only */
+        if (L->kind == POV_LIGHT_AREA && (L->parallel || L->light_type == POV_LIGHT_TYPE_CYLINDER))
+            return POV_GPU_E_UNSUPPORTED;   /* area lights: no parallel beams */
+        if ((L->light_type == POV_LIGHT_TYPE_SPOT || L->light_type == POV_LIGHT_TYPE_CYLINDER || L->parallel) &&
+            !(vlen(vsub(vload(L->points_at), vload(L->center))) > EPSILON))
+            return POV_GPU_E_UNSUPPORTED;   /* a beam needs its direction */
         if (L->kind == POV_LIGHT_AREA &&
             (L->area_size1 < 1 || L->area_size2 < 1 || L->area_size1 * L->area_size2 > AREA_MAX_POINTS ||
              L->jitter || (L->circular && (L->area_size1 < 2 || L->area_size2 < 2))))

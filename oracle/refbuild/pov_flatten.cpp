@@ -515,7 +515,9 @@ bool FlattenScene(const SceneData& sd, FlatScene& out, std::string& why)
     // light sources (LightSource, source/core/scene/object.h:313-351)
     for (const LightSource* l : sd.lightSources)
     {
-        if (l->Light_Type != POINT_SOURCE || l->Parallel || l->Projected_Through_Object != nullptr)
+        if (l->Projected_Through_Object != nullptr || l->Use_Full_Area_Lighting || l->Media_Attenuation ||
+            (l->Light_Type != POINT_SOURCE && l->Light_Type != SPOT_SOURCE && l->Light_Type != FILL_LIGHT_SOURCE &&
+             l->Light_Type != CYLINDER_SOURCE))
         {
             why = "light source of a kind the GPU path does not take";
             return false;
@@ -538,8 +540,15 @@ bool FlattenScene(const SceneData& sd, FlatScene& out, std::string& why)
             g.circular = l->Circular ? 1 : 0;
             g.orient = l->Orient ? 1 : 0;
         }
-        g.fade_distance = (float)l->Fade_Distance;
-        g.fade_power = (float)l->Fade_Power;
+        g.fade_distance = l->Fade_Distance;
+        g.fade_power = l->Fade_Power;
+        // Light_Type numbers are the ABI's (lightsource.h:78-81)
+        g.light_type = l->Light_Type;
+        g.parallel = l->Parallel ? 1 : 0;
+        Copy3(g.points_at, l->Points_At);
+        g.radius = l->Radius;
+        g.falloff = l->Falloff;
+        g.tightness = l->Coeff;
         out.lights.push_back(g);
     }
     PovGpuSceneDesc& d = out.desc;

@@ -9,7 +9,7 @@ import os
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "lib", "libpovgpu.so")
 
-POV_GPU_ABI_VERSION = 2
+POV_GPU_ABI_VERSION = 3
 
 POV_GPU_OK = 0
 POV_GPU_E_INVALID = -1
@@ -43,6 +43,10 @@ POV_FLAG_HOLLOW = 0x0080
 
 POV_LIGHT_POINT = 0
 POV_LIGHT_AREA = 1
+POV_LIGHT_TYPE_POINT = 1
+POV_LIGHT_TYPE_SPOT = 2
+POV_LIGHT_TYPE_SHADOWLESS = 3
+POV_LIGHT_TYPE_CYLINDER = 4
 
 
 class PovGpuObject(C.Structure):
@@ -110,7 +114,9 @@ class PovGpuLight(C.Structure):
                 ("area_size1", C.c_int32), ("area_size2", C.c_int32),
                 ("adaptive_level", C.c_int32), ("jitter", C.c_int32),
                 ("circular", C.c_int32), ("orient", C.c_int32),
-                ("fade_distance", C.c_float), ("fade_power", C.c_float)]
+                ("fade_distance", C.c_double), ("fade_power", C.c_double),
+                ("light_type", C.c_int32), ("parallel", C.c_int32), ("points_at", C.c_double * 3),
+                ("radius", C.c_double), ("falloff", C.c_double), ("tightness", C.c_double)]
 
 
 class PovGpuNormal(C.Structure):

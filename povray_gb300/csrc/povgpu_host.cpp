@@ -809,9 +809,11 @@ int validate_media(const PovGpuSceneDesc* d, std::vector<char>& cmat, int32_t* b
     if (bad) *bad = -1;
     if (containers > 0 && d->max_trace_level > 255)
         return POV_GPU_E_UNSUPPORTED;   // a ray's level is held in 8 bits of its state
-    for (int i = 0; containers > 0 && i < d->num_lights; i++)
-        if (d->lights[i].kind != POV_LIGHT_POINT)
-            return POV_GPU_E_UNSUPPORTED;   // media samples test point-light shadows only
+    for (int i = 0; containers > 0 && i < d->num_lights; i++) {
+        const PovGpuLight& L = d->lights[i];
+        if (L.kind != POV_LIGHT_POINT || L.light_type > POV_LIGHT_TYPE_POINT || L.parallel || L.fade_power > 0.0)
+            return POV_GPU_E_UNSUPPORTED;   // media samples test plain point-light shadows only
+    }
     return POV_GPU_OK;
 }
 
@@ -933,7 +935,17 @@ int validate(const PovGpuSceneDesc* d, int32_t* bad)
     }
     for (int i = 0; i < d->num_lights; i++) {
         const PovGpuLight& L = d->lights[i];
-        if ((L.kind != POV_LIGHT_POINT && L.kind != POV_LIGHT_AREA) || L.fade_power > 0.0f)
+        if ((L.kind != POV_LIGHT_POINT && L.kind != POV_LIGHT_AREA) || L.light_type < 0 ||
+            L.light_type > POV_LIGHT_TYPE_CYLINDER)
+            return POV_GPU_E_INVALID;
+        // a beam (spot, cylinder, parallel) needs its direction; area lights
+        // take no parallel beams
+        const double dx = L.points_at[0] - L.center[0], dy = L.points_at[1] - L.center[1],
+                     dz = L.points_at[2] - L.center[2];
+        const bool beam = L.light_type == POV_LIGHT_TYPE_SPOT || L.light_type == POV_LIGHT_TYPE_CYLINDER || L.parallel;
+        if (beam && !(std::sqrt(dx * dx + dy * dy + dz * dz) > 1.0e-10))
+            return POV_GPU_E_UNSUPPORTED;
+        if (L.kind == POV_LIGHT_AREA && (L.parallel || L.light_type == POV_LIGHT_TYPE_CYLINDER))
             return POV_GPU_E_UNSUPPORTED;
         // area lights: the grid fits the per-point visibility masks; jitter
         // draws on the reference's random stream and is not restated
@@ -1795,6 +1807,17 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
         lights[i].axis2 = make_float4((float)L.axis2[0], (float)L.axis2[1], (float)L.axis2[2], 0.f);
         lights[i].area = make_int4(L.area_size1, L.area_size2, L.adaptive_level,
                                    (L.circular ? 1 : 0) | (L.orient ? 2 : 0));
+        // Direction (Parse_Light_Source, parser.cpp:3521-3528)
+        double dv[3] = {L.points_at[0] - L.center[0], L.points_at[1] - L.center[1], L.points_at[2] - L.center[2]};
+        double dl = std::sqrt(dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
+        if (dl > 1.0e-10)
+            for (double& x : dv)
+                x /= dl;
+        const int type = L.light_type == 0 ? LIGHT_POINT : L.light_type;
+        lights[i].dir = make_float4((float)dv[0], (float)dv[1], (float)dv[2], (float)type);
+        const bool parallel = L.parallel || type == LIGHT_CYLINDER;
+        lights[i].beam = make_float4((float)L.radius, (float)L.falloff, (float)L.tightness, parallel ? 1.f : 0.f);
+        lights[i].fade = make_float4((float)L.fade_distance, (float)L.fade_power, 0.f, 0.f);
         if (L.kind == POV_LIGHT_AREA)
             num_area++;
     }

@@ -123,7 +123,11 @@ struct __align__(16) DevLight {
     float4 axis1;           // area light: Axis1 xyz, |Axis1|
     float4 axis2;           // area light: Axis2 xyz, -
     int4   area;            // Area_Size1, Area_Size2, Adaptive_Level, bit0 Circular | bit1 Orient
+    float4 dir;             // Direction (unit, points_at - center) xyz, w = Light_Type (LIGHT_*)
+    float4 beam;            // Radius, Falloff, Coeff (tightness), Parallel (0 / 1)
+    float4 fade;            // Fade_Distance, Fade_Power, -, -
 };
+constexpr int LIGHT_POINT = 1, LIGHT_SPOT = 2, LIGHT_SHADOWLESS = 3, LIGHT_CYLINDER = 4;
 constexpr int AREA_MAX_POINTS = 64;   // area-light grid points the GPU path holds per shading point
 
 struct __align__(16) DevMesh {

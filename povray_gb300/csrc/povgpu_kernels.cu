@@ -1568,6 +1568,73 @@ __device__ __forceinline__ float3 interior_fade(float4 I0, float4 I1, float dept
     return f3(I1.x + (1.0f - I1.x) * q, I1.y + (1.0f - I1.y) * q, I1.z + (1.0f - I1.z) * q);
 }
 
+// ComputeOneWhiteLightRay (trace.cpp:2710-2766) without jitter: the unit
+// direction from p towards the light and the distance along it.  A parallel
+// beam (a cylinder light, or a light marked parallel) runs against the
+// light's direction, its length the projection of the offset to the centre
+// on it (the reference's cosine-scaled distance, folded).
+__device__ __forceinline__ void light_ray(const DevLight& L, float3 p, float3& ld, float& ldist)
+{
+    const float3 lv = xyz(L.center) - p;
+    if (L.beam.w != 0.0f) {
+        ld = f3(-L.dir.x, -L.dir.y, -L.dir.z);
+        ldist = dot3(lv, ld);
+    } else {
+        ldist = sqrtf(dot3(lv, lv));
+        ld = lv * (1.0f / ldist);
+    }
+}
+
+// cubic_spline (lightsource.cpp:497-514).
+__device__ __forceinline__ float light_spline(float low, float high, float pos)
+{
+    if (pos < low)
+        return 0.0f;
+    if (pos >= high)
+        return 1.0f;
+    pos = (pos - low) / (high - low);
+    return (3.0f - 2.0f * pos) * pos * pos;
+}
+
+// Attenuate_Light (lightsource.cpp:544-632) of the light ray from p: a
+// spotlight's cone, a cylinder light's beam, then the fade with distance.
+__device__ __forceinline__ float attenuate_light(const DevLight& L, float3 p, float3 ld, float ldist)
+{
+    const int type = (int)L.dir.w;
+    const float3 dir = xyz(L.dir);
+    float att = 1.0f;
+    if (type == LIGHT_SPOT) {
+        float ct = dot3(ld, dir);
+        if (ldist > 0.0f)
+            ct = -ct;
+        if (ct <= 0.0f)
+            return 0.0f;
+        att = powf(ct, L.beam.z);
+        if (L.beam.x > 0.0f && ct < L.beam.x)
+            att *= light_spline(L.beam.y, L.beam.x, ct);
+    } else if (type == LIGHT_CYLINDER) {
+        const float3 v1 = p - xyz(L.center);
+        const float k = dot3(v1, dir);
+        if (k <= 0.0f)
+            return 0.0f;
+        const float3 off = v1 - dir * k;
+        const float len = sqrtf(dot3(off, off));
+        if (len >= L.beam.y)
+            return 0.0f;
+        const float dist = 1.0f - len / L.beam.y;
+        att = powf(dist, L.beam.z);
+        if (L.beam.x > 0.0f && len > L.beam.x)
+            att *= light_spline(0.0f, 1.0f - L.beam.x / L.beam.y, dist);
+    }
+    if (att > 0.0f && L.fade.y > 0.0f) {
+        if (fabsf(L.fade.x) >= EPSILON_F)
+            att *= 2.0f / (1.0f + powf(ldist / L.fade.x, L.fade.y));
+        else
+            att *= powf(ldist, -L.fade.y);
+    }
+    return att;
+}
+
 // One thread per ray of the level queue.  Emits shadow rays (one per lit
 // light, slot = ray*num_lights+light) and the one secondary ray of the hit:
 // the reflection ray, the continued ray through a media container's wall,
@@ -1678,19 +1745,19 @@ __global__ void __launch_bounds__(128) k_shade(
             bool emit = false;
             float3 contrib = f3(0.f, 0.f, 0.f);
             float3 ld = f3(0.f, 0.f, 1.f);
-            float ldist = 0.f;
-            bool area = false;
+            float ldist = 0.f, latt = 1.f;
+            bool area = false, fill = false;
             if (shaded) {
                 const DevLight& L = S.lights[l];
                 // the radiosity Trace runs with area lights off
                 // (GetRadiosityQualityFlags, radiosity.cpp:148-161)
                 area = L.center.w != 0.0f && !rad.gather;   // POV_LIGHT_AREA
-                float3 lv = xyz(L.center) - p;
-                ldist = sqrtf(dot3(lv, lv));
-                ld = lv * (1.0f / ldist);
+                fill = L.dir.w == (float)LIGHT_SHADOWLESS;
+                light_ray(L, p, ld, ldist);
+                latt = attenuate_light(L, p, ld, ldist);
                 float cs = dot3(N, ld);
                 bool lit = (oflags & 16) || cs >= EPSILON_F;
-                float3 lc = xyz(L.colour);
+                float3 lc = xyz(L.colour) * latt;
                 if (lit && !(fabsf(lc.x) < EPSILON_F && fabsf(lc.y) < EPSILON_F && fabsf(lc.z) < EPSILON_F)) {
                     emit = true;
                     float3 pig = pigc;
@@ -1699,14 +1766,15 @@ __global__ void __launch_bounds__(128) k_shade(
                         inten *= m->diffuse * m->opacity;
                         contrib = contrib + pig * lc * inten;
                     }
-                    if (m->phong > 0.0f && !rad.gather) {     // ComputePhongColour, trace.cpp:2520-2558
+                    // no highlights for radiosity rays nor shadowless lights (trace.cpp:1714)
+                    if (m->phong > 0.0f && !rad.gather && !fill) {     // ComputePhongColour, trace.cpp:2520-2558
                         float c2 = -2.0f * dot3(d, N);
                         float3 rd = d + N * c2;
                         float ci = dot3(rd, ld);
                         if (ci > 0.0f && (m->phong_size < 60.0f || ci > 0.0008f))
                             contrib = contrib + lc * (m->phong * powf(ci, m->phong_size));
                     }
-                    if (m->specular > 0.0f && !rad.gather) {  // ComputeSpecularColour, trace.cpp:2560-2593
+                    if (m->specular > 0.0f && !rad.gather && !fill) {  // ComputeSpecularColour, trace.cpp:2560-2593
                         float3 half = (ld - d) * 0.5f;
                         float hl = sqrtf(dot3(half, half));
                         if (hl > 0.0f) {
@@ -1718,13 +1786,15 @@ __global__ void __launch_bounds__(128) k_shade(
                 }
             }
             // point lights: one shadow ray; area lights: one item for the
-            // subdivision kernel (TraceAreaLightShadowRay)
-            int aslot = warp_reserve(aq_count, emit && area, mask);
-            if (emit && area) {
+            // subdivision kernel (TraceAreaLightShadowRay), which gets the
+            // light's attenuation in dir.w; shadowless lights: none
+            // (trace.cpp:1664)
+            int aslot = warp_reserve(aq_count, emit && area && !fill, mask);
+            if (emit && area && !fill) {
                 if (aslot < max_area) {
                     QRay ar;
                     ar.org = make_float4(p.x, p.y, p.z, __uint_as_float(__float_as_uint(SMALL_TOLERANCE_F) + 1u));
-                    ar.dir = make_float4(0.f, 0.f, 0.f, 0.f);
+                    ar.dir = make_float4(0.f, 0.f, 0.f, latt);
                     aq[aslot] = ar;
                     aq_slot[aslot] = i * nl + l;
                     aq_skip[aslot] = self;
@@ -1732,8 +1802,8 @@ __global__ void __launch_bounds__(128) k_shade(
                     set_error(err, DE_QUEUE_OVERFLOW);
                 }
             }
-            int slot = warp_reserve(sq_count, emit && !area, mask);
-            if (emit && !area) {
+            int slot = warp_reserve(sq_count, emit && !area && !fill, mask);
+            if (emit && !area && !fill) {
                 if (slot < max_shadow) {
                     QRay sr;
                     sr.org = make_float4(p.x, p.y, p.z, __uint_as_float(__float_as_uint(SMALL_TOLERANCE_F) + 1u));
@@ -2023,7 +2093,7 @@ __global__ void __launch_bounds__(128) k_area_shadow(DeviceScene S, const QRay* 
             a1 = a1 * L.axis1.w;
             a2 = a2 * L.axis1.w;
         }
-        const float3 lc = xyz(L.colour);
+        const float3 lc = xyz(L.colour) * it.dir.w;   // attenuated by the light's cone and fade
         const bool far_apart = fabsf(lc.x) + fabsf(lc.y) + fabsf(lc.z) > 0.1f;   // ColourDistance of lit vs black
         unsigned long long traced = 0, visible = 0;
         // region: u1 | v1 << 6 | u2 << 12 | v2 << 18 | level << 24

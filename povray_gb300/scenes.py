@@ -577,6 +577,80 @@ class Scene:
         self.lights.append(dict(kind=abi.POV_LIGHT_POINT, pos=tuple(map(float, pos)),
                                 rgb=tuple(map(float, rgb))))
 
+    def light(self, pos, rgb=(1.0, 1.0, 1.0), beam=None, point_at=None, radius=None, falloff=None,
+              tightness=None, parallel=False, shadowless=False, fade_distance=None, fade_power=None):
+        """light_source with the modifiers of Parse_Light_Source
+        (source/parser/parser.cpp:3345-3406), written in this order: `beam`
+        "spotlight" or "cylinder" (their defaults: radius 30 / falloff 45
+        degrees, tightness 0; radius 0.75, falloff 1, tightness 0 and
+        parallel), radius, falloff, tightness, parallel, point_at,
+        shadowless (which makes the light a fill light whatever came
+        before), fade_distance, fade_power.  A spotlight's radius and
+        falloff are angles in degrees, a cylinder's lengths."""
+        l = dict(kind=abi.POV_LIGHT_POINT, pos=tuple(map(float, pos)), rgb=tuple(map(float, rgb)),
+                 beam=beam, point_at=None if point_at is None else tuple(map(float, point_at)),
+                 radius=radius, falloff=falloff, tightness=tightness, parallel=bool(parallel),
+                 shadowless=bool(shadowless), fade_distance=fade_distance, fade_power=fade_power)
+        if beam not in (None, "spotlight", "cylinder"):
+            raise ValueError("beam: None, 'spotlight' or 'cylinder'")
+        self.lights.append(l)
+        return l
+
+    @staticmethod
+    def _light_fields(l):
+        """The LightSource fields the parser leaves for light dict `l`
+        (Parse_Light_Source, LightSource::LightSource defaults,
+        lightsource.cpp:355-400): light_type, parallel, points_at, radius,
+        falloff, tightness, fade_distance, fade_power."""
+        f = dict(light_type=1, parallel=False, points_at=(0.0, 0.0, 1.0), radius=0.0, falloff=0.0,
+                 tightness=0.0, fade_distance=0.0, fade_power=0.0)
+        deg = 0.01745329251994329576   # M_PI_180
+        if l.get("beam") == "spotlight":
+            f.update(light_type=2, radius=math.cos(30 * deg), falloff=math.cos(45 * deg))
+        elif l.get("beam") == "cylinder":
+            f.update(light_type=4, radius=0.75, falloff=1.0, parallel=True)
+        spot = f["light_type"] == 2
+        if l.get("radius") is not None:
+            f["radius"] = math.cos(float(l["radius"]) * deg) if spot else float(l["radius"])
+        if l.get("falloff") is not None:
+            f["falloff"] = math.cos(float(l["falloff"]) * deg) if spot else float(l["falloff"])
+        if l.get("tightness") is not None:
+            f["tightness"] = float(l["tightness"])
+        if l.get("point_at") is not None:
+            f["points_at"] = l["point_at"]
+        if l.get("parallel"):
+            f["parallel"] = True
+        if l.get("shadowless"):
+            f["light_type"] = 3
+        if l.get("fade_distance") is not None:
+            f["fade_distance"] = float(l["fade_distance"])
+        if l.get("fade_power") is not None:
+            f["fade_power"] = float(l["fade_power"])
+        # legacy (pre-3.8) scenes ignore fade_power without fade_distance
+        # (parser.cpp:3508-3513); the SDL here is #version 3.7
+        if f["fade_power"] != 0 and abs(f["fade_distance"]) < 1e-10:
+            f["fade_power"] = f["fade_distance"] = 0.0
+        return f
+
+    @staticmethod
+    def _light_sdl(l):
+        out = ""
+        if l.get("beam") is not None:
+            out += " " + l["beam"]
+        for key in ("radius", "falloff", "tightness"):
+            if l.get(key) is not None:
+                out += " %s %s" % (key, _g(l[key]))
+        if l.get("parallel"):
+            out += " parallel"
+        if l.get("point_at") is not None:   # after spotlight, cylinder or parallel (parser.cpp:3368-3377)
+            out += " point_at %s" % _v(l["point_at"])
+        if l.get("shadowless"):
+            out += " shadowless"
+        for key in ("fade_distance", "fade_power"):
+            if l.get(key) is not None:
+                out += " %s %s" % (key, _g(l[key]))
+        return out
+
     def area_light(self, pos, axis1, axis2, size1, size2, rgb=(1.0, 1.0, 1.0), adaptive=None,
                    circular=False, orient=False):
         """light_source with area_light (Parse_Light_Source,
@@ -623,6 +697,7 @@ class Scene:
                     extra += " circular"
                 if l["orient"]:
                     extra += " orient"
+            extra += self._light_sdl(l)
             out.append("light_source { %s color rgb %s%s }\n" % (_v(l["pos"]), _v(l["rgb"]), extra))
         for o in self.objects:
             out.append(self._sdl_node(o) + "\n")
@@ -751,6 +826,12 @@ class Scene:
                     lights[i].adaptive_level = int(l["adaptive"])
                 lights[i].circular = int(l["circular"])
                 lights[i].orient = int(l["orient"])
+            f = self._light_fields(l)
+            lights[i].light_type = f["light_type"]
+            lights[i].parallel = int(f["parallel"])
+            lights[i].points_at[:] = list(f["points_at"])
+            lights[i].radius, lights[i].falloff, lights[i].tightness = f["radius"], f["falloff"], f["tightness"]
+            lights[i].fade_distance, lights[i].fade_power = f["fade_distance"], f["fade_power"]
         meshes = (abi.PovGpuMesh * max(len(self.meshes), 1))()
         for i, m in enumerate(self.meshes):
             meshes[i].vertices = m.vertices.ctypes.data_as(C.POINTER(C.c_float))
@@ -1222,6 +1303,38 @@ def textured_spheres(width=320, height=240, n_spheres=12, seed=6, noise_generato
         c = (rng.uniform(-3.0, 3.0), rng.uniform(-1.0, 1.5), rng.uniform(0.0, 6.0))
         r = rng.uniform(0.5, 1.2)
         s.sphere(c, r, s.material(Material((1.0, 1.0, 1.0), phong=0.3, pattern=kinds[i % len(kinds)])))
+    return s
+
+
+def light_types(width=320, height=240, seed=7):
+    """The light source kinds on one floor: 14 spheres r U[0.5,1.1] on a
+    ring of radius 5.5 (seed 7, rgb U[0.3,1], phong 0.6) over the plane y=0
+    (grey 0.8, phong 0.3, reflection 0.1), camera (0,7,-17) looking at
+    (0,0.5,0), 50 degrees, max_trace_level 3.  Lights: a spotlight at
+    (-6,12,-4) on (-2,0,0), radius 15, falloff 25, tightness 5, fade_distance
+    12, fade_power 2; a cylinder light at (8,10,4) on (3,0,2), radius 1.5,
+    falloff 3, tightness 1; a parallel light at (0,20,-20) on the origin; a
+    shadowless fill light at (0,10,-15); a 3x3 area spotlight at (5,9,-6)
+    (axes <1.5,0,0>, <0,0,1.5>, adaptive 1) on (2,0,0), radius 20, falloff
+    30."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    n = 14
+    ang = np.arange(n) * (2.0 * math.pi / n) + rng.uniform(-0.1, 0.1, size=n)
+    radii = rng.uniform(0.5, 1.1, size=n)
+    colours = rng.uniform(0.3, 1.0, size=(n, 3))
+    s = Scene("light_types", width, height, (0.0, 7.0, -17.0), (0.0, 0.5, 0.0), 50.0, max_trace_level=3)
+    s.light((-6.0, 12.0, -4.0), (1.5, 1.35, 1.05), beam="spotlight", radius=15.0, falloff=25.0, tightness=5.0,
+            point_at=(-2.0, 0.0, 0.0), fade_distance=12.0, fade_power=2.0)
+    s.light((8.0, 10.0, 4.0), (0.5, 0.7, 1.0), beam="cylinder", radius=1.5, falloff=3.0, tightness=1.0,
+            point_at=(3.0, 0.0, 2.0))
+    s.light((0.0, 20.0, -20.0), (0.3, 0.3, 0.3), point_at=(0.0, 0.0, 0.0), parallel=True)
+    s.light((0.0, 10.0, -15.0), (0.15, 0.15, 0.15), shadowless=True)
+    s.area_light((5.0, 9.0, -6.0), (1.5, 0.0, 0.0), (0.0, 0.0, 1.5), 3, 3, rgb=(0.6, 0.4, 0.4), adaptive=1)
+    s.lights[-1].update(beam="spotlight", radius=20.0, falloff=30.0, point_at=(2.0, 0.0, 0.0))
+    for i in range(n):
+        c = (5.5 * math.cos(ang[i]), radii[i], 5.5 * math.sin(ang[i]))
+        s.sphere(c, radii[i], s.material(Material(colours[i], phong=0.6)))
+    s.plane((0.0, 1.0, 0.0), 0.0, s.material(Material((0.8, 0.8, 0.8), phong=0.3, reflection=0.1)))
     return s
 
 

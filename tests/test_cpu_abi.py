@@ -289,6 +289,50 @@ def test_normal_sdl_and_desc_agree():
         assert np.allclose(fwd @ inv, np.eye(4), atol=1e-12)
 
 
+def test_light_source_validation(gpu_lib):
+    """Light sources: Light_Type 0-4 and kind point/area (else invalid); a
+    spotlight, cylinder or parallel light needs point_at away from its
+    centre; area lights take no parallel beam; scenes with media containers
+    take plain point lights only.  The oracle applies the same rules."""
+    from oracle.pyoracle import Oracle
+    ok = (abi.POV_GPU_OK, abi.POV_GPU_E_NODEVICE, abi.POV_GPU_E_CUDA)
+    spot, cyl, par, fill, area = range(5)
+
+    def fresh():
+        return scenes.light_types(32, 24).desc()
+    desc, keep = fresh()
+    assert [desc.lights[i].light_type for i in range(5)] == [abi.POV_LIGHT_TYPE_SPOT, abi.POV_LIGHT_TYPE_CYLINDER,
+                                                               abi.POV_LIGHT_TYPE_POINT, abi.POV_LIGHT_TYPE_SHADOWLESS,
+                                                               abi.POV_LIGHT_TYPE_SPOT]
+    assert desc.lights[cyl].parallel == 1 and desc.lights[par].parallel == 1
+    assert _create(gpu_lib, desc)[0] in ok
+    desc, keep = fresh()
+    desc.lights[fill].light_type = 5
+    assert _create(gpu_lib, desc)[0] == abi.POV_GPU_E_INVALID
+    desc, keep = fresh()
+    desc.lights[spot].points_at[:] = list(desc.lights[spot].center)
+    assert _create(gpu_lib, desc)[0] == abi.POV_GPU_E_UNSUPPORTED
+    desc, keep = fresh()
+    desc.lights[area].light_type = abi.POV_LIGHT_TYPE_CYLINDER
+    assert _create(gpu_lib, desc)[0] == abi.POV_GPU_E_UNSUPPORTED
+    desc, keep = fresh()
+    desc.lights[area].parallel = 1
+    assert _create(gpu_lib, desc)[0] == abi.POV_GPU_E_UNSUPPORTED
+    Oracle(scenes.light_types(32, 24))
+    for change in (dict(beam="spotlight", point_at=(0.0, 0.0, 0.0)), dict(fade_distance=5.0, fade_power=2.0),
+                   dict(shadowless=True)):
+        m = scenes.media_spheres(32, 24, n_spheres=4)
+        m.lights[0].update(change)
+        d, k = m.desc()
+        assert _create(gpu_lib, d)[0] == abi.POV_GPU_E_UNSUPPORTED, change
+        with pytest.raises(abi.PovGpuError):
+            Oracle(m)
+    bad = scenes.light_types(32, 24)
+    bad.lights[area]["beam"] = "cylinder"
+    with pytest.raises(abi.PovGpuError):
+        Oracle(bad)
+
+
 def test_oracle_rejects_the_same_scenes():
     """The oracle applies the same rules as the library."""
     from oracle.pyoracle import Oracle

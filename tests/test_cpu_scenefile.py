@@ -23,6 +23,7 @@ differently.
 """
 import ctypes as C
 import os
+import struct
 
 import numpy as np
 import pytest
@@ -158,4 +159,7 @@ def test_scene_file_rejects_damage(tmp_path):
     bad.write_bytes(b"XXXX" + data[4:])
     with pytest.raises(ValueError):
         ParsedScene(str(bad), 320, 240)
-    assert abi.POV_GPU_ABI_VERSION == 2
+    # a file written for another layout of the C structs
+    bad.write_bytes(data[:8] + struct.pack("<I", abi.POV_GPU_ABI_VERSION + 1) + data[12:])
+    with pytest.raises(ValueError):
+        ParsedScene(str(bad), 320, 240)
