@@ -2567,6 +2567,32 @@ static int compute_refraction(const PovOracle* S, Thread* th, const Isect* is, V
     return tir;
 }
 
+/* Trace::ComputeRelativeIOR (trace.cpp:2595-2625): the ratio of iors the
+ * ray sees at a surface of interior `id`, from the ray's interior list. */
+static double relative_ior(const PovOracle* S, const Thread* th, int id)
+{
+    const double ior = S->ints[id].ior;
+    if (th->nrin == 0)
+        return ior / S->atm_ior;   /* entering from the atmosphere */
+    if (ray_inside(th, id))
+        return th->nrin == 1 ? S->atm_ior / ior : S->ints[th->rin[th->nrin - 1]].ior / ior;
+    return ior / S->ints[th->rin[th->nrin - 1]].ior;
+}
+
+/* Trace::FresnelR (trace.cpp:2679-2707): the unpolarised Fresnel
+ * reflectance for the cosine of incidence and the relative ior. */
+static double fresnel_r(double cos_ti, double n)
+{
+    const double sqrg = n * n + cos_ti * cos_ti - 1.0;
+    if (sqrg <= 0.0)
+        return 1.0;   /* total reflection */
+    const double g = sqrt(sqrg);
+    const double q1 = (g - cos_ti) / (g + cos_ti);
+    const double q2 = (cos_ti * (g + cos_ti) - 1.0) / (cos_ti * (g - cos_ti) + 1.0);
+    const double f = 0.5 * q1 * q1 * (1.0 + q2 * q2);
+    return f < 0.0 ? 0.0 : (f > 1.0 ? 1.0 : f);
+}
+
 /* ComputeTextureColour + ComputeLightedTexture (trace.cpp:457-586,739-1179)
  * for one plain layer; a pigment that filters or transmits gives its own
  * light scaled by its opacity and passes the transmitted ray's colour
@@ -2614,7 +2640,7 @@ static void shade(const PovOracle* S, Thread* th, const Isect* is, V3 D, double 
         att = S->desc.language_version < 370 ? (float)(1.0 - (filt * fmaxf(pig.r, fmaxf(pig.g, pig.b)) + trm))
                                              : (float)(1.0 - filt - trm);
 
-    /* ComputeReflectivity (trace.cpp:2627-2656), non-fresnel */
+    /* ComputeReflectivity (trace.cpp:2627-2656) */
     double cos_inc = -vdot(D, N);
     double wmax = fmax(fmax(m->reflection_max[0], m->reflection_max[1]), m->reflection_max[2]);
     double wmin = fmax(fmax(m->reflection_min[0], m->reflection_min[1]), m->reflection_min[2]);
@@ -2630,6 +2656,17 @@ static void shade(const PovOracle* S, Thread* th, const Isect* is, V3 D, double 
         reflec.r = (float)(frac * m->reflection_max[0] + (1.0 - frac) * m->reflection_min[0]);
         reflec.g = (float)(frac * m->reflection_max[1] + (1.0 - frac) * m->reflection_min[1]);
         reflec.b = (float)(frac * m->reflection_max[2] + (1.0 - frac) * m->reflection_min[2]);
+    }
+    if (m->reflection_fresnel) {
+        /* ComputeFresnel (trace.cpp:2673-2677) at the ray's relative ior,
+         * in float colour channels; the weight by the result's largest */
+        const double f = fresnel_r(cos_inc, relative_ior(S, th, S->obj_int[is->object]));
+        const float* rx = m->reflection_max;
+        const float* rn = m->reflection_min;
+        reflec.r = (float)(f * rx[0]) + (float)((1.0 - f) * rn[0]);
+        reflec.g = (float)(f * rx[1]) + (float)((1.0 - f) * rn[1]);
+        reflec.b = (float)(f * rx[2]) + (float)((1.0 - f) * rn[2]);
+        rweight = weight * fmax(fmax(reflec.r, reflec.g), reflec.b);
     }
 
     /* radiosity ambient (trace.cpp:793-800,896-980): one query per hit
@@ -2742,6 +2779,13 @@ static void shade(const PovOracle* S, Thread* th, const Isect* is, V3 D, double 
     if (see_through) {
         float pf[3] = {pig.r, pig.g, pig.b}, fil[3];
         transmitted_colour(m, pf, fil);
+        if (m->conserve_energy) {
+            /* conserve_energy: the filter loses what the surface reflects
+             * (trace.cpp:1070-1075) */
+            fil[0] *= fminf(1.0f, (float)(1.0 - reflec.r));
+            fil[1] *= fminf(1.0f, (float)(1.0 - reflec.g));
+            fil[2] *= fminf(1.0f, (float)(1.0 - reflec.b));
+        }
         const double trans = fmin(1.0, fabs((double)(float)(0.297 * fil[0] + 0.589 * fil[1] + 0.114 * fil[2])));
         if (trans > tk->adc) {
             const double w1 = fmax(fabs(fil[0]), fmax(fabs(fil[1]), fabs(fil[2])));
@@ -2796,6 +2840,7 @@ static double trace_ray(const PovOracle* S, Thread* th, V3 O, V3 D, double weigh
 {
     th->rays++;   /* Number_Of_Rays */
     col->r = col->g = col->b = 0.0f;
+    weight = (float)weight;   /* TraceRay takes the weight as COLC (float) */
     if (tk->level >= tk->max_level || weight < tk->adc)
         return HUGE_VAL;
     const int cont = flags & RAY_CONTINUED;
@@ -3748,6 +3793,16 @@ int pov_oracle_create(const PovGpuSceneDesc* desc, PovOracle** out, int32_t* bad
                 return POV_GPU_E_UNSUPPORTED;
             transparent = 1;
         }
+    }
+    /* the classic finish terms; fresnel reflection and conserve_energy on
+     * transparent surfaces only (they need the surface's interior) */
+    for (int i = 0; i < desc->num_materials; i++) {
+        const PovGpuMaterial* m = &desc->materials[i];
+        const int see = m->pigment[3] != 0.0f || m->pigment[4] != 0.0f;
+        if (m->fresnel != 0.0f || m->metallic != 0.0f || m->reflect_metallic != 0.0f || m->reflect_exp != 1.0f ||
+            m->irid != 0.0f || m->crand != 0.0f || m->diffuse_back != 0.0f ||
+            ((m->reflection_fresnel || m->conserve_energy) && !see))
+            return POV_GPU_E_UNSUPPORTED;
     }
     if (desc->num_interiors < 0 || (desc->num_interiors > 0 && !desc->interiors))
         return POV_GPU_E_INVALID;

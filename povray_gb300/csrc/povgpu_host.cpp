@@ -424,6 +424,7 @@ struct PathBufs {
     DevBuf mcbuf, mrounds;          // media containers: sample slots of a chunk, round lists
     DevBuf bin_keys, bin_hist, bin_order;   // textured scenes: the shade queue binned by material
     DevBuf rinA, rinB, srin;        // transparent scenes: per-ray and shadow-ray interior lists
+    DevBuf thrA, thrB;              // transparent surfaces that reflect: per-ray throughput
     DevBuf tcand, tkey;             // scenes with tori: deferred torus tests, per-ray nearest roots
     DevBuf tovf;                    // torus-free traversal: rays for the second launch
     DevBuf counters;
@@ -498,9 +499,53 @@ struct PathBufs {
         DevBuf* all[] = {&qA, &qB, &pathA, &pathB, &hits, &paths, &slot_contrib, &sq, &sq_slot, &blocked, &skipA,
                          &skipB, &sskip, &aq, &aq_slot, &aq_skip, &rq, &rq_amb, &quality, &first_t, &stateA,
                          &stateB, &smedium, &mlist, &mte, &mod, &mcbuf, &mrounds, &bin_keys, &bin_hist,
-                         &bin_order, &rinA, &rinB, &srin, &tcand, &tkey, &tovf, &counters};
+                         &bin_order, &rinA, &rinB, &srin, &thrA, &thrB, &tcand, &tkey, &tovf, &counters};
         for (DevBuf* b : all)
             b->release();
+    }
+
+    // Transparent surfaces that reflect (a ray may queue two): the per-pass
+    // scratch for `n` current rays, which holds nothing between passes --
+    // the hits, light slots, shadow rays, shade bins, torus lists.
+    cudaError_t ensure_work(size_t n, int nl, bool binned, bool tori, bool torus_free)
+    {
+        n = std::max<size_t>(n, 1);
+        nl = std::max(nl, 1);
+        cudaError_t e;
+#define PB_ENSURE(buf, bytes) if ((e = (buf).ensure(bytes)) != cudaSuccess) return e
+        PB_ENSURE(hits, sizeof(QHit) * n);
+        PB_ENSURE(slot_contrib, sizeof(float4) * n * nl);
+        PB_ENSURE(sq, sizeof(QRay) * n * nl);
+        PB_ENSURE(sq_slot, sizeof(int) * n * nl);
+        PB_ENSURE(blocked, (n * nl + 3) & ~(size_t)3);
+        PB_ENSURE(sskip, sizeof(uint2) * n * nl);
+        PB_ENSURE(srin, sizeof(uint64_t) * n * nl);
+        if (binned) {
+            PB_ENSURE(bin_keys, n);
+            PB_ENSURE(bin_order, sizeof(int) * n);
+        }
+        if (tori) {
+            PB_ENSURE(tcand, sizeof(uint2) * tcand_cap(n, nl));
+            PB_ENSURE(tkey, sizeof(unsigned long long) * n);
+        }
+        if (torus_free)
+            PB_ENSURE(tovf, sizeof(int) * n * nl);
+        return cudaSuccess;
+    }
+    // One side's queue arrays (A or B) for `n` rays; called only while
+    // that side is empty (the next queue, before the pass fills it).
+    cudaError_t ensure_side(int side, size_t n)
+    {
+        n = std::max<size_t>(n, 1);
+        cudaError_t e;
+        PB_ENSURE(side ? qB : qA, sizeof(QRay) * n);
+        PB_ENSURE(side ? pathB : pathA, sizeof(int) * n);
+        PB_ENSURE(side ? skipB : skipA, sizeof(uint2) * n);
+        PB_ENSURE(side ? stateB : stateA, sizeof(int) * n);
+        PB_ENSURE(side ? rinB : rinA, sizeof(uint64_t) * n);
+        PB_ENSURE(side ? thrB : thrA, sizeof(float4) * n);
+#undef PB_ENSURE
+        return cudaSuccess;
     }
 };
 
@@ -613,6 +658,7 @@ struct PovGpuScene {
     uint32_t graph_launches = 0;   // kernels in the graph
     bool   textured = false;   // some material has a pattern pigment or a normal: bin the shade queue
     bool   transparent = false;   // some surface filters or transmits: rays carry interior lists
+    bool   branching = false;     // some such surface also reflects: a hit may queue two rays
     bool   top_tori = false;      // tori outside CSG: traversal defers their FP64 tests
     bool   csg_torus = false;     // a CSG has a torus child: no torus-free traversal variant
     // bounding trees: the library's binned-SAH tree (nodes, refs) and, on
@@ -882,10 +928,7 @@ int validate_transparency(const PovGpuSceneDesc* d, const std::vector<char>& cma
         if (cmat[i] || (m.pigment[3] == 0.0f && m.pigment[4] == 0.0f))
             continue;
         *transparent = true;
-        bool refl = false;
-        for (int k = 0; k < 3; k++)
-            refl = refl || m.reflection_max[k] != 0.0f || m.reflection_min[k] != 0.0f;
-        if (m.pattern != 0 || refl)
+        if (m.pattern != 0)
             return POV_GPU_E_UNSUPPORTED;
     }
     if (d->num_interiors < 0 || (d->num_interiors > 0 && !d->interiors))
@@ -1008,10 +1051,13 @@ int validate(const PovGpuSceneDesc* d, int32_t* bad)
     }
     for (int i = 0; i < d->num_materials; i++) {
         const PovGpuMaterial& m = d->materials[i];
-        // the classic finish terms only (transparency: validate_transparency)
-        if (m.reflection_fresnel || m.fresnel != 0.0f ||
-            m.metallic != 0.0f || m.reflect_metallic != 0.0f || m.reflect_exp != 1.0f || m.irid != 0.0f ||
-            m.crand != 0.0f || m.diffuse_back != 0.0f || m.conserve_energy)
+        // the classic finish terms; fresnel reflection and conserve_energy
+        // on transparent surfaces only, whose interiors the device holds
+        // (transparency: validate_transparency)
+        const bool see = m.pigment[3] != 0.0f || m.pigment[4] != 0.0f;
+        if (m.fresnel != 0.0f || m.metallic != 0.0f || m.reflect_metallic != 0.0f || m.reflect_exp != 1.0f ||
+            m.irid != 0.0f || m.crand != 0.0f || m.diffuse_back != 0.0f ||
+            ((m.reflection_fresnel || m.conserve_energy) && !see))
             return POV_GPU_E_UNSUPPORTED;
     }
     const int n = d->num_objects;
@@ -1085,7 +1131,8 @@ DevMaterial make_material(const PovGpuMaterial& m, const float* ambient_light, b
     bool anyr = false;
     for (int k = 0; k < 3; k++)
         anyr = anyr || m.reflection_max[k] != 0.f || m.reflection_min[k] != 0.f;
-    d.has_reflection = anyr ? 1 : 0;
+    d.reflect_flags = (anyr ? REFL_ANY : 0) | (m.reflection_fresnel ? REFL_FRESNEL : 0) |
+                      (m.conserve_energy ? REFL_CONSERVE : 0);
     d.diffuse_raw = m.diffuse;
     d.pattern = m.pattern;
     d.normal = m.normal;
@@ -1533,11 +1580,15 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
     // filters nor transmits; a CSG whose children all are).
     const double atm_ior = d->atmosphere_ior > 0.0 ? d->atmosphere_ior : 1.0;
     sc->transparent = false;
+    sc->branching = false;
     for (int i = 0; i < d->num_objects; i++) {
         const PovGpuMaterial& m = d->materials[objects[i].material];
         if (d->objects[i].type < POV_OBJ_UNION && !is_container(d->objects[i]) &&
-            (m.pigment[3] != 0.0f || m.pigment[4] != 0.0f))
+            (m.pigment[3] != 0.0f || m.pigment[4] != 0.0f)) {
             sc->transparent = true;
+            for (int k = 0; k < 3; k++)
+                sc->branching = sc->branching || m.reflection_max[k] != 0.0f || m.reflection_min[k] != 0.0f;
+        }
     }
     std::vector<float4> interiors;
     std::vector<int32_t> obj_interior((size_t)std::max(d->num_objects, 1), 0);
@@ -2308,23 +2359,36 @@ int run_levels(PovGpuScene* sc, StageClock& clk, PathBufs& B, size_t maxq, int l
     const bool torus_free = sc->S.has_full_prims && !sc->csg_torus;
     CK(B.ensure(maxq, nl, nal, rad, sample_rays, sc->media_ni, sc->textured, transparent, sc->top_tori,
                 torus_free));
+    // transparent surfaces that also reflect: a ray may queue two rays, so
+    // the queue sides and the per-pass scratch grow with the ray count
+    // (the host reads each pass's count); rays carry their throughput
+    const bool branching = transparent && sc->branching;
+    size_t cap_work = maxq;                  // current rays the per-pass scratch holds
+    size_t cap_side[2] = {maxq, maxq};       // rays each queue side (A, B) holds
+    if (branching) {
+        CK(B.ensure_side(0, maxq));
+        CK(B.ensure_side(1, maxq));
+    }
     TorusDefer tdc{}, tds{};   // closest-hit and any-hit launches
     const bool defer = sc->top_tori || torus_free;
-    if (defer) {
-        tdc.count = tds.count = B.counters.as<int>() + C_TC;
-        tdc.ovf_count = tds.ovf_count = B.counters.as<int>() + C_TO;
-        tdc.ovf_work = tds.ovf_work = B.counters.as<int>() + C_TW;
-    }
-    if (sc->top_tori) {
-        tdc.cand = tds.cand = B.tcand.as<uint2>();
-        tdc.cap = tds.cap = (int)tcand_cap(maxq, nl);
-        tdc.key = B.tkey.as<unsigned long long>();
-    }
-    if (torus_free) {
-        tdc.ovf = tds.ovf = B.tovf.as<int>();
-        tdc.ovf_cap = (int)maxq;
-        tds.ovf_cap = (int)(maxq * nl);
-    }
+    auto bind_work = [&]() {
+        if (defer) {
+            tdc.count = tds.count = B.counters.as<int>() + C_TC;
+            tdc.ovf_count = tds.ovf_count = B.counters.as<int>() + C_TO;
+            tdc.ovf_work = tds.ovf_work = B.counters.as<int>() + C_TW;
+        }
+        if (sc->top_tori) {
+            tdc.cand = tds.cand = B.tcand.as<uint2>();
+            tdc.cap = tds.cap = (int)tcand_cap(cap_work, nl);
+            tdc.key = B.tkey.as<unsigned long long>();
+        }
+        if (torus_free) {
+            tdc.ovf = tds.ovf = B.tovf.as<int>();
+            tdc.ovf_cap = (int)cap_work;
+            tds.ovf_cap = (int)(cap_work * nl);
+        }
+    };
+    bind_work();
     cudaStream_t st = sc->active();
     int* cnt = B.counters.as<int>();
     unsigned long long* dstats = sc->stats.as<unsigned long long>();
@@ -2335,14 +2399,13 @@ int run_levels(PovGpuScene* sc, StageClock& clk, PathBufs& B, size_t maxq, int l
     const int grid_shade = std::max(1, std::min(sc->num_sms * sc->lc.shade_blocks_per_sm, (int)((maxq + 127) / 128)));
     const int tblock = sc->lc.trace_block, tocc = sc->lc.trace_occupancy;
     const size_t max_area = maxq * (size_t)nal;
-    QRay* qcur = B.qA.as<QRay>();
-    QRay* qnext = B.qB.as<QRay>();
-    int* pcur = B.pathA.as<int>();
-    int* pnext = B.pathB.as<int>();
-    int* ccur = cnt + C_QA;
-    int* cnext = cnt + C_QB;
-    uint2* kcur = B.skipA.as<uint2>();
-    uint2* knext = B.skipB.as<uint2>();
+    // the queue sides: the current pass reads side `side`, fills the other
+    int side = 0;
+    QRay *qcur, *qnext;
+    int *pcur, *pnext, *ccur, *cnext, *scur, *snext;
+    uint2 *kcur, *knext;
+    uint64_t *rcur, *rnext;
+    float4 *tcur, *tnext;
     ShadeRad sr{};
     sr.rq = rad ? B.rq.as<RadQuery>() : nullptr;
     sr.rq_count = cnt + C_RQ;
@@ -2359,10 +2422,30 @@ int run_levels(PovGpuScene* sc, StageClock& clk, PathBufs& B, size_t maxq, int l
     // every ray across one surface, and a pass limit ends a frame whose
     // rays still cross surfaces after it with an error (no ray is dropped
     // silently).
-    int* scur = staged ? B.stateA.as<int>() : nullptr;
-    int* snext = staged ? B.stateB.as<int>() : nullptr;
-    uint64_t* rcur = transparent ? B.rinA.as<uint64_t>() : nullptr;
-    uint64_t* rnext = transparent ? B.rinB.as<uint64_t>() : nullptr;
+    auto bind = [&]() {
+        DevBuf* q[2] = {&B.qA, &B.qB};
+        DevBuf* pa[2] = {&B.pathA, &B.pathB};
+        DevBuf* sk[2] = {&B.skipA, &B.skipB};
+        DevBuf* stt[2] = {&B.stateA, &B.stateB};
+        DevBuf* ri[2] = {&B.rinA, &B.rinB};
+        DevBuf* th[2] = {&B.thrA, &B.thrB};
+        const int o = side ^ 1;
+        qcur = q[side]->as<QRay>();
+        qnext = q[o]->as<QRay>();
+        pcur = pa[side]->as<int>();
+        pnext = pa[o]->as<int>();
+        ccur = cnt + (side ? C_QB : C_QA);
+        cnext = cnt + (side ? C_QA : C_QB);
+        kcur = sk[side]->as<uint2>();
+        knext = sk[o]->as<uint2>();
+        scur = staged ? stt[side]->as<int>() : nullptr;
+        snext = staged ? stt[o]->as<int>() : nullptr;
+        rcur = transparent ? ri[side]->as<uint64_t>() : nullptr;
+        rnext = transparent ? ri[o]->as<uint64_t>() : nullptr;
+        tcur = branching ? th[side]->as<float4>() : nullptr;
+        tnext = branching ? th[o]->as<float4>() : nullptr;
+    };
+    bind();
     const int max_pass = media         ? (max_level - level0) * (1 + 2 * S.num_containers)
                          : transparent ? (max_level - level0) * TRANSPARENT_PASSES_PER_LEVEL
                                        : max_level - level0;
@@ -2382,12 +2465,27 @@ int run_levels(PovGpuScene* sc, StageClock& clk, PathBufs& B, size_t maxq, int l
         }
         if (pass >= max_pass)
             break;
+        if (branching) {   // room for this pass's rays and up to two children each
+            const size_t ncur = pass == 0 ? maxq : std::min((size_t)*sc->pin_int(1), cap_side[side]);
+            if (ncur > cap_work) {
+                CK(B.ensure_work(ncur, nl, sc->textured, sc->top_tori, torus_free));
+                cap_work = ncur;
+                bind_work();
+            }
+            const size_t need = std::max(2 * ncur, maxq);
+            if (need > cap_side[side ^ 1]) {
+                CK(B.ensure_side(side ^ 1, need));
+                cap_side[side ^ 1] = need;
+                bind();
+            }
+        }
+        const int capq = (int)std::min(cap_work, cap_side[side]);   // the current queue's clamp
         CK(cudaMemsetAsync(cnext, 0, sizeof(int), st));
         CK(cudaMemsetAsync(cnt + C_SQ, 0, sizeof(int) * 3, st));   // SQ, W0, W1
         CK(cudaMemsetAsync(cnt + C_AQ, 0, sizeof(int) * 2, st));   // AQ, RQ
         CK(clk.begin(POV_GPU_STAGE_TRACE_CLOSEST));
         CK(launch_trace(S, false, qcur, ccur, cnt + C_W0, B.hits.as<QHit>(), nullptr, sc->stack_depth, grid_trace,
-                        derr, dstats, wc, (int)maxq, kcur, st, tblock, tocc, defer ? &tdc : nullptr));
+                        derr, dstats, wc, capq, kcur, st, tblock, tocc, defer ? &tdc : nullptr));
         CK(clk.end());
         if (sample_rays && pass == 0)
             CK(launch_first_hit(B.hits.as<QHit>(), ccur, (int)maxq, B.first_t.as<float>(), grid_shade, st));
@@ -2401,16 +2499,17 @@ int run_levels(PovGpuScene* sc, StageClock& clk, PathBufs& B, size_t maxq, int l
         }
         CK(clk.begin(POV_GPU_STAGE_SHADE));
         ShadeMedia sm{scur, snext, media ? B.smedium.as<int>() : nullptr, rcur, rnext,
-                      transparent ? B.srin.as<uint64_t>() : nullptr};
+                      transparent ? B.srin.as<uint64_t>() : nullptr, pass > 0 ? tcur : nullptr, tnext,
+                      branching ? 1 : 0, branching ? (int)cap_side[side ^ 1] : 0};
         const int* order = nullptr;
         if (sc->textured) {   // one material per warp in k_shade
-            CK(launch_shade_bins(S, B.hits.as<QHit>(), ccur, (int)maxq, B.bin_keys.as<uint8_t>(),
+            CK(launch_shade_bins(S, B.hits.as<QHit>(), ccur, capq, B.bin_keys.as<uint8_t>(),
                                  B.bin_hist.as<int>(), B.bin_order.as<int>(), grid_shade, st));
             order = B.bin_order.as<int>();
         }
         CK(launch_shade(S, level, max_level, qcur, pcur, B.hits.as<QHit>(), ccur, B.paths.as<PathState>(),
                         B.slot_contrib.as<float4>(), B.sq.as<QRay>(), B.sq_slot.as<int>(), cnt + C_SQ,
-                        B.sskip.as<uint2>(), qnext, pnext, knext, cnext, (int)maxq, (int)(maxq * nl),
+                        B.sskip.as<uint2>(), qnext, pnext, knext, cnext, capq, (int)((size_t)capq * nl),
                         B.aq.as<QRay>(), B.aq_slot.as<int>(), B.aq_skip.as<uint2>(), cnt + C_AQ, (int)max_area, sr,
                         sm, order, grid_shade, derr, dstats, st));
         CK(clk.end(sc->textured ? 4 : 1));
@@ -2431,18 +2530,19 @@ int run_levels(PovGpuScene* sc, StageClock& clk, PathBufs& B, size_t maxq, int l
                                          derr, dstats, st));
             else if (transparent)
                 CK(launch_shadow_filter(S, B.sq.as<QRay>(), B.sq_slot.as<int>(), B.sskip.as<uint2>(),
-                                        B.srin.as<uint64_t>(), cnt + C_SQ, (int)(maxq * nl), cnt + C_W1,
+                                        B.srin.as<uint64_t>(), cnt + C_SQ, (int)((size_t)capq * nl), cnt + C_W1,
                                         B.blocked.as<uint8_t>(), B.slot_contrib.as<float4>(), sc->stack_depth,
                                         grid_trace, derr, dstats, st));
             else
                 CK(launch_trace(S, true, B.sq.as<QRay>(), cnt + C_SQ, cnt + C_W1, nullptr, B.blocked.as<uint8_t>(),
-                                sc->stack_depth, grid_trace, derr, dstats, wc ? wc + 4 : nullptr, (int)(maxq * nl),
-                                B.sskip.as<uint2>(), st, tblock, tocc, defer ? &tds : nullptr));
+                                sc->stack_depth, grid_trace, derr, dstats, wc ? wc + 4 : nullptr,
+                                (int)((size_t)capq * nl), B.sskip.as<uint2>(), st, tblock, tocc,
+                                defer ? &tds : nullptr));
             CK(clk.end());
             CK(clk.begin(POV_GPU_STAGE_RESOLVE));
             CK(launch_resolve(pcur, ccur, sc->num_lights, B.sq_slot.as<int>(), B.blocked.as<uint8_t>(), cnt + C_SQ,
-                              B.slot_contrib.as<float4>(), B.paths.as<PathState>(), grid_shade, (int)maxq,
-                              (int)(maxq * nl), st));
+                              B.slot_contrib.as<float4>(), B.paths.as<PathState>(), grid_shade, capq,
+                              (int)((size_t)capq * nl), st, branching));
             CK(clk.end(2));
         }
         if (rad) {
@@ -2460,12 +2560,8 @@ int run_levels(PovGpuScene* sc, StageClock& clk, PathBufs& B, size_t maxq, int l
                 CK(clk.end());
             }
         }
-        std::swap(qcur, qnext);
-        std::swap(pcur, pnext);
-        std::swap(ccur, cnext);
-        std::swap(kcur, knext);
-        std::swap(scur, snext);
-        std::swap(rcur, rnext);
+        side ^= 1;
+        bind();
     }
     return POV_GPU_OK;
 }

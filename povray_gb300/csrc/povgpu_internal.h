@@ -58,6 +58,11 @@ struct __align__(16) ObjectShade {
 };
 
 // Material as the shading kernel reads it (float, pre-derived terms).
+// DevMaterial::reflect_flags: a reflection at all, its reflectivity by
+// ComputeFresnel at the ray's relative ior (transparent surfaces), and
+// conserve_energy (the transmitted light loses what is reflected).
+constexpr int REFL_ANY = 1, REFL_FRESNEL = 2, REFL_CONSERVE = 4;
+
 struct __align__(16) DevMaterial {
     float4 pigment;         // rgb, filter
     float4 emission;        // emission + ambient * ambient_light, rgb
@@ -69,7 +74,7 @@ struct __align__(16) DevMaterial {
     float phong_size;
     float specular;
     float roughness;        // already inverted
-    int32_t has_reflection;
+    int32_t reflect_flags;  // REFL_ANY | REFL_FRESNEL | REFL_CONSERVE
     float   diffuse_raw;    // Finish->Diffuse, the radiosity ambient's factor (trace.cpp:898)
     int32_t pattern;        // pigment pattern + 1 (0: the plain pigment above)
     int32_t normal;         // normal perturbation + 1 (0: the raw normal)
@@ -385,6 +390,14 @@ struct ShadeMedia {
     const uint64_t* q_rin;
     uint64_t*       nq_rin;
     uint64_t*       sq_rin;
+    // transparent surfaces that also reflect: a hit may queue two rays, so
+    // each ray carries its own throughput (rgb, weight; q_thr NULL: the
+    // path's, for the camera rays) and paths take their colour by atomic
+    // adds; nq_cap is the next queue's capacity (0: the current one's)
+    const float4* q_thr;
+    float4*       nq_thr;
+    int32_t       branching;
+    int32_t       nq_cap;
 };
 
 // A ray's interior list (Ray::GetInteriors): the ids of the interiors it

@@ -1635,11 +1635,37 @@ __device__ __forceinline__ float attenuate_light(const DevLight& L, float3 p, fl
     return att;
 }
 
+// Trace::ComputeRelativeIOR (trace.cpp:2595-2625): the ratio of iors a ray
+// with interior list `rin` sees at a surface of interior `id`.
+__device__ __forceinline__ float relative_ior(const DeviceScene& S, uint64_t rin, int id)
+{
+    const float ior = S.interiors[2 * id].x;
+    const int nr = rin_count(rin);
+    if (nr == 0)
+        return ior / S.atm_ior;
+    if (rin_find(rin, id) >= 0)
+        return nr == 1 ? S.atm_ior / ior : S.interiors[2 * rin_get(rin, nr - 1)].x / ior;
+    return ior / S.interiors[2 * rin_get(rin, nr - 1)].x;
+}
+
+// Trace::FresnelR (trace.cpp:2679-2707): unpolarised Fresnel reflectance.
+__device__ __forceinline__ float fresnel_r(float cos_ti, float n)
+{
+    const float sqrg = n * n + cos_ti * cos_ti - 1.0f;
+    if (sqrg <= 0.0f)
+        return 1.0f;
+    const float g = sqrtf(sqrg);
+    const float q1 = (g - cos_ti) / (g + cos_ti);
+    const float q2 = (cos_ti * (g + cos_ti) - 1.0f) / (cos_ti * (g - cos_ti) + 1.0f);
+    return fminf(1.0f, fmaxf(0.0f, 0.5f * q1 * q1 * (1.0f + q2 * q2)));
+}
+
 // One thread per ray of the level queue.  Emits shadow rays (one per lit
-// light, slot = ray*num_lights+light) and the one secondary ray of the hit:
+// light, slot = ray*num_lights+light) and the secondary rays of the hit:
 // the reflection ray, the continued ray through a media container's wall,
-// or the transmitted / refracted / totally reflected ray of a transparent
-// surface.
+// the transmitted / refracted / totally reflected ray of a transparent
+// surface, or (a transparent surface that reflects) the transmitted ray
+// first and then the reflection ray.
 __global__ void __launch_bounds__(128) k_shade(
     DeviceScene S, int level, int max_level, const QRay* __restrict__ q, const int* __restrict__ q_path,
     const QHit* __restrict__ hits, const int* __restrict__ q_count, PathState* __restrict__ paths,
@@ -1670,8 +1696,9 @@ __global__ void __launch_bounds__(128) k_shade(
         const int medium = state_medium(rstate);
         float3 o = xyz(r.org), d = xyz(r.dir);
         PathState ps = paths[path];
-        float3 thr = xyz(ps.throughput);
-        float weight = ps.throughput.w;
+        const float4 thr4 = med.q_thr ? med.q_thr[i] : ps.throughput;
+        float3 thr = xyz(thr4);
+        float weight = thr4.w;
         bool hit = h.prim != NO_PRIM;
         float3 col = f3(0.f, 0.f, 0.f);
         float3 p = o + d * h.t;
@@ -1823,27 +1850,28 @@ __global__ void __launch_bounds__(128) k_shade(
             slot_contrib[(size_t)i * nl + l] =
                 make_float4(contrib.x * thr.x, contrib.y * thr.y, contrib.z * thr.z, emit ? 1.0f : 0.0f);
         }
-        // reflection (ComputeReflectivity, trace.cpp:2627-2656, non-fresnel)
-        bool refl = false;
+        // reflectivity (ComputeReflectivity, trace.cpp:2627-2656): by the
+        // falloff, or by ComputeFresnel at the ray's relative ior; the
+        // reflection ray itself is decided after the transmitted one
         float3 reflec = f3(0.f, 0.f, 0.f);
         float rweight = 0.f;
-        float3 nd = f3(0.f, 0.f, 1.f);
-        if (shaded && m->has_reflection && !rad.gather) {
+        if (shaded && (m->reflect_flags & REFL_ANY) && !rad.gather) {
             float cos_inc = -dot3(d, N);
-            float falloff = m->reflect.w;
-            float frac = fabsf(falloff - 1.0f) > EPSILON_F ? powf(1.0f - cos_inc, falloff) : 1.0f - cos_inc;
             float3 rmax = xyz(m->reflect), rmin = xyz(m->reflect_min);
-            if (fabsf(frac) < EPSILON_F) reflec = rmin;
-            else if (fabsf(frac - 1.0f) < EPSILON_F) reflec = rmax;
-            else reflec = rmax * frac + rmin * (1.0f - frac);
-            rweight = weight * m->reflect_min.w;
-            if (reflec.x != 0.0f || reflec.y != 0.0f || reflec.z != 0.0f) {
-                c_refl++;
-                c_rays++;   // the TraceRay call is counted even when it bails
-                nd = mirror_dir(d, N, raw);
-                refl = (lvl + 1 < max_level) && (rweight >= rad.adc);
+            if ((m->reflect_flags & REFL_FRESNEL) && med.q_rin) {
+                const float f = fresnel_r(cos_inc, relative_ior(S, med.q_rin[i], S.obj_interior[hobj] & 0xffff));
+                reflec = rmax * f + rmin * (1.0f - f);
+                rweight = weight * fmaxf(reflec.x, fmaxf(reflec.y, reflec.z));
+            } else {
+                float falloff = m->reflect.w;
+                float frac = fabsf(falloff - 1.0f) > EPSILON_F ? powf(1.0f - cos_inc, falloff) : 1.0f - cos_inc;
+                if (fabsf(frac) < EPSILON_F) reflec = rmin;
+                else if (fabsf(frac - 1.0f) < EPSILON_F) reflec = rmax;
+                else reflec = rmax * frac + rmin * (1.0f - frac);
+                rweight = weight * m->reflect_min.w;
             }
         }
+        float3 nd = f3(0.f, 0.f, 1.f);   // the transmitted ray's direction
         // transmitted ray through a container wall: counted like any traced
         // ray, at the parent's trace level (TraceRay with continuedRay,
         // trace.cpp:155-160), entering or leaving the container's interior
@@ -1871,9 +1899,13 @@ __global__ void __launch_bounds__(128) k_shade(
         uint64_t trin = 0;
         int tstate = 0;
         float4 tthr = make_float4(0.f, 0.f, 0.f, 0.f);
+        bool tir = false;
         if (shaded && m->see_through && med.q_rin) {
-            const float3 fil = f3(pigc.x * m->pigment.w + m->transmit, pigc.y * m->pigment.w + m->transmit,
-                                  pigc.z * m->pigment.w + m->transmit);
+            float3 fil = f3(pigc.x * m->pigment.w + m->transmit, pigc.y * m->pigment.w + m->transmit,
+                            pigc.z * m->pigment.w + m->transmit);
+            if (m->reflect_flags & REFL_CONSERVE)   // the filter loses what is reflected (trace.cpp:1070-1075)
+                fil = fil * f3(fminf(1.0f, 1.0f - reflec.x), fminf(1.0f, 1.0f - reflec.y),
+                               fminf(1.0f, 1.0f - reflec.z));
             const float trans = fminf(1.0f, fabsf(0.297f * fil.x + 0.589f * fil.y + 0.114f * fil.z));
             if (trans > rad.adc) {
                 const float w1 = fmaxf(fabsf(fil.x), fmaxf(fabsf(fil.y), fabsf(fil.z)));
@@ -1917,6 +1949,7 @@ __global__ void __launch_bounds__(128) k_shade(
                         ln = N * -1.0f;
                     float tt = 1.0f + ior * ior * (nn * nn - 1.0f);
                     if (tt < 0.0f) {
+                        tir = true;
                         c_tir++;                        // Internal_Reflected_Rays_Traced
                         c_refl++;
                         nd = mirror_dir(d, N, raw);
@@ -1934,32 +1967,72 @@ __global__ void __launch_bounds__(128) k_shade(
                 tr = (lvl + 1 < max_level) && (weight * w1 >= rad.adc);
             }
         }
-        const bool spawn = refl || cont || tr;
-        int rs = warp_reserve(nq_count, spawn, mask);
-        if (spawn) {
-            if (rs < max_queue) {
+        // the reflected component (trace.cpp:1148-1178): after total
+        // internal reflection a single layer does not reflect again
+        bool refl = false;
+        float3 rd = f3(0.f, 0.f, 1.f);
+        if (!tir && (reflec.x != 0.0f || reflec.y != 0.0f || reflec.z != 0.0f)) {
+            c_refl++;
+            c_rays++;   // the TraceRay call is counted even when it bails
+            rd = mirror_dir(d, N, raw);
+            refl = (lvl + 1 < max_level) && (rweight >= rad.adc);
+        }
+        const int next_cap = med.nq_cap > 0 ? med.nq_cap : max_queue;
+        // the transmitted or continued ray
+        const bool spawn_t = cont || tr;
+        int ts = warp_reserve(nq_count, spawn_t, mask);
+        if (spawn_t) {
+            if (ts < next_cap) {
                 QRay rr;
                 rr.org = make_float4(p.x, p.y, p.z, kMinIsectDepth);
-                rr.dir = (refl || tr) ? make_float4(nd.x, nd.y, nd.z, CUDART_INF_F)
-                                      : make_float4(d.x, d.y, d.z, CUDART_INF_F);
-                nq[rs] = rr;
-                nq_path[rs] = path;
-                nq_skip[rs] = self;
+                rr.dir = tr ? make_float4(nd.x, nd.y, nd.z, CUDART_INF_F) : make_float4(d.x, d.y, d.z, CUDART_INF_F);
+                nq[ts] = rr;
+                nq_path[ts] = path;
+                nq_skip[ts] = self;
                 if (med.nq_state)
-                    med.nq_state[rs] = tr ? tstate : (refl ? ray_state(lvl + 1, medium) : ray_state(lvl, cont_medium));
+                    med.nq_state[ts] = tr ? tstate : ray_state(lvl, cont_medium);
                 if (med.nq_rin)
-                    med.nq_rin[rs] = trin;
-                if (refl)
-                    paths[path].throughput =
-                        make_float4(thr.x * reflec.x, thr.y * reflec.y, thr.z * reflec.z, rweight);
-                else if (tr)
-                    paths[path].throughput = tthr;
+                    med.nq_rin[ts] = trin;
+                const float4 t = tr ? tthr : thr4;
+                if (med.nq_thr)
+                    med.nq_thr[ts] = t;
+                else
+                    paths[path].throughput = t;
             } else {
                 set_error(err, DE_QUEUE_OVERFLOW);
             }
         }
-        float4 c = ps.colour;
-        paths[path].colour = make_float4(c.x + col.x * thr.x, c.y + col.y * thr.y, c.z + col.z * thr.z, c.w);
+        // the reflection ray (with the incoming ray's interiors)
+        int rs = warp_reserve(nq_count, refl, mask);
+        if (refl) {
+            if (rs < next_cap) {
+                QRay rr;
+                rr.org = make_float4(p.x, p.y, p.z, kMinIsectDepth);
+                rr.dir = make_float4(rd.x, rd.y, rd.z, CUDART_INF_F);
+                nq[rs] = rr;
+                nq_path[rs] = path;
+                nq_skip[rs] = self;
+                if (med.nq_state)
+                    med.nq_state[rs] = ray_state(lvl + 1, medium);
+                if (med.nq_rin)
+                    med.nq_rin[rs] = med.q_rin[i];
+                const float4 t = make_float4(thr.x * reflec.x, thr.y * reflec.y, thr.z * reflec.z, rweight);
+                if (med.nq_thr)
+                    med.nq_thr[rs] = t;
+                else
+                    paths[path].throughput = t;
+            } else {
+                set_error(err, DE_QUEUE_OVERFLOW);
+            }
+        }
+        if (med.branching) {   // another ray of the path may add in this pass
+            atomicAdd(&paths[path].colour.x, col.x * thr.x);
+            atomicAdd(&paths[path].colour.y, col.y * thr.y);
+            atomicAdd(&paths[path].colour.z, col.z * thr.z);
+        } else {
+            float4 c = ps.colour;
+            paths[path].colour = make_float4(c.x + col.x * thr.x, c.y + col.y * thr.y, c.z + col.z * thr.z, c.w);
+        }
     }
     // per-warp counter reduction
     for (int off = 16; off > 0; off >>= 1) {
@@ -2948,12 +3021,13 @@ __global__ void k_media_combine(const int* __restrict__ q_state, const int* __re
 }
 
 __global__ void k_resolve(const int* __restrict__ q_path, const int* __restrict__ q_count, int num_lights,
-                          const float4* __restrict__ slot_contrib, PathState* __restrict__ paths, int cap)
+                          const float4* __restrict__ slot_contrib, PathState* __restrict__ paths, int cap,
+                          int branching)
 {
     int n = min(*q_count, cap);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         int path = q_path[i];
-        float4 c = paths[path].colour;
+        float4 c = branching ? make_float4(0.f, 0.f, 0.f, 0.f) : paths[path].colour;
         for (int l = 0; l < num_lights; l++) {
             float4 s = slot_contrib[(size_t)i * num_lights + l];
             if (s.w != 0.0f) {   // w: 1 lit point light, area-light fraction, 0 blocked
@@ -2962,7 +3036,13 @@ __global__ void k_resolve(const int* __restrict__ q_path, const int* __restrict_
                 c.z += s.z * s.w;
             }
         }
-        paths[path].colour = c;
+        if (branching) {   // two rays of one path may share the pass
+            atomicAdd(&paths[path].colour.x, c.x);
+            atomicAdd(&paths[path].colour.y, c.y);
+            atomicAdd(&paths[path].colour.z, c.z);
+        } else {
+            paths[path].colour = c;
+        }
     }
 }
 
@@ -3534,10 +3614,10 @@ cudaError_t launch_area_shadow(const DeviceScene& S, const QRay* aq, const int* 
 
 cudaError_t launch_resolve(const int* q_path, const int* q_count, int num_lights, const int* sq_slot,
                            const uint8_t* blocked, const int* sq_count, float4* slot_contrib, PathState* paths,
-                           int grid, int cap_rays, int cap_shadow, cudaStream_t st)
+                           int grid, int cap_rays, int cap_shadow, cudaStream_t st, bool branching)
 {
     k_mark_blocked<<<grid, 256, 0, st>>>(sq_slot, blocked, sq_count, slot_contrib, cap_shadow);
-    k_resolve<<<grid, 256, 0, st>>>(q_path, q_count, num_lights, slot_contrib, paths, cap_rays);
+    k_resolve<<<grid, 256, 0, st>>>(q_path, q_count, num_lights, slot_contrib, paths, cap_rays, branching ? 1 : 0);
     return cudaGetLastError();
 }
 

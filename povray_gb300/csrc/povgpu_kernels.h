@@ -67,7 +67,7 @@ cudaError_t launch_area_shadow(const DeviceScene& S, const QRay* aq, const int* 
                                uint32_t* err, unsigned long long* stats, cudaStream_t st);
 cudaError_t launch_resolve(const int* q_path, const int* q_count, int num_lights, const int* sq_slot,
                            const uint8_t* blocked, const int* sq_count, float4* slot_contrib, PathState* paths,
-                           int grid, int cap_rays, int cap_shadow, cudaStream_t st);
+                           int grid, int cap_rays, int cap_shadow, cudaStream_t st, bool branching = false);
 cudaError_t launch_finalize(const PathState* paths, const int* count, int max_samples, const int* slot, float4* out,
                             cudaStream_t st);
 cudaError_t launch_refine(const DeviceScene& S, const double* org, const double* dir, QHit* hits, double* t64, int n,

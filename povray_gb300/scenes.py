@@ -337,7 +337,16 @@ class Normal:
 class Material:
     def __init__(self, rgb, ambient=0.1, diffuse=0.6, phong=0.0, phong_size=40.0,
                  specular=0.0, roughness=0.05, reflection=0.0, brilliance=1.0,
-                 emission=0.0, transmit=0.0, pattern=None, normal=None, filter=0.0):
+                 emission=0.0, transmit=0.0, pattern=None, normal=None, filter=0.0,
+                 reflection_min=None, fresnel=False, conserve_energy=False):
+        """`reflection` alone is the old syntax (min = max); with
+        `reflection_min` or `fresnel` the finish takes the block form
+        reflection { min, max fresnel } (Parse_Finish,
+        source/parser/parser_materials.cpp:2288-2348).  conserve_energy:
+        the transmitted light loses what the surface reflects."""
+        self.reflection_min = None if reflection_min is None else float(reflection_min)
+        self.fresnel = bool(fresnel)
+        self.conserve_energy = bool(conserve_energy)
         self.pattern = pattern
         self.normal = normal
         self.rgb = tuple(float(c) for c in rgb)
@@ -361,8 +370,13 @@ class Material:
             fin += " phong %s phong_size %s" % (_g(self.phong), _g(self.phong_size))
         if self.specular:
             fin += " specular %s roughness %s" % (_g(self.specular), _g(self.roughness))
-        if self.reflection:
+        if self.reflection_min is not None or self.fresnel:
+            rmin = self.reflection if self.reflection_min is None else self.reflection_min
+            fin += " reflection { %s, %s%s }" % (_g(rmin), _g(self.reflection), " fresnel on" if self.fresnel else "")
+        elif self.reflection:
             fin += " reflection %s" % _g(self.reflection)
+        if self.conserve_energy:
+            fin += " conserve_energy"
         if self.emission:
             fin += " emission %s" % _g(self.emission)
         if self.pattern is not None:
@@ -393,12 +407,12 @@ class Material:
         m.roughness = 1.0 / self.roughness
         m.metallic = 0.0
         m.reflection_max[:] = [self.reflection] * 3
-        m.reflection_min[:] = [self.reflection] * 3
+        m.reflection_min[:] = [self.reflection if self.reflection_min is None else self.reflection_min] * 3
         m.reflection_falloff = 1.0
         m.reflect_exp = 1.0
         m.reflect_metallic = 0.0
-        m.reflection_fresnel = 0
-        m.conserve_energy = 0
+        m.reflection_fresnel = int(self.fresnel)
+        m.conserve_energy = int(self.conserve_energy)
         m.fresnel = 0.0
         m.crand = 0.0
         m.irid = 0.0
@@ -1386,6 +1400,51 @@ def glass_spheres(width=320, height=240, max_trace_level=10):
     s.add(Scene.n_csg("intersection", [Scene.n_sphere((0.0, 0.0, 0.0), 0.9),
                                        Scene.n_box((-0.65, -0.65, -0.65), (0.65, 0.65, 0.65))],
                       translate=(5.3, 0.0, 1.0), mat=glass((0.7, 0.8, 1.0), filter=0.9), interior=Interior(ior=1.5)))
+    return s
+
+
+def glass_reflective(width=320, height=240, max_trace_level=8):
+    """Transparent surfaces that also reflect, so a hit traces the refracted
+    ray and then the reflected one: over the checker floor and wall of
+    glass_spheres, glass with fresnel reflection and conserve_energy
+    (reflection { 0, 1 fresnel on }, filter 0.9, ior 1.5), the same tinted
+    (rgb <1,0.6,0.4>, ior 1.33), dense fresnel glass (ior 2.4: total
+    internal reflection skips the reflection), glass with a constant
+    reflection 0.1 (filter 0.9, ior 1.5), a transmit-only ball with
+    reflection 0.15 (ior 1: transmitted rays), a fresnel glass sphere
+    holding an opaque mirror ball (reflection 0.6: its reflected rays keep
+    the glass's interior), two overlapping fresnel spheres of other iors,
+    and three opaque spheres with reflection 0.3 behind; two point lights.
+    Camera (0,3,-12) looking at (0,0.5,0), 55 deg; max_trace_level 8."""
+    s = Scene("glass_reflective", width, height, (0.0, 3.0, -12.0), (0.0, 0.5, 0.0), 55.0,
+              max_trace_level=max_trace_level)
+    s.point_light((8.0, 14.0, -10.0))
+    s.point_light((-10.0, 9.0, -4.0), (0.5, 0.5, 0.55))
+    floor = Pattern("checker", [(0.0, (0.9, 0.9, 0.85)), (1.0, (0.2, 0.3, 0.55))],
+                    [("scale", (1.0, 1.0, 1.0)), ("translate", (0.0, 0.5, 0.0))])
+    wall = Pattern("checker", [(0.0, (0.85, 0.6, 0.3)), (1.0, (0.95, 0.95, 0.9))],
+                   [("scale", (1.5, 1.5, 1.5)), ("translate", (0.0, 0.0, 0.75))])
+    s.plane((0.0, 1.0, 0.0), -1.0, s.material(Material((1.0, 1.0, 1.0), pattern=floor)))
+    s.plane((0.0, 0.0, -1.0), -9.0, s.material(Material((1.0, 1.0, 1.0), pattern=wall)))
+    for c, r, rgb in (((-3.0, 0.2, 5.0), 1.2, (0.8, 0.2, 0.15)), ((1.5, 0.0, 6.0), 1.0, (0.2, 0.7, 0.25)),
+                      ((4.5, 0.5, 4.0), 1.5, (0.25, 0.3, 0.85))):
+        s.sphere(c, r, s.material(Material(rgb, phong=0.4, reflection=0.3)))
+
+    def glass(rgb=(1.0, 1.0, 1.0), filter=0.0, transmit=0.0, fresnel=True, reflection=1.0):
+        return s.material(Material(rgb, ambient=0.0, diffuse=0.1, phong=0.8, phong_size=80.0, filter=filter,
+                                   transmit=transmit, reflection=reflection,
+                                   reflection_min=0.0 if fresnel else None, fresnel=fresnel,
+                                   conserve_energy=fresnel))
+    s.sphere((-4.2, 0.0, 0.0), 1.0, glass(filter=0.9), Interior(ior=1.5))
+    s.sphere((-1.8, 0.0, -0.5), 1.0, glass((1.0, 0.6, 0.4), filter=0.85), Interior(ior=1.33))
+    s.sphere((0.6, 0.0, 0.0), 1.0, glass((0.6, 0.9, 0.6), transmit=0.7, fresnel=False, reflection=0.15),
+             Interior(ior=1.0))
+    s.sphere((3.0, 0.0, -0.5), 1.0, glass(filter=0.95), Interior(ior=2.4))
+    s.sphere((-3.0, 2.6, 1.5), 0.9, glass(filter=0.9, fresnel=False, reflection=0.1), Interior(ior=1.5))
+    s.sphere((2.4, 2.8, 2.0), 1.3, glass(filter=0.92), Interior(ior=1.5))          # holds the mirror ball
+    s.sphere((2.4, 2.8, 2.0), 0.45, s.material(Material((0.9, 0.9, 0.9), phong=0.6, reflection=0.6)))
+    s.sphere((-0.6, 2.5, 2.5), 0.9, glass(filter=0.9), Interior(ior=1.3))             # two overlapping
+    s.sphere((0.1, 2.7, 2.3), 0.7, glass((1.0, 1.0, 0.6), filter=0.9), Interior(ior=1.6))
     return s
 
 

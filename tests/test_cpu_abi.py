@@ -82,10 +82,12 @@ def test_transformed_primitive_is_unsupported(gpu_lib):
 
 
 def test_transparency_validation(gpu_lib):
-    """Transparent surfaces: a plain pigment that filters or transmits, no
-    reflection beside it (one secondary ray per hit), interiors without
-    dispersion or caustics, no radiosity or area lights in the scene, the
-    camera inside no object; rejected before any device work."""
+    """Transparent surfaces: a plain pigment that filters or transmits
+    (reflection beside it, fresnel or not, with or without
+    conserve_energy), interiors without dispersion or caustics, no
+    radiosity or area lights in the scene, the camera inside no object;
+    fresnel reflection and conserve_energy on transparent surfaces only.
+    Rejected before any device work."""
     ok = (abi.POV_GPU_OK, abi.POV_GPU_E_NODEVICE, abi.POV_GPU_E_CUDA)
 
     def fresh():
@@ -95,7 +97,15 @@ def test_transparency_validation(gpu_lib):
     glass = [i for i in range(desc.num_materials) if desc.materials[i].pigment[3] > 0.0][0]
     desc, keep = fresh()
     desc.materials[glass].reflection_max[0] = 0.2        # a second secondary ray
-    assert _create(gpu_lib, desc)[0] == abi.POV_GPU_E_UNSUPPORTED
+    desc.materials[glass].reflection_fresnel = 1
+    desc.materials[glass].conserve_energy = 1
+    assert _create(gpu_lib, desc)[0] in ok
+    opaque = [i for i in range(desc.num_materials) if desc.materials[i].pigment[3] == 0.0
+              and desc.materials[i].pigment[4] == 0.0][0]
+    for field in ("reflection_fresnel", "conserve_energy"):   # they need the surface's interior
+        desc, keep = fresh()
+        setattr(desc.materials[opaque], field, 1)
+        assert _create(gpu_lib, desc)[0] == abi.POV_GPU_E_UNSUPPORTED, field
     desc, keep = fresh()
     desc.interiors[0].dispersion = 1.02
     assert _create(gpu_lib, desc)[0] == abi.POV_GPU_E_UNSUPPORTED

@@ -59,6 +59,36 @@ def _has_media(scene):
     return bool(getattr(scene, "medias", None))
 
 
+def _reflects_through_glass(scene):
+    """A transparent surface that also reflects (a hit traces two rays)."""
+    return any((m.filter or m.transmit) and m.reflection for m in scene.materials)
+
+
+def check_branching_counters(st, rs):
+    """Counters of scenes whose transparent surfaces also reflect.  The
+    refraction counters are exact.  Two count-only effects are bounded
+    (pixels are unaffected):
+    * Fresnel reflectance at a relative ior of exactly 1 (leaving the inner
+      of two nested interiors, trace.cpp:2611-2618) is zero in exact
+      arithmetic; computed, it is the residue of (1 + cos^2) - 1 - cos^2,
+      zero or not by the last bit of the cosine, and a non-zero one traces
+      (and counts) a reflection ray that bails at the ADC bailout at once:
+      rays and reflected rays differ by the same few, either way.
+    * The shadow cache (trace.cpp:1990-2023): a cached opaque object behind
+      a transparent one ends the reference's shadow ray in one counted
+      test where the full test counts the transparent surface too; the
+      oracle and the GPU never take the shortcut: one test and one success
+      more, never fewer."""
+    for k in ("transmitted_rays", "refracted_rays", "internal_reflected_rays"):
+        assert st[k] == rs[k], (k, st[k], rs[k])
+    dr = st["number_of_rays"] - rs["number_of_rays"]
+    assert dr == st["reflected_rays"] - rs["reflected_rays"], (st, rs)
+    assert abs(dr) <= 1e-3 * rs["number_of_rays"], (st, rs)
+    dt = st["shadow_ray_tests"] - rs["shadow_ray_tests"]
+    assert dt == st["shadow_rays_succeeded"] - rs["shadow_rays_succeeded"], (st, rs)
+    assert 0 <= dt <= 1e-3 * rs["shadow_ray_tests"], (st, rs)
+
+
 @pytest.mark.parametrize("case", sorted(CASES))
 def test_oracle_pixels_and_counters_match_reference(case):
     """Exact, except where the reference's light-source shadow cache decides
@@ -89,6 +119,11 @@ def test_oracle_pixels_and_counters_match_reference(case):
         bound = max(1e-4 * rs["shadow_ray_tests"], 0.01 * rs["number_of_rays"])
         for k in ("shadow_ray_tests", "shadow_rays_succeeded"):
             assert 0 <= st[k] - rs[k] <= bound, (k, st[k], rs[k])
+        assert compare_pixels(img, ref)["max_lsb"] <= 1
+    elif _reflects_through_glass(scene):
+        # one pixel in 10^4 may take another path at a grazing hit
+        assert diff.max() < 1.0 / 255.0 and (diff <= 1e-5).mean() >= 0.9999, float(diff.max())
+        check_branching_counters(st, rs)
         assert compare_pixels(img, ref)["max_lsb"] <= 1
     elif _has_area_light(scene):
         assert diff.max() < 1.0 / 255.0 and (diff <= 1e-5).mean() >= 0.999, float(diff.max())
