@@ -182,6 +182,15 @@ typedef struct PovGpuMaterial {
 #define POV_PATTERN_TRIANGULAR  21   /* TriangularPattern::Evaluate, pattern.cpp:6799  */
 #define POV_PATTERN_CUBIC       22   /* CubicPattern::Evaluate, pattern.cpp:6699       */
 #define POV_PATTERN_HEXAGON     23   /* HexagonPattern::Evaluate, pattern.cpp:6512 (3) */
+/* brick: discrete, two entries (mortar, brick), brick_size and mortar;
+ * spiral1 / spiral2: continuous with `arms` (triangle wave by default);
+ * cells: continuous, each unit cube's value from the reference's pattern
+ * random table (RandomDoubleSequence(0, 1, 32768): boost's mt19937 at its
+ * default seed through uniform_real, randomsequence.cpp:138-149) */
+#define POV_PATTERN_BRICK       24   /* BrickPattern::Evaluate, pattern.cpp:5495 (2)   */
+#define POV_PATTERN_SPIRAL1     25   /* Spiral1Pattern::EvaluateRaw, pattern.cpp:8396  */
+#define POV_PATTERN_SPIRAL2     26   /* Spiral2Pattern::EvaluateRaw, pattern.cpp:8473  */
+#define POV_PATTERN_CELLS       27   /* CellsPattern::EvaluateRaw, pattern.cpp:5652    */
 #define POV_WAVE_RAMP     0       /* the default of most patterns                    */
 #define POV_WAVE_SINE     1
 #define POV_WAVE_TRIANGLE 2       /* the default of marble and wood                  */
@@ -208,6 +217,10 @@ typedef struct PovGpuPattern {
     int32_t has_turbulence;       /* the pattern has a classic turbulence warp       */
     float   values[POV_PATTERN_MAX_ENTRIES];        /* colour map values, ascending   */
     float   colours[POV_PATTERN_MAX_ENTRIES][3];    /* colour map rgb                 */
+    double  brick_size[3];        /* brick: brickSize (<8, 3, 4.5> by default)       */
+    double  mortar;               /* brick: mortar, single precision (SNGL)          */
+    int32_t arms;                 /* spiral1 / spiral2: the number of arms           */
+    int32_t reserved;
 } PovGpuPattern;
 
 /* Normal perturbation (TNORMAL, source/core/material/pattern.h; applied by

@@ -1546,6 +1546,82 @@ static void noise_init(void)
     waves_init();
 }
 
+/* The pattern random table (gPatternRands = RandomDoubleSequence(0, 1,
+ * 32768), pattern.cpp:91): boost's mt19937 at its default seed 5489
+ * through uniform_real, x / 2^32 (randomsequence.cpp:138-149 with
+ * boost/random/uniform_real_distribution.hpp's generate_uniform_real) --
+ * the Mersenne Twister of Matsumoto and Nishimura (1998), restated.
+ * Hash3d yields indices below 4096, so the cells pattern reads only the
+ * first 4096 entries. */
+#define PATTERN_RANDS 4096
+static double g_prand[PATTERN_RANDS];
+static pthread_once_t g_prand_once = PTHREAD_ONCE_INIT;
+
+static void prand_init(void)
+{
+    uint32_t mt[624];
+    mt[0] = 5489u;
+    for (int i = 1; i < 624; i++)
+        mt[i] = 1812433253u * (mt[i - 1] ^ (mt[i - 1] >> 30)) + (uint32_t)i;
+    int idx = 624;
+    for (int n = 0; n < PATTERN_RANDS; n++) {
+        if (idx >= 624) {
+            for (int i = 0; i < 624; i++) {
+                const uint32_t y = (mt[i] & 0x80000000u) | (mt[(i + 1) % 624] & 0x7fffffffu);
+                mt[i] = mt[(i + 397) % 624] ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+            }
+            idx = 0;
+        }
+        uint32_t y = mt[idx++];
+        y ^= y >> 11;
+        y ^= (y << 7) & 0x9d2c5680u;
+        y ^= (y << 15) & 0xefc60000u;
+        y ^= y >> 18;
+        g_prand[n] = (double)y / 4294967296.0;
+    }
+}
+
+double pov_oracle_pattern_rand(int32_t i)
+{
+    pthread_once(&g_prand_once, prand_init);
+    return (i >= 0 && i < PATTERN_RANDS) ? g_prand[i] : -1.0;
+}
+
+/* Hash3d (texture.h:75-76) over the noise hash table. */
+static int hash3d(int a, int b, int c)
+{
+    return g_hash[g_hash[g_hash[a & 0xfff] ^ (b & 0xfff)] ^ (c & 0xfff)];
+}
+
+/* one coordinate's place within its brick or mortar period: the
+ * fraction after (int) truncation, lifted into [0, 1) (pattern.cpp:5520-5610) */
+static double brick_frac(double v)
+{
+    v -= (double)(int)v;
+    return v < 0.0 ? v + 1.0 : v;
+}
+
+/* BrickPattern::Evaluate (pattern.cpp:5495-5623): 0 in the mortar, 1 in a
+ * brick; courses of bricks offset by half a brick. */
+static double brick_value(const PovGpuPattern* pt, V3 T)
+{
+    const double mortar = pt->mortar, fudge = EPSILON + mortar;
+    const double x = T.x + fudge, y = T.y + fudge, z = T.z + fudge;
+    const double bw = pt->brick_size[0], bh = pt->brick_size[1], bd = pt->brick_size[2];
+    if (brick_frac(y / bh) <= mortar / bh)
+        return 0.0;
+    const double by = brick_frac((y / bh) * 0.5);
+    if (brick_frac(x / bw) <= mortar / bw && by <= 0.5)
+        return 0.0;
+    if (brick_frac(x / bw + 0.5) <= mortar / bw && by > 0.5)
+        return 0.0;
+    if (brick_frac(z / bd) <= mortar / bd && by > 0.5)
+        return 0.0;
+    if (brick_frac(z / bd + 0.5) <= mortar / bd && by <= 0.5)
+        return 0.0;
+    return 1.0;
+}
+
 static double scurve(double t) { return t * t * (3.0 - 2.0 * t); }
 static double lerp(double t, double a, double b) { return a + t * (b - a); }
 
@@ -1824,6 +1900,8 @@ static double pattern_value(const PovGpuPattern* pt, V3 T)
             }
         }
         value = fmod(value, 3.0);
+    } else if (pt->type == POV_PATTERN_BRICK) {
+        value = brick_value(pt, T);
     } else if (pt->type == POV_PATTERN_TRIANGULAR) {   /* pattern.cpp:6799-6866 */
         const double SQ3 = 1.7320508075688772935274463415059, SQ3_2 = 0.86602540378443864676372317075294;
         double xs = T.x - 3.0 * floor(T.x / 3.0);
@@ -1972,6 +2050,23 @@ static double pattern_value(const PovGpuPattern* pt, V3 T)
             break;
         case POV_PATTERN_ONION:   /* pattern.cpp:7934-7952 */
             value = fmod(sqrt(T.x * T.x + T.y * T.y + T.z * T.z), 1.0);
+            break;
+        case POV_PATTERN_SPIRAL1:   /* pattern.cpp:8396-8437 */
+        case POV_PATTERN_SPIRAL2: { /* pattern.cpp:8473-8515 */
+            const double turb = pt->has_turbulence ? pt->turbulence[0] * pov_turbulence(T, pt, gen) : 0.0;
+            const double rad = sqrt(T.x * T.x + T.y * T.y);
+            double phi = 0.0;   /* the angle about the z axis, 0 .. 2 pi */
+            if (rad != 0.0)
+                phi = T.x < 0.0 ? 3.0 * (M_PI_D / 2.0) - asin(T.y / rad) : (M_PI_D / 2.0) + asin(T.y / rad);
+            const double arm = T.z + rad + (double)pt->arms * phi / TWO_M_PI + turb;
+            value = pt->type == POV_PATTERN_SPIRAL1 ? arm : triangle_wave(rad) + triangle_wave(arm);
+            break;
+        }
+        case POV_PATTERN_CELLS:   /* pattern.cpp:5652-5660 */
+            pthread_once(&g_prand_once, prand_init);
+            value = fmin(g_prand[hash3d((int)floor(T.x + EPSILON), (int)floor(T.y + EPSILON),
+                                        (int)floor(T.z + EPSILON))],
+                         1.0);
             break;
         default: {   /* leopard, pattern.cpp:7179-7194 */
             const double t1 = sin(T.x), t2 = sin(T.y), t3 = sin(T.z);
@@ -3846,13 +3941,15 @@ int pov_oracle_create(const PovGpuSceneDesc* desc, PovOracle** out, int32_t* bad
         return POV_GPU_E_INVALID;
     for (int i = 0; i < desc->num_patterns; i++) {
         const PovGpuPattern* pt = &desc->patterns[i];
-        if (pt->type < POV_PATTERN_CHECKER || pt->type > POV_PATTERN_HEXAGON || pt->num_entries < 0 ||
+        if (pt->type < POV_PATTERN_CHECKER || pt->type > POV_PATTERN_CELLS || pt->num_entries < 0 ||
             pt->num_entries > POV_PATTERN_MAX_ENTRIES || pt->noise_generator < 1 || pt->noise_generator > 3 ||
             pt->wave_type < POV_WAVE_RAMP || pt->wave_type > POV_WAVE_POLY || pt->octaves < 1 || pt->octaves > 32 ||
             (pt->type == POV_PATTERN_CHECKER && pt->num_entries != 2) ||
             (pt->type == POV_PATTERN_SQUARE && pt->num_entries != 4) ||
             ((pt->type == POV_PATTERN_TRIANGULAR || pt->type == POV_PATTERN_CUBIC) && pt->num_entries != 6) ||
-            (pt->type == POV_PATTERN_HEXAGON && pt->num_entries != 3))
+            (pt->type == POV_PATTERN_HEXAGON && pt->num_entries != 3) ||
+            (pt->type == POV_PATTERN_BRICK && (pt->num_entries != 2 || !(pt->brick_size[0] > 0.0) ||
+                                               !(pt->brick_size[1] > 0.0) || !(pt->brick_size[2] > 0.0))))
             return POV_GPU_E_UNSUPPORTED;
         for (int k = 1; k < pt->num_entries; k++)
             if (pt->values[k] < pt->values[k - 1])
@@ -3865,7 +3962,8 @@ int pov_oracle_create(const PovGpuSceneDesc* desc, PovOracle** out, int32_t* bad
         if (nm->pattern < 1 || nm->pattern > desc->num_patterns)
             return POV_GPU_E_INVALID;
         const int nt = desc->patterns[nm->pattern - 1].type;
-        if (nt == POV_PATTERN_CHECKER || nt >= POV_PATTERN_SQUARE || !(nm->delta > 0.0f) ||
+        if (nt == POV_PATTERN_CHECKER || (nt >= POV_PATTERN_SQUARE && nt <= POV_PATTERN_BRICK) ||
+            !(nm->delta > 0.0f) ||
             !isfinite(nm->amount))
             return POV_GPU_E_UNSUPPORTED;
     }

@@ -22,6 +22,8 @@ typedef struct PovOracle PovOracle;
 int  pov_oracle_create(const PovGpuSceneDesc* desc, PovOracle** out, int32_t* bad_index);
 void pov_oracle_destroy(PovOracle* o);
 void pov_oracle_tree_info(const PovOracle* o, int32_t* top_nodes, int32_t* mesh_nodes);
+/* Entry i of the pattern random table (the cells pattern's values). */
+double pov_oracle_pattern_rand(int32_t i);
 
 /* Trace::FindIntersection for each ray (origins/directions: 3 doubles each). */
 int  pov_oracle_trace_rays(PovOracle* o, const double* origins, const double* directions,

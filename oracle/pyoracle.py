@@ -56,6 +56,8 @@ def lib():
         L.pov_oracle_set_pretrace_jitter.restype = C.c_int
         L.pov_oracle_tree_info.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
         L.pov_oracle_tree_info.restype = None
+        L.pov_oracle_pattern_rand.argtypes = [C.c_int32]
+        L.pov_oracle_pattern_rand.restype = C.c_double
         _lib = L
     return _lib
 
@@ -149,3 +151,8 @@ class Oracle:
         lib().pov_oracle_count_work(self.h, o.ctypes.data, d.ctypes.data, o.shape[0],
                                     C.byref(boxes), C.byref(prims))
         return int(boxes.value), int(prims.value)
+
+
+def pattern_rand(i):
+    """Entry i of the pattern random table the cells pattern reads."""
+    return float(lib().pov_oracle_pattern_rand(int(i)))

@@ -119,6 +119,10 @@ struct Walker
         if (dynamic_cast<const TriangularPattern*>(p)) return POV_PATTERN_TRIANGULAR;
         if (dynamic_cast<const CubicPattern*>(p)) return POV_PATTERN_CUBIC;
         if (dynamic_cast<const HexagonPattern*>(p)) return POV_PATTERN_HEXAGON;
+        if (dynamic_cast<const BrickPattern*>(p)) return POV_PATTERN_BRICK;
+        if (dynamic_cast<const Spiral1Pattern*>(p)) return POV_PATTERN_SPIRAL1;
+        if (dynamic_cast<const Spiral2Pattern*>(p)) return POV_PATTERN_SPIRAL2;
+        if (dynamic_cast<const CellsPattern*>(p)) return POV_PATTERN_CELLS;
         return 0;
     }
 
@@ -156,6 +160,12 @@ struct Walker
             Copy3(d.gradient, g->gradient);
         if (const AgatePattern* a = dynamic_cast<const AgatePattern*>(p))
             d.agate_turb = a->agateTurbScale;
+        if (const BrickPattern* b = dynamic_cast<const BrickPattern*>(p)) {
+            Copy3(d.brick_size, b->brickSize);
+            d.mortar = b->mortar;
+        }
+        if (const SpiralPattern* sp = dynamic_cast<const SpiralPattern*>(p))
+            d.arms = sp->arms;
         MATRIX ident;
         MIdentity(ident);
         CopyMatrix(d.inverse, ident);

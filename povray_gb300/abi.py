@@ -94,6 +94,10 @@ POV_PATTERN_SQUARE = 20
 POV_PATTERN_TRIANGULAR = 21
 POV_PATTERN_CUBIC = 22
 POV_PATTERN_HEXAGON = 23
+POV_PATTERN_BRICK = 24
+POV_PATTERN_SPIRAL1 = 25
+POV_PATTERN_SPIRAL2 = 26
+POV_PATTERN_CELLS = 27
 POV_WAVES = {"ramp": 0, "sine": 1, "triangle": 2, "scallop": 3, "cubic": 4, "poly": 5}
 POV_PATTERN_MAX_ENTRIES = 16
 
@@ -105,7 +109,9 @@ class PovGpuPattern(C.Structure):
                 ("turbulence", C.c_double * 3), ("omega", C.c_double), ("lambda", C.c_double),
                 ("agate_turb", C.c_double), ("octaves", C.c_int32), ("has_turbulence", C.c_int32),
                 ("values", C.c_float * POV_PATTERN_MAX_ENTRIES),
-                ("colours", (C.c_float * 3) * POV_PATTERN_MAX_ENTRIES)]
+                ("colours", (C.c_float * 3) * POV_PATTERN_MAX_ENTRIES),
+                ("brick_size", C.c_double * 3), ("mortar", C.c_double), ("arms", C.c_int32),
+                ("reserved", C.c_int32)]
 
 
 class PovGpuLight(C.Structure):

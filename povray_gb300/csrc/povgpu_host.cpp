@@ -639,7 +639,8 @@ struct PovGpuScene {
     // persistent scene data
     DevBuf nodes, refs, tri_v0, tri_e1, tri_e2, tri_global, tri_shade, tri_normal, tri_local, normals;
     DevBuf spheres, spheres64, boxes64, sphere_obj, sphere_flags, planes, plane_obj, boxes, tori, tori32, csgs, csg_children, objects,
-        materials, lights, medias, patterns, tnormals, noise_hash, noise_rtab, noise_perm, noise_grad, noise_waves;
+        materials, lights, medias, patterns, tnormals, noise_hash, noise_rtab, noise_perm, noise_grad, noise_waves,
+        noise_prand;
     DevBuf encode_buf;     // staging of pov_gpu_encode_u8 for host outputs
     DevBuf cam_tab;        // per-call column / row offsets of the camera rays
     PovGpuLaunchConfig lc{8, 128, 0, 16, 0, {0, 0, 0}};   // launch shapes (pov_gpu_set_launch_config)
@@ -736,7 +737,7 @@ struct PovGpuScene {
                          &hits, &out, &counters, &stats, &err, &rays_in, &t64, &corners, &aa_grid, &aa_mask,
                          &aa_subdiv, &aa_xy, &cellsA, &cellsB, &spos, &sslot, &wcount, &pos_count, &medias,
                          &encode_buf, &cam_tab, &patterns, &tnormals, &noise_hash, &noise_rtab, &noise_perm, &noise_grad,
-                         &noise_waves, &obj_interior, &interiors, &ref_nodes, &ref_refs};
+                         &noise_waves, &noise_prand, &obj_interior, &interiors, &ref_nodes, &ref_refs};
         for (DevBuf* b : all)
             b->release();
         top.release();
@@ -1016,13 +1017,15 @@ int validate(const PovGpuSceneDesc* d, int32_t* bad)
         return POV_GPU_E_INVALID;
     for (int i = 0; i < d->num_patterns; i++) {
         const PovGpuPattern& pt = d->patterns[i];
-        if (pt.type < POV_PATTERN_CHECKER || pt.type > POV_PATTERN_HEXAGON || pt.num_entries < 0 ||
+        if (pt.type < POV_PATTERN_CHECKER || pt.type > POV_PATTERN_CELLS || pt.num_entries < 0 ||
             pt.num_entries > POV_PATTERN_MAX_ENTRIES || pt.noise_generator < 1 || pt.noise_generator > 3 ||
             pt.wave_type < POV_WAVE_RAMP || pt.wave_type > POV_WAVE_POLY || pt.octaves < 1 || pt.octaves > 32 ||
             (pt.type == POV_PATTERN_CHECKER && pt.num_entries != 2) ||
             (pt.type == POV_PATTERN_SQUARE && pt.num_entries != 4) ||
             ((pt.type == POV_PATTERN_TRIANGULAR || pt.type == POV_PATTERN_CUBIC) && pt.num_entries != 6) ||
-            (pt.type == POV_PATTERN_HEXAGON && pt.num_entries != 3))
+            (pt.type == POV_PATTERN_HEXAGON && pt.num_entries != 3) ||
+            (pt.type == POV_PATTERN_BRICK && (pt.num_entries != 2 || !(pt.brick_size[0] > 0.0) ||
+                                              !(pt.brick_size[1] > 0.0) || !(pt.brick_size[2] > 0.0))))
             return POV_GPU_E_UNSUPPORTED;
         for (int k = 1; k < pt.num_entries; k++)
             if (pt.values[k] < pt.values[k - 1])
@@ -1035,7 +1038,9 @@ int validate(const PovGpuSceneDesc* d, int32_t* bad)
         if (nm.pattern < 1 || nm.pattern > d->num_patterns)
             return POV_GPU_E_INVALID;
         const int nt = d->patterns[nm.pattern - 1].type;
-        if (nt == POV_PATTERN_CHECKER || nt >= POV_PATTERN_SQUARE || !(nm.delta > 0.0f) || !std::isfinite(nm.amount))
+        // the discrete patterns' normal forms are normal maps (not built)
+        const bool discrete = nt == POV_PATTERN_CHECKER || (nt >= POV_PATTERN_SQUARE && nt <= POV_PATTERN_BRICK);
+        if (discrete || !(nm.delta > 0.0f) || !std::isfinite(nm.amount))
             return POV_GPU_E_UNSUPPORTED;
     }
     for (int i = 0; i < d->num_materials; i++) {
@@ -1399,11 +1404,43 @@ struct NoiseTables {
     std::vector<int32_t> perm = std::vector<int32_t>(1, 0);
     std::vector<float4> grad = std::vector<float4>(1, make_float4(0.f, 0.f, 0.f, 0.f));
     std::vector<float4> waves = std::vector<float4>(1, make_float4(0.f, 0.f, 0.f, 0.f));
+    std::vector<float> prand = std::vector<float>(1, 0.f);
 
     static int32_t next(int32_t x) { return (int32_t)(uint32_t)((int64_t)x * 1812433253LL + 12345LL); }
 
+    // The pattern random table the cells pattern reads (gPatternRands,
+    // pattern.cpp:91: RandomDoubleSequence(0, 1, 32768), i.e. boost's
+    // mt19937 at its default seed 5489 through uniform_real, x / 2^32,
+    // randomsequence.cpp:138-149): the Mersenne Twister of Matsumoto and
+    // Nishimura (1998).  Hash3d indices stay below 4096, so 4096 entries.
+    void build_prand()
+    {
+        uint32_t mt[624];
+        mt[0] = 5489u;
+        for (int i = 1; i < 624; i++)
+            mt[i] = 1812433253u * (mt[i - 1] ^ (mt[i - 1] >> 30)) + (uint32_t)i;
+        prand.assign(4096, 0.f);
+        int idx = 624;
+        for (int n = 0; n < 4096; n++) {
+            if (idx >= 624) {
+                for (int i = 0; i < 624; i++) {
+                    const uint32_t y = (mt[i] & 0x80000000u) | (mt[(i + 1) % 624] & 0x7fffffffu);
+                    mt[i] = mt[(i + 397) % 624] ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+                }
+                idx = 0;
+            }
+            uint32_t y = mt[idx++];
+            y ^= y >> 11;
+            y ^= (y << 7) & 0x9d2c5680u;
+            y ^= (y << 15) & 0xefc60000u;
+            y ^= y >> 18;
+            prand[n] = (float)((double)y / 4294967296.0);
+        }
+    }
+
     void build()
     {
+        build_prand();
         hash.assign(8192, 0);
         int32_t r = 0;
         for (int i = 0; i < 4096; i++)
@@ -1950,7 +1987,9 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
                              (float)pt.omega);
         q.wave = make_float4((float)pt.frequency, (float)pt.phase, (float)pt.exponent, (float)pt.lambda);
         q.kind = make_int4(pt.type, pt.noise_generator, pt.num_entries, pt.wave_type);
-        q.kind2 = make_int4(pt.octaves, pt.has_turbulence, 0, 0);
+        q.kind2 = make_int4(pt.octaves, pt.has_turbulence, pt.arms, 0);
+        q.brick = make_float4((float)pt.brick_size[0], (float)pt.brick_size[1], (float)pt.brick_size[2],
+                              (float)pt.mortar);
         for (int k = 0; k < POV_PATTERN_MAX_ENTRIES; k++) {
             q.values[k] = pt.values[k];
             q.colours[k] = make_float4(pt.colours[k][0], pt.colours[k][1], pt.colours[k][2], 0.f);
@@ -1991,6 +2030,7 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
     CK(upload(sc->noise_perm, nt.perm));
     CK(upload(sc->noise_grad, nt.grad));
     CK(upload(sc->noise_waves, nt.waves));
+    CK(upload(sc->noise_prand, nt.prand));
 
     sc->h_sphere_obj = B.sphere_obj;
     sc->h_plane_obj = B.plane_obj;
@@ -2048,6 +2088,7 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
     S.noise.perm = sc->noise_perm.as<int32_t>();
     S.noise.grad = sc->noise_grad.as<float4>();
     S.noise.waves = sc->noise_waves.as<float4>();
+    S.noise.prand = sc->noise_prand.as<float>();
     S.num_containers = (int)container_obj.size();
     sc->media_ni = container_obj.empty() ? 0 : media_ni;
     S.max_trace_level = d->max_trace_level;

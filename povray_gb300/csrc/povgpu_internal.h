@@ -95,7 +95,8 @@ struct __align__(16) DevPattern {
     float4 turb;            // classic turbulence vector xyz, omega
     float4 wave;            // frequency, phase, exponent, lambda
     int4   kind;            // type, noise generator, entries, wave type
-    int4   kind2;           // octaves, has turbulence, -, -
+    int4   kind2;           // octaves, has turbulence, spiral arms, -
+    float4 brick;           // brick_size xyz, mortar
     float  values[16];
     float4 colours[16];
 };
@@ -120,6 +121,7 @@ struct DevNoise {
     const int32_t*  perm;   // 2 * (2048 + 1) (InitSolidNoise)
     const float4*   grad;   // 2 * (2048 + 1)
     const float4*   waves;  // POV_NUM_WAVES wave sources xyz, frequency w (Initialize_Waves)
+    const float*    prand;  // 4096 entries of the pattern random table (gPatternRands)
 };
 
 struct __align__(16) DevLight {

@@ -1286,6 +1286,37 @@ __device__ float3 pattern_warp(const DeviceScene& S, const DevPattern& pt, float
 
 // Evaluate_TPat of a warped point T: the pattern's value with its frequency,
 // phase and wave (ContinuousPattern::Evaluate, pattern.cpp:354-390).
+// Hash3d (texture.h:75-76) over the noise hash table: an index below 4096.
+__device__ __forceinline__ int hash3d(const DevNoise& N, int a, int b, int c)
+{
+    const int h = __ldg(N.hash + (a & 0xfff));
+    return __ldg(N.hash + (__ldg(N.hash + (h ^ (b & 0xfff))) ^ (c & 0xfff)));
+}
+
+// a coordinate's place within its brick or mortar period: the fraction
+// after (int) truncation, lifted into [0, 1)
+__device__ __forceinline__ float brick_frac(float v)
+{
+    v -= (float)(int)v;
+    return v < 0.0f ? v + 1.0f : v;
+}
+
+// BrickPattern::Evaluate (pattern.cpp:5495-5623): 0 in the mortar, 1 in a
+// brick; courses offset by half a brick.
+__device__ __forceinline__ float brick_value(const DevPattern& pt, float3 T)
+{
+    const float mortar = pt.brick.w, fudge = 1.0e-10f + mortar;
+    const float x = T.x + fudge, y = T.y + fudge, z = T.z + fudge;
+    const float bw = pt.brick.x, bh = pt.brick.y, bd = pt.brick.z;
+    if (brick_frac(y / bh) <= mortar / bh)
+        return 0.0f;
+    const float by = brick_frac((y / bh) * 0.5f);
+    if (by <= 0.5f ? (brick_frac(x / bw) <= mortar / bw || brick_frac(z / bd + 0.5f) <= mortar / bd)
+                   : (brick_frac(x / bw + 0.5f) <= mortar / bw || brick_frac(z / bd) <= mortar / bd))
+        return 0.0f;
+    return 1.0f;
+}
+
 __device__ __noinline__ float pattern_value(const DeviceScene& S, const DevPattern& pt, float3 T)
 {
     const int kind = pt.kind.x, gen = pt.kind.y;
@@ -1329,6 +1360,8 @@ __device__ __noinline__ float pattern_value(const DeviceScene& S, const DevPatte
             tab = (zl / xl) < 1.0f ? below : above;
         }
         value = (zm >= 0 && zm < 6) ? (float)((tab >> (2 * zm)) & 3u) : 0.0f;
+    } else if (kind == POV_PATTERN_BRICK) {        // pattern.cpp:5495-5623
+        value = brick_value(pt, T);
     } else if (kind == POV_PATTERN_TRIANGULAR) {   // pattern.cpp:6799-6866
         const float SQ3 = 1.7320508075688772935f, SQ3_2 = 0.86602540378443864676f;
         float xs = T.x - 3.0f * floorf(T.x / 3.0f);
@@ -1423,6 +1456,18 @@ __device__ __noinline__ float pattern_value(const DeviceScene& S, const DevPatte
             value = value < 0.0f ? 1.0f : (value > 1.0f ? 0.0f : 1.0f - value);
         } else if (kind == POV_PATTERN_ONION) {    // pattern.cpp:7934-7952
             value = fmodf(sqrtf(T.x * T.x + T.y * T.y + T.z * T.z), 1.0f);
+        } else if (kind == POV_PATTERN_SPIRAL1 || kind == POV_PATTERN_SPIRAL2) {   // pattern.cpp:8396-8515
+            const float turb = pt.kind2.y ? pt.turb.x * pov_turbulence(S.noise, T, pt, gen) : 0.0f;
+            const float rad = sqrtf(T.x * T.x + T.y * T.y);
+            float phi = 0.0f;   // the angle about the z axis, 0 .. 2 pi
+            if (rad != 0.0f)
+                phi = T.x < 0.0f ? 4.71238898038468986f - asinf(T.y / rad) : 1.57079632679489662f + asinf(T.y / rad);
+            const float arm = T.z + rad + (float)pt.kind2.z * phi / 6.2831853071795864769f + turb;
+            value = kind == POV_PATTERN_SPIRAL1 ? arm : pat_triangle(rad) + pat_triangle(arm);
+        } else if (kind == POV_PATTERN_CELLS) {    // pattern.cpp:5652-5660
+            value = fminf(__ldg(S.noise.prand + hash3d(S.noise, (int)floorf(T.x + 1.0e-10f),
+                                                     (int)floorf(T.y + 1.0e-10f), (int)floorf(T.z + 1.0e-10f))),
+                          1.0f);
         } else {                                   // leopard, pattern.cpp:7179-7194
             const float v = (sinf(T.x) + sinf(T.y) + sinf(T.z)) / 3.0f;
             value = v * v;

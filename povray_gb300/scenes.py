@@ -216,13 +216,19 @@ class Pattern:
              "boxed": abi.POV_PATTERN_BOXED,
              # discrete, with a colour list of 4, 6 and 6 entries at 0..n-1
              "square": abi.POV_PATTERN_SQUARE, "triangular": abi.POV_PATTERN_TRIANGULAR,
-             "cubic": abi.POV_PATTERN_CUBIC, "hexagon": abi.POV_PATTERN_HEXAGON}
-    DISCRETE = ("checker", "square", "triangular", "cubic", "hexagon")
+             "cubic": abi.POV_PATTERN_CUBIC, "hexagon": abi.POV_PATTERN_HEXAGON,
+             # brick (discrete: mortar, brick), spiral1 / spiral2 (`arms`), cells
+             "brick": abi.POV_PATTERN_BRICK, "spiral1": abi.POV_PATTERN_SPIRAL1,
+             "spiral2": abi.POV_PATTERN_SPIRAL2, "cells": abi.POV_PATTERN_CELLS}
+    DISCRETE = ("checker", "square", "triangular", "cubic", "hexagon", "brick")
 
     def __init__(self, kind, colours, transforms=(), gradient=(1.0, 0.0, 0.0), noise_generator=None,
                  turbulence=None, octaves=6, omega=0.5, lambda_=2.0, wave=None, frequency=1.0, phase=0.0,
-                 exponent=1.0, agate_turb=1.0):
+                 exponent=1.0, agate_turb=1.0, brick_size=(8.0, 3.0, 4.5), mortar=0.5, arms=3):
         assert kind in self.KINDS
+        self.brick_size = tuple(float(x) for x in brick_size)
+        self.mortar = float(mortar)
+        self.arms = int(arms)
         self.kind = kind
         self.colours = [(float(v), tuple(float(c) for c in rgb)) for v, rgb in colours]
         self.transforms = [(op, tuple(float(x) for x in vec)) for op, vec in transforms]
@@ -239,8 +245,12 @@ class Pattern:
         amount (no colour map, the amount right after the pattern)."""
         if self.kind in self.DISCRETE:
             body = self.kind + "".join(" color rgb %s" % _v(c) for _, c in self.colours)
+            if self.kind == "brick":
+                body += " brick_size %s mortar %s" % (_v(self.brick_size), _g(self.mortar))
         else:
             head = "gradient %s" % _v(self.gradient) if self.kind == "gradient" else self.kind
+            if self.kind in ("spiral1", "spiral2"):
+                head += " %d" % self.arms
             if amount is not None:
                 body = "%s, %s" % (head, _g(amount))
             else:
@@ -275,7 +285,7 @@ class Pattern:
         d.type = self.KINDS[self.kind]
         d.noise_generator = 2 if self.noise_generator is None else int(self.noise_generator)
         d.num_entries = len(self.colours)
-        default_wave = "triangle" if self.kind in ("marble", "wood") else "ramp"
+        default_wave = "triangle" if self.kind in ("marble", "wood", "spiral1", "spiral2") else "ramp"
         d.wave_type = abi.POV_WAVES[self.wave or default_wave]
         inv = self.transform().inverse
         for i in range(4):
@@ -293,6 +303,9 @@ class Pattern:
         setattr(d, "lambda", self.lambda_)
         d.octaves = self.octaves
         d.agate_turb = self.agate_turb
+        d.brick_size[:] = self.brick_size
+        d.mortar = float(np.float32(self.mortar - 2.0e-10))   # SNGL, less EPSILON * 2 (parser_materials.cpp:2062)
+        d.arms = self.arms
         for k, (v, c) in enumerate(self.colours):
             d.values[k] = v
             d.colours[k][:] = c
@@ -1548,6 +1561,51 @@ def shaped_spheres(width=320, height=240, n_spheres=12, seed=8, noise_generator=
         nrm = None
         if i % 2 == 1:
             nrm = Normal(Pattern("radial" if i % 4 == 1 else "spherical", [], at, frequency=8.0), amount=0.6)
+        s.sphere(c, r, s.material(Material((1.0, 1.0, 1.0), phong=0.4, pattern=kinds[i % len(kinds)], normal=nrm)))
+    return s
+
+
+def patterned_spheres(width=320, height=240, n_spheres=10, seed=9, noise_generator=None):
+    """The brick, spiral and cells patterns: a brick wall (plane z=9, brick
+    size <0.8,0.3,0.5>, mortar 0.04), a cells floor (plane y=-2, scale
+    0.7), and `n_spheres` spheres r U[0.5,1.1] in a 6x6 area (seed 9)
+    cycling through spiral1 (3 arms), spiral2 (5 arms), cells (scale 0.3,
+    sine wave), brick (size <0.3,0.12,0.2>, mortar 0.02), spiral1 with
+    turbulence (0.3, octaves 4) and cells with frequency 3, the odd ones
+    with a spiral2 or cells slope normal; every pattern translated off
+    the lattice so no surface lies on a cell or mortar boundary; phong
+    0.4; one point light; camera (0,3,-10) looking at (0,0,2), 55 deg;
+    max_trace_level 2."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    s = Scene("patterned_spheres", width, height, (0.0, 3.0, -10.0), (0.0, 0.0, 2.0), 55.0, max_trace_level=2)
+    s.point_light((10.0, 15.0, -10.0))
+    ng = noise_generator
+    warm = [(0.0, (0.9, 0.85, 0.7)), (0.6, (0.6, 0.3, 0.15)), (1.0, (0.2, 0.1, 0.05))]
+    cool = [(0.0, (0.05, 0.1, 0.3)), (0.5, (0.5, 0.7, 0.9)), (1.0, (1.0, 1.0, 1.0))]
+    off = ("translate", (0.137, 0.071, 0.213))
+    wall = Pattern("brick", [(0, (0.75, 0.75, 0.7)), (1, (0.6, 0.18, 0.1))], [off],
+                   brick_size=(0.8, 0.3, 0.5), mortar=0.04)
+    s.plane((0.0, 0.0, -1.0), -9.0, s.material(Material((1.0, 1.0, 1.0), pattern=wall)))
+    floor = Pattern("cells", cool, [("scale", (0.7, 0.7, 0.7)), off])
+    s.plane((0.0, 1.0, 0.0), -2.0, s.material(Material((1.0, 1.0, 1.0), pattern=floor)))
+    for i in range(n_spheres):
+        c = (rng.uniform(-3.0, 3.0), rng.uniform(-1.0, 1.5), rng.uniform(0.0, 6.0))
+        r = rng.uniform(0.5, 1.1)
+        at = [off, ("translate", c)]
+        kinds = [
+            Pattern("spiral1", warm, [("scale", (0.4, 0.4, 0.4))] + at, arms=3),
+            Pattern("spiral2", cool, [("scale", (0.5, 0.5, 0.5)), ("rotate", (90.0, 0.0, 0.0))] + at, arms=5),
+            Pattern("cells", warm, [("scale", (0.3, 0.3, 0.3)), off], wave="sine"),
+            Pattern("brick", [(0, (0.9, 0.9, 0.85)), (1, (0.3, 0.5, 0.8))], [off], brick_size=(0.3, 0.12, 0.2),
+                    mortar=0.02),
+            Pattern("spiral1", cool, [("scale", (0.5, 0.5, 0.5))] + at, arms=2, turbulence=(0.3, 0.3, 0.3),
+                    octaves=4, noise_generator=ng),
+            Pattern("cells", cool, [("scale", (0.45, 0.45, 0.45)), off], frequency=3.0),
+        ]
+        nrm = None
+        if i % 2 == 1:
+            nrm = Normal(Pattern("spiral2" if i % 4 == 1 else "cells", [],
+                                 [("scale", (0.3, 0.3, 0.3))] + at, arms=4), amount=0.5)
         s.sphere(c, r, s.material(Material((1.0, 1.0, 1.0), phong=0.4, pattern=kinds[i % len(kinds)], normal=nrm)))
     return s
 

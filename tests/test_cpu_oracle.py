@@ -253,3 +253,16 @@ def test_converged_truth_fixture_reproduces():
     out, _ = Oracle(scene).render_converged(t["pixels"][pick], info["counts"], seed=info["seed"])
     assert np.allclose(out[:, :3], t["rgb"][pick], rtol=1e-5, atol=1e-7)
     assert info["noise_rel_rmse"] < 0.005
+
+
+def test_pattern_random_table_matches_reference():
+    """The cells pattern's random table (gPatternRands: boost's mt19937 at
+    its default seed through uniform_real, restated in the oracle and the
+    library) against the reference's own RandomDoubleSequence output: the
+    pretrace jitter table is the same generator's first 2047 values mapped
+    to [-1, 1), bit for bit."""
+    from oracle.pyoracle import pattern_rand
+    jitter = np.load(os.path.join(GOLDEN, "pretrace_jitter.npy"))
+    table = np.array([pattern_rand(i) for i in range(len(jitter))])
+    assert np.array_equal(table * 2.0 - 1.0, jitter)
+    assert all(0.0 <= pattern_rand(i) < 1.0 for i in range(0, 4096, 97))

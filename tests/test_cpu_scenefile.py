@@ -65,6 +65,10 @@ def _pattern_close(i, pa, pb):
             "frequency", "phase", "exponent", "omega", "lambda", "agate_turb", "turbulence"]
     if pa.type != abi.POV_PATTERN_GRADIENT:
         skip.append("gradient")
+    if pa.type != abi.POV_PATTERN_BRICK:
+        skip += ["brick_size", "mortar"]
+    if pa.type not in (abi.POV_PATTERN_SPIRAL1, abi.POV_PATTERN_SPIRAL2):
+        skip.append("arms")
     _close("pattern of object %d" % i, pa, pb, 1e-12, skip=tuple(skip))
     single = ["frequency", "phase", "exponent"]
     if pa.has_turbulence:
