@@ -191,6 +191,13 @@ typedef struct PovGpuMaterial {
 #define POV_PATTERN_SPIRAL1     25   /* Spiral1Pattern::EvaluateRaw, pattern.cpp:8396  */
 #define POV_PATTERN_SPIRAL2     26   /* Spiral2Pattern::EvaluateRaw, pattern.cpp:8473  */
 #define POV_PATTERN_CELLS       27   /* CellsPattern::EvaluateRaw, pattern.cpp:5652    */
+/* crackle: the form-weighted distances to the three nearest cell nuclei
+ * (one per unit cube, placed by the same random table) under the metric,
+ * plus the offset, or with `solid` the noise at the nearest nucleus; no
+ * repeat.  quilted: a pigment only (its normal form is a normal function
+ * of its own, normal.cpp:371-391, not built); frequency 0 by default. */
+#define POV_PATTERN_CRACKLE     28   /* CracklePattern::EvaluateRaw, pattern.cpp:5760  */
+#define POV_PATTERN_QUILTED     29   /* QuiltedPattern::EvaluateRaw, pattern.cpp:8067  */
 #define POV_WAVE_RAMP     0       /* the default of most patterns                    */
 #define POV_WAVE_SINE     1
 #define POV_WAVE_TRIANGLE 2       /* the default of marble and wood                  */
@@ -220,7 +227,11 @@ typedef struct PovGpuPattern {
     double  brick_size[3];        /* brick: brickSize (<8, 3, 4.5> by default)       */
     double  mortar;               /* brick: mortar, single precision (SNGL)          */
     int32_t arms;                 /* spiral1 / spiral2: the number of arms           */
-    int32_t reserved;
+    int32_t crackle_solid;        /* crackle: solid                                  */
+    double  crackle_form[3];      /* crackle: form (<-1, 1, 0> by default)           */
+    double  crackle_metric;       /* crackle: metric (2 by default)                  */
+    double  crackle_offset;       /* crackle: offset (0 by default)                  */
+    double  control0, control1;   /* quilted: control0, control1 (1, 1; SNGL)        */
 } PovGpuPattern;
 
 /* Normal perturbation (TNORMAL, source/core/material/pattern.h; applied by

@@ -1551,9 +1551,9 @@ static void noise_init(void)
  * through uniform_real, x / 2^32 (randomsequence.cpp:138-149 with
  * boost/random/uniform_real_distribution.hpp's generate_uniform_real) --
  * the Mersenne Twister of Matsumoto and Nishimura (1998), restated.
- * Hash3d yields indices below 4096, so the cells pattern reads only the
- * first 4096 entries. */
-#define PATTERN_RANDS 4096
+ * Hash3d yields indices below 4096 and crackle reads two past its index,
+ * so the patterns read only the first 4098 entries. */
+#define PATTERN_RANDS 4100
 static double g_prand[PATTERN_RANDS];
 static pthread_once_t g_prand_once = PTHREAD_ONCE_INIT;
 
@@ -1620,6 +1620,81 @@ static double brick_value(const PovGpuPattern* pt, V3 T)
     if (brick_frac(z / bd + 0.5) <= mortar / bd && by <= 0.5)
         return 0.0;
     return 1.0;
+}
+
+/* QuiltedPattern::EvaluateRaw with quilt_cubic (pattern.cpp:8067-8083,
+ * 8949-8968); FLOOR is texture.h:73's (one less at negative integers). */
+static double quilted_value(const PovGpuPattern* pt, V3 T)
+{
+#define QFLOOR(x) ((x) >= 0.0 ? floor(x) : (0.0 - floor(0.0 - (x)) - 1.0))
+    V3 v = v3(T.x - QFLOOR(T.x) - 0.5, T.y - QFLOOR(T.y) - 0.5, T.z - QFLOOR(T.z) - 0.5);
+#undef QFLOOR
+    const double t = vlen(v), it = 1.0 - t;
+    const double c = (t * t * t + 3.0 * t * it * it * pt->control0 + 3.0 * t * t * it * pt->control1) * 1.154700538;
+    v = vmul(v, c);
+    return (fabs(v.x) + fabs(v.y) + fabs(v.z)) / 3.0;
+}
+
+static double crackle_dist(const PovGpuPattern* pt, V3 dv)
+{
+    const double m = pt->crackle_metric;
+    if (m == 2.0)
+        return vdot(dv, dv);
+    if (m == 1.0)
+        return fabs(dv.x) + fabs(dv.y) + fabs(dv.z);
+    return pow(fabs(dv.x), m) + pow(fabs(dv.y), m) + pow(fabs(dv.z), m);
+}
+
+static double pov_noise(V3 P, int gen);
+
+/* CracklePattern::EvaluateRaw (pattern.cpp:5760-6010) without repeat: the
+ * nuclei of the 81 cubes within a "3d knight move" (InitialiseCrackleCubeTable,
+ * pattern.cpp:9348-9373, in its order; IntPickInCube, pattern.cpp:8808-8818),
+ * the three smallest distances under the metric kept as the reference keeps
+ * them, then the offset and the form (or the noise at the nearest nucleus
+ * when solid), clipped to [0, 1]. */
+static double crackle_value(const PovGpuPattern* pt, V3 T)
+{
+    pthread_once(&g_prand_once, prand_init);
+    const int fx = (int)floor(T.x - EPSILON), fy = (int)floor(T.y - EPSILON), fz = (int)floor(T.z - EPSILON);
+    V3 nuc[81];
+    int n = 0;
+    for (int ax = -2; ax <= 2; ax++)
+        for (int ay = -2; ay <= 2; ay++)
+            for (int az = -2; az <= 2; az++) {
+                if ((abs(ax) == 2) + (abs(ay) == 2) + (abs(az) == 2) > 1)
+                    continue;
+                const int cx = fx + ax, cy = fy + ay, cz = fz + az;
+                const int seed = hash3d(cx & 0xFFF, cy & 0xFFF, cz & 0xFFF);
+                nuc[n++] = v3(cx + g_prand[seed], cy + g_prand[seed + 1], cz + g_prand[seed + 2]);
+            }
+    double m1 = crackle_dist(pt, vsub(nuc[0], T)), m2 = crackle_dist(pt, vsub(nuc[1], T));
+    double m3 = crackle_dist(pt, vsub(nuc[2], T)), tf;
+    int idx = 0;
+    if (m2 < m1) { tf = m1; m1 = m2; m2 = tf; idx = 1; }
+    if (m3 < m1) { tf = m1; m1 = m3; m3 = tf; idx = 2; }
+    if (m3 < m2) { tf = m2; m2 = m3; m3 = tf; }
+    for (int i = 3; i < 81; i++) {
+        const double sum = crackle_dist(pt, vsub(nuc[i], T));
+        if (sum < m1) { m3 = m2; m2 = m1; m1 = sum; idx = i; }
+        else if (sum < m2) { m3 = m2; m2 = sum; }
+        else if (sum < m3) { m3 = sum; }
+    }
+    const double m = pt->crackle_metric, off = pt->crackle_offset;
+    if (off != 0.0) {
+        const double a = m == 2.0 ? off * off : (m == 1.0 ? off : pow(off, m));
+        m1 += a; m2 += a; m3 += a;
+    }
+    const double* f = pt->crackle_form;
+    if (pt->crackle_solid)
+        tf = pov_noise(nuc[idx], pt->noise_generator);
+    else if (m == 2.0)
+        tf = f[0] * sqrt(m1) + f[1] * sqrt(m2) + f[2] * sqrt(m3);
+    else if (m == 1.0)
+        tf = f[0] * m1 + f[1] * m2 + f[2] * m3;
+    else
+        tf = f[0] * pow(m1, 1.0 / m) + f[1] * pow(m2, 1.0 / m) + f[2] * pow(m3, 1.0 / m);
+    return fmax(fmin(tf, 1.0), 0.0);
 }
 
 static double scurve(double t) { return t * t * (3.0 - 2.0 * t); }
@@ -2062,6 +2137,12 @@ static double pattern_value(const PovGpuPattern* pt, V3 T)
             value = pt->type == POV_PATTERN_SPIRAL1 ? arm : triangle_wave(rad) + triangle_wave(arm);
             break;
         }
+        case POV_PATTERN_CRACKLE:
+            value = crackle_value(pt, T);
+            break;
+        case POV_PATTERN_QUILTED:
+            value = quilted_value(pt, T);
+            break;
         case POV_PATTERN_CELLS:   /* pattern.cpp:5652-5660 */
             pthread_once(&g_prand_once, prand_init);
             value = fmin(g_prand[hash3d((int)floor(T.x + EPSILON), (int)floor(T.y + EPSILON),
@@ -3941,7 +4022,8 @@ int pov_oracle_create(const PovGpuSceneDesc* desc, PovOracle** out, int32_t* bad
         return POV_GPU_E_INVALID;
     for (int i = 0; i < desc->num_patterns; i++) {
         const PovGpuPattern* pt = &desc->patterns[i];
-        if (pt->type < POV_PATTERN_CHECKER || pt->type > POV_PATTERN_CELLS || pt->num_entries < 0 ||
+        if (pt->type < POV_PATTERN_CHECKER || pt->type > POV_PATTERN_QUILTED || pt->num_entries < 0 ||
+            (pt->type == POV_PATTERN_CRACKLE && !(pt->crackle_metric > 0.0)) ||
             pt->num_entries > POV_PATTERN_MAX_ENTRIES || pt->noise_generator < 1 || pt->noise_generator > 3 ||
             pt->wave_type < POV_WAVE_RAMP || pt->wave_type > POV_WAVE_POLY || pt->octaves < 1 || pt->octaves > 32 ||
             (pt->type == POV_PATTERN_CHECKER && pt->num_entries != 2) ||
@@ -3963,6 +4045,7 @@ int pov_oracle_create(const PovGpuSceneDesc* desc, PovOracle** out, int32_t* bad
             return POV_GPU_E_INVALID;
         const int nt = desc->patterns[nm->pattern - 1].type;
         if (nt == POV_PATTERN_CHECKER || (nt >= POV_PATTERN_SQUARE && nt <= POV_PATTERN_BRICK) ||
+            nt == POV_PATTERN_QUILTED ||
             !(nm->delta > 0.0f) ||
             !isfinite(nm->amount))
             return POV_GPU_E_UNSUPPORTED;

@@ -123,6 +123,8 @@ struct Walker
         if (dynamic_cast<const Spiral1Pattern*>(p)) return POV_PATTERN_SPIRAL1;
         if (dynamic_cast<const Spiral2Pattern*>(p)) return POV_PATTERN_SPIRAL2;
         if (dynamic_cast<const CellsPattern*>(p)) return POV_PATTERN_CELLS;
+        if (dynamic_cast<const CracklePattern*>(p)) return POV_PATTERN_CRACKLE;
+        if (dynamic_cast<const QuiltedPattern*>(p)) return POV_PATTERN_QUILTED;
         return 0;
     }
 
@@ -166,6 +168,18 @@ struct Walker
         }
         if (const SpiralPattern* sp = dynamic_cast<const SpiralPattern*>(p))
             d.arms = sp->arms;
+        if (const CracklePattern* c = dynamic_cast<const CracklePattern*>(p)) {
+            if (c->repeat.x() || c->repeat.y() || c->repeat.z())
+                return Fail(index, "crackle repeat");
+            Copy3(d.crackle_form, c->crackleForm);
+            d.crackle_metric = c->crackleMetric;
+            d.crackle_offset = c->crackleOffset;
+            d.crackle_solid = c->crackleIsSolid ? 1 : 0;
+        }
+        if (const QuiltedPattern* q = dynamic_cast<const QuiltedPattern*>(p)) {
+            d.control0 = q->Control0;
+            d.control1 = q->Control1;
+        }
         MATRIX ident;
         MIdentity(ident);
         CopyMatrix(d.inverse, ident);

@@ -98,6 +98,8 @@ POV_PATTERN_BRICK = 24
 POV_PATTERN_SPIRAL1 = 25
 POV_PATTERN_SPIRAL2 = 26
 POV_PATTERN_CELLS = 27
+POV_PATTERN_CRACKLE = 28
+POV_PATTERN_QUILTED = 29
 POV_WAVES = {"ramp": 0, "sine": 1, "triangle": 2, "scallop": 3, "cubic": 4, "poly": 5}
 POV_PATTERN_MAX_ENTRIES = 16
 
@@ -111,7 +113,8 @@ class PovGpuPattern(C.Structure):
                 ("values", C.c_float * POV_PATTERN_MAX_ENTRIES),
                 ("colours", (C.c_float * 3) * POV_PATTERN_MAX_ENTRIES),
                 ("brick_size", C.c_double * 3), ("mortar", C.c_double), ("arms", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("crackle_solid", C.c_int32), ("crackle_form", C.c_double * 3), ("crackle_metric", C.c_double),
+                ("crackle_offset", C.c_double), ("control0", C.c_double), ("control1", C.c_double)]
 
 
 class PovGpuLight(C.Structure):

@@ -1017,7 +1017,8 @@ int validate(const PovGpuSceneDesc* d, int32_t* bad)
         return POV_GPU_E_INVALID;
     for (int i = 0; i < d->num_patterns; i++) {
         const PovGpuPattern& pt = d->patterns[i];
-        if (pt.type < POV_PATTERN_CHECKER || pt.type > POV_PATTERN_CELLS || pt.num_entries < 0 ||
+        if (pt.type < POV_PATTERN_CHECKER || pt.type > POV_PATTERN_QUILTED || pt.num_entries < 0 ||
+            (pt.type == POV_PATTERN_CRACKLE && !(pt.crackle_metric > 0.0)) ||
             pt.num_entries > POV_PATTERN_MAX_ENTRIES || pt.noise_generator < 1 || pt.noise_generator > 3 ||
             pt.wave_type < POV_WAVE_RAMP || pt.wave_type > POV_WAVE_POLY || pt.octaves < 1 || pt.octaves > 32 ||
             (pt.type == POV_PATTERN_CHECKER && pt.num_entries != 2) ||
@@ -1039,7 +1040,8 @@ int validate(const PovGpuSceneDesc* d, int32_t* bad)
             return POV_GPU_E_INVALID;
         const int nt = d->patterns[nm.pattern - 1].type;
         // the discrete patterns' normal forms are normal maps (not built)
-        const bool discrete = nt == POV_PATTERN_CHECKER || (nt >= POV_PATTERN_SQUARE && nt <= POV_PATTERN_BRICK);
+        const bool discrete = nt == POV_PATTERN_CHECKER || (nt >= POV_PATTERN_SQUARE && nt <= POV_PATTERN_BRICK) ||
+                              nt == POV_PATTERN_QUILTED;   // quilted's normal is its own function
         if (discrete || !(nm.delta > 0.0f) || !std::isfinite(nm.amount))
             return POV_GPU_E_UNSUPPORTED;
     }
@@ -1412,16 +1414,17 @@ struct NoiseTables {
     // pattern.cpp:91: RandomDoubleSequence(0, 1, 32768), i.e. boost's
     // mt19937 at its default seed 5489 through uniform_real, x / 2^32,
     // randomsequence.cpp:138-149): the Mersenne Twister of Matsumoto and
-    // Nishimura (1998).  Hash3d indices stay below 4096, so 4096 entries.
+    // Nishimura (1998).  Hash3d indices stay below 4096 and crackle reads
+    // two past its index: 4100 entries.
     void build_prand()
     {
         uint32_t mt[624];
         mt[0] = 5489u;
         for (int i = 1; i < 624; i++)
             mt[i] = 1812433253u * (mt[i - 1] ^ (mt[i - 1] >> 30)) + (uint32_t)i;
-        prand.assign(4096, 0.f);
+        prand.assign(4100, 0.f);
         int idx = 624;
-        for (int n = 0; n < 4096; n++) {
+        for (int n = 0; n < 4100; n++) {
             if (idx >= 624) {
                 for (int i = 0; i < 624; i++) {
                     const uint32_t y = (mt[i] & 0x80000000u) | (mt[(i + 1) % 624] & 0x7fffffffu);
@@ -1990,6 +1993,10 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
         q.kind2 = make_int4(pt.octaves, pt.has_turbulence, pt.arms, 0);
         q.brick = make_float4((float)pt.brick_size[0], (float)pt.brick_size[1], (float)pt.brick_size[2],
                               (float)pt.mortar);
+        q.crackle = make_float4((float)pt.crackle_form[0], (float)pt.crackle_form[1], (float)pt.crackle_form[2],
+                                (float)pt.crackle_metric);
+        q.crackle2 = make_float4((float)pt.crackle_offset, (float)pt.control0, (float)pt.control1,
+                                 pt.crackle_solid ? 1.f : 0.f);
         for (int k = 0; k < POV_PATTERN_MAX_ENTRIES; k++) {
             q.values[k] = pt.values[k];
             q.colours[k] = make_float4(pt.colours[k][0], pt.colours[k][1], pt.colours[k][2], 0.f);

@@ -97,6 +97,8 @@ struct __align__(16) DevPattern {
     int4   kind;            // type, noise generator, entries, wave type
     int4   kind2;           // octaves, has turbulence, spiral arms, -
     float4 brick;           // brick_size xyz, mortar
+    float4 crackle;         // crackle form xyz, metric
+    float4 crackle2;        // crackle offset, quilted control0, control1, crackle solid (0 / 1)
     float  values[16];
     float4 colours[16];
 };
@@ -121,7 +123,7 @@ struct DevNoise {
     const int32_t*  perm;   // 2 * (2048 + 1) (InitSolidNoise)
     const float4*   grad;   // 2 * (2048 + 1)
     const float4*   waves;  // POV_NUM_WAVES wave sources xyz, frequency w (Initialize_Waves)
-    const float*    prand;  // 4096 entries of the pattern random table (gPatternRands)
+    const float*    prand;  // 4100 entries of the pattern random table (gPatternRands)
 };
 
 struct __align__(16) DevLight {

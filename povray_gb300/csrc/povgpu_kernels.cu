@@ -1317,6 +1317,88 @@ __device__ __forceinline__ float brick_value(const DevPattern& pt, float3 T)
     return 1.0f;
 }
 
+// QuiltedPattern::EvaluateRaw with quilt_cubic (pattern.cpp:8067-8083,
+// 8949-8968); FLOOR as texture.h:73 has it (one less at negative integers).
+__device__ __forceinline__ float quilted_value(const DevPattern& pt, float3 T)
+{
+    auto qfloor = [](float x) { return x >= 0.0f ? floorf(x) : (0.0f - floorf(0.0f - x) - 1.0f); };
+    float3 v = f3(T.x - qfloor(T.x) - 0.5f, T.y - qfloor(T.y) - 0.5f, T.z - qfloor(T.z) - 0.5f);
+    const float t = sqrtf(dot3(v, v)), it = 1.0f - t;
+    const float c = (t * t * t + 3.0f * t * it * it * pt.crackle2.y + 3.0f * t * t * it * pt.crackle2.z) * 1.154700538f;
+    v = v * c;
+    return (fabsf(v.x) + fabsf(v.y) + fabsf(v.z)) / 3.0f;
+}
+
+__device__ __forceinline__ float crackle_dist(float m, float3 dv)
+{
+    if (m == 2.0f)
+        return dot3(dv, dv);
+    if (m == 1.0f)
+        return fabsf(dv.x) + fabsf(dv.y) + fabsf(dv.z);
+    return powf(fabsf(dv.x), m) + powf(fabsf(dv.y), m) + powf(fabsf(dv.z), m);
+}
+
+// CracklePattern::EvaluateRaw (pattern.cpp:5760-6010) without repeat: the
+// nuclei of the 81 cubes within a "3d knight move" in the order of
+// InitialiseCrackleCubeTable (pattern.cpp:9348-9373), each placed by
+// IntPickInCube (pattern.cpp:8808-8818); the three smallest distances
+// under the metric, kept as the reference keeps them; then the offset and
+// the form, or with `solid` the noise at the nearest nucleus.
+__device__ __noinline__ float crackle_value(const DeviceScene& S, const DevPattern& pt, float3 T, int gen)
+{
+    const int fx = (int)floorf(T.x - 1.0e-10f), fy = (int)floorf(T.y - 1.0e-10f), fz = (int)floorf(T.z - 1.0e-10f);
+    const float m = pt.crackle.w;
+    float m1 = 0.f, m2 = 0.f, m3 = 0.f;
+    float3 near = f3(0.f, 0.f, 0.f);
+    int i = 0;
+    for (int ax = -2; ax <= 2; ax++)
+        for (int ay = -2; ay <= 2; ay++)
+            for (int az = -2; az <= 2; az++) {
+                if ((abs(ax) == 2) + (abs(ay) == 2) + (abs(az) == 2) > 1)
+                    continue;
+                const int cx = fx + ax, cy = fy + ay, cz = fz + az;
+                const int seed = hash3d(S.noise, cx, cy, cz);
+                const float3 nu = f3((float)cx + __ldg(S.noise.prand + seed), (float)cy + __ldg(S.noise.prand + seed + 1),
+                                     (float)cz + __ldg(S.noise.prand + seed + 2));
+                const float sum = crackle_dist(m, nu - T);
+                if (i < 3) {   // the first three, sorted as the reference sorts them
+                    if (i == 0) {
+                        m1 = sum;
+                        near = nu;
+                    } else if (i == 1) {
+                        m2 = sum;
+                        if (m2 < m1) { const float t = m1; m1 = m2; m2 = t; near = nu; }
+                    } else {
+                        m3 = sum;
+                        if (m3 < m1) { const float t = m1; m1 = m3; m3 = t; near = nu; }
+                        if (m3 < m2) { const float t = m2; m2 = m3; m3 = t; }
+                    }
+                } else if (sum < m1) {
+                    m3 = m2; m2 = m1; m1 = sum; near = nu;
+                } else if (sum < m2) {
+                    m3 = m2; m2 = sum;
+                } else if (sum < m3) {
+                    m3 = sum;
+                }
+                i++;
+            }
+    const float off = pt.crackle2.x;
+    if (off != 0.0f) {
+        const float a = m == 2.0f ? off * off : (m == 1.0f ? off : powf(off, m));
+        m1 += a; m2 += a; m3 += a;
+    }
+    float tf;
+    if (pt.crackle2.w != 0.0f)
+        tf = pov_noise(S.noise, near, gen);
+    else if (m == 2.0f)
+        tf = pt.crackle.x * sqrtf(m1) + pt.crackle.y * sqrtf(m2) + pt.crackle.z * sqrtf(m3);
+    else if (m == 1.0f)
+        tf = pt.crackle.x * m1 + pt.crackle.y * m2 + pt.crackle.z * m3;
+    else
+        tf = pt.crackle.x * powf(m1, 1.0f / m) + pt.crackle.y * powf(m2, 1.0f / m) + pt.crackle.z * powf(m3, 1.0f / m);
+    return fmaxf(fminf(tf, 1.0f), 0.0f);
+}
+
 __device__ __noinline__ float pattern_value(const DeviceScene& S, const DevPattern& pt, float3 T)
 {
     const int kind = pt.kind.x, gen = pt.kind.y;
@@ -1464,6 +1546,10 @@ __device__ __noinline__ float pattern_value(const DeviceScene& S, const DevPatte
                 phi = T.x < 0.0f ? 4.71238898038468986f - asinf(T.y / rad) : 1.57079632679489662f + asinf(T.y / rad);
             const float arm = T.z + rad + (float)pt.kind2.z * phi / 6.2831853071795864769f + turb;
             value = kind == POV_PATTERN_SPIRAL1 ? arm : pat_triangle(rad) + pat_triangle(arm);
+        } else if (kind == POV_PATTERN_CRACKLE) {
+            value = crackle_value(S, pt, T, gen);
+        } else if (kind == POV_PATTERN_QUILTED) {
+            value = quilted_value(pt, T);
         } else if (kind == POV_PATTERN_CELLS) {    // pattern.cpp:5652-5660
             value = fminf(__ldg(S.noise.prand + hash3d(S.noise, (int)floorf(T.x + 1.0e-10f),
                                                      (int)floorf(T.y + 1.0e-10f), (int)floorf(T.z + 1.0e-10f))),

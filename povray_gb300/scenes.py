@@ -219,13 +219,22 @@ class Pattern:
              "cubic": abi.POV_PATTERN_CUBIC, "hexagon": abi.POV_PATTERN_HEXAGON,
              # brick (discrete: mortar, brick), spiral1 / spiral2 (`arms`), cells
              "brick": abi.POV_PATTERN_BRICK, "spiral1": abi.POV_PATTERN_SPIRAL1,
-             "spiral2": abi.POV_PATTERN_SPIRAL2, "cells": abi.POV_PATTERN_CELLS}
+             "spiral2": abi.POV_PATTERN_SPIRAL2, "cells": abi.POV_PATTERN_CELLS,
+             # crackle (form, metric, offset, solid), quilted (control0/1; pigment only)
+             "crackle": abi.POV_PATTERN_CRACKLE, "quilted": abi.POV_PATTERN_QUILTED}
     DISCRETE = ("checker", "square", "triangular", "cubic", "hexagon", "brick")
 
     def __init__(self, kind, colours, transforms=(), gradient=(1.0, 0.0, 0.0), noise_generator=None,
                  turbulence=None, octaves=6, omega=0.5, lambda_=2.0, wave=None, frequency=1.0, phase=0.0,
-                 exponent=1.0, agate_turb=1.0, brick_size=(8.0, 3.0, 4.5), mortar=0.5, arms=3):
+                 exponent=1.0, agate_turb=1.0, brick_size=(8.0, 3.0, 4.5), mortar=0.5, arms=3,
+                 form=None, metric=None, offset=None, solid=False, control0=None, control1=None):
         assert kind in self.KINDS
+        self.form = None if form is None else tuple(float(x) for x in form)
+        self.metric = None if metric is None else float(metric)
+        self.offset = None if offset is None else float(offset)
+        self.solid = bool(solid)
+        self.control0 = None if control0 is None else float(control0)
+        self.control1 = None if control1 is None else float(control1)
         self.brick_size = tuple(float(x) for x in brick_size)
         self.mortar = float(mortar)
         self.arms = int(arms)
@@ -238,6 +247,7 @@ class Pattern:
         self.octaves, self.omega, self.lambda_ = int(octaves), float(omega), float(lambda_)
         self.wave = wave
         self.frequency, self.phase, self.exponent = float(frequency), float(phase), float(exponent)
+        self.frequency_default = frequency == 1.0   # no frequency in the SDL: the pattern's default
         self.agate_turb = float(agate_turb)
 
     def sdl(self, amount=None):
@@ -258,6 +268,18 @@ class Pattern:
                 body = "%s color_map { %s }" % (head, cmap)
             if self.kind == "agate" and self.agate_turb != 1.0:
                 body += " agate_turb %s" % _g(self.agate_turb)
+            if self.form is not None:
+                body += " form %s" % _v(self.form)
+            if self.metric is not None:
+                body += " metric %s" % _g(self.metric)
+            if self.offset is not None:
+                body += " offset %s" % _g(self.offset)
+            if self.solid:
+                body += " solid"
+            if self.control0 is not None:
+                body += " control0 %s" % _g(self.control0)
+            if self.control1 is not None:
+                body += " control1 %s" % _g(self.control1)
             if self.wave is not None:
                 body += " %s_wave" % self.wave if self.wave != "poly" else " poly_wave %s" % _g(self.exponent)
             if self.frequency != 1.0:
@@ -306,6 +328,14 @@ class Pattern:
         d.brick_size[:] = self.brick_size
         d.mortar = float(np.float32(self.mortar - 2.0e-10))   # SNGL, less EPSILON * 2 (parser_materials.cpp:2062)
         d.arms = self.arms
+        d.crackle_form[:] = self.form if self.form is not None else (-1.0, 1.0, 0.0)
+        d.crackle_metric = 2.0 if self.metric is None else self.metric
+        d.crackle_offset = 0.0 if self.offset is None else self.offset
+        d.crackle_solid = int(self.solid)
+        d.control0 = float(np.float32(1.0 if self.control0 is None else self.control0))   # SNGL
+        d.control1 = float(np.float32(1.0 if self.control1 is None else self.control1))
+        if self.kind == "quilted" and self.frequency_default:
+            d.frequency = 0.0   # QuiltedPattern's default (pattern.cpp:667)
         for k, (v, c) in enumerate(self.colours):
             d.values[k] = v
             d.colours[k][:] = c
@@ -1565,14 +1595,16 @@ def shaped_spheres(width=320, height=240, n_spheres=12, seed=8, noise_generator=
     return s
 
 
-def patterned_spheres(width=320, height=240, n_spheres=10, seed=9, noise_generator=None):
-    """The brick, spiral and cells patterns: a brick wall (plane z=9, brick
+def patterned_spheres(width=320, height=240, n_spheres=12, seed=9, noise_generator=None):
+    """The brick, spiral, cells, crackle and quilted patterns: a brick wall (plane z=9, brick
     size <0.8,0.3,0.5>, mortar 0.04), a cells floor (plane y=-2, scale
     0.7), and `n_spheres` spheres r U[0.5,1.1] in a 6x6 area (seed 9)
     cycling through spiral1 (3 arms), spiral2 (5 arms), cells (scale 0.3,
     sine wave), brick (size <0.3,0.12,0.2>, mortar 0.02), spiral1 with
-    turbulence (0.3, octaves 4) and cells with frequency 3, the odd ones
-    with a spiral2 or cells slope normal; every pattern translated off
+    turbulence (0.3, octaves 4), cells with frequency 3, crackle, solid
+    crackle, crackle with form <0.8,0.3,0>, metric 1 and offset 0.1, and
+    quilted (control0 0.6, control1 0.9), the odd ones with a spiral2,
+    cells or crackle slope normal; every pattern translated off
     the lattice so no surface lies on a cell or mortar boundary; phong
     0.4; one point light; camera (0,3,-10) looking at (0,0,2), 55 deg;
     max_trace_level 2."""
@@ -1601,11 +1633,16 @@ def patterned_spheres(width=320, height=240, n_spheres=10, seed=9, noise_generat
             Pattern("spiral1", cool, [("scale", (0.5, 0.5, 0.5))] + at, arms=2, turbulence=(0.3, 0.3, 0.3),
                     octaves=4, noise_generator=ng),
             Pattern("cells", cool, [("scale", (0.45, 0.45, 0.45)), off], frequency=3.0),
+            Pattern("crackle", warm, [("scale", (0.35, 0.35, 0.35)), off]),
+            Pattern("crackle", cool, [("scale", (0.4, 0.4, 0.4)), off], solid=True, noise_generator=ng),
+            Pattern("crackle", warm, [("scale", (0.3, 0.3, 0.3)), off], form=(0.8, 0.3, 0.0), metric=1.0,
+                    offset=0.1),
+            Pattern("quilted", cool, [("scale", (0.3, 0.3, 0.3)), off], control0=0.6, control1=0.9),
         ]
         nrm = None
         if i % 2 == 1:
-            nrm = Normal(Pattern("spiral2" if i % 4 == 1 else "cells", [],
-                                 [("scale", (0.3, 0.3, 0.3))] + at, arms=4), amount=0.5)
+            nk = ("spiral2", "cells", "crackle")[(i // 2) % 3]
+            nrm = Normal(Pattern(nk, [], [("scale", (0.3, 0.3, 0.3))] + at, arms=4), amount=0.5)
         s.sphere(c, r, s.material(Material((1.0, 1.0, 1.0), phong=0.4, pattern=kinds[i % len(kinds)], normal=nrm)))
     return s
 

@@ -69,6 +69,10 @@ def _pattern_close(i, pa, pb):
         skip += ["brick_size", "mortar"]
     if pa.type not in (abi.POV_PATTERN_SPIRAL1, abi.POV_PATTERN_SPIRAL2):
         skip.append("arms")
+    if pa.type != abi.POV_PATTERN_CRACKLE:
+        skip += ["crackle_form", "crackle_metric", "crackle_offset", "crackle_solid"]
+    if pa.type != abi.POV_PATTERN_QUILTED:
+        skip += ["control0", "control1"]
     _close("pattern of object %d" % i, pa, pb, 1e-12, skip=tuple(skip))
     single = ["frequency", "phase", "exponent"]
     if pa.has_turbulence:
