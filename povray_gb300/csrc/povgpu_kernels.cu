@@ -1797,7 +1797,10 @@ __device__ __forceinline__ float fresnel_r(float cos_ti, float n)
 // the transmitted / refracted / totally reflected ray of a transparent
 // surface, or (a transparent surface that reflects) the transmitted ray
 // first and then the reflection ray.
-__global__ void __launch_bounds__(128) k_shade(
+// (128, 4): four resident blocks; without the cap the reflection-beside-
+// transparency paths take it to 168 registers and three blocks, and the
+// config-2 shade stage measured 0.478 ms against 0.385 ms with the cap
+__global__ void __launch_bounds__(128, 4) k_shade(
     DeviceScene S, int level, int max_level, const QRay* __restrict__ q, const int* __restrict__ q_path,
     const QHit* __restrict__ hits, const int* __restrict__ q_count, PathState* __restrict__ paths,
     float4* __restrict__ slot_contrib, QRay* __restrict__ sq, int* __restrict__ sq_slot, int* __restrict__ sq_count,
