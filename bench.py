@@ -367,10 +367,10 @@ def radiosity_sweep():
         del g
 
 
-# The reference's other configurations (config 1: 64 spheres at 320x240;
-# config 3: the CSG/torus grid with AA; config 4: the radiosity room; config
-# 5: the multi-view media scene), each timed briefly in the same run beside
-# the main line.
+# The reference's other benchmark workloads (64 spheres at 320x240; the
+# CSG/torus grid at 1080p with AA; the radiosity room at 720p; the
+# multi-view media scene), each timed briefly in the same run beside the
+# main line.
 OTHER_CONFIGS = (("spheres_plane", 320, 240), ("csg_torus_grid", 1920, 1080), ("radiosity_room", 1280, 720),
                  ("multiview_media", 0, 0))
 
