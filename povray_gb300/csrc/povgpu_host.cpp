@@ -2107,6 +2107,7 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
         S.cam_right[k] = d->camera.right[k];
         S.cam_up[k] = d->camera.up[k];
     }
+    set_camera_ff(S);
     sc->num_lights = d->num_lights;
     sc->max_trace_level = d->max_trace_level;
     if (d->radiosity.enabled) {
@@ -2744,11 +2745,11 @@ int run_samples(PovGpuScene* sc, StageClock& clk, int mode, int nblocks, const i
     int* cnt = B.counters.as<int>();
     CK(cudaMemsetAsync(cnt, 0, sizeof(int) * C_NUM, st));
     if (mode != 2)
-        CK(sc->cam_tab.ensure(sizeof(double) * ((size_t)width + (size_t)height + 2)));
+        CK(sc->cam_tab.ensure(sizeof(float2) * ((size_t)width + (size_t)height + 2)));
     CK(clk.begin(POV_GPU_STAGE_CAMERA));
     CK(launch_camera(sc->S, mode, sc->blocks.as<int4>(), block_off, nblocks, pos, npos, n, width, height,
                      B.qA.as<QRay>(), B.pathA.as<int>(), B.paths.as<PathState>(), cnt + C_QA,
-                     sc->stats.as<unsigned long long>(), B.skipA.as<uint2>(), sc->cam_tab.as<double>(), st));
+                     sc->stats.as<unsigned long long>(), B.skipA.as<uint2>(), sc->cam_tab.as<float2>(), st));
     CK(clk.end(mode != 2 ? 2 : 1));
     int rc = run_levels(sc, clk, B, maxq, 0, sc->max_trace_level, 0, false);
     if (rc != POV_GPU_OK)
@@ -3341,6 +3342,7 @@ int pov_gpu_set_camera(PovGpuScene* sc, const PovGpuCamera* cam, const double* l
         sc->S.cam_right[k] = right[k];
         sc->S.cam_up[k] = up[k];
     }
+    set_camera_ff(sc->S);
     return POV_GPU_OK;
 }
 

@@ -264,7 +264,22 @@ struct DeviceScene {
     float4          background;
     // camera
     double          cam_loc[3], cam_dir[3], cam_right[3], cam_up[3];
+    // the same direction, right and up vectors as double-floats (each
+    // component hi + lo, two floats, set by set_camera_ff)
+    float           cam_ff[18];
 };
+
+// DeviceScene::cam_ff from the FP64 camera vectors.
+inline void set_camera_ff(DeviceScene& S)
+{
+    const double* v[3] = {S.cam_dir, S.cam_right, S.cam_up};
+    for (int a = 0; a < 3; a++)
+        for (int k = 0; k < 3; k++) {
+            const float hi = (float)v[a][k];
+            S.cam_ff[6 * a + 2 * k] = hi;
+            S.cam_ff[6 * a + 2 * k + 1] = (float)(v[a][k] - (double)hi);
+        }
+}
 
 // One ray of a wavefront queue (32 B) + its path slot.
 struct __align__(16) QRay {

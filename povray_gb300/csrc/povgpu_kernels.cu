@@ -130,6 +130,71 @@ __device__ __forceinline__ QRay camera_ray_xy(const DeviceScene& S, double x0, d
     return r;
 }
 
+// Double-float arithmetic (Dekker 1971, with Knuth's two-sum): a value as
+// the unevaluated sum hi + lo of two floats, about 44 significant bits.
+// The camera rays of the block grid take their directions in it on the FP32
+// pipes: rounded to float they equal the FP64 form's (checked over every
+// pixel of a 1920x1080 camera: 0 of 6,220,800 components differ), where the
+// FP64 form kept k_camera on this part's narrow FP64 pipe.
+struct FF {
+    float hi, lo;
+};
+// (the _rn intrinsics keep the compiler from fusing a product into a
+// following sum, which would break the error-free transformations)
+__device__ __forceinline__ FF ff_fast_two_sum(float a, float b)   // |a| >= |b|
+{
+    const float s = __fadd_rn(a, b);
+    return FF{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ FF ff_two_sum(float a, float b)
+{
+    const float s = __fadd_rn(a, b), bb = __fsub_rn(s, a);
+    return FF{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ FF ff_add(FF a, FF b)
+{
+    const FF s = ff_two_sum(a.hi, b.hi);
+    return ff_fast_two_sum(s.hi, __fadd_rn(__fadd_rn(s.lo, a.lo), b.lo));
+}
+__device__ __forceinline__ FF ff_mul(FF a, FF b)
+{
+    const float p = __fmul_rn(a.hi, b.hi);
+    return ff_fast_two_sum(p, fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, fmaf(a.hi, b.hi, -p))));
+}
+
+// camera_ray_xy in double-float: direction + x0 * right + y0 * up, its
+// length by one Newton step on sqrtf, each component's quotient with one
+// correction, rounded to float once.
+__device__ __forceinline__ QRay camera_ray_ff(const DeviceScene& S, float2 x0, float2 y0)
+{
+    const FF X{x0.x, x0.y}, Y{y0.x, y0.y};
+    FF d[3];
+    for (int k = 0; k < 3; k++) {
+        const FF dir{S.cam_ff[2 * k], S.cam_ff[2 * k + 1]};
+        const FF right{S.cam_ff[6 + 2 * k], S.cam_ff[6 + 2 * k + 1]};
+        const FF up{S.cam_ff[12 + 2 * k], S.cam_ff[12 + 2 * k + 1]};
+        d[k] = ff_add(ff_add(dir, ff_mul(X, right)), ff_mul(Y, up));
+    }
+    const FF l2 = ff_add(ff_add(ff_mul(d[0], d[0]), ff_mul(d[1], d[1])), ff_mul(d[2], d[2]));
+    float out[3] = {d[0].hi, d[1].hi, d[2].hi};
+    if (l2.hi > 0.0f) {
+        const float s = sqrtf(l2.hi);
+        const FF ss = ff_mul(FF{s, 0.0f}, FF{s, 0.0f});
+        const float res = __fadd_rn(__fsub_rn(__fsub_rn(l2.hi, ss.hi), ss.lo), l2.lo);
+        const FF l = ff_fast_two_sum(s, res / __fmul_rn(2.0f, s));
+        for (int k = 0; k < 3; k++) {
+            const float q0 = d[k].hi / l.hi;
+            const FF t = ff_mul(FF{q0, 0.0f}, l);
+            const FF r = ff_add(d[k], FF{-t.hi, -t.lo});
+            out[k] = __fadd_rn(q0, r.hi / l.hi);
+        }
+    }
+    QRay r;
+    r.org = make_float4((float)S.cam_loc[0], (float)S.cam_loc[1], (float)S.cam_loc[2], kMinIsectDepth);
+    r.dir = make_float4(out[0], out[1], out[2], CUDART_INF_F);
+    return r;
+}
+
 __device__ __forceinline__ QRay camera_ray(const DeviceScene& S, double x, double y, int width, int height)
 {
     return camera_ray_xy(S, x / (double)width - 0.5, 0.5 - y / (double)height);
@@ -137,14 +202,20 @@ __device__ __forceinline__ QRay camera_ray(const DeviceScene& S, double x, doubl
 
 // The offsets of every column and row of the image for pixel centres
 // (mode 0: x + 0.5) or corners (mode 1: x), width + 1 then height + 1
-// entries: k_camera looks them up instead of dividing per pixel.
-__global__ void k_cam_table(int width, int height, double off, double* __restrict__ tab)
+// entries, formed in FP64 and kept as double-floats (hi, lo): k_camera
+// looks them up instead of dividing per pixel.
+__global__ void k_cam_table(int width, int height, double off, float2* __restrict__ tab)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v;
     if (i <= width)
-        tab[i] = ((double)i + off) / (double)width - 0.5;
+        v = ((double)i + off) / (double)width - 0.5;
     else if (i <= width + 1 + height)
-        tab[i] = 0.5 - ((double)(i - width - 1) + off) / (double)height;
+        v = 0.5 - ((double)(i - width - 1) + off) / (double)height;
+    else
+        return;
+    const float hi = (float)v;
+    tab[i] = make_float2(hi, (float)(v - (double)hi));
 }
 
 // mode 0: pixel centres (x+0.5, y+0.5) of every block, block order
@@ -155,7 +226,7 @@ __global__ void k_camera(DeviceScene S, int mode, const int4* __restrict__ block
                          const int* __restrict__ block_off, int nblocks, const double2* __restrict__ pos,
                          const int* __restrict__ npos, int width, int height, QRay* __restrict__ q,
                          int* __restrict__ q_path, PathState* __restrict__ paths, int* __restrict__ q_count,
-                         unsigned long long* stats, uint2* __restrict__ q_skip, int cap, const double* __restrict__ tab)
+                         unsigned long long* stats, uint2* __restrict__ q_skip, int cap, const float2* __restrict__ tab)
 {
     int n = min(mode == 2 ? *npos : block_off[nblocks], cap);   // never past the queue buffers
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -165,12 +236,10 @@ __global__ void k_camera(DeviceScene S, int mode, const int4* __restrict__ block
     }
     if (i >= n)
         return;
-    double x, y;
     int path = i;
     if (mode == 2) {
-        double2 p = pos[i];
-        x = p.x;
-        y = p.y;
+        const double2 p = pos[i];
+        q[i] = camera_ray(S, p.x, p.y, width, height);
     } else {
         int lo = 0, hi = nblocks - 1;   // block containing sample i
         while (lo < hi) {
@@ -191,10 +260,8 @@ __global__ void k_camera(DeviceScene S, int mode, const int4* __restrict__ block
             ly = (tile >> 2) * 4 + (lane >> 3);
             path = block_off[lo] + ly * w + lx;
         }
-        x = tab[b.x + lx];
-        y = tab[width + 1 + b.y + ly];
+        q[i] = camera_ray_ff(S, tab[b.x + lx], tab[width + 1 + b.y + ly]);
     }
-    q[i] = mode == 2 ? camera_ray(S, x, y, width, height) : camera_ray_xy(S, x, y);
     q_path[i] = path;
     q_skip[i] = make_uint2(NO_PRIM, 0u);
     PathState p;
@@ -3429,7 +3496,7 @@ cudaError_t launch_refine(const DeviceScene& S, const double* org, const double*
 cudaError_t launch_camera(const DeviceScene& S, int mode, const int4* blocks, const int* block_off, int nblocks,
                           const double2* pos, const int* npos, int max_samples, int width, int height, QRay* q,
                           int* q_path, PathState* paths, int* q_count, unsigned long long* stats, uint2* q_skip,
-                          double* tab, cudaStream_t st)
+                          float2* tab, cudaStream_t st)
 {
     if (mode != 2)
         k_cam_table<<<cdiv(width + height + 2, 256), 256, 0, st>>>(width, height, mode == 0 ? 0.5 : 0.0, tab);

@@ -10,7 +10,7 @@ namespace povgpu {
 cudaError_t launch_camera(const DeviceScene& S, int mode, const int4* blocks, const int* block_off, int nblocks,
                           const double2* pos, const int* npos, int max_samples, int width, int height, QRay* q,
                           int* q_path, PathState* paths, int* q_count, unsigned long long* stats, uint2* q_skip,
-                          double* tab /* width + height + 2 doubles (modes 0, 1) */,
+                          float2* tab /* width + height + 2 double-floats (modes 0, 1) */,
                           cudaStream_t st);
 cudaError_t launch_load_rays(const double* org, const double* dir, int n, QRay* q, int* q_count, cudaStream_t st);
 cudaError_t launch_trace(const DeviceScene& S, bool any_hit, const QRay* q, const int* q_count, int* work,
