@@ -232,6 +232,12 @@ typedef struct PovGpuPattern {
     double  crackle_metric;       /* crackle: metric (2 by default)                  */
     double  crackle_offset;       /* crackle: offset (0 by default)                  */
     double  control0, control1;   /* quilted: control0, control1 (1, 1; SNGL)        */
+    /* each colour map entry's filter and transmit (TransColour): a pigment
+     * with a non-zero one makes its surface transparent where the blended
+     * colour filters or transmits (Post_Pigment's HAS_FILTER: the object is
+     * not OPAQUE_FLAG) */
+    float   filters[POV_PATTERN_MAX_ENTRIES];
+    float   transmits[POV_PATTERN_MAX_ENTRIES];
 } PovGpuPattern;
 
 /* Normal perturbation (TNORMAL, source/core/material/pattern.h; applied by

@@ -2175,22 +2175,31 @@ static double pattern_value(const PovGpuPattern* pt, V3 T)
     return value;
 }
 
-static RGB pattern_pigment(const PovGpuPattern* pt, V3 P)
+/* The colour map at the pattern's value (BlendMap::Search and the linear
+ * blend, pattern.cpp:1068-1109): rgb, and through `ft` (when given) the
+ * entry's filter and transmit blended the same way. */
+static RGB pattern_pigment_ft(const PovGpuPattern* pt, V3 P, float ft[2])
 {
     const double value = pattern_value(pt, pattern_warp(pt, P));
     const int n = pt->num_entries;
     RGB c;
-    if (value >= pt->values[n - 1]) {
-        c.r = pt->colours[n - 1][0]; c.g = pt->colours[n - 1][1]; c.b = pt->colours[n - 1][2];
-        return c;
-    }
     int ip = 0, in = 0;
-    while (value > pt->values[in]) {
-        ip = in;
-        in++;
+    if (value >= pt->values[n - 1]) {
+        ip = in = n - 1;
+    } else {
+        while (value > pt->values[in]) {
+            ip = in;
+            in++;
+        }
+        if (value == pt->values[in])
+            ip = in;
     }
-    if (value == pt->values[in] || ip == in) {
+    if (ip == in) {
         c.r = pt->colours[in][0]; c.g = pt->colours[in][1]; c.b = pt->colours[in][2];
+        if (ft) {
+            ft[0] = pt->filters[in];
+            ft[1] = pt->transmits[in];
+        }
         return c;
     }
     const double pw = ((double)pt->values[in] - value) / ((double)pt->values[in] - (double)pt->values[ip]);
@@ -2198,7 +2207,22 @@ static RGB pattern_pigment(const PovGpuPattern* pt, V3 P)
     c.r = pt->colours[ip][0] * wp + pt->colours[in][0] * wn;
     c.g = pt->colours[ip][1] * wp + pt->colours[in][1] * wn;
     c.b = pt->colours[ip][2] * wp + pt->colours[in][2] * wn;
+    if (ft) {
+        ft[0] = pt->filters[ip] * wp + pt->filters[in] * wn;
+        ft[1] = pt->transmits[ip] * wp + pt->transmits[in] * wn;
+    }
     return c;
+}
+
+static RGB pattern_pigment(const PovGpuPattern* pt, V3 P) { return pattern_pigment_ft(pt, P, NULL); }
+
+/* a colour map with an entry that filters or transmits (HAS_FILTER) */
+static int pattern_transparent(const PovGpuPattern* pt)
+{
+    for (int k = 0; k < pt->num_entries; k++)
+        if (pt->filters[k] != 0.0f || pt->transmits[k] != 0.0f)
+            return 1;
+    return 0;
 }
 
 /* MInvTransNormal (matrix.cpp:495-508): temp[i] = v . M[i][0..2]; with the
@@ -2314,10 +2338,35 @@ static int container_media(const PovOracle* S, int32_t oi)
 
 /* Transparent surfaces.  TransColour::TransmittedColour (colour.h:1912):
  * pigment * filter + transmit, in float. */
-static void transmitted_colour(const PovGpuMaterial* m, const float pig[3], float out[3])
+static void transmitted_colour(const float pig[3], float filt, float trm, float out[3])
 {
     for (int k = 0; k < 3; k++)
-        out[k] = pig[k] * m->pigment[3] + m->pigment[4];
+        out[k] = pig[k] * filt + trm;
+}
+
+/* a material that can filter or transmit: its plain pigment, or an entry
+ * of its pattern's colour map */
+static int material_transparent(const PovGpuSceneDesc* d, const PovGpuMaterial* m)
+{
+    if (m->pattern > 0)
+        return pattern_transparent(&d->patterns[m->pattern - 1]);
+    return m->pigment[3] != 0.0f || m->pigment[4] != 0.0f;
+}
+
+/* the pigment at P with its filter and transmit (the plain pigment's, or
+ * the colour map's there) */
+static RGB material_pigment(const PovOracle* S, const PovGpuMaterial* m, V3 P, float* filt, float* trm)
+{
+    RGB c = {m->pigment[0], m->pigment[1], m->pigment[2]};
+    *filt = m->pigment[3];
+    *trm = m->pigment[4];
+    if (m->pattern > 0) {
+        float ft[2];
+        c = pattern_pigment_ft(&S->desc.patterns[m->pattern - 1], P, ft);
+        *filt = ft[0];
+        *trm = ft[1];
+    }
+    return c;
 }
 
 /* Object::IsOpaque (OPAQUE_FLAG, parser.cpp:9296-9297): a leaf whose plain
@@ -2331,8 +2380,7 @@ static int object_opaque(const PovOracle* S, int32_t oi)
                 return 0;
         return 1;
     }
-    const PovGpuMaterial* m = object_material(S, oi);
-    return m->pigment[3] == 0.0f && m->pigment[4] == 0.0f;
+    return !material_transparent(&S->desc, object_material(S, oi));
 }
 
 /* Ray::IsInterior: the current ray's interior list holds `id`. */
@@ -2396,11 +2444,13 @@ static int shadow_trace(const PovOracle* S, Thread* th, V3 P, V3 L, double dist,
              * gone and the object (the CSG it belongs to) is opaque
              * (TracePointLightShadowRay, trace.cpp:2040-2072). */
             const PovGpuMaterial* m = object_material(S, is.object);
-            if (m->pigment[3] == 0.0f && m->pigment[4] == 0.0f) {
+            float filt, trm;
+            const RGB pc = material_pigment(S, m, is.ipoint, &filt, &trm);
+            if (filt == 0.0f && trm == 0.0f) {
                 lc[0] = lc[1] = lc[2] = 0.0;
             } else {
-                float pig[3] = {m->pigment[0], m->pigment[1], m->pigment[2]}, fc[3];
-                transmitted_colour(m, pig, fc);
+                float pig[3] = {pc.r, pc.g, pc.b}, fc[3];
+                transmitted_colour(pig, filt, trm, fc);
                 const int id = S->obj_int[is.object];
                 const PovGpuInterior* I = &S->ints[id];
                 int in = -1;
@@ -2798,9 +2848,8 @@ static void shade(const PovOracle* S, Thread* th, const Isect* is, V3 D, double 
         raw = vmul(raw, -1.0);
     V3 N = raw;
     V3 ip = is->ipoint;
-    RGB pig = {m->pigment[0], m->pigment[1], m->pigment[2]};
-    if (m->pattern > 0)
-        pig = pattern_pigment(&S->desc.patterns[m->pattern - 1], is->ipoint);
+    float filt, trm;   /* the layer's filter and transmit at the hit */
+    RGB pig = material_pigment(S, m, is->ipoint, &filt, &trm);
     if (m->normal > 0) {
         const PovGpuNormal* nm = &S->desc.normals[m->normal - 1];
         N = perturb_normal(nm, &S->desc.patterns[nm->pattern - 1], ip, raw);
@@ -2809,7 +2858,7 @@ static void shade(const PovOracle* S, Thread* th, const Isect* is, V3 D, double 
     /* a transparent layer's own light is scaled by its opacity, 1 - filter -
      * transmit (TransColour::Opacity; LegacyOpacity before 3.7,
      * trace.cpp:877-881) */
-    const float filt = m->pigment[3], trm = m->pigment[4];
+
     const int see_through = filt != 0.0f || trm != 0.0f;
     double att = 1.0;
     if (see_through)
@@ -2954,7 +3003,7 @@ static void shade(const PovOracle* S, Thread* th, const Isect* is, V3 D, double 
     int tir = 0;
     if (see_through) {
         float pf[3] = {pig.r, pig.g, pig.b}, fil[3];
-        transmitted_colour(m, pf, fil);
+        transmitted_colour(pf, filt, trm, fil);
         if (m->conserve_energy) {
             /* conserve_energy: the filter loses what the surface reflects
              * (trace.cpp:1070-1075) */
@@ -3964,17 +4013,16 @@ int pov_oracle_create(const PovGpuSceneDesc* desc, PovOracle** out, int32_t* bad
         int used_by_container = 0;
         for (int k = 0; k < desc->num_objects; k++)
             used_by_container = used_by_container || (desc->objects[k].media > 0 && desc->objects[k].material == i);
-        if ((m->pigment[3] != 0.0f || m->pigment[4] != 0.0f) && !used_by_container) {
-            if (m->pattern != 0)
-                return POV_GPU_E_UNSUPPORTED;
+        if (material_transparent(desc, m) && !used_by_container)
             transparent = 1;
-        }
     }
     /* the classic finish terms; fresnel reflection and conserve_energy on
      * transparent surfaces only (they need the surface's interior) */
     for (int i = 0; i < desc->num_materials; i++) {
         const PovGpuMaterial* m = &desc->materials[i];
-        const int see = m->pigment[3] != 0.0f || m->pigment[4] != 0.0f;
+        const int see = m->pattern > 0 && m->pattern <= desc->num_patterns && desc->patterns
+                            ? pattern_transparent(&desc->patterns[m->pattern - 1])
+                            : (m->pigment[3] != 0.0f || m->pigment[4] != 0.0f);
         if (m->fresnel != 0.0f || m->metallic != 0.0f || m->reflect_metallic != 0.0f || m->reflect_exp != 1.0f ||
             m->irid != 0.0f || m->crand != 0.0f || m->diffuse_back != 0.0f ||
             ((m->reflection_fresnel || m->conserve_energy) && !see))

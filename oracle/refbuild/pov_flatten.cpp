@@ -209,8 +209,8 @@ struct Walker
                 return Fail(index, "colour map size");
             d.num_entries = (int32_t)e.size();
             for (size_t k = 0; k < e.size(); k++) {
-                if (e[k].Vals.filter() != 0.0f || e[k].Vals.transm() != 0.0f)
-                    return Fail(index, "colour map entry with filter or transmit");
+                d.filters[k] = e[k].Vals.filter();
+                d.transmits[k] = e[k].Vals.transm();
                 d.values[k] = e[k].value;
                 d.colours[k][0] = e[k].Vals.colour().Red();
                 d.colours[k][1] = e[k].Vals.colour().Green();

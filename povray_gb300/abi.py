@@ -114,7 +114,8 @@ class PovGpuPattern(C.Structure):
                 ("colours", (C.c_float * 3) * POV_PATTERN_MAX_ENTRIES),
                 ("brick_size", C.c_double * 3), ("mortar", C.c_double), ("arms", C.c_int32),
                 ("crackle_solid", C.c_int32), ("crackle_form", C.c_double * 3), ("crackle_metric", C.c_double),
-                ("crackle_offset", C.c_double), ("control0", C.c_double), ("control1", C.c_double)]
+                ("crackle_offset", C.c_double), ("control0", C.c_double), ("control1", C.c_double),
+                ("filters", C.c_float * POV_PATTERN_MAX_ENTRIES), ("transmits", C.c_float * POV_PATTERN_MAX_ENTRIES)]
 
 
 class PovGpuLight(C.Structure):

@@ -920,17 +920,17 @@ bool host_inside(const PovGpuSceneDesc* d, int i, const double* P)
 // containers, radiosity or area lights beside them; the camera inside no
 // object (its rays start with an empty interior list); a ray inside at most
 // RIN_MAX interiors (checked on the device).  Sets *transparent.
+bool material_transparent(const PovGpuSceneDesc* d, const PovGpuMaterial& m);
+
 int validate_transparency(const PovGpuSceneDesc* d, const std::vector<char>& cmat, bool* transparent,
                           int32_t* bad)
 {
     *transparent = false;
     for (int i = 0; i < d->num_materials; i++) {
         const PovGpuMaterial& m = d->materials[i];
-        if (cmat[i] || (m.pigment[3] == 0.0f && m.pigment[4] == 0.0f))
+        if (cmat[i] || !material_transparent(d, m))
             continue;
         *transparent = true;
-        if (m.pattern != 0)
-            return POV_GPU_E_UNSUPPORTED;
     }
     if (d->num_interiors < 0 || (d->num_interiors > 0 && !d->interiors))
         return POV_GPU_E_INVALID;
@@ -1061,7 +1061,7 @@ int validate(const PovGpuSceneDesc* d, int32_t* bad)
         // the classic finish terms; fresnel reflection and conserve_energy
         // on transparent surfaces only, whose interiors the device holds
         // (transparency: validate_transparency)
-        const bool see = m.pigment[3] != 0.0f || m.pigment[4] != 0.0f;
+        const bool see = material_transparent(d, m);
         if (m.fresnel != 0.0f || m.metallic != 0.0f || m.reflect_metallic != 0.0f || m.reflect_exp != 1.0f ||
             m.irid != 0.0f || m.crand != 0.0f || m.diffuse_back != 0.0f ||
             ((m.reflection_fresnel || m.conserve_energy) && !see))
@@ -1115,6 +1115,20 @@ int validate(const PovGpuSceneDesc* d, int32_t* bad)
     return POV_GPU_OK;
 }
 
+// A material that can filter or transmit: its plain pigment does, or (with
+// a pattern) an entry of the colour map does (Post_Pigment's HAS_FILTER).
+bool material_transparent(const PovGpuSceneDesc* d, const PovGpuMaterial& m)
+{
+    if (m.pattern > 0 && m.pattern <= d->num_patterns && d->patterns) {
+        const PovGpuPattern& pt = d->patterns[m.pattern - 1];
+        for (int k = 0; k < pt.num_entries && k < POV_PATTERN_MAX_ENTRIES; k++)
+            if (pt.filters[k] != 0.0f || pt.transmits[k] != 0.0f)
+                return true;
+        return false;
+    }
+    return m.pigment[3] != 0.0f || m.pigment[4] != 0.0f;
+}
+
 DevMaterial make_material(const PovGpuMaterial& m, const float* ambient_light, bool radiosity, int language_version)
 {
     DevMaterial d{};
@@ -1144,7 +1158,7 @@ DevMaterial make_material(const PovGpuMaterial& m, const float* ambient_light, b
     d.pattern = m.pattern;
     d.normal = m.normal;
     d.transmit = m.pigment[4];
-    d.see_through = (m.pigment[3] != 0.0f || m.pigment[4] != 0.0f) ? 1 : 0;
+    d.see_through = (m.pigment[3] != 0.0f || m.pigment[4] != 0.0f) ? SEE_PLAIN : 0;
     // TransColour::Opacity (LegacyOpacity before 3.7), in the colour's float
     d.opacity = 1.0f;
     if (d.see_through)
@@ -1623,8 +1637,7 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
     sc->branching = false;
     for (int i = 0; i < d->num_objects; i++) {
         const PovGpuMaterial& m = d->materials[objects[i].material];
-        if (d->objects[i].type < POV_OBJ_UNION && !is_container(d->objects[i]) &&
-            (m.pigment[3] != 0.0f || m.pigment[4] != 0.0f)) {
+        if (d->objects[i].type < POV_OBJ_UNION && !is_container(d->objects[i]) && material_transparent(d, m)) {
             sc->transparent = true;
             for (int k = 0; k < 3; k++)
                 sc->branching = sc->branching || m.reflection_max[k] != 0.0f || m.reflection_min[k] != 0.0f;
@@ -1663,8 +1676,8 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
         int nused = 0;
         for (int i = 0; i < d->num_objects; i++) {
             const PovGpuMaterial& m = d->materials[objects[i].material];
-            if (d->objects[i].type < POV_OBJ_UNION && !is_container(d->objects[i]) &&
-                (m.pigment[3] != 0.0f || m.pigment[4] != 0.0f) && remap[obj_interior[i]] < 0)
+            if (d->objects[i].type < POV_OBJ_UNION && !is_container(d->objects[i]) && material_transparent(d, m) &&
+                remap[obj_interior[i]] < 0)
                 remap[obj_interior[i]] = nused++;
         }
         if (nused > 256)
@@ -1683,8 +1696,7 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
         for (int i = d->num_objects - 1; i >= 0; i--) {
             const PovGpuObject& o = d->objects[i];
             if (o.type < POV_OBJ_UNION) {
-                const PovGpuMaterial& m = d->materials[objects[i].material];
-                opaque[i] = m.pigment[3] == 0.0f && m.pigment[4] == 0.0f;
+                opaque[i] = !material_transparent(d, d->materials[objects[i].material]);
             }
             if (o.parent >= 0 && !opaque[i])
                 opaque[o.parent] = 0;
@@ -1884,9 +1896,12 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
     }
 
     std::vector<DevMaterial> mats((size_t)d->num_materials);
-    for (int i = 0; i < d->num_materials; i++)
+    for (int i = 0; i < d->num_materials; i++) {
         mats[i] = make_material(d->materials[i], d->ambient_light,
                                 d->radiosity.enabled && d->language_version >= 370, d->language_version);
+        if (d->materials[i].pattern > 0 && material_transparent(d, d->materials[i]))
+            mats[i].see_through = SEE_PATTERN | (d->language_version < 370 ? SEE_LEGACY : 0);
+    }
     std::vector<DevLight> lights((size_t)std::max(d->num_lights, 1));
     int num_area = 0;
     for (int i = 0; i < d->num_lights; i++) {
@@ -1999,7 +2014,8 @@ int build_scene(PovGpuScene* sc, const PovGpuSceneDesc* d)
                                  pt.crackle_solid ? 1.f : 0.f);
         for (int k = 0; k < POV_PATTERN_MAX_ENTRIES; k++) {
             q.values[k] = pt.values[k];
-            q.colours[k] = make_float4(pt.colours[k][0], pt.colours[k][1], pt.colours[k][2], 0.f);
+            q.colours[k] = make_float4(pt.colours[k][0], pt.colours[k][1], pt.colours[k][2], pt.filters[k]);
+            q.transmits[k] = pt.transmits[k];
         }
     }
     // normal perturbations: the forward TRANSFORM's 3x3 rows

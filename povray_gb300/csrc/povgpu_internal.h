@@ -83,8 +83,12 @@ struct __align__(16) DevMaterial {
     // transmits at all
     float   transmit;
     float   opacity;
-    int32_t see_through;
+    int32_t see_through;    // SEE_PLAIN | SEE_PATTERN | SEE_LEGACY (0: opaque)
 };
+// DevMaterial::see_through: the plain pigment filters or transmits; the
+// pattern's colour map has an entry that does (filter, transmit and
+// opacity taken per hit); LegacyOpacity (scenes before 3.7)
+constexpr int SEE_PLAIN = 1, SEE_PATTERN = 2, SEE_LEGACY = 4;
 
 // Pattern pigment (Compute_Pigment with a colour map): the inverse TRANSFORM
 // as three columns (q_i = p . col_i + col_i.w), the gradient vector, the
@@ -100,7 +104,8 @@ struct __align__(16) DevPattern {
     float4 crackle;         // crackle form xyz, metric
     float4 crackle2;        // crackle offset, quilted control0, control1, crackle solid (0 / 1)
     float  values[16];
-    float4 colours[16];
+    float4 colours[16];     // rgb, filter
+    float  transmits[16];
 };
 
 // Normal perturbation (Perturb_Normal): the pattern's forward TRANSFORM as

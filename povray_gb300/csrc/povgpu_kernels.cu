@@ -1645,23 +1645,45 @@ __device__ __noinline__ float pattern_value(const DeviceScene& S, const DevPatte
 // Compute_Pigment of a pattern pigment at world point P (pigment.cpp:395-475):
 // the warped point's value through the colour map's linear blend
 // (BlendMap::Search, pattern.cpp:1068-1109).
-__device__ __noinline__ float3 pattern_pigment(const DeviceScene& S, int pi, float3 P)
+// ... and the blended entry's filter and transmit in `ft` (the colours'
+// w holds the filter, `transmits` the transmit).
+__device__ __noinline__ float3 pattern_pigment_ft(const DeviceScene& S, int pi, float3 P, float2& ft)
 {
     const DevPattern& pt = S.patterns[pi];
     const float value = pattern_value(S, pt, pattern_warp(S, pt, P));
     const int n = pt.kind.z;
-    if (value >= pt.values[n - 1])
-        return xyz(pt.colours[n - 1]);
     int ip = 0, in = 0;
-    while (in < n - 1 && value > pt.values[in]) {
-        ip = in;
-        in++;
+    if (value >= pt.values[n - 1]) {
+        ip = in = n - 1;
+    } else {
+        while (in < n - 1 && value > pt.values[in]) {
+            ip = in;
+            in++;
+        }
+        if (value == pt.values[in])
+            ip = in;
     }
-    if (value == pt.values[in] || ip == in)
+    if (ip == in) {
+        ft = make_float2(pt.colours[in].w, pt.transmits[in]);
         return xyz(pt.colours[in]);
+    }
     const float wp = (pt.values[in] - value) / (pt.values[in] - pt.values[ip]), wn = 1.0f - wp;
-    const float3 a = xyz(pt.colours[ip]), b = xyz(pt.colours[in]);
+    const float4 a = pt.colours[ip], b = pt.colours[in];
+    ft = make_float2(a.w * wp + b.w * wn, pt.transmits[ip] * wp + pt.transmits[in] * wn);
     return f3(a.x * wp + b.x * wn, a.y * wp + b.y * wn, a.z * wp + b.z * wn);
+}
+
+__device__ __forceinline__ float3 pattern_pigment(const DeviceScene& S, int pi, float3 P)
+{
+    float2 ft;
+    return pattern_pigment_ft(S, pi, P, ft);
+}
+
+// TransColour::Opacity (LegacyOpacity before 3.7) of a colour whose filter
+// and transmit come from a colour map.
+__device__ __forceinline__ float colour_opacity(const DevMaterial& m, float3 c, float filt, float trm)
+{
+    return (m.see_through & SEE_LEGACY) ? 1.0f - (filt * fmaxf(c.x, fmaxf(c.y, c.z)) + trm) : 1.0f - filt - trm;
 }
 
 // The layer normal of a textured hit (ComputeLightedTexture,
@@ -1911,6 +1933,7 @@ __global__ void __launch_bounds__(128, 4) k_shade(
         uint2 self = make_uint2(h.prim, skip_aux(h));
         bool container = false;
         float3 pigc = f3(0.f, 0.f, 0.f);   // the hit's pigment colour
+        float filt = 0.f, trm = 0.f, opac = 1.f;   // its filter, transmit and opacity
         int hobj = 0;
         if (hit) {
             SurfaceInfo si = surface(S, h, p);
@@ -1925,13 +1948,24 @@ __global__ void __launch_bounds__(128, 4) k_shade(
             if (dot3(N, d) > 0.0f)     // face the ray (trace.cpp:492-494)
                 N = N * -1.0f;
             raw = N;
-            pigc = m->pattern ? pattern_pigment(S, m->pattern - 1, p) : xyz(m->pigment);
+            if (m->see_through & SEE_PATTERN) {   // filter and transmit from the colour map here
+                float2 ft;
+                pigc = pattern_pigment_ft(S, m->pattern - 1, p, ft);
+                filt = ft.x;
+                trm = ft.y;
+                opac = colour_opacity(*m, pigc, filt, trm);
+            } else {
+                pigc = m->pattern ? pattern_pigment(S, m->pattern - 1, p) : xyz(m->pigment);
+                filt = m->pigment.w;
+                trm = m->transmit;
+                opac = m->opacity;
+            }
             if (m->normal)
                 N = perturb_normal(S, m->normal - 1, p, N);
             float4 em = m->emission;
             // a transparent layer's own light is scaled by its opacity
             // (trace.cpp:877-881,1002-1004)
-            const float att = m->opacity;
+            const float att = opac;
             col = container ? f3(0.f, 0.f, 0.f) : f3(pigc.x * em.x * att, pigc.y * em.y * att, pigc.z * em.z * att);
         } else {
             col = xyz(S.background);   // ComputeSky, background only
@@ -1992,7 +2026,7 @@ __global__ void __launch_bounds__(128, 4) k_shade(
                     float3 pig = pigc;
                     if (m->diffuse > 0.0f) {   // ComputeDiffuseColour, trace.cpp:2441-2484
                         float inten = m->brilliance != 1.0f ? powf(fabsf(cs), m->brilliance) : fabsf(cs);
-                        inten *= m->diffuse * m->opacity;
+                        inten *= m->diffuse * opac;
                         contrib = contrib + pig * lc * inten;
                     }
                     // no highlights for radiosity rays nor shadowless lights (trace.cpp:1714)
@@ -2103,8 +2137,7 @@ __global__ void __launch_bounds__(128, 4) k_shade(
         float4 tthr = make_float4(0.f, 0.f, 0.f, 0.f);
         bool tir = false;
         if (shaded && m->see_through && med.q_rin) {
-            float3 fil = f3(pigc.x * m->pigment.w + m->transmit, pigc.y * m->pigment.w + m->transmit,
-                            pigc.z * m->pigment.w + m->transmit);
+            float3 fil = f3(pigc.x * filt + trm, pigc.y * filt + trm, pigc.z * filt + trm);
             if (m->reflect_flags & REFL_CONSERVE)   // the filter loses what is reflected (trace.cpp:1070-1075)
                 fil = fil * f3(fminf(1.0f, 1.0f - reflec.x), fminf(1.0f, 1.0f - reflec.y),
                                fminf(1.0f, 1.0f - reflec.z));
@@ -2748,8 +2781,15 @@ __global__ void __launch_bounds__(128) k_shadow_filter(DeviceScene S, const QRay
             if (!m.see_through) {
                 lc = f3(0.f, 0.f, 0.f);
             } else {
-                const float w = m.pigment.w, tm = m.transmit;
-                float3 fc = f3(m.pigment.x * w + tm, m.pigment.y * w + tm, m.pigment.z * w + tm);
+                float w = m.pigment.w, tm = m.transmit;
+                float3 pc = xyz(m.pigment);
+                if (m.see_through & SEE_PATTERN) {   // the colour map at the crossing
+                    float2 ft;
+                    pc = pattern_pigment_ft(S, m.pattern - 1, o + d * t, ft);
+                    w = ft.x;
+                    tm = ft.y;
+                }
+                float3 fc = f3(pc.x * w + tm, pc.y * w + tm, pc.z * w + tm);
                 const int id = code & 0xffff;
                 const int at = rin_find(rin, id);
                 const float4 I0 = S.interiors[2 * id];

@@ -239,7 +239,9 @@ class Pattern:
         self.mortar = float(mortar)
         self.arms = int(arms)
         self.kind = kind
-        self.colours = [(float(v), tuple(float(c) for c in rgb)) for v, rgb in colours]
+        # entries (value, rgb) or (value, rgb, filter, transmit)
+        self.colours = [(float(e[0]), tuple(float(c) for c in e[1])) for e in colours]
+        self.ft = [(float(e[2]), float(e[3])) if len(e) > 2 else (0.0, 0.0) for e in colours]
         self.transforms = [(op, tuple(float(x) for x in vec)) for op, vec in transforms]
         self.gradient = tuple(float(x) for x in gradient)
         self.noise_generator = noise_generator
@@ -254,7 +256,7 @@ class Pattern:
         """The pigment body; with `amount`, the body of a normal of that
         amount (no colour map, the amount right after the pattern)."""
         if self.kind in self.DISCRETE:
-            body = self.kind + "".join(" color rgb %s" % _v(c) for _, c in self.colours)
+            body = self.kind + "".join(" color %s" % self._colour(k) for k in range(len(self.colours)))
             if self.kind == "brick":
                 body += " brick_size %s mortar %s" % (_v(self.brick_size), _g(self.mortar))
         else:
@@ -264,7 +266,7 @@ class Pattern:
             if amount is not None:
                 body = "%s, %s" % (head, _g(amount))
             else:
-                cmap = " ".join("[%s color rgb %s]" % (_f32(v), _v(c)) for v, c in self.colours)
+                cmap = " ".join("[%s color %s]" % (_f32(v), self._colour(k)) for k, (v, _c) in enumerate(self.colours))
                 body = "%s color_map { %s }" % (head, cmap)
             if self.kind == "agate" and self.agate_turb != 1.0:
                 body += " agate_turb %s" % _g(self.agate_turb)
@@ -294,6 +296,16 @@ class Pattern:
         for op, vec in self.transforms:
             body += " %s %s" % (op, _v(vec))
         return body
+
+    def _colour(self, k):
+        c = self.colours[k][1]
+        f, t = self.ft[k]
+        if f or t:
+            return "rgbft <%s,%s,%s,%s,%s>" % (_g(c[0]), _g(c[1]), _g(c[2]), _g(f), _g(t))
+        return "rgb %s" % _v(c)
+
+    def transparent(self):
+        return any(f or t for f, t in self.ft)
 
     def transform(self):
         t = Transform()
@@ -339,6 +351,7 @@ class Pattern:
         for k, (v, c) in enumerate(self.colours):
             d.values[k] = v
             d.colours[k][:] = c
+            d.filters[k], d.transmits[k] = self.ft[k]
         return d
 
 
@@ -1488,6 +1501,62 @@ def glass_reflective(width=320, height=240, max_trace_level=8):
     s.sphere((2.4, 2.8, 2.0), 0.45, s.material(Material((0.9, 0.9, 0.9), phong=0.6, reflection=0.6)))
     s.sphere((-0.6, 2.5, 2.5), 0.9, glass(filter=0.9), Interior(ior=1.3))             # two overlapping
     s.sphere((0.1, 2.7, 2.3), 0.7, glass((1.0, 1.0, 0.6), filter=0.9), Interior(ior=1.6))
+    return s
+
+
+def glass_patterns(width=320, height=240, max_trace_level=8):
+    """Pattern pigments whose colour maps filter or transmit, so a surface
+    is transparent where the blended colour is: over the checker floor and
+    wall of glass_spheres, a sphere of checker squares alternately clear
+    glass (filter 0.9) and opaque red, a marble sphere with filtering
+    veins, a gradient sphere from opaque blue to transmit 0.8, a bozo
+    sphere of clouded glass (ior 1.4), a crackle ball whose cells transmit,
+    and a glass box with an onion map (ior 1.3); opaque spheres behind;
+    two point lights whose shadows pass through the patterns.  Camera
+    (0,3,-12) looking at (0,0.5,0), 55 deg; max_trace_level 8."""
+    s = Scene("glass_patterns", width, height, (0.0, 3.0, -12.0), (0.0, 0.5, 0.0), 55.0,
+              max_trace_level=max_trace_level)
+    s.point_light((8.0, 14.0, -10.0))
+    s.point_light((-10.0, 9.0, -4.0), (0.5, 0.5, 0.55))
+    floor = Pattern("checker", [(0.0, (0.9, 0.9, 0.85)), (1.0, (0.2, 0.3, 0.55))],
+                    [("scale", (1.0, 1.0, 1.0)), ("translate", (0.0, 0.5, 0.0))])
+    wall = Pattern("checker", [(0.0, (0.85, 0.6, 0.3)), (1.0, (0.95, 0.95, 0.9))],
+                   [("scale", (1.5, 1.5, 1.5)), ("translate", (0.0, 0.0, 0.75))])
+    s.plane((0.0, 1.0, 0.0), -1.0, s.material(Material((1.0, 1.0, 1.0), pattern=floor)))
+    s.plane((0.0, 0.0, -1.0), -9.0, s.material(Material((1.0, 1.0, 1.0), pattern=wall)))
+    for c, r, rgb in (((-3.0, 0.2, 5.0), 1.2, (0.8, 0.2, 0.15)), ((1.5, 0.0, 6.0), 1.0, (0.2, 0.7, 0.25)),
+                      ((4.5, 0.5, 4.0), 1.5, (0.25, 0.3, 0.85))):
+        s.sphere(c, r, s.material(Material(rgb, phong=0.4)))
+    off = ("translate", (0.131, 0.077, 0.219))
+
+    def glass(pattern):
+        return s.material(Material((1.0, 1.0, 1.0), ambient=0.05, diffuse=0.4, phong=0.8, phong_size=80.0,
+                                   pattern=pattern))
+    s.sphere((-4.0, 0.0, 0.0), 1.0, glass(Pattern("checker", [(0, (1.0, 1.0, 1.0), 0.9, 0.0), (1, (0.8, 0.15, 0.1))],
+                                                  [("scale", (0.45, 0.45, 0.45)), off])),
+             Interior(ior=1.5))
+    s.sphere((-1.6, 0.0, -0.5), 1.0,
+             glass(Pattern("marble", [(0.0, (0.95, 0.95, 0.9)), (0.6, (0.9, 0.7, 0.5), 0.7, 0.0),
+                                      (1.0, (0.6, 0.9, 0.7), 0.9, 0.1)],
+                           [("scale", (0.5, 0.5, 0.5)), off], turbulence=(0.6, 0.6, 0.6))),
+             Interior(ior=1.33))
+    s.sphere((0.8, 0.0, 0.0), 1.0, glass(Pattern("gradient", [(0.0, (0.2, 0.3, 0.9)), (1.0, (0.9, 0.9, 1.0), 0.0, 0.8)],
+                                                  [("scale", (2.0, 2.0, 2.0)), ("translate", (0.0, -1.0, 0.0))],
+                                                  gradient=(0.0, 1.0, 0.0))),
+             Interior(ior=1.0))
+    s.sphere((3.2, 0.0, -0.5), 1.0, glass(Pattern("bozo", [(0.0, (0.95, 0.95, 1.0), 0.85, 0.0),
+                                                           (0.7, (0.8, 0.85, 0.9), 0.5, 0.0), (1.0, (0.5, 0.5, 0.55))],
+                                                  [("scale", (0.4, 0.4, 0.4)), off])),
+             Interior(ior=1.4))
+    s.sphere((-2.8, 2.6, 1.5), 0.9, glass(Pattern("crackle", [(0.0, (0.3, 0.2, 0.1)), (0.08, (0.9, 0.8, 0.5), 0.0, 0.7),
+                                                              (1.0, (1.0, 1.0, 0.9), 0.0, 0.9)],
+                                                  [("scale", (0.35, 0.35, 0.35)), off])),
+             Interior(ior=1.0))
+    s.add(Scene.n_box((1.0, 1.8, 1.0), (2.6, 3.4, 2.6),
+                      glass(Pattern("onion", [(0.0, (0.9, 0.95, 1.0), 0.9, 0.0), (0.5, (0.4, 0.6, 0.9), 0.6, 0.0),
+                                              (1.0, (0.9, 0.95, 1.0), 0.9, 0.0)],
+                                    [("scale", (0.5, 0.5, 0.5)), ("translate", (1.8, 2.6, 1.8))])),
+                      interior=Interior(ior=1.3)))
     return s
 
 

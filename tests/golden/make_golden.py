@@ -61,6 +61,7 @@ def cases():
         "light_types_160x120": (scenes.light_types(160, 120), 2, 9.0),
         "glass_reflective_160x120": (scenes.glass_reflective(160, 120), 2, 8.0),
         "patterned_spheres_160x120": (scenes.patterned_spheres(160, 120), 2, 8.0),
+        "glass_patterns_160x120": (scenes.glass_patterns(160, 120), 2, 8.0),
         "media_spheres_160x120": (scenes.media_spheres(160, 120), 2, 9.0),
         "media_hazy_160x120": (scenes.media_spheres(160, 120, scattering_type=2), 4, 9.0),
         "media_murky_160x120": (scenes.media_spheres(160, 120, scattering_type=3), 4, 9.0),
@@ -262,7 +263,8 @@ SCENE_FILE_CASES = ("spheres_plane_320x240", "mesh_spheres_small_160x90", "csg_t
                     "textured_spheres_160x120", "textured_turbulent_perlin_160x120", "bumpy_spheres_160x120",
                     "bumpy_waves_160x120", "shaped_spheres_160x120", "glass_spheres_160x120",
                     "media_sphere_160x120", "media_hg_160x120", "light_types_160x120",
-                    "glass_reflective_160x120", "patterned_spheres_160x120")
+                    "glass_reflective_160x120", "patterned_spheres_160x120",
+                    "glass_patterns_160x120")
 
 
 def write_scene_files(tmp):
