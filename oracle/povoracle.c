@@ -2926,10 +2926,16 @@ static void shade(const PovOracle* S, Thread* th, const Isect* is, V3 D, double 
             one_light_ray(L, ip, &ld, &ldist, lc);
             if (fabs(lc[0]) < EPSILON && fabs(lc[1]) < EPSILON && fabs(lc[2]) < EPSILON)
                 continue;   /* outside a spotlight's cone (trace.cpp:1648-1650) */
+            /* the light behind the surface: diffuse_back lights it from
+             * there, without highlights (trace.cpp:1652-1662,1714) */
+            int backside = 0;
             if (!(o->flags & POV_FLAG_DOUBLE_ILLUM)) {
                 double cs = vdot(N, ld);
-                if (cs < EPSILON)
-                    continue;
+                if (cs < EPSILON) {
+                    if (m->diffuse_back == 0.0f)
+                        continue;
+                    backside = 1;
+                }
             }
             const int fill = L->light_type == POV_LIGHT_TYPE_SHADOWLESS;
             /* TraceShadowRay level check (trace.cpp:1897-1901); a shadowless
@@ -2955,7 +2961,7 @@ static void shade(const PovOracle* S, Thread* th, const Isect* is, V3 D, double 
                 }
             }
             /* ComputeDiffuseColour (trace.cpp:2441-2484) */
-            double diffuse = m->diffuse * m->brilliance_adjust;
+            double diffuse = (backside ? m->diffuse_back : m->diffuse) * m->brilliance_adjust;
             if (diffuse > 0.0) {
                 double ci = vdot(N, ld);
                 double inten = m->brilliance != 1.0f ? pow(fabs(ci), m->brilliance) : fabs(ci);
@@ -2966,7 +2972,7 @@ static void shade(const PovOracle* S, Thread* th, const Isect* is, V3 D, double 
             }
             /* ComputePhongColour (trace.cpp:2520-2558); not for radiosity
              * rays nor shadowless lights (trace.cpp:1714) */
-            if (m->phong > 0.0f && !(flags & RAY_RADIOSITY) && !fill) {
+            if (m->phong > 0.0f && !(flags & RAY_RADIOSITY) && !fill && !backside) {
                 double c2 = -2.0 * vdot(D, N);
                 V3 rd = vadd(D, vmul(N, c2));
                 double ci = vdot(rd, ld);
@@ -2979,7 +2985,7 @@ static void shade(const PovOracle* S, Thread* th, const Isect* is, V3 D, double 
             }
             /* ComputeSpecularColour (trace.cpp:2560-2593); not for radiosity
              * rays nor shadowless lights */
-            if (m->specular > 0.0f && !(flags & RAY_RADIOSITY) && !fill) {
+            if (m->specular > 0.0f && !(flags & RAY_RADIOSITY) && !fill && !backside) {
                 V3 half = vmul(vadd(vmul(D, -1.0), ld), 0.5);
                 double hl = vlen(half);
                 if (hl > 0.0) {
@@ -4024,7 +4030,7 @@ int pov_oracle_create(const PovGpuSceneDesc* desc, PovOracle** out, int32_t* bad
                             ? pattern_transparent(&desc->patterns[m->pattern - 1])
                             : (m->pigment[3] != 0.0f || m->pigment[4] != 0.0f);
         if (m->fresnel != 0.0f || m->metallic != 0.0f || m->reflect_metallic != 0.0f || m->reflect_exp != 1.0f ||
-            m->irid != 0.0f || m->crand != 0.0f || m->diffuse_back != 0.0f ||
+            m->irid != 0.0f || m->crand != 0.0f || (m->diffuse_back != 0.0f && desc->radiosity.enabled) ||
             ((m->reflection_fresnel || m->conserve_energy) && !see))
             return POV_GPU_E_UNSUPPORTED;
     }

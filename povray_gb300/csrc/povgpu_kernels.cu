@@ -2003,14 +2003,18 @@ __global__ void __launch_bounds__(128, 4) k_shade(
                 set_error(err, DE_QUEUE_OVERFLOW);
             }
         }
-        // per-light terms (ComputeOneDiffuseLight, trace.cpp:1637-1729)
+        // per-light terms (ComputeOneDiffuseLight, trace.cpp:1637-1729), for
+        // a finish with a diffuse, back-diffuse, specular or phong term
+        // (trace.cpp:1017-1021)
+        const bool lights_on = shaded && (m->diffuse != 0.0f || m->diffuse_back != 0.0f || m->specular != 0.0f ||
+                                          m->phong != 0.0f);
         for (int l = 0; l < nl; l++) {
             bool emit = false;
             float3 contrib = f3(0.f, 0.f, 0.f);
             float3 ld = f3(0.f, 0.f, 1.f);
             float ldist = 0.f, latt = 1.f;
             bool area = false, fill = false;
-            if (shaded) {
+            if (lights_on) {
                 const DevLight& L = S.lights[l];
                 // the radiosity Trace runs with area lights off
                 // (GetRadiosityQualityFlags, radiosity.cpp:148-161)
@@ -2019,25 +2023,30 @@ __global__ void __launch_bounds__(128, 4) k_shade(
                 light_ray(L, p, ld, ldist);
                 latt = attenuate_light(L, p, ld, ldist);
                 float cs = dot3(N, ld);
-                bool lit = (oflags & 16) || cs >= EPSILON_F;
+                // a light behind the surface lights it through diffuse_back,
+                // without highlights (trace.cpp:1652-1662,1714)
+                const bool back = !(oflags & 16) && cs < EPSILON_F;
+                bool lit = !back || m->diffuse_back != 0.0f;
                 float3 lc = xyz(L.colour) * latt;
                 if (lit && !(fabsf(lc.x) < EPSILON_F && fabsf(lc.y) < EPSILON_F && fabsf(lc.z) < EPSILON_F)) {
                     emit = true;
                     float3 pig = pigc;
-                    if (m->diffuse > 0.0f) {   // ComputeDiffuseColour, trace.cpp:2441-2484
+                    const float dif = back ? m->diffuse_back : m->diffuse;
+                    if (dif > 0.0f) {   // ComputeDiffuseColour, trace.cpp:2441-2484
                         float inten = m->brilliance != 1.0f ? powf(fabsf(cs), m->brilliance) : fabsf(cs);
-                        inten *= m->diffuse * opac;
+                        inten *= dif * opac;
                         contrib = contrib + pig * lc * inten;
                     }
-                    // no highlights for radiosity rays nor shadowless lights (trace.cpp:1714)
-                    if (m->phong > 0.0f && !rad.gather && !fill) {     // ComputePhongColour, trace.cpp:2520-2558
+                    // no highlights for radiosity rays, shadowless lights or
+                    // the back side (trace.cpp:1714)
+                    if (m->phong > 0.0f && !rad.gather && !fill && !back) {     // ComputePhongColour, trace.cpp:2520-2558
                         float c2 = -2.0f * dot3(d, N);
                         float3 rd = d + N * c2;
                         float ci = dot3(rd, ld);
                         if (ci > 0.0f && (m->phong_size < 60.0f || ci > 0.0008f))
                             contrib = contrib + lc * (m->phong * powf(ci, m->phong_size));
                     }
-                    if (m->specular > 0.0f && !rad.gather && !fill) {  // ComputeSpecularColour, trace.cpp:2560-2593
+                    if (m->specular > 0.0f && !rad.gather && !fill && !back) {  // ComputeSpecularColour, trace.cpp:2560-2593
                         float3 half = (ld - d) * 0.5f;
                         float hl = sqrtf(dot3(half, half));
                         if (hl > 0.0f) {

@@ -394,12 +394,13 @@ class Material:
     def __init__(self, rgb, ambient=0.1, diffuse=0.6, phong=0.0, phong_size=40.0,
                  specular=0.0, roughness=0.05, reflection=0.0, brilliance=1.0,
                  emission=0.0, transmit=0.0, pattern=None, normal=None, filter=0.0,
-                 reflection_min=None, fresnel=False, conserve_energy=False):
+                 reflection_min=None, fresnel=False, conserve_energy=False, diffuse_back=0.0):
         """`reflection` alone is the old syntax (min = max); with
         `reflection_min` or `fresnel` the finish takes the block form
         reflection { min, max fresnel } (Parse_Finish,
         source/parser/parser_materials.cpp:2288-2348).  conserve_energy:
         the transmitted light loses what the surface reflects."""
+        self.diffuse_back = float(diffuse_back)   # `diffuse A, B`: B lights the back side
         self.reflection_min = None if reflection_min is None else float(reflection_min)
         self.fresnel = bool(fresnel)
         self.conserve_energy = bool(conserve_energy)
@@ -420,6 +421,8 @@ class Material:
 
     def sdl(self):
         fin = "ambient %s diffuse %s" % (_g(self.ambient), _g(self.diffuse))
+        if self.diffuse_back:
+            fin += ", %s" % _g(self.diffuse_back)
         if self.brilliance != 1.0:
             fin += " brilliance %s" % _g(self.brilliance)
         if self.phong:
@@ -453,7 +456,7 @@ class Material:
         m.ambient[:] = [self.ambient] * 3
         m.emission[:] = [self.emission] * 3
         m.diffuse = self.diffuse
-        m.diffuse_back = 0.0
+        m.diffuse_back = self.diffuse_back
         m.brilliance = self.brilliance
         m.brilliance_adjust = 1.0
         m.brilliance_adjust_rad = 2.0 / (self.brilliance + 1.0)
@@ -1557,6 +1560,27 @@ def glass_patterns(width=320, height=240, max_trace_level=8):
                                               (1.0, (0.9, 0.95, 1.0), 0.9, 0.0)],
                                     [("scale", (0.5, 0.5, 0.5)), ("translate", (1.8, 2.6, 1.8))])),
                       interior=Interior(ior=1.3)))
+    return s
+
+
+def backlit_sheets(width=320, height=240):
+    """Back-side diffuse light (finish { diffuse A, B }): thin boxes
+    (translucent sheets, diffuse 0.5, 0.4) and spheres (diffuse 0.6, 0.3,
+    phong 0.5) between the camera and a point light behind them, a second
+    light in front, a box with plain diffuse for contrast, over a floor
+    plane y=-1.5; camera (0,1.5,-9) looking at (0,0.5,0), 50 deg."""
+    s = Scene("backlit_sheets", width, height, (0.0, 1.5, -9.0), (0.0, 0.5, 0.0), 50.0, max_trace_level=3)
+    s.point_light((1.0, 4.0, 8.0), (1.2, 1.1, 0.9))
+    s.point_light((-6.0, 5.0, -6.0), (0.4, 0.4, 0.45))
+    s.plane((0.0, 1.0, 0.0), -1.5, s.material(Material((0.7, 0.75, 0.7))))
+    leaf = s.material(Material((0.4, 0.8, 0.3), ambient=0.05, diffuse=0.5, diffuse_back=0.4))
+    paper = s.material(Material((0.95, 0.9, 0.8), ambient=0.05, diffuse=0.5, diffuse_back=0.6))
+    s.add(Scene.n_box((-3.5, -1.0, 1.0), (-1.5, 2.0, 1.05), leaf))
+    s.add(Scene.n_box((1.2, -0.5, 0.5), (3.4, 2.5, 0.55), paper))
+    s.add(Scene.n_box((-0.9, -1.0, 2.0), (0.9, 1.0, 2.05), s.material(Material((0.9, 0.3, 0.3)))))
+    for c, r, rgb in (((-2.5, 0.0, -1.5), 0.7, (0.9, 0.6, 0.2)), ((0.2, 0.3, -2.0), 0.6, (0.3, 0.5, 0.9)),
+                      ((2.3, 0.0, -1.0), 0.8, (0.8, 0.8, 0.8))):
+        s.sphere(c, r, s.material(Material(rgb, diffuse=0.6, diffuse_back=0.3, phong=0.5)))
     return s
 
 
