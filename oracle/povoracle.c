@@ -2819,6 +2819,21 @@ static double fresnel_r(double cos_ti, double n)
     return f < 0.0 ? 0.0 : (f > 1.0 ? 1.0 : f);
 }
 
+/* ComputeMetallic (trace.cpp:2658-2671): colour c moved towards the
+ * pigment by `metallic`, less towards grazing angles (float channels). */
+static void compute_metallic(float c[3], double metallic, RGB pig, double cos_angle)
+{
+    if (metallic == 0.0)
+        return;
+    const double x = fabs(acos(cos_angle)) / (M_PI_D / 2.0);
+    double F = 0.014567225 / ((x - 1.12) * (x - 1.12)) - 0.011612903;
+    F = fmin(1.0, fmax(0.0, F));
+    const double k = metallic * (1.0 - F);
+    const float p[3] = {pig.r, pig.g, pig.b};
+    for (int i = 0; i < 3; i++)
+        c[i] *= (float)(1.0 + (float)((float)(p[i] - 1.0) * k));
+}
+
 /* ComputeTextureColour + ComputeLightedTexture (trace.cpp:457-586,739-1179)
  * for one plain layer; a pigment that filters or transmits gives its own
  * light scaled by its opacity and passes the transmitted ray's colour
@@ -2892,6 +2907,11 @@ static void shade(const PovOracle* S, Thread* th, const Isect* is, V3 D, double 
         reflec.g = (float)(f * rx[1]) + (float)((1.0 - f) * rn[1]);
         reflec.b = (float)(f * rx[2]) + (float)((1.0 - f) * rn[2]);
         rweight = weight * fmax(fmax(reflec.r, reflec.g), reflec.b);
+    }
+    if (m->reflect_metallic != 0.0f) {   /* ComputeMetallic on the reflectivity (trace.cpp:870) */
+        float rc[3] = {reflec.r, reflec.g, reflec.b};
+        compute_metallic(rc, m->reflect_metallic, pig, cos_inc);
+        reflec.r = rc[0]; reflec.g = rc[1]; reflec.b = rc[2];
     }
 
     /* radiosity ambient (trace.cpp:793-800,896-980): one query per hit
@@ -2978,9 +2998,11 @@ static void shade(const PovOracle* S, Thread* th, const Isect* is, V3 D, double 
                 double ci = vdot(rd, ld);
                 if (ci > 0.0 && (m->phong_size < 60 || ci > 0.0008)) {
                     double inten = m->phong * pow(ci, (double)m->phong_size);
-                    r += inten * lc[0];
-                    g += inten * lc[1];
-                    b += inten * lc[2];
+                    float cs[3] = {1.0f, 1.0f, 1.0f};
+                    compute_metallic(cs, m->metallic, pig, vdot(N, ld));
+                    r += inten * lc[0] * cs[0];
+                    g += inten * lc[1] * cs[1];
+                    b += inten * lc[2] * cs[2];
                 }
             }
             /* ComputeSpecularColour (trace.cpp:2560-2593); not for radiosity
@@ -2992,9 +3014,11 @@ static void shade(const PovOracle* S, Thread* th, const Isect* is, V3 D, double 
                     double ci = vdot(half, N) / hl;
                     if (ci > 0.0) {
                         double inten = m->specular * pow(ci, (double)m->roughness);
-                        r += inten * lc[0];
-                        g += inten * lc[1];
-                        b += inten * lc[2];
+                        float cs[3] = {1.0f, 1.0f, 1.0f};
+                        compute_metallic(cs, m->metallic, pig, vdot(half, ld) / hl);
+                        r += inten * lc[0] * cs[0];
+                        g += inten * lc[1] * cs[1];
+                        b += inten * lc[2] * cs[2];
                     }
                 }
             }
@@ -4029,7 +4053,7 @@ int pov_oracle_create(const PovGpuSceneDesc* desc, PovOracle** out, int32_t* bad
         const int see = m->pattern > 0 && m->pattern <= desc->num_patterns && desc->patterns
                             ? pattern_transparent(&desc->patterns[m->pattern - 1])
                             : (m->pigment[3] != 0.0f || m->pigment[4] != 0.0f);
-        if (m->fresnel != 0.0f || m->metallic != 0.0f || m->reflect_metallic != 0.0f || m->reflect_exp != 1.0f ||
+        if (m->fresnel != 0.0f || m->reflect_exp != 1.0f ||
             m->irid != 0.0f || m->crand != 0.0f || (m->diffuse_back != 0.0f && desc->radiosity.enabled) ||
             ((m->reflection_fresnel || m->conserve_energy) && !see))
             return POV_GPU_E_UNSUPPORTED;

@@ -1062,7 +1062,7 @@ int validate(const PovGpuSceneDesc* d, int32_t* bad)
         // on transparent surfaces only, whose interiors the device holds
         // (transparency: validate_transparency)
         const bool see = material_transparent(d, m);
-        if (m.fresnel != 0.0f || m.metallic != 0.0f || m.reflect_metallic != 0.0f || m.reflect_exp != 1.0f ||
+        if (m.fresnel != 0.0f || m.reflect_exp != 1.0f ||
             m.irid != 0.0f || m.crand != 0.0f || (m.diffuse_back != 0.0f && d->radiosity.enabled) ||
             ((m.reflection_fresnel || m.conserve_energy) && !see))
             return POV_GPU_E_UNSUPPORTED;
@@ -1145,6 +1145,8 @@ DevMaterial make_material(const PovGpuMaterial& m, const float* ambient_light, b
     d.reflect_min = make_float4(m.reflection_min[0], m.reflection_min[1], m.reflection_min[2], std::max(wmax, wmin));
     d.diffuse = m.diffuse * m.brilliance_adjust;
     d.diffuse_back = m.diffuse_back * m.brilliance_adjust;
+    d.metallic = m.metallic;
+    d.reflect_metallic = m.reflect_metallic;
     d.brilliance = m.brilliance;
     d.phong = m.phong;
     d.phong_size = m.phong_size;

@@ -85,6 +85,8 @@ struct __align__(16) DevMaterial {
     float   opacity;
     int32_t see_through;    // SEE_PLAIN | SEE_PATTERN | SEE_LEGACY (0: opaque)
     float   diffuse_back;   // diffuse_back * brilliance_adjust: light from behind the surface
+    float   metallic;       // highlights tinted by the pigment (ComputeMetallic)
+    float   reflect_metallic;   // the reflectivity tinted likewise
 };
 // DevMaterial::see_through: the plain pigment filters or transmits; the
 // pattern's colour map has an entry that does (filter, transmit and

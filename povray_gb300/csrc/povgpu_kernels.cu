@@ -1855,6 +1855,16 @@ __device__ __forceinline__ float attenuate_light(const DevLight& L, float3 p, fl
     return att;
 }
 
+// ComputeMetallic (trace.cpp:2658-2671): the factor that moves a highlight
+// or reflectivity towards the pigment by `metallic`, less towards grazing.
+__device__ __forceinline__ float3 metallic_factor(float metallic, float3 pig, float cos_angle)
+{
+    const float x = fabsf(acosf(fminf(1.0f, fmaxf(-1.0f, cos_angle)))) / 1.57079632679489662f;
+    const float F = fminf(1.0f, fmaxf(0.0f, 0.014567225f / ((x - 1.12f) * (x - 1.12f)) - 0.011612903f));
+    const float k = metallic * (1.0f - F);
+    return f3(1.0f + (pig.x - 1.0f) * k, 1.0f + (pig.y - 1.0f) * k, 1.0f + (pig.z - 1.0f) * k);
+}
+
 // Trace::ComputeRelativeIOR (trace.cpp:2595-2625): the ratio of iors a ray
 // with interior list `rin` sees at a surface of interior `id`.
 __device__ __forceinline__ float relative_ior(const DeviceScene& S, uint64_t rin, int id)
@@ -2043,16 +2053,24 @@ __global__ void __launch_bounds__(128, 4) k_shade(
                         float c2 = -2.0f * dot3(d, N);
                         float3 rd = d + N * c2;
                         float ci = dot3(rd, ld);
-                        if (ci > 0.0f && (m->phong_size < 60.0f || ci > 0.0008f))
-                            contrib = contrib + lc * (m->phong * powf(ci, m->phong_size));
+                        if (ci > 0.0f && (m->phong_size < 60.0f || ci > 0.0008f)) {
+                            float3 h = lc * (m->phong * powf(ci, m->phong_size));
+                            if (m->metallic != 0.0f)
+                                h = h * metallic_factor(m->metallic, pig, dot3(N, ld));
+                            contrib = contrib + h;
+                        }
                     }
                     if (m->specular > 0.0f && !rad.gather && !fill && !back) {  // ComputeSpecularColour, trace.cpp:2560-2593
                         float3 half = (ld - d) * 0.5f;
                         float hl = sqrtf(dot3(half, half));
                         if (hl > 0.0f) {
                             float ci = dot3(half, N) / hl;
-                            if (ci > 0.0f)
-                                contrib = contrib + lc * (m->specular * powf(ci, m->roughness));
+                            if (ci > 0.0f) {
+                                float3 h = lc * (m->specular * powf(ci, m->roughness));
+                                if (m->metallic != 0.0f)
+                                    h = h * metallic_factor(m->metallic, pig, dot3(half, ld) / hl);
+                                contrib = contrib + h;
+                            }
                         }
                     }
                 }
@@ -2115,6 +2133,8 @@ __global__ void __launch_bounds__(128, 4) k_shade(
                 else reflec = rmax * frac + rmin * (1.0f - frac);
                 rweight = weight * m->reflect_min.w;
             }
+            if (m->reflect_metallic != 0.0f)   // ComputeMetallic on the reflectivity (trace.cpp:870)
+                reflec = reflec * metallic_factor(m->reflect_metallic, pigc, cos_inc);
         }
         float3 nd = f3(0.f, 0.f, 1.f);   // the transmitted ray's direction
         // transmitted ray through a container wall: counted like any traced

@@ -394,13 +394,16 @@ class Material:
     def __init__(self, rgb, ambient=0.1, diffuse=0.6, phong=0.0, phong_size=40.0,
                  specular=0.0, roughness=0.05, reflection=0.0, brilliance=1.0,
                  emission=0.0, transmit=0.0, pattern=None, normal=None, filter=0.0,
-                 reflection_min=None, fresnel=False, conserve_energy=False, diffuse_back=0.0):
+                 reflection_min=None, fresnel=False, conserve_energy=False, diffuse_back=0.0, metallic=0.0,
+                 reflect_metallic=0.0):
         """`reflection` alone is the old syntax (min = max); with
         `reflection_min` or `fresnel` the finish takes the block form
         reflection { min, max fresnel } (Parse_Finish,
         source/parser/parser_materials.cpp:2288-2348).  conserve_energy:
         the transmitted light loses what the surface reflects."""
         self.diffuse_back = float(diffuse_back)   # `diffuse A, B`: B lights the back side
+        self.metallic = float(metallic)           # finish { metallic m }: tinted highlights
+        self.reflect_metallic = float(reflect_metallic)   # reflection { ... metallic m }
         self.reflection_min = None if reflection_min is None else float(reflection_min)
         self.fresnel = bool(fresnel)
         self.conserve_energy = bool(conserve_energy)
@@ -429,9 +432,13 @@ class Material:
             fin += " phong %s phong_size %s" % (_g(self.phong), _g(self.phong_size))
         if self.specular:
             fin += " specular %s roughness %s" % (_g(self.specular), _g(self.roughness))
-        if self.reflection_min is not None or self.fresnel:
+        if self.metallic:
+            fin += " metallic %s" % _g(self.metallic)
+        if self.reflection_min is not None or self.fresnel or self.reflect_metallic:
             rmin = self.reflection if self.reflection_min is None else self.reflection_min
-            fin += " reflection { %s, %s%s }" % (_g(rmin), _g(self.reflection), " fresnel on" if self.fresnel else "")
+            fin += " reflection { %s, %s%s%s }" % (_g(rmin), _g(self.reflection), " fresnel on" if self.fresnel else "",
+                                                  " metallic %s" % _g(self.reflect_metallic)
+                                                  if self.reflect_metallic else "")
         elif self.reflection:
             fin += " reflection %s" % _g(self.reflection)
         if self.conserve_energy:
@@ -464,12 +471,12 @@ class Material:
         m.phong_size = self.phong_size
         m.specular = self.specular
         m.roughness = 1.0 / self.roughness
-        m.metallic = 0.0
+        m.metallic = self.metallic
         m.reflection_max[:] = [self.reflection] * 3
         m.reflection_min[:] = [self.reflection if self.reflection_min is None else self.reflection_min] * 3
         m.reflection_falloff = 1.0
         m.reflect_exp = 1.0
-        m.reflect_metallic = 0.0
+        m.reflect_metallic = self.reflect_metallic
         m.reflection_fresnel = int(self.fresnel)
         m.conserve_energy = int(self.conserve_energy)
         m.fresnel = 0.0
@@ -1581,6 +1588,30 @@ def backlit_sheets(width=320, height=240):
     for c, r, rgb in (((-2.5, 0.0, -1.5), 0.7, (0.9, 0.6, 0.2)), ((0.2, 0.3, -2.0), 0.6, (0.3, 0.5, 0.9)),
                       ((2.3, 0.0, -1.0), 0.8, (0.8, 0.8, 0.8))):
         s.sphere(c, r, s.material(Material(rgb, diffuse=0.6, diffuse_back=0.3, phong=0.5)))
+    return s
+
+
+def metal_spheres(width=320, height=240):
+    """Metallic finishes: spheres of gold, copper, steel and a painted
+    metal with phong or specular highlights tinted by `metallic` (1, 0.8,
+    0.5) and reflections tinted by reflection's `metallic` (0.9, 0.6), a
+    plain reflective sphere for contrast, over a checker floor; two point
+    lights; camera (0,3,-10) looking at (0,0.5,0), 50 deg;
+    max_trace_level 4."""
+    s = Scene("metal_spheres", width, height, (0.0, 3.0, -10.0), (0.0, 0.5, 0.0), 50.0, max_trace_level=4)
+    s.point_light((6.0, 10.0, -8.0))
+    s.point_light((-8.0, 6.0, -4.0), (0.5, 0.5, 0.55))
+    floor = Pattern("checker", [(0.0, (0.85, 0.85, 0.8)), (1.0, (0.25, 0.3, 0.4))],
+                    [("translate", (0.0, 0.5, 0.0))])
+    s.plane((0.0, 1.0, 0.0), -1.0, s.material(Material((1.0, 1.0, 1.0), pattern=floor)))
+    for c, rgb, kw in (((-3.3, 0.0, 1.0), (0.95, 0.75, 0.3), dict(phong=0.9, phong_size=60.0, metallic=1.0,
+                                                                   reflection=0.5, reflect_metallic=0.9)),
+                       ((-1.1, 0.0, 0.0), (0.85, 0.45, 0.3), dict(specular=0.8, roughness=0.02, metallic=0.8,
+                                                                   reflection=0.4, reflect_metallic=0.6)),
+                       ((1.1, 0.0, 0.0), (0.7, 0.72, 0.75), dict(phong=0.7, metallic=0.5, reflection=0.35)),
+                       ((3.3, 0.0, 1.0), (0.2, 0.5, 0.25), dict(phong=0.6, specular=0.4, metallic=1.0)),
+                       ((0.0, 0.2, 2.8), (0.9, 0.9, 0.9), dict(phong=0.5, reflection=0.3))):
+        s.sphere(c, 1.0, s.material(Material(rgb, diffuse=0.5, **kw)))
     return s
 
 

@@ -63,6 +63,7 @@ def cases():
         "patterned_spheres_160x120": (scenes.patterned_spheres(160, 120), 2, 8.0),
         "glass_patterns_160x120": (scenes.glass_patterns(160, 120), 2, 8.0),
         "backlit_sheets_160x120": (scenes.backlit_sheets(160, 120), 2, 6.0),
+        "metal_spheres_160x120": (scenes.metal_spheres(160, 120), 2, 6.0),
         "media_spheres_160x120": (scenes.media_spheres(160, 120), 2, 9.0),
         "media_hazy_160x120": (scenes.media_spheres(160, 120, scattering_type=2), 4, 9.0),
         "media_murky_160x120": (scenes.media_spheres(160, 120, scattering_type=3), 4, 9.0),
