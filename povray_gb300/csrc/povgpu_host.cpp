@@ -1081,6 +1081,11 @@ int validate(const PovGpuSceneDesc* d, int32_t* bad)
         // and plane transforms are not on the GPU path
         if (o.type == POV_OBJ_TORUS ? !(o.flags & POV_FLAG_HAS_TRANS) : (o.flags & POV_FLAG_HAS_TRANS) != 0)
             return POV_GPU_E_UNSUPPORTED;
+        // no_shadow, no_reflection and no_image (the ray-kind object tests of
+        // FindIntersection's preconditions, trace.cpp:1943-1950) are not on
+        // the GPU path: refused rather than rendered as if absent
+        if (o.flags & (POV_FLAG_NO_SHADOW | POV_FLAG_NO_REFLECTION | POV_FLAG_NO_IMAGE))
+            return POV_GPU_E_UNSUPPORTED;
         if (is_csg(o.type)) {
             if (o.parent >= 0)
                 return POV_GPU_E_UNSUPPORTED;   // nested CSG

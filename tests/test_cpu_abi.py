@@ -343,6 +343,20 @@ def test_light_source_validation(gpu_lib):
         Oracle(bad)
 
 
+def test_object_ray_kind_flags_are_refused(gpu_lib):
+    """no_shadow, no_reflection and no_image objects are refused at create
+    (the GPU path does not filter objects by ray kind), with the object's
+    index; the other flags pass."""
+    ok = (abi.POV_GPU_OK, abi.POV_GPU_E_NODEVICE, abi.POV_GPU_E_CUDA)
+    for flag in (abi.POV_FLAG_NO_SHADOW, abi.POV_FLAG_NO_REFLECTION, abi.POV_FLAG_NO_IMAGE):
+        desc, keep = scenes.spheres_plane(32, 24, n_spheres=4).desc()
+        desc.objects[2].flags |= flag
+        assert _create(gpu_lib, desc) == (abi.POV_GPU_E_UNSUPPORTED, 2), flag
+    desc, keep = scenes.spheres_plane(32, 24, n_spheres=4).desc()
+    desc.objects[2].flags |= abi.POV_FLAG_DOUBLE_ILLUM
+    assert _create(gpu_lib, desc)[0] in ok
+
+
 def test_oracle_rejects_the_same_scenes():
     """The oracle applies the same rules as the library."""
     from oracle.pyoracle import Oracle
